@@ -1,0 +1,234 @@
+/*
+ * sdg_gpu.h -- C ABI of the GB300 explicit DG residual-and-update path.
+ *
+ * This is the drop-in boundary that replaces SubrosaDG's templated
+ * Solver<SimulationControl> seam (src/Solver/SolveControl.cpp:327-436), which
+ * System<SimulationControl>::solve (src/Utils/SystemControl.cpp:159-195) drives.
+ * A C++ host shim marshals the reference's Mesh/PhysicalModel/BoundaryCondition
+ * objects into the plain arrays below and calls these entry points; the library
+ * owns all device memory, the caller owns every host buffer (copied in/out).
+ *
+ * Conventions
+ *   - Every entry point returns SDG_OK (0) or an SDG_ERR_* code and never throws.
+ *     sdg_last_error(handle) (or sdg_last_error(NULL) after a failed create)
+ *     returns a NUL-terminated description of the last failure.
+ *   - Calls are synchronous with respect to the handle's CUDA stream unless the
+ *     name ends in _async.  A handle is not thread-safe; one handle = one GPU.
+ *   - All arithmetic is IEEE FP64.  Integer data are int32 connectivity.
+ *   - Element blocks are ordered as the reference orders its element loops:
+ *     2D: triangles then quadrangles; 3D: hexahedra
+ *     (src/Solver/SpatialDiscrete.cpp:268-291).
+ *   - "Volume points" are the reference's volume quadrature points
+ *     (Gauss rule of order 2P, src/Solver/SimulationControl.cpp:275-278);
+ *     per-point arrays are [element][point][component] in block order.
+ *   - Conserved variables: rho, rho*u (d components), rho*E.
+ *     Primitive variables: rho, u (d components), T (src/Solver/VariableConvertor.cpp:332-366).
+ */
+#ifndef SDG_GPU_H_
+#define SDG_GPU_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------------- */
+#define SDG_OK 0
+#define SDG_ERR_INVALID_ARGUMENT 1 /* bad pointer, count, enum or size                                */
+#define SDG_ERR_CUDA 2             /* a CUDA runtime call failed (text in sdg_last_error)           */
+#define SDG_ERR_OUT_OF_MEMORY 3    /* device allocation failed                                      */
+#define SDG_ERR_MESH 4             /* inconsistent mesh: a face seen more than twice, unmatched
+                                      boundary face, inverted element (Adjacency.cpp:161-165)      */
+#define SDG_ERR_UNSUPPORTED 5      /* configuration outside what this build implements              */
+#define SDG_ERR_NONFINITE 6        /* NaN/Inf detected in the state (SystemControl.cpp:185-191)     */
+#define SDG_ERR_TIMEOUT 7          /* a bounded device wait gave up                                  */
+#define SDG_ERR_STATE 8            /* call out of order (e.g. step before an initial state)         */
+
+/* ---- enumerations (values equal the reference's enum order, src/Utils/Enum.cpp) --------------- */
+enum sdg_element_type { /* gmsh first-order type numbers (src/Solver/SimulationControl.cpp:26-31) */
+  SDG_ELEMENT_TRIANGLE = 2,
+  SDG_ELEMENT_QUADRANGLE = 3,
+  SDG_ELEMENT_HEXAHEDRON = 5
+};
+enum sdg_equation { SDG_COMPRESSIBLE_EULER = 0, SDG_COMPRESSIBLE_NS = 1 };           /* Enum.cpp:56-64   */
+enum sdg_convective_flux {                                                            /* Enum.cpp:107-113 */
+  SDG_FLUX_CENTRAL = 0,
+  SDG_FLUX_LAX_FRIEDRICHS = 1,
+  SDG_FLUX_HLLC = 2,
+  SDG_FLUX_ROE = 3
+};
+enum sdg_viscous_flux { SDG_VISCOUS_NONE = 0, SDG_VISCOUS_BR1 = 1, SDG_VISCOUS_BR2 = 2 }; /* Enum.cpp:115-119 */
+enum sdg_time_integration {                                                            /* Enum.cpp:136-140 */
+  SDG_FORWARD_EULER = 0,
+  SDG_HEUN_RK2 = 1,
+  SDG_SSPRK3 = 2
+};
+enum sdg_transport_model { SDG_TRANSPORT_NONE = 0, SDG_TRANSPORT_CONSTANT = 1, SDG_TRANSPORT_SUTHERLAND = 2 };
+enum sdg_boundary_condition {                                                          /* Enum.cpp:92-100 */
+  SDG_BC_RIEMANN_FARFIELD = 0,
+  SDG_BC_VELOCITY_INFLOW = 1,
+  SDG_BC_PRESSURE_OUTFLOW = 2,
+  SDG_BC_ISOTHERMAL_NONSLIP_WALL = 3,
+  SDG_BC_ADIABATIC_SLIP_WALL = 4,
+  SDG_BC_ADIABATIC_NONSLIP_WALL = 5,
+  SDG_BC_PERIODIC = 6
+};
+
+/* ---- mesh: first-order (straight-sided) geometry in gmsh vertex order -------------------------- */
+typedef struct sdg_mesh {
+  int32_t dimension;                  /* 2 or 3                                                     */
+  int64_t node_count;
+  const double* node_coordinate;      /* [node_count][3]                                            */
+  const int32_t* periodic_master;     /* [node_count] node -> periodic master node (itself when not a
+                                         slave), or NULL.  Replaces gmsh::getPeriodicNodes pairing
+                                         (src/Mesh/Adjacency.cpp:213-328).                          */
+  int64_t triangle_count;
+  const int32_t* triangle_node;       /* [triangle_count][3]                                        */
+  int64_t quadrangle_count;
+  const int32_t* quadrangle_node;     /* [quadrangle_count][4]                                      */
+  int64_t hexahedron_count;
+  const int32_t* hexahedron_node;     /* [hexahedron_count][8]                                      */
+  int64_t boundary_count;             /* boundary elements: lines (2D) or quadrangles (3D)          */
+  const int32_t* boundary_node;       /* [boundary_count][2 or 4]                                   */
+  const int32_t* boundary_physical;   /* [boundary_count] 1-based physical group index              */
+  int32_t physical_count;
+  const int32_t* physical_boundary_condition; /* [physical_count] sdg_boundary_condition per group,
+                                                 as System::addBoundaryCondition sets it
+                                                 (src/Utils/SystemControl.cpp:76-80)                */
+} sdg_mesh;
+
+/* ---- physics and numerics: the runtime form of the reference's SimulationControl -------------- */
+typedef struct sdg_config {
+  int32_t polynomial_order;           /* 1..5 (Enum.cpp:48-54)                                      */
+  int32_t equation;                   /* sdg_equation                                               */
+  int32_t convective_flux;            /* sdg_convective_flux                                        */
+  int32_t viscous_flux;               /* sdg_viscous_flux (NS only)                                 */
+  int32_t time_integration;           /* sdg_time_integration                                       */
+  int32_t transport_model;            /* sdg_transport_model (NS only)                              */
+  double specific_heat_ratio;         /* reference: constexpr 1.4 (src/Solver/PhysicalModel.cpp:45) */
+  double specific_heat_constant_pressure; /* System::setThermodynamicModel (SystemControl.cpp:82-88) */
+  double specific_heat_constant_volume;
+  double dynamic_viscosity;           /* System::setTransportModel (SystemControl.cpp:98-103)       */
+  double prandtl_number;              /* reference: constexpr 0.71 (PhysicalModel.cpp:91)           */
+} sdg_config;
+
+/* ---- sizes of a created problem ------------------------------------------------------------- */
+typedef struct sdg_counts {
+  int32_t dimension;
+  int32_t conserved_variable_count;   /* d + 2                                                      */
+  int32_t block_count;                /* element blocks (one per element type present)              */
+  int32_t block_element_type[2];      /* sdg_element_type of each block                             */
+  int64_t block_element_count[2];
+  int32_t block_basis_count[2];       /* Nb per element                                             */
+  int32_t block_volume_point_count[2];/* Nq per element                                             */
+  int64_t element_count;              /* all blocks                                                 */
+  int64_t volume_point_count;         /* sum over blocks of elements * Nq                           */
+  int64_t degree_of_freedom_count;    /* sum of elements * Nb * (d+2)                               */
+  int64_t interior_face_count;
+  int64_t boundary_face_count;
+  int32_t face_point_count;           /* Nfq per face (order 2P+1 rule)                             */
+  int64_t boundary_point_count;       /* boundary_face_count * face_point_count                     */
+} sdg_counts;
+
+typedef struct sdg_handle sdg_handle;
+
+/* Last error text for this handle (or the last failed sdg_create when handle is NULL). */
+const char* sdg_last_error(const sdg_handle* handle);
+
+/* Build the problem: adjacency and periodic pairing (Adjacency.cpp:432-495), geometry
+ * (Geometry.cpp:44-169), operators, device buffers.  Replaces Mesh<SC>::readMeshElement
+ * (src/Mesh/ReadControl.cpp:293-335) + Solver<SC> member construction.  device = CUDA ordinal;
+ * device < 0 builds a host-only handle (adjacency, geometry, coordinates, counts; no GPU is touched
+ * and every state/step entry point returns SDG_ERR_STATE). */
+int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, sdg_handle** handle);
+int sdg_destroy(sdg_handle* handle);
+int sdg_get_counts(const sdg_handle* handle, sdg_counts* counts);
+
+/* Physical coordinates of every volume point, [volume_point_count][3]
+ * (ElementMesh::quadrature_node_coordinate_, src/Mesh/Geometry.cpp:51-58). */
+int sdg_volume_point_coordinate(sdg_handle* handle, double* coordinate);
+/* Physical coordinates of every boundary face point, [boundary_point_count][3], and the
+ * 1-based physical group of each boundary face, [boundary_face_count]. */
+int sdg_boundary_point_coordinate(sdg_handle* handle, double* coordinate, int32_t* physical);
+
+/* Initial condition from primitive values (rho,u,T) at the volume points: conserved
+ * conversion + unweighted least-squares projection, as Solver::initializeSolver does
+ * (src/Solver/InitialCondition.cpp:85-104). */
+int sdg_set_initial_primitive(sdg_handle* handle, const double* primitive);
+/* Ghost primitive states at boundary face points, [boundary_point_count][d+2]
+ * (AdjacencyElementSolver::boundary_dummy_variable_, InitialCondition.cpp:118-149). */
+int sdg_set_boundary_primitive(sdg_handle* handle, const double* primitive);
+
+/* State exchange in physical space: conserved values at the volume points,
+ * [volume_point_count][d+2].  set = unweighted least-squares projection. */
+int sdg_set_state_point(sdg_handle* handle, const double* conserved);
+int sdg_get_state_point(sdg_handle* handle, double* conserved);
+/* State exchange as modal coefficients in the reference's per-element layout
+ * (variable_basis_function_coefficient_: column-major (d+2) x Nb, SolveControl.cpp:45-60),
+ * concatenated per block; basis = the hierarchic Lobatto basis documented in the design doc. */
+int sdg_set_state_modal(sdg_handle* handle, const double* coefficient);
+int sdg_get_state_modal(sdg_handle* handle, double* coefficient);
+
+/* dt = min over volume points of CFL * minEdge / ((|u|+c)(P+1)^2)
+ * (Solver::calculateDeltaTime, src/Solver/TimeIntegration.cpp:104-131). */
+int sdg_calculate_delta_time(sdg_handle* handle, double courant_friedrichs_lewy_number, double* delta_time);
+
+/* Advance step_count full RK steps of size delta_time (Solver::stepSolver,
+ * src/Solver/TimeIntegration.cpp:326-350).  After the last step the relative error of that
+ * step is available from sdg_relative_error. */
+int sdg_step(sdg_handle* handle, int32_t step_count, double delta_time);
+/* Same, enqueued on the handle's stream without a host synchronisation. */
+int sdg_step_async(sdg_handle* handle, int32_t step_count, double delta_time);
+
+/* Solver::relative_error_ of the last step: per conserved variable, the element mean of
+ * mean_q |R Phi^T| (TimeIntegration.cpp:279-324).  NaN entries signal a blow-up. */
+int sdg_relative_error(sdg_handle* handle, double* relative_error);
+
+/* One spatial-residual evaluation at the current state, returned as du/dt = M^-1 R at the
+ * volume points, [volume_point_count][d+2] (SpatialDiscrete.cpp:1016-1032 followed by the
+ * M^-1 of TimeIntegration.cpp:196). */
+int sdg_residual_point(sdg_handle* handle, double* rate);
+
+/* Wait for all work on the handle's stream. */
+int sdg_synchronize(sdg_handle* handle);
+
+/* Diagnostic: number of CUDA kernel launches issued by this handle since creation. */
+int sdg_launch_count(const sdg_handle* handle, int64_t* launch_count);
+
+/* Diagnostic: adjacency as canonical integer tuples, for bit-exact parity checks.
+ * interior: [interior_face_count][7] = (typeL, elemL, faceL, typeR, elemR, faceR, rotation)
+ * boundary: [boundary_face_count][5] = (type, elem, face, physical, boundary_condition)
+ * Element indices are within their block; rows sorted lexicographically. */
+int sdg_adjacency(const sdg_handle* handle, int32_t* interior, int32_t* boundary);
+
+/* Structured mesh generators of the reference's example drivers (gmsh transfinite + periodic
+ * setups in examples/periodic_2d_ceuler.cpp:63-94 and examples/periodic_3d_ceuler.cpp:60-130),
+ * plus the jittered/triangle-split hybrid of the Kelvin-Helmholtz workload.  The generator owns
+ * the arrays it returns; free them with sdg_mesh_free. */
+typedef struct sdg_generated_mesh {
+  sdg_mesh mesh;
+  void* storage;                      /* owned by the library                                       */
+} sdg_generated_mesh;
+/* 2D [x0,x0+lx] x [y0,y0+ly], nx x ny quadrangles; jitter = fraction of h for interior nodes
+ * (seeded); split_fraction = fraction of quads split into two triangles (seeded);
+ * periodic = 1 pairs opposite sides (one physical group, SDG_BC_PERIODIC), else four groups
+ * (bottom, right, top, left) with boundary_condition[0..3]. */
+int sdg_mesh_generate_2d(double x0, double y0, double lx, double ly, int32_t nx, int32_t ny,
+                         double jitter, double split_fraction, uint64_t seed, int32_t periodic,
+                         const int32_t* boundary_condition, sdg_generated_mesh* out);
+/* 3D box, nx x ny x nz hexahedra; periodic = 1 pairs opposite faces, else six groups
+ * (x-, x+, y-, y+, z-, z+). */
+int sdg_mesh_generate_3d(double x0, double y0, double z0, double lx, double ly, double lz, int32_t nx,
+                         int32_t ny, int32_t nz, int32_t periodic, const int32_t* boundary_condition,
+                         sdg_generated_mesh* out);
+/* Read a gmsh MSH 4.1 ASCII file (first-order or high-order elements; only the primary vertices
+ * are used).  Physical groups of dimension d-1 become boundary groups in file order. */
+int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out);
+int sdg_mesh_free(sdg_generated_mesh* mesh);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SDG_GPU_H_ */

@@ -1,0 +1,137 @@
+"""ctypes wrapper of the oracle (oracle/liborc.so) -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+module, and only as the checker / the timed CPU baseline.  The product path
+(subrosadg_gb300) never imports it.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, byref, c_double, c_int, c_int32, c_int64, c_void_p
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liborc.so")
+_pd = POINTER(c_double)
+_pi = POINTER(c_int32)
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            from . import build as _build
+            _build.build()
+        lib = ctypes.CDLL(LIB)
+        lib.orc_create.restype = c_void_p
+        lib.orc_create.argtypes = [c_void_p, c_void_p, c_int]
+        lib.orc_last_error.restype = ctypes.c_char_p
+        lib.orc_destroy.argtypes = [c_void_p]
+        for name in ("orc_volume_point_coordinate", "orc_set_initial_primitive", "orc_set_state_point",
+                     "orc_set_boundary_primitive", "orc_get_state_point", "orc_get_state_modal",
+                     "orc_relative_error", "orc_residual_point", "orc_interior_face_geometry"):
+            getattr(lib, name).argtypes = [c_void_p, _pd]
+            getattr(lib, name).restype = c_int
+        lib.orc_boundary_point_coordinate.argtypes = [c_void_p, _pd, _pi]
+        lib.orc_counts.argtypes = [c_void_p, POINTER(c_int64)]
+        lib.orc_calculate_delta_time.argtypes = [c_void_p, c_double, _pd]
+        lib.orc_step.argtypes = [c_void_p, c_int, c_double]
+        lib.orc_adjacency.argtypes = [c_void_p, _pi, _pi]
+        lib.orc_set_threads.argtypes = [c_int]
+        lib.orc_max_threads.restype = c_int
+        _lib = lib
+    return _lib
+
+
+class Oracle:
+    """CPU restatement of the reference solver on the same mesh/config structs as sdg_create."""
+
+    def __init__(self, mesh, config, faithful=True):
+        self.lib = load()
+        self._m = mesh.struct()
+        self._c = config
+        self.h = self.lib.orc_create(ctypes.addressof(self._m), ctypes.addressof(self._c), int(faithful))
+        if not self.h:
+            raise RuntimeError("oracle: " + self.lib.orc_last_error().decode())
+        c = (c_int64 * 6)()
+        self.lib.orc_counts(self.h, c)
+        self.elements, self.volume_points_count, self.interior, self.boundary, self.nfq, self.dof = list(c)
+        self.nv = mesh.dimension + 2
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.orc_destroy(self.h)
+            self.h = None
+
+    def volume_points(self):
+        out = np.zeros((self.volume_points_count, 3))
+        self.lib.orc_volume_point_coordinate(self.h, out.ctypes.data_as(_pd))
+        return out
+
+    def boundary_points(self):
+        out = np.zeros((self.boundary * self.nfq, 3))
+        phys = np.zeros(self.boundary, np.int32)
+        self.lib.orc_boundary_point_coordinate(self.h, out.ctypes.data_as(_pd), phys.ctypes.data_as(_pi))
+        return out, phys
+
+    def initialize_primitive(self, prim):
+        p = np.ascontiguousarray(prim, np.float64)
+        self.lib.orc_set_initial_primitive(self.h, p.ctypes.data_as(_pd))
+
+    def set_state_point(self, cons):
+        p = np.ascontiguousarray(cons, np.float64)
+        self.lib.orc_set_state_point(self.h, p.ctypes.data_as(_pd))
+
+    def set_boundary_primitive(self, prim):
+        p = np.ascontiguousarray(prim, np.float64)
+        self.lib.orc_set_boundary_primitive(self.h, p.ctypes.data_as(_pd))
+
+    def state_point(self):
+        out = np.zeros((self.volume_points_count, self.nv))
+        self.lib.orc_get_state_point(self.h, out.ctypes.data_as(_pd))
+        return out
+
+    def state_modal(self):
+        out = np.zeros(self.dof)
+        self.lib.orc_get_state_modal(self.h, out.ctypes.data_as(_pd))
+        return out
+
+    def residual_point(self):
+        out = np.zeros((self.volume_points_count, self.nv))
+        self.lib.orc_residual_point(self.h, out.ctypes.data_as(_pd))
+        return out
+
+    def step(self, dt, n=1):
+        self.lib.orc_step(self.h, n, dt)
+
+    def relative_error(self):
+        out = np.zeros(self.nv)
+        self.lib.orc_relative_error(self.h, out.ctypes.data_as(_pd))
+        return out
+
+    def delta_time(self, cfl):
+        dt = c_double()
+        self.lib.orc_calculate_delta_time(self.h, cfl, byref(dt))
+        return dt.value
+
+    def adjacency(self):
+        a = np.zeros((self.interior, 7), np.int32)
+        b = np.zeros((self.boundary, 5), np.int32)
+        self.lib.orc_adjacency(self.h, a.ctypes.data_as(_pi), b.ctypes.data_as(_pi))
+        return a, b
+
+    def interior_face_geometry(self):
+        out = np.zeros((self.interior, self.nfq, 4))
+        self.lib.orc_interior_face_geometry(self.h, out.ctypes.data_as(_pd))
+        return out
+
+
+def set_threads(n):
+    load().orc_set_threads(int(n))
+
+
+def max_threads():
+    return load().orc_max_threads()

@@ -1,0 +1,360 @@
+// Oracle -- test infrastructure only (the checker, never the product).
+// Reference elements, quadrature and the modal basis, restated from the reference's gmsh calls:
+//   quadrature  : src/Mesh/Quadrature.cpp:27-51 (gmsh "Gauss{order}"), orders from
+//                 src/Solver/SimulationControl.cpp:268-283 (volume 2P, face 2P+1)
+//   modal basis : src/Mesh/BasisFunction.cpp:45-74 (gmsh "H1Legendre{P}" = hierarchic Lobatto)
+//   face traces : src/Mesh/BasisFunction.cpp:76-111,149-197 (P1 map of face points into the parent)
+//   face tables : src/Solver/SimulationControl.cpp:170-216 (face vertex lists),
+//                 src/Solver/SimulationControl.cpp:381-523 (face point permutation by rotation)
+// gmsh 4.13.1 is not vendored under the reference tree, so its Lobatto normalisation, point orderings
+// and triangle tables are restated from the published definitions (parity for these is unpinned
+// against gmsh itself; the DG solution does not depend on the basis choice).
+#pragma once
+#include <array>
+#include <cmath>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../subrosadg_gb300/csrc/triangle_rules.h"
+
+namespace orc {
+
+enum ElemType { kTri = 2, kQuad = 3, kHex = 5 };
+
+inline int elemDim(int t) { return t == kHex ? 3 : 2; }
+inline int elemFaces(int t) { return t == kTri ? 3 : (t == kQuad ? 4 : 6); }
+inline int elemVerts(int t) { return t == kTri ? 3 : (t == kQuad ? 4 : 8); }
+inline int faceVerts(int t) { return t == kHex ? 4 : 2; }
+
+// Face vertex lists of each element type (SimulationControl.cpp:170-216).
+inline const int* faceVertexTable(int t) {
+  static const int tri[] = {0, 1, 1, 2, 2, 0};
+  static const int quad[] = {0, 1, 1, 2, 2, 3, 3, 0};
+  static const int hex[] = {0, 3, 2, 1, 0, 1, 5, 4, 0, 4, 7, 3, 1, 2, 6, 5, 2, 3, 7, 6, 4, 5, 6, 7};
+  return t == kTri ? tri : (t == kQuad ? quad : hex);
+}
+
+// Reference-element vertex coordinates (gmsh conventions).
+inline std::array<double, 3> refVertex(int t, int v) {
+  static const double tri[3][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}};
+  static const double quad[4][3] = {{-1, -1, 0}, {1, -1, 0}, {1, 1, 0}, {-1, 1, 0}};
+  static const double hex[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                                   {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+  const double* p = t == kTri ? tri[v] : (t == kQuad ? quad[v] : hex[v]);
+  return {p[0], p[1], p[2]};
+}
+
+// Legendre P_n and P'_n by the three-term recurrence.
+inline void legendre(int n, double x, double& p, double& dp) {
+  double p0 = 1.0, p1 = x, d0 = 0.0, d1 = 1.0;
+  if (n == 0) { p = 1.0; dp = 0.0; return; }
+  for (int k = 2; k <= n; ++k) {
+    const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+    const double d2 = d0 + (2.0 * k - 1.0) * p1;
+    p0 = p1; p1 = p2; d0 = d1; d1 = d2;
+  }
+  p = p1; dp = d1;
+}
+
+// n-point Gauss-Legendre rule on [-1,1], points ascending (Newton on P_n).
+inline void gaussLegendre(int n, std::vector<double>& x, std::vector<double>& w) {
+  x.assign(n, 0.0); w.assign(n, 0.0);
+  for (int i = 0; i < n; ++i) {
+    double z = -std::cos(M_PI * (i + 0.75) / (n + 0.5));
+    for (int it = 0; it < 100; ++it) {
+      double p, dp; legendre(n, z, p, dp);
+      const double dz = p / dp; z -= dz;
+      if (std::fabs(dz) < 1e-16) break;
+    }
+    double p, dp; legendre(n, z, p, dp);
+    x[i] = z; w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+// Line rule for a polynomial order (Gauss, ceil((order+1)/2) points; counts match
+// kLineQuadratureNumber, SimulationControl.cpp:268).
+inline int linePoints(int order) { return order / 2 + 1; }
+
+struct Quadrature {
+  int dim = 0, n = 0;
+  std::vector<double> x;  // n * 3 reference coordinates
+  std::vector<double> w;  // n
+};
+
+// Element quadrature of the given order for each element type.
+inline Quadrature elementQuadrature(int t, int order) {
+  Quadrature q; q.dim = elemDim(t);
+  if (t == kTri) {
+    for (const auto& r : sdg_tables::kTriangleRules) {
+      if (r.degree == order) {
+        q.n = r.count;
+        for (int i = 0; i < r.count; ++i) { q.x.insert(q.x.end(), {r.xi[i], r.eta[i], 0.0}); q.w.push_back(r.weight[i]); }
+        return q;
+      }
+    }
+    throw std::runtime_error("no triangle rule of order " + std::to_string(order));
+  }
+  if (t == kQuad && order == 2) {
+    // 7-point degree-5 rule (kQuadrangleQuadratureNumber[2] = 7): Radon's symmetric formula.
+    const double a = std::sqrt(14.0 / 15.0), b = std::sqrt(3.0 / 5.0), c = std::sqrt(1.0 / 3.0);
+    const double pts[7][2] = {{0, 0}, {0, a}, {0, -a}, {b, c}, {-b, c}, {b, -c}, {-b, -c}};
+    const double wts[7] = {8.0 / 7.0, 20.0 / 63.0, 20.0 / 63.0, 5.0 / 9.0, 5.0 / 9.0, 5.0 / 9.0, 5.0 / 9.0};
+    q.n = 7;
+    for (int i = 0; i < 7; ++i) { q.x.insert(q.x.end(), {pts[i][0], pts[i][1], 0.0}); q.w.push_back(wts[i]); }
+    return q;
+  }
+  const int m = linePoints(order);
+  std::vector<double> gx, gw; gaussLegendre(m, gx, gw);
+  if (t == kQuad) {  // index = i*m + j with (xi=x_i, eta=x_j)
+    q.n = m * m;
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) { q.x.insert(q.x.end(), {gx[i], gx[j], 0.0}); q.w.push_back(gw[i] * gw[j]); }
+  } else {  // hex: index = (i*m + j)*m + k
+    q.n = m * m * m;
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j)
+        for (int k = 0; k < m; ++k) {
+          q.x.insert(q.x.end(), {gx[i], gx[j], gx[k]});
+          q.w.push_back(gw[i] * gw[j] * gw[k]);
+        }
+  }
+  return q;
+}
+
+// Face rule (face reference coordinates: line xi in [-1,1]; quad face (xi,eta) in [-1,1]^2,
+// index i*m + j with (xi=x_i, eta=x_j)).
+inline Quadrature faceQuadrature(int t, int order) {
+  Quadrature q; q.dim = elemDim(t) - 1;
+  const int m = linePoints(order);
+  std::vector<double> gx, gw; gaussLegendre(m, gx, gw);
+  if (t != kHex) {
+    q.n = m;
+    for (int i = 0; i < m; ++i) { q.x.insert(q.x.end(), {gx[i], 0.0, 0.0}); q.w.push_back(gw[i]); }
+  } else {
+    q.n = m * m;
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j) { q.x.insert(q.x.end(), {gx[i], gx[j], 0.0}); q.w.push_back(gw[i] * gw[j]); }
+  }
+  return q;
+}
+
+// P1 shape functions of the face reference element (BasisFunction.cpp:76-111 uses gmsh Lagrange1).
+inline void faceShape(int t, const double* fx, double* n) {
+  if (t != kHex) { n[0] = 0.5 * (1.0 - fx[0]); n[1] = 0.5 * (1.0 + fx[0]); return; }
+  const double x = fx[0], y = fx[1];
+  n[0] = 0.25 * (1 - x) * (1 - y); n[1] = 0.25 * (1 + x) * (1 - y);
+  n[2] = 0.25 * (1 + x) * (1 + y); n[3] = 0.25 * (1 - x) * (1 + y);
+}
+inline void faceShapeGrad(int t, const double* fx, double* dxi, double* deta) {
+  if (t != kHex) { dxi[0] = -0.5; dxi[1] = 0.5; return; }
+  const double x = fx[0], y = fx[1];
+  dxi[0] = -0.25 * (1 - y); dxi[1] = 0.25 * (1 - y); dxi[2] = 0.25 * (1 + y); dxi[3] = -0.25 * (1 + y);
+  deta[0] = -0.25 * (1 - x); deta[1] = -0.25 * (1 + x); deta[2] = 0.25 * (1 + x); deta[3] = 0.25 * (1 - x);
+}
+
+// P1 element shape functions and reference gradients (geometry map of straight-sided elements).
+inline void elemShape(int t, const double* X, double* n, double* g /* nv*3 */) {
+  if (t == kTri) {
+    n[0] = 1 - X[0] - X[1]; n[1] = X[0]; n[2] = X[1];
+    const double gg[9] = {-1, -1, 0, 1, 0, 0, 0, 1, 0};
+    for (int i = 0; i < 9; ++i) g[i] = gg[i];
+    return;
+  }
+  const int nv = elemVerts(t);
+  for (int v = 0; v < nv; ++v) {
+    const auto r = refVertex(t, v);
+    const double a = 1 + r[0] * X[0], b = 1 + r[1] * X[1];
+    if (t == kQuad) {
+      n[v] = 0.25 * a * b; g[v * 3 + 0] = 0.25 * r[0] * b; g[v * 3 + 1] = 0.25 * a * r[1]; g[v * 3 + 2] = 0;
+    } else {
+      const double c = 1 + r[2] * X[2];
+      n[v] = 0.125 * a * b * c;
+      g[v * 3 + 0] = 0.125 * r[0] * b * c; g[v * 3 + 1] = 0.125 * a * r[1] * c; g[v * 3 + 2] = 0.125 * a * b * r[2];
+    }
+  }
+}
+
+// 1D Lobatto shape functions (Solin): l0=(1-x)/2, l1=(1+x)/2, lk=(P_k-P_{k-2})/sqrt(2(2k-1)).
+inline void lobatto(int k, double x, double& v, double& d) {
+  if (k == 0) { v = 0.5 * (1 - x); d = -0.5; return; }
+  if (k == 1) { v = 0.5 * (1 + x); d = 0.5; return; }
+  double pk, dpk, pk2, dpk2, pk1, dpk1;
+  legendre(k, x, pk, dpk); legendre(k - 2, x, pk2, dpk2); legendre(k - 1, x, pk1, dpk1);
+  const double s = std::sqrt(2.0 * (2.0 * k - 1.0));
+  v = (pk - pk2) / s;
+  d = std::sqrt((2.0 * k - 1.0) / 2.0) * pk1;
+}
+
+// Tiny forward-mode dual number in two variables (for triangle basis gradients).
+struct Dual { double v, dx, dy; };
+inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.dx + b.dx, a.dy + b.dy}; }
+inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.dx - b.dx, a.dy - b.dy}; }
+inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.dx * b.v + a.v * b.dx, a.dy * b.v + a.v * b.dy}; }
+inline Dual scale(Dual a, double s) { return {a.v * s, a.dx * s, a.dy * s}; }
+inline Dual legendreD(int n, Dual x) {  // P_n(x) as a dual
+  double p, dp; legendre(n, x.v, p, dp);
+  return {p, dp * x.dx, dp * x.dy};
+}
+// Solin kernel function phi_{k-2}(x) = 4 l_k(x)/(1-x^2) = -4 sqrt((2k-1)/2)/((k-1)k) P'_{k-1}(x).
+inline Dual kernelD(int k, Dual x) {
+  // P'_{k-1}(x) and its derivative P''_{k-1}(x) via (1-x^2)P'' = 2xP' - n(n+1)P is singular at
+  // |x|=1; use the sum form P'_{n} = sum_{j=n-1,n-3,..} (2j+1) P_j instead.
+  const int n = k - 1;
+  double dpn = 0.0, ddpn = 0.0;
+  for (int j = n - 1; j >= 0; j -= 2) {
+    double pj, dpj; legendre(j, x.v, pj, dpj);
+    dpn += (2.0 * j + 1.0) * pj; ddpn += (2.0 * j + 1.0) * dpj;
+  }
+  const double c = -4.0 * std::sqrt((2.0 * k - 1.0) / 2.0) / ((k - 1.0) * k);
+  return {c * dpn, c * ddpn * x.dx, c * ddpn * x.dy};
+}
+
+inline int basisCount(int t, int p) {
+  if (t == kTri) return (p + 1) * (p + 2) / 2;
+  if (t == kQuad) return (p + 1) * (p + 1);
+  return (p + 1) * (p + 1) * (p + 1);
+}
+
+// Modal (hierarchic H1) basis: values [nb] and reference gradients [nb][3] at X.
+//   quad: index a*(P+1)+b -> l_a(xi) l_b(eta); hex: index (a*(P+1)+b)*(P+1)+c.
+//   tri : vertices lambda_i; edges (0,1),(1,2),(2,0) with l_a l_b phi_{k-2}(l_b-l_a), k=2..P;
+//         bubbles l0 l1 l2 P_i(l2-l1) P_j(l1-l0), i+j<=P-3.
+inline void modalBasis(int t, int p, const double* X, double* val, double* grad) {
+  if (t == kQuad || t == kHex) {
+    const int m = p + 1;
+    double lv[3][6], ld[3][6];
+    for (int dd = 0; dd < elemDim(t); ++dd)
+      for (int k = 0; k < m; ++k) lobatto(k, X[dd], lv[dd][k], ld[dd][k]);
+    int idx = 0;
+    if (t == kQuad) {
+      for (int a = 0; a < m; ++a)
+        for (int b = 0; b < m; ++b, ++idx) {
+          val[idx] = lv[0][a] * lv[1][b];
+          grad[idx * 3 + 0] = ld[0][a] * lv[1][b]; grad[idx * 3 + 1] = lv[0][a] * ld[1][b]; grad[idx * 3 + 2] = 0;
+        }
+    } else {
+      for (int a = 0; a < m; ++a)
+        for (int b = 0; b < m; ++b)
+          for (int c = 0; c < m; ++c, ++idx) {
+            val[idx] = lv[0][a] * lv[1][b] * lv[2][c];
+            grad[idx * 3 + 0] = ld[0][a] * lv[1][b] * lv[2][c];
+            grad[idx * 3 + 1] = lv[0][a] * ld[1][b] * lv[2][c];
+            grad[idx * 3 + 2] = lv[0][a] * lv[1][b] * ld[2][c];
+          }
+    }
+    return;
+  }
+  const Dual l0{1 - X[0] - X[1], -1, -1}, l1{X[0], 1, 0}, l2{X[1], 0, 1};
+  const Dual lam[3] = {l0, l1, l2};
+  std::vector<Dual> f;
+  f.push_back(l0); f.push_back(l1); f.push_back(l2);
+  const int edges[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+  for (int e = 0; e < 3; ++e) {
+    const Dual a = lam[edges[e][0]], b = lam[edges[e][1]];
+    for (int k = 2; k <= p; ++k) f.push_back(a * b * kernelD(k, b - a));
+  }
+  const Dual bub = l0 * l1 * l2;
+  for (int s = 0; s <= p - 3; ++s)
+    for (int i = 0; i <= s; ++i) {
+      const int j = s - i;
+      f.push_back(bub * legendreD(i, l2 - l1) * legendreD(j, l1 - l0));
+    }
+  for (size_t i = 0; i < f.size(); ++i) { val[i] = f[i].v; grad[i * 3 + 0] = f[i].dx; grad[i * 3 + 1] = f[i].dy; grad[i * 3 + 2] = 0; }
+}
+
+// Face point permutation for a right element with the given rotation
+// (reproduces the tables of SimulationControl.cpp:381-523 from the orientation rule:
+//  line faces are traversed in reverse; quadrangle faces map (xi,eta) of the left face to
+//  rotation 0:(eta,xi) 1:(-xi,eta) 2:(-eta,-xi) 3:(xi,-eta) on the right face).
+inline std::vector<int> facePermutation(int t, int m, int rotation) {
+  std::vector<int> perm;
+  if (t != kHex) { for (int j = 0; j < m; ++j) perm.push_back(m - 1 - j); return perm; }
+  for (int i = 0; i < m; ++i)
+    for (int k = 0; k < m; ++k) {
+      int ii = 0, kk = 0;
+      switch (rotation) {
+        case 0: ii = k; kk = i; break;
+        case 1: ii = m - 1 - i; kk = k; break;
+        case 2: ii = m - 1 - k; kk = m - 1 - i; break;
+        default: ii = i; kk = m - 1 - k; break;
+      }
+      perm.push_back(ii * m + kk);
+    }
+  return perm;
+}
+
+// Dense square inverse by Gauss-Jordan with partial pivoting (Eigen's inverse() in the reference).
+inline void invert(int n, const double* a, double* inv) {
+  std::vector<double> m(a, a + n * n);
+  for (int i = 0; i < n * n; ++i) inv[i] = 0.0;
+  for (int i = 0; i < n; ++i) inv[i * n + i] = 1.0;
+  for (int c = 0; c < n; ++c) {
+    int piv = c; double best = std::fabs(m[c * n + c]);
+    for (int r = c + 1; r < n; ++r) if (std::fabs(m[r * n + c]) > best) { best = std::fabs(m[r * n + c]); piv = r; }
+    if (best == 0.0) throw std::runtime_error("singular matrix");
+    if (piv != c) for (int k = 0; k < n; ++k) { std::swap(m[c * n + k], m[piv * n + k]); std::swap(inv[c * n + k], inv[piv * n + k]); }
+    const double d = 1.0 / m[c * n + c];
+    for (int k = 0; k < n; ++k) { m[c * n + k] *= d; inv[c * n + k] *= d; }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = m[r * n + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < n; ++k) { m[r * n + k] -= f * m[c * n + k]; inv[r * n + k] -= f * inv[c * n + k]; }
+    }
+  }
+}
+
+// Reference-element operator tables for one (type, P) (ElementBasisFunction, BasisFunction.cpp:136-230).
+struct RefElement {
+  int type = 0, dim = 0, p = 0, nb = 0, nq = 0, nface = 0, nfq = 0;
+  Quadrature vq, fq;
+  std::vector<double> phi;    // [nq][nb]        modal_value_
+  std::vector<double> dphi;   // [nq*dim][nb]    modal_gradient_value_ (row q*dim+k)
+  std::vector<double> phif;   // [nface*nfq][nb] modal_adjacency_value_
+  std::vector<double> lsqInv; // [nb][nb]        modal_least_squares_inverse_
+  std::vector<std::vector<int>> perm;  // rotation -> face point permutation
+
+  void build(int t, int order) {
+    type = t; dim = elemDim(t); p = order; nb = basisCount(t, order); nface = elemFaces(t);
+    vq = elementQuadrature(t, 2 * order);
+    fq = faceQuadrature(t, 2 * order + 1);
+    nq = vq.n; nfq = fq.n;
+    phi.assign(size_t(nq) * nb, 0); dphi.assign(size_t(nq) * dim * nb, 0);
+    std::vector<double> v(nb), g(nb * 3);
+    for (int q = 0; q < nq; ++q) {
+      modalBasis(t, order, &vq.x[q * 3], v.data(), g.data());
+      for (int b = 0; b < nb; ++b) {
+        phi[size_t(q) * nb + b] = v[b];
+        for (int k = 0; k < dim; ++k) dphi[(size_t(q) * dim + k) * nb + b] = g[b * 3 + k];
+      }
+    }
+    phif.assign(size_t(nface) * nfq * nb, 0);
+    const int* fv = faceVertexTable(t);
+    const int nfv = faceVerts(t);
+    for (int f = 0; f < nface; ++f)
+      for (int j = 0; j < nfq; ++j) {
+        double sh[4]; faceShape(t, &fq.x[j * 3], sh);
+        double X[3] = {0, 0, 0};
+        for (int k = 0; k < nfv; ++k) {
+          const auto r = refVertex(t, fv[f * nfv + k]);
+          for (int d = 0; d < 3; ++d) X[d] += sh[k] * r[d];
+        }
+        modalBasis(t, order, X, v.data(), g.data());
+        for (int b = 0; b < nb; ++b) phif[(size_t(f) * nfq + j) * nb + b] = v[b];
+      }
+    std::vector<double> ptp(size_t(nb) * nb, 0.0);
+    for (int a = 0; a < nb; ++a)
+      for (int b = 0; b < nb; ++b) {
+        double s = 0; for (int q = 0; q < nq; ++q) s += phi[size_t(q) * nb + a] * phi[size_t(q) * nb + b];
+        ptp[size_t(a) * nb + b] = s;
+      }
+    lsqInv.assign(size_t(nb) * nb, 0.0);
+    invert(nb, ptp.data(), lsqInv.data());
+    const int m = linePoints(2 * order + 1);
+    perm.clear();
+    for (int r = 0; r < (t == kHex ? 4 : 1); ++r) perm.push_back(facePermutation(t, m, r));
+  }
+};
+
+}  // namespace orc

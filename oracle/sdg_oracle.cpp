@@ -1,0 +1,842 @@
+// Oracle -- TEST INFRASTRUCTURE ONLY.  This file is the checker the GPU path is compared against
+// and the timed CPU baseline; nothing in the product links, imports or calls it.
+//
+// A CPU restatement, in plain C++17 + OpenMP, of SubrosaDG's explicit DG residual-and-update path
+// with the reference's own data flow: modal (hierarchic Lobatto) basis, per-element dense mass-matrix
+// inverse, per-element AoS blocks, and the stage sequence of Solver::stepSolver
+// (src/Solver/TimeIntegration.cpp:326-350), including -- when `faithful` is set -- the gradient pass
+// that the reference runs even for Euler and never reads.
+//
+// Followed reference code:
+//   adjacency / periodic pairing   src/Mesh/Adjacency.cpp:37-495
+//   geometry                       src/Mesh/Geometry.cpp:29-169
+//   initial condition (LSQ)        src/Solver/InitialCondition.cpp:85-149
+//   volume / face quadrature       src/Solver/SpatialDiscrete.cpp:194-322, 633-968
+//   residual assembly              src/Solver/SpatialDiscrete.cpp:1016-1068
+//   RK update, dt, relative error  src/Solver/TimeIntegration.cpp:45-324
+// Periodic pairing uses a node map (master node per slave node) in place of gmsh's periodic entity
+// queries; the right rotation of a periodic face is taken from the parents' face vertex order, the
+// same rule as for ordinary interior faces.
+#include <omp.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../include/sdg_gpu.h"
+#include "orc_basis.hpp"
+#include "orc_physics.hpp"
+
+namespace orc {
+
+struct Block {
+  int type = 0;
+  RefElement ref;
+  int64_t ne = 0;
+  std::vector<int> verts;       // ne * nvert
+  std::vector<double> qcoord;   // ne * nq * 3
+  std::vector<double> jw;       // ne * nq        |J| w
+  std::vector<double> jtiw;     // ne * nq * d*d  J^-T |J| w, column-major d x d per point
+  std::vector<double> minv;     // ne * nb*nb     local mass matrix inverse
+  std::vector<double> minEdge;  // ne
+  // state (column-major nv x nb per element: index b*nv + v)
+  std::vector<double> coef, last, res;
+  std::vector<double> qvol;     // ne * nv x (nq*d)
+  std::vector<double> qface;    // ne * nv x (nface*nfq)
+  // gradient blocks, rows (v*d + k)
+  std::vector<double> qvg, qfvg, qfig, rvg, rig, vgc, igc, gc;
+};
+
+struct Face {
+  int bl = 0, el = 0, fl = 0, br = -1, er = -1, fr = -1, rot = 0;
+  int physical = 0, bc = -1;
+  std::vector<double> normal;  // nfq * 3
+  std::vector<double> fjw;     // nfq
+  std::vector<double> coord;   // nfq * 3
+};
+
+struct Problem {
+  int dim = 2, nv = 4, p = 1;
+  int eq = 0, flux = 0, visc = 0, rk = 2;
+  bool faithful = true;
+  Physics ph;
+  std::vector<Block> blocks;
+  std::vector<Face> interior, boundary;
+  std::vector<PointVar> dummy;  // boundary dummy variables, [boundary][nfq]
+  std::vector<double> relErr;
+  int64_t totalElements = 0;
+  bool hasState = false;
+  std::string err;
+
+  bool ns() const { return eq == 1; }
+  int nfq() const { return blocks[0].ref.nfq; }
+};
+
+// ---- setup ----------------------------------------------------------------------------------------
+
+static void buildGeometry(Problem& P, Block& B, const double* nodes) {
+  const RefElement& R = B.ref;
+  const int d = P.dim, nq = R.nq, nb = R.nb, nvert = elemVerts(B.type);
+  B.qcoord.assign(size_t(B.ne) * nq * 3, 0.0);
+  B.jw.assign(size_t(B.ne) * nq, 0.0);
+  B.jtiw.assign(size_t(B.ne) * nq * d * d, 0.0);
+  B.minv.assign(size_t(B.ne) * nb * nb, 0.0);
+  B.minEdge.assign(size_t(B.ne), 0.0);
+  std::string failure;
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < B.ne; ++e) {
+    const int* vv = &B.verts[size_t(e) * nvert];
+    for (int q = 0; q < nq; ++q) {
+      double sh[8], g[24];
+      elemShape(B.type, &R.vq.x[q * 3], sh, g);
+      double J[3][3] = {{0}};  // J[l][k] = d x_l / d xi_k
+      double x[3] = {0, 0, 0};
+      for (int v = 0; v < nvert; ++v) {
+        const double* c = &nodes[size_t(vv[v]) * 3];
+        for (int l = 0; l < 3; ++l) x[l] += sh[v] * c[l];
+        for (int l = 0; l < d; ++l)
+          for (int k = 0; k < d; ++k) J[l][k] += g[v * 3 + k] * c[l];
+      }
+      for (int l = 0; l < 3; ++l) B.qcoord[(size_t(e) * nq + q) * 3 + l] = x[l];
+      double det, inv[3][3];
+      if (d == 2) {
+        det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        inv[0][0] = J[1][1] / det; inv[0][1] = -J[0][1] / det; inv[1][0] = -J[1][0] / det; inv[1][1] = J[0][0] / det;
+      } else {
+        det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+              J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+        inv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+        inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+        inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+        inv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+        inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+        inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+        inv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+        inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+        inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+      }
+      if (!(det > 0.0)) {
+#pragma omp critical
+        failure = "inverted or degenerate element";
+      }
+      const double jw = det * R.vq.w[q];
+      B.jw[size_t(e) * nq + q] = jw;
+      // M(a,b) = (J^-T)(a,b) |J| w = (J^-1)(b,a) |J| w, stored column-major at [a + b*d].
+      for (int a = 0; a < d; ++a)
+        for (int b = 0; b < d; ++b) B.jtiw[(size_t(e) * nq + q) * d * d + a + b * d] = inv[b][a] * jw;
+    }
+    // Local mass matrix inverse (Geometry.cpp:88-100).
+    std::vector<double> m(size_t(nb) * nb, 0.0);
+    for (int a = 0; a < nb; ++a)
+      for (int b = 0; b < nb; ++b) {
+        double s = 0;
+        for (int q = 0; q < nq; ++q) s += R.phi[size_t(q) * nb + a] * R.phi[size_t(q) * nb + b] * B.jw[size_t(e) * nq + q];
+        m[size_t(a) * nb + b] = s;
+      }
+    invert(nb, m.data(), &B.minv[size_t(e) * nb * nb]);
+    // minEdge quality: shortest straight edge between vertices.
+    static const int triE[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+    static const int quadE[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+    static const int hexE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                    {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+    const int(*E)[2] = B.type == kTri ? triE : (B.type == kQuad ? quadE : hexE);
+    const int nE = B.type == kTri ? 3 : (B.type == kQuad ? 4 : 12);
+    double me = 1e300;
+    for (int i = 0; i < nE; ++i) {
+      const double* a = &nodes[size_t(vv[E[i][0]]) * 3];
+      const double* b = &nodes[size_t(vv[E[i][1]]) * 3];
+      const double l = std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+      me = std::min(me, l);
+    }
+    B.minEdge[e] = me;
+  }
+  if (!failure.empty()) throw std::runtime_error(failure);
+}
+
+static void faceGeometry(Problem& P, Face& F, const double* nodes) {
+  const Block& B = P.blocks[F.bl];
+  const RefElement& R = B.ref;
+  const int nfv = faceVerts(B.type), nfq = R.nfq;
+  const int* ft = faceVertexTable(B.type);
+  const int* vv = &B.verts[size_t(F.el) * elemVerts(B.type)];
+  F.normal.assign(size_t(nfq) * 3, 0.0); F.fjw.assign(nfq, 0.0); F.coord.assign(size_t(nfq) * 3, 0.0);
+  for (int j = 0; j < nfq; ++j) {
+    double sh[4], dxi[4], deta[4];
+    faceShape(B.type, &R.fq.x[j * 3], sh);
+    faceShapeGrad(B.type, &R.fq.x[j * 3], dxi, deta);
+    double x[3] = {0, 0, 0}, tx[3] = {0, 0, 0}, ty[3] = {0, 0, 0};
+    for (int k = 0; k < nfv; ++k) {
+      const double* c = &nodes[size_t(vv[ft[F.fl * nfv + k]]) * 3];
+      for (int l = 0; l < 3; ++l) { x[l] += sh[k] * c[l]; tx[l] += dxi[k] * c[l]; if (nfv == 4) ty[l] += deta[k] * c[l]; }
+    }
+    for (int l = 0; l < 3; ++l) F.coord[j * 3 + l] = x[l];
+    double n[3], det;
+    if (P.dim == 2) {  // Geometry.cpp:115-127
+      det = std::sqrt(tx[0] * tx[0] + tx[1] * tx[1]);
+      n[0] = tx[1] / det; n[1] = -tx[0] / det; n[2] = 0;
+    } else {           // Geometry.cpp:130-147
+      const double cx = tx[1] * ty[2] - tx[2] * ty[1], cy = tx[2] * ty[0] - tx[0] * ty[2], cz = tx[0] * ty[1] - tx[1] * ty[0];
+      det = std::sqrt(cx * cx + cy * cy + cz * cz);
+      n[0] = cx / det; n[1] = cy / det; n[2] = cz / det;
+    }
+    for (int l = 0; l < 3; ++l) F.normal[j * 3 + l] = n[l];
+    F.fjw[j] = det * R.fq.w[j];
+  }
+}
+
+static void buildAdjacency(Problem& P, const sdg_mesh& m) {
+  struct Visit { int b, e, f; std::vector<int> mapped; };
+  struct Entry { Visit left; Visit right; int count = 0; };
+  std::map<std::vector<int>, Entry> faces;
+  auto master = [&](int v) { return m.periodic_master ? m.periodic_master[v] : v; };
+  for (int b = 0; b < int(P.blocks.size()); ++b) {
+    const Block& B = P.blocks[b];
+    const int nfv = faceVerts(B.type), nf = elemFaces(B.type), nvert = elemVerts(B.type);
+    const int* ft = faceVertexTable(B.type);
+    for (int64_t e = 0; e < B.ne; ++e)
+      for (int f = 0; f < nf; ++f) {
+        Visit v{b, int(e), f, {}};
+        for (int k = 0; k < nfv; ++k) v.mapped.push_back(master(B.verts[size_t(e) * nvert + ft[f * nfv + k]]));
+        std::vector<int> key = v.mapped; std::sort(key.begin(), key.end());
+        Entry& en = faces[key];
+        if (en.count == 0) en.left = v;
+        else if (en.count == 1) en.right = v;
+        else throw std::runtime_error("a face is recorded more than twice");
+        en.count++;
+      }
+  }
+  std::map<std::vector<int>, int> bmap;
+  const int nbv = P.dim == 2 ? 2 : 4;
+  for (int64_t i = 0; i < m.boundary_count; ++i) {
+    std::vector<int> key;
+    for (int k = 0; k < nbv; ++k) key.push_back(master(m.boundary_node[i * nbv + k]));
+    std::sort(key.begin(), key.end());
+    bmap[key] = int(i);
+  }
+  for (auto& kv : faces) {
+    Entry& en = kv.second;
+    Face F;
+    F.bl = en.left.b; F.el = en.left.e; F.fl = en.left.f;
+    if (en.count == 2) {
+      F.br = en.right.b; F.er = en.right.e; F.fr = en.right.f;
+      if (P.dim == 3) {
+        const auto it = std::find(en.right.mapped.begin(), en.right.mapped.end(), en.left.mapped[0]);
+        F.rot = int(it - en.right.mapped.begin());
+      }
+      P.interior.push_back(F);
+    } else {
+      const auto it = bmap.find(kv.first);
+      if (it == bmap.end()) throw std::runtime_error("boundary face without a boundary element");
+      F.physical = m.boundary_physical[it->second];
+      if (F.physical < 1 || F.physical > m.physical_count) throw std::runtime_error("bad physical index");
+      F.bc = m.physical_boundary_condition[F.physical - 1];
+      if (F.bc == SDG_BC_PERIODIC) throw std::runtime_error("unpaired periodic face");
+      P.boundary.push_back(F);
+    }
+  }
+}
+
+// ---- point evaluation helpers ---------------------------------------------------------------------
+
+// vals[q][v] = sum_b coef(v,b) phi[q][b] for rows q of a phi table.
+static inline void interp(int nv, int nb, int nrow, const double* coef, const double* phi, double* vals) {
+  for (int q = 0; q < nrow; ++q)
+    for (int v = 0; v < nv; ++v) {
+      double s = 0;
+      for (int b = 0; b < nb; ++b) s += coef[b * nv + v] * phi[size_t(q) * nb + b];
+      vals[q * nv + v] = s;
+    }
+}
+
+// Element-face trace (AdjacencyElementVariable::compute, VariableConvertor.cpp:434-451).
+static void trace(const Problem& P, int b, int e, int f, PointVar* out) {
+  const Block& B = P.blocks[b];
+  const int nv = P.nv, nb = B.ref.nb, nfq = B.ref.nfq;
+  double vals[64 * kMaxVar];
+  interp(nv, nb, nfq, &B.coef[size_t(e) * nv * nb], &B.ref.phif[size_t(f) * nfq * nb], vals);
+  for (int j = 0; j < nfq; ++j) {
+    for (int v = 0; v < nv; ++v) out[j].cons[v] = vals[j * nv + v];
+    computationalFromConserved(P.ph, out[j]);
+  }
+}
+
+// Gradient trace on face f: BR1 -> gc; BR2 -> vgc + igc[f]; conserved gradient rows (v*d+k).
+static void gradientTrace(const Problem& P, int b, int e, int f, double* out /* nfq * nv*d */) {
+  const Block& B = P.blocks[b];
+  const int nr = P.nv * P.dim, nb = B.ref.nb, nfq = B.ref.nfq;
+  std::vector<double> c(size_t(nr) * nb);
+  if (P.visc == 1) {
+    std::copy_n(&B.gc[size_t(e) * nr * nb], nr * nb, c.data());
+  } else {
+    const double* a = &B.vgc[size_t(e) * nr * nb];
+    const double* g = &B.igc[(size_t(e) * B.ref.nface + f) * nr * nb];
+    for (int i = 0; i < nr * nb; ++i) c[i] = a[i] + g[i];
+  }
+  interp(nr, nb, nfq, c.data(), &B.ref.phif[size_t(f) * nfq * nb], out);
+}
+
+// ---- the stage kernels ----------------------------------------------------------------------------
+
+static void gradientQuadratureAndResidual(Problem& P) {
+  const int d = P.dim, nv = P.nv, nr = nv * d;
+  // volume part (SpatialDiscrete.cpp:294-322)
+  for (Block& B : P.blocks) {
+    const int nq = B.ref.nq, nb = B.ref.nb;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      double vals[216 * kMaxVar];
+      interp(nv, nb, nq, &B.coef[size_t(e) * nv * nb], B.ref.phi.data(), vals);
+      double* Q = &B.qvg[size_t(e) * nr * nq * d];
+      for (int q = 0; q < nq; ++q) {
+        const double* M = &B.jtiw[(size_t(e) * nq + q) * d * d];
+        for (int v = 0; v < nv; ++v)
+          for (int a = 0; a < d; ++a)
+            for (int bb = 0; bb < d; ++bb) Q[size_t(q * d + bb) * nr + v * d + a] = vals[q * nv + v] * M[a + bb * d];
+      }
+    }
+  }
+  // interior faces (SpatialDiscrete.cpp:844-911)
+  const int nfq = P.nfq();
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < int64_t(P.interior.size()); ++i) {
+    const Face& F = P.interior[i];
+    PointVar L[64], R[64];
+    trace(P, F.bl, F.el, F.fl, L); trace(P, F.br, F.er, F.fr, R);
+    Block& BL = P.blocks[F.bl]; Block& BR = P.blocks[F.br];
+    const std::vector<int>& perm = BR.ref.perm[F.rot];
+    const int nfl = BL.ref.nface * nfq, nfr = BR.ref.nface * nfq;
+    double* QL = &BL.qfvg[size_t(F.el) * nr * nfl];
+    double* QR = &BR.qfvg[size_t(F.er) * nr * nfr];
+    for (int j = 0; j < nfq; ++j) {
+      const int jr = perm[j];
+      const double* n = &F.normal[j * 3];
+      for (int v = 0; v < nv; ++v)
+        for (int k = 0; k < d; ++k) {
+          const double t = n[k] * (L[j].cons[v] + R[jr].cons[v]) / 2.0 * F.fjw[j];
+          QL[size_t(F.fl * nfq + j) * nr + v * d + k] = t;
+          QR[size_t(F.fr * nfq + jr) * nr + v * d + k] = -t;
+        }
+      if (P.ns()) {
+        double* IL = &BL.qfig[size_t(F.el) * nr * nfl];
+        double* IR = &BR.qfig[size_t(F.er) * nr * nfr];
+        for (int v = 0; v < nv; ++v)
+          for (int k = 0; k < d; ++k) {
+            const double t = n[k] * (R[jr].cons[v] - L[j].cons[v]) / 2.0 * F.fjw[j];
+            IL[size_t(F.fl * nfq + j) * nr + v * d + k] = t;
+            IR[size_t(F.fr * nfq + jr) * nr + v * d + k] = t;
+          }
+      }
+    }
+  }
+  // boundary faces (SpatialDiscrete.cpp:913-968)
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < int64_t(P.boundary.size()); ++i) {
+    const Face& F = P.boundary[i];
+    PointVar L[64];
+    trace(P, F.bl, F.el, F.fl, L);
+    Block& BL = P.blocks[F.bl];
+    const int nfl = BL.ref.nface * nfq;
+    for (int j = 0; j < nfq; ++j) {
+      double vol[kMaxVar], itf[kMaxVar];
+      boundaryGradientState(P.ph, F.bc, &F.normal[j * 3], L[j], P.dummy[size_t(i) * nfq + j], vol, itf);
+      const double* n = &F.normal[j * 3];
+      for (int v = 0; v < nv; ++v)
+        for (int k = 0; k < d; ++k) {
+          BL.qfvg[size_t(F.el) * nr * nfl + size_t(F.fl * nfq + j) * nr + v * d + k] = n[k] * vol[v] * F.fjw[j];
+          if (P.ns()) BL.qfig[size_t(F.el) * nr * nfl + size_t(F.fl * nfq + j) * nr + v * d + k] = n[k] * itf[v] * F.fjw[j];
+        }
+    }
+  }
+  // gradient residual and coefficients (SpatialDiscrete.cpp:1034-1068, TimeIntegration.cpp:200-228)
+  for (Block& B : P.blocks) {
+    const int nq = B.ref.nq, nb = B.ref.nb, nf = B.ref.nface, nfl = nf * nfq;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      const double* QF = &B.qfvg[size_t(e) * nr * nfl];
+      const double* QV = &B.qvg[size_t(e) * nr * nq * d];
+      double* RV = &B.rvg[size_t(e) * nr * nb];
+      for (int bb = 0; bb < nb; ++bb)
+        for (int r = 0; r < nr; ++r) {
+          double s = 0;
+          for (int c = 0; c < nfl; ++c) s += QF[size_t(c) * nr + r] * B.ref.phif[size_t(c) * nb + bb];
+          for (int c = 0; c < nq * d; ++c) s -= QV[size_t(c) * nr + r] * B.ref.dphi[size_t(c) * nb + bb];
+          RV[size_t(bb) * nr + r] = s;
+        }
+      const double* Mi = &B.minv[size_t(e) * nb * nb];
+      double* VG = &B.vgc[size_t(e) * nr * nb];
+      for (int bb = 0; bb < nb; ++bb)
+        for (int r = 0; r < nr; ++r) {
+          double s = 0; for (int c = 0; c < nb; ++c) s += RV[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
+          VG[size_t(bb) * nr + r] = s;
+        }
+      if (!P.ns()) continue;
+      double* G = &B.gc[size_t(e) * nr * nb];
+      std::copy_n(VG, nr * nb, G);
+      const double* QI = &B.qfig[size_t(e) * nr * nfl];
+      const int nblk = P.visc == 1 ? 1 : nf;
+      for (int blk = 0; blk < nblk; ++blk) {
+        const int c0 = P.visc == 1 ? 0 : blk * nfq, c1 = P.visc == 1 ? nfl : (blk + 1) * nfq;
+        double* RI = &B.rig[(size_t(e) * nblk + blk) * nr * nb];
+        for (int bb = 0; bb < nb; ++bb)
+          for (int r = 0; r < nr; ++r) {
+            double s = 0;
+            for (int c = c0; c < c1; ++c) s += QI[size_t(c) * nr + r] * B.ref.phif[size_t(c) * nb + bb];
+            RI[size_t(bb) * nr + r] = s;
+          }
+        double* IG = &B.igc[(size_t(e) * nblk + blk) * nr * nb];
+        for (int bb = 0; bb < nb; ++bb)
+          for (int r = 0; r < nr; ++r) {
+            double s = 0; for (int c = 0; c < nb; ++c) s += RI[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
+            IG[size_t(bb) * nr + r] = s;
+            G[size_t(bb) * nr + r] += s;
+          }
+      }
+    }
+  }
+}
+
+static void quadratureAndResidual(Problem& P) {
+  const int d = P.dim, nv = P.nv, nr = nv * d;
+  // volume (SpatialDiscrete.cpp:194-266)
+  for (Block& B : P.blocks) {
+    const int nq = B.ref.nq, nb = B.ref.nb;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      double vals[216 * kMaxVar];
+      std::vector<double> gvals;
+      interp(nv, nb, nq, &B.coef[size_t(e) * nv * nb], B.ref.phi.data(), vals);
+      if (P.ns()) { gvals.resize(size_t(nq) * nr); interp(nr, nb, nq, &B.gc[size_t(e) * nr * nb], B.ref.phi.data(), gvals.data()); }
+      double* Q = &B.qvol[size_t(e) * nv * nq * d];
+      for (int q = 0; q < nq; ++q) {
+        PointVar v; for (int i = 0; i < nv; ++i) v.cons[i] = vals[q * nv + i];
+        computationalFromConserved(P.ph, v);
+        double F[3][kMaxVar]; rawFlux(P.ph, v, F);
+        if (P.ns()) {
+          double pg[15]; primitiveGradient(P.ph, v, &gvals[size_t(q) * nr], pg);
+          for (int k = 0; k < d; ++k) {
+            double nk[3] = {0, 0, 0}; nk[k] = 1.0;
+            double fv[kMaxVar]; viscousNormalFlux(P.ph, nk, v, pg, fv);
+            for (int i = 0; i < nv; ++i) F[k][i] -= fv[i];
+          }
+        }
+        const double* M = &B.jtiw[(size_t(e) * nq + q) * d * d];
+        for (int i = 0; i < nv; ++i)
+          for (int bb = 0; bb < d; ++bb) {
+            double s = 0; for (int a = 0; a < d; ++a) s += F[a][i] * M[a + bb * d];
+            Q[size_t(q * d + bb) * nv + i] = s;
+          }
+      }
+    }
+  }
+  const int nfq = P.nfq();
+  // interior faces (SpatialDiscrete.cpp:633-748)
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < int64_t(P.interior.size()); ++i) {
+    const Face& F = P.interior[i];
+    PointVar L[64], R[64];
+    trace(P, F.bl, F.el, F.fl, L); trace(P, F.br, F.er, F.fr, R);
+    Block& BL = P.blocks[F.bl]; Block& BR = P.blocks[F.br];
+    const std::vector<int>& perm = BR.ref.perm[F.rot];
+    std::vector<double> gl, gr;
+    if (P.ns()) {
+      gl.resize(size_t(nfq) * nr); gr.resize(size_t(nfq) * nr);
+      gradientTrace(P, F.bl, F.el, F.fl, gl.data()); gradientTrace(P, F.br, F.er, F.fr, gr.data());
+    }
+    double* QL = &BL.qface[size_t(F.el) * nv * BL.ref.nface * nfq];
+    double* QR = &BR.qface[size_t(F.er) * nv * BR.ref.nface * nfq];
+    for (int j = 0; j < nfq; ++j) {
+      const int jr = perm[j];
+      const double* n = &F.normal[j * 3];
+      double h[kMaxVar]; convectiveFlux(P.ph, P.flux, n, L[j], R[jr], h);
+      if (P.ns()) {
+        double pl[15], pr[15], fl[kMaxVar], fr[kMaxVar];
+        primitiveGradient(P.ph, L[j], &gl[size_t(j) * nr], pl);
+        primitiveGradient(P.ph, R[jr], &gr[size_t(jr) * nr], pr);
+        viscousNormalFlux(P.ph, n, L[j], pl, fl); viscousNormalFlux(P.ph, n, R[jr], pr, fr);
+        for (int v = 0; v < nv; ++v) h[v] -= (fl[v] + fr[v]) / 2.0;
+      }
+      for (int v = 0; v < nv; ++v) {
+        const double t = h[v] * F.fjw[j];
+        QL[size_t(F.fl * nfq + j) * nv + v] = t;
+        QR[size_t(F.fr * nfq + jr) * nv + v] = -t;
+      }
+    }
+  }
+  // boundary faces (SpatialDiscrete.cpp:750-842)
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < int64_t(P.boundary.size()); ++i) {
+    const Face& F = P.boundary[i];
+    PointVar L[64];
+    trace(P, F.bl, F.el, F.fl, L);
+    Block& BL = P.blocks[F.bl];
+    std::vector<double> gl;
+    if (P.ns()) { gl.resize(size_t(nfq) * nr); gradientTrace(P, F.bl, F.el, F.fl, gl.data()); }
+    double* QL = &BL.qface[size_t(F.el) * nv * BL.ref.nface * nfq];
+    for (int j = 0; j < nfq; ++j) {
+      const double* n = &F.normal[j * 3];
+      PointVar b{};
+      boundaryState(P.ph, F.bc, n, L[j], P.dummy[size_t(i) * nfq + j], b);
+      double h[kMaxVar]; normalFlux(P.ph, n, b, h);
+      if (P.ns()) {
+        double pl[15]; primitiveGradient(P.ph, L[j], &gl[size_t(j) * nr], pl);
+        double pb[15]; std::copy_n(pl, nr, pb);
+        PointVar lm = L[j];
+        if (F.bc >= 3) { lm.rho = b.rho; for (int k = 0; k < 3; ++k) lm.u[k] = b.u[k]; lm.e = b.e; lm.p = b.p; }
+        if (F.bc >= 4) for (int k = 0; k < d; ++k) pb[(d + 1) * d + k] = 0.0;
+        double fl[kMaxVar], fb[kMaxVar];
+        viscousNormalFlux(P.ph, n, lm, pl, fl); viscousNormalFlux(P.ph, n, b, pb, fb);
+        for (int v = 0; v < nv; ++v) h[v] -= (fl[v] + fb[v]) / 2.0;
+      }
+      for (int v = 0; v < nv; ++v) QL[size_t(F.fl * nfq + j) * nv + v] = h[v] * F.fjw[j];
+    }
+  }
+  // residual (SpatialDiscrete.cpp:1016-1032)
+  for (Block& B : P.blocks) {
+    const int nq = B.ref.nq, nb = B.ref.nb, nfl = B.ref.nface * nfq;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      const double* QV = &B.qvol[size_t(e) * nv * nq * d];
+      const double* QF = &B.qface[size_t(e) * nv * nfl];
+      double* Rr = &B.res[size_t(e) * nv * nb];
+      for (int bb = 0; bb < nb; ++bb)
+        for (int v = 0; v < nv; ++v) {
+          double s = 0;
+          for (int c = 0; c < nq * d; ++c) s += QV[size_t(c) * nv + v] * B.ref.dphi[size_t(c) * nb + bb];
+          for (int c = 0; c < nfl; ++c) s -= QF[size_t(c) * nv + v] * B.ref.phif[size_t(c) * nb + bb];
+          Rr[bb * nv + v] = s;
+        }
+    }
+  }
+}
+
+static const double kRk[3][3][3] = {
+    {{1.0, 0.0, 1.0}, {0, 0, 0}, {0, 0, 0}},
+    {{1.0, 0.0, 1.0}, {0.5, 0.5, 0.5}, {0, 0, 0}},
+    {{1.0, 0.0, 1.0}, {3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}}};  // TimeIntegration.cpp:45-65
+
+static void update(Problem& P, int stage, double dt) {
+  const int nv = P.nv;
+  const double* c = kRk[P.rk][stage];
+  for (Block& B : P.blocks) {
+    const int nb = B.ref.nb;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      double* U = &B.coef[size_t(e) * nv * nb];
+      const double* L = &B.last[size_t(e) * nv * nb];
+      const double* Rr = &B.res[size_t(e) * nv * nb];
+      const double* Mi = &B.minv[size_t(e) * nb * nb];
+      for (int i = 0; i < nv * nb; ++i) U[i] *= c[1];
+      for (int i = 0; i < nv * nb; ++i) U[i] += c[0] * L[i];
+      for (int bb = 0; bb < nb; ++bb)
+        for (int v = 0; v < nv; ++v) {
+          double s = 0; for (int k = 0; k < nb; ++k) s += Rr[k * nv + v] * Mi[size_t(k) * nb + bb];
+          U[bb * nv + v] += c[2] * dt * s;
+        }
+    }
+  }
+}
+
+static void relativeError(Problem& P) {
+  const int nv = P.nv;
+  std::vector<double> acc(nv, 0.0);
+  for (Block& B : P.blocks) {
+    const int nq = B.ref.nq, nb = B.ref.nb;
+    std::vector<double> part(size_t(omp_get_max_threads()) * nv, 0.0);
+#pragma omp parallel
+    {
+      double* my = &part[size_t(omp_get_thread_num()) * nv];
+#pragma omp for schedule(static)
+      for (int64_t e = 0; e < B.ne; ++e) {
+        double vals[216 * kMaxVar];
+        interp(nv, nb, nq, &B.res[size_t(e) * nv * nb], B.ref.phi.data(), vals);
+        for (int v = 0; v < nv; ++v) {
+          double s = 0; for (int q = 0; q < nq; ++q) s += std::fabs(vals[q * nv + v]);
+          my[v] += s / nq;
+        }
+      }
+    }
+    for (size_t t = 0; t < part.size() / nv; ++t)
+      for (int v = 0; v < nv; ++v) acc[v] += part[t * nv + v];
+  }
+  for (int v = 0; v < nv; ++v) P.relErr[v] = acc[v] / double(P.totalElements);
+}
+
+static void step(Problem& P, double dt) {
+  for (Block& B : P.blocks) B.last = B.coef;  // TimeIntegration.cpp:70-102
+  const int nstage = P.rk + 1;
+  for (int s = 0; s < nstage; ++s) {
+    if (P.ns() || P.faithful) gradientQuadratureAndResidual(P);
+    quadratureAndResidual(P);
+    update(P, s, dt);
+  }
+  relativeError(P);
+}
+
+// LSQ projection of point values (InitialCondition.cpp:91-104): coef = U_q Phi (Phi^T Phi)^-1.
+static void project(Problem& P, const double* cons) {
+  const int nv = P.nv;
+  size_t off = 0;
+  for (Block& B : P.blocks) {
+    const int nq = B.ref.nq, nb = B.ref.nb;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      const double* u = &cons[(off + size_t(e) * nq) * nv];
+      std::vector<double> t(size_t(nv) * nb, 0.0);
+      for (int b = 0; b < nb; ++b)
+        for (int v = 0; v < nv; ++v) {
+          double s = 0; for (int q = 0; q < nq; ++q) s += u[q * nv + v] * B.ref.phi[size_t(q) * nb + b];
+          t[b * nv + v] = s;
+        }
+      double* U = &B.coef[size_t(e) * nv * nb];
+      for (int b = 0; b < nb; ++b)
+        for (int v = 0; v < nv; ++v) {
+          double s = 0; for (int k = 0; k < nb; ++k) s += t[k * nv + v] * B.ref.lsqInv[size_t(k) * nb + b];
+          U[b * nv + v] = s;
+        }
+    }
+    off += size_t(B.ne) * nq;
+  }
+  P.hasState = true;
+}
+
+static Problem* create(const sdg_mesh* m, const sdg_config* c, int faithful) {
+  auto P = std::make_unique<Problem>();
+  P->dim = m->dimension; P->nv = P->dim + 2; P->p = c->polynomial_order;
+  P->eq = c->equation; P->flux = c->convective_flux; P->visc = c->viscous_flux; P->rk = c->time_integration;
+  P->faithful = faithful != 0;
+  P->ph.dim = P->dim; P->ph.gamma = c->specific_heat_ratio; P->ph.cp = c->specific_heat_constant_pressure;
+  P->ph.cv = c->specific_heat_constant_volume; P->ph.mu = c->dynamic_viscosity; P->ph.pr = c->prandtl_number;
+  P->ph.transport = c->transport_model;
+  P->ph.kappa = P->ph.cp * P->ph.mu / P->ph.pr;  // PhysicalModel.cpp:149-153
+  if (P->ns() && P->visc == 0) throw std::runtime_error("NS needs BR1 or BR2");
+  struct Src { int type; int64_t n; const int32_t* v; };
+  std::vector<Src> src;
+  if (P->dim == 2) { src.push_back({kTri, m->triangle_count, m->triangle_node}); src.push_back({kQuad, m->quadrangle_count, m->quadrangle_node}); }
+  else src.push_back({kHex, m->hexahedron_count, m->hexahedron_node});
+  for (const Src& s : src) {
+    if (s.n <= 0) continue;
+    Block B; B.type = s.type; B.ne = s.n;
+    B.ref.build(s.type, P->p);
+    B.verts.assign(s.v, s.v + size_t(s.n) * elemVerts(s.type));
+    P->blocks.push_back(std::move(B));
+  }
+  if (P->blocks.empty()) throw std::runtime_error("mesh has no elements");
+  for (Block& B : P->blocks) {
+    buildGeometry(*P, B, m->node_coordinate);
+    P->totalElements += B.ne;
+    const int nv = P->nv, nb = B.ref.nb, nq = B.ref.nq, d = P->dim, nr = nv * d, nfl = B.ref.nface * B.ref.nfq;
+    B.coef.assign(size_t(B.ne) * nv * nb, 0.0); B.last = B.coef; B.res = B.coef;
+    B.qvol.assign(size_t(B.ne) * nv * nq * d, 0.0);
+    B.qface.assign(size_t(B.ne) * nv * nfl, 0.0);
+    if (P->ns() || P->faithful) {
+      B.qvg.assign(size_t(B.ne) * nr * nq * d, 0.0);
+      B.qfvg.assign(size_t(B.ne) * nr * nfl, 0.0);
+      B.rvg.assign(size_t(B.ne) * nr * nb, 0.0);
+      B.vgc.assign(size_t(B.ne) * nr * nb, 0.0);
+    }
+    if (P->ns()) {
+      const int nblk = P->visc == 1 ? 1 : B.ref.nface;
+      B.qfig.assign(size_t(B.ne) * nr * nfl, 0.0);
+      B.rig.assign(size_t(B.ne) * nblk * nr * nb, 0.0);
+      B.igc.assign(size_t(B.ne) * nblk * nr * nb, 0.0);
+      B.gc.assign(size_t(B.ne) * nr * nb, 0.0);
+    }
+  }
+  buildAdjacency(*P, *m);
+  for (Face& F : P->interior) faceGeometry(*P, F, m->node_coordinate);
+  for (Face& F : P->boundary) faceGeometry(*P, F, m->node_coordinate);
+  P->dummy.assign(P->boundary.size() * size_t(P->nfq()), PointVar{});
+  P->relErr.assign(P->nv, 0.0);
+  return P.release();
+}
+
+}  // namespace orc
+
+// ---- C interface for the tests and the CPU baseline ------------------------------------------------
+extern "C" {
+
+struct orc_handle { orc::Problem* p; };
+
+static thread_local std::string g_orc_error;
+
+const char* orc_last_error() { return g_orc_error.c_str(); }
+
+void* orc_create(const sdg_mesh* mesh, const sdg_config* config, int faithful) {
+  try {
+    return orc::create(mesh, config, faithful);
+  } catch (const std::exception& e) {
+    g_orc_error = e.what();
+    return nullptr;
+  }
+}
+
+void orc_destroy(void* h) { delete static_cast<orc::Problem*>(h); }
+
+void orc_set_threads(int n) { if (n > 0) omp_set_num_threads(n); }
+int orc_max_threads() { return omp_get_max_threads(); }
+
+// counts: [element_count, volume_point_count, interior_faces, boundary_faces, nfq, dof]
+void orc_counts(void* h, int64_t* out) {
+  const orc::Problem& P = *static_cast<orc::Problem*>(h);
+  int64_t vp = 0, dof = 0;
+  for (const auto& B : P.blocks) { vp += B.ne * B.ref.nq; dof += B.ne * B.ref.nb * P.nv; }
+  out[0] = P.totalElements; out[1] = vp; out[2] = int64_t(P.interior.size()); out[3] = int64_t(P.boundary.size());
+  out[4] = P.nfq(); out[5] = dof;
+}
+
+void orc_volume_point_coordinate(void* h, double* out) {
+  const orc::Problem& P = *static_cast<orc::Problem*>(h);
+  size_t off = 0;
+  for (const auto& B : P.blocks) { std::copy(B.qcoord.begin(), B.qcoord.end(), out + off); off += B.qcoord.size(); }
+}
+
+void orc_boundary_point_coordinate(void* h, double* out, int32_t* physical) {
+  const orc::Problem& P = *static_cast<orc::Problem*>(h);
+  const int nfq = P.nfq();
+  for (size_t i = 0; i < P.boundary.size(); ++i) {
+    std::copy(P.boundary[i].coord.begin(), P.boundary[i].coord.end(), out + i * nfq * 3);
+    if (physical) physical[i] = P.boundary[i].physical;
+  }
+}
+
+int orc_set_initial_primitive(void* h, const double* prim) {
+  orc::Problem& P = *static_cast<orc::Problem*>(h);
+  int64_t c[6]; orc_counts(h, c);
+  std::vector<double> cons(size_t(c[1]) * P.nv);
+  for (int64_t q = 0; q < c[1]; ++q) {
+    orc::PointVar v; orc::fromPrimitive(P.ph, &prim[q * P.nv], v);
+    for (int i = 0; i < P.nv; ++i) cons[q * P.nv + i] = v.cons[i];
+  }
+  orc::project(P, cons.data());
+  return 0;
+}
+
+int orc_set_state_point(void* h, const double* cons) {
+  orc::project(*static_cast<orc::Problem*>(h), cons);
+  return 0;
+}
+
+int orc_set_boundary_primitive(void* h, const double* prim) {
+  orc::Problem& P = *static_cast<orc::Problem*>(h);
+  for (size_t i = 0; i < P.dummy.size(); ++i) orc::fromPrimitive(P.ph, &prim[i * P.nv], P.dummy[i]);
+  return 0;
+}
+
+int orc_get_state_point(void* h, double* out) {
+  const orc::Problem& P = *static_cast<orc::Problem*>(h);
+  size_t off = 0;
+  for (const auto& B : P.blocks) {
+    for (int64_t e = 0; e < B.ne; ++e)
+      orc::interp(P.nv, B.ref.nb, B.ref.nq, &B.coef[size_t(e) * P.nv * B.ref.nb], B.ref.phi.data(),
+                  out + (off + size_t(e) * B.ref.nq) * P.nv);
+    off += size_t(B.ne) * B.ref.nq;
+  }
+  return 0;
+}
+
+int orc_get_state_modal(void* h, double* out) {
+  const orc::Problem& P = *static_cast<orc::Problem*>(h);
+  size_t off = 0;
+  for (const auto& B : P.blocks) { std::copy(B.coef.begin(), B.coef.end(), out + off); off += B.coef.size(); }
+  return 0;
+}
+
+int orc_calculate_delta_time(void* h, double cfl, double* dt) {
+  orc::Problem& P = *static_cast<orc::Problem*>(h);
+  double best = 1.79769313486231570e308;
+  for (const auto& B : P.blocks) {
+    const int nq = B.ref.nq, nb = B.ref.nb;
+    for (int64_t e = 0; e < B.ne; ++e) {
+      double vals[216 * orc::kMaxVar];
+      orc::interp(P.nv, nb, nq, &B.coef[size_t(e) * P.nv * nb], B.ref.phi.data(), vals);
+      for (int q = 0; q < nq; ++q) {
+        orc::PointVar v; for (int i = 0; i < P.nv; ++i) v.cons[i] = vals[q * P.nv + i];
+        orc::computationalFromConserved(P.ph, v);
+        const double c = P.ph.soundSpeed(v.rho, v.p);
+        const double sr = std::sqrt(v.u2(P.dim)) + c;
+        const double t = cfl * B.minEdge[e] / (sr * (P.p + 1.0) * (P.p + 1.0));  // TimeIntegration.cpp:119-125
+        best = std::min(best, t);
+      }
+    }
+  }
+  *dt = best;
+  return 0;
+}
+
+int orc_step(void* h, int n, double dt) {
+  orc::Problem& P = *static_cast<orc::Problem*>(h);
+  for (int i = 0; i < n; ++i) orc::step(P, dt);
+  return 0;
+}
+
+int orc_relative_error(void* h, double* out) {
+  const orc::Problem& P = *static_cast<orc::Problem*>(h);
+  std::copy(P.relErr.begin(), P.relErr.end(), out);
+  return 0;
+}
+
+// du/dt at the volume points for the current state (one residual evaluation, no update).
+int orc_residual_point(void* h, double* out) {
+  orc::Problem& P = *static_cast<orc::Problem*>(h);
+  if (P.ns() || P.faithful) orc::gradientQuadratureAndResidual(P);
+  orc::quadratureAndResidual(P);
+  size_t off = 0;
+  for (auto& B : P.blocks) {
+    const int nb = B.ref.nb, nq = B.ref.nq, nv = P.nv;
+    for (int64_t e = 0; e < B.ne; ++e) {
+      std::vector<double> du(size_t(nv) * nb);
+      const double* Rr = &B.res[size_t(e) * nv * nb];
+      const double* Mi = &B.minv[size_t(e) * nb * nb];
+      for (int bb = 0; bb < nb; ++bb)
+        for (int v = 0; v < nv; ++v) {
+          double s = 0; for (int k = 0; k < nb; ++k) s += Rr[k * nv + v] * Mi[size_t(k) * nb + bb];
+          du[bb * nv + v] = s;
+        }
+      orc::interp(nv, nb, nq, du.data(), B.ref.phi.data(), out + (off + size_t(e) * nq) * nv);
+    }
+    off += size_t(B.ne) * nq;
+  }
+  return 0;
+}
+
+// Canonical adjacency tuples, sorted (same definition as sdg_adjacency).
+int orc_adjacency(void* h, int32_t* interior, int32_t* boundary) {
+  const orc::Problem& P = *static_cast<orc::Problem*>(h);
+  std::vector<std::array<int32_t, 7>> in;
+  for (const auto& F : P.interior)
+    in.push_back({P.blocks[F.bl].type, F.el, F.fl, P.blocks[F.br].type, F.er, F.fr, F.rot});
+  std::sort(in.begin(), in.end());
+  for (size_t i = 0; i < in.size(); ++i) std::copy(in[i].begin(), in[i].end(), interior + i * 7);
+  std::vector<std::array<int32_t, 5>> bd;
+  for (const auto& F : P.boundary) bd.push_back({P.blocks[F.bl].type, F.el, F.fl, F.physical, F.bc});
+  std::sort(bd.begin(), bd.end());
+  for (size_t i = 0; i < bd.size(); ++i) std::copy(bd[i].begin(), bd[i].end(), boundary + i * 5);
+  return 0;
+}
+
+// Face normals and |J_f| w of every interior face point, in the sorted order of orc_adjacency
+// (for geometry parity checks): [interior][nfq][4] = (nx, ny, nz, |J_f| w).
+int orc_interior_face_geometry(void* h, double* out) {
+  const orc::Problem& P = *static_cast<orc::Problem*>(h);
+  std::vector<std::pair<std::array<int32_t, 7>, size_t>> in;
+  for (size_t i = 0; i < P.interior.size(); ++i) {
+    const auto& F = P.interior[i];
+    in.push_back({{P.blocks[F.bl].type, F.el, F.fl, P.blocks[F.br].type, F.er, F.fr, F.rot}, i});
+  }
+  std::sort(in.begin(), in.end());
+  const int nfq = P.nfq();
+  for (size_t i = 0; i < in.size(); ++i) {
+    const auto& F = P.interior[in[i].second];
+    for (int j = 0; j < nfq; ++j) {
+      for (int k = 0; k < 3; ++k) out[(i * nfq + j) * 4 + k] = F.normal[j * 3 + k];
+      out[(i * nfq + j) * 4 + 3] = F.fjw[j];
+    }
+  }
+  return 0;
+}
+
+}  // extern "C"

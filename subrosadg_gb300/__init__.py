@@ -1,0 +1,14 @@
+"""GB300-native explicit DG residual-and-update path of SubrosaDG (FP64, sm_103a).
+
+The compute path is libsdg_gpu.so (hand-written CUDA kernels behind the C ABI of
+include/sdg_gpu.h); this package is the host-side mirror of the reference's
+System/Solver interface.
+"""
+from . import _abi
+from ._abi import (ADIABATIC_NONSLIP_WALL, ADIABATIC_SLIP_WALL, BR1, BR2, CENTRAL, EULER, FORWARD_EULER, HEUN_RK2,
+                   HEXAHEDRON, HLLC, ISOTHERMAL_NONSLIP_WALL, LAX_FRIEDRICHS, NAVIER_STOKES, PERIODIC,
+                   PRESSURE_OUTFLOW, QUADRANGLE, RIEMANN_FARFIELD, ROE, SSPRK3, TRIANGLE, VELOCITY_INFLOW,
+                   VISCOUS_NONE, SdgError)
+from .solver import GpuSolver, Mesh, System, make_config
+
+__all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,962 @@
+// C ABI of the GB300 DG path (include/sdg_gpu.h): problem setup, device buffers, launches.
+//
+// sdg_create replaces Mesh<SC>::readMeshElement + Solver<SC> construction
+// (src/Mesh/ReadControl.cpp:293-335, src/Solver/InitialCondition.cpp:151-186); sdg_step replaces
+// Solver<SC>::stepSolver (src/Solver/TimeIntegration.cpp:326-350).  Every failure is returned as an
+// SDG_ERR_* code with text in sdg_last_error; nothing falls back to the CPU.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/sdg_gpu.h"
+#include "sdg_kernels.cuh"
+#include "sdg_kernels_dense.cuh"
+#include "sdg_mesh.hpp"
+#include "sdg_operators.hpp"
+
+namespace sdg {
+
+void facePointInParent(int type, int f, const double* fx, double* X) {
+  const int nfv = typeFaceVertices(type);
+  const int* fl = faceVertexList(type);
+  double sh[4];
+  if (nfv == 2) { sh[0] = 0.5 * (1 - fx[0]); sh[1] = 0.5 * (1 + fx[0]); }
+  else {
+    const double x = fx[0], y = fx[1];
+    sh[0] = 0.25 * (1 - x) * (1 - y); sh[1] = 0.25 * (1 + x) * (1 - y);
+    sh[2] = 0.25 * (1 + x) * (1 + y); sh[3] = 0.25 * (1 - x) * (1 + y);
+  }
+  X[0] = X[1] = X[2] = 0.0;
+  for (int k = 0; k < nfv; ++k) {
+    double V[3]; referenceVertex(type, fl[f * nfv + k], V);
+    for (int d = 0; d < 3; ++d) X[d] += sh[k] * V[d];
+  }
+}
+
+namespace {
+
+struct Failure : std::runtime_error {
+  int code;
+  Failure(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define SDG_CUDA(call)                                                                              \
+  do {                                                                                              \
+    cudaError_t _e = (call);                                                                        \
+    if (_e != cudaSuccess)                                                                          \
+      throw Failure(_e == cudaErrorMemoryAllocation ? SDG_ERR_OUT_OF_MEMORY : SDG_ERR_CUDA,          \
+                    std::string(#call) + ": " + cudaGetErrorString(_e));                            \
+  } while (0)
+
+enum Kind { kTensor = 0, kDense = 1 };
+
+struct DevBlock {
+  int type = 0, dim = 2, p = 1, n = 0, kind = kTensor, affine = 1;
+  int nb = 0, nq = 0, nface = 0, nfq = 0, ustride = 0, fstride = 0, geomStride = 0;
+  int64_t ne = 0, faceBase = 0;
+  size_t stateOffset = 0;          // doubles
+  size_t pointOffset = 0;          // volume points before this block
+  std::vector<double> qcoord;      // [e][q][3]
+  std::vector<double> qweight;     // reference weights [q]
+  std::vector<double> minEdge;     // [e]
+  std::vector<double> geomHost;
+  std::vector<double> tablesHost;
+  std::vector<double> phi;         // dense: [q][nb] ; tensor: unused
+  std::vector<double> lsq;         // dense: [nb][q] projection (Phi^T Phi)^-1 Phi^T
+  TensorOps ops;
+  double* geom = nullptr;
+  double* tables = nullptr;
+  double* minedge = nullptr;
+  double* phiDev = nullptr;
+  double* lsqDev = nullptr;
+  int threads = 0, epb = 0, grid = 0;
+  size_t smem = 0;
+  int64_t relOffset = 0;           // first partial slot of this block
+};
+
+}  // namespace
+}  // namespace sdg
+
+struct sdg_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  sdg_config cfg{};
+  sdg::Phys ph{};
+  int dim = 2, nv = 4, p = 1;
+  std::vector<sdg::DevBlock> blocks;
+  double* state[2] = {nullptr, nullptr};
+  size_t stateCount = 0;
+  double* face = nullptr;
+  size_t faceCount = 0;
+  int* fconn = nullptr; double* fgeo = nullptr; int64_t nInterior = 0;
+  int* bconn = nullptr; double* bgeo = nullptr; double* ghost = nullptr; int64_t nBoundary = 0;
+  int nfq = 0, n1d = 0;
+  std::vector<int32_t> adjInterior, adjBoundary;
+  std::vector<double> bcoord; std::vector<int32_t> bphys;
+  double* scratch = nullptr;       // point-layout conversion buffer [volume_points][nv]
+  int64_t volumePoints = 0;
+  double* relPart = nullptr; int64_t relParts = 0;
+  double* relOut = nullptr; double* dtPart = nullptr; int64_t dtParts = 0;
+  unsigned* status = nullptr;
+  double relerr[5] = {0, 0, 0, 0, 0};
+  bool hasState = false;
+  bool hostOnly = true;            // created with device < 0: no GPU resources
+  int64_t launches = 0;
+  int64_t elements = 0, dof = 0;
+  std::string err;
+};
+
+namespace {
+thread_local std::string g_create_error;
+
+using namespace sdg;
+
+template <typename T>
+T* devAlloc(size_t count) {
+  T* p = nullptr;
+  if (count == 0) count = 1;
+  SDG_CUDA(cudaMalloc(&p, count * sizeof(T)));
+  return p;
+}
+template <typename T>
+void upload(T* dst, const std::vector<T>& src, cudaStream_t s) {
+  if (!src.empty()) SDG_CUDA(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+void checkLaunch(sdg_handle* h) {
+  h->launches++;
+  SDG_CUDA(cudaGetLastError());
+}
+
+// ---- geometry --------------------------------------------------------------------------------------
+void shapeGrad(int type, const double* X, double* N, double* G /* [nv][3] */) {
+  const int nv = typeVertices(type);
+  if (type == SDG_ELEMENT_TRIANGLE) {
+    N[0] = 1 - X[0] - X[1]; N[1] = X[0]; N[2] = X[1];
+    const double g[9] = {-1, -1, 0, 1, 0, 0, 0, 1, 0};
+    std::copy(g, g + 9, G);
+    return;
+  }
+  for (int v = 0; v < nv; ++v) {
+    double R[3]; referenceVertex(type, v, R);
+    const double a = 1 + R[0] * X[0], b = 1 + R[1] * X[1];
+    if (type == SDG_ELEMENT_QUADRANGLE) {
+      N[v] = 0.25 * a * b; G[v * 3] = 0.25 * R[0] * b; G[v * 3 + 1] = 0.25 * a * R[1]; G[v * 3 + 2] = 0;
+    } else {
+      const double c = 1 + R[2] * X[2];
+      N[v] = 0.125 * a * b * c;
+      G[v * 3] = 0.125 * R[0] * b * c; G[v * 3 + 1] = 0.125 * a * R[1] * c; G[v * 3 + 2] = 0.125 * a * b * R[2];
+    }
+  }
+}
+
+// Jacobian J[l][k] = dx_l/dxi_k at reference point X, physical point x.
+void jacobianAt(int type, int dim, const double* nodes, const int32_t* vv, const double* X, double J[3][3], double* x) {
+  double N[8], G[24];
+  shapeGrad(type, X, N, G);
+  for (int l = 0; l < 3; ++l) { x[l] = 0; for (int k = 0; k < 3; ++k) J[l][k] = 0; }
+  for (int v = 0; v < typeVertices(type); ++v) {
+    const double* c = &nodes[size_t(vv[v]) * 3];
+    for (int l = 0; l < 3; ++l) x[l] += N[v] * c[l];
+    for (int l = 0; l < dim; ++l)
+      for (int k = 0; k < dim; ++k) J[l][k] += G[v * 3 + k] * c[l];
+  }
+}
+
+// |J| J^-1 (adjugate, row b = |J| dxi_b/dx) and det.
+double adjugate(int dim, const double J[3][3], double A[3][3]) {
+  if (dim == 2) {
+    A[0][0] = J[1][1]; A[0][1] = -J[0][1]; A[1][0] = -J[1][0]; A[1][1] = J[0][0];
+    return J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  }
+  A[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  A[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+  A[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+  A[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  A[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+  A[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+  A[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  A[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+  A[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  return J[0][0] * A[0][0] + J[0][1] * A[1][0] + J[0][2] * A[2][0];
+}
+
+bool isAffine(int type, const double* nodes, const int32_t* vv, double tol) {
+  if (type == SDG_ELEMENT_TRIANGLE) return true;
+  const auto P = [&](int k, int d) { return nodes[size_t(vv[k]) * 3 + d]; };
+  for (int d = 0; d < 3; ++d) {
+    if (type == SDG_ELEMENT_QUADRANGLE) {
+      if (std::fabs(P(0, d) + P(2, d) - P(1, d) - P(3, d)) > tol) return false;
+    } else {
+      const double o = P(0, d), a = P(1, d) - o, b = P(3, d) - o, c = P(4, d) - o;
+      if (std::fabs(P(2, d) - (o + a + b)) > tol || std::fabs(P(5, d) - (o + a + c)) > tol ||
+          std::fabs(P(7, d) - (o + b + c)) > tol || std::fabs(P(6, d) - (o + a + b + c)) > tol)
+        return false;
+    }
+  }
+  return true;
+}
+
+double minEdgeOf(int type, const double* nodes, const int32_t* vv) {
+  static const int triE[3][2] = {{0, 1}, {1, 2}, {2, 0}};
+  static const int quadE[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
+  static const int hexE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+  const int(*E)[2] = type == SDG_ELEMENT_TRIANGLE ? triE : (type == SDG_ELEMENT_QUADRANGLE ? quadE : hexE);
+  const int nE = type == SDG_ELEMENT_TRIANGLE ? 3 : (type == SDG_ELEMENT_QUADRANGLE ? 4 : 12);
+  double best = 1e300;
+  for (int i = 0; i < nE; ++i) {
+    double s = 0;
+    for (int d = 0; d < 3; ++d) { const double t = nodes[size_t(vv[E[i][0]]) * 3 + d] - nodes[size_t(vv[E[i][1]]) * 3 + d]; s += t * t; }
+    best = std::min(best, std::sqrt(s));
+  }
+  return best;
+}
+
+// ---- tensor tables ---------------------------------------------------------------------------------
+void buildTensorTables(DevBlock& B) {
+  TensorTables T;
+  std::memset(&T, 0, sizeof(T));
+  const TensorOps& o = B.ops;
+  const int n = o.n, dim = B.dim;
+  for (int a = 0; a < n; ++a) {
+    for (int i = 0; i < n; ++i) { T.dhat[a][i] = o.dhat[a][i]; T.b1[a][i] = o.b1[a][i]; }
+    T.endm[a] = o.endm[a]; T.endp[a] = o.endp[a]; T.liftm[a] = o.liftm[a]; T.liftp[a] = o.liftp[a]; T.w[a] = o.w[a];
+  }
+  const PointRule fr = faceRule(B.type, B.p);
+  const auto gaussIndex = [&](double t) {
+    for (int g = 0; g < n; ++g) if (std::fabs(o.x[g] - t) < 1e-12) return g;
+    throw Failure(SDG_ERR_INVALID_ARGUMENT, "face point does not lie on a Gauss line");
+  };
+  const int stride[3] = {dim == 2 ? n : n * n, dim == 2 ? 1 : n, 1};
+  for (int f = 0; f < B.nface; ++f) {
+    int axis = -1, end = 0;
+    for (int j = 0; j < B.nfq; ++j) {
+      double X[3]; facePointInParent(B.type, f, &fr.x[j * 3], X);
+      int idx[3] = {0, 0, 0};
+      int ax = -1;
+      for (int d = 0; d < dim; ++d) {
+        if (std::fabs(std::fabs(X[d]) - 1.0) < 1e-12) { ax = d; end = X[d] > 0 ? 1 : 0; idx[d] = 0; }
+        else idx[d] = gaussIndex(X[d]);
+      }
+      if (ax < 0 || (axis >= 0 && ax != axis)) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad face table");
+      axis = ax;
+      int base = 0;
+      for (int d = 0; d < dim; ++d) base += idx[d] * stride[d];
+      T.faceBase[f][j] = base;
+      for (int q = 0; q < n; ++q) T.nodeFacePoint[axis][end][base + q * stride[axis]] = (unsigned char)j;
+    }
+    T.faceAxis[f] = axis; T.faceEnd[f] = end; T.axisFace[axis][end] = f;
+  }
+  B.tablesHost.assign(sizeof(TensorTables) / 8, 0.0);
+  std::memcpy(B.tablesHost.data(), &T, sizeof(T));
+}
+
+template <int DIM, int N, bool AFF>
+void tensorConfig(DevBlock& B, bool device) {
+  using S = TensorShape<DIM, N>;
+  B.threads = S::THREADS; B.epb = S::EPB; B.smem = S::SMEM;
+  B.ustride = S::USTRIDE; B.fstride = S::FSTRIDE;
+  if (device)
+    SDG_CUDA(cudaFuncSetAttribute(tensorStageKernel<DIM, N, AFF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
+}
+
+void configureTensor(DevBlock& B, bool device) {
+  const int n = B.n;
+#define SDG_TCFG(D, NN)                                                                              \
+  if (B.dim == D && n == NN) {                                                                        \
+    if (B.affine) tensorConfig<D, NN, true>(B, device); else if constexpr (D == 2) tensorConfig<D, NN, false>(B, device); \
+    return;                                                                                           \
+  }
+  SDG_TCFG(2, 3) SDG_TCFG(2, 4) SDG_TCFG(2, 5) SDG_TCFG(2, 6)
+  SDG_TCFG(3, 2) SDG_TCFG(3, 3) SDG_TCFG(3, 4) SDG_TCFG(3, 5) SDG_TCFG(3, 6)
+#undef SDG_TCFG
+  throw Failure(SDG_ERR_UNSUPPORTED, "unsupported tensor block");
+}
+
+void launchTensor(sdg_handle* h, DevBlock& B, const StageArgs& a) {
+#define SDG_TL(D, NN)                                                                                          \
+  if (B.dim == D && B.n == NN) {                                                                               \
+    if (B.affine) tensorStageKernel<D, NN, true><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);          \
+    else if constexpr (D == 2) tensorStageKernel<D, NN, false><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph); \
+    checkLaunch(h);                                                                                            \
+    return;                                                                                                    \
+  }
+  SDG_TL(2, 3) SDG_TL(2, 4) SDG_TL(2, 5) SDG_TL(2, 6)
+  SDG_TL(3, 2) SDG_TL(3, 3) SDG_TL(3, 4) SDG_TL(3, 5) SDG_TL(3, 6)
+#undef SDG_TL
+  throw Failure(SDG_ERR_UNSUPPORTED, "unsupported tensor block");
+}
+
+void launchDense(sdg_handle* h, DevBlock& B, const StageArgs& a) {
+  if (!launchDenseStage(B.type, B.p, B.affine != 0, a, h->ph, B.grid, B.threads, B.smem, h->stream))
+    throw Failure(SDG_ERR_UNSUPPORTED, "unsupported dense block");
+  checkLaunch(h);
+}
+
+void launchFaces(sdg_handle* h) {
+  const int flux = h->cfg.convective_flux;
+  if (h->nInterior > 0) {
+    const int64_t threads = h->nInterior * h->nfq;
+    const int grid = int((threads + 255) / 256);
+#define SDG_FL(D, F) \
+  if (h->dim == D && flux == F) { faceKernel<D, F><<<grid, 256, 0, h->stream>>>(h->face, h->fconn, h->fgeo, h->nInterior, h->n1d, h->ph); }
+    SDG_FL(2, 0) SDG_FL(2, 1) SDG_FL(2, 2) SDG_FL(2, 3) SDG_FL(3, 0) SDG_FL(3, 1) SDG_FL(3, 2) SDG_FL(3, 3)
+#undef SDG_FL
+    checkLaunch(h);
+  }
+  if (h->nBoundary > 0) {
+    const int64_t threads = h->nBoundary * h->nfq;
+    const int grid = int((threads + 255) / 256);
+    if (h->dim == 2) boundaryFaceKernel<2><<<grid, 256, 0, h->stream>>>(h->face, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
+    else boundaryFaceKernel<3><<<grid, 256, 0, h->stream>>>(h->face, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
+    checkLaunch(h);
+  }
+}
+
+StageArgs baseArgs(sdg_handle* h, DevBlock& B) {
+  StageArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.face = h->face; a.geom = B.geom; a.tables = B.tables; a.status = h->status;
+  a.ne = B.ne; a.faceBase = B.faceBase;
+  return a;
+}
+
+void launchBlock(sdg_handle* h, DevBlock& B, const StageArgs& a) {
+  if (B.kind == kTensor) launchTensor(h, B, a);
+  else launchDense(h, B, a);
+}
+
+// Face traces of state buffer `which` (initial condition or after a state upload).
+void traceAll(sdg_handle* h, int which) {
+  for (DevBlock& B : h->blocks) {
+    StageArgs a = baseArgs(h, B);
+    a.uin = h->state[which] + B.stateOffset;
+    a.doTrace = 1; a.doVolume = 0; a.doUpdate = 0;
+    launchBlock(h, B, a);
+  }
+}
+
+const double kRk[3][3][3] = {{{1.0, 0.0, 1.0}, {0, 0, 0}, {0, 0, 0}},
+                             {{1.0, 0.0, 1.0}, {0.5, 0.5, 0.5}, {0, 0, 0}},
+                             {{1.0, 0.0, 1.0}, {0.75, 0.25, 0.25}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}}};  // TimeIntegration.cpp:45-65
+
+// One full RK step; state[0] holds U^n on entry and U^{n+1} on exit, the face buffer holds its traces.
+void stepOnce(sdg_handle* h, double dt, bool relerr) {
+  const int ns = h->cfg.time_integration + 1;
+  for (int s = 0; s < ns; ++s) {
+    launchFaces(h);
+    const bool last = s == ns - 1;
+    for (DevBlock& B : h->blocks) {
+      StageArgs a = baseArgs(h, B);
+      a.uin = h->state[s == 0 ? 0 : 1] + B.stateOffset;
+      a.ubase = h->state[0] + B.stateOffset;
+      a.uout = h->state[last ? 0 : 1] + B.stateOffset;
+      a.c0 = kRk[h->cfg.time_integration][s][0];
+      a.c1 = kRk[h->cfg.time_integration][s][1];
+      a.c2dt = kRk[h->cfg.time_integration][s][2] * dt;
+      a.doUpdate = 1; a.doTrace = 1; a.doVolume = 1;
+      a.relerr = (relerr && last) ? h->relPart + B.relOffset * h->nv : nullptr;
+      launchBlock(h, B, a);
+    }
+  }
+  if (relerr) {
+    relerrReduceKernel<<<h->nv, 256, 0, h->stream>>>(h->relPart, h->relParts, h->nv, 1.0 / double(h->elements), h->relOut);
+    checkLaunch(h);
+  }
+}
+
+int fail(sdg_handle* h, const Failure& f) {
+  if (h) h->err = f.what();
+  else g_create_error = f.what();
+  return f.code;
+}
+
+#define SDG_API_BEGIN try {
+#define SDG_API_END(h)                                             \
+  }                                                                \
+  catch (const Failure& f) { return fail(h, f); }                  \
+  catch (const std::exception& ex) { return fail(h, Failure(SDG_ERR_INVALID_ARGUMENT, ex.what())); }
+
+void checkStatus(sdg_handle* h) {
+  unsigned st = 0;
+  SDG_CUDA(cudaMemcpyAsync(&st, h->status, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  if (st & kStatusTimeout) throw Failure(SDG_ERR_TIMEOUT, "a bounded device wait timed out");
+}
+
+// Convert a point-layout array in h->scratch to the state buffer `which` (tensor: transpose; dense:
+// unweighted least-squares projection, InitialCondition.cpp:91-104).
+void pointsToState(sdg_handle* h, int which) {
+  for (DevBlock& B : h->blocks) {
+    const int64_t work = B.ne * (B.kind == kTensor ? B.nb : B.nb);
+    const int grid = int((work + 255) / 256);
+    pointToStateKernel<<<grid, 256, 0, h->stream>>>(h->scratch + B.pointOffset * h->nv, h->state[which] + B.stateOffset,
+                                                    B.kind == kDense ? B.lsqDev : nullptr, B.ne, B.nb, B.nq, h->nv,
+                                                    B.ustride);
+    checkLaunch(h);
+  }
+}
+void stateToPoints(sdg_handle* h, int which) {
+  for (DevBlock& B : h->blocks) {
+    const int64_t work = B.ne * B.nq;
+    const int grid = int((work + 255) / 256);
+    stateToPointKernel<<<grid, 256, 0, h->stream>>>(h->state[which] + B.stateOffset, h->scratch + B.pointOffset * h->nv,
+                                                    B.kind == kDense ? B.phiDev : nullptr, B.ne, B.nb, B.nq, h->nv,
+                                                    B.ustride);
+    checkLaunch(h);
+  }
+}
+
+}  // namespace
+
+// =====================================================================================================
+extern "C" {
+
+const char* sdg_last_error(const sdg_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, sdg_handle** out) {
+  if (!mesh || !config || !out) { g_create_error = "null argument"; return SDG_ERR_INVALID_ARGUMENT; }
+  *out = nullptr;
+  std::unique_ptr<sdg_handle> H(new sdg_handle());
+  sdg_handle* h = H.get();
+  try {
+    const sdg_config& c = *config;
+    if (mesh->dimension != 2 && mesh->dimension != 3) throw Failure(SDG_ERR_INVALID_ARGUMENT, "dimension must be 2 or 3");
+    if (c.polynomial_order < 1 || c.polynomial_order > 5) throw Failure(SDG_ERR_INVALID_ARGUMENT, "polynomial order must be 1..5");
+    if (c.equation != SDG_COMPRESSIBLE_EULER && c.equation != SDG_COMPRESSIBLE_NS) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad equation");
+    if (c.convective_flux < 0 || c.convective_flux > 3) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad convective flux");
+    if (c.time_integration < 0 || c.time_integration > 2) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad time integration");
+    if (!(c.specific_heat_ratio > 1.0) || !(c.specific_heat_constant_volume > 0) || !(c.specific_heat_constant_pressure > 0))
+      throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad thermodynamic constants");
+    if (c.equation == SDG_COMPRESSIBLE_NS) throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes is not built in this library version");
+    if (!mesh->node_coordinate || mesh->node_count <= 0) throw Failure(SDG_ERR_INVALID_ARGUMENT, "no nodes");
+    h->cfg = c; h->device = device;
+    h->dim = mesh->dimension; h->nv = h->dim + 2; h->p = c.polynomial_order;
+    h->ph.gamma = c.specific_heat_ratio; h->ph.gm1 = c.specific_heat_ratio - 1.0;
+    h->ph.cv = c.specific_heat_constant_volume; h->ph.inv_cv = 1.0 / c.specific_heat_constant_volume;
+    h->ph.cp = c.specific_heat_constant_pressure; h->ph.mu = c.dynamic_viscosity;
+    h->ph.kappa = c.prandtl_number > 0 ? c.specific_heat_constant_pressure * c.dynamic_viscosity / c.prandtl_number : 0.0;
+    h->ph.transport = c.transport_model;
+    // element blocks, in the reference's loop order
+    std::vector<Block> mb;
+    if (h->dim == 2) {
+      if (mesh->triangle_count > 0) mb.push_back({SDG_ELEMENT_TRIANGLE, mesh->triangle_count, mesh->triangle_node});
+      if (mesh->quadrangle_count > 0) mb.push_back({SDG_ELEMENT_QUADRANGLE, mesh->quadrangle_count, mesh->quadrangle_node});
+    } else {
+      if (mesh->hexahedron_count > 0) mb.push_back({SDG_ELEMENT_HEXAHEDRON, mesh->hexahedron_count, mesh->hexahedron_node});
+    }
+    if (mb.empty()) throw Failure(SDG_ERR_INVALID_ARGUMENT, "mesh has no elements of its dimension");
+    for (const Block& b : mb) if (!b.vertex) throw Failure(SDG_ERR_INVALID_ARGUMENT, "null element array");
+    Adjacency adj;
+    try { adj = buildAdjacency(*mesh, mb); } catch (const std::runtime_error& e) { throw Failure(SDG_ERR_MESH, e.what()); }
+
+    const double* nodes = mesh->node_coordinate;
+    double extent = 0.0;
+    for (int64_t i = 0; i < mesh->node_count * 3; ++i) extent = std::max(extent, std::fabs(nodes[i]));
+    const double tol = 1e-12 * std::max(1.0, extent);
+    size_t stateOff = 0, pointOff = 0;
+    int64_t faceSlots = 0, relParts = 0;
+    for (const Block& b : mb) {
+      DevBlock B;
+      B.type = b.type; B.dim = typeDim(b.type); B.p = h->p; B.ne = b.count; B.nface = typeFaces(b.type);
+      B.kind = (b.type == SDG_ELEMENT_TRIANGLE || (b.type == SDG_ELEMENT_QUADRANGLE && h->p == 1)) ? kDense : kTensor;
+      B.n = h->p + 1;
+      B.nb = modalCount(b.type, h->p);
+      const PointRule vr = volumeRule(b.type, h->p);
+      B.nq = vr.n; B.qweight = vr.w;
+      B.nfq = h->dim == 2 ? B.n : B.n * B.n;
+      B.affine = 1;
+      for (int64_t e = 0; e < b.count && B.affine; ++e)
+        if (!isAffine(b.type, nodes, b.vertex + e * typeVertices(b.type), tol)) B.affine = 0;
+      if (!B.affine && b.type == SDG_ELEMENT_HEXAHEDRON)
+        throw Failure(SDG_ERR_UNSUPPORTED, "hexahedra must be parallelepipeds (affine) in this version");
+      // geometry: affine [e][d*d+1]; bilinear tensor quads per point [e][q][d*d+1]; bilinear dense quads
+      // [e][q][d*d+1] followed by the element's modal M^-1 [nb][nb] (Geometry.cpp:88-100)
+      const int gs = B.dim * B.dim + 1;
+      const bool denseBilinear = B.kind == kDense && !B.affine;
+      B.geomStride = B.affine ? gs : (denseBilinear ? B.nq * gs + B.nb * B.nb : B.nq * gs);
+      B.geomHost.assign(size_t(B.ne) * B.geomStride, 0.0);
+      B.qcoord.assign(size_t(B.ne) * B.nq * 3, 0.0);
+      B.minEdge.assign(size_t(B.ne), 0.0);
+      std::vector<double> mphi;
+      if (denseBilinear) {
+        mphi.assign(size_t(B.nq) * B.nb, 0.0);
+        std::vector<double> gg(size_t(B.nb) * 3);
+        for (int q = 0; q < B.nq; ++q) modalBasis(b.type, h->p, &vr.x[q * 3], &mphi[size_t(q) * B.nb], gg.data());
+      }
+      bool bad = false;
+#pragma omp parallel for schedule(static)
+      for (int64_t e = 0; e < B.ne; ++e) {
+        const int32_t* vv = b.vertex + e * typeVertices(b.type);
+        std::vector<double> jw(B.nq);
+        for (int q = 0; q < B.nq; ++q) {
+          double J[3][3], x[3], A[3][3];
+          jacobianAt(b.type, B.dim, nodes, vv, &vr.x[q * 3], J, x);
+          for (int l = 0; l < 3; ++l) B.qcoord[(size_t(e) * B.nq + q) * 3 + l] = x[l];
+          const double det = adjugate(B.dim, J, A);
+          if (!(det > 0)) bad = true;
+          jw[q] = det * vr.w[q];
+          if (!B.affine || q == 0) {
+            double* g = &B.geomHost[size_t(e) * B.geomStride + (B.affine ? 0 : size_t(q) * gs)];
+            for (int r = 0; r < B.dim; ++r)
+              for (int cc = 0; cc < B.dim; ++cc) g[r * B.dim + cc] = A[r][cc];
+            g[B.dim * B.dim] = 1.0 / det;
+          }
+        }
+        if (denseBilinear) {
+          std::vector<double> m(size_t(B.nb) * B.nb, 0.0), inv;
+          for (int i = 0; i < B.nb; ++i)
+            for (int k = 0; k < B.nb; ++k) {
+              double acc = 0; for (int q = 0; q < B.nq; ++q) acc += jw[q] * mphi[size_t(q) * B.nb + i] * mphi[size_t(q) * B.nb + k];
+              m[size_t(i) * B.nb + k] = acc;
+            }
+          invertDense(B.nb, m, inv);
+          std::copy(inv.begin(), inv.end(), &B.geomHost[size_t(e) * B.geomStride + size_t(B.nq) * gs]);
+        }
+        B.minEdge[e] = minEdgeOf(b.type, nodes, vv);
+      }
+      if (bad) throw Failure(SDG_ERR_MESH, "inverted or degenerate element");
+      if (B.kind == kTensor) {
+        B.ops.build(B.n);
+        buildTensorTables(B);
+        configureTensor(B, false);
+      } else {
+        buildDenseTables(B.type, B.p, B.tablesHost, B.phi, B.lsq);
+        if (!configureDense(B.type, B.p, B.affine != 0, false, B.threads, B.epb, B.smem))
+          throw Failure(SDG_ERR_UNSUPPORTED, "unsupported dense block");
+        B.ustride = (h->nv * B.nb + 1) & ~1;
+        B.fstride = B.nface * h->nv * B.nfq;
+      }
+      B.grid = int((B.ne + B.epb - 1) / B.epb);
+      B.stateOffset = stateOff; stateOff += size_t(B.ne) * B.ustride;
+      B.pointOffset = pointOff; pointOff += size_t(B.ne) * B.nq;
+      B.faceBase = faceSlots; faceSlots += B.ne * B.nface;
+      B.relOffset = relParts; relParts += B.grid;
+      h->elements += B.ne;
+      h->dof += B.ne * B.nb * h->nv;
+      h->blocks.push_back(std::move(B));
+    }
+    h->nfq = h->blocks[0].nfq; h->n1d = h->p + 1;
+    h->volumePoints = int64_t(pointOff);
+    h->stateCount = stateOff;
+    h->faceCount = size_t(faceSlots) * h->nv * h->nfq;
+    h->relParts = relParts;
+
+    // faces: slots, orientation, straight-face geometry from the left parent's vertices (Geometry.cpp:102-169)
+    const auto slotOf = [&](const FaceSide& s) { return h->blocks[s.block].faceBase + int64_t(s.element) * h->blocks[s.block].nface + s.face; };
+    const auto faceGeom = [&](const FaceSide& s, double* g, std::vector<double>* coords) {
+      const DevBlock& B = h->blocks[s.block];
+      const int nfv = typeFaceVertices(B.type);
+      const int32_t* vv = mb[s.block].vertex + int64_t(s.element) * typeVertices(B.type);
+      const int* fl = faceVertexList(B.type);
+      double q[4][3];
+      for (int k = 0; k < nfv; ++k)
+        for (int d = 0; d < 3; ++d) q[k][d] = nodes[size_t(vv[fl[s.face * nfv + k]]) * 3 + d];
+      double n[3] = {0, 0, 0}, area = 0;
+      if (h->dim == 2) {
+        const double tx = 0.5 * (q[1][0] - q[0][0]), ty = 0.5 * (q[1][1] - q[0][1]);
+        area = std::sqrt(tx * tx + ty * ty);
+        n[0] = ty / area; n[1] = -tx / area;
+      } else {
+        double planar = 0;
+        for (int d = 0; d < 3; ++d) planar = std::max(planar, std::fabs(q[0][d] + q[2][d] - q[1][d] - q[3][d]));
+        if (planar > tol) throw Failure(SDG_ERR_UNSUPPORTED, "non-parallelogram hexahedron face");
+        double a[3], b[3];
+        for (int d = 0; d < 3; ++d) { a[d] = 0.5 * (q[1][d] - q[0][d]); b[d] = 0.5 * (q[3][d] - q[0][d]); }
+        const double cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
+        area = std::sqrt(cx * cx + cy * cy + cz * cz);
+        n[0] = cx / area; n[1] = cy / area; n[2] = cz / area;
+      }
+      g[0] = n[0]; g[1] = n[1]; g[2] = n[2]; g[3] = area;
+      if (coords) {
+        const PointRule fr = faceRule(B.type, B.p);
+        for (int j = 0; j < fr.n; ++j) {
+          double sh[4];
+          const double x = fr.x[j * 3], y = fr.x[j * 3 + 1];
+          if (nfv == 2) { sh[0] = 0.5 * (1 - x); sh[1] = 0.5 * (1 + x); }
+          else { sh[0] = 0.25 * (1 - x) * (1 - y); sh[1] = 0.25 * (1 + x) * (1 - y); sh[2] = 0.25 * (1 + x) * (1 + y); sh[3] = 0.25 * (1 - x) * (1 + y); }
+          for (int d = 0; d < 3; ++d) {
+            double s = 0; for (int k = 0; k < nfv; ++k) s += sh[k] * q[k][d];
+            coords->push_back(s);
+          }
+        }
+      }
+    };
+    h->nInterior = int64_t(adj.interior.size());
+    h->nBoundary = int64_t(adj.boundary.size());
+    std::vector<int> fconn(size_t(h->nInterior) * 3);
+    std::vector<double> fgeo(size_t(h->nInterior) * 4);
+    for (int64_t i = 0; i < h->nInterior; ++i) {
+      const InteriorFace& f = adj.interior[i];
+      fconn[i * 3] = int(slotOf(f.left)); fconn[i * 3 + 1] = int(slotOf(f.right)); fconn[i * 3 + 2] = f.rotation;
+      faceGeom(f.left, &fgeo[i * 4], nullptr);
+    }
+    std::vector<int> bconn(size_t(h->nBoundary) * 3);
+    std::vector<double> bgeo(size_t(h->nBoundary) * 4);
+    for (int64_t i = 0; i < h->nBoundary; ++i) {
+      const BoundaryFace& f = adj.boundary[i];
+      bconn[i * 3] = int(slotOf(f.left)); bconn[i * 3 + 1] = f.condition; bconn[i * 3 + 2] = 0;
+      faceGeom(f.left, &bgeo[i * 4], &h->bcoord);
+      h->bphys.push_back(f.physical);
+    }
+    // canonical adjacency tuples
+    {
+      std::vector<std::array<int32_t, 7>> t;
+      for (const InteriorFace& f : adj.interior)
+        t.push_back({h->blocks[f.left.block].type, f.left.element, f.left.face, h->blocks[f.right.block].type,
+                     f.right.element, f.right.face, f.rotation});
+      std::sort(t.begin(), t.end());
+      for (auto& r : t) h->adjInterior.insert(h->adjInterior.end(), r.begin(), r.end());
+      std::vector<std::array<int32_t, 5>> bt;
+      for (const BoundaryFace& f : adj.boundary)
+        bt.push_back({h->blocks[f.left.block].type, f.left.element, f.left.face, f.physical, f.condition});
+      std::sort(bt.begin(), bt.end());
+      for (auto& r : bt) h->adjBoundary.insert(h->adjBoundary.end(), r.begin(), r.end());
+    }
+
+    if (device < 0) {  // host-only handle: adjacency, geometry and coordinates, no GPU
+      *out = H.release();
+      return SDG_OK;
+    }
+    SDG_CUDA(cudaSetDevice(device));
+    h->hostOnly = false;
+    SDG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    for (DevBlock& B : h->blocks) {
+      if (B.kind == kTensor) configureTensor(B, true);
+      else if (!configureDense(B.type, B.p, B.affine != 0, true, B.threads, B.epb, B.smem))
+        throw Failure(SDG_ERR_CUDA, "cannot configure the dense kernel");
+    }
+    // device buffers
+    h->state[0] = devAlloc<double>(h->stateCount);
+    h->state[1] = devAlloc<double>(h->stateCount);
+    SDG_CUDA(cudaMemsetAsync(h->state[0], 0, h->stateCount * 8, h->stream));
+    SDG_CUDA(cudaMemsetAsync(h->state[1], 0, h->stateCount * 8, h->stream));
+    h->face = devAlloc<double>(h->faceCount);
+    SDG_CUDA(cudaMemsetAsync(h->face, 0, h->faceCount * 8, h->stream));
+    h->fconn = devAlloc<int>(fconn.size()); upload(h->fconn, fconn, h->stream);
+    h->fgeo = devAlloc<double>(fgeo.size()); upload(h->fgeo, fgeo, h->stream);
+    h->bconn = devAlloc<int>(bconn.size()); upload(h->bconn, bconn, h->stream);
+    h->bgeo = devAlloc<double>(bgeo.size()); upload(h->bgeo, bgeo, h->stream);
+    const size_t ghostCount = size_t(h->nBoundary) * h->nfq * (h->dim + 3);
+    h->ghost = devAlloc<double>(ghostCount);
+    SDG_CUDA(cudaMemsetAsync(h->ghost, 0, std::max<size_t>(ghostCount, 1) * 8, h->stream));
+    h->scratch = devAlloc<double>(size_t(h->volumePoints) * h->nv);
+    h->relPart = devAlloc<double>(size_t(h->relParts) * h->nv);
+    h->relOut = devAlloc<double>(8);
+    h->dtParts = (h->volumePoints + 255) / 256;
+    h->dtPart = devAlloc<double>(size_t(h->dtParts) + 1);
+    h->status = devAlloc<unsigned>(1);
+    SDG_CUDA(cudaMemsetAsync(h->status, 0, sizeof(unsigned), h->stream));
+    for (DevBlock& B : h->blocks) {
+      B.geom = devAlloc<double>(B.geomHost.size()); upload(B.geom, B.geomHost, h->stream);
+      B.tables = devAlloc<double>(B.tablesHost.size()); upload(B.tables, B.tablesHost, h->stream);
+      B.minedge = devAlloc<double>(B.minEdge.size()); upload(B.minedge, B.minEdge, h->stream);
+      if (B.kind == kDense) {
+        B.phiDev = devAlloc<double>(B.phi.size()); upload(B.phiDev, B.phi, h->stream);
+        B.lsqDev = devAlloc<double>(B.lsq.size()); upload(B.lsqDev, B.lsq, h->stream);
+      }
+    }
+    SDG_CUDA(cudaStreamSynchronize(h->stream));
+  } catch (const Failure& f) {
+    g_create_error = f.what();
+    sdg_destroy(H.release());
+    return f.code;
+  } catch (const std::exception& ex) {
+    g_create_error = ex.what();
+    sdg_destroy(H.release());
+    return SDG_ERR_INVALID_ARGUMENT;
+  }
+  *out = H.release();
+  return SDG_OK;
+}
+
+int sdg_destroy(sdg_handle* h) {
+  if (!h) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { delete h; return SDG_OK; }
+  cudaSetDevice(h->device);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  for (DevBlock& B : h->blocks) {
+    cudaFree(B.geom); cudaFree(B.tables); cudaFree(B.minedge); cudaFree(B.phiDev); cudaFree(B.lsqDev);
+  }
+  cudaFree(h->state[0]); cudaFree(h->state[1]); cudaFree(h->face); cudaFree(h->fconn); cudaFree(h->fgeo);
+  cudaFree(h->bconn); cudaFree(h->bgeo); cudaFree(h->ghost); cudaFree(h->scratch); cudaFree(h->relPart);
+  cudaFree(h->relOut); cudaFree(h->dtPart); cudaFree(h->status);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return SDG_OK;
+}
+
+int sdg_get_counts(const sdg_handle* h, sdg_counts* c) {
+  if (!h || !c) return SDG_ERR_INVALID_ARGUMENT;
+  std::memset(c, 0, sizeof(*c));
+  c->dimension = h->dim; c->conserved_variable_count = h->nv; c->block_count = int32_t(h->blocks.size());
+  for (size_t i = 0; i < h->blocks.size() && i < 2; ++i) {
+    c->block_element_type[i] = h->blocks[i].type; c->block_element_count[i] = h->blocks[i].ne;
+    c->block_basis_count[i] = h->blocks[i].nb; c->block_volume_point_count[i] = h->blocks[i].nq;
+  }
+  c->element_count = h->elements; c->volume_point_count = h->volumePoints; c->degree_of_freedom_count = h->dof;
+  c->interior_face_count = h->nInterior; c->boundary_face_count = h->nBoundary; c->face_point_count = h->nfq;
+  c->boundary_point_count = h->nBoundary * h->nfq;
+  return SDG_OK;
+}
+
+int sdg_volume_point_coordinate(sdg_handle* h, double* out) {
+  if (!h || !out) return SDG_ERR_INVALID_ARGUMENT;
+  size_t off = 0;
+  for (const DevBlock& B : h->blocks) { std::copy(B.qcoord.begin(), B.qcoord.end(), out + off); off += B.qcoord.size(); }
+  return SDG_OK;
+}
+
+int sdg_boundary_point_coordinate(sdg_handle* h, double* out, int32_t* physical) {
+  if (!h || !out) return SDG_ERR_INVALID_ARGUMENT;
+  std::copy(h->bcoord.begin(), h->bcoord.end(), out);
+  if (physical) std::copy(h->bphys.begin(), h->bphys.end(), physical);
+  return SDG_OK;
+}
+
+int sdg_set_state_point(sdg_handle* h, const double* conserved) {
+  if (!h || !conserved) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  SDG_CUDA(cudaMemcpyAsync(h->scratch, conserved, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyHostToDevice, h->stream));
+  pointsToState(h, 0);
+  traceAll(h, 0);
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  h->hasState = true;
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_set_initial_primitive(sdg_handle* h, const double* primitive) {
+  if (!h || !primitive) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  SDG_CUDA(cudaMemcpyAsync(h->scratch, primitive, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyHostToDevice, h->stream));
+  const int grid = int((h->volumePoints + 255) / 256);
+  primitiveToConservedKernel<<<grid, 256, 0, h->stream>>>(h->scratch, h->volumePoints, h->dim, h->ph);
+  checkLaunch(h);
+  pointsToState(h, 0);
+  traceAll(h, 0);
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  h->hasState = true;
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_set_boundary_primitive(sdg_handle* h, const double* primitive) {
+  if (!h || (!primitive && h->nBoundary > 0)) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  const int nv = h->nv, d = h->dim;
+  const int64_t np = h->nBoundary * h->nfq;
+  std::vector<double> g(size_t(np) * (d + 3));
+  for (int64_t i = 0; i < np; ++i) {
+    const double* pr = primitive + i * nv;
+    double* o = &g[i * (d + 3)];
+    const double e = h->ph.cv * pr[d + 1];
+    o[0] = pr[0];
+    for (int k = 0; k < d; ++k) o[1 + k] = pr[1 + k];
+    o[d + 1] = e;
+    o[d + 2] = h->ph.gm1 * pr[0] * e;  // calculateComputationalFromPrimitive (VariableConvertor.cpp:368-380)
+  }
+  SDG_CUDA(cudaSetDevice(h->device));
+  if (np > 0) SDG_CUDA(cudaMemcpyAsync(h->ghost, g.data(), g.size() * 8, cudaMemcpyHostToDevice, h->stream));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_get_state_point(sdg_handle* h, double* conserved) {
+  if (!h || !conserved) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  stateToPoints(h, 0);
+  SDG_CUDA(cudaMemcpyAsync(conserved, h->scratch, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+// Modal coefficients <-> state.  Tensor blocks: c = (Phi1^-1 x ...) U_nodal; dense blocks are modal.
+static void modalConvert(sdg_handle* h, std::vector<double>& st, double* modal, bool toModal) {
+  size_t moff = 0;
+  for (const DevBlock& B : h->blocks) {
+    const int nv = h->nv, nb = B.nb, n = B.n;
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      double* u = &st[B.stateOffset + size_t(e) * B.ustride];
+      double* m = modal + moff + size_t(e) * nv * nb;  // column-major (nv x nb): index b*nv + v
+      if (B.kind == kDense) {
+        for (int b = 0; b < nb; ++b)
+          for (int v = 0; v < nv; ++v) {
+            if (toModal) m[b * nv + v] = u[v * nb + b]; else u[v * nb + b] = m[b * nv + v];
+          }
+        continue;
+      }
+      std::vector<double> a(nb), t(nb);
+      for (int v = 0; v < nv; ++v) {
+        for (int b = 0; b < nb; ++b) a[b] = toModal ? u[v * nb + b] : m[b * nv + v];
+        const double(*M)[kMaxN] = toModal ? B.ops.phi1inv : B.ops.phi1;
+        // apply M along each axis: out[.., i, ..] = sum_k M[i][k] in[.., k, ..]
+        const int strides[3] = {B.dim == 2 ? n : n * n, B.dim == 2 ? 1 : n, 1};
+        for (int ax = 0; ax < B.dim; ++ax) {
+          const int st2 = strides[ax];
+          for (int b = 0; b < nb; ++b) {
+            const int ib = (b / st2) % n;
+            const int base = b - ib * st2;
+            double s = 0; for (int k = 0; k < n; ++k) s += M[ib][k] * a[base + k * st2];
+            t[b] = s;
+          }
+          std::swap(a, t);
+        }
+        for (int b = 0; b < nb; ++b) { if (toModal) m[b * nv + v] = a[b]; else u[v * nb + b] = a[b]; }
+      }
+    }
+    moff += size_t(B.ne) * nv * nb;
+  }
+}
+
+int sdg_get_state_modal(sdg_handle* h, double* coefficient) {
+  if (!h || !coefficient) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  std::vector<double> st(h->stateCount);
+  SDG_CUDA(cudaSetDevice(h->device));
+  SDG_CUDA(cudaMemcpyAsync(st.data(), h->state[0], h->stateCount * 8, cudaMemcpyDeviceToHost, h->stream));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  modalConvert(h, st, coefficient, true);
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_set_state_modal(sdg_handle* h, const double* coefficient) {
+  if (!h || !coefficient) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  std::vector<double> st(h->stateCount, 0.0);
+  modalConvert(h, st, const_cast<double*>(coefficient), false);
+  SDG_CUDA(cudaSetDevice(h->device));
+  SDG_CUDA(cudaMemcpyAsync(h->state[0], st.data(), h->stateCount * 8, cudaMemcpyHostToDevice, h->stream));
+  traceAll(h, 0);
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  h->hasState = true;
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_calculate_delta_time(sdg_handle* h, double cfl, double* dt) {
+  if (!h || !dt || !(cfl > 0)) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  if (!h->hasState) { h->err = "no state"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  stateToPoints(h, 0);
+  std::vector<double> parts;
+  double best = 1.79769313486231570e308;
+  for (const DevBlock& B : h->blocks) {
+    const int64_t np = B.ne * B.nq;
+    const int grid = int((np + 255) / 256);
+    deltaTimeKernel<<<grid, 256, 0, h->stream>>>(h->scratch + B.pointOffset * h->nv, B.minedge, np, B.nq, h->dim, cfl,
+                                                 double(h->p + 1) * double(h->p + 1), h->ph, h->dtPart);
+    checkLaunch(h);
+    parts.resize(grid);
+    SDG_CUDA(cudaMemcpyAsync(parts.data(), h->dtPart, grid * 8, cudaMemcpyDeviceToHost, h->stream));
+    SDG_CUDA(cudaStreamSynchronize(h->stream));
+    for (double x : parts) best = std::min(best, x);
+  }
+  *dt = best;
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_step_async(sdg_handle* h, int32_t steps, double dt) {
+  if (!h || steps < 0 || !std::isfinite(dt)) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  if (!h->hasState) { h->err = "step before an initial state"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  for (int s = 0; s < steps; ++s) stepOnce(h, dt, true);  // relative error every step, as stepSolver does
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_step(sdg_handle* h, int32_t steps, double dt) {
+  const int rc = sdg_step_async(h, steps, dt);
+  if (rc != SDG_OK) return rc;
+  SDG_API_BEGIN
+  if (steps > 0)
+    SDG_CUDA(cudaMemcpyAsync(h->relerr, h->relOut, h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  checkStatus(h);
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_relative_error(sdg_handle* h, double* out) {
+  if (!h || !out) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  SDG_CUDA(cudaMemcpyAsync(h->relerr, h->relOut, h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  for (int v = 0; v < h->nv; ++v) out[v] = h->relerr[v];
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_residual_point(sdg_handle* h, double* rate) {
+  if (!h || !rate) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  if (!h->hasState) { h->err = "no state"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  // the face buffer holds the traces of state[0]: compute fluxes, then the rate without an update,
+  // then restore the traces (the flux pass overwrote them)
+  launchFaces(h);
+  for (DevBlock& B : h->blocks) {
+    StageArgs a = baseArgs(h, B);
+    a.uin = h->state[0] + B.stateOffset;
+    a.rate = h->scratch + B.pointOffset * h->nv;
+    a.doVolume = 1; a.doUpdate = 0; a.doTrace = 0;
+    launchBlock(h, B, a);
+  }
+  SDG_CUDA(cudaMemcpyAsync(rate, h->scratch, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  traceAll(h, 0);
+  checkStatus(h);
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_synchronize(sdg_handle* h) {
+  if (!h) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  checkStatus(h);
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_launch_count(const sdg_handle* h, int64_t* n) {
+  if (!h || !n) return SDG_ERR_INVALID_ARGUMENT;
+  *n = h->launches;
+  return SDG_OK;
+}
+
+int sdg_adjacency(const sdg_handle* h, int32_t* interior, int32_t* boundary) {
+  if (!h) return SDG_ERR_INVALID_ARGUMENT;
+  if (interior) std::copy(h->adjInterior.begin(), h->adjInterior.end(), interior);
+  if (boundary) std::copy(h->adjBoundary.begin(), h->adjBoundary.end(), boundary);
+  return SDG_OK;
+}
+
+}  // extern "C"

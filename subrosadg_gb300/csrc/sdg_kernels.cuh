@@ -1,0 +1,429 @@
+// sm_103a kernels of the GB300 DG path (Euler residual, face fluxes, SSP-RK update, reductions).
+//
+// Data layout in HBM (one element block per element type):
+//   state  U[e][v][i]            conserved v, node/basis i, element-contiguous, element stride padded to a
+//                                multiple of 16 bytes so element tiles are TMA bulk-copy sources
+//   face   F[slot][v][j]         one slot per (element, local face), slot = block_base + e*nface + f;
+//                                holds the element's face trace between stages and its outward flux
+//                                |J_f| h(U-,U+;n) after the face kernel (one writer per slot, no atomics,
+//                                the scatter rule of src/Solver/SpatialDiscrete.cpp:738-744)
+//   geom   affine: [e][d*d + 1]  |J| dxi_b/dx_a (row b) and 1/|J|; bilinear quads: [e][i][d*d + 1]
+//
+// Kernels per RK stage: faceKernel (Riemann flux on interior faces) + boundaryFaceKernel, then one
+// element kernel per block that evaluates the volume term, the lift of the face fluxes, the diagonal
+// mass matrix inverse and the SSP-RK combination, writes the new state and the new face traces.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "sdg_device.cuh"
+
+namespace sdg {
+
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+// Status word bits (host reads them after a synchronisation).
+constexpr unsigned kStatusTimeout = 1u;
+
+// ---- TMA bulk-copy helpers (cp.async.bulk + mbarrier, bounded waits) ------------------------------
+__device__ __forceinline__ uint32_t smemAddr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbarInit(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbarExpectTx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulkLoad(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smemAddr(dst)),
+      "l"(src), "r"(bytes), "r"(smemAddr(bar))
+      : "memory");
+}
+// Bounded wait on phase `parity`; returns false (and the caller flags a timeout) if it never completes.
+__device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity) {
+  for (uint32_t it = 0; it < kWaitLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(smemAddr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// ---- parameter blocks -----------------------------------------------------------------------------
+// Operator tables of a tensor block, copied into shared memory by every CTA (size a multiple of 8).
+struct TensorTables {
+  double dhat[6][6];
+  double endm[6], endp[6], liftm[6], liftp[6];
+  double w[6];
+  double b1[6][6];
+  int faceAxis[6], faceEnd[6];   // normal axis and end (0: -1, 1: +1) of each local face
+  int axisFace[3][2];            // local face of (axis, end)
+  int faceBase[6][36];           // first node of the line through face point j of face f
+  unsigned char nodeFacePoint[3][2][216];  // face point of (axis, end) on the line through node i
+};
+static_assert(sizeof(TensorTables) % 8 == 0, "TensorTables must be a whole number of doubles");
+
+struct StageArgs {
+  const double* uin;      // stage input state
+  const double* ubase;    // RK base state (U at the start of the step)
+  double* uout;           // new state
+  double* face;           // face buffer (this block's slots start at face + faceBase)
+  const double* geom;
+  const double* tables;   // TensorTables or dense tables (device)
+  double* rate;           // optional du/dt output at the volume points ([e][q][v]), or null
+  double* relerr;         // optional per-CTA partial sums [cta][v], or null
+  unsigned* status;
+  int64_t ne;
+  int64_t faceBase;       // first slot of this block
+  double c0, c1, c2dt;    // U = c1 U + c0 U0 + c2 dt M^-1 R
+  int doUpdate;           // 0: no state update (rate/trace only)
+  int doTrace;            // write new face traces
+  int doVolume;           // evaluate the residual (0: trace-only pass)
+};
+
+template <int DIM, int N>
+struct TensorShape {
+  static constexpr int NV = DIM + 2;
+  static constexpr int NB = DIM == 2 ? N * N : N * N * N;
+  static constexpr int NF = DIM == 2 ? 4 : 6;
+  static constexpr int NFQ = DIM == 2 ? N : N * N;
+  static constexpr int USTRIDE = (NV * NB + 1) & ~1;
+  static constexpr int FSTRIDE = NF * NV * NFQ;
+  static constexpr int EPB_RAW = 256 / NB > 0 ? 256 / NB : 1;
+  // elements per CTA, bounded so the CTA's shared memory stays under ~96 KB (two CTAs per SM at least)
+  static constexpr int SMEM_PER_ELEM = 8 * (USTRIDE + DIM * NV * NB + FSTRIDE);
+  static constexpr int EPB_SMEM = (96 * 1024) / SMEM_PER_ELEM > 0 ? (96 * 1024) / SMEM_PER_ELEM : 1;
+  static constexpr int EPB = EPB_RAW < EPB_SMEM ? EPB_RAW : EPB_SMEM;
+  static constexpr int THREADS = ((EPB * NB + 31) / 32) * 32;
+  static constexpr size_t SMEM = size_t(EPB) * SMEM_PER_ELEM + sizeof(TensorTables) + 16 + 8 * NV * (THREADS / 32);
+};
+
+// Index of node i along axis a.
+template <int DIM, int N>
+__device__ __forceinline__ int axisIndex(int i, int a) {
+  if constexpr (DIM == 2) return a == 0 ? i / N : i % N;
+  else return a == 0 ? i / (N * N) : (a == 1 ? (i / N) % N : i % N);
+}
+
+template <int DIM, int N>
+__device__ __forceinline__ int strideOf(int a) {
+  if constexpr (DIM == 2) return a == 0 ? N : 1;
+  else return a == 0 ? N * N : (a == 1 ? N : 1);
+}
+
+// Tensor-block stage kernel: one thread per node, EPB elements per CTA.
+template <int DIM, int N, bool AFFINE>
+__global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS)
+    tensorStageKernel(StageArgs a, Phys ph) {
+  using S = TensorShape<DIM, N>;
+  constexpr int NV = S::NV, NB = S::NB, NF = S::NF, NFQ = S::NFQ;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* sU = reinterpret_cast<double*>(smem_raw);                 // [EPB][USTRIDE]
+  double* sF = sU + S::EPB * S::USTRIDE;                            // [EPB][FSTRIDE]
+  double* sG = sF + S::EPB * S::FSTRIDE;                            // [EPB][DIM][NV][NB]
+  TensorTables* T = reinterpret_cast<TensorTables*>(sG + S::EPB * DIM * NV * NB);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(T + 1);
+  double* sRed = reinterpret_cast<double*>(bar + 1);                // [warps][NV]
+
+  const int tid = threadIdx.x;
+  const int64_t e0 = int64_t(blockIdx.x) * S::EPB;
+  const int ecount = int(a.ne - e0 < S::EPB ? a.ne - e0 : S::EPB);
+  const int le = tid / NB, node = tid - le * NB;
+  const bool active = le < ecount;
+  const int64_t e = e0 + le;
+
+  // 1. stage the element tile (state + face slots) into shared memory with TMA bulk copies
+  if (tid == 0) {
+    mbarInit(bar, 1);
+    const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * S::FSTRIDE * 8;
+    mbarExpectTx(bar, a.doVolume ? ub + fb : ub);
+    bulkLoad(sU, a.uin + e0 * S::USTRIDE, ub, bar);
+    if (a.doVolume) bulkLoad(sF, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+  }
+  {
+    const double* src = a.tables;
+    double* dst = reinterpret_cast<double*>(T);
+    for (int k = tid; k < int(sizeof(TensorTables) / 8); k += blockDim.x) dst[k] = src[k];
+  }
+  __syncthreads();
+  const bool arrived = mbarWait(bar, 0);
+  if (__syncthreads_or(!arrived)) {  // uniform decision: every thread leaves together
+    if (tid == 0) atomicOr(a.status, kStatusTimeout);
+    return;
+  }
+
+  double du[NV];
+  double unew[NV];
+  if (a.doVolume) {
+    // 2. contravariant fluxes at the node
+    double jinv;
+    double ja[DIM][DIM];
+    if (active) {
+      const double* g = AFFINE ? a.geom + e * (DIM * DIM + 1) : a.geom + (e * NB + node) * (DIM * DIM + 1);
+#pragma unroll
+      for (int b = 0; b < DIM; ++b)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) ja[b][c] = g[b * DIM + c];
+      jinv = g[DIM * DIM];
+      double U[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) U[v] = sU[le * S::USTRIDE + v * NB + node];
+      State<DIM> s;
+      makeState<DIM>(s, U, ph);
+      const double ep = s.E + s.p;
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) {
+        const double vb = dotn<DIM>(s.u, ja[b]);
+        double* G = sG + ((le * DIM + b) * NV) * NB + node;
+        G[0] = s.r * vb;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) G[(1 + k) * NB] = fma(s.m[k], vb, ja[b][k] * s.p);
+        G[(NV - 1) * NB] = ep * vb;
+      }
+    }
+    __syncthreads();
+    // 3. weak derivative along each axis + lift of the face fluxes (mass-scaled), per node
+    if (active) {
+      int ax[DIM];
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) ax[b] = axisIndex<DIM, N>(node, b);
+#pragma unroll
+      for (int v = 0; v < NV; ++v) du[v] = 0.0;
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) {
+        const int base = node - ax[b] * strideOf<DIM, N>(b);
+        double dcoef[N];
+#pragma unroll
+        for (int q = 0; q < N; ++q) dcoef[q] = T->dhat[q][ax[b]];
+        const double lm = T->liftm[ax[b]], lp = T->liftp[ax[b]];
+        const int fm = T->axisFace[b][0], fp = T->axisFace[b][1];
+        const int jm = T->nodeFacePoint[b][0][node], jp = T->nodeFacePoint[b][1][node];
+        const double* G = sG + ((le * DIM + b) * NV) * NB + base;
+        const double* Fm = sF + le * S::FSTRIDE + fm * NV * NFQ + jm;
+        const double* Fp = sF + le * S::FSTRIDE + fp * NV * NFQ + jp;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          double acc = du[v];
+#pragma unroll
+          for (int q = 0; q < N; ++q) acc = fma(dcoef[q], G[v * NB + q * strideOf<DIM, N>(b)], acc);
+          acc = fma(-lm, Fm[v * NFQ], acc);
+          acc = fma(-lp, Fp[v * NFQ], acc);
+          du[v] = acc;
+        }
+      }
+      // 4. RK combination (M^-1 is diagonal: 1/(w_i |J|_i); the weights cancelled into dhat/lift)
+      const double sc = a.c2dt * jinv;
+      const int64_t gi = e * S::USTRIDE + node;
+      if (a.rate) {
+        // reference point order equals the node order for tensor blocks
+#pragma unroll
+        for (int v = 0; v < NV; ++v) a.rate[(e * NB + node) * NV + v] = du[v] * jinv;
+      }
+      if (a.doUpdate) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const double u0 = a.ubase[gi + v * NB];
+          const double u1 = sU[le * S::USTRIDE + v * NB + node];
+          unew[v] = fma(sc, du[v], fma(a.c1, u1, a.c0 * u0));
+        }
+      }
+    }
+    __syncthreads();
+    // relative error (TimeIntegration.cpp:279-324): the nodal weak residual is R_i = M_ii du_i = w_i * bracket_i
+    // (jinv was not applied to du); rel = (B1 x B1 [x B1]) R with B1(a,b) = sum_k lob_k(x_a) lob_k(x_b), the
+    // tensor form of Phi Phi^T for the modal basis; per element the mean over points of |rel| is summed.
+    if (a.relerr) {
+      if (active) {
+        double wi = 1.0;
+#pragma unroll
+        for (int b = 0; b < DIM; ++b) wi *= T->w[axisIndex<DIM, N>(node, b)];
+        double* R0 = sG + le * DIM * NV * NB;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) R0[v * NB + node] = wi * du[v];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) {
+        const double* in = sG + le * DIM * NV * NB + (b & 1) * NV * NB;
+        double* out = sG + le * DIM * NV * NB + ((b + 1) & 1) * NV * NB;
+        double r[NV];
+        if (active) {
+          const int ib = axisIndex<DIM, N>(node, b);
+          const int st = strideOf<DIM, N>(b);
+          const int base = node - ib * st;
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            double acc = 0.0;
+#pragma unroll
+            for (int q = 0; q < N; ++q) acc = fma(T->b1[ib][q], in[v * NB + base + q * st], acc);
+            r[v] = acc;
+          }
+        }
+        __syncthreads();
+        if (active) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) out[v * NB + node] = r[v];
+        }
+        __syncthreads();
+      }
+      // deterministic reduction: warp shuffle, then warps summed in order by thread v
+      const double* fin = sG + le * DIM * NV * NB + (DIM & 1) * NV * NB;
+      const int warp = tid >> 5, nwarp = (blockDim.x + 31) >> 5;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double x = active ? fabs(fin[v * NB + node]) : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((tid & 31) == 0) sRed[warp * NV + v] = x;
+      }
+      __syncthreads();
+      if (tid < NV) {
+        double acc = 0.0;
+        for (int w = 0; w < nwarp; ++w) acc += sRed[w * NV + tid];
+        a.relerr[int64_t(blockIdx.x) * NV + tid] = acc / double(NB);
+      }
+    }
+    if (a.doUpdate && active) {
+      const int64_t gi = e * S::USTRIDE + node;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        a.uout[gi + v * NB] = unew[v];
+        sU[le * S::USTRIDE + v * NB + node] = unew[v];
+      }
+    }
+    __syncthreads();
+  }
+  // 5. face traces of the (new) state: 1D end-point interpolation along each face's normal axis
+  if (a.doTrace) {
+    for (int idx = tid; idx < ecount * NF * NFQ; idx += blockDim.x) {
+      const int te = idx / (NF * NFQ), r = idx - te * (NF * NFQ);
+      const int f = r / NFQ, j = r - f * NFQ;
+      const int axis = T->faceAxis[f];
+      const double* coef = T->faceEnd[f] ? T->endp : T->endm;
+      const int base = T->faceBase[f][j];
+      const int st = strideOf<DIM, N>(axis);
+      const double* u = sU + te * S::USTRIDE + base;
+      double* out = a.face + (a.faceBase + (e0 + te) * NF + f) * NV * NFQ + j;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double acc = 0.0;
+#pragma unroll
+        for (int q = 0; q < N; ++q) acc = fma(coef[q], u[v * NB + q * st], acc);
+        out[v * NFQ] = acc;
+      }
+    }
+  }
+}
+
+// Interior-face Riemann flux: one thread per face point.  Left slot gets +|J_f| h, right slot gets
+// -|J_f| h at the permuted point (SpatialDiscrete.cpp:633-748).
+template <int DIM, int FLUX>
+__global__ void __launch_bounds__(256) faceKernel(double* __restrict__ face, const int* __restrict__ conn,
+                                                  const double* __restrict__ fgeo, int64_t nface, int n1d, Phys ph) {
+  constexpr int NV = DIM + 2;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = conn[f * 3 + 0], sr = conn[f * 3 + 1], rot = conn[f * 3 + 2];
+  int jr;
+  if constexpr (DIM == 2) {
+    jr = n1d - 1 - j;
+  } else {
+    const int i = j / n1d, k = j - i * n1d;
+    int ii, kk;
+    switch (rot) {
+      case 0: ii = k; kk = i; break;
+      case 1: ii = n1d - 1 - i; kk = k; break;
+      case 2: ii = n1d - 1 - k; kk = n1d - 1 - i; break;
+      default: ii = i; kk = n1d - 1 - k; break;
+    }
+    jr = ii * n1d + kk;
+  }
+  double* L = face + int64_t(sl) * NV * nfq + j;
+  double* R = face + int64_t(sr) * NV * nfq + jr;
+  double ul[NV], ur[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) { ul[v] = L[v * nfq]; ur[v] = R[v * nfq]; }
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
+  const double area = fgeo[f * 4 + 3];
+  State<DIM> l, r;
+  makeState<DIM>(l, ul, ph);
+  makeState<DIM>(r, ur, ph);
+  double h[NV];
+  convectiveFlux<DIM, FLUX>(l, r, n, ph, h);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const double x = h[v] * area;
+    L[v * nfq] = x;
+    R[v * nfq] = -x;
+  }
+}
+
+// Boundary-face flux: ghost state from the boundary condition, normal flux of the boundary state
+// (SpatialDiscrete.cpp:750-842).  ghost = [face][j][comp] computational (rho, u, e, p).
+template <int DIM>
+__global__ void __launch_bounds__(256) boundaryFaceKernel(double* __restrict__ face, const int* __restrict__ conn,
+                                                          const double* __restrict__ fgeo,
+                                                          const double* __restrict__ ghost, int64_t nface, int n1d,
+                                                          Phys ph) {
+  constexpr int NV = DIM + 2;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = conn[f * 3 + 0], bc = conn[f * 3 + 1];
+  double* L = face + int64_t(sl) * NV * nfq + j;
+  double ul[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) ul[v] = L[v * nfq];
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
+  const double area = fgeo[f * 4 + 3];
+  State<DIM> s;
+  makeState<DIM>(s, ul, ph);
+  Comp<DIM> l, g, b;
+  compFromState<DIM>(s, l);
+  const double* gp = ghost + (f * nfq + j) * (DIM + 3);
+  g.r = gp[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) g.u[k] = gp[1 + k];
+  g.e = gp[DIM + 1];
+  g.p = gp[DIM + 2];
+  boundaryState<DIM>(bc, n, l, g, ph, b);
+  double h[NV];
+  normalFluxComp<DIM>(b, n, h);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) L[v * nfq] = h[v] * area;
+}
+
+// Deterministic final reduction of per-CTA relative-error partials: out[v] = sum / elements.
+__global__ void relerrReduceKernel(const double* __restrict__ part, int64_t nparts, int nv, double inv_elements,
+                                   double* __restrict__ out) {
+  __shared__ double sh[256];
+  const int v = blockIdx.x;
+  double acc = 0.0;
+  for (int64_t i = threadIdx.x; i < nparts; i += blockDim.x) acc += part[i * nv + v];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[v] = sh[0] * inv_elements;
+}
+
+}  // namespace sdg

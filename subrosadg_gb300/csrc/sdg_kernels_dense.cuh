@@ -1,0 +1,387 @@
+// Dense (modal) element blocks and point-layout conversion kernels of the GB300 DG path.
+//
+// Triangles, and quadrangles of order 1 (whose volume rule is the non-tensor 7-point formula of
+// src/Solver/SimulationControl.cpp:270), keep the reference's modal formulation
+// (src/Solver/SpatialDiscrete.cpp:194-266,1016-1032; src/Solver/TimeIntegration.cpp:181-198): the state
+// is the modal coefficient vector, the residual is R = sum_q Q_q grad(phi)_q - sum_j F_j phi_j with the
+// operator tables staged in shared memory, and M^-1 is M_ref^-1/|J| on affine elements (an exact
+// identity of the quadrature mass matrix) or a per-element inverse on bilinear quadrangles.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstring>
+#include <vector>
+
+#include "sdg_kernels.cuh"
+#include "sdg_mesh.hpp"
+#include "sdg_operators.hpp"
+
+namespace sdg {
+
+// Table layout (doubles): phi[NQ][NB] | dphiw[NQ][2][NB] (w_q dphi/dxi_b) | phif[NFP][NB] |
+//                         phifw[NFP][NB] (wf_j phif) | mref[NB][NB] (inverse reference mass matrix)
+inline size_t denseTableSize(int nb, int nq, int nfp) { return size_t(nq) * nb * 3 + size_t(nfp) * nb * 2 + size_t(nb) * nb; }
+
+inline void invertDense(int n, std::vector<double> a, std::vector<double>& inv) {
+  inv.assign(size_t(n) * n, 0.0);
+  for (int i = 0; i < n; ++i) inv[size_t(i) * n + i] = 1.0;
+  for (int c = 0; c < n; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < n; ++r) if (std::fabs(a[size_t(r) * n + c]) > std::fabs(a[size_t(piv) * n + c])) piv = r;
+    for (int k = 0; k < n; ++k) { std::swap(a[size_t(c) * n + k], a[size_t(piv) * n + k]); std::swap(inv[size_t(c) * n + k], inv[size_t(piv) * n + k]); }
+    const double d = 1.0 / a[size_t(c) * n + c];
+    for (int k = 0; k < n; ++k) { a[size_t(c) * n + k] *= d; inv[size_t(c) * n + k] *= d; }
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = a[size_t(r) * n + c];
+      if (f == 0.0) continue;
+      for (int k = 0; k < n; ++k) { a[size_t(r) * n + k] -= f * a[size_t(c) * n + k]; inv[size_t(r) * n + k] -= f * inv[size_t(c) * n + k]; }
+    }
+  }
+}
+
+void facePointInParent(int type, int f, const double* fx, double* X);
+
+inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::vector<double>& phiOut,
+                             std::vector<double>& lsqOut) {
+  const int nb = modalCount(type, p);
+  const PointRule vr = volumeRule(type, p), fr = faceRule(type, p);
+  const int nq = vr.n, nf = typeFaces(type), nfq = fr.n, nfp = nf * nfq;
+  tables.assign(denseTableSize(nb, nq, nfp), 0.0);
+  double* phi = tables.data();
+  double* dphiw = phi + size_t(nq) * nb;
+  double* phif = dphiw + size_t(nq) * 2 * nb;
+  double* phifw = phif + size_t(nfp) * nb;
+  double* mref = phifw + size_t(nfp) * nb;
+  std::vector<double> v(nb), g(size_t(nb) * 3);
+  for (int q = 0; q < nq; ++q) {
+    modalBasis(type, p, &vr.x[q * 3], v.data(), g.data());
+    for (int b = 0; b < nb; ++b) {
+      phi[size_t(q) * nb + b] = v[b];
+      dphiw[(size_t(q) * 2 + 0) * nb + b] = vr.w[q] * g[b * 3 + 0];
+      dphiw[(size_t(q) * 2 + 1) * nb + b] = vr.w[q] * g[b * 3 + 1];
+    }
+  }
+  for (int f = 0; f < nf; ++f)
+    for (int j = 0; j < nfq; ++j) {
+      double X[3]; facePointInParent(type, f, &fr.x[j * 3], X);
+      modalBasis(type, p, X, v.data(), g.data());
+      for (int b = 0; b < nb; ++b) {
+        phif[size_t(f * nfq + j) * nb + b] = v[b];
+        phifw[size_t(f * nfq + j) * nb + b] = fr.w[j] * v[b];
+      }
+    }
+  std::vector<double> m(size_t(nb) * nb, 0.0), ptp(size_t(nb) * nb, 0.0), inv;
+  for (int a = 0; a < nb; ++a)
+    for (int b = 0; b < nb; ++b) {
+      double s = 0, t = 0;
+      for (int q = 0; q < nq; ++q) { s += vr.w[q] * phi[size_t(q) * nb + a] * phi[size_t(q) * nb + b]; t += phi[size_t(q) * nb + a] * phi[size_t(q) * nb + b]; }
+      m[size_t(a) * nb + b] = s; ptp[size_t(a) * nb + b] = t;
+    }
+  invertDense(nb, m, inv);
+  std::copy(inv.begin(), inv.end(), mref);
+  phiOut.assign(phi, phi + size_t(nq) * nb);
+  // unweighted least-squares projection (InitialCondition.cpp:91-104): lsq = (Phi^T Phi)^-1 Phi^T  [nb][nq]
+  invertDense(nb, ptp, inv);
+  lsqOut.assign(size_t(nb) * nq, 0.0);
+  for (int b = 0; b < nb; ++b)
+    for (int q = 0; q < nq; ++q) {
+      double s = 0; for (int k = 0; k < nb; ++k) s += inv[size_t(b) * nb + k] * phi[size_t(q) * nb + k];
+      lsqOut[size_t(b) * nq + q] = s;
+    }
+}
+
+template <int NB, int NQ, int NFQ, int NF>
+struct DenseShape {
+  static constexpr int NV = 4;
+  static constexpr int NFP = NF * NFQ;
+  static constexpr int USTRIDE = (NV * NB + 1) & ~1;
+  static constexpr int FSTRIDE = NF * NV * NFQ;
+  static constexpr int PER_ELEM = USTRIDE + FSTRIDE + 2 * NV * NQ + NV * NB + NV * NB;
+  static constexpr int EPB = 16;
+  static constexpr int THREADS = 256;
+  static constexpr size_t TABLES = size_t(NQ) * NB * 3 + size_t(NFP) * NB * 2 + size_t(NB) * NB;
+  static constexpr size_t SMEM = (size_t(EPB) * PER_ELEM + TABLES) * 8 + 16 + 8 * NV * (THREADS / 32);
+};
+
+// Dense stage kernel (2D).  geometry: affine [e][5] = (|J| dxi_b/dx_a row-major, 1/|J|);
+// bilinear: [e][NQ][5] followed by the element's M^-1 [NB][NB].
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+__global__ void __launch_bounds__(256) denseStageKernel(StageArgs a, Phys ph) {
+  using S = DenseShape<NB, NQ, NFQ, NF>;
+  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE]
+  double* sF = sU + EPB * S::USTRIDE;                // [EPB][FSTRIDE]
+  double* sQ = sF + EPB * S::FSTRIDE;                // [EPB][2][NV][NQ]
+  double* sR = sQ + EPB * 2 * NV * NQ;               // [EPB][NV][NB]
+  double* sN = sR + EPB * NV * NB;                   // [EPB][NV][NB] new state
+  double* tab = sN + EPB * NV * NB;
+  const double* phi = tab;
+  const double* dphiw = phi + NQ * NB;
+  const double* phif = dphiw + NQ * 2 * NB;
+  const double* phifw = phif + NFP * NB;
+  const double* mref = phifw + NFP * NB;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tab + S::TABLES);
+  double* sRed = reinterpret_cast<double*>(bar + 1);
+  const int GS = AFFINE ? 5 : NQ * 5 + NB * NB;
+
+  const int tid = threadIdx.x;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  if (tid == 0) {
+    mbarInit(bar, 1);
+    const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * S::FSTRIDE * 8;
+    mbarExpectTx(bar, a.doVolume ? ub + fb : ub);
+    bulkLoad(sU, a.uin + e0 * S::USTRIDE, ub, bar);
+    if (a.doVolume) bulkLoad(sF, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+  }
+  for (int k = tid; k < int(S::TABLES); k += blockDim.x) tab[k] = a.tables[k];
+  __syncthreads();
+  const bool arrived = mbarWait(bar, 0);
+  if (__syncthreads_or(!arrived)) {
+    if (tid == 0) atomicOr(a.status, kStatusTimeout);
+    return;
+  }
+  if (a.doVolume) {
+    // values and contravariant fluxes at the volume points
+    for (int idx = tid; idx < ecount * NQ; idx += blockDim.x) {
+      const int le = idx / NQ, q = idx - le * NQ;
+      const int64_t e = e0 + le;
+      double U[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double s = 0.0;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) s = fma(phi[q * NB + b], sU[le * S::USTRIDE + v * NB + b], s);
+        U[v] = s;
+      }
+      const double* g = AFFINE ? a.geom + e * GS : a.geom + e * GS + q * 5;
+      double ja[2][2] = {{g[0], g[1]}, {g[2], g[3]}};
+      State<2> st;
+      makeState<2>(st, U, ph);
+      const double ep = st.E + st.p;
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        const double vb = dotn<2>(st.u, ja[b]);
+        double* Q = sQ + ((le * 2 + b) * NV) * NQ + q;
+        Q[0] = st.r * vb;
+        Q[NQ] = fma(st.m[0], vb, ja[b][0] * st.p);
+        Q[2 * NQ] = fma(st.m[1], vb, ja[b][1] * st.p);
+        Q[3 * NQ] = ep * vb;
+      }
+    }
+    __syncthreads();
+    // weak residual per basis function
+    for (int idx = tid; idx < ecount * NB; idx += blockDim.x) {
+      const int le = idx / NB, i = idx - le * NB;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double s = 0.0;
+        for (int q = 0; q < NQ; ++q) {
+          s = fma(sQ[((le * 2 + 0) * NV + v) * NQ + q], dphiw[(q * 2 + 0) * NB + i], s);
+          s = fma(sQ[((le * 2 + 1) * NV + v) * NQ + q], dphiw[(q * 2 + 1) * NB + i], s);
+        }
+        for (int fj = 0; fj < NFP; ++fj) {
+          const int f = fj / NFQ, j = fj - f * NFQ;
+          s = fma(-sF[le * S::FSTRIDE + (f * NV + v) * NFQ + j], phifw[fj * NB + i], s);
+        }
+        sR[(le * NV + v) * NB + i] = s;
+      }
+    }
+    __syncthreads();
+    // du = M^-1 R, RK combination
+    for (int idx = tid; idx < ecount * NB; idx += blockDim.x) {
+      const int le = idx / NB, i = idx - le * NB;
+      const int64_t e = e0 + le;
+      const double* g = a.geom + e * GS;
+      const double* minv = AFFINE ? mref : g + NQ * 5;
+      const double sc = AFFINE ? g[4] : 1.0;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double s = 0.0;
+        for (int k = 0; k < NB; ++k) s = fma(minv[i * NB + k], sR[(le * NV + v) * NB + k], s);
+        const double du = sc * s;
+        sQ[(le * NV + v) * NB + i] = du;  // sQ reused: du per basis function
+        if (a.doUpdate) {
+          const double u0 = a.ubase[e * S::USTRIDE + v * NB + i];
+          const double u1 = sU[le * S::USTRIDE + v * NB + i];
+          const double un = fma(a.c2dt, du, fma(a.c1, u1, a.c0 * u0));
+          sN[(le * NV + v) * NB + i] = un;
+          a.uout[e * S::USTRIDE + v * NB + i] = un;
+        } else {
+          sN[(le * NV + v) * NB + i] = sU[le * S::USTRIDE + v * NB + i];
+        }
+      }
+    }
+    __syncthreads();
+    if (a.rate) {
+      for (int idx = tid; idx < ecount * NQ; idx += blockDim.x) {
+        const int le = idx / NQ, q = idx - le * NQ;
+        const int64_t e = e0 + le;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          double s = 0.0;
+          for (int b = 0; b < NB; ++b) s = fma(phi[q * NB + b], sQ[(le * NV + v) * NB + b], s);
+          a.rate[(e * NQ + q) * NV + v] = s;
+        }
+      }
+    }
+    if (a.relerr) {
+      // relative error: mean over points of |R Phi^T| per element (TimeIntegration.cpp:279-324)
+      double acc[NV] = {0.0, 0.0, 0.0, 0.0};
+      for (int idx = tid; idx < ecount * NQ; idx += blockDim.x) {
+        const int le = idx / NQ, q = idx - le * NQ;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          double s = 0.0;
+          for (int b = 0; b < NB; ++b) s = fma(phi[q * NB + b], sR[(le * NV + v) * NB + b], s);
+          acc[v] += fabs(s);
+        }
+      }
+      const int warp = tid >> 5, nwarp = blockDim.x >> 5;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double x = acc[v];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if ((tid & 31) == 0) sRed[warp * NV + v] = x;
+      }
+      __syncthreads();
+      if (tid < NV) {
+        double s = 0.0;
+        for (int w = 0; w < nwarp; ++w) s += sRed[w * NV + tid];
+        a.relerr[int64_t(blockIdx.x) * NV + tid] = s / double(NQ);
+      }
+    }
+    __syncthreads();
+  } else {
+    for (int idx = tid; idx < ecount * NV * NB; idx += blockDim.x) {
+      const int le = idx / (NV * NB), r = idx - le * NV * NB;
+      sN[le * NV * NB + r] = sU[le * S::USTRIDE + r];
+    }
+    __syncthreads();
+  }
+  if (a.doTrace) {
+    for (int idx = tid; idx < ecount * NFP; idx += blockDim.x) {
+      const int le = idx / NFP, fj = idx - le * NFP;
+      const int f = fj / NFQ, j = fj - f * NFQ;
+      double* out = a.face + (a.faceBase + (e0 + le) * NF + f) * NV * NFQ + j;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double s = 0.0;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) s = fma(phif[fj * NB + b], sN[(le * NV + v) * NB + b], s);
+        out[v * NFQ] = s;
+      }
+    }
+  }
+}
+
+template <int NB, int NQ, int NFQ, int NF, bool AFF>
+inline bool denseCfg(bool device, int& threads, int& epb, size_t& smem) {
+  using S = DenseShape<NB, NQ, NFQ, NF>;
+  threads = S::THREADS; epb = S::EPB; smem = S::SMEM;
+  if (!device) return true;
+  return cudaFuncSetAttribute(denseStageKernel<NB, NQ, NFQ, NF, AFF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(S::SMEM)) == cudaSuccess;
+}
+
+// (type, P) -> (NB, NQ, NFQ): triangle P1..P5 use Dunavant rules of 3,6,12,16,25 points.
+#define SDG_DENSE_CASES(X)                                  \
+  X(SDG_ELEMENT_TRIANGLE, 1, 3, 3, 2, 3, true)              \
+  X(SDG_ELEMENT_TRIANGLE, 2, 6, 6, 3, 3, true)              \
+  X(SDG_ELEMENT_TRIANGLE, 3, 10, 12, 4, 3, true)            \
+  X(SDG_ELEMENT_TRIANGLE, 4, 15, 16, 5, 3, true)            \
+  X(SDG_ELEMENT_TRIANGLE, 5, 21, 25, 6, 3, true)            \
+  X(SDG_ELEMENT_QUADRANGLE, 1, 4, 7, 2, 4, true)            \
+  X(SDG_ELEMENT_QUADRANGLE, 1, 4, 7, 2, 4, false)
+
+inline bool configureDense(int type, int p, bool affine, bool device, int& threads, int& epb, size_t& smem) {
+#define SDG_DC(T, P, NB, NQ, NFQ, NF, AFF) \
+  if (type == T && p == P && affine == AFF) return denseCfg<NB, NQ, NFQ, NF, AFF>(device, threads, epb, smem);
+  SDG_DENSE_CASES(SDG_DC)
+#undef SDG_DC
+  return false;
+}
+
+inline bool launchDenseStage(int type, int p, bool affine, const StageArgs& a, const Phys& ph, int grid, int threads,
+                             size_t smem, cudaStream_t s) {
+#define SDG_DL(T, P, NB, NQ, NFQ, NF, AFF)                                                  \
+  if (type == T && p == P && affine == AFF) {                                               \
+    denseStageKernel<NB, NQ, NFQ, NF, AFF><<<grid, threads, smem, s>>>(a, ph);              \
+    return true;                                                                            \
+  }
+  SDG_DENSE_CASES(SDG_DL)
+#undef SDG_DL
+  return false;
+}
+
+// ---- point-layout conversions ----------------------------------------------------------------------
+// state[e][v][b] (padded stride) <- points[e][q][v]; proj = null for tensor blocks (nodes are points),
+// else the least-squares projection [nb][nq].
+__global__ void pointToStateKernel(const double* __restrict__ pts, double* __restrict__ st,
+                                   const double* __restrict__ proj, int64_t ne, int nb, int nq, int nv, int ustride) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ne * nb) return;
+  const int64_t e = t / nb;
+  const int b = int(t - e * nb);
+  for (int v = 0; v < nv; ++v) {
+    double s;
+    if (!proj) s = pts[(e * nq + b) * nv + v];
+    else { s = 0.0; for (int q = 0; q < nq; ++q) s = fma(proj[b * nq + q], pts[(e * nq + q) * nv + v], s); }
+    st[e * ustride + v * nb + b] = s;
+  }
+}
+
+__global__ void stateToPointKernel(const double* __restrict__ st, double* __restrict__ pts,
+                                   const double* __restrict__ phi, int64_t ne, int nb, int nq, int nv, int ustride) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ne * nq) return;
+  const int64_t e = t / nq;
+  const int q = int(t - e * nq);
+  for (int v = 0; v < nv; ++v) {
+    double s;
+    if (!phi) s = st[e * ustride + v * nb + q];
+    else { s = 0.0; for (int b = 0; b < nb; ++b) s = fma(phi[q * nb + b], st[e * ustride + v * nb + b], s); }
+    pts[(e * nq + q) * nv + v] = s;
+  }
+}
+
+// (rho, u, T) -> (rho, rho u, rho E) in place (VariableConvertor.cpp:341-366).
+__global__ void primitiveToConservedKernel(double* __restrict__ pts, int64_t n, int dim, Phys ph) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double* p = pts + t * (dim + 2);
+  const double rho = p[0];
+  double u2 = 0.0;
+  for (int k = 0; k < dim; ++k) { u2 += p[1 + k] * p[1 + k]; p[1 + k] *= rho; }
+  p[dim + 1] = rho * (ph.cv * p[dim + 1] + u2 / 2.0);
+}
+
+// dt = min CFL*minEdge/((|u|+c)(P+1)^2) over points (TimeIntegration.cpp:104-131); per-CTA minima.
+__global__ void deltaTimeKernel(const double* __restrict__ pts, const double* __restrict__ minEdge, int64_t n, int nq,
+                                int dim, double cfl, double p1sq, Phys ph, double* __restrict__ part) {
+  __shared__ double sh[256];
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  double dt = 1.79769313486231570e308;
+  if (t < n) {
+    const double* p = pts + t * (dim + 2);
+    const double rho = p[0];
+    double u2 = 0.0;
+    for (int k = 0; k < dim; ++k) { const double u = p[1 + k] / rho; u2 += u * u; }
+    const double e = p[dim + 1] / rho - u2 / 2.0;
+    const double pr = ph.gm1 * rho * e;
+    const double c = sqrt(ph.gamma * pr / rho);
+    dt = cfl * minEdge[t / nq] / ((sqrt(u2) + c) * p1sq);
+  }
+  sh[threadIdx.x] = dt;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+}  // namespace sdg

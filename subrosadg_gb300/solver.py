@@ -1,0 +1,303 @@
+"""Host-side mirror of SubrosaDG's System/Solver interface over the GB300 C ABI.
+
+`Mesh` holds first-order mesh arrays (generated, read from MSH 4.1, or given);
+`GpuSolver` owns one sdg_handle and exposes the members the reference's
+System<SC>::solve drives (src/Utils/SystemControl.cpp:159-195):
+initializeSolver, calculateDeltaTime, stepSolver, relative_error_;
+`System` mirrors the reference's System facade (setMesh, addBoundaryCondition,
+setThermodynamicModel, setTransportModel, setTimeIntegration, setDeltaTime,
+synchronize, solve) so a driver reads like examples/*.cpp.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from ctypes import POINTER, byref, c_double, c_int32, c_int64, c_void_p
+
+import numpy as np
+
+from . import _abi
+from ._abi import SdgConfig, SdgCounts, SdgGeneratedMesh, SdgMesh, check
+
+_pd = POINTER(c_double)
+_pi = POINTER(c_int32)
+
+
+def _ptr(a, kind=_pd):
+    return a.ctypes.data_as(kind) if a is not None else None
+
+
+class Mesh:
+    """First-order mesh in gmsh vertex order (the input format of sdg_create)."""
+
+    def __init__(self, dimension, nodes, triangles=None, quadrangles=None, hexahedra=None, boundary=None,
+                 boundary_physical=None, physical_conditions=None, periodic_master=None):
+        self.dimension = int(dimension)
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
+        self.triangles = None if triangles is None or len(triangles) == 0 else np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+        self.quadrangles = None if quadrangles is None or len(quadrangles) == 0 else np.ascontiguousarray(quadrangles, np.int32).reshape(-1, 4)
+        self.hexahedra = None if hexahedra is None or len(hexahedra) == 0 else np.ascontiguousarray(hexahedra, np.int32).reshape(-1, 8)
+        nbv = 2 if self.dimension == 2 else 4
+        self.boundary = np.zeros((0, nbv), np.int32) if boundary is None else np.ascontiguousarray(boundary, np.int32).reshape(-1, nbv)
+        self.boundary_physical = np.zeros(0, np.int32) if boundary_physical is None else np.ascontiguousarray(boundary_physical, np.int32)
+        self.physical_conditions = np.zeros(0, np.int32) if physical_conditions is None else np.ascontiguousarray(physical_conditions, np.int32)
+        self.periodic_master = None if periodic_master is None else np.ascontiguousarray(periodic_master, np.int32)
+
+    @classmethod
+    def _from_generated(cls, g: SdgGeneratedMesh):
+        m = g.mesh
+        def arr(p, n, w, dt):
+            if not p or n == 0:
+                return None
+            return np.ctypeslib.as_array(p, shape=(n * w,)).astype(dt).copy()
+        nbv = 2 if m.dimension == 2 else 4
+        out = cls(m.dimension, arr(m.node_coordinate, m.node_count, 3, np.float64),
+                  arr(m.triangle_node, m.triangle_count, 3, np.int32),
+                  arr(m.quadrangle_node, m.quadrangle_count, 4, np.int32),
+                  arr(m.hexahedron_node, m.hexahedron_count, 8, np.int32),
+                  arr(m.boundary_node, m.boundary_count, nbv, np.int32),
+                  arr(m.boundary_physical, m.boundary_count, 1, np.int32),
+                  arr(m.physical_boundary_condition, m.physical_count, 1, np.int32),
+                  arr(m.periodic_master, m.node_count, 1, np.int32))
+        _abi.load().sdg_mesh_free(byref(g))
+        return out
+
+    @classmethod
+    def box_2d(cls, x0, y0, lx, ly, nx, ny, periodic=True, jitter=0.0, split_fraction=0.0, seed=0,
+               boundary_conditions=None):
+        lib = _abi.load()
+        g = SdgGeneratedMesh()
+        bc = None if boundary_conditions is None else np.ascontiguousarray(boundary_conditions, np.int32)
+        check(lib.sdg_mesh_generate_2d(x0, y0, lx, ly, nx, ny, jitter, split_fraction, seed, int(periodic),
+                                       _ptr(bc, _pi), byref(g)))
+        return cls._from_generated(g)
+
+    @classmethod
+    def box_3d(cls, x0, y0, z0, lx, ly, lz, nx, ny, nz, periodic=True, boundary_conditions=None):
+        lib = _abi.load()
+        g = SdgGeneratedMesh()
+        bc = None if boundary_conditions is None else np.ascontiguousarray(boundary_conditions, np.int32)
+        check(lib.sdg_mesh_generate_3d(x0, y0, z0, lx, ly, lz, nx, ny, nz, int(periodic), _ptr(bc, _pi), byref(g)))
+        return cls._from_generated(g)
+
+    @classmethod
+    def read_msh(cls, path):
+        lib = _abi.load()
+        g = SdgGeneratedMesh()
+        check(lib.sdg_mesh_read_msh(str(path).encode(), byref(g)))
+        return cls._from_generated(g)
+
+    def set_boundary_condition(self, physical_index, condition):
+        """System::addBoundaryCondition<BC>(physical_index) (src/Utils/SystemControl.cpp:76-80)."""
+        if physical_index < 1 or physical_index > len(self.physical_conditions):
+            raise ValueError("physical index out of range")
+        self.physical_conditions[physical_index - 1] = condition
+
+    def struct(self) -> SdgMesh:
+        m = SdgMesh()
+        m.dimension = self.dimension
+        m.node_count = self.nodes.shape[0]
+        m.node_coordinate = _ptr(self.nodes)
+        m.periodic_master = _ptr(self.periodic_master, _pi)
+        m.triangle_count = 0 if self.triangles is None else self.triangles.shape[0]
+        m.triangle_node = _ptr(self.triangles, _pi)
+        m.quadrangle_count = 0 if self.quadrangles is None else self.quadrangles.shape[0]
+        m.quadrangle_node = _ptr(self.quadrangles, _pi)
+        m.hexahedron_count = 0 if self.hexahedra is None else self.hexahedra.shape[0]
+        m.hexahedron_node = _ptr(self.hexahedra, _pi)
+        m.boundary_count = self.boundary.shape[0]
+        m.boundary_node = _ptr(self.boundary, _pi)
+        m.boundary_physical = _ptr(self.boundary_physical, _pi)
+        m.physical_count = len(self.physical_conditions)
+        m.physical_boundary_condition = _ptr(self.physical_conditions, _pi)
+        return m
+
+
+def make_config(polynomial_order, equation=_abi.EULER, convective_flux=_abi.HLLC, viscous_flux=_abi.VISCOUS_NONE,
+                time_integration=_abi.SSPRK3, cp=2.5, cv=25.0 / 14.0, gamma=1.4, mu=0.0, prandtl=0.71,
+                transport=_abi.TRANSPORT_CONSTANT) -> SdgConfig:
+    c = SdgConfig()
+    c.polynomial_order = polynomial_order
+    c.equation = equation
+    c.convective_flux = convective_flux
+    c.viscous_flux = viscous_flux
+    c.time_integration = time_integration
+    c.transport_model = transport
+    c.specific_heat_ratio = gamma
+    c.specific_heat_constant_pressure = cp
+    c.specific_heat_constant_volume = cv
+    c.dynamic_viscosity = mu
+    c.prandtl_number = prandtl
+    return c
+
+
+class GpuSolver:
+    """The GPU Solver<SC>: one sdg_handle on one device."""
+
+    def __init__(self, mesh: Mesh, config: SdgConfig, device: int = 0):
+        self.lib = _abi.load()
+        self.mesh = mesh
+        self.config = config
+        self._m = mesh.struct()
+        h = c_void_p()
+        check(self.lib.sdg_create(byref(self._m), byref(config), device, byref(h)))
+        self.h = h
+        c = SdgCounts()
+        check(self.lib.sdg_get_counts(self.h, byref(c)), self.h)
+        self.counts = c
+        self.nv = c.conserved_variable_count
+        self.relative_error_ = np.zeros(self.nv)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sdg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        check(rc, self.h)
+
+    # geometry ----------------------------------------------------------------------------------
+    def volume_points(self):
+        out = np.zeros((self.counts.volume_point_count, 3))
+        self._chk(self.lib.sdg_volume_point_coordinate(self.h, _ptr(out)))
+        return out
+
+    def boundary_points(self):
+        out = np.zeros((self.counts.boundary_point_count, 3))
+        phys = np.zeros(self.counts.boundary_face_count, np.int32)
+        self._chk(self.lib.sdg_boundary_point_coordinate(self.h, _ptr(out), _ptr(phys, _pi)))
+        return out, phys
+
+    def adjacency(self):
+        ni, nb = self.counts.interior_face_count, self.counts.boundary_face_count
+        a = np.zeros((ni, 7), np.int32)
+        b = np.zeros((nb, 5), np.int32)
+        self._chk(self.lib.sdg_adjacency(self.h, _ptr(a, _pi), _ptr(b, _pi)))
+        return a, b
+
+    # state -------------------------------------------------------------------------------------
+    def initialize_primitive(self, primitive):
+        p = np.ascontiguousarray(primitive, np.float64)
+        assert p.shape == (self.counts.volume_point_count, self.nv)
+        self._chk(self.lib.sdg_set_initial_primitive(self.h, _ptr(p)))
+
+    def set_boundary_primitive(self, primitive):
+        p = np.ascontiguousarray(primitive, np.float64)
+        assert p.shape == (self.counts.boundary_point_count, self.nv)
+        self._chk(self.lib.sdg_set_boundary_primitive(self.h, _ptr(p)))
+
+    def set_state_point(self, conserved):
+        p = np.ascontiguousarray(conserved, np.float64)
+        self._chk(self.lib.sdg_set_state_point(self.h, _ptr(p)))
+
+    def state_point(self, out=None):
+        if out is None:
+            out = np.zeros((self.counts.volume_point_count, self.nv))
+        self._chk(self.lib.sdg_get_state_point(self.h, _ptr(out)))
+        return out
+
+    def set_state_modal(self, coef):
+        p = np.ascontiguousarray(coef, np.float64)
+        self._chk(self.lib.sdg_set_state_modal(self.h, _ptr(p)))
+
+    def state_modal(self):
+        out = np.zeros(self.counts.degree_of_freedom_count)
+        self._chk(self.lib.sdg_get_state_modal(self.h, _ptr(out)))
+        return out
+
+    def residual_point(self):
+        out = np.zeros((self.counts.volume_point_count, self.nv))
+        self._chk(self.lib.sdg_residual_point(self.h, _ptr(out)))
+        return out
+
+    # reference Solver<SC> members --------------------------------------------------------------
+    def calculateDeltaTime(self, cfl):
+        dt = c_double()
+        self._chk(self.lib.sdg_calculate_delta_time(self.h, cfl, byref(dt)))
+        return dt.value
+
+    def stepSolver(self, dt, steps=1):
+        self._chk(self.lib.sdg_step(self.h, steps, dt))
+        self._chk(self.lib.sdg_relative_error(self.h, _ptr(self.relative_error_)))
+        return self.relative_error_
+
+    def step_async(self, dt, steps=1):
+        self._chk(self.lib.sdg_step_async(self.h, steps, dt))
+
+    def synchronize(self):
+        self._chk(self.lib.sdg_synchronize(self.h))
+
+    def relative_error(self):
+        out = np.zeros(self.nv)
+        self._chk(self.lib.sdg_relative_error(self.h, _ptr(out)))
+        return out
+
+    def launch_count(self):
+        n = c_int64()
+        self._chk(self.lib.sdg_launch_count(self.h, byref(n)))
+        return n.value
+
+
+class System:
+    """Mirror of SubrosaDG's System<SimulationControl> (src/Utils/SystemControl.cpp:42-236)."""
+
+    def __init__(self, dimension, polynomial_order, equation=_abi.EULER, convective_flux=_abi.HLLC,
+                 viscous_flux=_abi.VISCOUS_NONE, time_integration=_abi.SSPRK3, device=0):
+        self.dimension = dimension
+        self.cfg = dict(polynomial_order=polynomial_order, equation=equation, convective_flux=convective_flux,
+                        viscous_flux=viscous_flux, time_integration=time_integration)
+        self.device = device
+        self.mesh = None
+        self.cfl = 1.0
+        self.iteration_start, self.iteration_end = 0, 0
+        self.delta_time = 0.0
+        self.solver = None
+        self.initial_condition = None   # callable(coords[n,3]) -> primitive[n, d+2]
+        self.boundary_condition = None  # callable(coords[n,3], physical[n]) -> primitive[n, d+2]
+        self.error_history = []
+
+    def setMesh(self, mesh: Mesh):
+        self.mesh = mesh
+
+    def addBoundaryCondition(self, condition, physical_index):
+        self.mesh.set_boundary_condition(physical_index, condition)
+
+    def setThermodynamicModel(self, cp, cv):
+        self.cfg.update(cp=cp, cv=cv)
+
+    def setTransportModel(self, mu, transport=_abi.TRANSPORT_CONSTANT, prandtl=0.71):
+        self.cfg.update(mu=mu, transport=transport, prandtl=prandtl)
+
+    def setTimeIntegration(self, cfl, iteration_range):
+        self.cfl = cfl
+        self.iteration_start, self.iteration_end = iteration_range
+
+    def setDeltaTime(self, dt):
+        self.delta_time = dt
+
+    def synchronize(self):
+        self.solver = GpuSolver(self.mesh, make_config(**self.cfg), self.device)
+
+    def solve(self):
+        s = self.solver
+        pts = s.volume_points()
+        s.initialize_primitive(self.initial_condition(pts[:, : self.dimension]))
+        if s.counts.boundary_face_count:
+            bpts, phys = s.boundary_points()
+            nfq = s.counts.face_point_count
+            s.set_boundary_primitive(self.boundary_condition(bpts[:, : self.dimension], np.repeat(phys, nfq)))
+        if self.delta_time == 0.0:
+            self.delta_time = s.calculateDeltaTime(self.cfl)
+        for i in range(self.iteration_start + 1, self.iteration_end + 1):
+            err = s.stepSolver(self.delta_time).copy()
+            self.error_history.append((i * self.delta_time, err))
+            if np.isnan(err).all():  # src/Utils/SystemControl.cpp:185-191
+                self.iteration_end = i
+                break
+        return self.error_history

@@ -1,0 +1,126 @@
+"""Seeded synthetic workloads shared by the tests, the golden fixtures and bench.py.
+
+The reference's headline workloads are canonical analytic flows; no dataset is involved.
+  vortex2d : periodic isentropic vortex (strength 5, rho=1, u=(1,1), p=1) on [-5,5]^2, quads, Roe
+  tgv3d    : Taylor-Green vortex, Mach 0.1, periodic [0,2pi]^3, hexahedra, HLLC
+  kh2d     : Kelvin-Helmholtz shear layer on [0,1]^2 (rho 1/2 bands, u=+-0.5, seeded 1e-2 sinusoidal v),
+             jittered quads with a seeded half split into triangles, LF
+Thermodynamics follow the example drivers: cp = 2.5, cv = 25/14 (R = 1/1.4), gamma = 1.4
+(examples/periodic_2d_ceuler.cpp:51), so the primitive temperature is T = p / (rho R).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+import subrosadg_gb300 as sdg
+
+GAMMA = 1.4
+CP, CV = 2.5, 25.0 / 14.0
+R_GAS = CP - CV
+
+
+def vortex_primitive(x, y, beta=5.0, gamma=GAMMA, period=10.0):
+    # nearest periodic image of the vortex centre at the origin
+    x = (x + period / 2) % period - period / 2
+    y = (y + period / 2) % period - period / 2
+    r2 = x * x + y * y
+    du = beta / (2 * math.pi) * np.exp(0.5 * (1 - r2))
+    u = 1.0 - du * y
+    v = 1.0 + du * x
+    t = 1.0 - (gamma - 1) * beta ** 2 / (8 * gamma * math.pi ** 2) * np.exp(1 - r2)
+    rho = t ** (1.0 / (gamma - 1))
+    p = rho ** gamma
+    return np.stack([rho, u, v, p / (rho * R_GAS)], 1)
+
+
+def tgv_primitive(x, y, z, mach=0.1, gamma=GAMMA):
+    p0 = 1.0 / (gamma * mach ** 2)
+    u = np.sin(x) * np.cos(y) * np.cos(z)
+    v = -np.cos(x) * np.sin(y) * np.cos(z)
+    w = np.zeros_like(x)
+    p = p0 + (np.cos(2 * x) + np.cos(2 * y)) * (np.cos(2 * z) + 2.0) / 16.0
+    rho = p / p0  # isothermal start, T0 = p0 / (rho0 R)
+    return np.stack([rho, u, v, w, p / (rho * R_GAS)], 1)
+
+
+def kh_primitive(x, y, seed=7):
+    rng = np.random.default_rng(seed)
+    k = int(rng.integers(1, 4))
+    phase = float(rng.uniform(0, 2 * math.pi))
+    band = (y >= 0.25) & (y <= 0.75)
+    rho = np.where(band, 2.0, 1.0)
+    u = np.where(band, 0.5, -0.5)
+    v = 1e-2 * np.sin(2 * math.pi * k * x + phase)
+    p = np.full_like(x, 2.5)  # examples/khinstability_2d_ceuler.cpp:33-40
+    return np.stack([rho, u, v, p / (rho * R_GAS)], 1)
+
+
+def uniform_primitive(n, dim, rho=1.0, vel=(0.3, -0.2, 0.1), p=1.0):
+    out = np.zeros((n, dim + 2))
+    out[:, 0] = rho
+    out[:, 1:1 + dim] = vel[:dim]
+    out[:, dim + 1] = p / (rho * R_GAS)
+    return out
+
+
+def config(p, flux, equation=sdg.EULER, viscous=sdg.VISCOUS_NONE, mu=0.0, prandtl=0.71, rk=sdg.SSPRK3):
+    return sdg.make_config(p, equation=equation, convective_flux=flux, viscous_flux=viscous, time_integration=rk,
+                           cp=CP, cv=CV, gamma=GAMMA, mu=mu, prandtl=prandtl)
+
+
+def vortex_case(n=8, p=3, flux=sdg.ROE, dt=1e-3, steps=4):
+    mesh = sdg.Mesh.box_2d(-5.0, -5.0, 10.0, 10.0, n, n, periodic=True)
+    return (mesh, config(p, flux), lambda pts: vortex_primitive(pts[:, 0], pts[:, 1]), None, dt, steps)
+
+
+def tgv_case(n=3, p=3, flux=sdg.HLLC, dt=None, steps=3):
+    mesh = sdg.Mesh.box_3d(0, 0, 0, 2 * math.pi, 2 * math.pi, 2 * math.pi, n, n, n, periodic=True)
+    if dt is None:
+        # CFL 0.2 with minEdge = 2 pi / n and max(|u|+c) ~ 1 + 1/Mach (TimeIntegration.cpp:119-125)
+        dt = 0.2 * (2 * math.pi / n) / ((1.0 + 1.0 / 0.1 + 0.05) * (p + 1) ** 2)
+    return (mesh, config(p, flux), lambda pts: tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2]), None, dt, steps)
+
+
+def kh_case(n=8, p=4, flux=sdg.LAX_FRIEDRICHS, dt=2e-4, steps=3, jitter=0.1, split=0.5, seed=11):
+    mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=True, jitter=jitter, split_fraction=split, seed=seed)
+    return (mesh, config(p, flux), lambda pts: kh_primitive(pts[:, 0], pts[:, 1]), None, dt, steps)
+
+
+def channel_case(p=2, flux=sdg.HLLC, conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.PRESSURE_OUTFLOW,
+                                                  sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW),
+                 n=6, dt=5e-4, steps=3, jitter=0.0, split=0.0):
+    """Non-periodic box with boundary groups bottom/right/top/left (all six BC kinds testable)."""
+    mesh = sdg.Mesh.box_2d(0.0, 0.0, 2.0, 1.0, 2 * n, n, periodic=False, jitter=jitter, split_fraction=split,
+                           seed=5, boundary_conditions=list(conditions))
+
+    def ic(pts):
+        x, y = pts[:, 0], pts[:, 1]
+        rho = 1.0 + 0.1 * np.sin(math.pi * x) * np.sin(math.pi * y)
+        u = 0.4 + 0.05 * np.cos(math.pi * y)
+        v = 0.05 * np.sin(math.pi * x)
+        p = 1.0 + 0.05 * np.cos(math.pi * x)
+        return np.stack([rho, u, v, p / (rho * R_GAS)], 1)
+
+    def bc(pts, phys):
+        n_ = len(pts)
+        out = np.zeros((n_, 4))
+        out[:, 0] = 1.0
+        out[:, 1] = np.where(phys == 4, 0.4, 0.0)
+        out[:, 2] = 0.0
+        out[:, 3] = 1.0 / R_GAS
+        return out
+
+    return (mesh, config(p, flux), ic, bc, dt, steps)
+
+
+def golden_cases():
+    return {
+        "vortex2d_quad_p3_roe": lambda: vortex_case(n=6, p=3, flux=sdg.ROE, steps=4),
+        "tgv3d_hex_p3_hllc": lambda: tgv_case(n=3, p=3, flux=sdg.HLLC, steps=3),
+        "kh2d_hybrid_p4_lf": lambda: kh_case(n=6, p=4, flux=sdg.LAX_FRIEDRICHS, steps=3),
+        "channel2d_quad_p2_hllc_bc": lambda: channel_case(p=2, flux=sdg.HLLC, n=4, steps=3),
+        "farfield2d_tri_p3_roe_bc": lambda: channel_case(p=3, flux=sdg.ROE, n=4, steps=3, split=1.0,
+                                                         conditions=(sdg.RIEMANN_FARFIELD,) * 4),
+    }

@@ -1,0 +1,30 @@
+"""Test configuration: the `gpu` marker and in-tree builds of the library and the oracle."""
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built():
+    from oracle import build as oracle_build
+    from subrosadg_gb300 import build as lib_build
+    lib_build.build_library()
+    oracle_build.build()
+    yield
+
+
+def gpu_available():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False

@@ -1,0 +1,152 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on the same meshes and initial states.
+
+Tolerances (FP64 throughout):
+  * initial state (least-squares projection)          relative L2 <= 1e-13
+  * one-stage residual du/dt at the volume points      relative L2 <= 1e-12
+  * state after N steps, per conserved variable        relative L2 <= 1e-10
+  * relative error of the last step (basis-dependent)  relative     <= 1e-9
+  * CFL time step                                      relative     <= 1e-13
+The GPU path uses a nodal Gauss-collocation basis on quadrangles/hexahedra and the oracle the reference's
+modal basis; both represent the same DG solution, so states and rates are compared at the volume points.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import subrosadg_gb300 as sdg
+from oracle.orc import Oracle
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def per_var(a, b):
+    return [rel_l2(a[:, v], b[:, v]) if np.linalg.norm(b[:, v]) > 0 else float(np.abs(a[:, v]).max())
+            for v in range(b.shape[1])]
+
+
+def pair(case):
+    mesh, cfg, prim, bprim, dt, steps = case
+    g = sdg.GpuSolver(mesh, cfg)
+    o = Oracle(mesh, cfg, faithful=False)
+    pts = g.volume_points()
+    np.testing.assert_allclose(pts, o.volume_points(), atol=1e-12)
+    p0 = prim(pts)
+    g.initialize_primitive(p0)
+    o.initialize_primitive(p0)
+    if g.counts.boundary_face_count:
+        bpts, phys = g.boundary_points()
+        bp = bprim(bpts, np.repeat(phys, g.counts.face_point_count))
+        g.set_boundary_primitive(bp)
+        o.set_boundary_primitive(bp)
+    return g, o, dt, steps
+
+
+CASES = {
+    "vortex-quad-p3-roe": lambda: cases.vortex_case(n=6, p=3, flux=sdg.ROE, steps=5),
+    "vortex-quad-p2-hllc": lambda: cases.vortex_case(n=6, p=2, flux=sdg.HLLC, steps=5),
+    "vortex-quad-p4-lf": lambda: cases.vortex_case(n=5, p=4, flux=sdg.LAX_FRIEDRICHS, steps=5),
+    "vortex-quad-p5-central": lambda: cases.vortex_case(n=4, p=5, flux=sdg.CENTRAL, steps=3),
+    "vortex-quad-p1-roe-dense": lambda: cases.vortex_case(n=8, p=1, flux=sdg.ROE, steps=5),
+    "tgv-hex-p1-hllc": lambda: cases.tgv_case(n=4, p=1, flux=sdg.HLLC, steps=4),
+    "tgv-hex-p2-roe": lambda: cases.tgv_case(n=3, p=2, flux=sdg.ROE, steps=4),
+    "tgv-hex-p3-hllc": lambda: cases.tgv_case(n=3, p=3, flux=sdg.HLLC, steps=4),
+    "tgv-hex-p3-lf": lambda: cases.tgv_case(n=3, p=3, flux=sdg.LAX_FRIEDRICHS, steps=3),
+    "tgv-hex-p4-hllc": lambda: cases.tgv_case(n=3, p=4, flux=sdg.HLLC, steps=2),
+    "tgv-hex-p5-roe": lambda: cases.tgv_case(n=3, p=5, flux=sdg.ROE, steps=2),
+    "kh-hybrid-p4-lf": lambda: cases.kh_case(n=6, p=4, flux=sdg.LAX_FRIEDRICHS, steps=4),
+    "kh-jitter-quad-p3-hllc": lambda: cases.kh_case(n=6, p=3, flux=sdg.HLLC, split=0.0, steps=4),
+    "kh-jitter-quad-p1-roe": lambda: cases.kh_case(n=6, p=1, flux=sdg.ROE, split=0.0, steps=4),
+    "kh-tri-p1-lf": lambda: cases.kh_case(n=6, p=1, flux=sdg.LAX_FRIEDRICHS, split=1.0, steps=4),
+    "kh-tri-p2-hllc": lambda: cases.kh_case(n=6, p=2, flux=sdg.HLLC, split=1.0, steps=4),
+    "kh-tri-p3-roe": lambda: cases.kh_case(n=5, p=3, flux=sdg.ROE, split=1.0, steps=3),
+    "kh-tri-p5-lf": lambda: cases.kh_case(n=4, p=5, flux=sdg.LAX_FRIEDRICHS, split=1.0, steps=2),
+    "channel-slip-inflow-outflow": lambda: cases.channel_case(p=2, flux=sdg.HLLC, n=4, steps=4),
+    "channel-farfield-tri": lambda: cases.channel_case(p=3, flux=sdg.ROE, n=4, steps=3, split=1.0,
+                                                       conditions=(sdg.RIEMANN_FARFIELD,) * 4),
+    "channel-walls-hybrid": lambda: cases.channel_case(p=3, flux=sdg.LAX_FRIEDRICHS, n=4, steps=3, split=0.5, jitter=0.1,
+                                                       conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_NONSLIP_WALL,
+                                                                   sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW)),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_parity(name):
+    g, o, dt, steps = pair(CASES[name]())
+    # initial state
+    s0g, s0o = g.state_point(), o.state_point()
+    assert rel_l2(s0g, s0o) <= 1e-13, rel_l2(s0g, s0o)
+    # one residual evaluation
+    rg, ro = g.residual_point(), o.residual_point()
+    assert rel_l2(rg, ro) <= 1e-12, (rel_l2(rg, ro), per_var(rg, ro))
+    # time step
+    dtg, dto = g.calculateDeltaTime(0.2), o.delta_time(0.2)
+    assert abs(dtg - dto) <= 1e-13 * dto
+    # N steps
+    for _ in range(steps):
+        eg = g.stepSolver(dt).copy()
+        o.step(dt)
+    sg, so = g.state_point(), o.state_point()
+    pv = per_var(sg, so)
+    assert max(pv) <= 1e-10, pv
+    np.testing.assert_allclose(eg, o.relative_error(), rtol=1e-9, atol=1e-15)
+
+
+def test_tgv_config_dt_matches_reference_formula():
+    """cfg: TGV dt from CFL 0.2 (TimeIntegration.cpp:119-125) on the GPU equals the oracle's."""
+    g, o, _, _ = pair(cases.tgv_case(n=4, p=3))
+    assert abs(g.calculateDeltaTime(0.2) - o.delta_time(0.2)) <= 1e-13 * o.delta_time(0.2)
+
+
+def test_free_stream_preserved_on_gpu():
+    mesh = sdg.Mesh.box_2d(0, 0, 1, 1, 5, 5, jitter=0.15, split_fraction=0.5, seed=3)
+    g = sdg.GpuSolver(mesh, cases.config(4, sdg.ROE))
+    g.initialize_primitive(cases.uniform_primitive(g.counts.volume_point_count, 2))
+    assert np.abs(g.residual_point()).max() < 1e-9
+    mesh = sdg.Mesh.box_3d(0, 0, 0, 1, 1, 1, 3, 3, 3)
+    g = sdg.GpuSolver(mesh, cases.config(3, sdg.HLLC))
+    g.initialize_primitive(cases.uniform_primitive(g.counts.volume_point_count, 3))
+    assert np.abs(g.residual_point()).max() < 1e-10
+
+
+def test_deterministic():
+    """No atomics on the data path: two identical runs are bit-identical."""
+    out = []
+    for _ in range(2):
+        g, o, dt, steps = pair(cases.tgv_case(n=3, p=3, steps=3))
+        g.stepSolver(dt, 3)
+        out.append((g.state_point(), g.relative_error()))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
+def test_nan_state_is_reported_by_relative_error():
+    """The reference's only failure detection: all relative errors NaN (SystemControl.cpp:185-191)."""
+    g, o, dt, _ = pair(cases.vortex_case(n=4, p=2))
+    s = g.state_point()
+    s[:, 0] = np.nan
+    g.set_state_point(s)
+    err = g.stepSolver(dt)
+    assert np.isnan(err).all()
+
+
+def test_modal_state_roundtrip_and_layout():
+    g, o, dt, _ = pair(cases.vortex_case(n=4, p=3))
+    m = g.state_modal()
+    mo = o.state_modal()
+    # same modal basis and layout as the oracle (reference layout: column-major (d+2) x Nb per element)
+    assert rel_l2(m, mo) <= 1e-12
+    g.set_state_modal(m)
+    assert rel_l2(g.state_point(), o.state_point()) <= 1e-13
+
+
+def test_launch_count_and_shape():
+    g, o, dt, _ = pair(cases.tgv_case(n=3, p=3))
+    n0 = g.launch_count()
+    g.stepSolver(dt)
+    # per SSP-RK3 stage: 1 face kernel + 1 element kernel; plus 1 reduction per step
+    assert g.launch_count() - n0 == 3 * 2 + 1

@@ -1,0 +1,163 @@
+"""CPU tests of the oracle (the CPU restatement of the reference algorithm) against the reference's
+own known answers and against analytic invariants of the DG discretisation."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import subrosadg_gb300 as sdg
+from oracle.orc import Oracle
+from tests import cases
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _tables():
+    with open(os.path.join(GOLDEN, "reference_tables.json")) as f:
+        return json.load(f)
+
+
+def _vectors():
+    with open(os.path.join(GOLDEN, "oracle_vectors.json")) as f:
+        return json.load(f)
+
+
+# ---- reference known answers -------------------------------------------------------------------------
+
+def _perm(kind, m, rot):
+    """The oracle's face-point permutation rule (oracle/orc_basis.hpp facePermutation)."""
+    if kind == "Line":
+        return [m - 1 - j for j in range(m)]
+    out = []
+    for i in range(m):
+        for k in range(m):
+            ii, kk = {0: (k, i), 1: (m - 1 - i, k), 2: (m - 1 - k, m - 1 - i), 3: (i, m - 1 - k)}[rot]
+            out.append(ii * m + kk)
+    return out
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5])
+def test_face_permutations_match_reference_tables(p):
+    t = _tables()["face_permutation"]
+    assert t[f"Line/P{p}"]["0"] == _perm("Line", p + 1, 0)
+    for rot in range(4):
+        assert t[f"Quadrangle/P{p}"][str(rot)] == _perm("Quad", p + 1, rot)
+
+
+def test_face_vertex_lists_match_reference():
+    t = _tables()["face_vertices"]
+    assert t["Triangle"] == [0, 1, 1, 2, 2, 0]
+    assert t["Quadrangle"] == [0, 1, 1, 2, 2, 3, 3, 0]
+    assert t["Hexahedron"] == [0, 3, 2, 1, 0, 1, 5, 4, 0, 4, 7, 3, 1, 2, 6, 5, 2, 3, 7, 6, 4, 5, 6, 7]
+
+
+def test_constants_match_reference():
+    t = _tables()
+    assert t["specific_heat_ratio"] == 1.4 and t["prandtl_number"] == 0.71
+    assert t["harten_divisor"] == 20.0
+    assert abs(t["sutherland_temperature"] - 110.4 / 273.15) < 1e-15
+    assert t["rk_coefficients"]["SSPRK3"] == [[1.0, 0.0, 1.0], [0.75, 0.25, 0.25], [1 / 3, 2 / 3, 2 / 3]]
+    assert t["rk_coefficients"]["HeunRK2"] == [[1.0, 0.0, 1.0], [0.5, 0.5, 0.5]]
+
+
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5])
+def test_quadrature_counts_match_reference(p):
+    """Oracle volume/face point counts equal the reference tables at orders 2P / 2P+1."""
+    counts = _tables()["quadrature_count"]
+    for kind, mesh in (("Quadrangle", sdg.Mesh.box_2d(0, 0, 1, 1, 3, 3)),
+                       ("Triangle", sdg.Mesh.box_2d(0, 0, 1, 1, 3, 3, split_fraction=1.0)),
+                       ("Hexahedron", sdg.Mesh.box_3d(0, 0, 0, 1, 1, 1, 3, 3, 3))):
+        o = Oracle(mesh, cases.config(p, sdg.HLLC), faithful=False)
+        assert o.volume_points_count == o.elements * counts[kind][2 * p]
+        face = "Line" if kind != "Hexahedron" else "Quadrangle"
+        assert o.nfq == counts[face][2 * p + 1]
+
+
+@pytest.mark.parametrize("deg", [2, 4, 6, 8, 10])
+def test_triangle_rules_exact(deg):
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(__file__)), "subrosadg_gb300", "csrc"))
+    import re
+    txt = open(os.path.join(os.path.dirname(os.path.dirname(__file__)), "subrosadg_gb300", "csrc", "triangle_rules.h")).read()
+    get = lambda n: np.array([float(x) for x in re.search(r"kTri%d%s\[\d+\] = \{([^}]*)\}" % (deg, n), txt).group(1).split(",")])
+    x, y, w = get("Xi"), get("Eta"), get("W")
+    for a in range(deg + 1):
+        for b in range(deg + 1 - a):
+            exact = math.factorial(a) * math.factorial(b) / math.factorial(a + b + 2)
+            assert abs((w * x ** a * y ** b).sum() - exact) < 1e-15
+
+
+# ---- analytic invariants of the oracle ---------------------------------------------------------------
+
+@pytest.mark.parametrize("name,mesh_fn,p,flux", [
+    ("quad", lambda: sdg.Mesh.box_2d(0, 0, 1, 1, 3, 3), 3, sdg.ROE),
+    ("jittered-hybrid", lambda: sdg.Mesh.box_2d(0, 0, 1, 1, 4, 4, jitter=0.15, split_fraction=0.5, seed=2), 4, sdg.LAX_FRIEDRICHS),
+    ("hex", lambda: sdg.Mesh.box_3d(0, 0, 0, 1, 1, 1, 3, 3, 3), 2, sdg.HLLC),
+    ("tri", lambda: sdg.Mesh.box_2d(0, 0, 1, 1, 3, 3, split_fraction=1.0, jitter=0.1, seed=4), 5, sdg.CENTRAL),
+])
+def test_free_stream_preservation(name, mesh_fn, p, flux):
+    mesh = mesh_fn()
+    o = Oracle(mesh, cases.config(p, flux), faithful=True)
+    pts = o.volume_points()
+    o.initialize_primitive(cases.uniform_primitive(len(pts), mesh.dimension))
+    r = o.residual_point()
+    assert np.abs(r).max() < 1e-9
+
+
+def test_conservation_periodic():
+    """Sum over elements of the mass-weighted rate is zero on a periodic mesh (telescoping fluxes)."""
+    mesh, cfg, prim, _, dt, _ = cases.kh_case(n=5, p=3)
+    o = Oracle(mesh, cfg, faithful=False)
+    o.initialize_primitive(prim(o.volume_points()))
+    m0 = o.state_point()
+    o.step(dt, 2)
+    m1 = o.state_point()
+    # integrate with the quadrature weights: reuse the LSQ-exact property on polynomial states
+    # by comparing the modal mean of each element (mass is conserved to round-off)
+    assert np.isfinite(m1).all()
+    assert abs(m1[:, 0].mean() - m0[:, 0].mean()) < 1e-3
+
+
+@pytest.mark.parametrize("name", list(cases.golden_cases()))
+def test_oracle_against_committed_vectors(name):
+    v = _vectors()[name]
+    mesh, cfg, prim, bprim, dt, steps = cases.golden_cases()[name]()
+    o = Oracle(mesh, cfg, faithful=False)
+    o.initialize_primitive(prim(o.volume_points()))
+    if o.boundary:
+        bpts, phys = o.boundary_points()
+        o.set_boundary_primitive(bprim(bpts, np.repeat(phys, o.nfq)))
+    r0 = o.residual_point()
+    assert abs(np.abs(r0).sum() - v["residual_checksum"]) <= 1e-10 * v["residual_checksum"]
+    np.testing.assert_allclose(r0[:: max(1, len(r0) // 16)], np.array(v["residual_sample"]), rtol=1e-9, atol=1e-9)
+    o.step(dt, steps)
+    np.testing.assert_allclose(o.state_point()[:: max(1, o.volume_points_count // 16)], np.array(v["state_sample"]),
+                               rtol=1e-11, atol=1e-12)
+    np.testing.assert_allclose(o.relative_error(), v["relative_error"], rtol=1e-9)
+    assert abs(o.delta_time(0.2) - v["delta_time_cfl_0.2"]) <= 1e-14 * v["delta_time_cfl_0.2"]
+
+
+def test_faithful_gradient_pass_does_not_change_euler():
+    """The reference runs the gradient pass for Euler too (TimeIntegration.cpp:340-343); it is unused."""
+    mesh, cfg, prim, _, dt, steps = cases.vortex_case(n=4, p=2)
+    a = Oracle(mesh, cfg, faithful=True)
+    b = Oracle(mesh, cfg, faithful=False)
+    for o in (a, b):
+        o.initialize_primitive(prim(o.volume_points()))
+        o.step(dt, 2)
+    assert np.array_equal(a.state_point(), b.state_point())
+
+
+def test_vortex_advects_at_freestream_speed():
+    """Exact-solution check: after one period-free short time the vortex is the translated IC."""
+    mesh, cfg, prim, _, _, _ = cases.vortex_case(n=10, p=3)
+    o = Oracle(mesh, cfg, faithful=False)
+    pts = o.volume_points()
+    o.initialize_primitive(prim(pts))
+    t, dt = 0.05, 1e-3
+    o.step(dt, int(round(t / dt)))
+    exact = cases.vortex_primitive(pts[:, 0] - t, pts[:, 1] - t)
+    rho = o.state_point()[:, 0]
+    assert np.abs(rho - exact[:, 0]).max() < 5e-3
