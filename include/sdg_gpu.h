@@ -196,6 +196,20 @@ int sdg_synchronize(sdg_handle* handle);
 /* Diagnostic: number of CUDA kernel launches issued by this handle since creation. */
 int sdg_launch_count(const sdg_handle* handle, int64_t* launch_count);
 
+/* The handle's CUDA stream (a cudaStream_t), for callers that enqueue their own work or events on it. */
+int sdg_get_stream(const sdg_handle* handle, void** stream);
+
+/* Diagnostic kernel timing.  While enabled every launch is bracketed by CUDA events on the handle's
+ * stream; sdg_kernel_time synchronises and returns, per kernel class -- 0 element stage kernels,
+ * 1 interior-face flux, 2 boundary-face flux, 3 other (reductions, conversions) -- the summed device
+ * milliseconds and launch counts since timing was (re-)enabled. */
+int sdg_set_kernel_timing(sdg_handle* handle, int32_t enable);
+int sdg_kernel_time(sdg_handle* handle, double* milliseconds, int64_t* launches);
+
+/* Diagnostic: sustained FP64 FMA rate of the device, in GFLOP/s (2 flops per FMA), from an
+ * independent-chain FMA kernel run for about `milliseconds` ms.  Used as the FP64 roofline. */
+int sdg_measure_fp64_peak(int32_t device, double milliseconds, double* gflops);
+
 /* Diagnostic: adjacency as canonical integer tuples, for bit-exact parity checks.
  * interior: [interior_face_count][7] = (typeL, elemL, faceL, typeR, elemR, faceR, rotation)
  * boundary: [boundary_face_count][5] = (type, elem, face, physical, boundary_condition)

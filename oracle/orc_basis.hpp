@@ -313,6 +313,7 @@ struct RefElement {
   std::vector<double> dphi;   // [nq*dim][nb]    modal_gradient_value_ (row q*dim+k)
   std::vector<double> phif;   // [nface*nfq][nb] modal_adjacency_value_
   std::vector<double> lsqInv; // [nb][nb]        modal_least_squares_inverse_
+  std::vector<double> ptp;    // [nb][nb]        Phi^T Phi
   std::vector<std::vector<int>> perm;  // rotation -> face point permutation
 
   void build(int t, int order) {
@@ -343,7 +344,7 @@ struct RefElement {
         modalBasis(t, order, X, v.data(), g.data());
         for (int b = 0; b < nb; ++b) phif[(size_t(f) * nfq + j) * nb + b] = v[b];
       }
-    std::vector<double> ptp(size_t(nb) * nb, 0.0);
+    ptp.assign(size_t(nb) * nb, 0.0);
     for (int a = 0; a < nb; ++a)
       for (int b = 0; b < nb; ++b) {
         double s = 0; for (int q = 0; q < nq; ++q) s += phi[size_t(q) * nb + a] * phi[size_t(q) * nb + b];

@@ -42,6 +42,7 @@ struct Block {
   std::vector<double> jw;       // ne * nq        |J| w
   std::vector<double> jtiw;     // ne * nq * d*d  J^-T |J| w, column-major d x d per point
   std::vector<double> minv;     // ne * nb*nb     local mass matrix inverse
+  std::vector<double> mass;     // ne * nb*nb     local mass matrix (kept when refining solves)
   std::vector<double> minEdge;  // ne
   // state (column-major nv x nb per element: index b*nv + v)
   std::vector<double> coef, last, res;
@@ -63,6 +64,11 @@ struct Problem {
   int dim = 2, nv = 4, p = 1;
   int eq = 0, flux = 0, visc = 0, rk = 2;
   bool faithful = true;
+  // Refine each M^-1 product / least-squares solve with one residual-correction step.  The reference
+  // multiplies by the explicit inverse (TimeIntegration.cpp:196); refinement removes the
+  // condition-number round-off of the hierarchic basis at high order so the checker stays accurate to
+  // ~1e-15.  Off for the timed CPU baseline, which mirrors the reference's arithmetic exactly.
+  bool refine = true;
   Physics ph;
   std::vector<Block> blocks;
   std::vector<Face> interior, boundary;
@@ -85,6 +91,7 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
   B.jw.assign(size_t(B.ne) * nq, 0.0);
   B.jtiw.assign(size_t(B.ne) * nq * d * d, 0.0);
   B.minv.assign(size_t(B.ne) * nb * nb, 0.0);
+  if (P.refine) B.mass.assign(size_t(B.ne) * nb * nb, 0.0);
   B.minEdge.assign(size_t(B.ne), 0.0);
   std::string failure;
 #pragma omp parallel for schedule(static)
@@ -138,6 +145,7 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
         m[size_t(a) * nb + b] = s;
       }
     invert(nb, m.data(), &B.minv[size_t(e) * nb * nb]);
+    if (P.refine) std::copy(m.begin(), m.end(), &B.mass[size_t(e) * nb * nb]);
     // minEdge quality: shortest straight edge between vertices.
     static const int triE[3][2] = {{0, 1}, {1, 2}, {2, 0}};
     static const int quadE[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
@@ -279,6 +287,32 @@ static void gradientTrace(const Problem& P, int b, int e, int f, double* out /* 
   interp(nr, nb, nfq, c.data(), &B.ref.phif[size_t(f) * nfq * nb], out);
 }
 
+// x = R M^-1 for an (nr x nb, column-major) block R (TimeIntegration.cpp:196,205-225), optionally refined:
+// x += (R - x M) M^-1.
+static void applyMinv(const Problem& P, const Block& B, int64_t e, int nr, const double* R, double* x) {
+  const int nb = B.ref.nb;
+  const double* Mi = &B.minv[size_t(e) * nb * nb];
+  for (int bb = 0; bb < nb; ++bb)
+    for (int r = 0; r < nr; ++r) {
+      double s = 0; for (int c = 0; c < nb; ++c) s += R[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
+      x[size_t(bb) * nr + r] = s;
+    }
+  if (!P.refine) return;
+  const double* M = &B.mass[size_t(e) * nb * nb];
+  std::vector<double> res(size_t(nr) * nb);
+  for (int bb = 0; bb < nb; ++bb)
+    for (int r = 0; r < nr; ++r) {
+      double s = R[size_t(bb) * nr + r];
+      for (int c = 0; c < nb; ++c) s -= x[size_t(c) * nr + r] * M[size_t(c) * nb + bb];
+      res[size_t(bb) * nr + r] = s;
+    }
+  for (int bb = 0; bb < nb; ++bb)
+    for (int r = 0; r < nr; ++r) {
+      double s = 0; for (int c = 0; c < nb; ++c) s += res[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
+      x[size_t(bb) * nr + r] += s;
+    }
+}
+
 // ---- the stage kernels ----------------------------------------------------------------------------
 
 static void gradientQuadratureAndResidual(Problem& P) {
@@ -366,13 +400,8 @@ static void gradientQuadratureAndResidual(Problem& P) {
           for (int c = 0; c < nq * d; ++c) s -= QV[size_t(c) * nr + r] * B.ref.dphi[size_t(c) * nb + bb];
           RV[size_t(bb) * nr + r] = s;
         }
-      const double* Mi = &B.minv[size_t(e) * nb * nb];
       double* VG = &B.vgc[size_t(e) * nr * nb];
-      for (int bb = 0; bb < nb; ++bb)
-        for (int r = 0; r < nr; ++r) {
-          double s = 0; for (int c = 0; c < nb; ++c) s += RV[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
-          VG[size_t(bb) * nr + r] = s;
-        }
+      applyMinv(P, B, e, nr, RV, VG);
       if (!P.ns()) continue;
       double* G = &B.gc[size_t(e) * nr * nb];
       std::copy_n(VG, nr * nb, G);
@@ -388,12 +417,8 @@ static void gradientQuadratureAndResidual(Problem& P) {
             RI[size_t(bb) * nr + r] = s;
           }
         double* IG = &B.igc[(size_t(e) * nblk + blk) * nr * nb];
-        for (int bb = 0; bb < nb; ++bb)
-          for (int r = 0; r < nr; ++r) {
-            double s = 0; for (int c = 0; c < nb; ++c) s += RI[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
-            IG[size_t(bb) * nr + r] = s;
-            G[size_t(bb) * nr + r] += s;
-          }
+        applyMinv(P, B, e, nr, RI, IG);
+        for (int i = 0; i < nr * nb; ++i) G[i] += IG[i];
       }
     }
   }
@@ -528,14 +553,11 @@ static void update(Problem& P, int stage, double dt) {
       double* U = &B.coef[size_t(e) * nv * nb];
       const double* L = &B.last[size_t(e) * nv * nb];
       const double* Rr = &B.res[size_t(e) * nv * nb];
-      const double* Mi = &B.minv[size_t(e) * nb * nb];
+      std::vector<double> du(size_t(nv) * nb);
+      applyMinv(P, B, e, nv, Rr, du.data());
       for (int i = 0; i < nv * nb; ++i) U[i] *= c[1];
       for (int i = 0; i < nv * nb; ++i) U[i] += c[0] * L[i];
-      for (int bb = 0; bb < nb; ++bb)
-        for (int v = 0; v < nv; ++v) {
-          double s = 0; for (int k = 0; k < nb; ++k) s += Rr[k * nv + v] * Mi[size_t(k) * nb + bb];
-          U[bb * nv + v] += c[2] * dt * s;
-        }
+      for (int i = 0; i < nv * nb; ++i) U[i] += c[2] * dt * du[i];
     }
   }
 }
@@ -597,6 +619,20 @@ static void project(Problem& P, const double* cons) {
           double s = 0; for (int k = 0; k < nb; ++k) s += t[k * nv + v] * B.ref.lsqInv[size_t(k) * nb + b];
           U[b * nv + v] = s;
         }
+      if (P.refine) {  // one correction step of the normal equations (Phi^T Phi) c = Phi^T u
+        std::vector<double> r(size_t(nv) * nb);
+        for (int b = 0; b < nb; ++b)
+          for (int v = 0; v < nv; ++v) {
+            double s = t[b * nv + v];
+            for (int k = 0; k < nb; ++k) s -= U[k * nv + v] * B.ref.ptp[size_t(k) * nb + b];
+            r[b * nv + v] = s;
+          }
+        for (int b = 0; b < nb; ++b)
+          for (int v = 0; v < nv; ++v) {
+            double s = 0; for (int k = 0; k < nb; ++k) s += r[k * nv + v] * B.ref.lsqInv[size_t(k) * nb + b];
+            U[b * nv + v] += s;
+          }
+      }
     }
     off += size_t(B.ne) * nq;
   }
@@ -605,6 +641,7 @@ static void project(Problem& P, const double* cons) {
 
 static Problem* create(const sdg_mesh* m, const sdg_config* c, int faithful) {
   auto P = std::make_unique<Problem>();
+  P->refine = faithful == 0;  // parity checker: refined solves; faithful CPU baseline: plain inverse
   P->dim = m->dimension; P->nv = P->dim + 2; P->p = c->polynomial_order;
   P->eq = c->equation; P->flux = c->convective_flux; P->visc = c->viscous_flux; P->rk = c->time_integration;
   P->faithful = faithful != 0;
@@ -789,13 +826,7 @@ int orc_residual_point(void* h, double* out) {
     const int nb = B.ref.nb, nq = B.ref.nq, nv = P.nv;
     for (int64_t e = 0; e < B.ne; ++e) {
       std::vector<double> du(size_t(nv) * nb);
-      const double* Rr = &B.res[size_t(e) * nv * nb];
-      const double* Mi = &B.minv[size_t(e) * nb * nb];
-      for (int bb = 0; bb < nb; ++bb)
-        for (int v = 0; v < nv; ++v) {
-          double s = 0; for (int k = 0; k < nb; ++k) s += Rr[k * nv + v] * Mi[size_t(k) * nb + bb];
-          du[bb * nv + v] = s;
-        }
+      orc::applyMinv(P, B, e, nv, &B.res[size_t(e) * nv * nb], du.data());
       orc::interp(nv, nb, nq, du.data(), B.ref.phi.data(), out + (off + size_t(e) * nq) * nv);
     }
     off += size_t(B.ne) * nq;

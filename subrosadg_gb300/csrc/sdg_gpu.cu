@@ -24,6 +24,21 @@
 
 namespace sdg {
 
+// Independent-chain FP64 FMA kernel (bounded loop, no waits): measures the FP64 pipe throughput.
+__global__ void fp64ProbeKernel(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) x[c] = threadIdx.x * 1e-3 + c;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = fma(x[c], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 void facePointInParent(int type, int f, const double* fx, double* X) {
   const int nfv = typeFaceVertices(type);
   const int* fl = faceVertexList(type);
@@ -110,6 +125,10 @@ struct sdg_handle {
   bool hasState = false;
   bool hostOnly = true;            // created with device < 0: no GPU resources
   int64_t launches = 0;
+  bool timing = false;             // bracket launches with events (sdg_set_kernel_timing)
+  std::vector<std::array<cudaEvent_t, 2>> timedEvents;
+  std::vector<int> timedClass;
+  int pendingClass = 3;
   int64_t elements = 0, dof = 0;
   std::string err;
 };
@@ -131,9 +150,27 @@ void upload(T* dst, const std::vector<T>& src, cudaStream_t s) {
   if (!src.empty()) SDG_CUDA(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
 }
 
+void dropTimingEvents(sdg_handle* h) {
+  for (auto& ev : h->timedEvents) { cudaEventDestroy(ev[0]); cudaEventDestroy(ev[1]); }
+  h->timedEvents.clear();
+  h->timedClass.clear();
+}
+
+// Optional event bracketing of each launch (diagnostic kernel timing).
+void beginLaunch(sdg_handle* h, int cls) {
+  if (!h->timing) return;
+  std::array<cudaEvent_t, 2> ev;
+  SDG_CUDA(cudaEventCreate(&ev[0]));
+  SDG_CUDA(cudaEventCreate(&ev[1]));
+  SDG_CUDA(cudaEventRecord(ev[0], h->stream));
+  h->timedEvents.push_back(ev);
+  h->timedClass.push_back(cls);
+}
+
 void checkLaunch(sdg_handle* h) {
   h->launches++;
   SDG_CUDA(cudaGetLastError());
+  if (h->timing && !h->timedEvents.empty()) SDG_CUDA(cudaEventRecord(h->timedEvents.back()[1], h->stream));
 }
 
 // ---- geometry --------------------------------------------------------------------------------------
@@ -282,6 +319,7 @@ void configureTensor(DevBlock& B, bool device) {
 }
 
 void launchTensor(sdg_handle* h, DevBlock& B, const StageArgs& a) {
+  beginLaunch(h, 0);
 #define SDG_TL(D, NN)                                                                                          \
   if (B.dim == D && B.n == NN) {                                                                               \
     if (B.affine) tensorStageKernel<D, NN, true><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);          \
@@ -296,6 +334,7 @@ void launchTensor(sdg_handle* h, DevBlock& B, const StageArgs& a) {
 }
 
 void launchDense(sdg_handle* h, DevBlock& B, const StageArgs& a) {
+  beginLaunch(h, 0);
   if (!launchDenseStage(B.type, B.p, B.affine != 0, a, h->ph, B.grid, B.threads, B.smem, h->stream))
     throw Failure(SDG_ERR_UNSUPPORTED, "unsupported dense block");
   checkLaunch(h);
@@ -306,6 +345,7 @@ void launchFaces(sdg_handle* h) {
   if (h->nInterior > 0) {
     const int64_t threads = h->nInterior * h->nfq;
     const int grid = int((threads + 255) / 256);
+    beginLaunch(h, 1);
 #define SDG_FL(D, F) \
   if (h->dim == D && flux == F) { faceKernel<D, F><<<grid, 256, 0, h->stream>>>(h->face, h->fconn, h->fgeo, h->nInterior, h->n1d, h->ph); }
     SDG_FL(2, 0) SDG_FL(2, 1) SDG_FL(2, 2) SDG_FL(2, 3) SDG_FL(3, 0) SDG_FL(3, 1) SDG_FL(3, 2) SDG_FL(3, 3)
@@ -315,6 +355,7 @@ void launchFaces(sdg_handle* h) {
   if (h->nBoundary > 0) {
     const int64_t threads = h->nBoundary * h->nfq;
     const int grid = int((threads + 255) / 256);
+    beginLaunch(h, 2);
     if (h->dim == 2) boundaryFaceKernel<2><<<grid, 256, 0, h->stream>>>(h->face, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
     else boundaryFaceKernel<3><<<grid, 256, 0, h->stream>>>(h->face, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
     checkLaunch(h);
@@ -368,6 +409,7 @@ void stepOnce(sdg_handle* h, double dt, bool relerr) {
     }
   }
   if (relerr) {
+    beginLaunch(h, 3);
     relerrReduceKernel<<<h->nv, 256, 0, h->stream>>>(h->relPart, h->relParts, h->nv, 1.0 / double(h->elements), h->relOut);
     checkLaunch(h);
   }
@@ -413,6 +455,34 @@ void stateToPoints(sdg_handle* h, int which) {
                                                     B.ustride);
     checkLaunch(h);
   }
+}
+
+double measureFp64Peak(int device, double ms) {
+  SDG_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  SDG_CUDA(cudaGetDeviceProperties(&prop, device));
+  const int threads = 256, blocks = prop.multiProcessorCount * 8;
+  double* out = devAlloc<double>(size_t(threads) * blocks);
+  cudaEvent_t e0, e1;
+  SDG_CUDA(cudaEventCreate(&e0));
+  SDG_CUDA(cudaEventCreate(&e1));
+  int iters = 256;
+  float t = 0.f;
+  fp64ProbeKernel<<<blocks, threads>>>(out, 16, 1.0000001, 1e-9);
+  SDG_CUDA(cudaDeviceSynchronize());
+  for (int round = 0; round < 12; ++round) {
+    SDG_CUDA(cudaEventRecord(e0));
+    fp64ProbeKernel<<<blocks, threads>>>(out, iters, 1.0000001, 1e-9);
+    SDG_CUDA(cudaEventRecord(e1));
+    SDG_CUDA(cudaEventSynchronize(e1));
+    SDG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    if (t >= 0.5 * ms || iters >= (1 << 22)) break;
+    iters *= 2;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  return 2.0 * 8.0 * double(threads) * blocks * iters / (double(t) * 1e6);
 }
 
 }  // namespace
@@ -683,6 +753,7 @@ int sdg_destroy(sdg_handle* h) {
   if (h->hostOnly) { delete h; return SDG_OK; }
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  dropTimingEvents(h);
   for (DevBlock& B : h->blocks) {
     cudaFree(B.geom); cudaFree(B.tables); cudaFree(B.minedge); cudaFree(B.phiDev); cudaFree(B.lsqDev);
   }
@@ -949,6 +1020,52 @@ int sdg_synchronize(sdg_handle* h) {
 int sdg_launch_count(const sdg_handle* h, int64_t* n) {
   if (!h || !n) return SDG_ERR_INVALID_ARGUMENT;
   *n = h->launches;
+  return SDG_OK;
+}
+
+int sdg_get_stream(const sdg_handle* h, void** stream) {
+  if (!h || !stream) return SDG_ERR_INVALID_ARGUMENT;
+  *stream = h->stream;
+  return SDG_OK;
+}
+
+int sdg_set_kernel_timing(sdg_handle* h, int32_t enable) {
+  if (!h) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  dropTimingEvents(h);
+  h->timing = enable != 0;
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_kernel_time(sdg_handle* h, double* ms, int64_t* launches) {
+  if (!h || !ms || !launches) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  for (int k = 0; k < 4; ++k) { ms[k] = 0.0; launches[k] = 0; }
+  for (size_t i = 0; i < h->timedEvents.size(); ++i) {
+    float t = 0.f;
+    SDG_CUDA(cudaEventElapsedTime(&t, h->timedEvents[i][0], h->timedEvents[i][1]));
+    ms[h->timedClass[i]] += t;
+    launches[h->timedClass[i]] += 1;
+  }
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_measure_fp64_peak(int32_t device, double milliseconds, double* gflops) {
+  if (!gflops || !(milliseconds > 0)) return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    *gflops = measureFp64Peak(device, milliseconds);
+  } catch (const Failure& f) {
+    g_create_error = f.what();
+    return f.code;
+  }
   return SDG_OK;
 }
 

@@ -136,7 +136,7 @@ def test_oracle_against_committed_vectors(name):
     np.testing.assert_allclose(o.state_point()[:: max(1, o.volume_points_count // 16)], np.array(v["state_sample"]),
                                rtol=1e-11, atol=1e-12)
     np.testing.assert_allclose(o.relative_error(), v["relative_error"], rtol=1e-9)
-    assert abs(o.delta_time(0.2) - v["delta_time_cfl_0.2"]) <= 1e-14 * v["delta_time_cfl_0.2"]
+    assert abs(o.delta_time(0.2) - v["delta_time_cfl_0.2"]) <= 1e-12 * v["delta_time_cfl_0.2"]
 
 
 def test_faithful_gradient_pass_does_not_change_euler():
