@@ -13,19 +13,19 @@ from ctypes import POINTER, byref, c_double, c_int, c_int32, c_int64, c_void_p
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB = os.path.join(HERE, "liborc.so")
+LIBS = {"double": os.path.join(HERE, "liborc.so"), "extended": os.path.join(HERE, "liborc_ext.so")}
 _pd = POINTER(c_double)
 _pi = POINTER(c_int32)
-_lib = None
+_libs = {}
 
 
-def load():
-    global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
+def load(precision="double"):
+    if precision not in _libs:
+        path = LIBS[precision]
+        if not os.path.exists(path):
             from . import build as _build
             _build.build()
-        lib = ctypes.CDLL(LIB)
+        lib = ctypes.CDLL(path)
         lib.orc_create.restype = c_void_p
         lib.orc_create.argtypes = [c_void_p, c_void_p, c_int]
         lib.orc_last_error.restype = ctypes.c_char_p
@@ -42,18 +42,26 @@ def load():
         lib.orc_adjacency.argtypes = [c_void_p, _pi, _pi]
         lib.orc_set_threads.argtypes = [c_int]
         lib.orc_max_threads.restype = c_int
-        _lib = lib
-    return _lib
+        lib.orc_real_digits.restype = c_int
+        _libs[precision] = lib
+    return _libs[precision]
 
 
 class Oracle:
-    """CPU restatement of the reference solver on the same mesh/config structs as sdg_create."""
+    """CPU restatement of the reference solver on the same mesh/config structs as sdg_create.
 
-    def __init__(self, mesh, config, faithful=True):
-        self.lib = load()
+    faithful=True : the reference's arithmetic -- gradient pass also for Euler, plain explicit inverses
+                    (the timed CPU baseline);
+    faithful=False: the checker -- no unused gradient pass, solves refined by one correction step.
+    precision     : "double" (the reference's Real) or "extended" (long double truth).
+    """
+
+    def __init__(self, mesh, config, faithful=True, precision="double"):
+        self.lib = load(precision)
         self._m = mesh.struct()
         self._c = config
-        self.h = self.lib.orc_create(ctypes.addressof(self._m), ctypes.addressof(self._c), int(faithful))
+        flags = 3 if faithful else 0
+        self.h = self.lib.orc_create(ctypes.addressof(self._m), ctypes.addressof(self._c), flags)
         if not self.h:
             raise RuntimeError("oracle: " + self.lib.orc_last_error().decode())
         c = (c_int64 * 6)()
@@ -129,8 +137,8 @@ class Oracle:
         return out
 
 
-def set_threads(n):
-    load().orc_set_threads(int(n))
+def set_threads(n, precision="double"):
+    load(precision).orc_set_threads(int(n))
 
 
 def max_threads():

@@ -11,6 +11,7 @@
 // against gmsh itself; the DG solution does not depend on the basis choice).
 #pragma once
 #include <array>
+#include <limits>
 #include <cmath>
 #include <stdexcept>
 #include <string>
@@ -19,6 +20,13 @@
 #include "../subrosadg_gb300/csrc/triangle_rules.h"
 
 namespace orc {
+
+#ifndef ORC_REAL
+#define ORC_REAL double
+#endif
+// Arithmetic type of the oracle: double (the reference's Real, src/Utils/BasicDataType.cpp:35-39) or
+// long double for an extended-precision truth (build flag -DORC_REAL="long double").
+using Real = ORC_REAL;
 
 enum ElemType { kTri = 2, kQuad = 3, kHex = 5 };
 
@@ -36,38 +44,38 @@ inline const int* faceVertexTable(int t) {
 }
 
 // Reference-element vertex coordinates (gmsh conventions).
-inline std::array<double, 3> refVertex(int t, int v) {
-  static const double tri[3][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}};
-  static const double quad[4][3] = {{-1, -1, 0}, {1, -1, 0}, {1, 1, 0}, {-1, 1, 0}};
-  static const double hex[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+inline std::array<Real, 3> refVertex(int t, int v) {
+  static const Real tri[3][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}};
+  static const Real quad[4][3] = {{-1, -1, 0}, {1, -1, 0}, {1, 1, 0}, {-1, 1, 0}};
+  static const Real hex[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
                                    {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
-  const double* p = t == kTri ? tri[v] : (t == kQuad ? quad[v] : hex[v]);
+  const Real* p = t == kTri ? tri[v] : (t == kQuad ? quad[v] : hex[v]);
   return {p[0], p[1], p[2]};
 }
 
 // Legendre P_n and P'_n by the three-term recurrence.
-inline void legendre(int n, double x, double& p, double& dp) {
-  double p0 = 1.0, p1 = x, d0 = 0.0, d1 = 1.0;
+inline void legendre(int n, Real x, Real& p, Real& dp) {
+  Real p0 = 1.0, p1 = x, d0 = 0.0, d1 = 1.0;
   if (n == 0) { p = 1.0; dp = 0.0; return; }
   for (int k = 2; k <= n; ++k) {
-    const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
-    const double d2 = d0 + (2.0 * k - 1.0) * p1;
+    const Real p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+    const Real d2 = d0 + (2.0 * k - 1.0) * p1;
     p0 = p1; p1 = p2; d0 = d1; d1 = d2;
   }
   p = p1; dp = d1;
 }
 
 // n-point Gauss-Legendre rule on [-1,1], points ascending (Newton on P_n).
-inline void gaussLegendre(int n, std::vector<double>& x, std::vector<double>& w) {
+inline void gaussLegendre(int n, std::vector<Real>& x, std::vector<Real>& w) {
   x.assign(n, 0.0); w.assign(n, 0.0);
   for (int i = 0; i < n; ++i) {
-    double z = -std::cos(M_PI * (i + 0.75) / (n + 0.5));
+    Real z = -std::cos(Real(M_PI) * (i + Real(0.75)) / (n + Real(0.5)));
     for (int it = 0; it < 100; ++it) {
-      double p, dp; legendre(n, z, p, dp);
-      const double dz = p / dp; z -= dz;
-      if (std::fabs(dz) < 1e-16) break;
+      Real p, dp; legendre(n, z, p, dp);
+      const Real dz = p / dp; z -= dz;
+      if (std::fabs(dz) <= 4 * std::numeric_limits<Real>::epsilon()) break;
     }
-    double p, dp; legendre(n, z, p, dp);
+    Real p, dp; legendre(n, z, p, dp);
     x[i] = z; w[i] = 2.0 / ((1.0 - z * z) * dp * dp);
   }
 }
@@ -78,8 +86,8 @@ inline int linePoints(int order) { return order / 2 + 1; }
 
 struct Quadrature {
   int dim = 0, n = 0;
-  std::vector<double> x;  // n * 3 reference coordinates
-  std::vector<double> w;  // n
+  std::vector<Real> x;  // n * 3 reference coordinates
+  std::vector<Real> w;  // n
 };
 
 // Element quadrature of the given order for each element type.
@@ -97,15 +105,15 @@ inline Quadrature elementQuadrature(int t, int order) {
   }
   if (t == kQuad && order == 2) {
     // 7-point degree-5 rule (kQuadrangleQuadratureNumber[2] = 7): Radon's symmetric formula.
-    const double a = std::sqrt(14.0 / 15.0), b = std::sqrt(3.0 / 5.0), c = std::sqrt(1.0 / 3.0);
-    const double pts[7][2] = {{0, 0}, {0, a}, {0, -a}, {b, c}, {-b, c}, {b, -c}, {-b, -c}};
-    const double wts[7] = {8.0 / 7.0, 20.0 / 63.0, 20.0 / 63.0, 5.0 / 9.0, 5.0 / 9.0, 5.0 / 9.0, 5.0 / 9.0};
+    const Real a = std::sqrt(14.0 / 15.0), b = std::sqrt(3.0 / 5.0), c = std::sqrt(1.0 / 3.0);
+    const Real pts[7][2] = {{0, 0}, {0, a}, {0, -a}, {b, c}, {-b, c}, {b, -c}, {-b, -c}};
+    const Real wts[7] = {8.0 / 7.0, 20.0 / 63.0, 20.0 / 63.0, 5.0 / 9.0, 5.0 / 9.0, 5.0 / 9.0, 5.0 / 9.0};
     q.n = 7;
     for (int i = 0; i < 7; ++i) { q.x.insert(q.x.end(), {pts[i][0], pts[i][1], 0.0}); q.w.push_back(wts[i]); }
     return q;
   }
   const int m = linePoints(order);
-  std::vector<double> gx, gw; gaussLegendre(m, gx, gw);
+  std::vector<Real> gx, gw; gaussLegendre(m, gx, gw);
   if (t == kQuad) {  // index = i*m + j with (xi=x_i, eta=x_j)
     q.n = m * m;
     for (int i = 0; i < m; ++i)
@@ -127,7 +135,7 @@ inline Quadrature elementQuadrature(int t, int order) {
 inline Quadrature faceQuadrature(int t, int order) {
   Quadrature q; q.dim = elemDim(t) - 1;
   const int m = linePoints(order);
-  std::vector<double> gx, gw; gaussLegendre(m, gx, gw);
+  std::vector<Real> gx, gw; gaussLegendre(m, gx, gw);
   if (t != kHex) {
     q.n = m;
     for (int i = 0; i < m; ++i) { q.x.insert(q.x.end(), {gx[i], 0.0, 0.0}); q.w.push_back(gw[i]); }
@@ -140,35 +148,35 @@ inline Quadrature faceQuadrature(int t, int order) {
 }
 
 // P1 shape functions of the face reference element (BasisFunction.cpp:76-111 uses gmsh Lagrange1).
-inline void faceShape(int t, const double* fx, double* n) {
+inline void faceShape(int t, const Real* fx, Real* n) {
   if (t != kHex) { n[0] = 0.5 * (1.0 - fx[0]); n[1] = 0.5 * (1.0 + fx[0]); return; }
-  const double x = fx[0], y = fx[1];
+  const Real x = fx[0], y = fx[1];
   n[0] = 0.25 * (1 - x) * (1 - y); n[1] = 0.25 * (1 + x) * (1 - y);
   n[2] = 0.25 * (1 + x) * (1 + y); n[3] = 0.25 * (1 - x) * (1 + y);
 }
-inline void faceShapeGrad(int t, const double* fx, double* dxi, double* deta) {
+inline void faceShapeGrad(int t, const Real* fx, Real* dxi, Real* deta) {
   if (t != kHex) { dxi[0] = -0.5; dxi[1] = 0.5; return; }
-  const double x = fx[0], y = fx[1];
+  const Real x = fx[0], y = fx[1];
   dxi[0] = -0.25 * (1 - y); dxi[1] = 0.25 * (1 - y); dxi[2] = 0.25 * (1 + y); dxi[3] = -0.25 * (1 + y);
   deta[0] = -0.25 * (1 - x); deta[1] = -0.25 * (1 + x); deta[2] = 0.25 * (1 + x); deta[3] = 0.25 * (1 - x);
 }
 
 // P1 element shape functions and reference gradients (geometry map of straight-sided elements).
-inline void elemShape(int t, const double* X, double* n, double* g /* nv*3 */) {
+inline void elemShape(int t, const Real* X, Real* n, Real* g /* nv*3 */) {
   if (t == kTri) {
     n[0] = 1 - X[0] - X[1]; n[1] = X[0]; n[2] = X[1];
-    const double gg[9] = {-1, -1, 0, 1, 0, 0, 0, 1, 0};
+    const Real gg[9] = {-1, -1, 0, 1, 0, 0, 0, 1, 0};
     for (int i = 0; i < 9; ++i) g[i] = gg[i];
     return;
   }
   const int nv = elemVerts(t);
   for (int v = 0; v < nv; ++v) {
     const auto r = refVertex(t, v);
-    const double a = 1 + r[0] * X[0], b = 1 + r[1] * X[1];
+    const Real a = 1 + r[0] * X[0], b = 1 + r[1] * X[1];
     if (t == kQuad) {
       n[v] = 0.25 * a * b; g[v * 3 + 0] = 0.25 * r[0] * b; g[v * 3 + 1] = 0.25 * a * r[1]; g[v * 3 + 2] = 0;
     } else {
-      const double c = 1 + r[2] * X[2];
+      const Real c = 1 + r[2] * X[2];
       n[v] = 0.125 * a * b * c;
       g[v * 3 + 0] = 0.125 * r[0] * b * c; g[v * 3 + 1] = 0.125 * a * r[1] * c; g[v * 3 + 2] = 0.125 * a * b * r[2];
     }
@@ -176,24 +184,24 @@ inline void elemShape(int t, const double* X, double* n, double* g /* nv*3 */) {
 }
 
 // 1D Lobatto shape functions (Solin): l0=(1-x)/2, l1=(1+x)/2, lk=(P_k-P_{k-2})/sqrt(2(2k-1)).
-inline void lobatto(int k, double x, double& v, double& d) {
+inline void lobatto(int k, Real x, Real& v, Real& d) {
   if (k == 0) { v = 0.5 * (1 - x); d = -0.5; return; }
   if (k == 1) { v = 0.5 * (1 + x); d = 0.5; return; }
-  double pk, dpk, pk2, dpk2, pk1, dpk1;
+  Real pk, dpk, pk2, dpk2, pk1, dpk1;
   legendre(k, x, pk, dpk); legendre(k - 2, x, pk2, dpk2); legendre(k - 1, x, pk1, dpk1);
-  const double s = std::sqrt(2.0 * (2.0 * k - 1.0));
+  const Real s = std::sqrt(2.0 * (2.0 * k - 1.0));
   v = (pk - pk2) / s;
   d = std::sqrt((2.0 * k - 1.0) / 2.0) * pk1;
 }
 
 // Tiny forward-mode dual number in two variables (for triangle basis gradients).
-struct Dual { double v, dx, dy; };
+struct Dual { Real v, dx, dy; };
 inline Dual operator+(Dual a, Dual b) { return {a.v + b.v, a.dx + b.dx, a.dy + b.dy}; }
 inline Dual operator-(Dual a, Dual b) { return {a.v - b.v, a.dx - b.dx, a.dy - b.dy}; }
 inline Dual operator*(Dual a, Dual b) { return {a.v * b.v, a.dx * b.v + a.v * b.dx, a.dy * b.v + a.v * b.dy}; }
-inline Dual scale(Dual a, double s) { return {a.v * s, a.dx * s, a.dy * s}; }
+inline Dual scale(Dual a, Real s) { return {a.v * s, a.dx * s, a.dy * s}; }
 inline Dual legendreD(int n, Dual x) {  // P_n(x) as a dual
-  double p, dp; legendre(n, x.v, p, dp);
+  Real p, dp; legendre(n, x.v, p, dp);
   return {p, dp * x.dx, dp * x.dy};
 }
 // Solin kernel function phi_{k-2}(x) = 4 l_k(x)/(1-x^2) = -4 sqrt((2k-1)/2)/((k-1)k) P'_{k-1}(x).
@@ -201,12 +209,12 @@ inline Dual kernelD(int k, Dual x) {
   // P'_{k-1}(x) and its derivative P''_{k-1}(x) via (1-x^2)P'' = 2xP' - n(n+1)P is singular at
   // |x|=1; use the sum form P'_{n} = sum_{j=n-1,n-3,..} (2j+1) P_j instead.
   const int n = k - 1;
-  double dpn = 0.0, ddpn = 0.0;
+  Real dpn = 0.0, ddpn = 0.0;
   for (int j = n - 1; j >= 0; j -= 2) {
-    double pj, dpj; legendre(j, x.v, pj, dpj);
+    Real pj, dpj; legendre(j, x.v, pj, dpj);
     dpn += (2.0 * j + 1.0) * pj; ddpn += (2.0 * j + 1.0) * dpj;
   }
-  const double c = -4.0 * std::sqrt((2.0 * k - 1.0) / 2.0) / ((k - 1.0) * k);
+  const Real c = -4.0 * std::sqrt((2.0 * k - 1.0) / 2.0) / ((k - 1.0) * k);
   return {c * dpn, c * ddpn * x.dx, c * ddpn * x.dy};
 }
 
@@ -220,10 +228,10 @@ inline int basisCount(int t, int p) {
 //   quad: index a*(P+1)+b -> l_a(xi) l_b(eta); hex: index (a*(P+1)+b)*(P+1)+c.
 //   tri : vertices lambda_i; edges (0,1),(1,2),(2,0) with l_a l_b phi_{k-2}(l_b-l_a), k=2..P;
 //         bubbles l0 l1 l2 P_i(l2-l1) P_j(l1-l0), i+j<=P-3.
-inline void modalBasis(int t, int p, const double* X, double* val, double* grad) {
+inline void modalBasis(int t, int p, const Real* X, Real* val, Real* grad) {
   if (t == kQuad || t == kHex) {
     const int m = p + 1;
-    double lv[3][6], ld[3][6];
+    Real lv[3][6], ld[3][6];
     for (int dd = 0; dd < elemDim(t); ++dd)
       for (int k = 0; k < m; ++k) lobatto(k, X[dd], lv[dd][k], ld[dd][k]);
     int idx = 0;
@@ -285,20 +293,20 @@ inline std::vector<int> facePermutation(int t, int m, int rotation) {
 }
 
 // Dense square inverse by Gauss-Jordan with partial pivoting (Eigen's inverse() in the reference).
-inline void invert(int n, const double* a, double* inv) {
-  std::vector<double> m(a, a + n * n);
+inline void invert(int n, const Real* a, Real* inv) {
+  std::vector<Real> m(a, a + n * n);
   for (int i = 0; i < n * n; ++i) inv[i] = 0.0;
   for (int i = 0; i < n; ++i) inv[i * n + i] = 1.0;
   for (int c = 0; c < n; ++c) {
-    int piv = c; double best = std::fabs(m[c * n + c]);
+    int piv = c; Real best = std::fabs(m[c * n + c]);
     for (int r = c + 1; r < n; ++r) if (std::fabs(m[r * n + c]) > best) { best = std::fabs(m[r * n + c]); piv = r; }
     if (best == 0.0) throw std::runtime_error("singular matrix");
     if (piv != c) for (int k = 0; k < n; ++k) { std::swap(m[c * n + k], m[piv * n + k]); std::swap(inv[c * n + k], inv[piv * n + k]); }
-    const double d = 1.0 / m[c * n + c];
+    const Real d = 1.0 / m[c * n + c];
     for (int k = 0; k < n; ++k) { m[c * n + k] *= d; inv[c * n + k] *= d; }
     for (int r = 0; r < n; ++r) {
       if (r == c) continue;
-      const double f = m[r * n + c];
+      const Real f = m[r * n + c];
       if (f == 0.0) continue;
       for (int k = 0; k < n; ++k) { m[r * n + k] -= f * m[c * n + k]; inv[r * n + k] -= f * inv[c * n + k]; }
     }
@@ -309,11 +317,11 @@ inline void invert(int n, const double* a, double* inv) {
 struct RefElement {
   int type = 0, dim = 0, p = 0, nb = 0, nq = 0, nface = 0, nfq = 0;
   Quadrature vq, fq;
-  std::vector<double> phi;    // [nq][nb]        modal_value_
-  std::vector<double> dphi;   // [nq*dim][nb]    modal_gradient_value_ (row q*dim+k)
-  std::vector<double> phif;   // [nface*nfq][nb] modal_adjacency_value_
-  std::vector<double> lsqInv; // [nb][nb]        modal_least_squares_inverse_
-  std::vector<double> ptp;    // [nb][nb]        Phi^T Phi
+  std::vector<Real> phi;    // [nq][nb]        modal_value_
+  std::vector<Real> dphi;   // [nq*dim][nb]    modal_gradient_value_ (row q*dim+k)
+  std::vector<Real> phif;   // [nface*nfq][nb] modal_adjacency_value_
+  std::vector<Real> lsqInv; // [nb][nb]        modal_least_squares_inverse_
+  std::vector<Real> ptp;    // [nb][nb]        Phi^T Phi
   std::vector<std::vector<int>> perm;  // rotation -> face point permutation
 
   void build(int t, int order) {
@@ -322,7 +330,7 @@ struct RefElement {
     fq = faceQuadrature(t, 2 * order + 1);
     nq = vq.n; nfq = fq.n;
     phi.assign(size_t(nq) * nb, 0); dphi.assign(size_t(nq) * dim * nb, 0);
-    std::vector<double> v(nb), g(nb * 3);
+    std::vector<Real> v(nb), g(nb * 3);
     for (int q = 0; q < nq; ++q) {
       modalBasis(t, order, &vq.x[q * 3], v.data(), g.data());
       for (int b = 0; b < nb; ++b) {
@@ -335,8 +343,8 @@ struct RefElement {
     const int nfv = faceVerts(t);
     for (int f = 0; f < nface; ++f)
       for (int j = 0; j < nfq; ++j) {
-        double sh[4]; faceShape(t, &fq.x[j * 3], sh);
-        double X[3] = {0, 0, 0};
+        Real sh[4]; faceShape(t, &fq.x[j * 3], sh);
+        Real X[3] = {0, 0, 0};
         for (int k = 0; k < nfv; ++k) {
           const auto r = refVertex(t, fv[f * nfv + k]);
           for (int d = 0; d < 3; ++d) X[d] += sh[k] * r[d];
@@ -347,7 +355,7 @@ struct RefElement {
     ptp.assign(size_t(nb) * nb, 0.0);
     for (int a = 0; a < nb; ++a)
       for (int b = 0; b < nb; ++b) {
-        double s = 0; for (int q = 0; q < nq; ++q) s += phi[size_t(q) * nb + a] * phi[size_t(q) * nb + b];
+        Real s = 0; for (int q = 0; q < nq; ++q) s += phi[size_t(q) * nb + a] * phi[size_t(q) * nb + b];
         ptp[size_t(a) * nb + b] = s;
       }
     lsqInv.assign(size_t(nb) * nb, 0.0);

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <memory>
 #include <string>
@@ -38,26 +39,26 @@ struct Block {
   RefElement ref;
   int64_t ne = 0;
   std::vector<int> verts;       // ne * nvert
-  std::vector<double> qcoord;   // ne * nq * 3
-  std::vector<double> jw;       // ne * nq        |J| w
-  std::vector<double> jtiw;     // ne * nq * d*d  J^-T |J| w, column-major d x d per point
-  std::vector<double> minv;     // ne * nb*nb     local mass matrix inverse
-  std::vector<double> mass;     // ne * nb*nb     local mass matrix (kept when refining solves)
-  std::vector<double> minEdge;  // ne
+  std::vector<Real> qcoord;   // ne * nq * 3
+  std::vector<Real> jw;       // ne * nq        |J| w
+  std::vector<Real> jtiw;     // ne * nq * d*d  J^-T |J| w, column-major d x d per point
+  std::vector<Real> minv;     // ne * nb*nb     local mass matrix inverse
+  std::vector<Real> mass;     // ne * nb*nb     local mass matrix (kept when refining solves)
+  std::vector<Real> minEdge;  // ne
   // state (column-major nv x nb per element: index b*nv + v)
-  std::vector<double> coef, last, res;
-  std::vector<double> qvol;     // ne * nv x (nq*d)
-  std::vector<double> qface;    // ne * nv x (nface*nfq)
+  std::vector<Real> coef, last, res;
+  std::vector<Real> qvol;     // ne * nv x (nq*d)
+  std::vector<Real> qface;    // ne * nv x (nface*nfq)
   // gradient blocks, rows (v*d + k)
-  std::vector<double> qvg, qfvg, qfig, rvg, rig, vgc, igc, gc;
+  std::vector<Real> qvg, qfvg, qfig, rvg, rig, vgc, igc, gc;
 };
 
 struct Face {
   int bl = 0, el = 0, fl = 0, br = -1, er = -1, fr = -1, rot = 0;
   int physical = 0, bc = -1;
-  std::vector<double> normal;  // nfq * 3
-  std::vector<double> fjw;     // nfq
-  std::vector<double> coord;   // nfq * 3
+  std::vector<Real> normal;  // nfq * 3
+  std::vector<Real> fjw;     // nfq
+  std::vector<Real> coord;   // nfq * 3
 };
 
 struct Problem {
@@ -73,7 +74,7 @@ struct Problem {
   std::vector<Block> blocks;
   std::vector<Face> interior, boundary;
   std::vector<PointVar> dummy;  // boundary dummy variables, [boundary][nfq]
-  std::vector<double> relErr;
+  std::vector<Real> relErr;
   int64_t totalElements = 0;
   bool hasState = false;
   std::string err;
@@ -98,10 +99,10 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
   for (int64_t e = 0; e < B.ne; ++e) {
     const int* vv = &B.verts[size_t(e) * nvert];
     for (int q = 0; q < nq; ++q) {
-      double sh[8], g[24];
+      Real sh[8], g[24];
       elemShape(B.type, &R.vq.x[q * 3], sh, g);
-      double J[3][3] = {{0}};  // J[l][k] = d x_l / d xi_k
-      double x[3] = {0, 0, 0};
+      Real J[3][3] = {{0}};  // J[l][k] = d x_l / d xi_k
+      Real x[3] = {0, 0, 0};
       for (int v = 0; v < nvert; ++v) {
         const double* c = &nodes[size_t(vv[v]) * 3];
         for (int l = 0; l < 3; ++l) x[l] += sh[v] * c[l];
@@ -109,7 +110,7 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
           for (int k = 0; k < d; ++k) J[l][k] += g[v * 3 + k] * c[l];
       }
       for (int l = 0; l < 3; ++l) B.qcoord[(size_t(e) * nq + q) * 3 + l] = x[l];
-      double det, inv[3][3];
+      Real det, inv[3][3];
       if (d == 2) {
         det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
         inv[0][0] = J[1][1] / det; inv[0][1] = -J[0][1] / det; inv[1][0] = -J[1][0] / det; inv[1][1] = J[0][0] / det;
@@ -130,17 +131,17 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
 #pragma omp critical
         failure = "inverted or degenerate element";
       }
-      const double jw = det * R.vq.w[q];
+      const Real jw = det * R.vq.w[q];
       B.jw[size_t(e) * nq + q] = jw;
       // M(a,b) = (J^-T)(a,b) |J| w = (J^-1)(b,a) |J| w, stored column-major at [a + b*d].
       for (int a = 0; a < d; ++a)
         for (int b = 0; b < d; ++b) B.jtiw[(size_t(e) * nq + q) * d * d + a + b * d] = inv[b][a] * jw;
     }
     // Local mass matrix inverse (Geometry.cpp:88-100).
-    std::vector<double> m(size_t(nb) * nb, 0.0);
+    std::vector<Real> m(size_t(nb) * nb, 0.0);
     for (int a = 0; a < nb; ++a)
       for (int b = 0; b < nb; ++b) {
-        double s = 0;
+        Real s = 0;
         for (int q = 0; q < nq; ++q) s += R.phi[size_t(q) * nb + a] * R.phi[size_t(q) * nb + b] * B.jw[size_t(e) * nq + q];
         m[size_t(a) * nb + b] = s;
       }
@@ -153,11 +154,11 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
                                     {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
     const int(*E)[2] = B.type == kTri ? triE : (B.type == kQuad ? quadE : hexE);
     const int nE = B.type == kTri ? 3 : (B.type == kQuad ? 4 : 12);
-    double me = 1e300;
+    Real me = 1e300;
     for (int i = 0; i < nE; ++i) {
       const double* a = &nodes[size_t(vv[E[i][0]]) * 3];
       const double* b = &nodes[size_t(vv[E[i][1]]) * 3];
-      const double l = std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
+      const Real l = std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
       me = std::min(me, l);
     }
     B.minEdge[e] = me;
@@ -173,21 +174,21 @@ static void faceGeometry(Problem& P, Face& F, const double* nodes) {
   const int* vv = &B.verts[size_t(F.el) * elemVerts(B.type)];
   F.normal.assign(size_t(nfq) * 3, 0.0); F.fjw.assign(nfq, 0.0); F.coord.assign(size_t(nfq) * 3, 0.0);
   for (int j = 0; j < nfq; ++j) {
-    double sh[4], dxi[4], deta[4];
+    Real sh[4], dxi[4], deta[4];
     faceShape(B.type, &R.fq.x[j * 3], sh);
     faceShapeGrad(B.type, &R.fq.x[j * 3], dxi, deta);
-    double x[3] = {0, 0, 0}, tx[3] = {0, 0, 0}, ty[3] = {0, 0, 0};
+    Real x[3] = {0, 0, 0}, tx[3] = {0, 0, 0}, ty[3] = {0, 0, 0};
     for (int k = 0; k < nfv; ++k) {
       const double* c = &nodes[size_t(vv[ft[F.fl * nfv + k]]) * 3];
       for (int l = 0; l < 3; ++l) { x[l] += sh[k] * c[l]; tx[l] += dxi[k] * c[l]; if (nfv == 4) ty[l] += deta[k] * c[l]; }
     }
     for (int l = 0; l < 3; ++l) F.coord[j * 3 + l] = x[l];
-    double n[3], det;
+    Real n[3], det;
     if (P.dim == 2) {  // Geometry.cpp:115-127
       det = std::sqrt(tx[0] * tx[0] + tx[1] * tx[1]);
       n[0] = tx[1] / det; n[1] = -tx[0] / det; n[2] = 0;
     } else {           // Geometry.cpp:130-147
-      const double cx = tx[1] * ty[2] - tx[2] * ty[1], cy = tx[2] * ty[0] - tx[0] * ty[2], cz = tx[0] * ty[1] - tx[1] * ty[0];
+      const Real cx = tx[1] * ty[2] - tx[2] * ty[1], cy = tx[2] * ty[0] - tx[0] * ty[2], cz = tx[0] * ty[1] - tx[1] * ty[0];
       det = std::sqrt(cx * cx + cy * cy + cz * cz);
       n[0] = cx / det; n[1] = cy / det; n[2] = cz / det;
     }
@@ -251,10 +252,10 @@ static void buildAdjacency(Problem& P, const sdg_mesh& m) {
 // ---- point evaluation helpers ---------------------------------------------------------------------
 
 // vals[q][v] = sum_b coef(v,b) phi[q][b] for rows q of a phi table.
-static inline void interp(int nv, int nb, int nrow, const double* coef, const double* phi, double* vals) {
+static inline void interp(int nv, int nb, int nrow, const Real* coef, const Real* phi, Real* vals) {
   for (int q = 0; q < nrow; ++q)
     for (int v = 0; v < nv; ++v) {
-      double s = 0;
+      Real s = 0;
       for (int b = 0; b < nb; ++b) s += coef[b * nv + v] * phi[size_t(q) * nb + b];
       vals[q * nv + v] = s;
     }
@@ -264,7 +265,7 @@ static inline void interp(int nv, int nb, int nrow, const double* coef, const do
 static void trace(const Problem& P, int b, int e, int f, PointVar* out) {
   const Block& B = P.blocks[b];
   const int nv = P.nv, nb = B.ref.nb, nfq = B.ref.nfq;
-  double vals[64 * kMaxVar];
+  Real vals[64 * kMaxVar];
   interp(nv, nb, nfq, &B.coef[size_t(e) * nv * nb], &B.ref.phif[size_t(f) * nfq * nb], vals);
   for (int j = 0; j < nfq; ++j) {
     for (int v = 0; v < nv; ++v) out[j].cons[v] = vals[j * nv + v];
@@ -273,15 +274,15 @@ static void trace(const Problem& P, int b, int e, int f, PointVar* out) {
 }
 
 // Gradient trace on face f: BR1 -> gc; BR2 -> vgc + igc[f]; conserved gradient rows (v*d+k).
-static void gradientTrace(const Problem& P, int b, int e, int f, double* out /* nfq * nv*d */) {
+static void gradientTrace(const Problem& P, int b, int e, int f, Real* out /* nfq * nv*d */) {
   const Block& B = P.blocks[b];
   const int nr = P.nv * P.dim, nb = B.ref.nb, nfq = B.ref.nfq;
-  std::vector<double> c(size_t(nr) * nb);
+  std::vector<Real> c(size_t(nr) * nb);
   if (P.visc == 1) {
     std::copy_n(&B.gc[size_t(e) * nr * nb], nr * nb, c.data());
   } else {
-    const double* a = &B.vgc[size_t(e) * nr * nb];
-    const double* g = &B.igc[(size_t(e) * B.ref.nface + f) * nr * nb];
+    const Real* a = &B.vgc[size_t(e) * nr * nb];
+    const Real* g = &B.igc[(size_t(e) * B.ref.nface + f) * nr * nb];
     for (int i = 0; i < nr * nb; ++i) c[i] = a[i] + g[i];
   }
   interp(nr, nb, nfq, c.data(), &B.ref.phif[size_t(f) * nfq * nb], out);
@@ -289,26 +290,26 @@ static void gradientTrace(const Problem& P, int b, int e, int f, double* out /* 
 
 // x = R M^-1 for an (nr x nb, column-major) block R (TimeIntegration.cpp:196,205-225), optionally refined:
 // x += (R - x M) M^-1.
-static void applyMinv(const Problem& P, const Block& B, int64_t e, int nr, const double* R, double* x) {
+static void applyMinv(const Problem& P, const Block& B, int64_t e, int nr, const Real* R, Real* x) {
   const int nb = B.ref.nb;
-  const double* Mi = &B.minv[size_t(e) * nb * nb];
+  const Real* Mi = &B.minv[size_t(e) * nb * nb];
   for (int bb = 0; bb < nb; ++bb)
     for (int r = 0; r < nr; ++r) {
-      double s = 0; for (int c = 0; c < nb; ++c) s += R[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
+      Real s = 0; for (int c = 0; c < nb; ++c) s += R[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
       x[size_t(bb) * nr + r] = s;
     }
   if (!P.refine) return;
-  const double* M = &B.mass[size_t(e) * nb * nb];
-  std::vector<double> res(size_t(nr) * nb);
+  const Real* M = &B.mass[size_t(e) * nb * nb];
+  std::vector<Real> res(size_t(nr) * nb);
   for (int bb = 0; bb < nb; ++bb)
     for (int r = 0; r < nr; ++r) {
-      double s = R[size_t(bb) * nr + r];
+      Real s = R[size_t(bb) * nr + r];
       for (int c = 0; c < nb; ++c) s -= x[size_t(c) * nr + r] * M[size_t(c) * nb + bb];
       res[size_t(bb) * nr + r] = s;
     }
   for (int bb = 0; bb < nb; ++bb)
     for (int r = 0; r < nr; ++r) {
-      double s = 0; for (int c = 0; c < nb; ++c) s += res[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
+      Real s = 0; for (int c = 0; c < nb; ++c) s += res[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
       x[size_t(bb) * nr + r] += s;
     }
 }
@@ -322,11 +323,11 @@ static void gradientQuadratureAndResidual(Problem& P) {
     const int nq = B.ref.nq, nb = B.ref.nb;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
-      double vals[216 * kMaxVar];
+      Real vals[216 * kMaxVar];
       interp(nv, nb, nq, &B.coef[size_t(e) * nv * nb], B.ref.phi.data(), vals);
-      double* Q = &B.qvg[size_t(e) * nr * nq * d];
+      Real* Q = &B.qvg[size_t(e) * nr * nq * d];
       for (int q = 0; q < nq; ++q) {
-        const double* M = &B.jtiw[(size_t(e) * nq + q) * d * d];
+        const Real* M = &B.jtiw[(size_t(e) * nq + q) * d * d];
         for (int v = 0; v < nv; ++v)
           for (int a = 0; a < d; ++a)
             for (int bb = 0; bb < d; ++bb) Q[size_t(q * d + bb) * nr + v * d + a] = vals[q * nv + v] * M[a + bb * d];
@@ -343,23 +344,23 @@ static void gradientQuadratureAndResidual(Problem& P) {
     Block& BL = P.blocks[F.bl]; Block& BR = P.blocks[F.br];
     const std::vector<int>& perm = BR.ref.perm[F.rot];
     const int nfl = BL.ref.nface * nfq, nfr = BR.ref.nface * nfq;
-    double* QL = &BL.qfvg[size_t(F.el) * nr * nfl];
-    double* QR = &BR.qfvg[size_t(F.er) * nr * nfr];
+    Real* QL = &BL.qfvg[size_t(F.el) * nr * nfl];
+    Real* QR = &BR.qfvg[size_t(F.er) * nr * nfr];
     for (int j = 0; j < nfq; ++j) {
       const int jr = perm[j];
-      const double* n = &F.normal[j * 3];
+      const Real* n = &F.normal[j * 3];
       for (int v = 0; v < nv; ++v)
         for (int k = 0; k < d; ++k) {
-          const double t = n[k] * (L[j].cons[v] + R[jr].cons[v]) / 2.0 * F.fjw[j];
+          const Real t = n[k] * (L[j].cons[v] + R[jr].cons[v]) / 2.0 * F.fjw[j];
           QL[size_t(F.fl * nfq + j) * nr + v * d + k] = t;
           QR[size_t(F.fr * nfq + jr) * nr + v * d + k] = -t;
         }
       if (P.ns()) {
-        double* IL = &BL.qfig[size_t(F.el) * nr * nfl];
-        double* IR = &BR.qfig[size_t(F.er) * nr * nfr];
+        Real* IL = &BL.qfig[size_t(F.el) * nr * nfl];
+        Real* IR = &BR.qfig[size_t(F.er) * nr * nfr];
         for (int v = 0; v < nv; ++v)
           for (int k = 0; k < d; ++k) {
-            const double t = n[k] * (R[jr].cons[v] - L[j].cons[v]) / 2.0 * F.fjw[j];
+            const Real t = n[k] * (R[jr].cons[v] - L[j].cons[v]) / 2.0 * F.fjw[j];
             IL[size_t(F.fl * nfq + j) * nr + v * d + k] = t;
             IR[size_t(F.fr * nfq + jr) * nr + v * d + k] = t;
           }
@@ -375,9 +376,9 @@ static void gradientQuadratureAndResidual(Problem& P) {
     Block& BL = P.blocks[F.bl];
     const int nfl = BL.ref.nface * nfq;
     for (int j = 0; j < nfq; ++j) {
-      double vol[kMaxVar], itf[kMaxVar];
+      Real vol[kMaxVar], itf[kMaxVar];
       boundaryGradientState(P.ph, F.bc, &F.normal[j * 3], L[j], P.dummy[size_t(i) * nfq + j], vol, itf);
-      const double* n = &F.normal[j * 3];
+      const Real* n = &F.normal[j * 3];
       for (int v = 0; v < nv; ++v)
         for (int k = 0; k < d; ++k) {
           BL.qfvg[size_t(F.el) * nr * nfl + size_t(F.fl * nfq + j) * nr + v * d + k] = n[k] * vol[v] * F.fjw[j];
@@ -390,33 +391,33 @@ static void gradientQuadratureAndResidual(Problem& P) {
     const int nq = B.ref.nq, nb = B.ref.nb, nf = B.ref.nface, nfl = nf * nfq;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
-      const double* QF = &B.qfvg[size_t(e) * nr * nfl];
-      const double* QV = &B.qvg[size_t(e) * nr * nq * d];
-      double* RV = &B.rvg[size_t(e) * nr * nb];
+      const Real* QF = &B.qfvg[size_t(e) * nr * nfl];
+      const Real* QV = &B.qvg[size_t(e) * nr * nq * d];
+      Real* RV = &B.rvg[size_t(e) * nr * nb];
       for (int bb = 0; bb < nb; ++bb)
         for (int r = 0; r < nr; ++r) {
-          double s = 0;
+          Real s = 0;
           for (int c = 0; c < nfl; ++c) s += QF[size_t(c) * nr + r] * B.ref.phif[size_t(c) * nb + bb];
           for (int c = 0; c < nq * d; ++c) s -= QV[size_t(c) * nr + r] * B.ref.dphi[size_t(c) * nb + bb];
           RV[size_t(bb) * nr + r] = s;
         }
-      double* VG = &B.vgc[size_t(e) * nr * nb];
+      Real* VG = &B.vgc[size_t(e) * nr * nb];
       applyMinv(P, B, e, nr, RV, VG);
       if (!P.ns()) continue;
-      double* G = &B.gc[size_t(e) * nr * nb];
+      Real* G = &B.gc[size_t(e) * nr * nb];
       std::copy_n(VG, nr * nb, G);
-      const double* QI = &B.qfig[size_t(e) * nr * nfl];
+      const Real* QI = &B.qfig[size_t(e) * nr * nfl];
       const int nblk = P.visc == 1 ? 1 : nf;
       for (int blk = 0; blk < nblk; ++blk) {
         const int c0 = P.visc == 1 ? 0 : blk * nfq, c1 = P.visc == 1 ? nfl : (blk + 1) * nfq;
-        double* RI = &B.rig[(size_t(e) * nblk + blk) * nr * nb];
+        Real* RI = &B.rig[(size_t(e) * nblk + blk) * nr * nb];
         for (int bb = 0; bb < nb; ++bb)
           for (int r = 0; r < nr; ++r) {
-            double s = 0;
+            Real s = 0;
             for (int c = c0; c < c1; ++c) s += QI[size_t(c) * nr + r] * B.ref.phif[size_t(c) * nb + bb];
             RI[size_t(bb) * nr + r] = s;
           }
-        double* IG = &B.igc[(size_t(e) * nblk + blk) * nr * nb];
+        Real* IG = &B.igc[(size_t(e) * nblk + blk) * nr * nb];
         applyMinv(P, B, e, nr, RI, IG);
         for (int i = 0; i < nr * nb; ++i) G[i] += IG[i];
       }
@@ -431,27 +432,27 @@ static void quadratureAndResidual(Problem& P) {
     const int nq = B.ref.nq, nb = B.ref.nb;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
-      double vals[216 * kMaxVar];
-      std::vector<double> gvals;
+      Real vals[216 * kMaxVar];
+      std::vector<Real> gvals;
       interp(nv, nb, nq, &B.coef[size_t(e) * nv * nb], B.ref.phi.data(), vals);
       if (P.ns()) { gvals.resize(size_t(nq) * nr); interp(nr, nb, nq, &B.gc[size_t(e) * nr * nb], B.ref.phi.data(), gvals.data()); }
-      double* Q = &B.qvol[size_t(e) * nv * nq * d];
+      Real* Q = &B.qvol[size_t(e) * nv * nq * d];
       for (int q = 0; q < nq; ++q) {
         PointVar v; for (int i = 0; i < nv; ++i) v.cons[i] = vals[q * nv + i];
         computationalFromConserved(P.ph, v);
-        double F[3][kMaxVar]; rawFlux(P.ph, v, F);
+        Real F[3][kMaxVar]; rawFlux(P.ph, v, F);
         if (P.ns()) {
-          double pg[15]; primitiveGradient(P.ph, v, &gvals[size_t(q) * nr], pg);
+          Real pg[15]; primitiveGradient(P.ph, v, &gvals[size_t(q) * nr], pg);
           for (int k = 0; k < d; ++k) {
-            double nk[3] = {0, 0, 0}; nk[k] = 1.0;
-            double fv[kMaxVar]; viscousNormalFlux(P.ph, nk, v, pg, fv);
+            Real nk[3] = {0, 0, 0}; nk[k] = 1.0;
+            Real fv[kMaxVar]; viscousNormalFlux(P.ph, nk, v, pg, fv);
             for (int i = 0; i < nv; ++i) F[k][i] -= fv[i];
           }
         }
-        const double* M = &B.jtiw[(size_t(e) * nq + q) * d * d];
+        const Real* M = &B.jtiw[(size_t(e) * nq + q) * d * d];
         for (int i = 0; i < nv; ++i)
           for (int bb = 0; bb < d; ++bb) {
-            double s = 0; for (int a = 0; a < d; ++a) s += F[a][i] * M[a + bb * d];
+            Real s = 0; for (int a = 0; a < d; ++a) s += F[a][i] * M[a + bb * d];
             Q[size_t(q * d + bb) * nv + i] = s;
           }
       }
@@ -466,26 +467,26 @@ static void quadratureAndResidual(Problem& P) {
     trace(P, F.bl, F.el, F.fl, L); trace(P, F.br, F.er, F.fr, R);
     Block& BL = P.blocks[F.bl]; Block& BR = P.blocks[F.br];
     const std::vector<int>& perm = BR.ref.perm[F.rot];
-    std::vector<double> gl, gr;
+    std::vector<Real> gl, gr;
     if (P.ns()) {
       gl.resize(size_t(nfq) * nr); gr.resize(size_t(nfq) * nr);
       gradientTrace(P, F.bl, F.el, F.fl, gl.data()); gradientTrace(P, F.br, F.er, F.fr, gr.data());
     }
-    double* QL = &BL.qface[size_t(F.el) * nv * BL.ref.nface * nfq];
-    double* QR = &BR.qface[size_t(F.er) * nv * BR.ref.nface * nfq];
+    Real* QL = &BL.qface[size_t(F.el) * nv * BL.ref.nface * nfq];
+    Real* QR = &BR.qface[size_t(F.er) * nv * BR.ref.nface * nfq];
     for (int j = 0; j < nfq; ++j) {
       const int jr = perm[j];
-      const double* n = &F.normal[j * 3];
-      double h[kMaxVar]; convectiveFlux(P.ph, P.flux, n, L[j], R[jr], h);
+      const Real* n = &F.normal[j * 3];
+      Real h[kMaxVar]; convectiveFlux(P.ph, P.flux, n, L[j], R[jr], h);
       if (P.ns()) {
-        double pl[15], pr[15], fl[kMaxVar], fr[kMaxVar];
+        Real pl[15], pr[15], fl[kMaxVar], fr[kMaxVar];
         primitiveGradient(P.ph, L[j], &gl[size_t(j) * nr], pl);
         primitiveGradient(P.ph, R[jr], &gr[size_t(jr) * nr], pr);
         viscousNormalFlux(P.ph, n, L[j], pl, fl); viscousNormalFlux(P.ph, n, R[jr], pr, fr);
         for (int v = 0; v < nv; ++v) h[v] -= (fl[v] + fr[v]) / 2.0;
       }
       for (int v = 0; v < nv; ++v) {
-        const double t = h[v] * F.fjw[j];
+        const Real t = h[v] * F.fjw[j];
         QL[size_t(F.fl * nfq + j) * nv + v] = t;
         QR[size_t(F.fr * nfq + jr) * nv + v] = -t;
       }
@@ -498,21 +499,21 @@ static void quadratureAndResidual(Problem& P) {
     PointVar L[64];
     trace(P, F.bl, F.el, F.fl, L);
     Block& BL = P.blocks[F.bl];
-    std::vector<double> gl;
+    std::vector<Real> gl;
     if (P.ns()) { gl.resize(size_t(nfq) * nr); gradientTrace(P, F.bl, F.el, F.fl, gl.data()); }
-    double* QL = &BL.qface[size_t(F.el) * nv * BL.ref.nface * nfq];
+    Real* QL = &BL.qface[size_t(F.el) * nv * BL.ref.nface * nfq];
     for (int j = 0; j < nfq; ++j) {
-      const double* n = &F.normal[j * 3];
+      const Real* n = &F.normal[j * 3];
       PointVar b{};
       boundaryState(P.ph, F.bc, n, L[j], P.dummy[size_t(i) * nfq + j], b);
-      double h[kMaxVar]; normalFlux(P.ph, n, b, h);
+      Real h[kMaxVar]; normalFlux(P.ph, n, b, h);
       if (P.ns()) {
-        double pl[15]; primitiveGradient(P.ph, L[j], &gl[size_t(j) * nr], pl);
-        double pb[15]; std::copy_n(pl, nr, pb);
+        Real pl[15]; primitiveGradient(P.ph, L[j], &gl[size_t(j) * nr], pl);
+        Real pb[15]; std::copy_n(pl, nr, pb);
         PointVar lm = L[j];
         if (F.bc >= 3) { lm.rho = b.rho; for (int k = 0; k < 3; ++k) lm.u[k] = b.u[k]; lm.e = b.e; lm.p = b.p; }
         if (F.bc >= 4) for (int k = 0; k < d; ++k) pb[(d + 1) * d + k] = 0.0;
-        double fl[kMaxVar], fb[kMaxVar];
+        Real fl[kMaxVar], fb[kMaxVar];
         viscousNormalFlux(P.ph, n, lm, pl, fl); viscousNormalFlux(P.ph, n, b, pb, fb);
         for (int v = 0; v < nv; ++v) h[v] -= (fl[v] + fb[v]) / 2.0;
       }
@@ -524,12 +525,12 @@ static void quadratureAndResidual(Problem& P) {
     const int nq = B.ref.nq, nb = B.ref.nb, nfl = B.ref.nface * nfq;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
-      const double* QV = &B.qvol[size_t(e) * nv * nq * d];
-      const double* QF = &B.qface[size_t(e) * nv * nfl];
-      double* Rr = &B.res[size_t(e) * nv * nb];
+      const Real* QV = &B.qvol[size_t(e) * nv * nq * d];
+      const Real* QF = &B.qface[size_t(e) * nv * nfl];
+      Real* Rr = &B.res[size_t(e) * nv * nb];
       for (int bb = 0; bb < nb; ++bb)
         for (int v = 0; v < nv; ++v) {
-          double s = 0;
+          Real s = 0;
           for (int c = 0; c < nq * d; ++c) s += QV[size_t(c) * nv + v] * B.ref.dphi[size_t(c) * nb + bb];
           for (int c = 0; c < nfl; ++c) s -= QF[size_t(c) * nv + v] * B.ref.phif[size_t(c) * nb + bb];
           Rr[bb * nv + v] = s;
@@ -538,22 +539,22 @@ static void quadratureAndResidual(Problem& P) {
   }
 }
 
-static const double kRk[3][3][3] = {
+static const Real kRk[3][3][3] = {
     {{1.0, 0.0, 1.0}, {0, 0, 0}, {0, 0, 0}},
     {{1.0, 0.0, 1.0}, {0.5, 0.5, 0.5}, {0, 0, 0}},
     {{1.0, 0.0, 1.0}, {3.0 / 4.0, 1.0 / 4.0, 1.0 / 4.0}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}}};  // TimeIntegration.cpp:45-65
 
-static void update(Problem& P, int stage, double dt) {
+static void update(Problem& P, int stage, Real dt) {
   const int nv = P.nv;
-  const double* c = kRk[P.rk][stage];
+  const Real* c = kRk[P.rk][stage];
   for (Block& B : P.blocks) {
     const int nb = B.ref.nb;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
-      double* U = &B.coef[size_t(e) * nv * nb];
-      const double* L = &B.last[size_t(e) * nv * nb];
-      const double* Rr = &B.res[size_t(e) * nv * nb];
-      std::vector<double> du(size_t(nv) * nb);
+      Real* U = &B.coef[size_t(e) * nv * nb];
+      const Real* L = &B.last[size_t(e) * nv * nb];
+      const Real* Rr = &B.res[size_t(e) * nv * nb];
+      std::vector<Real> du(size_t(nv) * nb);
       applyMinv(P, B, e, nv, Rr, du.data());
       for (int i = 0; i < nv * nb; ++i) U[i] *= c[1];
       for (int i = 0; i < nv * nb; ++i) U[i] += c[0] * L[i];
@@ -564,19 +565,19 @@ static void update(Problem& P, int stage, double dt) {
 
 static void relativeError(Problem& P) {
   const int nv = P.nv;
-  std::vector<double> acc(nv, 0.0);
+  std::vector<Real> acc(nv, 0.0);
   for (Block& B : P.blocks) {
     const int nq = B.ref.nq, nb = B.ref.nb;
-    std::vector<double> part(size_t(omp_get_max_threads()) * nv, 0.0);
+    std::vector<Real> part(size_t(omp_get_max_threads()) * nv, 0.0);
 #pragma omp parallel
     {
-      double* my = &part[size_t(omp_get_thread_num()) * nv];
+      Real* my = &part[size_t(omp_get_thread_num()) * nv];
 #pragma omp for schedule(static)
       for (int64_t e = 0; e < B.ne; ++e) {
-        double vals[216 * kMaxVar];
+        Real vals[216 * kMaxVar];
         interp(nv, nb, nq, &B.res[size_t(e) * nv * nb], B.ref.phi.data(), vals);
         for (int v = 0; v < nv; ++v) {
-          double s = 0; for (int q = 0; q < nq; ++q) s += std::fabs(vals[q * nv + v]);
+          Real s = 0; for (int q = 0; q < nq; ++q) s += std::fabs(vals[q * nv + v]);
           my[v] += s / nq;
         }
       }
@@ -584,10 +585,10 @@ static void relativeError(Problem& P) {
     for (size_t t = 0; t < part.size() / nv; ++t)
       for (int v = 0; v < nv; ++v) acc[v] += part[t * nv + v];
   }
-  for (int v = 0; v < nv; ++v) P.relErr[v] = acc[v] / double(P.totalElements);
+  for (int v = 0; v < nv; ++v) P.relErr[v] = acc[v] / Real(P.totalElements);
 }
 
-static void step(Problem& P, double dt) {
+static void step(Problem& P, Real dt) {
   for (Block& B : P.blocks) B.last = B.coef;  // TimeIntegration.cpp:70-102
   const int nstage = P.rk + 1;
   for (int s = 0; s < nstage; ++s) {
@@ -599,37 +600,37 @@ static void step(Problem& P, double dt) {
 }
 
 // LSQ projection of point values (InitialCondition.cpp:91-104): coef = U_q Phi (Phi^T Phi)^-1.
-static void project(Problem& P, const double* cons) {
+static void project(Problem& P, const Real* cons) {
   const int nv = P.nv;
   size_t off = 0;
   for (Block& B : P.blocks) {
     const int nq = B.ref.nq, nb = B.ref.nb;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
-      const double* u = &cons[(off + size_t(e) * nq) * nv];
-      std::vector<double> t(size_t(nv) * nb, 0.0);
+      const Real* u = &cons[(off + size_t(e) * nq) * nv];
+      std::vector<Real> t(size_t(nv) * nb, 0.0);
       for (int b = 0; b < nb; ++b)
         for (int v = 0; v < nv; ++v) {
-          double s = 0; for (int q = 0; q < nq; ++q) s += u[q * nv + v] * B.ref.phi[size_t(q) * nb + b];
+          Real s = 0; for (int q = 0; q < nq; ++q) s += u[q * nv + v] * B.ref.phi[size_t(q) * nb + b];
           t[b * nv + v] = s;
         }
-      double* U = &B.coef[size_t(e) * nv * nb];
+      Real* U = &B.coef[size_t(e) * nv * nb];
       for (int b = 0; b < nb; ++b)
         for (int v = 0; v < nv; ++v) {
-          double s = 0; for (int k = 0; k < nb; ++k) s += t[k * nv + v] * B.ref.lsqInv[size_t(k) * nb + b];
+          Real s = 0; for (int k = 0; k < nb; ++k) s += t[k * nv + v] * B.ref.lsqInv[size_t(k) * nb + b];
           U[b * nv + v] = s;
         }
       if (P.refine) {  // one correction step of the normal equations (Phi^T Phi) c = Phi^T u
-        std::vector<double> r(size_t(nv) * nb);
+        std::vector<Real> r(size_t(nv) * nb);
         for (int b = 0; b < nb; ++b)
           for (int v = 0; v < nv; ++v) {
-            double s = t[b * nv + v];
+            Real s = t[b * nv + v];
             for (int k = 0; k < nb; ++k) s -= U[k * nv + v] * B.ref.ptp[size_t(k) * nb + b];
             r[b * nv + v] = s;
           }
         for (int b = 0; b < nb; ++b)
           for (int v = 0; v < nv; ++v) {
-            double s = 0; for (int k = 0; k < nb; ++k) s += r[k * nv + v] * B.ref.lsqInv[size_t(k) * nb + b];
+            Real s = 0; for (int k = 0; k < nb; ++k) s += r[k * nv + v] * B.ref.lsqInv[size_t(k) * nb + b];
             U[b * nv + v] += s;
           }
       }
@@ -639,9 +640,10 @@ static void project(Problem& P, const double* cons) {
   P.hasState = true;
 }
 
-static Problem* create(const sdg_mesh* m, const sdg_config* c, int faithful) {
+static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
   auto P = std::make_unique<Problem>();
-  P->refine = faithful == 0;  // parity checker: refined solves; faithful CPU baseline: plain inverse
+  const int faithful = flags & 1;
+  P->refine = (flags & 2) == 0;
   P->dim = m->dimension; P->nv = P->dim + 2; P->p = c->polynomial_order;
   P->eq = c->equation; P->flux = c->convective_flux; P->visc = c->viscous_flux; P->rk = c->time_integration;
   P->faithful = faithful != 0;
@@ -694,6 +696,9 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int faithful) {
 }  // namespace orc
 
 // ---- C interface for the tests and the CPU baseline ------------------------------------------------
+// Only these symbols are exported (the library is built with -fvisibility=hidden), so the double and
+// long-double builds can be loaded into one process without their C++ internals interposing.
+#pragma GCC visibility push(default)
 extern "C" {
 
 struct orc_handle { orc::Problem* p; };
@@ -702,9 +707,12 @@ static thread_local std::string g_orc_error;
 
 const char* orc_last_error() { return g_orc_error.c_str(); }
 
-void* orc_create(const sdg_mesh* mesh, const sdg_config* config, int faithful) {
+// flags: bit 0 = run the gradient pass also for Euler (as the reference does); bit 1 = multiply by the
+// plain explicit inverses (no refinement), i.e. the reference's arithmetic.  The timed CPU baseline uses 3,
+// the parity checker 0.
+void* orc_create(const sdg_mesh* mesh, const sdg_config* config, int flags) {
   try {
-    return orc::create(mesh, config, faithful);
+    return orc::create(mesh, config, flags);
   } catch (const std::exception& e) {
     g_orc_error = e.what();
     return nullptr;
@@ -715,6 +723,7 @@ void orc_destroy(void* h) { delete static_cast<orc::Problem*>(h); }
 
 void orc_set_threads(int n) { if (n > 0) omp_set_num_threads(n); }
 int orc_max_threads() { return omp_get_max_threads(); }
+int orc_real_digits() { return std::numeric_limits<orc::Real>::digits; }
 
 // counts: [element_count, volume_point_count, interior_faces, boundary_faces, nfq, dof]
 void orc_counts(void* h, int64_t* out) {
@@ -743,9 +752,11 @@ void orc_boundary_point_coordinate(void* h, double* out, int32_t* physical) {
 int orc_set_initial_primitive(void* h, const double* prim) {
   orc::Problem& P = *static_cast<orc::Problem*>(h);
   int64_t c[6]; orc_counts(h, c);
-  std::vector<double> cons(size_t(c[1]) * P.nv);
+  std::vector<orc::Real> cons(size_t(c[1]) * P.nv);
   for (int64_t q = 0; q < c[1]; ++q) {
-    orc::PointVar v; orc::fromPrimitive(P.ph, &prim[q * P.nv], v);
+    orc::Real pr[orc::kMaxVar];
+    for (int i = 0; i < P.nv; ++i) pr[i] = prim[q * P.nv + i];
+    orc::PointVar v; orc::fromPrimitive(P.ph, pr, v);
     for (int i = 0; i < P.nv; ++i) cons[q * P.nv + i] = v.cons[i];
   }
   orc::project(P, cons.data());
@@ -753,13 +764,20 @@ int orc_set_initial_primitive(void* h, const double* prim) {
 }
 
 int orc_set_state_point(void* h, const double* cons) {
-  orc::project(*static_cast<orc::Problem*>(h), cons);
+  orc::Problem& P = *static_cast<orc::Problem*>(h);
+  int64_t c[6]; orc_counts(h, c);
+  std::vector<orc::Real> v(cons, cons + size_t(c[1]) * P.nv);
+  orc::project(P, v.data());
   return 0;
 }
 
 int orc_set_boundary_primitive(void* h, const double* prim) {
   orc::Problem& P = *static_cast<orc::Problem*>(h);
-  for (size_t i = 0; i < P.dummy.size(); ++i) orc::fromPrimitive(P.ph, &prim[i * P.nv], P.dummy[i]);
+  for (size_t i = 0; i < P.dummy.size(); ++i) {
+    orc::Real pr[orc::kMaxVar];
+    for (int k = 0; k < P.nv; ++k) pr[k] = prim[i * P.nv + k];
+    orc::fromPrimitive(P.ph, pr, P.dummy[i]);
+  }
   return 0;
 }
 
@@ -767,9 +785,11 @@ int orc_get_state_point(void* h, double* out) {
   const orc::Problem& P = *static_cast<orc::Problem*>(h);
   size_t off = 0;
   for (const auto& B : P.blocks) {
-    for (int64_t e = 0; e < B.ne; ++e)
-      orc::interp(P.nv, B.ref.nb, B.ref.nq, &B.coef[size_t(e) * P.nv * B.ref.nb], B.ref.phi.data(),
-                  out + (off + size_t(e) * B.ref.nq) * P.nv);
+    std::vector<orc::Real> tmp(size_t(B.ref.nq) * P.nv);
+    for (int64_t e = 0; e < B.ne; ++e) {
+      orc::interp(P.nv, B.ref.nb, B.ref.nq, &B.coef[size_t(e) * P.nv * B.ref.nb], B.ref.phi.data(), tmp.data());
+      std::copy(tmp.begin(), tmp.end(), out + (off + size_t(e) * B.ref.nq) * P.nv);
+    }
     off += size_t(B.ne) * B.ref.nq;
   }
   return 0;
@@ -784,18 +804,18 @@ int orc_get_state_modal(void* h, double* out) {
 
 int orc_calculate_delta_time(void* h, double cfl, double* dt) {
   orc::Problem& P = *static_cast<orc::Problem*>(h);
-  double best = 1.79769313486231570e308;
+  orc::Real best = 1.79769313486231570e308;
   for (const auto& B : P.blocks) {
     const int nq = B.ref.nq, nb = B.ref.nb;
     for (int64_t e = 0; e < B.ne; ++e) {
-      double vals[216 * orc::kMaxVar];
+      orc::Real vals[216 * orc::kMaxVar];
       orc::interp(P.nv, nb, nq, &B.coef[size_t(e) * P.nv * nb], B.ref.phi.data(), vals);
       for (int q = 0; q < nq; ++q) {
         orc::PointVar v; for (int i = 0; i < P.nv; ++i) v.cons[i] = vals[q * P.nv + i];
         orc::computationalFromConserved(P.ph, v);
-        const double c = P.ph.soundSpeed(v.rho, v.p);
-        const double sr = std::sqrt(v.u2(P.dim)) + c;
-        const double t = cfl * B.minEdge[e] / (sr * (P.p + 1.0) * (P.p + 1.0));  // TimeIntegration.cpp:119-125
+        const orc::Real c = P.ph.soundSpeed(v.rho, v.p);
+        const orc::Real sr = std::sqrt(v.u2(P.dim)) + c;
+        const orc::Real t = orc::Real(cfl) * B.minEdge[e] / (sr * (P.p + 1.0) * (P.p + 1.0));  // TimeIntegration.cpp:119-125
         best = std::min(best, t);
       }
     }
@@ -806,7 +826,7 @@ int orc_calculate_delta_time(void* h, double cfl, double* dt) {
 
 int orc_step(void* h, int n, double dt) {
   orc::Problem& P = *static_cast<orc::Problem*>(h);
-  for (int i = 0; i < n; ++i) orc::step(P, dt);
+  for (int i = 0; i < n; ++i) orc::step(P, orc::Real(dt));
   return 0;
 }
 
@@ -825,9 +845,10 @@ int orc_residual_point(void* h, double* out) {
   for (auto& B : P.blocks) {
     const int nb = B.ref.nb, nq = B.ref.nq, nv = P.nv;
     for (int64_t e = 0; e < B.ne; ++e) {
-      std::vector<double> du(size_t(nv) * nb);
+      std::vector<orc::Real> du(size_t(nv) * nb), tmp(size_t(nq) * nv);
       orc::applyMinv(P, B, e, nv, &B.res[size_t(e) * nv * nb], du.data());
-      orc::interp(nv, nb, nq, du.data(), B.ref.phi.data(), out + (off + size_t(e) * nq) * nv);
+      orc::interp(nv, nb, nq, du.data(), B.ref.phi.data(), tmp.data());
+      std::copy(tmp.begin(), tmp.end(), out + (off + size_t(e) * nq) * nv);
     }
     off += size_t(B.ne) * nq;
   }
@@ -871,3 +892,4 @@ int orc_interior_face_geometry(void* h, double* out) {
 }
 
 }  // extern "C"
+#pragma GCC visibility pop

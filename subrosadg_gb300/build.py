@@ -56,7 +56,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
 
     def compile_unit(u):
         obj = os.path.join(objdir, u + ".o")
-        cmd = [nvcc, "-std=c++17", GENCODE, "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp,-O3",
+        cmd = [nvcc, "-std=c++17", GENCODE, "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-fopenmp,-O3,-fvisibility=hidden",
                "-c", os.path.join(CSRC, u), "-o", obj]
         if verbose:
             cmd.insert(4, "-Xptxas=-v")

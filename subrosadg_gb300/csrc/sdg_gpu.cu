@@ -488,6 +488,7 @@ double measureFp64Peak(int device, double ms) {
 }  // namespace
 
 // =====================================================================================================
+#pragma GCC visibility push(default)
 extern "C" {
 
 const char* sdg_last_error(const sdg_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
@@ -1077,3 +1078,4 @@ int sdg_adjacency(const sdg_handle* h, int32_t* interior, int32_t* boundary) {
 }
 
 }  // extern "C"
+#pragma GCC visibility pop

@@ -152,6 +152,7 @@ void publish(MeshStorage* s, int dim, sdg_generated_mesh* out) {
 
 }  // namespace
 
+#pragma GCC visibility push(default)
 extern "C" {
 
 int sdg_mesh_generate_2d(double x0, double y0, double lx, double ly, int32_t nx, int32_t ny, double jitter,
@@ -447,3 +448,4 @@ int sdg_mesh_free(sdg_generated_mesh* m) {
 }
 
 }  // extern "C"
+#pragma GCC visibility pop

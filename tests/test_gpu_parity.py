@@ -30,20 +30,25 @@ def per_var(a, b):
             for v in range(b.shape[1])]
 
 
-def pair(case):
+def pair(case, precision="extended"):
+    """GPU solver and oracle on the same mesh, configuration, initial and boundary states.  The default
+    oracle is the extended-precision build: the exact answer of the discrete scheme to ~1e-18."""
     mesh, cfg, prim, bprim, dt, steps = case
     g = sdg.GpuSolver(mesh, cfg)
-    o = Oracle(mesh, cfg, faithful=False)
+    o = Oracle(mesh, cfg, faithful=False, precision=precision)
     pts = g.volume_points()
     np.testing.assert_allclose(pts, o.volume_points(), atol=1e-12)
     p0 = prim(pts)
     g.initialize_primitive(p0)
     o.initialize_primitive(p0)
     if g.counts.boundary_face_count:
+        # each side enumerates its boundary faces in its own order: evaluate the ghost state at each
+        # side's own boundary points
+        nfq = g.counts.face_point_count
         bpts, phys = g.boundary_points()
-        bp = bprim(bpts, np.repeat(phys, g.counts.face_point_count))
-        g.set_boundary_primitive(bp)
-        o.set_boundary_primitive(bp)
+        g.set_boundary_primitive(bprim(bpts, np.repeat(phys, nfq)))
+        bpo, pho = o.boundary_points()
+        o.set_boundary_primitive(bprim(bpo, np.repeat(pho, nfq)))
     return g, o, dt, steps
 
 

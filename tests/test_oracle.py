@@ -141,13 +141,33 @@ def test_oracle_against_committed_vectors(name):
 
 def test_faithful_gradient_pass_does_not_change_euler():
     """The reference runs the gradient pass for Euler too (TimeIntegration.cpp:340-343); it is unused."""
+    import ctypes
+    from oracle import orc
     mesh, cfg, prim, _, dt, steps = cases.vortex_case(n=4, p=2)
-    a = Oracle(mesh, cfg, faithful=True)
-    b = Oracle(mesh, cfg, faithful=False)
-    for o in (a, b):
+    lib = orc.load()
+    out = []
+    for flags in (1, 0):  # with / without the gradient pass, same (refined) arithmetic otherwise
+        o = Oracle(mesh, cfg, faithful=False)
+        lib.orc_destroy(o.h)
+        o.h = lib.orc_create(ctypes.addressof(o._m), ctypes.addressof(o._c), flags)
         o.initialize_primitive(prim(o.volume_points()))
         o.step(dt, 2)
-    assert np.array_equal(a.state_point(), b.state_point())
+        out.append(o.state_point())
+    assert np.array_equal(out[0], out[1])
+
+
+def test_extended_precision_oracle_agrees_with_double():
+    """The long-double build of the oracle is the same algorithm: it agrees with the double build to
+    the double build's round-off, and resolves more digits."""
+    from oracle import orc
+    assert orc.load("extended").orc_real_digits() > 53
+    mesh, cfg, prim, _, dt, steps = cases.tgv_case(n=3, p=2)
+    res = []
+    for prec in ("double", "extended"):
+        o = Oracle(mesh, cfg, faithful=False, precision=prec)
+        o.initialize_primitive(prim(o.volume_points()))
+        res.append(o.residual_point())
+    assert np.linalg.norm(res[0] - res[1]) <= 1e-10 * np.linalg.norm(res[1])
 
 
 def test_vortex_advects_at_freestream_speed():
