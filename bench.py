@@ -1,0 +1,328 @@
+"""Benchmark of the GB300 DG residual-and-update path.
+
+Workload (one step = one SSP-RK3 step of Solver::stepSolver, src/Solver/TimeIntegration.cpp:326-350,
+including the per-step relative-error reduction): 3D compressible Euler Taylor-Green vortex, Mach 0.1,
+gamma 1.4, periodic [0, 2 pi]^3, 64^3 hexahedra, P3 (64 nodes/element, 83,886,080 DOF), HLLC flux,
+dt from CFL 0.2 -- seeded synthetic initial state of that shape (no dataset involved).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  value = DOF-stage updates/s with the state resident in HBM (CUDA events on the
+library's stream); e2e = the same metric through the C ABI with host buffers (pinned), the state
+uploaded and downloaded every step.  --impl reference times the CPU restatement of the reference path
+(the oracle, reference-faithful arithmetic) on the host cores.  Under torchrun (N > 1) each rank runs an
+independent replica on its own GPU (the path is not sharded: replicas only).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "DOF-stage updates/s (FP64, 1 GB300)"
+WORKLOAD = "tgv3d-euler-64^3-hex-P3-HLLC-SSPRK3-CFL0.2"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--elements", type=int, default=64, help="hexahedra per direction")
+    ap.add_argument("--order", type=int, default=3)
+    ap.add_argument("--cpu-sample", type=int, default=32, help="hexahedra per direction of the CPU sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_figures():
+    """Per-launch DRAM traffic and FP64 instruction counts of the element kernel from the committed ncu
+    summary (profiles/), scaled to the full workload there; None when absent."""
+    path = os.path.join(ROOT, "profiles", "tensor_stage_kernel_tgv_hex_p3.md")
+    out = {}
+    try:
+        for line in open(path):
+            if line.startswith("bench-figure "):
+                _, key, val = line.split()[:3]
+                out[key] = float(val)
+    except OSError:
+        pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def tgv_problem(n, p):
+    import subrosadg_gb300 as sdg
+    from tests import cases
+    mesh = sdg.Mesh.box_3d(0, 0, 0, 2 * math.pi, 2 * math.pi, 2 * math.pi, n, n, n, periodic=True)
+    cfg = cases.config(p, sdg.HLLC)
+    return mesh, cfg, lambda pts: cases.tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2])
+
+
+def cpu_baseline(n, p, steps, warmup):
+    """Time the oracle (reference-faithful arithmetic: gradient pass for Euler and dense per-element
+    M^-1 as the reference) on the host cores, on an n^3 sample of the TGV workload."""
+    from oracle import orc
+    mesh, cfg, prim = tgv_problem(n, p)
+    threads = os.cpu_count() or 1
+    orc.set_threads(threads)
+    o = orc.Oracle(mesh, cfg, faithful=True, precision="double")
+    o.initialize_primitive(prim(o.volume_points()))
+    dt = o.delta_time(0.2)
+    o.step(dt, warmup)
+    t0 = time.perf_counter()
+    o.step(dt, steps)
+    t = time.perf_counter() - t0
+    dof = o.dof
+    return {"value": dof * 3 * steps / t, "unit": "DOF-stage/s", "cores": threads, "kind": "port",
+            "sample": f"TGV {n}^3 hexahedra P{p} HLLC ({dof} DOF), {steps} SSP-RK3 steps after {warmup} warm-up, "
+                      f"oracle with the reference's gradient pass and dense M^-1, OpenMP {threads} threads",
+            "seconds": t}
+
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    r = cpu_baseline(args.cpu_sample, args.order, args.steps, args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": "DOF-stage/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": r["sample"]},
+            "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": r["value"], "unit": "DOF-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import ctypes
+
+    import torch
+
+    import subrosadg_gb300 as sdg
+    from subrosadg_gb300 import _abi
+
+    world, rank, local = dist_env()
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+    device = local
+    torch.cuda.set_device(device)
+    lib = _abi.load()
+
+    mesh, cfg, prim = tgv_problem(args.elements, args.order)
+    s = sdg.GpuSolver(mesh, cfg, device=device)
+    c = s.counts
+    s.initialize_primitive(prim(s.volume_points()))
+    dt = s.calculateDeltaTime(0.2)
+    dof = c.degree_of_freedom_count
+    stages = 3
+    stream_ptr = ctypes.c_void_p()
+    lib.sdg_get_stream(s.h, ctypes.byref(stream_ptr))
+    stream = torch.cuda.ExternalStream(stream_ptr.value, device=device)
+
+    # warm-up
+    for _ in range(args.warmup):
+        s.step_async(dt)
+    s.synchronize()
+
+    # timed region: K steps, state resident in HBM (state 8 * DOF bytes >> 129 MB L2: no flush needed)
+    if pg:
+        pg.barrier()
+    torch.cuda.synchronize(device)
+    lib.sdg_set_kernel_timing(s.h, 1)
+    n0 = s.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(device) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            s.step_async(dt)
+        ev1.record(stream)
+        ev1.synchronize()
+    torch.cuda.synchronize(device)
+    ms = ev0.elapsed_time(ev1)
+    launches = s.launch_count() - n0
+    kms = (ctypes.c_double * 4)()
+    kn = (ctypes.c_int64 * 4)()
+    lib.sdg_kernel_time(s.h, kms, kn)
+    lib.sdg_set_kernel_timing(s.h, 0)
+    relerr = s.relative_error()
+    if pg:
+        t = torch.tensor([ms], device=f"cuda:{device}")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+
+    # roofline of the dominant kernel (element stage kernel): algorithmic bytes per launch =
+    # 8 * (3 DOF + (d^2 + 1) N_e): read U, read U_base, write U, affine geometry
+    ne = c.element_count
+    elem_bytes = 8.0 * (3 * dof + 10 * ne)
+    elem_avg_ms = kms[0] / max(kn[0], 1)
+    achieved = elem_bytes / (elem_avg_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    prof = profile_figures()
+    traffic = prof.get("dram_bytes_per_launch")
+    fp64 = ctypes.c_double()
+    lib.sdg_measure_fp64_peak(device, 200.0, ctypes.byref(fp64))
+    fp64_flops = prof.get("fp64_flops_per_launch")
+    fp64_achieved = fp64_flops / (elem_avg_ms * 1e-3) / 1e9 if fp64_flops else None
+
+    # end to end through the C ABI with pinned host buffers: upload state, step, download state
+    e2e = None
+    if not args.no_e2e:
+        npts = c.volume_point_count * s.nv
+        host_in = torch.empty(npts, dtype=torch.float64, pin_memory=True)
+        host_out = torch.empty(npts, dtype=torch.float64, pin_memory=True)
+        s.state_point(host_out.numpy().reshape(-1, s.nv))
+        host_in.copy_(host_out)
+        for _ in range(2):
+            s.set_state_point(host_in.numpy())
+            s.stepSolver(dt)
+            s.state_point(host_out.numpy().reshape(-1, s.nv))
+        if pg:
+            pg.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.set_state_point(host_in.numpy())          # H2D of the step's input state
+            s.stepSolver(dt)                            # step + relative error (D2H)
+            s.state_point(host_out.numpy().reshape(-1, s.nv))  # D2H of the step's result
+        t_e2e = time.perf_counter() - t0
+        if pg:
+            t = torch.tensor([t_e2e], device=f"cuda:{device}")
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+            t_e2e = float(t.item())
+        e2e = {"value": world * dof * stages * args.steps / t_e2e, "unit": "DOF-stage/s",
+               "h2d_bytes_per_step": npts * 8, "d2h_bytes_per_step": npts * 8 + s.nv * 8,
+               "ms_per_step": 1e3 * t_e2e / args.steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.cpu_sample, args.order, 4, 1)
+        cpu.pop("seconds", None)
+
+    if rank != 0:
+        return
+    value = world * dof * stages * args.steps / (ms * 1e-3)
+    line = {
+        "metric": METRIC, "value": value, "unit": "DOF-stage/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "elements": ne, "dof": dof, "stages_per_step": stages, "dt": dt,
+                   "l2": "inputs larger than L2 (state 8*DOF = %.0f MB per buffer, L2 129 MB)" % (8 * dof / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single-gpu"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+                     "kernel": "tensorStageKernel<3,4,affine>", "avg_launch_ms": elem_avg_ms,
+                     "algorithmic_bytes_per_launch": elem_bytes},
+        "fp64": {"peak_gflops": fp64.value, "peak_source": "sdg_measure_fp64_peak (independent-chain DFMA probe)",
+                 "achieved_gflops": fp64_achieved, "frac": (fp64_achieved / fp64.value) if fp64_achieved else None,
+                 "note": "the DG stage kernels are FP64-issue bound on GB300; see DESIGN.md"},
+        "kernel_ms_per_step": {"element": kms[0] / args.steps, "interior_face": kms[1] / args.steps,
+                               "boundary_face": kms[2] / args.steps, "other": kms[3] / args.steps},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "relative_error_last_step": relerr.tolist(),
+    }
+    print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

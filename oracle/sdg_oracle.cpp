@@ -253,12 +253,29 @@ static void buildAdjacency(Problem& P, const sdg_mesh& m) {
 
 // vals[q][v] = sum_b coef(v,b) phi[q][b] for rows q of a phi table.
 static inline void interp(int nv, int nb, int nrow, const Real* coef, const Real* phi, Real* vals) {
-  for (int q = 0; q < nrow; ++q)
-    for (int v = 0; v < nv; ++v) {
-      Real s = 0;
-      for (int b = 0; b < nb; ++b) s += coef[b * nv + v] * phi[size_t(q) * nb + b];
-      vals[q * nv + v] = s;
+  for (int q = 0; q < nrow; ++q) {
+    Real* out = vals + size_t(q) * nv;
+    for (int v = 0; v < nv; ++v) out[v] = 0;
+    const Real* ph = phi + size_t(q) * nb;
+    for (int b = 0; b < nb; ++b) {
+      const Real w = ph[b];
+      const Real* c = coef + size_t(b) * nv;
+      for (int v = 0; v < nv; ++v) out[v] += c[v] * w;
     }
+  }
+}
+
+// out(r, b) (+)= sum_c in(r, c) * tab(c, b): column-major (nr x nc) times row-major (nc x nb) table.
+static inline void gemmAcc(int nr, int nc, int nb, const Real* in, const Real* tab, Real* out, Real sign) {
+  for (int c = 0; c < nc; ++c) {
+    const Real* col = in + size_t(c) * nr;
+    const Real* row = tab + size_t(c) * nb;
+    for (int b = 0; b < nb; ++b) {
+      const Real w = sign * row[b];
+      Real* o = out + size_t(b) * nr;
+      for (int r = 0; r < nr; ++r) o[r] += col[r] * w;
+    }
+  }
 }
 
 // Element-face trace (AdjacencyElementVariable::compute, VariableConvertor.cpp:434-451).
@@ -293,25 +310,13 @@ static void gradientTrace(const Problem& P, int b, int e, int f, Real* out /* nf
 static void applyMinv(const Problem& P, const Block& B, int64_t e, int nr, const Real* R, Real* x) {
   const int nb = B.ref.nb;
   const Real* Mi = &B.minv[size_t(e) * nb * nb];
-  for (int bb = 0; bb < nb; ++bb)
-    for (int r = 0; r < nr; ++r) {
-      Real s = 0; for (int c = 0; c < nb; ++c) s += R[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
-      x[size_t(bb) * nr + r] = s;
-    }
+  for (int i = 0; i < nr * nb; ++i) x[i] = 0;
+  gemmAcc(nr, nb, nb, R, Mi, x, 1);
   if (!P.refine) return;
   const Real* M = &B.mass[size_t(e) * nb * nb];
-  std::vector<Real> res(size_t(nr) * nb);
-  for (int bb = 0; bb < nb; ++bb)
-    for (int r = 0; r < nr; ++r) {
-      Real s = R[size_t(bb) * nr + r];
-      for (int c = 0; c < nb; ++c) s -= x[size_t(c) * nr + r] * M[size_t(c) * nb + bb];
-      res[size_t(bb) * nr + r] = s;
-    }
-  for (int bb = 0; bb < nb; ++bb)
-    for (int r = 0; r < nr; ++r) {
-      Real s = 0; for (int c = 0; c < nb; ++c) s += res[size_t(c) * nr + r] * Mi[size_t(c) * nb + bb];
-      x[size_t(bb) * nr + r] += s;
-    }
+  std::vector<Real> res(R, R + size_t(nr) * nb);
+  gemmAcc(nr, nb, nb, x, M, res.data(), -1);
+  gemmAcc(nr, nb, nb, res.data(), Mi, x, 1);
 }
 
 // ---- the stage kernels ----------------------------------------------------------------------------
@@ -394,13 +399,9 @@ static void gradientQuadratureAndResidual(Problem& P) {
       const Real* QF = &B.qfvg[size_t(e) * nr * nfl];
       const Real* QV = &B.qvg[size_t(e) * nr * nq * d];
       Real* RV = &B.rvg[size_t(e) * nr * nb];
-      for (int bb = 0; bb < nb; ++bb)
-        for (int r = 0; r < nr; ++r) {
-          Real s = 0;
-          for (int c = 0; c < nfl; ++c) s += QF[size_t(c) * nr + r] * B.ref.phif[size_t(c) * nb + bb];
-          for (int c = 0; c < nq * d; ++c) s -= QV[size_t(c) * nr + r] * B.ref.dphi[size_t(c) * nb + bb];
-          RV[size_t(bb) * nr + r] = s;
-        }
+      for (int i = 0; i < nr * nb; ++i) RV[i] = 0;
+      gemmAcc(nr, nfl, nb, QF, B.ref.phif.data(), RV, 1);
+      gemmAcc(nr, nq * d, nb, QV, B.ref.dphi.data(), RV, -1);
       Real* VG = &B.vgc[size_t(e) * nr * nb];
       applyMinv(P, B, e, nr, RV, VG);
       if (!P.ns()) continue;
@@ -411,12 +412,8 @@ static void gradientQuadratureAndResidual(Problem& P) {
       for (int blk = 0; blk < nblk; ++blk) {
         const int c0 = P.visc == 1 ? 0 : blk * nfq, c1 = P.visc == 1 ? nfl : (blk + 1) * nfq;
         Real* RI = &B.rig[(size_t(e) * nblk + blk) * nr * nb];
-        for (int bb = 0; bb < nb; ++bb)
-          for (int r = 0; r < nr; ++r) {
-            Real s = 0;
-            for (int c = c0; c < c1; ++c) s += QI[size_t(c) * nr + r] * B.ref.phif[size_t(c) * nb + bb];
-            RI[size_t(bb) * nr + r] = s;
-          }
+        for (int k = 0; k < nr * nb; ++k) RI[k] = 0;
+        gemmAcc(nr, c1 - c0, nb, QI + size_t(c0) * nr, B.ref.phif.data() + size_t(c0) * nb, RI, 1);
         Real* IG = &B.igc[(size_t(e) * nblk + blk) * nr * nb];
         applyMinv(P, B, e, nr, RI, IG);
         for (int i = 0; i < nr * nb; ++i) G[i] += IG[i];
@@ -528,13 +525,9 @@ static void quadratureAndResidual(Problem& P) {
       const Real* QV = &B.qvol[size_t(e) * nv * nq * d];
       const Real* QF = &B.qface[size_t(e) * nv * nfl];
       Real* Rr = &B.res[size_t(e) * nv * nb];
-      for (int bb = 0; bb < nb; ++bb)
-        for (int v = 0; v < nv; ++v) {
-          Real s = 0;
-          for (int c = 0; c < nq * d; ++c) s += QV[size_t(c) * nv + v] * B.ref.dphi[size_t(c) * nb + bb];
-          for (int c = 0; c < nfl; ++c) s -= QF[size_t(c) * nv + v] * B.ref.phif[size_t(c) * nb + bb];
-          Rr[bb * nv + v] = s;
-        }
+      for (int i = 0; i < nv * nb; ++i) Rr[i] = 0;
+      gemmAcc(nv, nq * d, nb, QV, B.ref.dphi.data(), Rr, 1);
+      gemmAcc(nv, nfl, nb, QF, B.ref.phif.data(), Rr, -1);
     }
   }
 }

@@ -1,8 +1,11 @@
 """GPU parity: the CUDA path (through the C ABI) against the oracle on the same meshes and initial states.
 
-Tolerances (FP64 throughout):
+The truth is the oracle built in extended precision (long double): the reference's algorithm evaluated to
+~1e-18 on the same double inputs.  Tolerances (the GPU path computes in FP64 throughout):
   * initial state (least-squares projection)          relative L2 <= 1e-13
-  * one-stage residual du/dt at the volume points      relative L2 <= 1e-12
+  * one-stage residual du/dt at the volume points      relative L2 <= 1e-12, or -- where FP64 round-off of
+    the problem itself is above that, i.e. the reference's own FP64 arithmetic (the faithful double oracle)
+    misses 1e-12 -- at least 10x closer to the truth than the reference's FP64 arithmetic
   * state after N steps, per conserved variable        relative L2 <= 1e-10
   * relative error of the last step (basis-dependent)  relative     <= 1e-9
   * CFL time step                                      relative     <= 1e-13
@@ -80,6 +83,17 @@ CASES = {
 }
 
 
+def reference_arithmetic_residual(case):
+    """Residual of the reference's own FP64 arithmetic (double oracle, plain inverses) on the same input."""
+    mesh, cfg, prim, bprim, dt, steps = case
+    o = Oracle(mesh, cfg, faithful=True, precision="double")
+    o.initialize_primitive(prim(o.volume_points()))
+    if o.boundary:
+        bpo, pho = o.boundary_points()
+        o.set_boundary_primitive(bprim(bpo, np.repeat(pho, o.nfq)))
+    return o.residual_point()
+
+
 @pytest.mark.parametrize("name", list(CASES))
 def test_parity(name):
     g, o, dt, steps = pair(CASES[name]())
@@ -88,7 +102,11 @@ def test_parity(name):
     assert rel_l2(s0g, s0o) <= 1e-13, rel_l2(s0g, s0o)
     # one residual evaluation
     rg, ro = g.residual_point(), o.residual_point()
-    assert rel_l2(rg, ro) <= 1e-12, (rel_l2(rg, ro), per_var(rg, ro))
+    err = rel_l2(rg, ro)
+    if err > 1e-12:
+        ref_err = rel_l2(reference_arithmetic_residual(CASES[name]()), ro)
+        print(f"{name}: GPU residual error {err:.2e}, reference FP64 arithmetic error {ref_err:.2e}")
+        assert ref_err > 1e-12 and err <= 0.1 * ref_err, (err, ref_err, per_var(rg, ro))
     # time step
     dtg, dto = g.calculateDeltaTime(0.2), o.delta_time(0.2)
     assert abs(dtg - dto) <= 1e-13 * dto
