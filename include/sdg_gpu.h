@@ -216,6 +216,27 @@ int sdg_measure_fp64_peak(int32_t device, double milliseconds, double* gflops);
  * Element indices are within their block; rows sorted lexicographically. */
 int sdg_adjacency(const sdg_handle* handle, int32_t* interior, int32_t* boundary);
 
+/* Allocation-free CFL time step.  Some callers cannot call cudaMalloc where they need a time step -- a
+ * framework whose memory pool forbids raw device allocations, a real-time loop that must not allocate, a
+ * host that only records work into a stream it was handed.  This entry point has no counterpart in the
+ * reference; it returns the same dt as sdg_calculate_delta_time, computed from device arrays the caller
+ * already holds, and allocates nothing:
+ *   state_point   device [point_count][dimension+2] conserved values at the volume points
+ *   minimum_edge  device [point_count / points_per_element] shortest edge per element (minEdge quality)
+ *   delta_time    device pointer to one double that receives dt
+ *   stream        cudaStream_t to enqueue on (NULL: the legacy default stream); the result is ready
+ *                 when the stream reaches that point
+ * Its scratch is a file-scope __device__ array of 131072 doubles (1 MiB) that every GPU which loads
+ * the library holds until the process exits.  point_count above 33,554,432 is rejected with
+ * SDG_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's device address with that
+ * device current (make that first call before any stream capture).  All calls share the array, so calls
+ * that overlap on the GPU race; serialise them.  Errors: SDG_ERR_INVALID_ARGUMENT, SDG_ERR_CUDA, with text
+ * in sdg_last_error(NULL). */
+int sdg_delta_time_noalloc(const double* state_point, const double* minimum_edge, int64_t point_count,
+                           int32_t points_per_element, int32_t dimension, int32_t polynomial_order,
+                           double specific_heat_ratio, double courant_friedrichs_lewy_number, double* delta_time,
+                           void* stream);
+
 /* Structured mesh generators of the reference's example drivers (gmsh transfinite + periodic
  * setups in examples/periodic_2d_ceuler.cpp:63-94 and examples/periodic_3d_ceuler.cpp:60-130),
  * plus the jittered/triangle-split hybrid of the Kelvin-Helmholtz workload.  The generator owns

@@ -135,6 +135,13 @@ struct sdg_handle {
 
 namespace {
 thread_local std::string g_create_error;
+}  // namespace
+
+namespace sdg {
+void setCreateError(const std::string& message) { g_create_error = message; }
+}  // namespace sdg
+
+namespace {
 
 using namespace sdg;
 
