@@ -229,8 +229,8 @@ def run_ours(args):
     torch.cuda.synchronize(device)
     ms = ev0.elapsed_time(ev1)
     launches = s.launch_count() - n0
-    kms = (ctypes.c_double * 4)()
-    kn = (ctypes.c_int64 * 4)()
+    kms = (ctypes.c_double * 5)()
+    kn = (ctypes.c_int64 * 5)()
     lib.sdg_kernel_time(s.h, kms, kn)
     lib.sdg_set_kernel_timing(s.h, 0)
     relerr = s.relative_error()

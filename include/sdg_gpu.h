@@ -201,8 +201,9 @@ int sdg_get_stream(const sdg_handle* handle, void** stream);
 
 /* Diagnostic kernel timing.  While enabled every launch is bracketed by CUDA events on the handle's
  * stream; sdg_kernel_time synchronises and returns, per kernel class -- 0 element stage kernels,
- * 1 interior-face flux, 2 boundary-face flux, 3 other (reductions, conversions) -- the summed device
- * milliseconds and launch counts since timing was (re-)enabled. */
+ * 1 interior-face flux / trace exchange, 2 boundary-face flux / exchange, 3 other (reductions,
+ * conversions), 4 gradient kernels (Navier-Stokes) -- the summed device milliseconds and launch counts
+ * (arrays of 5) since timing was (re-)enabled. */
 int sdg_set_kernel_timing(sdg_handle* handle, int32_t enable);
 int sdg_kernel_time(sdg_handle* handle, double* milliseconds, int64_t* launches);
 

@@ -18,6 +18,7 @@ namespace sdg {
 struct Phys {
   double gamma, gm1, cv, inv_cv, cp, mu, kappa;
   int transport;  // 1 constant, 2 Sutherland
+  double hllc_g2;  // (gamma + 1) / (2 gamma), the HLLC wave-speed factor
 };
 
 // Reciprocal: rcp.approx.ftz.f64 estimate refined by two Newton-Raphson steps r <- r + r(1 - x r)
@@ -100,7 +101,7 @@ __device__ __forceinline__ void fluxHLLC(const State<D>& l, const State<D>& r, c
   const double cl = sqrt(ph.gamma * l.p * l.ir), cr = sqrt(ph.gamma * r.p * r.ir);
   const double rhoAvg = 0.5 * (l.r + r.r), cAvg = 0.5 * (cl + cr);
   const double ps = fmax(0.0, fma(-(unr - unl), rhoAvg * cAvg, 0.5 * (l.p + r.p)));
-  const double g2 = (ph.gamma + 1.0) / (2.0 * ph.gamma);
+  const double g2 = ph.hllc_g2;
   const double ql = ps <= l.p ? 1.0 : sqrt(fma(g2, fma(ps, rcp(l.p), -1.0), 1.0));
   const double sl = fma(-cl, ql, unl);
   if (sl >= 0.0) { normalFlux(l, n, unl, h); return; }
@@ -255,6 +256,87 @@ __device__ __forceinline__ void boundaryState(int bc, const double* n, const Com
 #pragma unroll
     for (int k = 0; k < D; ++k) b.u[k] = g.u[k];
   }
+}
+
+// ---- viscous terms (ViscousFlux.cpp:58-170, VariableConvertor.cpp:574-620, PhysicalModel.cpp:86-165) ----
+
+// Primitive gradient from the conserved gradient g[v*D + k] at a state with velocity u, 1/rho ir and
+// total energy per mass Et = E/rho:  grad rho, grad u_m (gu[k][m] = d_k u_m), grad T.
+template <int D>
+struct PrimGrad {
+  double gu[D][D];
+  double gT[D];
+};
+
+template <int D>
+__device__ __forceinline__ void primitiveGradient(const double* g, const double* u, double ir, double Et,
+                                                  const Phys& ph, PrimGrad<D>& pg) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const double dr = g[k];
+    double ge = fma(-dr, Et, g[(D + 1) * D + k]) * ir;
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      const double gum = fma(-dr, u[m], g[(1 + m) * D + k]) * ir;
+      pg.gu[k][m] = gum;
+      ge = fma(-gum, u[m], ge);
+    }
+    pg.gT[k] = ge * ph.inv_cv;
+  }
+}
+
+// Dynamic viscosity and thermal conductivity at temperature T (constant or Sutherland,
+// PhysicalModel.cpp:86-123): Sutherland ratio sqrt(T^3) (1 + S) / (T + S), S = 110.4 / 273.15.
+__device__ __forceinline__ void transport(double T, const Phys& ph, double& mu, double& kappa) {
+  if (ph.transport == 2) {
+    const double S = 110.4 / 273.15;
+    const double r = sqrt(T * T * T) * (1.0 + S) / (T + S);
+    mu = ph.mu * r;
+    kappa = ph.kappa * r;
+  } else {
+    mu = ph.mu;
+    kappa = ph.kappa;
+  }
+}
+
+// Viscous stress tau and the energy flux q_k = sum_m tau_km u_m + kappa dT/dx_k.
+template <int D>
+__device__ __forceinline__ void viscousTensor(const PrimGrad<D>& pg, const double* u, double T, const Phys& ph,
+                                              double tau[D][D], double* q) {
+  double mu, kappa;
+  transport(T, ph, mu, kappa);
+  double div = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) div += pg.gu[k][k];
+  const double lam = (2.0 / 3.0) * mu * div;
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+#pragma unroll
+    for (int m = 0; m < D; ++m) tau[k][m] = mu * (pg.gu[k][m] + pg.gu[m][k]) - (k == m ? lam : 0.0);
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    double s = kappa * pg.gT[k];
+#pragma unroll
+    for (int m = 0; m < D; ++m) s = fma(tau[k][m], u[m], s);
+    q[k] = s;
+  }
+}
+
+// Viscous normal flux (0, tau.n, q.n) from velocity u, temperature T and primitive gradient pg.
+template <int D>
+__device__ __forceinline__ void viscousNormalFlux(const PrimGrad<D>& pg, const double* u, double T, const double* n,
+                                                  const Phys& ph, double* f) {
+  double tau[D][D], q[D];
+  viscousTensor<D>(pg, u, T, ph, tau, q);
+  f[0] = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) s = fma(tau[k][m], n[k], s);
+    f[1 + m] = s;
+  }
+  f[D + 1] = dotn<D>(q, n);
 }
 
 }  // namespace sdg

@@ -19,6 +19,7 @@
 #include "../../include/sdg_gpu.h"
 #include "sdg_kernels.cuh"
 #include "sdg_kernels_dense.cuh"
+#include "sdg_kernels_ns.cuh"
 #include "sdg_mesh.hpp"
 #include "sdg_operators.hpp"
 
@@ -94,6 +95,11 @@ struct DevBlock {
   double* lsqDev = nullptr;
   int threads = 0, epb = 0, grid = 0;
   size_t smem = 0;
+  int gthreads = 0, gepb = 0;      // gradient kernel (Navier-Stokes)
+  size_t gsmem = 0;
+  std::vector<double> fmetricHost; // bilinear blocks: [e][nface][d] outward n|J_f|
+  double* fmetric = nullptr;
+  size_t gradOffset = 0;           // doubles into the gradient buffer
   int64_t relOffset = 0;           // first partial slot of this block
 };
 
@@ -111,6 +117,12 @@ struct sdg_handle {
   size_t stateCount = 0;
   double* face = nullptr;
   size_t faceCount = 0;
+  bool ns = false;                 // Navier-Stokes: gradient pass + viscous fluxes
+  double* faceOther = nullptr;     // NS: neighbour traces
+  double* faceGrad = nullptr;      // NS: gradient traces
+  double* faceFlux = nullptr;      // NS: face fluxes
+  double* grad = nullptr;          // NS: total gradient at the nodes
+  size_t gradCount = 0;
   int* fconn = nullptr; double* fgeo = nullptr; int64_t nInterior = 0;
   int* bconn = nullptr; double* bgeo = nullptr; double* ghost = nullptr; int64_t nBoundary = 0;
   int nfq = 0, n1d = 0;
@@ -304,19 +316,27 @@ void buildTensorTables(DevBlock& B) {
 }
 
 template <int DIM, int N, bool AFF>
-void tensorConfig(DevBlock& B, bool device) {
+void tensorConfig(DevBlock& B, bool device, bool visc) {
   using S = TensorShape<DIM, N>;
   B.threads = S::THREADS; B.epb = S::EPB; B.smem = S::SMEM;
   B.ustride = S::USTRIDE; B.fstride = S::FSTRIDE;
-  if (device)
-    SDG_CUDA(cudaFuncSetAttribute(tensorStageKernel<DIM, N, AFF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
+  using G = GradShape<DIM, N, AFF>;
+  B.gthreads = G::THREADS; B.gepb = G::EPB; B.gsmem = G::SMEM;
+  if (device) {
+    SDG_CUDA(cudaFuncSetAttribute(tensorStageKernel<DIM, N, AFF, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
+    if (visc) {
+      SDG_CUDA(cudaFuncSetAttribute(tensorStageKernel<DIM, N, AFF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
+      SDG_CUDA(cudaFuncSetAttribute(tensorGradientKernel<DIM, N, AFF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(G::SMEM)));
+    }
+  }
 }
 
-void configureTensor(DevBlock& B, bool device) {
+void configureTensor(DevBlock& B, bool device, bool visc) {
   const int n = B.n;
 #define SDG_TCFG(D, NN)                                                                              \
   if (B.dim == D && n == NN) {                                                                        \
-    if (B.affine) tensorConfig<D, NN, true>(B, device); else if constexpr (D == 2) tensorConfig<D, NN, false>(B, device); \
+    if (B.affine) tensorConfig<D, NN, true>(B, device, visc);                                         \
+    else if constexpr (D == 2) tensorConfig<D, NN, false>(B, device, visc);                           \
     return;                                                                                           \
   }
   SDG_TCFG(2, 3) SDG_TCFG(2, 4) SDG_TCFG(2, 5) SDG_TCFG(2, 6)
@@ -327,16 +347,38 @@ void configureTensor(DevBlock& B, bool device) {
 
 void launchTensor(sdg_handle* h, DevBlock& B, const StageArgs& a) {
   beginLaunch(h, 0);
-#define SDG_TL(D, NN)                                                                                          \
-  if (B.dim == D && B.n == NN) {                                                                               \
-    if (B.affine) tensorStageKernel<D, NN, true><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);          \
-    else if constexpr (D == 2) tensorStageKernel<D, NN, false><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph); \
-    checkLaunch(h);                                                                                            \
-    return;                                                                                                    \
+  const bool visc = a.grad != nullptr;
+#define SDG_TL(D, NN)                                                                                           \
+  if (B.dim == D && B.n == NN) {                                                                                \
+    if (B.affine) {                                                                                             \
+      if (visc) tensorStageKernel<D, NN, true, true><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);       \
+      else tensorStageKernel<D, NN, true, false><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);           \
+    } else if constexpr (D == 2) {                                                                              \
+      if (visc) tensorStageKernel<D, NN, false, true><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);      \
+      else tensorStageKernel<D, NN, false, false><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);          \
+    }                                                                                                           \
+    checkLaunch(h);                                                                                             \
+    return;                                                                                                     \
   }
   SDG_TL(2, 3) SDG_TL(2, 4) SDG_TL(2, 5) SDG_TL(2, 6)
   SDG_TL(3, 2) SDG_TL(3, 3) SDG_TL(3, 4) SDG_TL(3, 5) SDG_TL(3, 6)
 #undef SDG_TL
+  throw Failure(SDG_ERR_UNSUPPORTED, "unsupported tensor block");
+}
+
+void launchGradientTensor(sdg_handle* h, DevBlock& B, const GradArgs& a) {
+  beginLaunch(h, 4);
+  const int grid = int((B.ne + B.gepb - 1) / B.gepb);
+#define SDG_GL(D, NN)                                                                                    \
+  if (B.dim == D && B.n == NN) {                                                                         \
+    if (B.affine) tensorGradientKernel<D, NN, true><<<grid, B.gthreads, B.gsmem, h->stream>>>(a);        \
+    else if constexpr (D == 2) tensorGradientKernel<D, NN, false><<<grid, B.gthreads, B.gsmem, h->stream>>>(a); \
+    checkLaunch(h);                                                                                      \
+    return;                                                                                              \
+  }
+  SDG_GL(2, 3) SDG_GL(2, 4) SDG_GL(2, 5) SDG_GL(2, 6)
+  SDG_GL(3, 2) SDG_GL(3, 3) SDG_GL(3, 4) SDG_GL(3, 5) SDG_GL(3, 6)
+#undef SDG_GL
   throw Failure(SDG_ERR_UNSUPPORTED, "unsupported tensor block");
 }
 
@@ -369,11 +411,63 @@ void launchFaces(sdg_handle* h) {
   }
 }
 
+// Navier-Stokes gradient pass: neighbour traces across faces, then the BR gradient of every block.
+void gradientPass(sdg_handle* h, int which) {
+  if (h->nInterior > 0) {
+    const int grid = int((h->nInterior * h->nfq + 255) / 256);
+    beginLaunch(h, 1);
+    if (h->dim == 2) exchangeKernel<2><<<grid, 256, 0, h->stream>>>(h->face, h->faceOther, h->fconn, h->nInterior, h->n1d);
+    else exchangeKernel<3><<<grid, 256, 0, h->stream>>>(h->face, h->faceOther, h->fconn, h->nInterior, h->n1d);
+    checkLaunch(h);
+  }
+  if (h->nBoundary > 0) {
+    const int grid = int((h->nBoundary * h->nfq + 255) / 256);
+    beginLaunch(h, 2);
+    if (h->dim == 2) exchangeBoundaryKernel<2><<<grid, 256, 0, h->stream>>>(h->face, h->faceOther, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
+    else exchangeBoundaryKernel<3><<<grid, 256, 0, h->stream>>>(h->face, h->faceOther, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
+    checkLaunch(h);
+  }
+  for (DevBlock& B : h->blocks) {
+    GradArgs g;
+    std::memset(&g, 0, sizeof(g));
+    g.u = h->state[which] + B.stateOffset;
+    g.face = h->face; g.faceOther = h->faceOther; g.faceGrad = h->faceGrad;
+    g.grad = h->grad + B.gradOffset; g.geom = B.geom; g.fmetric = B.fmetric; g.tables = B.tables;
+    g.status = h->status; g.ne = B.ne; g.faceBase = B.faceBase;
+    g.br2 = h->cfg.viscous_flux == SDG_VISCOUS_BR2;
+    if (B.kind == kTensor) launchGradientTensor(h, B, g);
+    else throw Failure(SDG_ERR_UNSUPPORTED, "dense Navier-Stokes block");
+  }
+}
+
+void launchFacesNS(sdg_handle* h) {
+  const int flux = h->cfg.convective_flux;
+  if (h->nInterior > 0) {
+    const int grid = int((h->nInterior * h->nfq + 255) / 256);
+    beginLaunch(h, 1);
+#define SDG_NFL(D, F)                                                                                              \
+  if (h->dim == D && flux == F)                                                                                    \
+    nsFaceKernel<D, F><<<grid, 256, 0, h->stream>>>(h->face, h->faceGrad, h->faceFlux, h->fconn, h->fgeo, h->nInterior, \
+                                                    h->n1d, h->ph);
+    SDG_NFL(2, 0) SDG_NFL(2, 1) SDG_NFL(2, 2) SDG_NFL(2, 3) SDG_NFL(3, 0) SDG_NFL(3, 1) SDG_NFL(3, 2) SDG_NFL(3, 3)
+#undef SDG_NFL
+    checkLaunch(h);
+  }
+  if (h->nBoundary > 0) {
+    const int grid = int((h->nBoundary * h->nfq + 255) / 256);
+    beginLaunch(h, 2);
+    if (h->dim == 2) nsBoundaryFaceKernel<2><<<grid, 256, 0, h->stream>>>(h->face, h->faceGrad, h->faceFlux, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
+    else nsBoundaryFaceKernel<3><<<grid, 256, 0, h->stream>>>(h->face, h->faceGrad, h->faceFlux, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
+    checkLaunch(h);
+  }
+}
+
 StageArgs baseArgs(sdg_handle* h, DevBlock& B) {
   StageArgs a;
   std::memset(&a, 0, sizeof(a));
   a.face = h->face; a.geom = B.geom; a.tables = B.tables; a.status = h->status;
   a.ne = B.ne; a.faceBase = B.faceBase;
+  if (h->ns) { a.fluxSrc = h->faceFlux; a.grad = h->grad + B.gradOffset; }
   return a;
 }
 
@@ -400,7 +494,12 @@ const double kRk[3][3][3] = {{{1.0, 0.0, 1.0}, {0, 0, 0}, {0, 0, 0}},
 void stepOnce(sdg_handle* h, double dt, bool relerr) {
   const int ns = h->cfg.time_integration + 1;
   for (int s = 0; s < ns; ++s) {
-    launchFaces(h);
+    if (h->ns) {
+      gradientPass(h, s == 0 ? 0 : 1);
+      launchFacesNS(h);
+    } else {
+      launchFaces(h);
+    }
     const bool last = s == ns - 1;
     for (DevBlock& B : h->blocks) {
       StageArgs a = baseArgs(h, B);
@@ -514,7 +613,14 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     if (c.time_integration < 0 || c.time_integration > 2) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad time integration");
     if (!(c.specific_heat_ratio > 1.0) || !(c.specific_heat_constant_volume > 0) || !(c.specific_heat_constant_pressure > 0))
       throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad thermodynamic constants");
-    if (c.equation == SDG_COMPRESSIBLE_NS) throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes is not built in this library version");
+    if (c.equation == SDG_COMPRESSIBLE_NS) {
+      if (c.viscous_flux != SDG_VISCOUS_BR1 && c.viscous_flux != SDG_VISCOUS_BR2)
+        throw Failure(SDG_ERR_INVALID_ARGUMENT, "Navier-Stokes needs BR1 or BR2");
+      if (!(c.dynamic_viscosity >= 0) || !(c.prandtl_number > 0)) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad transport constants");
+      if (c.transport_model != SDG_TRANSPORT_CONSTANT && c.transport_model != SDG_TRANSPORT_SUTHERLAND)
+        throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad transport model");
+      h->ns = true;
+    }
     if (!mesh->node_coordinate || mesh->node_count <= 0) throw Failure(SDG_ERR_INVALID_ARGUMENT, "no nodes");
     h->cfg = c; h->device = device;
     h->dim = mesh->dimension; h->nv = h->dim + 2; h->p = c.polynomial_order;
@@ -523,6 +629,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     h->ph.cp = c.specific_heat_constant_pressure; h->ph.mu = c.dynamic_viscosity;
     h->ph.kappa = c.prandtl_number > 0 ? c.specific_heat_constant_pressure * c.dynamic_viscosity / c.prandtl_number : 0.0;
     h->ph.transport = c.transport_model;
+    h->ph.hllc_g2 = (c.specific_heat_ratio + 1.0) / (2.0 * c.specific_heat_ratio);
     // element blocks, in the reference's loop order
     std::vector<Block> mb;
     if (h->dim == 2) {
@@ -605,8 +712,9 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       if (B.kind == kTensor) {
         B.ops.build(B.n);
         buildTensorTables(B);
-        configureTensor(B, false);
+        configureTensor(B, false, c.equation == SDG_COMPRESSIBLE_NS);
       } else {
+        if (h->ns) throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes on triangles / P1 quadrangles is not built yet");
         buildDenseTables(B.type, B.p, B.tablesHost, B.phi, B.lsq);
         if (!configureDense(B.type, B.p, B.affine != 0, false, B.threads, B.epb, B.smem))
           throw Failure(SDG_ERR_UNSUPPORTED, "unsupported dense block");
@@ -615,6 +723,22 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       }
       B.grid = int((B.ne + B.epb - 1) / B.epb);
       B.stateOffset = stateOff; stateOff += size_t(B.ne) * B.ustride;
+      B.gradOffset = h->gradCount; h->gradCount += size_t(B.ne) * h->nv * B.dim * B.nb;
+      if (!B.affine) {  // outward n|J_f| of each local face (straight faces: constant along the face)
+        B.fmetricHost.assign(size_t(B.ne) * B.nface * B.dim, 0.0);
+        const int* fl = faceVertexList(b.type);
+        const int nfv = typeFaceVertices(b.type);
+        for (int64_t e = 0; e < B.ne; ++e) {
+          const int32_t* vv = b.vertex + e * typeVertices(b.type);
+          for (int f = 0; f < B.nface; ++f) {
+            const double* p0 = &nodes[size_t(vv[fl[f * nfv]]) * 3];
+            const double* p1 = &nodes[size_t(vv[fl[f * nfv + 1]]) * 3];
+            const double tx = 0.5 * (p1[0] - p0[0]), ty = 0.5 * (p1[1] - p0[1]);
+            B.fmetricHost[(size_t(e) * B.nface + f) * 2 + 0] = ty;
+            B.fmetricHost[(size_t(e) * B.nface + f) * 2 + 1] = -tx;
+          }
+        }
+      }
       B.pointOffset = pointOff; pointOff += size_t(B.ne) * B.nq;
       B.faceBase = faceSlots; faceSlots += B.ne * B.nface;
       B.relOffset = relParts; relParts += B.grid;
@@ -708,7 +832,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     h->hostOnly = false;
     SDG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     for (DevBlock& B : h->blocks) {
-      if (B.kind == kTensor) configureTensor(B, true);
+      if (B.kind == kTensor) configureTensor(B, true, h->ns);
       else if (!configureDense(B.type, B.p, B.affine != 0, true, B.threads, B.epb, B.smem))
         throw Failure(SDG_ERR_CUDA, "cannot configure the dense kernel");
     }
@@ -719,6 +843,16 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     SDG_CUDA(cudaMemsetAsync(h->state[1], 0, h->stateCount * 8, h->stream));
     h->face = devAlloc<double>(h->faceCount);
     SDG_CUDA(cudaMemsetAsync(h->face, 0, h->faceCount * 8, h->stream));
+    if (h->ns) {
+      h->faceOther = devAlloc<double>(h->faceCount);
+      h->faceGrad = devAlloc<double>(h->faceCount * h->dim);
+      h->faceFlux = devAlloc<double>(h->faceCount);
+      h->grad = devAlloc<double>(h->gradCount);
+      SDG_CUDA(cudaMemsetAsync(h->faceOther, 0, h->faceCount * 8, h->stream));
+      SDG_CUDA(cudaMemsetAsync(h->faceGrad, 0, h->faceCount * h->dim * 8, h->stream));
+      SDG_CUDA(cudaMemsetAsync(h->faceFlux, 0, h->faceCount * 8, h->stream));
+      SDG_CUDA(cudaMemsetAsync(h->grad, 0, h->gradCount * 8, h->stream));
+    }
     h->fconn = devAlloc<int>(fconn.size()); upload(h->fconn, fconn, h->stream);
     h->fgeo = devAlloc<double>(fgeo.size()); upload(h->fgeo, fgeo, h->stream);
     h->bconn = devAlloc<int>(bconn.size()); upload(h->bconn, bconn, h->stream);
@@ -737,6 +871,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       B.geom = devAlloc<double>(B.geomHost.size()); upload(B.geom, B.geomHost, h->stream);
       B.tables = devAlloc<double>(B.tablesHost.size()); upload(B.tables, B.tablesHost, h->stream);
       B.minedge = devAlloc<double>(B.minEdge.size()); upload(B.minedge, B.minEdge, h->stream);
+      if (!B.fmetricHost.empty()) { B.fmetric = devAlloc<double>(B.fmetricHost.size()); upload(B.fmetric, B.fmetricHost, h->stream); }
       if (B.kind == kDense) {
         B.phiDev = devAlloc<double>(B.phi.size()); upload(B.phiDev, B.phi, h->stream);
         B.lsqDev = devAlloc<double>(B.lsq.size()); upload(B.lsqDev, B.lsq, h->stream);
@@ -763,11 +898,12 @@ int sdg_destroy(sdg_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   dropTimingEvents(h);
   for (DevBlock& B : h->blocks) {
-    cudaFree(B.geom); cudaFree(B.tables); cudaFree(B.minedge); cudaFree(B.phiDev); cudaFree(B.lsqDev);
+    cudaFree(B.geom); cudaFree(B.tables); cudaFree(B.minedge); cudaFree(B.phiDev); cudaFree(B.lsqDev); cudaFree(B.fmetric);
   }
   cudaFree(h->state[0]); cudaFree(h->state[1]); cudaFree(h->face); cudaFree(h->fconn); cudaFree(h->fgeo);
   cudaFree(h->bconn); cudaFree(h->bgeo); cudaFree(h->ghost); cudaFree(h->scratch); cudaFree(h->relPart);
   cudaFree(h->relOut); cudaFree(h->dtPart); cudaFree(h->status);
+  cudaFree(h->faceOther); cudaFree(h->faceGrad); cudaFree(h->faceFlux); cudaFree(h->grad);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return SDG_OK;
@@ -1001,7 +1137,12 @@ int sdg_residual_point(sdg_handle* h, double* rate) {
   SDG_CUDA(cudaSetDevice(h->device));
   // the face buffer holds the traces of state[0]: compute fluxes, then the rate without an update,
   // then restore the traces (the flux pass overwrote them)
-  launchFaces(h);
+  if (h->ns) {
+    gradientPass(h, 0);
+    launchFacesNS(h);
+  } else {
+    launchFaces(h);
+  }
   for (DevBlock& B : h->blocks) {
     StageArgs a = baseArgs(h, B);
     a.uin = h->state[0] + B.stateOffset;
@@ -1055,7 +1196,7 @@ int sdg_kernel_time(sdg_handle* h, double* ms, int64_t* launches) {
   SDG_API_BEGIN
   SDG_CUDA(cudaSetDevice(h->device));
   SDG_CUDA(cudaStreamSynchronize(h->stream));
-  for (int k = 0; k < 4; ++k) { ms[k] = 0.0; launches[k] = 0; }
+  for (int k = 0; k < 5; ++k) { ms[k] = 0.0; launches[k] = 0; }
   for (size_t i = 0; i < h->timedEvents.size(); ++i) {
     float t = 0.f;
     SDG_CUDA(cudaEventElapsedTime(&t, h->timedEvents[i][0], h->timedEvents[i][1]));

@@ -87,6 +87,8 @@ struct StageArgs {
   int doUpdate;           // 0: no state update (rate/trace only)
   int doTrace;            // write new face traces
   int doVolume;           // evaluate the residual (0: trace-only pass)
+  const double* fluxSrc;  // face-flux slots to lift (null: the face buffer itself, the Euler layout)
+  const double* grad;     // Navier-Stokes: total gradient at the nodes [e][nv*d][NB]
 };
 
 template <int DIM, int N>
@@ -120,7 +122,7 @@ __device__ __forceinline__ int strideOf(int a) {
 }
 
 // Tensor-block stage kernel: one thread per node, EPB elements per CTA.
-template <int DIM, int N, bool AFFINE>
+template <int DIM, int N, bool AFFINE, bool VISC>
 __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS)
     tensorStageKernel(StageArgs a, Phys ph) {
   using S = TensorShape<DIM, N>;
@@ -146,7 +148,7 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS)
     const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * S::FSTRIDE * 8;
     mbarExpectTx(bar, a.doVolume ? ub + fb : ub);
     bulkLoad(sU, a.uin + e0 * S::USTRIDE, ub, bar);
-    if (a.doVolume) bulkLoad(sF, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+    if (a.doVolume) bulkLoad(sF, (a.fluxSrc ? a.fluxSrc : a.face) + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
   {
     const double* src = a.tables;
@@ -179,14 +181,36 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS)
       State<DIM> s;
       makeState<DIM>(s, U, ph);
       const double ep = s.E + s.p;
+      double tau[DIM][DIM], q[DIM];
+      if constexpr (VISC) {
+        // viscous flux from the total gradient at the node (ViscousFlux.cpp:58-103)
+        double g[NV * DIM];
+#pragma unroll
+        for (int c = 0; c < NV * DIM; ++c) g[c] = a.grad[(e * NV * DIM + c) * NB + node];
+        PrimGrad<DIM> pg;
+        primitiveGradient<DIM>(g, s.u, s.ir, s.E * s.ir, ph, pg);
+        double u2 = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) u2 = fma(s.u[k], s.u[k], u2);
+        viscousTensor<DIM>(pg, s.u, fma(-0.5, u2, s.E * s.ir) * ph.inv_cv, ph, tau, q);
+      }
 #pragma unroll
       for (int b = 0; b < DIM; ++b) {
         const double vb = dotn<DIM>(s.u, ja[b]);
         double* G = sG + ((le * DIM + b) * NV) * NB + node;
         G[0] = s.r * vb;
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) G[(1 + k) * NB] = fma(s.m[k], vb, ja[b][k] * s.p);
-        G[(NV - 1) * NB] = ep * vb;
+        for (int k = 0; k < DIM; ++k) {
+          double x = fma(s.m[k], vb, ja[b][k] * s.p);
+          if constexpr (VISC) {
+#pragma unroll
+            for (int c = 0; c < DIM; ++c) x = fma(-ja[b][c], tau[c][k], x);
+          }
+          G[(1 + k) * NB] = x;
+        }
+        double xe = ep * vb;
+        if constexpr (VISC) xe -= dotn<DIM>(q, ja[b]);
+        G[(NV - 1) * NB] = xe;
       }
     }
     __syncthreads();

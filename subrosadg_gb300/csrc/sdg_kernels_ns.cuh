@@ -1,0 +1,429 @@
+// Navier-Stokes (BR1/BR2) kernels of the GB300 DG path: trace exchange, weak gradient, viscous face flux.
+//
+// Per RK stage the reference runs the gradient pass (src/Solver/TimeIntegration.cpp:340-343):
+//   volume gradient quadrature      SpatialDiscrete.cpp:294-322
+//   face gradient fluxes            SpatialDiscrete.cpp:844-968  ({U} n |J_f| w, and 1/2 [U] n |J_f| w)
+//   gradient residual + M^-1        SpatialDiscrete.cpp:1034-1068, TimeIntegration.cpp:200-228
+// then the viscous volume flux (SpatialDiscrete.cpp:194-266) and the central viscous face flux
+// (SpatialDiscrete.cpp:633-842, ViscousFlux.cpp:138-170).
+//
+// With the nodal Gauss basis the gradient of conserved variable v, component k, at node i is
+//   w_k(i) = (1/|J|_i) [ sum_f Lhat_e(i_b) nF_f[k] X_f(j) - sum_b sum_a Dhat(a, i_b) (U |J| dxi_b/dx_k)(a) ]
+// with X = the neighbour trace U+ for the total gradient (the BR1 gradient, and the BR2 volume gradient:
+// {U} + 1/2 [U] = U+), X = {U} for the BR2 "volume" part.  nF_f = n |J_f| of face f; for affine elements
+// Nanson's relation gives nF_f = +-|J| dxi_b/dx (the metric row of the face's axis).  BR2 face gradients add
+// the face's own lift r_f, whose trace at its face is nF_f 1/2[U] sum_a l_a(end)^2 / (w_a |J|_a).
+//
+// Face buffers (NS): face = own traces, faceOther = neighbour traces (exchange kernel),
+// faceGrad = gradient traces [slot][v*d+k][j], faceFlux = outward |J_f| (h - h_visc) per slot.
+#pragma once
+#include "sdg_kernels.cuh"
+
+namespace sdg {
+
+struct GradArgs {
+  const double* u;          // state [e][USTRIDE]
+  const double* face;       // own traces
+  const double* faceOther;  // neighbour traces
+  double* faceGrad;         // gradient traces out, slot stride d*nv*nfq
+  double* grad;             // total gradient at the nodes out, [e][nv*d][NB]
+  const double* geom;       // as the stage kernel
+  const double* fmetric;    // bilinear blocks: [e][nface][d] outward n|J_f|; null for affine
+  const double* tables;
+  unsigned* status;
+  int64_t ne, faceBase;
+  int br2;
+};
+
+// Exchange of traces across interior faces: each side receives the other side's trace at its own points.
+template <int DIM>
+__global__ void __launch_bounds__(256) exchangeKernel(const double* __restrict__ face, double* __restrict__ other,
+                                                      const int* __restrict__ conn, int64_t nface, int n1d) {
+  constexpr int NV = DIM + 2;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = conn[f * 3 + 0], sr = conn[f * 3 + 1], rot = conn[f * 3 + 2];
+  int jr;
+  if constexpr (DIM == 2) {
+    jr = n1d - 1 - j;
+  } else {
+    const int i = j / n1d, k = j - i * n1d;
+    int ii, kk;
+    switch (rot) {
+      case 0: ii = k; kk = i; break;
+      case 1: ii = n1d - 1 - i; kk = k; break;
+      case 2: ii = n1d - 1 - k; kk = n1d - 1 - i; break;
+      default: ii = i; kk = n1d - 1 - k; break;
+    }
+    jr = ii * n1d + kk;
+  }
+  const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const double a = face[L + v * nfq], b = face[R + v * nfq];
+    other[L + v * nfq] = b;
+    other[R + v * nfq] = a;
+  }
+}
+
+// Boundary neighbour trace for the gradient: 2 U_b - U, where U_b is the boundary's gradient state
+// (BoundaryCondition.cpp: U for farfield/inflow/outflow, the wall state for walls); then {U} = U_b and
+// the interface jump 1/2 (U+ - U) = U_b - U, as the reference's boundary gradient fluxes.
+template <int DIM>
+__global__ void __launch_bounds__(256) exchangeBoundaryKernel(const double* __restrict__ face, double* __restrict__ other,
+                                                              const int* __restrict__ conn,
+                                                              const double* __restrict__ fgeo,
+                                                              const double* __restrict__ ghost, int64_t nface, int n1d,
+                                                              Phys ph) {
+  constexpr int NV = DIM + 2;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = conn[f * 3 + 0], bc = conn[f * 3 + 1];
+  const int64_t L = int64_t(sl) * NV * nfq + j;
+  double ul[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) ul[v] = face[L + v * nfq];
+  if (bc <= 2) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) other[L + v * nfq] = ul[v];
+    return;
+  }
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
+  State<DIM> s;
+  makeState<DIM>(s, ul, ph);
+  Comp<DIM> l, g, b;
+  compFromState<DIM>(s, l);
+  const double* gp = ghost + (f * nfq + j) * (DIM + 3);
+  g.r = gp[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) g.u[k] = gp[1 + k];
+  g.e = gp[DIM + 1];
+  g.p = gp[DIM + 2];
+  boundaryState<DIM>(bc, n, l, g, ph, b);
+  double ub[NV], u2 = 0.0;
+  ub[0] = b.r;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) { ub[1 + k] = b.r * b.u[k]; u2 += b.u[k] * b.u[k]; }
+  ub[DIM + 1] = b.r * (b.e + 0.5 * u2);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) other[L + v * nfq] = 2.0 * ub[v] - ul[v];
+}
+
+template <int DIM, int N, bool AFFINE>
+struct GradShape {
+  using S = TensorShape<DIM, N>;
+  static constexpr int NV = S::NV, NB = S::NB, NF = S::NF, NFQ = S::NFQ;
+  static constexpr int FS = NF * NV * NFQ;      // trace slots per element (one area)
+  static constexpr int GSTR = NV * DIM * NB;    // gradient doubles per element
+  static constexpr int PSZ = AFFINE ? 0 : DIM * DIM * NV * NB;  // bilinear: U |J| dxi_b/dx_k per node
+  // shared memory per element: state, own traces, other traces, gradient (total and volume), scratch
+  static constexpr int PER_ELEM = S::USTRIDE + 2 * FS + 2 * GSTR + PSZ + NB;
+  static constexpr int EPB_SMEM = (100 * 1024) / (8 * PER_ELEM) > 0 ? (100 * 1024) / (8 * PER_ELEM) : 1;
+  static constexpr int EPB = S::EPB_RAW < EPB_SMEM ? S::EPB_RAW : EPB_SMEM;
+  static constexpr int THREADS = ((EPB * NB + 31) / 32) * 32;
+  static constexpr size_t SMEM = size_t(EPB) * PER_ELEM * 8 + sizeof(TensorTables) + 16;
+};
+
+// Weak (BR) gradient of a tensor block: one thread per node.  Writes the total gradient at the nodes and
+// the face gradient traces (BR1: total gradient; BR2: volume gradient + the face's own lift).
+template <int DIM, int N, bool AFFINE>
+__global__ void __launch_bounds__(GradShape<DIM, N, AFFINE>::THREADS) tensorGradientKernel(GradArgs a) {
+  using G = GradShape<DIM, N, AFFINE>;
+  using S = TensorShape<DIM, N>;
+  constexpr int NV = G::NV, NB = G::NB, NF = G::NF, NFQ = G::NFQ, FS = G::FS, EPB = G::EPB;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE]
+  double* sS = sU + EPB * S::USTRIDE;                // own traces [EPB][FS]
+  double* sO = sS + EPB * FS;                        // other traces [EPB][FS]
+  double* sGt = sO + EPB * FS;                       // total gradient [EPB][NV*DIM][NB]
+  double* sGv = sGt + EPB * G::GSTR;                 // BR2 volume gradient [EPB][NV*DIM][NB]
+  double* sP = sGv + EPB * G::GSTR;                  // bilinear: U |J| dxi_b/dx_k [EPB][DIM*DIM*NV][NB]
+  double* sJ = sP + EPB * G::PSZ;                    // 1/|J| per node [EPB][NB]
+  TensorTables* T = reinterpret_cast<TensorTables*>(sJ + EPB * NB);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(T + 1);
+
+  const int tid = threadIdx.x;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  const int le = tid / NB, node = tid - le * NB;
+  const bool active = le < ecount;
+  const int64_t e = e0 + le;
+  if (tid == 0) {
+    mbarInit(bar, 1);
+    const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * FS * 8;
+    mbarExpectTx(bar, ub + 2 * fb);
+    bulkLoad(sU, a.u + e0 * S::USTRIDE, ub, bar);
+    bulkLoad(sS, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+    bulkLoad(sO, a.faceOther + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+  }
+  for (int k = tid; k < int(sizeof(TensorTables) / 8); k += blockDim.x)
+    reinterpret_cast<double*>(T)[k] = a.tables[k];
+  __syncthreads();
+  const bool arrived = mbarWait(bar, 0);
+  if (__syncthreads_or(!arrived)) {
+    if (tid == 0) atomicOr(a.status, kStatusTimeout);
+    return;
+  }
+  constexpr int GS = DIM * DIM + 1;
+  int ax[DIM];
+#pragma unroll
+  for (int b = 0; b < DIM; ++b) ax[b] = axisIndex<DIM, N>(node, b);
+  double jinv = 0.0, ja[DIM][DIM];
+  if (active) {
+    const double* g = AFFINE ? a.geom + e * GS : a.geom + (e * NB + node) * GS;
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) ja[b][c] = g[b * DIM + c];
+    jinv = g[DIM * DIM];
+    sJ[le * NB + node] = jinv;
+    if constexpr (!AFFINE) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        const double u = sU[le * S::USTRIDE + v * NB + node];
+#pragma unroll
+        for (int b = 0; b < DIM; ++b)
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) sP[((le * DIM + b) * DIM + k) * NV * NB + v * NB + node] = u * ja[b][k];
+      }
+    }
+  }
+  __syncthreads();
+  if (active) {
+    double nF[DIM][2][DIM];  // outward n|J_f| of the faces (axis b, end)
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int en = 0; en < 2; ++en)
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          if constexpr (AFFINE) nF[b][en][k] = en ? ja[b][k] : -ja[b][k];
+          else nF[b][en][k] = a.fmetric[(e * NF + T->axisFace[b][en]) * DIM + k];
+        }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double tot[DIM], vol[DIM];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) { tot[k] = 0.0; vol[k] = 0.0; }
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) {
+        const int st = strideOf<DIM, N>(b);
+        const int base = node - ax[b] * st;
+        const double lm = T->liftm[ax[b]], lp = T->liftp[ax[b]];
+        const int fm = T->axisFace[b][0], fp = T->axisFace[b][1];
+        const int jm = T->nodeFacePoint[b][0][node], jp = T->nodeFacePoint[b][1][node];
+        const double om = sO[le * FS + (fm * NV + v) * NFQ + jm], op = sO[le * FS + (fp * NV + v) * NFQ + jp];
+        const double sm = sS[le * FS + (fm * NV + v) * NFQ + jm], sp = sS[le * FS + (fp * NV + v) * NFQ + jp];
+        if constexpr (AFFINE) {
+          double dref = 0.0;
+#pragma unroll
+          for (int q = 0; q < N; ++q) dref = fma(T->dhat[q][ax[b]], sU[le * S::USTRIDE + v * NB + base + q * st], dref);
+          // |J| dxi_b/dx_k . (Lhat+ X+ - Lhat- X- - dref); nF(b,+) = -nF(b,-) = |J| dxi_b/dx
+          const double tt = fma(lp, op, fma(-lm, om, -dref));
+          const double tv = fma(lp, 0.5 * (op + sp), fma(-lm, 0.5 * (om + sm), -dref));
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) { tot[k] = fma(ja[b][k], tt, tot[k]); vol[k] = fma(ja[b][k], tv, vol[k]); }
+        } else {
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) {
+            double dk = 0.0;
+            const double* P = sP + ((le * DIM + b) * DIM + k) * NV * NB + v * NB + base;
+#pragma unroll
+            for (int q = 0; q < N; ++q) dk = fma(T->dhat[q][ax[b]], P[q * st], dk);
+            tot[k] = fma(lp * nF[b][1][k], op, fma(lm * nF[b][0][k], om, tot[k] - dk));
+            vol[k] = fma(lp * nF[b][1][k], 0.5 * (op + sp), fma(lm * nF[b][0][k], 0.5 * (om + sm), vol[k] - dk));
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        const double gt = tot[k] * jinv, gv = vol[k] * jinv;
+        sGt[(le * NV * DIM + v * DIM + k) * NB + node] = gt;
+        sGv[(le * NV * DIM + v * DIM + k) * NB + node] = gv;
+        a.grad[(e * NV * DIM + v * DIM + k) * NB + node] = gt;
+      }
+    }
+  }
+  __syncthreads();
+  // face gradient traces
+  for (int idx = tid; idx < ecount * NF * NFQ; idx += blockDim.x) {
+    const int te = idx / (NF * NFQ), r = idx - te * (NF * NFQ);
+    const int f = r / NFQ, j = r - f * NFQ;
+    const int axis = T->faceAxis[f], en = T->faceEnd[f];
+    const double* coef = en ? T->endp : T->endm;
+    const double* lift = en ? T->liftp : T->liftm;
+    const int base = T->faceBase[f][j];
+    const int st = strideOf<DIM, N>(axis);
+    const int64_t ee = e0 + te;
+    double* out = a.faceGrad + (a.faceBase + ee * NF + f) * NV * DIM * NFQ + j;
+    const double* src = a.br2 ? sGv : sGt;
+    double nf[DIM], cl = 0.0;
+    if (a.br2) {
+      // lift trace factor sum_a l_a(end)^2 / (w_a |J|_a) and the face's n|J_f|
+#pragma unroll
+      for (int q = 0; q < N; ++q) cl = fma(coef[q] * lift[q], sJ[te * NB + base + q * st], cl);
+      if constexpr (AFFINE) {
+        const double* g = a.geom + ee * GS;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) nf[k] = en ? g[axis * DIM + k] : -g[axis * DIM + k];
+      } else {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) nf[k] = a.fmetric[(ee * NF + f) * DIM + k];
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      const double jump = a.br2 ? 0.5 * (sO[te * FS + (f * NV + v) * NFQ + j] - sS[te * FS + (f * NV + v) * NFQ + j]) : 0.0;
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        const double* gsrc = src + (te * NV * DIM + v * DIM + k) * NB + base;
+        double acc = 0.0;
+#pragma unroll
+        for (int q = 0; q < N; ++q) acc = fma(coef[q], gsrc[q * st], acc);
+        if (a.br2) acc = fma(cl * nf[k], jump, acc);
+        out[(v * DIM + k) * NFQ] = acc;
+      }
+    }
+  }
+}
+
+// Interior-face Navier-Stokes flux: Riemann flux minus the central viscous flux of the two sides'
+// (state, gradient) traces, times |J_f|; +/- scatter as the Euler face kernel.
+template <int DIM, int FLUX>
+__global__ void __launch_bounds__(256) nsFaceKernel(const double* __restrict__ face, const double* __restrict__ faceGrad,
+                                                    double* __restrict__ faceFlux, const int* __restrict__ conn,
+                                                    const double* __restrict__ fgeo, int64_t nface, int n1d, Phys ph) {
+  constexpr int NV = DIM + 2;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = conn[f * 3 + 0], sr = conn[f * 3 + 1], rot = conn[f * 3 + 2];
+  int jr;
+  if constexpr (DIM == 2) {
+    jr = n1d - 1 - j;
+  } else {
+    const int i = j / n1d, k = j - i * n1d;
+    int ii, kk;
+    switch (rot) {
+      case 0: ii = k; kk = i; break;
+      case 1: ii = n1d - 1 - i; kk = k; break;
+      case 2: ii = n1d - 1 - k; kk = n1d - 1 - i; break;
+      default: ii = i; kk = n1d - 1 - k; break;
+    }
+    jr = ii * n1d + kk;
+  }
+  const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
+  const int64_t LG = int64_t(sl) * NV * DIM * nfq + j, RG = int64_t(sr) * NV * DIM * nfq + jr;
+  double ul[NV], ur[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) { ul[v] = face[L + v * nfq]; ur[v] = face[R + v * nfq]; }
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
+  const double area = fgeo[f * 4 + 3];
+  State<DIM> l, r;
+  makeState<DIM>(l, ul, ph);
+  makeState<DIM>(r, ur, ph);
+  double h[NV];
+  convectiveFlux<DIM, FLUX>(l, r, n, ph, h);
+  double fl[NV], fr[NV];
+  {
+    double g[NV * DIM];
+#pragma unroll
+    for (int c = 0; c < NV * DIM; ++c) g[c] = faceGrad[LG + c * nfq];
+    PrimGrad<DIM> pg;
+    primitiveGradient<DIM>(g, l.u, l.ir, l.E * l.ir, ph, pg);
+    double u2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) u2 = fma(l.u[k], l.u[k], u2);
+    const double T = fma(-0.5, u2, l.E * l.ir) * ph.inv_cv;
+    viscousNormalFlux<DIM>(pg, l.u, T, n, ph, fl);
+  }
+  {
+    double g[NV * DIM];
+#pragma unroll
+    for (int c = 0; c < NV * DIM; ++c) g[c] = faceGrad[RG + c * nfq];
+    PrimGrad<DIM> pg;
+    primitiveGradient<DIM>(g, r.u, r.ir, r.E * r.ir, ph, pg);
+    double u2 = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) u2 = fma(r.u[k], r.u[k], u2);
+    const double T = fma(-0.5, u2, r.E * r.ir) * ph.inv_cv;
+    viscousNormalFlux<DIM>(pg, r.u, T, n, ph, fr);
+  }
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    const double x = fma(-0.5, fl[v] + fr[v], h[v]) * area;
+    faceFlux[L + v * nfq] = x;
+    faceFlux[R + v * nfq] = -x;
+  }
+}
+
+// Boundary-face Navier-Stokes flux (SpatialDiscrete.cpp:750-842 with modifyBoundaryVariable,
+// BoundaryCondition.cpp): convective flux of the boundary state; viscous flux averaged between the
+// interior side (walls: the wall state) and the boundary state, both with the interior primitive gradient
+// (adiabatic walls: zero temperature gradient on the boundary side).
+template <int DIM>
+__global__ void __launch_bounds__(256) nsBoundaryFaceKernel(const double* __restrict__ face,
+                                                            const double* __restrict__ faceGrad,
+                                                            double* __restrict__ faceFlux, const int* __restrict__ conn,
+                                                            const double* __restrict__ fgeo,
+                                                            const double* __restrict__ ghost, int64_t nface, int n1d,
+                                                            Phys ph) {
+  constexpr int NV = DIM + 2;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = conn[f * 3 + 0], bc = conn[f * 3 + 1];
+  const int64_t L = int64_t(sl) * NV * nfq + j, LG = int64_t(sl) * NV * DIM * nfq + j;
+  double ul[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) ul[v] = face[L + v * nfq];
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
+  const double area = fgeo[f * 4 + 3];
+  State<DIM> s;
+  makeState<DIM>(s, ul, ph);
+  Comp<DIM> l, g, b;
+  compFromState<DIM>(s, l);
+  const double* gp = ghost + (f * nfq + j) * (DIM + 3);
+  g.r = gp[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) g.u[k] = gp[1 + k];
+  g.e = gp[DIM + 1];
+  g.p = gp[DIM + 2];
+  boundaryState<DIM>(bc, n, l, g, ph, b);
+  double h[NV];
+  normalFluxComp<DIM>(b, n, h);
+  double gr[NV * DIM];
+#pragma unroll
+  for (int c = 0; c < NV * DIM; ++c) gr[c] = faceGrad[LG + c * nfq];
+  PrimGrad<DIM> pl;
+  primitiveGradient<DIM>(gr, s.u, s.ir, s.E * s.ir, ph, pl);
+  const Comp<DIM>& lm = bc >= 3 ? b : l;
+  double fl[NV], fb[NV];
+  viscousNormalFlux<DIM>(pl, lm.u, lm.e * ph.inv_cv, n, ph, fl);
+  PrimGrad<DIM> pb = pl;
+  if (bc >= 4) {
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) pb.gT[k] = 0.0;
+  }
+  viscousNormalFlux<DIM>(pb, b.u, b.e * ph.inv_cv, n, ph, fb);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) faceFlux[L + v * nfq] = fma(-0.5, fl[v] + fb[v], h[v]) * area;
+}
+
+}  // namespace sdg

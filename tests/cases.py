@@ -70,30 +70,45 @@ def config(p, flux, equation=sdg.EULER, viscous=sdg.VISCOUS_NONE, mu=0.0, prandt
                            cp=CP, cv=CV, gamma=GAMMA, mu=mu, prandtl=prandtl)
 
 
-def vortex_case(n=8, p=3, flux=sdg.ROE, dt=1e-3, steps=4):
+def ns_config(p, flux, viscous, mu, prandtl=0.71, transport=sdg.TRANSPORT_CONSTANT):
+    """Compressible Navier-Stokes with BR1/BR2 (the reference fixes Pr = 0.71, PhysicalModel.cpp:91)."""
+    c = config(p, flux, equation=sdg.NAVIER_STOKES, viscous=viscous, mu=mu, prandtl=prandtl)
+    c.transport_model = transport
+    return c
+
+
+def vortex_case(n=8, p=3, flux=sdg.ROE, dt=1e-3, steps=4, viscous=None, mu=0.0):
     mesh = sdg.Mesh.box_2d(-5.0, -5.0, 10.0, 10.0, n, n, periodic=True)
-    return (mesh, config(p, flux), lambda pts: vortex_primitive(pts[:, 0], pts[:, 1]), None, dt, steps)
+    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
+    return (mesh, cfg, lambda pts: vortex_primitive(pts[:, 0], pts[:, 1]), None, dt, steps)
 
 
-def tgv_case(n=3, p=3, flux=sdg.HLLC, dt=None, steps=3):
+def tgv_case(n=3, p=3, flux=sdg.HLLC, dt=None, steps=3, viscous=None, mu=1.0 / 1600.0):
+    """Taylor-Green vortex; with `viscous` the Navier-Stokes case at Re = 1/mu (1600 by default)."""
     mesh = sdg.Mesh.box_3d(0, 0, 0, 2 * math.pi, 2 * math.pi, 2 * math.pi, n, n, n, periodic=True)
     if dt is None:
         # CFL 0.2 with minEdge = 2 pi / n and max(|u|+c) ~ 1 + 1/Mach (TimeIntegration.cpp:119-125)
         dt = 0.2 * (2 * math.pi / n) / ((1.0 + 1.0 / 0.1 + 0.05) * (p + 1) ** 2)
-    return (mesh, config(p, flux), lambda pts: tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2]), None, dt, steps)
+    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
+    return (mesh, cfg, lambda pts: tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2]), None, dt, steps)
 
 
-def kh_case(n=8, p=4, flux=sdg.LAX_FRIEDRICHS, dt=2e-4, steps=3, jitter=0.1, split=0.5, seed=11):
+def kh_case(n=8, p=4, flux=sdg.LAX_FRIEDRICHS, dt=2e-4, steps=3, jitter=0.1, split=0.5, seed=11, viscous=None,
+            mu=1e-4):
+    """Kelvin-Helmholtz; with `viscous` the Navier-Stokes case at Re = 1/mu (1e4 by default)."""
     mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=True, jitter=jitter, split_fraction=split, seed=seed)
-    return (mesh, config(p, flux), lambda pts: kh_primitive(pts[:, 0], pts[:, 1]), None, dt, steps)
+    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
+    return (mesh, cfg, lambda pts: kh_primitive(pts[:, 0], pts[:, 1]), None, dt, steps)
 
 
 def channel_case(p=2, flux=sdg.HLLC, conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.PRESSURE_OUTFLOW,
                                                   sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW),
-                 n=6, dt=5e-4, steps=3, jitter=0.0, split=0.0):
+                 n=6, dt=5e-4, steps=3, jitter=0.0, split=0.0, viscous=None, mu=0.0,
+                 transport=sdg.TRANSPORT_CONSTANT):
     """Non-periodic box with boundary groups bottom/right/top/left (all six BC kinds testable)."""
     mesh = sdg.Mesh.box_2d(0.0, 0.0, 2.0, 1.0, 2 * n, n, periodic=False, jitter=jitter, split_fraction=split,
                            seed=5, boundary_conditions=list(conditions))
+    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu, transport=transport)
 
     def ic(pts):
         x, y = pts[:, 0], pts[:, 1]
@@ -109,10 +124,10 @@ def channel_case(p=2, flux=sdg.HLLC, conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.PR
         out[:, 0] = 1.0
         out[:, 1] = np.where(phys == 4, 0.4, 0.0)
         out[:, 2] = 0.0
-        out[:, 3] = 1.0 / R_GAS
+        out[:, 3] = np.where(phys == 1, 1.2, 1.0) / R_GAS  # a warmer bottom wall (isothermal case)
         return out
 
-    return (mesh, config(p, flux), ic, bc, dt, steps)
+    return (mesh, cfg, ic, bc, dt, steps)
 
 
 def golden_cases():

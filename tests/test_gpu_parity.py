@@ -80,6 +80,21 @@ CASES = {
     "channel-walls-hybrid": lambda: cases.channel_case(p=3, flux=sdg.LAX_FRIEDRICHS, n=4, steps=3, split=0.5, jitter=0.1,
                                                        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_NONSLIP_WALL,
                                                                    sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW)),
+    # Navier-Stokes (BR1 / BR2); viscosities large enough that the viscous terms are not round-off
+    "ns-vortex-quad-p2-br1-roe": lambda: cases.vortex_case(n=5, p=2, flux=sdg.ROE, steps=4, viscous=sdg.BR1, mu=0.05),
+    "ns-vortex-quad-p3-br2-hllc": lambda: cases.vortex_case(n=5, p=3, flux=sdg.HLLC, steps=4, viscous=sdg.BR2, mu=0.05),
+    "ns-kh-jitter-quad-p4-br2-lf": lambda: cases.kh_case(n=5, p=4, flux=sdg.LAX_FRIEDRICHS, split=0.0, steps=3,
+                                                         viscous=sdg.BR2, mu=2e-3),
+    "ns-kh-jitter-quad-p2-br1-lf": lambda: cases.kh_case(n=6, p=2, flux=sdg.LAX_FRIEDRICHS, split=0.0, steps=3,
+                                                         viscous=sdg.BR1, mu=2e-3),
+    "ns-tgv-hex-p3-br1-roe": lambda: cases.tgv_case(n=3, p=3, flux=sdg.ROE, steps=3, viscous=sdg.BR1, mu=0.02),
+    "ns-tgv-hex-p2-br2-hllc": lambda: cases.tgv_case(n=3, p=2, flux=sdg.HLLC, steps=3, viscous=sdg.BR2, mu=0.02),
+    "ns-channel-walls-quad-p2-br2": lambda: cases.channel_case(p=2, flux=sdg.HLLC, n=4, steps=3, viscous=sdg.BR2, mu=0.01,
+                                                               conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW,
+                                                                           sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "ns-channel-farfield-slip-quad-p3-br1-sutherland": lambda: cases.channel_case(
+        p=3, flux=sdg.ROE, n=4, steps=3, viscous=sdg.BR1, mu=0.01, transport=sdg.TRANSPORT_SUTHERLAND,
+        conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD)),
 }
 
 
