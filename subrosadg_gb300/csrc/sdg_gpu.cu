@@ -435,8 +435,18 @@ void gradientPass(sdg_handle* h, int which) {
     g.grad = h->grad + B.gradOffset; g.geom = B.geom; g.fmetric = B.fmetric; g.tables = B.tables;
     g.status = h->status; g.ne = B.ne; g.faceBase = B.faceBase;
     g.br2 = h->cfg.viscous_flux == SDG_VISCOUS_BR2;
-    if (B.kind == kTensor) launchGradientTensor(h, B, g);
-    else throw Failure(SDG_ERR_UNSUPPORTED, "dense Navier-Stokes block");
+    if (B.kind == kTensor) {
+      launchGradientTensor(h, B, g);
+    } else {
+      DenseGradArgs d;
+      std::memset(&d, 0, sizeof(d));
+      d.u = g.u; d.face = g.face; d.faceOther = g.faceOther; d.faceGrad = g.faceGrad; d.grad = g.grad;
+      d.geom = g.geom; d.fmetric = g.fmetric; d.tables = g.tables; d.status = g.status; d.ne = g.ne;
+      d.faceBase = g.faceBase; d.br2 = g.br2;
+      beginLaunch(h, 4);
+      if (!launchDenseGradient(B.type, B.p, B.affine != 0, d, h->stream)) throw Failure(SDG_ERR_UNSUPPORTED, "dense gradient");
+      checkLaunch(h);
+    }
   }
 }
 
@@ -714,7 +724,6 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         buildTensorTables(B);
         configureTensor(B, false, c.equation == SDG_COMPRESSIBLE_NS);
       } else {
-        if (h->ns) throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes on triangles / P1 quadrangles is not built yet");
         buildDenseTables(B.type, B.p, B.tablesHost, B.phi, B.lsq);
         if (!configureDense(B.type, B.p, B.affine != 0, false, B.threads, B.epb, B.smem))
           throw Failure(SDG_ERR_UNSUPPORTED, "unsupported dense block");
@@ -724,7 +733,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       B.grid = int((B.ne + B.epb - 1) / B.epb);
       B.stateOffset = stateOff; stateOff += size_t(B.ne) * B.ustride;
       B.gradOffset = h->gradCount; h->gradCount += size_t(B.ne) * h->nv * B.dim * B.nb;
-      if (!B.affine) {  // outward n|J_f| of each local face (straight faces: constant along the face)
+      if (!B.affine || B.kind == kDense) {  // outward n|J_f| of each local face (straight faces: constant)
         B.fmetricHost.assign(size_t(B.ne) * B.nface * B.dim, 0.0);
         const int* fl = faceVertexList(b.type);
         const int nfv = typeFaceVertices(b.type);

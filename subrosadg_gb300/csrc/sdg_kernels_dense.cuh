@@ -106,7 +106,7 @@ struct DenseShape {
 
 // Dense stage kernel (2D).  geometry: affine [e][5] = (|J| dxi_b/dx_a row-major, 1/|J|);
 // bilinear: [e][NQ][5] followed by the element's M^-1 [NB][NB].
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
 __global__ void __launch_bounds__(256) denseStageKernel(StageArgs a, Phys ph) {
   using S = DenseShape<NB, NQ, NFQ, NF>;
   constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB;
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(256) denseStageKernel(StageArgs a, Phys ph) {
     const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * S::FSTRIDE * 8;
     mbarExpectTx(bar, a.doVolume ? ub + fb : ub);
     bulkLoad(sU, a.uin + e0 * S::USTRIDE, ub, bar);
-    if (a.doVolume) bulkLoad(sF, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+    if (a.doVolume) bulkLoad(sF, (a.fluxSrc ? a.fluxSrc : a.face) + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
   for (int k = tid; k < int(S::TABLES); k += blockDim.x) tab[k] = a.tables[k];
   __syncthreads();
@@ -161,14 +161,31 @@ __global__ void __launch_bounds__(256) denseStageKernel(StageArgs a, Phys ph) {
       State<2> st;
       makeState<2>(st, U, ph);
       const double ep = st.E + st.p;
+      double tau[2][2] = {{0.0, 0.0}, {0.0, 0.0}}, qh[2] = {0.0, 0.0};
+      if constexpr (VISC) {
+        // gradient at the point from the element's modal gradient coefficients [nv*2][NB]
+        double g[NV * 2];
+        const double* gc = a.grad + e * NV * 2 * NB;
+#pragma unroll
+        for (int c = 0; c < NV * 2; ++c) {
+          double acc = 0.0;
+#pragma unroll
+          for (int b = 0; b < NB; ++b) acc = fma(phi[q * NB + b], gc[c * NB + b], acc);
+          g[c] = acc;
+        }
+        PrimGrad<2> pg;
+        primitiveGradient<2>(g, st.u, st.ir, st.E * st.ir, ph, pg);
+        const double u2 = fma(st.u[0], st.u[0], st.u[1] * st.u[1]);
+        viscousTensor<2>(pg, st.u, fma(-0.5, u2, st.E * st.ir) * ph.inv_cv, ph, tau, qh);
+      }
 #pragma unroll
       for (int b = 0; b < 2; ++b) {
         const double vb = dotn<2>(st.u, ja[b]);
         double* Q = sQ + ((le * 2 + b) * NV) * NQ + q;
         Q[0] = st.r * vb;
-        Q[NQ] = fma(st.m[0], vb, ja[b][0] * st.p);
-        Q[2 * NQ] = fma(st.m[1], vb, ja[b][1] * st.p);
-        Q[3 * NQ] = ep * vb;
+        Q[NQ] = fma(-ja[b][1], tau[1][0], fma(-ja[b][0], tau[0][0], fma(st.m[0], vb, ja[b][0] * st.p)));
+        Q[2 * NQ] = fma(-ja[b][1], tau[1][1], fma(-ja[b][0], tau[0][1], fma(st.m[1], vb, ja[b][1] * st.p)));
+        Q[3 * NQ] = ep * vb - dotn<2>(qh, ja[b]);
       }
     }
     __syncthreads();
@@ -278,13 +295,212 @@ __global__ void __launch_bounds__(256) denseStageKernel(StageArgs a, Phys ph) {
   }
 }
 
+
+// ---- Navier-Stokes gradient of a dense (modal) block -------------------------------------------------
+// R_vg(v*2+k, i) = sum_fj wf_j nF_f[k] X_fj(v) phi_i(x_fj) - sum_q sum_b U_q(v) |J| dxi_b/dx_k w_q dphi_i/dxi_b,
+// gradient coefficients = M^-1 R_vg (SpatialDiscrete.cpp:294-322,844-968,1034-1068; TimeIntegration.cpp:200-228).
+// X = U+ (neighbour trace) gives the total gradient (BR1, and the BR2 volume-point gradient); X = {U} the BR2
+// volume part, to which face f adds its own lift r_f = M^-1 sum_{j in f} wf_j nF_f 1/2[U] phi.
+template <int NB, int NQ, int NFQ, int NF>
+struct DenseGradShape {
+  static constexpr int NV = 4, NFP = NF * NFQ, EPB = 8, THREADS = 256;
+  static constexpr int USTRIDE = (NV * NB + 1) & ~1;
+  static constexpr int FS = NF * NV * NFQ;
+  static constexpr int PER_ELEM = USTRIDE + 2 * FS + NV * NQ + 3 * NV * 2 * NB;
+  static constexpr size_t TABLES = size_t(NQ) * NB * 3 + size_t(NFP) * NB * 2 + size_t(NB) * NB;
+  static constexpr size_t SMEM = (size_t(EPB) * PER_ELEM + TABLES) * 8 + 16;
+};
+
+struct DenseGradArgs {
+  const double* u;
+  const double* face;
+  const double* faceOther;
+  double* faceGrad;
+  double* grad;             // modal gradient coefficients [e][nv*2][NB]
+  const double* geom;
+  const double* fmetric;    // [e][NF][2] outward n|J_f|
+  const double* tables;
+  unsigned* status;
+  int64_t ne, faceBase;
+  int br2;
+};
+
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+__global__ void __launch_bounds__(256) denseGradientKernel(DenseGradArgs a) {
+  using G = DenseGradShape<NB, NQ, NFQ, NF>;
+  constexpr int NV = 4, NFP = G::NFP, EPB = G::EPB, FS = G::FS, NR = NV * 2;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE] modal coefficients
+  double* sS = sU + EPB * G::USTRIDE;                // own traces [EPB][FS]
+  double* sO = sS + EPB * FS;                        // other traces [EPB][FS]
+  double* sUq = sO + EPB * FS;                       // values at the volume points [EPB][NV][NQ]
+  double* sRt = sUq + EPB * NV * NQ;                 // total gradient residual / coefficients [EPB][NR][NB]
+  double* sRv = sRt + EPB * NR * NB;                 // BR2 volume part [EPB][NR][NB]
+  double* sRf = sRv + EPB * NR * NB;                 // BR2 face-lift residual of one face [EPB][NR][NB]
+  double* tab = sRf + EPB * NR * NB;
+  const double* phi = tab;
+  const double* dphiw = phi + NQ * NB;
+  const double* phif = dphiw + NQ * 2 * NB;
+  const double* phifw = phif + NFP * NB;
+  const double* mref = phifw + NFP * NB;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tab + G::TABLES);
+  const int GS = AFFINE ? 5 : NQ * 5 + NB * NB;
+
+  const int tid = threadIdx.x;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  if (tid == 0) {
+    mbarInit(bar, 1);
+    const uint32_t ub = uint32_t(ecount) * G::USTRIDE * 8, fb = uint32_t(ecount) * FS * 8;
+    mbarExpectTx(bar, ub + 2 * fb);
+    bulkLoad(sU, a.u + e0 * G::USTRIDE, ub, bar);
+    bulkLoad(sS, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+    bulkLoad(sO, a.faceOther + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+  }
+  for (int k = tid; k < int(G::TABLES); k += blockDim.x) tab[k] = a.tables[k];
+  __syncthreads();
+  const bool arrived = mbarWait(bar, 0);
+  if (__syncthreads_or(!arrived)) {
+    if (tid == 0) atomicOr(a.status, kStatusTimeout);
+    return;
+  }
+  // values at the volume points
+  for (int idx = tid; idx < ecount * NV * NQ; idx += blockDim.x) {
+    const int le = idx / (NV * NQ), r = idx - le * NV * NQ;
+    const int v = r / NQ, q = r - v * NQ;
+    double acc = 0.0;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) acc = fma(phi[q * NB + b], sU[le * G::USTRIDE + v * NB + b], acc);
+    sUq[(le * NV + v) * NQ + q] = acc;
+  }
+  __syncthreads();
+  // gradient residuals (total, BR2 volume part)
+  for (int idx = tid; idx < ecount * NV * NB; idx += blockDim.x) {
+    const int le = idx / (NV * NB), r = idx - le * NV * NB;
+    const int v = r / NB, i = r - v * NB;
+    const int64_t e = e0 + le;
+    double tot[2] = {0.0, 0.0}, vol[2] = {0.0, 0.0};
+    const double* nF = a.fmetric + e * NF * 2;
+    for (int fj = 0; fj < NFP; ++fj) {
+      const int f = fj / NFQ, j = fj - f * NFQ;
+      const double w = phifw[fj * NB + i];
+      const double o = sO[le * FS + (f * NV + v) * NFQ + j], sv = sS[le * FS + (f * NV + v) * NFQ + j];
+      const double xt = w * o, xv = w * 0.5 * (o + sv);
+      tot[0] = fma(xt, nF[f * 2 + 0], tot[0]); tot[1] = fma(xt, nF[f * 2 + 1], tot[1]);
+      vol[0] = fma(xv, nF[f * 2 + 0], vol[0]); vol[1] = fma(xv, nF[f * 2 + 1], vol[1]);
+    }
+    double d[2][2] = {{0.0, 0.0}, {0.0, 0.0}};  // d[b][k] = sum_q U_q |J| dxi_b/dx_k w_q dphi_i/dxi_b
+    for (int q = 0; q < NQ; ++q) {
+      const double uq = sUq[(le * NV + v) * NQ + q];
+      const double* g = AFFINE ? a.geom + e * GS : a.geom + e * GS + q * 5;
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        const double t = uq * dphiw[(q * 2 + b) * NB + i];
+        d[b][0] = fma(t, g[b * 2 + 0], d[b][0]);
+        d[b][1] = fma(t, g[b * 2 + 1], d[b][1]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      sRt[(le * NR + v * 2 + k) * NB + i] = tot[k] - d[0][k] - d[1][k];
+      sRv[(le * NR + v * 2 + k) * NB + i] = vol[k] - d[0][k] - d[1][k];
+    }
+  }
+  __syncthreads();
+  // M^-1 (affine: M_ref^-1 / |J|; bilinear: the element's inverse); total coefficients -> global
+  for (int idx = tid; idx < ecount * NR * NB; idx += blockDim.x) {
+    const int le = idx / (NR * NB), r = idx - le * NR * NB;
+    const int c = r / NB, i = r - c * NB;
+    const int64_t e = e0 + le;
+    const double* g = a.geom + e * GS;
+    const double* minv = AFFINE ? mref : g + NQ * 5;
+    const double sc = AFFINE ? g[4] : 1.0;
+    double t = 0.0, w = 0.0;
+    for (int k = 0; k < NB; ++k) {
+      t = fma(minv[i * NB + k], sRt[(le * NR + c) * NB + k], t);
+      w = fma(minv[i * NB + k], sRv[(le * NR + c) * NB + k], w);
+    }
+    a.grad[(e * NR + c) * NB + i] = sc * t;
+    sRf[(le * NR + c) * NB + i] = sc * w;  // staged: BR2 volume coefficients
+  }
+  __syncthreads();
+  for (int idx = tid; idx < ecount * NR * NB; idx += blockDim.x) {
+    const int le = idx / (NR * NB), r = idx - le * NR * NB;
+    sRv[le * NR * NB + r] = sRf[le * NR * NB + r];
+    if (!a.br2) sRt[le * NR * NB + r] = a.grad[((e0 + le) * NR) * NB + r];
+  }
+  __syncthreads();
+  if (!a.br2) {
+    // BR1 face gradient traces: trace of the total gradient
+    for (int idx = tid; idx < ecount * NFP; idx += blockDim.x) {
+      const int le = idx / NFP, fj = idx - le * NFP;
+      const int f = fj / NFQ, j = fj - f * NFQ;
+      double* out = a.faceGrad + (a.faceBase + (e0 + le) * NF + f) * NR * NFQ + j;
+#pragma unroll
+      for (int c = 0; c < NR; ++c) {
+        double acc = 0.0;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) acc = fma(phif[fj * NB + b], sRt[(le * NR + c) * NB + b], acc);
+        out[c * NFQ] = acc;
+      }
+    }
+    return;
+  }
+  // BR2: for each face f, trace of (volume gradient + r_f), r_f = M^-1 sum_{j in f} wf_j nF_f 1/2[U] phi
+  for (int f = 0; f < NF; ++f) {
+    for (int idx = tid; idx < ecount * NV * NB; idx += blockDim.x) {
+      const int le = idx / (NV * NB), r = idx - le * NV * NB;
+      const int v = r / NB, i = r - v * NB;
+      const double* nF = a.fmetric + (e0 + le) * NF * 2 + f * 2;
+      double acc = 0.0;
+      for (int j = 0; j < NFQ; ++j) {
+        const double jump = 0.5 * (sO[le * FS + (f * NV + v) * NFQ + j] - sS[le * FS + (f * NV + v) * NFQ + j]);
+        acc = fma(phifw[(f * NFQ + j) * NB + i], jump, acc);
+      }
+      sRt[(le * NR + v * 2 + 0) * NB + i] = acc * nF[0];
+      sRt[(le * NR + v * 2 + 1) * NB + i] = acc * nF[1];
+    }
+    __syncthreads();
+    for (int idx = tid; idx < ecount * NR * NB; idx += blockDim.x) {
+      const int le = idx / (NR * NB), r = idx - le * NR * NB;
+      const int c = r / NB, i = r - c * NB;
+      const int64_t e = e0 + le;
+      const double* g = a.geom + e * GS;
+      const double* minv = AFFINE ? mref : g + NQ * 5;
+      const double sc = AFFINE ? g[4] : 1.0;
+      double t = 0.0;
+      for (int k = 0; k < NB; ++k) t = fma(minv[i * NB + k], sRt[(le * NR + c) * NB + k], t);
+      sRf[(le * NR + c) * NB + i] = sRv[(le * NR + c) * NB + i] + sc * t;
+    }
+    __syncthreads();
+    for (int idx = tid; idx < ecount * NFQ; idx += blockDim.x) {
+      const int le = idx / NFQ, j = idx - le * NFQ;
+      const int fj = f * NFQ + j;
+      double* out = a.faceGrad + (a.faceBase + (e0 + le) * NF + f) * NR * NFQ + j;
+#pragma unroll
+      for (int c = 0; c < NR; ++c) {
+        double acc = 0.0;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) acc = fma(phif[fj * NB + b], sRf[(le * NR + c) * NB + b], acc);
+        out[c * NFQ] = acc;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 template <int NB, int NQ, int NFQ, int NF, bool AFF>
 inline bool denseCfg(bool device, int& threads, int& epb, size_t& smem) {
   using S = DenseShape<NB, NQ, NFQ, NF>;
   threads = S::THREADS; epb = S::EPB; smem = S::SMEM;
   if (!device) return true;
-  return cudaFuncSetAttribute(denseStageKernel<NB, NQ, NFQ, NF, AFF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              int(S::SMEM)) == cudaSuccess;
+  using G = DenseGradShape<NB, NQ, NFQ, NF>;
+  return cudaFuncSetAttribute(denseStageKernel<NB, NQ, NFQ, NF, AFF, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(S::SMEM)) == cudaSuccess &&
+         cudaFuncSetAttribute(denseStageKernel<NB, NQ, NFQ, NF, AFF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(S::SMEM)) == cudaSuccess &&
+         cudaFuncSetAttribute(denseGradientKernel<NB, NQ, NFQ, NF, AFF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              int(G::SMEM)) == cudaSuccess;
 }
 
 // (type, P) -> (NB, NQ, NFQ): triangle P1..P5 use Dunavant rules of 3,6,12,16,25 points.
@@ -296,6 +512,19 @@ inline bool denseCfg(bool device, int& threads, int& epb, size_t& smem) {
   X(SDG_ELEMENT_TRIANGLE, 5, 21, 25, 6, 3, true)            \
   X(SDG_ELEMENT_QUADRANGLE, 1, 4, 7, 2, 4, true)            \
   X(SDG_ELEMENT_QUADRANGLE, 1, 4, 7, 2, 4, false)
+
+inline bool launchDenseGradient(int type, int p, bool affine, const DenseGradArgs& a, cudaStream_t s) {
+#define SDG_DG(T, P, NB, NQ, NFQ, NF, AFF)                                                          \
+  if (type == T && p == P && affine == AFF) {                                                       \
+    using G = DenseGradShape<NB, NQ, NFQ, NF>;                                                      \
+    const int grid = int((a.ne + G::EPB - 1) / G::EPB);                                            \
+    denseGradientKernel<NB, NQ, NFQ, NF, AFF><<<grid, G::THREADS, G::SMEM, s>>>(a);                 \
+    return true;                                                                                    \
+  }
+  SDG_DENSE_CASES(SDG_DG)
+#undef SDG_DG
+  return false;
+}
 
 inline bool configureDense(int type, int p, bool affine, bool device, int& threads, int& epb, size_t& smem) {
 #define SDG_DC(T, P, NB, NQ, NFQ, NF, AFF) \
@@ -309,7 +538,8 @@ inline bool launchDenseStage(int type, int p, bool affine, const StageArgs& a, c
                              size_t smem, cudaStream_t s) {
 #define SDG_DL(T, P, NB, NQ, NFQ, NF, AFF)                                                  \
   if (type == T && p == P && affine == AFF) {                                               \
-    denseStageKernel<NB, NQ, NFQ, NF, AFF><<<grid, threads, smem, s>>>(a, ph);              \
+    if (a.grad) denseStageKernel<NB, NQ, NFQ, NF, AFF, true><<<grid, threads, smem, s>>>(a, ph); \
+    else denseStageKernel<NB, NQ, NFQ, NF, AFF, false><<<grid, threads, smem, s>>>(a, ph);  \
     return true;                                                                            \
   }
   SDG_DENSE_CASES(SDG_DL)

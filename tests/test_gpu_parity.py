@@ -95,6 +95,20 @@ CASES = {
     "ns-channel-farfield-slip-quad-p3-br1-sutherland": lambda: cases.channel_case(
         p=3, flux=sdg.ROE, n=4, steps=3, viscous=sdg.BR1, mu=0.01, transport=sdg.TRANSPORT_SUTHERLAND,
         conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD)),
+    # Navier-Stokes on dense (modal) blocks: triangles, P1 quadrangles, and the hybrid BR2 Kelvin-Helmholtz workload
+    "ns-kh-hybrid-p4-br2-lf": lambda: cases.kh_case(n=6, p=4, flux=sdg.LAX_FRIEDRICHS, steps=3, viscous=sdg.BR2,
+                                                    mu=2e-3),
+    "ns-kh-tri-p3-br1-roe": lambda: cases.kh_case(n=5, p=3, flux=sdg.ROE, split=1.0, steps=3, viscous=sdg.BR1, mu=2e-3),
+    "ns-kh-tri-p2-br2-hllc": lambda: cases.kh_case(n=5, p=2, flux=sdg.HLLC, split=1.0, steps=3, viscous=sdg.BR2,
+                                                   mu=2e-3),
+    "ns-vortex-quad-p1-br2-roe": lambda: cases.vortex_case(n=6, p=1, flux=sdg.ROE, steps=4, viscous=sdg.BR2, mu=0.05),
+    "ns-kh-jitter-quad-p1-br1-lf": lambda: cases.kh_case(n=6, p=1, flux=sdg.LAX_FRIEDRICHS, split=0.0, steps=3,
+                                                         viscous=sdg.BR1, mu=2e-3),
+    "ns-channel-walls-hybrid-p3-br2": lambda: cases.channel_case(
+        p=3, flux=sdg.LAX_FRIEDRICHS, n=4, steps=3, split=0.5, jitter=0.1, viscous=sdg.BR2, mu=0.01,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_NONSLIP_WALL, sdg.ADIABATIC_SLIP_WALL,
+                    sdg.VELOCITY_INFLOW)),
+    "ns-tri-p5-br2-hllc": lambda: cases.kh_case(n=4, p=5, flux=sdg.HLLC, split=1.0, steps=2, viscous=sdg.BR2, mu=2e-3),
 }
 
 
