@@ -263,6 +263,65 @@ int sdg_mesh_generate_3d(double x0, double y0, double z0, double lx, double ly, 
 int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out);
 int sdg_mesh_free(sdg_generated_mesh* mesh);
 
+/* ---- launch shapes: CUDA-graph replay and the autotuner -------------------------------------------
+ * sdg_step replays a CUDA graph of one full step (all stages and the relative-error reduction),
+ * captured on first use and again when dt or a tile shape changes; enable = 0 issues the launches
+ * one by one instead (kernel timing always does).  The reference has no equivalent: its step is a
+ * oneTBB loop (src/Solver/TimeIntegration.cpp:326-350). */
+int sdg_set_graph(sdg_handle* handle, int32_t enable);
+/* Elements per CTA and threads per CTA of block `block`'s stage kernel and gradient kernel. */
+int sdg_get_tile(const sdg_handle* handle, int32_t block, int32_t* elements_per_cta, int32_t* threads,
+                 int32_t* gradient_elements_per_cta, int32_t* gradient_threads);
+int sdg_set_tile(sdg_handle* handle, int32_t block, int32_t elements_per_cta, int32_t threads,
+                 int32_t gradient_elements_per_cta, int32_t gradient_threads);
+/* Autotuner: times every admissible tile of each block's stage kernel (and, for Navier-Stokes, its
+ * gradient kernel) on the handle's current state and keeps the fastest.  Results are cached per
+ * (device, kernel variant) for the process; flags bit 0 re-times cached variants.  The state is not
+ * changed.  Tiles change only how elements are grouped into CTAs: the state a step produces is the
+ * same bit for bit; the relative-error sums are regrouped (round-off only). */
+#define SDG_AUTOTUNE_RETIME 1
+int sdg_autotune(sdg_handle* handle, int32_t flags);
+
+/* ---- batched solves: many independent problems in one set of launches -----------------------------
+ * A batch advances `count` handles (any mix of meshes, element types, orders, Euler / Navier-Stokes,
+ * physical constants; all on one device) together.  Per RK stage, every kernel class of every
+ * (element type, order, affine, viscous) variant runs as ONE persistent launch over a work list of
+ * (instance argument set, tile) items spanning all instances; independent launches of one dependency
+ * level run on forked streams, and the full step is captured in a CUDA graph.  The handles stay
+ * usable on their own; the batch does not own them.  Each instance's results (state, relative error,
+ * status) are exactly those of sdg_step on the handle with the same tiles. */
+typedef struct sdg_batch sdg_batch;
+typedef struct sdg_batch_counts {
+  int32_t instance_count;
+  int32_t launches_per_step;          /* batched kernel launches per step (graph nodes)             */
+  int32_t sequential_launches_per_step; /* launches per step when each instance runs alone         */
+  int32_t persistent_ctas_per_sm;     /* CTAs per SM of the persistent launches (0: one per item)   */
+  int64_t work_items_per_step;
+  int64_t element_count;
+  int64_t degree_of_freedom_count;
+  int32_t stage_count;                /* RK stages per step of the instance with the most           */
+} sdg_batch_counts;
+/* Instances may be host-only handles (device < 0): the batch then only plans (sdg_batch_get_counts). */
+int sdg_batch_create(sdg_handle* const* instances, int32_t count, sdg_batch** batch);
+int sdg_batch_destroy(sdg_batch* batch);
+int sdg_batch_get_counts(const sdg_batch* batch, sdg_batch_counts* counts);
+/* dt of every instance, [count]; required before the first step, cheap to change (no re-capture). */
+int sdg_batch_set_delta_time(sdg_batch* batch, const double* delta_time);
+/* persistent CTAs per SM (0 = one CTA per work item); the autotuner picks it. */
+int sdg_batch_set_persistence(sdg_batch* batch, int32_t ctas_per_sm);
+/* step_count steps of every instance: graph replay of the batched launches (enqueued on the batch's
+ * stream; sdg_batch_synchronize waits and checks every instance's status). */
+int sdg_batch_step_async(sdg_batch* batch, int32_t step_count);
+/* The same steps as one-instance launches, instance after instance on the batch's stream (the
+ * comparison baseline: what the instances cost without batching). */
+int sdg_batch_step_sequential_async(sdg_batch* batch, int32_t step_count);
+int sdg_batch_synchronize(sdg_batch* batch);
+/* Autotuner over the batch: each distinct variant's tiles (sdg_autotune on the first instance that
+ * has it, shared by the rest), then the persistence; instance states are restored afterwards. */
+int sdg_batch_autotune(sdg_batch* batch, int32_t flags);
+int sdg_batch_get_stream(const sdg_batch* batch, void** stream);
+const char* sdg_batch_last_error(const sdg_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,6 +9,6 @@ from ._abi import (ADIABATIC_NONSLIP_WALL, ADIABATIC_SLIP_WALL, BR1, BR2, CENTRA
                    HEXAHEDRON, HLLC, ISOTHERMAL_NONSLIP_WALL, LAX_FRIEDRICHS, NAVIER_STOKES, PERIODIC,
                    PRESSURE_OUTFLOW, QUADRANGLE, RIEMANN_FARFIELD, ROE, SSPRK3, TRANSPORT_CONSTANT,
                    TRANSPORT_NONE, TRANSPORT_SUTHERLAND, TRIANGLE, VELOCITY_INFLOW, VISCOUS_NONE, SdgError)
-from .solver import GpuSolver, Mesh, System, make_config
+from .solver import Batch, GpuSolver, Mesh, System, make_config
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -24,6 +24,7 @@ ERRORS = {
     7: "SDG_ERR_TIMEOUT",
     8: "SDG_ERR_STATE",
 }
+globals().update({name: code for code, name in ERRORS.items()})
 
 TRIANGLE, QUADRANGLE, HEXAHEDRON = 2, 3, 5
 EULER, NAVIER_STOKES = 0, 1
@@ -97,6 +98,22 @@ class SdgGeneratedMesh(ctypes.Structure):
     _fields_ = [("mesh", SdgMesh), ("storage", c_void_p)]
 
 
+class SdgBatchCounts(ctypes.Structure):
+    _fields_ = [
+        ("instance_count", c_int32),
+        ("launches_per_step", c_int32),
+        ("sequential_launches_per_step", c_int32),
+        ("persistent_ctas_per_sm", c_int32),
+        ("work_items_per_step", c_int64),
+        ("element_count", c_int64),
+        ("degree_of_freedom_count", c_int64),
+        ("stage_count", c_int32),
+    ]
+
+
+AUTOTUNE_RETIME = 1
+
+
 # name -> (restype, argtypes); every symbol include/sdg_gpu.h declares.
 SIGNATURES = {
     "sdg_last_error": (c_char_p, [c_void_p]),
@@ -131,6 +148,21 @@ SIGNATURES = {
                                        c_int32, c_int32, c_int32, _p_int32, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_read_msh": (c_int32, [c_char_p, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_free": (c_int32, [POINTER(SdgGeneratedMesh)]),
+    "sdg_set_graph": (c_int32, [c_void_p, c_int32]),
+    "sdg_get_tile": (c_int32, [c_void_p, c_int32, _p_int32, _p_int32, _p_int32, _p_int32]),
+    "sdg_set_tile": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_int32, c_int32]),
+    "sdg_autotune": (c_int32, [c_void_p, c_int32]),
+    "sdg_batch_create": (c_int32, [POINTER(c_void_p), c_int32, POINTER(c_void_p)]),
+    "sdg_batch_destroy": (c_int32, [c_void_p]),
+    "sdg_batch_get_counts": (c_int32, [c_void_p, POINTER(SdgBatchCounts)]),
+    "sdg_batch_set_delta_time": (c_int32, [c_void_p, _p_double]),
+    "sdg_batch_set_persistence": (c_int32, [c_void_p, c_int32]),
+    "sdg_batch_step_async": (c_int32, [c_void_p, c_int32]),
+    "sdg_batch_step_sequential_async": (c_int32, [c_void_p, c_int32]),
+    "sdg_batch_synchronize": (c_int32, [c_void_p]),
+    "sdg_batch_autotune": (c_int32, [c_void_p, c_int32]),
+    "sdg_batch_get_stream": (c_int32, [c_void_p, POINTER(c_void_p)]),
+    "sdg_batch_last_error": (c_char_p, [c_void_p]),
 }
 
 _lib = None

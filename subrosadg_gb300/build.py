@@ -3,7 +3,7 @@
     python -m subrosadg_gb300.build [--force] [-v]
 
 libsdg_gpu.so (CUDA kernels + C ABI + host mesh layer) is compiled with nvcc
-for sm_103a only, two translation units in parallel.  Outputs are git-ignored.
+for sm_103a only, its translation units in parallel (one per kernel family).  Outputs are git-ignored.
 """
 from __future__ import annotations
 
@@ -45,7 +45,8 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     """Compile libsdg_gpu.so (CUDA kernels + C ABI + host mesh layer)."""
     os.makedirs(LIBDIR, exist_ok=True)
     target = os.path.join(LIBDIR, "libsdg_gpu.so")
-    units = ["sdg_gpu.cu", "sdg_mesh.cpp", "sdg_noalloc.cu"]
+    units = ["sdg_variants_tensor.cu", "sdg_variants_dense.cu", "sdg_variants_face.cu", "sdg_gpu.cu", "sdg_batch.cu",
+             "sdg_mesh.cpp", "sdg_noalloc.cu"]
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".cpp", ".hpp", ".h"))]
     deps.append(os.path.join(ROOT, "include", "sdg_gpu.h"))
     if not force and not _stale(target, deps):

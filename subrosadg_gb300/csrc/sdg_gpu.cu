@@ -16,12 +16,11 @@
 #include <string>
 #include <vector>
 
-#include "../../include/sdg_gpu.h"
-#include "sdg_kernels.cuh"
-#include "sdg_kernels_dense.cuh"
-#include "sdg_kernels_ns.cuh"
-#include "sdg_mesh.hpp"
-#include "sdg_operators.hpp"
+#include <map>
+#include <mutex>
+#include <set>
+
+#include "sdg_internal.hpp"
 
 namespace sdg {
 
@@ -57,93 +56,75 @@ void facePointInParent(int type, int f, const double* fx, double* X) {
   }
 }
 
-namespace {
+// ---- point-layout conversions ----------------------------------------------------------------------
+// state[e][v][b] (padded stride) <- points[e][q][v]; proj = null for tensor blocks (nodes are points),
+// else the least-squares projection [nb][nq].
+__global__ void pointToStateKernel(const double* __restrict__ pts, double* __restrict__ st,
+                                   const double* __restrict__ proj, int64_t ne, int nb, int nq, int nv, int ustride) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ne * nb) return;
+  const int64_t e = t / nb;
+  const int b = int(t - e * nb);
+  for (int v = 0; v < nv; ++v) {
+    double s;
+    if (!proj) s = pts[(e * nq + b) * nv + v];
+    else { s = 0.0; for (int q = 0; q < nq; ++q) s = fma(proj[b * nq + q], pts[(e * nq + q) * nv + v], s); }
+    st[e * ustride + v * nb + b] = s;
+  }
+}
 
-struct Failure : std::runtime_error {
-  int code;
-  Failure(int c, const std::string& m) : std::runtime_error(m), code(c) {}
-};
+__global__ void stateToPointKernel(const double* __restrict__ st, double* __restrict__ pts,
+                                   const double* __restrict__ phi, int64_t ne, int nb, int nq, int nv, int ustride) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ne * nq) return;
+  const int64_t e = t / nq;
+  const int q = int(t - e * nq);
+  for (int v = 0; v < nv; ++v) {
+    double s;
+    if (!phi) s = st[e * ustride + v * nb + q];
+    else { s = 0.0; for (int b = 0; b < nb; ++b) s = fma(phi[q * nb + b], st[e * ustride + v * nb + b], s); }
+    pts[(e * nq + q) * nv + v] = s;
+  }
+}
 
-#define SDG_CUDA(call)                                                                              \
-  do {                                                                                              \
-    cudaError_t _e = (call);                                                                        \
-    if (_e != cudaSuccess)                                                                          \
-      throw Failure(_e == cudaErrorMemoryAllocation ? SDG_ERR_OUT_OF_MEMORY : SDG_ERR_CUDA,          \
-                    std::string(#call) + ": " + cudaGetErrorString(_e));                            \
-  } while (0)
+// (rho, u, T) -> (rho, rho u, rho E) in place (VariableConvertor.cpp:341-366).
+__global__ void primitiveToConservedKernel(double* __restrict__ pts, int64_t n, int dim, Phys ph) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  double* p = pts + t * (dim + 2);
+  const double rho = p[0];
+  double u2 = 0.0;
+  for (int k = 0; k < dim; ++k) { u2 += p[1 + k] * p[1 + k]; p[1 + k] *= rho; }
+  p[dim + 1] = rho * (ph.cv * p[dim + 1] + u2 / 2.0);
+}
 
-enum Kind { kTensor = 0, kDense = 1 };
+// dt = min CFL*minEdge/((|u|+c)(P+1)^2) over points (TimeIntegration.cpp:104-131); per-CTA minima.
+__global__ void deltaTimeKernel(const double* __restrict__ pts, const double* __restrict__ minEdge, int64_t n, int nq,
+                                int dim, double cfl, double p1sq, Phys ph, double* __restrict__ part) {
+  __shared__ double sh[256];
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  double dt = 1.79769313486231570e308;
+  if (t < n) {
+    const double* p = pts + t * (dim + 2);
+    const double rho = p[0];
+    double u2 = 0.0;
+    for (int k = 0; k < dim; ++k) { const double u = p[1 + k] / rho; u2 += u * u; }
+    const double e = p[dim + 1] / rho - u2 / 2.0;
+    const double pr = ph.gm1 * rho * e;
+    const double c = sqrt(ph.gamma * pr / rho);
+    dt = cfl * minEdge[t / nq] / ((sqrt(u2) + c) * p1sq);
+  }
+  sh[threadIdx.x] = dt;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
 
-struct DevBlock {
-  int type = 0, dim = 2, p = 1, n = 0, kind = kTensor, affine = 1;
-  int nb = 0, nq = 0, nface = 0, nfq = 0, ustride = 0, fstride = 0, geomStride = 0;
-  int64_t ne = 0, faceBase = 0;
-  size_t stateOffset = 0;          // doubles
-  size_t pointOffset = 0;          // volume points before this block
-  std::vector<double> qcoord;      // [e][q][3]
-  std::vector<double> qweight;     // reference weights [q]
-  std::vector<double> minEdge;     // [e]
-  std::vector<double> geomHost;
-  std::vector<double> tablesHost;
-  std::vector<double> phi;         // dense: [q][nb] ; tensor: unused
-  std::vector<double> lsq;         // dense: [nb][q] projection (Phi^T Phi)^-1 Phi^T
-  TensorOps ops;
-  double* geom = nullptr;
-  double* tables = nullptr;
-  double* minedge = nullptr;
-  double* phiDev = nullptr;
-  double* lsqDev = nullptr;
-  int threads = 0, epb = 0, grid = 0;
-  size_t smem = 0;
-  int gthreads = 0, gepb = 0;      // gradient kernel (Navier-Stokes)
-  size_t gsmem = 0;
-  std::vector<double> fmetricHost; // bilinear blocks: [e][nface][d] outward n|J_f|
-  double* fmetric = nullptr;
-  size_t gradOffset = 0;           // doubles into the gradient buffer
-  int64_t relOffset = 0;           // first partial slot of this block
-};
 
-}  // namespace
 }  // namespace sdg
-
-struct sdg_handle {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  sdg_config cfg{};
-  sdg::Phys ph{};
-  int dim = 2, nv = 4, p = 1;
-  std::vector<sdg::DevBlock> blocks;
-  double* state[2] = {nullptr, nullptr};
-  size_t stateCount = 0;
-  double* face = nullptr;
-  size_t faceCount = 0;
-  bool ns = false;                 // Navier-Stokes: gradient pass + viscous fluxes
-  double* faceOther = nullptr;     // NS: neighbour traces
-  double* faceGrad = nullptr;      // NS: gradient traces
-  double* faceFlux = nullptr;      // NS: face fluxes
-  double* grad = nullptr;          // NS: total gradient at the nodes
-  size_t gradCount = 0;
-  int* fconn = nullptr; double* fgeo = nullptr; int64_t nInterior = 0;
-  int* bconn = nullptr; double* bgeo = nullptr; double* ghost = nullptr; int64_t nBoundary = 0;
-  int nfq = 0, n1d = 0;
-  std::vector<int32_t> adjInterior, adjBoundary;
-  std::vector<double> bcoord; std::vector<int32_t> bphys;
-  double* scratch = nullptr;       // point-layout conversion buffer [volume_points][nv]
-  int64_t volumePoints = 0;
-  double* relPart = nullptr; int64_t relParts = 0;
-  double* relOut = nullptr; double* dtPart = nullptr; int64_t dtParts = 0;
-  unsigned* status = nullptr;
-  double relerr[5] = {0, 0, 0, 0, 0};
-  bool hasState = false;
-  bool hostOnly = true;            // created with device < 0: no GPU resources
-  int64_t launches = 0;
-  bool timing = false;             // bracket launches with events (sdg_set_kernel_timing)
-  std::vector<std::array<cudaEvent_t, 2>> timedEvents;
-  std::vector<int> timedClass;
-  int pendingClass = 3;
-  int64_t elements = 0, dof = 0;
-  std::string err;
-};
 
 namespace {
 thread_local std::string g_create_error;
@@ -176,21 +157,22 @@ void dropTimingEvents(sdg_handle* h) {
 }
 
 // Optional event bracketing of each launch (diagnostic kernel timing).
-void beginLaunch(sdg_handle* h, int cls) {
+void beginLaunch(sdg_handle* h, int cls, cudaStream_t s) {
   if (!h->timing) return;
   std::array<cudaEvent_t, 2> ev;
   SDG_CUDA(cudaEventCreate(&ev[0]));
   SDG_CUDA(cudaEventCreate(&ev[1]));
-  SDG_CUDA(cudaEventRecord(ev[0], h->stream));
+  SDG_CUDA(cudaEventRecord(ev[0], s));
   h->timedEvents.push_back(ev);
   h->timedClass.push_back(cls);
 }
 
-void checkLaunch(sdg_handle* h) {
+void checkLaunch(sdg_handle* h, cudaStream_t s) {
   h->launches++;
   SDG_CUDA(cudaGetLastError());
-  if (h->timing && !h->timedEvents.empty()) SDG_CUDA(cudaEventRecord(h->timedEvents.back()[1], h->stream));
+  if (h->timing && !h->timedEvents.empty()) SDG_CUDA(cudaEventRecord(h->timedEvents.back()[1], s));
 }
+void checkLaunch(sdg_handle* h) { checkLaunch(h, h->stream); }
 
 // ---- geometry --------------------------------------------------------------------------------------
 void shapeGrad(int type, const double* X, double* N, double* G /* [nv][3] */) {
@@ -315,204 +297,186 @@ void buildTensorTables(DevBlock& B) {
   std::memcpy(B.tablesHost.data(), &T, sizeof(T));
 }
 
-template <int DIM, int N, bool AFF>
-void tensorConfig(DevBlock& B, bool device, bool visc) {
-  using S = TensorShape<DIM, N>;
-  B.threads = S::THREADS; B.epb = S::EPB; B.smem = S::SMEM;
-  B.ustride = S::USTRIDE; B.fstride = S::FSTRIDE;
-  using G = GradShape<DIM, N, AFF>;
-  B.gthreads = G::THREADS; B.gepb = G::EPB; B.gsmem = G::SMEM;
-  if (device) {
-    SDG_CUDA(cudaFuncSetAttribute(tensorStageKernel<DIM, N, AFF, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
-    if (visc) {
-      SDG_CUDA(cudaFuncSetAttribute(tensorStageKernel<DIM, N, AFF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(S::SMEM)));
-      SDG_CUDA(cudaFuncSetAttribute(tensorGradientKernel<DIM, N, AFF>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(G::SMEM)));
-    }
-  }
+}  // namespace
+
+namespace sdg {
+
+// ---- kernel configuration ---------------------------------------------------------------------------
+namespace {
+std::mutex g_kernel_mutex;
+std::set<std::pair<int, const void*>> g_configured;
+std::map<int, int> g_optin, g_sms;
+}  // namespace
+
+int sharedMemoryOptin(int device) {
+  std::lock_guard<std::mutex> lock(g_kernel_mutex);
+  auto it = g_optin.find(device);
+  if (it != g_optin.end()) return it->second;
+  int v = 0;
+  SDG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  g_optin[device] = v;
+  return v;
 }
 
-void configureTensor(DevBlock& B, bool device, bool visc) {
-  const int n = B.n;
-#define SDG_TCFG(D, NN)                                                                              \
-  if (B.dim == D && n == NN) {                                                                        \
-    if (B.affine) tensorConfig<D, NN, true>(B, device, visc);                                         \
-    else if constexpr (D == 2) tensorConfig<D, NN, false>(B, device, visc);                           \
-    return;                                                                                           \
-  }
-  SDG_TCFG(2, 3) SDG_TCFG(2, 4) SDG_TCFG(2, 5) SDG_TCFG(2, 6)
-  SDG_TCFG(3, 2) SDG_TCFG(3, 3) SDG_TCFG(3, 4) SDG_TCFG(3, 5) SDG_TCFG(3, 6)
-#undef SDG_TCFG
-  throw Failure(SDG_ERR_UNSUPPORTED, "unsupported tensor block");
+int multiprocessorCount(int device) {
+  std::lock_guard<std::mutex> lock(g_kernel_mutex);
+  auto it = g_sms.find(device);
+  if (it != g_sms.end()) return it->second;
+  int v = 0;
+  SDG_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device));
+  g_sms[device] = v;
+  return v;
 }
 
-void launchTensor(sdg_handle* h, DevBlock& B, const StageArgs& a) {
-  beginLaunch(h, 0);
-  const bool visc = a.grad != nullptr;
-#define SDG_TL(D, NN)                                                                                           \
-  if (B.dim == D && B.n == NN) {                                                                                \
-    if (B.affine) {                                                                                             \
-      if (visc) tensorStageKernel<D, NN, true, true><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);       \
-      else tensorStageKernel<D, NN, true, false><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);           \
-    } else if constexpr (D == 2) {                                                                              \
-      if (visc) tensorStageKernel<D, NN, false, true><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);      \
-      else tensorStageKernel<D, NN, false, false><<<B.grid, B.threads, B.smem, h->stream>>>(a, h->ph);          \
-    }                                                                                                           \
-    checkLaunch(h);                                                                                             \
-    return;                                                                                                     \
-  }
-  SDG_TL(2, 3) SDG_TL(2, 4) SDG_TL(2, 5) SDG_TL(2, 6)
-  SDG_TL(3, 2) SDG_TL(3, 3) SDG_TL(3, 4) SDG_TL(3, 5) SDG_TL(3, 6)
-#undef SDG_TL
-  throw Failure(SDG_ERR_UNSUPPORTED, "unsupported tensor block");
+void configureKernel(const void* fn, int device) {
+  if (!fn) return;
+  const int optin = sharedMemoryOptin(device);
+  std::lock_guard<std::mutex> lock(g_kernel_mutex);
+  if (!g_configured.insert({device, fn}).second) return;
+  SDG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
 }
 
-void launchGradientTensor(sdg_handle* h, DevBlock& B, const GradArgs& a) {
-  beginLaunch(h, 4);
-  const int grid = int((B.ne + B.gepb - 1) / B.gepb);
-#define SDG_GL(D, NN)                                                                                    \
-  if (B.dim == D && B.n == NN) {                                                                         \
-    if (B.affine) tensorGradientKernel<D, NN, true><<<grid, B.gthreads, B.gsmem, h->stream>>>(a);        \
-    else if constexpr (D == 2) tensorGradientKernel<D, NN, false><<<grid, B.gthreads, B.gsmem, h->stream>>>(a); \
-    checkLaunch(h);                                                                                      \
-    return;                                                                                              \
-  }
-  SDG_GL(2, 3) SDG_GL(2, 4) SDG_GL(2, 5) SDG_GL(2, 6)
-  SDG_GL(3, 2) SDG_GL(3, 3) SDG_GL(3, 4) SDG_GL(3, 5) SDG_GL(3, 6)
-#undef SDG_GL
-  throw Failure(SDG_ERR_UNSUPPORTED, "unsupported tensor block");
+void setStageTile(DevBlock& B, bool ns, int epb, int threads) {
+  const KernelVariant& v = B.stageV[ns ? 1 : 0];
+  B.epb = epb;
+  B.threads = v.nodeThreads ? v.threadsFor(epb) : threads;
+  B.smem = v.smem(B.epb, B.threads);
+  B.grid = (B.ne + epb - 1) / epb;
 }
 
-void launchDense(sdg_handle* h, DevBlock& B, const StageArgs& a) {
-  beginLaunch(h, 0);
-  if (!launchDenseStage(B.type, B.p, B.affine != 0, a, h->ph, B.grid, B.threads, B.smem, h->stream))
-    throw Failure(SDG_ERR_UNSUPPORTED, "unsupported dense block");
-  checkLaunch(h);
+void setGradTile(DevBlock& B, int epb, int threads) {
+  B.gepb = epb;
+  B.gthreads = B.gradV.nodeThreads ? B.gradV.threadsFor(epb) : threads;
+  B.gsmem = B.gradV.smem(B.gepb, B.gthreads);
+  B.ggrid = (B.ne + epb - 1) / epb;
 }
 
-void launchFaces(sdg_handle* h) {
-  const int flux = h->cfg.convective_flux;
-  if (h->nInterior > 0) {
-    const int64_t threads = h->nInterior * h->nfq;
-    const int grid = int((threads + 255) / 256);
-    beginLaunch(h, 1);
-#define SDG_FL(D, F) \
-  if (h->dim == D && flux == F) { faceKernel<D, F><<<grid, 256, 0, h->stream>>>(h->face, h->fconn, h->fgeo, h->nInterior, h->n1d, h->ph); }
-    SDG_FL(2, 0) SDG_FL(2, 1) SDG_FL(2, 2) SDG_FL(2, 3) SDG_FL(3, 0) SDG_FL(3, 1) SDG_FL(3, 2) SDG_FL(3, 3)
-#undef SDG_FL
-    checkLaunch(h);
-  }
-  if (h->nBoundary > 0) {
-    const int64_t threads = h->nBoundary * h->nfq;
-    const int grid = int((threads + 255) / 256);
-    beginLaunch(h, 2);
-    if (h->dim == 2) boundaryFaceKernel<2><<<grid, 256, 0, h->stream>>>(h->face, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
-    else boundaryFaceKernel<3><<<grid, 256, 0, h->stream>>>(h->face, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
-    checkLaunch(h);
-  }
+namespace {
+
+// Kernel variants of a block (element kind, order, affine) and its default tiles.
+void resolveBlock(DevBlock& B, bool ns) {
+  for (int visc = 0; visc < 2; ++visc)
+    B.stageV[visc] = B.kind == kTensor ? tensorStageVariant(B.dim, B.n, B.affine != 0, visc != 0)
+                                       : denseStageVariant(B.type, B.p, B.affine != 0, visc != 0);
+  B.gradV = B.kind == kTensor ? tensorGradVariant(B.dim, B.n, B.affine != 0) : denseGradVariant(B.type, B.p, B.affine != 0);
+  if (!B.stageV[0].valid() || !B.stageV[1].valid() || !B.gradV.valid())
+    throw Failure(SDG_ERR_UNSUPPORTED, "unsupported element block (type, order, affine)");
+  const KernelVariant& v = B.stageV[ns ? 1 : 0];
+  B.ustride = ((B.dim + 2) * B.nb + 1) & ~1;
+  B.fstride = B.nface * (B.dim + 2) * B.nfq;
+  setStageTile(B, ns, v.epb, v.threads);
+  setGradTile(B, B.gradV.epb, B.gradV.threads);
 }
 
-// Navier-Stokes gradient pass: neighbour traces across faces, then the BR gradient of every block.
-void gradientPass(sdg_handle* h, int which) {
-  if (h->nInterior > 0) {
-    const int grid = int((h->nInterior * h->nfq + 255) / 256);
-    beginLaunch(h, 1);
-    if (h->dim == 2) exchangeKernel<2><<<grid, 256, 0, h->stream>>>(h->face, h->faceOther, h->fconn, h->nInterior, h->n1d);
-    else exchangeKernel<3><<<grid, 256, 0, h->stream>>>(h->face, h->faceOther, h->fconn, h->nInterior, h->n1d);
-    checkLaunch(h);
-  }
-  if (h->nBoundary > 0) {
-    const int grid = int((h->nBoundary * h->nfq + 255) / 256);
-    beginLaunch(h, 2);
-    if (h->dim == 2) exchangeBoundaryKernel<2><<<grid, 256, 0, h->stream>>>(h->face, h->faceOther, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
-    else exchangeBoundaryKernel<3><<<grid, 256, 0, h->stream>>>(h->face, h->faceOther, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
-    checkLaunch(h);
-  }
-  for (DevBlock& B : h->blocks) {
-    GradArgs g;
-    std::memset(&g, 0, sizeof(g));
-    g.u = h->state[which] + B.stateOffset;
-    g.face = h->face; g.faceOther = h->faceOther; g.faceGrad = h->faceGrad;
-    g.grad = h->grad + B.gradOffset; g.geom = B.geom; g.fmetric = B.fmetric; g.tables = B.tables;
-    g.status = h->status; g.ne = B.ne; g.faceBase = B.faceBase;
-    g.br2 = h->cfg.viscous_flux == SDG_VISCOUS_BR2;
-    if (B.kind == kTensor) {
-      launchGradientTensor(h, B, g);
-    } else {
-      DenseGradArgs d;
-      std::memset(&d, 0, sizeof(d));
-      d.u = g.u; d.face = g.face; d.faceOther = g.faceOther; d.faceGrad = g.faceGrad; d.grad = g.grad;
-      d.geom = g.geom; d.fmetric = g.fmetric; d.tables = g.tables; d.status = g.status; d.ne = g.ne;
-      d.faceBase = g.faceBase; d.br2 = g.br2;
-      beginLaunch(h, 4);
-      if (!launchDenseGradient(B.type, B.p, B.affine != 0, d, h->stream)) throw Failure(SDG_ERR_UNSUPPORTED, "dense gradient");
-      checkLaunch(h);
-    }
-  }
-}
+}  // namespace
 
-void launchFacesNS(sdg_handle* h) {
-  const int flux = h->cfg.convective_flux;
-  if (h->nInterior > 0) {
-    const int grid = int((h->nInterior * h->nfq + 255) / 256);
-    beginLaunch(h, 1);
-#define SDG_NFL(D, F)                                                                                              \
-  if (h->dim == D && flux == F)                                                                                    \
-    nsFaceKernel<D, F><<<grid, 256, 0, h->stream>>>(h->face, h->faceGrad, h->faceFlux, h->fconn, h->fgeo, h->nInterior, \
-                                                    h->n1d, h->ph);
-    SDG_NFL(2, 0) SDG_NFL(2, 1) SDG_NFL(2, 2) SDG_NFL(2, 3) SDG_NFL(3, 0) SDG_NFL(3, 1) SDG_NFL(3, 2) SDG_NFL(3, 3)
-#undef SDG_NFL
-    checkLaunch(h);
-  }
-  if (h->nBoundary > 0) {
-    const int grid = int((h->nBoundary * h->nfq + 255) / 256);
-    beginLaunch(h, 2);
-    if (h->dim == 2) nsBoundaryFaceKernel<2><<<grid, 256, 0, h->stream>>>(h->face, h->faceGrad, h->faceFlux, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
-    else nsBoundaryFaceKernel<3><<<grid, 256, 0, h->stream>>>(h->face, h->faceGrad, h->faceFlux, h->bconn, h->bgeo, h->ghost, h->nBoundary, h->n1d, h->ph);
-    checkLaunch(h);
-  }
-}
-
-StageArgs baseArgs(sdg_handle* h, DevBlock& B) {
-  StageArgs a;
+// ---- launch records ---------------------------------------------------------------------------------
+Rec stageRec(sdg_handle* h, DevBlock& B) {
+  Rec r;
+  r.kind = kRecStage; r.cls = 0;
+  const KernelVariant& v = B.stageV[h->ns ? 1 : 0];
+  r.fn = v.single; r.bfn = v.batch;
+  r.threads = B.threads; r.epb = B.epb; r.smem = B.smem; r.units = B.grid;
+  StageArgs& a = r.sa;
   std::memset(&a, 0, sizeof(a));
   a.face = h->face; a.geom = B.geom; a.tables = B.tables; a.status = h->status;
-  a.ne = B.ne; a.faceBase = B.faceBase;
+  a.ne = B.ne; a.faceBase = B.faceBase; a.epb = B.epb;
   if (h->ns) { a.fluxSrc = h->faceFlux; a.grad = h->grad + B.gradOffset; }
-  return a;
+  r.ph = h->ph;
+  return r;
 }
 
-void launchBlock(sdg_handle* h, DevBlock& B, const StageArgs& a) {
-  if (B.kind == kTensor) launchTensor(h, B, a);
-  else launchDense(h, B, a);
-}
-
-// Face traces of state buffer `which` (initial condition or after a state upload).
-void traceAll(sdg_handle* h, int which) {
-  for (DevBlock& B : h->blocks) {
-    StageArgs a = baseArgs(h, B);
-    a.uin = h->state[which] + B.stateOffset;
-    a.doTrace = 1; a.doVolume = 0; a.doUpdate = 0;
-    launchBlock(h, B, a);
+Rec gradRec(sdg_handle* h, DevBlock& B, int which) {
+  Rec r;
+  r.cls = 4;
+  r.fn = B.gradV.single; r.bfn = B.gradV.batch;
+  r.threads = B.gthreads; r.epb = B.gepb; r.smem = B.gsmem; r.units = B.ggrid;
+  const double* u = h->state[which] ? h->state[which] + B.stateOffset : nullptr;
+  double* g = h->grad ? h->grad + B.gradOffset : nullptr;
+  const int br2 = h->cfg.viscous_flux == SDG_VISCOUS_BR2;
+  if (B.kind == kTensor) {
+    r.kind = kRecGradTensor;
+    GradArgs& a = r.ga;
+    std::memset(&a, 0, sizeof(a));
+    a.u = u; a.face = h->face; a.faceOther = h->faceOther; a.faceGrad = h->faceGrad; a.grad = g;
+    a.geom = B.geom; a.fmetric = B.fmetric; a.tables = B.tables; a.status = h->status;
+    a.ne = B.ne; a.faceBase = B.faceBase; a.br2 = br2; a.epb = B.gepb;
+  } else {
+    r.kind = kRecGradDense;
+    DenseGradArgs& a = r.da;
+    std::memset(&a, 0, sizeof(a));
+    a.u = u; a.face = h->face; a.faceOther = h->faceOther; a.faceGrad = h->faceGrad; a.grad = g;
+    a.geom = B.geom; a.fmetric = B.fmetric; a.tables = B.tables; a.status = h->status;
+    a.ne = B.ne; a.faceBase = B.faceBase; a.br2 = br2; a.epb = B.gepb;
   }
+  return r;
+}
+
+namespace {
+
+bool boundaryOp(int op) { return op == kOpFaceBoundary || op == kOpExchangeBoundary || op == kOpFaceNSBoundary; }
+
+Rec faceRec(sdg_handle* h, int op) {
+  Rec r;
+  r.kind = kRecFace;
+  const bool bnd = boundaryOp(op);
+  r.cls = bnd ? 2 : 1;
+  r.fn = h->faceV[op].single; r.bfn = h->faceV[op].batch;
+  r.threads = kFaceThreads; r.epb = 1; r.smem = 0;
+  FaceArgs& f = r.fa;
+  std::memset(&f, 0, sizeof(f));
+  f.face = h->face; f.other = h->faceOther; f.faceGrad = h->faceGrad; f.faceFlux = h->faceFlux;
+  f.conn = bnd ? h->bconn : h->fconn; f.fgeo = bnd ? h->bgeo : h->fgeo; f.ghost = h->ghost;
+  f.nface = bnd ? h->nBoundary : h->nInterior; f.n1d = h->n1d; f.ph = h->ph;
+  r.units = (f.nface * h->nfq + kFaceThreads - 1) / kFaceThreads;
+  return r;
+}
+
+Rec relRec(sdg_handle* h) {
+  Rec r;
+  r.kind = kRecRelerr; r.cls = 3;
+  const KernelVariant v = relerrVariant();
+  r.fn = v.single; r.bfn = v.batch;
+  r.threads = 256; r.epb = 1; r.smem = 0; r.units = h->nv;
+  RelArgs& a = r.ra;
+  std::memset(&a, 0, sizeof(a));
+  a.part = h->relPart; a.out = h->relOut; a.inv_elements = 1.0 / double(h->elements); a.nv = h->nv;
+  a.nranges = int(h->blocks.size());
+  for (size_t b = 0; b < h->blocks.size(); ++b) { a.offset[b] = h->blocks[b].relOffset; a.count[b] = h->blocks[b].grid; }
+  return r;
 }
 
 const double kRk[3][3][3] = {{{1.0, 0.0, 1.0}, {0, 0, 0}, {0, 0, 0}},
                              {{1.0, 0.0, 1.0}, {0.5, 0.5, 0.5}, {0, 0, 0}},
                              {{1.0, 0.0, 1.0}, {0.75, 0.25, 0.25}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}}};  // TimeIntegration.cpp:45-65
 
+// Face fluxes of the state in buffer `which` (whose traces the face buffer holds): NS gradient pass first.
+void emitFluxes(sdg_handle* h, int which, int seq, std::vector<Rec>& out) {
+  const auto push = [&](Rec r, int level) { r.seq = seq + level; out.push_back(r); };
+  if (h->ns) {
+    if (h->nInterior > 0) push(faceRec(h, kOpExchange), 0);
+    if (h->nBoundary > 0) push(faceRec(h, kOpExchangeBoundary), 0);
+    for (DevBlock& B : h->blocks) push(gradRec(h, B, which), 1);
+    if (h->nInterior > 0) push(faceRec(h, kOpFaceNS), 2);
+    if (h->nBoundary > 0) push(faceRec(h, kOpFaceNSBoundary), 2);
+  } else {
+    if (h->nInterior > 0) push(faceRec(h, kOpFace), 2);
+    if (h->nBoundary > 0) push(faceRec(h, kOpFaceBoundary), 2);
+  }
+}
+
+}  // namespace
+
 // One full RK step; state[0] holds U^n on entry and U^{n+1} on exit, the face buffer holds its traces.
-void stepOnce(sdg_handle* h, double dt, bool relerr) {
+// Stage s: fluxes of its input, then per block volume + lift + update + new traces (TimeIntegration.cpp:326-350).
+void emitStep(sdg_handle* h, double dt, bool relerr, std::vector<Rec>& out) {
   const int ns = h->cfg.time_integration + 1;
   for (int s = 0; s < ns; ++s) {
-    if (h->ns) {
-      gradientPass(h, s == 0 ? 0 : 1);
-      launchFacesNS(h);
-    } else {
-      launchFaces(h);
-    }
+    emitFluxes(h, s == 0 ? 0 : 1, s * 8, out);
     const bool last = s == ns - 1;
     for (DevBlock& B : h->blocks) {
-      StageArgs a = baseArgs(h, B);
+      Rec r = stageRec(h, B);
+      StageArgs& a = r.sa;
       a.uin = h->state[s == 0 ? 0 : 1] + B.stateOffset;
       a.ubase = h->state[0] + B.stateOffset;
       a.uout = h->state[last ? 0 : 1] + B.stateOffset;
@@ -521,14 +485,103 @@ void stepOnce(sdg_handle* h, double dt, bool relerr) {
       a.c2dt = kRk[h->cfg.time_integration][s][2] * dt;
       a.doUpdate = 1; a.doTrace = 1; a.doVolume = 1;
       a.relerr = (relerr && last) ? h->relPart + B.relOffset * h->nv : nullptr;
-      launchBlock(h, B, a);
+      r.seq = s * 8 + 3;
+      out.push_back(r);
     }
   }
   if (relerr) {
-    beginLaunch(h, 3);
-    relerrReduceKernel<<<h->nv, 256, 0, h->stream>>>(h->relPart, h->relParts, h->nv, 1.0 / double(h->elements), h->relOut);
-    checkLaunch(h);
+    Rec r = relRec(h);
+    r.seq = 8 * ns;
+    out.push_back(r);
   }
+}
+
+namespace {
+
+void launchOne(const Rec& r, cudaStream_t s) {
+  void* p[2];
+  switch (r.kind) {
+    case kRecStage: p[0] = const_cast<StageArgs*>(&r.sa); p[1] = const_cast<Phys*>(&r.ph); break;
+    case kRecGradTensor: p[0] = const_cast<GradArgs*>(&r.ga); break;
+    case kRecGradDense: p[0] = const_cast<DenseGradArgs*>(&r.da); break;
+    case kRecFace: p[0] = const_cast<FaceArgs*>(&r.fa); break;
+    default: p[0] = const_cast<RelArgs*>(&r.ra); break;
+  }
+  if (r.units <= 0) return;
+  if (r.units > 0x7fffffffLL) throw Failure(SDG_ERR_UNSUPPORTED, "launch exceeds the grid limit");
+  SDG_CUDA(cudaLaunchKernel(r.fn, dim3(unsigned(r.units)), dim3(unsigned(r.threads)), p, r.smem, s));
+}
+
+}  // namespace
+
+void runRecs(sdg_handle* h, const std::vector<Rec>& recs, cudaStream_t stream) {
+  for (const Rec& r : recs) {
+    if (r.units <= 0) continue;
+    beginLaunch(h, r.cls, stream);
+    launchOne(r, stream);
+    checkLaunch(h, stream);
+  }
+}
+
+void dropGraph(sdg_handle* h) {
+  if (h->graphExec) cudaGraphExecDestroy(h->graphExec);
+  h->graphExec = nullptr;
+  h->graphKernels = 0;
+}
+
+// Face traces of state buffer `which` (initial condition or after a state upload).
+void traceAll(sdg_handle* h, int which) {
+  std::vector<Rec> recs;
+  for (DevBlock& B : h->blocks) {
+    Rec r = stageRec(h, B);
+    r.sa.uin = h->state[which] + B.stateOffset;
+    r.sa.doTrace = 1; r.sa.doVolume = 0; r.sa.doUpdate = 0;
+    recs.push_back(r);
+  }
+  runRecs(h, recs, h->stream);
+}
+
+void checkStatus(sdg_handle* h) {
+  unsigned st = 0;
+  SDG_CUDA(cudaMemcpyAsync(&st, h->status, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  if (st & kStatusTimeout) throw Failure(SDG_ERR_TIMEOUT, "a bounded device wait timed out");
+}
+
+namespace {
+
+// One step through a captured CUDA graph (re-captured when dt or the tiles change).
+void stepGraph(sdg_handle* h, double dt) {
+  if (!h->graphExec || h->graphDt != dt) {
+    dropGraph(h);
+    std::vector<Rec> recs;
+    emitStep(h, dt, true, recs);
+    cudaGraph_t graph = nullptr;
+    SDG_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      for (const Rec& r : recs) launchOne(r, h->stream);
+    } catch (...) {
+      cudaStreamEndCapture(h->stream, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    SDG_CUDA(cudaStreamEndCapture(h->stream, &graph));
+    const cudaError_t e = cudaGraphInstantiate(&h->graphExec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) { h->graphExec = nullptr; SDG_CUDA(e); }
+    h->graphDt = dt;
+    h->graphKernels = 0;
+    for (const Rec& r : recs) h->graphKernels += r.units > 0;
+  }
+  SDG_CUDA(cudaGraphLaunch(h->graphExec, h->stream));
+  h->launches += h->graphKernels;
+}
+
+void stepOnce(sdg_handle* h, double dt) {
+  if (h->useGraph && !h->timing) { stepGraph(h, dt); return; }
+  std::vector<Rec> recs;
+  emitStep(h, dt, true, recs);
+  runRecs(h, recs, h->stream);
 }
 
 int fail(sdg_handle* h, const Failure& f) {
@@ -543,12 +596,6 @@ int fail(sdg_handle* h, const Failure& f) {
   catch (const Failure& f) { return fail(h, f); }                  \
   catch (const std::exception& ex) { return fail(h, Failure(SDG_ERR_INVALID_ARGUMENT, ex.what())); }
 
-void checkStatus(sdg_handle* h) {
-  unsigned st = 0;
-  SDG_CUDA(cudaMemcpyAsync(&st, h->status, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
-  SDG_CUDA(cudaStreamSynchronize(h->stream));
-  if (st & kStatusTimeout) throw Failure(SDG_ERR_TIMEOUT, "a bounded device wait timed out");
-}
 
 // Convert a point-layout array in h->scratch to the state buffer `which` (tensor: transpose; dense:
 // unweighted least-squares projection, InitialCondition.cpp:91-104).
@@ -602,6 +649,9 @@ double measureFp64Peak(int device, double ms) {
 }
 
 }  // namespace
+}  // namespace sdg
+
+using namespace sdg;
 
 // =====================================================================================================
 #pragma GCC visibility push(default)
@@ -722,15 +772,10 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       if (B.kind == kTensor) {
         B.ops.build(B.n);
         buildTensorTables(B);
-        configureTensor(B, false, c.equation == SDG_COMPRESSIBLE_NS);
       } else {
         buildDenseTables(B.type, B.p, B.tablesHost, B.phi, B.lsq);
-        if (!configureDense(B.type, B.p, B.affine != 0, false, B.threads, B.epb, B.smem))
-          throw Failure(SDG_ERR_UNSUPPORTED, "unsupported dense block");
-        B.ustride = (h->nv * B.nb + 1) & ~1;
-        B.fstride = B.nface * h->nv * B.nfq;
       }
-      B.grid = int((B.ne + B.epb - 1) / B.epb);
+      resolveBlock(B, c.equation == SDG_COMPRESSIBLE_NS);
       B.stateOffset = stateOff; stateOff += size_t(B.ne) * B.ustride;
       B.gradOffset = h->gradCount; h->gradCount += size_t(B.ne) * h->nv * B.dim * B.nb;
       if (!B.affine || B.kind == kDense) {  // outward n|J_f| of each local face (straight faces: constant)
@@ -750,12 +795,13 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       }
       B.pointOffset = pointOff; pointOff += size_t(B.ne) * B.nq;
       B.faceBase = faceSlots; faceSlots += B.ne * B.nface;
-      B.relOffset = relParts; relParts += B.grid;
+      B.relOffset = relParts; relParts += B.ne;  // room for the smallest tile (one element per CTA)
       h->elements += B.ne;
       h->dof += B.ne * B.nb * h->nv;
       h->blocks.push_back(std::move(B));
     }
     h->nfq = h->blocks[0].nfq; h->n1d = h->p + 1;
+    for (int op = 0; op < 6; ++op) h->faceV[op] = facePointVariant(op, h->dim, c.convective_flux);
     h->volumePoints = int64_t(pointOff);
     h->stateCount = stateOff;
     h->faceCount = size_t(faceSlots) * h->nv * h->nfq;
@@ -841,10 +887,12 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     h->hostOnly = false;
     SDG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     for (DevBlock& B : h->blocks) {
-      if (B.kind == kTensor) configureTensor(B, true, h->ns);
-      else if (!configureDense(B.type, B.p, B.affine != 0, true, B.threads, B.epb, B.smem))
-        throw Failure(SDG_ERR_CUDA, "cannot configure the dense kernel");
+      for (const KernelVariant* v : {&B.stageV[0], &B.stageV[1], &B.gradV}) {
+        configureKernel(v->single, device);
+        configureKernel(v->batch, device);
+      }
     }
+    for (const KernelVariant& v : h->faceV) { configureKernel(v.single, device); configureKernel(v.batch, device); }
     // device buffers
     h->state[0] = devAlloc<double>(h->stateCount);
     h->state[1] = devAlloc<double>(h->stateCount);
@@ -906,6 +954,7 @@ int sdg_destroy(sdg_handle* h) {
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
   dropTimingEvents(h);
+  dropGraph(h);
   for (DevBlock& B : h->blocks) {
     cudaFree(B.geom); cudaFree(B.tables); cudaFree(B.minedge); cudaFree(B.phiDev); cudaFree(B.lsqDev); cudaFree(B.fmetric);
   }
@@ -1110,7 +1159,7 @@ int sdg_step_async(sdg_handle* h, int32_t steps, double dt) {
   if (!h->hasState) { h->err = "step before an initial state"; return SDG_ERR_STATE; }
   SDG_API_BEGIN
   SDG_CUDA(cudaSetDevice(h->device));
-  for (int s = 0; s < steps; ++s) stepOnce(h, dt, true);  // relative error every step, as stepSolver does
+  for (int s = 0; s < steps; ++s) stepOnce(h, dt);  // relative error every step, as stepSolver does
   return SDG_OK;
   SDG_API_END(h)
 }
@@ -1146,19 +1195,16 @@ int sdg_residual_point(sdg_handle* h, double* rate) {
   SDG_CUDA(cudaSetDevice(h->device));
   // the face buffer holds the traces of state[0]: compute fluxes, then the rate without an update,
   // then restore the traces (the flux pass overwrote them)
-  if (h->ns) {
-    gradientPass(h, 0);
-    launchFacesNS(h);
-  } else {
-    launchFaces(h);
-  }
+  std::vector<Rec> recs;
+  emitFluxes(h, 0, 0, recs);
   for (DevBlock& B : h->blocks) {
-    StageArgs a = baseArgs(h, B);
-    a.uin = h->state[0] + B.stateOffset;
-    a.rate = h->scratch + B.pointOffset * h->nv;
-    a.doVolume = 1; a.doUpdate = 0; a.doTrace = 0;
-    launchBlock(h, B, a);
+    Rec r = stageRec(h, B);
+    r.sa.uin = h->state[0] + B.stateOffset;
+    r.sa.rate = h->scratch + B.pointOffset * h->nv;
+    r.sa.doVolume = 1; r.sa.doUpdate = 0; r.sa.doTrace = 0;
+    recs.push_back(r);
   }
+  runRecs(h, recs, h->stream);
   SDG_CUDA(cudaMemcpyAsync(rate, h->scratch, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
   traceAll(h, 0);
   checkStatus(h);
@@ -1194,6 +1240,7 @@ int sdg_set_kernel_timing(sdg_handle* h, int32_t enable) {
   SDG_CUDA(cudaSetDevice(h->device));
   SDG_CUDA(cudaStreamSynchronize(h->stream));
   dropTimingEvents(h);
+  dropGraph(h);
   h->timing = enable != 0;
   return SDG_OK;
   SDG_API_END(h)

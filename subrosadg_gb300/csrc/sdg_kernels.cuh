@@ -43,6 +43,8 @@ __device__ __forceinline__ void bulkLoad(void* dst, const void* src, uint32_t by
       "l"(src), "r"(bytes), "r"(smemAddr(bar))
       : "memory");
 }
+// Orders this thread's earlier generic-proxy accesses of shared memory before later bulk copies into it.
+__device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 // Bounded wait on phase `parity`; returns false (and the caller flags a timeout) if it never completes.
 __device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity) {
   for (uint32_t it = 0; it < kWaitLimit; ++it) {
@@ -89,6 +91,7 @@ struct StageArgs {
   int doVolume;           // evaluate the residual (0: trace-only pass)
   const double* fluxSrc;  // face-flux slots to lift (null: the face buffer itself, the Euler layout)
   const double* grad;     // Navier-Stokes: total gradient at the nodes [e][nv*d][NB]
+  int epb;                // elements per CTA tile (tile t covers elements [t*epb, t*epb + epb))
 };
 
 template <int DIM, int N>
@@ -106,7 +109,14 @@ struct TensorShape {
   static constexpr int EPB = EPB_RAW < EPB_SMEM ? EPB_RAW : EPB_SMEM;
   static constexpr int THREADS = ((EPB * NB + 31) / 32) * 32;
   static constexpr size_t SMEM = size_t(EPB) * SMEM_PER_ELEM + sizeof(TensorTables) + 16 + 8 * NV * (THREADS / 32);
+  // any tile size: one thread per node, rounded up to whole warps
+  static constexpr int threadsFor(int epb) { return ((epb * NB + 31) / 32) * 32; }
+  static constexpr size_t smemFor(int epb) {
+    return size_t(epb) * SMEM_PER_ELEM + sizeof(TensorTables) + 16 + 8 * NV * size_t(threadsFor(epb) / 32);
+  }
 };
+
+constexpr int kMaxTileThreads = 512;
 
 // Index of node i along axis a.
 template <int DIM, int N>
@@ -121,45 +131,62 @@ __device__ __forceinline__ int strideOf(int a) {
   else return a == 0 ? N * N : (a == 1 ? N : 1);
 }
 
-// Tensor-block stage kernel: one thread per node, EPB elements per CTA.
+// Tensor-block stage tile: one thread per node, a.epb elements per CTA.  Shared memory (dynamic):
+// sU [epb][USTRIDE] | sF [epb][FSTRIDE] | sG [epb][DIM][NV][NB] | TensorTables | mbarrier | sRed [warps][NV].
+template <int DIM, int N>
+__device__ __forceinline__ uint64_t* tensorStageBarrier(int epb) {
+  using S = TensorShape<DIM, N>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* sG = reinterpret_cast<double*>(smem_raw) + epb * (S::USTRIDE + S::FSTRIDE);
+  return reinterpret_cast<uint64_t*>(reinterpret_cast<TensorTables*>(sG + epb * DIM * S::NV * S::NB) + 1);
+}
+
+// One tile of a stage: the CTA's mbarrier is initialised, `parity` is the phase this tile's copies complete;
+// `loadTables` copies the operator tables (identical for every tile of a (type, order) variant).  Returns
+// false after a timed-out copy (status flagged, every thread returns together).
 template <int DIM, int N, bool AFFINE, bool VISC>
-__global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS)
-    tensorStageKernel(StageArgs a, Phys ph) {
+__device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& ph, int64_t tile, uint32_t parity,
+                                                bool loadTables) {
   using S = TensorShape<DIM, N>;
   constexpr int NV = S::NV, NB = S::NB, NF = S::NF, NFQ = S::NFQ;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  double* sU = reinterpret_cast<double*>(smem_raw);                 // [EPB][USTRIDE]
-  double* sF = sU + S::EPB * S::USTRIDE;                            // [EPB][FSTRIDE]
-  double* sG = sF + S::EPB * S::FSTRIDE;                            // [EPB][DIM][NV][NB]
-  TensorTables* T = reinterpret_cast<TensorTables*>(sG + S::EPB * DIM * NV * NB);
+  const int epb = a.epb;
+  double* sU = reinterpret_cast<double*>(smem_raw);                 // [epb][USTRIDE]
+  double* sF = sU + epb * S::USTRIDE;                               // [epb][FSTRIDE]
+  double* sG = sF + epb * S::FSTRIDE;                               // [epb][DIM][NV][NB]
+  TensorTables* T = reinterpret_cast<TensorTables*>(sG + epb * DIM * NV * NB);
   uint64_t* bar = reinterpret_cast<uint64_t*>(T + 1);
   double* sRed = reinterpret_cast<double*>(bar + 1);                // [warps][NV]
 
   const int tid = threadIdx.x;
-  const int64_t e0 = int64_t(blockIdx.x) * S::EPB;
-  const int ecount = int(a.ne - e0 < S::EPB ? a.ne - e0 : S::EPB);
+  const int64_t e0 = tile * epb;
+  const int ecount = int(a.ne - e0 < epb ? a.ne - e0 : epb);
   const int le = tid / NB, node = tid - le * NB;
   const bool active = le < ecount;
   const int64_t e = e0 + le;
 
+  __syncthreads();  // the previous tile's readers of sU/sF are done
   // 1. stage the element tile (state + face slots) into shared memory with TMA bulk copies
   if (tid == 0) {
-    mbarInit(bar, 1);
+    fenceProxyAsync();
     const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * S::FSTRIDE * 8;
     mbarExpectTx(bar, a.doVolume ? ub + fb : ub);
     bulkLoad(sU, a.uin + e0 * S::USTRIDE, ub, bar);
     if (a.doVolume) bulkLoad(sF, (a.fluxSrc ? a.fluxSrc : a.face) + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
-  {
+  if (loadTables) {
     const double* src = a.tables;
     double* dst = reinterpret_cast<double*>(T);
     for (int k = tid; k < int(sizeof(TensorTables) / 8); k += blockDim.x) dst[k] = src[k];
   }
   __syncthreads();
-  const bool arrived = mbarWait(bar, 0);
+  const bool arrived = mbarWait(bar, parity);
   if (__syncthreads_or(!arrived)) {  // uniform decision: every thread leaves together
-    if (tid == 0) atomicOr(a.status, kStatusTimeout);
-    return;
+    if (tid == 0) {
+      atomicOr(a.status, kStatusTimeout);
+      mbarWait(bar, parity);  // bounded: let copies still in flight land before the CTA exits
+    }
+    return false;
   }
 
   double du[NV];
@@ -312,7 +339,7 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS)
       if (tid < NV) {
         double acc = 0.0;
         for (int w = 0; w < nwarp; ++w) acc += sRed[w * NV + tid];
-        a.relerr[int64_t(blockIdx.x) * NV + tid] = acc / double(NB);
+        a.relerr[tile * NV + tid] = acc / double(NB);
       }
     }
     if (a.doUpdate && active) {
@@ -345,23 +372,59 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS)
       }
     }
   }
+  return true;
 }
 
-// Interior-face Riemann flux: one thread per face point.  Left slot gets +|J_f| h, right slot gets
-// -|J_f| h at the permuted point (SpatialDiscrete.cpp:633-748).
-template <int DIM, int FLUX>
-__global__ void __launch_bounds__(256) faceKernel(double* __restrict__ face, const int* __restrict__ conn,
-                                                  const double* __restrict__ fgeo, int64_t nface, int n1d, Phys ph) {
-  constexpr int NV = DIM + 2;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const int64_t f = t / nfq;
-  if (f >= nface) return;
-  const int j = int(t - f * nfq);
-  const int sl = conn[f * 3 + 0], sr = conn[f * 3 + 1], rot = conn[f * 3 + 2];
-  int jr;
+// One CTA per tile.
+template <int DIM, int N, bool AFFINE, bool VISC>
+__global__ void __launch_bounds__(kMaxTileThreads) tensorStageKernel(StageArgs a, Phys ph) {
+  if (threadIdx.x == 0) mbarInit(tensorStageBarrier<DIM, N>(a.epb), 1);
+  tensorStageTile<DIM, N, AFFINE, VISC>(a, ph, blockIdx.x, 0u, true);
+}
+
+// Persistent batched launch: CTA c runs work items c, c + gridDim.x, ... of a list of (argument set, tile)
+// pairs that spans many independent instances of one (type, order) variant.  The barrier is initialised
+// once and its phase alternates per tile; the tables are loaded once per CTA.
+template <int DIM, int N, bool AFFINE, bool VISC>
+__global__ void __launch_bounds__(kMaxTileThreads)
+    tensorStageBatchKernel(const StageArgs* __restrict__ args, const Phys* __restrict__ phys,
+                           const int2* __restrict__ items, int nitems, int epb) {
+  if (threadIdx.x == 0) mbarInit(tensorStageBarrier<DIM, N>(epb), 1);
+  uint32_t parity = 0;
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const int2 it = items[w];
+    const StageArgs a = args[it.x];
+    const Phys ph = phys[it.x];
+    if (!tensorStageTile<DIM, N, AFFINE, VISC>(a, ph, it.y, parity, w == int(blockIdx.x))) return;
+    parity ^= 1u;
+  }
+}
+
+// ---- face-point operations -----------------------------------------------------------------------
+// One thread per face point; the same argument block serves the one-instance kernels and the batched
+// persistent kernels.  Slot layout: see the file header.
+struct FaceArgs {
+  double* face;              // traces (the Euler flux operations overwrite them with |J_f| h)
+  double* other;             // Navier-Stokes: neighbour traces
+  const double* faceGrad;    // Navier-Stokes: gradient traces [slot][v*d+k][j]
+  double* faceFlux;          // Navier-Stokes: face fluxes
+  const int* conn;           // interior: (slot L, slot R, rotation); boundary: (slot, condition, 0)
+  const double* fgeo;        // per face (n, |J_f|)
+  const double* ghost;       // boundary: [face][j][rho, u, e, p]
+  int64_t nface;
+  int n1d, pad;
+  Phys ph;
+};
+
+enum FaceOp { kOpFace = 0, kOpFaceBoundary = 1, kOpExchange = 2, kOpExchangeBoundary = 3, kOpFaceNS = 4,
+              kOpFaceNSBoundary = 5 };
+
+// Point of the right face that coincides with point j of the left face (rotation of the right face's
+// vertex list; SimulationControl.cpp:381-523 permutations).
+template <int DIM>
+__device__ __forceinline__ int rightPoint(int j, int rot, int n1d) {
   if constexpr (DIM == 2) {
-    jr = n1d - 1 - j;
+    return n1d - 1 - j;
   } else {
     const int i = j / n1d, k = j - i * n1d;
     int ii, kk;
@@ -371,22 +434,36 @@ __global__ void __launch_bounds__(256) faceKernel(double* __restrict__ face, con
       case 2: ii = n1d - 1 - k; kk = n1d - 1 - i; break;
       default: ii = i; kk = n1d - 1 - k; break;
     }
-    jr = ii * n1d + kk;
+    return ii * n1d + kk;
   }
-  double* L = face + int64_t(sl) * NV * nfq + j;
-  double* R = face + int64_t(sr) * NV * nfq + jr;
+}
+
+// Interior-face Riemann flux.  Left slot gets +|J_f| h, right slot gets -|J_f| h at the permuted point
+// (SpatialDiscrete.cpp:633-748).
+template <int DIM, int FLUX>
+__device__ __forceinline__ void faceInteriorPoint(const FaceArgs& a, int64_t t) {
+  constexpr int NV = DIM + 2;
+  const int n1d = a.n1d;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
+  const int jr = rightPoint<DIM>(j, rot, n1d);
+  double* L = a.face + int64_t(sl) * NV * nfq + j;
+  double* R = a.face + int64_t(sr) * NV * nfq + jr;
   double ul[NV], ur[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) { ul[v] = L[v * nfq]; ur[v] = R[v * nfq]; }
   double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
-  const double area = fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double area = a.fgeo[f * 4 + 3];
   State<DIM> l, r;
-  makeState<DIM>(l, ul, ph);
-  makeState<DIM>(r, ur, ph);
+  makeState<DIM>(l, ul, a.ph);
+  makeState<DIM>(r, ur, a.ph);
   double h[NV];
-  convectiveFlux<DIM, FLUX>(l, r, n, ph, h);
+  convectiveFlux<DIM, FLUX>(l, r, n, a.ph, h);
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
     const double x = h[v] * area;
@@ -396,58 +473,48 @@ __global__ void __launch_bounds__(256) faceKernel(double* __restrict__ face, con
 }
 
 // Boundary-face flux: ghost state from the boundary condition, normal flux of the boundary state
-// (SpatialDiscrete.cpp:750-842).  ghost = [face][j][comp] computational (rho, u, e, p).
+// (SpatialDiscrete.cpp:750-842).
 template <int DIM>
-__global__ void __launch_bounds__(256) boundaryFaceKernel(double* __restrict__ face, const int* __restrict__ conn,
-                                                          const double* __restrict__ fgeo,
-                                                          const double* __restrict__ ghost, int64_t nface, int n1d,
-                                                          Phys ph) {
+__device__ __forceinline__ void faceBoundaryPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
+  const int n1d = a.n1d;
   const int nfq = DIM == 2 ? n1d : n1d * n1d;
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
-  if (f >= nface) return;
+  if (f >= a.nface) return;
   const int j = int(t - f * nfq);
-  const int sl = conn[f * 3 + 0], bc = conn[f * 3 + 1];
-  double* L = face + int64_t(sl) * NV * nfq + j;
+  const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
+  double* L = a.face + int64_t(sl) * NV * nfq + j;
   double ul[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) ul[v] = L[v * nfq];
   double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
-  const double area = fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double area = a.fgeo[f * 4 + 3];
   State<DIM> s;
-  makeState<DIM>(s, ul, ph);
+  makeState<DIM>(s, ul, a.ph);
   Comp<DIM> l, g, b;
   compFromState<DIM>(s, l);
-  const double* gp = ghost + (f * nfq + j) * (DIM + 3);
+  const double* gp = a.ghost + (f * nfq + j) * (DIM + 3);
   g.r = gp[0];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) g.u[k] = gp[1 + k];
   g.e = gp[DIM + 1];
   g.p = gp[DIM + 2];
-  boundaryState<DIM>(bc, n, l, g, ph, b);
+  boundaryState<DIM>(bc, n, l, g, a.ph, b);
   double h[NV];
   normalFluxComp<DIM>(b, n, h);
 #pragma unroll
   for (int v = 0; v < NV; ++v) L[v * nfq] = h[v] * area;
 }
 
-// Deterministic final reduction of per-CTA relative-error partials: out[v] = sum / elements.
-__global__ void relerrReduceKernel(const double* __restrict__ part, int64_t nparts, int nv, double inv_elements,
-                                   double* __restrict__ out) {
-  __shared__ double sh[256];
-  const int v = blockIdx.x;
-  double acc = 0.0;
-  for (int64_t i = threadIdx.x; i < nparts; i += blockDim.x) acc += part[i * nv + v];
-  sh[threadIdx.x] = acc;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) out[v] = sh[0] * inv_elements;
-}
+// Deterministic final reduction of per-tile relative-error partials: out[v] = sum / elements.
+struct RelArgs {
+  const double* part;        // [slot][nv]
+  int64_t offset[2], count[2];  // used slot ranges (one per element block)
+  double* out;
+  double inv_elements;
+  int nranges, nv;
+};
 
 }  // namespace sdg

@@ -102,15 +102,27 @@ struct DenseShape {
   static constexpr int THREADS = 256;
   static constexpr size_t TABLES = size_t(NQ) * NB * 3 + size_t(NFP) * NB * 2 + size_t(NB) * NB;
   static constexpr size_t SMEM = (size_t(EPB) * PER_ELEM + TABLES) * 8 + 16 + 8 * NV * (THREADS / 32);
+  static constexpr size_t smemFor(int epb, int threads) {
+    return (size_t(epb) * PER_ELEM + TABLES) * 8 + 16 + 8 * NV * size_t(threads / 32);
+  }
 };
 
-// Dense stage kernel (2D).  geometry: affine [e][5] = (|J| dxi_b/dx_a row-major, 1/|J|);
-// bilinear: [e][NQ][5] followed by the element's M^-1 [NB][NB].
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
-__global__ void __launch_bounds__(256) denseStageKernel(StageArgs a, Phys ph) {
+template <int NB, int NQ, int NFQ, int NF>
+__device__ __forceinline__ uint64_t* denseStageBarrier(int epb) {
   using S = DenseShape<NB, NQ, NFQ, NF>;
-  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB;
   extern __shared__ __align__(128) unsigned char smem_raw[];
+  return reinterpret_cast<uint64_t*>(reinterpret_cast<double*>(smem_raw) + epb * S::PER_ELEM + S::TABLES);
+}
+
+// Dense stage tile (2D), a.epb elements per CTA, any whole number of warps.  geometry: affine [e][5] =
+// (|J| dxi_b/dx_a row-major, 1/|J|); bilinear: [e][NQ][5] followed by the element's M^-1 [NB][NB].
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
+__device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& ph, int64_t tile, uint32_t parity,
+                                               bool loadTables) {
+  using S = DenseShape<NB, NQ, NFQ, NF>;
+  constexpr int NV = 4, NFP = S::NFP;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int EPB = a.epb;
   double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE]
   double* sF = sU + EPB * S::USTRIDE;                // [EPB][FSTRIDE]
   double* sQ = sF + EPB * S::FSTRIDE;                // [EPB][2][NV][NQ]
@@ -127,21 +139,26 @@ __global__ void __launch_bounds__(256) denseStageKernel(StageArgs a, Phys ph) {
   const int GS = AFFINE ? 5 : NQ * 5 + NB * NB;
 
   const int tid = threadIdx.x;
-  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int64_t e0 = tile * EPB;
   const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  __syncthreads();
   if (tid == 0) {
-    mbarInit(bar, 1);
+    fenceProxyAsync();
     const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * S::FSTRIDE * 8;
     mbarExpectTx(bar, a.doVolume ? ub + fb : ub);
     bulkLoad(sU, a.uin + e0 * S::USTRIDE, ub, bar);
     if (a.doVolume) bulkLoad(sF, (a.fluxSrc ? a.fluxSrc : a.face) + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
-  for (int k = tid; k < int(S::TABLES); k += blockDim.x) tab[k] = a.tables[k];
+  if (loadTables)
+    for (int k = tid; k < int(S::TABLES); k += blockDim.x) tab[k] = a.tables[k];
   __syncthreads();
-  const bool arrived = mbarWait(bar, 0);
+  const bool arrived = mbarWait(bar, parity);
   if (__syncthreads_or(!arrived)) {
-    if (tid == 0) atomicOr(a.status, kStatusTimeout);
-    return;
+    if (tid == 0) {
+      atomicOr(a.status, kStatusTimeout);
+      mbarWait(bar, parity);
+    }
+    return false;
   }
   if (a.doVolume) {
     // values and contravariant fluxes at the volume points
@@ -268,7 +285,7 @@ __global__ void __launch_bounds__(256) denseStageKernel(StageArgs a, Phys ph) {
       if (tid < NV) {
         double s = 0.0;
         for (int w = 0; w < nwarp; ++w) s += sRed[w * NV + tid];
-        a.relerr[int64_t(blockIdx.x) * NV + tid] = s / double(NQ);
+        a.relerr[tile * NV + tid] = s / double(NQ);
       }
     }
     __syncthreads();
@@ -293,6 +310,28 @@ __global__ void __launch_bounds__(256) denseStageKernel(StageArgs a, Phys ph) {
       }
     }
   }
+  return true;
+}
+
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
+__global__ void __launch_bounds__(kMaxTileThreads) denseStageKernel(StageArgs a, Phys ph) {
+  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF>(a.epb), 1);
+  denseStageTile<NB, NQ, NFQ, NF, AFFINE, VISC>(a, ph, blockIdx.x, 0u, true);
+}
+
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
+__global__ void __launch_bounds__(kMaxTileThreads)
+    denseStageBatchKernel(const StageArgs* __restrict__ args, const Phys* __restrict__ phys,
+                          const int2* __restrict__ items, int nitems, int epb) {
+  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF>(epb), 1);
+  uint32_t parity = 0;
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const int2 it = items[w];
+    const StageArgs a = args[it.x];
+    const Phys ph = phys[it.x];
+    if (!denseStageTile<NB, NQ, NFQ, NF, AFFINE, VISC>(a, ph, it.y, parity, w == int(blockIdx.x))) return;
+    parity ^= 1u;
+  }
 }
 
 
@@ -309,7 +348,15 @@ struct DenseGradShape {
   static constexpr int PER_ELEM = USTRIDE + 2 * FS + NV * NQ + 3 * NV * 2 * NB;
   static constexpr size_t TABLES = size_t(NQ) * NB * 3 + size_t(NFP) * NB * 2 + size_t(NB) * NB;
   static constexpr size_t SMEM = (size_t(EPB) * PER_ELEM + TABLES) * 8 + 16;
+  static constexpr size_t smemFor(int epb) { return (size_t(epb) * PER_ELEM + TABLES) * 8 + 16; }
 };
+
+template <int NB, int NQ, int NFQ, int NF>
+__device__ __forceinline__ uint64_t* denseGradBarrier(int epb) {
+  using G = DenseGradShape<NB, NQ, NFQ, NF>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  return reinterpret_cast<uint64_t*>(reinterpret_cast<double*>(smem_raw) + epb * G::PER_ELEM + G::TABLES);
+}
 
 struct DenseGradArgs {
   const double* u;
@@ -323,12 +370,14 @@ struct DenseGradArgs {
   unsigned* status;
   int64_t ne, faceBase;
   int br2;
+  int epb;
 };
 
 template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
-__global__ void __launch_bounds__(256) denseGradientKernel(DenseGradArgs a) {
+__device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_t tile, uint32_t parity, bool loadTables) {
   using G = DenseGradShape<NB, NQ, NFQ, NF>;
-  constexpr int NV = 4, NFP = G::NFP, EPB = G::EPB, FS = G::FS, NR = NV * 2;
+  constexpr int NV = 4, NFP = G::NFP, FS = G::FS, NR = NV * 2;
+  const int EPB = a.epb;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE] modal coefficients
   double* sS = sU + EPB * G::USTRIDE;                // own traces [EPB][FS]
@@ -347,22 +396,27 @@ __global__ void __launch_bounds__(256) denseGradientKernel(DenseGradArgs a) {
   const int GS = AFFINE ? 5 : NQ * 5 + NB * NB;
 
   const int tid = threadIdx.x;
-  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int64_t e0 = tile * EPB;
   const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  __syncthreads();
   if (tid == 0) {
-    mbarInit(bar, 1);
+    fenceProxyAsync();
     const uint32_t ub = uint32_t(ecount) * G::USTRIDE * 8, fb = uint32_t(ecount) * FS * 8;
     mbarExpectTx(bar, ub + 2 * fb);
     bulkLoad(sU, a.u + e0 * G::USTRIDE, ub, bar);
     bulkLoad(sS, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
     bulkLoad(sO, a.faceOther + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
-  for (int k = tid; k < int(G::TABLES); k += blockDim.x) tab[k] = a.tables[k];
+  if (loadTables)
+    for (int k = tid; k < int(G::TABLES); k += blockDim.x) tab[k] = a.tables[k];
   __syncthreads();
-  const bool arrived = mbarWait(bar, 0);
+  const bool arrived = mbarWait(bar, parity);
   if (__syncthreads_or(!arrived)) {
-    if (tid == 0) atomicOr(a.status, kStatusTimeout);
-    return;
+    if (tid == 0) {
+      atomicOr(a.status, kStatusTimeout);
+      mbarWait(bar, parity);
+    }
+    return false;
   }
   // values at the volume points
   for (int idx = tid; idx < ecount * NV * NQ; idx += blockDim.x) {
@@ -444,7 +498,7 @@ __global__ void __launch_bounds__(256) denseGradientKernel(DenseGradArgs a) {
         out[c * NFQ] = acc;
       }
     }
-    return;
+    return true;
   }
   // BR2: for each face f, trace of (volume gradient + r_f), r_f = M^-1 sum_{j in f} wf_j nF_f 1/2[U] phi
   for (int f = 0; f < NF; ++f) {
@@ -487,20 +541,26 @@ __global__ void __launch_bounds__(256) denseGradientKernel(DenseGradArgs a) {
     }
     __syncthreads();
   }
+  return true;
 }
 
-template <int NB, int NQ, int NFQ, int NF, bool AFF>
-inline bool denseCfg(bool device, int& threads, int& epb, size_t& smem) {
-  using S = DenseShape<NB, NQ, NFQ, NF>;
-  threads = S::THREADS; epb = S::EPB; smem = S::SMEM;
-  if (!device) return true;
-  using G = DenseGradShape<NB, NQ, NFQ, NF>;
-  return cudaFuncSetAttribute(denseStageKernel<NB, NQ, NFQ, NF, AFF, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              int(S::SMEM)) == cudaSuccess &&
-         cudaFuncSetAttribute(denseStageKernel<NB, NQ, NFQ, NF, AFF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              int(S::SMEM)) == cudaSuccess &&
-         cudaFuncSetAttribute(denseGradientKernel<NB, NQ, NFQ, NF, AFF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              int(G::SMEM)) == cudaSuccess;
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+__global__ void __launch_bounds__(kMaxTileThreads) denseGradientKernel(DenseGradArgs a) {
+  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF>(a.epb), 1);
+  denseGradientTile<NB, NQ, NFQ, NF, AFFINE>(a, blockIdx.x, 0u, true);
+}
+
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+__global__ void __launch_bounds__(kMaxTileThreads)
+    denseGradientBatchKernel(const DenseGradArgs* __restrict__ args, const int2* __restrict__ items, int nitems, int epb) {
+  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF>(epb), 1);
+  uint32_t parity = 0;
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const int2 it = items[w];
+    const DenseGradArgs a = args[it.x];
+    if (!denseGradientTile<NB, NQ, NFQ, NF, AFFINE>(a, it.y, parity, w == int(blockIdx.x))) return;
+    parity ^= 1u;
+  }
 }
 
 // (type, P) -> (NB, NQ, NFQ): triangle P1..P5 use Dunavant rules of 3,6,12,16,25 points.
@@ -512,106 +572,5 @@ inline bool denseCfg(bool device, int& threads, int& epb, size_t& smem) {
   X(SDG_ELEMENT_TRIANGLE, 5, 21, 25, 6, 3, true)            \
   X(SDG_ELEMENT_QUADRANGLE, 1, 4, 7, 2, 4, true)            \
   X(SDG_ELEMENT_QUADRANGLE, 1, 4, 7, 2, 4, false)
-
-inline bool launchDenseGradient(int type, int p, bool affine, const DenseGradArgs& a, cudaStream_t s) {
-#define SDG_DG(T, P, NB, NQ, NFQ, NF, AFF)                                                          \
-  if (type == T && p == P && affine == AFF) {                                                       \
-    using G = DenseGradShape<NB, NQ, NFQ, NF>;                                                      \
-    const int grid = int((a.ne + G::EPB - 1) / G::EPB);                                            \
-    denseGradientKernel<NB, NQ, NFQ, NF, AFF><<<grid, G::THREADS, G::SMEM, s>>>(a);                 \
-    return true;                                                                                    \
-  }
-  SDG_DENSE_CASES(SDG_DG)
-#undef SDG_DG
-  return false;
-}
-
-inline bool configureDense(int type, int p, bool affine, bool device, int& threads, int& epb, size_t& smem) {
-#define SDG_DC(T, P, NB, NQ, NFQ, NF, AFF) \
-  if (type == T && p == P && affine == AFF) return denseCfg<NB, NQ, NFQ, NF, AFF>(device, threads, epb, smem);
-  SDG_DENSE_CASES(SDG_DC)
-#undef SDG_DC
-  return false;
-}
-
-inline bool launchDenseStage(int type, int p, bool affine, const StageArgs& a, const Phys& ph, int grid, int threads,
-                             size_t smem, cudaStream_t s) {
-#define SDG_DL(T, P, NB, NQ, NFQ, NF, AFF)                                                  \
-  if (type == T && p == P && affine == AFF) {                                               \
-    if (a.grad) denseStageKernel<NB, NQ, NFQ, NF, AFF, true><<<grid, threads, smem, s>>>(a, ph); \
-    else denseStageKernel<NB, NQ, NFQ, NF, AFF, false><<<grid, threads, smem, s>>>(a, ph);  \
-    return true;                                                                            \
-  }
-  SDG_DENSE_CASES(SDG_DL)
-#undef SDG_DL
-  return false;
-}
-
-// ---- point-layout conversions ----------------------------------------------------------------------
-// state[e][v][b] (padded stride) <- points[e][q][v]; proj = null for tensor blocks (nodes are points),
-// else the least-squares projection [nb][nq].
-__global__ void pointToStateKernel(const double* __restrict__ pts, double* __restrict__ st,
-                                   const double* __restrict__ proj, int64_t ne, int nb, int nq, int nv, int ustride) {
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= ne * nb) return;
-  const int64_t e = t / nb;
-  const int b = int(t - e * nb);
-  for (int v = 0; v < nv; ++v) {
-    double s;
-    if (!proj) s = pts[(e * nq + b) * nv + v];
-    else { s = 0.0; for (int q = 0; q < nq; ++q) s = fma(proj[b * nq + q], pts[(e * nq + q) * nv + v], s); }
-    st[e * ustride + v * nb + b] = s;
-  }
-}
-
-__global__ void stateToPointKernel(const double* __restrict__ st, double* __restrict__ pts,
-                                   const double* __restrict__ phi, int64_t ne, int nb, int nq, int nv, int ustride) {
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= ne * nq) return;
-  const int64_t e = t / nq;
-  const int q = int(t - e * nq);
-  for (int v = 0; v < nv; ++v) {
-    double s;
-    if (!phi) s = st[e * ustride + v * nb + q];
-    else { s = 0.0; for (int b = 0; b < nb; ++b) s = fma(phi[q * nb + b], st[e * ustride + v * nb + b], s); }
-    pts[(e * nq + q) * nv + v] = s;
-  }
-}
-
-// (rho, u, T) -> (rho, rho u, rho E) in place (VariableConvertor.cpp:341-366).
-__global__ void primitiveToConservedKernel(double* __restrict__ pts, int64_t n, int dim, Phys ph) {
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (t >= n) return;
-  double* p = pts + t * (dim + 2);
-  const double rho = p[0];
-  double u2 = 0.0;
-  for (int k = 0; k < dim; ++k) { u2 += p[1 + k] * p[1 + k]; p[1 + k] *= rho; }
-  p[dim + 1] = rho * (ph.cv * p[dim + 1] + u2 / 2.0);
-}
-
-// dt = min CFL*minEdge/((|u|+c)(P+1)^2) over points (TimeIntegration.cpp:104-131); per-CTA minima.
-__global__ void deltaTimeKernel(const double* __restrict__ pts, const double* __restrict__ minEdge, int64_t n, int nq,
-                                int dim, double cfl, double p1sq, Phys ph, double* __restrict__ part) {
-  __shared__ double sh[256];
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  double dt = 1.79769313486231570e308;
-  if (t < n) {
-    const double* p = pts + t * (dim + 2);
-    const double rho = p[0];
-    double u2 = 0.0;
-    for (int k = 0; k < dim; ++k) { const double u = p[1 + k] / rho; u2 += u * u; }
-    const double e = p[dim + 1] / rho - u2 / 2.0;
-    const double pr = ph.gm1 * rho * e;
-    const double c = sqrt(ph.gamma * pr / rho);
-    dt = cfl * minEdge[t / nq] / ((sqrt(u2) + c) * p1sq);
-  }
-  sh[threadIdx.x] = dt;
-  __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) sh[threadIdx.x] = fmin(sh[threadIdx.x], sh[threadIdx.x + s]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
-}
 
 }  // namespace sdg

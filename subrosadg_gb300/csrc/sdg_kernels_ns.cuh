@@ -33,39 +33,26 @@ struct GradArgs {
   unsigned* status;
   int64_t ne, faceBase;
   int br2;
+  int epb;                  // elements per CTA tile
 };
 
 // Exchange of traces across interior faces: each side receives the other side's trace at its own points.
 template <int DIM>
-__global__ void __launch_bounds__(256) exchangeKernel(const double* __restrict__ face, double* __restrict__ other,
-                                                      const int* __restrict__ conn, int64_t nface, int n1d) {
+__device__ __forceinline__ void exchangePoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
+  const int n1d = a.n1d;
   const int nfq = DIM == 2 ? n1d : n1d * n1d;
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
-  if (f >= nface) return;
+  if (f >= a.nface) return;
   const int j = int(t - f * nfq);
-  const int sl = conn[f * 3 + 0], sr = conn[f * 3 + 1], rot = conn[f * 3 + 2];
-  int jr;
-  if constexpr (DIM == 2) {
-    jr = n1d - 1 - j;
-  } else {
-    const int i = j / n1d, k = j - i * n1d;
-    int ii, kk;
-    switch (rot) {
-      case 0: ii = k; kk = i; break;
-      case 1: ii = n1d - 1 - i; kk = k; break;
-      case 2: ii = n1d - 1 - k; kk = n1d - 1 - i; break;
-      default: ii = i; kk = n1d - 1 - k; break;
-    }
-    jr = ii * n1d + kk;
-  }
+  const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
+  const int jr = rightPoint<DIM>(j, rot, n1d);
   const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
-    const double a = face[L + v * nfq], b = face[R + v * nfq];
-    other[L + v * nfq] = b;
-    other[R + v * nfq] = a;
+    const double x = a.face[L + v * nfq], y = a.face[R + v * nfq];
+    a.other[L + v * nfq] = y;
+    a.other[R + v * nfq] = x;
   }
 }
 
@@ -73,48 +60,44 @@ __global__ void __launch_bounds__(256) exchangeKernel(const double* __restrict__
 // (BoundaryCondition.cpp: U for farfield/inflow/outflow, the wall state for walls); then {U} = U_b and
 // the interface jump 1/2 (U+ - U) = U_b - U, as the reference's boundary gradient fluxes.
 template <int DIM>
-__global__ void __launch_bounds__(256) exchangeBoundaryKernel(const double* __restrict__ face, double* __restrict__ other,
-                                                              const int* __restrict__ conn,
-                                                              const double* __restrict__ fgeo,
-                                                              const double* __restrict__ ghost, int64_t nface, int n1d,
-                                                              Phys ph) {
+__device__ __forceinline__ void exchangeBoundaryPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
+  const int n1d = a.n1d;
   const int nfq = DIM == 2 ? n1d : n1d * n1d;
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
-  if (f >= nface) return;
+  if (f >= a.nface) return;
   const int j = int(t - f * nfq);
-  const int sl = conn[f * 3 + 0], bc = conn[f * 3 + 1];
+  const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
   const int64_t L = int64_t(sl) * NV * nfq + j;
   double ul[NV];
 #pragma unroll
-  for (int v = 0; v < NV; ++v) ul[v] = face[L + v * nfq];
+  for (int v = 0; v < NV; ++v) ul[v] = a.face[L + v * nfq];
   if (bc <= 2) {
 #pragma unroll
-    for (int v = 0; v < NV; ++v) other[L + v * nfq] = ul[v];
+    for (int v = 0; v < NV; ++v) a.other[L + v * nfq] = ul[v];
     return;
   }
   double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
   State<DIM> s;
-  makeState<DIM>(s, ul, ph);
+  makeState<DIM>(s, ul, a.ph);
   Comp<DIM> l, g, b;
   compFromState<DIM>(s, l);
-  const double* gp = ghost + (f * nfq + j) * (DIM + 3);
+  const double* gp = a.ghost + (f * nfq + j) * (DIM + 3);
   g.r = gp[0];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) g.u[k] = gp[1 + k];
   g.e = gp[DIM + 1];
   g.p = gp[DIM + 2];
-  boundaryState<DIM>(bc, n, l, g, ph, b);
+  boundaryState<DIM>(bc, n, l, g, a.ph, b);
   double ub[NV], u2 = 0.0;
   ub[0] = b.r;
 #pragma unroll
   for (int k = 0; k < DIM; ++k) { ub[1 + k] = b.r * b.u[k]; u2 += b.u[k] * b.u[k]; }
   ub[DIM + 1] = b.r * (b.e + 0.5 * u2);
 #pragma unroll
-  for (int v = 0; v < NV; ++v) other[L + v * nfq] = 2.0 * ub[v] - ul[v];
+  for (int v = 0; v < NV; ++v) a.other[L + v * nfq] = 2.0 * ub[v] - ul[v];
 }
 
 template <int DIM, int N, bool AFFINE>
@@ -130,47 +113,62 @@ struct GradShape {
   static constexpr int EPB = S::EPB_RAW < EPB_SMEM ? S::EPB_RAW : EPB_SMEM;
   static constexpr int THREADS = ((EPB * NB + 31) / 32) * 32;
   static constexpr size_t SMEM = size_t(EPB) * PER_ELEM * 8 + sizeof(TensorTables) + 16;
+  static constexpr int threadsFor(int epb) { return ((epb * NB + 31) / 32) * 32; }
+  static constexpr size_t smemFor(int epb) { return size_t(epb) * PER_ELEM * 8 + sizeof(TensorTables) + 16; }
 };
 
-// Weak (BR) gradient of a tensor block: one thread per node.  Writes the total gradient at the nodes and
-// the face gradient traces (BR1: total gradient; BR2: volume gradient + the face's own lift).
 template <int DIM, int N, bool AFFINE>
-__global__ void __launch_bounds__(GradShape<DIM, N, AFFINE>::THREADS) tensorGradientKernel(GradArgs a) {
+__device__ __forceinline__ uint64_t* tensorGradBarrier(int epb) {
+  using G = GradShape<DIM, N, AFFINE>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* end = reinterpret_cast<double*>(smem_raw) + epb * G::PER_ELEM;
+  return reinterpret_cast<uint64_t*>(reinterpret_cast<TensorTables*>(end) + 1);
+}
+
+// Weak (BR) gradient of a tensor block, one tile: one thread per node.  Writes the total gradient at the
+// nodes and the face gradient traces (BR1: total gradient; BR2: volume gradient + the face's own lift).
+template <int DIM, int N, bool AFFINE>
+__device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t tile, uint32_t parity, bool loadTables) {
   using G = GradShape<DIM, N, AFFINE>;
   using S = TensorShape<DIM, N>;
-  constexpr int NV = G::NV, NB = G::NB, NF = G::NF, NFQ = G::NFQ, FS = G::FS, EPB = G::EPB;
+  constexpr int NV = G::NV, NB = G::NB, NF = G::NF, NFQ = G::NFQ, FS = G::FS;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE]
-  double* sS = sU + EPB * S::USTRIDE;                // own traces [EPB][FS]
-  double* sO = sS + EPB * FS;                        // other traces [EPB][FS]
-  double* sGt = sO + EPB * FS;                       // total gradient [EPB][NV*DIM][NB]
-  double* sGv = sGt + EPB * G::GSTR;                 // BR2 volume gradient [EPB][NV*DIM][NB]
-  double* sP = sGv + EPB * G::GSTR;                  // bilinear: U |J| dxi_b/dx_k [EPB][DIM*DIM*NV][NB]
-  double* sJ = sP + EPB * G::PSZ;                    // 1/|J| per node [EPB][NB]
-  TensorTables* T = reinterpret_cast<TensorTables*>(sJ + EPB * NB);
+  const int epb = a.epb;
+  double* sU = reinterpret_cast<double*>(smem_raw);  // [epb][USTRIDE]
+  double* sS = sU + epb * S::USTRIDE;                // own traces [epb][FS]
+  double* sO = sS + epb * FS;                        // other traces [epb][FS]
+  double* sGt = sO + epb * FS;                       // total gradient [epb][NV*DIM][NB]
+  double* sGv = sGt + epb * G::GSTR;                 // BR2 volume gradient [epb][NV*DIM][NB]
+  double* sP = sGv + epb * G::GSTR;                  // bilinear: U |J| dxi_b/dx_k [epb][DIM*DIM*NV][NB]
+  double* sJ = sP + epb * G::PSZ;                    // 1/|J| per node [epb][NB]
+  TensorTables* T = reinterpret_cast<TensorTables*>(sJ + epb * NB);
   uint64_t* bar = reinterpret_cast<uint64_t*>(T + 1);
 
   const int tid = threadIdx.x;
-  const int64_t e0 = int64_t(blockIdx.x) * EPB;
-  const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  const int64_t e0 = tile * epb;
+  const int ecount = int(a.ne - e0 < epb ? a.ne - e0 : epb);
   const int le = tid / NB, node = tid - le * NB;
   const bool active = le < ecount;
   const int64_t e = e0 + le;
+  __syncthreads();
   if (tid == 0) {
-    mbarInit(bar, 1);
+    fenceProxyAsync();
     const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * FS * 8;
     mbarExpectTx(bar, ub + 2 * fb);
     bulkLoad(sU, a.u + e0 * S::USTRIDE, ub, bar);
     bulkLoad(sS, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
     bulkLoad(sO, a.faceOther + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
-  for (int k = tid; k < int(sizeof(TensorTables) / 8); k += blockDim.x)
-    reinterpret_cast<double*>(T)[k] = a.tables[k];
+  if (loadTables)
+    for (int k = tid; k < int(sizeof(TensorTables) / 8); k += blockDim.x) reinterpret_cast<double*>(T)[k] = a.tables[k];
   __syncthreads();
-  const bool arrived = mbarWait(bar, 0);
+  const bool arrived = mbarWait(bar, parity);
   if (__syncthreads_or(!arrived)) {
-    if (tid == 0) atomicOr(a.status, kStatusTimeout);
-    return;
+    if (tid == 0) {
+      atomicOr(a.status, kStatusTimeout);
+      mbarWait(bar, parity);
+    }
+    return false;
   }
   constexpr int GS = DIM * DIM + 1;
   int ax[DIM];
@@ -293,44 +291,50 @@ __global__ void __launch_bounds__(GradShape<DIM, N, AFFINE>::THREADS) tensorGrad
       }
     }
   }
+  return true;
+}
+
+template <int DIM, int N, bool AFFINE>
+__global__ void __launch_bounds__(kMaxTileThreads) tensorGradientKernel(GradArgs a) {
+  if (threadIdx.x == 0) mbarInit(tensorGradBarrier<DIM, N, AFFINE>(a.epb), 1);
+  tensorGradientTile<DIM, N, AFFINE>(a, blockIdx.x, 0u, true);
+}
+
+template <int DIM, int N, bool AFFINE>
+__global__ void __launch_bounds__(kMaxTileThreads)
+    tensorGradientBatchKernel(const GradArgs* __restrict__ args, const int2* __restrict__ items, int nitems, int epb) {
+  if (threadIdx.x == 0) mbarInit(tensorGradBarrier<DIM, N, AFFINE>(epb), 1);
+  uint32_t parity = 0;
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const int2 it = items[w];
+    const GradArgs a = args[it.x];
+    if (!tensorGradientTile<DIM, N, AFFINE>(a, it.y, parity, w == int(blockIdx.x))) return;
+    parity ^= 1u;
+  }
 }
 
 // Interior-face Navier-Stokes flux: Riemann flux minus the central viscous flux of the two sides'
-// (state, gradient) traces, times |J_f|; +/- scatter as the Euler face kernel.
+// (state, gradient) traces, times |J_f|; +/- scatter as the Euler face operation.
 template <int DIM, int FLUX>
-__global__ void __launch_bounds__(256) nsFaceKernel(const double* __restrict__ face, const double* __restrict__ faceGrad,
-                                                    double* __restrict__ faceFlux, const int* __restrict__ conn,
-                                                    const double* __restrict__ fgeo, int64_t nface, int n1d, Phys ph) {
+__device__ __forceinline__ void faceNSPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
+  const int n1d = a.n1d;
   const int nfq = DIM == 2 ? n1d : n1d * n1d;
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
-  if (f >= nface) return;
+  if (f >= a.nface) return;
   const int j = int(t - f * nfq);
-  const int sl = conn[f * 3 + 0], sr = conn[f * 3 + 1], rot = conn[f * 3 + 2];
-  int jr;
-  if constexpr (DIM == 2) {
-    jr = n1d - 1 - j;
-  } else {
-    const int i = j / n1d, k = j - i * n1d;
-    int ii, kk;
-    switch (rot) {
-      case 0: ii = k; kk = i; break;
-      case 1: ii = n1d - 1 - i; kk = k; break;
-      case 2: ii = n1d - 1 - k; kk = n1d - 1 - i; break;
-      default: ii = i; kk = n1d - 1 - k; break;
-    }
-    jr = ii * n1d + kk;
-  }
+  const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
+  const int jr = rightPoint<DIM>(j, rot, n1d);
   const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
   const int64_t LG = int64_t(sl) * NV * DIM * nfq + j, RG = int64_t(sr) * NV * DIM * nfq + jr;
+  const Phys& ph = a.ph;
   double ul[NV], ur[NV];
 #pragma unroll
-  for (int v = 0; v < NV; ++v) { ul[v] = face[L + v * nfq]; ur[v] = face[R + v * nfq]; }
+  for (int v = 0; v < NV; ++v) { ul[v] = a.face[L + v * nfq]; ur[v] = a.face[R + v * nfq]; }
   double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
-  const double area = fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double area = a.fgeo[f * 4 + 3];
   State<DIM> l, r;
   makeState<DIM>(l, ul, ph);
   makeState<DIM>(r, ur, ph);
@@ -340,7 +344,7 @@ __global__ void __launch_bounds__(256) nsFaceKernel(const double* __restrict__ f
   {
     double g[NV * DIM];
 #pragma unroll
-    for (int c = 0; c < NV * DIM; ++c) g[c] = faceGrad[LG + c * nfq];
+    for (int c = 0; c < NV * DIM; ++c) g[c] = a.faceGrad[LG + c * nfq];
     PrimGrad<DIM> pg;
     primitiveGradient<DIM>(g, l.u, l.ir, l.E * l.ir, ph, pg);
     double u2 = 0.0;
@@ -352,7 +356,7 @@ __global__ void __launch_bounds__(256) nsFaceKernel(const double* __restrict__ f
   {
     double g[NV * DIM];
 #pragma unroll
-    for (int c = 0; c < NV * DIM; ++c) g[c] = faceGrad[RG + c * nfq];
+    for (int c = 0; c < NV * DIM; ++c) g[c] = a.faceGrad[RG + c * nfq];
     PrimGrad<DIM> pg;
     primitiveGradient<DIM>(g, r.u, r.ir, r.E * r.ir, ph, pg);
     double u2 = 0.0;
@@ -364,8 +368,8 @@ __global__ void __launch_bounds__(256) nsFaceKernel(const double* __restrict__ f
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
     const double x = fma(-0.5, fl[v] + fr[v], h[v]) * area;
-    faceFlux[L + v * nfq] = x;
-    faceFlux[R + v * nfq] = -x;
+    a.faceFlux[L + v * nfq] = x;
+    a.faceFlux[R + v * nfq] = -x;
   }
 }
 
@@ -374,32 +378,28 @@ __global__ void __launch_bounds__(256) nsFaceKernel(const double* __restrict__ f
 // interior side (walls: the wall state) and the boundary state, both with the interior primitive gradient
 // (adiabatic walls: zero temperature gradient on the boundary side).
 template <int DIM>
-__global__ void __launch_bounds__(256) nsBoundaryFaceKernel(const double* __restrict__ face,
-                                                            const double* __restrict__ faceGrad,
-                                                            double* __restrict__ faceFlux, const int* __restrict__ conn,
-                                                            const double* __restrict__ fgeo,
-                                                            const double* __restrict__ ghost, int64_t nface, int n1d,
-                                                            Phys ph) {
+__device__ __forceinline__ void faceNSBoundaryPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
+  const int n1d = a.n1d;
   const int nfq = DIM == 2 ? n1d : n1d * n1d;
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
-  if (f >= nface) return;
+  if (f >= a.nface) return;
   const int j = int(t - f * nfq);
-  const int sl = conn[f * 3 + 0], bc = conn[f * 3 + 1];
+  const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
   const int64_t L = int64_t(sl) * NV * nfq + j, LG = int64_t(sl) * NV * DIM * nfq + j;
+  const Phys& ph = a.ph;
   double ul[NV];
 #pragma unroll
-  for (int v = 0; v < NV; ++v) ul[v] = face[L + v * nfq];
+  for (int v = 0; v < NV; ++v) ul[v] = a.face[L + v * nfq];
   double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = fgeo[f * 4 + k];
-  const double area = fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double area = a.fgeo[f * 4 + 3];
   State<DIM> s;
   makeState<DIM>(s, ul, ph);
   Comp<DIM> l, g, b;
   compFromState<DIM>(s, l);
-  const double* gp = ghost + (f * nfq + j) * (DIM + 3);
+  const double* gp = a.ghost + (f * nfq + j) * (DIM + 3);
   g.r = gp[0];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) g.u[k] = gp[1 + k];
@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(256) nsBoundaryFaceKernel(const double* __rest
   normalFluxComp<DIM>(b, n, h);
   double gr[NV * DIM];
 #pragma unroll
-  for (int c = 0; c < NV * DIM; ++c) gr[c] = faceGrad[LG + c * nfq];
+  for (int c = 0; c < NV * DIM; ++c) gr[c] = a.faceGrad[LG + c * nfq];
   PrimGrad<DIM> pl;
   primitiveGradient<DIM>(gr, s.u, s.ir, s.E * s.ir, ph, pl);
   const Comp<DIM>& lm = bc >= 3 ? b : l;
@@ -423,7 +423,35 @@ __global__ void __launch_bounds__(256) nsBoundaryFaceKernel(const double* __rest
   }
   viscousNormalFlux<DIM>(pb, b.u, b.e * ph.inv_cv, n, ph, fb);
 #pragma unroll
-  for (int v = 0; v < NV; ++v) faceFlux[L + v * nfq] = fma(-0.5, fl[v] + fb[v], h[v]) * area;
+  for (int v = 0; v < NV; ++v) a.faceFlux[L + v * nfq] = fma(-0.5, fl[v] + fb[v], h[v]) * area;
+}
+
+// ---- face-point kernels ----------------------------------------------------------------------------
+template <int OP, int DIM, int FLUX>
+__device__ __forceinline__ void facePointOp(const FaceArgs& a, int64_t t) {
+  if constexpr (OP == kOpFace) faceInteriorPoint<DIM, FLUX>(a, t);
+  else if constexpr (OP == kOpFaceBoundary) faceBoundaryPoint<DIM>(a, t);
+  else if constexpr (OP == kOpExchange) exchangePoint<DIM>(a, t);
+  else if constexpr (OP == kOpExchangeBoundary) exchangeBoundaryPoint<DIM>(a, t);
+  else if constexpr (OP == kOpFaceNS) faceNSPoint<DIM, FLUX>(a, t);
+  else faceNSBoundaryPoint<DIM>(a, t);
+}
+
+constexpr int kFaceThreads = 256;
+
+template <int OP, int DIM, int FLUX>
+__global__ void __launch_bounds__(kFaceThreads) facePointKernel(FaceArgs a) {
+  facePointOp<OP, DIM, FLUX>(a, int64_t(blockIdx.x) * blockDim.x + threadIdx.x);
+}
+
+// Persistent batched launch over (argument set, chunk of kFaceThreads points) work items.
+template <int OP, int DIM, int FLUX>
+__global__ void __launch_bounds__(kFaceThreads)
+    facePointBatchKernel(const FaceArgs* __restrict__ args, const int2* __restrict__ items, int nitems) {
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const int2 it = items[w];
+    facePointOp<OP, DIM, FLUX>(args[it.x], int64_t(it.y) * blockDim.x + threadIdx.x);
+  }
 }
 
 }  // namespace sdg

@@ -1,0 +1,40 @@
+// Kernel variant registry of the GB300 DG path (host side).
+//
+// Every (element kind, dimension or type, order, affine, viscous) combination is one template
+// instantiation of a tile kernel; every (face operation, dimension, flux) one of a face-point kernel.
+// Each kernel family is instantiated in exactly one translation unit (sdg_variants_*.cu), which hands
+// out the kernel entry points as plain pointers for cudaLaunchKernel, with the shared-memory shape the
+// host needs to size a launch for any elements-per-CTA value.  One-instance launches, CUDA-graph
+// capture, the batched persistent launches and the autotuner all go through these pointers.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+
+namespace sdg {
+
+struct KernelVariant {
+  const void* single = nullptr;   // one CTA per tile / per chunk of points
+  const void* batch = nullptr;    // persistent kernel over a work list of (argument set, tile) items
+  int nb = 0;                     // nodes (tensor) or basis functions (dense) per element
+  int epb = 1;                    // default elements per CTA
+  int threads = 256;              // default threads per CTA
+  bool nodeThreads = false;       // threads follow epb: one per node, rounded up to whole warps
+  size_t perElem = 0, fixed = 0, perWarp = 0;  // dynamic shared memory = epb*perElem + fixed + perWarp*warps
+  size_t smem(int e, int t) const { return size_t(e) * perElem + fixed + perWarp * size_t((t + 31) / 32); }
+  int threadsFor(int e) const { return nodeThreads ? ((e * nb + 31) / 32) * 32 : threads; }
+  bool valid() const { return single != nullptr; }
+};
+
+// Tile kernels (elements of one block per CTA).  Unsupported combinations return an invalid variant.
+KernelVariant tensorStageVariant(int dim, int n, bool affine, bool visc);
+KernelVariant tensorGradVariant(int dim, int n, bool affine);
+KernelVariant denseStageVariant(int type, int p, bool affine, bool visc);
+KernelVariant denseGradVariant(int type, int p, bool affine);
+// Face-point kernels (FaceOp op, flux only for the Riemann operations) and the relative-error reduction.
+KernelVariant facePointVariant(int op, int dim, int flux);
+KernelVariant relerrVariant();
+
+// Largest tile size the kernels are compiled for (their __launch_bounds__).
+constexpr int kMaxThreads = 512;
+
+}  // namespace sdg

@@ -1,0 +1,49 @@
+// Dense (modal: triangles, P1 quadrangles) stage and gradient kernels: the one translation unit that
+// instantiates them, and their registry entries.
+#include "sdg_kernels_dense.cuh"
+#include "sdg_kernels_ns.cuh"
+#include "sdg_variants.hpp"
+
+namespace sdg {
+
+namespace {
+template <int NB, int NQ, int NFQ, int NF, bool AFF, bool VISC>
+KernelVariant stageOf() {
+  using S = DenseShape<NB, NQ, NFQ, NF>;
+  KernelVariant v;
+  v.single = reinterpret_cast<const void*>(&denseStageKernel<NB, NQ, NFQ, NF, AFF, VISC>);
+  v.batch = reinterpret_cast<const void*>(&denseStageBatchKernel<NB, NQ, NFQ, NF, AFF, VISC>);
+  v.nb = NB; v.epb = S::EPB; v.threads = S::THREADS; v.nodeThreads = false;
+  v.perElem = size_t(S::PER_ELEM) * 8; v.fixed = S::TABLES * 8 + 16; v.perWarp = 8 * S::NV;
+  return v;
+}
+template <int NB, int NQ, int NFQ, int NF, bool AFF>
+KernelVariant gradOf() {
+  using G = DenseGradShape<NB, NQ, NFQ, NF>;
+  KernelVariant v;
+  v.single = reinterpret_cast<const void*>(&denseGradientKernel<NB, NQ, NFQ, NF, AFF>);
+  v.batch = reinterpret_cast<const void*>(&denseGradientBatchKernel<NB, NQ, NFQ, NF, AFF>);
+  v.nb = NB; v.epb = G::EPB; v.threads = G::THREADS; v.nodeThreads = false;
+  v.perElem = size_t(G::PER_ELEM) * 8; v.fixed = G::TABLES * 8 + 16; v.perWarp = 0;
+  return v;
+}
+}  // namespace
+
+KernelVariant denseStageVariant(int type, int p, bool affine, bool visc) {
+#define SDG_DS(T, P, NB, NQ, NFQ, NF, AFF)                                                                  \
+  if (type == T && p == P && affine == AFF)                                                                 \
+    return visc ? stageOf<NB, NQ, NFQ, NF, AFF, true>() : stageOf<NB, NQ, NFQ, NF, AFF, false>();
+  SDG_DENSE_CASES(SDG_DS)
+#undef SDG_DS
+  return KernelVariant();
+}
+
+KernelVariant denseGradVariant(int type, int p, bool affine) {
+#define SDG_DG(T, P, NB, NQ, NFQ, NF, AFF) \
+  if (type == T && p == P && affine == AFF) return gradOf<NB, NQ, NFQ, NF, AFF>();
+  SDG_DENSE_CASES(SDG_DG)
+#undef SDG_DG
+  return KernelVariant();
+}
+
+}  // namespace sdg

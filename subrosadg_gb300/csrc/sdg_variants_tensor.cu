@@ -1,0 +1,57 @@
+// Tensor-block (quadrangles P>=2, hexahedra) stage and gradient kernels: the one translation unit that
+// instantiates them, and their registry entries.
+#include "sdg_kernels_ns.cuh"
+#include "sdg_variants.hpp"
+
+namespace sdg {
+
+namespace {
+template <int DIM, int N, bool AFF, bool VISC>
+KernelVariant stageOf() {
+  using S = TensorShape<DIM, N>;
+  KernelVariant v;
+  v.single = reinterpret_cast<const void*>(&tensorStageKernel<DIM, N, AFF, VISC>);
+  v.batch = reinterpret_cast<const void*>(&tensorStageBatchKernel<DIM, N, AFF, VISC>);
+  v.nb = S::NB; v.epb = S::EPB; v.threads = S::THREADS; v.nodeThreads = true;
+  v.perElem = S::SMEM_PER_ELEM; v.fixed = sizeof(TensorTables) + 16; v.perWarp = 8 * S::NV;
+  return v;
+}
+template <int DIM, int N, bool AFF>
+KernelVariant gradOf() {
+  using G = GradShape<DIM, N, AFF>;
+  KernelVariant v;
+  v.single = reinterpret_cast<const void*>(&tensorGradientKernel<DIM, N, AFF>);
+  v.batch = reinterpret_cast<const void*>(&tensorGradientBatchKernel<DIM, N, AFF>);
+  v.nb = G::NB; v.epb = G::EPB; v.threads = G::THREADS; v.nodeThreads = true;
+  v.perElem = size_t(G::PER_ELEM) * 8; v.fixed = sizeof(TensorTables) + 16; v.perWarp = 0;
+  return v;
+}
+}  // namespace
+
+#define SDG_TENSOR_ORDERS(X) X(2, 3) X(2, 4) X(2, 5) X(2, 6) X(3, 2) X(3, 3) X(3, 4) X(3, 5) X(3, 6)
+
+KernelVariant tensorStageVariant(int dim, int n, bool affine, bool visc) {
+#define SDG_TS(D, NN)                                                                                   \
+  if (dim == D && n == NN) {                                                                            \
+    if (affine) return visc ? stageOf<D, NN, true, true>() : stageOf<D, NN, true, false>();             \
+    if constexpr (D == 2) return visc ? stageOf<D, NN, false, true>() : stageOf<D, NN, false, false>(); \
+    return KernelVariant();                                                                             \
+  }
+  SDG_TENSOR_ORDERS(SDG_TS)
+#undef SDG_TS
+  return KernelVariant();
+}
+
+KernelVariant tensorGradVariant(int dim, int n, bool affine) {
+#define SDG_TG(D, NN)                                         \
+  if (dim == D && n == NN) {                                  \
+    if (affine) return gradOf<D, NN, true>();                 \
+    if constexpr (D == 2) return gradOf<D, NN, false>();      \
+    return KernelVariant();                                   \
+  }
+  SDG_TENSOR_ORDERS(SDG_TG)
+#undef SDG_TG
+  return KernelVariant();
+}
+
+}  // namespace sdg

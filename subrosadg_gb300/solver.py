@@ -243,6 +243,87 @@ class GpuSolver:
         self._chk(self.lib.sdg_launch_count(self.h, byref(n)))
         return n.value
 
+    # launch shapes -----------------------------------------------------------------------------
+    def set_graph(self, enable: bool):
+        self._chk(self.lib.sdg_set_graph(self.h, int(bool(enable))))
+
+    def tile(self, block=0):
+        """(stage elements/CTA, stage threads, gradient elements/CTA, gradient threads) of a block."""
+        v = [ctypes.c_int32() for _ in range(4)]
+        self._chk(self.lib.sdg_get_tile(self.h, block, *[byref(x) for x in v]))
+        return tuple(x.value for x in v)
+
+    def set_tile(self, block, epb, threads, gradient_epb, gradient_threads):
+        self._chk(self.lib.sdg_set_tile(self.h, block, epb, threads, gradient_epb, gradient_threads))
+
+    def autotune(self, retime=False):
+        self._chk(self.lib.sdg_autotune(self.h, _abi.AUTOTUNE_RETIME if retime else 0))
+        return [self.tile(b) for b in range(self.counts.block_count)]
+
+
+class Batch:
+    """Many independent GpuSolver instances advanced together (sdg_batch_*): one persistent launch per
+    kernel variant and dependency level per RK stage, the step captured in a CUDA graph."""
+
+    def __init__(self, solvers):
+        self.lib = _abi.load()
+        self.solvers = list(solvers)
+        arr = (c_void_p * len(self.solvers))(*[s.h for s in self.solvers])
+        b = c_void_p()
+        rc = self.lib.sdg_batch_create(arr, len(self.solvers), byref(b))
+        check(rc, None)
+        self.b = b
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.lib.sdg_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _chk(self, rc):
+        if rc != _abi.SDG_OK:
+            msg = self.lib.sdg_batch_last_error(self.b)
+            raise _abi.SdgError(rc, msg.decode() if msg else "")
+
+    def counts(self):
+        c = _abi.SdgBatchCounts()
+        self._chk(self.lib.sdg_batch_get_counts(self.b, byref(c)))
+        return {k: getattr(c, k) for k, _ in c._fields_}
+
+    def set_delta_time(self, dts):
+        d = np.ascontiguousarray(dts, np.float64)
+        assert d.shape == (len(self.solvers),)
+        self._chk(self.lib.sdg_batch_set_delta_time(self.b, _ptr(d)))
+
+    def set_persistence(self, ctas_per_sm):
+        self._chk(self.lib.sdg_batch_set_persistence(self.b, ctas_per_sm))
+
+    def step_async(self, steps=1):
+        self._chk(self.lib.sdg_batch_step_async(self.b, steps))
+
+    def step_sequential_async(self, steps=1):
+        self._chk(self.lib.sdg_batch_step_sequential_async(self.b, steps))
+
+    def synchronize(self):
+        self._chk(self.lib.sdg_batch_synchronize(self.b))
+
+    def step(self, steps=1):
+        self.step_async(steps)
+        self.synchronize()
+
+    def autotune(self, retime=False):
+        self._chk(self.lib.sdg_batch_autotune(self.b, _abi.AUTOTUNE_RETIME if retime else 0))
+
+    def stream(self):
+        s = c_void_p()
+        self._chk(self.lib.sdg_batch_get_stream(self.b, byref(s)))
+        return s.value
+
 
 class System:
     """Mirror of SubrosaDG's System<SimulationControl> (src/Utils/SystemControl.cpp:42-236)."""
