@@ -8,10 +8,18 @@ dt from CFL 0.2 -- seeded synthetic initial state of that shape (no dataset invo
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 Prints one JSON line.  value = DOF-stage updates/s with the state resident in HBM (CUDA events on the
-library's stream); e2e = the same metric through the C ABI with host buffers (pinned), the state
-uploaded and downloaded every step.  --impl reference times the CPU restatement of the reference path
-(the oracle, reference-faithful arithmetic) on the host cores.  Under torchrun (N > 1) each rank runs an
-independent replica on its own GPU (the path is not sharded: replicas only).
+library's stream, the step replayed as a CUDA graph); e2e = the same metric through the C ABI with host
+buffers (pinned), the state uploaded and downloaded every step.  The line also carries the other
+workloads of the metric, each measured the same way on this GPU:
+  batched      256 independent 2D Euler / Navier-Stokes Kelvin-Helmholtz solves (500..50,000 elements,
+               P1..P5, quads or hybrid, Mach 0.1..0.8, Re 1e2..1e4): one batched graph step of all
+               instances against the same instances stepped one after another with plain launches
+  ns_hybrid    2D Navier-Stokes BR2 Kelvin-Helmholtz, Re 1e4, 256^2 jittered quads with a 50% triangle
+               split, P4, Lax-Friedrichs
+  vortex2d     2D Euler isentropic vortex, 40^2 quads, P3, Roe, dt 1e-3 (L2-resident, launch bound)
+--impl reference times the CPU restatement of the reference path (the oracle, reference-faithful
+arithmetic) on the host cores.  Under torchrun (N > 1) each rank runs an independent replica on its own
+GPU (the path is not sharded: replicas only).
 """
 from __future__ import annotations
 
@@ -37,7 +45,7 @@ WORKLOAD = "tgv3d-euler-64^3-hex-P3-HLLC-SSPRK3-CFL0.2"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--elements", type=int, default=64, help="hexahedra per direction")
@@ -45,6 +53,10 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=32, help="hexahedra per direction of the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="headline workload only")
+    ap.add_argument("--batch-count", type=int, default=256)
+    ap.add_argument("--batch-max-elements", type=int, default=50000)
+    ap.add_argument("--ns-elements", type=int, default=256, help="quads per direction of the NS hybrid mesh")
     return ap.parse_args()
 
 
@@ -81,7 +93,7 @@ def profile_figures():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms during the timed region."""
 
     FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
@@ -96,7 +108,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -179,6 +191,121 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _timed(torch, stream, fn, steps):
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(steps):
+        fn()
+    ev1.record(stream)
+    ev1.synchronize()
+    return ev0.elapsed_time(ev1)
+
+
+def bench_batched(args, device, torch):
+    """Batched workload: all instances in one batched graph step versus one instance after another."""
+    import subrosadg_gb300 as sdg
+    from tests import cases
+    t0 = time.perf_counter()
+    inst, params = cases.batch_instances(args.batch_count, max_elements=args.batch_max_elements)
+    solvers = []
+    for mesh, cfg, prim in inst:
+        g = sdg.GpuSolver(mesh, cfg, device=device)
+        g.initialize_primitive(prim(g.volume_points()))
+        solvers.append(g)
+    dts = [g.calculateDeltaTime(0.2) for g in solvers]
+    b = sdg.Batch(solvers)
+    b.set_delta_time(dts)
+    setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b.autotune()
+    tune = time.perf_counter() - t0
+    c = b.counts()
+    stream = torch.cuda.ExternalStream(b.stream(), device=device)
+    steps = max(3, args.steps)
+    b.step(args.warmup)
+    with ClockSampler(device) as clocks:
+        ms_batch = _timed(torch, stream, lambda: b.step_async(1), steps)
+    b.synchronize()
+    b.step_sequential_async(1)
+    b.synchronize()
+    ms_seq = _timed(torch, stream, lambda: b.step_sequential_async(1), steps)
+    b.synchronize()
+    dof_stages = sum(g.counts.degree_of_freedom_count * 3 for g in solvers)
+    out = {
+        "workload": f"{len(solvers)} independent 2D Kelvin-Helmholtz solves (Euler or NS BR2, LF, SSP-RK3)",
+        "instances": len(solvers), "elements": c["element_count"], "dof": c["degree_of_freedom_count"],
+        "navier_stokes_instances": sum(p["navier_stokes"] for p in params),
+        "orders": sorted({p["order"] for p in params}),
+        "value": dof_stages * steps / (ms_batch * 1e-3), "unit": "DOF-stage/s",
+        "ms_per_step": ms_batch / steps, "launches_per_step": c["launches_per_step"],
+        "persistent_ctas_per_sm": c["persistent_ctas_per_sm"],
+        "sequential": {"value": dof_stages * steps / (ms_seq * 1e-3), "ms_per_step": ms_seq / steps,
+                       "launches_per_step": c["sequential_launches_per_step"],
+                       "mode": "plain per-instance launches, instance after instance, same stream and tiles"},
+        "speedup_vs_sequential": ms_seq / ms_batch,
+        "setup_s": setup, "autotune_s": tune, "clocks": clocks.summary(),
+    }
+    b.close()
+    for g in solvers:
+        g.close()
+    return out
+
+
+def bench_ns_hybrid(args, device, torch):
+    """2D Navier-Stokes BR2 Kelvin-Helmholtz, Re 1e4, Pr 0.71, hybrid 256^2 mesh, P4, LF."""
+    import subrosadg_gb300 as sdg
+    from tests import cases
+    n = args.ns_elements
+    mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=True, jitter=0.1, split_fraction=0.5, seed=11)
+    cfg = cases.ns_config(4, sdg.LAX_FRIEDRICHS, sdg.BR2, 1e-4)
+    g = sdg.GpuSolver(mesh, cfg, device=device)
+    g.initialize_primitive(cases.kh_primitive(*g.volume_points()[:, :2].T))
+    dt = g.calculateDeltaTime(0.2)
+    g.autotune()
+    import ctypes
+    sp = ctypes.c_void_p()
+    g.lib.sdg_get_stream(g.h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value, device=device)
+    for _ in range(args.warmup):
+        g.step_async(dt)
+    g.synchronize()
+    steps = max(3, args.steps)
+    ms = _timed(torch, stream, lambda: g.step_async(dt), steps)
+    g.synchronize()
+    dof = g.counts.degree_of_freedom_count
+    out = {"workload": f"ns-kh2d-BR2-Re1e4-{n}^2-hybrid-P4-LF", "elements": g.counts.element_count, "dof": dof,
+           "value": dof * 3 * steps / (ms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": ms / steps,
+           "tiles": [g.tile(k) for k in range(g.counts.block_count)]}
+    g.close()
+    return out
+
+
+def bench_vortex(args, device, torch):
+    """2D Euler isentropic vortex, 40^2 quads, P3, Roe, dt 1e-3: state ~0.8 MB (L2-resident)."""
+    import ctypes
+
+    import subrosadg_gb300 as sdg
+    from tests import cases
+    mesh, cfg, prim, _, _, _ = cases.vortex_case(n=40, p=3, flux=sdg.ROE)
+    g = sdg.GpuSolver(mesh, cfg, device=device)
+    g.initialize_primitive(prim(g.volume_points()))
+    sp = ctypes.c_void_p()
+    g.lib.sdg_get_stream(g.h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value, device=device)
+    for _ in range(20):
+        g.step_async(1e-3)
+    g.synchronize()
+    steps = 200
+    ms = _timed(torch, stream, lambda: g.step_async(1e-3), steps)
+    g.synchronize()
+    dof = g.counts.degree_of_freedom_count
+    out = {"workload": "vortex2d-euler-40^2-quad-P3-Roe-dt1e-3", "dof": dof, "steps": steps,
+           "value": dof * 3 * steps / (ms * 1e-3), "unit": "DOF-stage/s", "us_per_step": 1e3 * ms / steps,
+           "note": "state L2-resident: latency and launch bound (graph replay of 7 launches per step)"}
+    g.close()
+    return out
+
+
 def run_ours(args):
     import ctypes
 
@@ -213,11 +340,11 @@ def run_ours(args):
         s.step_async(dt)
     s.synchronize()
 
-    # timed region: K steps, state resident in HBM (state 8 * DOF bytes >> 129 MB L2: no flush needed)
+    # timed region: K steps, state resident in HBM (state 8 * DOF bytes >> 129 MB L2: no flush needed),
+    # each step one CUDA-graph replay of all stage launches and the relative-error reduction
     if pg:
         pg.barrier()
     torch.cuda.synchronize(device)
-    lib.sdg_set_kernel_timing(s.h, 1)
     n0 = s.launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(device) as clocks:
@@ -229,15 +356,22 @@ def run_ours(args):
     torch.cuda.synchronize(device)
     ms = ev0.elapsed_time(ev1)
     launches = s.launch_count() - n0
-    kms = (ctypes.c_double * 5)()
-    kn = (ctypes.c_int64 * 5)()
-    lib.sdg_kernel_time(s.h, kms, kn)
-    lib.sdg_set_kernel_timing(s.h, 0)
+    s.synchronize()
     relerr = s.relative_error()
     if pg:
         t = torch.tensor([ms], device=f"cuda:{device}")
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
         ms = float(t.item())
+    # per-kernel device times: a separate pass with every launch bracketed by events on the stream
+    ksteps = max(1, min(args.steps, 3))
+    lib.sdg_set_kernel_timing(s.h, 1)
+    for _ in range(ksteps):
+        s.step_async(dt)
+    kms = (ctypes.c_double * 5)()
+    kn = (ctypes.c_int64 * 5)()
+    lib.sdg_kernel_time(s.h, kms, kn)
+    lib.sdg_set_kernel_timing(s.h, 0)
+    s.synchronize()
 
     # roofline of the dominant kernel (element stage kernel): algorithmic bytes per launch =
     # 8 * (3 DOF + (d^2 + 1) N_e): read U, read U_base, write U, affine geometry
@@ -303,14 +437,20 @@ def run_ours(args):
         "fp64": {"peak_gflops": fp64.value, "peak_source": "sdg_measure_fp64_peak (independent-chain DFMA probe)",
                  "achieved_gflops": fp64_achieved, "frac": (fp64_achieved / fp64.value) if fp64_achieved else None,
                  "note": "the DG stage kernels are FP64-issue bound on GB300; see DESIGN.md"},
-        "kernel_ms_per_step": {"element": kms[0] / args.steps, "interior_face": kms[1] / args.steps,
-                               "boundary_face": kms[2] / args.steps, "other": kms[3] / args.steps},
+        "kernel_ms_per_step": {"element": kms[0] / ksteps, "interior_face": kms[1] / ksteps,
+                               "boundary_face": kms[2] / ksteps, "reduction": kms[3] / ksteps,
+                               "gradient": kms[4] / ksteps},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "e2e": e2e,
         "cpu_baseline": cpu,
         "relative_error_last_step": relerr.tolist(),
     }
+    s.close()
+    if not args.no_extra:
+        line["batched"] = bench_batched(args, device, torch)
+        line["ns_hybrid"] = bench_ns_hybrid(args, device, torch)
+        line["vortex2d"] = bench_vortex(args, device, torch)
     print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()

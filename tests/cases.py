@@ -45,7 +45,7 @@ def tgv_primitive(x, y, z, mach=0.1, gamma=GAMMA):
     return np.stack([rho, u, v, w, p / (rho * R_GAS)], 1)
 
 
-def kh_primitive(x, y, seed=7):
+def kh_primitive(x, y, seed=7, pressure=2.5):
     rng = np.random.default_rng(seed)
     k = int(rng.integers(1, 4))
     phase = float(rng.uniform(0, 2 * math.pi))
@@ -53,7 +53,7 @@ def kh_primitive(x, y, seed=7):
     rho = np.where(band, 2.0, 1.0)
     u = np.where(band, 0.5, -0.5)
     v = 1e-2 * np.sin(2 * math.pi * k * x + phase)
-    p = np.full_like(x, 2.5)  # examples/khinstability_2d_ceuler.cpp:33-40
+    p = np.full_like(x, pressure)  # 2.5: examples/khinstability_2d_ceuler.cpp:33-40
     return np.stack([rho, u, v, p / (rho * R_GAS)], 1)
 
 
@@ -128,6 +128,34 @@ def channel_case(p=2, flux=sdg.HLLC, conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.PR
         return out
 
     return (mesh, cfg, ic, bc, dt, steps)
+
+
+def batch_instances(count=256, seed=2024, min_elements=500, max_elements=50000, orders=(1, 2, 3, 4, 5)):
+    """The batched workload: `count` independent 2D Kelvin-Helmholtz solves on [0,1]^2 (periodic), element
+    counts log-uniform in [min_elements, max_elements], P uniform in `orders`, jittered (10% of h) quads or
+    the hybrid with a 50% triangle split, Mach of the shear speed uniform in [0.1, 0.8] (p = rho c^2 / gamma
+    with c = 0.5 / Mach in the light band), Re = 1 / mu log-uniform in [1e2, 1e4], Euler or Navier-Stokes
+    (BR2) with equal odds, Lax-Friedrichs flux, SSP-RK3.  Returns a list of (mesh, cfg, primitive) and the
+    parameter records."""
+    rng = np.random.default_rng(seed)
+    out, params = [], []
+    for i in range(count):
+        target = math.exp(rng.uniform(math.log(min_elements), math.log(max_elements)))
+        p = int(rng.choice(orders))
+        hybrid = bool(rng.random() < 0.5)
+        mach = float(rng.uniform(0.1, 0.8))
+        re = float(math.exp(rng.uniform(math.log(1e2), math.log(1e4))))
+        ns = bool(rng.random() < 0.5)
+        split = 0.5 if hybrid else 0.0
+        n = max(3, int(round(math.sqrt(target / (1.0 + split)))))
+        mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=True, jitter=0.1, split_fraction=split,
+                               seed=seed * 1000 + i)
+        cfg = ns_config(p, sdg.LAX_FRIEDRICHS, sdg.BR2, 1.0 / re) if ns else config(p, sdg.LAX_FRIEDRICHS)
+        pressure = 0.25 / (GAMMA * mach * mach)
+        out.append((mesh, cfg, (lambda pr, sd: (lambda pts: kh_primitive(pts[:, 0], pts[:, 1], seed=sd, pressure=pr)))(
+            pressure, seed + i)))
+        params.append({"n": n, "order": p, "hybrid": hybrid, "mach": mach, "reynolds": re, "navier_stokes": ns})
+    return out, params
 
 
 def golden_cases():
