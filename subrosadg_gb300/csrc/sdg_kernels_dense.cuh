@@ -19,8 +19,15 @@
 namespace sdg {
 
 // Table layout (doubles): phi[NQ][NB] | dphiw[NQ][2][NB] (w_q dphi/dxi_b) | phif[NFP][NB] |
-//                         phifw[NFP][NB] (wf_j phif) | mref[NB][NB] (inverse reference mass matrix)
+//                         phifw[NFP][NB] (wf_j phif) | mref[NB][NB] (inverse reference mass matrix) |
+//   modal gradient operators of affine elements (M = |J| M_ref folds M^-1 into them):
+//                         dmod[2][NB][NB]  D_b = M_ref^-1 S_b, S_b(k,m) = sum_q w_q dphi_k/dxi_b phi_m
+//                         emod[NF][NB][NFQ] E_f = M_ref^-1 Phi_f^T W_f (lift of face f's point values)
+//                         lmod[NF][NFQ][NFQ] L_f = Phi_f E_f (trace at face f of the lift from face f)
 inline size_t denseTableSize(int nb, int nq, int nfp) { return size_t(nq) * nb * 3 + size_t(nfp) * nb * 2 + size_t(nb) * nb; }
+inline size_t denseGradOperatorSize(int nb, int nf, int nfq) {
+  return size_t(2) * nb * nb + size_t(nf) * nb * nfq + size_t(nf) * nfq * nfq;
+}
 
 inline void invertDense(int n, std::vector<double> a, std::vector<double>& inv) {
   inv.assign(size_t(n) * n, 0.0);
@@ -47,7 +54,7 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
   const int nb = modalCount(type, p);
   const PointRule vr = volumeRule(type, p), fr = faceRule(type, p);
   const int nq = vr.n, nf = typeFaces(type), nfq = fr.n, nfp = nf * nfq;
-  tables.assign(denseTableSize(nb, nq, nfp), 0.0);
+  tables.assign(denseTableSize(nb, nq, nfp) + denseGradOperatorSize(nb, nf, nfq), 0.0);
   double* phi = tables.data();
   double* dphiw = phi + size_t(nq) * nb;
   double* phif = dphiw + size_t(nq) * 2 * nb;
@@ -80,6 +87,45 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
     }
   invertDense(nb, m, inv);
   std::copy(inv.begin(), inv.end(), mref);
+  {
+    double* dmod = mref + size_t(nb) * nb;
+    double* emod = dmod + size_t(2) * nb * nb;
+    double* lmod = emod + size_t(nf) * nb * nfq;
+    for (int b = 0; b < 2; ++b) {
+      std::vector<long double> sb(size_t(nb) * nb, 0.0L);
+      for (int k = 0; k < nb; ++k)
+        for (int mm = 0; mm < nb; ++mm) {
+          long double acc = 0.0L;
+          for (int q = 0; q < nq; ++q)
+            acc += (long double)dphiw[(size_t(q) * 2 + b) * nb + k] * (long double)phi[size_t(q) * nb + mm];
+          sb[size_t(k) * nb + mm] = acc;
+        }
+      for (int i = 0; i < nb; ++i)
+        for (int mm = 0; mm < nb; ++mm) {
+          long double acc = 0.0L;
+          for (int k = 0; k < nb; ++k) acc += (long double)inv[size_t(i) * nb + k] * sb[size_t(k) * nb + mm];
+          dmod[(size_t(b) * nb + i) * nb + mm] = double(acc);
+        }
+    }
+    std::vector<long double> ef(size_t(nf) * nb * nfq, 0.0L);
+    for (int f = 0; f < nf; ++f)
+      for (int i = 0; i < nb; ++i)
+        for (int j = 0; j < nfq; ++j) {
+          long double acc = 0.0L;
+          for (int k = 0; k < nb; ++k)
+            acc += (long double)inv[size_t(i) * nb + k] * (long double)phifw[size_t(f * nfq + j) * nb + k];
+          ef[(size_t(f) * nb + i) * nfq + j] = acc;
+          emod[(size_t(f) * nb + i) * nfq + j] = double(acc);
+        }
+    for (int f = 0; f < nf; ++f)
+      for (int j = 0; j < nfq; ++j)
+        for (int jj = 0; jj < nfq; ++jj) {
+          long double acc = 0.0L;
+          for (int i = 0; i < nb; ++i)
+            acc += (long double)phif[size_t(f * nfq + j) * nb + i] * ef[(size_t(f) * nb + i) * nfq + jj];
+          lmod[(size_t(f) * nfq + j) * nfq + jj] = double(acc);
+        }
+  }
   phiOut.assign(phi, phi + size_t(nq) * nb);
   // unweighted least-squares projection (InitialCondition.cpp:91-104): lsq = (Phi^T Phi)^-1 Phi^T  [nb][nq]
   invertDense(nb, ptp, inv);
@@ -340,20 +386,23 @@ __global__ void __launch_bounds__(kMaxTileThreads)
 // gradient coefficients = M^-1 R_vg (SpatialDiscrete.cpp:294-322,844-968,1034-1068; TimeIntegration.cpp:200-228).
 // X = U+ (neighbour trace) gives the total gradient (BR1, and the BR2 volume-point gradient); X = {U} the BR2
 // volume part, to which face f adds its own lift r_f = M^-1 sum_{j in f} wf_j nF_f 1/2[U] phi.
-template <int NB, int NQ, int NFQ, int NF>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
 struct DenseGradShape {
   static constexpr int NV = 4, NFP = NF * NFQ, EPB = 8, THREADS = 256;
   static constexpr int USTRIDE = (NV * NB + 1) & ~1;
   static constexpr int FS = NF * NV * NFQ;
-  static constexpr int PER_ELEM = USTRIDE + 2 * FS + NV * NQ + 3 * NV * 2 * NB;
-  static constexpr size_t TABLES = size_t(NQ) * NB * 3 + size_t(NFP) * NB * 2 + size_t(NB) * NB;
+  // affine: modal operators (phif, dmod, emod, lmod) and one coefficient block per element;
+  // bilinear: the general form with the element's own M^-1
+  static constexpr int PER_ELEM = AFFINE ? USTRIDE + 2 * FS + NV * 2 * NB : USTRIDE + 2 * FS + NV * NQ + 3 * NV * 2 * NB;
+  static constexpr size_t TABLES = AFFINE ? size_t(NFP) * NB + size_t(2) * NB * NB + size_t(NF) * NB * NFQ + size_t(NF) * NFQ * NFQ
+                                          : size_t(NQ) * NB * 3 + size_t(NFP) * NB * 2 + size_t(NB) * NB;
   static constexpr size_t SMEM = (size_t(EPB) * PER_ELEM + TABLES) * 8 + 16;
   static constexpr size_t smemFor(int epb) { return (size_t(epb) * PER_ELEM + TABLES) * 8 + 16; }
 };
 
-template <int NB, int NQ, int NFQ, int NF>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
 __device__ __forceinline__ uint64_t* denseGradBarrier(int epb) {
-  using G = DenseGradShape<NB, NQ, NFQ, NF>;
+  using G = DenseGradShape<NB, NQ, NFQ, NF, AFFINE>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   return reinterpret_cast<uint64_t*>(reinterpret_cast<double*>(smem_raw) + epb * G::PER_ELEM + G::TABLES);
 }
@@ -373,9 +422,131 @@ struct DenseGradArgs {
   int epb;
 };
 
+// Affine elements: with M = |J| M_ref and constant metric, the gradient coefficients are
+//   w_tot(v,k) = (1/|J|) [ sum_f nF_f[k] E_f U+_f(v) - sum_b |J| dxi_b/dx_k D_b u(v) ]
+//   w_vol(v,k) = w_tot(v,k) - (1/|J|) sum_f nF_f[k] E_f (1/2 [U])_f(v)
+// and the BR2 trace at face f adds (1/|J|) nF_f L_f (1/2 [U])_f: the same quantities as the general form
+// below, with M^-1 folded into the precomputed operators.
+template <int NB, int NQ, int NFQ, int NF>
+__device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, int64_t tile, uint32_t parity,
+                                                        bool loadTables) {
+  using G = DenseGradShape<NB, NQ, NFQ, NF, true>;
+  constexpr int NV = 4, NFP = G::NFP, FS = G::FS, NR = NV * 2;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  const int EPB = a.epb;
+  double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE] modal coefficients
+  double* sS = sU + EPB * G::USTRIDE;                // own traces [EPB][FS]
+  double* sO = sS + EPB * FS;                        // other traces [EPB][FS]
+  double* sW = sO + EPB * FS;                        // coefficients whose traces are the face gradients [EPB][NR][NB]
+  double* tab = sW + EPB * NR * NB;
+  const double* phif = tab;                          // [NFP][NB]
+  const double* dmod = phif + NFP * NB;              // [2][NB][NB]
+  const double* emod = dmod + 2 * NB * NB;           // [NF][NB][NFQ]
+  const double* lmod = emod + NF * NB * NFQ;         // [NF][NFQ][NFQ]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tab + G::TABLES);
+
+  const int tid = threadIdx.x;
+  const int64_t e0 = tile * EPB;
+  const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  __syncthreads();
+  if (tid == 0) {
+    fenceProxyAsync();
+    const uint32_t ub = uint32_t(ecount) * G::USTRIDE * 8, fb = uint32_t(ecount) * FS * 8;
+    mbarExpectTx(bar, ub + 2 * fb);
+    bulkLoad(sU, a.u + e0 * G::USTRIDE, ub, bar);
+    bulkLoad(sS, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+    bulkLoad(sO, a.faceOther + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+  }
+  if (loadTables) {
+    constexpr int OFF_PHIF = NQ * NB * 3, OFF_DMOD = NQ * NB * 3 + NFP * NB * 2 + NB * NB;
+    constexpr int NOPS = 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
+    for (int k = tid; k < NFP * NB; k += blockDim.x) tab[k] = a.tables[OFF_PHIF + k];
+    for (int k = tid; k < NOPS; k += blockDim.x) tab[NFP * NB + k] = a.tables[OFF_DMOD + k];
+  }
+  __syncthreads();
+  const bool arrived = mbarWait(bar, parity);
+  if (__syncthreads_or(!arrived)) {
+    if (tid == 0) {
+      atomicOr(a.status, kStatusTimeout);
+      mbarWait(bar, parity);
+    }
+    return false;
+  }
+  // 1. coefficients per (element, variable, basis function)
+  for (int idx = tid; idx < ecount * NV * NB; idx += blockDim.x) {
+    const int le = idx / (NV * NB), r = idx - le * NV * NB;
+    const int v = r / NB, i = r - v * NB;
+    const int64_t e = e0 + le;
+    const double* g = a.geom + e * 5;
+    const double ja00 = g[0], ja01 = g[1], ja10 = g[2], ja11 = g[3], jinv = g[4];
+    const double* u = sU + le * G::USTRIDE + v * NB;
+    double d0 = 0.0, d1 = 0.0;
+#pragma unroll
+    for (int m = 0; m < NB; ++m) {
+      d0 = fma(dmod[i * NB + m], u[m], d0);
+      d1 = fma(dmod[(NB + i) * NB + m], u[m], d1);
+    }
+    double tot0 = -fma(ja00, d0, ja10 * d1), tot1 = -fma(ja01, d0, ja11 * d1);
+    double jmp0 = 0.0, jmp1 = 0.0;
+    const double* nF = a.fmetric + e * NF * 2;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const double* O = sO + le * FS + (f * NV + v) * NFQ;
+      const double* S = sS + le * FS + (f * NV + v) * NFQ;
+      const double* E = emod + (f * NB + i) * NFQ;
+      double ep = 0.0, ej = 0.0;
+#pragma unroll
+      for (int j = 0; j < NFQ; ++j) {
+        ep = fma(E[j], O[j], ep);
+        ej = fma(E[j], 0.5 * (O[j] - S[j]), ej);
+      }
+      const double n0 = nF[f * 2 + 0], n1 = nF[f * 2 + 1];
+      tot0 = fma(n0, ep, tot0); tot1 = fma(n1, ep, tot1);
+      jmp0 = fma(n0, ej, jmp0); jmp1 = fma(n1, ej, jmp1);
+    }
+    const double g0 = jinv * tot0, g1 = jinv * tot1;
+    a.grad[(e * NR + v * 2 + 0) * NB + i] = g0;
+    a.grad[(e * NR + v * 2 + 1) * NB + i] = g1;
+    sW[(le * NR + v * 2 + 0) * NB + i] = a.br2 ? jinv * (tot0 - jmp0) : g0;
+    sW[(le * NR + v * 2 + 1) * NB + i] = a.br2 ? jinv * (tot1 - jmp1) : g1;
+  }
+  __syncthreads();
+  // 2. face gradient traces per (element, face point, variable)
+  for (int idx = tid; idx < ecount * NFP * NV; idx += blockDim.x) {
+    const int le = idx / (NFP * NV), r = idx - le * NFP * NV;
+    const int fj = r / NV, v = r - fj * NV;
+    const int f = fj / NFQ, j = fj - f * NFQ;
+    const int64_t e = e0 + le;
+    const double* w0 = sW + (le * NR + v * 2) * NB;
+    const double* w1 = w0 + NB;
+    double acc0 = 0.0, acc1 = 0.0;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      acc0 = fma(phif[fj * NB + b], w0[b], acc0);
+      acc1 = fma(phif[fj * NB + b], w1[b], acc1);
+    }
+    if (a.br2) {
+      const double* O = sO + le * FS + (f * NV + v) * NFQ;
+      const double* S = sS + le * FS + (f * NV + v) * NFQ;
+      const double* L = lmod + (f * NFQ + j) * NFQ;
+      double lift = 0.0;
+#pragma unroll
+      for (int jj = 0; jj < NFQ; ++jj) lift = fma(L[jj], 0.5 * (O[jj] - S[jj]), lift);
+      lift *= a.geom[e * 5 + 4];
+      acc0 = fma(a.fmetric[(e * NF + f) * 2 + 0], lift, acc0);
+      acc1 = fma(a.fmetric[(e * NF + f) * 2 + 1], lift, acc1);
+    }
+    double* out = a.faceGrad + (a.faceBase + e * NF + f) * NR * NFQ + j;
+    out[(v * 2 + 0) * NFQ] = acc0;
+    out[(v * 2 + 1) * NFQ] = acc1;
+  }
+  return true;
+}
+
 template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
 __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_t tile, uint32_t parity, bool loadTables) {
-  using G = DenseGradShape<NB, NQ, NFQ, NF>;
+  if constexpr (AFFINE) return denseGradientAffineTile<NB, NQ, NFQ, NF>(a, tile, parity, loadTables);
+  using G = DenseGradShape<NB, NQ, NFQ, NF, AFFINE>;
   constexpr int NV = 4, NFP = G::NFP, FS = G::FS, NR = NV * 2;
   const int EPB = a.epb;
   extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -546,14 +717,14 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
 
 template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
 __global__ void __launch_bounds__(kMaxTileThreads) denseGradientKernel(DenseGradArgs a) {
-  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF>(a.epb), 1);
+  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF, AFFINE>(a.epb), 1);
   denseGradientTile<NB, NQ, NFQ, NF, AFFINE>(a, blockIdx.x, 0u, true);
 }
 
 template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
 __global__ void __launch_bounds__(kMaxTileThreads)
     denseGradientBatchKernel(const DenseGradArgs* __restrict__ args, const int2* __restrict__ items, int nitems, int epb) {
-  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF>(epb), 1);
+  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF, AFFINE>(epb), 1);
   uint32_t parity = 0;
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const int2 it = items[w];

@@ -19,7 +19,7 @@ KernelVariant stageOf() {
 }
 template <int NB, int NQ, int NFQ, int NF, bool AFF>
 KernelVariant gradOf() {
-  using G = DenseGradShape<NB, NQ, NFQ, NF>;
+  using G = DenseGradShape<NB, NQ, NFQ, NF, AFF>;
   KernelVariant v;
   v.single = reinterpret_cast<const void*>(&denseGradientKernel<NB, NQ, NFQ, NF, AFF>);
   v.batch = reinterpret_cast<const void*>(&denseGradientBatchKernel<NB, NQ, NFQ, NF, AFF>);
