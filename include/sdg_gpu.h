@@ -322,6 +322,34 @@ int sdg_batch_autotune(sdg_batch* batch, int32_t flags);
 int sdg_batch_get_stream(const sdg_batch* batch, void** stream);
 const char* sdg_batch_last_error(const sdg_batch* batch);
 
+/* ---- derivatives: tangent-linear model and discrete adjoint ---------------------------------------
+ * Exact derivatives of the discrete scheme the forward path runs (the reference has none): for the
+ * residual R(U) = du/dt and for whole SSP-RK trajectories, with respect to the state and to the dynamic
+ * viscosity mu.  All vectors are in the volume-point layout of sdg_set_state_point ([point][d+2],
+ * conserved variables).  Supported: affine tensor blocks (quadrangles P>=2 with parallelogram sides,
+ * hexahedra), meshes without boundary faces, Euler or Navier-Stokes with BR1; else SDG_ERR_UNSUPPORTED. */
+/* w_q |J|_q of every volume point: integral of f = sum over points of weight * f (functionals). */
+int sdg_volume_point_weight(sdg_handle* handle, double* weight);
+/* Change the dynamic viscosity (and kappa = cp mu / Pr) of a Navier-Stokes handle. */
+int sdg_set_viscosity(sdg_handle* handle, double dynamic_viscosity);
+/* rate_tangent = R'(U) tangent + dR/dmu viscosity_tangent at the current state U. */
+int sdg_jvp_residual(sdg_handle* handle, const double* tangent, double viscosity_tangent, double* rate_tangent);
+/* cotangent = R'(U)^T rate_cotangent, viscosity_cotangent = <rate_cotangent, dR/dmu> (may be NULL). */
+int sdg_vjp_residual(sdg_handle* handle, const double* rate_cotangent, double* cotangent,
+                     double* viscosity_cotangent);
+/* Advance step_count steps of size delta_time (as sdg_step) and carry the tangent of the state along:
+ * tangent_out = dU_N/dU_0 tangent_in + dU_N/dmu viscosity_tangent. */
+int sdg_jvp_steps(sdg_handle* handle, int32_t step_count, double delta_time, const double* tangent_in,
+                  double viscosity_tangent, double* tangent_out);
+/* Discrete adjoint of step_count steps from the current state U_0 (the state is U_N on return, as after
+ * sdg_step): initial_cotangent = (dU_N/dU_0)^T final_cotangent, viscosity_cotangent =
+ * (dU_N/dmu)^T final_cotangent.  The state is kept every checkpoint_interval steps on the forward sweep
+ * and each interval's stage states are recomputed from its checkpoint on the way back. */
+int sdg_adjoint_steps(sdg_handle* handle, int32_t step_count, double delta_time, int32_t checkpoint_interval,
+                      const double* final_cotangent, double* initial_cotangent, double* viscosity_cotangent);
+/* Device bytes held for checkpoints and stage states (grown on demand, released with the handle). */
+int sdg_adjoint_memory(sdg_handle* handle, int64_t* bytes);
+
 #ifdef __cplusplus
 }
 #endif

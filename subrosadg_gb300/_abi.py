@@ -163,6 +163,13 @@ SIGNATURES = {
     "sdg_batch_autotune": (c_int32, [c_void_p, c_int32]),
     "sdg_batch_get_stream": (c_int32, [c_void_p, POINTER(c_void_p)]),
     "sdg_batch_last_error": (c_char_p, [c_void_p]),
+    "sdg_volume_point_weight": (c_int32, [c_void_p, _p_double]),
+    "sdg_set_viscosity": (c_int32, [c_void_p, c_double]),
+    "sdg_jvp_residual": (c_int32, [c_void_p, _p_double, c_double, _p_double]),
+    "sdg_vjp_residual": (c_int32, [c_void_p, _p_double, _p_double, _p_double]),
+    "sdg_jvp_steps": (c_int32, [c_void_p, c_int32, c_double, _p_double, c_double, _p_double]),
+    "sdg_adjoint_steps": (c_int32, [c_void_p, c_int32, c_double, c_int32, _p_double, _p_double, _p_double]),
+    "sdg_adjoint_memory": (c_int32, [c_void_p, POINTER(c_int64)]),
 }
 
 _lib = None

@@ -1,0 +1,56 @@
+"""torch.autograd binding of the discrete adjoint: a differentiable SSP-RK trajectory.
+
+    u_final = trajectory(solver, u0, mu, steps, dt, checkpoint_interval)
+
+u0 is the state at the volume points ([points][d+2] conserved, float64), mu a 0-d float64 tensor (the
+dynamic viscosity; Navier-Stokes handles only).  The forward runs sdg_step on the GPU; backward runs
+sdg_adjoint_steps (checkpointed reverse sweep) and returns dL/du0 and dL/dmu for any loss L computed in
+torch from u_final, e.g. the kinetic energy sum(w * rho |u|^2 / 2) with w = solver.volume_weights().
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _abi
+
+
+class _Trajectory(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, u0, mu, solver, steps, dt, interval):
+        ns = solver.config.equation == _abi.NAVIER_STOKES
+        if ns:
+            solver.set_viscosity(float(mu))
+        u0_host = u0.detach().to("cpu", torch.float64).contiguous().numpy()
+        solver.set_state_point(u0_host)
+        solver.stepSolver(dt, steps)
+        uN = solver.state_point()
+        ctx.solver, ctx.steps, ctx.dt, ctx.interval, ctx.ns = solver, steps, dt, interval, ns
+        ctx.u0 = u0_host.copy()
+        ctx.mu = float(mu)
+        ctx.device = u0.device
+        return torch.from_numpy(uN).to(u0.device)
+
+    @staticmethod
+    def backward(ctx, grad_uN):
+        s = ctx.solver
+        if ctx.ns:
+            s.set_viscosity(ctx.mu)
+        s.set_state_point(ctx.u0)
+        g = grad_uN.detach().to("cpu", torch.float64).contiguous().numpy()
+        lam0, mubar = s.adjoint_steps(ctx.dt, ctx.steps, g, ctx.interval)
+        dmu = torch.tensor(mubar if ctx.ns else 0.0, dtype=torch.float64)
+        return torch.from_numpy(np.ascontiguousarray(lam0)).to(ctx.device), dmu, None, None, None, None
+
+
+def trajectory(solver, u0: torch.Tensor, mu: torch.Tensor, steps: int, dt: float, checkpoint_interval: int = 25):
+    """U_N as a differentiable function of (u0, mu) through `steps` steps of size dt."""
+    return _Trajectory.apply(u0, mu, solver, steps, dt, checkpoint_interval)
+
+
+def kinetic_energy(solver, u: torch.Tensor) -> torch.Tensor:
+    """Integral of rho |u|^2 / 2 over the domain from point values (volume-point quadrature)."""
+    w = torch.from_numpy(solver.volume_weights()).to(u.device)
+    d = u.shape[1] - 2
+    rho, m = u[:, 0], u[:, 1:1 + d]
+    return torch.sum(w * 0.5 * torch.sum(m * m, 1) / rho)

@@ -1,0 +1,489 @@
+// Tangent-linear model and discrete adjoint of the GB300 DG path (sdg_jvp_*, sdg_vjp_*, sdg_adjoint_steps).
+//
+// The reference has no differentiation; these are the spec additions.  Both are exact derivatives of
+// the discrete scheme the forward path runs (same quadrature, same fluxes, same SSP-RK stages), so
+//   <lambda, JVP(dU)> = <VJP(lambda), dU>
+// holds to round-off, for one residual and for whole trajectories.  Scope: element blocks that are affine
+// tensor blocks (quadrangles P>=2 with straight parallelogram sides, hexahedra), interior (periodic) faces,
+// Euler or Navier-Stokes with BR1; other configurations return SDG_ERR_UNSUPPORTED.
+//
+// Trajectories: the tangent runs stage by stage beside the forward state.  The adjoint stores the state
+// every `checkpoint_interval` steps on a forward sweep, then per segment (last first) recomputes the
+// segment's stage inputs from its checkpoint and walks them backwards:
+//   stage s of the step:  U_{s+1} = c0 U^n + c1 U_s + c2 dt R(U_s)
+//   reverse:              lam_s = c1 lam_{s+1} + c2 dt R'(U_s)^T lam_{s+1},   lam^n += c0 lam_{s+1}
+// and dJ/dmu accumulates c2 dt <lam_{s+1}, dR/dmu(U_s)>.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "sdg_internal.hpp"
+#include "sdg_kernels_adjoint.cuh"
+
+using namespace sdg;
+
+struct AdjointState {
+  AdjointKernels k;
+  double* dU[2] = {nullptr, nullptr};
+  double* dface = nullptr;
+  double* dfaceOther = nullptr;
+  double* dgrad = nullptr;
+  double* dfaceGrad = nullptr;
+  double* dflux = nullptr;
+  double* lamIn = nullptr;
+  double* lamStage = nullptr;
+  double* lamBase = nullptr;
+  double* lamU = nullptr;
+  double* lamG = nullptr;
+  double* lamH = nullptr;
+  double* lamTr = nullptr;
+  double* lamTg = nullptr;
+  double* lamUp = nullptr;
+  double* muPart = nullptr;
+  int64_t muTiles = 0, muFaces = 0;
+  double* pts = nullptr;           // point-layout conversion buffer
+  std::vector<double*> pool;       // checkpoints and stage states (grown on demand)
+  int64_t launches = 0;
+};
+
+namespace sdg {
+void destroyAdjoint(sdg_handle* h) {
+  AdjointState* A = h->adj;
+  if (!A) return;
+  for (double* p : {A->dU[0], A->dU[1], A->dface, A->dfaceOther, A->dgrad, A->dfaceGrad, A->dflux, A->lamIn,
+                    A->lamStage, A->lamBase, A->lamU, A->lamG, A->lamH, A->lamTr, A->lamTg, A->lamUp, A->muPart,
+                    A->pts})
+    cudaFree(p);
+  for (double* p : A->pool) cudaFree(p);
+  delete A;
+  h->adj = nullptr;
+}
+}  // namespace sdg
+
+namespace {
+
+double* alloc(size_t n) {
+  double* p = nullptr;
+  SDG_CUDA(cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(double)));
+  return p;
+}
+
+AdjointState* adjoint(sdg_handle* h) {
+  if (h->hostOnly) throw Failure(SDG_ERR_STATE, "host-only handle (created with device < 0)");
+  if (!h->hasState) throw Failure(SDG_ERR_STATE, "no state");
+  if (h->adj) return h->adj;
+  for (const DevBlock& B : h->blocks)
+    if (B.kind != kTensor || !B.affine)
+      throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (quadrangles P>=2, hexahedra)");
+  if (h->nBoundary > 0) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need a mesh without boundary faces (periodic)");
+  if (h->ns && h->cfg.viscous_flux != SDG_VISCOUS_BR1) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of BR2 are not built");
+  std::unique_ptr<AdjointState> A(new AdjointState());
+  adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, A->k);
+  adjointTileKernels(h->dim, h->blocks[0].n, h->ns, A->k);
+  if (!A->k.valid()) throw Failure(SDG_ERR_UNSUPPORTED, "no derivative kernels for this configuration");
+  SDG_CUDA(cudaSetDevice(h->device));
+  for (const void* fn : {A->k.jvpStage, A->k.vjpVolume, A->k.vjpGradient, A->k.vjpTrace}) configureKernel(fn, h->device);
+  const size_t S = h->stateCount, F = h->faceCount;
+  A->dU[0] = alloc(S); A->dU[1] = alloc(S);
+  A->dface = alloc(F); A->dflux = alloc(F);
+  A->lamIn = alloc(S); A->lamStage = alloc(S); A->lamBase = alloc(S); A->lamU = alloc(S);
+  A->lamH = alloc(F); A->lamTr = alloc(F);
+  if (h->ns) {
+    A->dfaceOther = alloc(F); A->dgrad = alloc(h->gradCount); A->dfaceGrad = alloc(F * h->dim);
+    A->lamG = alloc(h->gradCount); A->lamTg = alloc(F * h->dim); A->lamUp = alloc(F);
+  }
+  for (const DevBlock& B : h->blocks) A->muTiles += (B.ne + A->k.epb - 1) / A->k.epb;
+  A->muFaces = (h->nInterior * h->nfq + kFaceThreads - 1) / kFaceThreads;
+  A->muPart = alloc(size_t(A->muTiles + A->muFaces));
+  A->pts = alloc(size_t(h->volumePoints) * h->nv);
+  for (double* p : {A->dU[0], A->dU[1], A->dface, A->dflux, A->lamIn, A->lamStage, A->lamBase, A->lamU, A->lamH, A->lamTr})
+    SDG_CUDA(cudaMemsetAsync(p, 0, (p == A->dface || p == A->dflux || p == A->lamH || p == A->lamTr ? F : S) * 8, h->stream));
+  if (h->ns) {
+    SDG_CUDA(cudaMemsetAsync(A->dfaceOther, 0, F * 8, h->stream));
+    SDG_CUDA(cudaMemsetAsync(A->dgrad, 0, h->gradCount * 8, h->stream));
+    SDG_CUDA(cudaMemsetAsync(A->dfaceGrad, 0, F * h->dim * 8, h->stream));
+    SDG_CUDA(cudaMemsetAsync(A->lamG, 0, h->gradCount * 8, h->stream));
+    SDG_CUDA(cudaMemsetAsync(A->lamTg, 0, F * h->dim * 8, h->stream));
+    SDG_CUDA(cudaMemsetAsync(A->lamUp, 0, F * 8, h->stream));
+  }
+  SDG_CUDA(cudaMemsetAsync(A->muPart, 0, size_t(A->muTiles + A->muFaces) * 8, h->stream));
+  h->adj = A.release();
+  return h->adj;
+}
+
+AdjArgs baseArgs(sdg_handle* h, const DevBlock* B, const double* U) {
+  AdjArgs a;
+  std::memset(&a, 0, sizeof(a));
+  if (B) {
+    a.u = U + B->stateOffset; a.geom = B->geom; a.tables = B->tables;
+    a.grad = h->ns ? h->grad + B->gradOffset : nullptr;
+    a.ne = B->ne; a.faceBase = B->faceBase;
+  }
+  a.face = h->face; a.faceGrad = h->faceGrad; a.conn = h->fconn; a.fgeo = h->fgeo; a.status = h->status;
+  a.nface = h->nInterior; a.n1d = h->n1d; a.epb = h->adj->k.epb;
+  return a;
+}
+
+void launch(sdg_handle* h, const void* fn, int64_t grid, int threads, size_t smem, AdjArgs& a, bool withPhys) {
+  if (grid <= 0) return;
+  Phys ph = h->ph;
+  void* p[2] = {&a, &ph};
+  SDG_CUDA(cudaLaunchKernel(fn, dim3(unsigned(grid)), dim3(unsigned(threads)), p, smem, h->stream));
+  SDG_CUDA(cudaGetLastError());
+  h->launches++;
+  (void)withPhys;
+}
+
+int64_t tiles(const sdg_handle* h, const DevBlock& B) { return (B.ne + h->adj->k.epb - 1) / h->adj->k.epb; }
+int64_t faceGrid(const sdg_handle* h) { return (h->nInterior * h->nfq + kFaceThreads - 1) / kFaceThreads; }
+
+// Traces of state buffer `u` into `face` (the forward stage kernel's trace-only pass).
+void traces(sdg_handle* h, const double* u, double* face) {
+  std::vector<Rec> recs;
+  for (DevBlock& B : h->blocks) {
+    Rec r = stageRec(h, B);
+    r.sa.uin = u + B.stateOffset;
+    r.sa.face = face;
+    r.sa.doTrace = 1; r.sa.doVolume = 0; r.sa.doUpdate = 0;
+    recs.push_back(r);
+  }
+  runRecs(h, recs, h->stream);
+}
+
+// BR1 gradient pass of state `u` whose traces are in `face`: neighbour traces into `other`, node gradient
+// into `grad`, gradient traces into `faceGrad` (the forward kernels; linear, so they serve tangents too).
+void gradientOf(sdg_handle* h, const double* u, double* face, double* other, double* grad, double* faceGrad) {
+  std::vector<Rec> recs;
+  Rec x = faceRec(h, kOpExchange);
+  x.fa.face = face; x.fa.other = other;
+  recs.push_back(x);
+  for (DevBlock& B : h->blocks) {
+    Rec r = gradRec(h, B, 0);
+    r.ga.u = u + B.stateOffset; r.ga.face = face; r.ga.faceOther = other;
+    r.ga.grad = grad + B.gradOffset; r.ga.faceGrad = faceGrad;
+    recs.push_back(r);
+  }
+  runRecs(h, recs, h->stream);
+}
+
+// Forward quantities at state `u` (= state[1]): traces in h->face; NS: h->faceOther, h->grad, h->faceGrad.
+void forwardAt(sdg_handle* h, const double* u) {
+  traces(h, u, h->face);
+  if (h->ns) gradientOf(h, u, h->face, h->faceOther, h->grad, h->faceGrad);
+}
+
+// Tangent face fluxes into dflux from tangent traces dface (and dfaceGrad), forward traces in h->face.
+void tangentFaces(sdg_handle* h, double dmu) {
+  AdjointState* A = h->adj;
+  AdjArgs a = baseArgs(h, nullptr, nullptr);
+  a.dface = A->dface; a.dfaceGrad = A->dfaceGrad; a.dflux = A->dflux; a.dmu = dmu;
+  launch(h, A->k.jvpFace, faceGrid(h), kFaceThreads, 0, a, true);
+}
+
+// Tangent element kernels: from tangent state du (traces in dface, dflux computed), write drate and/or
+// the RK tangent update dout = c0 dbase + c1 du + c2dt dR with its traces.
+void tangentElements(sdg_handle* h, const double* u, const double* du, double dmu, double* drate, const double* dbase,
+                     double* dout, double c0, double c1, double c2dt) {
+  AdjointState* A = h->adj;
+  for (DevBlock& B : h->blocks) {
+    AdjArgs a = baseArgs(h, &B, u);
+    a.du = du + B.stateOffset;
+    a.dgrad = h->ns ? A->dgrad + B.gradOffset : nullptr;
+    a.dflux = A->dflux; a.dmu = dmu;
+    a.drate = drate ? drate + B.stateOffset : nullptr;
+    a.dbase = dbase ? dbase + B.stateOffset : nullptr;
+    a.dout = dout ? dout + B.stateOffset : nullptr;
+    a.dtrace = dout ? A->dface : nullptr;
+    a.c0 = c0; a.c1 = c1; a.c2dt = c2dt;
+    launch(h, A->k.jvpStage, tiles(h, B), A->k.threads, A->k.jvpSmem, a, true);
+  }
+}
+
+// Tangent of the residual at state[1] (forward quantities computed here) in direction du.
+void jvpResidual(sdg_handle* h, const double* du, double dmu, double* drate) {
+  AdjointState* A = h->adj;
+  forwardAt(h, h->state[1]);
+  traces(h, du, A->dface);
+  if (h->ns) gradientOf(h, du, A->dface, A->dfaceOther, A->dgrad, A->dfaceGrad);
+  tangentFaces(h, dmu);
+  tangentElements(h, h->state[1], du, dmu, drate, nullptr, nullptr, 0.0, 0.0, 0.0);
+}
+
+// Adjoint of the residual at state[1] (forward quantities already computed by forwardAt) for cotangent lam.
+// Without RK coefficients (lamStage = lamBase = null) the result R'^T lam goes to A->lamU.  Returns
+// sum(muPart) = mu <lam, dR/dmu> (NS) after a synchronisation, else 0.
+double vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* lamStage, double* lamBase,
+                   bool accumulateAll, double c0, double c1, double c2dt) {
+  AdjointState* A = h->adj;
+  const int NT = A->k.threads;
+  int64_t tileOff = 0;
+  for (DevBlock& B : h->blocks) {
+    AdjArgs a = baseArgs(h, &B, h->state[1]);
+    a.lam = lam + B.stateOffset; a.lamU = A->lamU + B.stateOffset;
+    a.lamG = h->ns ? A->lamG + B.gradOffset : nullptr;
+    a.lamH = A->lamH; a.muPart = A->muPart + tileOff;
+    launch(h, A->k.vjpVolume, tiles(h, B), NT, A->k.vjpSmem, a, true);
+    tileOff += tiles(h, B);
+  }
+  {
+    AdjArgs a = baseArgs(h, nullptr, nullptr);
+    a.lamH = A->lamH; a.lamTr = A->lamTr; a.lamTg = A->lamTg; a.muPart = A->muPart + A->muTiles;
+    launch(h, A->k.vjpFace, faceGrid(h), kFaceThreads, 0, a, true);
+  }
+  if (h->ns) {
+    for (DevBlock& B : h->blocks) {
+      AdjArgs a = baseArgs(h, &B, h->state[1]);
+      a.lamG = A->lamG + B.gradOffset; a.lamTg = A->lamTg; a.lamU = A->lamU + B.stateOffset; a.lamUp = A->lamUp;
+      launch(h, A->k.vjpGradient, tiles(h, B), NT, A->k.vjpSmem, a, false);
+    }
+    AdjArgs a = baseArgs(h, nullptr, nullptr);
+    a.lamUp = A->lamUp; a.lamTr = A->lamTr;
+    launch(h, A->k.vjpExchange, faceGrid(h), kFaceThreads, 0, a, false);
+  }
+  for (DevBlock& B : h->blocks) {
+    AdjArgs a = baseArgs(h, &B, h->state[1]);
+    a.lamU = A->lamU + B.stateOffset; a.lamTr = A->lamTr;
+    a.lamIn = lamIn ? lamIn + B.stateOffset : nullptr;
+    a.lamStage = lamStage ? lamStage + B.stateOffset : nullptr;
+    a.lamBase = lamBase ? lamBase + B.stateOffset : nullptr;
+    a.accumulateAll = accumulateAll;
+    a.c0 = c0; a.c1 = c1; a.c2dt = c2dt;
+    launch(h, A->k.vjpTrace, tiles(h, B), NT, A->k.vjpSmem, a, false);
+  }
+  if (!h->ns) return 0.0;
+  std::vector<double> part(size_t(A->muTiles + A->muFaces));
+  SDG_CUDA(cudaMemcpyAsync(part.data(), A->muPart, part.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+  double s = 0.0;
+  for (double x : part) s += x;
+  return s;
+}
+
+void uploadPoints(sdg_handle* h, const double* host, double* st) {
+  AdjointState* A = h->adj;
+  SDG_CUDA(cudaMemcpyAsync(A->pts, host, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyHostToDevice, h->stream));
+  pointsToStateBuffer(h, A->pts, st);
+}
+
+void downloadPoints(sdg_handle* h, const double* st, double* host) {
+  AdjointState* A = h->adj;
+  stateToPointsBuffer(h, st, A->pts);
+  SDG_CUDA(cudaMemcpyAsync(host, A->pts, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+void copyState(sdg_handle* h, double* dst, const double* src) {
+  SDG_CUDA(cudaMemcpyAsync(dst, src, h->stateCount * 8, cudaMemcpyDeviceToDevice, h->stream));
+}
+
+double* poolBuffer(sdg_handle* h, size_t i) {
+  AdjointState* A = h->adj;
+  while (A->pool.size() <= i) A->pool.push_back(alloc(h->stateCount));
+  return A->pool[i];
+}
+
+// Forward step records split by stage (records of stage s have seq / 8 == s).
+std::vector<std::vector<Rec>> stepByStage(sdg_handle* h, double dt, int stages) {
+  std::vector<Rec> all;
+  emitStep(h, dt, false, all);
+  std::vector<std::vector<Rec>> out(stages);
+  for (const Rec& r : all) out[std::min(stages - 1, r.seq / 8)].push_back(r);
+  return out;
+}
+
+// Tangent-linear of `steps` steps: the forward state advances too.
+void jvpSteps(sdg_handle* h, int steps, double dt, double dmu) {
+  AdjointState* A = h->adj;
+  const int ti = h->cfg.time_integration, S = ti + 1;
+  traces(h, A->dU[0], A->dface);
+  const auto stages = stepByStage(h, dt, S);
+  for (int n = 0; n < steps; ++n) {
+    for (int s = 0; s < S; ++s) {
+      const int in = s == 0 ? 0 : 1, out = s == S - 1 ? 0 : 1;
+      std::vector<Rec> flux, update;
+      for (const Rec& r : stages[s]) (r.seq % 8 < 3 ? flux : update).push_back(r);
+      if (h->ns) {
+        runRecs(h, flux, h->stream);  // forward gradient pass and viscous face fluxes (traces stay in face)
+        gradientOf(h, A->dU[in], A->dface, A->dfaceOther, A->dgrad, A->dfaceGrad);
+        tangentFaces(h, dmu);
+      } else {
+        tangentFaces(h, dmu);         // reads the traces before the Euler face kernel overwrites them
+        runRecs(h, flux, h->stream);
+      }
+      tangentElements(h, h->state[in], A->dU[in], dmu, nullptr, A->dU[0], A->dU[out], kRk[ti][s][0], kRk[ti][s][1],
+                      kRk[ti][s][2] * dt);
+      runRecs(h, update, h->stream);
+    }
+  }
+}
+
+// Discrete adjoint of `steps` steps from the current state (U_0): on entry A->lamIn holds dJ/dU_N; on exit
+// A->lamIn holds dJ/dU_0 and the state is U_N.  Returns dJ/dmu (NS; 0 for Euler).
+double adjointSteps(sdg_handle* h, int steps, double dt, int interval) {
+  AdjointState* A = h->adj;
+  const int ti = h->cfg.time_integration, S = ti + 1;
+  const int segments = (steps + interval - 1) / interval;
+  // forward sweep with checkpoints (pool[0..segments-1]); pool[segments] keeps U_N
+  for (int g = 0; g < segments; ++g) {
+    copyState(h, poolBuffer(h, g), h->state[0]);
+    const int n = std::min(interval, steps - g * interval);
+    std::vector<Rec> recs;
+    emitStep(h, dt, true, recs);
+    for (int k = 0; k < n; ++k) runRecs(h, recs, h->stream);
+  }
+  double* finalState = poolBuffer(h, segments);
+  copyState(h, finalState, h->state[0]);
+  const size_t storeBase = size_t(segments) + 1;
+  const auto stages = stepByStage(h, dt, S);
+  SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
+  double mubar = 0.0;
+  for (int g = segments - 1; g >= 0; --g) {
+    const int n0 = g * interval, n1 = std::min(steps, n0 + interval);
+    // recompute the segment, keeping every stage input
+    copyState(h, h->state[0], poolBuffer(h, g));
+    traces(h, h->state[0], h->face);
+    for (int n = n0; n < n1; ++n)
+      for (int s = 0; s < S; ++s) {
+        copyState(h, poolBuffer(h, storeBase + size_t(n - n0) * S + s), h->state[s == 0 ? 0 : 1]);
+        runRecs(h, stages[s], h->stream);
+      }
+    // reverse
+    for (int n = n1 - 1; n >= n0; --n)
+      for (int s = S - 1; s >= 0; --s) {
+        copyState(h, h->state[1], poolBuffer(h, storeBase + size_t(n - n0) * S + s));
+        forwardAt(h, h->state[1]);
+        const double c0 = kRk[ti][s][0], c1 = kRk[ti][s][1], c2dt = kRk[ti][s][2] * dt;
+        double m;
+        if (s > 0) {
+          m = vjpResidual(h, A->lamIn, A->lamIn, A->lamStage, A->lamBase, false, c0, c1, c2dt);
+          std::swap(A->lamIn, A->lamStage);
+        } else {
+          m = vjpResidual(h, A->lamIn, A->lamIn, nullptr, A->lamBase, true, c0, c1, c2dt);
+          std::swap(A->lamIn, A->lamBase);
+          SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
+        }
+        if (h->ns && h->ph.mu > 0.0) mubar += c2dt * m / h->ph.mu;
+      }
+  }
+  copyState(h, h->state[0], finalState);
+  traces(h, h->state[0], h->face);
+  return mubar;
+}
+
+int adjFail(sdg_handle* h, const Failure& f) {
+  h->err = f.what();
+  return f.code;
+}
+
+}  // namespace
+
+#pragma GCC visibility push(default)
+extern "C" {
+
+int sdg_volume_point_weight(sdg_handle* h, double* weight) {
+  if (!h || !weight) return SDG_ERR_INVALID_ARGUMENT;
+  for (const DevBlock& B : h->blocks) {
+    const int gs = B.dim * B.dim + 1;
+    for (int64_t e = 0; e < B.ne; ++e)
+      for (int q = 0; q < B.nq; ++q) {
+        const double jinv = B.affine ? B.geomHost[size_t(e) * B.geomStride + gs - 1]
+                                     : B.geomHost[size_t(e) * B.geomStride + size_t(q) * gs + gs - 1];
+        weight[B.pointOffset + size_t(e) * B.nq + q] = B.qweight[q] / jinv;
+      }
+  }
+  return SDG_OK;
+}
+
+int sdg_set_viscosity(sdg_handle* h, double mu) {
+  if (!h || !(mu >= 0.0) || !std::isfinite(mu)) return SDG_ERR_INVALID_ARGUMENT;
+  h->cfg.dynamic_viscosity = mu;
+  h->ph.mu = mu;
+  h->ph.kappa = h->cfg.prandtl_number > 0 ? h->cfg.specific_heat_constant_pressure * mu / h->cfg.prandtl_number : 0.0;
+  dropGraph(h);
+  return SDG_OK;
+}
+
+int sdg_jvp_residual(sdg_handle* h, const double* tangent, double viscosity_tangent, double* rate_tangent) {
+  if (!h || !tangent || !rate_tangent || !std::isfinite(viscosity_tangent)) return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    AdjointState* A = adjoint(h);
+    SDG_CUDA(cudaSetDevice(h->device));
+    copyState(h, h->state[1], h->state[0]);
+    uploadPoints(h, tangent, A->dU[0]);
+    jvpResidual(h, A->dU[0], viscosity_tangent, A->dU[1]);
+    downloadPoints(h, A->dU[1], rate_tangent);
+    traces(h, h->state[0], h->face);
+    checkStatus(h);
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_vjp_residual(sdg_handle* h, const double* rate_cotangent, double* cotangent, double* viscosity_cotangent) {
+  if (!h || !rate_cotangent || !cotangent) return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    AdjointState* A = adjoint(h);
+    SDG_CUDA(cudaSetDevice(h->device));
+    copyState(h, h->state[1], h->state[0]);
+    uploadPoints(h, rate_cotangent, A->lamIn);
+    forwardAt(h, h->state[1]);
+    const double m = vjpResidual(h, A->lamIn, nullptr, nullptr, nullptr, false, 0.0, 0.0, 0.0);
+    downloadPoints(h, A->lamU, cotangent);
+    if (viscosity_cotangent) *viscosity_cotangent = h->ns && h->ph.mu > 0.0 ? m / h->ph.mu : 0.0;
+    traces(h, h->state[0], h->face);
+    checkStatus(h);
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_jvp_steps(sdg_handle* h, int32_t steps, double dt, const double* tangent_in, double viscosity_tangent,
+                  double* tangent_out) {
+  if (!h || steps < 0 || !tangent_in || !tangent_out || !std::isfinite(dt) || !std::isfinite(viscosity_tangent))
+    return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    AdjointState* A = adjoint(h);
+    SDG_CUDA(cudaSetDevice(h->device));
+    uploadPoints(h, tangent_in, A->dU[0]);
+    jvpSteps(h, steps, dt, viscosity_tangent);
+    downloadPoints(h, A->dU[0], tangent_out);
+    checkStatus(h);
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_adjoint_steps(sdg_handle* h, int32_t steps, double dt, int32_t interval, const double* final_cotangent,
+                      double* initial_cotangent, double* viscosity_cotangent) {
+  if (!h || steps < 1 || interval < 1 || !final_cotangent || !initial_cotangent || !std::isfinite(dt))
+    return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    AdjointState* A = adjoint(h);
+    SDG_CUDA(cudaSetDevice(h->device));
+    uploadPoints(h, final_cotangent, A->lamIn);
+    const double m = adjointSteps(h, steps, dt, interval);
+    downloadPoints(h, A->lamIn, initial_cotangent);
+    if (viscosity_cotangent) *viscosity_cotangent = m;
+    checkStatus(h);
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_adjoint_memory(sdg_handle* h, int64_t* bytes) {
+  if (!h || !bytes) return SDG_ERR_INVALID_ARGUMENT;
+  *bytes = 0;
+  if (!h->adj) return SDG_OK;
+  const AdjointState* A = h->adj;
+  *bytes = int64_t(A->pool.size()) * int64_t(h->stateCount) * 8;
+  return SDG_OK;
+}
+
+}  // extern "C"
+#pragma GCC visibility pop

@@ -10,8 +10,14 @@
 // The arithmetic is reorganised to cut FP64 instructions (the GB300 FP64 pipe issues ~2 DFMA/clk/SM):
 // one reciprocal of rho per point instead of d+1 divisions, and divisions as a hardware reciprocal
 // estimate refined by Newton-Raphson.  Results agree with the reference formulas to round-off.
+//
+// The interior physics (states, convective fluxes, viscous terms) is generic over the scalar type T:
+// double is the forward path; the dual numbers of sdg_dual.cuh give its exact derivatives for the
+// tangent-linear and adjoint kernels.  The boundary states are double only.
 #pragma once
 #include <cstdint>
+
+#include "sdg_dual.cuh"
 
 namespace sdg {
 
@@ -26,7 +32,11 @@ struct Phys {
 // least doubles the number of correct bits; the result is within a few ulp of 1/x.
 __device__ __forceinline__ double rcp(double x) {
   double r;
+#ifdef __CUDA_ARCH__
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+#else
+  r = 1.0 / x;  // host builds of this header (tests of the pointwise physics)
+#endif
   double e = fma(-x, r, 1.0);
   r = fma(r, e, r);
   e = fma(-x, r, 1.0);
@@ -34,149 +44,149 @@ __device__ __forceinline__ double rcp(double x) {
   return r;
 }
 
-template <int D>
+template <int D, class T = double>
 struct State {
-  double r, m[D], E;   // conserved
-  double ir, u[D], p;  // 1/rho, velocity, pressure
+  T r, m[D], E;   // conserved
+  T ir, u[D], p;  // 1/rho, velocity, pressure
 };
 
-template <int D>
-__device__ __forceinline__ void makeState(State<D>& s, const double* U, const Phys& ph) {
+template <int D, class T>
+__device__ __forceinline__ void makeState(State<D, T>& s, const T* U, const Phys& ph) {
   s.r = U[0];
 #pragma unroll
   for (int k = 0; k < D; ++k) s.m[k] = U[1 + k];
   s.E = U[D + 1];
-  s.ir = rcp(s.r);
-  double mu = 0.0;
+  s.ir = rcpT(s.r);
+  T mu = T(0.0);
 #pragma unroll
-  for (int k = 0; k < D; ++k) { s.u[k] = s.m[k] * s.ir; mu = fma(s.m[k], s.u[k], mu); }
-  s.p = ph.gm1 * fma(-0.5, mu, s.E);
+  for (int k = 0; k < D; ++k) { s.u[k] = s.m[k] * s.ir; mu = fmaT(s.m[k], s.u[k], mu); }
+  s.p = ph.gm1 * fmaT(-0.5, mu, s.E);
 }
 
-template <int D>
-__device__ __forceinline__ double dotn(const double* a, const double* n) {
-  double s = a[0] * n[0];
+template <int D, class T>
+__device__ __forceinline__ T dotn(const T* a, const double* n) {
+  T s = a[0] * n[0];
 #pragma unroll
-  for (int k = 1; k < D; ++k) s = fma(a[k], n[k], s);
+  for (int k = 1; k < D; ++k) s = fmaT(a[k], n[k], s);
   return s;
 }
 
-template <int D>
-__device__ __forceinline__ void normalFlux(const State<D>& s, const double* n, double un, double* f) {
+template <int D, class T>
+__device__ __forceinline__ void normalFlux(const State<D, T>& s, const double* n, T un, T* f) {
   f[0] = s.r * un;
 #pragma unroll
-  for (int k = 0; k < D; ++k) f[1 + k] = fma(s.m[k], un, s.p * n[k]);
+  for (int k = 0; k < D; ++k) f[1 + k] = fmaT(s.m[k], un, s.p * n[k]);
   f[D + 1] = (s.E + s.p) * un;
 }
 
-template <int D>
-__device__ __forceinline__ void fluxCentral(const State<D>& l, const State<D>& r, const double* n, double* h) {
-  double fl[D + 2], fr[D + 2];
+template <int D, class T>
+__device__ __forceinline__ void fluxCentral(const State<D, T>& l, const State<D, T>& r, const double* n, T* h) {
+  T fl[D + 2], fr[D + 2];
   normalFlux(l, n, dotn<D>(l.u, n), fl);
   normalFlux(r, n, dotn<D>(r.u, n), fr);
 #pragma unroll
   for (int i = 0; i < D + 2; ++i) h[i] = 0.5 * (fl[i] + fr[i]);
 }
 
-template <int D>
-__device__ __forceinline__ void fluxLaxFriedrichs(const State<D>& l, const State<D>& r, const double* n,
-                                                  const Phys& ph, double* h) {
-  const double unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
-  double fl[D + 2], fr[D + 2];
+template <int D, class T>
+__device__ __forceinline__ void fluxLaxFriedrichs(const State<D, T>& l, const State<D, T>& r, const double* n,
+                                                  const Phys& ph, T* h) {
+  const T unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
+  T fl[D + 2], fr[D + 2];
   normalFlux(l, n, unl, fl);
   normalFlux(r, n, unr, fr);
-  const double cl = sqrt(ph.gamma * l.p * l.ir), cr = sqrt(ph.gamma * r.p * r.ir);
-  const double sr = fmax(fabs(unl) + cl, fabs(unr) + cr);
-  h[0] = 0.5 * fma(-sr, r.r - l.r, fl[0] + fr[0]);
+  const T cl = sqrtT(ph.gamma * l.p * l.ir), cr = sqrtT(ph.gamma * r.p * r.ir);
+  const T sr = fmaxT(fabsT(unl) + cl, fabsT(unr) + cr);
+  h[0] = 0.5 * fmaT(-sr, r.r - l.r, fl[0] + fr[0]);
 #pragma unroll
-  for (int k = 0; k < D; ++k) h[1 + k] = 0.5 * fma(-sr, r.m[k] - l.m[k], fl[1 + k] + fr[1 + k]);
-  h[D + 1] = 0.5 * fma(-sr, r.E - l.E, fl[D + 1] + fr[D + 1]);
+  for (int k = 0; k < D; ++k) h[1 + k] = 0.5 * fmaT(-sr, r.m[k] - l.m[k], fl[1 + k] + fr[1 + k]);
+  h[D + 1] = 0.5 * fmaT(-sr, r.E - l.E, fl[D + 1] + fr[D + 1]);
 }
 
 // HLLC with PVRS pressure estimate and Toro's wave-speed factors (ConvectiveFlux.cpp:136-238).
-template <int D>
-__device__ __forceinline__ void fluxHLLC(const State<D>& l, const State<D>& r, const double* n, const Phys& ph,
-                                         double* h) {
-  const double unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
-  const double cl = sqrt(ph.gamma * l.p * l.ir), cr = sqrt(ph.gamma * r.p * r.ir);
-  const double rhoAvg = 0.5 * (l.r + r.r), cAvg = 0.5 * (cl + cr);
-  const double ps = fmax(0.0, fma(-(unr - unl), rhoAvg * cAvg, 0.5 * (l.p + r.p)));
+template <int D, class T>
+__device__ __forceinline__ void fluxHLLC(const State<D, T>& l, const State<D, T>& r, const double* n, const Phys& ph,
+                                         T* h) {
+  const T unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
+  const T cl = sqrtT(ph.gamma * l.p * l.ir), cr = sqrtT(ph.gamma * r.p * r.ir);
+  const T rhoAvg = 0.5 * (l.r + r.r), cAvg = 0.5 * (cl + cr);
+  const T ps = fmaxT(0.0, fmaT(-(unr - unl), rhoAvg * cAvg, 0.5 * (l.p + r.p)));
   const double g2 = ph.hllc_g2;
-  const double ql = ps <= l.p ? 1.0 : sqrt(fma(g2, fma(ps, rcp(l.p), -1.0), 1.0));
-  const double sl = fma(-cl, ql, unl);
+  const T ql = ps <= l.p ? T(1.0) : sqrtT(fmaT(g2, fmaT(ps, rcpT(l.p), -1.0), 1.0));
+  const T sl = fmaT(-cl, ql, unl);
   if (sl >= 0.0) { normalFlux(l, n, unl, h); return; }
-  const double qr = ps <= r.p ? 1.0 : sqrt(fma(g2, fma(ps, rcp(r.p), -1.0), 1.0));
-  const double sr = fma(cr, qr, unr);
+  const T qr = ps <= r.p ? T(1.0) : sqrtT(fmaT(g2, fmaT(ps, rcpT(r.p), -1.0), 1.0));
+  const T sr = fmaT(cr, qr, unr);
   if (sr <= 0.0) { normalFlux(r, n, unr, h); return; }
-  const double al = l.r * (sl - unl), ar = r.r * (sr - unr);
-  const double ss = (r.p - l.p + al * unl - ar * unr) * rcp(al - ar);
+  const T al = l.r * (sl - unl), ar = r.r * (sr - unr);
+  const T ss = (r.p - l.p + al * unl - ar * unr) * rcpT(al - ar);
   const bool left = ss >= 0.0;
-  const State<D>& s = left ? l : r;
-  const double sk = left ? sl : sr, un = left ? unl : unr, a = left ? al : ar;
-  double f[D + 2];
+  const State<D, T>& s = left ? l : r;
+  const T sk = left ? sl : sr, un = left ? unl : unr, a = left ? al : ar;
+  T f[D + 2];
   normalFlux(s, n, un, f);
-  const double inv = rcp(sk - ss);
+  const T inv = rcpT(sk - ss);
   // star state minus the side's conserved state, times the wave speed
-  const double rs = a * inv;
-  h[0] = fma(sk, rs - s.r, f[0]);
-  const double dp = ps - s.p;
+  const T rs = a * inv;
+  h[0] = fmaT(sk, rs - s.r, f[0]);
+  const T dp = ps - s.p;
 #pragma unroll
   for (int k = 0; k < D; ++k) {
-    const double ms = fma(a, s.u[k], dp * n[k]) * inv;
-    h[1 + k] = fma(sk, ms - s.m[k], f[1 + k]);
+    const T ms = fmaT(a, s.u[k], dp * n[k]) * inv;
+    h[1 + k] = fmaT(sk, ms - s.m[k], f[1 + k]);
   }
-  const double Es = fma(a, s.E * s.ir, fma(ps, ss, -s.p * un)) * inv;
-  h[D + 1] = fma(sk, Es - s.E, f[D + 1]);
+  const T Es = fmaT(a, s.E * s.ir, fmaT(ps, ss, -s.p * un)) * inv;
+  h[D + 1] = fmaT(sk, Es - s.E, f[D + 1]);
 }
 
 // Roe flux with Harten's entropy fix, delta = c/20 (ConvectiveFlux.cpp:240-350).
-template <int D>
-__device__ __forceinline__ void fluxRoe(const State<D>& l, const State<D>& r, const double* n, const Phys& ph,
-                                        double* h) {
+template <int D, class T>
+__device__ __forceinline__ void fluxRoe(const State<D, T>& l, const State<D, T>& r, const double* n, const Phys& ph,
+                                        T* h) {
   const double g = ph.gamma;
-  const double unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
-  double fl[D + 2], fr[D + 2];
+  const T unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
+  T fl[D + 2], fr[D + 2];
   normalFlux(l, n, unl, fl);
   normalFlux(r, n, unr, fr);
-  const double sl = sqrt(l.r), sr = sqrt(r.r);
-  const double is = rcp(sl + sr);
-  const double wl = sl * is, wr = sr * is;
-  const double rho = sl * sr;
-  double u[D], u2 = 0.0, un = 0.0;
+  const T sl = sqrtT(l.r), sr = sqrtT(r.r);
+  const T is = rcpT(sl + sr);
+  const T wl = sl * is, wr = sr * is;
+  const T rho = sl * sr;
+  T u[D], u2 = T(0.0), un = T(0.0);
 #pragma unroll
-  for (int k = 0; k < D; ++k) { u[k] = fma(wl, l.u[k], wr * r.u[k]); u2 = fma(u[k], u[k], u2); un = fma(u[k], n[k], un); }
+  for (int k = 0; k < D; ++k) { u[k] = fmaT(wl, l.u[k], wr * r.u[k]); u2 = fmaT(u[k], u[k], u2); un = fmaT(u[k], n[k], un); }
   // total enthalpy H = (E + p)/rho
-  const double hl = (l.E + l.p) * l.ir, hr = (r.E + r.p) * r.ir;
-  const double ht = fma(wl, hl, wr * hr);
+  const T hl = (l.E + l.p) * l.ir, hr = (r.E + r.p) * r.ir;
+  const T ht = fmaT(wl, hl, wr * hr);
   // c^2 = gamma p / rho with p = (gamma-1) rho e and e = (H - u^2/2)/gamma
-  const double c2 = (g - 1.0) * fma(-0.5, u2, ht);
-  const double c = sqrt(c2);
-  const double ic2 = rcp(c2);
-  const double drho = r.r - l.r, dp = r.p - l.p;
-  double du[D], dun = 0.0, udu = 0.0;
+  const T c2 = (g - 1.0) * fmaT(-0.5, u2, ht);
+  const T c = sqrtT(c2);
+  const T ic2 = rcpT(c2);
+  const T drho = r.r - l.r, dp = r.p - l.p;
+  T du[D], dun = T(0.0), udu = T(0.0);
 #pragma unroll
-  for (int k = 0; k < D; ++k) { du[k] = r.u[k] - l.u[k]; dun = fma(du[k], n[k], dun); udu = fma(u[k], du[k], udu); }
-  const double delta = c * 0.05;
-  const double lm = un - c, lp = un + c;
-  const double a1 = fabs(lm) > delta ? fabs(lm) : fma(lm, lm, delta * delta) * (10.0 * rcp(c));
-  const double a4 = fabs(lp) > delta ? fabs(lp) : fma(lp, lp, delta * delta) * (10.0 * rcp(c));
-  const double aun = fabs(un);
-  const double rc = rho * c;
-  const double s1 = a1 * fma(-rc, dun, dp) * (0.5 * ic2);
-  const double s2 = aun * fma(-dp, ic2, drho);
-  const double s3 = aun * rho;
-  const double s4 = a4 * fma(rc, dun, dp) * (0.5 * ic2);
-  const double s14 = s1 + s4, d14 = (s4 - s1) * c;
+  for (int k = 0; k < D; ++k) { du[k] = r.u[k] - l.u[k]; dun = fmaT(du[k], n[k], dun); udu = fmaT(u[k], du[k], udu); }
+  const T delta = c * 0.05;
+  const T lm = un - c, lp = un + c;
+  const T a1 = fabsT(lm) > delta ? fabsT(lm) : fmaT(lm, lm, delta * delta) * (10.0 * rcpT(c));
+  const T a4 = fabsT(lp) > delta ? fabsT(lp) : fmaT(lp, lp, delta * delta) * (10.0 * rcpT(c));
+  const T aun = fabsT(un);
+  const T rc = rho * c;
+  const T s1 = a1 * fmaT(-rc, dun, dp) * (0.5 * ic2);
+  const T s2 = aun * fmaT(-dp, ic2, drho);
+  const T s3 = aun * rho;
+  const T s4 = a4 * fmaT(rc, dun, dp) * (0.5 * ic2);
+  const T s14 = s1 + s4, d14 = (s4 - s1) * c;
   h[0] = 0.5 * (fl[0] + fr[0] - (s14 + s2));
 #pragma unroll
   for (int k = 0; k < D; ++k)
-    h[1 + k] = 0.5 * (fl[1 + k] + fr[1 + k] - fma(u[k], s14 + s2, fma(d14, n[k], s3 * fma(-dun, n[k], du[k]))));
-  h[D + 1] = 0.5 * (fl[D + 1] + fr[D + 1] - fma(ht, s14, fma(d14, un, fma(0.5 * u2, s2, s3 * fma(-un, dun, udu)))));
+    h[1 + k] = 0.5 * (fl[1 + k] + fr[1 + k] - fmaT(u[k], s14 + s2, fmaT(d14, n[k], s3 * fmaT(-dun, n[k], du[k]))));
+  h[D + 1] = 0.5 * (fl[D + 1] + fr[D + 1] - fmaT(ht, s14, fmaT(d14, un, fmaT(0.5 * u2, s2, s3 * fmaT(-un, dun, udu)))));
 }
 
-template <int D, int FLUX>
-__device__ __forceinline__ void convectiveFlux(const State<D>& l, const State<D>& r, const double* n, const Phys& ph,
-                                               double* h) {
+template <int D, int FLUX, class T>
+__device__ __forceinline__ void convectiveFlux(const State<D, T>& l, const State<D, T>& r, const double* n,
+                                               const Phys& ph, T* h) {
   if constexpr (FLUX == 0) fluxCentral<D>(l, r, n, h);
   else if constexpr (FLUX == 1) fluxLaxFriedrichs<D>(l, r, n, ph, h);
   else if constexpr (FLUX == 2) fluxHLLC<D>(l, r, n, ph, h);
@@ -262,24 +272,24 @@ __device__ __forceinline__ void boundaryState(int bc, const double* n, const Com
 
 // Primitive gradient from the conserved gradient g[v*D + k] at a state with velocity u, 1/rho ir and
 // total energy per mass Et = E/rho:  grad rho, grad u_m (gu[k][m] = d_k u_m), grad T.
-template <int D>
+template <int D, class T = double>
 struct PrimGrad {
-  double gu[D][D];
-  double gT[D];
+  T gu[D][D];
+  T gT[D];
 };
 
-template <int D>
-__device__ __forceinline__ void primitiveGradient(const double* g, const double* u, double ir, double Et,
-                                                  const Phys& ph, PrimGrad<D>& pg) {
+template <int D, class T>
+__device__ __forceinline__ void primitiveGradient(const T* g, const T* u, T ir, T Et, const Phys& ph,
+                                                  PrimGrad<D, T>& pg) {
 #pragma unroll
   for (int k = 0; k < D; ++k) {
-    const double dr = g[k];
-    double ge = fma(-dr, Et, g[(D + 1) * D + k]) * ir;
+    const T dr = g[k];
+    T ge = fmaT(-dr, Et, g[(D + 1) * D + k]) * ir;
 #pragma unroll
     for (int m = 0; m < D; ++m) {
-      const double gum = fma(-dr, u[m], g[(1 + m) * D + k]) * ir;
+      const T gum = fmaT(-dr, u[m], g[(1 + m) * D + k]) * ir;
       pg.gu[k][m] = gum;
-      ge = fma(-gum, u[m], ge);
+      ge = fmaT(-gum, u[m], ge);
     }
     pg.gT[k] = ge * ph.inv_cv;
   }
@@ -287,53 +297,54 @@ __device__ __forceinline__ void primitiveGradient(const double* g, const double*
 
 // Dynamic viscosity and thermal conductivity at temperature T (constant or Sutherland,
 // PhysicalModel.cpp:86-123): Sutherland ratio sqrt(T^3) (1 + S) / (T + S), S = 110.4 / 273.15.
-__device__ __forceinline__ void transport(double T, const Phys& ph, double& mu, double& kappa) {
+template <class T>
+__device__ __forceinline__ void transport(T temp, const Phys& ph, T& mu, T& kappa) {
   if (ph.transport == 2) {
     const double S = 110.4 / 273.15;
-    const double r = sqrt(T * T * T) * (1.0 + S) / (T + S);
+    const T r = sqrtT(temp * temp * temp) * (1.0 + S) / (temp + S);
     mu = ph.mu * r;
     kappa = ph.kappa * r;
   } else {
-    mu = ph.mu;
-    kappa = ph.kappa;
+    mu = T(ph.mu);
+    kappa = T(ph.kappa);
   }
 }
 
 // Viscous stress tau and the energy flux q_k = sum_m tau_km u_m + kappa dT/dx_k.
-template <int D>
-__device__ __forceinline__ void viscousTensor(const PrimGrad<D>& pg, const double* u, double T, const Phys& ph,
-                                              double tau[D][D], double* q) {
-  double mu, kappa;
-  transport(T, ph, mu, kappa);
-  double div = 0.0;
+template <int D, class T>
+__device__ __forceinline__ void viscousTensor(const PrimGrad<D, T>& pg, const T* u, T temp, const Phys& ph,
+                                              T tau[D][D], T* q) {
+  T mu, kappa;
+  transport(temp, ph, mu, kappa);
+  T div = T(0.0);
 #pragma unroll
   for (int k = 0; k < D; ++k) div += pg.gu[k][k];
-  const double lam = (2.0 / 3.0) * mu * div;
+  const T lam = (2.0 / 3.0) * mu * div;
 #pragma unroll
   for (int k = 0; k < D; ++k)
 #pragma unroll
-    for (int m = 0; m < D; ++m) tau[k][m] = mu * (pg.gu[k][m] + pg.gu[m][k]) - (k == m ? lam : 0.0);
+    for (int m = 0; m < D; ++m) tau[k][m] = mu * (pg.gu[k][m] + pg.gu[m][k]) - (k == m ? lam : T(0.0));
 #pragma unroll
   for (int k = 0; k < D; ++k) {
-    double s = kappa * pg.gT[k];
+    T s = kappa * pg.gT[k];
 #pragma unroll
-    for (int m = 0; m < D; ++m) s = fma(tau[k][m], u[m], s);
+    for (int m = 0; m < D; ++m) s = fmaT(tau[k][m], u[m], s);
     q[k] = s;
   }
 }
 
 // Viscous normal flux (0, tau.n, q.n) from velocity u, temperature T and primitive gradient pg.
-template <int D>
-__device__ __forceinline__ void viscousNormalFlux(const PrimGrad<D>& pg, const double* u, double T, const double* n,
-                                                  const Phys& ph, double* f) {
-  double tau[D][D], q[D];
-  viscousTensor<D>(pg, u, T, ph, tau, q);
-  f[0] = 0.0;
+template <int D, class T>
+__device__ __forceinline__ void viscousNormalFlux(const PrimGrad<D, T>& pg, const T* u, T temp, const double* n,
+                                                  const Phys& ph, T* f) {
+  T tau[D][D], q[D];
+  viscousTensor<D>(pg, u, temp, ph, tau, q);
+  f[0] = T(0.0);
 #pragma unroll
   for (int m = 0; m < D; ++m) {
-    double s = 0.0;
+    T s = T(0.0);
 #pragma unroll
-    for (int k = 0; k < D; ++k) s = fma(tau[k][m], n[k], s);
+    for (int k = 0; k < D; ++k) s = fmaT(tau[k][m], n[k], s);
     f[1 + m] = s;
   }
   f[D + 1] = dotn<D>(q, n);

@@ -413,8 +413,8 @@ Rec gradRec(sdg_handle* h, DevBlock& B, int which) {
 }
 
 namespace {
-
 bool boundaryOp(int op) { return op == kOpFaceBoundary || op == kOpExchangeBoundary || op == kOpFaceNSBoundary; }
+}  // namespace
 
 Rec faceRec(sdg_handle* h, int op) {
   Rec r;
@@ -432,6 +432,8 @@ Rec faceRec(sdg_handle* h, int op) {
   return r;
 }
 
+namespace {
+
 Rec relRec(sdg_handle* h) {
   Rec r;
   r.kind = kRecRelerr; r.cls = 3;
@@ -446,9 +448,13 @@ Rec relRec(sdg_handle* h) {
   return r;
 }
 
+}  // namespace
+
 const double kRk[3][3][3] = {{{1.0, 0.0, 1.0}, {0, 0, 0}, {0, 0, 0}},
                              {{1.0, 0.0, 1.0}, {0.5, 0.5, 0.5}, {0, 0, 0}},
                              {{1.0, 0.0, 1.0}, {0.75, 0.25, 0.25}, {1.0 / 3.0, 2.0 / 3.0, 2.0 / 3.0}}};  // TimeIntegration.cpp:45-65
+
+namespace {
 
 // Face fluxes of the state in buffer `which` (whose traces the face buffer holds): NS gradient pass first.
 void emitFluxes(sdg_handle* h, int which, int seq, std::vector<Rec>& out) {
@@ -609,6 +615,30 @@ void pointsToState(sdg_handle* h, int which) {
     checkLaunch(h);
   }
 }
+}  // namespace
+
+void pointsToStateBuffer(sdg_handle* h, const double* pts, double* st) {
+  for (DevBlock& B : h->blocks) {
+    const int grid = int((B.ne * B.nb + 255) / 256);
+    pointToStateKernel<<<grid, 256, 0, h->stream>>>(pts + B.pointOffset * h->nv, st + B.stateOffset,
+                                                    B.kind == kDense ? B.lsqDev : nullptr, B.ne, B.nb, B.nq, h->nv,
+                                                    B.ustride);
+    checkLaunch(h);
+  }
+}
+
+void stateToPointsBuffer(sdg_handle* h, const double* st, double* pts) {
+  for (DevBlock& B : h->blocks) {
+    const int grid = int((B.ne * B.nq + 255) / 256);
+    stateToPointKernel<<<grid, 256, 0, h->stream>>>(st + B.stateOffset, pts + B.pointOffset * h->nv,
+                                                    B.kind == kDense ? B.phiDev : nullptr, B.ne, B.nb, B.nq, h->nv,
+                                                    B.ustride);
+    checkLaunch(h);
+  }
+}
+
+namespace {
+
 void stateToPoints(sdg_handle* h, int which) {
   for (DevBlock& B : h->blocks) {
     const int64_t work = B.ne * B.nq;
@@ -955,6 +985,7 @@ int sdg_destroy(sdg_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   dropTimingEvents(h);
   dropGraph(h);
+  destroyAdjoint(h);
   for (DevBlock& B : h->blocks) {
     cudaFree(B.geom); cudaFree(B.tables); cudaFree(B.minedge); cudaFree(B.phiDev); cudaFree(B.lsqDev); cudaFree(B.fmetric);
   }

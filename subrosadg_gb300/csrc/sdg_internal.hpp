@@ -133,6 +133,7 @@ struct sdg_handle {
   double graphDt = 0.0;
   int64_t graphKernels = 0;
   int64_t elements = 0, dof = 0;
+  struct AdjointState* adj = nullptr;  // tangent-linear / adjoint buffers, created on first use
   std::string err;
 };
 
@@ -152,4 +153,13 @@ void traceAll(sdg_handle* h, int which);
 void checkStatus(sdg_handle* h);
 // Error text returned by sdg_last_error(NULL) (failures before a handle exists).
 void setCreateError(const std::string& message);
+// Face-point record of operation `op` (FaceOp) over the handle's interior or boundary faces.
+Rec faceRec(sdg_handle* h, int op);
+// SSP-RK coefficients (c0 on the step's base state, c1 on the stage input, c2 on dt R) per scheme and stage.
+extern const double kRk[3][3][3];
+// Point layout [point][v] <-> state layout of device buffers (tensor: transpose; dense: projection).
+void pointsToStateBuffer(sdg_handle* h, const double* pts, double* st);
+void stateToPointsBuffer(sdg_handle* h, const double* st, double* pts);
+// Tangent-linear / adjoint resources of a handle (sdg_adjoint.cu), released with the handle.
+void destroyAdjoint(sdg_handle* h);
 }  // namespace sdg

@@ -34,6 +34,23 @@ KernelVariant denseGradVariant(int type, int p, bool affine);
 KernelVariant facePointVariant(int op, int dim, int flux);
 KernelVariant relerrVariant();
 
+// Tangent-linear and adjoint kernels of affine tensor blocks (sdg_kernels_adjoint.cuh), interior faces.
+struct AdjointKernels {
+  const void* jvpFace = nullptr;      // (AdjArgs, Phys), one thread per face point
+  const void* vjpFace = nullptr;      // (AdjArgs, Phys), one thread per face point
+  const void* vjpExchange = nullptr;  // (AdjArgs), one thread per face point
+  const void* jvpStage = nullptr;     // (AdjArgs, Phys), one CTA per tile of epb elements
+  const void* vjpVolume = nullptr;    // (AdjArgs, Phys)
+  const void* vjpGradient = nullptr;  // (AdjArgs)
+  const void* vjpTrace = nullptr;     // (AdjArgs)
+  int epb = 0, threads = 0;
+  size_t jvpSmem = 0, vjpSmem = 0;
+  bool valid() const { return jvpStage && jvpFace; }
+};
+// Face kernels depend on (dim, flux, viscous); tile kernels on (dim, nodes per direction, viscous).
+void adjointFaceKernels(int dim, int flux, bool visc, AdjointKernels& k);
+void adjointTileKernels(int dim, int n, bool visc, AdjointKernels& k);
+
 // Largest tile size the kernels are compiled for (their __launch_bounds__).
 constexpr int kMaxThreads = 512;
 

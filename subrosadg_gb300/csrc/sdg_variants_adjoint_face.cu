@@ -1,0 +1,31 @@
+// Tangent-linear and adjoint face kernels (interior faces): the one translation unit that instantiates them.
+#include "sdg_kernels_adjoint.cuh"
+#include "sdg_variants.hpp"
+
+namespace sdg {
+
+namespace {
+template <int DIM, int FLUX, bool VISC>
+void faceOf(AdjointKernels& k) {
+  k.jvpFace = reinterpret_cast<const void*>(&jvpFaceKernel<DIM, FLUX, VISC>);
+  k.vjpFace = reinterpret_cast<const void*>(&vjpFaceKernel<DIM, FLUX, VISC>);
+  k.vjpExchange = reinterpret_cast<const void*>(&vjpExchangeKernel<DIM>);
+}
+template <int DIM, bool VISC>
+void fluxOf(int flux, AdjointKernels& k) {
+  switch (flux) {
+    case 0: faceOf<DIM, 0, VISC>(k); break;
+    case 1: faceOf<DIM, 1, VISC>(k); break;
+    case 2: faceOf<DIM, 2, VISC>(k); break;
+    case 3: faceOf<DIM, 3, VISC>(k); break;
+    default: break;
+  }
+}
+}  // namespace
+
+void adjointFaceKernels(int dim, int flux, bool visc, AdjointKernels& k) {
+  if (dim == 2) { if (visc) fluxOf<2, true>(flux, k); else fluxOf<2, false>(flux, k); }
+  else if (dim == 3) { if (visc) fluxOf<3, true>(flux, k); else fluxOf<3, false>(flux, k); }
+}
+
+}  // namespace sdg

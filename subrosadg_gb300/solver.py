@@ -260,6 +260,59 @@ class GpuSolver:
         self._chk(self.lib.sdg_autotune(self.h, _abi.AUTOTUNE_RETIME if retime else 0))
         return [self.tile(b) for b in range(self.counts.block_count)]
 
+    # derivatives -------------------------------------------------------------------------------
+    def _points(self):
+        return np.zeros((self.counts.volume_point_count, self.nv))
+
+    def volume_weights(self):
+        """w_q |J|_q per volume point (integrals of point values)."""
+        w = np.zeros(self.counts.volume_point_count)
+        self._chk(self.lib.sdg_volume_point_weight(self.h, _ptr(w)))
+        return w
+
+    def set_viscosity(self, mu):
+        self._chk(self.lib.sdg_set_viscosity(self.h, float(mu)))
+        self.config.dynamic_viscosity = float(mu)
+
+    def jvp_residual(self, tangent, viscosity_tangent=0.0):
+        t = np.ascontiguousarray(tangent, np.float64)
+        out = self._points()
+        self._chk(self.lib.sdg_jvp_residual(self.h, _ptr(t), float(viscosity_tangent), _ptr(out)))
+        return out
+
+    def vjp_residual(self, cotangent):
+        c = np.ascontiguousarray(cotangent, np.float64)
+        out = self._points()
+        mu = c_double()
+        self._chk(self.lib.sdg_vjp_residual(self.h, _ptr(c), _ptr(out), byref(mu)))
+        return out, mu.value
+
+    def jvp_steps(self, dt, steps, tangent, viscosity_tangent=0.0):
+        t = np.ascontiguousarray(tangent, np.float64)
+        out = self._points()
+        self._chk(self.lib.sdg_jvp_steps(self.h, steps, dt, _ptr(t), float(viscosity_tangent), _ptr(out)))
+        return out
+
+    def adjoint_steps(self, dt, steps, final_cotangent, checkpoint_interval=25):
+        c = np.ascontiguousarray(final_cotangent, np.float64)
+        out = self._points()
+        mu = c_double()
+        self._chk(self.lib.sdg_adjoint_steps(self.h, steps, dt, checkpoint_interval, _ptr(c), _ptr(out), byref(mu)))
+        return out, mu.value
+
+    def kinetic_energy(self, state=None, weights=None):
+        """J = integral of rho |u|^2 / 2 and dJ/dU in the point layout."""
+        u = self.state_point() if state is None else state
+        w = self.volume_weights() if weights is None else weights
+        d = self.nv - 2
+        rho, m = u[:, 0], u[:, 1:1 + d]
+        vel = m / rho[:, None]
+        J = float(np.sum(w * 0.5 * np.sum(m * vel, 1)))
+        g = np.zeros_like(u)
+        g[:, 0] = -0.5 * w * np.sum(vel * vel, 1)
+        g[:, 1:1 + d] = w[:, None] * vel
+        return J, g
+
 
 class Batch:
     """Many independent GpuSolver instances advanced together (sdg_batch_*): one persistent launch per

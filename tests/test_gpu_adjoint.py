@@ -1,0 +1,219 @@
+"""GPU tests of the tangent-linear model and the discrete adjoint.
+
+Pins, for the residual R(U) = du/dt and for SSP-RK trajectories (with checkpointing):
+  - JVP against central finite differences of the forward residual (step h relative 1e-6: truncation
+    ~h^2, round-off ~1e-16/h, so agreement ~1e-8; tolerance 1e-6 relative L2);
+  - the dot-product identity <lam, JVP(dU)> = <VJP(lam), dU> (+ the viscosity terms) to 1e-11 relative,
+    which holds to round-off because both are exact derivatives of the same discrete operator;
+  - the adjoint gradient of the integrated kinetic energy with respect to U_0 (a seeded random direction)
+    and to mu against central finite differences of the forward trajectory (h = 1e-6, tolerance 1e-6).
+The symmetric analytic flows put face points exactly on the non-differentiable sets of the Riemann
+solvers (bitwise-equal wave speeds in Lax-Friedrichs' max on the vortex's symmetry lines, S* = 0 in HLLC
+on the Taylor-Green's symmetry planes), where the tangent takes the branch of the forward evaluation and
+central differences average the two one-sided slopes; the initial states here carry a seeded smooth
+perturbation that breaks the symmetry.
+"""
+import numpy as np
+import pytest
+
+import subrosadg_gb300 as sdg
+from subrosadg_gb300 import _abi
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "euler-quad-p3-roe": lambda: cases.vortex_case(n=4, p=3, flux=sdg.ROE),
+    "euler-quad-p2-lf": lambda: cases.vortex_case(n=4, p=2, flux=sdg.LAX_FRIEDRICHS),
+    "euler-hex-p2-hllc": lambda: cases.tgv_case(n=3, p=2, flux=sdg.HLLC),
+    "euler-hex-p3-central": lambda: cases.tgv_case(n=3, p=3, flux=sdg.CENTRAL),
+    "ns-hex-p3-br1-roe": lambda: cases.tgv_case(n=3, p=3, flux=sdg.ROE, viscous=sdg.BR1, mu=0.02),
+    "ns-quad-p4-br1-hllc": lambda: cases.vortex_case(n=3, p=4, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.05),
+    "ns-quad-p3-br1-sutherland-lf": lambda: _sutherland(cases.vortex_case(n=4, p=3, flux=sdg.LAX_FRIEDRICHS,
+                                                                          viscous=sdg.BR1, mu=0.05)),
+}
+
+
+def _sutherland(case):
+    case[1].transport_model = sdg.TRANSPORT_SUTHERLAND
+    return case
+
+
+def smooth_perturbation(pts, nv, seed=11, amplitude=0.02):
+    """Seeded sum of low-order sine modes per primitive variable (relative amplitude)."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((len(pts), nv))
+    for v in range(nv):
+        for _ in range(3):
+            k = rng.integers(1, 3, size=3) * 2 * np.pi / 10.0
+            out[:, v] += rng.uniform(-1, 1) * np.sin(pts @ k + rng.uniform(0, 2 * np.pi))
+    return amplitude * out
+
+
+def make(name):
+    mesh, cfg, prim, _, dt, steps = CASES[name]()
+    s = sdg.GpuSolver(mesh, cfg, device=0)
+    pts = s.volume_points()
+    p0 = prim(pts)
+    s.initialize_primitive(p0 * (1.0 + smooth_perturbation(pts, p0.shape[1])))
+    return s, dt
+
+
+def direction(u, seed):
+    """Seeded perturbation scaled per variable by the state's own magnitude."""
+    rng = np.random.default_rng(seed)
+    scale = np.abs(u).mean(0) + 1e-3
+    return rng.standard_normal(u.shape) * scale
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.ravel(a - b)) / max(np.linalg.norm(np.ravel(b)), 1e-300))
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_jvp_residual_matches_central_differences(name):
+    s, _ = make(name)
+    u = s.state_point()
+    d = direction(u, 1)
+    jvp = s.jvp_residual(d)
+    # Lax-Friedrichs' max(|u.n| + c) switches sides at face points where the two are within ~h of each
+    # other; the difference quotient straddles the switch there (an error that shrinks with h), so its
+    # step is smaller
+    lf = s.config.convective_flux == sdg.LAX_FRIEDRICHS
+    h, tol = (1e-8, 1e-5) if lf else (1e-6, 1e-6)
+    s.set_state_point(u + h * d)
+    rp = s.residual_point()
+    s.set_state_point(u - h * d)
+    rm = s.residual_point()
+    s.set_state_point(u)
+    fd = (rp - rm) / (2 * h)
+    assert rel(jvp, fd) < tol, rel(jvp, fd)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_vjp_is_the_transpose_of_jvp(name):
+    s, _ = make(name)
+    u = s.state_point()
+    d = direction(u, 2)
+    lam = np.random.default_rng(3).standard_normal(u.shape)
+    jvp = s.jvp_residual(d)
+    vjp, mubar = s.vjp_residual(lam)
+    lhs, rhs = float(np.sum(lam * jvp)), float(np.sum(vjp * d))
+    assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+    if s.config.equation == sdg.NAVIER_STOKES:
+        dmu = s.jvp_residual(np.zeros_like(u), viscosity_tangent=1.0)
+        lm = float(np.sum(lam * dmu))
+        assert abs(lm - mubar) <= 1e-11 * max(abs(lm), 1e-300), (lm, mubar)
+        # and against differences in mu
+        mu = s.config.dynamic_viscosity
+        hm = 1e-6 * mu
+        s.set_viscosity(mu + hm)
+        rp = s.residual_point()
+        s.set_viscosity(mu - hm)
+        rm = s.residual_point()
+        s.set_viscosity(mu)
+        assert rel(dmu, (rp - rm) / (2 * hm)) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["euler-quad-p3-roe", "euler-hex-p2-hllc", "ns-hex-p3-br1-roe",
+                                  "ns-quad-p4-br1-hllc"])
+def test_trajectory_dot_product_with_checkpointing(name):
+    steps, interval = 5, 2
+    a, dt = make(name)
+    b, _ = make(name)
+    u0 = a.state_point()
+    d0 = direction(u0, 4)
+    dmu = 0.3 if a.config.equation == sdg.NAVIER_STOKES else 0.0
+    dN = a.jvp_steps(dt, steps, d0, viscosity_tangent=dmu)
+    uN_tlm = a.state_point()
+    lamN = np.random.default_rng(5).standard_normal(u0.shape)
+    lam0, mubar = b.adjoint_steps(dt, steps, lamN, checkpoint_interval=interval)
+    uN_adj = b.state_point()
+    # both leave the handle at U_N, equal to a plain forward run
+    c, _ = make(name)
+    c.stepSolver(dt, steps)
+    assert np.array_equal(uN_tlm, c.state_point())
+    assert np.array_equal(uN_adj, c.state_point())
+    lhs = float(np.sum(lamN * dN))
+    rhs = float(np.sum(lam0 * d0)) + mubar * dmu
+    assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), abs(rhs)), (lhs, rhs)
+
+
+def test_checkpoint_interval_does_not_change_the_adjoint():
+    lams = []
+    for interval in (1, 3, 7):
+        s, dt = make("ns-hex-p3-br1-roe")
+        lamN = np.random.default_rng(6).standard_normal(s.state_point().shape)
+        lam0, mubar = s.adjoint_steps(dt, 6, lamN, checkpoint_interval=interval)
+        lams.append((lam0, mubar))
+    for lam0, mubar in lams[1:]:
+        assert np.array_equal(lam0, lams[0][0])
+        assert mubar == lams[0][1]
+
+
+# HLLC and Lax-Friedrichs switch branches (PVRS pressure against each side's pressure, the larger wave
+# speed) at many face points of a low-Mach trajectory, where difference quotients straddle the switches;
+# the trajectory checks use the smooth fluxes (cfg: Roe + BR1 is the adjoint workload)
+@pytest.mark.parametrize("name", ["euler-hex-p3-central", "ns-hex-p3-br1-roe", "euler-quad-p3-roe"])
+def test_kinetic_energy_gradient_matches_finite_differences(name):
+    steps, interval = 6, 3
+    s, dt = make(name)
+    u0 = s.state_point()
+    w = s.volume_weights()
+    d0 = direction(u0, 7)
+
+    def J(u, mu=None):
+        if mu is not None:
+            s.set_viscosity(mu)
+        s.set_state_point(u)
+        s.stepSolver(dt, steps)
+        return s.kinetic_energy(weights=w)[0]
+
+    mu0 = s.config.dynamic_viscosity
+    J0 = J(u0)
+    _, lamN = s.kinetic_energy(weights=w)
+    s.set_state_point(u0)
+    lam0, mubar = s.adjoint_steps(dt, steps, lamN, checkpoint_interval=interval)
+    h = 1e-6
+    fd = (J(u0 + h * d0) - J(u0 - h * d0)) / (2 * h)
+    ad = float(np.sum(lam0 * d0))
+    assert abs(fd - ad) <= 1e-6 * max(abs(fd), abs(ad)), (fd, ad, J0)
+    if s.config.equation == sdg.NAVIER_STOKES:
+        hm = 1e-6 * mu0
+        fdm = (J(u0, mu0 + hm) - J(u0, mu0 - hm)) / (2 * hm)
+        s.set_viscosity(mu0)
+        assert abs(fdm - mubar) <= 1e-6 * max(abs(fdm), abs(mubar)), (fdm, mubar)
+
+
+def test_torch_autograd_binding():
+    import torch
+
+    from subrosadg_gb300 import autograd as sa
+    s, dt = make("ns-hex-p3-br1-roe")
+    u0 = torch.from_numpy(s.state_point()).requires_grad_(True)
+    mu = torch.tensor(s.config.dynamic_viscosity, dtype=torch.float64, requires_grad=True)
+    uN = sa.trajectory(s, u0, mu, steps=4, dt=dt, checkpoint_interval=2)
+    J = sa.kinetic_energy(s, uN)
+    J.backward()
+    # the same gradient through the C ABI directly
+    t, _ = make("ns-hex-p3-br1-roe")
+    t.stepSolver(dt, 4)
+    _, lamN = t.kinetic_energy()
+    t2, _ = make("ns-hex-p3-br1-roe")
+    lam0, mubar = t2.adjoint_steps(dt, 4, lamN, checkpoint_interval=2)
+    assert np.allclose(u0.grad.numpy(), lam0, rtol=1e-12, atol=1e-14 * np.abs(lam0).max())
+    assert abs(float(mu.grad) - mubar) <= 1e-10 * abs(mubar)
+
+
+def test_derivatives_refuse_unsupported_configurations():
+    hybrid = sdg.GpuSolver(*cases.kh_case(n=4, p=3)[:2], device=0)
+    hybrid.initialize_primitive(cases.kh_primitive(*hybrid.volume_points()[:, :2].T))
+    with pytest.raises(sdg.SdgError) as e:
+        hybrid.jvp_residual(np.zeros((hybrid.counts.volume_point_count, 4)))
+    assert e.value.code == _abi.SDG_ERR_UNSUPPORTED
+    mesh, cfg, ic, bc, _, _ = cases.channel_case(p=2, n=3)
+    walls = sdg.GpuSolver(mesh, cfg, device=0)
+    walls.initialize_primitive(ic(walls.volume_points()))
+    with pytest.raises(sdg.SdgError) as e:
+        walls.vjp_residual(np.zeros((walls.counts.volume_point_count, 4)))
+    assert e.value.code == _abi.SDG_ERR_UNSUPPORTED
