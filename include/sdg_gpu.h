@@ -347,6 +347,13 @@ int sdg_jvp_steps(sdg_handle* handle, int32_t step_count, double delta_time, con
  * and each interval's stage states are recomputed from its checkpoint on the way back. */
 int sdg_adjoint_steps(sdg_handle* handle, int32_t step_count, double delta_time, int32_t checkpoint_interval,
                       const double* final_cotangent, double* initial_cotangent, double* viscosity_cotangent);
+/* The same trajectory in two calls, for callers that need U_N before choosing the cotangent (a loss
+ * evaluated on U_N, an autograd engine): sdg_forward_steps advances step_count steps keeping the
+ * checkpoints, sdg_adjoint_recorded then runs only the reverse sweep of that trajectory (the state must
+ * not have changed in between: SDG_ERR_STATE). */
+int sdg_forward_steps(sdg_handle* handle, int32_t step_count, double delta_time, int32_t checkpoint_interval);
+int sdg_adjoint_recorded(sdg_handle* handle, const double* final_cotangent, double* initial_cotangent,
+                         double* viscosity_cotangent);
 /* Device bytes held for checkpoints and stage states (grown on demand, released with the handle). */
 int sdg_adjoint_memory(sdg_handle* handle, int64_t* bytes);
 

@@ -170,6 +170,8 @@ SIGNATURES = {
     "sdg_jvp_steps": (c_int32, [c_void_p, c_int32, c_double, _p_double, c_double, _p_double]),
     "sdg_adjoint_steps": (c_int32, [c_void_p, c_int32, c_double, c_int32, _p_double, _p_double, _p_double]),
     "sdg_adjoint_memory": (c_int32, [c_void_p, POINTER(c_int64)]),
+    "sdg_forward_steps": (c_int32, [c_void_p, c_int32, c_double, c_int32]),
+    "sdg_adjoint_recorded": (c_int32, [c_void_p, _p_double, _p_double, _p_double]),
 }
 
 _lib = None

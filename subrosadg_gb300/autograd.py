@@ -3,8 +3,9 @@
     u_final = trajectory(solver, u0, mu, steps, dt, checkpoint_interval)
 
 u0 is the state at the volume points ([points][d+2] conserved, float64), mu a 0-d float64 tensor (the
-dynamic viscosity; Navier-Stokes handles only).  The forward runs sdg_step on the GPU; backward runs
-sdg_adjoint_steps (checkpointed reverse sweep) and returns dL/du0 and dL/dmu for any loss L computed in
+dynamic viscosity; Navier-Stokes handles only).  The forward runs sdg_forward_steps on the GPU (the
+steps with their checkpoints kept); backward runs sdg_adjoint_recorded (the checkpointed reverse sweep of
+that trajectory; if the solver's state changed in between, it replays the forward first) and returns dL/du0 and dL/dmu for any loss L computed in
 torch from u_final, e.g. the kinetic energy sum(w * rho |u|^2 / 2) with w = solver.volume_weights().
 """
 from __future__ import annotations
@@ -23,7 +24,7 @@ class _Trajectory(torch.autograd.Function):
             solver.set_viscosity(float(mu))
         u0_host = u0.detach().to("cpu", torch.float64).contiguous().numpy()
         solver.set_state_point(u0_host)
-        solver.stepSolver(dt, steps)
+        solver.forward_steps(dt, steps, interval)  # keeps the checkpoints for the backward pass
         uN = solver.state_point()
         ctx.solver, ctx.steps, ctx.dt, ctx.interval, ctx.ns = solver, steps, dt, interval, ns
         ctx.u0 = u0_host.copy()
@@ -34,11 +35,16 @@ class _Trajectory(torch.autograd.Function):
     @staticmethod
     def backward(ctx, grad_uN):
         s = ctx.solver
-        if ctx.ns:
-            s.set_viscosity(ctx.mu)
-        s.set_state_point(ctx.u0)
         g = grad_uN.detach().to("cpu", torch.float64).contiguous().numpy()
-        lam0, mubar = s.adjoint_steps(ctx.dt, ctx.steps, g, ctx.interval)
+        try:
+            lam0, mubar = s.adjoint_recorded(g)     # the forward's trajectory is still the solver's state
+        except _abi.SdgError as e:
+            if e.code != _abi.SDG_ERR_STATE:
+                raise
+            if ctx.ns:                              # the solver was used in between: replay the forward
+                s.set_viscosity(ctx.mu)
+            s.set_state_point(ctx.u0)
+            lam0, mubar = s.adjoint_steps(ctx.dt, ctx.steps, g, ctx.interval)
         dmu = torch.tensor(mubar if ctx.ns else 0.0, dtype=torch.float64)
         return torch.from_numpy(np.ascontiguousarray(lam0)).to(ctx.device), dmu, None, None, None, None
 

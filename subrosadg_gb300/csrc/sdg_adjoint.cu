@@ -24,6 +24,32 @@
 
 using namespace sdg;
 
+namespace sdg {
+// out += scale * sum(part[0..n)): one CTA, deterministic order (the dJ/dmu accumulator stays on the device).
+__global__ void __launch_bounds__(256) muAccumulateKernel(const double* __restrict__ part, int64_t n, double scale,
+                                                          double* __restrict__ out) {
+  __shared__ double sh[256];
+  double acc = 0.0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) acc += part[i];
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out += scale * sh[0];
+}
+
+}  // namespace sdg
+
+// A forward trajectory kept for a later reverse sweep (sdg_forward_steps / sdg_adjoint_recorded).
+struct Trajectory {
+  bool valid = false;
+  uint64_t version = 0;   // the handle's state version at U_N
+  int steps = 0, interval = 0, segments = 0;
+  double dt = 0.0;
+};
+
 struct AdjointState {
   AdjointKernels k;
   double* dU[2] = {nullptr, nullptr};
@@ -45,7 +71,8 @@ struct AdjointState {
   int64_t muTiles = 0, muFaces = 0;
   double* pts = nullptr;           // point-layout conversion buffer
   std::vector<double*> pool;       // checkpoints and stage states (grown on demand)
-  int64_t launches = 0;
+  double* muAcc = nullptr;         // device accumulator of dJ/dmu
+  Trajectory traj;
 };
 
 namespace sdg {
@@ -54,7 +81,7 @@ void destroyAdjoint(sdg_handle* h) {
   if (!A) return;
   for (double* p : {A->dU[0], A->dU[1], A->dface, A->dfaceOther, A->dgrad, A->dfaceGrad, A->dflux, A->lamIn,
                     A->lamStage, A->lamBase, A->lamU, A->lamG, A->lamH, A->lamTr, A->lamTg, A->lamUp, A->muPart,
-                    A->pts})
+                    A->pts, A->muAcc})
     cudaFree(p);
   for (double* p : A->pool) cudaFree(p);
   delete A;
@@ -98,6 +125,8 @@ AdjointState* adjoint(sdg_handle* h) {
   A->muFaces = (h->nInterior * h->nfq + kFaceThreads - 1) / kFaceThreads;
   A->muPart = alloc(size_t(A->muTiles + A->muFaces));
   A->pts = alloc(size_t(h->volumePoints) * h->nv);
+  A->muAcc = alloc(1);
+  SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
   for (double* p : {A->dU[0], A->dU[1], A->dface, A->dflux, A->lamIn, A->lamStage, A->lamBase, A->lamU, A->lamH, A->lamTr})
     SDG_CUDA(cudaMemsetAsync(p, 0, (p == A->dface || p == A->dflux || p == A->lamH || p == A->lamTr ? F : S) * 8, h->stream));
   if (h->ns) {
@@ -212,10 +241,10 @@ void jvpResidual(sdg_handle* h, const double* du, double dmu, double* drate) {
 }
 
 // Adjoint of the residual at state[1] (forward quantities already computed by forwardAt) for cotangent lam.
-// Without RK coefficients (lamStage = lamBase = null) the result R'^T lam goes to A->lamU.  Returns
-// sum(muPart) = mu <lam, dR/dmu> (NS) after a synchronisation, else 0.
-double vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* lamStage, double* lamBase,
-                   bool accumulateAll, double c0, double c1, double c2dt) {
+// Without RK coefficients (lamStage = lamBase = null) the result R'^T lam goes to A->lamU.  For
+// Navier-Stokes, A->muAcc += muScale * mu <lam, dR/dmu> on the device.
+void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* lamStage, double* lamBase,
+                 bool accumulateAll, double c0, double c1, double c2dt, double muScale) {
   AdjointState* A = h->adj;
   const int NT = A->k.threads;
   int64_t tileOff = 0;
@@ -252,13 +281,17 @@ double vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double
     a.c0 = c0; a.c1 = c1; a.c2dt = c2dt;
     launch(h, A->k.vjpTrace, tiles(h, B), NT, A->k.vjpSmem, a, false);
   }
-  if (!h->ns) return 0.0;
-  std::vector<double> part(size_t(A->muTiles + A->muFaces));
-  SDG_CUDA(cudaMemcpyAsync(part.data(), A->muPart, part.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+  if (!h->ns) return;
+  muAccumulateKernel<<<1, 256, 0, h->stream>>>(A->muPart, A->muTiles + A->muFaces, muScale, A->muAcc);
+  SDG_CUDA(cudaGetLastError());
+  h->launches++;
+}
+
+double readMu(sdg_handle* h) {
+  double m = 0.0;
+  SDG_CUDA(cudaMemcpyAsync(&m, h->adj->muAcc, 8, cudaMemcpyDeviceToHost, h->stream));
   SDG_CUDA(cudaStreamSynchronize(h->stream));
-  double s = 0.0;
-  for (double x : part) s += x;
-  return s;
+  return m;
 }
 
 void uploadPoints(sdg_handle* h, const double* host, double* st) {
@@ -319,29 +352,41 @@ void jvpSteps(sdg_handle* h, int steps, double dt, double dmu) {
   }
 }
 
-// Discrete adjoint of `steps` steps from the current state (U_0): on entry A->lamIn holds dJ/dU_N; on exit
-// A->lamIn holds dJ/dU_0 and the state is U_N.  Returns dJ/dmu (NS; 0 for Euler).
-double adjointSteps(sdg_handle* h, int steps, double dt, int interval) {
+// Forward sweep of `steps` steps from the current state U_0, keeping U every `interval` steps
+// (pool[0..segments)) and U_N (pool[segments]); records the trajectory for the reverse sweep.
+void forwardSweep(sdg_handle* h, int steps, double dt, int interval) {
   AdjointState* A = h->adj;
-  const int ti = h->cfg.time_integration, S = ti + 1;
   const int segments = (steps + interval - 1) / interval;
-  // forward sweep with checkpoints (pool[0..segments-1]); pool[segments] keeps U_N
+  std::vector<Rec> recs;
+  emitStep(h, dt, true, recs);
   for (int g = 0; g < segments; ++g) {
     copyState(h, poolBuffer(h, g), h->state[0]);
     const int n = std::min(interval, steps - g * interval);
-    std::vector<Rec> recs;
-    emitStep(h, dt, true, recs);
     for (int k = 0; k < n; ++k) runRecs(h, recs, h->stream);
   }
-  double* finalState = poolBuffer(h, segments);
-  copyState(h, finalState, h->state[0]);
+  copyState(h, poolBuffer(h, segments), h->state[0]);
+  h->stateVersion++;
+  A->traj.valid = true;
+  A->traj.version = h->stateVersion;
+  A->traj.steps = steps; A->traj.interval = interval; A->traj.segments = segments; A->traj.dt = dt;
+}
+
+// Reverse sweep of the recorded trajectory: on entry A->lamIn holds dJ/dU_N; on exit it holds dJ/dU_0 and
+// the state is U_N again.  Returns dJ/dmu (Navier-Stokes; 0 for Euler).
+double backwardSweep(sdg_handle* h) {
+  AdjointState* A = h->adj;
+  const Trajectory T = A->traj;
+  const int ti = h->cfg.time_integration, S = ti + 1;
+  const int steps = T.steps, interval = T.interval, segments = T.segments;
+  const double dt = T.dt;
   const size_t storeBase = size_t(segments) + 1;
   const auto stages = stepByStage(h, dt, S);
   SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
-  double mubar = 0.0;
+  SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
+  const double muScale = h->ns && h->ph.mu > 0.0 ? 1.0 / h->ph.mu : 0.0;
   for (int g = segments - 1; g >= 0; --g) {
     const int n0 = g * interval, n1 = std::min(steps, n0 + interval);
-    // recompute the segment, keeping every stage input
+    // recompute the segment from its checkpoint, keeping every stage input
     copyState(h, h->state[0], poolBuffer(h, g));
     traces(h, h->state[0], h->face);
     for (int n = n0; n < n1; ++n)
@@ -355,21 +400,19 @@ double adjointSteps(sdg_handle* h, int steps, double dt, int interval) {
         copyState(h, h->state[1], poolBuffer(h, storeBase + size_t(n - n0) * S + s));
         forwardAt(h, h->state[1]);
         const double c0 = kRk[ti][s][0], c1 = kRk[ti][s][1], c2dt = kRk[ti][s][2] * dt;
-        double m;
         if (s > 0) {
-          m = vjpResidual(h, A->lamIn, A->lamIn, A->lamStage, A->lamBase, false, c0, c1, c2dt);
+          vjpResidual(h, A->lamIn, A->lamIn, A->lamStage, A->lamBase, false, c0, c1, c2dt, c2dt * muScale);
           std::swap(A->lamIn, A->lamStage);
         } else {
-          m = vjpResidual(h, A->lamIn, A->lamIn, nullptr, A->lamBase, true, c0, c1, c2dt);
+          vjpResidual(h, A->lamIn, A->lamIn, nullptr, A->lamBase, true, c0, c1, c2dt, c2dt * muScale);
           std::swap(A->lamIn, A->lamBase);
           SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
         }
-        if (h->ns && h->ph.mu > 0.0) mubar += c2dt * m / h->ph.mu;
       }
   }
-  copyState(h, h->state[0], finalState);
+  copyState(h, h->state[0], poolBuffer(h, segments));
   traces(h, h->state[0], h->face);
-  return mubar;
+  return h->ns ? readMu(h) : 0.0;
 }
 
 int adjFail(sdg_handle* h, const Failure& f) {
@@ -402,6 +445,7 @@ int sdg_set_viscosity(sdg_handle* h, double mu) {
   h->ph.mu = mu;
   h->ph.kappa = h->cfg.prandtl_number > 0 ? h->cfg.specific_heat_constant_pressure * mu / h->cfg.prandtl_number : 0.0;
   dropGraph(h);
+  h->stateVersion++;
   return SDG_OK;
 }
 
@@ -430,9 +474,11 @@ int sdg_vjp_residual(sdg_handle* h, const double* rate_cotangent, double* cotang
     copyState(h, h->state[1], h->state[0]);
     uploadPoints(h, rate_cotangent, A->lamIn);
     forwardAt(h, h->state[1]);
-    const double m = vjpResidual(h, A->lamIn, nullptr, nullptr, nullptr, false, 0.0, 0.0, 0.0);
+    SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
+    vjpResidual(h, A->lamIn, nullptr, nullptr, nullptr, false, 0.0, 0.0, 0.0,
+                h->ns && h->ph.mu > 0.0 ? 1.0 / h->ph.mu : 0.0);
     downloadPoints(h, A->lamU, cotangent);
-    if (viscosity_cotangent) *viscosity_cotangent = h->ns && h->ph.mu > 0.0 ? m / h->ph.mu : 0.0;
+    if (viscosity_cotangent) *viscosity_cotangent = h->ns ? readMu(h) : 0.0;
     traces(h, h->state[0], h->face);
     checkStatus(h);
   } catch (const Failure& f) {
@@ -450,6 +496,7 @@ int sdg_jvp_steps(sdg_handle* h, int32_t steps, double dt, const double* tangent
     SDG_CUDA(cudaSetDevice(h->device));
     uploadPoints(h, tangent_in, A->dU[0]);
     jvpSteps(h, steps, dt, viscosity_tangent);
+    h->stateVersion++;
     downloadPoints(h, A->dU[0], tangent_out);
     checkStatus(h);
   } catch (const Failure& f) {
@@ -465,8 +512,42 @@ int sdg_adjoint_steps(sdg_handle* h, int32_t steps, double dt, int32_t interval,
   try {
     AdjointState* A = adjoint(h);
     SDG_CUDA(cudaSetDevice(h->device));
+    forwardSweep(h, steps, dt, interval);
     uploadPoints(h, final_cotangent, A->lamIn);
-    const double m = adjointSteps(h, steps, dt, interval);
+    const double m = backwardSweep(h);
+    downloadPoints(h, A->lamIn, initial_cotangent);
+    if (viscosity_cotangent) *viscosity_cotangent = m;
+    checkStatus(h);
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_forward_steps(sdg_handle* h, int32_t steps, double dt, int32_t interval) {
+  if (!h || steps < 1 || interval < 1 || !std::isfinite(dt)) return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    adjoint(h);
+    SDG_CUDA(cudaSetDevice(h->device));
+    forwardSweep(h, steps, dt, interval);
+    SDG_CUDA(cudaMemcpyAsync(h->relerr, h->relOut, h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+    checkStatus(h);
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_adjoint_recorded(sdg_handle* h, const double* final_cotangent, double* initial_cotangent,
+                         double* viscosity_cotangent) {
+  if (!h || !final_cotangent || !initial_cotangent) return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    AdjointState* A = adjoint(h);
+    if (!A->traj.valid || A->traj.version != h->stateVersion)
+      throw Failure(SDG_ERR_STATE, "no recorded trajectory ends at the current state (sdg_forward_steps first)");
+    SDG_CUDA(cudaSetDevice(h->device));
+    uploadPoints(h, final_cotangent, A->lamIn);
+    const double m = backwardSweep(h);
     downloadPoints(h, A->lamIn, initial_cotangent);
     if (viscosity_cotangent) *viscosity_cotangent = m;
     checkStatus(h);

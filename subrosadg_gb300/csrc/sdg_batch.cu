@@ -270,6 +270,7 @@ void ready(sdg_batch* b) {
 
 void stepBatch(sdg_batch* b, int steps) {
   ready(b);
+  for (sdg_handle* h : b->inst) h->stateVersion++;
   for (int s = 0; s < steps; ++s) SDG_CUDA(cudaGraphLaunch(b->exec, b->stream));
 }
 
@@ -551,6 +552,7 @@ int sdg_batch_step_sequential_async(sdg_batch* b, int32_t steps) {
     if (!b->haveDt) throw Failure(SDG_ERR_STATE, "sdg_batch_set_delta_time before the first step");
     SDG_CUDA(cudaSetDevice(b->device));
     if (!b->built) build(b);
+    for (sdg_handle* h : b->inst) h->stateVersion++;
     for (int s = 0; s < steps; ++s)
       for (size_t i = 0; i < b->inst.size(); ++i) runRecs(b->inst[i], b->seqRecs[i], b->stream);
   } catch (const Failure& f) {

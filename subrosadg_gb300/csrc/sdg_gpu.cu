@@ -354,11 +354,12 @@ void setGradTile(DevBlock& B, int epb, int threads) {
 namespace {
 
 // Kernel variants of a block (element kind, order, affine) and its default tiles.
-void resolveBlock(DevBlock& B, bool ns) {
+void resolveBlock(DevBlock& B, bool ns, bool br2) {
   for (int visc = 0; visc < 2; ++visc)
     B.stageV[visc] = B.kind == kTensor ? tensorStageVariant(B.dim, B.n, B.affine != 0, visc != 0)
                                        : denseStageVariant(B.type, B.p, B.affine != 0, visc != 0);
-  B.gradV = B.kind == kTensor ? tensorGradVariant(B.dim, B.n, B.affine != 0) : denseGradVariant(B.type, B.p, B.affine != 0);
+  B.gradV = B.kind == kTensor ? tensorGradVariant(B.dim, B.n, B.affine != 0, br2)
+                              : denseGradVariant(B.type, B.p, B.affine != 0);
   if (!B.stageV[0].valid() || !B.stageV[1].valid() || !B.gradV.valid())
     throw Failure(SDG_ERR_UNSUPPORTED, "unsupported element block (type, order, affine)");
   const KernelVariant& v = B.stageV[ns ? 1 : 0];
@@ -805,7 +806,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       } else {
         buildDenseTables(B.type, B.p, B.tablesHost, B.phi, B.lsq);
       }
-      resolveBlock(B, c.equation == SDG_COMPRESSIBLE_NS);
+      resolveBlock(B, c.equation == SDG_COMPRESSIBLE_NS, c.viscous_flux == SDG_VISCOUS_BR2);
       B.stateOffset = stateOff; stateOff += size_t(B.ne) * B.ustride;
       B.gradOffset = h->gradCount; h->gradCount += size_t(B.ne) * h->nv * B.dim * B.nb;
       if (!B.affine || B.kind == kDense) {  // outward n|J_f| of each local face (straight faces: constant)
@@ -1036,6 +1037,7 @@ int sdg_set_state_point(sdg_handle* h, const double* conserved) {
   traceAll(h, 0);
   SDG_CUDA(cudaStreamSynchronize(h->stream));
   h->hasState = true;
+  h->stateVersion++;
   return SDG_OK;
   SDG_API_END(h)
 }
@@ -1053,6 +1055,7 @@ int sdg_set_initial_primitive(sdg_handle* h, const double* primitive) {
   traceAll(h, 0);
   SDG_CUDA(cudaStreamSynchronize(h->stream));
   h->hasState = true;
+  h->stateVersion++;
   return SDG_OK;
   SDG_API_END(h)
 }
@@ -1155,6 +1158,7 @@ int sdg_set_state_modal(sdg_handle* h, const double* coefficient) {
   traceAll(h, 0);
   SDG_CUDA(cudaStreamSynchronize(h->stream));
   h->hasState = true;
+  h->stateVersion++;
   return SDG_OK;
   SDG_API_END(h)
 }
@@ -1191,6 +1195,7 @@ int sdg_step_async(sdg_handle* h, int32_t steps, double dt) {
   SDG_API_BEGIN
   SDG_CUDA(cudaSetDevice(h->device));
   for (int s = 0; s < steps; ++s) stepOnce(h, dt);  // relative error every step, as stepSolver does
+  h->stateVersion++;
   return SDG_OK;
   SDG_API_END(h)
 }

@@ -134,6 +134,7 @@ struct sdg_handle {
   int64_t graphKernels = 0;
   int64_t elements = 0, dof = 0;
   struct AdjointState* adj = nullptr;  // tangent-linear / adjoint buffers, created on first use
+  uint64_t stateVersion = 0;          // bumped by every call that changes the state or the physics
   std::string err;
 };
 

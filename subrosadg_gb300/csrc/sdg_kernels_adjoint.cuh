@@ -152,6 +152,351 @@ __device__ __forceinline__ void viscousTransposeG(const double* U, const Phys& p
   }
 }
 
+
+// ---- hand-written reverse sweeps (adjoints of the forward formulas, line by line) ---------------------
+// Euler contravariant volume fluxes Q_b = (rho vb, m vb + ja_b p, (E + p) vb), vb = u . ja_b:
+// lamU = sum_b (dQ_b/dU)^T lq[b].
+template <int D>
+__device__ __forceinline__ void eulerVolumeReverse(const double* U, const double ja[D][D], const double lq[D][D + 2],
+                                                   const Phys& ph, double* lamU) {
+  constexpr int NV = D + 2;
+  const double rho = U[0], E = U[D + 1];
+  const double ir = rcp(rho);
+  double u[D], mu2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) { u[k] = U[1 + k] * ir; mu2 = fma(U[1 + k], u[k], mu2); }
+  const double p = ph.gm1 * fma(-0.5, mu2, E), ep = E + p;
+  double lrho = 0.0, lE = 0.0, lp = 0.0, lm[D], lu[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) { lm[k] = 0.0; lu[k] = 0.0; }
+#pragma unroll
+  for (int b = 0; b < D; ++b) {
+    double vb = 0.0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) vb = fma(u[k], ja[b][k], vb);
+    double lvb = fma(lq[b][0], rho, lq[b][NV - 1] * ep);
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      lvb = fma(lq[b][1 + k], U[1 + k], lvb);
+      lp = fma(lq[b][1 + k], ja[b][k], lp);
+      lm[k] = fma(lq[b][1 + k], vb, lm[k]);
+    }
+    lp = fma(lq[b][NV - 1], vb, lp);
+    lrho = fma(lq[b][0], vb, lrho);
+    lE = fma(lq[b][NV - 1], vb, lE);
+#pragma unroll
+    for (int k = 0; k < D; ++k) lu[k] = fma(lvb, ja[b][k], lu[k]);
+  }
+  lE = fma(ph.gm1, lp, lE);
+  const double hp = -0.5 * ph.gm1 * lp;
+  double lir = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    lm[k] = fma(hp, u[k], lm[k]);
+    lu[k] = fma(hp, U[1 + k], lu[k]);
+    lm[k] = fma(lu[k], ir, lm[k]);
+    lir = fma(lu[k], U[1 + k], lir);
+  }
+  lrho = fma(-ir * ir, lir, lrho);
+  lamU[0] = lrho;
+#pragma unroll
+  for (int k = 0; k < D; ++k) lamU[1 + k] = lm[k];
+  lamU[NV - 1] = lE;
+}
+
+// Viscous fluxes Fv_c (direction c) = (0, tau[c][.], q[c]) at state U with conserved gradient g:
+// lamU += (dFv/dU)^T lamF, lamg += (dFv/dg)^T lamF, and the return value is sum_c lamF[c] . Fv_c
+// (the mu-derivative term: Fv is proportional to the reference viscosity).
+template <int D>
+__device__ __forceinline__ double viscousReverse(const double* U, const double* g, const double lamF[D][D + 2],
+                                                 const Phys& ph, double* lamU, double* lamg) {
+  constexpr int NV = D + 2;
+  const double rho = U[0], E = U[D + 1];
+  const double ir = rcp(rho);
+  double u[D], u2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) { u[k] = U[1 + k] * ir; u2 = fma(u[k], u[k], u2); }
+  const double Et = E * ir;
+  const double temp = fma(-0.5, u2, Et) * ph.inv_cv;
+  double mu, kappa;
+  transport(temp, ph, mu, kappa);
+  double dr[D], B[D], A[D][D], gum[D][D], gT[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    dr[k] = g[k];
+    B[k] = fma(-dr[k], Et, g[(D + 1) * D + k]);
+    double ge = B[k] * ir;
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      A[k][m] = fma(-dr[k], u[m], g[(1 + m) * D + k]);
+      gum[k][m] = A[k][m] * ir;
+      ge = fma(-gum[k][m], u[m], ge);
+    }
+    gT[k] = ge * ph.inv_cv;
+  }
+  double div = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) div += gum[k][k];
+  double tau[D][D], q[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+#pragma unroll
+    for (int m = 0; m < D; ++m) tau[k][m] = mu * (gum[k][m] + gum[m][k]) - (k == m ? (2.0 / 3.0) * mu * div : 0.0);
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    double s = kappa * gT[k];
+#pragma unroll
+    for (int m = 0; m < D; ++m) s = fma(tau[k][m], u[m], s);
+    q[k] = s;
+  }
+  // value term
+  double fdot = 0.0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+#pragma unroll
+    for (int m = 0; m < D; ++m) fdot = fma(lamF[c][1 + m], tau[c][m], fdot);
+    fdot = fma(lamF[c][NV - 1], q[c], fdot);
+  }
+  // reverse: q[c] = kappa gT[c] + sum_m tau[c][m] u[m]
+  double lt[D][D], lu[D], lgT[D], lkappa = 0.0;
+#pragma unroll
+  for (int m = 0; m < D; ++m) lu[m] = 0.0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const double le = lamF[c][NV - 1];
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      lt[c][m] = fma(le, u[m], lamF[c][1 + m]);
+      lu[m] = fma(le, tau[c][m], lu[m]);
+    }
+    lgT[c] = kappa * le;
+    lkappa = fma(le, gT[c], lkappa);
+  }
+  // tau = mu (gum + gum^T) - 2/3 mu div I
+  double tr = 0.0, lmu = 0.0;
+#pragma unroll
+  for (int j = 0; j < D; ++j) tr += lt[j][j];
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+#pragma unroll
+    for (int m = 0; m < D; ++m)
+      lmu = fma(lt[k][m], gum[k][m] + gum[m][k] - (k == m ? (2.0 / 3.0) * div : 0.0), lmu);
+  double lir = 0.0, lEt = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const double lge = ph.inv_cv * lgT[k];
+    lamg[(D + 1) * D + k] = fma(ir, lge, lamg[(D + 1) * D + k]);
+    lir = fma(B[k], lge, lir);
+    lEt = fma(-dr[k] * ir, lge, lEt);
+    double ldr = -Et * ir * lge;
+#pragma unroll
+    for (int m = 0; m < D; ++m) {
+      double lg = mu * (lt[k][m] + lt[m][k]);
+      if (k == m) lg -= (2.0 / 3.0) * mu * tr;
+      lg = fma(-u[m], lge, lg);              // ge contains -gum[k][m] u[m]
+      lu[m] = fma(-gum[k][m], lge, lu[m]);
+      lamg[(1 + m) * D + k] = fma(ir, lg, lamg[(1 + m) * D + k]);
+      ldr = fma(-u[m] * ir, lg, ldr);
+      lir = fma(lg, A[k][m], lir);
+      lu[m] = fma(-dr[k] * ir, lg, lu[m]);
+    }
+    lamg[k] += ldr;
+  }
+  // transport law: Sutherland mu = mu0 r(T), kappa = kappa0 r(T), r'(T) = r (3/(2T) - 1/(T+S))
+  if (ph.transport == 2) {
+    const double S = 110.4 / 273.15;
+    const double r = sqrt(temp * temp * temp) * (1.0 + S) / (temp + S);
+    const double dr_dT = r * (1.5 / temp - 1.0 / (temp + S));
+    const double lT = (lmu * ph.mu + lkappa * ph.kappa) * dr_dT;
+    lEt = fma(ph.inv_cv, lT, lEt);
+#pragma unroll
+    for (int m = 0; m < D; ++m) lu[m] = fma(-ph.inv_cv * lT, u[m], lu[m]);
+  }
+  // Et = E ir, u = m ir, ir = 1/rho
+  lamU[NV - 1] = fma(ir, lEt, lamU[NV - 1]);
+  lir = fma(E, lEt, lir);
+#pragma unroll
+  for (int m = 0; m < D; ++m) {
+    lamU[1 + m] = fma(ir, lu[m], lamU[1 + m]);
+    lir = fma(U[1 + m], lu[m], lir);
+  }
+  lamU[0] = fma(-ir * ir, lir, lamU[0]);
+  return fdot;
+}
+
+// Roe flux with Harten's entropy fix (fluxRoe): lamL += (dh/dUL)^T lh, lamR += (dh/dUR)^T lh.
+template <int D>
+__device__ __forceinline__ void roeReverse(const double* UL, const double* UR, const double* n, const Phys& ph,
+                                           const double* lh, double* lamL, double* lamR) {
+  constexpr int NV = D + 2;
+  State<D> l, r;
+  makeState<D>(l, UL, ph);
+  makeState<D>(r, UR, ph);
+  const double g = ph.gamma;
+  const double unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
+  const double sl = sqrt(l.r), sr = sqrt(r.r);
+  const double is = rcp(sl + sr);
+  const double wl = sl * is, wr = sr * is;
+  const double rho = sl * sr;
+  double u[D], u2 = 0.0, un = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) { u[k] = fma(wl, l.u[k], wr * r.u[k]); u2 = fma(u[k], u[k], u2); un = fma(u[k], n[k], un); }
+  const double hl = (l.E + l.p) * l.ir, hr = (r.E + r.p) * r.ir;
+  const double ht = fma(wl, hl, wr * hr);
+  const double c2 = (g - 1.0) * fma(-0.5, u2, ht);
+  const double c = sqrt(c2);
+  const double ic2 = rcp(c2);
+  const double ic = rcp(c);
+  const double drho = r.r - l.r, dp = r.p - l.p;
+  double du[D], dun = 0.0, udu = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) { du[k] = r.u[k] - l.u[k]; dun = fma(du[k], n[k], dun); udu = fma(u[k], du[k], udu); }
+  const double delta = c * 0.05;
+  const double lmv = un - c, lpv = un + c;
+  const bool e1 = fabs(lmv) > delta, e4 = fabs(lpv) > delta;
+  const double a1 = e1 ? fabs(lmv) : fma(lmv, lmv, delta * delta) * (10.0 * ic);
+  const double a4 = e4 ? fabs(lpv) : fma(lpv, lpv, delta * delta) * (10.0 * ic);
+  const double aun = fabs(un);
+  const double rc = rho * c;
+  const double X1 = fma(-rc, dun, dp), X4 = fma(rc, dun, dp), h2 = 0.5 * ic2;
+  const double s1 = a1 * X1 * h2, s4 = a4 * X4 * h2;
+  const double s2 = aun * fma(-dp, ic2, drho);
+  const double s3 = aun * rho;
+  const double s14 = s1 + s4, d14 = (s4 - s1) * c;
+  // h = 1/2 (fl + fr) - 1/2 Diss: cotangents of the dissipation terms
+  double mk[D];
+  const double m0 = -0.5 * lh[0], mE = -0.5 * lh[NV - 1];
+#pragma unroll
+  for (int k = 0; k < D; ++k) mk[k] = -0.5 * lh[1 + k];
+  double mu_u = 0.0, mu_n = 0.0, mu_dd = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    mu_u = fma(mk[k], u[k], mu_u);
+    mu_n = fma(mk[k], n[k], mu_n);
+    mu_dd = fma(mk[k], fma(-dun, n[k], du[k]), mu_dd);
+  }
+  const double ls14 = m0 + mu_u + mE * ht;
+  const double ls2 = m0 + mu_u + mE * 0.5 * u2;
+  const double ld14 = fma(mE, un, mu_n);
+  const double ls3 = fma(mE, fma(-un, dun, udu), mu_dd);
+  double lu[D], ldu[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    lu[k] = fma(mk[k], s14 + s2, mE * s3 * du[k]);
+    ldu[k] = fma(mk[k], s3, mE * s3 * u[k]);
+  }
+  double lu2 = mE * 0.5 * s2;
+  double lht = mE * s14;
+  double lun = mE * fma(-s3, dun, d14);
+  double ldun = -s3 * fma(mE, un, mu_n);
+  double ls1 = fma(-ld14, c, ls14), ls4 = fma(ld14, c, ls14);
+  double lc = ld14 * (s4 - s1);
+  const double la1 = ls1 * X1 * h2, la4 = ls4 * X4 * h2;
+  const double lX1 = ls1 * a1 * h2, lX4 = ls4 * a4 * h2;
+  const double lh2 = fma(ls1 * a1, X1, ls4 * a4 * X4);
+  double ldp = lX1 + lX4;
+  double lrc = (lX4 - lX1) * dun;
+  ldun = fma(lX4 - lX1, rc, ldun);
+  double lic2 = 0.5 * lh2;
+  double laun = ls2 * fma(-dp, ic2, drho);
+  double ldrho = ls2 * aun;
+  ldp = fma(-ls2 * aun, ic2, ldp);
+  lic2 = fma(-ls2 * aun, dp, lic2);
+  laun = fma(ls3, rho, laun);
+  double lrho = ls3 * aun;
+  lrho = fma(lrc, c, lrho);
+  lc = fma(lrc, rho, lc);
+  lun += un < 0.0 ? -laun : laun;
+  double llm, llp, ldelta = 0.0;
+  if (e1) { llm = lmv < 0.0 ? -la1 : la1; }
+  else {
+    llm = la1 * 2.0 * lmv * 10.0 * ic;
+    ldelta = fma(la1 * 2.0 * delta, 10.0 * ic, ldelta);
+    lc = fma(-la1 * fma(lmv, lmv, delta * delta), 10.0 * ic * ic, lc);
+  }
+  if (e4) { llp = lpv < 0.0 ? -la4 : la4; }
+  else {
+    llp = la4 * 2.0 * lpv * 10.0 * ic;
+    ldelta = fma(la4 * 2.0 * delta, 10.0 * ic, ldelta);
+    lc = fma(-la4 * fma(lpv, lpv, delta * delta), 10.0 * ic * ic, lc);
+  }
+  lun += llm + llp;
+  lc += llp - llm + 0.05 * ldelta;
+  const double lc2 = lc * 0.5 * ic - lic2 * ic2 * ic2;
+  lht = fma(g - 1.0, lc2, lht);
+  lu2 = fma(-0.5 * (g - 1.0), lc2, lu2);
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    lu[k] = fma(2.0 * u[k], lu2, fma(n[k], lun, lu[k]));
+    ldu[k] = fma(n[k], ldun, ldu[k]);
+  }
+  // left / right primitive cotangents
+  double llu[D], lru[D];
+  double llr = -ldrho, lrr = ldrho, llp_ = -ldp, lrp_ = ldp;
+  const double lwl0 = lht * hl, lhl = lht * wl, lwr0 = lht * hr, lhr = lht * wr;
+  double lwl = lwl0, lwr = lwr0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    llu[k] = fma(lu[k], wl, -ldu[k]);
+    lru[k] = fma(lu[k], wr, ldu[k]);
+    lwl = fma(lu[k], l.u[k], lwl);
+    lwr = fma(lu[k], r.u[k], lwr);
+  }
+  double lsl = fma(lrho, sr, lwl * is), lsr = fma(lrho, sl, lwr * is);
+  const double lsum = -is * is * fma(lwl, sl, lwr * sr);
+  lsl += lsum; lsr += lsum;
+  llr = fma(lsl, 0.5 * rcp(sl), llr);
+  lrr = fma(lsr, 0.5 * rcp(sr), lrr);
+  double lLE = lhl * l.ir, lRE = lhr * r.ir;
+  llp_ = fma(lhl, l.ir, llp_);
+  lrp_ = fma(lhr, r.ir, lrp_);
+  double lLir = lhl * (l.E + l.p), lRir = lhr * (r.E + r.p);
+  // 1/2 (fl + fr): normal fluxes of each side
+  double gk[D];
+  const double g0 = 0.5 * lh[0], gE = 0.5 * lh[NV - 1];
+#pragma unroll
+  for (int k = 0; k < D; ++k) gk[k] = 0.5 * lh[1 + k];
+  double lunl = fma(g0, l.r, gE * (l.E + l.p)), lunr = fma(g0, r.r, gE * (r.E + r.p));
+  double lLm[D], lRm[D], gn = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    lunl = fma(gk[k], l.m[k], lunl);
+    lunr = fma(gk[k], r.m[k], lunr);
+    lLm[k] = gk[k] * unl;
+    lRm[k] = gk[k] * unr;
+    gn = fma(gk[k], n[k], gn);
+  }
+  llr = fma(g0, unl, llr);
+  lrr = fma(g0, unr, lrr);
+  llp_ += fma(gE, unl, gn);
+  lrp_ += fma(gE, unr, gn);
+  lLE = fma(gE, unl, lLE);
+  lRE = fma(gE, unr, lRE);
+#pragma unroll
+  for (int k = 0; k < D; ++k) { llu[k] = fma(n[k], lunl, llu[k]); lru[k] = fma(n[k], lunr, lru[k]); }
+  // states: p = gm1 (E - 1/2 m.u), u = m ir, ir = 1/rho
+  lLE = fma(ph.gm1, llp_, lLE);
+  lRE = fma(ph.gm1, lrp_, lRE);
+  const double hpl = -0.5 * ph.gm1 * llp_, hpr = -0.5 * ph.gm1 * lrp_;
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    lLm[k] = fma(hpl, l.u[k], lLm[k]);
+    llu[k] = fma(hpl, l.m[k], llu[k]);
+    lRm[k] = fma(hpr, r.u[k], lRm[k]);
+    lru[k] = fma(hpr, r.m[k], lru[k]);
+    lLm[k] = fma(llu[k], l.ir, lLm[k]);
+    lRm[k] = fma(lru[k], r.ir, lRm[k]);
+    lLir = fma(llu[k], l.m[k], lLir);
+    lRir = fma(lru[k], r.m[k], lRir);
+  }
+  llr = fma(-l.ir * l.ir, lLir, llr);
+  lrr = fma(-r.ir * r.ir, lRir, lrr);
+  lamL[0] += llr; lamR[0] += lrr;
+#pragma unroll
+  for (int k = 0; k < D; ++k) { lamL[1 + k] += lLm[k]; lamR[1 + k] += lRm[k]; }
+  lamL[NV - 1] += lLE; lamR[NV - 1] += lRE;
+}
+
 // ---- work buffers -------------------------------------------------------------------------------------
 struct AdjArgs {
   const double* u;        // stage input state [e][USTRIDE]
@@ -399,7 +744,6 @@ template <int DIM, int N, bool VISC>
 __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(AdjArgs a, Phys ph) {
   using A = AdjShape<DIM, N>;
   constexpr int NV = A::NV, NB = A::NB, NF = A::NF, NFQ = A::NFQ, EPB = A::EPB;
-  using DK = Dual<NV>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* sS = reinterpret_cast<double*>(smem_raw);  // [EPB][NV][NB] s = lam / |J|
   TensorTables* T = reinterpret_cast<TensorTables*>(sS + EPB * NV * NB);
@@ -441,35 +785,14 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(
         lq[b][v] = acc;
       }
     }
-    // Jacobian with respect to U (G held fixed): one Dual<NV> pass
-    DK U[NV], gg[VISC ? NV * DIM : 1];
+    // Jacobian transposes with respect to U (G held fixed) and, for Navier-Stokes, G
+    double Uv[NV], lu[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-      U[v] = DK(a.u[e * A::USTRIDE + v * NB + node]);
-      U[v].d[v] = 1.0;
-    }
+    for (int v = 0; v < NV; ++v) Uv[v] = a.u[e * A::USTRIDE + v * NB + node];
+    eulerVolumeReverse<DIM>(Uv, ja, lq, ph, lu);
     if constexpr (VISC) {
-#pragma unroll
-      for (int c = 0; c < NV * DIM; ++c) gg[c] = DK(a.grad[(e * NV * DIM + c) * NB + node]);
-    }
-    DK Q[DIM][NV], Qv[DIM][NV];
-    nodeFlux<DIM, VISC>(U, gg, ja, ph, Q, Qv);
-#pragma unroll
-    for (int w = 0; w < NV; ++w) {
-      double acc = 0.0;
-#pragma unroll
-      for (int b = 0; b < DIM; ++b)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) acc = fma(lq[b][v], Q[b][v].d[w], acc);
-      a.lamU[e * A::USTRIDE + w * NB + node] = acc;
-    }
-    if constexpr (VISC) {
-#pragma unroll
-      for (int b = 0; b < DIM; ++b)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) mupart = fma(lq[b][v], Qv[b][v].v, mupart);
-      // lamF[c][v] = lambda of Fv_c(v): Q_b contains -sum_c ja[b][c] Fv_c
-      double lamF[DIM][NV];
+      // lamF[c][v] = cotangent of Fv_c(v): Q_b contains -sum_c ja[b][c] Fv_c
+      double lamF[DIM][NV], gg[NV * DIM], lg[NV * DIM];
 #pragma unroll
       for (int c = 0; c < DIM; ++c)
 #pragma unroll
@@ -479,15 +802,14 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(
           for (int b = 0; b < DIM; ++b) acc = fma(-ja[b][c], lq[b][v], acc);
           lamF[c][v] = acc;
         }
-      double Uv[NV], lg[NV * DIM];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) Uv[v] = U[v].v;
-#pragma unroll
-      for (int c = 0; c < NV * DIM; ++c) lg[c] = 0.0;
-      viscousTransposeG<DIM>(Uv, ph, lamF, lg);
+      for (int c = 0; c < NV * DIM; ++c) { gg[c] = a.grad[(e * NV * DIM + c) * NB + node]; lg[c] = 0.0; }
+      mupart = viscousReverse<DIM>(Uv, gg, lamF, ph, lu, lg);
 #pragma unroll
       for (int c = 0; c < NV * DIM; ++c) a.lamG[(e * NV * DIM + c) * NB + node] = lg[c];
     }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.lamU[e * A::USTRIDE + v * NB + node] = lu[v];
   }
   if constexpr (VISC) blockSum(mupart, a.muPart + blockIdx.x, sRed);
   // transposed lift: lamH(f, j) = -sum over the line through (f, j) of lift(a) s(a)
@@ -510,8 +832,9 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(
   }
 }
 
-// V2: face point.  lam_h = lamH(L) - lamH(R) (the +/- scatter); trace cotangents from Dual<NV> passes
-// seeded on UL and on UR; NS gradient-trace cotangents by the viscous transpose; muPart = <lam_h, hv>.
+// V2: face point.  lam_h = lamH(L) - lamH(R) (the +/- scatter); trace cotangents of the convective flux
+// (Roe: hand-written reverse sweep; other fluxes: Dual<NV> passes seeded on UL and on UR) and, for
+// Navier-Stokes, of each side's viscous flux (state and gradient parts); muPart = <lam_h, hv>.
 template <int DIM, int FLUX, bool VISC>
 __global__ void __launch_bounds__(kFaceThreads) vjpFaceKernel(AdjArgs a, Phys ph) {
   constexpr int NV = DIM + 2;
@@ -527,48 +850,49 @@ __global__ void __launch_bounds__(kFaceThreads) vjpFaceKernel(AdjArgs a, Phys ph
     const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
     const int jr = rightPoint<DIM>(j, rot, n1d);
     const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
-    const int64_t LG = int64_t(sl) * NV * DIM * nfq + j, RG = int64_t(sr) * NV * DIM * nfq + jr;
     double n[DIM];
 #pragma unroll
     for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
     const double area = a.fgeo[f * 4 + 3];
-    double lh[NV], ul[NV], ur[NV];
+    double lh[NV], ul[NV], ur[NV], laml[NV], lamr[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       lh[v] = (a.lamH[L + v * nfq] - a.lamH[R + v * nfq]) * area;
       ul[v] = a.face[L + v * nfq];
       ur[v] = a.face[R + v * nfq];
+      laml[v] = 0.0;
+      lamr[v] = 0.0;
     }
+    if constexpr (FLUX == 3) {
+      roeReverse<DIM>(ul, ur, n, ph, lh, laml, lamr);
+    } else {
 #pragma unroll
-    for (int side = 0; side < 2; ++side) {
-      DK xl[NV], xr[NV], gl[VISC ? NV * DIM : 1], gr[VISC ? NV * DIM : 1];
+      for (int side = 0; side < 2; ++side) {
+        DK xl[NV], xr[NV];
 #pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        xl[v] = DK(ul[v]);
-        xr[v] = DK(ur[v]);
-        if (side == 0) xl[v].d[v] = 1.0; else xr[v].d[v] = 1.0;
-      }
-      if constexpr (VISC) {
+        for (int v = 0; v < NV; ++v) {
+          xl[v] = DK(ul[v]);
+          xr[v] = DK(ur[v]);
+          if (side == 0) xl[v].d[v] = 1.0; else xr[v].d[v] = 1.0;
+        }
+        State<DIM, DK> l, r;
+        makeState<DIM>(l, xl, ph);
+        makeState<DIM>(r, xr, ph);
+        DK h[NV];
+        convectiveFlux<DIM, FLUX>(l, r, n, ph, h);
+        double* out = side == 0 ? laml : lamr;
 #pragma unroll
-        for (int c = 0; c < NV * DIM; ++c) { gl[c] = DK(a.faceGrad[LG + c * nfq]); gr[c] = DK(a.faceGrad[RG + c * nfq]); }
-      }
-      DK h[NV], hv[NV];
-      faceFluxPoint<DIM, FLUX, VISC>(xl, xr, gl, gr, n, ph, h, hv);
-      if (side == 0 && VISC) {
+        for (int w = 0; w < NV; ++w) {
+          double acc = 0.0;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) mupart = fma(lh[v], hv[v].v, mupart);
-      }
-      double* out = a.lamTr + (side == 0 ? L : R);
-#pragma unroll
-      for (int w = 0; w < NV; ++w) {
-        double acc = 0.0;
-#pragma unroll
-        for (int v = 0; v < NV; ++v) acc = fma(lh[v], h[v].d[w], acc);
-        out[w * nfq] = acc;
+          for (int v = 0; v < NV; ++v) acc = fma(lh[v], h[v].d[w], acc);
+          out[w] = acc;
+        }
       }
     }
     if constexpr (VISC) {
       // h contains -1/2 Fv(U_side, G_side).n on each side: lamF[c][v] = -1/2 n_c lam_h(v)
+      const int64_t LG = int64_t(sl) * NV * DIM * nfq + j, RG = int64_t(sr) * NV * DIM * nfq + jr;
       double lamF[DIM][NV];
 #pragma unroll
       for (int c = 0; c < DIM; ++c)
@@ -576,14 +900,20 @@ __global__ void __launch_bounds__(kFaceThreads) vjpFaceKernel(AdjArgs a, Phys ph
         for (int v = 0; v < NV; ++v) lamF[c][v] = -0.5 * n[c] * lh[v];
 #pragma unroll
       for (int side = 0; side < 2; ++side) {
-        double lg[NV * DIM];
+        const int64_t G0 = side == 0 ? LG : RG;
+        double gg[NV * DIM], lg[NV * DIM];
 #pragma unroll
-        for (int c = 0; c < NV * DIM; ++c) lg[c] = 0.0;
-        viscousTransposeG<DIM>(side == 0 ? ul : ur, ph, lamF, lg);
-        double* out = a.lamTg + (side == 0 ? LG : RG);
+        for (int c = 0; c < NV * DIM; ++c) { gg[c] = a.faceGrad[G0 + c * nfq]; lg[c] = 0.0; }
+        mupart += viscousReverse<DIM>(side == 0 ? ul : ur, gg, lamF, ph, side == 0 ? laml : lamr, lg);
+        double* out = a.lamTg + G0;
 #pragma unroll
         for (int c = 0; c < NV * DIM; ++c) out[c * nfq] = lg[c];
       }
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      a.lamTr[L + v * nfq] = laml[v];
+      a.lamTr[R + v * nfq] = lamr[v];
     }
   }
   if constexpr (VISC) blockSum(mupart, a.muPart + blockIdx.x, sRed);

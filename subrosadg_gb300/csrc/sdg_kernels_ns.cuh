@@ -100,15 +100,16 @@ __device__ __forceinline__ void exchangeBoundaryPoint(const FaceArgs& a, int64_t
   for (int v = 0; v < NV; ++v) a.other[L + v * nfq] = 2.0 * ub[v] - ul[v];
 }
 
-template <int DIM, int N, bool AFFINE>
+template <int DIM, int N, bool AFFINE, bool BR2>
 struct GradShape {
   using S = TensorShape<DIM, N>;
   static constexpr int NV = S::NV, NB = S::NB, NF = S::NF, NFQ = S::NFQ;
   static constexpr int FS = NF * NV * NFQ;      // trace slots per element (one area)
   static constexpr int GSTR = NV * DIM * NB;    // gradient doubles per element
   static constexpr int PSZ = AFFINE ? 0 : DIM * DIM * NV * NB;  // bilinear: U |J| dxi_b/dx_k per node
-  // shared memory per element: state, own traces, other traces, gradient (total and volume), scratch
-  static constexpr int PER_ELEM = S::USTRIDE + 2 * FS + 2 * GSTR + PSZ + NB;
+  // shared memory per element: state, own traces, other traces, gradient (total; BR2 also the volume
+  // gradient), metric products (bilinear), 1/|J|
+  static constexpr int PER_ELEM = S::USTRIDE + (BR2 ? 2 : 1) * FS + (BR2 ? 2 : 1) * GSTR + PSZ + NB;
   static constexpr int EPB_SMEM = (100 * 1024) / (8 * PER_ELEM) > 0 ? (100 * 1024) / (8 * PER_ELEM) : 1;
   static constexpr int EPB = S::EPB_RAW < EPB_SMEM ? S::EPB_RAW : EPB_SMEM;
   static constexpr int THREADS = ((EPB * NB + 31) / 32) * 32;
@@ -117,9 +118,9 @@ struct GradShape {
   static constexpr size_t smemFor(int epb) { return size_t(epb) * PER_ELEM * 8 + sizeof(TensorTables) + 16; }
 };
 
-template <int DIM, int N, bool AFFINE>
+template <int DIM, int N, bool AFFINE, bool BR2>
 __device__ __forceinline__ uint64_t* tensorGradBarrier(int epb) {
-  using G = GradShape<DIM, N, AFFINE>;
+  using G = GradShape<DIM, N, AFFINE, BR2>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* end = reinterpret_cast<double*>(smem_raw) + epb * G::PER_ELEM;
   return reinterpret_cast<uint64_t*>(reinterpret_cast<TensorTables*>(end) + 1);
@@ -127,18 +128,18 @@ __device__ __forceinline__ uint64_t* tensorGradBarrier(int epb) {
 
 // Weak (BR) gradient of a tensor block, one tile: one thread per node.  Writes the total gradient at the
 // nodes and the face gradient traces (BR1: total gradient; BR2: volume gradient + the face's own lift).
-template <int DIM, int N, bool AFFINE>
+template <int DIM, int N, bool AFFINE, bool BR2>
 __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t tile, uint32_t parity, bool loadTables) {
-  using G = GradShape<DIM, N, AFFINE>;
+  using G = GradShape<DIM, N, AFFINE, BR2>;
   using S = TensorShape<DIM, N>;
   constexpr int NV = G::NV, NB = G::NB, NF = G::NF, NFQ = G::NFQ, FS = G::FS;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int epb = a.epb;
   double* sU = reinterpret_cast<double*>(smem_raw);  // [epb][USTRIDE]
-  double* sS = sU + epb * S::USTRIDE;                // own traces [epb][FS]
-  double* sO = sS + epb * FS;                        // other traces [epb][FS]
+  double* sS = sU + epb * S::USTRIDE;                // own traces [epb][FS] (BR2 only)
+  double* sO = sS + (BR2 ? epb * FS : 0);            // other traces [epb][FS]
   double* sGt = sO + epb * FS;                       // total gradient [epb][NV*DIM][NB]
-  double* sGv = sGt + epb * G::GSTR;                 // BR2 volume gradient [epb][NV*DIM][NB]
+  double* sGv = sGt + (BR2 ? epb * G::GSTR : 0);    // BR2 volume gradient [epb][NV*DIM][NB]
   double* sP = sGv + epb * G::GSTR;                  // bilinear: U |J| dxi_b/dx_k [epb][DIM*DIM*NV][NB]
   double* sJ = sP + epb * G::PSZ;                    // 1/|J| per node [epb][NB]
   TensorTables* T = reinterpret_cast<TensorTables*>(sJ + epb * NB);
@@ -154,9 +155,9 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
   if (tid == 0) {
     fenceProxyAsync();
     const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * FS * 8;
-    mbarExpectTx(bar, ub + 2 * fb);
+    mbarExpectTx(bar, ub + (BR2 ? 2 : 1) * fb);
     bulkLoad(sU, a.u + e0 * S::USTRIDE, ub, bar);
-    bulkLoad(sS, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
+    if (BR2) bulkLoad(sS, a.face + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
     bulkLoad(sO, a.faceOther + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
   if (loadTables)
@@ -219,16 +220,21 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
         const int fm = T->axisFace[b][0], fp = T->axisFace[b][1];
         const int jm = T->nodeFacePoint[b][0][node], jp = T->nodeFacePoint[b][1][node];
         const double om = sO[le * FS + (fm * NV + v) * NFQ + jm], op = sO[le * FS + (fp * NV + v) * NFQ + jp];
-        const double sm = sS[le * FS + (fm * NV + v) * NFQ + jm], sp = sS[le * FS + (fp * NV + v) * NFQ + jp];
+        const double sm = BR2 ? sS[le * FS + (fm * NV + v) * NFQ + jm] : 0.0;
+        const double sp = BR2 ? sS[le * FS + (fp * NV + v) * NFQ + jp] : 0.0;
         if constexpr (AFFINE) {
           double dref = 0.0;
 #pragma unroll
           for (int q = 0; q < N; ++q) dref = fma(T->dhat[q][ax[b]], sU[le * S::USTRIDE + v * NB + base + q * st], dref);
           // |J| dxi_b/dx_k . (Lhat+ X+ - Lhat- X- - dref); nF(b,+) = -nF(b,-) = |J| dxi_b/dx
           const double tt = fma(lp, op, fma(-lm, om, -dref));
-          const double tv = fma(lp, 0.5 * (op + sp), fma(-lm, 0.5 * (om + sm), -dref));
 #pragma unroll
-          for (int k = 0; k < DIM; ++k) { tot[k] = fma(ja[b][k], tt, tot[k]); vol[k] = fma(ja[b][k], tv, vol[k]); }
+          for (int k = 0; k < DIM; ++k) tot[k] = fma(ja[b][k], tt, tot[k]);
+          if constexpr (BR2) {
+            const double tv = fma(lp, 0.5 * (op + sp), fma(-lm, 0.5 * (om + sm), -dref));
+#pragma unroll
+            for (int k = 0; k < DIM; ++k) vol[k] = fma(ja[b][k], tv, vol[k]);
+          }
         } else {
 #pragma unroll
           for (int k = 0; k < DIM; ++k) {
@@ -237,15 +243,16 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
 #pragma unroll
             for (int q = 0; q < N; ++q) dk = fma(T->dhat[q][ax[b]], P[q * st], dk);
             tot[k] = fma(lp * nF[b][1][k], op, fma(lm * nF[b][0][k], om, tot[k] - dk));
-            vol[k] = fma(lp * nF[b][1][k], 0.5 * (op + sp), fma(lm * nF[b][0][k], 0.5 * (om + sm), vol[k] - dk));
+            if constexpr (BR2)
+              vol[k] = fma(lp * nF[b][1][k], 0.5 * (op + sp), fma(lm * nF[b][0][k], 0.5 * (om + sm), vol[k] - dk));
           }
         }
       }
 #pragma unroll
       for (int k = 0; k < DIM; ++k) {
-        const double gt = tot[k] * jinv, gv = vol[k] * jinv;
+        const double gt = tot[k] * jinv;
         sGt[(le * NV * DIM + v * DIM + k) * NB + node] = gt;
-        sGv[(le * NV * DIM + v * DIM + k) * NB + node] = gv;
+        if constexpr (BR2) sGv[(le * NV * DIM + v * DIM + k) * NB + node] = vol[k] * jinv;
         a.grad[(e * NV * DIM + v * DIM + k) * NB + node] = gt;
       }
     }
@@ -262,9 +269,9 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
     const int st = strideOf<DIM, N>(axis);
     const int64_t ee = e0 + te;
     double* out = a.faceGrad + (a.faceBase + ee * NF + f) * NV * DIM * NFQ + j;
-    const double* src = a.br2 ? sGv : sGt;
+    const double* src = BR2 ? sGv : sGt;
     double nf[DIM], cl = 0.0;
-    if (a.br2) {
+    if constexpr (BR2) {
       // lift trace factor sum_a l_a(end)^2 / (w_a |J|_a) and the face's n|J_f|
 #pragma unroll
       for (int q = 0; q < N; ++q) cl = fma(coef[q] * lift[q], sJ[te * NB + base + q * st], cl);
@@ -279,14 +286,14 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const double jump = a.br2 ? 0.5 * (sO[te * FS + (f * NV + v) * NFQ + j] - sS[te * FS + (f * NV + v) * NFQ + j]) : 0.0;
+      const double jump = BR2 ? 0.5 * (sO[te * FS + (f * NV + v) * NFQ + j] - sS[te * FS + (f * NV + v) * NFQ + j]) : 0.0;
 #pragma unroll
       for (int k = 0; k < DIM; ++k) {
         const double* gsrc = src + (te * NV * DIM + v * DIM + k) * NB + base;
         double acc = 0.0;
 #pragma unroll
         for (int q = 0; q < N; ++q) acc = fma(coef[q], gsrc[q * st], acc);
-        if (a.br2) acc = fma(cl * nf[k], jump, acc);
+        if constexpr (BR2) acc = fma(cl * nf[k], jump, acc);
         out[(v * DIM + k) * NFQ] = acc;
       }
     }
@@ -294,21 +301,21 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
   return true;
 }
 
-template <int DIM, int N, bool AFFINE>
+template <int DIM, int N, bool AFFINE, bool BR2>
 __global__ void __launch_bounds__(kMaxTileThreads) tensorGradientKernel(GradArgs a) {
-  if (threadIdx.x == 0) mbarInit(tensorGradBarrier<DIM, N, AFFINE>(a.epb), 1);
-  tensorGradientTile<DIM, N, AFFINE>(a, blockIdx.x, 0u, true);
+  if (threadIdx.x == 0) mbarInit(tensorGradBarrier<DIM, N, AFFINE, BR2>(a.epb), 1);
+  tensorGradientTile<DIM, N, AFFINE, BR2>(a, blockIdx.x, 0u, true);
 }
 
-template <int DIM, int N, bool AFFINE>
+template <int DIM, int N, bool AFFINE, bool BR2>
 __global__ void __launch_bounds__(kMaxTileThreads)
     tensorGradientBatchKernel(const GradArgs* __restrict__ args, const int2* __restrict__ items, int nitems, int epb) {
-  if (threadIdx.x == 0) mbarInit(tensorGradBarrier<DIM, N, AFFINE>(epb), 1);
+  if (threadIdx.x == 0) mbarInit(tensorGradBarrier<DIM, N, AFFINE, BR2>(epb), 1);
   uint32_t parity = 0;
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const int2 it = items[w];
     const GradArgs a = args[it.x];
-    if (!tensorGradientTile<DIM, N, AFFINE>(a, it.y, parity, w == int(blockIdx.x))) return;
+    if (!tensorGradientTile<DIM, N, AFFINE, BR2>(a, it.y, parity, w == int(blockIdx.x))) return;
     parity ^= 1u;
   }
 }

@@ -27,7 +27,7 @@ struct KernelVariant {
 
 // Tile kernels (elements of one block per CTA).  Unsupported combinations return an invalid variant.
 KernelVariant tensorStageVariant(int dim, int n, bool affine, bool visc);
-KernelVariant tensorGradVariant(int dim, int n, bool affine);
+KernelVariant tensorGradVariant(int dim, int n, bool affine, bool br2);
 KernelVariant denseStageVariant(int type, int p, bool affine, bool visc);
 KernelVariant denseGradVariant(int type, int p, bool affine);
 // Face-point kernels (FaceOp op, flux only for the Riemann operations) and the relative-error reduction.

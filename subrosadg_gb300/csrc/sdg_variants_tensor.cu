@@ -16,12 +16,12 @@ KernelVariant stageOf() {
   v.perElem = S::SMEM_PER_ELEM; v.fixed = sizeof(TensorTables) + 16; v.perWarp = 8 * S::NV;
   return v;
 }
-template <int DIM, int N, bool AFF>
+template <int DIM, int N, bool AFF, bool BR2>
 KernelVariant gradOf() {
-  using G = GradShape<DIM, N, AFF>;
+  using G = GradShape<DIM, N, AFF, BR2>;
   KernelVariant v;
-  v.single = reinterpret_cast<const void*>(&tensorGradientKernel<DIM, N, AFF>);
-  v.batch = reinterpret_cast<const void*>(&tensorGradientBatchKernel<DIM, N, AFF>);
+  v.single = reinterpret_cast<const void*>(&tensorGradientKernel<DIM, N, AFF, BR2>);
+  v.batch = reinterpret_cast<const void*>(&tensorGradientBatchKernel<DIM, N, AFF, BR2>);
   v.nb = G::NB; v.epb = G::EPB; v.threads = G::THREADS; v.nodeThreads = true;
   v.perElem = size_t(G::PER_ELEM) * 8; v.fixed = sizeof(TensorTables) + 16; v.perWarp = 0;
   return v;
@@ -42,12 +42,12 @@ KernelVariant tensorStageVariant(int dim, int n, bool affine, bool visc) {
   return KernelVariant();
 }
 
-KernelVariant tensorGradVariant(int dim, int n, bool affine) {
-#define SDG_TG(D, NN)                                         \
-  if (dim == D && n == NN) {                                  \
-    if (affine) return gradOf<D, NN, true>();                 \
-    if constexpr (D == 2) return gradOf<D, NN, false>();      \
-    return KernelVariant();                                   \
+KernelVariant tensorGradVariant(int dim, int n, bool affine, bool br2) {
+#define SDG_TG(D, NN)                                                                         \
+  if (dim == D && n == NN) {                                                                  \
+    if (affine) return br2 ? gradOf<D, NN, true, true>() : gradOf<D, NN, true, false>();       \
+    if constexpr (D == 2) return br2 ? gradOf<D, NN, false, true>() : gradOf<D, NN, false, false>(); \
+    return KernelVariant();                                                                   \
   }
   SDG_TENSOR_ORDERS(SDG_TG)
 #undef SDG_TG

@@ -300,6 +300,18 @@ class GpuSolver:
         self._chk(self.lib.sdg_adjoint_steps(self.h, steps, dt, checkpoint_interval, _ptr(c), _ptr(out), byref(mu)))
         return out, mu.value
 
+    def forward_steps(self, dt, steps, checkpoint_interval=25):
+        """Advance `steps` steps keeping the checkpoints of the trajectory (for adjoint_recorded)."""
+        self._chk(self.lib.sdg_forward_steps(self.h, steps, dt, checkpoint_interval))
+
+    def adjoint_recorded(self, final_cotangent):
+        """Reverse sweep of the last forward_steps trajectory (the state must still be its U_N)."""
+        c = np.ascontiguousarray(final_cotangent, np.float64)
+        out = self._points()
+        mu = c_double()
+        self._chk(self.lib.sdg_adjoint_recorded(self.h, _ptr(c), _ptr(out), byref(mu)))
+        return out, mu.value
+
     def kinetic_energy(self, state=None, weights=None):
         """J = integral of rho |u|^2 / 2 and dJ/dU in the point layout."""
         u = self.state_point() if state is None else state

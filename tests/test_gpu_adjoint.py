@@ -217,3 +217,20 @@ def test_derivatives_refuse_unsupported_configurations():
     with pytest.raises(sdg.SdgError) as e:
         walls.vjp_residual(np.zeros((walls.counts.volume_point_count, 4)))
     assert e.value.code == _abi.SDG_ERR_UNSUPPORTED
+
+
+def test_recorded_trajectory_adjoint_equals_the_one_call_adjoint():
+    a, dt = make("ns-hex-p3-br1-roe")
+    b, _ = make("ns-hex-p3-br1-roe")
+    lamN = np.random.default_rng(8).standard_normal(a.state_point().shape)
+    lam_a, mu_a = a.adjoint_steps(dt, 5, lamN, checkpoint_interval=2)
+    b.forward_steps(dt, 5, checkpoint_interval=2)
+    assert np.array_equal(b.state_point(), a.state_point())
+    lam_b, mu_b = b.adjoint_recorded(lamN)
+    assert np.array_equal(lam_a, lam_b) and mu_a == mu_b
+    # any state change in between invalidates the recorded trajectory
+    b.forward_steps(dt, 2, checkpoint_interval=2)
+    b.stepSolver(dt, 1)
+    with pytest.raises(sdg.SdgError) as e:
+        b.adjoint_recorded(lamN)
+    assert e.value.code == _abi.SDG_ERR_STATE
