@@ -17,6 +17,9 @@ workloads of the metric, each measured the same way on this GPU:
   ns_hybrid    2D Navier-Stokes BR2 Kelvin-Helmholtz, Re 1e4, 256^2 jittered quads with a 50% triangle
                split, P4, Lax-Friedrichs
   vortex2d     2D Euler isentropic vortex, 40^2 quads, P3, Roe, dt 1e-3 (L2-resident, launch bound)
+  adjoint      3D Navier-Stokes BR1 Taylor-Green, Re 1600, Mach 0.1, 32^3 hexahedra, P3, Roe, 500 SSP-RK3 steps:
+               forward, checkpointed adjoint (every 25 steps) of the integrated kinetic energy, reverse sweep
+               of a recorded trajectory, and central-difference checks of dJ/dU0 (seeded direction) and dJ/dmu
 --impl reference times the CPU restatement of the reference path (the oracle, reference-faithful
 arithmetic) on the host cores.  Under torchrun (N > 1) each rank runs an independent replica on its own
 GPU (the path is not sharded: replicas only).
@@ -54,9 +57,14 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="headline workload only")
+    ap.add_argument("--extra", default="batched,ns_hybrid,vortex2d,adjoint",
+                    help="comma list of the other workloads to measure")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-max-elements", type=int, default=50000)
     ap.add_argument("--ns-elements", type=int, default=256, help="quads per direction of the NS hybrid mesh")
+    ap.add_argument("--adjoint-elements", type=int, default=32)
+    ap.add_argument("--adjoint-steps", type=int, default=500)
+    ap.add_argument("--no-adjoint-check", action="store_true", help="skip the finite-difference checks")
     return ap.parse_args()
 
 
@@ -306,6 +314,76 @@ def bench_vortex(args, device, torch):
     return out
 
 
+def bench_adjoint(args, device, torch):
+    """cfg5: gradient of the integrated kinetic energy at the final time w.r.t. U0 and mu."""
+    import subrosadg_gb300 as sdg
+    from tests import cases
+    n, steps, K = args.adjoint_elements, args.adjoint_steps, 25
+    mesh, cfg, prim, _, _, _ = cases.tgv_case(n=n, p=3, flux=sdg.ROE, viscous=sdg.BR1, mu=1.0 / 1600.0)
+    s = sdg.GpuSolver(mesh, cfg, device=device)
+    s.initialize_primitive(prim(s.volume_points()))
+    s.autotune()
+    dt = s.calculateDeltaTime(0.2)
+    u0 = s.state_point()
+    w = s.volume_weights()
+    mu0 = s.config.dynamic_viscosity
+    s.stepSolver(dt, 3)
+    s.set_state_point(u0)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    s.stepSolver(dt, steps)
+    t_fwd = time.perf_counter() - t0
+    J0, lamN = s.kinetic_energy(weights=w)
+    s.set_state_point(u0)
+    t0 = time.perf_counter()
+    lam0, mubar = s.adjoint_steps(dt, steps, lamN, checkpoint_interval=K)
+    t_adj = time.perf_counter() - t0
+    s.set_state_point(u0)
+    s.forward_steps(dt, steps, checkpoint_interval=K)
+    t0 = time.perf_counter()
+    lam1, mubar1 = s.adjoint_recorded(lamN)
+    t_rev = time.perf_counter() - t0
+    mem = ctypes_int64(s)
+    out = {"workload": f"ns-tgv3d-BR1-Roe-Re1600-Ma0.1-{n}^3-hex-P3-{steps}steps-checkpoint{K}",
+           "dof": s.counts.degree_of_freedom_count, "steps": steps, "J": J0,
+           "forward_ms_per_step": 1e3 * t_fwd / steps, "adjoint_ms_per_step": 1e3 * t_adj / steps,
+           "adjoint_over_forward": t_adj / t_fwd, "reverse_only_over_forward": t_rev / t_fwd,
+           "recorded_equals_one_call": bool(np.array_equal(lam0, lam1) and mubar == mubar1),
+           "dJ_dmu": mubar, "checkpoint_bytes": mem,
+           "note": "wall-clock of synchronous calls; full adjoint = forward sweep with checkpoints + per-segment "
+                   "recompute + reverse sweep"}
+    if not args.no_adjoint_check:
+        rng = np.random.default_rng(2025)
+        d0 = rng.standard_normal(u0.shape) * (np.abs(u0).mean(0) + 1e-3)
+        h = 1e-6
+
+        def J(u, mu=mu0):
+            s.set_viscosity(mu)
+            s.set_state_point(u)
+            s.stepSolver(dt, steps)
+            return s.kinetic_energy(weights=w)[0]
+
+        fd = (J(u0 + h * d0) - J(u0 - h * d0)) / (2 * h)
+        ad = float(np.sum(lam0 * d0))
+        hm = h * mu0
+        fdm = (J(u0, mu0 + hm) - J(u0, mu0 - hm)) / (2 * hm)
+        s.set_viscosity(mu0)
+        out["check"] = {"direction": "seeded normal, scaled per variable by the mean |U| (seed 2025)", "h": h,
+                        "dJ_dU0_dot_d": {"adjoint": ad, "central_difference": fd,
+                                         "relative_difference": abs(ad - fd) / max(abs(fd), 1e-300)},
+                        "dJ_dmu": {"adjoint": mubar, "central_difference": fdm,
+                                   "relative_difference": abs(mubar - fdm) / max(abs(fdm), 1e-300)}}
+    s.close()
+    return out
+
+
+def ctypes_int64(s):
+    import ctypes
+    v = ctypes.c_int64()
+    s.lib.sdg_adjoint_memory(s.h, ctypes.byref(v))
+    return v.value
+
+
 def run_ours(args):
     import ctypes
 
@@ -381,10 +459,10 @@ def run_ours(args):
     achieved = elem_bytes / (elem_avg_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peaks()
     prof = profile_figures()
-    traffic = prof.get("dram_bytes_per_launch")
+    traffic = prof["dram_bytes_per_element"] * ne if "dram_bytes_per_element" in prof else None
     fp64 = ctypes.c_double()
     lib.sdg_measure_fp64_peak(device, 200.0, ctypes.byref(fp64))
-    fp64_flops = prof.get("fp64_flops_per_launch")
+    fp64_flops = prof["fp64_flops_per_element"] * ne if "fp64_flops_per_element" in prof else None
     fp64_achieved = fp64_flops / (elem_avg_ms * 1e-3) / 1e9 if fp64_flops else None
 
     # end to end through the C ABI with pinned host buffers: upload state, step, download state
@@ -436,7 +514,10 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": elem_bytes},
         "fp64": {"peak_gflops": fp64.value, "peak_source": "sdg_measure_fp64_peak (independent-chain DFMA probe)",
                  "achieved_gflops": fp64_achieved, "frac": (fp64_achieved / fp64.value) if fp64_achieved else None,
-                 "note": "the DG stage kernels are FP64-issue bound on GB300; see DESIGN.md"},
+                 "achieved_source": "ncu FP64 instruction counts of a 40^3 launch (2 per DFMA) scaled by elements "
+                                    "(profiles/tensor_stage_kernel_tgv_hex_p3.md) / the live launch time",
+                 "pipe_active_pct": prof.get("fp64_pipe_active_pct"),
+                 "note": "the DG stage kernels are FP64-issue bound on GB300"},
         "kernel_ms_per_step": {"element": kms[0] / ksteps, "interior_face": kms[1] / ksteps,
                                "boundary_face": kms[2] / ksteps, "reduction": kms[3] / ksteps,
                                "gradient": kms[4] / ksteps},
@@ -448,9 +529,10 @@ def run_ours(args):
     }
     s.close()
     if not args.no_extra:
-        line["batched"] = bench_batched(args, device, torch)
-        line["ns_hybrid"] = bench_ns_hybrid(args, device, torch)
-        line["vortex2d"] = bench_vortex(args, device, torch)
+        extras = {"batched": bench_batched, "ns_hybrid": bench_ns_hybrid, "vortex2d": bench_vortex,
+                  "adjoint": bench_adjoint}
+        for name in [x for x in args.extra.split(",") if x]:
+            line[name] = extras[name](args, device, torch)
     print(json.dumps(line), flush=True)
     if pg:
         pg.destroy_process_group()

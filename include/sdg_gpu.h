@@ -263,6 +263,16 @@ int sdg_mesh_generate_3d(double x0, double y0, double z0, double lx, double ly, 
 int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out);
 int sdg_mesh_free(sdg_generated_mesh* mesh);
 
+/* ---- raw-binary solution files (the reference's writeRawBinary / LastStep and SpecificFile restarts,
+ * src/View/RawBinary.cpp:42-191, src/Solver/InitialCondition.cpp:40-80) ---------------------------------
+ * u64 ZSTD_compressBound(payload) + one zstd level-1 frame; payload per element the column-major
+ * (d+2) x Nb modal coefficients (Navier-Stokes: then the (d+2)*d x Nb gradient coefficients), then per
+ * boundary face its parent's coefficients (in this library's boundary-face order), then one artificial
+ * viscosity value per mesh node (zero).  Needs libzstd.so.1 at run time (else SDG_ERR_UNSUPPORTED).
+ * lower_order = 1 reads a file written at order P-1 into the leading coefficients (SpecificFile). */
+int sdg_write_raw_binary(sdg_handle* handle, const char* path);
+int sdg_read_raw_binary(sdg_handle* handle, const char* path, int32_t lower_order);
+
 /* ---- launch shapes: CUDA-graph replay and the autotuner -------------------------------------------
  * sdg_step replays a CUDA graph of one full step (all stages and the relative-error reduction),
  * captured on first use and again when dt or a tile shape changes; enable = 0 issues the launches

@@ -148,6 +148,8 @@ SIGNATURES = {
                                        c_int32, c_int32, c_int32, _p_int32, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_read_msh": (c_int32, [c_char_p, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_free": (c_int32, [POINTER(SdgGeneratedMesh)]),
+    "sdg_write_raw_binary": (c_int32, [c_void_p, c_char_p]),
+    "sdg_read_raw_binary": (c_int32, [c_void_p, c_char_p, c_int32]),
     "sdg_set_graph": (c_int32, [c_void_p, c_int32]),
     "sdg_get_tile": (c_int32, [c_void_p, c_int32, _p_int32, _p_int32, _p_int32, _p_int32]),
     "sdg_set_tile": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_int32, c_int32]),

@@ -46,8 +46,8 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(LIBDIR, exist_ok=True)
     target = os.path.join(LIBDIR, "libsdg_gpu.so")
     units = ["sdg_variants_tensor.cu", "sdg_variants_dense.cu", "sdg_variants_face.cu", "sdg_variants_adjoint_face.cu",
-             "sdg_variants_adjoint_tile.cu", "sdg_gpu.cu", "sdg_batch.cu", "sdg_adjoint.cu", "sdg_mesh.cpp",
-             "sdg_noalloc.cu"]
+             "sdg_variants_adjoint_tile.cu", "sdg_gpu.cu", "sdg_batch.cu", "sdg_adjoint.cu", "sdg_rawbinary.cu",
+             "sdg_mesh.cpp", "sdg_noalloc.cu"]
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".cpp", ".hpp", ".h"))]
     deps.append(os.path.join(ROOT, "include", "sdg_gpu.h"))
     if not force and not _stale(target, deps):
@@ -69,7 +69,7 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
 
     with ThreadPoolExecutor(max_workers=len(units)) as ex:
         objs = list(ex.map(compile_unit, units))
-    _run([nvcc, GENCODE, "-shared", "-Xcompiler", "-fopenmp", "-o", target] + objs, CSRC)
+    _run([nvcc, GENCODE, "-shared", "-Xcompiler", "-fopenmp", "-o", target] + objs + ["-ldl"], CSRC)
     return target
 
 

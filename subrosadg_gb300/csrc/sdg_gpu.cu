@@ -713,7 +713,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       h->ns = true;
     }
     if (!mesh->node_coordinate || mesh->node_count <= 0) throw Failure(SDG_ERR_INVALID_ARGUMENT, "no nodes");
-    h->cfg = c; h->device = device;
+    h->cfg = c; h->device = device; h->nodeCount = mesh->node_count;
     h->dim = mesh->dimension; h->nv = h->dim + 2; h->p = c.polynomial_order;
     h->ph.gamma = c.specific_heat_ratio; h->ph.gm1 = c.specific_heat_ratio - 1.0;
     h->ph.cv = c.specific_heat_constant_volume; h->ph.inv_cv = 1.0 / c.specific_heat_constant_volume;
@@ -894,6 +894,8 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       bconn[i * 3] = int(slotOf(f.left)); bconn[i * 3 + 1] = f.condition; bconn[i * 3 + 2] = 0;
       faceGeom(f.left, &bgeo[i * 4], &h->bcoord);
       h->bphys.push_back(f.physical);
+      h->boundaryParent.push_back(f.left.block);
+      h->boundaryParent.push_back(f.left.element);
     }
     // canonical adjacency tuples
     {

@@ -116,6 +116,8 @@ struct sdg_handle {
   int nfq = 0, n1d = 0;
   std::vector<int32_t> adjInterior, adjBoundary;
   std::vector<double> bcoord; std::vector<int32_t> bphys;
+  std::vector<int32_t> boundaryParent;  // per boundary face: (block, element) of its parent
+  int64_t nodeCount = 0;                // mesh nodes (raw-binary files carry one value per node)
   double* scratch = nullptr;       // point-layout conversion buffer [volume_points][nv]
   int64_t volumePoints = 0;
   double* relPart = nullptr; int64_t relParts = 0;

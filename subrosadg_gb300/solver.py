@@ -243,6 +243,15 @@ class GpuSolver:
         self._chk(self.lib.sdg_launch_count(self.h, byref(n)))
         return n.value
 
+    # raw-binary files ---------------------------------------------------------------------------
+    def writeRawBinary(self, path):
+        """Solver::writeRawBinary: the reference's zstd raw-binary solution file."""
+        self._chk(self.lib.sdg_write_raw_binary(self.h, str(path).encode()))
+
+    def read_raw_binary(self, path, lower_order=False):
+        """Restart from a raw-binary file (LastStep; lower_order: SpecificFile written at order P-1)."""
+        self._chk(self.lib.sdg_read_raw_binary(self.h, str(path).encode(), int(bool(lower_order))))
+
     # launch shapes -----------------------------------------------------------------------------
     def set_graph(self, enable: bool):
         self._chk(self.lib.sdg_set_graph(self.h, int(bool(enable))))

@@ -1,0 +1,110 @@
+"""GPU tests of the raw-binary solution files (the reference's writeRawBinary and its LastStep / SpecificFile
+restarts, src/View/RawBinary.cpp:42-191, src/Solver/InitialCondition.cpp:40-80).
+
+The file is decoded here independently of the library (libzstd through ctypes): header = ZSTD_compressBound of
+the payload, payload = per element the column-major (d+2) x Nb modal coefficients (Navier-Stokes: then the
+(d+2)*d x Nb gradient coefficients), per boundary face its parent's coefficients, one zero per mesh node.
+"""
+import ctypes
+import ctypes.util
+
+import numpy as np
+import pytest
+
+import subrosadg_gb300 as sdg
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _zstd():
+    name = ctypes.util.find_library("zstd") or "libzstd.so.1"
+    try:
+        z = ctypes.CDLL(name)
+    except OSError:
+        pytest.skip("libzstd is not available")
+    z.ZSTD_compressBound.restype = ctypes.c_size_t
+    z.ZSTD_compressBound.argtypes = [ctypes.c_size_t]
+    z.ZSTD_decompress.restype = ctypes.c_size_t
+    z.ZSTD_decompress.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t]
+    z.ZSTD_isError.restype = ctypes.c_uint
+    z.ZSTD_isError.argtypes = [ctypes.c_size_t]
+    return z
+
+
+def decode(path):
+    z = _zstd()
+    data = open(path, "rb").read()
+    header = int.from_bytes(data[:8], "little")
+    frame = data[8:]
+    out = ctypes.create_string_buffer(header)
+    got = z.ZSTD_decompress(out, header, frame, len(frame))
+    assert not z.ZSTD_isError(got)
+    assert header == z.ZSTD_compressBound(got)
+    return np.frombuffer(out.raw[:got], dtype=np.float64)
+
+
+def make(case):
+    mesh, cfg, prim, bprim, dt, _ = case
+    s = sdg.GpuSolver(mesh, cfg, device=0)
+    s.initialize_primitive(prim(s.volume_points()))
+    if bprim is not None:
+        pts, phys = s.boundary_points()
+        s.set_boundary_primitive(bprim(pts, np.repeat(phys, s.counts.face_point_count)))
+    return s, dt, mesh
+
+
+@pytest.mark.parametrize("name,case", [
+    ("euler-hybrid-p3", lambda: cases.kh_case(n=4, p=3, steps=1)),
+    ("ns-hex-p2-br1", lambda: cases.tgv_case(n=3, p=2, viscous=sdg.BR1, mu=0.02)),
+    ("ns-channel-walls-p2-br2", lambda: cases.channel_case(p=2, n=3, viscous=sdg.BR2, mu=0.01,
+                                                           conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW,
+                                                                       sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW))),
+])
+def test_raw_binary_layout(tmp_path, name, case):
+    s, dt, mesh = make(case())
+    s.stepSolver(dt, 2)
+    path = tmp_path / "state.zst"
+    s.writeRawBinary(path)
+    payload = decode(path)
+    c = s.counts
+    nv, d = c.conserved_variable_count, c.dimension
+    ns = s.config.equation == sdg.NAVIER_STOKES
+    modal = s.state_modal()
+    per = lambda nb: nv * nb * (1 + (d if ns else 0))
+    pos, moff, parents = 0, 0, []
+    for k in range(c.block_count):
+        nb, ne = c.block_basis_count[k], c.block_element_count[k]
+        for e in range(ne):
+            np.testing.assert_array_equal(payload[pos:pos + nv * nb], modal[moff + e * nv * nb: moff + (e + 1) * nv * nb])
+            pos += per(nb)
+        moff += ne * nv * nb
+    # boundary faces: one parent record each; then one zero per mesh node
+    nb_face = c.boundary_face_count
+    tail = payload[pos:]
+    assert len(tail) >= nb_face * per(min(c.block_basis_count[k] for k in range(c.block_count)))
+    assert np.all(payload[-len(mesh.nodes):] == 0.0)
+
+
+def test_raw_binary_last_step_restart(tmp_path):
+    s, dt, _ = make(cases.tgv_case(n=3, p=3, viscous=sdg.BR1, mu=0.02))
+    s.stepSolver(dt, 2)
+    u = s.state_point()
+    path = tmp_path / "last.zst"
+    s.writeRawBinary(path)
+    s.stepSolver(dt, 3)
+    s.read_raw_binary(path)
+    np.testing.assert_allclose(s.state_point(), u, rtol=1e-14, atol=1e-14 * np.abs(u).max())
+
+
+def test_raw_binary_specific_file_from_lower_order(tmp_path):
+    lo, dt, _ = make(cases.kh_case(n=4, p=2, split=0.0, jitter=0.0))
+    lo.stepSolver(dt, 1)
+    path = tmp_path / "p2.zst"
+    lo.writeRawBinary(path)
+    hi, _, _ = make(cases.kh_case(n=4, p=3, split=0.0, jitter=0.0))
+    hi.read_raw_binary(path, lower_order=True)
+    m_lo, m_hi = lo.state_modal().reshape(-1, 9 * 4), hi.state_modal().reshape(-1, 16 * 4)
+    # leading Nb(P-1) columns copied, the rest zero (InitialCondition.cpp:58-80)
+    np.testing.assert_allclose(m_hi[:, :36], m_lo, rtol=1e-13, atol=1e-13)
+    assert np.all(np.abs(m_hi[:, 36:]) < 1e-13)
