@@ -14,6 +14,8 @@ workloads of the metric, each measured the same way on this GPU:
   batched      256 independent 2D Euler / Navier-Stokes Kelvin-Helmholtz solves (500..50,000 elements,
                P1..P5, quads or hybrid, Mach 0.1..0.8, Re 1e2..1e4): one batched graph step of all
                instances against the same instances stepped one after another with plain launches
+  batched_small the same generator with element counts log-uniform in [500, 2,000] (the regime where one
+               instance cannot fill the GPU)
   ns_hybrid    2D Navier-Stokes BR2 Kelvin-Helmholtz, Re 1e4, 256^2 jittered quads with a 50% triangle
                split, P4, Lax-Friedrichs
   vortex2d     2D Euler isentropic vortex, 40^2 quads, P3, Roe, dt 1e-3 (L2-resident, launch bound)
@@ -57,7 +59,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="headline workload only")
-    ap.add_argument("--extra", default="batched,ns_hybrid,vortex2d,adjoint",
+    ap.add_argument("--extra", default="batched,batched_small,ns_hybrid,vortex2d,adjoint",
                     help="comma list of the other workloads to measure")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-max-elements", type=int, default=50000)
@@ -209,12 +211,12 @@ def _timed(torch, stream, fn, steps):
     return ev0.elapsed_time(ev1)
 
 
-def bench_batched(args, device, torch):
+def bench_batched(args, device, torch, max_elements=None):
     """Batched workload: all instances in one batched graph step versus one instance after another."""
     import subrosadg_gb300 as sdg
     from tests import cases
     t0 = time.perf_counter()
-    inst, params = cases.batch_instances(args.batch_count, max_elements=args.batch_max_elements)
+    inst, params = cases.batch_instances(args.batch_count, max_elements=max_elements or args.batch_max_elements)
     solvers = []
     for mesh, cfg, prim in inst:
         g = sdg.GpuSolver(mesh, cfg, device=device)
@@ -530,7 +532,8 @@ def run_ours(args):
     s.close()
     if not args.no_extra:
         extras = {"batched": bench_batched, "ns_hybrid": bench_ns_hybrid, "vortex2d": bench_vortex,
-                  "adjoint": bench_adjoint}
+                  "adjoint": bench_adjoint,
+                  "batched_small": lambda a, d, t: bench_batched(a, d, t, max_elements=2000)}
         for name in [x for x in args.extra.split(",") if x]:
             line[name] = extras[name](args, device, torch)
     print(json.dumps(line), flush=True)

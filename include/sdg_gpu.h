@@ -51,13 +51,20 @@ enum sdg_element_type { /* gmsh first-order type numbers (src/Solver/SimulationC
   SDG_ELEMENT_QUADRANGLE = 3,
   SDG_ELEMENT_HEXAHEDRON = 5
 };
-enum sdg_equation { SDG_COMPRESSIBLE_EULER = 0, SDG_COMPRESSIBLE_NS = 1 };           /* Enum.cpp:56-64   */
+enum sdg_equation {                                                                    /* Enum.cpp:56-64   */
+  SDG_COMPRESSIBLE_EULER = 0,
+  SDG_COMPRESSIBLE_NS = 1,
+  SDG_INCOMPRESSIBLE_EULER = 2, /* the weakly compressible fluid of EquationOfState WeakCompressibleFluid:  */
+  SDG_INCOMPRESSIBLE_NS = 3     /* conserved (rho, rho u, rho e), p = c0^2 (rho - rho0) + 0.01 rho0 c0^2     */
+};
 enum sdg_convective_flux {                                                            /* Enum.cpp:107-113 */
   SDG_FLUX_CENTRAL = 0,
   SDG_FLUX_LAX_FRIEDRICHS = 1,
   SDG_FLUX_HLLC = 2,
-  SDG_FLUX_ROE = 3
+  SDG_FLUX_ROE = 3,
+  SDG_FLUX_EXACT = 4          /* incompressible models only (ConvectiveFlux.cpp:352-414)                   */
 };
+enum sdg_source_term { SDG_SOURCE_NONE = 0, SDG_SOURCE_BOUSSINESQ = 1 };               /* Enum.cpp:71-74   */
 enum sdg_viscous_flux { SDG_VISCOUS_NONE = 0, SDG_VISCOUS_BR1 = 1, SDG_VISCOUS_BR2 = 2 }; /* Enum.cpp:115-119 */
 enum sdg_time_integration {                                                            /* Enum.cpp:136-140 */
   SDG_FORWARD_EULER = 0,
@@ -111,6 +118,14 @@ typedef struct sdg_config {
   double specific_heat_constant_volume;
   double dynamic_viscosity;           /* System::setTransportModel (SystemControl.cpp:98-103)       */
   double prandtl_number;              /* reference: constexpr 0.71 (PhysicalModel.cpp:91)           */
+  /* incompressible models (System::setEquationOfState, PhysicalModel.cpp:57-78); compressible ones use the
+     ideal gas with specific_heat_ratio and compressible fluxes (Central, LF, HLLC, Roe)                     */
+  double reference_sound_speed;       /* c0                                                             */
+  double reference_density;           /* rho0                                                           */
+  int32_t source_term;                /* sdg_source_term                                                */
+  double thermal_expansion_coefficient; /* Boussinesq beta (SourceTerm.cpp:35-38), gravity 1 along the last
+                                           coordinate (y in 2D, z in 3D)                                   */
+  double reference_temperature;       /* Boussinesq T_ref                                               */
 } sdg_config;
 
 /* ---- sizes of a created problem ------------------------------------------------------------- */

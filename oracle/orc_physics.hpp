@@ -6,6 +6,9 @@
 //   viscous fluxes      : src/Solver/ViscousFlux.cpp:25-170
 //   physical model      : src/Solver/PhysicalModel.cpp:26-165
 //   boundary conditions : src/Solver/BoundaryCondition.cpp:79-547
+//   incompressible model: PhysicalModel.cpp:57-78 (weakly compressible EOS), ConvectiveFlux.cpp:45-91,352-414
+//                         (rho e flux, Exact flux), VariableConvertor.cpp:310-337,598-612, ViscousFlux.cpp:84-101,
+//                         BoundaryCondition.cpp:153-180,243-270 (farfield star state), SourceTerm.cpp:29-58
 #pragma once
 #include <algorithm>
 #include <cmath>
@@ -18,10 +21,16 @@ struct Physics {
   int dim = 2;
   Real gamma = 1.4, cp = 0, cv = 0, mu = 0, pr = 0.71, kappa = 0;
   int transport = 1;  // 1 constant, 2 Sutherland
+  // incompressible model: last conserved variable rho e, p = c0^2 (rho - rho0) + 0.01 rho0 c0^2, sound speed c0
+  bool incomp = false;
+  Real c0 = 0, rho0 = 0, padd = 0;
+  // Boussinesq source rho beta (T - Tref) g on the last momentum component, g = 1
+  int source = 0;
+  Real beta = 0, tref = 0;
   Real temperatureFromInternalEnergy(Real e) const { return e / cv; }
   Real internalEnergyFromTemperature(Real t) const { return cv * t; }
-  Real pressure(Real rho, Real e) const { return (gamma - 1.0) * rho * e; }
-  Real soundSpeed(Real rho, Real p) const { return std::sqrt(gamma * p / rho); }
+  Real pressure(Real rho, Real e) const { return incomp ? c0 * c0 * (rho - rho0) + padd : (gamma - 1.0) * rho * e; }
+  Real soundSpeed(Real rho, Real p) const { return incomp ? c0 : std::sqrt(gamma * p / rho); }
   Real entropy(Real rho, Real p) const { return p / std::pow(rho, gamma); }
   Real sutherlandRatio(Real t) const {
     const Real s = Real(110.4) / Real(273.15);
@@ -42,14 +51,14 @@ inline void computationalFromConserved(const Physics& ph, PointVar& v) {
   const int d = ph.dim;
   v.rho = v.cons[0];
   for (int k = 0; k < d; ++k) v.u[k] = v.cons[1 + k] / v.rho;
-  v.e = v.cons[d + 1] / v.rho - v.u2(d) / 2.0;
+  v.e = ph.incomp ? v.cons[d + 1] / v.rho : v.cons[d + 1] / v.rho - v.u2(d) / 2.0;
   v.p = ph.pressure(v.rho, v.e);
 }
 inline void conservedFromComputational(const Physics& ph, PointVar& v) {
   const int d = ph.dim;
   v.cons[0] = v.rho;
   for (int k = 0; k < d; ++k) v.cons[1 + k] = v.rho * v.u[k];
-  v.cons[d + 1] = v.rho * (v.e + v.u2(d) / 2.0);
+  v.cons[d + 1] = ph.incomp ? v.rho * v.e : v.rho * (v.e + v.u2(d) / 2.0);
 }
 // primitive (rho, u, T) -> conserved and computational (VariableConvertor.cpp:341-380).
 inline void fromPrimitive(const Physics& ph, const Real* prim, PointVar& v) {
@@ -68,7 +77,7 @@ inline void normalFlux(const Physics& ph, const Real* n, const PointVar& v, Real
   f[0] = v.rho * un;
   for (int k = 0; k < d; ++k) f[1 + k] = v.rho * un * v.u[k] + v.p * n[k];
   const Real et = v.e + v.u2(d) / 2.0;
-  f[d + 1] = (v.rho * et + v.p) * un;
+  f[d + 1] = ph.incomp ? v.rho * v.e * un : (v.rho * et + v.p) * un;
 }
 
 // Raw convective flux F (d x nv, [k][var]) (ConvectiveFlux.cpp:27-57).
@@ -78,7 +87,7 @@ inline void rawFlux(const Physics& ph, const PointVar& v, Real f[3][kMaxVar]) {
   for (int k = 0; k < d; ++k) {
     f[k][0] = v.rho * v.u[k];
     for (int m = 0; m < d; ++m) f[k][1 + m] = v.rho * v.u[k] * v.u[m] + (k == m ? v.p : 0.0);
-    f[k][d + 1] = (v.rho * et + v.p) * v.u[k];
+    f[k][d + 1] = ph.incomp ? v.rho * v.e * v.u[k] : (v.rho * et + v.p) * v.u[k];
   }
 }
 
@@ -173,13 +182,43 @@ inline void roeFlux(const Physics& ph, const Real* n, const PointVar& l, const P
   for (int i = 0; i < nv; ++i) h[i] = ((fl[i] + fr[i]) - (col[0][i] + col[1][i] + col[2][i] + col[3][i])) / 2.0;
 }
 
+// Star state of the incompressible model between l and r across n (ConvectiveFlux.cpp:352-414; the
+// farfield condition uses the same state, BoundaryCondition.cpp:153-180,243-270): rho* from the two densities
+// and the normal-velocity jump, un* from their mean and the density ratio; e* and the tangential velocity come
+// from the upwind side (r when un* < 0), with rho* e* = rho_k e_k.
+inline void exactStarState(const Physics& ph, const Real* n, const PointVar& l, const PointVar& r, bool upwindRight,
+                           PointVar& s) {
+  const int d = ph.dim;
+  const Real c = ph.c0;
+  Real unl = 0, unr = 0; for (int k = 0; k < d; ++k) { unl += l.u[k] * n[k]; unr += r.u[k] * n[k]; }
+  s.rho = std::sqrt(l.rho * r.rho * std::exp((unl - unr) / c));
+  const Real uns = (unl + unr) / 2.0 + std::log(l.rho / r.rho) * c / 2.0;
+  const PointVar& k = upwindRight ? r : l;
+  const Real unk = upwindRight ? unr : unl;
+  s.e = k.e * k.rho / s.rho;
+  for (int j = 0; j < 3; ++j) s.u[j] = 0.0;
+  for (int j = 0; j < d; ++j) s.u[j] = k.u[j] + (uns - unk) * n[j];
+  s.p = ph.pressure(s.rho, s.e);
+}
+
+inline void exactFlux(const Physics& ph, const Real* n, const PointVar& l, const PointVar& r, Real* h) {
+  const int d = ph.dim;
+  const Real c = ph.c0;
+  Real unl = 0, unr = 0; for (int k = 0; k < d; ++k) { unl += l.u[k] * n[k]; unr += r.u[k] * n[k]; }
+  const Real uns = (unl + unr) / 2.0 + std::log(l.rho / r.rho) * c / 2.0;
+  PointVar s{};
+  exactStarState(ph, n, l, r, uns < 0.0, s);
+  normalFlux(ph, n, s, h);
+}
+
 inline void convectiveFlux(const Physics& ph, int kind, const Real* n, const PointVar& l, const PointVar& r,
                            Real* h) {
   switch (kind) {
     case 0: centralFlux(ph, n, l, r, h); break;
     case 1: laxFriedrichsFlux(ph, n, l, r, h); break;
     case 2: hllcFlux(ph, n, l, r, h); break;
-    default: roeFlux(ph, n, l, r, h); break;
+    case 3: roeFlux(ph, n, l, r, h); break;
+    default: exactFlux(ph, n, l, r, h); break;
   }
 }
 
@@ -194,10 +233,11 @@ inline void primitiveGradient(const Physics& ph, const PointVar& v, const Real* 
       gu[j][m] = (cg[(1 + m) * d + j] - drho[j] * v.u[m]) / v.rho;
       pg[(1 + m) * d + j] = gu[j][m];
     }
-  const Real et = v.cons[d + 1] / v.rho;
+  const Real et = v.cons[d + 1] / v.rho;  // total (compressible) or internal (incompressible) energy per mass
   for (int j = 0; j < d; ++j) {
     Real ge = (cg[(d + 1) * d + j] - drho[j] * et) / v.rho;
-    for (int m = 0; m < d; ++m) ge -= gu[j][m] * v.u[m];
+    if (!ph.incomp)
+      for (int m = 0; m < d; ++m) ge -= gu[j][m] * v.u[m];
     pg[(d + 1) * d + j] = ph.temperatureFromInternalEnergy(ge);
   }
 }
@@ -219,7 +259,8 @@ inline void viscousNormalFlux(const Physics& ph, const Real* n, const PointVar& 
   for (int k = 0; k < d; ++k) {
     raw[k][0] = 0.0;
     for (int m = 0; m < d; ++m) raw[k][1 + m] = tau[k][m];
-    Real tu = 0; for (int m = 0; m < d; ++m) tu += tau[k][m] * v.u[m];
+    Real tu = 0;
+    if (!ph.incomp) for (int m = 0; m < d; ++m) tu += tau[k][m] * v.u[m];  // incompressible: conduction only
     raw[k][d + 1] = tu + kap * pg[(d + 1) * d + k];
   }
   for (int i = 0; i < d + 2; ++i) { Real s = 0; for (int k = 0; k < d; ++k) s += raw[k][i] * n[k]; f[i] = s; }
@@ -237,6 +278,10 @@ inline void boundaryState(const Physics& ph, int bc, const Real* n, const PointV
   switch (bc) {
     case 0: {  // RiemannFarfield
       if (std::fabs(mn) > 1.0) { copyComp(mn < 0.0 ? ghost : l); break; }
+      if (ph.incomp) {  // the exact-flux star state, internal energy and tangential velocity from the upwind side
+        exactStarState(ph, n, l, ghost, mn < 0.0, b);
+        break;
+      }
       Real ung = 0; for (int k = 0; k < d; ++k) ung += ghost.u[k] * n[k];
       const Real rm = ung - 2.0 * ph.soundSpeed(ghost.rho, ghost.p) / (g - 1.0);
       const Real rp = unl + 2.0 * ph.soundSpeed(l.rho, l.p) / (g - 1.0);

@@ -14,6 +14,7 @@
 //   volume / face quadrature       src/Solver/SpatialDiscrete.cpp:194-322, 633-968
 //   residual assembly              src/Solver/SpatialDiscrete.cpp:1016-1068
 //   RK update, dt, relative error  src/Solver/TimeIntegration.cpp:45-324
+//   source term (Boussinesq)       src/Solver/SpatialDiscrete.cpp:254-262,1026-1029, SourceTerm.cpp:29-58
 // Periodic pairing uses a node map (master node per slave node) in place of gmsh's periodic entity
 // queries; the right rotation of a periodic face is taken from the parents' face vertex order, the
 // same rule as for ordinary interior faces.
@@ -49,6 +50,7 @@ struct Block {
   std::vector<Real> coef, last, res;
   std::vector<Real> qvol;     // ne * nv x (nq*d)
   std::vector<Real> qface;    // ne * nv x (nface*nfq)
+  std::vector<Real> qsrc;     // ne * nv x nq  source |J| w (Boussinesq only)
   // gradient blocks, rows (v*d + k)
   std::vector<Real> qvg, qfvg, qfig, rvg, rig, vgc, igc, gc;
 };
@@ -79,7 +81,7 @@ struct Problem {
   bool hasState = false;
   std::string err;
 
-  bool ns() const { return eq == 1; }
+  bool ns() const { return eq == 1 || eq == 3; }  // compressible or incompressible Navier-Stokes
   int nfq() const { return blocks[0].ref.nfq; }
 };
 
@@ -452,6 +454,11 @@ static void quadratureAndResidual(Problem& P) {
             Real s = 0; for (int a = 0; a < d; ++a) s += F[a][i] * M[a + bb * d];
             Q[size_t(q * d + bb) * nv + i] = s;
           }
+        if (P.ph.source) {  // rho beta (T - Tref) g on the last momentum component, times |J| w
+          Real* S = &B.qsrc[(size_t(e) * nq + q) * nv];
+          for (int i = 0; i < nv; ++i) S[i] = 0.0;
+          S[d] = v.rho * P.ph.beta * (P.ph.temperatureFromInternalEnergy(v.e) - P.ph.tref) * 1.0 * B.jw[size_t(e) * nq + q];
+        }
       }
     }
   }
@@ -528,6 +535,7 @@ static void quadratureAndResidual(Problem& P) {
       for (int i = 0; i < nv * nb; ++i) Rr[i] = 0;
       gemmAcc(nv, nq * d, nb, QV, B.ref.dphi.data(), Rr, 1);
       gemmAcc(nv, nfl, nb, QF, B.ref.phif.data(), Rr, -1);
+      if (P.ph.source) gemmAcc(nv, nq, nb, &B.qsrc[size_t(e) * nv * nq], B.ref.phi.data(), Rr, 1);
     }
   }
 }
@@ -644,6 +652,16 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
   P->ph.cv = c->specific_heat_constant_volume; P->ph.mu = c->dynamic_viscosity; P->ph.pr = c->prandtl_number;
   P->ph.transport = c->transport_model;
   P->ph.kappa = P->ph.cp * P->ph.mu / P->ph.pr;  // PhysicalModel.cpp:149-153
+  P->ph.incomp = c->equation == SDG_INCOMPRESSIBLE_EULER || c->equation == SDG_INCOMPRESSIBLE_NS;
+  if (P->ph.incomp) {  // PhysicalModel.cpp:57-78
+    P->ph.c0 = c->reference_sound_speed; P->ph.rho0 = c->reference_density;
+    P->ph.padd = 0.01 * P->ph.rho0 * P->ph.c0 * P->ph.c0;
+    if (P->flux == SDG_FLUX_HLLC || P->flux == SDG_FLUX_ROE) throw std::runtime_error("HLLC/Roe need the ideal gas");
+  } else if (P->flux == SDG_FLUX_EXACT) {
+    throw std::runtime_error("the Exact flux belongs to the incompressible models");
+  }
+  P->ph.source = c->source_term;
+  P->ph.beta = c->thermal_expansion_coefficient; P->ph.tref = c->reference_temperature;
   if (P->ns() && P->visc == 0) throw std::runtime_error("NS needs BR1 or BR2");
   struct Src { int type; int64_t n; const int32_t* v; };
   std::vector<Src> src;
@@ -664,6 +682,7 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
     B.coef.assign(size_t(B.ne) * nv * nb, 0.0); B.last = B.coef; B.res = B.coef;
     B.qvol.assign(size_t(B.ne) * nv * nq * d, 0.0);
     B.qface.assign(size_t(B.ne) * nv * nfl, 0.0);
+    if (P->ph.source) B.qsrc.assign(size_t(B.ne) * nv * nq, 0.0);
     if (P->ns() || P->faithful) {
       B.qvg.assign(size_t(B.ne) * nr * nq * d, 0.0);
       B.qfvg.assign(size_t(B.ne) * nr * nfl, 0.0);

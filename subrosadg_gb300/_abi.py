@@ -27,8 +27,9 @@ ERRORS = {
 globals().update({name: code for code, name in ERRORS.items()})
 
 TRIANGLE, QUADRANGLE, HEXAHEDRON = 2, 3, 5
-EULER, NAVIER_STOKES = 0, 1
-CENTRAL, LAX_FRIEDRICHS, HLLC, ROE = 0, 1, 2, 3
+EULER, NAVIER_STOKES, INCOMPRESSIBLE_EULER, INCOMPRESSIBLE_NAVIER_STOKES = 0, 1, 2, 3
+SOURCE_NONE, SOURCE_BOUSSINESQ = 0, 1
+CENTRAL, LAX_FRIEDRICHS, HLLC, ROE, EXACT = 0, 1, 2, 3, 4
 VISCOUS_NONE, BR1, BR2 = 0, 1, 2
 FORWARD_EULER, HEUN_RK2, SSPRK3 = 0, 1, 2
 TRANSPORT_NONE, TRANSPORT_CONSTANT, TRANSPORT_SUTHERLAND = 0, 1, 2
@@ -72,6 +73,11 @@ class SdgConfig(ctypes.Structure):
         ("specific_heat_constant_volume", c_double),
         ("dynamic_viscosity", c_double),
         ("prandtl_number", c_double),
+        ("reference_sound_speed", c_double),
+        ("reference_density", c_double),
+        ("source_term", c_int32),
+        ("thermal_expansion_coefficient", c_double),
+        ("reference_temperature", c_double),
     ]
 
 

@@ -106,6 +106,8 @@ AdjointState* adjoint(sdg_handle* h) {
       throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (quadrangles P>=2, hexahedra)");
   if (h->nBoundary > 0) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need a mesh without boundary faces (periodic)");
   if (h->ns && h->cfg.viscous_flux != SDG_VISCOUS_BR1) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of BR2 are not built");
+  if (h->ph.incomp || h->ph.source)
+    throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the incompressible models and source terms are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, A->k);
   adjointTileKernels(h->dim, h->blocks[0].n, h->ns, A->k);

@@ -25,6 +25,14 @@ struct Phys {
   double gamma, gm1, cv, inv_cv, cp, mu, kappa;
   int transport;  // 1 constant, 2 Sutherland
   double hllc_g2;  // (gamma + 1) / (2 gamma), the HLLC wave-speed factor
+  // the reference's incompressible model (IncompresibleEuler/NS with EquationOfState WeakCompressibleFluid,
+  // PhysicalModel.cpp:57-78): the last conserved variable is rho e (internal energy), p = c0^2 (rho - rho0) +
+  // 0.01 rho0 c0^2, the sound speed is c0
+  int incomp;
+  double c0, c02, rho0, padd;  // c0, c0^2, rho0, 0.01 rho0 c0^2
+  // Boussinesq buoyancy (SourceTerm.cpp:29-58): rho beta (T - Tref) g on the last momentum component, g = 1
+  int source;
+  double beta, tref;
 };
 
 // Reciprocal: rcp.approx.ftz.f64 estimate refined by two Newton-Raphson steps r <- r + r(1 - x r)
@@ -44,6 +52,13 @@ __device__ __forceinline__ double rcp(double x) {
   return r;
 }
 
+// Weakly compressible pressure c0^2 (rho - rho0) + padd, in the reference's association: rho - rho0 is exact
+// (Sterbenz) for rho within a factor 2 of rho0, so the c0^2 amplification acts on an exact difference.
+template <class T>
+__device__ __forceinline__ T weakPressure(const T& r, const Phys& ph) {
+  return fmaT(ph.c02, r - ph.rho0, ph.padd);
+}
+
 template <int D, class T = double>
 struct State {
   T r, m[D], E;   // conserved
@@ -60,7 +75,28 @@ __device__ __forceinline__ void makeState(State<D, T>& s, const T* U, const Phys
   T mu = T(0.0);
 #pragma unroll
   for (int k = 0; k < D; ++k) { s.u[k] = s.m[k] * s.ir; mu = fmaT(s.m[k], s.u[k], mu); }
-  s.p = ph.gm1 * fmaT(-0.5, mu, s.E);
+  s.p = ph.incomp ? weakPressure(s.r, ph) : ph.gm1 * fmaT(-0.5, mu, s.E);
+}
+
+// E + p of the compressible energy flux (E u + p u); the incompressible model transports rho e (no p u).
+template <int D, class T>
+__device__ __forceinline__ T energyFluxFactor(const State<D, T>& s, const Phys& ph) {
+  return ph.incomp ? s.E : s.E + s.p;
+}
+
+// Temperature e / cv: compressible e = E/rho - |u|^2/2, incompressible e = (rho e)/rho.
+template <int D, class T>
+__device__ __forceinline__ T temperatureOf(const State<D, T>& s, const Phys& ph) {
+  if (ph.incomp) return s.E * s.ir * ph.inv_cv;
+  T u2 = T(0.0);
+#pragma unroll
+  for (int k = 0; k < D; ++k) u2 = fmaT(s.u[k], s.u[k], u2);
+  return fmaT(-0.5, u2, s.E * s.ir) * ph.inv_cv;
+}
+
+template <int D, class T>
+__device__ __forceinline__ T soundSpeed(const State<D, T>& s, const Phys& ph) {
+  return ph.incomp ? T(ph.c0) : sqrtT(ph.gamma * s.p * s.ir);
 }
 
 template <int D, class T>
@@ -72,18 +108,19 @@ __device__ __forceinline__ T dotn(const T* a, const double* n) {
 }
 
 template <int D, class T>
-__device__ __forceinline__ void normalFlux(const State<D, T>& s, const double* n, T un, T* f) {
+__device__ __forceinline__ void normalFlux(const State<D, T>& s, const double* n, T un, T* f, const Phys& ph) {
   f[0] = s.r * un;
 #pragma unroll
   for (int k = 0; k < D; ++k) f[1 + k] = fmaT(s.m[k], un, s.p * n[k]);
-  f[D + 1] = (s.E + s.p) * un;
+  f[D + 1] = energyFluxFactor(s, ph) * un;
 }
 
 template <int D, class T>
-__device__ __forceinline__ void fluxCentral(const State<D, T>& l, const State<D, T>& r, const double* n, T* h) {
+__device__ __forceinline__ void fluxCentral(const State<D, T>& l, const State<D, T>& r, const double* n,
+                                            const Phys& ph, T* h) {
   T fl[D + 2], fr[D + 2];
-  normalFlux(l, n, dotn<D>(l.u, n), fl);
-  normalFlux(r, n, dotn<D>(r.u, n), fr);
+  normalFlux(l, n, dotn<D>(l.u, n), fl, ph);
+  normalFlux(r, n, dotn<D>(r.u, n), fr, ph);
 #pragma unroll
   for (int i = 0; i < D + 2; ++i) h[i] = 0.5 * (fl[i] + fr[i]);
 }
@@ -93,9 +130,9 @@ __device__ __forceinline__ void fluxLaxFriedrichs(const State<D, T>& l, const St
                                                   const Phys& ph, T* h) {
   const T unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
   T fl[D + 2], fr[D + 2];
-  normalFlux(l, n, unl, fl);
-  normalFlux(r, n, unr, fr);
-  const T cl = sqrtT(ph.gamma * l.p * l.ir), cr = sqrtT(ph.gamma * r.p * r.ir);
+  normalFlux(l, n, unl, fl, ph);
+  normalFlux(r, n, unr, fr, ph);
+  const T cl = soundSpeed(l, ph), cr = soundSpeed(r, ph);
   const T sr = fmaxT(fabsT(unl) + cl, fabsT(unr) + cr);
   h[0] = 0.5 * fmaT(-sr, r.r - l.r, fl[0] + fr[0]);
 #pragma unroll
@@ -114,17 +151,17 @@ __device__ __forceinline__ void fluxHLLC(const State<D, T>& l, const State<D, T>
   const double g2 = ph.hllc_g2;
   const T ql = ps <= l.p ? T(1.0) : sqrtT(fmaT(g2, fmaT(ps, rcpT(l.p), -1.0), 1.0));
   const T sl = fmaT(-cl, ql, unl);
-  if (sl >= 0.0) { normalFlux(l, n, unl, h); return; }
+  if (sl >= 0.0) { normalFlux(l, n, unl, h, ph); return; }
   const T qr = ps <= r.p ? T(1.0) : sqrtT(fmaT(g2, fmaT(ps, rcpT(r.p), -1.0), 1.0));
   const T sr = fmaT(cr, qr, unr);
-  if (sr <= 0.0) { normalFlux(r, n, unr, h); return; }
+  if (sr <= 0.0) { normalFlux(r, n, unr, h, ph); return; }
   const T al = l.r * (sl - unl), ar = r.r * (sr - unr);
   const T ss = (r.p - l.p + al * unl - ar * unr) * rcpT(al - ar);
   const bool left = ss >= 0.0;
   const State<D, T>& s = left ? l : r;
   const T sk = left ? sl : sr, un = left ? unl : unr, a = left ? al : ar;
   T f[D + 2];
-  normalFlux(s, n, un, f);
+  normalFlux(s, n, un, f, ph);
   const T inv = rcpT(sk - ss);
   // star state minus the side's conserved state, times the wave speed
   const T rs = a * inv;
@@ -146,8 +183,8 @@ __device__ __forceinline__ void fluxRoe(const State<D, T>& l, const State<D, T>&
   const double g = ph.gamma;
   const T unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
   T fl[D + 2], fr[D + 2];
-  normalFlux(l, n, unl, fl);
-  normalFlux(r, n, unr, fr);
+  normalFlux(l, n, unl, fl, ph);
+  normalFlux(r, n, unr, fr, ph);
   const T sl = sqrtT(l.r), sr = sqrtT(r.r);
   const T is = rcpT(sl + sr);
   const T wl = sl * is, wr = sr * is;
@@ -184,13 +221,41 @@ __device__ __forceinline__ void fluxRoe(const State<D, T>& l, const State<D, T>&
   h[D + 1] = 0.5 * (fl[D + 1] + fr[D + 1] - fmaT(ht, s14, fmaT(d14, un, fmaT(0.5 * u2, s2, s3 * fmaT(-un, dun, udu)))));
 }
 
+// Exact flux of the incompressible model (ConvectiveFlux.cpp:352-414): the star state of the two
+// characteristic relations with constant sound speed c0,
+//   rho* = sqrt(rhoL rhoR exp((unL - unR)/c0)),  un* = (unL + unR)/2 + c0 ln(rhoL/rhoR)/2,
+// upwind internal energy (rho e conserved across: e* = e_k rho_k / rho*) and tangential velocity, p* from the
+// equation of state; the flux is the normal flux of the star state.
+template <int D, class T>
+__device__ __forceinline__ void fluxExact(const State<D, T>& l, const State<D, T>& r, const double* n, const Phys& ph,
+                                          T* h) {
+  const double c0 = ph.c0;
+  const T unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
+  const T rs = sqrtT(l.r * r.r * expT((unl - unr) * (1.0 / c0)));
+  const T uns = fmaT(logT(l.r * r.ir), 0.5 * c0, 0.5 * (unl + unr));
+  const bool right = uns < 0.0;
+  const State<D, T>& k = right ? r : l;
+  const T unk = right ? unr : unl;
+  const T irs = rcpT(rs);
+  const T res = k.E * irs;  // rho* e* = rho_k e_k: conserved internal energy density of the upwind side
+  T us[D];
+#pragma unroll
+  for (int j = 0; j < D; ++j) us[j] = fmaT(uns - unk, n[j], k.u[j]);
+  const T ps = weakPressure(rs, ph);
+  h[0] = rs * uns;
+#pragma unroll
+  for (int j = 0; j < D; ++j) h[1 + j] = fmaT(rs * uns, us[j], ps * n[j]);
+  h[D + 1] = rs * res * uns;
+}
+
 template <int D, int FLUX, class T>
 __device__ __forceinline__ void convectiveFlux(const State<D, T>& l, const State<D, T>& r, const double* n,
                                                const Phys& ph, T* h) {
-  if constexpr (FLUX == 0) fluxCentral<D>(l, r, n, h);
+  if constexpr (FLUX == 0) fluxCentral<D>(l, r, n, ph, h);
   else if constexpr (FLUX == 1) fluxLaxFriedrichs<D>(l, r, n, ph, h);
   else if constexpr (FLUX == 2) fluxHLLC<D>(l, r, n, ph, h);
-  else fluxRoe<D>(l, r, n, ph, h);
+  else if constexpr (FLUX == 3) fluxRoe<D>(l, r, n, ph, h);
+  else fluxExact<D>(l, r, n, ph, h);
 }
 
 // Computational variables (rho, u, e, p) used by the boundary states.
@@ -200,19 +265,30 @@ struct Comp {
 };
 
 template <int D>
-__device__ __forceinline__ void compFromState(const State<D>& s, Comp<D>& c) {
+__device__ __forceinline__ void compFromState(const State<D>& s, Comp<D>& c, const Phys& ph) {
   c.r = s.r;
 #pragma unroll
   for (int k = 0; k < D; ++k) c.u[k] = s.u[k];
   c.p = s.p;
+  if (ph.incomp) { c.e = s.E * s.ir; return; }
   double u2 = 0.0;
 #pragma unroll
   for (int k = 0; k < D; ++k) u2 = fma(s.u[k], s.u[k], u2);
   c.e = fma(-0.5, u2, s.E * s.ir);
 }
 
+// The last conserved variable of a computational state: rho E (compressible) or rho e (incompressible).
 template <int D>
-__device__ __forceinline__ void normalFluxComp(const Comp<D>& c, const double* n, double* f) {
+__device__ __forceinline__ double energyOfComp(const Comp<D>& c, const Phys& ph) {
+  if (ph.incomp) return c.r * c.e;
+  double u2 = 0.0;
+#pragma unroll
+  for (int k = 0; k < D; ++k) u2 += c.u[k] * c.u[k];
+  return c.r * (c.e + 0.5 * u2);
+}
+
+template <int D>
+__device__ __forceinline__ void normalFluxComp(const Comp<D>& c, const double* n, double* f, const Phys& ph) {
   const double un = dotn<D>(c.u, n);
   double u2 = 0.0;
 #pragma unroll
@@ -220,7 +296,7 @@ __device__ __forceinline__ void normalFluxComp(const Comp<D>& c, const double* n
   f[0] = c.r * un;
 #pragma unroll
   for (int k = 0; k < D; ++k) f[1 + k] = fma(c.r * un, c.u[k], c.p * n[k]);
-  f[D + 1] = fma(c.r, fma(0.5, u2, c.e), c.p) * un;
+  f[D + 1] = ph.incomp ? c.r * c.e * un : fma(c.r, fma(0.5, u2, c.e), c.p) * un;
 }
 
 // Boundary state (BoundaryCondition.cpp:79-547): l = interior trace, g = ghost (user) state.
@@ -229,9 +305,23 @@ __device__ __forceinline__ void boundaryState(int bc, const double* n, const Com
                                               const Phys& ph, Comp<D>& b) {
   const double gam = ph.gamma;
   const double unl = dotn<D>(l.u, n);
-  const double mn = unl / sqrt(gam * l.p / l.r);
+  const double mn = unl / (ph.incomp ? ph.c0 : sqrt(gam * l.p / l.r));
   if (bc == 0) {  // Riemann farfield
     if (fabs(mn) > 1.0) { b = mn < 0.0 ? g : l; return; }
+    if (ph.incomp) {
+      // the exact-flux star state between the interior and the ghost (BoundaryCondition.cpp:153-180,243-270)
+      const double c0 = ph.c0, ung = dotn<D>(g.u, n);
+      const double rb = sqrt(l.r * g.r * exp((unl - ung) / c0));
+      const double unb = (unl + ung) / 2.0 + log(l.r / g.r) * c0 / 2.0;
+      const Comp<D>& s = mn < 0.0 ? g : l;
+      const double uns = mn < 0.0 ? ung : unl;
+      b.r = rb;
+      b.e = s.e * s.r / rb;
+#pragma unroll
+      for (int k = 0; k < D; ++k) b.u[k] = s.u[k] + (unb - uns) * n[k];
+      b.p = weakPressure(rb, ph);
+      return;
+    }
     const double ung = dotn<D>(g.u, n);
     const double rm = ung - 2.0 * sqrt(gam * g.p / g.r) / (gam - 1.0);
     const double rp = unl + 2.0 * sqrt(gam * l.p / l.r) / (gam - 1.0);
@@ -256,7 +346,7 @@ __device__ __forceinline__ void boundaryState(int bc, const double* n, const Com
 #pragma unroll
     for (int k = 0; k < D; ++k) b.u[k] = g.u[k];
     b.e = g.e;
-    b.p = ph.gm1 * b.r * g.e;
+    b.p = ph.incomp ? weakPressure(b.r, ph) : ph.gm1 * b.r * g.e;
   } else if (bc == 4) {  // adiabatic slip wall
     b = l;
 #pragma unroll
@@ -278,6 +368,8 @@ struct PrimGrad {
   T gT[D];
 };
 
+// Et = E/rho: total energy per mass (compressible) or internal energy per mass (incompressible, whose
+// internal-energy gradient has no -grad(u).u term, VariableConvertor.cpp:598-610).
 template <int D, class T>
 __device__ __forceinline__ void primitiveGradient(const T* g, const T* u, T ir, T Et, const Phys& ph,
                                                   PrimGrad<D, T>& pg) {
@@ -289,7 +381,7 @@ __device__ __forceinline__ void primitiveGradient(const T* g, const T* u, T ir, 
     for (int m = 0; m < D; ++m) {
       const T gum = fmaT(-dr, u[m], g[(1 + m) * D + k]) * ir;
       pg.gu[k][m] = gum;
-      ge = fmaT(-gum, u[m], ge);
+      if (!ph.incomp) ge = fmaT(-gum, u[m], ge);
     }
     pg.gT[k] = ge * ph.inv_cv;
   }
@@ -327,8 +419,10 @@ __device__ __forceinline__ void viscousTensor(const PrimGrad<D, T>& pg, const T*
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     T s = kappa * pg.gT[k];
+    if (!ph.incomp) {  // incompressible: the internal-energy flux is conduction only (ViscousFlux.cpp:84-101)
 #pragma unroll
-    for (int m = 0; m < D; ++m) s = fmaT(tau[k][m], u[m], s);
+      for (int m = 0; m < D; ++m) s = fmaT(tau[k][m], u[m], s);
+    }
     q[k] = s;
   }
 }

@@ -164,6 +164,22 @@ template <int K> __device__ __forceinline__ Dual<K> sqrtT(const Dual<K>& x) {
   for (int k = 0; k < K; ++k) o.d[k] = h * x.d[k];
   return o;
 }
+__device__ __forceinline__ double expT(double x) { return exp(x); }
+template <int K> __device__ __forceinline__ Dual<K> expT(const Dual<K>& x) {
+  const double e = exp(x.v);
+  Dual<K> o; o.v = e;
+#pragma unroll
+  for (int k = 0; k < K; ++k) o.d[k] = e * x.d[k];
+  return o;
+}
+__device__ __forceinline__ double logT(double x) { return log(x); }
+template <int K> __device__ __forceinline__ Dual<K> logT(const Dual<K>& x) {
+  const double ix = 1.0 / x.v;
+  Dual<K> o; o.v = log(x.v);
+#pragma unroll
+  for (int k = 0; k < K; ++k) o.d[k] = ix * x.d[k];
+  return o;
+}
 __device__ __forceinline__ double fabsT(double x) { return fabs(x); }
 template <int K> __device__ __forceinline__ Dual<K> fabsT(const Dual<K>& x) { return x.v < 0.0 ? -x : x; }
 __device__ __forceinline__ double fmaxT(double a, double b) { return fmax(a, b); }

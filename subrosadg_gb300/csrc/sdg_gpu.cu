@@ -58,7 +58,10 @@ void facePointInParent(int type, int f, const double* fx, double* X) {
 
 // ---- point-layout conversions ----------------------------------------------------------------------
 // state[e][v][b] (padded stride) <- points[e][q][v]; proj = null for tensor blocks (nodes are points),
-// else the least-squares projection [nb][nq].
+// else the least-squares projection [nb][nq] followed by its row sums [nb].  The projection is applied to
+// u - u_0 (u_0 = the element's first point value) and u_0 added back through the row sums: for nearly uniform
+// fields (the weakly compressible density, whose c0^2 amplification reaches the pressure) the rounding then
+// scales with the variation of u, not with u.
 __global__ void pointToStateKernel(const double* __restrict__ pts, double* __restrict__ st,
                                    const double* __restrict__ proj, int64_t ne, int nb, int nq, int nv, int ustride) {
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -68,7 +71,12 @@ __global__ void pointToStateKernel(const double* __restrict__ pts, double* __res
   for (int v = 0; v < nv; ++v) {
     double s;
     if (!proj) s = pts[(e * nq + b) * nv + v];
-    else { s = 0.0; for (int q = 0; q < nq; ++q) s = fma(proj[b * nq + q], pts[(e * nq + q) * nv + v], s); }
+    else {
+      const double u0 = pts[(e * nq) * nv + v];
+      s = 0.0;
+      for (int q = 0; q < nq; ++q) s = fma(proj[b * nq + q], pts[(e * nq + q) * nv + v] - u0, s);
+      s = fma(proj[nb * nq + b], u0, s);
+    }
     st[e * ustride + v * nb + b] = s;
   }
 }
@@ -95,7 +103,8 @@ __global__ void primitiveToConservedKernel(double* __restrict__ pts, int64_t n, 
   const double rho = p[0];
   double u2 = 0.0;
   for (int k = 0; k < dim; ++k) { u2 += p[1 + k] * p[1 + k]; p[1 + k] *= rho; }
-  p[dim + 1] = rho * (ph.cv * p[dim + 1] + u2 / 2.0);
+  // incompressible: rho e with e = cv T (VariableConvertor.cpp:354-362)
+  p[dim + 1] = ph.incomp ? rho * (ph.cv * p[dim + 1]) : rho * (ph.cv * p[dim + 1] + u2 / 2.0);
 }
 
 // dt = min CFL*minEdge/((|u|+c)(P+1)^2) over points (TimeIntegration.cpp:104-131); per-CTA minima.
@@ -111,7 +120,7 @@ __global__ void deltaTimeKernel(const double* __restrict__ pts, const double* __
     for (int k = 0; k < dim; ++k) { const double u = p[1 + k] / rho; u2 += u * u; }
     const double e = p[dim + 1] / rho - u2 / 2.0;
     const double pr = ph.gm1 * rho * e;
-    const double c = sqrt(ph.gamma * pr / rho);
+    const double c = ph.incomp ? ph.c0 : sqrt(ph.gamma * pr / rho);
     dt = cfl * minEdge[t / nq] / ((sqrt(u2) + c) * p1sq);
   }
   sh[threadIdx.x] = dt;
@@ -699,12 +708,22 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     const sdg_config& c = *config;
     if (mesh->dimension != 2 && mesh->dimension != 3) throw Failure(SDG_ERR_INVALID_ARGUMENT, "dimension must be 2 or 3");
     if (c.polynomial_order < 1 || c.polynomial_order > 5) throw Failure(SDG_ERR_INVALID_ARGUMENT, "polynomial order must be 1..5");
-    if (c.equation != SDG_COMPRESSIBLE_EULER && c.equation != SDG_COMPRESSIBLE_NS) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad equation");
-    if (c.convective_flux < 0 || c.convective_flux > 3) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad convective flux");
+    if (c.equation < SDG_COMPRESSIBLE_EULER || c.equation > SDG_INCOMPRESSIBLE_NS) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad equation");
+    const bool incomp = c.equation == SDG_INCOMPRESSIBLE_EULER || c.equation == SDG_INCOMPRESSIBLE_NS;
+    const bool viscous = c.equation == SDG_COMPRESSIBLE_NS || c.equation == SDG_INCOMPRESSIBLE_NS;
+    if (c.convective_flux < 0 || c.convective_flux > 4) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad convective flux");
+    if (incomp && (c.convective_flux == SDG_FLUX_HLLC || c.convective_flux == SDG_FLUX_ROE))
+      throw Failure(SDG_ERR_INVALID_ARGUMENT, "HLLC and Roe need the ideal gas (incompressible models: Central, LF, Exact)");
+    if (!incomp && c.convective_flux == SDG_FLUX_EXACT)
+      throw Failure(SDG_ERR_INVALID_ARGUMENT, "the Exact flux belongs to the incompressible models");
+    if (incomp && (!(c.reference_sound_speed > 0) || !(c.reference_density > 0)))
+      throw Failure(SDG_ERR_INVALID_ARGUMENT, "incompressible models need reference_sound_speed and reference_density > 0");
+    if (c.source_term != SDG_SOURCE_NONE && c.source_term != SDG_SOURCE_BOUSSINESQ)
+      throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad source term");
     if (c.time_integration < 0 || c.time_integration > 2) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad time integration");
     if (!(c.specific_heat_ratio > 1.0) || !(c.specific_heat_constant_volume > 0) || !(c.specific_heat_constant_pressure > 0))
       throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad thermodynamic constants");
-    if (c.equation == SDG_COMPRESSIBLE_NS) {
+    if (viscous) {
       if (c.viscous_flux != SDG_VISCOUS_BR1 && c.viscous_flux != SDG_VISCOUS_BR2)
         throw Failure(SDG_ERR_INVALID_ARGUMENT, "Navier-Stokes needs BR1 or BR2");
       if (!(c.dynamic_viscosity >= 0) || !(c.prandtl_number > 0)) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad transport constants");
@@ -721,6 +740,15 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     h->ph.kappa = c.prandtl_number > 0 ? c.specific_heat_constant_pressure * c.dynamic_viscosity / c.prandtl_number : 0.0;
     h->ph.transport = c.transport_model;
     h->ph.hllc_g2 = (c.specific_heat_ratio + 1.0) / (2.0 * c.specific_heat_ratio);
+    h->ph.incomp = incomp ? 1 : 0;
+    h->ph.c0 = incomp ? c.reference_sound_speed : 0.0;
+    h->ph.c02 = h->ph.c0 * h->ph.c0;
+    // p = c0^2 (rho - rho0) + 0.01 rho0 c0^2 (calculatePressureAdditionFromSoundSpeedDensity)
+    h->ph.rho0 = incomp ? c.reference_density : 0.0;
+    h->ph.padd = incomp ? 0.01 * c.reference_density * c.reference_sound_speed * c.reference_sound_speed : 0.0;
+    h->ph.source = c.source_term;
+    h->ph.beta = c.thermal_expansion_coefficient;
+    h->ph.tref = c.reference_temperature;
     // element blocks, in the reference's loop order
     std::vector<Block> mb;
     if (h->dim == 2) {
@@ -1076,7 +1104,8 @@ int sdg_set_boundary_primitive(sdg_handle* h, const double* primitive) {
     o[0] = pr[0];
     for (int k = 0; k < d; ++k) o[1 + k] = pr[1 + k];
     o[d + 1] = e;
-    o[d + 2] = h->ph.gm1 * pr[0] * e;  // calculateComputationalFromPrimitive (VariableConvertor.cpp:368-380)
+    // calculateComputationalFromPrimitive (VariableConvertor.cpp:368-380): the equation of state
+    o[d + 2] = h->ph.incomp ? std::fma(h->ph.c02, pr[0] - h->ph.rho0, h->ph.padd) : h->ph.gm1 * pr[0] * e;
   }
   SDG_CUDA(cudaSetDevice(h->device));
   if (np > 0) SDG_CUDA(cudaMemcpyAsync(h->ghost, g.data(), g.size() * 8, cudaMemcpyHostToDevice, h->stream));

@@ -46,7 +46,7 @@ struct DevBlock {
   std::vector<double> geomHost;
   std::vector<double> tablesHost;
   std::vector<double> phi;         // dense: [q][nb] ; tensor: unused
-  std::vector<double> lsq;         // dense: [nb][q] projection (Phi^T Phi)^-1 Phi^T
+  std::vector<double> lsq;         // dense: [nb][q] projection (Phi^T Phi)^-1 Phi^T, then its [nb] row sums
   TensorOps ops;
   double* geom = nullptr;
   double* tables = nullptr;

@@ -207,7 +207,7 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
       for (int v = 0; v < NV; ++v) U[v] = sU[le * S::USTRIDE + v * NB + node];
       State<DIM> s;
       makeState<DIM>(s, U, ph);
-      const double ep = s.E + s.p;
+      const double ep = energyFluxFactor(s, ph);
       double tau[DIM][DIM], q[DIM];
       if constexpr (VISC) {
         // viscous flux from the total gradient at the node (ViscousFlux.cpp:58-103)
@@ -219,7 +219,8 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
         double u2 = 0.0;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) u2 = fma(s.u[k], s.u[k], u2);
-        viscousTensor<DIM>(pg, s.u, fma(-0.5, u2, s.E * s.ir) * ph.inv_cv, ph, tau, q);
+        viscousTensor<DIM>(pg, s.u, ph.incomp ? s.E * s.ir * ph.inv_cv : fma(-0.5, u2, s.E * s.ir) * ph.inv_cv, ph,
+                           tau, q);
       }
 #pragma unroll
       for (int b = 0; b < DIM; ++b) {
@@ -269,6 +270,16 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
           acc = fma(-lp, Fp[v * NFQ], acc);
           du[v] = acc;
         }
+      }
+      // Boussinesq buoyancy on the last momentum component (SourceTerm.cpp:29-58): the nodal source S_i
+      // enters as S_i |J|_i (it is divided by w_i |J|_i with the rest of the residual)
+      if (ph.source) {
+        double U[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) U[v] = sU[le * S::USTRIDE + v * NB + node];
+        State<DIM> s;
+        makeState<DIM>(s, U, ph);
+        du[DIM] = fma(s.r * ph.beta * (temperatureOf(s, ph) - ph.tref), 1.0 / jinv, du[DIM]);
       }
       // 4. RK combination (M^-1 is diagonal: 1/(w_i |J|_i); the weights cancelled into dhat/lift)
       const double sc = a.c2dt * jinv;
@@ -494,7 +505,7 @@ __device__ __forceinline__ void faceBoundaryPoint(const FaceArgs& a, int64_t t) 
   State<DIM> s;
   makeState<DIM>(s, ul, a.ph);
   Comp<DIM> l, g, b;
-  compFromState<DIM>(s, l);
+  compFromState<DIM>(s, l, a.ph);
   const double* gp = a.ghost + (f * nfq + j) * (DIM + 3);
   g.r = gp[0];
 #pragma unroll
@@ -503,7 +514,7 @@ __device__ __forceinline__ void faceBoundaryPoint(const FaceArgs& a, int64_t t) 
   g.p = gp[DIM + 2];
   boundaryState<DIM>(bc, n, l, g, a.ph, b);
   double h[NV];
-  normalFluxComp<DIM>(b, n, h);
+  normalFluxComp<DIM>(b, n, h, a.ph);
 #pragma unroll
   for (int v = 0; v < NV; ++v) L[v * nfq] = h[v] * area;
 }

@@ -30,7 +30,7 @@ __device__ __forceinline__ void nodeFlux(const T* U, const T* g, const double ja
   constexpr int NV = DIM + 2;
   State<DIM, T> s;
   makeState<DIM>(s, U, ph);
-  const T ep = s.E + s.p;
+  const T ep = energyFluxFactor(s, ph);
   T tau[DIM][DIM], q[DIM];
   if constexpr (VISC) {
     PrimGrad<DIM, T> pg;
@@ -38,7 +38,7 @@ __device__ __forceinline__ void nodeFlux(const T* U, const T* g, const double ja
     T u2 = T(0.0);
 #pragma unroll
     for (int k = 0; k < DIM; ++k) u2 = fmaT(s.u[k], s.u[k], u2);
-    viscousTensor<DIM>(pg, s.u, fmaT(-0.5, u2, s.E * s.ir) * ph.inv_cv, ph, tau, q);
+    viscousTensor<DIM>(pg, s.u, temperatureOf(s, ph), ph, tau, q);
   }
 #pragma unroll
   for (int b = 0; b < DIM; ++b) {
@@ -89,7 +89,7 @@ __device__ __forceinline__ void faceFluxPoint(const T* ul, const T* ur, const T*
       T u2 = T(0.0);
 #pragma unroll
       for (int k = 0; k < DIM; ++k) u2 = fmaT(l.u[k], l.u[k], u2);
-      viscousNormalFlux<DIM>(pg, l.u, fmaT(-0.5, u2, l.E * l.ir) * ph.inv_cv, n, ph, fl);
+      viscousNormalFlux<DIM>(pg, l.u, temperatureOf(l, ph), n, ph, fl);
     }
     {
       PrimGrad<DIM, T> pg;
@@ -97,7 +97,7 @@ __device__ __forceinline__ void faceFluxPoint(const T* ul, const T* ur, const T*
       T u2 = T(0.0);
 #pragma unroll
       for (int k = 0; k < DIM; ++k) u2 = fmaT(r.u[k], r.u[k], u2);
-      viscousNormalFlux<DIM>(pg, r.u, fmaT(-0.5, u2, r.E * r.ir) * ph.inv_cv, n, ph, fr);
+      viscousNormalFlux<DIM>(pg, r.u, temperatureOf(r, ph), n, ph, fr);
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) {

@@ -24,24 +24,29 @@ namespace sdg {
 //                         dmod[2][NB][NB]  D_b = M_ref^-1 S_b, S_b(k,m) = sum_q w_q dphi_k/dxi_b phi_m
 //                         emod[NF][NB][NFQ] E_f = M_ref^-1 Phi_f^T W_f (lift of face f's point values)
 //                         lmod[NF][NFQ][NFQ] L_f = Phi_f E_f (trace at face f of the lift from face f)
+//   source weights:        phiw[NQ][NB] w_q phi (volume source terms)
 inline size_t denseTableSize(int nb, int nq, int nfp) { return size_t(nq) * nb * 3 + size_t(nfp) * nb * 2 + size_t(nb) * nb; }
 inline size_t denseGradOperatorSize(int nb, int nf, int nfq) {
   return size_t(2) * nb * nb + size_t(nf) * nb * nfq + size_t(nf) * nfq * nfq;
 }
+inline size_t denseSourceTableOffset(int nb, int nq, int nfp, int nf, int nfq) {
+  return denseTableSize(nb, nq, nfp) + denseGradOperatorSize(nb, nf, nfq);
+}
 
-inline void invertDense(int n, std::vector<double> a, std::vector<double>& inv) {
-  inv.assign(size_t(n) * n, 0.0);
-  for (int i = 0; i < n; ++i) inv[size_t(i) * n + i] = 1.0;
+template <class R>
+inline void invertDense(int n, std::vector<R> a, std::vector<R>& inv) {
+  inv.assign(size_t(n) * n, R(0));
+  for (int i = 0; i < n; ++i) inv[size_t(i) * n + i] = R(1);
   for (int c = 0; c < n; ++c) {
     int piv = c;
     for (int r = c + 1; r < n; ++r) if (std::fabs(a[size_t(r) * n + c]) > std::fabs(a[size_t(piv) * n + c])) piv = r;
     for (int k = 0; k < n; ++k) { std::swap(a[size_t(c) * n + k], a[size_t(piv) * n + k]); std::swap(inv[size_t(c) * n + k], inv[size_t(piv) * n + k]); }
-    const double d = 1.0 / a[size_t(c) * n + c];
+    const R d = R(1) / a[size_t(c) * n + c];
     for (int k = 0; k < n; ++k) { a[size_t(c) * n + k] *= d; inv[size_t(c) * n + k] *= d; }
     for (int r = 0; r < n; ++r) {
       if (r == c) continue;
-      const double f = a[size_t(r) * n + c];
-      if (f == 0.0) continue;
+      const R f = a[size_t(r) * n + c];
+      if (f == R(0)) continue;
       for (int k = 0; k < n; ++k) { a[size_t(r) * n + k] -= f * a[size_t(c) * n + k]; inv[size_t(r) * n + k] -= f * inv[size_t(c) * n + k]; }
     }
   }
@@ -54,7 +59,7 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
   const int nb = modalCount(type, p);
   const PointRule vr = volumeRule(type, p), fr = faceRule(type, p);
   const int nq = vr.n, nf = typeFaces(type), nfq = fr.n, nfp = nf * nfq;
-  tables.assign(denseTableSize(nb, nq, nfp) + denseGradOperatorSize(nb, nf, nfq), 0.0);
+  tables.assign(denseSourceTableOffset(nb, nq, nfp, nf, nfq) + size_t(nq) * nb, 0.0);
   double* phi = tables.data();
   double* dphiw = phi + size_t(nq) * nb;
   double* phif = dphiw + size_t(nq) * 2 * nb;
@@ -78,14 +83,20 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
         phifw[size_t(f * nfq + j) * nb + b] = fr.w[j] * v[b];
       }
     }
-  std::vector<double> m(size_t(nb) * nb, 0.0), ptp(size_t(nb) * nb, 0.0), inv;
+  // reference mass matrix and Phi^T Phi, and their inverses, in long double (rounded once to double)
+  std::vector<long double> m(size_t(nb) * nb, 0.0L), ptp(size_t(nb) * nb, 0.0L), invl;
   for (int a = 0; a < nb; ++a)
     for (int b = 0; b < nb; ++b) {
-      double s = 0, t = 0;
-      for (int q = 0; q < nq; ++q) { s += vr.w[q] * phi[size_t(q) * nb + a] * phi[size_t(q) * nb + b]; t += phi[size_t(q) * nb + a] * phi[size_t(q) * nb + b]; }
+      long double s = 0, t = 0;
+      for (int q = 0; q < nq; ++q) {
+        const long double pa = phi[size_t(q) * nb + a], pb = phi[size_t(q) * nb + b];
+        s += (long double)vr.w[q] * pa * pb;
+        t += pa * pb;
+      }
       m[size_t(a) * nb + b] = s; ptp[size_t(a) * nb + b] = t;
     }
-  invertDense(nb, m, inv);
+  invertDense(nb, m, invl);
+  std::vector<double> inv(invl.begin(), invl.end());
   std::copy(inv.begin(), inv.end(), mref);
   {
     double* dmod = mref + size_t(nb) * nb;
@@ -126,15 +137,27 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
           lmod[(size_t(f) * nfq + j) * nfq + jj] = double(acc);
         }
   }
+  {
+    double* phiw = tables.data() + denseSourceTableOffset(nb, nq, nfp, nf, nfq);
+    for (int q = 0; q < nq; ++q)
+      for (int b = 0; b < nb; ++b) phiw[size_t(q) * nb + b] = vr.w[q] * phi[size_t(q) * nb + b];
+  }
   phiOut.assign(phi, phi + size_t(nq) * nb);
-  // unweighted least-squares projection (InitialCondition.cpp:91-104): lsq = (Phi^T Phi)^-1 Phi^T  [nb][nq]
-  invertDense(nb, ptp, inv);
-  lsqOut.assign(size_t(nb) * nq, 0.0);
-  for (int b = 0; b < nb; ++b)
+  // unweighted least-squares projection (InitialCondition.cpp:91-104): lsq = (Phi^T Phi)^-1 Phi^T  [nb][nq],
+  // followed by its row sums [nb] (lsq applied to the constant 1: 1/phi_0 for the constant mode, 0 otherwise),
+  // which let the projection act on u - u_ref and add u_ref back exactly
+  invertDense(nb, ptp, invl);
+  lsqOut.assign(size_t(nb) * nq + nb, 0.0);
+  for (int b = 0; b < nb; ++b) {
+    long double row = 0.0L;
     for (int q = 0; q < nq; ++q) {
-      double s = 0; for (int k = 0; k < nb; ++k) s += inv[size_t(b) * nb + k] * phi[size_t(q) * nb + k];
-      lsqOut[size_t(b) * nq + q] = s;
+      long double s = 0;
+      for (int k = 0; k < nb; ++k) s += invl[size_t(b) * nb + k] * (long double)phi[size_t(q) * nb + k];
+      lsqOut[size_t(b) * nq + q] = double(s);
+      row += s;
     }
+    lsqOut[size_t(nb) * nq + b] = double(row);
+  }
 }
 
 template <int NB, int NQ, int NFQ, int NF>
@@ -223,7 +246,9 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
       double ja[2][2] = {{g[0], g[1]}, {g[2], g[3]}};
       State<2> st;
       makeState<2>(st, U, ph);
-      const double ep = st.E + st.p;
+      const double ep = energyFluxFactor(st, ph);
+      // Boussinesq buoyancy S |J| at the point, kept in the new-state buffer until the residual pass
+      if (ph.source) sN[le * NV * NB + q] = st.r * ph.beta * (temperatureOf(st, ph) - ph.tref) / g[4];
       double tau[2][2] = {{0.0, 0.0}, {0.0, 0.0}}, qh[2] = {0.0, 0.0};
       if constexpr (VISC) {
         // gradient at the point from the element's modal gradient coefficients [nv*2][NB]
@@ -239,7 +264,8 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
         PrimGrad<2> pg;
         primitiveGradient<2>(g, st.u, st.ir, st.E * st.ir, ph, pg);
         const double u2 = fma(st.u[0], st.u[0], st.u[1] * st.u[1]);
-        viscousTensor<2>(pg, st.u, fma(-0.5, u2, st.E * st.ir) * ph.inv_cv, ph, tau, qh);
+        viscousTensor<2>(pg, st.u, ph.incomp ? st.E * st.ir * ph.inv_cv : fma(-0.5, u2, st.E * st.ir) * ph.inv_cv, ph,
+                         tau, qh);
       }
 #pragma unroll
       for (int b = 0; b < 2; ++b) {
@@ -265,6 +291,10 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
         for (int fj = 0; fj < NFP; ++fj) {
           const int f = fj / NFQ, j = fj - f * NFQ;
           s = fma(-sF[le * S::FSTRIDE + (f * NV + v) * NFQ + j], phifw[fj * NB + i], s);
+        }
+        if (ph.source && v == 2) {  // y momentum: sum_q w_q |J|_q S_q phi_i(x_q)
+          const double* phiw = a.tables + (NQ * NB * 3 + NFP * NB * 2 + NB * NB + 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ);
+          for (int q = 0; q < NQ; ++q) s = fma(sN[le * NV * NB + q], phiw[q * NB + i], s);
         }
         sR[(le * NV + v) * NB + i] = s;
       }

@@ -83,7 +83,7 @@ __device__ __forceinline__ void exchangeBoundaryPoint(const FaceArgs& a, int64_t
   State<DIM> s;
   makeState<DIM>(s, ul, a.ph);
   Comp<DIM> l, g, b;
-  compFromState<DIM>(s, l);
+  compFromState<DIM>(s, l, a.ph);
   const double* gp = a.ghost + (f * nfq + j) * (DIM + 3);
   g.r = gp[0];
 #pragma unroll
@@ -91,11 +91,11 @@ __device__ __forceinline__ void exchangeBoundaryPoint(const FaceArgs& a, int64_t
   g.e = gp[DIM + 1];
   g.p = gp[DIM + 2];
   boundaryState<DIM>(bc, n, l, g, a.ph, b);
-  double ub[NV], u2 = 0.0;
+  double ub[NV];
   ub[0] = b.r;
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) { ub[1 + k] = b.r * b.u[k]; u2 += b.u[k] * b.u[k]; }
-  ub[DIM + 1] = b.r * (b.e + 0.5 * u2);
+  for (int k = 0; k < DIM; ++k) ub[1 + k] = b.r * b.u[k];
+  ub[DIM + 1] = energyOfComp<DIM>(b, a.ph);
 #pragma unroll
   for (int v = 0; v < NV; ++v) a.other[L + v * nfq] = 2.0 * ub[v] - ul[v];
 }
@@ -357,7 +357,7 @@ __device__ __forceinline__ void faceNSPoint(const FaceArgs& a, int64_t t) {
     double u2 = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) u2 = fma(l.u[k], l.u[k], u2);
-    const double T = fma(-0.5, u2, l.E * l.ir) * ph.inv_cv;
+    const double T = ph.incomp ? l.E * l.ir * ph.inv_cv : fma(-0.5, u2, l.E * l.ir) * ph.inv_cv;
     viscousNormalFlux<DIM>(pg, l.u, T, n, ph, fl);
   }
   {
@@ -369,7 +369,7 @@ __device__ __forceinline__ void faceNSPoint(const FaceArgs& a, int64_t t) {
     double u2 = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) u2 = fma(r.u[k], r.u[k], u2);
-    const double T = fma(-0.5, u2, r.E * r.ir) * ph.inv_cv;
+    const double T = ph.incomp ? r.E * r.ir * ph.inv_cv : fma(-0.5, u2, r.E * r.ir) * ph.inv_cv;
     viscousNormalFlux<DIM>(pg, r.u, T, n, ph, fr);
   }
 #pragma unroll
@@ -405,7 +405,7 @@ __device__ __forceinline__ void faceNSBoundaryPoint(const FaceArgs& a, int64_t t
   State<DIM> s;
   makeState<DIM>(s, ul, ph);
   Comp<DIM> l, g, b;
-  compFromState<DIM>(s, l);
+  compFromState<DIM>(s, l, a.ph);
   const double* gp = a.ghost + (f * nfq + j) * (DIM + 3);
   g.r = gp[0];
 #pragma unroll
@@ -414,7 +414,7 @@ __device__ __forceinline__ void faceNSBoundaryPoint(const FaceArgs& a, int64_t t
   g.p = gp[DIM + 2];
   boundaryState<DIM>(bc, n, l, g, ph, b);
   double h[NV];
-  normalFluxComp<DIM>(b, n, h);
+  normalFluxComp<DIM>(b, n, h, ph);
   double gr[NV * DIM];
 #pragma unroll
   for (int c = 0; c < NV * DIM; ++c) gr[c] = a.faceGrad[LG + c * nfq];

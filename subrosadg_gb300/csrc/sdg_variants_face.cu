@@ -43,6 +43,7 @@ KernelVariant faceFluxOf(int flux) {
     case 1: return faceOf<OP, DIM, 1>();
     case 2: return faceOf<OP, DIM, 2>();
     case 3: return faceOf<OP, DIM, 3>();
+    case 4: return faceOf<OP, DIM, 4>();
     default: return KernelVariant();
   }
 }

@@ -115,7 +115,8 @@ class Mesh:
 
 def make_config(polynomial_order, equation=_abi.EULER, convective_flux=_abi.HLLC, viscous_flux=_abi.VISCOUS_NONE,
                 time_integration=_abi.SSPRK3, cp=2.5, cv=25.0 / 14.0, gamma=1.4, mu=0.0, prandtl=0.71,
-                transport=_abi.TRANSPORT_CONSTANT) -> SdgConfig:
+                transport=_abi.TRANSPORT_CONSTANT, sound_speed=0.0, density=1.0, source=_abi.SOURCE_NONE,
+                thermal_expansion=0.0, reference_temperature=0.0) -> SdgConfig:
     c = SdgConfig()
     c.polynomial_order = polynomial_order
     c.equation = equation
@@ -128,6 +129,11 @@ def make_config(polynomial_order, equation=_abi.EULER, convective_flux=_abi.HLLC
     c.specific_heat_constant_volume = cv
     c.dynamic_viscosity = mu
     c.prandtl_number = prandtl
+    c.reference_sound_speed = sound_speed
+    c.reference_density = density
+    c.source_term = source
+    c.thermal_expansion_coefficient = thermal_expansion
+    c.reference_temperature = reference_temperature
     return c
 
 

@@ -130,6 +130,140 @@ def channel_case(p=2, flux=sdg.HLLC, conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.PR
     return (mesh, cfg, ic, bc, dt, steps)
 
 
+# ---- incompressible model (weakly compressible EOS p = c0^2 (rho - rho0) + 0.01 rho0 c0^2, cp = cv = 1) ----------
+# Workload shapes follow the reference's incompressible example drivers (examples/taylorvortex_2d_incns.cpp,
+# lidcavity_2d_incns.cpp, thermalcavity_2d_incns.cpp, shearlayer_2d_inceuler.cpp): rho0 = 1, cp = cv = 1,
+# Pr = 0.71; primitive temperature T = e / cv.
+
+def inc_config(p, flux, viscous=None, mu=0.0, c0=10.0, rho0=1.0, source=sdg.SOURCE_NONE, beta=0.0, tref=0.0,
+               transport=sdg.TRANSPORT_CONSTANT):
+    eq = sdg.INCOMPRESSIBLE_EULER if viscous is None else sdg.INCOMPRESSIBLE_NAVIER_STOKES
+    return sdg.make_config(p, equation=eq, convective_flux=flux,
+                           viscous_flux=sdg.VISCOUS_NONE if viscous is None else viscous, cp=1.0, cv=1.0, gamma=GAMMA,
+                           mu=mu, transport=transport, sound_speed=c0, density=rho0, source=source,
+                           thermal_expansion=beta, reference_temperature=tref)
+
+
+def taylor_vortex_case(n=6, p=4, flux=sdg.EXACT, viscous=sdg.BR2, mu=1e-3, c0=32.0, dt=2e-5, steps=3,
+                       jitter=0.0, split=0.0):
+    """Incompressible Taylor vortex on the periodic unit square (examples/taylorvortex_2d_incns.cpp:31-44):
+    rho = 0.99 + (cos 4 pi x + cos 4 pi y) / (4 c0^2), u = sin 2 pi x cos 2 pi y, v = -cos 2 pi x sin 2 pi y, T = 1."""
+    mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=True, jitter=jitter, split_fraction=split, seed=3)
+    cfg = inc_config(p, flux, viscous, mu, c0)
+
+    def ic(pts):
+        x, y = pts[:, 0], pts[:, 1]
+        rho = (np.cos(4 * math.pi * x) + np.cos(4 * math.pi * y)) / 4.0 / c0 ** 2 + 0.99
+        u = np.sin(2 * math.pi * x) * np.cos(2 * math.pi * y)
+        v = -np.cos(2 * math.pi * x) * np.sin(2 * math.pi * y)
+        return np.stack([rho, u, v, np.ones_like(x)], 1)
+
+    return (mesh, cfg, ic, None, dt, steps)
+
+
+def shear_layer_case(n=6, p=3, flux=sdg.LAX_FRIEDRICHS, c0=10.0, dt=1e-4, steps=3, jitter=0.1, split=0.5,
+                     viscous=None, mu=0.0):
+    """Incompressible double shear layer on the periodic unit square (shearlayer_2d_inceuler.cpp shape):
+    u = tanh(80 (y - 1/4)) or tanh(80 (3/4 - y)), v = 0.05 sin(2 pi x), rho = 1, T = 1 + 0.1 sin(2 pi y)."""
+    mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=True, jitter=jitter, split_fraction=split, seed=9)
+    cfg = inc_config(p, flux, viscous, mu, c0)
+
+    def ic(pts):
+        x, y = pts[:, 0], pts[:, 1]
+        u = np.where(y <= 0.5, np.tanh(30.0 * (y - 0.25)), np.tanh(30.0 * (0.75 - y)))
+        v = 0.05 * np.sin(2 * math.pi * x)
+        rho = np.ones_like(x) + 0.002 * np.cos(2 * math.pi * x)
+        return np.stack([rho, u, v, 1.0 + 0.1 * np.sin(2 * math.pi * y)], 1)
+
+    return (mesh, cfg, ic, None, dt, steps)
+
+
+def cavity_case(p=3, flux=sdg.LAX_FRIEDRICHS, viscous=sdg.BR2, mu=2e-3, c0=10.0, n=5, dt=2e-4, steps=3,
+                jitter=0.0, split=0.0, conditions=None, boussinesq=False, lid=1.0):
+    """Lid-driven (lidcavity_2d_incns.cpp) or differentially heated (thermalcavity_2d_incns.cpp, Boussinesq
+    beta = 1, Tref = 0.5) unit cavity; groups bottom/right/top/left.  The lid case moves the top wall at `lid`;
+    the thermal case holds the right wall at T = 0 and the left at T = 1."""
+    if conditions is None:
+        conditions = ((sdg.ADIABATIC_NONSLIP_WALL, sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_NONSLIP_WALL,
+                       sdg.ISOTHERMAL_NONSLIP_WALL) if boussinesq else (sdg.ADIABATIC_NONSLIP_WALL,) * 4)
+    mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=False, jitter=jitter, split_fraction=split, seed=4,
+                           boundary_conditions=list(conditions))
+    cfg = inc_config(p, flux, viscous, mu, c0, source=sdg.SOURCE_BOUSSINESQ if boussinesq else sdg.SOURCE_NONE,
+                     beta=1.0 if boussinesq else 0.0, tref=0.5 if boussinesq else 0.0)
+
+    def ic(pts):
+        x, y = pts[:, 0], pts[:, 1]
+        rho = 1.0 + 0.003 * np.sin(math.pi * x) * np.sin(math.pi * y)
+        u = 0.1 * np.sin(math.pi * x) * np.sin(2 * math.pi * y)
+        v = -0.1 * np.sin(2 * math.pi * x) * np.sin(math.pi * y)
+        t = 0.5 + 0.3 * (0.5 - x) + 0.05 * np.sin(math.pi * y)
+        return np.stack([rho, u, v, t], 1)
+
+    def bc(pts, phys):
+        out = np.zeros((len(pts), 4))
+        out[:, 0] = 1.0
+        out[:, 1] = np.where(phys == 3, 0.0 if boussinesq else lid, 0.0)
+        out[:, 3] = np.where(phys == 4, 1.0, np.where(phys == 2, 0.0, 0.5))
+        return out
+
+    return (mesh, cfg, ic, bc, dt, steps)
+
+
+def inc_channel_case(p=2, flux=sdg.EXACT, viscous=None, mu=0.0, c0=10.0, n=4, dt=2e-4, steps=3, split=0.0,
+                     conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL,
+                                 sdg.RIEMANN_FARFIELD)):
+    """Incompressible flow through [0,2]x[0,1] at u = 0.4 with farfield / inflow / outflow groups
+    (the cylinder and aerofoil drivers' boundary set)."""
+    mesh = sdg.Mesh.box_2d(0.0, 0.0, 2.0, 1.0, 2 * n, n, periodic=False, split_fraction=split, seed=6,
+                           boundary_conditions=list(conditions))
+    cfg = inc_config(p, flux, viscous, mu, c0)
+
+    def ic(pts):
+        x, y = pts[:, 0], pts[:, 1]
+        rho = 1.0 + 0.004 * np.sin(math.pi * x) * np.sin(math.pi * y)
+        u = 0.4 + 0.05 * np.cos(math.pi * y)
+        v = 0.05 * np.sin(math.pi * x)
+        return np.stack([rho, u, v, 1.0 + 0.05 * np.cos(math.pi * x)], 1)
+
+    def bc(pts, phys):
+        out = np.zeros((len(pts), 4))
+        out[:, 0] = np.where(phys == 2, 0.999, 1.0)
+        out[:, 1] = 0.4
+        out[:, 3] = 1.0
+        return out
+
+    return (mesh, cfg, ic, bc, dt, steps)
+
+
+def cavity_3d_case(p=2, flux=sdg.EXACT, viscous=sdg.BR1, mu=2e-3, c0=10.0, n=3, dt=2e-4, steps=3, boussinesq=False):
+    """3D cavity on hexahedra (lidcavity_3d_incns.cpp / thermalcavity_3d_incns.cpp shapes); groups
+    x-, x+, y-, y+, z-, z+.  Lid: the z+ wall moves at u = 1.  Thermal: x- at T = 1, x+ at T = 0, buoyancy
+    on w."""
+    conds = ([sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ISOTHERMAL_NONSLIP_WALL] + [sdg.ADIABATIC_NONSLIP_WALL] * 4
+             if boussinesq else [sdg.ADIABATIC_NONSLIP_WALL] * 6)
+    mesh = sdg.Mesh.box_3d(0, 0, 0, 1, 1, 1, n, n, n, periodic=False, boundary_conditions=conds)
+    cfg = inc_config(p, flux, viscous, mu, c0, source=sdg.SOURCE_BOUSSINESQ if boussinesq else sdg.SOURCE_NONE,
+                     beta=1.0 if boussinesq else 0.0, tref=0.5 if boussinesq else 0.0)
+
+    def ic(pts):
+        x, y, z = pts[:, 0], pts[:, 1], pts[:, 2]
+        rho = 1.0 + 0.003 * np.sin(math.pi * x) * np.sin(math.pi * y) * np.sin(math.pi * z)
+        u = 0.1 * np.sin(math.pi * x) * np.sin(2 * math.pi * z)
+        v = 0.05 * np.sin(math.pi * y) * np.sin(math.pi * x)
+        w = -0.1 * np.sin(2 * math.pi * x) * np.sin(math.pi * z)
+        t = 0.5 + 0.3 * (0.5 - x) + 0.05 * np.sin(math.pi * z)
+        return np.stack([rho, u, v, w, t], 1)
+
+    def bc(pts, phys):
+        out = np.zeros((len(pts), 5))
+        out[:, 0] = 1.0
+        out[:, 1] = np.where(phys == 6, 0.0 if boussinesq else 1.0, 0.0)
+        out[:, 4] = np.where(phys == 1, 1.0, np.where(phys == 2, 0.0, 0.5))
+        return out
+
+    return (mesh, cfg, ic, bc, dt, steps)
+
+
 def batch_instances(count=256, seed=2024, min_elements=500, max_elements=50000, orders=(1, 2, 3, 4, 5)):
     """The batched workload: `count` independent 2D Kelvin-Helmholtz solves on [0,1]^2 (periodic), element
     counts log-uniform in [min_elements, max_elements], P uniform in `orders`, jittered (10% of h) quads or

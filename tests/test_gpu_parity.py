@@ -109,6 +109,30 @@ CASES = {
         conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_NONSLIP_WALL, sdg.ADIABATIC_SLIP_WALL,
                     sdg.VELOCITY_INFLOW)),
     "ns-tri-p5-br2-hllc": lambda: cases.kh_case(n=4, p=5, flux=sdg.HLLC, split=1.0, steps=2, viscous=sdg.BR2, mu=2e-3),
+    # incompressible model (weakly compressible EOS; Exact / LF / Central fluxes; Boussinesq source)
+    "inc-taylorvortex-quad-p4-exact-br2": lambda: cases.taylor_vortex_case(n=5, p=4, mu=1e-2),
+    "inc-taylorvortex-hybrid-p3-exact-br1": lambda: cases.taylor_vortex_case(n=5, p=3, viscous=sdg.BR1, mu=1e-2,
+                                                                            jitter=0.1, split=0.5),
+    "inc-taylorvortex-quad-p1-exact-br2-dense": lambda: cases.taylor_vortex_case(n=6, p=1, mu=1e-2),
+    "inc-shearlayer-hybrid-p3-lf": lambda: cases.shear_layer_case(n=6, p=3),
+    "inc-shearlayer-tri-p2-central": lambda: cases.shear_layer_case(n=6, p=2, flux=sdg.CENTRAL, split=1.0),
+    "inc-shearlayer-quad-p5-exact": lambda: cases.shear_layer_case(n=4, p=5, flux=sdg.EXACT, split=0.0, steps=2),
+    "inc-lidcavity-quad-p3-lf-br2": lambda: cases.cavity_case(p=3, mu=1e-2),
+    "inc-thermalcavity-quad-p2-exact-br2-boussinesq": lambda: cases.cavity_case(p=2, flux=sdg.EXACT, mu=1e-2,
+                                                                                boussinesq=True, c0=3.0),
+    "inc-thermalcavity-hybrid-p3-exact-br1-boussinesq": lambda: cases.cavity_case(
+        p=3, flux=sdg.EXACT, viscous=sdg.BR1, mu=1e-2, boussinesq=True, c0=3.0, jitter=0.1, split=0.5),
+    "inc-channel-farfield-quad-p2-exact": lambda: cases.inc_channel_case(p=2),
+    "inc-channel-inflow-outflow-tri-p3-lf": lambda: cases.inc_channel_case(
+        p=3, flux=sdg.LAX_FRIEDRICHS, split=1.0,
+        conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "inc-ns-channel-walls-quad-p3-exact-br2": lambda: cases.inc_channel_case(
+        p=3, viscous=sdg.BR2, mu=1e-2,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "inc-lidcavity-hex-p2-exact-br1": lambda: cases.cavity_3d_case(p=2, mu=1e-2),
+    "inc-thermalcavity-hex-p3-lf-br2-boussinesq": lambda: cases.cavity_3d_case(
+        p=3, flux=sdg.LAX_FRIEDRICHS, viscous=sdg.BR2, mu=1e-2, boussinesq=True, c0=3.0),
+    "inc-euler-cavity-hex-p3-exact": lambda: cases.cavity_3d_case(p=3, viscous=None, mu=0.0),
 }
 
 
@@ -135,7 +159,12 @@ def test_parity(name):
     if err > 1e-12:
         ref_err = rel_l2(reference_arithmetic_residual(CASES[name]()), ro)
         print(f"{name}: GPU residual error {err:.2e}, reference FP64 arithmetic error {ref_err:.2e}")
-        assert ref_err > 1e-12 and err <= 0.1 * ref_err, (err, ref_err, per_var(rg, ro))
+        if not (ref_err > 1e-12 and err <= 0.1 * ref_err):
+            # diagnostic: the truth at the GPU's own state separates projection error from residual arithmetic
+            o.set_state_point(g.state_point())
+            own = rel_l2(rg, o.residual_point())
+            raise AssertionError(f"residual {err:.3e} (reference arithmetic {ref_err:.3e}, at the GPU's own state "
+                                 f"{own:.3e}) per variable {per_var(rg, ro)}")
     # time step
     dtg, dto = g.calculateDeltaTime(0.2), o.delta_time(0.2)
     assert abs(dtg - dto) <= 1e-13 * dto
