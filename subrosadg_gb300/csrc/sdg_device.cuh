@@ -75,7 +75,16 @@ __device__ __forceinline__ void makeState(State<D, T>& s, const T* U, const Phys
   T mu = T(0.0);
 #pragma unroll
   for (int k = 0; k < D; ++k) { s.u[k] = s.m[k] * s.ir; mu = fmaT(s.m[k], s.u[k], mu); }
-  s.p = ph.incomp ? weakPressure(s.r, ph) : ph.gm1 * fmaT(-0.5, mu, s.E);
+  if constexpr (ScalarTraits<T>::dual) {
+    s.p = ph.incomp ? weakPressure(s.r, ph) : ph.gm1 * fmaT(-0.5, mu, s.E);
+  } else {
+    // one FMA pair serves both models, its operands picked by selects (no FP64 work for the unused model):
+    // compressible (gamma - 1)(E - m.u/2) + 0, incompressible c0^2 (rho - rho0) + padd; both round as the
+    // separate forms do (fma(a, x, 0) = round(a x), fma(1, r, -rho0) = round(r - rho0))
+    const bool inc = ph.incomp;
+    const double x = fma(inc ? 1.0 : -0.5, inc ? s.r : mu, inc ? -ph.rho0 : s.E);
+    s.p = fma(inc ? ph.c02 : ph.gm1, x, inc ? ph.padd : 0.0);
+  }
 }
 
 // E + p of the compressible energy flux (E u + p u); the incompressible model transports rho e (no p u).
@@ -87,11 +96,10 @@ __device__ __forceinline__ T energyFluxFactor(const State<D, T>& s, const Phys& 
 // Temperature e / cv: compressible e = E/rho - |u|^2/2, incompressible e = (rho e)/rho.
 template <int D, class T>
 __device__ __forceinline__ T temperatureOf(const State<D, T>& s, const Phys& ph) {
-  if (ph.incomp) return s.E * s.ir * ph.inv_cv;
   T u2 = T(0.0);
 #pragma unroll
   for (int k = 0; k < D; ++k) u2 = fmaT(s.u[k], s.u[k], u2);
-  return fmaT(-0.5, u2, s.E * s.ir) * ph.inv_cv;
+  return fmaT(ph.incomp ? 0.0 : -0.5, u2, s.E * s.ir) * ph.inv_cv;
 }
 
 template <int D, class T>

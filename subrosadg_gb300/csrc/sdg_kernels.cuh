@@ -219,7 +219,7 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
         double u2 = 0.0;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) u2 = fma(s.u[k], s.u[k], u2);
-        viscousTensor<DIM>(pg, s.u, ph.incomp ? s.E * s.ir * ph.inv_cv : fma(-0.5, u2, s.E * s.ir) * ph.inv_cv, ph,
+        viscousTensor<DIM>(pg, s.u, fma(ph.incomp ? 0.0 : -0.5, u2, s.E * s.ir) * ph.inv_cv, ph,
                            tau, q);
       }
 #pragma unroll

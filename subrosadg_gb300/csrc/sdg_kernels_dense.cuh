@@ -264,7 +264,7 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
         PrimGrad<2> pg;
         primitiveGradient<2>(g, st.u, st.ir, st.E * st.ir, ph, pg);
         const double u2 = fma(st.u[0], st.u[0], st.u[1] * st.u[1]);
-        viscousTensor<2>(pg, st.u, ph.incomp ? st.E * st.ir * ph.inv_cv : fma(-0.5, u2, st.E * st.ir) * ph.inv_cv, ph,
+        viscousTensor<2>(pg, st.u, fma(ph.incomp ? 0.0 : -0.5, u2, st.E * st.ir) * ph.inv_cv, ph,
                          tau, qh);
       }
 #pragma unroll

@@ -357,7 +357,7 @@ __device__ __forceinline__ void faceNSPoint(const FaceArgs& a, int64_t t) {
     double u2 = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) u2 = fma(l.u[k], l.u[k], u2);
-    const double T = ph.incomp ? l.E * l.ir * ph.inv_cv : fma(-0.5, u2, l.E * l.ir) * ph.inv_cv;
+    const double T = fma(ph.incomp ? 0.0 : -0.5, u2, l.E * l.ir) * ph.inv_cv;
     viscousNormalFlux<DIM>(pg, l.u, T, n, ph, fl);
   }
   {
@@ -369,7 +369,7 @@ __device__ __forceinline__ void faceNSPoint(const FaceArgs& a, int64_t t) {
     double u2 = 0.0;
 #pragma unroll
     for (int k = 0; k < DIM; ++k) u2 = fma(r.u[k], r.u[k], u2);
-    const double T = ph.incomp ? r.E * r.ir * ph.inv_cv : fma(-0.5, u2, r.E * r.ir) * ph.inv_cv;
+    const double T = fma(ph.incomp ? 0.0 : -0.5, u2, r.E * r.ir) * ph.inv_cv;
     viscousNormalFlux<DIM>(pg, r.u, T, n, ph, fr);
   }
 #pragma unroll
