@@ -65,6 +65,7 @@ enum sdg_convective_flux {                                                      
   SDG_FLUX_EXACT = 4          /* incompressible models only (ConvectiveFlux.cpp:352-414)                   */
 };
 enum sdg_source_term { SDG_SOURCE_NONE = 0, SDG_SOURCE_BOUSSINESQ = 1 };               /* Enum.cpp:71-74   */
+enum sdg_shock_capturing { SDG_SHOCK_NONE = 0, SDG_SHOCK_ARTIFICIAL_VISCOSITY = 1 };    /* Enum.cpp:76-79   */
 enum sdg_viscous_flux { SDG_VISCOUS_NONE = 0, SDG_VISCOUS_BR1 = 1, SDG_VISCOUS_BR2 = 2 }; /* Enum.cpp:115-119 */
 enum sdg_time_integration {                                                            /* Enum.cpp:136-140 */
   SDG_FORWARD_EULER = 0,
@@ -126,6 +127,11 @@ typedef struct sdg_config {
   double thermal_expansion_coefficient; /* Boussinesq beta (SourceTerm.cpp:35-38), gravity 1 along the last
                                            coordinate (y in 2D, z in 3D)                                   */
   double reference_temperature;       /* Boussinesq T_ref                                               */
+  /* shock capturing (System::setArtificialViscosity, SystemControl.cpp:105-108): per-step Persson-Peraire
+     density sensor, eps = factor * h / P ramped over [s0 - tolerance, s0 + tolerance], vertex max        */
+  int32_t shock_capturing;            /* sdg_shock_capturing                                            */
+  double empirical_tolerance;         /* kappa of the sensor ramp (> 0 with artificial viscosity)       */
+  double artificial_viscosity_factor; /* eps0 (the reference's default 1.0)                             */
 } sdg_config;
 
 /* ---- sizes of a created problem ------------------------------------------------------------- */
@@ -277,6 +283,11 @@ int sdg_mesh_generate_3d(double x0, double y0, double z0, double lx, double ly, 
  * are used).  Physical groups of dimension d-1 become boundary groups in file order. */
 int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out);
 int sdg_mesh_free(sdg_generated_mesh* mesh);
+
+/* Artificial viscosity of the current state at every mesh node (the reference's node_artificial_viscosity_,
+ * SpatialDiscrete.cpp:37-192): the sensor, the max over each node's elements.  Zeros without shock capturing.
+ * out: [node_count]. */
+int sdg_get_node_artificial_viscosity(sdg_handle* handle, double* out);
 
 /* ---- raw-binary solution files (the reference's writeRawBinary / LastStep and SpecificFile restarts,
  * src/View/RawBinary.cpp:42-191, src/Solver/InitialCondition.cpp:40-80) ---------------------------------

@@ -35,6 +35,8 @@ def load(precision="double"):
                      "orc_relative_error", "orc_residual_point", "orc_interior_face_geometry"):
             getattr(lib, name).argtypes = [c_void_p, _pd]
             getattr(lib, name).restype = c_int
+        lib.orc_node_artificial_viscosity.argtypes = [c_void_p, _pd]
+        lib.orc_node_artificial_viscosity.restype = c_int
         lib.orc_boundary_point_coordinate.argtypes = [c_void_p, _pd, _pi]
         lib.orc_counts.argtypes = [c_void_p, POINTER(c_int64)]
         lib.orc_calculate_delta_time.argtypes = [c_void_p, c_double, _pd]
@@ -68,6 +70,13 @@ class Oracle:
         self.lib.orc_counts(self.h, c)
         self.elements, self.volume_points_count, self.interior, self.boundary, self.nfq, self.dof = list(c)
         self.nv = mesh.dimension + 2
+        self.node_count = len(mesh.nodes)
+
+    def node_artificial_viscosity(self):
+        """Artificial viscosity of the current state at the mesh nodes (zeros without shock capturing)."""
+        out = np.zeros(self.node_count)
+        self.lib.orc_node_artificial_viscosity(self.h, out.ctypes.data_as(_pd))
+        return out
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -323,6 +323,12 @@ struct RefElement {
   std::vector<Real> lsqInv; // [nb][nb]        modal_least_squares_inverse_
   std::vector<Real> ptp;    // [nb][nb]        Phi^T Phi
   std::vector<std::vector<int>> perm;  // rotation -> face point permutation
+  // artificial viscosity: first-order nodal basis at the volume and face points (BasisFunction.cpp:138-140,
+  // 177,205: nodal_value_, nodal_adjacency_value_) and the modes of degree P (the sensor's high-order part)
+  int nvert = 0;
+  std::vector<Real> nodal;   // [nq][nvert]
+  std::vector<Real> nodalf;  // [nface*nfq][nvert]
+  std::vector<int> high;     // [nb] 1 for the modes of degree P
 
   void build(int t, int order) {
     type = t; dim = elemDim(t); p = order; nb = basisCount(t, order); nface = elemFaces(t);
@@ -351,7 +357,37 @@ struct RefElement {
         }
         modalBasis(t, order, X, v.data(), g.data());
         for (int b = 0; b < nb; ++b) phif[(size_t(f) * nfq + j) * nb + b] = v[b];
+        Real sh8[8], g8[24];
+        elemShape(t, X, sh8, g8);
+        nodalf.resize(size_t(nface) * nfq * elemVerts(t));
+        for (int k = 0; k < elemVerts(t); ++k) nodalf[(size_t(f) * nfq + j) * elemVerts(t) + k] = sh8[k];
       }
+    nvert = elemVerts(t);
+    nodal.assign(size_t(nq) * nvert, 0);
+    for (int q = 0; q < nq; ++q) {
+      Real sh8[8], g8[24];
+      elemShape(t, &vq.x[q * 3], sh8, g8);
+      for (int k = 0; k < nvert; ++k) nodal[size_t(q) * nvert + k] = sh8[k];
+    }
+    // degree of each mode: tensor blocks max(a, b[, c]) of the Lobatto indices (l_0, l_1 linear, l_k of
+    // degree k); triangles: vertices 1, edge modes k, bubbles i + j + 3
+    high.assign(nb, 0);
+    for (int b = 0; b < nb; ++b) {
+      int deg = 0;
+      if (t == kQuad || t == kHex) {
+        int r = b;
+        for (int dd = 0; dd < dim; ++dd) { deg = std::max(deg, std::max(1, r % (order + 1))); r /= order + 1; }
+      } else if (b < 3) {
+        deg = 1;
+      } else if (b < 3 + 3 * (order - 1)) {
+        deg = 2 + (b - 3) % (order - 1);
+      } else {
+        int idx = b - 3 - 3 * (order - 1), sdeg = 0;
+        while (idx > sdeg) { idx -= sdeg + 1; ++sdeg; }
+        deg = sdeg + 3;
+      }
+      high[b] = order == 1 || deg == order ? 1 : 0;  // P1: the whole density (SpatialDiscrete.cpp:51-52)
+    }
     ptp.assign(size_t(nb) * nb, 0.0);
     for (int a = 0; a < nb; ++a)
       for (int b = 0; b < nb; ++b) {

@@ -15,6 +15,8 @@
 //   residual assembly              src/Solver/SpatialDiscrete.cpp:1016-1068
 //   RK update, dt, relative error  src/Solver/TimeIntegration.cpp:45-324
 //   source term (Boussinesq)       src/Solver/SpatialDiscrete.cpp:254-262,1026-1029, SourceTerm.cpp:29-58
+//   artificial viscosity           src/Solver/SpatialDiscrete.cpp:37-192 (sensor, vertex max), :204-250 (volume),
+//                                  :528-631,685-734 (faces), :785-834 (boundary), ViscousFlux.cpp:105-200
 // Periodic pairing uses a node map (master node per slave node) in place of gmsh's periodic entity
 // queries; the right rotation of a periodic face is taken from the parents' face vertex order, the
 // same rule as for ordinary interior faces.
@@ -46,6 +48,8 @@ struct Block {
   std::vector<Real> minv;     // ne * nb*nb     local mass matrix inverse
   std::vector<Real> mass;     // ne * nb*nb     local mass matrix (kept when refining solves)
   std::vector<Real> minEdge;  // ne
+  std::vector<Real> innerRadius;  // ne (artificial viscosity length scale)
+  std::vector<Real> epsV;     // ne * nvert  artificial viscosity at the element's vertices
   // state (column-major nv x nb per element: index b*nv + v)
   std::vector<Real> coef, last, res;
   std::vector<Real> qvol;     // ne * nv x (nq*d)
@@ -81,11 +85,59 @@ struct Problem {
   bool hasState = false;
   std::string err;
 
+  // artificial viscosity (ShockCapturingEnum::ArtificialViscosity): empirical tolerance and factor
+  bool av = false;
+  Real avTol = 0, avFactor = 1;
+  std::vector<Real> nodeAV;   // per mesh node, the max over its elements
   bool ns() const { return eq == 1 || eq == 3; }  // compressible or incompressible Navier-Stokes
+  bool gradientPass() const { return ns() || faithful || av; }
   int nfq() const { return blocks[0].ref.nfq; }
 };
 
 // ---- setup ----------------------------------------------------------------------------------------
+
+// Inner radius (gmsh quality "innerRadius", the artificial-viscosity length, Geometry.cpp:31-41; gmsh 4.13.1 is
+// not vendored): the inscribed radius 2A/perimeter of a triangle, the same tangential-polygon formula for a
+// quadrangle (A from its diagonals), and 3V/S for a hexahedron (V by 2x2x2 Gauss quadrature of the trilinear map,
+// S from each face's diagonals) -- exact for squares and cubes.
+static Real innerRadiusOf(int type, const double* nodes, const int* vv) {
+  auto X = [&](int k, int d) { return Real(nodes[size_t(vv[k]) * 3 + d]); };
+  auto sub = [&](int a, int b, Real* o) { for (int d = 0; d < 3; ++d) o[d] = X(a, d) - X(b, d); };
+  auto norm = [](const Real* a) { return std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); };
+  auto crossNorm = [&](const Real* a, const Real* b) {
+    const Real c[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};
+    return norm(c);
+  };
+  if (type == kTri || type == kQuad) {
+    const int nv = type == kTri ? 3 : 4;
+    Real per = 0, e[3];
+    for (int i = 0; i < nv; ++i) { sub((i + 1) % nv, i, e); per += norm(e); }
+    Real d1[3], d2[3];
+    if (type == kTri) { sub(1, 0, d1); sub(2, 0, d2); }
+    else { sub(2, 0, d1); sub(3, 1, d2); }
+    return crossNorm(d1, d2) / per;  // 2 (|d1 x d2| / 2) / perimeter
+  }
+  static const int faces[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {0, 4, 7, 3}, {1, 2, 6, 5}, {2, 3, 7, 6}, {4, 5, 6, 7}};
+  Real area = 0;
+  for (const auto& f : faces) {
+    Real d1[3], d2[3];
+    sub(f[2], f[0], d1); sub(f[3], f[1], d2);
+    area += crossNorm(d1, d2) / 2.0;
+  }
+  const Real g = 1.0 / std::sqrt(3.0);
+  Real vol = 0;
+  for (int q = 0; q < 8; ++q) {
+    const Real xi[3] = {(q & 1) ? g : -g, (q & 2) ? g : -g, (q & 4) ? g : -g};
+    Real sh[8], gr[24], J[3][3] = {{0}};
+    elemShape(kHex, xi, sh, gr);
+    for (int k = 0; k < 8; ++k)
+      for (int l = 0; l < 3; ++l)
+        for (int m = 0; m < 3; ++m) J[l][m] += gr[k * 3 + m] * X(k, l);
+    vol += J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+           J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  }
+  return 3.0 * vol / area;
+}
 
 static void buildGeometry(Problem& P, Block& B, const double* nodes) {
   const RefElement& R = B.ref;
@@ -96,6 +148,7 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
   B.minv.assign(size_t(B.ne) * nb * nb, 0.0);
   if (P.refine) B.mass.assign(size_t(B.ne) * nb * nb, 0.0);
   B.minEdge.assign(size_t(B.ne), 0.0);
+  B.innerRadius.assign(size_t(B.ne), 0.0);
   std::string failure;
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < B.ne; ++e) {
@@ -164,6 +217,7 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
       me = std::min(me, l);
     }
     B.minEdge[e] = me;
+    B.innerRadius[e] = innerRadiusOf(B.type, nodes, vv);
   }
   if (!failure.empty()) throw std::runtime_error(failure);
 }
@@ -424,6 +478,74 @@ static void gradientQuadratureAndResidual(Problem& P) {
   }
 }
 
+// Artificial viscosity of every element (SpatialDiscrete.cpp:37-89): the Persson-Peraire sensor
+// s = log10(int rho_h^2 / int rho^2) with rho_h the degree-P modes of the density (the whole density for P1);
+// eps = 0 below s0 - kappa, eps0 h/P above s0 + kappa, and the sine ramp between; then the max over the
+// elements sharing each mesh node (:91-109) and the elements' vertex values from their nodes (:111-124).
+// s0 per order (SimulationControl.cpp:892-893).
+static const Real kAvTolerance[5] = {0.0, -1.20411998266, -1.90848501888, -2.40823996531, -2.79588001734};
+static const Real kPiReal = Real(3.141592653589793238462643383279502884L);
+
+static void artificialViscosity(Problem& P) {
+  const Real s0 = kAvTolerance[P.p - 1];
+  std::fill(P.nodeAV.begin(), P.nodeAV.end(), Real(0));
+  for (Block& B : P.blocks) {
+    const int nq = B.ref.nq, nb = B.ref.nb, nv = P.nv, nvert = B.ref.nvert;
+    std::vector<Real> eps(size_t(B.ne));
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < B.ne; ++e) {
+      const Real* c = &B.coef[size_t(e) * nv * nb];
+      Real num = 0, den = 0;
+      for (int q = 0; q < nq; ++q) {
+        Real all = 0, hi = 0;
+        for (int b = 0; b < nb; ++b) {
+          const Real t = B.ref.phi[size_t(q) * nb + b] * c[b * nv];
+          all += t;
+          if (B.ref.high[b]) hi += t;
+        }
+        const Real w = B.jw[size_t(e) * nq + q];
+        num += hi * (hi * w);
+        den += all * (all * w);
+      }
+      const Real sc = std::log10(num / den);
+      const Real full = P.avFactor * (B.innerRadius[e] / Real(P.p));
+      if (sc < s0 - P.avTol) eps[e] = 0;
+      else if (sc > s0 + P.avTol) eps[e] = full;
+      else eps[e] = full * (1.0 + std::sin(kPiReal * (sc - s0) / (2.0 * P.avTol))) / 2.0;
+    }
+    for (int64_t e = 0; e < B.ne; ++e)
+      for (int k = 0; k < nvert; ++k) {
+        Real& n = P.nodeAV[size_t(B.verts[size_t(e) * nvert + k])];
+        n = std::max(n, eps[e]);
+      }
+  }
+  for (Block& B : P.blocks) {
+    const int nvert = B.ref.nvert;
+    for (int64_t e = 0; e < B.ne; ++e)
+      for (int k = 0; k < nvert; ++k)
+        B.epsV[size_t(e) * nvert + k] = P.nodeAV[size_t(B.verts[size_t(e) * nvert + k])];
+  }
+}
+
+// Volume-gradient trace on face f (the artificial viscosity's gradient, ViscousFluxEnum::None:
+// variable_volume_gradient_basis_function_coefficient_), conserved rows (v*d+k).
+static void volumeGradientTrace(const Problem& P, int b, int e, int f, Real* out /* nfq * nv*d */) {
+  const Block& B = P.blocks[b];
+  const int nr = P.nv * P.dim, nb = B.ref.nb, nfq = B.ref.nfq;
+  interp(nr, nb, nfq, &B.vgc[size_t(e) * nr * nb], &B.ref.phif[size_t(f) * nfq * nb], out);
+}
+
+// Artificial viscosity at face f's points of element e (nodal_adjacency_value_ x vertex values).
+static void faceViscosity(const Problem& P, int b, int e, int f, Real* out /* nfq */) {
+  const Block& B = P.blocks[b];
+  const int nvert = B.ref.nvert, nfq = B.ref.nfq;
+  for (int j = 0; j < nfq; ++j) {
+    Real s = 0;
+    for (int k = 0; k < nvert; ++k) s += B.ref.nodalf[(size_t(f) * nfq + j) * nvert + k] * B.epsV[size_t(e) * nvert + k];
+    out[j] = s;
+  }
+}
+
 static void quadratureAndResidual(Problem& P) {
   const int d = P.dim, nv = P.nv, nr = nv * d;
   // volume (SpatialDiscrete.cpp:194-266)
@@ -435,6 +557,8 @@ static void quadratureAndResidual(Problem& P) {
       std::vector<Real> gvals;
       interp(nv, nb, nq, &B.coef[size_t(e) * nv * nb], B.ref.phi.data(), vals);
       if (P.ns()) { gvals.resize(size_t(nq) * nr); interp(nr, nb, nq, &B.gc[size_t(e) * nr * nb], B.ref.phi.data(), gvals.data()); }
+      std::vector<Real> avg;
+      if (P.av) { avg.resize(size_t(nq) * nr); interp(nr, nb, nq, &B.vgc[size_t(e) * nr * nb], B.ref.phi.data(), avg.data()); }
       Real* Q = &B.qvol[size_t(e) * nv * nq * d];
       for (int q = 0; q < nq; ++q) {
         PointVar v; for (int i = 0; i < nv; ++i) v.cons[i] = vals[q * nv + i];
@@ -447,6 +571,12 @@ static void quadratureAndResidual(Problem& P) {
             Real fv[kMaxVar]; viscousNormalFlux(P.ph, nk, v, pg, fv);
             for (int i = 0; i < nv; ++i) F[k][i] -= fv[i];
           }
+        }
+        if (P.av) {  // eps(x_q) times the volume gradient (ViscousFlux.cpp:105-113)
+          Real eq = 0;
+          for (int k = 0; k < B.ref.nvert; ++k) eq += B.ref.nodal[size_t(q) * B.ref.nvert + k] * B.epsV[size_t(e) * B.ref.nvert + k];
+          for (int k = 0; k < d; ++k)
+            for (int i = 0; i < nv; ++i) F[k][i] -= eq * avg[size_t(q) * nr + i * d + k];
         }
         const Real* M = &B.jtiw[(size_t(e) * nq + q) * d * d];
         for (int i = 0; i < nv; ++i)
@@ -476,6 +606,12 @@ static void quadratureAndResidual(Problem& P) {
       gl.resize(size_t(nfq) * nr); gr.resize(size_t(nfq) * nr);
       gradientTrace(P, F.bl, F.el, F.fl, gl.data()); gradientTrace(P, F.br, F.er, F.fr, gr.data());
     }
+    std::vector<Real> al, ar, el_, er_;
+    if (P.av) {
+      al.resize(size_t(nfq) * nr); ar.resize(size_t(nfq) * nr); el_.resize(nfq); er_.resize(nfq);
+      volumeGradientTrace(P, F.bl, F.el, F.fl, al.data()); volumeGradientTrace(P, F.br, F.er, F.fr, ar.data());
+      faceViscosity(P, F.bl, F.el, F.fl, el_.data()); faceViscosity(P, F.br, F.er, F.fr, er_.data());
+    }
     Real* QL = &BL.qface[size_t(F.el) * nv * BL.ref.nface * nfq];
     Real* QR = &BR.qface[size_t(F.er) * nv * BR.ref.nface * nfq];
     for (int j = 0; j < nfq; ++j) {
@@ -488,6 +624,16 @@ static void quadratureAndResidual(Problem& P) {
         primitiveGradient(P.ph, R[jr], &gr[size_t(jr) * nr], pr);
         viscousNormalFlux(P.ph, n, L[j], pl, fl); viscousNormalFlux(P.ph, n, R[jr], pr, fr);
         for (int v = 0; v < nv; ++v) h[v] -= (fl[v] + fr[v]) / 2.0;
+      }
+      if (P.av) {  // central artificial viscous flux (ViscousFlux.cpp:183-197)
+        for (int v = 0; v < nv; ++v) {
+          Real sl = 0, sr = 0;
+          for (int k = 0; k < d; ++k) {
+            sl += el_[j] * al[size_t(j) * nr + v * d + k] * n[k];
+            sr += er_[jr] * ar[size_t(jr) * nr + v * d + k] * n[k];
+          }
+          h[v] -= (sl + sr) / 2.0;
+        }
       }
       for (int v = 0; v < nv; ++v) {
         const Real t = h[v] * F.fjw[j];
@@ -505,6 +651,11 @@ static void quadratureAndResidual(Problem& P) {
     Block& BL = P.blocks[F.bl];
     std::vector<Real> gl;
     if (P.ns()) { gl.resize(size_t(nfq) * nr); gradientTrace(P, F.bl, F.el, F.fl, gl.data()); }
+    std::vector<Real> al, el_;
+    if (P.av) {
+      al.resize(size_t(nfq) * nr); el_.resize(nfq);
+      volumeGradientTrace(P, F.bl, F.el, F.fl, al.data()); faceViscosity(P, F.bl, F.el, F.fl, el_.data());
+    }
     Real* QL = &BL.qface[size_t(F.el) * nv * BL.ref.nface * nfq];
     for (int j = 0; j < nfq; ++j) {
       const Real* n = &F.normal[j * 3];
@@ -521,6 +672,12 @@ static void quadratureAndResidual(Problem& P) {
         viscousNormalFlux(P.ph, n, lm, pl, fl); viscousNormalFlux(P.ph, n, b, pb, fb);
         for (int v = 0; v < nv; ++v) h[v] -= (fl[v] + fb[v]) / 2.0;
       }
+      if (P.av)  // the interior side's artificial viscous flux only (SpatialDiscrete.cpp:815-834)
+        for (int v = 0; v < nv; ++v) {
+          Real s = 0;
+          for (int k = 0; k < d; ++k) s += el_[j] * al[size_t(j) * nr + v * d + k] * n[k];
+          h[v] -= s;
+        }
       for (int v = 0; v < nv; ++v) QL[size_t(F.fl * nfq + j) * nv + v] = h[v] * F.fjw[j];
     }
   }
@@ -591,9 +748,10 @@ static void relativeError(Problem& P) {
 
 static void step(Problem& P, Real dt) {
   for (Block& B : P.blocks) B.last = B.coef;  // TimeIntegration.cpp:70-102
+  if (P.av) artificialViscosity(P);            // once per step, TimeIntegration.cpp:336-338
   const int nstage = P.rk + 1;
   for (int s = 0; s < nstage; ++s) {
-    if (P.ns() || P.faithful) gradientQuadratureAndResidual(P);
+    if (P.gradientPass()) gradientQuadratureAndResidual(P);
     quadratureAndResidual(P);
     update(P, s, dt);
   }
@@ -660,6 +818,9 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
   } else if (P->flux == SDG_FLUX_EXACT) {
     throw std::runtime_error("the Exact flux belongs to the incompressible models");
   }
+  P->av = c->shock_capturing == SDG_SHOCK_ARTIFICIAL_VISCOSITY;  // SystemControl.cpp:105-108
+  P->avTol = c->empirical_tolerance; P->avFactor = c->artificial_viscosity_factor;
+  if (P->av && !(P->avTol > 0)) throw std::runtime_error("artificial viscosity needs empirical_tolerance > 0");
   P->ph.source = c->source_term;
   P->ph.beta = c->thermal_expansion_coefficient; P->ph.tref = c->reference_temperature;
   if (P->ns() && P->visc == 0) throw std::runtime_error("NS needs BR1 or BR2");
@@ -683,7 +844,8 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
     B.qvol.assign(size_t(B.ne) * nv * nq * d, 0.0);
     B.qface.assign(size_t(B.ne) * nv * nfl, 0.0);
     if (P->ph.source) B.qsrc.assign(size_t(B.ne) * nv * nq, 0.0);
-    if (P->ns() || P->faithful) {
+    if (P->av) B.epsV.assign(size_t(B.ne) * B.ref.nvert, 0.0);
+    if (P->gradientPass()) {
       B.qvg.assign(size_t(B.ne) * nr * nq * d, 0.0);
       B.qfvg.assign(size_t(B.ne) * nr * nfl, 0.0);
       B.rvg.assign(size_t(B.ne) * nr * nb, 0.0);
@@ -697,6 +859,7 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
       B.gc.assign(size_t(B.ne) * nr * nb, 0.0);
     }
   }
+  if (P->av) P->nodeAV.assign(size_t(m->node_count), 0.0);
   buildAdjacency(*P, *m);
   for (Face& F : P->interior) faceGeometry(*P, F, m->node_coordinate);
   for (Face& F : P->boundary) faceGeometry(*P, F, m->node_coordinate);
@@ -851,7 +1014,8 @@ int orc_relative_error(void* h, double* out) {
 // du/dt at the volume points for the current state (one residual evaluation, no update).
 int orc_residual_point(void* h, double* out) {
   orc::Problem& P = *static_cast<orc::Problem*>(h);
-  if (P.ns() || P.faithful) orc::gradientQuadratureAndResidual(P);
+  if (P.av) orc::artificialViscosity(P);
+  if (P.gradientPass()) orc::gradientQuadratureAndResidual(P);
   orc::quadratureAndResidual(P);
   size_t off = 0;
   for (auto& B : P.blocks) {
@@ -864,6 +1028,15 @@ int orc_residual_point(void* h, double* out) {
     }
     off += size_t(B.ne) * nq;
   }
+  return 0;
+}
+
+// Artificial viscosity of the current state at every mesh node (zeros without shock capturing).
+int orc_node_artificial_viscosity(void* h, double* out) {
+  orc::Problem& P = *static_cast<orc::Problem*>(h);
+  if (!P.av) return 0;
+  orc::artificialViscosity(P);
+  for (size_t i = 0; i < P.nodeAV.size(); ++i) out[i] = double(P.nodeAV[i]);
   return 0;
 }
 

@@ -29,6 +29,7 @@ globals().update({name: code for code, name in ERRORS.items()})
 TRIANGLE, QUADRANGLE, HEXAHEDRON = 2, 3, 5
 EULER, NAVIER_STOKES, INCOMPRESSIBLE_EULER, INCOMPRESSIBLE_NAVIER_STOKES = 0, 1, 2, 3
 SOURCE_NONE, SOURCE_BOUSSINESQ = 0, 1
+SHOCK_NONE, ARTIFICIAL_VISCOSITY = 0, 1
 CENTRAL, LAX_FRIEDRICHS, HLLC, ROE, EXACT = 0, 1, 2, 3, 4
 VISCOUS_NONE, BR1, BR2 = 0, 1, 2
 FORWARD_EULER, HEUN_RK2, SSPRK3 = 0, 1, 2
@@ -78,6 +79,9 @@ class SdgConfig(ctypes.Structure):
         ("source_term", c_int32),
         ("thermal_expansion_coefficient", c_double),
         ("reference_temperature", c_double),
+        ("shock_capturing", c_int32),
+        ("empirical_tolerance", c_double),
+        ("artificial_viscosity_factor", c_double),
     ]
 
 
@@ -154,6 +158,7 @@ SIGNATURES = {
                                        c_int32, c_int32, c_int32, _p_int32, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_read_msh": (c_int32, [c_char_p, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_free": (c_int32, [POINTER(SdgGeneratedMesh)]),
+    "sdg_get_node_artificial_viscosity": (c_int32, [c_void_p, _p_double]),
     "sdg_write_raw_binary": (c_int32, [c_void_p, c_char_p]),
     "sdg_read_raw_binary": (c_int32, [c_void_p, c_char_p, c_int32]),
     "sdg_set_graph": (c_int32, [c_void_p, c_int32]),

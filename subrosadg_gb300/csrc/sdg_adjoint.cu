@@ -106,6 +106,7 @@ AdjointState* adjoint(sdg_handle* h) {
       throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (quadrangles P>=2, hexahedra)");
   if (h->nBoundary > 0) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need a mesh without boundary faces (periodic)");
   if (h->ns && h->cfg.viscous_flux != SDG_VISCOUS_BR1) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of BR2 are not built");
+  if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
   if (h->ph.incomp || h->ph.source)
     throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the incompressible models and source terms are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());

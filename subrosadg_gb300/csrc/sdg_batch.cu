@@ -324,13 +324,13 @@ std::vector<Candidate> candidates(const KernelVariant& v, int64_t ne, int optin)
 
 // Tune one kernel of block B; `stage` selects the stage kernel, else the gradient kernel.
 void tuneKernel(sdg_handle* h, DevBlock& B, bool stage, bool retime) {
-  const KernelVariant& v = stage ? B.stageV[h->ns ? 1 : 0] : B.gradV;
+  const KernelVariant& v = stage ? B.stageV[stageSlot(h)] : B.gradV;
   const auto key = std::make_tuple(h->device, v.single, sizeClass(B.ne));
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     auto it = g_tune.find(key);
     if (it != g_tune.end() && !retime) {
-      if (stage) setStageTile(B, h->ns, it->second.first, it->second.second);
+      if (stage) setStageTile(B, stageSlot(h), it->second.first, it->second.second);
       else setGradTile(B, it->second.first, it->second.second);
       return;
     }
@@ -339,7 +339,7 @@ void tuneKernel(sdg_handle* h, DevBlock& B, bool stage, bool retime) {
   float best = 1e30f;
   Candidate pick{stage ? B.epb : B.gepb, stage ? B.threads : B.gthreads};
   for (const Candidate& c : candidates(v, B.ne, optin)) {
-    if (stage) setStageTile(B, h->ns, c.epb, c.threads);
+    if (stage) setStageTile(B, stageSlot(h), c.epb, c.threads);
     else setGradTile(B, c.epb, c.threads);
     const Rec r = stage ? stageProbe(h, B) : gradRec(h, B, 0);
     // repetitions: about 2 ms of work per candidate, at least 3
@@ -348,7 +348,7 @@ void tuneKernel(sdg_handle* h, DevBlock& B, bool stage, bool retime) {
     const float t = timeLaunches({r}, h, reps);
     if (t < best) { best = t; pick = c; }
   }
-  if (stage) setStageTile(B, h->ns, pick.epb, pick.threads);
+  if (stage) setStageTile(B, stageSlot(h), pick.epb, pick.threads);
   else setGradTile(B, pick.epb, pick.threads);
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   g_tune[key] = {pick.epb, pick.threads};
@@ -363,7 +363,7 @@ void autotune(sdg_handle* h, int flags) {
   const int64_t launches = h->launches;
   for (DevBlock& B : h->blocks) {
     tuneKernel(h, B, true, flags & SDG_AUTOTUNE_RETIME);
-    if (h->ns) tuneKernel(h, B, false, flags & SDG_AUTOTUNE_RETIME);
+    if (viscousPath(h)) tuneKernel(h, B, false, flags & SDG_AUTOTUNE_RETIME);
   }
   h->timing = timing;
   h->launches = launches;  // probes are not the solver's launches
@@ -408,11 +408,11 @@ int sdg_set_tile(sdg_handle* h, int32_t block, int32_t epb, int32_t threads, int
       const int tt = v.nodeThreads ? v.threadsFor(e) : t;
       return tt >= 32 && tt <= kMaxThreads && tt % 32 == 0 && v.smem(e, tt) <= size_t(limit);
     };
-    if (!check(B.stageV[h->ns ? 1 : 0], epb, threads) || !check(B.gradV, gepb, gthreads)) {
+    if (!check(B.stageV[stageSlot(h)], epb, threads) || !check(B.gradV, gepb, gthreads)) {
       h->err = "tile outside the kernel's limits (threads 32..512 in whole warps, shared memory)";
       return SDG_ERR_INVALID_ARGUMENT;
     }
-    setStageTile(B, h->ns, epb, threads);
+    setStageTile(B, stageSlot(h), epb, threads);
     setGradTile(B, gepb, gthreads);
     dropGraph(h);
   } catch (const Failure& f) {
@@ -448,6 +448,11 @@ int sdg_batch_create(sdg_handle* const* instances, int32_t count, sdg_batch** ou
   b->device = b->inst[0]->device;
   for (sdg_handle* h : b->inst)
     if (h->hostOnly != b->planOnly || (!h->hostOnly && h->device != b->device)) return SDG_ERR_INVALID_ARGUMENT;
+  for (sdg_handle* h : b->inst)
+    if (h->av) {  // the per-step sensor records have no batched kernels
+      setCreateError("batches of artificial-viscosity instances are not built");
+      return SDG_ERR_UNSUPPORTED;
+    }
   for (size_t i = 0; i < b->inst.size(); ++i)
     for (size_t j = 0; j < i; ++j)
       if (b->inst[i] == b->inst[j]) return SDG_ERR_INVALID_ARGUMENT;  // an instance appears once
@@ -585,7 +590,7 @@ int sdg_batch_autotune(sdg_batch* b, int32_t flags) {
     std::map<const void*, std::pair<sdg_handle*, int>> largest;  // stage kernel -> (instance, block)
     for (sdg_handle* h : b->inst)
       for (size_t k = 0; k < h->blocks.size(); ++k) {
-        const void* fn = h->blocks[k].stageV[h->ns ? 1 : 0].single;
+        const void* fn = h->blocks[k].stageV[stageSlot(h)].single;
         auto it = largest.find(fn);
         if (it == largest.end() || it->second.first->blocks[it->second.second].ne < h->blocks[k].ne)
           largest[fn] = {h, int(k)};
@@ -597,13 +602,13 @@ int sdg_batch_autotune(sdg_batch* b, int32_t flags) {
       h->timing = false;
       const int64_t launches = h->launches;
       tuneKernel(h, B, true, flags & SDG_AUTOTUNE_RETIME);
-      if (h->ns) tuneKernel(h, B, false, flags & SDG_AUTOTUNE_RETIME);
+      if (viscousPath(h)) tuneKernel(h, B, false, flags & SDG_AUTOTUNE_RETIME);
       h->timing = timing;
       h->launches = launches;
       for (sdg_handle* o : b->inst)
         for (DevBlock& C : o->blocks)
-          if (C.stageV[o->ns ? 1 : 0].single == kv.first) {
-            setStageTile(C, o->ns, B.epb, B.threads);
+          if (C.stageV[stageSlot(o)].single == kv.first) {
+            setStageTile(C, stageSlot(o), B.epb, B.threads);
             setGradTile(C, B.gepb, B.gthreads);
             dropGraph(o);
           }

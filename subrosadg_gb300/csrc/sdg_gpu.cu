@@ -345,8 +345,8 @@ void configureKernel(const void* fn, int device) {
   SDG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
 }
 
-void setStageTile(DevBlock& B, bool ns, int epb, int threads) {
-  const KernelVariant& v = B.stageV[ns ? 1 : 0];
+void setStageTile(DevBlock& B, int slot, int epb, int threads) {
+  const KernelVariant& v = B.stageV[slot];
   B.epb = epb;
   B.threads = v.nodeThreads ? v.threadsFor(epb) : threads;
   B.smem = v.smem(B.epb, B.threads);
@@ -363,18 +363,18 @@ void setGradTile(DevBlock& B, int epb, int threads) {
 namespace {
 
 // Kernel variants of a block (element kind, order, affine) and its default tiles.
-void resolveBlock(DevBlock& B, bool ns, bool br2) {
-  for (int visc = 0; visc < 2; ++visc)
-    B.stageV[visc] = B.kind == kTensor ? tensorStageVariant(B.dim, B.n, B.affine != 0, visc != 0)
-                                       : denseStageVariant(B.type, B.p, B.affine != 0, visc != 0);
+void resolveBlock(DevBlock& B, int slot, bool br2) {
+  for (int visc = 0; visc < 3; ++visc)
+    B.stageV[visc] = B.kind == kTensor ? tensorStageVariant(B.dim, B.n, B.affine != 0, visc)
+                                       : denseStageVariant(B.type, B.p, B.affine != 0, visc);
   B.gradV = B.kind == kTensor ? tensorGradVariant(B.dim, B.n, B.affine != 0, br2)
                               : denseGradVariant(B.type, B.p, B.affine != 0);
-  if (!B.stageV[0].valid() || !B.stageV[1].valid() || !B.gradV.valid())
+  if (!B.stageV[0].valid() || !B.stageV[1].valid() || !B.stageV[2].valid() || !B.gradV.valid())
     throw Failure(SDG_ERR_UNSUPPORTED, "unsupported element block (type, order, affine)");
-  const KernelVariant& v = B.stageV[ns ? 1 : 0];
+  const KernelVariant& v = B.stageV[slot];
   B.ustride = ((B.dim + 2) * B.nb + 1) & ~1;
   B.fstride = B.nface * (B.dim + 2) * B.nfq;
-  setStageTile(B, ns, v.epb, v.threads);
+  setStageTile(B, slot, v.epb, v.threads);
   setGradTile(B, B.gradV.epb, B.gradV.threads);
 }
 
@@ -384,14 +384,15 @@ void resolveBlock(DevBlock& B, bool ns, bool br2) {
 Rec stageRec(sdg_handle* h, DevBlock& B) {
   Rec r;
   r.kind = kRecStage; r.cls = 0;
-  const KernelVariant& v = B.stageV[h->ns ? 1 : 0];
+  const KernelVariant& v = B.stageV[stageSlot(h)];
   r.fn = v.single; r.bfn = v.batch;
   r.threads = B.threads; r.epb = B.epb; r.smem = B.smem; r.units = B.grid;
   StageArgs& a = r.sa;
   std::memset(&a, 0, sizeof(a));
   a.face = h->face; a.geom = B.geom; a.tables = B.tables; a.status = h->status;
   a.ne = B.ne; a.faceBase = B.faceBase; a.epb = B.epb;
-  if (h->ns) { a.fluxSrc = h->faceFlux; a.grad = h->grad + B.gradOffset; }
+  if (viscousPath(h)) { a.fluxSrc = h->faceFlux; a.grad = h->grad + B.gradOffset; }
+  if (h->av) { a.av = 1; a.epsV = B.epsV; a.avTab = B.avTab; }
   r.ph = h->ph;
   return r;
 }
@@ -403,7 +404,8 @@ Rec gradRec(sdg_handle* h, DevBlock& B, int which) {
   r.threads = B.gthreads; r.epb = B.gepb; r.smem = B.gsmem; r.units = B.ggrid;
   const double* u = h->state[which] ? h->state[which] + B.stateOffset : nullptr;
   double* g = h->grad ? h->grad + B.gradOffset : nullptr;
-  const int br2 = h->cfg.viscous_flux == SDG_VISCOUS_BR2;
+  // artificial viscosity runs the BR2 layout (own and neighbour traces, the volume gradient)
+  const int br2 = h->cfg.viscous_flux == SDG_VISCOUS_BR2 || h->av;
   if (B.kind == kTensor) {
     r.kind = kRecGradTensor;
     GradArgs& a = r.ga;
@@ -411,6 +413,7 @@ Rec gradRec(sdg_handle* h, DevBlock& B, int which) {
     a.u = u; a.face = h->face; a.faceOther = h->faceOther; a.faceGrad = h->faceGrad; a.grad = g;
     a.geom = B.geom; a.fmetric = B.fmetric; a.tables = B.tables; a.status = h->status;
     a.ne = B.ne; a.faceBase = B.faceBase; a.br2 = br2; a.epb = B.gepb;
+    if (h->av) { a.av = 1; a.epsV = B.epsV; a.avTab = B.avTab; }
   } else {
     r.kind = kRecGradDense;
     DenseGradArgs& a = r.da;
@@ -418,12 +421,15 @@ Rec gradRec(sdg_handle* h, DevBlock& B, int which) {
     a.u = u; a.face = h->face; a.faceOther = h->faceOther; a.faceGrad = h->faceGrad; a.grad = g;
     a.geom = B.geom; a.fmetric = B.fmetric; a.tables = B.tables; a.status = h->status;
     a.ne = B.ne; a.faceBase = B.faceBase; a.br2 = br2; a.epb = B.gepb;
+    if (h->av) { a.av = 1; a.epsV = B.epsV; a.avTab = B.avTab; }
   }
   return r;
 }
 
 namespace {
-bool boundaryOp(int op) { return op == kOpFaceBoundary || op == kOpExchangeBoundary || op == kOpFaceNSBoundary; }
+bool boundaryOp(int op) {
+  return op == kOpFaceBoundary || op == kOpExchangeBoundary || op == kOpFaceNSBoundary || op == kOpFaceAVBoundary;
+}
 }  // namespace
 
 Rec faceRec(sdg_handle* h, int op) {
@@ -469,12 +475,12 @@ namespace {
 // Face fluxes of the state in buffer `which` (whose traces the face buffer holds): NS gradient pass first.
 void emitFluxes(sdg_handle* h, int which, int seq, std::vector<Rec>& out) {
   const auto push = [&](Rec r, int level) { r.seq = seq + level; out.push_back(r); };
-  if (h->ns) {
+  if (viscousPath(h)) {
     if (h->nInterior > 0) push(faceRec(h, kOpExchange), 0);
     if (h->nBoundary > 0) push(faceRec(h, kOpExchangeBoundary), 0);
     for (DevBlock& B : h->blocks) push(gradRec(h, B, which), 1);
-    if (h->nInterior > 0) push(faceRec(h, kOpFaceNS), 2);
-    if (h->nBoundary > 0) push(faceRec(h, kOpFaceNSBoundary), 2);
+    if (h->nInterior > 0) push(faceRec(h, h->av ? kOpFaceAV : kOpFaceNS), 2);
+    if (h->nBoundary > 0) push(faceRec(h, h->av ? kOpFaceAVBoundary : kOpFaceNSBoundary), 2);
   } else {
     if (h->nInterior > 0) push(faceRec(h, kOpFace), 2);
     if (h->nBoundary > 0) push(faceRec(h, kOpFaceBoundary), 2);
@@ -487,6 +493,9 @@ void emitFluxes(sdg_handle* h, int which, int seq, std::vector<Rec>& out) {
 // Stage s: fluxes of its input, then per block volume + lift + update + new traces (TimeIntegration.cpp:326-350).
 void emitStep(sdg_handle* h, double dt, bool relerr, std::vector<Rec>& out) {
   const int ns = h->cfg.time_integration + 1;
+  // artificial viscosity of the step's initial state, once per step (TimeIntegration.cpp:336-338); its
+  // three dependent levels sit before stage 0's (-3, -2, -1)
+  if (h->av) emitArtificialViscosity(h, -3, out);
   for (int s = 0; s < ns; ++s) {
     emitFluxes(h, s == 0 ? 0 : 1, s * 8, out);
     const bool last = s == ns - 1;
@@ -521,6 +530,7 @@ void launchOne(const Rec& r, cudaStream_t s) {
     case kRecGradTensor: p[0] = const_cast<GradArgs*>(&r.ga); break;
     case kRecGradDense: p[0] = const_cast<DenseGradArgs*>(&r.da); break;
     case kRecFace: p[0] = const_cast<FaceArgs*>(&r.fa); break;
+    case kRecAv: p[0] = const_cast<AvArgs*>(&r.av); break;
     default: p[0] = const_cast<RelArgs*>(&r.ra); break;
   }
   if (r.units <= 0) return;
@@ -721,6 +731,15 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     if (c.source_term != SDG_SOURCE_NONE && c.source_term != SDG_SOURCE_BOUSSINESQ)
       throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad source term");
     if (c.time_integration < 0 || c.time_integration > 2) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad time integration");
+    if (c.shock_capturing != SDG_SHOCK_NONE && c.shock_capturing != SDG_SHOCK_ARTIFICIAL_VISCOSITY)
+      throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad shock capturing");
+    if (c.shock_capturing == SDG_SHOCK_ARTIFICIAL_VISCOSITY) {
+      if (!(c.empirical_tolerance > 0) || !(c.artificial_viscosity_factor >= 0))
+        throw Failure(SDG_ERR_INVALID_ARGUMENT, "artificial viscosity needs empirical_tolerance > 0 and factor >= 0");
+      if (c.equation != SDG_COMPRESSIBLE_EULER)
+        throw Failure(SDG_ERR_UNSUPPORTED, "artificial viscosity is built for the compressible Euler equations");
+      h->av = true;
+    }
     if (!(c.specific_heat_ratio > 1.0) || !(c.specific_heat_constant_volume > 0) || !(c.specific_heat_constant_pressure > 0))
       throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad thermodynamic constants");
     if (viscous) {
@@ -834,7 +853,14 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       } else {
         buildDenseTables(B.type, B.p, B.tablesHost, B.phi, B.lsq);
       }
-      resolveBlock(B, c.equation == SDG_COMPRESSIBLE_NS, c.viscous_flux == SDG_VISCOUS_BR2);
+      resolveBlock(B, h->av ? 2 : (viscous ? 1 : 0), c.viscous_flux == SDG_VISCOUS_BR2 || h->av);
+      if (h->av) {
+        const int nvt = typeVertices(b.type);
+        B.vertHost.assign(b.vertex, b.vertex + size_t(B.ne) * nvt);
+        B.innerHost.resize(size_t(B.ne));
+        for (int64_t e = 0; e < B.ne; ++e) B.innerHost[e] = innerRadiusOf(b.type, nodes, b.vertex + e * nvt);
+        buildAvTables(B);
+      }
       B.stateOffset = stateOff; stateOff += size_t(B.ne) * B.ustride;
       B.gradOffset = h->gradCount; h->gradCount += size_t(B.ne) * h->nv * B.dim * B.nb;
       if (!B.affine || B.kind == kDense) {  // outward n|J_f| of each local face (straight faces: constant)
@@ -860,7 +886,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       h->blocks.push_back(std::move(B));
     }
     h->nfq = h->blocks[0].nfq; h->n1d = h->p + 1;
-    for (int op = 0; op < 6; ++op) h->faceV[op] = facePointVariant(op, h->dim, c.convective_flux);
+    for (int op = 0; op < kFaceOps; ++op) h->faceV[op] = facePointVariant(op, h->dim, c.convective_flux);
     h->volumePoints = int64_t(pointOff);
     h->stateCount = stateOff;
     h->faceCount = size_t(faceSlots) * h->nv * h->nfq;
@@ -948,7 +974,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     h->hostOnly = false;
     SDG_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
     for (DevBlock& B : h->blocks) {
-      for (const KernelVariant* v : {&B.stageV[0], &B.stageV[1], &B.gradV}) {
+      for (const KernelVariant* v : {&B.stageV[0], &B.stageV[1], &B.stageV[2], &B.gradV}) {
         configureKernel(v->single, device);
         configureKernel(v->batch, device);
       }
@@ -961,7 +987,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     SDG_CUDA(cudaMemsetAsync(h->state[1], 0, h->stateCount * 8, h->stream));
     h->face = devAlloc<double>(h->faceCount);
     SDG_CUDA(cudaMemsetAsync(h->face, 0, h->faceCount * 8, h->stream));
-    if (h->ns) {
+    if (viscousPath(h)) {
       h->faceOther = devAlloc<double>(h->faceCount);
       h->faceGrad = devAlloc<double>(h->faceCount * h->dim);
       h->faceFlux = devAlloc<double>(h->faceCount);
@@ -994,6 +1020,17 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         B.phiDev = devAlloc<double>(B.phi.size()); upload(B.phiDev, B.phi, h->stream);
         B.lsqDev = devAlloc<double>(B.lsq.size()); upload(B.lsqDev, B.lsq, h->stream);
       }
+      if (h->av) {
+        B.vertDev = devAlloc<int32_t>(B.vertHost.size()); upload(B.vertDev, B.vertHost, h->stream);
+        B.innerDev = devAlloc<double>(B.innerHost.size()); upload(B.innerDev, B.innerHost, h->stream);
+        B.avTab = devAlloc<double>(B.avTabHost.size()); upload(B.avTab, B.avTabHost, h->stream);
+        B.epsV = devAlloc<double>(B.vertHost.size());
+        SDG_CUDA(cudaMemsetAsync(B.epsV, 0, B.vertHost.size() * 8, h->stream));
+      }
+    }
+    if (h->av) {
+      h->nodeAV = devAlloc<double>(size_t(h->nodeCount));
+      SDG_CUDA(cudaMemsetAsync(h->nodeAV, 0, size_t(h->nodeCount) * 8, h->stream));
     }
     SDG_CUDA(cudaStreamSynchronize(h->stream));
   } catch (const Failure& f) {
@@ -1019,7 +1056,9 @@ int sdg_destroy(sdg_handle* h) {
   destroyAdjoint(h);
   for (DevBlock& B : h->blocks) {
     cudaFree(B.geom); cudaFree(B.tables); cudaFree(B.minedge); cudaFree(B.phiDev); cudaFree(B.lsqDev); cudaFree(B.fmetric);
+    cudaFree(B.vertDev); cudaFree(B.innerDev); cudaFree(B.epsV); cudaFree(B.avTab);
   }
+  cudaFree(h->nodeAV);
   cudaFree(h->state[0]); cudaFree(h->state[1]); cudaFree(h->face); cudaFree(h->fconn); cudaFree(h->fgeo);
   cudaFree(h->bconn); cudaFree(h->bgeo); cudaFree(h->ghost); cudaFree(h->scratch); cudaFree(h->relPart);
   cudaFree(h->relOut); cudaFree(h->dtPart); cudaFree(h->status);
@@ -1263,6 +1302,7 @@ int sdg_residual_point(sdg_handle* h, double* rate) {
   // the face buffer holds the traces of state[0]: compute fluxes, then the rate without an update,
   // then restore the traces (the flux pass overwrote them)
   std::vector<Rec> recs;
+  if (h->av) emitArtificialViscosity(h, -3, recs);  // the state's own artificial viscosity
   emitFluxes(h, 0, 0, recs);
   for (DevBlock& B : h->blocks) {
     Rec r = stageRec(h, B);

@@ -53,7 +53,7 @@ struct DevBlock {
   double* minedge = nullptr;
   double* phiDev = nullptr;
   double* lsqDev = nullptr;
-  KernelVariant stageV[2];         // stage kernels: [0] Euler, [1] viscous
+  KernelVariant stageV[3];         // stage kernels: [0] Euler, [1] Navier-Stokes, [2] artificial viscosity
   KernelVariant gradV;             // gradient kernel (Navier-Stokes)
   int epb = 0, threads = 0;        // stage tile: elements per CTA, threads per CTA
   int64_t grid = 0;                // stage tiles (CTAs of a one-instance launch)
@@ -65,10 +65,18 @@ struct DevBlock {
   double* fmetric = nullptr;
   size_t gradOffset = 0;           // doubles into the gradient buffer
   int64_t relOffset = 0;           // first relative-error partial slot (one slot per possible tile)
+  // artificial viscosity: element vertices (mesh nodes), inner radius, vertex values, tables
+  std::vector<int32_t> vertHost;   // [e][nvert]
+  std::vector<double> innerHost;   // [e]
+  std::vector<double> avTabHost;
+  int32_t* vertDev = nullptr;
+  double* innerDev = nullptr;
+  double* epsV = nullptr;          // [e][nvert]
+  double* avTab = nullptr;
 };
 
 // One kernel launch of a step: the kernel pair, its one-instance launch shape and its arguments.
-enum RecKind { kRecStage = 0, kRecGradTensor = 1, kRecGradDense = 2, kRecFace = 3, kRecRelerr = 4 };
+enum RecKind { kRecStage = 0, kRecGradTensor = 1, kRecGradDense = 2, kRecFace = 3, kRecRelerr = 4, kRecAv = 5 };
 struct Rec {
   int kind = 0;
   int cls = 0;                     // timing class: 0 element, 1 interior face, 2 boundary face, 3 reduction, 4 gradient
@@ -84,6 +92,7 @@ struct Rec {
   DenseGradArgs da;
   FaceArgs fa;
   RelArgs ra;
+  AvArgs av;
 };
 
 // Sets the dynamic shared memory limit of a kernel to the device's opt-in maximum (once per device).
@@ -100,12 +109,14 @@ struct sdg_handle {
   sdg::Phys ph{};
   int dim = 2, nv = 4, p = 1;
   std::vector<sdg::DevBlock> blocks;
-  sdg::KernelVariant faceV[6];     // face-point kernels per FaceOp
+  sdg::KernelVariant faceV[sdg::kFaceOps];  // face-point kernels per FaceOp
   double* state[2] = {nullptr, nullptr};
   size_t stateCount = 0;
   double* face = nullptr;
   size_t faceCount = 0;
   bool ns = false;                 // Navier-Stokes: gradient pass + viscous fluxes
+  bool av = false;                 // artificial viscosity: gradient pass + artificial viscous fluxes
+  double* nodeAV = nullptr;        // artificial viscosity per mesh node [nodeCount]
   double* faceOther = nullptr;     // NS: neighbour traces
   double* faceGrad = nullptr;      // NS: gradient traces
   double* faceFlux = nullptr;      // NS: face fluxes
@@ -149,7 +160,7 @@ void runRecs(sdg_handle* h, const std::vector<Rec>& recs, cudaStream_t stream);
 Rec stageRec(sdg_handle* h, DevBlock& B);
 Rec gradRec(sdg_handle* h, DevBlock& B, int which);
 // Tile shapes.
-void setStageTile(DevBlock& B, bool ns, int epb, int threads);
+void setStageTile(DevBlock& B, int slot, int epb, int threads);  // slot: stageV index
 void setGradTile(DevBlock& B, int epb, int threads);
 void dropGraph(sdg_handle* h);
 void traceAll(sdg_handle* h, int which);
@@ -165,4 +176,12 @@ void pointsToStateBuffer(sdg_handle* h, const double* pts, double* st);
 void stateToPointsBuffer(sdg_handle* h, const double* st, double* pts);
 // Tangent-linear / adjoint resources of a handle (sdg_adjoint.cu), released with the handle.
 void destroyAdjoint(sdg_handle* h);
+// The gradient pass and viscous-layout buffers run for Navier-Stokes and for artificial viscosity.
+inline bool viscousPath(const sdg_handle* h) { return h->ns || h->av; }
+// The stage-kernel slot of a handle (DevBlock::stageV).
+inline int stageSlot(const sdg_handle* h) { return h->av ? 2 : (h->ns ? 1 : 0); }
+// Artificial viscosity (sdg_av.cu): inner radius of an element, the block tables, the per-step records.
+double innerRadiusOf(int type, const double* nodes, const int32_t* vertices);
+void buildAvTables(DevBlock& B);
+void emitArtificialViscosity(sdg_handle* h, int seq, std::vector<Rec>& out);
 }  // namespace sdg

@@ -90,8 +90,37 @@ struct StageArgs {
   int doTrace;            // write new face traces
   int doVolume;           // evaluate the residual (0: trace-only pass)
   const double* fluxSrc;  // face-flux slots to lift (null: the face buffer itself, the Euler layout)
-  const double* grad;     // Navier-Stokes: total gradient at the nodes [e][nv*d][NB]
+  const double* grad;     // Navier-Stokes: total gradient at the nodes [e][nv*d][NB]; artificial viscosity:
+                          // tensor blocks eps times the volume gradient at the nodes, dense blocks the modal
+                          // volume-gradient coefficients
   int epb;                // elements per CTA tile (tile t covers elements [t*epb, t*epb + epb))
+  int av;                 // artificial viscosity (the viscous variant with the flux eps grad U)
+  const double* epsV;     // artificial viscosity at the element vertices [e][nvert]
+  const double* avTab;    // artificial-viscosity tables of the block (avTableLayout)
+};
+
+// Artificial-viscosity tables of a block (doubles):
+//   tensor: x[N] (Gauss nodes on [-1,1]) | w[N] | phi1[N][N] (lob_m(x_i)) | phi1inv[N][N]
+//   dense : phi[NQ][NB] | high[NB] (1 for the modes of degree P) | w[NQ] | nodal[NQ][NVERT] | nodalf[NFP][NVERT]
+// nodal / nodalf: the first-order nodal (vertex) basis at the volume and face points.
+inline __host__ __device__ int avDenseNodalOffset(int nb, int nq) { return nq * nb + nb + nq; }
+inline __host__ __device__ int avDenseNodalFaceOffset(int nb, int nq, int nvert) {
+  return avDenseNodalOffset(nb, nq) + nq * nvert;
+}
+
+// Per-step artificial viscosity (SpatialDiscrete.cpp:37-124): kind 0 zeroes the node field, 1 / 2 run the
+// sensor of a tensor / dense block (max into the nodes), 3 gathers the vertex values of a block.
+struct AvArgs {
+  const double* u;        // block state
+  const double* geom;     // block geometry (the stage kernel's layout)
+  const int* vert;        // [e][nvert] mesh node of each vertex
+  const double* inner;    // [e] inner radius
+  const double* tab;      // avTableLayout
+  double* nodeAV;         // [nodes]
+  double* epsV;           // [e][nvert]
+  int64_t ne, nodes;
+  int kind, dim, n, nb, nq, nvert, ustride, affine, p, pad;
+  double s0, kappa, factor;
 };
 
 template <int DIM, int N>
@@ -144,7 +173,7 @@ __device__ __forceinline__ uint64_t* tensorStageBarrier(int epb) {
 // One tile of a stage: the CTA's mbarrier is initialised, `parity` is the phase this tile's copies complete;
 // `loadTables` copies the operator tables (identical for every tile of a (type, order) variant).  Returns
 // false after a timed-out copy (status flagged, every thread returns together).
-template <int DIM, int N, bool AFFINE, bool VISC>
+template <int DIM, int N, bool AFFINE, int VISC>
 __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& ph, int64_t tile, uint32_t parity,
                                                 bool loadTables) {
   using S = TensorShape<DIM, N>;
@@ -209,13 +238,17 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
       makeState<DIM>(s, U, ph);
       const double ep = energyFluxFactor(s, ph);
       double tau[DIM][DIM], q[DIM];
-      if constexpr (VISC) {
-        // viscous flux from the total gradient at the node (ViscousFlux.cpp:58-103)
-        double g[NV * DIM];
+      double gv[VISC ? NV * DIM : 1];
+      if constexpr (VISC != 0) {
+        // Navier-Stokes: viscous flux from the total gradient at the node (ViscousFlux.cpp:58-103);
+        // artificial viscosity: the gradient kernel stored eps times the volume gradient, the flux itself
+        // (ViscousFlux.cpp:105-113)
 #pragma unroll
-        for (int c = 0; c < NV * DIM; ++c) g[c] = a.grad[(e * NV * DIM + c) * NB + node];
+        for (int c = 0; c < NV * DIM; ++c) gv[c] = a.grad[(e * NV * DIM + c) * NB + node];
+      }
+      if constexpr (VISC == 1) {
         PrimGrad<DIM> pg;
-        primitiveGradient<DIM>(g, s.u, s.ir, s.E * s.ir, ph, pg);
+        primitiveGradient<DIM>(gv, s.u, s.ir, s.E * s.ir, ph, pg);
         double u2 = 0.0;
 #pragma unroll
         for (int k = 0; k < DIM; ++k) u2 = fma(s.u[k], s.u[k], u2);
@@ -230,15 +263,24 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
 #pragma unroll
         for (int k = 0; k < DIM; ++k) {
           double x = fma(s.m[k], vb, ja[b][k] * s.p);
-          if constexpr (VISC) {
+          if constexpr (VISC == 1) {
 #pragma unroll
             for (int c = 0; c < DIM; ++c) x = fma(-ja[b][c], tau[c][k], x);
           }
           G[(1 + k) * NB] = x;
         }
         double xe = ep * vb;
-        if constexpr (VISC) xe -= dotn<DIM>(q, ja[b]);
+        if constexpr (VISC == 1) xe -= dotn<DIM>(q, ja[b]);
         G[(NV - 1) * NB] = xe;
+        if constexpr (VISC == 2) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            double x = G[v * NB];
+#pragma unroll
+            for (int c = 0; c < DIM; ++c) x = fma(-ja[b][c], gv[v * DIM + c], x);
+            G[v * NB] = x;
+          }
+        }
       }
     }
     __syncthreads();
@@ -387,7 +429,7 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
 }
 
 // One CTA per tile.
-template <int DIM, int N, bool AFFINE, bool VISC>
+template <int DIM, int N, bool AFFINE, int VISC>
 __global__ void __launch_bounds__(kMaxTileThreads) tensorStageKernel(StageArgs a, Phys ph) {
   if (threadIdx.x == 0) mbarInit(tensorStageBarrier<DIM, N>(a.epb), 1);
   tensorStageTile<DIM, N, AFFINE, VISC>(a, ph, blockIdx.x, 0u, true);
@@ -396,7 +438,7 @@ __global__ void __launch_bounds__(kMaxTileThreads) tensorStageKernel(StageArgs a
 // Persistent batched launch: CTA c runs work items c, c + gridDim.x, ... of a list of (argument set, tile)
 // pairs that spans many independent instances of one (type, order) variant.  The barrier is initialised
 // once and its phase alternates per tile; the tables are loaded once per CTA.
-template <int DIM, int N, bool AFFINE, bool VISC>
+template <int DIM, int N, bool AFFINE, int VISC>
 __global__ void __launch_bounds__(kMaxTileThreads)
     tensorStageBatchKernel(const StageArgs* __restrict__ args, const Phys* __restrict__ phys,
                            const int2* __restrict__ items, int nitems, int epb) {
@@ -428,7 +470,8 @@ struct FaceArgs {
 };
 
 enum FaceOp { kOpFace = 0, kOpFaceBoundary = 1, kOpExchange = 2, kOpExchangeBoundary = 3, kOpFaceNS = 4,
-              kOpFaceNSBoundary = 5 };
+              kOpFaceNSBoundary = 5, kOpFaceAV = 6, kOpFaceAVBoundary = 7 };
+constexpr int kFaceOps = 8;
 
 // Point of the right face that coincides with point j of the left face (rotation of the right face's
 // vertex list; SimulationControl.cpp:381-523 permutations).

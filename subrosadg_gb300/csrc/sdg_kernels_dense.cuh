@@ -185,7 +185,7 @@ __device__ __forceinline__ uint64_t* denseStageBarrier(int epb) {
 
 // Dense stage tile (2D), a.epb elements per CTA, any whole number of warps.  geometry: affine [e][5] =
 // (|J| dxi_b/dx_a row-major, 1/|J|); bilinear: [e][NQ][5] followed by the element's M^-1 [NB][NB].
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC>
 __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& ph, int64_t tile, uint32_t parity,
                                                bool loadTables) {
   using S = DenseShape<NB, NQ, NFQ, NF>;
@@ -250,7 +250,8 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
       // Boussinesq buoyancy S |J| at the point, kept in the new-state buffer until the residual pass
       if (ph.source) sN[le * NV * NB + q] = st.r * ph.beta * (temperatureOf(st, ph) - ph.tref) / g[4];
       double tau[2][2] = {{0.0, 0.0}, {0.0, 0.0}}, qh[2] = {0.0, 0.0};
-      if constexpr (VISC) {
+      double avf[VISC == 2 ? NV * 2 : 1];
+      if constexpr (VISC != 0) {
         // gradient at the point from the element's modal gradient coefficients [nv*2][NB]
         double g[NV * 2];
         const double* gc = a.grad + e * NV * 2 * NB;
@@ -261,11 +262,21 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
           for (int b = 0; b < NB; ++b) acc = fma(phi[q * NB + b], gc[c * NB + b], acc);
           g[c] = acc;
         }
-        PrimGrad<2> pg;
-        primitiveGradient<2>(g, st.u, st.ir, st.E * st.ir, ph, pg);
-        const double u2 = fma(st.u[0], st.u[0], st.u[1] * st.u[1]);
-        viscousTensor<2>(pg, st.u, fma(ph.incomp ? 0.0 : -0.5, u2, st.E * st.ir) * ph.inv_cv, ph,
-                         tau, qh);
+        if constexpr (VISC == 2) {
+          // artificial viscous flux eps(x_q) grad U (ViscousFlux.cpp:105-113), eps from the vertex values
+          const double* nod = a.avTab + avDenseNodalOffset(NB, NQ) + q * NF;
+          double eps = 0.0;
+#pragma unroll
+          for (int v = 0; v < NF; ++v) eps = fma(nod[v], a.epsV[e * NF + v], eps);
+#pragma unroll
+          for (int c = 0; c < NV * 2; ++c) avf[c] = eps * g[c];
+        } else {
+          PrimGrad<2> pg;
+          primitiveGradient<2>(g, st.u, st.ir, st.E * st.ir, ph, pg);
+          const double u2 = fma(st.u[0], st.u[0], st.u[1] * st.u[1]);
+          viscousTensor<2>(pg, st.u, fma(ph.incomp ? 0.0 : -0.5, u2, st.E * st.ir) * ph.inv_cv, ph,
+                           tau, qh);
+        }
       }
 #pragma unroll
       for (int b = 0; b < 2; ++b) {
@@ -275,6 +286,11 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
         Q[NQ] = fma(-ja[b][1], tau[1][0], fma(-ja[b][0], tau[0][0], fma(st.m[0], vb, ja[b][0] * st.p)));
         Q[2 * NQ] = fma(-ja[b][1], tau[1][1], fma(-ja[b][0], tau[0][1], fma(st.m[1], vb, ja[b][1] * st.p)));
         Q[3 * NQ] = ep * vb - dotn<2>(qh, ja[b]);
+        if constexpr (VISC == 2) {
+#pragma unroll
+          for (int v = 0; v < NV; ++v)
+            Q[v * NQ] = fma(-ja[b][1], avf[v * 2 + 1], fma(-ja[b][0], avf[v * 2 + 0], Q[v * NQ]));
+        }
       }
     }
     __syncthreads();
@@ -389,13 +405,13 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
   return true;
 }
 
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC>
 __global__ void __launch_bounds__(kMaxTileThreads) denseStageKernel(StageArgs a, Phys ph) {
   if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF>(a.epb), 1);
   denseStageTile<NB, NQ, NFQ, NF, AFFINE, VISC>(a, ph, blockIdx.x, 0u, true);
 }
 
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC>
 __global__ void __launch_bounds__(kMaxTileThreads)
     denseStageBatchKernel(const StageArgs* __restrict__ args, const Phys* __restrict__ phys,
                           const int2* __restrict__ items, int nitems, int epb) {
@@ -450,7 +466,21 @@ struct DenseGradArgs {
   int64_t ne, faceBase;
   int br2;
   int epb;
+  int av;                   // artificial viscosity: grad = the volume-gradient coefficients, traces eps times
+                            // the volume-gradient trace, no lifts
+  const double* epsV;       // [e][nvert]
+  const double* avTab;      // dense artificial-viscosity table
 };
+
+// Artificial viscosity at face point fj of element e of a dense block (nodal_adjacency_value_ x vertex values).
+template <int NB, int NQ, int NVERT>
+__device__ __forceinline__ double denseFaceEps(const DenseGradArgs& a, int64_t e, int fj) {
+  const double* nf = a.avTab + avDenseNodalFaceOffset(NB, NQ, NVERT) + fj * NVERT;
+  double s = 0.0;
+#pragma unroll
+  for (int v = 0; v < NVERT; ++v) s = fma(nf[v], a.epsV[e * NVERT + v], s);
+  return s;
+}
 
 // Affine elements: with M = |J| M_ref and constant metric, the gradient coefficients are
 //   w_tot(v,k) = (1/|J|) [ sum_f nF_f[k] E_f U+_f(v) - sum_b |J| dxi_b/dx_k D_b u(v) ]
@@ -535,8 +565,9 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
       jmp0 = fma(n0, ej, jmp0); jmp1 = fma(n1, ej, jmp1);
     }
     const double g0 = jinv * tot0, g1 = jinv * tot1;
-    a.grad[(e * NR + v * 2 + 0) * NB + i] = g0;
-    a.grad[(e * NR + v * 2 + 1) * NB + i] = g1;
+    // artificial viscosity keeps the volume-gradient coefficients (ViscousFluxEnum::None gradient)
+    a.grad[(e * NR + v * 2 + 0) * NB + i] = a.av ? jinv * (tot0 - jmp0) : g0;
+    a.grad[(e * NR + v * 2 + 1) * NB + i] = a.av ? jinv * (tot1 - jmp1) : g1;
     sW[(le * NR + v * 2 + 0) * NB + i] = a.br2 ? jinv * (tot0 - jmp0) : g0;
     sW[(le * NR + v * 2 + 1) * NB + i] = a.br2 ? jinv * (tot1 - jmp1) : g1;
   }
@@ -555,7 +586,11 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
       acc0 = fma(phif[fj * NB + b], w0[b], acc0);
       acc1 = fma(phif[fj * NB + b], w1[b], acc1);
     }
-    if (a.br2) {
+    if (a.av) {
+      const double eps = denseFaceEps<NB, NQ, NF>(a, e, fj);
+      acc0 *= eps;
+      acc1 *= eps;
+    } else if (a.br2) {
       const double* O = sO + le * FS + (f * NV + v) * NFQ;
       const double* S = sS + le * FS + (f * NV + v) * NFQ;
       const double* L = lmod + (f * NFQ + j) * NFQ;
@@ -675,7 +710,7 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
       t = fma(minv[i * NB + k], sRt[(le * NR + c) * NB + k], t);
       w = fma(minv[i * NB + k], sRv[(le * NR + c) * NB + k], w);
     }
-    a.grad[(e * NR + c) * NB + i] = sc * t;
+    a.grad[(e * NR + c) * NB + i] = a.av ? sc * w : sc * t;
     sRf[(le * NR + c) * NB + i] = sc * w;  // staged: BR2 volume coefficients
   }
   __syncthreads();
@@ -685,18 +720,21 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
     if (!a.br2) sRt[le * NR * NB + r] = a.grad[((e0 + le) * NR) * NB + r];
   }
   __syncthreads();
-  if (!a.br2) {
-    // BR1 face gradient traces: trace of the total gradient
+  if (!a.br2 || a.av) {
+    // BR1 face gradient traces: trace of the total gradient; artificial viscosity: eps times the trace of
+    // the volume gradient
+    const double* src = a.av ? sRv : sRt;
     for (int idx = tid; idx < ecount * NFP; idx += blockDim.x) {
       const int le = idx / NFP, fj = idx - le * NFP;
       const int f = fj / NFQ, j = fj - f * NFQ;
       double* out = a.faceGrad + (a.faceBase + (e0 + le) * NF + f) * NR * NFQ + j;
+      const double eps = a.av ? denseFaceEps<NB, NQ, NF>(a, e0 + le, fj) : 1.0;
 #pragma unroll
       for (int c = 0; c < NR; ++c) {
         double acc = 0.0;
 #pragma unroll
-        for (int b = 0; b < NB; ++b) acc = fma(phif[fj * NB + b], sRt[(le * NR + c) * NB + b], acc);
-        out[c * NFQ] = acc;
+        for (int b = 0; b < NB; ++b) acc = fma(phif[fj * NB + b], src[(le * NR + c) * NB + b], acc);
+        out[c * NFQ] = eps * acc;
       }
     }
     return true;

@@ -34,6 +34,10 @@ struct GradArgs {
   int64_t ne, faceBase;
   int br2;
   int epb;                  // elements per CTA tile
+  int av;                   // artificial viscosity (BR2 layout): grad = eps times the volume gradient, traces
+                            // eps times the volume-gradient trace, no lifts
+  const double* epsV;       // [e][nvert] artificial viscosity at the vertices
+  const double* avTab;      // tensor artificial-viscosity table (x[N] first)
 };
 
 // Exchange of traces across interior faces: each side receives the other side's trace at its own points.
@@ -98,6 +102,27 @@ __device__ __forceinline__ void exchangeBoundaryPoint(const FaceArgs& a, int64_t
   ub[DIM + 1] = energyOfComp<DIM>(b, a.ph);
 #pragma unroll
   for (int v = 0; v < NV; ++v) a.other[L + v * nfq] = 2.0 * ub[v] - ul[v];
+}
+
+// First-order nodal (vertex) basis of a quadrangle / hexahedron at reference point X (gmsh vertex order:
+// (-1,-1), (1,-1), (1,1), (-1,1), then the same at z = +1), the artificial viscosity's interpolation
+// (BasisFunction.cpp:200-208 nodal_value_).
+template <int DIM>
+__device__ __forceinline__ double vertexWeight(int v, const double* X) {
+  const double sx = (v & 3) == 1 || (v & 3) == 2 ? 1.0 : -1.0;
+  const double sy = (v & 3) >= 2 ? 1.0 : -1.0;
+  double w = 0.25 * (1.0 + sx * X[0]) * (1.0 + sy * X[1]);
+  if constexpr (DIM == 3) w *= 0.5 * (1.0 + (v >= 4 ? 1.0 : -1.0) * X[2]);
+  return w;
+}
+
+template <int DIM>
+__device__ __forceinline__ double vertexInterp(const double* epsV, const double* X) {
+  constexpr int NVERT = DIM == 2 ? 4 : 8;
+  double s = 0.0;
+#pragma unroll
+  for (int v = 0; v < NVERT; ++v) s = fma(vertexWeight<DIM>(v, X), epsV[v], s);
+  return s;
 }
 
 template <int DIM, int N, bool AFFINE, bool BR2>
@@ -196,6 +221,15 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
     }
   }
   __syncthreads();
+  double epsNode = 0.0;
+  if constexpr (BR2) {
+    if (a.av && active) {
+      double X[DIM];
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) X[b] = a.avTab[ax[b]];
+      epsNode = vertexInterp<DIM>(a.epsV + e * (DIM == 2 ? 4 : 8), X);
+    }
+  }
   if (active) {
     double nF[DIM][2][DIM];  // outward n|J_f| of the faces (axis b, end)
 #pragma unroll
@@ -253,7 +287,8 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
         const double gt = tot[k] * jinv;
         sGt[(le * NV * DIM + v * DIM + k) * NB + node] = gt;
         if constexpr (BR2) sGv[(le * NV * DIM + v * DIM + k) * NB + node] = vol[k] * jinv;
-        a.grad[(e * NV * DIM + v * DIM + k) * NB + node] = gt;
+        // artificial viscosity: the node's eps times the volume gradient (SpatialDiscrete.cpp:211-250)
+        a.grad[(e * NV * DIM + v * DIM + k) * NB + node] = BR2 && a.av ? epsNode * (vol[k] * jinv) : gt;
       }
     }
   }
@@ -270,7 +305,15 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
     const int64_t ee = e0 + te;
     double* out = a.faceGrad + (a.faceBase + ee * NF + f) * NV * DIM * NFQ + j;
     const double* src = BR2 ? sGv : sGt;
-    double nf[DIM], cl = 0.0;
+    double nf[DIM], cl = 0.0, epsF = 1.0;
+    if constexpr (BR2) {
+      if (a.av) {  // eps at the face point (nodal_adjacency_value_ of the parent, SpatialDiscrete.cpp:528-631)
+        double X[DIM];
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) X[c] = c == axis ? (en ? 1.0 : -1.0) : a.avTab[axisIndex<DIM, N>(base, c)];
+        epsF = vertexInterp<DIM>(a.epsV + ee * (DIM == 2 ? 4 : 8), X);
+      }
+    }
     if constexpr (BR2) {
       // lift trace factor sum_a l_a(end)^2 / (w_a |J|_a) and the face's n|J_f|
 #pragma unroll
@@ -293,7 +336,7 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
         double acc = 0.0;
 #pragma unroll
         for (int q = 0; q < N; ++q) acc = fma(coef[q], gsrc[q * st], acc);
-        if constexpr (BR2) acc = fma(cl * nf[k], jump, acc);
+        if constexpr (BR2) acc = a.av ? epsF * acc : fma(cl * nf[k], jump, acc);
         out[(v * DIM + k) * NFQ] = acc;
       }
     }
@@ -433,6 +476,90 @@ __device__ __forceinline__ void faceNSBoundaryPoint(const FaceArgs& a, int64_t t
   for (int v = 0; v < NV; ++v) a.faceFlux[L + v * nfq] = fma(-0.5, fl[v] + fb[v], h[v]) * area;
 }
 
+// Interior-face Euler flux with artificial viscosity: Riemann flux minus the central artificial viscous flux
+// 1/2 (eps_L G_L + eps_R G_R).n, the gradient traces already scaled by each side's eps at the point
+// (SpatialDiscrete.cpp:685-734, ViscousFlux.cpp:183-197).
+template <int DIM, int FLUX>
+__device__ __forceinline__ void faceAVPoint(const FaceArgs& a, int64_t t) {
+  constexpr int NV = DIM + 2;
+  const int n1d = a.n1d;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
+  const int jr = rightPoint<DIM>(j, rot, n1d);
+  const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
+  const int64_t LG = int64_t(sl) * NV * DIM * nfq + j, RG = int64_t(sr) * NV * DIM * nfq + jr;
+  const Phys& ph = a.ph;
+  double ul[NV], ur[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) { ul[v] = a.face[L + v * nfq]; ur[v] = a.face[R + v * nfq]; }
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double area = a.fgeo[f * 4 + 3];
+  State<DIM> l, r;
+  makeState<DIM>(l, ul, ph);
+  makeState<DIM>(r, ur, ph);
+  double h[NV];
+  convectiveFlux<DIM, FLUX>(l, r, n, ph, h);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    double gl = 0.0, gr = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      gl = fma(a.faceGrad[LG + (v * DIM + k) * nfq], n[k], gl);
+      gr = fma(a.faceGrad[RG + (v * DIM + k) * nfq], n[k], gr);
+    }
+    const double x = fma(-0.5, gl + gr, h[v]) * area;
+    a.faceFlux[L + v * nfq] = x;
+    a.faceFlux[R + v * nfq] = -x;
+  }
+}
+
+// Boundary-face Euler flux with artificial viscosity: normal flux of the boundary state minus the interior
+// side's artificial viscous flux eps_L G_L.n (SpatialDiscrete.cpp:815-834).
+template <int DIM>
+__device__ __forceinline__ void faceAVBoundaryPoint(const FaceArgs& a, int64_t t) {
+  constexpr int NV = DIM + 2;
+  const int n1d = a.n1d;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
+  const int64_t L = int64_t(sl) * NV * nfq + j, LG = int64_t(sl) * NV * DIM * nfq + j;
+  const Phys& ph = a.ph;
+  double ul[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) ul[v] = a.face[L + v * nfq];
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double area = a.fgeo[f * 4 + 3];
+  State<DIM> s;
+  makeState<DIM>(s, ul, ph);
+  Comp<DIM> l, g, b;
+  compFromState<DIM>(s, l, ph);
+  const double* gp = a.ghost + (f * nfq + j) * (DIM + 3);
+  g.r = gp[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) g.u[k] = gp[1 + k];
+  g.e = gp[DIM + 1];
+  g.p = gp[DIM + 2];
+  boundaryState<DIM>(bc, n, l, g, ph, b);
+  double h[NV];
+  normalFluxComp<DIM>(b, n, h, ph);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    double gl = 0.0;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) gl = fma(a.faceGrad[LG + (v * DIM + k) * nfq], n[k], gl);
+    a.faceFlux[L + v * nfq] = (h[v] - gl) * area;
+  }
+}
+
 // ---- face-point kernels ----------------------------------------------------------------------------
 template <int OP, int DIM, int FLUX>
 __device__ __forceinline__ void facePointOp(const FaceArgs& a, int64_t t) {
@@ -441,7 +568,9 @@ __device__ __forceinline__ void facePointOp(const FaceArgs& a, int64_t t) {
   else if constexpr (OP == kOpExchange) exchangePoint<DIM>(a, t);
   else if constexpr (OP == kOpExchangeBoundary) exchangeBoundaryPoint<DIM>(a, t);
   else if constexpr (OP == kOpFaceNS) faceNSPoint<DIM, FLUX>(a, t);
-  else faceNSBoundaryPoint<DIM>(a, t);
+  else if constexpr (OP == kOpFaceNSBoundary) faceNSBoundaryPoint<DIM>(a, t);
+  else if constexpr (OP == kOpFaceAV) faceAVPoint<DIM, FLUX>(a, t);
+  else faceAVBoundaryPoint<DIM>(a, t);
 }
 
 constexpr int kFaceThreads = 256;

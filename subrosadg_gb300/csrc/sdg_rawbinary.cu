@@ -8,7 +8,7 @@
 //                coefficients, column-major (d+2)*d x Nb (row v*d + k)
 //   per boundary face: the parent element's coefficients (and gradient), in this library's boundary-face
 //                order (the reference's is gmsh/unordered_map order)
-//   per mesh node: the artificial viscosity (zero: no shock capturing in this path)
+//   per mesh node: the artificial viscosity of the current state (zero without shock capturing)
 // libzstd is loaded at run time (libzstd.so.1, its public C API); without it the calls return
 // SDG_ERR_UNSUPPORTED.
 #include <dlfcn.h>
@@ -144,7 +144,13 @@ int sdg_write_raw_binary(sdg_handle* h, const char* path) {
         payload.insert(payload.end(), g, g + size_t(nr) * B.nb);
       }
     }
-    payload.insert(payload.end(), size_t(h->nodeCount), 0.0);  // node artificial viscosity
+    // node artificial viscosity (the current state's; zeros without shock capturing)
+    const size_t nodeStart = payload.size();
+    payload.insert(payload.end(), size_t(h->nodeCount), 0.0);
+    if (h->av) {
+      const int rc2 = sdg_get_node_artificial_viscosity(h, payload.data() + nodeStart);
+      if (rc2 != SDG_OK) return rc2;
+    }
     const size_t raw = payload.size() * sizeof(double);
     const size_t bound = z.compressBound(raw);
     std::vector<char> packed(bound);

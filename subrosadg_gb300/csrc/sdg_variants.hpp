@@ -26,9 +26,9 @@ struct KernelVariant {
 };
 
 // Tile kernels (elements of one block per CTA).  Unsupported combinations return an invalid variant.
-KernelVariant tensorStageVariant(int dim, int n, bool affine, bool visc);
+KernelVariant tensorStageVariant(int dim, int n, bool affine, int visc);  // visc: 0 Euler, 1 NS, 2 AV
 KernelVariant tensorGradVariant(int dim, int n, bool affine, bool br2);
-KernelVariant denseStageVariant(int type, int p, bool affine, bool visc);
+KernelVariant denseStageVariant(int type, int p, bool affine, int visc);
 KernelVariant denseGradVariant(int type, int p, bool affine);
 // Face-point kernels (FaceOp op, flux only for the Riemann operations) and the relative-error reduction.
 KernelVariant facePointVariant(int op, int dim, int flux);

@@ -7,7 +7,7 @@
 namespace sdg {
 
 namespace {
-template <int NB, int NQ, int NFQ, int NF, bool AFF, bool VISC>
+template <int NB, int NQ, int NFQ, int NF, bool AFF, int VISC>
 KernelVariant stageOf() {
   using S = DenseShape<NB, NQ, NFQ, NF>;
   KernelVariant v;
@@ -29,10 +29,11 @@ KernelVariant gradOf() {
 }
 }  // namespace
 
-KernelVariant denseStageVariant(int type, int p, bool affine, bool visc) {
+KernelVariant denseStageVariant(int type, int p, bool affine, int visc) {
 #define SDG_DS(T, P, NB, NQ, NFQ, NF, AFF)                                                                  \
   if (type == T && p == P && affine == AFF)                                                                 \
-    return visc ? stageOf<NB, NQ, NFQ, NF, AFF, true>() : stageOf<NB, NQ, NFQ, NF, AFF, false>();
+    return visc == 2 ? stageOf<NB, NQ, NFQ, NF, AFF, 2>()                                                   \
+                     : visc ? stageOf<NB, NQ, NFQ, NF, AFF, 1>() : stageOf<NB, NQ, NFQ, NF, AFF, 0>();
   SDG_DENSE_CASES(SDG_DS)
 #undef SDG_DS
   return KernelVariant();

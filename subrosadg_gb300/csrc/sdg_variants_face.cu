@@ -1,5 +1,6 @@
-// Face-point kernels (Riemann fluxes, boundary fluxes, Navier-Stokes trace exchange and viscous face
-// fluxes) and the relative-error reduction: the one translation unit that instantiates them.
+// Face-point kernels (Riemann fluxes, boundary fluxes, Navier-Stokes trace exchange, viscous and
+// artificial viscous face fluxes) and the relative-error reduction: the one translation unit that
+// instantiates them.
 #include "sdg_kernels_ns.cuh"
 #include "sdg_variants.hpp"
 
@@ -56,6 +57,8 @@ KernelVariant faceDimOf(int op, int flux) {
     case kOpExchangeBoundary: return faceOf<kOpExchangeBoundary, DIM, 0>();
     case kOpFaceNS: return faceFluxOf<kOpFaceNS, DIM>(flux);
     case kOpFaceNSBoundary: return faceOf<kOpFaceNSBoundary, DIM, 0>();
+    case kOpFaceAV: return faceFluxOf<kOpFaceAV, DIM>(flux);
+    case kOpFaceAVBoundary: return faceOf<kOpFaceAVBoundary, DIM, 0>();
     default: return KernelVariant();
   }
 }

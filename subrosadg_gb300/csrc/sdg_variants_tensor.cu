@@ -6,7 +6,7 @@
 namespace sdg {
 
 namespace {
-template <int DIM, int N, bool AFF, bool VISC>
+template <int DIM, int N, bool AFF, int VISC>
 KernelVariant stageOf() {
   using S = TensorShape<DIM, N>;
   KernelVariant v;
@@ -30,12 +30,13 @@ KernelVariant gradOf() {
 
 #define SDG_TENSOR_ORDERS(X) X(2, 3) X(2, 4) X(2, 5) X(2, 6) X(3, 2) X(3, 3) X(3, 4) X(3, 5) X(3, 6)
 
-KernelVariant tensorStageVariant(int dim, int n, bool affine, bool visc) {
-#define SDG_TS(D, NN)                                                                                   \
-  if (dim == D && n == NN) {                                                                            \
-    if (affine) return visc ? stageOf<D, NN, true, true>() : stageOf<D, NN, true, false>();             \
-    if constexpr (D == 2) return visc ? stageOf<D, NN, false, true>() : stageOf<D, NN, false, false>(); \
-    return KernelVariant();                                                                             \
+KernelVariant tensorStageVariant(int dim, int n, bool affine, int visc) {
+#define SDG_TS(D, NN)                                                                                        \
+  if (dim == D && n == NN) {                                                                                 \
+    if (affine) return visc == 2 ? stageOf<D, NN, true, 2>() : visc ? stageOf<D, NN, true, 1>() : stageOf<D, NN, true, 0>(); \
+    if constexpr (D == 2)                                                                                    \
+      return visc == 2 ? stageOf<D, NN, false, 2>() : visc ? stageOf<D, NN, false, 1>() : stageOf<D, NN, false, 0>(); \
+    return KernelVariant();                                                                                  \
   }
   SDG_TENSOR_ORDERS(SDG_TS)
 #undef SDG_TS

@@ -116,7 +116,8 @@ class Mesh:
 def make_config(polynomial_order, equation=_abi.EULER, convective_flux=_abi.HLLC, viscous_flux=_abi.VISCOUS_NONE,
                 time_integration=_abi.SSPRK3, cp=2.5, cv=25.0 / 14.0, gamma=1.4, mu=0.0, prandtl=0.71,
                 transport=_abi.TRANSPORT_CONSTANT, sound_speed=0.0, density=1.0, source=_abi.SOURCE_NONE,
-                thermal_expansion=0.0, reference_temperature=0.0) -> SdgConfig:
+                thermal_expansion=0.0, reference_temperature=0.0, shock_capturing=_abi.SHOCK_NONE,
+                empirical_tolerance=0.0, artificial_viscosity_factor=1.0) -> SdgConfig:
     c = SdgConfig()
     c.polynomial_order = polynomial_order
     c.equation = equation
@@ -134,6 +135,9 @@ def make_config(polynomial_order, equation=_abi.EULER, convective_flux=_abi.HLLC
     c.source_term = source
     c.thermal_expansion_coefficient = thermal_expansion
     c.reference_temperature = reference_temperature
+    c.shock_capturing = shock_capturing
+    c.empirical_tolerance = empirical_tolerance
+    c.artificial_viscosity_factor = artificial_viscosity_factor
     return c
 
 
@@ -248,6 +252,12 @@ class GpuSolver:
         n = c_int64()
         self._chk(self.lib.sdg_launch_count(self.h, byref(n)))
         return n.value
+
+    def node_artificial_viscosity(self):
+        """Artificial viscosity of the current state at every mesh node (zeros without shock capturing)."""
+        out = np.zeros(len(self.mesh.nodes))
+        self._chk(self.lib.sdg_get_node_artificial_viscosity(self.h, _ptr(out)))
+        return out
 
     # raw-binary files ---------------------------------------------------------------------------
     def writeRawBinary(self, path):
@@ -434,6 +444,20 @@ class System:
 
     def setTransportModel(self, mu, transport=_abi.TRANSPORT_CONSTANT, prandtl=0.71):
         self.cfg.update(mu=mu, transport=transport, prandtl=prandtl)
+
+    def setEquationOfState(self, reference_sound_speed, reference_density):
+        """Weakly compressible fluid of the incompressible models (PhysicalModel.cpp:57-78)."""
+        self.cfg.update(sound_speed=reference_sound_speed, density=reference_density)
+
+    def setSourceTerm(self, thermal_expansion_coefficient, reference_temperature):
+        """Boussinesq buoyancy (SourceTerm.cpp:29-58)."""
+        self.cfg.update(source=_abi.SOURCE_BOUSSINESQ, thermal_expansion=thermal_expansion_coefficient,
+                        reference_temperature=reference_temperature)
+
+    def setArtificialViscosity(self, empirical_tolerance, artificial_viscosity_factor=1.0):
+        """Shock capturing (SystemControl.cpp:105-108)."""
+        self.cfg.update(shock_capturing=_abi.ARTIFICIAL_VISCOSITY, empirical_tolerance=empirical_tolerance,
+                        artificial_viscosity_factor=artificial_viscosity_factor)
 
     def setTimeIntegration(self, cfl, iteration_range):
         self.cfl = cfl

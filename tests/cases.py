@@ -264,6 +264,54 @@ def cavity_3d_case(p=2, flux=sdg.EXACT, viscous=sdg.BR1, mu=2e-3, c0=10.0, n=3, 
     return (mesh, cfg, ic, bc, dt, steps)
 
 
+# ---- artificial viscosity (shock capturing, System::setArtificialViscosity) -------------------------------
+# The reference's shock drivers (examples/sodshock/explosion/sedovblast/khinstability_2d_ceuler.cpp) run
+# compressible Euler with setArtificialViscosity(kappa[, factor]).
+
+def with_av(case, tolerance=1.0, factor=1.0):
+    """The same case with artificial viscosity switched on."""
+    mesh, cfg, ic, bc, dt, steps = case
+    cfg.shock_capturing = sdg.ARTIFICIAL_VISCOSITY
+    cfg.empirical_tolerance = tolerance
+    cfg.artificial_viscosity_factor = factor
+    return (mesh, cfg, ic, bc, dt, steps)
+
+
+def shock_tube_case(p=3, flux=sdg.HLLC, n=8, dt=2e-4, steps=3, split=0.0, jitter=0.0, dim=2, tolerance=1.0,
+                    factor=1.0):
+    """Sod's shock tube (rho, p) = (1, 1) | (0.125, 0.1) at x = 0.5 in a slip-walled box [0,1] x [0,1/4]
+    (x [0,1/4] in 3D), smoothed over a few % of the length so the projected state stays positive."""
+    if dim == 2:
+        mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 0.25, n, max(2, n // 4), periodic=False, jitter=jitter,
+                               split_fraction=split, seed=12, boundary_conditions=[sdg.ADIABATIC_SLIP_WALL] * 4)
+    else:
+        mesh = sdg.Mesh.box_3d(0, 0, 0, 1.0, 0.25, 0.25, n, max(2, n // 4), max(2, n // 4), periodic=False,
+                               boundary_conditions=[sdg.ADIABATIC_SLIP_WALL] * 6)
+    cfg = config(p, flux)
+
+    def ic(pts):
+        x = pts[:, 0]
+        t = 0.5 * (1.0 + np.tanh((x - 0.5) / 0.02))
+        rho = 1.0 + (0.125 - 1.0) * t
+        pr = 1.0 + (0.1 - 1.0) * t
+        out = np.zeros((len(pts), dim + 2))
+        out[:, 0] = rho
+        out[:, 1] = 0.05 * np.sin(math.pi * pts[:, 1] * 4)
+        out[:, 2] = 0.03 * np.sin(4 * math.pi * x)  # small transverse velocities: no variable is identically 0
+        if dim == 3:
+            out[:, 3] = 0.03 * np.sin(4 * math.pi * x + 1.0) * np.cos(4 * math.pi * pts[:, 2])
+        out[:, dim + 1] = pr / (rho * R_GAS)
+        return out
+
+    def bc(pts, phys):
+        out = np.zeros((len(pts), dim + 2))
+        out[:, 0] = 1.0
+        out[:, dim + 1] = 1.0 / R_GAS
+        return out
+
+    return with_av((mesh, cfg, ic, bc, dt, steps), tolerance, factor)
+
+
 def batch_instances(count=256, seed=2024, min_elements=500, max_elements=50000, orders=(1, 2, 3, 4, 5)):
     """The batched workload: `count` independent 2D Kelvin-Helmholtz solves on [0,1]^2 (periodic), element
     counts log-uniform in [min_elements, max_elements], P uniform in `orders`, jittered (10% of h) quads or

@@ -133,6 +133,17 @@ CASES = {
     "inc-thermalcavity-hex-p3-lf-br2-boussinesq": lambda: cases.cavity_3d_case(
         p=3, flux=sdg.LAX_FRIEDRICHS, viscous=sdg.BR2, mu=1e-2, boussinesq=True, c0=3.0),
     "inc-euler-cavity-hex-p3-exact": lambda: cases.cavity_3d_case(p=3, viscous=None, mu=0.0),
+    # artificial viscosity (shock capturing): Sod tubes in slip-walled boxes and the Kelvin-Helmholtz bands
+    "av-shocktube-quad-p3-hllc": lambda: cases.shock_tube_case(p=3, n=8),
+    "av-shocktube-hybrid-p2-lf": lambda: cases.shock_tube_case(p=2, flux=sdg.LAX_FRIEDRICHS, split=0.5, jitter=0.1),
+    "av-shocktube-tri-p4-roe": lambda: cases.shock_tube_case(p=4, flux=sdg.ROE, split=1.0, n=6),
+    "av-shocktube-quad-p1-hllc-dense": lambda: cases.shock_tube_case(p=1, n=8),
+    "av-shocktube-jitter-quad-p4-roe": lambda: cases.shock_tube_case(p=4, flux=sdg.ROE, jitter=0.1, n=6),
+    "av-shocktube-hex-p2-hllc": lambda: cases.shock_tube_case(p=2, dim=3, n=8),
+    "av-shocktube-hex-p4-roe": lambda: cases.shock_tube_case(p=4, flux=sdg.ROE, dim=3, n=6, steps=2),
+    "av-kh-hybrid-p4-lf": lambda: cases.with_av(cases.kh_case(n=6, p=4, steps=3), tolerance=1.0),
+    "av-kh-jitter-quad-p5-hllc": lambda: cases.with_av(cases.kh_case(n=4, p=5, flux=sdg.HLLC, split=0.0, steps=2),
+                                                       tolerance=2.0, factor=0.5),
 }
 
 
@@ -153,6 +164,10 @@ def test_parity(name):
     # initial state
     s0g, s0o = g.state_point(), o.state_point()
     assert rel_l2(s0g, s0o) <= 1e-13, rel_l2(s0g, s0o)
+    if g.config.shock_capturing:  # the artificial viscosity field of the initial state
+        ag, ao = g.node_artificial_viscosity(), o.node_artificial_viscosity()
+        assert ao.max() > 0.0
+        np.testing.assert_allclose(ag, ao, rtol=1e-9, atol=1e-13 * ao.max())
     # one residual evaluation
     rg, ro = g.residual_point(), o.residual_point()
     err = rel_l2(rg, ro)

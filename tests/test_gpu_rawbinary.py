@@ -108,3 +108,16 @@ def test_raw_binary_specific_file_from_lower_order(tmp_path):
     # leading Nb(P-1) columns copied, the rest zero (InitialCondition.cpp:58-80)
     np.testing.assert_allclose(m_hi[:, :36], m_lo, rtol=1e-13, atol=1e-13)
     assert np.all(np.abs(m_hi[:, 36:]) < 1e-13)
+
+
+def test_raw_binary_carries_the_node_artificial_viscosity(tmp_path):
+    """With shock capturing the file's trailing node block is the node artificial viscosity of the state
+    (RawBinary.cpp:185-190 writes node_artificial_viscosity_)."""
+    s, dt, mesh = make(cases.shock_tube_case(p=3, n=8))
+    s.stepSolver(dt, 1)
+    path = tmp_path / "av.zst"
+    s.writeRawBinary(path)
+    payload = decode(path)
+    av = s.node_artificial_viscosity()
+    assert av.max() > 0
+    np.testing.assert_array_equal(payload[-len(mesh.nodes):], av)
