@@ -390,7 +390,8 @@ int sdg_adjoint_steps(sdg_handle* handle, int32_t step_count, double delta_time,
 int sdg_forward_steps(sdg_handle* handle, int32_t step_count, double delta_time, int32_t checkpoint_interval);
 int sdg_adjoint_recorded(sdg_handle* handle, const double* final_cotangent, double* initial_cotangent,
                          double* viscosity_cotangent);
-/* Device bytes held for checkpoints and stage states (grown on demand, released with the handle). */
+/* Device bytes held for checkpoints, stage states and (Navier-Stokes, when HBM has room) the forward quantities
+ * of one segment's stage inputs (grown on demand, released with the handle). */
 int sdg_adjoint_memory(sdg_handle* handle, int64_t* bytes);
 
 #ifdef __cplusplus

@@ -73,6 +73,16 @@ struct AdjointState {
   std::vector<double*> pool;       // checkpoints and stage states (grown on demand)
   double* muAcc = nullptr;         // device accumulator of dJ/dmu
   Trajectory traj;
+  // Navier-Stokes forward quantities of every stage input of one checkpoint segment (traces, node gradient,
+  // gradient traces), kept by the segment's recompute so the reverse stages read them instead of recomputing
+  // them; allocated when HBM has room, else the reverse recomputes them (forwardAt)
+  double* fwdStore = nullptr;
+  size_t fwdSlots = 0;
+  bool fwdTried = false;
+  // forward quantities the reverse kernels read (null: the handle's own buffers)
+  const double* curFace = nullptr;
+  const double* curGrad = nullptr;
+  const double* curFaceGrad = nullptr;
 };
 
 namespace sdg {
@@ -84,6 +94,7 @@ void destroyAdjoint(sdg_handle* h) {
                     A->pts, A->muAcc})
     cudaFree(p);
   for (double* p : A->pool) cudaFree(p);
+  cudaFree(A->fwdStore);
   delete A;
   h->adj = nullptr;
 }
@@ -148,12 +159,16 @@ AdjointState* adjoint(sdg_handle* h) {
 AdjArgs baseArgs(sdg_handle* h, const DevBlock* B, const double* U) {
   AdjArgs a;
   std::memset(&a, 0, sizeof(a));
+  const AdjointState* A = h->adj;
+  const double* grad = A->curGrad ? A->curGrad : h->grad;
   if (B) {
     a.u = U + B->stateOffset; a.geom = B->geom; a.tables = B->tables;
-    a.grad = h->ns ? h->grad + B->gradOffset : nullptr;
+    a.grad = h->ns ? grad + B->gradOffset : nullptr;
     a.ne = B->ne; a.faceBase = B->faceBase;
   }
-  a.face = h->face; a.faceGrad = h->faceGrad; a.conn = h->fconn; a.fgeo = h->fgeo; a.status = h->status;
+  a.face = A->curFace ? A->curFace : h->face;
+  a.faceGrad = A->curFaceGrad ? A->curFaceGrad : h->faceGrad;
+  a.conn = h->fconn; a.fgeo = h->fgeo; a.status = h->status;
   a.nface = h->nInterior; a.n1d = h->n1d; a.epb = h->adj->k.epb;
   return a;
 }
@@ -374,6 +389,70 @@ void forwardSweep(sdg_handle* h, int steps, double dt, int interval) {
   A->traj.steps = steps; A->traj.interval = interval; A->traj.segments = segments; A->traj.dt = dt;
 }
 
+// Doubles of one stored stage input: traces, node gradient, gradient traces.
+size_t fwdSlotSize(const sdg_handle* h) { return h->faceCount * (1 + h->dim) + h->gradCount; }
+
+// The forward store for `slots` stage inputs, allocated once when the device keeps at least 2 GiB free
+// beside it; false (recompute in the reverse) otherwise.
+bool forwardStore(sdg_handle* h, size_t slots) {
+  AdjointState* A = h->adj;
+  if (!h->ns) return false;
+  if (A->fwdStore && A->fwdSlots >= slots) return true;
+  if (A->fwdTried && !A->fwdStore) return false;
+  cudaFree(A->fwdStore);
+  A->fwdStore = nullptr; A->fwdSlots = 0; A->fwdTried = true;
+  size_t freeB = 0, totalB = 0;
+  SDG_CUDA(cudaMemGetInfo(&freeB, &totalB));
+  const size_t bytes = slots * fwdSlotSize(h) * sizeof(double);
+  if (bytes + (size_t(2) << 30) > freeB) return false;
+  if (cudaMalloc(&A->fwdStore, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    A->fwdStore = nullptr;
+    return false;
+  }
+  A->fwdSlots = slots;
+  return true;
+}
+
+double* fwdSlot(sdg_handle* h, size_t i) { return h->adj->fwdStore + i * fwdSlotSize(h); }
+
+// Keep the traces of the current stage input (h->face) in stored slot i.
+void keepTraces(sdg_handle* h, size_t i) {
+  SDG_CUDA(cudaMemcpyAsync(fwdSlot(h, i), h->face, h->faceCount * 8, cudaMemcpyDeviceToDevice, h->stream));
+}
+
+// Records of one stage whose node gradient and gradient traces live in stored slot i: the gradient kernels
+// write them there and the face and stage kernels read them there (no copy).
+std::vector<Rec> intoSlot(sdg_handle* h, const std::vector<Rec>& recs, size_t i) {
+  double* g = fwdSlot(h, i) + h->faceCount;
+  double* fg = g + h->gradCount;
+  const auto rebase = [&](auto* p, const double* from, size_t count, double* to) {
+    using P = decltype(p);
+    if (p && p >= from && p < from + count) return P(to + (p - from));
+    return p;
+  };
+  std::vector<Rec> out = recs;
+  const size_t G = h->gradCount, FG = h->faceCount * h->dim;
+  for (Rec& r : out) {
+    r.ga.grad = rebase(r.ga.grad, h->grad, G, g); r.ga.faceGrad = rebase(r.ga.faceGrad, h->faceGrad, FG, fg);
+    r.da.grad = rebase(r.da.grad, h->grad, G, g); r.da.faceGrad = rebase(r.da.faceGrad, h->faceGrad, FG, fg);
+    r.fa.faceGrad = rebase(r.fa.faceGrad, h->faceGrad, FG, fg);
+    r.sa.grad = rebase(r.sa.grad, h->grad, G, g);
+  }
+  return out;
+}
+
+void useForward(sdg_handle* h, size_t i) {
+  AdjointState* A = h->adj;
+  const double* d = fwdSlot(h, i);
+  A->curFace = d; A->curGrad = d + h->faceCount; A->curFaceGrad = d + h->faceCount + h->gradCount;
+}
+
+void useOwnForward(sdg_handle* h) {
+  AdjointState* A = h->adj;
+  A->curFace = A->curGrad = A->curFaceGrad = nullptr;
+}
+
 // Reverse sweep of the recorded trajectory: on entry A->lamIn holds dJ/dU_N; on exit it holds dJ/dU_0 and
 // the state is U_N again.  Returns dJ/dmu (Navier-Stokes; 0 for Euler).
 double backwardSweep(sdg_handle* h) {
@@ -384,24 +463,34 @@ double backwardSweep(sdg_handle* h) {
   const double dt = T.dt;
   const size_t storeBase = size_t(segments) + 1;
   const auto stages = stepByStage(h, dt, S);
+  const bool keep = forwardStore(h, size_t(interval) * S);
   SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
   SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
   const double muScale = h->ns && h->ph.mu > 0.0 ? 1.0 / h->ph.mu : 0.0;
   for (int g = segments - 1; g >= 0; --g) {
     const int n0 = g * interval, n1 = std::min(steps, n0 + interval);
-    // recompute the segment from its checkpoint, keeping every stage input
+    // recompute the segment from its checkpoint, keeping every stage input (and, with room, its forward
+    // quantities: the flux records leave the traces, gradient and gradient traces of the stage input)
     copyState(h, h->state[0], poolBuffer(h, g));
     traces(h, h->state[0], h->face);
     for (int n = n0; n < n1; ++n)
       for (int s = 0; s < S; ++s) {
-        copyState(h, poolBuffer(h, storeBase + size_t(n - n0) * S + s), h->state[s == 0 ? 0 : 1]);
-        runRecs(h, stages[s], h->stream);
+        const size_t slot = size_t(n - n0) * S + s;
+        copyState(h, poolBuffer(h, storeBase + slot), h->state[s == 0 ? 0 : 1]);
+        if (keep) {
+          keepTraces(h, slot);
+          runRecs(h, intoSlot(h, stages[s], slot), h->stream);
+        } else {
+          runRecs(h, stages[s], h->stream);
+        }
       }
     // reverse
     for (int n = n1 - 1; n >= n0; --n)
       for (int s = S - 1; s >= 0; --s) {
-        copyState(h, h->state[1], poolBuffer(h, storeBase + size_t(n - n0) * S + s));
-        forwardAt(h, h->state[1]);
+        const size_t slot = size_t(n - n0) * S + s;
+        copyState(h, h->state[1], poolBuffer(h, storeBase + slot));
+        if (keep) useForward(h, slot);
+        else forwardAt(h, h->state[1]);
         const double c0 = kRk[ti][s][0], c1 = kRk[ti][s][1], c2dt = kRk[ti][s][2] * dt;
         if (s > 0) {
           vjpResidual(h, A->lamIn, A->lamIn, A->lamStage, A->lamBase, false, c0, c1, c2dt, c2dt * muScale);
@@ -411,6 +500,7 @@ double backwardSweep(sdg_handle* h) {
           std::swap(A->lamIn, A->lamBase);
           SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
         }
+        useOwnForward(h);
       }
   }
   copyState(h, h->state[0], poolBuffer(h, segments));
@@ -566,6 +656,7 @@ int sdg_adjoint_memory(sdg_handle* h, int64_t* bytes) {
   if (!h->adj) return SDG_OK;
   const AdjointState* A = h->adj;
   *bytes = int64_t(A->pool.size()) * int64_t(h->stateCount) * 8;
+  if (A->fwdStore) *bytes += int64_t(A->fwdSlots) * int64_t(fwdSlotSize(h)) * 8;
   return SDG_OK;
 }
 
