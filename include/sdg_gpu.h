@@ -390,6 +390,17 @@ int sdg_adjoint_steps(sdg_handle* handle, int32_t step_count, double delta_time,
 int sdg_forward_steps(sdg_handle* handle, int32_t step_count, double delta_time, int32_t checkpoint_interval);
 int sdg_adjoint_recorded(sdg_handle* handle, const double* final_cotangent, double* initial_cotangent,
                          double* viscosity_cotangent);
+/* Cotangent of the ghost primitive (rho, u, T) of every boundary point ([boundary_point_count][d+2], the order
+ * of sdg_boundary_point_coordinate) accumulated by the last sdg_vjp_residual / sdg_adjoint_steps /
+ * sdg_adjoint_recorded: the gradient with respect to the boundary (freestream) states.  Euler only. */
+int sdg_adjoint_boundary_cotangent(sdg_handle* handle, double* cotangent);
+/* Surface force of boundary group `physical` (1-based mesh physical index) on the current state: the sum over its
+ * face points of w |J_f| (p n - tau n) from the interior traces, n out of the fluid (the reference's View force,
+ * VariableConvertor.cpp:883-906).  force: [dimension]. */
+int sdg_surface_force(sdg_handle* handle, int32_t physical, double* force);
+/* Cotangent of direction . force with respect to the state ([volume_points][nv], the layout of the
+ * adjoint's final cotangent): the Euler pressure force (Navier-Stokes: SDG_ERR_UNSUPPORTED). */
+int sdg_surface_force_cotangent(sdg_handle* handle, int32_t physical, const double* direction, double* cotangent);
 /* Device bytes held for checkpoints, stage states and (Navier-Stokes, when HBM has room) the forward quantities
  * of one segment's stage inputs (grown on demand, released with the handle). */
 int sdg_adjoint_memory(sdg_handle* handle, int64_t* bytes);

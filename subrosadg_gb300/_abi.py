@@ -159,6 +159,9 @@ SIGNATURES = {
     "sdg_mesh_read_msh": (c_int32, [c_char_p, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_free": (c_int32, [POINTER(SdgGeneratedMesh)]),
     "sdg_get_node_artificial_viscosity": (c_int32, [c_void_p, _p_double]),
+    "sdg_adjoint_boundary_cotangent": (c_int32, [c_void_p, _p_double]),
+    "sdg_surface_force": (c_int32, [c_void_p, c_int32, _p_double]),
+    "sdg_surface_force_cotangent": (c_int32, [c_void_p, c_int32, _p_double, _p_double]),
     "sdg_write_raw_binary": (c_int32, [c_void_p, c_char_p]),
     "sdg_read_raw_binary": (c_int32, [c_void_p, c_char_p, c_int32]),
     "sdg_set_graph": (c_int32, [c_void_p, c_int32]),

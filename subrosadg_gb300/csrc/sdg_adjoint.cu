@@ -72,6 +72,7 @@ struct AdjointState {
   double* pts = nullptr;           // point-layout conversion buffer
   std::vector<double*> pool;       // checkpoints and stage states (grown on demand)
   double* muAcc = nullptr;         // device accumulator of dJ/dmu
+  double* lamGhost = nullptr;      // Euler with boundary faces: cotangent of each boundary point's ghost primitive
   Trajectory traj;
   // Navier-Stokes forward quantities of every stage input of one checkpoint segment (traces, node gradient,
   // gradient traces), kept by the segment's recompute so the reverse stages read them instead of recomputing
@@ -91,7 +92,7 @@ void destroyAdjoint(sdg_handle* h) {
   if (!A) return;
   for (double* p : {A->dU[0], A->dU[1], A->dface, A->dfaceOther, A->dgrad, A->dfaceGrad, A->dflux, A->lamIn,
                     A->lamStage, A->lamBase, A->lamU, A->lamG, A->lamH, A->lamTr, A->lamTg, A->lamUp, A->muPart,
-                    A->pts, A->muAcc})
+                    A->pts, A->muAcc, A->lamGhost})
     cudaFree(p);
   for (double* p : A->pool) cudaFree(p);
   cudaFree(A->fwdStore);
@@ -115,7 +116,8 @@ AdjointState* adjoint(sdg_handle* h) {
   for (const DevBlock& B : h->blocks)
     if (B.kind != kTensor || !B.affine)
       throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (quadrangles P>=2, hexahedra)");
-  if (h->nBoundary > 0) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need a mesh without boundary faces (periodic)");
+  if (h->nBoundary > 0 && h->ns)
+    throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes derivatives need a mesh without boundary faces (periodic)");
   if (h->ns && h->cfg.viscous_flux != SDG_VISCOUS_BR1) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of BR2 are not built");
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
   if (h->ph.incomp || h->ph.source)
@@ -141,6 +143,10 @@ AdjointState* adjoint(sdg_handle* h) {
   A->pts = alloc(size_t(h->volumePoints) * h->nv);
   A->muAcc = alloc(1);
   SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
+  if (h->nBoundary > 0) {
+    A->lamGhost = alloc(size_t(h->nBoundary) * h->nfq * h->nv);
+    SDG_CUDA(cudaMemsetAsync(A->lamGhost, 0, size_t(h->nBoundary) * h->nfq * h->nv * 8, h->stream));
+  }
   for (double* p : {A->dU[0], A->dU[1], A->dface, A->dflux, A->lamIn, A->lamStage, A->lamBase, A->lamU, A->lamH, A->lamTr})
     SDG_CUDA(cudaMemsetAsync(p, 0, (p == A->dface || p == A->dflux || p == A->lamH || p == A->lamTr ? F : S) * 8, h->stream));
   if (h->ns) {
@@ -185,6 +191,14 @@ void launch(sdg_handle* h, const void* fn, int64_t grid, int threads, size_t sme
 
 int64_t tiles(const sdg_handle* h, const DevBlock& B) { return (B.ne + h->adj->k.epb - 1) / h->adj->k.epb; }
 int64_t faceGrid(const sdg_handle* h) { return (h->nInterior * h->nfq + kFaceThreads - 1) / kFaceThreads; }
+int64_t boundaryGrid(const sdg_handle* h) { return (h->nBoundary * h->nfq + kFaceThreads - 1) / kFaceThreads; }
+
+// Arguments of the boundary-face derivative kernels (Euler).
+AdjArgs boundaryArgs(sdg_handle* h) {
+  AdjArgs a = baseArgs(h, nullptr, nullptr);
+  a.conn = h->bconn; a.fgeo = h->bgeo; a.nface = h->nBoundary; a.ghost = h->ghost;
+  return a;
+}
 
 // Traces of state buffer `u` into `face` (the forward stage kernel's trace-only pass).
 void traces(sdg_handle* h, const double* u, double* face) {
@@ -206,6 +220,11 @@ void gradientOf(sdg_handle* h, const double* u, double* face, double* other, dou
   Rec x = faceRec(h, kOpExchange);
   x.fa.face = face; x.fa.other = other;
   recs.push_back(x);
+  if (h->nBoundary > 0) {
+    Rec xb = faceRec(h, kOpExchangeBoundary);
+    xb.fa.face = face; xb.fa.other = other;
+    recs.push_back(xb);
+  }
   for (DevBlock& B : h->blocks) {
     Rec r = gradRec(h, B, 0);
     r.ga.u = u + B.stateOffset; r.ga.face = face; r.ga.faceOther = other;
@@ -227,6 +246,11 @@ void tangentFaces(sdg_handle* h, double dmu) {
   AdjArgs a = baseArgs(h, nullptr, nullptr);
   a.dface = A->dface; a.dfaceGrad = A->dfaceGrad; a.dflux = A->dflux; a.dmu = dmu;
   launch(h, A->k.jvpFace, faceGrid(h), kFaceThreads, 0, a, true);
+  if (h->nBoundary > 0) {
+    AdjArgs b = boundaryArgs(h);
+    b.dface = A->dface; b.dflux = A->dflux;
+    launch(h, A->k.jvpBoundary, boundaryGrid(h), kFaceThreads, 0, b, true);
+  }
 }
 
 // Tangent element kernels: from tangent state du (traces in dface, dflux computed), write drate and/or
@@ -262,7 +286,7 @@ void jvpResidual(sdg_handle* h, const double* du, double dmu, double* drate) {
 // Without RK coefficients (lamStage = lamBase = null) the result R'^T lam goes to A->lamU.  For
 // Navier-Stokes, A->muAcc += muScale * mu <lam, dR/dmu> on the device.
 void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* lamStage, double* lamBase,
-                 bool accumulateAll, double c0, double c1, double c2dt, double muScale) {
+                 bool accumulateAll, double c0, double c1, double c2dt, double muScale, double ghostScale) {
   AdjointState* A = h->adj;
   const int NT = A->k.threads;
   int64_t tileOff = 0;
@@ -278,6 +302,11 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
     AdjArgs a = baseArgs(h, nullptr, nullptr);
     a.lamH = A->lamH; a.lamTr = A->lamTr; a.lamTg = A->lamTg; a.muPart = A->muPart + A->muTiles;
     launch(h, A->k.vjpFace, faceGrid(h), kFaceThreads, 0, a, true);
+  }
+  if (h->nBoundary > 0) {  // boundary slots of lamTr, and the ghost cotangent (weight ghostScale)
+    AdjArgs b = boundaryArgs(h);
+    b.lamH = A->lamH; b.lamTr = A->lamTr; b.lamGhost = A->lamGhost; b.ghostScale = ghostScale;
+    launch(h, A->k.vjpBoundary, boundaryGrid(h), kFaceThreads, 0, b, true);
   }
   if (h->ns) {
     for (DevBlock& B : h->blocks) {
@@ -303,6 +332,11 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
   muAccumulateKernel<<<1, 256, 0, h->stream>>>(A->muPart, A->muTiles + A->muFaces, muScale, A->muAcc);
   SDG_CUDA(cudaGetLastError());
   h->launches++;
+}
+
+void clearGhost(sdg_handle* h) {
+  if (h->adj->lamGhost)
+    SDG_CUDA(cudaMemsetAsync(h->adj->lamGhost, 0, size_t(h->nBoundary) * h->nfq * h->nv * 8, h->stream));
 }
 
 double readMu(sdg_handle* h) {
@@ -466,6 +500,7 @@ double backwardSweep(sdg_handle* h) {
   const bool keep = forwardStore(h, size_t(interval) * S);
   SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
   SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
+  clearGhost(h);
   const double muScale = h->ns && h->ph.mu > 0.0 ? 1.0 / h->ph.mu : 0.0;
   for (int g = segments - 1; g >= 0; --g) {
     const int n0 = g * interval, n1 = std::min(steps, n0 + interval);
@@ -493,10 +528,10 @@ double backwardSweep(sdg_handle* h) {
         else forwardAt(h, h->state[1]);
         const double c0 = kRk[ti][s][0], c1 = kRk[ti][s][1], c2dt = kRk[ti][s][2] * dt;
         if (s > 0) {
-          vjpResidual(h, A->lamIn, A->lamIn, A->lamStage, A->lamBase, false, c0, c1, c2dt, c2dt * muScale);
+          vjpResidual(h, A->lamIn, A->lamIn, A->lamStage, A->lamBase, false, c0, c1, c2dt, c2dt * muScale, c2dt);
           std::swap(A->lamIn, A->lamStage);
         } else {
-          vjpResidual(h, A->lamIn, A->lamIn, nullptr, A->lamBase, true, c0, c1, c2dt, c2dt * muScale);
+          vjpResidual(h, A->lamIn, A->lamIn, nullptr, A->lamBase, true, c0, c1, c2dt, c2dt * muScale, c2dt);
           std::swap(A->lamIn, A->lamBase);
           SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
         }
@@ -506,6 +541,33 @@ double backwardSweep(sdg_handle* h) {
   copyState(h, h->state[0], poolBuffer(h, segments));
   traces(h, h->state[0], h->face);
   return h->ns ? readMu(h) : 0.0;
+}
+
+// Device inputs of the surface-force kernels for boundary group `physical` (1-based mesh physical index).
+struct ForceInputs {
+  int* select = nullptr;
+  double* fw = nullptr;
+  double* out = nullptr;
+  ~ForceInputs() { cudaFree(select); cudaFree(fw); cudaFree(out); }
+};
+
+ForceArgs forceInputs(sdg_handle* h, int physical, ForceInputs& in, bool pointOut) {
+  if (h->nBoundary == 0) throw Failure(SDG_ERR_INVALID_ARGUMENT, "the mesh has no boundary faces");
+  std::vector<int> sel(size_t(h->nBoundary));
+  bool any = false;
+  for (int64_t i = 0; i < h->nBoundary; ++i) { sel[i] = h->bphys[i] == physical; any = any || sel[i]; }
+  if (!any) throw Failure(SDG_ERR_INVALID_ARGUMENT, "no boundary face belongs to that physical group");
+  const PointRule fr = faceRule(h->blocks[0].type, h->p);
+  SDG_CUDA(cudaMalloc(&in.select, sel.size() * sizeof(int)));
+  SDG_CUDA(cudaMalloc(&in.fw, fr.w.size() * 8));
+  SDG_CUDA(cudaMemcpyAsync(in.select, sel.data(), sel.size() * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  SDG_CUDA(cudaMemcpyAsync(in.fw, fr.w.data(), fr.w.size() * 8, cudaMemcpyHostToDevice, h->stream));
+  if (pointOut) SDG_CUDA(cudaMalloc(&in.out, size_t(h->nBoundary) * h->nfq * h->dim * 8));
+  ForceArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.face = h->face; a.faceGrad = h->faceGrad; a.conn = h->bconn; a.fgeo = h->bgeo; a.select = in.select;
+  a.fw = in.fw; a.out = in.out; a.nface = h->nBoundary; a.n1d = h->n1d; a.ns = h->ns ? 1 : 0;
+  return a;
 }
 
 int adjFail(sdg_handle* h, const Failure& f) {
@@ -568,8 +630,9 @@ int sdg_vjp_residual(sdg_handle* h, const double* rate_cotangent, double* cotang
     uploadPoints(h, rate_cotangent, A->lamIn);
     forwardAt(h, h->state[1]);
     SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
+    clearGhost(h);
     vjpResidual(h, A->lamIn, nullptr, nullptr, nullptr, false, 0.0, 0.0, 0.0,
-                h->ns && h->ph.mu > 0.0 ? 1.0 / h->ph.mu : 0.0);
+                h->ns && h->ph.mu > 0.0 ? 1.0 / h->ph.mu : 0.0, 1.0);
     downloadPoints(h, A->lamU, cotangent);
     if (viscosity_cotangent) *viscosity_cotangent = h->ns ? readMu(h) : 0.0;
     traces(h, h->state[0], h->face);
@@ -644,6 +707,84 @@ int sdg_adjoint_recorded(sdg_handle* h, const double* final_cotangent, double* i
     downloadPoints(h, A->lamIn, initial_cotangent);
     if (viscosity_cotangent) *viscosity_cotangent = m;
     checkStatus(h);
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_surface_force(sdg_handle* h, int32_t physical, double* force) {
+  if (!h || !force) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  if (!h->hasState) { h->err = "no state"; return SDG_ERR_STATE; }
+  try {
+    SDG_CUDA(cudaSetDevice(h->device));
+    if (h->ph.incomp) throw Failure(SDG_ERR_UNSUPPORTED, "the surface force is built for the compressible models");
+    // the gradient traces of the current state (the step leaves those of its last stage input)
+    if (h->ns) gradientOf(h, h->state[0], h->face, h->faceOther, h->grad, h->faceGrad);
+    ForceInputs in;
+    const ForceArgs a = forceInputs(h, physical, in, true);
+    const int64_t pts = h->nBoundary * h->nfq;
+    const unsigned grid = unsigned((pts + kFaceThreads - 1) / kFaceThreads);
+    if (h->dim == 2) surfaceForceKernel<2><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
+    else surfaceForceKernel<3><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
+    SDG_CUDA(cudaGetLastError());
+    h->launches++;
+    std::vector<double> part(size_t(pts) * h->dim);
+    SDG_CUDA(cudaMemcpyAsync(part.data(), in.out, part.size() * 8, cudaMemcpyDeviceToHost, h->stream));
+    SDG_CUDA(cudaStreamSynchronize(h->stream));
+    for (int k = 0; k < h->dim; ++k) force[k] = 0.0;
+    for (int64_t i = 0; i < pts; ++i)
+      for (int k = 0; k < h->dim; ++k) force[k] += part[size_t(i) * h->dim + k];
+    checkStatus(h);
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_surface_force_cotangent(sdg_handle* h, int32_t physical, const double* direction, double* cotangent) {
+  if (!h || !direction || !cotangent) return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    AdjointState* A = adjoint(h);
+    if (h->ns) throw Failure(SDG_ERR_UNSUPPORTED, "the surface-force cotangent is built for the Euler equations");
+    SDG_CUDA(cudaSetDevice(h->device));
+    ForceInputs in;
+    ForceArgs a = forceInputs(h, physical, in, false);
+    for (int k = 0; k < h->dim; ++k) a.dir[k] = direction[k];
+    a.out = A->lamTr;
+    SDG_CUDA(cudaMemsetAsync(A->lamTr, 0, h->faceCount * 8, h->stream));
+    SDG_CUDA(cudaMemsetAsync(A->lamU, 0, h->stateCount * 8, h->stream));
+    const int64_t pts = h->nBoundary * h->nfq;
+    const unsigned grid = unsigned((pts + kFaceThreads - 1) / kFaceThreads);
+    if (h->dim == 2) surfaceForceTraceCotangentKernel<2><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
+    else surfaceForceTraceCotangentKernel<3><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
+    SDG_CUDA(cudaGetLastError());
+    h->launches++;
+    // the transposed trace operator: lamU = T^T lamTr (the element kernel of the reverse without its
+    // volume and RK parts)
+    for (DevBlock& B : h->blocks) {
+      AdjArgs t = baseArgs(h, &B, h->state[0]);
+      t.lamU = A->lamU + B.stateOffset; t.lamTr = A->lamTr;
+      launch(h, A->k.vjpTrace, tiles(h, B), A->k.threads, A->k.vjpSmem, t, false);
+    }
+    downloadPoints(h, A->lamU, cotangent);
+    checkStatus(h);
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_adjoint_boundary_cotangent(sdg_handle* h, double* out) {
+  if (!h || !out) return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    AdjointState* A = adjoint(h);
+    const size_t n = size_t(h->nBoundary) * h->nfq * h->nv;
+    if (n == 0) return SDG_OK;
+    SDG_CUDA(cudaSetDevice(h->device));
+    SDG_CUDA(cudaMemcpyAsync(out, A->lamGhost, n * 8, cudaMemcpyDeviceToHost, h->stream));
+    SDG_CUDA(cudaStreamSynchronize(h->stream));
   } catch (const Failure& f) {
     return adjFail(h, f);
   }

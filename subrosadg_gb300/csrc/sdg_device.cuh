@@ -266,63 +266,65 @@ __device__ __forceinline__ void convectiveFlux(const State<D, T>& l, const State
   else fluxExact<D>(l, r, n, ph, h);
 }
 
-// Computational variables (rho, u, e, p) used by the boundary states.
-template <int D>
+// Computational variables (rho, u, e, p) used by the boundary states; generic over the scalar type like the
+// rest of the pointwise physics (double: the forward path; Dual<K>: its derivatives).
+template <int D, class T = double>
 struct Comp {
-  double r, u[D], e, p;
+  T r, u[D], e, p;
 };
 
-template <int D>
-__device__ __forceinline__ void compFromState(const State<D>& s, Comp<D>& c, const Phys& ph) {
+template <int D, class T>
+__device__ __forceinline__ void compFromState(const State<D, T>& s, Comp<D, T>& c, const Phys& ph) {
   c.r = s.r;
 #pragma unroll
   for (int k = 0; k < D; ++k) c.u[k] = s.u[k];
   c.p = s.p;
   if (ph.incomp) { c.e = s.E * s.ir; return; }
-  double u2 = 0.0;
+  T u2 = T(0.0);
 #pragma unroll
-  for (int k = 0; k < D; ++k) u2 = fma(s.u[k], s.u[k], u2);
-  c.e = fma(-0.5, u2, s.E * s.ir);
+  for (int k = 0; k < D; ++k) u2 = fmaT(s.u[k], s.u[k], u2);
+  c.e = fmaT(-0.5, u2, s.E * s.ir);
 }
 
 // The last conserved variable of a computational state: rho E (compressible) or rho e (incompressible).
-template <int D>
-__device__ __forceinline__ double energyOfComp(const Comp<D>& c, const Phys& ph) {
+template <int D, class T>
+__device__ __forceinline__ T energyOfComp(const Comp<D, T>& c, const Phys& ph) {
   if (ph.incomp) return c.r * c.e;
-  double u2 = 0.0;
+  T u2 = T(0.0);
 #pragma unroll
   for (int k = 0; k < D; ++k) u2 += c.u[k] * c.u[k];
   return c.r * (c.e + 0.5 * u2);
 }
 
-template <int D>
-__device__ __forceinline__ void normalFluxComp(const Comp<D>& c, const double* n, double* f, const Phys& ph) {
-  const double un = dotn<D>(c.u, n);
-  double u2 = 0.0;
+template <int D, class T>
+__device__ __forceinline__ void normalFluxComp(const Comp<D, T>& c, const double* n, T* f, const Phys& ph) {
+  const T un = dotn<D>(c.u, n);
+  T u2 = T(0.0);
 #pragma unroll
-  for (int k = 0; k < D; ++k) u2 = fma(c.u[k], c.u[k], u2);
+  for (int k = 0; k < D; ++k) u2 = fmaT(c.u[k], c.u[k], u2);
   f[0] = c.r * un;
 #pragma unroll
-  for (int k = 0; k < D; ++k) f[1 + k] = fma(c.r * un, c.u[k], c.p * n[k]);
-  f[D + 1] = ph.incomp ? c.r * c.e * un : fma(c.r, fma(0.5, u2, c.e), c.p) * un;
+  for (int k = 0; k < D; ++k) f[1 + k] = fmaT(c.r * un, c.u[k], c.p * n[k]);
+  f[D + 1] = ph.incomp ? c.r * c.e * un : fmaT(c.r, fmaT(0.5, u2, c.e), c.p) * un;
 }
 
 // Boundary state (BoundaryCondition.cpp:79-547): l = interior trace, g = ghost (user) state.
-template <int D>
-__device__ __forceinline__ void boundaryState(int bc, const double* n, const Comp<D>& l, const Comp<D>& g,
-                                              const Phys& ph, Comp<D>& b) {
+template <int D, class T>
+__device__ __forceinline__ void boundaryState(int bc, const double* n, const Comp<D, T>& l, const Comp<D, T>& g,
+                                              const Phys& ph, Comp<D, T>& b) {
   const double gam = ph.gamma;
-  const double unl = dotn<D>(l.u, n);
-  const double mn = unl / (ph.incomp ? ph.c0 : sqrt(gam * l.p / l.r));
+  const T unl = dotn<D>(l.u, n);
+  const T mn = ph.incomp ? unl / ph.c0 : unl / sqrtT(gam * l.p / l.r);
   if (bc == 0) {  // Riemann farfield
-    if (fabs(mn) > 1.0) { b = mn < 0.0 ? g : l; return; }
+    if (fabsT(mn) > 1.0) { b = mn < 0.0 ? g : l; return; }
     if (ph.incomp) {
       // the exact-flux star state between the interior and the ghost (BoundaryCondition.cpp:153-180,243-270)
-      const double c0 = ph.c0, ung = dotn<D>(g.u, n);
-      const double rb = sqrt(l.r * g.r * exp((unl - ung) / c0));
-      const double unb = (unl + ung) / 2.0 + log(l.r / g.r) * c0 / 2.0;
-      const Comp<D>& s = mn < 0.0 ? g : l;
-      const double uns = mn < 0.0 ? ung : unl;
+      const double c0 = ph.c0;
+      const T ung = dotn<D>(g.u, n);
+      const T rb = sqrtT(l.r * g.r * expT((unl - ung) / c0));
+      const T unb = (unl + ung) / 2.0 + logT(l.r / g.r) * c0 / 2.0;
+      const Comp<D, T>& s = mn < 0.0 ? g : l;
+      const T uns = mn < 0.0 ? ung : unl;
       b.r = rb;
       b.e = s.e * s.r / rb;
 #pragma unroll
@@ -330,17 +332,17 @@ __device__ __forceinline__ void boundaryState(int bc, const double* n, const Com
       b.p = weakPressure(rb, ph);
       return;
     }
-    const double ung = dotn<D>(g.u, n);
-    const double rm = ung - 2.0 * sqrt(gam * g.p / g.r) / (gam - 1.0);
-    const double rp = unl + 2.0 * sqrt(gam * l.p / l.r) / (gam - 1.0);
-    const double unb = 0.5 * (rm + rp);
-    const Comp<D>& s = mn < 0.0 ? g : l;
-    const double uns = dotn<D>(s.u, n);
+    const T ung = dotn<D>(g.u, n);
+    const T rm = ung - 2.0 * sqrtT(gam * g.p / g.r) / (gam - 1.0);
+    const T rp = unl + 2.0 * sqrtT(gam * l.p / l.r) / (gam - 1.0);
+    const T unb = 0.5 * (rm + rp);
+    const Comp<D, T>& s = mn < 0.0 ? g : l;
+    const T uns = dotn<D>(s.u, n);
 #pragma unroll
     for (int k = 0; k < D; ++k) b.u[k] = s.u[k] + (unb - uns) * n[k];
-    const double cb = (gam - 1.0) * (rp - rm) / 4.0;
-    const double sb = s.p / pow(s.r, gam);
-    b.r = pow(cb * cb / (gam * sb), 1.0 / (gam - 1.0));
+    const T cb = (gam - 1.0) * (rp - rm) / 4.0;
+    const T sb = s.p / powT(s.r, gam);
+    b.r = powT(cb * cb / (gam * sb), 1.0 / (gam - 1.0));
     b.p = b.r * cb * cb / gam;
     b.e = b.p / ((gam - 1.0) * b.r);
   } else if (bc == 1) {  // velocity inflow

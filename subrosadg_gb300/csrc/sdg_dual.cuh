@@ -4,7 +4,7 @@
 // generic over its scalar type: with double it is the forward path, with Dual<1> it is its tangent-linear
 // model (exact, no differencing), and with Dual<K> seeded on K inputs it yields K columns of the pointwise
 // Jacobian, which the adjoint kernels contract with the adjoint vector (J^T lambda, column by column).
-// The scalar helpers below (fmaT, rcpT, sqrtT, fabsT, fmaxT, valueOf) are overloaded for double, where
+// The scalar helpers below (fmaT, rcpT, sqrtT, expT, logT, powT, fabsT, fmaxT, valueOf) are overloaded for double, where
 // they are the hardware operations the forward path uses, and for Dual<K>.
 #pragma once
 
@@ -178,6 +178,14 @@ template <int K> __device__ __forceinline__ Dual<K> logT(const Dual<K>& x) {
   Dual<K> o; o.v = log(x.v);
 #pragma unroll
   for (int k = 0; k < K; ++k) o.d[k] = ix * x.d[k];
+  return o;
+}
+__device__ __forceinline__ double powT(double x, double y) { return pow(x, y); }
+template <int K> __device__ __forceinline__ Dual<K> powT(const Dual<K>& x, double y) {
+  const double p = pow(x.v, y), dp = y * pow(x.v, y - 1.0);
+  Dual<K> o; o.v = p;
+#pragma unroll
+  for (int k = 0; k < K; ++k) o.d[k] = dp * x.d[k];
   return o;
 }
 __device__ __forceinline__ double fabsT(double x) { return fabs(x); }

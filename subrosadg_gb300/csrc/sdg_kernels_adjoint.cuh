@@ -537,7 +537,197 @@ struct AdjArgs {
   unsigned* status;
   int64_t ne, faceBase, nface;
   int n1d, epb;
+  // boundary faces (Euler): ghost states [face][j][rho, u, e, p]; cotangent of each boundary point's ghost
+  // primitive (rho, u, T), accumulated with weight ghostScale
+  const double* ghost;
+  double* lamGhost;
+  double ghostScale;
 };
+
+// ---- surface force (the reference's View force, VariableConvertor.cpp:883-906, Paraview.cpp:99-106) ------
+// Per boundary point of the selected faces: w_j |J_f| (p n - tau n) from the interior trace (and, for
+// Navier-Stokes, its gradient trace); n points out of the fluid.
+struct ForceArgs {
+  const double* face;       // traces [slot][nv][nfq]
+  const double* faceGrad;   // Navier-Stokes gradient traces [slot][nv*d][nfq] (or null)
+  const int* conn;          // boundary (slot, condition, 0)
+  const double* fgeo;       // boundary (n, |J_f|)
+  const int* select;        // [face] 1 for the faces of the group
+  const double* fw;         // face-rule weights [nfq]
+  double* out;              // force: [point][d]; cotangent: the trace cotangent slots [slot][nv][nfq]
+  double dir[3];            // cotangent: the direction of the force component
+  int64_t nface;
+  int n1d, ns;
+};
+
+template <int DIM>
+__global__ void __launch_bounds__(kFaceThreads) surfaceForceKernel(ForceArgs a, Phys ph) {
+  constexpr int NV = DIM + 2;
+  const int nfq = DIM == 2 ? a.n1d : a.n1d * a.n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  double* out = a.out + t * DIM;
+  if (!a.select[f]) {
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) out[k] = 0.0;
+    return;
+  }
+  const int64_t L = int64_t(a.conn[f * 3]) * NV * nfq + j;
+  double ul[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) ul[v] = a.face[L + v * nfq];
+  State<DIM> s;
+  makeState<DIM>(s, ul, ph);
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double wa = a.fw[j] * a.fgeo[f * 4 + 3];
+  double tn[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) tn[k] = 0.0;
+  if (a.ns) {
+    const int64_t LG = int64_t(a.conn[f * 3]) * NV * DIM * nfq + j;
+    double g[NV * DIM];
+#pragma unroll
+    for (int c = 0; c < NV * DIM; ++c) g[c] = a.faceGrad[LG + c * nfq];
+    PrimGrad<DIM> pg;
+    primitiveGradient<DIM>(g, s.u, s.ir, s.E * s.ir, ph, pg);
+    double tau[DIM][DIM], q[DIM];
+    viscousTensor<DIM>(pg, s.u, temperatureOf(s, ph), ph, tau, q);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+#pragma unroll
+      for (int m = 0; m < DIM; ++m) tn[k] = fma(tau[k][m], n[m], tn[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) out[k] = wa * fma(s.p, n[k], -tn[k]);
+}
+
+// Cotangent of the direction component of the Euler pressure force with respect to the interior traces:
+// w_j |J_f| (n.dir) dp/dU at each selected boundary point (zero elsewhere; the slots are boundary-owned).
+template <int DIM>
+__global__ void __launch_bounds__(kFaceThreads) surfaceForceTraceCotangentKernel(ForceArgs a, Phys ph) {
+  constexpr int NV = DIM + 2;
+  using DK = Dual<NV>;
+  const int nfq = DIM == 2 ? a.n1d : a.n1d * a.n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  const int64_t L = int64_t(a.conn[f * 3]) * NV * nfq + j;
+  double nd = 0.0;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) nd = fma(a.fgeo[f * 4 + k], a.dir[k], nd);
+  const double scale = a.select[f] ? a.fw[j] * a.fgeo[f * 4 + 3] * nd : 0.0;
+  DK x[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) { x[v] = DK(a.face[L + v * nfq]); x[v].d[v] = 1.0; }
+  State<DIM, DK> s;
+  makeState<DIM>(s, x, ph);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) a.out[L + v * nfq] = scale * s.p.d[v];
+}
+
+// ---- boundary faces (Euler) -------------------------------------------------------------------------
+// Boundary flux |J_f| F(U_b(U_L, g)).n (SpatialDiscrete.cpp:750-842): the tangent in the interior trace, and
+// its transpose to the trace and to the ghost primitive (rho, u, T) of the point, e = cv T and p from the
+// equation of state as the ghost states are built (VariableConvertor.cpp:341-380).
+template <int DIM, class T>
+__device__ __forceinline__ void boundaryFluxOf(const T* ul, const T* gprim, const double* n, int bc, const Phys& ph,
+                                               T* h) {
+  State<DIM, T> s;
+  makeState<DIM>(s, ul, ph);
+  Comp<DIM, T> l, g, b;
+  compFromState<DIM>(s, l, ph);
+  g.r = gprim[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) g.u[k] = gprim[1 + k];
+  g.e = ph.cv * gprim[DIM + 1];
+  g.p = ph.gm1 * g.r * g.e;
+  boundaryState<DIM>(bc, n, l, g, ph, b);
+  normalFluxComp<DIM>(b, n, h, ph);
+}
+
+template <int DIM>
+__device__ __forceinline__ void ghostPrimitive(const AdjArgs& a, int64_t point, const Phys& ph, double* gp) {
+  const double* g = a.ghost + point * (DIM + 3);
+  gp[0] = g[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) gp[1 + k] = g[1 + k];
+  gp[DIM + 1] = g[DIM + 1] * ph.inv_cv;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kFaceThreads) jvpBoundaryKernel(AdjArgs a, Phys ph) {
+  constexpr int NV = DIM + 2;
+  using D1 = Dual<1>;
+  const int n1d = a.n1d;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
+  const int64_t L = int64_t(sl) * NV * nfq + j;
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double area = a.fgeo[f * 4 + 3];
+  double gp[NV];
+  ghostPrimitive<DIM>(a, t, ph, gp);
+  D1 ul[NV], gd[NV], h[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    ul[v].v = a.face[L + v * nfq]; ul[v].d[0] = a.dface[L + v * nfq];
+    gd[v] = D1(gp[v]);
+  }
+  boundaryFluxOf<DIM>(ul, gd, n, bc, ph, h);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) a.dflux[L + v * nfq] = h[v].d[0] * area;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(kFaceThreads) vjpBoundaryKernel(AdjArgs a, Phys ph) {
+  constexpr int NV = DIM + 2;
+  using DK = Dual<NV>;
+  const int n1d = a.n1d;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
+  const int64_t L = int64_t(sl) * NV * nfq + j;
+  double n[DIM];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double area = a.fgeo[f * 4 + 3];
+  double lh[NV], ul[NV], gp[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) { lh[v] = a.lamH[L + v * nfq] * area; ul[v] = a.face[L + v * nfq]; }
+  ghostPrimitive<DIM>(a, t, ph, gp);
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {  // 0: the interior trace, 1: the ghost primitive
+    DK x[NV], g[NV], h[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      x[v] = DK(ul[v]);
+      g[v] = DK(gp[v]);
+      if (side == 0) x[v].d[v] = 1.0; else g[v].d[v] = 1.0;
+    }
+    boundaryFluxOf<DIM>(x, g, n, bc, ph, h);
+#pragma unroll
+    for (int w = 0; w < NV; ++w) {
+      double acc = 0.0;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc = fma(lh[v], h[v].d[w], acc);
+      if (side == 0) a.lamTr[L + w * nfq] = acc;
+      else if (a.lamGhost) a.lamGhost[t * NV + w] = fma(a.ghostScale, acc, a.lamGhost[t * NV + w]);
+    }
+  }
+}
 
 // ---- tangent-linear --------------------------------------------------------------------------------------
 // Face point: dH = |J_f| (dh/dUL dUL + dh/dUR dUR [+ dh/dG dG] + dmu/mu hv), scattered +/- as the forward.

@@ -1,4 +1,5 @@
-// Tangent-linear and adjoint face kernels (interior faces): the one translation unit that instantiates them.
+// Tangent-linear and adjoint face kernels (interior faces; boundary faces for Euler): the one translation unit that
+// instantiates them.
 #include "sdg_kernels_adjoint.cuh"
 #include "sdg_variants.hpp"
 
@@ -26,6 +27,10 @@ void fluxOf(int flux, AdjointKernels& k) {
 void adjointFaceKernels(int dim, int flux, bool visc, AdjointKernels& k) {
   if (dim == 2) { if (visc) fluxOf<2, true>(flux, k); else fluxOf<2, false>(flux, k); }
   else if (dim == 3) { if (visc) fluxOf<3, true>(flux, k); else fluxOf<3, false>(flux, k); }
+  if (!visc) {
+    k.jvpBoundary = dim == 2 ? reinterpret_cast<const void*>(&jvpBoundaryKernel<2>) : reinterpret_cast<const void*>(&jvpBoundaryKernel<3>);
+    k.vjpBoundary = dim == 2 ? reinterpret_cast<const void*>(&vjpBoundaryKernel<2>) : reinterpret_cast<const void*>(&vjpBoundaryKernel<3>);
+  }
 }
 
 }  // namespace sdg

@@ -253,6 +253,25 @@ class GpuSolver:
         self._chk(self.lib.sdg_launch_count(self.h, byref(n)))
         return n.value
 
+    def surface_force(self, physical):
+        """Force on boundary group `physical`: sum of w |J_f| (p n - tau n) over its face points."""
+        out = np.zeros(self.counts.dimension)
+        self._chk(self.lib.sdg_surface_force(self.h, int(physical), _ptr(out)))
+        return out
+
+    def surface_force_cotangent(self, physical, direction):
+        """d(direction . force)/dU at the volume points (Euler)."""
+        d = np.ascontiguousarray(np.asarray(direction, dtype=np.float64).reshape(-1)[: self.counts.dimension])
+        out = np.zeros((self.counts.volume_point_count, self.nv))
+        self._chk(self.lib.sdg_surface_force_cotangent(self.h, int(physical), _ptr(d), _ptr(out)))
+        return out
+
+    def adjoint_boundary_cotangent(self):
+        """Cotangent of each boundary point's ghost primitive (rho, u, T) from the last adjoint call (Euler)."""
+        out = np.zeros((self.counts.boundary_point_count, self.nv))
+        self._chk(self.lib.sdg_adjoint_boundary_cotangent(self.h, _ptr(out)))
+        return out
+
     def node_artificial_viscosity(self):
         """Artificial viscosity of the current state at every mesh node (zeros without shock capturing)."""
         out = np.zeros(len(self.mesh.nodes))

@@ -31,7 +31,39 @@ CASES = {
     "ns-quad-p4-br1-hllc": lambda: cases.vortex_case(n=3, p=4, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.05),
     "ns-quad-p3-br1-sutherland-lf": lambda: _sutherland(cases.vortex_case(n=4, p=3, flux=sdg.LAX_FRIEDRICHS,
                                                                           viscous=sdg.BR1, mu=0.05)),
+    # Euler with boundary faces (slip walls, velocity inflow, pressure outflow, Riemann farfield)
+    "euler-channel-quad-p3-roe": lambda: cases.channel_case(p=3, flux=sdg.ROE, n=3),
+    "euler-channel-farfield-quad-p2-hllc": lambda: cases.channel_case(p=2, flux=sdg.HLLC, n=3,
+                                                                      conditions=(sdg.RIEMANN_FARFIELD,) * 4),
+    "euler-box-walls-farfield-hex-p2-roe": lambda: _box3d(p=2, flux=sdg.ROE),
 }
+
+
+def _box3d(p=2, flux=sdg.ROE, n=3):
+    """3D compressible box [0,2]x[0,1]x[0,1]: slip walls on y and z, farfield in x."""
+    mesh = sdg.Mesh.box_3d(0, 0, 0, 2.0, 1.0, 1.0, 2 * n, n, n, periodic=False,
+                           boundary_conditions=[sdg.RIEMANN_FARFIELD, sdg.RIEMANN_FARFIELD] + [sdg.ADIABATIC_SLIP_WALL] * 4)
+    cfg = cases.config(p, flux)
+
+    def ic(pts):
+        x, y, z = pts[:, 0], pts[:, 1], pts[:, 2]
+        rho = 1.0 + 0.1 * np.sin(np.pi * x) * np.sin(np.pi * y)
+        out = np.zeros((len(pts), 5))
+        out[:, 0] = rho
+        out[:, 1] = 0.4 + 0.05 * np.cos(np.pi * z)
+        out[:, 2] = 0.05 * np.sin(np.pi * x)
+        out[:, 3] = 0.03 * np.sin(np.pi * y)
+        out[:, 4] = (1.0 + 0.05 * np.cos(np.pi * x)) / (rho * cases.R_GAS)
+        return out
+
+    def bc(pts, phys):
+        out = np.zeros((len(pts), 5))
+        out[:, 0] = 1.0
+        out[:, 1] = 0.4
+        out[:, 4] = 1.0 / cases.R_GAS
+        return out
+
+    return (mesh, cfg, ic, bc, 5e-4, 3)
 
 
 def _sutherland(case):
@@ -51,11 +83,14 @@ def smooth_perturbation(pts, nv, seed=11, amplitude=0.02):
 
 
 def make(name):
-    mesh, cfg, prim, _, dt, steps = CASES[name]()
+    mesh, cfg, prim, bprim, dt, steps = CASES[name]()
     s = sdg.GpuSolver(mesh, cfg, device=0)
     pts = s.volume_points()
     p0 = prim(pts)
     s.initialize_primitive(p0 * (1.0 + smooth_perturbation(pts, p0.shape[1])))
+    if s.counts.boundary_face_count:
+        bpts, phys = s.boundary_points()
+        s.set_boundary_primitive(bprim(bpts, np.repeat(phys, s.counts.face_point_count)))
     return s, dt
 
 
@@ -211,7 +246,7 @@ def test_derivatives_refuse_unsupported_configurations():
     with pytest.raises(sdg.SdgError) as e:
         hybrid.jvp_residual(np.zeros((hybrid.counts.volume_point_count, 4)))
     assert e.value.code == _abi.SDG_ERR_UNSUPPORTED
-    mesh, cfg, ic, bc, _, _ = cases.channel_case(p=2, n=3)
+    mesh, cfg, ic, bc, _, _ = cases.channel_case(p=2, n=3, viscous=sdg.BR1, mu=0.01)  # Navier-Stokes walls
     walls = sdg.GpuSolver(mesh, cfg, device=0)
     walls.initialize_primitive(ic(walls.volume_points()))
     with pytest.raises(sdg.SdgError) as e:
@@ -234,3 +269,71 @@ def test_recorded_trajectory_adjoint_equals_the_one_call_adjoint():
     with pytest.raises(sdg.SdgError) as e:
         b.adjoint_recorded(lamN)
     assert e.value.code == _abi.SDG_ERR_STATE
+
+
+# ---- surface force and boundary (freestream) gradients (Euler) -------------------------------------------
+
+def test_surface_force_of_a_fluid_at_rest_is_the_pressure_times_the_area():
+    """Uniform fluid at rest at p0 in a closed slip box [0,2]x[0,1]: the bottom wall (group 1, outward normal
+    -y) carries (0, -2 p0), the right wall (group 2) (p0, 0)."""
+    mesh = sdg.Mesh.box_2d(0.0, 0.0, 2.0, 1.0, 4, 2, periodic=False, boundary_conditions=[sdg.ADIABATIC_SLIP_WALL] * 4)
+    s = sdg.GpuSolver(mesh, cases.config(3, sdg.HLLC), device=0)
+    p0 = 1.7
+    prim = np.zeros((s.counts.volume_point_count, 4))
+    prim[:, 0] = 1.2
+    prim[:, 3] = p0 / (1.2 * cases.R_GAS)
+    s.initialize_primitive(prim)
+    bpts, _ = s.boundary_points()
+    s.set_boundary_primitive(np.repeat(prim[:1], len(bpts), 0))
+    np.testing.assert_allclose(s.surface_force(1), [0.0, -2.0 * p0], rtol=1e-14, atol=1e-14)
+    np.testing.assert_allclose(s.surface_force(2), [p0, 0.0], rtol=1e-14, atol=1e-14)
+
+
+@pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-box-walls-farfield-hex-p2-roe"])
+def test_surface_force_cotangent_matches_central_differences(name):
+    s, _ = make(name)
+    group, e = (1, [0.3, -1.0]) if s.counts.dimension == 2 else (3, [0.2, -1.0, 0.4])
+    u = s.state_point()
+    cot = s.surface_force_cotangent(group, e)
+    d = direction(u, 5)
+    h = 1e-6
+    s.set_state_point(u + h * d)
+    jp = float(np.dot(s.surface_force(group), e))
+    s.set_state_point(u - h * d)
+    jm = float(np.dot(s.surface_force(group), e))
+    s.set_state_point(u)
+    fd = (jp - jm) / (2 * h)
+    assert abs(float(np.sum(cot * d)) - fd) <= 1e-7 * abs(fd), (float(np.sum(cot * d)), fd)
+
+
+@pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-channel-farfield-quad-p2-hllc",
+                                  "euler-box-walls-farfield-hex-p2-roe"])
+def test_force_gradient_through_a_trajectory(name):
+    """J = e . force on a wall after N steps: dJ/dU_0 in a seeded direction and dJ/d(boundary primitives) in a
+    seeded direction of every boundary point's (rho, u, T), against central differences of the trajectory."""
+    s, dt = make(name)
+    group, e = (1, [0.3, -1.0]) if s.counts.dimension == 2 else (3, [0.2, -1.0, 0.4])
+    steps = 6
+    u0 = s.state_point()
+    bpts, phys = s.boundary_points()
+    g0 = CASES[name]()[3](bpts, np.repeat(phys, s.counts.face_point_count))
+
+    def J(u, g):
+        s.set_state_point(u)
+        s.set_boundary_primitive(g)
+        s.stepSolver(dt, steps)
+        return float(np.dot(s.surface_force(group), e))
+
+    s.set_state_point(u0)
+    s.set_boundary_primitive(g0)
+    s.forward_steps(dt, steps, 2)
+    cot = s.surface_force_cotangent(group, e)
+    gu, _ = s.adjoint_recorded(cot)
+    gg = s.adjoint_boundary_cotangent()
+    du = direction(u0, 7)
+    dg = direction(g0, 8)
+    h = 1e-6
+    fd_u = (J(u0 + h * du, g0) - J(u0 - h * du, g0)) / (2 * h)
+    fd_g = (J(u0, g0 + h * dg) - J(u0, g0 - h * dg)) / (2 * h)
+    assert abs(float(np.sum(gu * du)) - fd_u) <= 1e-6 * abs(fd_u), (float(np.sum(gu * du)), fd_u)
+    assert abs(float(np.sum(gg * dg)) - fd_g) <= 1e-6 * abs(fd_g), (float(np.sum(gg * dg)), fd_g)
