@@ -72,7 +72,9 @@ struct AdjointState {
   double* pts = nullptr;           // point-layout conversion buffer
   std::vector<double*> pool;       // checkpoints and stage states (grown on demand)
   double* muAcc = nullptr;         // device accumulator of dJ/dmu
-  double* lamGhost = nullptr;      // Euler with boundary faces: cotangent of each boundary point's ghost primitive
+  double* lamGhost = nullptr;      // with boundary faces: cotangent of each boundary point's ghost primitive
+  bool ghostPending = false;       // lamGhost holds a functional's own part for the next reverse sweep
+  int64_t muBoundary = 0;          // dJ/dmu partial slots of the boundary kernel (Navier-Stokes)
   Trajectory traj;
   // Navier-Stokes forward quantities of every stage input of one checkpoint segment (traces, node gradient,
   // gradient traces), kept by the segment's recompute so the reverse stages read them instead of recomputing
@@ -116,8 +118,6 @@ AdjointState* adjoint(sdg_handle* h) {
   for (const DevBlock& B : h->blocks)
     if (B.kind != kTensor || !B.affine)
       throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (quadrangles P>=2, hexahedra)");
-  if (h->nBoundary > 0 && h->ns)
-    throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes derivatives need a mesh without boundary faces (periodic)");
   if (h->ns && h->cfg.viscous_flux != SDG_VISCOUS_BR1) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of BR2 are not built");
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
   if (h->ph.incomp || h->ph.source)
@@ -139,7 +139,8 @@ AdjointState* adjoint(sdg_handle* h) {
   }
   for (const DevBlock& B : h->blocks) A->muTiles += (B.ne + A->k.epb - 1) / A->k.epb;
   A->muFaces = (h->nInterior * h->nfq + kFaceThreads - 1) / kFaceThreads;
-  A->muPart = alloc(size_t(A->muTiles + A->muFaces));
+  A->muBoundary = h->ns ? (h->nBoundary * h->nfq + kFaceThreads - 1) / kFaceThreads : 0;
+  A->muPart = alloc(size_t(A->muTiles + A->muFaces + A->muBoundary));
   A->pts = alloc(size_t(h->volumePoints) * h->nv);
   A->muAcc = alloc(1);
   SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
@@ -157,7 +158,7 @@ AdjointState* adjoint(sdg_handle* h) {
     SDG_CUDA(cudaMemsetAsync(A->lamTg, 0, F * h->dim * 8, h->stream));
     SDG_CUDA(cudaMemsetAsync(A->lamUp, 0, F * 8, h->stream));
   }
-  SDG_CUDA(cudaMemsetAsync(A->muPart, 0, size_t(A->muTiles + A->muFaces) * 8, h->stream));
+  SDG_CUDA(cudaMemsetAsync(A->muPart, 0, size_t(A->muTiles + A->muFaces + A->muBoundary) * 8, h->stream));
   h->adj = A.release();
   return h->adj;
 }
@@ -215,15 +216,27 @@ void traces(sdg_handle* h, const double* u, double* face) {
 
 // BR1 gradient pass of state `u` whose traces are in `face`: neighbour traces into `other`, node gradient
 // into `grad`, gradient traces into `faceGrad` (the forward kernels; linear, so they serve tangents too).
-void gradientOf(sdg_handle* h, const double* u, double* face, double* other, double* grad, double* faceGrad) {
+// tangent: u, face are a tangent state and its traces; the boundary exchange (the walls' states) is then the
+// linearisation at the forward traces in h->face.
+void gradientOf(sdg_handle* h, const double* u, double* face, double* other, double* grad, double* faceGrad,
+                bool tangent = false) {
   std::vector<Rec> recs;
   Rec x = faceRec(h, kOpExchange);
   x.fa.face = face; x.fa.other = other;
   recs.push_back(x);
-  if (h->nBoundary > 0) {
+  if (h->nBoundary > 0 && !tangent) {
     Rec xb = faceRec(h, kOpExchangeBoundary);
     xb.fa.face = face; xb.fa.other = other;
     recs.push_back(xb);
+  }
+  if (h->nBoundary > 0 && tangent) {
+    runRecs(h, recs, h->stream);
+    recs.clear();
+    AdjArgs b = baseArgs(h, nullptr, nullptr);
+    b.conn = h->bconn; b.fgeo = h->bgeo; b.nface = h->nBoundary; b.ghost = h->ghost;
+    b.dface = face; b.dother = other;
+    launch(h, h->adj->k.jvpExchangeBoundary, (h->nBoundary * h->nfq + kFaceThreads - 1) / kFaceThreads, kFaceThreads, 0,
+           b, true);
   }
   for (DevBlock& B : h->blocks) {
     Rec r = gradRec(h, B, 0);
@@ -248,7 +261,7 @@ void tangentFaces(sdg_handle* h, double dmu) {
   launch(h, A->k.jvpFace, faceGrid(h), kFaceThreads, 0, a, true);
   if (h->nBoundary > 0) {
     AdjArgs b = boundaryArgs(h);
-    b.dface = A->dface; b.dflux = A->dflux;
+    b.dface = A->dface; b.dfaceGrad = A->dfaceGrad; b.dflux = A->dflux; b.dmu = dmu;
     launch(h, A->k.jvpBoundary, boundaryGrid(h), kFaceThreads, 0, b, true);
   }
 }
@@ -277,7 +290,7 @@ void jvpResidual(sdg_handle* h, const double* du, double dmu, double* drate) {
   AdjointState* A = h->adj;
   forwardAt(h, h->state[1]);
   traces(h, du, A->dface);
-  if (h->ns) gradientOf(h, du, A->dface, A->dfaceOther, A->dgrad, A->dfaceGrad);
+  if (h->ns) gradientOf(h, du, A->dface, A->dfaceOther, A->dgrad, A->dfaceGrad, true);
   tangentFaces(h, dmu);
   tangentElements(h, h->state[1], du, dmu, drate, nullptr, nullptr, 0.0, 0.0, 0.0);
 }
@@ -303,9 +316,10 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
     a.lamH = A->lamH; a.lamTr = A->lamTr; a.lamTg = A->lamTg; a.muPart = A->muPart + A->muTiles;
     launch(h, A->k.vjpFace, faceGrid(h), kFaceThreads, 0, a, true);
   }
-  if (h->nBoundary > 0) {  // boundary slots of lamTr, and the ghost cotangent (weight ghostScale)
+  if (h->nBoundary > 0) {  // boundary slots of lamTr (NS: lamTg), and the ghost cotangent (weight ghostScale)
     AdjArgs b = boundaryArgs(h);
-    b.lamH = A->lamH; b.lamTr = A->lamTr; b.lamGhost = A->lamGhost; b.ghostScale = ghostScale;
+    b.lamH = A->lamH; b.lamTr = A->lamTr; b.lamTg = A->lamTg; b.lamGhost = A->lamGhost; b.ghostScale = ghostScale;
+    b.muPart = A->muPart + A->muTiles + A->muFaces;
     launch(h, A->k.vjpBoundary, boundaryGrid(h), kFaceThreads, 0, b, true);
   }
   if (h->ns) {
@@ -317,6 +331,11 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
     AdjArgs a = baseArgs(h, nullptr, nullptr);
     a.lamUp = A->lamUp; a.lamTr = A->lamTr;
     launch(h, A->k.vjpExchange, faceGrid(h), kFaceThreads, 0, a, false);
+    if (h->nBoundary > 0) {
+      AdjArgs b = boundaryArgs(h);
+      b.lamUp = A->lamUp; b.lamTr = A->lamTr; b.lamGhost = A->lamGhost; b.ghostScale = ghostScale;
+      launch(h, A->k.vjpExchangeBoundary, boundaryGrid(h), kFaceThreads, 0, b, true);
+    }
   }
   for (DevBlock& B : h->blocks) {
     AdjArgs a = baseArgs(h, &B, h->state[1]);
@@ -329,7 +348,7 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
     launch(h, A->k.vjpTrace, tiles(h, B), NT, A->k.vjpSmem, a, false);
   }
   if (!h->ns) return;
-  muAccumulateKernel<<<1, 256, 0, h->stream>>>(A->muPart, A->muTiles + A->muFaces, muScale, A->muAcc);
+  muAccumulateKernel<<<1, 256, 0, h->stream>>>(A->muPart, A->muTiles + A->muFaces + A->muBoundary, muScale, A->muAcc);
   SDG_CUDA(cudaGetLastError());
   h->launches++;
 }
@@ -391,7 +410,7 @@ void jvpSteps(sdg_handle* h, int steps, double dt, double dmu) {
       for (const Rec& r : stages[s]) (r.seq % 8 < 3 ? flux : update).push_back(r);
       if (h->ns) {
         runRecs(h, flux, h->stream);  // forward gradient pass and viscous face fluxes (traces stay in face)
-        gradientOf(h, A->dU[in], A->dface, A->dfaceOther, A->dgrad, A->dfaceGrad);
+        gradientOf(h, A->dU[in], A->dface, A->dfaceOther, A->dgrad, A->dfaceGrad, true);
         tangentFaces(h, dmu);
       } else {
         tangentFaces(h, dmu);         // reads the traces before the Euler face kernel overwrites them
@@ -500,7 +519,8 @@ double backwardSweep(sdg_handle* h) {
   const bool keep = forwardStore(h, size_t(interval) * S);
   SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
   SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
-  clearGhost(h);
+  if (!A->ghostPending) clearGhost(h);  // a functional's cotangent may have left its own ghost part
+  A->ghostPending = false;
   const double muScale = h->ns && h->ph.mu > 0.0 ? 1.0 / h->ph.mu : 0.0;
   for (int g = segments - 1; g >= 0; --g) {
     const int n0 = g * interval, n1 = std::min(steps, n0 + interval);
@@ -631,6 +651,7 @@ int sdg_vjp_residual(sdg_handle* h, const double* rate_cotangent, double* cotang
     forwardAt(h, h->state[1]);
     SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
     clearGhost(h);
+    A->ghostPending = false;
     vjpResidual(h, A->lamIn, nullptr, nullptr, nullptr, false, 0.0, 0.0, 0.0,
                 h->ns && h->ph.mu > 0.0 ? 1.0 / h->ph.mu : 0.0, 1.0);
     downloadPoints(h, A->lamU, cotangent);
@@ -747,21 +768,41 @@ int sdg_surface_force_cotangent(sdg_handle* h, int32_t physical, const double* d
   if (!h || !direction || !cotangent) return SDG_ERR_INVALID_ARGUMENT;
   try {
     AdjointState* A = adjoint(h);
-    if (h->ns) throw Failure(SDG_ERR_UNSUPPORTED, "the surface-force cotangent is built for the Euler equations");
     SDG_CUDA(cudaSetDevice(h->device));
+    // forward quantities of the current state: traces (kept by the step) and, NS, the gradient pass
+    if (h->ns) gradientOf(h, h->state[0], h->face, h->faceOther, h->grad, h->faceGrad);
     ForceInputs in;
     ForceArgs a = forceInputs(h, physical, in, false);
     for (int k = 0; k < h->dim; ++k) a.dir[k] = direction[k];
     a.out = A->lamTr;
     SDG_CUDA(cudaMemsetAsync(A->lamTr, 0, h->faceCount * 8, h->stream));
     SDG_CUDA(cudaMemsetAsync(A->lamU, 0, h->stateCount * 8, h->stream));
+    if (h->ns) {
+      SDG_CUDA(cudaMemsetAsync(A->lamTg, 0, h->faceCount * h->dim * 8, h->stream));
+      SDG_CUDA(cudaMemsetAsync(A->lamG, 0, h->gradCount * 8, h->stream));
+    }
+    clearGhost(h);
     const int64_t pts = h->nBoundary * h->nfq;
     const unsigned grid = unsigned((pts + kFaceThreads - 1) / kFaceThreads);
-    if (h->dim == 2) surfaceForceTraceCotangentKernel<2><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
-    else surfaceForceTraceCotangentKernel<3><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
+    if (h->dim == 2) surfaceForceTraceCotangentKernel<2><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph, A->lamTg);
+    else surfaceForceTraceCotangentKernel<3><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph, A->lamTg);
     SDG_CUDA(cudaGetLastError());
     h->launches++;
-    // the transposed trace operator: lamU = T^T lamTr (the element kernel of the reverse without its
+    if (h->ns) {  // the gradient traces' cotangent back through the gradient pass (vjpResidual's NS part)
+      for (DevBlock& B : h->blocks) {
+        AdjArgs g = baseArgs(h, &B, h->state[0]);
+        g.lamG = A->lamG + B.gradOffset; g.lamTg = A->lamTg; g.lamU = A->lamU + B.stateOffset; g.lamUp = A->lamUp;
+        launch(h, A->k.vjpGradient, tiles(h, B), A->k.threads, A->k.vjpSmem, g, false);
+      }
+      AdjArgs x = baseArgs(h, nullptr, nullptr);
+      x.lamUp = A->lamUp; x.lamTr = A->lamTr;
+      launch(h, A->k.vjpExchange, faceGrid(h), kFaceThreads, 0, x, false);
+      AdjArgs b = boundaryArgs(h);
+      b.lamUp = A->lamUp; b.lamTr = A->lamTr; b.lamGhost = A->lamGhost; b.ghostScale = 1.0;
+      launch(h, A->k.vjpExchangeBoundary, boundaryGrid(h), kFaceThreads, 0, b, true);
+    }
+    A->ghostPending = true;  // the functional's own ghost dependence joins the next reverse sweep's
+    // the transposed trace operator: lamU += T^T lamTr (the element kernel of the reverse without its
     // volume and RK parts)
     for (DevBlock& B : h->blocks) {
       AdjArgs t = baseArgs(h, &B, h->state[0]);

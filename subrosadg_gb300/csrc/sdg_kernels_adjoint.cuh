@@ -537,8 +537,9 @@ struct AdjArgs {
   unsigned* status;
   int64_t ne, faceBase, nface;
   int n1d, epb;
-  // boundary faces (Euler): ghost states [face][j][rho, u, e, p]; cotangent of each boundary point's ghost
-  // primitive (rho, u, T), accumulated with weight ghostScale
+  // boundary faces: ghost states [face][j][rho, u, e, p]; cotangent of each boundary point's ghost
+  // primitive (rho, u, T), accumulated with weight ghostScale; NS: the tangent of the neighbour traces
+  double* dother;
   const double* ghost;
   double* lamGhost;
   double ghostScale;
@@ -605,29 +606,72 @@ __global__ void __launch_bounds__(kFaceThreads) surfaceForceKernel(ForceArgs a, 
   for (int k = 0; k < DIM; ++k) out[k] = wa * fma(s.p, n[k], -tn[k]);
 }
 
-// Cotangent of the direction component of the Euler pressure force with respect to the interior traces:
-// w_j |J_f| (n.dir) dp/dU at each selected boundary point (zero elsewhere; the slots are boundary-owned).
+// dir . (p n - tau n) at a boundary point from its trace and (Navier-Stokes) gradient trace, generic.
+template <int DIM, class T>
+__device__ __forceinline__ T forceDotOf(const T* ul, const T* gr, const double* n, const double* dir, bool ns,
+                                        const Phys& ph) {
+  State<DIM, T> s;
+  makeState<DIM>(s, ul, ph);
+  double nd = 0.0;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) nd = fma(n[k], dir[k], nd);
+  T out = s.p * nd;
+  if (ns) {
+    PrimGrad<DIM, T> pg;
+    primitiveGradient<DIM>(gr, s.u, s.ir, s.E * s.ir, ph, pg);
+    T tau[DIM][DIM], q[DIM];
+    viscousTensor<DIM>(pg, s.u, temperatureOf(s, ph), ph, tau, q);
+#pragma unroll
+    for (int k = 0; k < DIM; ++k)
+#pragma unroll
+      for (int m = 0; m < DIM; ++m) out = out - dir[k] * tau[k][m] * n[m];
+  }
+  return out;
+}
+
+// Cotangent of the direction component of the force with respect to the interior traces (and, Navier-Stokes,
+// the gradient traces) of the selected boundary points; zero elsewhere (the slots are boundary-owned).
+// out: trace slots [slot][nv][nfq]; outG: gradient-trace slots [slot][nv*d][nfq].
 template <int DIM>
-__global__ void __launch_bounds__(kFaceThreads) surfaceForceTraceCotangentKernel(ForceArgs a, Phys ph) {
-  constexpr int NV = DIM + 2;
+__global__ void __launch_bounds__(kFaceThreads) surfaceForceTraceCotangentKernel(ForceArgs a, Phys ph, double* outG) {
+  constexpr int NV = DIM + 2, NG = NV * DIM;
   using DK = Dual<NV>;
+  using DG = Dual<NG>;
   const int nfq = DIM == 2 ? a.n1d : a.n1d * a.n1d;
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
-  const int64_t L = int64_t(a.conn[f * 3]) * NV * nfq + j;
-  double nd = 0.0;
+  const int64_t L = int64_t(a.conn[f * 3]) * NV * nfq + j, LG = int64_t(a.conn[f * 3]) * NG * nfq + j;
+  double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) nd = fma(a.fgeo[f * 4 + k], a.dir[k], nd);
-  const double scale = a.select[f] ? a.fw[j] * a.fgeo[f * 4 + 3] * nd : 0.0;
-  DK x[NV];
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double scale = a.select[f] ? a.fw[j] * a.fgeo[f * 4 + 3] : 0.0;
+  double ul[NV], gg[NG];
 #pragma unroll
-  for (int v = 0; v < NV; ++v) { x[v] = DK(a.face[L + v * nfq]); x[v].d[v] = 1.0; }
-  State<DIM, DK> s;
-  makeState<DIM>(s, x, ph);
+  for (int v = 0; v < NV; ++v) ul[v] = a.face[L + v * nfq];
 #pragma unroll
-  for (int v = 0; v < NV; ++v) a.out[L + v * nfq] = scale * s.p.d[v];
+  for (int c = 0; c < NG; ++c) gg[c] = a.ns ? a.faceGrad[LG + c * nfq] : 0.0;
+  {
+    DK x[NV], gr[NG];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) { x[v] = DK(ul[v]); x[v].d[v] = 1.0; }
+#pragma unroll
+    for (int c = 0; c < NG; ++c) gr[c] = DK(gg[c]);
+    const DK J = forceDotOf<DIM>(x, gr, n, a.dir, a.ns != 0, ph);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) a.out[L + v * nfq] = scale * J.d[v];
+  }
+  if (a.ns) {
+    DG x[NV], gr[NG];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) x[v] = DG(ul[v]);
+#pragma unroll
+    for (int c = 0; c < NG; ++c) { gr[c] = DG(gg[c]); gr[c].d[c] = 1.0; }
+    const DG J = forceDotOf<DIM>(x, gr, n, a.dir, true, ph);
+#pragma unroll
+    for (int c = 0; c < NG; ++c) outG[LG + c * nfq] = scale * J.d[c];
+  }
 }
 
 // ---- boundary faces (Euler) -------------------------------------------------------------------------
@@ -651,12 +695,251 @@ __device__ __forceinline__ void boundaryFluxOf(const T* ul, const T* gprim, cons
 }
 
 template <int DIM>
-__device__ __forceinline__ void ghostPrimitive(const AdjArgs& a, int64_t point, const Phys& ph, double* gp) {
-  const double* g = a.ghost + point * (DIM + 3);
+__device__ __forceinline__ void ghostPrimitiveOf(const double* ghost, int64_t point, const Phys& ph, double* gp) {
+  const double* g = ghost + point * (DIM + 3);
   gp[0] = g[0];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) gp[1 + k] = g[1 + k];
   gp[DIM + 1] = g[DIM + 1] * ph.inv_cv;
+}
+
+__device__ __forceinline__ void blockSum(double x, double* part, double* sRed);
+
+// Navier-Stokes boundary flux (faceNSBoundaryPoint's arithmetic, generic): convective flux of the boundary
+// state minus the average of the viscous fluxes of (walls: the wall state; else the interior) and of the
+// boundary state, both with the interior primitive gradient (adiabatic walls: no temperature gradient on the
+// boundary side).  hv = the viscous part (linear in the viscosity).
+template <int DIM, class T>
+__device__ __forceinline__ void boundaryNSFluxOf(const T* ul, const T* gr, const T* gprim, const double* n, int bc,
+                                                 const Phys& ph, T* h, T* hv) {
+  constexpr int NV = DIM + 2;
+  State<DIM, T> s;
+  makeState<DIM>(s, ul, ph);
+  Comp<DIM, T> l, g, b;
+  compFromState<DIM>(s, l, ph);
+  g.r = gprim[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) g.u[k] = gprim[1 + k];
+  g.e = ph.cv * gprim[DIM + 1];
+  g.p = ph.gm1 * g.r * g.e;
+  boundaryState<DIM>(bc, n, l, g, ph, b);
+  normalFluxComp<DIM>(b, n, h, ph);
+  PrimGrad<DIM, T> pl;
+  primitiveGradient<DIM>(gr, s.u, s.ir, s.E * s.ir, ph, pl);
+  const Comp<DIM, T>& lm = bc >= 3 ? b : l;
+  T fl[NV], fb[NV];
+  viscousNormalFlux<DIM>(pl, lm.u, lm.e * ph.inv_cv, n, ph, fl);
+  PrimGrad<DIM, T> pb = pl;
+  if (bc >= 4) {
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) pb.gT[k] = T(0.0);
+  }
+  viscousNormalFlux<DIM>(pb, b.u, b.e * ph.inv_cv, n, ph, fb);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    hv[v] = -0.5 * (fl[v] + fb[v]);
+    h[v] = h[v] + hv[v];
+  }
+}
+
+// Neighbour trace of the gradient pass at a boundary point (exchangeBoundaryPoint, generic): 2 U_b - U with
+// U_b = U for farfield / inflow / outflow and the wall's boundary state otherwise.
+template <int DIM, class T>
+__device__ __forceinline__ void boundaryOtherOf(const T* ul, const T* gprim, const double* n, int bc, const Phys& ph,
+                                                T* other) {
+  constexpr int NV = DIM + 2;
+  if (bc <= 2) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) other[v] = ul[v];
+    return;
+  }
+  State<DIM, T> s;
+  makeState<DIM>(s, ul, ph);
+  Comp<DIM, T> l, g, b;
+  compFromState<DIM>(s, l, ph);
+  g.r = gprim[0];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) g.u[k] = gprim[1 + k];
+  g.e = ph.cv * gprim[DIM + 1];
+  g.p = ph.gm1 * g.r * g.e;
+  boundaryState<DIM>(bc, n, l, g, ph, b);
+  T ub[NV];
+  ub[0] = b.r;
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) ub[1 + k] = b.r * b.u[k];
+  ub[DIM + 1] = energyOfComp<DIM>(b, ph);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) other[v] = 2.0 * ub[v] - ul[v];
+}
+
+// Tangent of the boundary exchange: dother = (2 dU_b/dU - I) dU.
+template <int DIM>
+__global__ void __launch_bounds__(kFaceThreads) jvpExchangeBoundaryKernel(AdjArgs a, Phys ph) {
+  constexpr int NV = DIM + 2;
+  using D1 = Dual<1>;
+  const int n1d = a.n1d;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
+  const int64_t L = int64_t(sl) * NV * nfq + j;
+  double n[DIM], gp[NV];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
+  D1 ul[NV], gd[NV], o[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    ul[v].v = a.face[L + v * nfq]; ul[v].d[0] = a.dface[L + v * nfq];
+    gd[v] = D1(gp[v]);
+  }
+  boundaryOtherOf<DIM>(ul, gd, n, bc, ph, o);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) a.dother[L + v * nfq] = o[v].d[0];
+}
+
+// Transpose of the boundary exchange: lamTr += (2 dU_b/dU - I)^T lamUp; ghost += 2 (dU_b/dg)^T lamUp.
+template <int DIM>
+__global__ void __launch_bounds__(kFaceThreads) vjpExchangeBoundaryKernel(AdjArgs a, Phys ph) {
+  constexpr int NV = DIM + 2;
+  using DK = Dual<NV>;
+  const int n1d = a.n1d;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
+  const int64_t L = int64_t(sl) * NV * nfq + j;
+  double n[DIM], gp[NV], lo[NV], ul[NV];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
+#pragma unroll
+  for (int v = 0; v < NV; ++v) { lo[v] = a.lamUp[L + v * nfq]; ul[v] = a.face[L + v * nfq]; }
+#pragma unroll
+  for (int side = 0; side < 2; ++side) {
+    DK x[NV], g[NV], o[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      x[v] = DK(ul[v]);
+      g[v] = DK(gp[v]);
+      if (side == 0) x[v].d[v] = 1.0; else g[v].d[v] = 1.0;
+    }
+    boundaryOtherOf<DIM>(x, g, n, bc, ph, o);
+#pragma unroll
+    for (int w = 0; w < NV; ++w) {
+      double acc = 0.0;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc = fma(lo[v], o[v].d[w], acc);
+      if (side == 0) a.lamTr[L + w * nfq] += acc;
+      else if (a.lamGhost) a.lamGhost[t * NV + w] = fma(a.ghostScale, acc, a.lamGhost[t * NV + w]);
+    }
+  }
+}
+
+// Navier-Stokes boundary-face tangent: dH = |J_f| (dh/dU dU + dh/dG dG + dmu/mu hv).
+template <int DIM>
+__global__ void __launch_bounds__(kFaceThreads) jvpBoundaryNSKernel(AdjArgs a, Phys ph) {
+  constexpr int NV = DIM + 2;
+  using D1 = Dual<1>;
+  const int n1d = a.n1d;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  if (f >= a.nface) return;
+  const int j = int(t - f * nfq);
+  const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
+  const int64_t L = int64_t(sl) * NV * nfq + j, LG = int64_t(sl) * NV * DIM * nfq + j;
+  double n[DIM], gp[NV];
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  const double area = a.fgeo[f * 4 + 3];
+  ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
+  D1 ul[NV], gd[NV], gr[NV * DIM], h[NV], hv[NV];
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    ul[v].v = a.face[L + v * nfq]; ul[v].d[0] = a.dface[L + v * nfq];
+    gd[v] = D1(gp[v]);
+  }
+#pragma unroll
+  for (int c = 0; c < NV * DIM; ++c) { gr[c].v = a.faceGrad[LG + c * nfq]; gr[c].d[0] = a.dfaceGrad[LG + c * nfq]; }
+  boundaryNSFluxOf<DIM>(ul, gr, gd, n, bc, ph, h, hv);
+  const double mscale = ph.mu > 0.0 ? a.dmu / ph.mu : 0.0;
+#pragma unroll
+  for (int v = 0; v < NV; ++v) a.dflux[L + v * nfq] = fma(mscale, hv[v].v, h[v].d[0]) * area;
+}
+
+// Navier-Stokes boundary-face transpose: the trace (Dual<d+2>), gradient-trace (Dual<(d+2)d>) and ghost
+// (Dual<d+2>) cotangents, and the viscosity term <lam_h, hv>.
+template <int DIM>
+__global__ void __launch_bounds__(kFaceThreads) vjpBoundaryNSKernel(AdjArgs a, Phys ph) {
+  constexpr int NV = DIM + 2, NG = NV * DIM;
+  using DK = Dual<NV>;
+  using DG = Dual<NG>;
+  __shared__ double sRed[kFaceThreads / 32];
+  const int n1d = a.n1d;
+  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t f = t / nfq;
+  double mupart = 0.0;
+  if (f < a.nface) {
+    const int j = int(t - f * nfq);
+    const int sl = a.conn[f * 3 + 0], bc = a.conn[f * 3 + 1];
+    const int64_t L = int64_t(sl) * NV * nfq + j, LG = int64_t(sl) * NV * DIM * nfq + j;
+    double n[DIM], gp[NV], lh[NV], ul[NV], gg[NG];
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+    const double area = a.fgeo[f * 4 + 3];
+    ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) { lh[v] = a.lamH[L + v * nfq] * area; ul[v] = a.face[L + v * nfq]; }
+#pragma unroll
+    for (int c = 0; c < NG; ++c) gg[c] = a.faceGrad[LG + c * nfq];
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {  // 0: the trace, 1: the ghost primitive
+      DK x[NV], g[NV], gr[NG], h[NV], hv[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        x[v] = DK(ul[v]);
+        g[v] = DK(gp[v]);
+        if (side == 0) x[v].d[v] = 1.0; else g[v].d[v] = 1.0;
+      }
+#pragma unroll
+      for (int c = 0; c < NG; ++c) gr[c] = DK(gg[c]);
+      boundaryNSFluxOf<DIM>(x, gr, g, n, bc, ph, h, hv);
+      if (side == 0) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) mupart = fma(lh[v], hv[v].v, mupart);
+      }
+#pragma unroll
+      for (int w = 0; w < NV; ++w) {
+        double acc = 0.0;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc = fma(lh[v], h[v].d[w], acc);
+        if (side == 0) a.lamTr[L + w * nfq] = acc;
+        else if (a.lamGhost) a.lamGhost[t * NV + w] = fma(a.ghostScale, acc, a.lamGhost[t * NV + w]);
+      }
+    }
+    {  // gradient traces
+      DG x[NV], g[NV], gr[NG], h[NV], hv[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) { x[v] = DG(ul[v]); g[v] = DG(gp[v]); }
+#pragma unroll
+      for (int c = 0; c < NG; ++c) { gr[c] = DG(gg[c]); gr[c].d[c] = 1.0; }
+      boundaryNSFluxOf<DIM>(x, gr, g, n, bc, ph, h, hv);
+#pragma unroll
+      for (int c = 0; c < NG; ++c) {
+        double acc = 0.0;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc = fma(lh[v], h[v].d[c], acc);
+        a.lamTg[LG + c * nfq] = acc;
+      }
+    }
+  }
+  blockSum(mupart, a.muPart + blockIdx.x, sRed);
 }
 
 template <int DIM>
@@ -676,7 +959,7 @@ __global__ void __launch_bounds__(kFaceThreads) jvpBoundaryKernel(AdjArgs a, Phy
   for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
   const double area = a.fgeo[f * 4 + 3];
   double gp[NV];
-  ghostPrimitive<DIM>(a, t, ph, gp);
+  ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
   D1 ul[NV], gd[NV], h[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
@@ -707,7 +990,7 @@ __global__ void __launch_bounds__(kFaceThreads) vjpBoundaryKernel(AdjArgs a, Phy
   double lh[NV], ul[NV], gp[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) { lh[v] = a.lamH[L + v * nfq] * area; ul[v] = a.face[L + v * nfq]; }
-  ghostPrimitive<DIM>(a, t, ph, gp);
+  ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
 #pragma unroll
   for (int side = 0; side < 2; ++side) {  // 0: the interior trace, 1: the ghost primitive
     DK x[NV], g[NV], h[NV];

@@ -43,8 +43,10 @@ struct AdjointKernels {
   const void* vjpVolume = nullptr;    // (AdjArgs, Phys)
   const void* vjpGradient = nullptr;  // (AdjArgs)
   const void* vjpTrace = nullptr;     // (AdjArgs)
-  const void* jvpBoundary = nullptr;  // (AdjArgs, Phys), one thread per boundary face point (Euler)
+  const void* jvpBoundary = nullptr;  // (AdjArgs, Phys), one thread per boundary face point
   const void* vjpBoundary = nullptr;  // (AdjArgs, Phys)
+  const void* jvpExchangeBoundary = nullptr;  // (AdjArgs, Phys), Navier-Stokes: the gradient pass's wall states
+  const void* vjpExchangeBoundary = nullptr;  // (AdjArgs, Phys)
   int epb = 0, threads = 0;
   size_t jvpSmem = 0, vjpSmem = 0;
   bool valid() const { return jvpStage && jvpFace; }

@@ -36,14 +36,25 @@ CASES = {
     "euler-channel-farfield-quad-p2-hllc": lambda: cases.channel_case(p=2, flux=sdg.HLLC, n=3,
                                                                       conditions=(sdg.RIEMANN_FARFIELD,) * 4),
     "euler-box-walls-farfield-hex-p2-roe": lambda: _box3d(p=2, flux=sdg.ROE),
+    # Navier-Stokes BR1 with walls (isothermal / adiabatic no-slip, slip), inflow, outflow, farfield
+    "ns-channel-walls-quad-p3-br1-roe": lambda: cases.channel_case(
+        p=3, flux=sdg.ROE, n=3, viscous=sdg.BR1, mu=0.01,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "ns-channel-farfield-quad-p2-br1-hllc": lambda: cases.channel_case(
+        p=2, flux=sdg.HLLC, n=3, viscous=sdg.BR1, mu=0.02,
+        conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD)),
+    "ns-box-walls-hex-p2-br1-roe": lambda: _box3d(p=2, flux=sdg.ROE, viscous=True),
 }
 
 
-def _box3d(p=2, flux=sdg.ROE, n=3):
-    """3D compressible box [0,2]x[0,1]x[0,1]: slip walls on y and z, farfield in x."""
+def _box3d(p=2, flux=sdg.ROE, n=3, viscous=False):
+    """3D compressible box [0,2]x[0,1]x[0,1]: farfield in x; slip walls on y and z (Navier-Stokes: an isothermal
+    no-slip y- wall, adiabatic no-slip elsewhere)."""
+    walls = ([sdg.ISOTHERMAL_NONSLIP_WALL] + [sdg.ADIABATIC_NONSLIP_WALL] * 3 if viscous
+             else [sdg.ADIABATIC_SLIP_WALL] * 4)
     mesh = sdg.Mesh.box_3d(0, 0, 0, 2.0, 1.0, 1.0, 2 * n, n, n, periodic=False,
-                           boundary_conditions=[sdg.RIEMANN_FARFIELD, sdg.RIEMANN_FARFIELD] + [sdg.ADIABATIC_SLIP_WALL] * 4)
-    cfg = cases.config(p, flux)
+                           boundary_conditions=[sdg.RIEMANN_FARFIELD, sdg.RIEMANN_FARFIELD] + walls)
+    cfg = cases.ns_config(p, flux, sdg.BR1, 0.02) if viscous else cases.config(p, flux)
 
     def ic(pts):
         x, y, z = pts[:, 0], pts[:, 1], pts[:, 2]
@@ -246,7 +257,7 @@ def test_derivatives_refuse_unsupported_configurations():
     with pytest.raises(sdg.SdgError) as e:
         hybrid.jvp_residual(np.zeros((hybrid.counts.volume_point_count, 4)))
     assert e.value.code == _abi.SDG_ERR_UNSUPPORTED
-    mesh, cfg, ic, bc, _, _ = cases.channel_case(p=2, n=3, viscous=sdg.BR1, mu=0.01)  # Navier-Stokes walls
+    mesh, cfg, ic, bc, _, _ = cases.channel_case(p=2, n=3, viscous=sdg.BR2, mu=0.01)  # BR2 is not differentiated
     walls = sdg.GpuSolver(mesh, cfg, device=0)
     walls.initialize_primitive(ic(walls.volume_points()))
     with pytest.raises(sdg.SdgError) as e:
@@ -289,7 +300,8 @@ def test_surface_force_of_a_fluid_at_rest_is_the_pressure_times_the_area():
     np.testing.assert_allclose(s.surface_force(2), [p0, 0.0], rtol=1e-14, atol=1e-14)
 
 
-@pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-box-walls-farfield-hex-p2-roe"])
+@pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-box-walls-farfield-hex-p2-roe",
+                                  "ns-channel-walls-quad-p3-br1-roe", "ns-box-walls-hex-p2-br1-roe"])
 def test_surface_force_cotangent_matches_central_differences(name):
     s, _ = make(name)
     group, e = (1, [0.3, -1.0]) if s.counts.dimension == 2 else (3, [0.2, -1.0, 0.4])
@@ -307,7 +319,8 @@ def test_surface_force_cotangent_matches_central_differences(name):
 
 
 @pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-channel-farfield-quad-p2-hllc",
-                                  "euler-box-walls-farfield-hex-p2-roe"])
+                                  "euler-box-walls-farfield-hex-p2-roe", "ns-channel-walls-quad-p3-br1-roe",
+                                  "ns-channel-farfield-quad-p2-br1-hllc", "ns-box-walls-hex-p2-br1-roe"])
 def test_force_gradient_through_a_trajectory(name):
     """J = e . force on a wall after N steps: dJ/dU_0 in a seeded direction and dJ/d(boundary primitives) in a
     seeded direction of every boundary point's (rho, u, T), against central differences of the trajectory."""
@@ -328,7 +341,7 @@ def test_force_gradient_through_a_trajectory(name):
     s.set_boundary_primitive(g0)
     s.forward_steps(dt, steps, 2)
     cot = s.surface_force_cotangent(group, e)
-    gu, _ = s.adjoint_recorded(cot)
+    gu, gmu = s.adjoint_recorded(cot)
     gg = s.adjoint_boundary_cotangent()
     du = direction(u0, 7)
     dg = direction(g0, 8)
@@ -337,3 +350,23 @@ def test_force_gradient_through_a_trajectory(name):
     fd_g = (J(u0, g0 + h * dg) - J(u0, g0 - h * dg)) / (2 * h)
     assert abs(float(np.sum(gu * du)) - fd_u) <= 1e-6 * abs(fd_u), (float(np.sum(gu * du)), fd_u)
     assert abs(float(np.sum(gg * dg)) - fd_g) <= 1e-6 * abs(fd_g), (float(np.sum(gg * dg)), fd_g)
+    if s.config.equation == sdg.NAVIER_STOKES:
+        # and the viscosity: the adjoint gives the trajectory's part, the force's own (tau is linear in mu)
+        # is its value at U_N with the state held
+        mu = s.config.dynamic_viscosity
+        hm = 1e-6 * mu
+        s.set_state_point(u0)
+        s.set_boundary_primitive(g0)
+        s.stepSolver(dt, steps)
+        s.set_viscosity(mu + hm)
+        fp = float(np.dot(s.surface_force(group), e))
+        s.set_viscosity(mu - hm)
+        fm = float(np.dot(s.surface_force(group), e))
+        direct = (fp - fm) / (2 * hm)
+        s.set_viscosity(mu + hm)
+        jp = J(u0, g0)
+        s.set_viscosity(mu - hm)
+        jm = J(u0, g0)
+        s.set_viscosity(mu)
+        fd_mu = (jp - jm) / (2 * hm)
+        assert abs(gmu + direct - fd_mu) <= 1e-6 * abs(fd_mu), (gmu, direct, fd_mu)
