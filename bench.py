@@ -71,10 +71,8 @@ def parse():
 
 
 def dist_env():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from subrosadg_gb300 import replicas
+    return replicas.env()
 
 
 def measured_peaks():
@@ -392,7 +390,7 @@ def run_ours(args):
     import torch
 
     import subrosadg_gb300 as sdg
-    from subrosadg_gb300 import _abi
+    from subrosadg_gb300 import _abi, replicas
 
     world, rank, local = dist_env()
     pg = None
@@ -422,8 +420,7 @@ def run_ours(args):
 
     # timed region: K steps, state resident in HBM (state 8 * DOF bytes >> 129 MB L2: no flush needed),
     # each step one CUDA-graph replay of all stage launches and the relative-error reduction
-    if pg:
-        pg.barrier()
+    replicas.barrier(pg)
     torch.cuda.synchronize(device)
     n0 = s.launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -438,10 +435,7 @@ def run_ours(args):
     launches = s.launch_count() - n0
     s.synchronize()
     relerr = s.relative_error()
-    if pg:
-        t = torch.tensor([ms], device=f"cuda:{device}")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(pg, ms, device=f"cuda:{device}")
     # per-kernel device times: a separate pass with every launch bracketed by events on the stream
     ksteps = max(1, min(args.steps, 3))
     lib.sdg_set_kernel_timing(s.h, 1)
@@ -479,18 +473,14 @@ def run_ours(args):
             s.set_state_point(host_in.numpy())
             s.stepSolver(dt)
             s.state_point(host_out.numpy().reshape(-1, s.nv))
-        if pg:
-            pg.barrier()
+        replicas.barrier(pg)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             s.set_state_point(host_in.numpy())          # H2D of the step's input state
             s.stepSolver(dt)                            # step + relative error (D2H)
             s.state_point(host_out.numpy().reshape(-1, s.nv))  # D2H of the step's result
         t_e2e = time.perf_counter() - t0
-        if pg:
-            t = torch.tensor([t_e2e], device=f"cuda:{device}")
-            pg.all_reduce(t, op=pg.ReduceOp.MAX)
-            t_e2e = float(t.item())
+        t_e2e = replicas.max_over_ranks(pg, t_e2e, device=f"cuda:{device}")
         e2e = {"value": world * dof * stages * args.steps / t_e2e, "unit": "DOF-stage/s",
                "h2d_bytes_per_step": npts * 8, "d2h_bytes_per_step": npts * 8 + s.nv * 8,
                "ms_per_step": 1e3 * t_e2e / args.steps}
