@@ -484,6 +484,8 @@ static void gradientQuadratureAndResidual(Problem& P) {
 // elements sharing each mesh node (:91-109) and the elements' vertex values from their nodes (:111-124).
 // s0 per order (SimulationControl.cpp:892-893).
 static const Real kAvTolerance[5] = {0.0, -1.20411998266, -1.90848501888, -2.40823996531, -2.79588001734};
+static const Real kWeakPressureAddition = 0.01;  // PhysicalModel.cpp:63-66
+static const Real kBoussinesqGravity = 1.0;      // SourceTerm.cpp:31
 static const Real kPiReal = Real(3.141592653589793238462643383279502884L);
 
 static void artificialViscosity(Problem& P) {
@@ -587,7 +589,8 @@ static void quadratureAndResidual(Problem& P) {
         if (P.ph.source) {  // rho beta (T - Tref) g on the last momentum component, times |J| w
           Real* S = &B.qsrc[(size_t(e) * nq + q) * nv];
           for (int i = 0; i < nv; ++i) S[i] = 0.0;
-          S[d] = v.rho * P.ph.beta * (P.ph.temperatureFromInternalEnergy(v.e) - P.ph.tref) * 1.0 * B.jw[size_t(e) * nq + q];
+          S[d] = v.rho * P.ph.beta * (P.ph.temperatureFromInternalEnergy(v.e) - P.ph.tref) * kBoussinesqGravity *
+                 B.jw[size_t(e) * nq + q];
         }
       }
     }
@@ -813,7 +816,7 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
   P->ph.incomp = c->equation == SDG_INCOMPRESSIBLE_EULER || c->equation == SDG_INCOMPRESSIBLE_NS;
   if (P->ph.incomp) {  // PhysicalModel.cpp:57-78
     P->ph.c0 = c->reference_sound_speed; P->ph.rho0 = c->reference_density;
-    P->ph.padd = 0.01 * P->ph.rho0 * P->ph.c0 * P->ph.c0;
+    P->ph.padd = kWeakPressureAddition * P->ph.rho0 * P->ph.c0 * P->ph.c0;
     if (P->flux == SDG_FLUX_HLLC || P->flux == SDG_FLUX_ROE) throw std::runtime_error("HLLC/Roe need the ideal gas");
   } else if (P->flux == SDG_FLUX_EXACT) {
     throw std::runtime_error("the Exact flux belongs to the incompressible models");
@@ -898,6 +901,16 @@ void orc_destroy(void* h) { delete static_cast<orc::Problem*>(h); }
 
 void orc_set_threads(int n) { if (n > 0) omp_set_num_threads(n); }
 int orc_max_threads() { return omp_get_max_threads(); }
+
+// Constants of the restated model, for the checks against the reference's own tables.
+double orc_constant(const char* name) {
+  const std::string n(name ? name : "");
+  if (n == "weak_pressure_addition") return double(orc::kWeakPressureAddition);
+  if (n == "boussinesq_gravity") return double(orc::kBoussinesqGravity);
+  for (int p = 1; p <= 5; ++p)
+    if (n == "artificial_viscosity_tolerance_" + std::to_string(p)) return double(orc::kAvTolerance[p - 1]);
+  return std::numeric_limits<double>::quiet_NaN();
+}
 int orc_real_digits() { return std::numeric_limits<orc::Real>::digits; }
 
 // counts: [element_count, volume_point_count, interior_faces, boundary_faces, nfq, dof]

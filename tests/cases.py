@@ -348,4 +348,13 @@ def golden_cases():
         "channel2d_quad_p2_hllc_bc": lambda: channel_case(p=2, flux=sdg.HLLC, n=4, steps=3),
         "farfield2d_tri_p3_roe_bc": lambda: channel_case(p=3, flux=sdg.ROE, n=4, steps=3, split=1.0,
                                                          conditions=(sdg.RIEMANN_FARFIELD,) * 4),
+        "ns_kh2d_hybrid_p3_br2_lf": lambda: kh_case(n=5, p=3, steps=2, viscous=sdg.BR2, mu=2e-3),
+        "ns_channel2d_walls_p2_br1_hllc": lambda: channel_case(
+            p=2, flux=sdg.HLLC, n=4, steps=2, viscous=sdg.BR1, mu=0.01,
+            conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_NONSLIP_WALL,
+                        sdg.VELOCITY_INFLOW)),
+        "inc_taylorvortex2d_p3_exact_br2": lambda: taylor_vortex_case(n=4, p=3, mu=1e-2, steps=2),
+        "inc_thermalcavity2d_p2_exact_br2_boussinesq": lambda: cavity_case(p=2, flux=sdg.EXACT, mu=1e-2,
+                                                                          boussinesq=True, c0=3.0, n=4, steps=2),
+        "av_shocktube2d_hybrid_p3_hllc": lambda: shock_tube_case(p=3, n=8, split=0.5, steps=2),
     }

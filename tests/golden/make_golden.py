@@ -86,6 +86,14 @@ def reference_tables(ref):
     out["sutherland_temperature"] = float(st.group(1)) / float(st.group(2))
     cf = open(os.path.join(ref, "src/Solver/ConvectiveFlux.cpp")).read()
     out["harten_divisor"] = float(re.search(r"harten_delta = roe_sound_speed / ([0-9.]+)_r", cf).group(1))
+    # weakly compressible pressure addition factor (p = c0^2 (rho - rho0) + f rho0 c0^2) and Boussinesq gravity
+    out["weak_pressure_addition"] = float(
+        re.search(r"reference_pressure_addition =\s*([0-9.]+) \* this->reference_density", pm).group(1))
+    stf = open(os.path.join(ref, "src/Solver/SourceTerm.cpp")).read()
+    out["boussinesq_gravity"] = float(re.search(r"kGravity = ([0-9.]+)_r", stf).group(1))
+    # artificial-viscosity sensor thresholds s0(P) (the uncommented table)
+    m = re.search(r"^inline constexpr std::array<Real, 5> kArtificialViscosityTolerance\{([^}]*)\}", sc, re.M)
+    out["artificial_viscosity_tolerance"] = [float(x) for x in m.group(1).replace("\n", " ").split(",")]
     return out
 
 

@@ -53,6 +53,22 @@ def test_face_vertex_lists_match_reference():
     assert t["Hexahedron"] == [0, 3, 2, 1, 0, 1, 5, 4, 0, 4, 7, 3, 1, 2, 6, 5, 2, 3, 7, 6, 4, 5, 6, 7]
 
 
+def test_model_constants_match_reference():
+    """Constants of the incompressible model, the Boussinesq source and the artificial-viscosity sensor,
+    read as text from the reference (PhysicalModel.cpp:63-66, SourceTerm.cpp:31, SimulationControl.cpp:892-893),
+    against the values the oracle uses."""
+    import ctypes
+    from oracle import orc
+    lib = orc.load()
+    lib.orc_constant.restype = ctypes.c_double
+    lib.orc_constant.argtypes = [ctypes.c_char_p]
+    t = _tables()
+    assert lib.orc_constant(b"weak_pressure_addition") == t["weak_pressure_addition"] == 0.01
+    assert lib.orc_constant(b"boussinesq_gravity") == t["boussinesq_gravity"] == 1.0
+    for p in range(1, 6):
+        assert lib.orc_constant(f"artificial_viscosity_tolerance_{p}".encode()) == t["artificial_viscosity_tolerance"][p - 1]
+
+
 def test_constants_match_reference():
     t = _tables()
     assert t["specific_heat_ratio"] == 1.4 and t["prandtl_number"] == 0.71
