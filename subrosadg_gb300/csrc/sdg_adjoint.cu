@@ -5,7 +5,8 @@
 //   <lambda, JVP(dU)> = <VJP(lambda), dU>
 // holds to round-off, for one residual and for whole trajectories.  Scope: element blocks that are affine
 // tensor blocks (quadrangles P>=2 with straight parallelogram sides, hexahedra), interior (periodic) faces,
-// Euler or Navier-Stokes with BR1; other configurations return SDG_ERR_UNSUPPORTED.
+// Euler or Navier-Stokes with BR1 or BR2, with or without boundary faces; other configurations return
+// SDG_ERR_UNSUPPORTED.
 //
 // Trajectories: the tangent runs stage by stage beside the forward state.  The adjoint stores the state
 // every `checkpoint_interval` steps on a forward sweep, then per segment (last first) recomputes the
@@ -118,13 +119,12 @@ AdjointState* adjoint(sdg_handle* h) {
   for (const DevBlock& B : h->blocks)
     if (B.kind != kTensor || !B.affine)
       throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (quadrangles P>=2, hexahedra)");
-  if (h->ns && h->cfg.viscous_flux != SDG_VISCOUS_BR1) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of BR2 are not built");
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
   if (h->ph.incomp || h->ph.source)
     throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the incompressible models and source terms are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, A->k);
-  adjointTileKernels(h->dim, h->blocks[0].n, h->ns, A->k);
+  adjointTileKernels(h->dim, h->blocks[0].n, h->ns, h->ns && h->cfg.viscous_flux == SDG_VISCOUS_BR2, A->k);
   if (!A->k.valid()) throw Failure(SDG_ERR_UNSUPPORTED, "no derivative kernels for this configuration");
   SDG_CUDA(cudaSetDevice(h->device));
   for (const void* fn : {A->k.jvpStage, A->k.vjpVolume, A->k.vjpGradient, A->k.vjpTrace}) configureKernel(fn, h->device);
@@ -214,7 +214,7 @@ void traces(sdg_handle* h, const double* u, double* face) {
   runRecs(h, recs, h->stream);
 }
 
-// BR1 gradient pass of state `u` whose traces are in `face`: neighbour traces into `other`, node gradient
+// Gradient pass (BR1 or BR2) of state `u` whose traces are in `face`: neighbour traces into `other`, node gradient
 // into `grad`, gradient traces into `faceGrad` (the forward kernels; linear, so they serve tangents too).
 // tangent: u, face are a tangent state and its traces; the boundary exchange (the walls' states) is then the
 // linearisation at the forward traces in h->face.
@@ -326,6 +326,7 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
     for (DevBlock& B : h->blocks) {
       AdjArgs a = baseArgs(h, &B, h->state[1]);
       a.lamG = A->lamG + B.gradOffset; a.lamTg = A->lamTg; a.lamU = A->lamU + B.stateOffset; a.lamUp = A->lamUp;
+      a.lamTr = A->lamTr;  // BR2: the own traces' share
       launch(h, A->k.vjpGradient, tiles(h, B), NT, A->k.vjpSmem, a, false);
     }
     AdjArgs a = baseArgs(h, nullptr, nullptr);
@@ -792,6 +793,7 @@ int sdg_surface_force_cotangent(sdg_handle* h, int32_t physical, const double* d
       for (DevBlock& B : h->blocks) {
         AdjArgs g = baseArgs(h, &B, h->state[0]);
         g.lamG = A->lamG + B.gradOffset; g.lamTg = A->lamTg; g.lamU = A->lamU + B.stateOffset; g.lamUp = A->lamUp;
+        g.lamTr = A->lamTr;
         launch(h, A->k.vjpGradient, tiles(h, B), A->k.threads, A->k.vjpSmem, g, false);
       }
       AdjArgs x = baseArgs(h, nullptr, nullptr);

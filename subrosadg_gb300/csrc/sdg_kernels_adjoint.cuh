@@ -1480,6 +1480,114 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpGradientKerne
   }
 }
 
+// V3 for BR2.  The node gradient (volume terms) is the BR1 gradient G = (1/|J|) sum_b JA_b (lift_b U+ - Dhat_b U);
+// the gradient trace at face f is the trace of the volume part V = (1/|J|) sum_b JA_b (lift_b {U} - Dhat_b U)
+// plus face f's own lift, cl nF_f 1/2 (U+ - U-) at the point (tensorGradientTile, BR2).  With
+// t_b = (1/|J|) sum_k JA[b][k] lamG(k) and v_b the same of T^T lamTg:
+//   lamU  -= Dhat_b^T (t_b + v_b)
+//   lamUp  = +-lift (t_b + v_b/2) + cl/2 nF.lamTg         (the neighbour traces U+)
+//   lamTr += +-lift v_b/2         - cl/2 nF.lamTg         (the own traces U-)
+template <int DIM, int N>
+__global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpGradientBR2Kernel(AdjArgs a) {
+  using A = AdjShape<DIM, N>;
+  constexpr int NV = A::NV, NB = A::NB, NF = A::NF, NFQ = A::NFQ, EPB = A::EPB, GS = NV * DIM;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* sT = reinterpret_cast<double*>(smem_raw);  // [EPB][DIM][NV][NB]  t_b + v_b
+  double* sV = sT + EPB * DIM * NV * NB;             // [EPB][DIM][NV][NB]  v_b
+  TensorTables* T = reinterpret_cast<TensorTables*>(sV + EPB * DIM * NV * NB);
+  const int tid = threadIdx.x;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  const int le = tid / NB, node = tid - le * NB;
+  const bool active = le < ecount;
+  const int64_t e = e0 + le;
+  loadTensorTables<DIM, N>(T, a.tables);
+  __syncthreads();
+  if (active) {
+    const double* g = a.geom + e * (DIM * DIM + 1);
+    double ja[DIM][DIM];
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) ja[b][c] = g[b * DIM + c];
+    const double jinv = g[DIM * DIM];
+    double lg[GS], lv[GS];
+#pragma unroll
+    for (int c = 0; c < GS; ++c) { lg[c] = a.lamG[(e * GS + c) * NB + node]; lv[c] = 0.0; }
+#pragma unroll
+    for (int b = 0; b < DIM; ++b) {
+      const int ab = axisIndex<DIM, N>(node, b);
+#pragma unroll
+      for (int en = 0; en < 2; ++en) {
+        const int f = T->axisFace[b][en];
+        const int j = T->nodeFacePoint[b][en][node];
+        const double c = en ? T->endp[ab] : T->endm[ab];
+        const double* src = a.lamTg + (a.faceBase + e * NF + f) * GS * NFQ + j;
+#pragma unroll
+        for (int k = 0; k < GS; ++k) lv[k] = fma(c, src[k * NFQ], lv[k]);
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double at = 0.0, av = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) { at = fma(ja[b][k], lg[v * DIM + k], at); av = fma(ja[b][k], lv[v * DIM + k], av); }
+        sT[((le * DIM + b) * NV + v) * NB + node] = jinv * (at + av);
+        sV[((le * DIM + b) * NV + v) * NB + node] = jinv * av;
+      }
+  }
+  __syncthreads();
+  if (active) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double acc = 0.0;
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) {
+        const int ab = axisIndex<DIM, N>(node, b);
+        const int st = strideOf<DIM, N>(b);
+        const int base = node - ab * st;
+#pragma unroll
+        for (int q = 0; q < N; ++q) acc = fma(T->dhat[ab][q], sT[((le * DIM + b) * NV + v) * NB + base + q * st], acc);
+      }
+      a.lamU[e * A::USTRIDE + v * NB + node] -= acc;
+    }
+  }
+  for (int idx = tid; idx < ecount * NF * NFQ; idx += blockDim.x) {
+    const int te = idx / (NF * NFQ), r = idx - te * (NF * NFQ);
+    const int f = r / NFQ, j = r - f * NFQ;
+    const int axis = T->faceAxis[f], en = T->faceEnd[f];
+    const double* lift = en ? T->liftp : T->liftm;
+    const double* coef = en ? T->endp : T->endm;
+    const double sign = en ? 1.0 : -1.0;
+    const int base = T->faceBase[f][j];
+    const int st = strideOf<DIM, N>(axis);
+    const int64_t ee = e0 + te;
+    const double* gm = a.geom + ee * (DIM * DIM + 1);
+    double cl = 0.0;  // lift trace factor sum_q l_q(end) lift_q / |J| (affine)
+#pragma unroll
+    for (int q = 0; q < N; ++q) cl = fma(coef[q], lift[q], cl);
+    cl *= gm[DIM * DIM];
+    const double* tb = sT + (te * DIM + axis) * NV * NB + base;
+    const double* vb = sV + (te * DIM + axis) * NV * NB + base;
+    const int64_t slot = a.faceBase + ee * NF + f;
+    const double* ltg = a.lamTg + slot * GS * NFQ + j;
+    double* up = a.lamUp + slot * NV * NFQ + j;
+    double* tr = a.lamTr + slot * NV * NFQ + j;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double at = 0.0, av = 0.0, nl = 0.0;
+#pragma unroll
+      for (int q = 0; q < N; ++q) { at = fma(lift[q], tb[v * NB + q * st], at); av = fma(lift[q], vb[v * NB + q * st], av); }
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) nl = fma(sign * gm[axis * DIM + k], ltg[(v * DIM + k) * NFQ], nl);
+      up[v * NFQ] = fma(0.5 * cl, nl, sign * fma(-0.5, av, at));
+      tr[v * NFQ] += fma(-0.5 * cl, nl, 0.5 * sign * av);
+    }
+  }
+}
+
 // V4 (NS): transposed exchange, lamTr(R, jr) += lamUp(L, j) and lamTr(L, j) += lamUp(R, jr).
 template <int DIM>
 __global__ void __launch_bounds__(kFaceThreads) vjpExchangeKernel(AdjArgs a) {

@@ -51,9 +51,9 @@ struct AdjointKernels {
   size_t jvpSmem = 0, vjpSmem = 0;
   bool valid() const { return jvpStage && jvpFace; }
 };
-// Face kernels depend on (dim, flux, viscous); tile kernels on (dim, nodes per direction, viscous).
+// Face kernels depend on (dim, flux, viscous); tile kernels on (dim, nodes per direction, viscous, BR2).
 void adjointFaceKernels(int dim, int flux, bool visc, AdjointKernels& k);
-void adjointTileKernels(int dim, int n, bool visc, AdjointKernels& k);
+void adjointTileKernels(int dim, int n, bool visc, bool br2, AdjointKernels& k);
 
 // Largest tile size the kernels are compiled for (their __launch_bounds__).
 constexpr int kMaxThreads = 512;

@@ -44,6 +44,12 @@ CASES = {
         p=2, flux=sdg.HLLC, n=3, viscous=sdg.BR1, mu=0.02,
         conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD)),
     "ns-box-walls-hex-p2-br1-roe": lambda: _box3d(p=2, flux=sdg.ROE, viscous=True),
+    # BR2 (the face gradients carry each face's own lift)
+    "ns-hex-p2-br2-hllc": lambda: cases.tgv_case(n=3, p=2, flux=sdg.HLLC, viscous=sdg.BR2, mu=0.02),
+    "ns-quad-p3-br2-roe": lambda: cases.vortex_case(n=4, p=3, flux=sdg.ROE, viscous=sdg.BR2, mu=0.05),
+    "ns-channel-walls-quad-p3-br2-roe": lambda: cases.channel_case(
+        p=3, flux=sdg.ROE, n=3, viscous=sdg.BR2, mu=0.01,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
 }
 
 
@@ -162,7 +168,7 @@ def test_vjp_is_the_transpose_of_jvp(name):
 
 
 @pytest.mark.parametrize("name", ["euler-quad-p3-roe", "euler-hex-p2-hllc", "ns-hex-p3-br1-roe",
-                                  "ns-quad-p4-br1-hllc"])
+                                  "ns-quad-p4-br1-hllc", "ns-hex-p2-br2-hllc", "ns-channel-walls-quad-p3-br2-roe"])
 def test_trajectory_dot_product_with_checkpointing(name):
     steps, interval = 5, 2
     a, dt = make(name)
@@ -257,7 +263,7 @@ def test_derivatives_refuse_unsupported_configurations():
     with pytest.raises(sdg.SdgError) as e:
         hybrid.jvp_residual(np.zeros((hybrid.counts.volume_point_count, 4)))
     assert e.value.code == _abi.SDG_ERR_UNSUPPORTED
-    mesh, cfg, ic, bc, _, _ = cases.channel_case(p=2, n=3, viscous=sdg.BR2, mu=0.01)  # BR2 is not differentiated
+    mesh, cfg, ic, bc, _, _ = cases.shock_tube_case(p=2, n=8)  # artificial viscosity is not differentiated
     walls = sdg.GpuSolver(mesh, cfg, device=0)
     walls.initialize_primitive(ic(walls.volume_points()))
     with pytest.raises(sdg.SdgError) as e:
@@ -320,7 +326,8 @@ def test_surface_force_cotangent_matches_central_differences(name):
 
 @pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-channel-farfield-quad-p2-hllc",
                                   "euler-box-walls-farfield-hex-p2-roe", "ns-channel-walls-quad-p3-br1-roe",
-                                  "ns-channel-farfield-quad-p2-br1-hllc", "ns-box-walls-hex-p2-br1-roe"])
+                                  "ns-channel-farfield-quad-p2-br1-hllc", "ns-box-walls-hex-p2-br1-roe",
+                                  "ns-channel-walls-quad-p3-br2-roe"])
 def test_force_gradient_through_a_trajectory(name):
     """J = e . force on a wall after N steps: dJ/dU_0 in a seeded direction and dJ/d(boundary primitives) in a
     seeded direction of every boundary point's (rho, u, T), against central differences of the trajectory."""
