@@ -363,7 +363,8 @@ const char* sdg_batch_last_error(const sdg_batch* batch);
  * residual R(U) = du/dt and for whole SSP-RK trajectories, with respect to the state and to the dynamic
  * viscosity mu.  All vectors are in the volume-point layout of sdg_set_state_point ([point][d+2],
  * conserved variables).  Supported: affine tensor blocks (quadrangles P>=2 with parallelogram sides,
- * hexahedra), meshes without boundary faces, Euler or Navier-Stokes with BR1; else SDG_ERR_UNSUPPORTED. */
+ * hexahedra), any boundary faces, compressible or incompressible Euler or Navier-Stokes (BR1, BR2), the
+ * Boussinesq source; else (dense blocks, artificial viscosity) SDG_ERR_UNSUPPORTED. */
 /* w_q |J|_q of every volume point: integral of f = sum over points of weight * f (functionals). */
 int sdg_volume_point_weight(sdg_handle* handle, double* weight);
 /* Change the dynamic viscosity (and kappa = cp mu / Pr) of a Navier-Stokes handle. */
@@ -392,14 +393,15 @@ int sdg_adjoint_recorded(sdg_handle* handle, const double* final_cotangent, doub
                          double* viscosity_cotangent);
 /* Cotangent of the ghost primitive (rho, u, T) of every boundary point ([boundary_point_count][d+2], the order
  * of sdg_boundary_point_coordinate) accumulated by the last sdg_vjp_residual / sdg_adjoint_steps /
- * sdg_adjoint_recorded: the gradient with respect to the boundary (freestream) states.  Euler only. */
+ * sdg_adjoint_recorded (and the ghost part left by sdg_surface_force_cotangent for Navier-Stokes walls): the
+ * gradient with respect to the boundary (freestream) states. */
 int sdg_adjoint_boundary_cotangent(sdg_handle* handle, double* cotangent);
 /* Surface force of boundary group `physical` (1-based mesh physical index) on the current state: the sum over its
  * face points of w |J_f| (p n - tau n) from the interior traces, n out of the fluid (the reference's View force,
  * VariableConvertor.cpp:883-906).  force: [dimension]. */
 int sdg_surface_force(sdg_handle* handle, int32_t physical, double* force);
 /* Cotangent of direction . force with respect to the state ([volume_points][nv], the layout of the
- * adjoint's final cotangent): the Euler pressure force (Navier-Stokes: SDG_ERR_UNSUPPORTED). */
+ * adjoint's final cotangent): pressure and (Navier-Stokes) viscous stress through the gradient traces. */
 int sdg_surface_force_cotangent(sdg_handle* handle, int32_t physical, const double* direction, double* cotangent);
 /* Device bytes held for checkpoints, stage states and (Navier-Stokes, when HBM has room) the forward quantities
  * of one segment's stage inputs (grown on demand, released with the handle). */

@@ -120,11 +120,10 @@ AdjointState* adjoint(sdg_handle* h) {
     if (B.kind != kTensor || !B.affine)
       throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (quadrangles P>=2, hexahedra)");
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
-  if (h->ph.incomp || h->ph.source)
-    throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the incompressible models and source terms are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
-  adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, A->k);
-  adjointTileKernels(h->dim, h->blocks[0].n, h->ns, h->ns && h->cfg.viscous_flux == SDG_VISCOUS_BR2, A->k);
+  const bool gen = h->ph.incomp || h->ph.source;
+  adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, gen, A->k);
+  adjointTileKernels(h->dim, h->blocks[0].n, h->ns, h->ns && h->cfg.viscous_flux == SDG_VISCOUS_BR2, gen, A->k);
   if (!A->k.valid()) throw Failure(SDG_ERR_UNSUPPORTED, "no derivative kernels for this configuration");
   SDG_CUDA(cudaSetDevice(h->device));
   for (const void* fn : {A->k.jvpStage, A->k.vjpVolume, A->k.vjpGradient, A->k.vjpTrace}) configureKernel(fn, h->device);
@@ -741,7 +740,6 @@ int sdg_surface_force(sdg_handle* h, int32_t physical, double* force) {
   if (!h->hasState) { h->err = "no state"; return SDG_ERR_STATE; }
   try {
     SDG_CUDA(cudaSetDevice(h->device));
-    if (h->ph.incomp) throw Failure(SDG_ERR_UNSUPPORTED, "the surface force is built for the compressible models");
     // the gradient traces of the current state (the step leaves those of its last stage input)
     if (h->ns) gradientOf(h, h->state[0], h->face, h->faceOther, h->grad, h->faceGrad);
     ForceInputs in;

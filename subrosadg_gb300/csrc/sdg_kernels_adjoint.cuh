@@ -1,5 +1,6 @@
 // Tangent-linear (JVP) and adjoint (VJP) kernels of the residual of affine tensor blocks (quadrangles
-// P>=2 and hexahedra), Euler or Navier-Stokes BR1, interior faces.
+// P>=2 and hexahedra): compressible and incompressible Euler / Navier-Stokes (BR1, BR2), interior and boundary
+// faces, the Boussinesq source.
 //
 // Forward residual of one stage (nodal Gauss collocation, see sdg_kernels.cuh / sdg_kernels_ns.cuh):
 //   Tr = T U                 face traces                       (linear)
@@ -152,6 +153,121 @@ __device__ __forceinline__ void viscousTransposeG(const double* U, const Phys& p
   }
 }
 
+
+// ---- dual-number transposes (the incompressible model and the Boussinesq source) -----------------------
+// Volume: lamU = sum_b (dQ_b/dU)^T lq[b] + lam_S dS/dU (S the buoyancy on the last momentum component),
+// lamG = sum_b (dQ_b/dG)^T lq[b]; returns sum_b lq[b] . Qv_b (the viscosity term).  Used only by the GEN
+// instantiations, so the compressible kernels keep their hand-written sweeps and register allocation.
+template <int DIM, bool VISC>
+__device__ __forceinline__ double volumeReverseGeneric(const double* U, const double* G, const double (*ja)[DIM],
+                                                    const double (*lq)[DIM + 2], double lamS, const Phys& ph,
+                                                    double* lamU, double* lamG) {
+  constexpr int NV = DIM + 2, NG = NV * DIM;
+  using DK = Dual<NV>;
+  double mupart = 0.0;
+  {
+    DK x[NV], g[VISC ? NG : 1], Q[DIM][NV], Qv[DIM][NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) { x[v] = DK(U[v]); x[v].d[v] = 1.0; }
+    if constexpr (VISC) {
+#pragma unroll
+      for (int c = 0; c < NG; ++c) g[c] = DK(G[c]);
+    }
+    nodeFlux<DIM, VISC>(x, g, ja, ph, Q, Qv);
+#pragma unroll
+    for (int w = 0; w < NV; ++w) {
+      double acc = 0.0;
+#pragma unroll
+      for (int b = 0; b < DIM; ++b)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc = fma(lq[b][v], Q[b][v].d[w], acc);
+      lamU[w] = acc;
+    }
+#pragma unroll
+    for (int b = 0; b < DIM; ++b)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) mupart = fma(lq[b][v], Qv[b][v].v, mupart);
+    if (ph.source) {
+      State<DIM, DK> st;
+      makeState<DIM>(st, x, ph);
+      const DK S = st.r * ph.beta * (temperatureOf(st, ph) - ph.tref);
+#pragma unroll
+      for (int w = 0; w < NV; ++w) lamU[w] = fma(lamS, S.d[w], lamU[w]);
+    }
+  }
+  if constexpr (VISC) {
+    using DG = Dual<NG>;
+    DG x[NV], g[NG], Q[DIM][NV], Qv[DIM][NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) x[v] = DG(U[v]);
+#pragma unroll
+    for (int c = 0; c < NG; ++c) { g[c] = DG(G[c]); g[c].d[c] = 1.0; }
+    nodeFlux<DIM, VISC>(x, g, ja, ph, Q, Qv);
+#pragma unroll
+    for (int c = 0; c < NG; ++c) {
+      double acc = 0.0;
+#pragma unroll
+      for (int b = 0; b < DIM; ++b)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) acc = fma(lq[b][v], Q[b][v].d[c], acc);
+      lamG[c] = acc;
+    }
+  }
+  return mupart;
+}
+
+// Face: one side's viscous flux enters h as -1/2 Fv(U, G).n; lamU += its transpose in U, lamG = in G;
+// returns the viscosity term sum_v lh[v] (-1/2 Fv.n)(v).
+template <int DIM>
+__device__ __forceinline__ double faceViscousReverseGeneric(const double* U, const double* G, const double* n,
+                                                         const double* lh, const Phys& ph, double* lamU,
+                                                         double* lamG) {
+  constexpr int NV = DIM + 2, NG = NV * DIM;
+  double mupart = 0.0;
+  {
+    using DK = Dual<NV>;
+    DK x[NV], g[NG], f[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) { x[v] = DK(U[v]); x[v].d[v] = 1.0; }
+#pragma unroll
+    for (int c = 0; c < NG; ++c) g[c] = DK(G[c]);
+    State<DIM, DK> s;
+    makeState<DIM>(s, x, ph);
+    PrimGrad<DIM, DK> pg;
+    primitiveGradient<DIM>(g, s.u, s.ir, s.E * s.ir, ph, pg);
+    viscousNormalFlux<DIM>(pg, s.u, temperatureOf(s, ph), n, ph, f);
+#pragma unroll
+    for (int w = 0; w < NV; ++w) {
+      double acc = 0.0;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc = fma(lh[v], f[v].d[w], acc);
+      lamU[w] = fma(-0.5, acc, lamU[w]);
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) mupart = fma(-0.5 * lh[v], f[v].v, mupart);
+  }
+  {
+    using DG = Dual<NG>;
+    DG x[NV], g[NG], f[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) x[v] = DG(U[v]);
+#pragma unroll
+    for (int c = 0; c < NG; ++c) { g[c] = DG(G[c]); g[c].d[c] = 1.0; }
+    State<DIM, DG> s;
+    makeState<DIM>(s, x, ph);
+    PrimGrad<DIM, DG> pg;
+    primitiveGradient<DIM>(g, s.u, s.ir, s.E * s.ir, ph, pg);
+    viscousNormalFlux<DIM>(pg, s.u, temperatureOf(s, ph), n, ph, f);
+#pragma unroll
+    for (int c = 0; c < NG; ++c) {
+      double acc = 0.0;
+#pragma unroll
+      for (int v = 0; v < NV; ++v) acc = fma(lh[v], f[v].d[c], acc);
+      lamG[c] = -0.5 * acc;
+    }
+  }
+  return mupart;
+}
 
 // ---- hand-written reverse sweeps (adjoints of the forward formulas, line by line) ---------------------
 // Euler contravariant volume fluxes Q_b = (rho vb, m vb + ja_b p, (E + p) vb), vb = u . ja_b:
@@ -689,7 +805,7 @@ __device__ __forceinline__ void boundaryFluxOf(const T* ul, const T* gprim, cons
 #pragma unroll
   for (int k = 0; k < DIM; ++k) g.u[k] = gprim[1 + k];
   g.e = ph.cv * gprim[DIM + 1];
-  g.p = ph.gm1 * g.r * g.e;
+  g.p = ph.incomp ? weakPressure(g.r, ph) : ph.gm1 * g.r * g.e;
   boundaryState<DIM>(bc, n, l, g, ph, b);
   normalFluxComp<DIM>(b, n, h, ph);
 }
@@ -721,7 +837,7 @@ __device__ __forceinline__ void boundaryNSFluxOf(const T* ul, const T* gr, const
 #pragma unroll
   for (int k = 0; k < DIM; ++k) g.u[k] = gprim[1 + k];
   g.e = ph.cv * gprim[DIM + 1];
-  g.p = ph.gm1 * g.r * g.e;
+  g.p = ph.incomp ? weakPressure(g.r, ph) : ph.gm1 * g.r * g.e;
   boundaryState<DIM>(bc, n, l, g, ph, b);
   normalFluxComp<DIM>(b, n, h, ph);
   PrimGrad<DIM, T> pl;
@@ -761,7 +877,7 @@ __device__ __forceinline__ void boundaryOtherOf(const T* ul, const T* gprim, con
 #pragma unroll
   for (int k = 0; k < DIM; ++k) g.u[k] = gprim[1 + k];
   g.e = ph.cv * gprim[DIM + 1];
-  g.p = ph.gm1 * g.r * g.e;
+  g.p = ph.incomp ? weakPressure(g.r, ph) : ph.gm1 * g.r * g.e;
   boundaryState<DIM>(bc, n, l, g, ph, b);
   T ub[NV];
   ub[0] = b.r;
@@ -1161,6 +1277,15 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) jvpStageKernel(A
         du[v] = acc;
       }
     }
+    if (ph.source) {  // tangent of the buoyancy S |J| on the last momentum component
+      D1 U[NV];
+#pragma unroll
+      for (int v = 0; v < NV; ++v) { U[v].v = sU[le * A::USTRIDE + v * NB + node]; U[v].d[0] = sD[le * A::USTRIDE + v * NB + node]; }
+      State<DIM, D1> st;
+      makeState<DIM>(st, U, ph);
+      const D1 S = st.r * ph.beta * (temperatureOf(st, ph) - ph.tref);
+      du[DIM] = fma(S.d[0], 1.0 / jinv, du[DIM]);
+    }
     const int64_t gi = e * A::USTRIDE + node;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
@@ -1213,7 +1338,7 @@ __device__ __forceinline__ void blockSum(double x, double* part, double* sRed) {
 
 // V1: s = lam/|J|; lamQ_b by the transposed derivative; node Jacobians by Dual<NV> over U;
 // lamG (NS) by the viscous transpose; lamH by the transposed lift.  muPart[tile] = <lamQ, Qv>.
-template <int DIM, int N, bool VISC>
+template <int DIM, int N, bool VISC, bool GEN>
 __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(AdjArgs a, Phys ph) {
   using A = AdjShape<DIM, N>;
   constexpr int NV = A::NV, NB = A::NB, NF = A::NF, NFQ = A::NFQ, EPB = A::EPB;
@@ -1262,6 +1387,18 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(
     double Uv[NV], lu[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) Uv[v] = a.u[e * A::USTRIDE + v * NB + node];
+    if constexpr (GEN) {  // the dual-number transpose (incompressible model, buoyancy)
+      double gg[VISC ? NV * DIM : 1], lg[VISC ? NV * DIM : 1];
+      if constexpr (VISC) {
+#pragma unroll
+        for (int c = 0; c < NV * DIM; ++c) gg[c] = a.grad[(e * NV * DIM + c) * NB + node];
+      }
+      mupart = volumeReverseGeneric<DIM, VISC>(Uv, gg, ja, lq, a.lam[e * A::USTRIDE + DIM * NB + node], ph, lu, lg);
+      if constexpr (VISC) {
+#pragma unroll
+        for (int c = 0; c < NV * DIM; ++c) a.lamG[(e * NV * DIM + c) * NB + node] = lg[c];
+      }
+    } else {
     eulerVolumeReverse<DIM>(Uv, ja, lq, ph, lu);
     if constexpr (VISC) {
       // lamF[c][v] = cotangent of Fv_c(v): Q_b contains -sum_c ja[b][c] Fv_c
@@ -1280,6 +1417,7 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(
       mupart = viscousReverse<DIM>(Uv, gg, lamF, ph, lu, lg);
 #pragma unroll
       for (int c = 0; c < NV * DIM; ++c) a.lamG[(e * NV * DIM + c) * NB + node] = lg[c];
+    }
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) a.lamU[e * A::USTRIDE + v * NB + node] = lu[v];
@@ -1308,7 +1446,7 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(
 // V2: face point.  lam_h = lamH(L) - lamH(R) (the +/- scatter); trace cotangents of the convective flux
 // (Roe: hand-written reverse sweep; other fluxes: Dual<NV> passes seeded on UL and on UR) and, for
 // Navier-Stokes, of each side's viscous flux (state and gradient parts); muPart = <lam_h, hv>.
-template <int DIM, int FLUX, bool VISC>
+template <int DIM, int FLUX, bool VISC, bool GEN>
 __global__ void __launch_bounds__(kFaceThreads) vjpFaceKernel(AdjArgs a, Phys ph) {
   constexpr int NV = DIM + 2;
   using DK = Dual<NV>;
@@ -1377,7 +1515,10 @@ __global__ void __launch_bounds__(kFaceThreads) vjpFaceKernel(AdjArgs a, Phys ph
         double gg[NV * DIM], lg[NV * DIM];
 #pragma unroll
         for (int c = 0; c < NV * DIM; ++c) { gg[c] = a.faceGrad[G0 + c * nfq]; lg[c] = 0.0; }
-        mupart += viscousReverse<DIM>(side == 0 ? ul : ur, gg, lamF, ph, side == 0 ? laml : lamr, lg);
+        if constexpr (GEN)
+          mupart += faceViscousReverseGeneric<DIM>(side == 0 ? ul : ur, gg, n, lh, ph, side == 0 ? laml : lamr, lg);
+        else
+          mupart += viscousReverse<DIM>(side == 0 ? ul : ur, gg, lamF, ph, side == 0 ? laml : lamr, lg);
         double* out = a.lamTg + G0;
 #pragma unroll
         for (int c = 0; c < NV * DIM; ++c) out[c * nfq] = lg[c];

@@ -52,8 +52,9 @@ struct AdjointKernels {
   bool valid() const { return jvpStage && jvpFace; }
 };
 // Face kernels depend on (dim, flux, viscous); tile kernels on (dim, nodes per direction, viscous, BR2).
-void adjointFaceKernels(int dim, int flux, bool visc, AdjointKernels& k);
-void adjointTileKernels(int dim, int n, bool visc, bool br2, AdjointKernels& k);
+// gen: the dual-number transposes (incompressible model, Boussinesq source) instead of the hand-written ones.
+void adjointFaceKernels(int dim, int flux, bool visc, bool gen, AdjointKernels& k);
+void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, AdjointKernels& k);
 
 // Largest tile size the kernels are compiled for (their __launch_bounds__).
 constexpr int kMaxThreads = 512;

@@ -7,26 +7,28 @@ namespace sdg {
 
 namespace {
 template <int DIM, int FLUX, bool VISC>
-void faceOf(AdjointKernels& k) {
+void faceOf(AdjointKernels& k, bool gen) {
   k.jvpFace = reinterpret_cast<const void*>(&jvpFaceKernel<DIM, FLUX, VISC>);
-  k.vjpFace = reinterpret_cast<const void*>(&vjpFaceKernel<DIM, FLUX, VISC>);
+  k.vjpFace = gen && VISC ? reinterpret_cast<const void*>(&vjpFaceKernel<DIM, FLUX, VISC, VISC>)
+                          : reinterpret_cast<const void*>(&vjpFaceKernel<DIM, FLUX, VISC, false>);
   k.vjpExchange = reinterpret_cast<const void*>(&vjpExchangeKernel<DIM>);
 }
 template <int DIM, bool VISC>
-void fluxOf(int flux, AdjointKernels& k) {
+void fluxOf(int flux, AdjointKernels& k, bool gen) {
   switch (flux) {
-    case 0: faceOf<DIM, 0, VISC>(k); break;
-    case 1: faceOf<DIM, 1, VISC>(k); break;
-    case 2: faceOf<DIM, 2, VISC>(k); break;
-    case 3: faceOf<DIM, 3, VISC>(k); break;
+    case 0: faceOf<DIM, 0, VISC>(k, gen); break;
+    case 1: faceOf<DIM, 1, VISC>(k, gen); break;
+    case 2: faceOf<DIM, 2, VISC>(k, gen); break;
+    case 3: faceOf<DIM, 3, VISC>(k, false); break;   // Roe: compressible only
+    case 4: faceOf<DIM, 4, VISC>(k, gen); break;
     default: break;
   }
 }
 }  // namespace
 
-void adjointFaceKernels(int dim, int flux, bool visc, AdjointKernels& k) {
-  if (dim == 2) { if (visc) fluxOf<2, true>(flux, k); else fluxOf<2, false>(flux, k); }
-  else if (dim == 3) { if (visc) fluxOf<3, true>(flux, k); else fluxOf<3, false>(flux, k); }
+void adjointFaceKernels(int dim, int flux, bool visc, bool gen, AdjointKernels& k) {
+  if (dim == 2) { if (visc) fluxOf<2, true>(flux, k, gen); else fluxOf<2, false>(flux, k, gen); }
+  else if (dim == 3) { if (visc) fluxOf<3, true>(flux, k, gen); else fluxOf<3, false>(flux, k, gen); }
   const auto pick = [dim](const void* two, const void* three) { return dim == 2 ? two : three; };
   if (!visc) {
     k.jvpBoundary = pick(reinterpret_cast<const void*>(&jvpBoundaryKernel<2>), reinterpret_cast<const void*>(&jvpBoundaryKernel<3>));

@@ -7,10 +7,11 @@ namespace sdg {
 
 namespace {
 template <int DIM, int N, bool VISC>
-void tileOf(AdjointKernels& k, bool br2) {
+void tileOf(AdjointKernels& k, bool br2, bool gen) {
   using A = AdjShape<DIM, N>;
   k.jvpStage = reinterpret_cast<const void*>(&jvpStageKernel<DIM, N, VISC>);
-  k.vjpVolume = reinterpret_cast<const void*>(&vjpVolumeKernel<DIM, N, VISC>);
+  k.vjpVolume = gen ? reinterpret_cast<const void*>(&vjpVolumeKernel<DIM, N, VISC, true>)
+                    : reinterpret_cast<const void*>(&vjpVolumeKernel<DIM, N, VISC, false>);
   k.vjpGradient = br2 ? reinterpret_cast<const void*>(&vjpGradientBR2Kernel<DIM, N>)
                       : reinterpret_cast<const void*>(&vjpGradientKernel<DIM, N>);
   k.vjpTrace = reinterpret_cast<const void*>(&vjpTraceKernel<DIM, N>);
@@ -18,9 +19,9 @@ void tileOf(AdjointKernels& k, bool br2) {
 }
 }  // namespace
 
-void adjointTileKernels(int dim, int n, bool visc, bool br2, AdjointKernels& k) {
+void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, AdjointKernels& k) {
 #define SDG_AT(D, NN) \
-  if (dim == D && n == NN) { if (visc) tileOf<D, NN, true>(k, br2); else tileOf<D, NN, false>(k, false); return; }
+  if (dim == D && n == NN) { if (visc) tileOf<D, NN, true>(k, br2, gen); else tileOf<D, NN, false>(k, false, gen); return; }
   SDG_AT(2, 3) SDG_AT(2, 4) SDG_AT(2, 5) SDG_AT(2, 6) SDG_AT(3, 2) SDG_AT(3, 3) SDG_AT(3, 4) SDG_AT(3, 5) SDG_AT(3, 6)
 #undef SDG_AT
 }

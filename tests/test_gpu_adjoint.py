@@ -22,6 +22,8 @@ from tests import cases
 
 pytestmark = pytest.mark.gpu
 
+VISCOUS = (sdg.NAVIER_STOKES, sdg.INCOMPRESSIBLE_NAVIER_STOKES)
+
 CASES = {
     "euler-quad-p3-roe": lambda: cases.vortex_case(n=4, p=3, flux=sdg.ROE),
     "euler-quad-p2-lf": lambda: cases.vortex_case(n=4, p=2, flux=sdg.LAX_FRIEDRICHS),
@@ -50,6 +52,22 @@ CASES = {
     "ns-channel-walls-quad-p3-br2-roe": lambda: cases.channel_case(
         p=3, flux=sdg.ROE, n=3, viscous=sdg.BR2, mu=0.01,
         conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
+    # incompressible model (weakly compressible EOS; Central / Lax-Friedrichs / Exact), Boussinesq source
+    "inc-euler-shearlayer-quad-p3-exact": lambda: cases.shear_layer_case(n=4, p=3, flux=sdg.EXACT, jitter=0.0,
+                                                                         split=0.0),
+    "inc-euler-shearlayer-quad-p2-central": lambda: cases.shear_layer_case(n=4, p=2, flux=sdg.CENTRAL, jitter=0.0,
+                                                                           split=0.0),
+    "inc-ns-taylorvortex-quad-p4-exact-br2": lambda: cases.taylor_vortex_case(n=4, p=4, mu=1e-2, c0=10.0, dt=1e-4),
+    "inc-ns-taylorvortex-quad-p3-lf-br1": lambda: cases.taylor_vortex_case(n=4, p=3, flux=sdg.LAX_FRIEDRICHS,
+                                                                           viscous=sdg.BR1, mu=1e-2, c0=10.0, dt=1e-4),
+    "inc-euler-channel-farfield-quad-p2-exact": lambda: cases.inc_channel_case(p=2, n=3),
+    "inc-ns-lidcavity-quad-p3-lf-br2": lambda: cases.cavity_case(p=3, n=4, mu=1e-2),
+    "inc-ns-thermalcavity-quad-p3-exact-br1-boussinesq": lambda: cases.cavity_case(
+        p=3, n=4, flux=sdg.EXACT, viscous=sdg.BR1, mu=1e-2, boussinesq=True),
+    "inc-ns-lidcavity-hex-p2-lf-br2": lambda: cases.cavity_3d_case(p=2, n=3, flux=sdg.LAX_FRIEDRICHS,
+                                                                    viscous=sdg.BR2, mu=1e-2),
+    "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq": lambda: cases.cavity_3d_case(p=2, n=3, mu=1e-2,
+                                                                                      boussinesq=True),
 }
 
 
@@ -111,10 +129,10 @@ def make(name):
     return s, dt
 
 
-def direction(u, seed):
-    """Seeded perturbation scaled per variable by the state's own magnitude."""
+def direction(u, seed, floor=1e-3):
+    """Seeded perturbation scaled per variable by the state's own magnitude (at least `floor`)."""
     rng = np.random.default_rng(seed)
-    scale = np.abs(u).mean(0) + 1e-3
+    scale = np.abs(u).mean(0) + floor
     return rng.standard_normal(u.shape) * scale
 
 
@@ -129,10 +147,11 @@ def test_jvp_residual_matches_central_differences(name):
     d = direction(u, 1)
     jvp = s.jvp_residual(d)
     # Lax-Friedrichs' max(|u.n| + c) switches sides at face points where the two are within ~h of each
-    # other; the difference quotient straddles the switch there (an error that shrinks with h), so its
-    # step is smaller
-    lf = s.config.convective_flux == sdg.LAX_FRIEDRICHS
-    h, tol = (1e-8, 1e-5) if lf else (1e-6, 1e-6)
+    # other, and the Exact flux takes its upwind side from the sign of u* (exactly 0 where the initial
+    # state's normal velocity vanishes at a face point); the difference quotient straddles the switch there
+    # (an error that shrinks with h), so its step is smaller
+    flux = s.config.convective_flux
+    h, tol = {sdg.LAX_FRIEDRICHS: (1e-8, 1e-5), sdg.EXACT: (1e-7, 1e-6)}.get(flux, (1e-6, 1e-6))
     s.set_state_point(u + h * d)
     rp = s.residual_point()
     s.set_state_point(u - h * d)
@@ -152,7 +171,7 @@ def test_vjp_is_the_transpose_of_jvp(name):
     vjp, mubar = s.vjp_residual(lam)
     lhs, rhs = float(np.sum(lam * jvp)), float(np.sum(vjp * d))
     assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), abs(rhs)), (lhs, rhs)
-    if s.config.equation == sdg.NAVIER_STOKES:
+    if s.config.equation in VISCOUS:
         dmu = s.jvp_residual(np.zeros_like(u), viscosity_tangent=1.0)
         lm = float(np.sum(lam * dmu))
         assert abs(lm - mubar) <= 1e-11 * max(abs(lm), 1e-300), (lm, mubar)
@@ -168,6 +187,7 @@ def test_vjp_is_the_transpose_of_jvp(name):
 
 
 @pytest.mark.parametrize("name", ["euler-quad-p3-roe", "euler-hex-p2-hllc", "ns-hex-p3-br1-roe",
+                                  "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq",
                                   "ns-quad-p4-br1-hllc", "ns-hex-p2-br2-hllc", "ns-channel-walls-quad-p3-br2-roe"])
 def test_trajectory_dot_product_with_checkpointing(name):
     steps, interval = 5, 2
@@ -175,7 +195,7 @@ def test_trajectory_dot_product_with_checkpointing(name):
     b, _ = make(name)
     u0 = a.state_point()
     d0 = direction(u0, 4)
-    dmu = 0.3 if a.config.equation == sdg.NAVIER_STOKES else 0.0
+    dmu = 0.3 if a.config.equation in VISCOUS else 0.0
     dN = a.jvp_steps(dt, steps, d0, viscosity_tangent=dmu)
     uN_tlm = a.state_point()
     lamN = np.random.default_rng(5).standard_normal(u0.shape)
@@ -206,7 +226,8 @@ def test_checkpoint_interval_does_not_change_the_adjoint():
 # HLLC and Lax-Friedrichs switch branches (PVRS pressure against each side's pressure, the larger wave
 # speed) at many face points of a low-Mach trajectory, where difference quotients straddle the switches;
 # the trajectory checks use the smooth fluxes (cfg: Roe + BR1 is the adjoint workload)
-@pytest.mark.parametrize("name", ["euler-hex-p3-central", "ns-hex-p3-br1-roe", "euler-quad-p3-roe"])
+@pytest.mark.parametrize("name", ["euler-hex-p3-central", "ns-hex-p3-br1-roe", "euler-quad-p3-roe",
+                                  "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-euler-shearlayer-quad-p2-central"])
 def test_kinetic_energy_gradient_matches_finite_differences(name):
     steps, interval = 6, 3
     s, dt = make(name)
@@ -230,7 +251,7 @@ def test_kinetic_energy_gradient_matches_finite_differences(name):
     fd = (J(u0 + h * d0) - J(u0 - h * d0)) / (2 * h)
     ad = float(np.sum(lam0 * d0))
     assert abs(fd - ad) <= 1e-6 * max(abs(fd), abs(ad)), (fd, ad, J0)
-    if s.config.equation == sdg.NAVIER_STOKES:
+    if s.config.equation in VISCOUS:
         hm = 1e-6 * mu0
         fdm = (J(u0, mu0 + hm) - J(u0, mu0 - hm)) / (2 * hm)
         s.set_viscosity(mu0)
@@ -307,7 +328,8 @@ def test_surface_force_of_a_fluid_at_rest_is_the_pressure_times_the_area():
 
 
 @pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-box-walls-farfield-hex-p2-roe",
-                                  "ns-channel-walls-quad-p3-br1-roe", "ns-box-walls-hex-p2-br1-roe"])
+                                  "ns-channel-walls-quad-p3-br1-roe", "ns-box-walls-hex-p2-br1-roe",
+                                  "inc-ns-thermalcavity-quad-p3-exact-br1-boussinesq", "inc-ns-lidcavity-hex-p2-lf-br2"])
 def test_surface_force_cotangent_matches_central_differences(name):
     s, _ = make(name)
     group, e = (1, [0.3, -1.0]) if s.counts.dimension == 2 else (3, [0.2, -1.0, 0.4])
@@ -327,7 +349,9 @@ def test_surface_force_cotangent_matches_central_differences(name):
 @pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-channel-farfield-quad-p2-hllc",
                                   "euler-box-walls-farfield-hex-p2-roe", "ns-channel-walls-quad-p3-br1-roe",
                                   "ns-channel-farfield-quad-p2-br1-hllc", "ns-box-walls-hex-p2-br1-roe",
-                                  "ns-channel-walls-quad-p3-br2-roe"])
+                                  "ns-channel-walls-quad-p3-br2-roe", "inc-euler-channel-farfield-quad-p2-exact",
+                                  "inc-ns-lidcavity-quad-p3-lf-br2", "inc-ns-thermalcavity-quad-p3-exact-br1-boussinesq",
+                                  "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq"])
 def test_force_gradient_through_a_trajectory(name):
     """J = e . force on a wall after N steps: dJ/dU_0 in a seeded direction and dJ/d(boundary primitives) in a
     seeded direction of every boundary point's (rho, u, T), against central differences of the trajectory."""
@@ -350,18 +374,22 @@ def test_force_gradient_through_a_trajectory(name):
     cot = s.surface_force_cotangent(group, e)
     gu, gmu = s.adjoint_recorded(cot)
     gg = s.adjoint_boundary_cotangent()
+    # the weakly compressible pressure c0^2 (rho - rho0) scales the density's rounding by c0^2, so the
+    # difference quotients of the incompressible cases take larger steps (round-off ~ 1e-14 / h) and a ghost
+    # direction whose zero velocities (walls at rest) are perturbed at 0.1
+    inc = s.config.equation in (sdg.INCOMPRESSIBLE_EULER, sdg.INCOMPRESSIBLE_NAVIER_STOKES)
     du = direction(u0, 7)
-    dg = direction(g0, 8)
-    h = 1e-6
+    dg = direction(g0, 8, floor=0.1 if inc else 1e-3)
+    h = 1e-5 if inc else 1e-6
     fd_u = (J(u0 + h * du, g0) - J(u0 - h * du, g0)) / (2 * h)
     fd_g = (J(u0, g0 + h * dg) - J(u0, g0 - h * dg)) / (2 * h)
     assert abs(float(np.sum(gu * du)) - fd_u) <= 1e-6 * abs(fd_u), (float(np.sum(gu * du)), fd_u)
     assert abs(float(np.sum(gg * dg)) - fd_g) <= 1e-6 * abs(fd_g), (float(np.sum(gg * dg)), fd_g)
-    if s.config.equation == sdg.NAVIER_STOKES:
+    if s.config.equation in VISCOUS:
         # and the viscosity: the adjoint gives the trajectory's part, the force's own (tau is linear in mu)
         # is its value at U_N with the state held
         mu = s.config.dynamic_viscosity
-        hm = 1e-6 * mu
+        hm = (1e-4 if inc else 1e-6) * mu
         s.set_state_point(u0)
         s.set_boundary_primitive(g0)
         s.stepSolver(dt, steps)
