@@ -47,6 +47,7 @@ extern "C" {
 
 /* ---- enumerations (values equal the reference's enum order, src/Utils/Enum.cpp) --------------- */
 enum sdg_element_type { /* gmsh first-order type numbers (src/Solver/SimulationControl.cpp:26-31) */
+  SDG_ELEMENT_LINE = 1,     /* DimensionEnum::D1 / MeshModelEnum::Line; its faces are points */
   SDG_ELEMENT_TRIANGLE = 2,
   SDG_ELEMENT_QUADRANGLE = 3,
   SDG_ELEMENT_HEXAHEDRON = 5
@@ -85,25 +86,31 @@ enum sdg_boundary_condition {                                                   
 
 /* ---- mesh: first-order (straight-sided) geometry in gmsh vertex order -------------------------- */
 typedef struct sdg_mesh {
-  int32_t dimension;                  /* 2 or 3                                                     */
+  int32_t dimension;                  /* 1, 2 or 3                                                  */
   int64_t node_count;
   const double* node_coordinate;      /* [node_count][3]                                            */
   const int32_t* periodic_master;     /* [node_count] node -> periodic master node (itself when not a
                                          slave), or NULL.  Replaces gmsh::getPeriodicNodes pairing
-                                         (src/Mesh/Adjacency.cpp:213-328).                          */
+                                         (src/Mesh/Adjacency.cpp:213-328).  1D without a map: the two
+                                         periodic boundary points are joined, the first one's element
+                                         on the left (Adjacency.cpp:185-211).                       */
   int64_t triangle_count;
   const int32_t* triangle_node;       /* [triangle_count][3]                                        */
   int64_t quadrangle_count;
   const int32_t* quadrangle_node;     /* [quadrangle_count][4]                                      */
   int64_t hexahedron_count;
   const int32_t* hexahedron_node;     /* [hexahedron_count][8]                                      */
-  int64_t boundary_count;             /* boundary elements: lines (2D) or quadrangles (3D)          */
-  const int32_t* boundary_node;       /* [boundary_count][2 or 4]                                   */
+  int64_t boundary_count;             /* boundary elements: points (1D), lines (2D), quadrangles (3D) */
+  const int32_t* boundary_node;       /* [boundary_count][1, 2 or 4]                                */
   const int32_t* boundary_physical;   /* [boundary_count] 1-based physical group index              */
   int32_t physical_count;
   const int32_t* physical_boundary_condition; /* [physical_count] sdg_boundary_condition per group,
                                                  as System::addBoundaryCondition sets it
                                                  (src/Utils/SystemControl.cpp:76-80)                */
+  int64_t line_count;                 /* 1D: line elements, vertex 0 then vertex 1 (x increasing: the
+                                         reference's point normals are -1 at local face 0 and +1 at
+                                         local face 1, Geometry.cpp:102-112)                        */
+  const int32_t* line_node;           /* [line_count][2]                                            */
 } sdg_mesh;
 
 /* ---- physics and numerics: the runtime form of the reference's SimulationControl -------------- */
@@ -274,13 +281,18 @@ typedef struct sdg_generated_mesh {
 int sdg_mesh_generate_2d(double x0, double y0, double lx, double ly, int32_t nx, int32_t ny,
                          double jitter, double split_fraction, uint64_t seed, int32_t periodic,
                          const int32_t* boundary_condition, sdg_generated_mesh* out);
+/* 1D segment [x0, x0+lx], nx lines (examples/sod_1d_ceuler.cpp:68-82 and periodic_1d_ceuler.cpp:63-77:
+ * gmsh transfinite curves); periodic = 1 joins the two end points (one group, SDG_BC_PERIODIC), else two
+ * groups (x0 end, x0+lx end) with boundary_condition[0..1]. */
+int sdg_mesh_generate_1d(double x0, double lx, int32_t nx, int32_t periodic, const int32_t* boundary_condition,
+                         sdg_generated_mesh* out);
 /* 3D box, nx x ny x nz hexahedra; periodic = 1 pairs opposite faces, else six groups
  * (x-, x+, y-, y+, z-, z+). */
 int sdg_mesh_generate_3d(double x0, double y0, double z0, double lx, double ly, double lz, int32_t nx,
                          int32_t ny, int32_t nz, int32_t periodic, const int32_t* boundary_condition,
                          sdg_generated_mesh* out);
 /* Read a gmsh MSH 4.1 ASCII file (first-order or high-order elements; only the primary vertices
- * are used).  Physical groups of dimension d-1 become boundary groups in file order. */
+ * are used).  Physical groups of dimension d-1 (points in 1D) become boundary groups in file order. */
 int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out);
 int sdg_mesh_free(sdg_generated_mesh* mesh);
 

@@ -28,28 +28,30 @@ namespace orc {
 // long double for an extended-precision truth (build flag -DORC_REAL="long double").
 using Real = ORC_REAL;
 
-enum ElemType { kTri = 2, kQuad = 3, kHex = 5 };
+enum ElemType { kLine = 1, kTri = 2, kQuad = 3, kHex = 5 };
 
-inline int elemDim(int t) { return t == kHex ? 3 : 2; }
-inline int elemFaces(int t) { return t == kTri ? 3 : (t == kQuad ? 4 : 6); }
-inline int elemVerts(int t) { return t == kTri ? 3 : (t == kQuad ? 4 : 8); }
-inline int faceVerts(int t) { return t == kHex ? 4 : 2; }
+inline int elemDim(int t) { return t == kLine ? 1 : (t == kHex ? 3 : 2); }
+inline int elemFaces(int t) { return t == kLine ? 2 : (t == kTri ? 3 : (t == kQuad ? 4 : 6)); }
+inline int elemVerts(int t) { return t == kLine ? 2 : (t == kTri ? 3 : (t == kQuad ? 4 : 8)); }
+inline int faceVerts(int t) { return t == kLine ? 1 : (t == kHex ? 4 : 2); }
 
 // Face vertex lists of each element type (SimulationControl.cpp:170-216).
 inline const int* faceVertexTable(int t) {
+  static const int line[] = {0, 1};
   static const int tri[] = {0, 1, 1, 2, 2, 0};
   static const int quad[] = {0, 1, 1, 2, 2, 3, 3, 0};
   static const int hex[] = {0, 3, 2, 1, 0, 1, 5, 4, 0, 4, 7, 3, 1, 2, 6, 5, 2, 3, 7, 6, 4, 5, 6, 7};
-  return t == kTri ? tri : (t == kQuad ? quad : hex);
+  return t == kLine ? line : (t == kTri ? tri : (t == kQuad ? quad : hex));
 }
 
 // Reference-element vertex coordinates (gmsh conventions).
 inline std::array<Real, 3> refVertex(int t, int v) {
+  static const Real line[2][3] = {{-1, 0, 0}, {1, 0, 0}};
   static const Real tri[3][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}};
   static const Real quad[4][3] = {{-1, -1, 0}, {1, -1, 0}, {1, 1, 0}, {-1, 1, 0}};
   static const Real hex[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
                                    {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
-  const Real* p = t == kTri ? tri[v] : (t == kQuad ? quad[v] : hex[v]);
+  const Real* p = t == kLine ? line[v] : (t == kTri ? tri[v] : (t == kQuad ? quad[v] : hex[v]));
   return {p[0], p[1], p[2]};
 }
 
@@ -114,7 +116,10 @@ inline Quadrature elementQuadrature(int t, int order) {
   }
   const int m = linePoints(order);
   std::vector<Real> gx, gw; gaussLegendre(m, gx, gw);
-  if (t == kQuad) {  // index = i*m + j with (xi=x_i, eta=x_j)
+  if (t == kLine) {
+    q.n = m;
+    for (int i = 0; i < m; ++i) { q.x.insert(q.x.end(), {gx[i], 0.0, 0.0}); q.w.push_back(gw[i]); }
+  } else if (t == kQuad) {  // index = i*m + j with (xi=x_i, eta=x_j)
     q.n = m * m;
     for (int i = 0; i < m; ++i)
       for (int j = 0; j < m; ++j) { q.x.insert(q.x.end(), {gx[i], gx[j], 0.0}); q.w.push_back(gw[i] * gw[j]); }
@@ -134,6 +139,10 @@ inline Quadrature elementQuadrature(int t, int order) {
 // index i*m + j with (xi=x_i, eta=x_j)).
 inline Quadrature faceQuadrature(int t, int order) {
   Quadrature q; q.dim = elemDim(t) - 1;
+  if (t == kLine) {  // point faces: one point of weight 1 (kPoint rules, SimulationControl.cpp:287-289)
+    q.n = 1; q.x = {0.0, 0.0, 0.0}; q.w = {1.0};
+    return q;
+  }
   const int m = linePoints(order);
   std::vector<Real> gx, gw; gaussLegendre(m, gx, gw);
   if (t != kHex) {
@@ -149,12 +158,14 @@ inline Quadrature faceQuadrature(int t, int order) {
 
 // P1 shape functions of the face reference element (BasisFunction.cpp:76-111 uses gmsh Lagrange1).
 inline void faceShape(int t, const Real* fx, Real* n) {
+  if (t == kLine) { n[0] = 1.0; return; }
   if (t != kHex) { n[0] = 0.5 * (1.0 - fx[0]); n[1] = 0.5 * (1.0 + fx[0]); return; }
   const Real x = fx[0], y = fx[1];
   n[0] = 0.25 * (1 - x) * (1 - y); n[1] = 0.25 * (1 + x) * (1 - y);
   n[2] = 0.25 * (1 + x) * (1 + y); n[3] = 0.25 * (1 - x) * (1 + y);
 }
 inline void faceShapeGrad(int t, const Real* fx, Real* dxi, Real* deta) {
+  if (t == kLine) { dxi[0] = 0.0; return; }
   if (t != kHex) { dxi[0] = -0.5; dxi[1] = 0.5; return; }
   const Real x = fx[0], y = fx[1];
   dxi[0] = -0.25 * (1 - y); dxi[1] = 0.25 * (1 - y); dxi[2] = 0.25 * (1 + y); dxi[3] = -0.25 * (1 + y);
@@ -163,6 +174,12 @@ inline void faceShapeGrad(int t, const Real* fx, Real* dxi, Real* deta) {
 
 // P1 element shape functions and reference gradients (geometry map of straight-sided elements).
 inline void elemShape(int t, const Real* X, Real* n, Real* g /* nv*3 */) {
+  if (t == kLine) {
+    n[0] = 0.5 * (1 - X[0]); n[1] = 0.5 * (1 + X[0]);
+    const Real gg[6] = {-0.5, 0, 0, 0.5, 0, 0};
+    for (int i = 0; i < 6; ++i) g[i] = gg[i];
+    return;
+  }
   if (t == kTri) {
     n[0] = 1 - X[0] - X[1]; n[1] = X[0]; n[2] = X[1];
     const Real gg[9] = {-1, -1, 0, 1, 0, 0, 0, 1, 0};
@@ -219,16 +236,24 @@ inline Dual kernelD(int k, Dual x) {
 }
 
 inline int basisCount(int t, int p) {
+  if (t == kLine) return p + 1;
   if (t == kTri) return (p + 1) * (p + 2) / 2;
   if (t == kQuad) return (p + 1) * (p + 1);
   return (p + 1) * (p + 1) * (p + 1);
 }
 
 // Modal (hierarchic H1) basis: values [nb] and reference gradients [nb][3] at X.
-//   quad: index a*(P+1)+b -> l_a(xi) l_b(eta); hex: index (a*(P+1)+b)*(P+1)+c.
+//   line: index a -> l_a(xi); quad: index a*(P+1)+b -> l_a(xi) l_b(eta); hex: index (a*(P+1)+b)*(P+1)+c.
 //   tri : vertices lambda_i; edges (0,1),(1,2),(2,0) with l_a l_b phi_{k-2}(l_b-l_a), k=2..P;
 //         bubbles l0 l1 l2 P_i(l2-l1) P_j(l1-l0), i+j<=P-3.
 inline void modalBasis(int t, int p, const Real* X, Real* val, Real* grad) {
+  if (t == kLine) {
+    for (int a = 0; a <= p; ++a) {
+      Real v, d; lobatto(a, X[0], v, d);
+      val[a] = v; grad[a * 3 + 0] = d; grad[a * 3 + 1] = 0; grad[a * 3 + 2] = 0;
+    }
+    return;
+  }
   if (t == kQuad || t == kHex) {
     const int m = p + 1;
     Real lv[3][6], ld[3][6];
@@ -374,7 +399,7 @@ struct RefElement {
     high.assign(nb, 0);
     for (int b = 0; b < nb; ++b) {
       int deg = 0;
-      if (t == kQuad || t == kHex) {
+      if (t == kLine || t == kQuad || t == kHex) {
         int r = b;
         for (int dd = 0; dd < dim; ++dd) { deg = std::max(deg, std::max(1, r % (order + 1))); r /= order + 1; }
       } else if (b < 3) {
@@ -396,7 +421,7 @@ struct RefElement {
       }
     lsqInv.assign(size_t(nb) * nb, 0.0);
     invert(nb, ptp.data(), lsqInv.data());
-    const int m = linePoints(2 * order + 1);
+    const int m = t == kLine ? 1 : linePoints(2 * order + 1);
     perm.clear();
     for (int r = 0; r < (t == kHex ? 4 : 1); ++r) perm.push_back(facePermutation(t, m, r));
   }

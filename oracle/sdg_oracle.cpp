@@ -102,6 +102,7 @@ struct Problem {
 // S from each face's diagonals) -- exact for squares and cubes.
 static Real innerRadiusOf(int type, const double* nodes, const int* vv) {
   auto X = [&](int k, int d) { return Real(nodes[size_t(vv[k]) * 3 + d]); };
+  if (type == kLine) return std::fabs(X(1, 0) - X(0, 0)) / 2.0;  // gmsh MLine: half the length
   auto sub = [&](int a, int b, Real* o) { for (int d = 0; d < 3; ++d) o[d] = X(a, d) - X(b, d); };
   auto norm = [](const Real* a) { return std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); };
   auto crossNorm = [&](const Real* a, const Real* b) {
@@ -166,7 +167,10 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
       }
       for (int l = 0; l < 3; ++l) B.qcoord[(size_t(e) * nq + q) * 3 + l] = x[l];
       Real det, inv[3][3];
-      if (d == 2) {
+      if (d == 1) {
+        det = J[0][0];
+        inv[0][0] = 1.0 / det;
+      } else if (d == 2) {
         det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
         inv[0][0] = J[1][1] / det; inv[0][1] = -J[0][1] / det; inv[1][0] = -J[1][0] / det; inv[1][1] = J[0][0] / det;
       } else {
@@ -203,12 +207,13 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
     invert(nb, m.data(), &B.minv[size_t(e) * nb * nb]);
     if (P.refine) std::copy(m.begin(), m.end(), &B.mass[size_t(e) * nb * nb]);
     // minEdge quality: shortest straight edge between vertices.
+    static const int lineE[1][2] = {{0, 1}};
     static const int triE[3][2] = {{0, 1}, {1, 2}, {2, 0}};
     static const int quadE[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
     static const int hexE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
                                     {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
-    const int(*E)[2] = B.type == kTri ? triE : (B.type == kQuad ? quadE : hexE);
-    const int nE = B.type == kTri ? 3 : (B.type == kQuad ? 4 : 12);
+    const int(*E)[2] = B.type == kLine ? lineE : (B.type == kTri ? triE : (B.type == kQuad ? quadE : hexE));
+    const int nE = B.type == kLine ? 1 : (B.type == kTri ? 3 : (B.type == kQuad ? 4 : 12));
     Real me = 1e300;
     for (int i = 0; i < nE; ++i) {
       const double* a = &nodes[size_t(vv[E[i][0]]) * 3];
@@ -240,7 +245,10 @@ static void faceGeometry(Problem& P, Face& F, const double* nodes) {
     }
     for (int l = 0; l < 3; ++l) F.coord[j * 3 + l] = x[l];
     Real n[3], det;
-    if (P.dim == 2) {  // Geometry.cpp:115-127
+    if (P.dim == 1) {  // Geometry.cpp:102-112: -1 at local face 0, +1 at local face 1; a point's measure is 1
+      det = 1.0;
+      n[0] = F.fl == 0 ? -1.0 : 1.0; n[1] = 0; n[2] = 0;
+    } else if (P.dim == 2) {  // Geometry.cpp:115-127
       det = std::sqrt(tx[0] * tx[0] + tx[1] * tx[1]);
       n[0] = tx[1] / det; n[1] = -tx[0] / det; n[2] = 0;
     } else {           // Geometry.cpp:130-147
@@ -275,13 +283,14 @@ static void buildAdjacency(Problem& P, const sdg_mesh& m) {
       }
   }
   std::map<std::vector<int>, int> bmap;
-  const int nbv = P.dim == 2 ? 2 : 4;
+  const int nbv = P.dim == 1 ? 1 : (P.dim == 2 ? 2 : 4);
   for (int64_t i = 0; i < m.boundary_count; ++i) {
     std::vector<int> key;
     for (int k = 0; k < nbv; ++k) key.push_back(master(m.boundary_node[i * nbv + k]));
     std::sort(key.begin(), key.end());
     bmap[key] = int(i);
   }
+  std::vector<std::pair<int, Face>> periodicEnds;
   for (auto& kv : faces) {
     Entry& en = kv.second;
     Face F;
@@ -299,9 +308,23 @@ static void buildAdjacency(Problem& P, const sdg_mesh& m) {
       F.physical = m.boundary_physical[it->second];
       if (F.physical < 1 || F.physical > m.physical_count) throw std::runtime_error("bad physical index");
       F.bc = m.physical_boundary_condition[F.physical - 1];
+      if (F.bc == SDG_BC_PERIODIC && P.dim == 1 && !m.periodic_master) {
+        periodicEnds.push_back({it->second, F});
+        continue;
+      }
       if (F.bc == SDG_BC_PERIODIC) throw std::runtime_error("unpaired periodic face");
       P.boundary.push_back(F);
     }
+  }
+  // 1D periodic without a node map (Adjacency.cpp:185-211): the first two point elements are joined, the
+  // first one's parent on the left
+  if (!periodicEnds.empty()) {
+    if (periodicEnds.size() != 2) throw std::runtime_error("a 1D periodic mesh needs two periodic end points");
+    std::sort(periodicEnds.begin(), periodicEnds.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+    Face F;
+    F.bl = periodicEnds[0].second.bl; F.el = periodicEnds[0].second.el; F.fl = periodicEnds[0].second.fl;
+    F.br = periodicEnds[1].second.bl; F.er = periodicEnds[1].second.el; F.fr = periodicEnds[1].second.fl;
+    P.interior.push_back(F);
   }
 }
 
@@ -829,7 +852,8 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
   if (P->ns() && P->visc == 0) throw std::runtime_error("NS needs BR1 or BR2");
   struct Src { int type; int64_t n; const int32_t* v; };
   std::vector<Src> src;
-  if (P->dim == 2) { src.push_back({kTri, m->triangle_count, m->triangle_node}); src.push_back({kQuad, m->quadrangle_count, m->quadrangle_node}); }
+  if (P->dim == 1) src.push_back({kLine, m->line_count, m->line_node});
+  else if (P->dim == 2) { src.push_back({kTri, m->triangle_count, m->triangle_node}); src.push_back({kQuad, m->quadrangle_count, m->quadrangle_node}); }
   else src.push_back({kHex, m->hexahedron_count, m->hexahedron_node});
   for (const Src& s : src) {
     if (s.n <= 0) continue;

@@ -6,7 +6,7 @@ System/Solver interface.
 """
 from . import _abi
 from ._abi import (ADIABATIC_NONSLIP_WALL, ADIABATIC_SLIP_WALL, BR1, BR2, CENTRAL, EULER, EXACT, FORWARD_EULER,
-                   HEUN_RK2, HEXAHEDRON, HLLC, INCOMPRESSIBLE_EULER, INCOMPRESSIBLE_NAVIER_STOKES,
+                   HEUN_RK2, HEXAHEDRON, HLLC, INCOMPRESSIBLE_EULER, INCOMPRESSIBLE_NAVIER_STOKES, LINE,
                    ISOTHERMAL_NONSLIP_WALL, LAX_FRIEDRICHS, NAVIER_STOKES, PERIODIC, PRESSURE_OUTFLOW, QUADRANGLE,
                    RIEMANN_FARFIELD, ROE, SHOCK_NONE, ARTIFICIAL_VISCOSITY, SOURCE_BOUSSINESQ, SOURCE_NONE, SSPRK3, TRANSPORT_CONSTANT,
                    TRANSPORT_NONE, TRANSPORT_SUTHERLAND, TRIANGLE, VELOCITY_INFLOW, VISCOUS_NONE, SdgError)

@@ -35,7 +35,7 @@ __device__ double avTensorSensor(const AvArgs& a, int64_t e) {
   double rho[kAvMaxNb], c[kAvMaxNb], t[kAvMaxNb];
   const double* u = a.u + e * a.ustride;
   for (int i = 0; i < nb; ++i) { rho[i] = u[i]; c[i] = u[i]; }
-  const int strides[3] = {dim == 2 ? n : n * n, dim == 2 ? 1 : n, 1};
+  const int strides[3] = {dim == 1 ? 1 : (dim == 2 ? n : n * n), dim == 2 ? 1 : n, 1};
   // nodal -> modal along each axis
   for (int ax = 0; ax < dim; ++ax) {
     const int st = strides[ax];
@@ -146,13 +146,18 @@ Rec avRec(int kind, int64_t count) {
 
 }  // namespace
 
-// Inner radius (gmsh quality "innerRadius", Geometry.cpp:31-41; gmsh 4.13.1 is not vendored): 2A/perimeter for
+// Inner radius (gmsh quality "innerRadius", Geometry.cpp:31-41; gmsh 4.13.1 is not vendored): half the length of
+// a line (gmsh MLine), 2A/perimeter for
 // triangles and quadrangles (A of a quadrangle from its diagonals), 3V/S for hexahedra (V by 2x2x2 Gauss
 // quadrature of the trilinear map, each face's area from its diagonals); exact for squares and cubes.
 double innerRadiusOf(int type, const double* nodes, const int32_t* vv) {
   auto sub = [&](int a, int b, double* o) {
     for (int d = 0; d < 3; ++d) o[d] = nodes[size_t(vv[a]) * 3 + d] - nodes[size_t(vv[b]) * 3 + d];
   };
+  if (type == SDG_ELEMENT_LINE) {  // gmsh's MLine inner radius: half the length
+    double e[3]; sub(1, 0, e);
+    return norm3(e) / 2.0;
+  }
   if (type == SDG_ELEMENT_TRIANGLE || type == SDG_ELEMENT_QUADRANGLE) {
     const int nv = type == SDG_ELEMENT_TRIANGLE ? 3 : 4;
     double per = 0, e[3];

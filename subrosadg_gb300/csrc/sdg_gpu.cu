@@ -43,7 +43,8 @@ void facePointInParent(int type, int f, const double* fx, double* X) {
   const int nfv = typeFaceVertices(type);
   const int* fl = faceVertexList(type);
   double sh[4];
-  if (nfv == 2) { sh[0] = 0.5 * (1 - fx[0]); sh[1] = 0.5 * (1 + fx[0]); }
+  if (nfv == 1) sh[0] = 1.0;
+  else if (nfv == 2) { sh[0] = 0.5 * (1 - fx[0]); sh[1] = 0.5 * (1 + fx[0]); }
   else {
     const double x = fx[0], y = fx[1];
     sh[0] = 0.25 * (1 - x) * (1 - y); sh[1] = 0.25 * (1 + x) * (1 - y);
@@ -186,6 +187,12 @@ void checkLaunch(sdg_handle* h) { checkLaunch(h, h->stream); }
 // ---- geometry --------------------------------------------------------------------------------------
 void shapeGrad(int type, const double* X, double* N, double* G /* [nv][3] */) {
   const int nv = typeVertices(type);
+  if (type == SDG_ELEMENT_LINE) {
+    N[0] = 0.5 * (1 - X[0]); N[1] = 0.5 * (1 + X[0]);
+    const double g[6] = {-0.5, 0, 0, 0.5, 0, 0};
+    std::copy(g, g + 6, G);
+    return;
+  }
   if (type == SDG_ELEMENT_TRIANGLE) {
     N[0] = 1 - X[0] - X[1]; N[1] = X[0]; N[2] = X[1];
     const double g[9] = {-1, -1, 0, 1, 0, 0, 0, 1, 0};
@@ -220,6 +227,7 @@ void jacobianAt(int type, int dim, const double* nodes, const int32_t* vv, const
 
 // |J| J^-1 (adjugate, row b = |J| dxi_b/dx) and det.
 double adjugate(int dim, const double J[3][3], double A[3][3]) {
+  if (dim == 1) { A[0][0] = 1.0; return J[0][0]; }
   if (dim == 2) {
     A[0][0] = J[1][1]; A[0][1] = -J[0][1]; A[1][0] = -J[1][0]; A[1][1] = J[0][0];
     return J[0][0] * J[1][1] - J[0][1] * J[1][0];
@@ -237,7 +245,7 @@ double adjugate(int dim, const double J[3][3], double A[3][3]) {
 }
 
 bool isAffine(int type, const double* nodes, const int32_t* vv, double tol) {
-  if (type == SDG_ELEMENT_TRIANGLE) return true;
+  if (type == SDG_ELEMENT_TRIANGLE || type == SDG_ELEMENT_LINE) return true;
   const auto P = [&](int k, int d) { return nodes[size_t(vv[k]) * 3 + d]; };
   for (int d = 0; d < 3; ++d) {
     if (type == SDG_ELEMENT_QUADRANGLE) {
@@ -253,11 +261,13 @@ bool isAffine(int type, const double* nodes, const int32_t* vv, double tol) {
 }
 
 double minEdgeOf(int type, const double* nodes, const int32_t* vv) {
+  static const int lineE[1][2] = {{0, 1}};
   static const int triE[3][2] = {{0, 1}, {1, 2}, {2, 0}};
   static const int quadE[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
   static const int hexE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
-  const int(*E)[2] = type == SDG_ELEMENT_TRIANGLE ? triE : (type == SDG_ELEMENT_QUADRANGLE ? quadE : hexE);
-  const int nE = type == SDG_ELEMENT_TRIANGLE ? 3 : (type == SDG_ELEMENT_QUADRANGLE ? 4 : 12);
+  const int(*E)[2] = type == SDG_ELEMENT_LINE ? lineE
+                     : (type == SDG_ELEMENT_TRIANGLE ? triE : (type == SDG_ELEMENT_QUADRANGLE ? quadE : hexE));
+  const int nE = type == SDG_ELEMENT_LINE ? 1 : (type == SDG_ELEMENT_TRIANGLE ? 3 : (type == SDG_ELEMENT_QUADRANGLE ? 4 : 12));
   double best = 1e300;
   for (int i = 0; i < nE; ++i) {
     double s = 0;
@@ -282,7 +292,7 @@ void buildTensorTables(DevBlock& B) {
     for (int g = 0; g < n; ++g) if (std::fabs(o.x[g] - t) < 1e-12) return g;
     throw Failure(SDG_ERR_INVALID_ARGUMENT, "face point does not lie on a Gauss line");
   };
-  const int stride[3] = {dim == 2 ? n : n * n, dim == 2 ? 1 : n, 1};
+  const int stride[3] = {dim == 1 ? 1 : (dim == 2 ? n : n * n), dim == 2 ? 1 : n, 1};
   for (int f = 0; f < B.nface; ++f) {
     int axis = -1, end = 0;
     for (int j = 0; j < B.nfq; ++j) {
@@ -716,7 +726,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
   sdg_handle* h = H.get();
   try {
     const sdg_config& c = *config;
-    if (mesh->dimension != 2 && mesh->dimension != 3) throw Failure(SDG_ERR_INVALID_ARGUMENT, "dimension must be 2 or 3");
+    if (mesh->dimension < 1 || mesh->dimension > 3) throw Failure(SDG_ERR_INVALID_ARGUMENT, "dimension must be 1, 2 or 3");
     if (c.polynomial_order < 1 || c.polynomial_order > 5) throw Failure(SDG_ERR_INVALID_ARGUMENT, "polynomial order must be 1..5");
     if (c.equation < SDG_COMPRESSIBLE_EULER || c.equation > SDG_INCOMPRESSIBLE_NS) throw Failure(SDG_ERR_INVALID_ARGUMENT, "bad equation");
     const bool incomp = c.equation == SDG_INCOMPRESSIBLE_EULER || c.equation == SDG_INCOMPRESSIBLE_NS;
@@ -770,7 +780,9 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     h->ph.tref = c.reference_temperature;
     // element blocks, in the reference's loop order
     std::vector<Block> mb;
-    if (h->dim == 2) {
+    if (h->dim == 1) {
+      if (mesh->line_count > 0) mb.push_back({SDG_ELEMENT_LINE, mesh->line_count, mesh->line_node});
+    } else if (h->dim == 2) {
       if (mesh->triangle_count > 0) mb.push_back({SDG_ELEMENT_TRIANGLE, mesh->triangle_count, mesh->triangle_node});
       if (mesh->quadrangle_count > 0) mb.push_back({SDG_ELEMENT_QUADRANGLE, mesh->quadrangle_count, mesh->quadrangle_node});
     } else {
@@ -795,7 +807,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       B.nb = modalCount(b.type, h->p);
       const PointRule vr = volumeRule(b.type, h->p);
       B.nq = vr.n; B.qweight = vr.w;
-      B.nfq = h->dim == 2 ? B.n : B.n * B.n;
+      B.nfq = h->dim == 1 ? 1 : (h->dim == 2 ? B.n : B.n * B.n);
       B.affine = 1;
       for (int64_t e = 0; e < b.count && B.affine; ++e)
         if (!isAffine(b.type, nodes, b.vertex + e * typeVertices(b.type), tol)) B.affine = 0;
@@ -903,7 +915,10 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       for (int k = 0; k < nfv; ++k)
         for (int d = 0; d < 3; ++d) q[k][d] = nodes[size_t(vv[fl[s.face * nfv + k]]) * 3 + d];
       double n[3] = {0, 0, 0}, area = 0;
-      if (h->dim == 2) {
+      if (h->dim == 1) {  // Geometry.cpp:102-112: -1 at local face 0, +1 at local face 1; measure 1
+        n[0] = s.face == 0 ? -1.0 : 1.0;
+        area = 1.0;
+      } else if (h->dim == 2) {
         const double tx = 0.5 * (q[1][0] - q[0][0]), ty = 0.5 * (q[1][1] - q[0][1]);
         area = std::sqrt(tx * tx + ty * ty);
         n[0] = ty / area; n[1] = -tx / area;
@@ -923,7 +938,8 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         for (int j = 0; j < fr.n; ++j) {
           double sh[4];
           const double x = fr.x[j * 3], y = fr.x[j * 3 + 1];
-          if (nfv == 2) { sh[0] = 0.5 * (1 - x); sh[1] = 0.5 * (1 + x); }
+          if (nfv == 1) sh[0] = 1.0;
+          else if (nfv == 2) { sh[0] = 0.5 * (1 - x); sh[1] = 0.5 * (1 + x); }
           else { sh[0] = 0.25 * (1 - x) * (1 - y); sh[1] = 0.25 * (1 + x) * (1 - y); sh[2] = 0.25 * (1 + x) * (1 + y); sh[3] = 0.25 * (1 - x) * (1 + y); }
           for (int d = 0; d < 3; ++d) {
             double s = 0; for (int k = 0; k < nfv; ++k) s += sh[k] * q[k][d];
@@ -1186,7 +1202,7 @@ static void modalConvert(sdg_handle* h, std::vector<double>& st, double* modal, 
         for (int b = 0; b < nb; ++b) a[b] = toModal ? u[v * nb + b] : m[b * nv + v];
         const double(*M)[kMaxN] = toModal ? B.ops.phi1inv : B.ops.phi1;
         // apply M along each axis: out[.., i, ..] = sum_k M[i][k] in[.., k, ..]
-        const int strides[3] = {B.dim == 2 ? n : n * n, B.dim == 2 ? 1 : n, 1};
+        const int strides[3] = {B.dim == 1 ? 1 : (B.dim == 2 ? n : n * n), B.dim == 2 ? 1 : n, 1};
         for (int ax = 0; ax < B.dim; ++ax) {
           const int st2 = strides[ax];
           for (int b = 0; b < nb; ++b) {

@@ -123,12 +123,18 @@ struct AvArgs {
   double s0, kappa, factor;
 };
 
+// Points per face of a tensor block: 1 (the point faces of a line), N (quadrangle edges), N^2 (hexahedron faces).
+template <int DIM>
+__host__ __device__ __forceinline__ constexpr int nfqOf(int n1d) {
+  return DIM == 1 ? 1 : (DIM == 2 ? n1d : n1d * n1d);
+}
+
 template <int DIM, int N>
 struct TensorShape {
   static constexpr int NV = DIM + 2;
-  static constexpr int NB = DIM == 2 ? N * N : N * N * N;
-  static constexpr int NF = DIM == 2 ? 4 : 6;
-  static constexpr int NFQ = DIM == 2 ? N : N * N;
+  static constexpr int NB = DIM == 1 ? N : (DIM == 2 ? N * N : N * N * N);
+  static constexpr int NF = 2 * DIM;
+  static constexpr int NFQ = nfqOf<DIM>(N);
   static constexpr int USTRIDE = (NV * NB + 1) & ~1;
   static constexpr int FSTRIDE = NF * NV * NFQ;
   static constexpr int EPB_RAW = 256 / NB > 0 ? 256 / NB : 1;
@@ -150,13 +156,15 @@ constexpr int kMaxTileThreads = 512;
 // Index of node i along axis a.
 template <int DIM, int N>
 __device__ __forceinline__ int axisIndex(int i, int a) {
-  if constexpr (DIM == 2) return a == 0 ? i / N : i % N;
+  if constexpr (DIM == 1) return i;
+  else if constexpr (DIM == 2) return a == 0 ? i / N : i % N;
   else return a == 0 ? i / (N * N) : (a == 1 ? (i / N) % N : i % N);
 }
 
 template <int DIM, int N>
 __device__ __forceinline__ int strideOf(int a) {
-  if constexpr (DIM == 2) return a == 0 ? N : 1;
+  if constexpr (DIM == 1) return 1;
+  else if constexpr (DIM == 2) return a == 0 ? N : 1;
   else return a == 0 ? N * N : (a == 1 ? N : 1);
 }
 
@@ -477,7 +485,9 @@ constexpr int kFaceOps = 8;
 // vertex list; SimulationControl.cpp:381-523 permutations).
 template <int DIM>
 __device__ __forceinline__ int rightPoint(int j, int rot, int n1d) {
-  if constexpr (DIM == 2) {
+  if constexpr (DIM == 1) {
+    return 0;
+  } else if constexpr (DIM == 2) {
     return n1d - 1 - j;
   } else {
     const int i = j / n1d, k = j - i * n1d;
@@ -498,7 +508,7 @@ template <int DIM, int FLUX>
 __device__ __forceinline__ void faceInteriorPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
@@ -532,7 +542,7 @@ template <int DIM>
 __device__ __forceinline__ void faceBoundaryPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);

@@ -680,7 +680,7 @@ struct ForceArgs {
 template <int DIM>
 __global__ void __launch_bounds__(kFaceThreads) surfaceForceKernel(ForceArgs a, Phys ph) {
   constexpr int NV = DIM + 2;
-  const int nfq = DIM == 2 ? a.n1d : a.n1d * a.n1d;
+  const int nfq = nfqOf<DIM>(a.n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
@@ -753,7 +753,7 @@ __global__ void __launch_bounds__(kFaceThreads) surfaceForceTraceCotangentKernel
   constexpr int NV = DIM + 2, NG = NV * DIM;
   using DK = Dual<NV>;
   using DG = Dual<NG>;
-  const int nfq = DIM == 2 ? a.n1d : a.n1d * a.n1d;
+  const int nfq = nfqOf<DIM>(a.n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
@@ -894,7 +894,7 @@ __global__ void __launch_bounds__(kFaceThreads) jvpExchangeBoundaryKernel(AdjArg
   constexpr int NV = DIM + 2;
   using D1 = Dual<1>;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
@@ -922,7 +922,7 @@ __global__ void __launch_bounds__(kFaceThreads) vjpExchangeBoundaryKernel(AdjArg
   constexpr int NV = DIM + 2;
   using DK = Dual<NV>;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
@@ -962,7 +962,7 @@ __global__ void __launch_bounds__(kFaceThreads) jvpBoundaryNSKernel(AdjArgs a, P
   constexpr int NV = DIM + 2;
   using D1 = Dual<1>;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
@@ -997,7 +997,7 @@ __global__ void __launch_bounds__(kFaceThreads) vjpBoundaryNSKernel(AdjArgs a, P
   using DG = Dual<NG>;
   __shared__ double sRed[kFaceThreads / 32];
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   double mupart = 0.0;
@@ -1063,7 +1063,7 @@ __global__ void __launch_bounds__(kFaceThreads) jvpBoundaryKernel(AdjArgs a, Phy
   constexpr int NV = DIM + 2;
   using D1 = Dual<1>;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
@@ -1092,7 +1092,7 @@ __global__ void __launch_bounds__(kFaceThreads) vjpBoundaryKernel(AdjArgs a, Phy
   constexpr int NV = DIM + 2;
   using DK = Dual<NV>;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
@@ -1135,7 +1135,7 @@ __device__ __forceinline__ void jvpFacePoint(const AdjArgs& a, const Phys& ph, i
   constexpr int NV = DIM + 2;
   using D1 = Dual<1>;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
@@ -1452,7 +1452,7 @@ __global__ void __launch_bounds__(kFaceThreads) vjpFaceKernel(AdjArgs a, Phys ph
   using DK = Dual<NV>;
   __shared__ double sRed[kFaceThreads / 32];
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   double mupart = 0.0;
@@ -1734,7 +1734,7 @@ template <int DIM>
 __global__ void __launch_bounds__(kFaceThreads) vjpExchangeKernel(AdjArgs a) {
   constexpr int NV = DIM + 2;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int64_t f = t / nfq;
   if (f >= a.nface) return;

@@ -45,7 +45,7 @@ template <int DIM>
 __device__ __forceinline__ void exchangePoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
@@ -67,7 +67,7 @@ template <int DIM>
 __device__ __forceinline__ void exchangeBoundaryPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
@@ -104,11 +104,12 @@ __device__ __forceinline__ void exchangeBoundaryPoint(const FaceArgs& a, int64_t
   for (int v = 0; v < NV; ++v) a.other[L + v * nfq] = 2.0 * ub[v] - ul[v];
 }
 
-// First-order nodal (vertex) basis of a quadrangle / hexahedron at reference point X (gmsh vertex order:
-// (-1,-1), (1,-1), (1,1), (-1,1), then the same at z = +1), the artificial viscosity's interpolation
-// (BasisFunction.cpp:200-208 nodal_value_).
+// First-order nodal (vertex) basis of a line / quadrangle / hexahedron at reference point X (gmsh vertex
+// order: -1, 1; (-1,-1), (1,-1), (1,1), (-1,1), then the same at z = +1), the artificial viscosity's
+// interpolation (BasisFunction.cpp:200-208 nodal_value_).
 template <int DIM>
 __device__ __forceinline__ double vertexWeight(int v, const double* X) {
+  if constexpr (DIM == 1) return 0.5 * (1.0 + (v == 1 ? 1.0 : -1.0) * X[0]);
   const double sx = (v & 3) == 1 || (v & 3) == 2 ? 1.0 : -1.0;
   const double sy = (v & 3) >= 2 ? 1.0 : -1.0;
   double w = 0.25 * (1.0 + sx * X[0]) * (1.0 + sy * X[1]);
@@ -118,7 +119,7 @@ __device__ __forceinline__ double vertexWeight(int v, const double* X) {
 
 template <int DIM>
 __device__ __forceinline__ double vertexInterp(const double* epsV, const double* X) {
-  constexpr int NVERT = DIM == 2 ? 4 : 8;
+  constexpr int NVERT = 1 << DIM;
   double s = 0.0;
 #pragma unroll
   for (int v = 0; v < NVERT; ++v) s = fma(vertexWeight<DIM>(v, X), epsV[v], s);
@@ -227,7 +228,7 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
       double X[DIM];
 #pragma unroll
       for (int b = 0; b < DIM; ++b) X[b] = a.avTab[ax[b]];
-      epsNode = vertexInterp<DIM>(a.epsV + e * (DIM == 2 ? 4 : 8), X);
+      epsNode = vertexInterp<DIM>(a.epsV + e * (1 << DIM), X);
     }
   }
   if (active) {
@@ -311,7 +312,7 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
         double X[DIM];
 #pragma unroll
         for (int c = 0; c < DIM; ++c) X[c] = c == axis ? (en ? 1.0 : -1.0) : a.avTab[axisIndex<DIM, N>(base, c)];
-        epsF = vertexInterp<DIM>(a.epsV + ee * (DIM == 2 ? 4 : 8), X);
+        epsF = vertexInterp<DIM>(a.epsV + ee * (1 << DIM), X);
       }
     }
     if constexpr (BR2) {
@@ -369,7 +370,7 @@ template <int DIM, int FLUX>
 __device__ __forceinline__ void faceNSPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
@@ -431,7 +432,7 @@ template <int DIM>
 __device__ __forceinline__ void faceNSBoundaryPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
@@ -483,7 +484,7 @@ template <int DIM, int FLUX>
 __device__ __forceinline__ void faceAVPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
@@ -524,7 +525,7 @@ template <int DIM>
 __device__ __forceinline__ void faceAVBoundaryPoint(const FaceArgs& a, int64_t t) {
   constexpr int NV = DIM + 2;
   const int n1d = a.n1d;
-  const int nfq = DIM == 2 ? n1d : n1d * n1d;
+  const int nfq = nfqOf<DIM>(n1d);
   const int64_t f = t / nfq;
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);

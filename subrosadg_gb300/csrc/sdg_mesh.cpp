@@ -16,10 +16,11 @@
 namespace sdg {
 
 const int* faceVertexList(int t) {
+  static const int line[] = {0, 1};
   static const int tri[] = {0, 1, 1, 2, 2, 0};
   static const int quad[] = {0, 1, 1, 2, 2, 3, 3, 0};
   static const int hex[] = {0, 3, 2, 1, 0, 1, 5, 4, 0, 4, 7, 3, 1, 2, 6, 5, 2, 3, 7, 6, 4, 5, 6, 7};
-  return t == SDG_ELEMENT_TRIANGLE ? tri : (t == SDG_ELEMENT_QUADRANGLE ? quad : hex);
+  return t == SDG_ELEMENT_LINE ? line : (t == SDG_ELEMENT_TRIANGLE ? tri : (t == SDG_ELEMENT_QUADRANGLE ? quad : hex));
 }
 
 namespace {
@@ -89,7 +90,7 @@ Adjacency buildAdjacency(const sdg_mesh& mesh, const std::vector<Block>& blocks)
   }
   // Boundary elements keyed the same way.
   std::unordered_map<FaceKey, int64_t, FaceKeyHash> bmap;
-  const int nbv = mesh.dimension == 2 ? 2 : 4;
+  const int nbv = mesh.dimension == 1 ? 1 : (mesh.dimension == 2 ? 2 : 4);
   bmap.reserve(size_t(mesh.boundary_count) + 16);
   for (int64_t i = 0; i < mesh.boundary_count; ++i) {
     FaceKey key;
@@ -103,6 +104,7 @@ Adjacency buildAdjacency(const sdg_mesh& mesh, const std::vector<Block>& blocks)
   }
   Adjacency adj;
   adj.interior.reserve(order.size());
+  std::vector<std::pair<int64_t, FaceSide>> periodicPoints;  // 1D periodic ends without a node map
   for (const FaceKey& key : order) {
     const Visit& vis = faces.at(key);
     if (vis.count == 2) {
@@ -115,10 +117,22 @@ Adjacency buildAdjacency(const sdg_mesh& mesh, const std::vector<Block>& blocks)
       f.physical = mesh.boundary_physical ? mesh.boundary_physical[it->second] : 0;
       if (f.physical < 1 || f.physical > mesh.physical_count) throw std::runtime_error("boundary physical index out of range");
       f.condition = mesh.physical_boundary_condition[f.physical - 1];
+      if (f.condition == SDG_BC_PERIODIC && mesh.dimension == 1 && !mesh.periodic_master) {
+        periodicPoints.push_back({it->second, vis.side});
+        continue;
+      }
       if (f.condition == SDG_BC_PERIODIC) throw std::runtime_error("periodic boundary face without a periodic partner");
       if (f.condition < 0 || f.condition > SDG_BC_PERIODIC) throw std::runtime_error("unknown boundary condition");
       adj.boundary.push_back(f);
     }
+  }
+  if (!periodicPoints.empty()) {
+    // the reference joins the first two point elements: the first one's parent is the left side
+    if (periodicPoints.size() != 2) throw std::runtime_error("a 1D periodic mesh needs exactly two periodic end points");
+    std::sort(periodicPoints.begin(), periodicPoints.end(),
+              [](const auto& a, const auto& b) { return a.first < b.first; });
+    InteriorFace f; f.left = periodicPoints[0].second; f.right = periodicPoints[1].second;
+    adj.interior.push_back(f);
   }
   return adj;
 }
@@ -131,7 +145,7 @@ namespace {
 
 struct MeshStorage {
   std::vector<double> node;
-  std::vector<int32_t> periodic, tri, quad, hex, bnode, bphys, bc;
+  std::vector<int32_t> periodic, line, tri, quad, hex, bnode, bphys, bc;
 };
 
 void publish(MeshStorage* s, int dim, sdg_generated_mesh* out) {
@@ -144,6 +158,7 @@ void publish(MeshStorage* s, int dim, sdg_generated_mesh* out) {
   m.triangle_count = int64_t(s->tri.size() / 3); m.triangle_node = s->tri.empty() ? nullptr : s->tri.data();
   m.quadrangle_count = int64_t(s->quad.size() / 4); m.quadrangle_node = s->quad.empty() ? nullptr : s->quad.data();
   m.hexahedron_count = int64_t(s->hex.size() / 8); m.hexahedron_node = s->hex.empty() ? nullptr : s->hex.data();
+  m.line_count = int64_t(s->line.size() / 2); m.line_node = s->line.empty() ? nullptr : s->line.data();
   m.boundary_count = int64_t(s->bphys.size()); m.boundary_node = s->bnode.empty() ? nullptr : s->bnode.data();
   m.boundary_physical = s->bphys.empty() ? nullptr : s->bphys.data();
   m.physical_count = int32_t(s->bc.size()); m.physical_boundary_condition = s->bc.data();
@@ -228,6 +243,27 @@ int sdg_mesh_generate_2d(double x0, double y0, double lx, double ly, int32_t nx,
   if (periodic) s->bc = {SDG_BC_PERIODIC};
   else s->bc.assign(boundary_condition, boundary_condition + 4);
   publish(s, 2, out);
+  return SDG_OK;
+}
+
+int sdg_mesh_generate_1d(double x0, double lx, int32_t nx, int32_t periodic, const int32_t* boundary_condition,
+                         sdg_generated_mesh* out) {
+  if (!out || nx < 1 || !(lx > 0) || (!periodic && !boundary_condition)) return SDG_ERR_INVALID_ARGUMENT;
+  if (periodic && nx < 3) return SDG_ERR_INVALID_ARGUMENT;  // the two ends of one element would coincide
+  auto* s = new MeshStorage();
+  s->node.resize(size_t(nx + 1) * 3, 0.0);
+  for (int i = 0; i <= nx; ++i) s->node[size_t(i) * 3] = x0 + lx * double(i) / nx;
+  for (int i = 0; i < nx; ++i) s->line.insert(s->line.end(), {i, i + 1});
+  if (periodic) {
+    s->periodic.resize(size_t(nx + 1));
+    for (int i = 0; i <= nx; ++i) s->periodic[size_t(i)] = i == nx ? 0 : i;
+  }
+  // boundary points: the x0 end (group 1) and the x0 + lx end (group 2), or one periodic group
+  s->bnode = {0, nx};
+  s->bphys = {1, periodic ? 1 : 2};
+  if (periodic) s->bc = {SDG_BC_PERIODIC};
+  else s->bc.assign(boundary_condition, boundary_condition + 2);
+  publish(s, 1, out);
   return SDG_OK;
 }
 
@@ -386,7 +422,7 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
         }
       }
     }
-    if (maxDim < 2) throw std::runtime_error("no 2D/3D elements in the mesh");
+    if (maxDim < 1) throw std::runtime_error("no line, surface or volume elements in the mesh");
     const auto idx = [&](int64_t tag) {
       const auto it = nodeIndex.find(tag);
       if (it == nodeIndex.end()) throw std::runtime_error("element references an unknown node");
@@ -395,7 +431,7 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
     for (const RawEl& r : raw) {
       int dim = 0, nn = 0, nprim = 0; typeInfo(r.type, dim, nn, nprim);
       if (dim == maxDim) {
-        std::vector<int32_t>* dst = nprim == 3 ? &s->tri : (nprim == 4 ? &s->quad : &s->hex);
+        std::vector<int32_t>* dst = maxDim == 1 ? &s->line : (nprim == 3 ? &s->tri : (nprim == 4 ? &s->quad : &s->hex));
         if (maxDim == 3 && nprim != 8) throw std::runtime_error("only hexahedra are supported in 3D");
         for (int64_t v : r.v) dst->push_back(idx(v));
       } else if (dim == maxDim - 1) {

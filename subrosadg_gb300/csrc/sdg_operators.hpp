@@ -141,18 +141,19 @@ inline Dual2 dkernel(int k, Dual2 t) {
 }
 
 inline int modalCount(int type, int p) {
+  if (type == SDG_ELEMENT_LINE) return p + 1;
   if (type == SDG_ELEMENT_TRIANGLE) return (p + 1) * (p + 2) / 2;
   if (type == SDG_ELEMENT_QUADRANGLE) return (p + 1) * (p + 1);
   return (p + 1) * (p + 1) * (p + 1);
 }
 
 // Modal basis values and reference gradients at (xi, eta[, zeta]).
-//   quadrangle: index a*(P+1)+b -> l_a(xi) l_b(eta); hexahedron: (a*(P+1)+b)*(P+1)+c.
+//   line: index a -> l_a(xi); quadrangle: index a*(P+1)+b -> l_a(xi) l_b(eta); hexahedron: (a*(P+1)+b)*(P+1)+c.
 //   triangle  : lambda_0..2; edge functions lambda_a lambda_b phi_{k-2}(lambda_b - lambda_a) on edges
 //               (0,1),(1,2),(2,0), k = 2..P; bubbles lambda_0 lambda_1 lambda_2 P_i(l2-l1) P_j(l1-l0), i+j <= P-3.
 inline void modalBasis(int type, int p, const double* X, double* val, double* grad /* [nb][3] */) {
   if (type != SDG_ELEMENT_TRIANGLE) {
-    const int m = p + 1, dim = type == SDG_ELEMENT_HEXAHEDRON ? 3 : 2;
+    const int m = p + 1, dim = type == SDG_ELEMENT_HEXAHEDRON ? 3 : (type == SDG_ELEMENT_LINE ? 1 : 2);
     double lv[3][kMaxN], ld[3][kMaxN];
     for (int d = 0; d < dim; ++d)
       for (int k = 0; k < m; ++k) {
@@ -162,7 +163,9 @@ inline void modalBasis(int type, int p, const double* X, double* val, double* gr
         else { double pk1, dd; legendreP(k - 1, X[d], &pk1, &dd); ld[d][k] = std::sqrt((2.0 * k - 1.0) / 2.0) * pk1; }
       }
     int idx = 0;
-    if (dim == 2) {
+    if (dim == 1) {
+      for (int a = 0; a < m; ++a, ++idx) { val[idx] = lv[0][a]; grad[idx * 3] = ld[0][a]; grad[idx * 3 + 1] = grad[idx * 3 + 2] = 0; }
+    } else if (dim == 2) {
       for (int a = 0; a < m; ++a)
         for (int b = 0; b < m; ++b, ++idx) {
           val[idx] = lv[0][a] * lv[1][b];
@@ -224,7 +227,9 @@ inline PointRule volumeRule(int type, int p) {
   const int n = p + 1;
   double g[kMaxN], gw[kMaxN];
   gaussRule(n, g, gw);
-  if (type == SDG_ELEMENT_QUADRANGLE) {
+  if (type == SDG_ELEMENT_LINE) {  // kLineQuadratureNumber[2P] = P + 1 Gauss points
+    for (int i = 0; i < n; ++i) { r.x.insert(r.x.end(), {g[i], 0.0, 0.0}); r.w.push_back(gw[i]); }
+  } else if (type == SDG_ELEMENT_QUADRANGLE) {
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j) { r.x.insert(r.x.end(), {g[i], g[j], 0.0}); r.w.push_back(gw[i] * gw[j]); }
   } else {
@@ -236,9 +241,11 @@ inline PointRule volumeRule(int type, int p) {
   return r;
 }
 
-// Face rule of order 2P+1 in face coordinates: P+1 Gauss points per face direction.
+// Face rule of order 2P+1 in face coordinates: P+1 Gauss points per face direction (the point faces of a
+// line: one point of weight 1).
 inline PointRule faceRule(int type, int p) {
   PointRule r;
+  if (type == SDG_ELEMENT_LINE) { r.n = 1; r.x = {0.0, 0.0, 0.0}; r.w = {1.0}; return r; }
   const int n = p + 1;
   double g[kMaxN], gw[kMaxN];
   gaussRule(n, g, gw);
@@ -253,11 +260,13 @@ inline PointRule faceRule(int type, int p) {
 }
 
 inline void referenceVertex(int type, int v, double* X) {
+  static const double line[2][3] = {{-1, 0, 0}, {1, 0, 0}};
   static const double tri[3][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}};
   static const double quad[4][3] = {{-1, -1, 0}, {1, -1, 0}, {1, 1, 0}, {-1, 1, 0}};
   static const double hex[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
                                    {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
-  const double* s = type == SDG_ELEMENT_TRIANGLE ? tri[v] : (type == SDG_ELEMENT_QUADRANGLE ? quad[v] : hex[v]);
+  const double* s = type == SDG_ELEMENT_LINE ? line[v]
+                    : (type == SDG_ELEMENT_TRIANGLE ? tri[v] : (type == SDG_ELEMENT_QUADRANGLE ? quad[v] : hex[v]));
   X[0] = s[0]; X[1] = s[1]; X[2] = s[2];
 }
 

@@ -58,7 +58,7 @@ const Zstd& zstd() {
 // Phi1^-1 along each axis of every (element, component) vector of nb values.
 void nodalToModal(const DevBlock& B, double* v /* [nb] */, std::vector<double>& t) {
   const int n = B.n, nb = B.nb;
-  const int strides[3] = {B.dim == 2 ? n : n * n, B.dim == 2 ? 1 : n, 1};
+  const int strides[3] = {B.dim == 1 ? 1 : (B.dim == 2 ? n : n * n), B.dim == 2 ? 1 : n, 1};
   t.assign(nb, 0.0);
   for (int ax = 0; ax < B.dim; ++ax) {
     const int st = strides[ax];

@@ -65,6 +65,7 @@ KernelVariant faceDimOf(int op, int flux) {
 }  // namespace
 
 KernelVariant facePointVariant(int op, int dim, int flux) {
+  if (dim == 1) return faceDimOf<1>(op, flux);
   if (dim == 2) return faceDimOf<2>(op, flux);
   if (dim == 3) return faceDimOf<3>(op, flux);
   return KernelVariant();

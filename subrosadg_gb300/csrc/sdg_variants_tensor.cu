@@ -1,4 +1,4 @@
-// Tensor-block (quadrangles P>=2, hexahedra) stage and gradient kernels: the one translation unit that
+// Tensor-block (lines, quadrangles P>=2, hexahedra) stage and gradient kernels: the one translation unit that
 // instantiates them, and their registry entries.
 #include "sdg_kernels_ns.cuh"
 #include "sdg_variants.hpp"
@@ -28,7 +28,8 @@ KernelVariant gradOf() {
 }
 }  // namespace
 
-#define SDG_TENSOR_ORDERS(X) X(2, 3) X(2, 4) X(2, 5) X(2, 6) X(3, 2) X(3, 3) X(3, 4) X(3, 5) X(3, 6)
+#define SDG_TENSOR_ORDERS(X) \
+  X(1, 2) X(1, 3) X(1, 4) X(1, 5) X(1, 6) X(2, 3) X(2, 4) X(2, 5) X(2, 6) X(3, 2) X(3, 3) X(3, 4) X(3, 5) X(3, 6)
 
 KernelVariant tensorStageVariant(int dim, int n, bool affine, int visc) {
 #define SDG_TS(D, NN)                                                                                        \

@@ -31,13 +31,14 @@ class Mesh:
     """First-order mesh in gmsh vertex order (the input format of sdg_create)."""
 
     def __init__(self, dimension, nodes, triangles=None, quadrangles=None, hexahedra=None, boundary=None,
-                 boundary_physical=None, physical_conditions=None, periodic_master=None):
+                 boundary_physical=None, physical_conditions=None, periodic_master=None, lines=None):
         self.dimension = int(dimension)
         self.nodes = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
+        self.lines = None if lines is None or len(lines) == 0 else np.ascontiguousarray(lines, np.int32).reshape(-1, 2)
         self.triangles = None if triangles is None or len(triangles) == 0 else np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
         self.quadrangles = None if quadrangles is None or len(quadrangles) == 0 else np.ascontiguousarray(quadrangles, np.int32).reshape(-1, 4)
         self.hexahedra = None if hexahedra is None or len(hexahedra) == 0 else np.ascontiguousarray(hexahedra, np.int32).reshape(-1, 8)
-        nbv = 2 if self.dimension == 2 else 4
+        nbv = {1: 1, 2: 2}.get(self.dimension, 4)
         self.boundary = np.zeros((0, nbv), np.int32) if boundary is None else np.ascontiguousarray(boundary, np.int32).reshape(-1, nbv)
         self.boundary_physical = np.zeros(0, np.int32) if boundary_physical is None else np.ascontiguousarray(boundary_physical, np.int32)
         self.physical_conditions = np.zeros(0, np.int32) if physical_conditions is None else np.ascontiguousarray(physical_conditions, np.int32)
@@ -50,7 +51,7 @@ class Mesh:
             if not p or n == 0:
                 return None
             return np.ctypeslib.as_array(p, shape=(n * w,)).astype(dt).copy()
-        nbv = 2 if m.dimension == 2 else 4
+        nbv = {1: 1, 2: 2}.get(m.dimension, 4)
         out = cls(m.dimension, arr(m.node_coordinate, m.node_count, 3, np.float64),
                   arr(m.triangle_node, m.triangle_count, 3, np.int32),
                   arr(m.quadrangle_node, m.quadrangle_count, 4, np.int32),
@@ -58,9 +59,19 @@ class Mesh:
                   arr(m.boundary_node, m.boundary_count, nbv, np.int32),
                   arr(m.boundary_physical, m.boundary_count, 1, np.int32),
                   arr(m.physical_boundary_condition, m.physical_count, 1, np.int32),
-                  arr(m.periodic_master, m.node_count, 1, np.int32))
+                  arr(m.periodic_master, m.node_count, 1, np.int32),
+                  arr(m.line_node, m.line_count, 2, np.int32))
         _abi.load().sdg_mesh_free(byref(g))
         return out
+
+    @classmethod
+    def line_1d(cls, x0, lx, nx, periodic=True, boundary_conditions=None):
+        """[x0, x0 + lx] in nx lines: periodic (one group) or groups 1 (x0 end) and 2 (x0 + lx end)."""
+        lib = _abi.load()
+        g = SdgGeneratedMesh()
+        bc = None if boundary_conditions is None else np.ascontiguousarray(boundary_conditions, np.int32)
+        check(lib.sdg_mesh_generate_1d(x0, lx, nx, int(periodic), _ptr(bc, _pi), byref(g)))
+        return cls._from_generated(g)
 
     @classmethod
     def box_2d(cls, x0, y0, lx, ly, nx, ny, periodic=True, jitter=0.0, split_fraction=0.0, seed=0,
@@ -110,6 +121,8 @@ class Mesh:
         m.boundary_physical = _ptr(self.boundary_physical, _pi)
         m.physical_count = len(self.physical_conditions)
         m.physical_boundary_condition = _ptr(self.physical_conditions, _pi)
+        m.line_count = 0 if self.lines is None else self.lines.shape[0]
+        m.line_node = _ptr(self.lines, _pi)
         return m
 
 

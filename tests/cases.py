@@ -130,6 +130,82 @@ def channel_case(p=2, flux=sdg.HLLC, conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.PR
     return (mesh, cfg, ic, bc, dt, steps)
 
 
+# ---- 1D (DimensionEnum::D1, line meshes): the reference's 1D drivers ------------------------------------------
+
+def density_wave_1d_case(n=40, p=3, flux=sdg.HLLC, dt=1e-4, steps=5, viscous=None, mu=0.0):
+    """Periodic density wave on [0, 2] (examples/periodic_1d_ceuler.cpp:31-38, 63-77): rho = 1 + 0.2 sin(pi x),
+    u = 1, T = 1.4 / rho (p = 1); Navier-Stokes with `viscous`."""
+    mesh = sdg.Mesh.line_1d(0.0, 2.0, n, periodic=True)
+    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
+
+    def ic(pts):
+        rho = 1.0 + 0.2 * np.sin(math.pi * pts[:, 0])
+        return np.stack([rho, np.ones_like(rho), 1.4 / rho], 1)
+
+    return (mesh, cfg, ic, None, dt, steps)
+
+
+def sod_1d_case(n=100, p=3, flux=sdg.HLLC, tolerance=0.5, factor=1.0, dt=2e-6, steps=4,
+                conditions=(sdg.RIEMANN_FARFIELD, sdg.RIEMANN_FARFIELD), av=True, smooth=0.0):
+    """Sod's tube with a left stream on [0, 1] (examples/sod_1d_ceuler.cpp:28-50, 56-82): (rho, u, T) =
+    (1, 0.75, 1.4) | (0.125, 0, 1.12) at x = 0.5, farfield ends holding the two states, artificial viscosity.
+    With the driver's 100 elements the jump lies on an element boundary, where the sensor sees constant
+    elements (no artificial viscosity until the jump has spread into them).  Inside an element a sharp jump's
+    interpolant overshoots to negative end-point traces at P >= 2 (the reference's own projection does the
+    same); `smooth` > 0 spreads it as a tanh of that width instead."""
+    mesh = sdg.Mesh.line_1d(0.0, 1.0, n, periodic=False, boundary_conditions=list(conditions))
+    left, right = np.array([1.0, 0.75, 1.4]), np.array([0.125, 0.0, 0.8 * 1.4])
+
+    def ic(pts):
+        if smooth > 0:
+            t = 0.5 * (1.0 + np.tanh((pts[:, 0] - 0.5) / smooth))[:, None]
+            return left * (1.0 - t) + right * t
+        return np.where((pts[:, 0] <= 0.5)[:, None], left, right)
+
+    def bc(pts, phys):
+        return np.where((phys == 1)[:, None], left, right)
+
+    case = (mesh, config(p, flux), ic, bc, dt, steps)
+    return with_av(case, tolerance, factor) if av else case
+
+
+def shu_osher_1d_case(n=100, p=3, flux=sdg.HLLC, tolerance=3.0, factor=1.0, dt=2e-5, steps=4, smooth=0.0):
+    """Shu-Osher shock / entropy-wave interaction on [-5, 5] (examples/shuosher_1d_ceuler.cpp:28-52, 58-84):
+    (3.857143, 2.629369, 3.750342) for x <= -4, else rho = 1 + 0.2 sin 5x, u = 0, T = 1.4 / rho."""
+    mesh = sdg.Mesh.line_1d(-5.0, 10.0, n, periodic=False, boundary_conditions=[sdg.RIEMANN_FARFIELD] * 2)
+    post = np.array([3.857143, 2.629369, 3.750342])
+    far = np.array([1.0 + 0.2 * math.sin(25.0), 0.0, 1.4 / (1.0 + 0.2 * math.sin(25.0))])
+
+    def ic(pts):
+        x = pts[:, 0]
+        rho = 1.0 + 0.2 * np.sin(5.0 * x)
+        wave = np.stack([rho, np.zeros_like(x), 1.4 / rho], 1)
+        if smooth > 0:
+            t = 0.5 * (1.0 + np.tanh((x + 4.0) / smooth))[:, None]
+            return post * (1.0 - t) + wave * t
+        return np.where((x <= -4.0)[:, None], post, wave)
+
+    def bc(pts, phys):
+        return np.where((phys == 1)[:, None], post, far)
+
+    return with_av((mesh, config(p, flux), ic, bc, dt, steps), tolerance, factor)
+
+
+def inc_wave_1d_case(n=20, p=3, flux=sdg.EXACT, viscous=None, mu=0.0, c0=3.0, dt=1e-4, steps=4):
+    """Weakly compressible acoustic / entropy wave on the periodic segment [0, 1].  The momentum residual
+    c0^2 d(rho)/dx moves by ~ulp(rho) (P+1)^2 / h relative to c0^2 drho k under one ulp of rounding of the state:
+    a 2 % density wave keeps that FP64 floor near 1e-13 (a 0.2 % wave puts it at ~1e-12)."""
+    mesh = sdg.Mesh.line_1d(0.0, 1.0, n, periodic=True)
+    cfg = inc_config(p, flux, viscous, mu, c0)
+
+    def ic(pts):
+        x = pts[:, 0]
+        return np.stack([1.0 + 0.02 * np.sin(2 * math.pi * x), 0.3 + 0.05 * np.cos(2 * math.pi * x),
+                         1.0 + 0.1 * np.sin(4 * math.pi * x)], 1)
+
+    return (mesh, cfg, ic, None, dt, steps)
+
+
 # ---- incompressible model (weakly compressible EOS p = c0^2 (rho - rho0) + 0.01 rho0 c0^2, cp = cv = 1) ----------
 # Workload shapes follow the reference's incompressible example drivers (examples/taylorvortex_2d_incns.cpp,
 # lidcavity_2d_incns.cpp, thermalcavity_2d_incns.cpp, shearlayer_2d_inceuler.cpp): rho0 = 1, cp = cv = 1,
@@ -357,4 +433,6 @@ def golden_cases():
         "inc_thermalcavity2d_p2_exact_br2_boussinesq": lambda: cavity_case(p=2, flux=sdg.EXACT, mu=1e-2,
                                                                           boussinesq=True, c0=3.0, n=4, steps=2),
         "av_shocktube2d_hybrid_p3_hllc": lambda: shock_tube_case(p=3, n=8, split=0.5, steps=2),
+        "wave1d_line_p3_hllc": lambda: density_wave_1d_case(n=10, p=3, steps=3),
+        "av_sod1d_line_p3_hllc": lambda: sod_1d_case(n=19, p=3, steps=3),
     }

@@ -5,6 +5,7 @@ reference tree at /root/reference):
   * face quadrature permutations by rotation   src/Solver/SimulationControl.cpp:381-523
   * quadrature point counts by order           src/Solver/SimulationControl.cpp:268-273
   * face vertex lists                          src/Solver/SimulationControl.cpp:170-216
+  * point-face normals of lines                src/Mesh/Geometry.cpp:102-112
   * SSP-RK / Heun / Euler coefficient tables   src/Solver/TimeIntegration.cpp:45-65
   * gamma, Prandtl, Sutherland constants       src/Solver/PhysicalModel.cpp:45,91,109
 Part 2 -- oracle reference vectors on small seeded meshes (the oracle is the CPU restatement
@@ -67,10 +68,15 @@ def reference_tables(ref):
     out["quadrature_count"] = counts
     body = _func_body(sc, "getElementPerAdjacencyNodeIndex()")
     faces = {}
-    for name in ("Triangle", "Quadrangle", "Hexahedron"):
+    for name in ("Line", "Triangle", "Quadrangle", "Hexahedron"):
         m = re.search(r"ElementType == ElementEnum::%s\) \{\s*return \{([^}]*)\};" % name, body, re.S)
         faces[name] = [int(x) for x in m.group(1).replace("\n", " ").split(",")]
     out["face_vertices"] = faces
+    # outward normals of a line's point faces by their sequence in the parent (Geometry.cpp:102-112)
+    geo = open(os.path.join(ref, "src/Mesh/Geometry.cpp")).read()
+    body = _func_body(geo, "calculateNormalVector(const Isize adjacency_sequence_in_parent")
+    out["point_normals"] = {int(m.group(1)): float(m.group(2)) for m in re.finditer(
+        r"adjacency_sequence_in_parent == (\d)\) \{\s*normal_vector\(0, 0\) = ([-0-9.]+)_r;", body)}
     ti = open(os.path.join(ref, "src/Solver/TimeIntegration.cpp")).read()
     rk = {}
     for name in ("ForwardEuler", "HeunRK2", "SSPRK3"):

@@ -58,6 +58,8 @@ def test_host_only_handle_refuses_state_calls():
     ("hybrid-jitter", lambda: sdg.Mesh.box_2d(0, 0, 1, 1, 9, 7, jitter=0.1, split_fraction=0.5, seed=9)),
     ("walls", lambda: sdg.Mesh.box_2d(0, 0, 2, 1, 6, 3, periodic=False, boundary_conditions=[4, 2, 4, 1])),
     ("walls-hex", lambda: sdg.Mesh.box_3d(0, 0, 0, 1, 1, 1, 2, 3, 2, periodic=False, boundary_conditions=[0, 1, 2, 3, 4, 5])),
+    ("periodic-line", lambda: sdg.Mesh.line_1d(0, 2, 7)),
+    ("farfield-line", lambda: sdg.Mesh.line_1d(-5, 10, 9, periodic=False, boundary_conditions=[0, 0])),
 ])
 def test_adjacency_bit_exact_with_oracle(name, mesh_fn):
     mesh = mesh_fn()
@@ -74,7 +76,8 @@ def test_adjacency_bit_exact_with_oracle(name, mesh_fn):
         sides.add((r[0], r[1], r[2])); sides.add((r[3], r[4], r[5]))
     for r in b1:
         sides.add((r[0], r[1], r[2]))
-    nfaces = sum(n * k for n, k in ((0 if mesh.triangles is None else len(mesh.triangles), 3),
+    nfaces = sum(n * k for n, k in ((0 if mesh.lines is None else len(mesh.lines), 2),
+                                    (0 if mesh.triangles is None else len(mesh.triangles), 3),
                                     (0 if mesh.quadrangles is None else len(mesh.quadrangles), 4),
                                     (0 if mesh.hexahedra is None else len(mesh.hexahedra), 6)))
     assert len(sides) == nfaces
@@ -156,3 +159,55 @@ def test_msh_reader_roundtrip(tmp_path):
     s = sdg.GpuSolver(m, cases.config(2, sdg.HLLC), device=-1)
     a, b = s.adjacency()
     assert len(a) == 4 and len(b) == 8
+
+
+def _msh_1d(tmp_path, n, groups):
+    """MSH 4.1 file of [0, 1] in n lines (the 1D example drivers' transfinite curve); groups: the physical tag of
+    each end point (equal tags: one group holding both)."""
+    nodes = [i / n for i in range(n + 1)]
+    txt = ["$MeshFormat", "4.1 0 8", "$EndMeshFormat", "$Entities", "2 1 0 0",
+           f"1 0 0 0 1 {groups[0]}", f"2 1 0 0 1 {groups[1]}", "1 0 0 0 1 0 0 1 9 2 1 -2", "$EndEntities",
+           "$Nodes", f"3 {n + 1} 1 {n + 1}", "0 1 0 1", "1", "0 0 0", "0 2 0 1", "2", "1 0 0",
+           f"1 1 0 {n - 1}"]
+    txt += [str(k + 3) for k in range(n - 1)]
+    txt += [f"{x} 0 0" for x in nodes[1:-1]]
+    txt += ["$EndNodes", "$Elements", f"3 {n + 2} 1 {n + 2}", "0 1 15 1", "1 1", "0 2 15 1", "2 2", f"1 1 1 {n}"]
+    order = [1] + [k + 3 for k in range(n - 1)] + [2]
+    for i in range(n):
+        txt.append(f"{i + 3} {order[i]} {order[i + 1]}")
+    txt += ["$EndElements"]
+    path = tmp_path / "line.msh"
+    path.write_text("\n".join(txt) + "\n")
+    return sdg.Mesh.read_msh(path)
+
+
+def test_msh_reader_1d_farfield_and_periodic(tmp_path):
+    """1D meshes as the reference's 1D drivers write them: point physical groups; two farfield groups
+    (sod_1d_ceuler.cpp:75-77), or one periodic group holding both end points (periodic_1d_ceuler.cpp:70),
+    whose two points the reference joins into one interior face (Adjacency.cpp:185-211)."""
+    m = _msh_1d(tmp_path, 6, (1, 2))
+    assert m.dimension == 1 and len(m.lines) == 6 and len(m.boundary) == 2 and len(m.physical_conditions) == 2
+    m.set_boundary_condition(1, sdg.RIEMANN_FARFIELD)
+    m.set_boundary_condition(2, sdg.RIEMANN_FARFIELD)
+    s = sdg.GpuSolver(m, cases.config(3, sdg.HLLC), device=-1)
+    a, b = s.adjacency()
+    assert len(a) == 5 and len(b) == 2
+    assert b[:, 2].tolist() == [0, 1] and b[:, 3].tolist() == [1, 2]
+    o = Oracle(m, cases.config(3, sdg.HLLC), faithful=False)
+    a2, b2 = o.adjacency()
+    assert np.array_equal(a, a2) and np.array_equal(b, b2)
+    p = _msh_1d(tmp_path, 6, (1, 1))
+    assert len(p.physical_conditions) == 1
+    p.set_boundary_condition(1, sdg.PERIODIC)
+    s = sdg.GpuSolver(p, cases.config(3, sdg.HLLC), device=-1)
+    a, b = s.adjacency()
+    assert len(a) == 6 and len(b) == 0
+    # the joined face (type, element, face of each side, rotation): the first point element's parent (element 0,
+    # its local face 0) on the left
+    assert [sdg.LINE, 0, 0, sdg.LINE, 5, 1, 0] in a.tolist()
+    o = Oracle(p, cases.config(3, sdg.HLLC), faithful=False)
+    a2, b2 = o.adjacency()
+    assert np.array_equal(a, a2)
+    # the generated periodic line (a periodic node map) gives the same faces
+    g = sdg.GpuSolver(sdg.Mesh.line_1d(0, 1, 6), cases.config(3, sdg.HLLC), device=-1)
+    assert np.array_equal(g.adjacency()[0], a)

@@ -144,7 +144,41 @@ CASES = {
     "av-kh-hybrid-p4-lf": lambda: cases.with_av(cases.kh_case(n=6, p=4, steps=3), tolerance=1.0),
     "av-kh-jitter-quad-p5-hllc": lambda: cases.with_av(cases.kh_case(n=4, p=5, flux=sdg.HLLC, split=0.0, steps=2),
                                                        tolerance=2.0, factor=0.5),
+    # 1D (line meshes, point faces): the periodic density wave, Sod and Shu-Osher with artificial viscosity,
+    # Navier-Stokes and the incompressible model
+    "line-wave-p1-roe": lambda: cases.density_wave_1d_case(p=1, flux=sdg.ROE),
+    "line-wave-p2-lf": lambda: cases.density_wave_1d_case(p=2, flux=sdg.LAX_FRIEDRICHS),
+    "line-wave-p3-hllc": lambda: cases.density_wave_1d_case(p=3),
+    "line-wave-p4-central": lambda: cases.density_wave_1d_case(n=20, p=4, flux=sdg.CENTRAL),
+    "line-wave-p5-roe": lambda: cases.density_wave_1d_case(n=20, p=5, flux=sdg.ROE, dt=5e-5),
+    "line-sod-walls-p3-roe": lambda: cases.sod_1d_case(n=40, p=3, flux=sdg.ROE, av=False, dt=1e-5,
+                                                       conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.ADIABATIC_SLIP_WALL)),
+    "line-sod-inflow-outflow-p2-hllc": lambda: cases.sod_1d_case(n=40, p=2, av=False, dt=1e-5,
+                                                                 conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW)),
+    "ns-line-wave-p3-br1-hllc": lambda: cases.density_wave_1d_case(n=20, p=3, viscous=sdg.BR1, mu=0.01),
+    "ns-line-wave-p4-br2-roe": lambda: cases.density_wave_1d_case(n=20, p=4, flux=sdg.ROE, viscous=sdg.BR2, mu=0.01,
+                                                                  dt=5e-5),
+    "ns-line-sod-walls-p2-br2-lf": lambda: _ns(cases.sod_1d_case(
+        n=40, p=2, flux=sdg.LAX_FRIEDRICHS, av=False, dt=1e-5,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_NONSLIP_WALL)), sdg.BR2, 0.01),
+    # (odd element counts put the jumps inside elements, where the sensor sees them)
+    "av-sod-line-p3-hllc": lambda: cases.sod_1d_case(n=99, p=3),
+    "av-sod-line-p4-roe": lambda: cases.sod_1d_case(n=99, p=4, flux=sdg.ROE),
+    "av-sod-line-p1-lf": lambda: cases.sod_1d_case(n=99, p=1, flux=sdg.LAX_FRIEDRICHS),
+    "av-shuosher-line-p3-hllc": lambda: cases.shu_osher_1d_case(n=99, smooth=0.04, dt=5e-6),
+    "av-shuosher-line-p5-roe": lambda: cases.shu_osher_1d_case(n=99, p=5, flux=sdg.ROE, smooth=0.04, dt=5e-6),
+    "av-shuosher-line-p2-lf": lambda: cases.shu_osher_1d_case(n=99, p=2, flux=sdg.LAX_FRIEDRICHS, smooth=0.04,
+                                                              dt=5e-6),
+    "inc-line-wave-p3-exact": lambda: cases.inc_wave_1d_case(),
+    "inc-ns-line-wave-p4-lf-br2": lambda: cases.inc_wave_1d_case(p=4, flux=sdg.LAX_FRIEDRICHS, viscous=sdg.BR2, mu=0.01,
+                                                                 dt=5e-5),
 }
+
+
+def _ns(case, viscous, mu):
+    """The same case as Navier-Stokes with `viscous` and viscosity mu."""
+    mesh, cfg, ic, bc, dt, steps = case
+    return (mesh, cases.ns_config(cfg.polynomial_order, cfg.convective_flux, viscous, mu), ic, bc, dt, steps)
 
 
 def reference_arithmetic_residual(case):
@@ -230,8 +264,10 @@ def test_nan_state_is_reported_by_relative_error():
     assert np.isnan(err).all()
 
 
-def test_modal_state_roundtrip_and_layout():
-    g, o, dt, _ = pair(cases.vortex_case(n=4, p=3))
+@pytest.mark.parametrize("case", [lambda: cases.vortex_case(n=4, p=3), lambda: cases.density_wave_1d_case(n=6, p=4)],
+                         ids=["quad-p3", "line-p4"])
+def test_modal_state_roundtrip_and_layout(case):
+    g, o, dt, _ = pair(case())
     m = g.state_modal()
     mo = o.state_modal()
     # same modal basis and layout as the oracle (reference layout: column-major (d+2) x Nb per element)

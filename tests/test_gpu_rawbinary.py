@@ -60,6 +60,8 @@ def make(case):
     ("ns-channel-walls-p2-br2", lambda: cases.channel_case(p=2, n=3, viscous=sdg.BR2, mu=0.01,
                                                            conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW,
                                                                        sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW))),
+    ("euler-line-p3-farfield", lambda: cases.sod_1d_case(n=9, p=3, av=False)),
+    ("ns-line-p2-br1", lambda: cases.density_wave_1d_case(n=8, p=2, viscous=sdg.BR1, mu=0.01)),
 ])
 def test_raw_binary_layout(tmp_path, name, case):
     s, dt, mesh = make(case())
