@@ -374,7 +374,7 @@ const char* sdg_batch_last_error(const sdg_batch* batch);
  * Exact derivatives of the discrete scheme the forward path runs (the reference has none): for the
  * residual R(U) = du/dt and for whole SSP-RK trajectories, with respect to the state and to the dynamic
  * viscosity mu.  All vectors are in the volume-point layout of sdg_set_state_point ([point][d+2],
- * conserved variables).  Supported: affine tensor blocks (quadrangles P>=2 with parallelogram sides,
+ * conserved variables).  Supported: affine tensor blocks (lines, quadrangles P>=2 with parallelogram sides,
  * hexahedra), any boundary faces, compressible or incompressible Euler or Navier-Stokes (BR1, BR2), the
  * Boussinesq source; else (dense blocks, artificial viscosity) SDG_ERR_UNSUPPORTED. */
 /* w_q |J|_q of every volume point: integral of f = sum over points of weight * f (functionals). */

@@ -118,7 +118,7 @@ AdjointState* adjoint(sdg_handle* h) {
   if (h->adj) return h->adj;
   for (const DevBlock& B : h->blocks)
     if (B.kind != kTensor || !B.affine)
-      throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (quadrangles P>=2, hexahedra)");
+      throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (lines, quadrangles P>=2, hexahedra)");
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   const bool gen = h->ph.incomp || h->ph.source;
@@ -746,7 +746,8 @@ int sdg_surface_force(sdg_handle* h, int32_t physical, double* force) {
     const ForceArgs a = forceInputs(h, physical, in, true);
     const int64_t pts = h->nBoundary * h->nfq;
     const unsigned grid = unsigned((pts + kFaceThreads - 1) / kFaceThreads);
-    if (h->dim == 2) surfaceForceKernel<2><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
+    if (h->dim == 1) surfaceForceKernel<1><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
+    else if (h->dim == 2) surfaceForceKernel<2><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
     else surfaceForceKernel<3><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph);
     SDG_CUDA(cudaGetLastError());
     h->launches++;
@@ -783,7 +784,8 @@ int sdg_surface_force_cotangent(sdg_handle* h, int32_t physical, const double* d
     clearGhost(h);
     const int64_t pts = h->nBoundary * h->nfq;
     const unsigned grid = unsigned((pts + kFaceThreads - 1) / kFaceThreads);
-    if (h->dim == 2) surfaceForceTraceCotangentKernel<2><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph, A->lamTg);
+    if (h->dim == 1) surfaceForceTraceCotangentKernel<1><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph, A->lamTg);
+    else if (h->dim == 2) surfaceForceTraceCotangentKernel<2><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph, A->lamTg);
     else surfaceForceTraceCotangentKernel<3><<<grid, kFaceThreads, 0, h->stream>>>(a, h->ph, A->lamTg);
     SDG_CUDA(cudaGetLastError());
     h->launches++;

@@ -26,21 +26,30 @@ void fluxOf(int flux, AdjointKernels& k, bool gen) {
 }
 }  // namespace
 
-void adjointFaceKernels(int dim, int flux, bool visc, bool gen, AdjointKernels& k) {
-  if (dim == 2) { if (visc) fluxOf<2, true>(flux, k, gen); else fluxOf<2, false>(flux, k, gen); }
-  else if (dim == 3) { if (visc) fluxOf<3, true>(flux, k, gen); else fluxOf<3, false>(flux, k, gen); }
-  const auto pick = [dim](const void* two, const void* three) { return dim == 2 ? two : three; };
+namespace {
+template <int DIM>
+void boundaryOf(bool visc, AdjointKernels& k) {
   if (!visc) {
-    k.jvpBoundary = pick(reinterpret_cast<const void*>(&jvpBoundaryKernel<2>), reinterpret_cast<const void*>(&jvpBoundaryKernel<3>));
-    k.vjpBoundary = pick(reinterpret_cast<const void*>(&vjpBoundaryKernel<2>), reinterpret_cast<const void*>(&vjpBoundaryKernel<3>));
+    k.jvpBoundary = reinterpret_cast<const void*>(&jvpBoundaryKernel<DIM>);
+    k.vjpBoundary = reinterpret_cast<const void*>(&vjpBoundaryKernel<DIM>);
   } else {
-    k.jvpBoundary = pick(reinterpret_cast<const void*>(&jvpBoundaryNSKernel<2>), reinterpret_cast<const void*>(&jvpBoundaryNSKernel<3>));
-    k.vjpBoundary = pick(reinterpret_cast<const void*>(&vjpBoundaryNSKernel<2>), reinterpret_cast<const void*>(&vjpBoundaryNSKernel<3>));
-    k.jvpExchangeBoundary = pick(reinterpret_cast<const void*>(&jvpExchangeBoundaryKernel<2>),
-                                 reinterpret_cast<const void*>(&jvpExchangeBoundaryKernel<3>));
-    k.vjpExchangeBoundary = pick(reinterpret_cast<const void*>(&vjpExchangeBoundaryKernel<2>),
-                                 reinterpret_cast<const void*>(&vjpExchangeBoundaryKernel<3>));
+    k.jvpBoundary = reinterpret_cast<const void*>(&jvpBoundaryNSKernel<DIM>);
+    k.vjpBoundary = reinterpret_cast<const void*>(&vjpBoundaryNSKernel<DIM>);
+    k.jvpExchangeBoundary = reinterpret_cast<const void*>(&jvpExchangeBoundaryKernel<DIM>);
+    k.vjpExchangeBoundary = reinterpret_cast<const void*>(&vjpExchangeBoundaryKernel<DIM>);
   }
+}
+template <int DIM>
+void dimOf(int flux, bool visc, bool gen, AdjointKernels& k) {
+  if (visc) fluxOf<DIM, true>(flux, k, gen); else fluxOf<DIM, false>(flux, k, gen);
+  boundaryOf<DIM>(visc, k);
+}
+}  // namespace
+
+void adjointFaceKernels(int dim, int flux, bool visc, bool gen, AdjointKernels& k) {
+  if (dim == 1) dimOf<1>(flux, visc, gen, k);
+  else if (dim == 2) dimOf<2>(flux, visc, gen, k);
+  else if (dim == 3) dimOf<3>(flux, visc, gen, k);
 }
 
 }  // namespace sdg

@@ -68,7 +68,25 @@ CASES = {
                                                                     viscous=sdg.BR2, mu=1e-2),
     "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq": lambda: cases.cavity_3d_case(p=2, n=3, mu=1e-2,
                                                                                       boussinesq=True),
+    # 1D (line meshes): periodic, farfield ends, walls; Euler, Navier-Stokes, incompressible
+    "euler-line-p3-roe": lambda: cases.density_wave_1d_case(n=8, p=3, flux=sdg.ROE),
+    "euler-line-farfield-p2-hllc": lambda: cases.sod_1d_case(n=9, p=2, av=False, smooth=0.15, dt=2e-4),
+    "ns-line-p4-br1-roe": lambda: cases.density_wave_1d_case(n=6, p=4, flux=sdg.ROE, viscous=sdg.BR1, mu=0.02),
+    "ns-line-walls-p3-br2-roe": lambda: _ns1d(cases.sod_1d_case(
+        n=9, p=3, flux=sdg.ROE, av=False, smooth=0.15, dt=2e-4,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_NONSLIP_WALL)), sdg.BR2, 0.02),
+    "inc-line-p3-exact": lambda: cases.inc_wave_1d_case(n=8),
 }
+
+
+def _ns1d(case, viscous, mu):
+    mesh, cfg, ic, bc, dt, steps = case
+    return (mesh, cases.ns_config(cfg.polynomial_order, cfg.convective_flux, viscous, mu), ic, bc, dt, steps)
+
+
+def _force_group(s):
+    """A wall group and a force direction of the case's dimension."""
+    return {1: (1, [1.0]), 2: (1, [0.3, -1.0]), 3: (3, [0.2, -1.0, 0.4])}[s.counts.dimension]
 
 
 def _box3d(p=2, flux=sdg.ROE, n=3, viscous=False):
@@ -188,6 +206,7 @@ def test_vjp_is_the_transpose_of_jvp(name):
 
 @pytest.mark.parametrize("name", ["euler-quad-p3-roe", "euler-hex-p2-hllc", "ns-hex-p3-br1-roe",
                                   "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq",
+                                  "ns-line-p4-br1-roe",
                                   "ns-quad-p4-br1-hllc", "ns-hex-p2-br2-hllc", "ns-channel-walls-quad-p3-br2-roe"])
 def test_trajectory_dot_product_with_checkpointing(name):
     steps, interval = 5, 2
@@ -227,7 +246,8 @@ def test_checkpoint_interval_does_not_change_the_adjoint():
 # speed) at many face points of a low-Mach trajectory, where difference quotients straddle the switches;
 # the trajectory checks use the smooth fluxes (cfg: Roe + BR1 is the adjoint workload)
 @pytest.mark.parametrize("name", ["euler-hex-p3-central", "ns-hex-p3-br1-roe", "euler-quad-p3-roe",
-                                  "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-euler-shearlayer-quad-p2-central"])
+                                  "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-euler-shearlayer-quad-p2-central",
+                                  "ns-line-walls-p3-br2-roe"])
 def test_kinetic_energy_gradient_matches_finite_differences(name):
     steps, interval = 6, 3
     s, dt = make(name)
@@ -329,10 +349,11 @@ def test_surface_force_of_a_fluid_at_rest_is_the_pressure_times_the_area():
 
 @pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-box-walls-farfield-hex-p2-roe",
                                   "ns-channel-walls-quad-p3-br1-roe", "ns-box-walls-hex-p2-br1-roe",
-                                  "inc-ns-thermalcavity-quad-p3-exact-br1-boussinesq", "inc-ns-lidcavity-hex-p2-lf-br2"])
+                                  "inc-ns-thermalcavity-quad-p3-exact-br1-boussinesq", "inc-ns-lidcavity-hex-p2-lf-br2",
+                                  "ns-line-walls-p3-br2-roe"])
 def test_surface_force_cotangent_matches_central_differences(name):
     s, _ = make(name)
-    group, e = (1, [0.3, -1.0]) if s.counts.dimension == 2 else (3, [0.2, -1.0, 0.4])
+    group, e = _force_group(s)
     u = s.state_point()
     cot = s.surface_force_cotangent(group, e)
     d = direction(u, 5)
@@ -351,12 +372,13 @@ def test_surface_force_cotangent_matches_central_differences(name):
                                   "ns-channel-farfield-quad-p2-br1-hllc", "ns-box-walls-hex-p2-br1-roe",
                                   "ns-channel-walls-quad-p3-br2-roe", "inc-euler-channel-farfield-quad-p2-exact",
                                   "inc-ns-lidcavity-quad-p3-lf-br2", "inc-ns-thermalcavity-quad-p3-exact-br1-boussinesq",
-                                  "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq"])
+                                  "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq", "euler-line-farfield-p2-hllc",
+                                  "ns-line-walls-p3-br2-roe"])
 def test_force_gradient_through_a_trajectory(name):
     """J = e . force on a wall after N steps: dJ/dU_0 in a seeded direction and dJ/d(boundary primitives) in a
     seeded direction of every boundary point's (rho, u, T), against central differences of the trajectory."""
     s, dt = make(name)
-    group, e = (1, [0.3, -1.0]) if s.counts.dimension == 2 else (3, [0.2, -1.0, 0.4])
+    group, e = _force_group(s)
     steps = 6
     u0 = s.state_point()
     bpts, phys = s.boundary_points()
