@@ -3,10 +3,12 @@
 // The reference has no differentiation; these are the spec additions.  Both are exact derivatives of
 // the discrete scheme the forward path runs (same quadrature, same fluxes, same SSP-RK stages), so
 //   <lambda, JVP(dU)> = <VJP(lambda), dU>
-// holds to round-off, for one residual and for whole trajectories.  Scope: element blocks that are affine
-// tensor blocks (quadrangles P>=2 with straight parallelogram sides, hexahedra), interior (periodic) faces,
-// Euler or Navier-Stokes with BR1 or BR2, with or without boundary faces; other configurations return
-// SDG_ERR_UNSUPPORTED.
+// holds to round-off, for one residual and for whole trajectories.  Scope: compressible or incompressible
+// Euler on every element block (tensor blocks: lines, quadrangles -- affine or bilinear --, hexahedra; dense
+// blocks: triangles and first-order quadrangles), Navier-Stokes with BR1 or BR2 on affine tensor blocks, the
+// Boussinesq source, with or without boundary faces; other configurations (Navier-Stokes on dense or bilinear
+// blocks, artificial viscosity) return SDG_ERR_UNSUPPORTED.  The cotangents of the point-layout API are mapped
+// by the transposes of the point <-> state conversions (dense blocks: Phi^T in, P^T out, P the projection).
 //
 // Trajectories: the tangent runs stage by stage beside the forward state.  The adjoint stores the state
 // every `checkpoint_interval` steps on a forward sweep, then per segment (last first) recomputes the
@@ -52,7 +54,8 @@ struct Trajectory {
 };
 
 struct AdjointState {
-  AdjointKernels k;
+  AdjointKernels k;                    // face kernels
+  std::vector<AdjointTileKernels> bk;  // element kernels of each block
   double* dU[2] = {nullptr, nullptr};
   double* dface = nullptr;
   double* dfaceOther = nullptr;
@@ -117,16 +120,26 @@ AdjointState* adjoint(sdg_handle* h) {
   if (!h->hasState) throw Failure(SDG_ERR_STATE, "no state");
   if (h->adj) return h->adj;
   for (const DevBlock& B : h->blocks)
-    if (B.kind != kTensor || !B.affine)
-      throw Failure(SDG_ERR_UNSUPPORTED, "derivatives need affine tensor blocks (lines, quadrangles P>=2, hexahedra)");
+    if (h->ns && (B.kind != kTensor || !B.affine))
+      throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes derivatives need affine tensor blocks (lines, quadrangles P>=2, hexahedra)");
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   const bool gen = h->ph.incomp || h->ph.source;
   adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, gen, A->k);
-  adjointTileKernels(h->dim, h->blocks[0].n, h->ns, h->ns && h->cfg.viscous_flux == SDG_VISCOUS_BR2, gen, A->k);
   if (!A->k.valid()) throw Failure(SDG_ERR_UNSUPPORTED, "no derivative kernels for this configuration");
+  for (const DevBlock& B : h->blocks) {
+    AdjointTileKernels t;
+    if (B.kind == kTensor)
+      adjointTileKernels(h->dim, B.n, h->ns, h->ns && h->cfg.viscous_flux == SDG_VISCOUS_BR2, gen, B.affine != 0, t);
+    else
+      adjointDenseKernels(B.type, B.p, B.affine != 0, gen, t);
+    if (!t.valid() || (h->ns && !t.vjpGradient))
+      throw Failure(SDG_ERR_UNSUPPORTED, "no derivative kernels for this element block");
+    A->bk.push_back(t);
+  }
   SDG_CUDA(cudaSetDevice(h->device));
-  for (const void* fn : {A->k.jvpStage, A->k.vjpVolume, A->k.vjpGradient, A->k.vjpTrace}) configureKernel(fn, h->device);
+  for (const AdjointTileKernels& t : A->bk)
+    for (const void* fn : {t.jvpStage, t.vjpVolume, t.vjpGradient, t.vjpTrace}) configureKernel(fn, h->device);
   const size_t S = h->stateCount, F = h->faceCount;
   A->dU[0] = alloc(S); A->dU[1] = alloc(S);
   A->dface = alloc(F); A->dflux = alloc(F);
@@ -136,7 +149,7 @@ AdjointState* adjoint(sdg_handle* h) {
     A->dfaceOther = alloc(F); A->dgrad = alloc(h->gradCount); A->dfaceGrad = alloc(F * h->dim);
     A->lamG = alloc(h->gradCount); A->lamTg = alloc(F * h->dim); A->lamUp = alloc(F);
   }
-  for (const DevBlock& B : h->blocks) A->muTiles += (B.ne + A->k.epb - 1) / A->k.epb;
+  for (size_t b = 0; b < h->blocks.size(); ++b) A->muTiles += (h->blocks[b].ne + A->bk[b].epb - 1) / A->bk[b].epb;
   A->muFaces = (h->nInterior * h->nfq + kFaceThreads - 1) / kFaceThreads;
   A->muBoundary = h->ns ? (h->nBoundary * h->nfq + kFaceThreads - 1) / kFaceThreads : 0;
   A->muPart = alloc(size_t(A->muTiles + A->muFaces + A->muBoundary));
@@ -162,6 +175,10 @@ AdjointState* adjoint(sdg_handle* h) {
   return h->adj;
 }
 
+// Index of block B in the handle, and its element kernels.
+size_t blockIndex(const sdg_handle* h, const DevBlock& B) { return size_t(&B - h->blocks.data()); }
+const AdjointTileKernels& tileKernels(const sdg_handle* h, const DevBlock& B) { return h->adj->bk[blockIndex(h, B)]; }
+
 AdjArgs baseArgs(sdg_handle* h, const DevBlock* B, const double* U) {
   AdjArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -175,7 +192,7 @@ AdjArgs baseArgs(sdg_handle* h, const DevBlock* B, const double* U) {
   a.face = A->curFace ? A->curFace : h->face;
   a.faceGrad = A->curFaceGrad ? A->curFaceGrad : h->faceGrad;
   a.conn = h->fconn; a.fgeo = h->fgeo; a.status = h->status;
-  a.nface = h->nInterior; a.n1d = h->n1d; a.epb = h->adj->k.epb;
+  a.nface = h->nInterior; a.n1d = h->n1d; a.epb = B ? tileKernels(h, *B).epb : 0;
   return a;
 }
 
@@ -189,7 +206,10 @@ void launch(sdg_handle* h, const void* fn, int64_t grid, int threads, size_t sme
   (void)withPhys;
 }
 
-int64_t tiles(const sdg_handle* h, const DevBlock& B) { return (B.ne + h->adj->k.epb - 1) / h->adj->k.epb; }
+int64_t tiles(const sdg_handle* h, const DevBlock& B) {
+  const int epb = tileKernels(h, B).epb;
+  return (B.ne + epb - 1) / epb;
+}
 int64_t faceGrid(const sdg_handle* h) { return (h->nInterior * h->nfq + kFaceThreads - 1) / kFaceThreads; }
 int64_t boundaryGrid(const sdg_handle* h) { return (h->nBoundary * h->nfq + kFaceThreads - 1) / kFaceThreads; }
 
@@ -280,7 +300,8 @@ void tangentElements(sdg_handle* h, const double* u, const double* du, double dm
     a.dout = dout ? dout + B.stateOffset : nullptr;
     a.dtrace = dout ? A->dface : nullptr;
     a.c0 = c0; a.c1 = c1; a.c2dt = c2dt;
-    launch(h, A->k.jvpStage, tiles(h, B), A->k.threads, A->k.jvpSmem, a, true);
+    const AdjointTileKernels& t = tileKernels(h, B);
+    launch(h, t.jvpStage, tiles(h, B), t.threads, t.jvpSmem, a, true);
   }
 }
 
@@ -300,14 +321,14 @@ void jvpResidual(sdg_handle* h, const double* du, double dmu, double* drate) {
 void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* lamStage, double* lamBase,
                  bool accumulateAll, double c0, double c1, double c2dt, double muScale, double ghostScale) {
   AdjointState* A = h->adj;
-  const int NT = A->k.threads;
   int64_t tileOff = 0;
   for (DevBlock& B : h->blocks) {
+    const AdjointTileKernels& t = tileKernels(h, B);
     AdjArgs a = baseArgs(h, &B, h->state[1]);
     a.lam = lam + B.stateOffset; a.lamU = A->lamU + B.stateOffset;
     a.lamG = h->ns ? A->lamG + B.gradOffset : nullptr;
     a.lamH = A->lamH; a.muPart = A->muPart + tileOff;
-    launch(h, A->k.vjpVolume, tiles(h, B), NT, A->k.vjpSmem, a, true);
+    launch(h, t.vjpVolume, tiles(h, B), t.threads, t.vjpSmem, a, true);
     tileOff += tiles(h, B);
   }
   {
@@ -323,10 +344,11 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
   }
   if (h->ns) {
     for (DevBlock& B : h->blocks) {
+      const AdjointTileKernels& t = tileKernels(h, B);
       AdjArgs a = baseArgs(h, &B, h->state[1]);
       a.lamG = A->lamG + B.gradOffset; a.lamTg = A->lamTg; a.lamU = A->lamU + B.stateOffset; a.lamUp = A->lamUp;
       a.lamTr = A->lamTr;  // BR2: the own traces' share
-      launch(h, A->k.vjpGradient, tiles(h, B), NT, A->k.vjpSmem, a, false);
+      launch(h, t.vjpGradient, tiles(h, B), t.threads, t.vjpSmem, a, false);
     }
     AdjArgs a = baseArgs(h, nullptr, nullptr);
     a.lamUp = A->lamUp; a.lamTr = A->lamTr;
@@ -345,7 +367,8 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
     a.lamBase = lamBase ? lamBase + B.stateOffset : nullptr;
     a.accumulateAll = accumulateAll;
     a.c0 = c0; a.c1 = c1; a.c2dt = c2dt;
-    launch(h, A->k.vjpTrace, tiles(h, B), NT, A->k.vjpSmem, a, false);
+    const AdjointTileKernels& t = tileKernels(h, B);
+    launch(h, t.vjpTrace, tiles(h, B), t.threads, t.vjpSmem, a, false);
   }
   if (!h->ns) return;
   muAccumulateKernel<<<1, 256, 0, h->stream>>>(A->muPart, A->muTiles + A->muFaces + A->muBoundary, muScale, A->muAcc);
@@ -374,6 +397,21 @@ void uploadPoints(sdg_handle* h, const double* host, double* st) {
 void downloadPoints(sdg_handle* h, const double* st, double* host) {
   AdjointState* A = h->adj;
   stateToPointsBuffer(h, st, A->pts);
+  SDG_CUDA(cudaMemcpyAsync(host, A->pts, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  SDG_CUDA(cudaStreamSynchronize(h->stream));
+}
+
+// Cotangents in the point layout: the transposed conversions (on dense blocks Phi^T in, P^T out), so that the
+// point-layout VJP is the transpose of the point-layout JVP.
+void uploadCotangent(sdg_handle* h, const double* host, double* st) {
+  AdjointState* A = h->adj;
+  SDG_CUDA(cudaMemcpyAsync(A->pts, host, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyHostToDevice, h->stream));
+  cotangentPointsToState(h, A->pts, st);
+}
+
+void downloadCotangent(sdg_handle* h, const double* st, double* host) {
+  AdjointState* A = h->adj;
+  cotangentStateToPoints(h, st, A->pts);
   SDG_CUDA(cudaMemcpyAsync(host, A->pts, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
   SDG_CUDA(cudaStreamSynchronize(h->stream));
 }
@@ -647,14 +685,14 @@ int sdg_vjp_residual(sdg_handle* h, const double* rate_cotangent, double* cotang
     AdjointState* A = adjoint(h);
     SDG_CUDA(cudaSetDevice(h->device));
     copyState(h, h->state[1], h->state[0]);
-    uploadPoints(h, rate_cotangent, A->lamIn);
+    uploadCotangent(h, rate_cotangent, A->lamIn);
     forwardAt(h, h->state[1]);
     SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
     clearGhost(h);
     A->ghostPending = false;
     vjpResidual(h, A->lamIn, nullptr, nullptr, nullptr, false, 0.0, 0.0, 0.0,
                 h->ns && h->ph.mu > 0.0 ? 1.0 / h->ph.mu : 0.0, 1.0);
-    downloadPoints(h, A->lamU, cotangent);
+    downloadCotangent(h, A->lamU, cotangent);
     if (viscosity_cotangent) *viscosity_cotangent = h->ns ? readMu(h) : 0.0;
     traces(h, h->state[0], h->face);
     checkStatus(h);
@@ -690,9 +728,9 @@ int sdg_adjoint_steps(sdg_handle* h, int32_t steps, double dt, int32_t interval,
     AdjointState* A = adjoint(h);
     SDG_CUDA(cudaSetDevice(h->device));
     forwardSweep(h, steps, dt, interval);
-    uploadPoints(h, final_cotangent, A->lamIn);
+    uploadCotangent(h, final_cotangent, A->lamIn);
     const double m = backwardSweep(h);
-    downloadPoints(h, A->lamIn, initial_cotangent);
+    downloadCotangent(h, A->lamIn, initial_cotangent);
     if (viscosity_cotangent) *viscosity_cotangent = m;
     checkStatus(h);
   } catch (const Failure& f) {
@@ -723,9 +761,9 @@ int sdg_adjoint_recorded(sdg_handle* h, const double* final_cotangent, double* i
     if (!A->traj.valid || A->traj.version != h->stateVersion)
       throw Failure(SDG_ERR_STATE, "no recorded trajectory ends at the current state (sdg_forward_steps first)");
     SDG_CUDA(cudaSetDevice(h->device));
-    uploadPoints(h, final_cotangent, A->lamIn);
+    uploadCotangent(h, final_cotangent, A->lamIn);
     const double m = backwardSweep(h);
-    downloadPoints(h, A->lamIn, initial_cotangent);
+    downloadCotangent(h, A->lamIn, initial_cotangent);
     if (viscosity_cotangent) *viscosity_cotangent = m;
     checkStatus(h);
   } catch (const Failure& f) {
@@ -794,7 +832,8 @@ int sdg_surface_force_cotangent(sdg_handle* h, int32_t physical, const double* d
         AdjArgs g = baseArgs(h, &B, h->state[0]);
         g.lamG = A->lamG + B.gradOffset; g.lamTg = A->lamTg; g.lamU = A->lamU + B.stateOffset; g.lamUp = A->lamUp;
         g.lamTr = A->lamTr;
-        launch(h, A->k.vjpGradient, tiles(h, B), A->k.threads, A->k.vjpSmem, g, false);
+        const AdjointTileKernels& t = tileKernels(h, B);
+        launch(h, t.vjpGradient, tiles(h, B), t.threads, t.vjpSmem, g, false);
       }
       AdjArgs x = baseArgs(h, nullptr, nullptr);
       x.lamUp = A->lamUp; x.lamTr = A->lamTr;
@@ -809,9 +848,10 @@ int sdg_surface_force_cotangent(sdg_handle* h, int32_t physical, const double* d
     for (DevBlock& B : h->blocks) {
       AdjArgs t = baseArgs(h, &B, h->state[0]);
       t.lamU = A->lamU + B.stateOffset; t.lamTr = A->lamTr;
-      launch(h, A->k.vjpTrace, tiles(h, B), A->k.threads, A->k.vjpSmem, t, false);
+      const AdjointTileKernels& tk = tileKernels(h, B);
+      launch(h, tk.vjpTrace, tiles(h, B), tk.threads, tk.vjpSmem, t, false);
     }
-    downloadPoints(h, A->lamU, cotangent);
+    downloadCotangent(h, A->lamU, cotangent);
     checkStatus(h);
   } catch (const Failure& f) {
     return adjFail(h, f);

@@ -96,6 +96,34 @@ __global__ void stateToPointKernel(const double* __restrict__ st, double* __rest
   }
 }
 
+// Transposes of the two conversions on dense blocks, for cotangents: st = Phi^T pts (of stateToPoint) and
+// pts = P^T st (of pointToState, P the least-squares projection [nb][nq]).
+__global__ void phiTransposeKernel(const double* __restrict__ pts, double* __restrict__ st, const double* __restrict__ phi,
+                                   int64_t ne, int nb, int nq, int nv, int ustride) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ne * nb) return;
+  const int64_t e = t / nb;
+  const int b = int(t - e * nb);
+  for (int v = 0; v < nv; ++v) {
+    double s = 0.0;
+    for (int q = 0; q < nq; ++q) s = fma(phi[q * nb + b], pts[(e * nq + q) * nv + v], s);
+    st[e * ustride + v * nb + b] = s;
+  }
+}
+
+__global__ void projTransposeKernel(const double* __restrict__ st, double* __restrict__ pts, const double* __restrict__ proj,
+                                    int64_t ne, int nb, int nq, int nv, int ustride) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= ne * nq) return;
+  const int64_t e = t / nq;
+  const int q = int(t - e * nq);
+  for (int v = 0; v < nv; ++v) {
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) s = fma(proj[b * nq + q], st[e * ustride + v * nb + b], s);
+    pts[(e * nq + q) * nv + v] = s;
+  }
+}
+
 // (rho, u, T) -> (rho, rho u, rho E) in place (VariableConvertor.cpp:341-366).
 __global__ void primitiveToConservedKernel(double* __restrict__ pts, int64_t n, int dim, Phys ph) {
   const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
@@ -653,6 +681,34 @@ void pointsToStateBuffer(sdg_handle* h, const double* pts, double* st) {
     pointToStateKernel<<<grid, 256, 0, h->stream>>>(pts + B.pointOffset * h->nv, st + B.stateOffset,
                                                     B.kind == kDense ? B.lsqDev : nullptr, B.ne, B.nb, B.nq, h->nv,
                                                     B.ustride);
+    checkLaunch(h);
+  }
+}
+
+// Cotangents: the transposes of stateToPointsBuffer (points -> state) and of pointsToStateBuffer (state ->
+// points).  On tensor blocks both maps are the same permutation of the layout, whose transpose is its inverse.
+void cotangentPointsToState(sdg_handle* h, const double* pts, double* st) {
+  for (DevBlock& B : h->blocks) {
+    const int grid = int((B.ne * B.nb + 255) / 256);
+    if (B.kind == kDense)
+      phiTransposeKernel<<<grid, 256, 0, h->stream>>>(pts + B.pointOffset * h->nv, st + B.stateOffset, B.phiDev, B.ne,
+                                                      B.nb, B.nq, h->nv, B.ustride);
+    else
+      pointToStateKernel<<<grid, 256, 0, h->stream>>>(pts + B.pointOffset * h->nv, st + B.stateOffset, nullptr, B.ne,
+                                                      B.nb, B.nq, h->nv, B.ustride);
+    checkLaunch(h);
+  }
+}
+
+void cotangentStateToPoints(sdg_handle* h, const double* st, double* pts) {
+  for (DevBlock& B : h->blocks) {
+    const int grid = int((B.ne * B.nq + 255) / 256);
+    if (B.kind == kDense)
+      projTransposeKernel<<<grid, 256, 0, h->stream>>>(st + B.stateOffset, pts + B.pointOffset * h->nv, B.lsqDev, B.ne,
+                                                       B.nb, B.nq, h->nv, B.ustride);
+    else
+      stateToPointKernel<<<grid, 256, 0, h->stream>>>(st + B.stateOffset, pts + B.pointOffset * h->nv, nullptr, B.ne,
+                                                      B.nb, B.nq, h->nv, B.ustride);
     checkLaunch(h);
   }
 }

@@ -174,6 +174,8 @@ extern const double kRk[3][3][3];
 // Point layout [point][v] <-> state layout of device buffers (tensor: transpose; dense: projection).
 void pointsToStateBuffer(sdg_handle* h, const double* pts, double* st);
 void stateToPointsBuffer(sdg_handle* h, const double* st, double* pts);
+void cotangentPointsToState(sdg_handle* h, const double* pts, double* st);
+void cotangentStateToPoints(sdg_handle* h, const double* st, double* pts);
 // Tangent-linear / adjoint resources of a handle (sdg_adjoint.cu), released with the handle.
 void destroyAdjoint(sdg_handle* h);
 // The gradient pass and viscous-layout buffers run for Navier-Stokes and for artificial viscosity.

@@ -1200,7 +1200,7 @@ __device__ __forceinline__ void loadTensorTables(TensorTables* T, const double* 
 
 // Tangent element kernel: dR = (1/|J|)[sum_b Dhat_b dQ_b - Lift dH]; RK combination of the tangents and
 // the traces of the new tangent state (the forward stage kernel's structure on tangents).
-template <int DIM, int N, bool VISC>
+template <int DIM, int N, bool VISC, bool AFF = true>
 __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) jvpStageKernel(AdjArgs a, Phys ph) {
   using A = AdjShape<DIM, N>;
   constexpr int NV = A::NV, NB = A::NB, NF = A::NF, NFQ = A::NFQ, EPB = A::EPB;
@@ -1226,7 +1226,8 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) jvpStageKernel(A
   __syncthreads();
   double jinv = 0.0;
   if (active) {
-    const double* g = a.geom + e * (DIM * DIM + 1);
+    // affine: one metric per element; bilinear quadrangles: per node (the forward stage tile's geometry)
+    const double* g = AFF ? a.geom + e * (DIM * DIM + 1) : a.geom + (e * NB + node) * (DIM * DIM + 1);
     double ja[DIM][DIM];
 #pragma unroll
     for (int b = 0; b < DIM; ++b)
@@ -1338,7 +1339,7 @@ __device__ __forceinline__ void blockSum(double x, double* part, double* sRed) {
 
 // V1: s = lam/|J|; lamQ_b by the transposed derivative; node Jacobians by Dual<NV> over U;
 // lamG (NS) by the viscous transpose; lamH by the transposed lift.  muPart[tile] = <lamQ, Qv>.
-template <int DIM, int N, bool VISC, bool GEN>
+template <int DIM, int N, bool VISC, bool GEN, bool AFF = true>
 __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(AdjArgs a, Phys ph) {
   using A = AdjShape<DIM, N>;
   constexpr int NV = A::NV, NB = A::NB, NF = A::NF, NFQ = A::NFQ, EPB = A::EPB;
@@ -1354,15 +1355,16 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpVolumeKernel(
   const int64_t e = e0 + le;
   loadTensorTables<DIM, N>(T, a.tables);
   double jinv = 0.0;
+  const double* geo = AFF ? a.geom + e * (DIM * DIM + 1) : a.geom + (e * NB + node) * (DIM * DIM + 1);
   if (active) {
-    jinv = a.geom[e * (DIM * DIM + 1) + DIM * DIM];
+    jinv = geo[DIM * DIM];
 #pragma unroll
     for (int v = 0; v < NV; ++v) sS[(le * NV + v) * NB + node] = jinv * a.lam[e * A::USTRIDE + v * NB + node];
   }
   __syncthreads();
   double mupart = 0.0;
   if (active) {
-    const double* g = a.geom + e * (DIM * DIM + 1);
+    const double* g = geo;
     double ja[DIM][DIM];
 #pragma unroll
     for (int b = 0; b < DIM; ++b)

@@ -34,27 +34,35 @@ KernelVariant denseGradVariant(int type, int p, bool affine);
 KernelVariant facePointVariant(int op, int dim, int flux);
 KernelVariant relerrVariant();
 
-// Tangent-linear and adjoint kernels of affine tensor blocks (sdg_kernels_adjoint.cuh), interior faces.
+// Tangent-linear and adjoint face kernels (sdg_kernels_adjoint.cuh), shared by every element block.
 struct AdjointKernels {
   const void* jvpFace = nullptr;      // (AdjArgs, Phys), one thread per face point
   const void* vjpFace = nullptr;      // (AdjArgs, Phys), one thread per face point
   const void* vjpExchange = nullptr;  // (AdjArgs), one thread per face point
-  const void* jvpStage = nullptr;     // (AdjArgs, Phys), one CTA per tile of epb elements
-  const void* vjpVolume = nullptr;    // (AdjArgs, Phys)
-  const void* vjpGradient = nullptr;  // (AdjArgs)
-  const void* vjpTrace = nullptr;     // (AdjArgs)
   const void* jvpBoundary = nullptr;  // (AdjArgs, Phys), one thread per boundary face point
   const void* vjpBoundary = nullptr;  // (AdjArgs, Phys)
   const void* jvpExchangeBoundary = nullptr;  // (AdjArgs, Phys), Navier-Stokes: the gradient pass's wall states
   const void* vjpExchangeBoundary = nullptr;  // (AdjArgs, Phys)
+  bool valid() const { return jvpFace && vjpFace; }
+};
+// Tangent-linear and adjoint element kernels of one block (tensor: sdg_kernels_adjoint.cuh; dense:
+// sdg_kernels_adjoint_dense.cuh), one CTA per tile of epb elements.
+struct AdjointTileKernels {
+  const void* jvpStage = nullptr;     // (AdjArgs, Phys)
+  const void* vjpVolume = nullptr;    // (AdjArgs, Phys)
+  const void* vjpGradient = nullptr;  // (AdjArgs), Navier-Stokes
+  const void* vjpTrace = nullptr;     // (AdjArgs)
   int epb = 0, threads = 0;
   size_t jvpSmem = 0, vjpSmem = 0;
-  bool valid() const { return jvpStage && jvpFace; }
+  bool valid() const { return jvpStage && vjpVolume && vjpTrace; }
 };
-// Face kernels depend on (dim, flux, viscous); tile kernels on (dim, nodes per direction, viscous, BR2).
-// gen: the dual-number transposes (incompressible model, Boussinesq source) instead of the hand-written ones.
+// Face kernels depend on (dim, flux, viscous); tensor tile kernels on (dim, nodes per direction, viscous, BR2,
+// affine: bilinear quadrangles for the Euler equations only); dense tile kernels on (type, order, affine),
+// the Euler equations.  gen: the dual-number transposes (incompressible model, Boussinesq source) instead of
+// the hand-written ones.  Unsupported combinations leave the kernels null.
 void adjointFaceKernels(int dim, int flux, bool visc, bool gen, AdjointKernels& k);
-void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, AdjointKernels& k);
+void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, bool affine, AdjointTileKernels& k);
+void adjointDenseKernels(int type, int p, bool affine, bool gen, AdjointTileKernels& k);
 
 // Largest tile size the kernels are compiled for (their __launch_bounds__).
 constexpr int kMaxThreads = 512;

@@ -1,4 +1,5 @@
-// Tangent-linear and adjoint element (tile) kernels of affine tensor blocks (lines, quadrangles, hexahedra): the one translation unit that
+// Tangent-linear and adjoint element (tile) kernels of tensor blocks (lines, quadrangles, hexahedra; bilinear
+// quadrangles for the Euler equations): the one translation unit that
 // instantiates them.
 #include "sdg_kernels_adjoint.cuh"
 #include "sdg_variants.hpp"
@@ -7,7 +8,7 @@ namespace sdg {
 
 namespace {
 template <int DIM, int N, bool VISC>
-void tileOf(AdjointKernels& k, bool br2, bool gen) {
+void tileOf(AdjointTileKernels& k, bool br2, bool gen) {
   using A = AdjShape<DIM, N>;
   k.jvpStage = reinterpret_cast<const void*>(&jvpStageKernel<DIM, N, VISC>);
   k.vjpVolume = gen ? reinterpret_cast<const void*>(&vjpVolumeKernel<DIM, N, VISC, true>)
@@ -17,9 +18,30 @@ void tileOf(AdjointKernels& k, bool br2, bool gen) {
   k.vjpTrace = reinterpret_cast<const void*>(&vjpTraceKernel<DIM, N>);
   k.epb = A::EPB; k.threads = A::THREADS; k.jvpSmem = A::JVP_SMEM; k.vjpSmem = A::VJP_SMEM;
 }
+// Bilinear quadrangles (per-node metric), the Euler equations.
+template <int N>
+void bilinearOf(AdjointTileKernels& k, bool gen) {
+  using A = AdjShape<2, N>;
+  k.jvpStage = reinterpret_cast<const void*>(&jvpStageKernel<2, N, false, false>);
+  k.vjpVolume = gen ? reinterpret_cast<const void*>(&vjpVolumeKernel<2, N, false, true, false>)
+                    : reinterpret_cast<const void*>(&vjpVolumeKernel<2, N, false, false, false>);
+  k.vjpTrace = reinterpret_cast<const void*>(&vjpTraceKernel<2, N>);
+  k.epb = A::EPB; k.threads = A::THREADS; k.jvpSmem = A::JVP_SMEM; k.vjpSmem = A::VJP_SMEM;
+}
 }  // namespace
 
-void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, AdjointKernels& k) {
+void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, bool affine, AdjointTileKernels& k) {
+  if (!affine) {
+    if (dim != 2 || visc) return;
+    switch (n) {
+      case 3: bilinearOf<3>(k, gen); break;
+      case 4: bilinearOf<4>(k, gen); break;
+      case 5: bilinearOf<5>(k, gen); break;
+      case 6: bilinearOf<6>(k, gen); break;
+      default: break;
+    }
+    return;
+  }
 #define SDG_AT(D, NN) \
   if (dim == D && n == NN) { if (visc) tileOf<D, NN, true>(k, br2, gen); else tileOf<D, NN, false>(k, false, gen); return; }
   SDG_AT(1, 2) SDG_AT(1, 3) SDG_AT(1, 4) SDG_AT(1, 5) SDG_AT(1, 6)

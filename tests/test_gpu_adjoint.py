@@ -76,6 +76,25 @@ CASES = {
         n=9, p=3, flux=sdg.ROE, av=False, smooth=0.15, dt=2e-4,
         conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_NONSLIP_WALL)), sdg.BR2, 0.02),
     "inc-line-p3-exact": lambda: cases.inc_wave_1d_case(n=8),
+    # dense (modal) blocks -- triangles, first-order and bilinear quadrangles -- and hybrid meshes with bilinear
+    # tensor quadrangles: the Euler equations
+    "euler-tri-p2-hllc": lambda: cases.kh_case(n=4, p=2, flux=sdg.HLLC, split=1.0),
+    "euler-tri-p3-central": lambda: cases.kh_case(n=4, p=3, flux=sdg.CENTRAL, split=1.0),
+    "euler-tri-p5-roe": lambda: cases.kh_case(n=3, p=5, flux=sdg.ROE, split=1.0, dt=5e-5),
+    "euler-quad-p1-roe-dense": lambda: cases.vortex_case(n=4, p=1, flux=sdg.ROE),
+    "euler-jitter-quad-p1-hllc-bilinear": lambda: cases.kh_case(n=4, p=1, flux=sdg.HLLC, split=0.0),
+    "euler-hybrid-p3-lf-bilinear": lambda: cases.kh_case(n=4, p=3, flux=sdg.LAX_FRIEDRICHS, split=0.5),
+    "euler-jitter-quad-p4-roe-bilinear": lambda: cases.kh_case(n=3, p=4, flux=sdg.ROE, split=0.0, dt=1e-4),
+    "euler-channel-tri-p3-roe": lambda: cases.channel_case(p=3, flux=sdg.ROE, n=3, split=1.0),
+    # (the Riemann farfield takes the tangential velocity and entropy of the ghost or of the interior by the sign of
+    # u.n: a jump where u.n crosses 0, as on a farfield side parallel to the stream; farfield on the stream's ends)
+    "euler-channel-hybrid-farfield-p2-hllc": lambda: cases.channel_case(
+        p=2, flux=sdg.HLLC, n=3, split=0.5, jitter=0.1,
+        conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD)),
+    "inc-euler-shearlayer-tri-p3-exact": lambda: cases.shear_layer_case(n=4, p=3, flux=sdg.EXACT, split=1.0),
+    "inc-euler-thermalcavity-hybrid-p2-exact-boussinesq": lambda: cases.cavity_case(
+        p=2, flux=sdg.EXACT, viscous=None, mu=0.0, n=4, split=0.5, boussinesq=True, c0=3.0,
+        conditions=(sdg.ADIABATIC_SLIP_WALL,) * 4),
 }
 
 
@@ -206,7 +225,7 @@ def test_vjp_is_the_transpose_of_jvp(name):
 
 @pytest.mark.parametrize("name", ["euler-quad-p3-roe", "euler-hex-p2-hllc", "ns-hex-p3-br1-roe",
                                   "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq",
-                                  "ns-line-p4-br1-roe",
+                                  "ns-line-p4-br1-roe", "euler-hybrid-p3-lf-bilinear", "euler-tri-p5-roe",
                                   "ns-quad-p4-br1-hllc", "ns-hex-p2-br2-hllc", "ns-channel-walls-quad-p3-br2-roe"])
 def test_trajectory_dot_product_with_checkpointing(name):
     steps, interval = 5, 2
@@ -247,7 +266,7 @@ def test_checkpoint_interval_does_not_change_the_adjoint():
 # the trajectory checks use the smooth fluxes (cfg: Roe + BR1 is the adjoint workload)
 @pytest.mark.parametrize("name", ["euler-hex-p3-central", "ns-hex-p3-br1-roe", "euler-quad-p3-roe",
                                   "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-euler-shearlayer-quad-p2-central",
-                                  "ns-line-walls-p3-br2-roe"])
+                                  "ns-line-walls-p3-br2-roe", "euler-tri-p3-central"])
 def test_kinetic_energy_gradient_matches_finite_differences(name):
     steps, interval = 6, 3
     s, dt = make(name)
@@ -299,7 +318,8 @@ def test_torch_autograd_binding():
 
 
 def test_derivatives_refuse_unsupported_configurations():
-    hybrid = sdg.GpuSolver(*cases.kh_case(n=4, p=3)[:2], device=0)
+    # Navier-Stokes on dense or bilinear blocks (the hybrid Kelvin-Helmholtz mesh)
+    hybrid = sdg.GpuSolver(*cases.kh_case(n=4, p=3, viscous=sdg.BR2, mu=1e-3)[:2], device=0)
     hybrid.initialize_primitive(cases.kh_primitive(*hybrid.volume_points()[:, :2].T))
     with pytest.raises(sdg.SdgError) as e:
         hybrid.jvp_residual(np.zeros((hybrid.counts.volume_point_count, 4)))
@@ -350,7 +370,8 @@ def test_surface_force_of_a_fluid_at_rest_is_the_pressure_times_the_area():
 @pytest.mark.parametrize("name", ["euler-channel-quad-p3-roe", "euler-box-walls-farfield-hex-p2-roe",
                                   "ns-channel-walls-quad-p3-br1-roe", "ns-box-walls-hex-p2-br1-roe",
                                   "inc-ns-thermalcavity-quad-p3-exact-br1-boussinesq", "inc-ns-lidcavity-hex-p2-lf-br2",
-                                  "ns-line-walls-p3-br2-roe"])
+                                  "ns-line-walls-p3-br2-roe", "euler-channel-tri-p3-roe",
+                                  "euler-channel-hybrid-farfield-p2-hllc"])
 def test_surface_force_cotangent_matches_central_differences(name):
     s, _ = make(name)
     group, e = _force_group(s)
@@ -373,7 +394,8 @@ def test_surface_force_cotangent_matches_central_differences(name):
                                   "ns-channel-walls-quad-p3-br2-roe", "inc-euler-channel-farfield-quad-p2-exact",
                                   "inc-ns-lidcavity-quad-p3-lf-br2", "inc-ns-thermalcavity-quad-p3-exact-br1-boussinesq",
                                   "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq", "euler-line-farfield-p2-hllc",
-                                  "ns-line-walls-p3-br2-roe"])
+                                  "ns-line-walls-p3-br2-roe", "euler-channel-tri-p3-roe",
+                                  "euler-channel-hybrid-farfield-p2-hllc"])
 def test_force_gradient_through_a_trajectory(name):
     """J = e . force on a wall after N steps: dJ/dU_0 in a seeded direction and dJ/d(boundary primitives) in a
     seeded direction of every boundary point's (rho, u, T), against central differences of the trajectory."""
