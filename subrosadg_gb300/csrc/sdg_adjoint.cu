@@ -328,7 +328,7 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
     a.lam = lam + B.stateOffset; a.lamU = A->lamU + B.stateOffset;
     a.lamG = h->ns ? A->lamG + B.gradOffset : nullptr;
     a.lamH = A->lamH; a.muPart = A->muPart + tileOff;
-    launch(h, t.vjpVolume, tiles(h, B), t.threads, t.vjpSmem, a, true);
+    launch(h, t.vjpVolume, tiles(h, B), t.threads, t.volSmem, a, true);
     tileOff += tiles(h, B);
   }
   {
@@ -348,7 +348,7 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
       AdjArgs a = baseArgs(h, &B, h->state[1]);
       a.lamG = A->lamG + B.gradOffset; a.lamTg = A->lamTg; a.lamU = A->lamU + B.stateOffset; a.lamUp = A->lamUp;
       a.lamTr = A->lamTr;  // BR2: the own traces' share
-      launch(h, t.vjpGradient, tiles(h, B), t.threads, t.vjpSmem, a, false);
+      launch(h, t.vjpGradient, tiles(h, B), t.threads, t.gradSmem, a, false);
     }
     AdjArgs a = baseArgs(h, nullptr, nullptr);
     a.lamUp = A->lamUp; a.lamTr = A->lamTr;
@@ -368,7 +368,7 @@ void vjpResidual(sdg_handle* h, const double* lam, const double* lamIn, double* 
     a.accumulateAll = accumulateAll;
     a.c0 = c0; a.c1 = c1; a.c2dt = c2dt;
     const AdjointTileKernels& t = tileKernels(h, B);
-    launch(h, t.vjpTrace, tiles(h, B), t.threads, t.vjpSmem, a, false);
+    launch(h, t.vjpTrace, tiles(h, B), t.threads, t.traceSmem, a, false);
   }
   if (!h->ns) return;
   muAccumulateKernel<<<1, 256, 0, h->stream>>>(A->muPart, A->muTiles + A->muFaces + A->muBoundary, muScale, A->muAcc);
@@ -833,7 +833,7 @@ int sdg_surface_force_cotangent(sdg_handle* h, int32_t physical, const double* d
         g.lamG = A->lamG + B.gradOffset; g.lamTg = A->lamTg; g.lamU = A->lamU + B.stateOffset; g.lamUp = A->lamUp;
         g.lamTr = A->lamTr;
         const AdjointTileKernels& t = tileKernels(h, B);
-        launch(h, t.vjpGradient, tiles(h, B), t.threads, t.vjpSmem, g, false);
+        launch(h, t.vjpGradient, tiles(h, B), t.threads, t.gradSmem, g, false);
       }
       AdjArgs x = baseArgs(h, nullptr, nullptr);
       x.lamUp = A->lamUp; x.lamTr = A->lamTr;
@@ -849,7 +849,7 @@ int sdg_surface_force_cotangent(sdg_handle* h, int32_t physical, const double* d
       AdjArgs t = baseArgs(h, &B, h->state[0]);
       t.lamU = A->lamU + B.stateOffset; t.lamTr = A->lamTr;
       const AdjointTileKernels& tk = tileKernels(h, B);
-      launch(h, tk.vjpTrace, tiles(h, B), tk.threads, tk.vjpSmem, t, false);
+      launch(h, tk.vjpTrace, tiles(h, B), tk.threads, tk.traceSmem, t, false);
     }
     downloadCotangent(h, A->lamU, cotangent);
     checkStatus(h);

@@ -1186,10 +1186,13 @@ struct AdjShape {
   static constexpr int THREADS = S::THREADS;
   // tangent element tile: u, du | tangent flux slots | tangent contravariant fluxes [DIM][NV][NB]
   static constexpr size_t JVP_SMEM = size_t(EPB) * 8 * (2 * USTRIDE + FSTRIDE + DIM * NV * NB) + sizeof(TensorTables);
-  // adjoint element tiles: scaled cotangent s [NV][NB] | node-gradient cotangent [NV*DIM][NB] |
-  // t_b [DIM][NV][NB] | slot cotangents (FSTRIDE * DIM for the gradient traces)
-  static constexpr size_t VJP_SMEM =
-      size_t(EPB) * 8 * (USTRIDE + GSTR + DIM * NV * NB + FSTRIDE * DIM) + sizeof(TensorTables);
+  // adjoint element tiles, each its own layout (the shared memory bounds how many CTAs an SM keeps):
+  //   volume:   scaled cotangent s [NV][NB] | tables | one double per warp (the viscosity term's sum)
+  //   gradient: t_b [DIM][NV][NB] (BR2: and v_b) | tables
+  //   trace:    tables
+  static constexpr size_t VOL_SMEM = size_t(EPB) * 8 * NV * NB + sizeof(TensorTables) + 8 * 32;
+  static constexpr size_t GRAD_SMEM = size_t(EPB) * 8 * 2 * DIM * NV * NB + sizeof(TensorTables);
+  static constexpr size_t TRACE_SMEM = sizeof(TensorTables);
 };
 
 template <int DIM, int N>

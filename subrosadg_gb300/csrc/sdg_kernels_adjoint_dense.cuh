@@ -34,6 +34,7 @@ struct DenseAdjShape {
   static constexpr int VJP_PER = NV * NB + NV * NQ;
   static constexpr size_t JVP_SMEM = (size_t(EPB) * JVP_PER + TABLES + NQ * NB) * 8;
   static constexpr size_t VJP_SMEM = (size_t(EPB) * VJP_PER + TABLES + NQ * NB) * 8;
+  static constexpr size_t TRACE_SMEM = size_t(TABLES + NQ * NB) * 8;
 };
 
 // Geometry of point q of element e: contravariant metric, 1/|J| at the point; the M^-1 of the element and its

@@ -53,7 +53,7 @@ struct AdjointTileKernels {
   const void* vjpGradient = nullptr;  // (AdjArgs), Navier-Stokes
   const void* vjpTrace = nullptr;     // (AdjArgs)
   int epb = 0, threads = 0;
-  size_t jvpSmem = 0, vjpSmem = 0;
+  size_t jvpSmem = 0, volSmem = 0, gradSmem = 0, traceSmem = 0;  // dynamic shared memory of each kernel
   bool valid() const { return jvpStage && vjpVolume && vjpTrace; }
 };
 // Face kernels depend on (dim, flux, viscous); tensor tile kernels on (dim, nodes per direction, viscous, BR2,

@@ -16,7 +16,8 @@ void tileOf(AdjointTileKernels& k, bool br2, bool gen) {
   k.vjpGradient = br2 ? reinterpret_cast<const void*>(&vjpGradientBR2Kernel<DIM, N>)
                       : reinterpret_cast<const void*>(&vjpGradientKernel<DIM, N>);
   k.vjpTrace = reinterpret_cast<const void*>(&vjpTraceKernel<DIM, N>);
-  k.epb = A::EPB; k.threads = A::THREADS; k.jvpSmem = A::JVP_SMEM; k.vjpSmem = A::VJP_SMEM;
+  k.epb = A::EPB; k.threads = A::THREADS; k.jvpSmem = A::JVP_SMEM;
+  k.volSmem = A::VOL_SMEM; k.gradSmem = A::GRAD_SMEM; k.traceSmem = A::TRACE_SMEM;
 }
 // Bilinear quadrangles (per-node metric), the Euler equations.
 template <int N>
@@ -26,7 +27,8 @@ void bilinearOf(AdjointTileKernels& k, bool gen) {
   k.vjpVolume = gen ? reinterpret_cast<const void*>(&vjpVolumeKernel<2, N, false, true, false>)
                     : reinterpret_cast<const void*>(&vjpVolumeKernel<2, N, false, false, false>);
   k.vjpTrace = reinterpret_cast<const void*>(&vjpTraceKernel<2, N>);
-  k.epb = A::EPB; k.threads = A::THREADS; k.jvpSmem = A::JVP_SMEM; k.vjpSmem = A::VJP_SMEM;
+  k.epb = A::EPB; k.threads = A::THREADS; k.jvpSmem = A::JVP_SMEM;
+  k.volSmem = A::VOL_SMEM; k.gradSmem = A::GRAD_SMEM; k.traceSmem = A::TRACE_SMEM;
 }
 }  // namespace
 

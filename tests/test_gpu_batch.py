@@ -39,10 +39,19 @@ MIXED = {
     "ns-channel-walls-p2": lambda: cases.channel_case(p=2, flux=sdg.HLLC, n=4, viscous=sdg.BR2, mu=0.01,
                                                       conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW,
                                                                   sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "euler-line-p3-hllc": lambda: cases.density_wave_1d_case(n=20, p=3),
+    "ns-line-walls-p2-br2": lambda: _ns(cases.sod_1d_case(n=30, p=2, av=False, smooth=0.05, dt=1e-5,
+                                                          conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.RIEMANN_FARFIELD)),
+                                        sdg.BR2, 0.01),
 }
 
 
-@pytest.mark.parametrize("name", ["euler-hybrid-p4-lf", "ns-hex-p3-br1-roe", "ns-tri-p1-br1"])
+def _ns(case, viscous, mu):
+    mesh, cfg, prim, bprim, dt, steps = case
+    return (mesh, cases.ns_config(cfg.polynomial_order, cfg.convective_flux, viscous, mu), prim, bprim, dt, steps)
+
+
+@pytest.mark.parametrize("name", ["euler-hybrid-p4-lf", "ns-hex-p3-br1-roe", "ns-tri-p1-br1", "ns-line-walls-p2-br2"])
 def test_graph_replay_equals_plain_launches(name):
     a, dt, steps = make(MIXED[name]())
     b, _, _ = make(MIXED[name]())
