@@ -5,9 +5,9 @@
 //   <lambda, JVP(dU)> = <VJP(lambda), dU>
 // holds to round-off, for one residual and for whole trajectories.  Scope: compressible or incompressible
 // Euler on every element block (tensor blocks: lines, quadrangles -- affine or bilinear --, hexahedra; dense
-// blocks: triangles and first-order quadrangles), Navier-Stokes with BR1 or BR2 on affine tensor blocks, the
-// Boussinesq source, with or without boundary faces; other configurations (Navier-Stokes on dense or bilinear
-// blocks, artificial viscosity) return SDG_ERR_UNSUPPORTED.  The cotangents of the point-layout API are mapped
+// blocks: triangles and first-order quadrangles), Navier-Stokes with BR1 or BR2 on affine elements of both
+// kinds, the Boussinesq source, with or without boundary faces; other configurations (Navier-Stokes on
+// bilinear quadrangles, artificial viscosity) return SDG_ERR_UNSUPPORTED.  The cotangents of the point-layout API are mapped
 // by the transposes of the point <-> state conversions (dense blocks: Phi^T in, P^T out, P the projection).
 //
 // Trajectories: the tangent runs stage by stage beside the forward state.  The adjoint stores the state
@@ -120,8 +120,8 @@ AdjointState* adjoint(sdg_handle* h) {
   if (!h->hasState) throw Failure(SDG_ERR_STATE, "no state");
   if (h->adj) return h->adj;
   for (const DevBlock& B : h->blocks)
-    if (h->ns && (B.kind != kTensor || !B.affine))
-      throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes derivatives need affine tensor blocks (lines, quadrangles P>=2, hexahedra)");
+    if (h->ns && !B.affine)
+      throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes derivatives need affine elements (bilinear quadrangles are not built)");
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   const bool gen = h->ph.incomp || h->ph.source;
@@ -132,7 +132,7 @@ AdjointState* adjoint(sdg_handle* h) {
     if (B.kind == kTensor)
       adjointTileKernels(h->dim, B.n, h->ns, h->ns && h->cfg.viscous_flux == SDG_VISCOUS_BR2, gen, B.affine != 0, t);
     else
-      adjointDenseKernels(B.type, B.p, B.affine != 0, gen, t);
+      adjointDenseKernels(B.type, B.p, B.affine != 0, gen, h->ns, h->cfg.viscous_flux == SDG_VISCOUS_BR2, t);
     if (!t.valid() || (h->ns && !t.vjpGradient))
       throw Failure(SDG_ERR_UNSUPPORTED, "no derivative kernels for this element block");
     A->bk.push_back(t);
@@ -185,7 +185,7 @@ AdjArgs baseArgs(sdg_handle* h, const DevBlock* B, const double* U) {
   const AdjointState* A = h->adj;
   const double* grad = A->curGrad ? A->curGrad : h->grad;
   if (B) {
-    a.u = U + B->stateOffset; a.geom = B->geom; a.tables = B->tables;
+    a.u = U + B->stateOffset; a.geom = B->geom; a.tables = B->tables; a.fmetric = B->fmetric;
     a.grad = h->ns ? grad + B->gradOffset : nullptr;
     a.ne = B->ne; a.faceBase = B->faceBase;
   }
@@ -259,8 +259,13 @@ void gradientOf(sdg_handle* h, const double* u, double* face, double* other, dou
   }
   for (DevBlock& B : h->blocks) {
     Rec r = gradRec(h, B, 0);
-    r.ga.u = u + B.stateOffset; r.ga.face = face; r.ga.faceOther = other;
-    r.ga.grad = grad + B.gradOffset; r.ga.faceGrad = faceGrad;
+    if (r.kind == kRecGradDense) {  // dense blocks carry their gradient pass in the dense argument block
+      r.da.u = u + B.stateOffset; r.da.face = face; r.da.faceOther = other;
+      r.da.grad = grad + B.gradOffset; r.da.faceGrad = faceGrad;
+    } else {
+      r.ga.u = u + B.stateOffset; r.ga.face = face; r.ga.faceOther = other;
+      r.ga.grad = grad + B.gradOffset; r.ga.faceGrad = faceGrad;
+    }
     recs.push_back(r);
   }
   runRecs(h, recs, h->stream);

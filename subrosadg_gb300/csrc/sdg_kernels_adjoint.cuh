@@ -659,6 +659,7 @@ struct AdjArgs {
   const double* ghost;
   double* lamGhost;
   double ghostScale;
+  const double* fmetric;  // dense blocks: outward n|J_f| of each local face [e][NF][d]
 };
 
 // ---- surface force (the reference's View force, VariableConvertor.cpp:883-906, Paraview.cpp:99-106) ------

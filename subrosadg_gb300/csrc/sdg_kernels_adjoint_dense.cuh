@@ -1,7 +1,8 @@
 // Tangent-linear (JVP) and adjoint (VJP) element kernels of dense (modal) blocks -- triangles and first-order
-// quadrangles, affine or bilinear -- for the Euler equations (compressible or incompressible, with the
-// Boussinesq source).  The face kernels of sdg_kernels_adjoint.cuh serve these blocks unchanged: they work on
-// the face slots, whose layout [slot][nv][nfq] is the same for every block kind.
+// quadrangles -- for the Euler equations (compressible or incompressible, with the Boussinesq source; affine or
+// bilinear elements) and for Navier-Stokes BR1 / BR2 (affine elements).  The face kernels of
+// sdg_kernels_adjoint.cuh serve these blocks unchanged: they work on the face slots, whose layout
+// [slot][nv][nfq] (gradient traces [slot][nv*2][nfq]) is the same for every block kind.
 //
 // Forward residual of a dense block (denseStageTile, SpatialDiscrete.cpp:194-266,1016-1032):
 //   U_q = Phi U                           values at the volume points        (linear)
@@ -13,6 +14,8 @@
 // transposed sequence:
 //   lamR = s M^-T lam;  lamQ_b(q) = dPhiw_b lamR;  lamH(fj) = -Phifw_fj lamR (the flux slots)
 //   lamU_q = sum_b (dQ_b/dU)^T lamQ_b (+ lamS dS/dU),  lamU = Phi^T lamU_q;   then lamU += Phi_f^T lamTr.
+// Navier-Stokes adds the viscous fluxes of the modal gradient w at the points (Q_b depends on U_q and
+// G_q = Phi w: lamw = Phi^T lamG_q) and the transposed gradient pass (vjpDenseGradientKernel).
 #pragma once
 #include "sdg_kernels_adjoint.cuh"
 #include "sdg_kernels_dense.cuh"
@@ -30,11 +33,14 @@ struct DenseAdjShape {
   static constexpr int PHIW = NQ * NB * 3 + NFP * NB * 2 + NB * NB + 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
   // tangent: u, du | tangent flux slots | tangent fluxes [2][NV][NQ] | tangent source [NQ] | tangent residual
   static constexpr int JVP_PER = 2 * USTRIDE + FSTRIDE + 2 * NV * NQ + NQ + NV * NB;
-  // adjoint: lamR [NV][NB] | point cotangents [NV][NQ]
-  static constexpr int VJP_PER = NV * NB + NV * NQ;
+  // adjoint: lamR [NV][NB] | point cotangents [NV][NQ] | Navier-Stokes: point gradient cotangents [NV*2][NQ]
+  static constexpr int VJP_PER = NV * NB + NV * NQ + 2 * NV * NQ;
   static constexpr size_t JVP_SMEM = (size_t(EPB) * JVP_PER + TABLES + NQ * NB) * 8;
-  static constexpr size_t VJP_SMEM = (size_t(EPB) * VJP_PER + TABLES + NQ * NB) * 8;
+  static constexpr size_t VJP_SMEM = (size_t(EPB) * VJP_PER + TABLES + NQ * NB) * 8 + 8 * 32;
   static constexpr size_t TRACE_SMEM = size_t(TABLES + NQ * NB) * 8;
+  // gradient transpose (affine): lamTot and lamJmp [NV*2][NB] | phif | dmod | emod | lmod
+  static constexpr int GOPS = NFP * NB + 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
+  static constexpr size_t GRAD_SMEM = (size_t(EPB) * 2 * 2 * NV * NB + GOPS) * 8;
 };
 
 // Geometry of point q of element e: contravariant metric, 1/|J| at the point; the M^-1 of the element and its
@@ -54,7 +60,7 @@ __device__ __forceinline__ void loadDenseAdjTables(double* tab, const double* sr
 
 // Tangent element kernel of a dense block: dR at the stage input u in direction du (face tangents in dflux), the
 // rate tangent and / or the RK combination dout = c0 dbase + c1 du + c2dt s M^-1 dR with the traces of dout.
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
 __global__ void __launch_bounds__(256) jvpDenseStageKernel(AdjArgs a, Phys ph) {
   using S = DenseAdjShape<NB, NQ, NFQ, NF>;
   constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB, GS = AFFINE ? 5 : NQ * 5 + NB * NB;
@@ -99,12 +105,25 @@ __global__ void __launch_bounds__(256) jvpDenseStageKernel(AdjArgs a, Phys ph) {
     }
     const double* g = densePointGeom<NB, NQ, AFFINE>(a.geom, e, q);
     const double ja[2][2] = {{g[0], g[1]}, {g[2], g[3]}};
-    D1 gg[1], Q[2][NV], Qv[2][NV];
-    nodeFlux<2, false>(U, gg, ja, ph, Q, Qv);
+    D1 gg[VISC ? NV * 2 : 1], Q[2][NV], Qv[2][NV];
+    if constexpr (VISC) {  // the gradient at the point from the modal gradient coefficients and their tangent
+#pragma unroll
+      for (int c = 0; c < NV * 2; ++c) {
+        double x = 0.0, dx = 0.0;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+          x = fma(phi[q * NB + b], a.grad[(e * NV * 2 + c) * NB + b], x);
+          dx = fma(phi[q * NB + b], a.dgrad[(e * NV * 2 + c) * NB + b], dx);
+        }
+        gg[c].v = x; gg[c].d[0] = dx;
+      }
+    }
+    nodeFlux<2, VISC>(U, gg, ja, ph, Q, Qv);
+    const double mscale = VISC && ph.mu > 0.0 ? a.dmu / ph.mu : 0.0;
 #pragma unroll
     for (int b = 0; b < 2; ++b)
 #pragma unroll
-      for (int v = 0; v < NV; ++v) sQ[((le * 2 + b) * NV + v) * NQ + q] = Q[b][v].d[0];
+      for (int v = 0; v < NV; ++v) sQ[((le * 2 + b) * NV + v) * NQ + q] = fma(mscale, Qv[b][v].v, Q[b][v].d[0]);
     if (ph.source) {
       State<2, D1> st;
       makeState<2>(st, U, ph);
@@ -172,14 +191,16 @@ __global__ void __launch_bounds__(256) jvpDenseStageKernel(AdjArgs a, Phys ph) {
 
 // Adjoint of the volume and lift terms of a dense block: lamU (state layout) and lamH (the flux slots of the
 // block's faces) from lam, the cotangent of du/dt.
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool GEN>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool GEN, bool VISC>
 __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) {
   using S = DenseAdjShape<NB, NQ, NFQ, NF>;
-  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB, GS = AFFINE ? 5 : NQ * 5 + NB * NB;
+  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB, GS = AFFINE ? 5 : NQ * 5 + NB * NB, NR = NV * 2;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* sL = reinterpret_cast<double*>(smem_raw);  // [EPB][NV][NB] lamR = s M^-T lam
   double* sP = sL + EPB * NV * NB;                   // [EPB][NV][NQ] point cotangents of U_q
-  double* tab = sP + EPB * NV * NQ;
+  double* sPG = sP + EPB * NV * NQ;                  // [EPB][NR][NQ] point cotangents of G_q (Navier-Stokes)
+  double* tab = sPG + EPB * NR * NQ;
+  double* sRed = tab + S::TABLES + NQ * NB;          // one double per warp
   const double* phi = tab;
   const double* dphiw = phi + NQ * NB;
   const double* phifw = dphiw + NQ * 2 * NB + NFP * NB;
@@ -190,6 +211,7 @@ __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) 
   const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
   loadDenseAdjTables<NB, NQ, NFQ, NF>(tab, a.tables);
   __syncthreads();
+  double mupart = 0.0;
   for (int idx = tid; idx < ecount * NB; idx += blockDim.x) {
     const int le = idx / NB, k = idx - le * NB;
     const int64_t e = e0 + le;
@@ -227,7 +249,17 @@ __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) 
     }
     const double* g = densePointGeom<NB, NQ, AFFINE>(a.geom, e, q);
     const double ja[2][2] = {{g[0], g[1]}, {g[2], g[3]}};
-    double lu[NV];
+    double lu[NV], gg[VISC ? NR : 1], lg[VISC ? NR : 1];
+    if constexpr (VISC) {
+#pragma unroll
+      for (int c = 0; c < NR; ++c) {
+        double x = 0.0;
+#pragma unroll
+        for (int b = 0; b < NB; ++b) x = fma(phi[q * NB + b], a.grad[(e * NR + c) * NB + b], x);
+        gg[c] = x;
+        lg[c] = 0.0;
+      }
+    }
     if constexpr (GEN) {
       // the source enters R as w_q |J|_q S(U_q) phi: its cotangent is |J|_q (phiw^T lamR)_q on the last momentum
       double lamS = 0.0;
@@ -236,15 +268,40 @@ __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) 
         for (int i = 0; i < NB; ++i) lamS = fma(phiw[q * NB + i], sL[(le * NV + 2) * NB + i], lamS);
         lamS /= g[4];
       }
-      double gg[1], lg[1];
-      volumeReverseGeneric<2, false>(U, gg, ja, lq, lamS, ph, lu, lg);
+      mupart += volumeReverseGeneric<2, VISC>(U, gg, ja, lq, lamS, ph, lu, lg);
     } else {
       eulerVolumeReverse<2>(U, ja, lq, ph, lu);
+      if constexpr (VISC) {
+        // lamF[c][v] = cotangent of Fv_c(v): Q_b contains -sum_c ja[b][c] Fv_c
+        double lamF[2][NV];
+#pragma unroll
+        for (int c = 0; c < 2; ++c)
+#pragma unroll
+          for (int v = 0; v < NV; ++v) lamF[c][v] = -fma(ja[0][c], lq[0][v], ja[1][c] * lq[1][v]);
+        mupart += viscousReverse<2>(U, gg, lamF, ph, lu, lg);
+      }
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) sP[(le * NV + v) * NQ + q] = lu[v];
+    if constexpr (VISC) {
+#pragma unroll
+      for (int c = 0; c < NR; ++c) sPG[(le * NR + c) * NQ + q] = lg[c];
+    }
   }
+  if constexpr (VISC) blockSum(mupart, a.muPart + blockIdx.x, sRed);
   __syncthreads();
+  if constexpr (VISC) {  // lamw = Phi^T lamG_q
+    for (int idx = tid; idx < ecount * NB; idx += blockDim.x) {
+      const int le = idx / NB, i = idx - le * NB;
+      const int64_t e = e0 + le;
+#pragma unroll
+      for (int c = 0; c < NR; ++c) {
+        double x = 0.0;
+        for (int q = 0; q < NQ; ++q) x = fma(phi[q * NB + i], sPG[(le * NR + c) * NQ + q], x);
+        a.lamG[(e * NR + c) * NB + i] = x;
+      }
+    }
+  }
   for (int idx = tid; idx < ecount * NB; idx += blockDim.x) {
     const int le = idx / NB, i = idx - le * NB;
     const int64_t e = e0 + le;
@@ -267,6 +324,93 @@ __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) 
       for (int i = 0; i < NB; ++i) s = fma(-phifw[fj * NB + i], sL[(le * NV + v) * NB + i], s);
       out[v * NFQ] = s;
     }
+  }
+}
+
+// Transposed gradient pass of an affine dense block (denseGradientAffineTile).  Forward, per element:
+//   tot_k = -sum_b ja[b][k] (D_b u) + sum_f nF_f[k] E_f O_f,   jmp_k = sum_f nF_f[k] E_f (O_f - S_f)/2
+//   grad_k = jinv tot_k;  BR1: w_k = grad_k;  BR2: w_k = jinv (tot_k - jmp_k)
+//   gradient trace at (f, j): (Phi_f w_k)_j (+ BR2: jinv nF_f[k] (L_f (O_f - S_f)/2)_j)
+// with S the own traces and O the neighbour traces.  Transposed, with lamVol = Phi_f^T lamTg:
+//   lamTot = jinv (lamG + lamVol),  lamJmp = -jinv lamVol (BR2),
+//   lamU -= sum_b D_b^T (sum_k ja[b][k] lamTot_k),
+//   lamO_f = E_f^T (nF_f . lamTot);  BR2: lamD_f = E_f^T (nF_f . lamJmp) + jinv L_f^T (nF_f . lamTg_f),
+//   lamUp = lamO + lamD/2 (the neighbour traces), lamTr += -lamD/2 (the own traces).
+template <int NB, int NQ, int NFQ, int NF, bool BR2>
+__global__ void __launch_bounds__(256) vjpDenseGradientKernel(AdjArgs a) {
+  using S = DenseAdjShape<NB, NQ, NFQ, NF>;
+  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB, NR = NV * 2;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* sT = reinterpret_cast<double*>(smem_raw);  // [EPB][NR][NB] lamTot
+  double* sJ = sT + EPB * NR * NB;                   // [EPB][NR][NB] lamJmp (BR2)
+  double* tab = sJ + EPB * NR * NB;
+  const double* phif = tab;                          // [NFP][NB]
+  const double* dmod = phif + NFP * NB;              // [2][NB][NB]
+  const double* emod = dmod + 2 * NB * NB;           // [NF][NB][NFQ]
+  const double* lmod = emod + NF * NB * NFQ;         // [NF][NFQ][NFQ]
+  const int tid = threadIdx.x;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  {
+    constexpr int OFF_PHIF = NQ * NB * 3, OFF_DMOD = NQ * NB * 3 + NFP * NB * 2 + NB * NB;
+    constexpr int NOPS = 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
+    for (int k = tid; k < NFP * NB; k += blockDim.x) tab[k] = a.tables[OFF_PHIF + k];
+    for (int k = tid; k < NOPS; k += blockDim.x) tab[NFP * NB + k] = a.tables[OFF_DMOD + k];
+  }
+  __syncthreads();
+  for (int idx = tid; idx < ecount * NR * NB; idx += blockDim.x) {
+    const int le = idx / (NR * NB), r = idx - le * NR * NB;
+    const int c = r / NB, i = r - c * NB;
+    const int64_t e = e0 + le;
+    const double jinv = a.geom[e * 5 + 4];
+    double vol = 0.0;
+    for (int fj = 0; fj < NFP; ++fj) {
+      const int f = fj / NFQ, j = fj - f * NFQ;
+      vol = fma(phif[fj * NB + i], a.lamTg[(a.faceBase + e * NF + f) * NR * NFQ + c * NFQ + j], vol);
+    }
+    sT[(le * NR + c) * NB + i] = jinv * (a.lamG[(e * NR + c) * NB + i] + vol);
+    if constexpr (BR2) sJ[(le * NR + c) * NB + i] = -jinv * vol;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < ecount * NV * NB; idx += blockDim.x) {
+    const int le = idx / (NV * NB), r = idx - le * NV * NB;
+    const int v = r / NB, m = r - v * NB;
+    const int64_t e = e0 + le;
+    const double* g = a.geom + e * 5;
+    double acc = 0.0;
+    for (int i = 0; i < NB; ++i) {
+      const double t0 = sT[(le * NR + v * 2 + 0) * NB + i], t1 = sT[(le * NR + v * 2 + 1) * NB + i];
+      const double d0 = fma(g[0], t0, g[1] * t1), d1 = fma(g[2], t0, g[3] * t1);  // sum_k ja[b][k] lamTot_k
+      acc = fma(dmod[i * NB + m], d0, acc);
+      acc = fma(dmod[(NB + i) * NB + m], d1, acc);
+    }
+    a.lamU[e * S::USTRIDE + v * NB + m] -= acc;
+  }
+  for (int idx = tid; idx < ecount * NFP * NV; idx += blockDim.x) {
+    const int le = idx / (NFP * NV), r = idx - le * NFP * NV;
+    const int fj = r / NV, v = r - fj * NV;
+    const int f = fj / NFQ, j = fj - f * NFQ;
+    const int64_t e = e0 + le;
+    const double jinv = a.geom[e * 5 + 4];
+    const double n0 = a.fmetric[(e * NF + f) * 2 + 0], n1 = a.fmetric[(e * NF + f) * 2 + 1];
+    double lo = 0.0, ld = 0.0;
+    for (int i = 0; i < NB; ++i) {
+      const double E = emod[(f * NB + i) * NFQ + j];
+      lo = fma(E, fma(n0, sT[(le * NR + v * 2 + 0) * NB + i], n1 * sT[(le * NR + v * 2 + 1) * NB + i]), lo);
+      if constexpr (BR2)
+        ld = fma(E, fma(n0, sJ[(le * NR + v * 2 + 0) * NB + i], n1 * sJ[(le * NR + v * 2 + 1) * NB + i]), ld);
+    }
+    const int64_t slot = (a.faceBase + e * NF + f);
+    if constexpr (BR2) {
+      const double* tg = a.lamTg + slot * NR * NFQ;
+      double lift = 0.0;
+#pragma unroll
+      for (int jj = 0; jj < NFQ; ++jj)
+        lift = fma(lmod[(f * NFQ + jj) * NFQ + j], fma(n0, tg[(v * 2 + 0) * NFQ + jj], n1 * tg[(v * 2 + 1) * NFQ + jj]), lift);
+      ld = fma(jinv, lift, ld);
+      a.lamTr[slot * NV * NFQ + v * NFQ + j] += -0.5 * ld;
+    }
+    a.lamUp[slot * NV * NFQ + v * NFQ + j] = fma(0.5, ld, lo);
   }
 }
 

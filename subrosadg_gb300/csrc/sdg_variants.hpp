@@ -57,12 +57,12 @@ struct AdjointTileKernels {
   bool valid() const { return jvpStage && vjpVolume && vjpTrace; }
 };
 // Face kernels depend on (dim, flux, viscous); tensor tile kernels on (dim, nodes per direction, viscous, BR2,
-// affine: bilinear quadrangles for the Euler equations only); dense tile kernels on (type, order, affine),
-// the Euler equations.  gen: the dual-number transposes (incompressible model, Boussinesq source) instead of
-// the hand-written ones.  Unsupported combinations leave the kernels null.
+// affine: bilinear quadrangles for the Euler equations only); dense tile kernels on (type, order, affine,
+// viscous, BR2: Navier-Stokes on affine elements).  gen: the dual-number transposes (incompressible model,
+// Boussinesq source) instead of the hand-written ones.  Unsupported combinations leave the kernels null.
 void adjointFaceKernels(int dim, int flux, bool visc, bool gen, AdjointKernels& k);
 void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, bool affine, AdjointTileKernels& k);
-void adjointDenseKernels(int type, int p, bool affine, bool gen, AdjointTileKernels& k);
+void adjointDenseKernels(int type, int p, bool affine, bool gen, bool visc, bool br2, AdjointTileKernels& k);
 
 // Largest tile size the kernels are compiled for (their __launch_bounds__).
 constexpr int kMaxThreads = 512;

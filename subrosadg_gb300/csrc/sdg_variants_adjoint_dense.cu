@@ -1,26 +1,37 @@
-// Tangent-linear and adjoint element kernels of dense blocks (triangles, first-order quadrangles), the Euler
-// equations: the one translation unit that instantiates them.
+// Tangent-linear and adjoint element kernels of dense blocks (triangles, first-order quadrangles): the Euler
+// equations on every element, Navier-Stokes BR1 / BR2 on affine ones; the one translation unit that instantiates
+// them.
 #include "sdg_kernels_adjoint_dense.cuh"
 #include "sdg_variants.hpp"
 
 namespace sdg {
 
 namespace {
-template <int NB, int NQ, int NFQ, int NF, bool AFF>
-void denseOf(AdjointTileKernels& k, bool gen) {
+template <int NB, int NQ, int NFQ, int NF, bool AFF, bool VISC>
+void denseOf(AdjointTileKernels& k, bool gen, bool br2) {
   using S = DenseAdjShape<NB, NQ, NFQ, NF>;
-  k.jvpStage = reinterpret_cast<const void*>(&jvpDenseStageKernel<NB, NQ, NFQ, NF, AFF>);
-  k.vjpVolume = gen ? reinterpret_cast<const void*>(&vjpDenseVolumeKernel<NB, NQ, NFQ, NF, AFF, true>)
-                    : reinterpret_cast<const void*>(&vjpDenseVolumeKernel<NB, NQ, NFQ, NF, AFF, false>);
+  k.jvpStage = reinterpret_cast<const void*>(&jvpDenseStageKernel<NB, NQ, NFQ, NF, AFF, VISC>);
+  k.vjpVolume = gen ? reinterpret_cast<const void*>(&vjpDenseVolumeKernel<NB, NQ, NFQ, NF, AFF, true, VISC>)
+                    : reinterpret_cast<const void*>(&vjpDenseVolumeKernel<NB, NQ, NFQ, NF, AFF, false, VISC>);
   k.vjpTrace = reinterpret_cast<const void*>(&vjpDenseTraceKernel<NB, NQ, NFQ, NF>);
+  if constexpr (VISC) {
+    k.vjpGradient = br2 ? reinterpret_cast<const void*>(&vjpDenseGradientKernel<NB, NQ, NFQ, NF, true>)
+                        : reinterpret_cast<const void*>(&vjpDenseGradientKernel<NB, NQ, NFQ, NF, false>);
+    k.gradSmem = S::GRAD_SMEM;
+  }
   k.epb = S::EPB; k.threads = S::THREADS; k.jvpSmem = S::JVP_SMEM; k.volSmem = S::VJP_SMEM;
   k.traceSmem = S::TRACE_SMEM;
 }
+template <int NB, int NQ, int NFQ, int NF, bool AFF>
+void denseOf(AdjointTileKernels& k, bool gen, bool visc, bool br2) {
+  if (!visc) { denseOf<NB, NQ, NFQ, NF, AFF, false>(k, gen, false); return; }
+  if constexpr (AFF) denseOf<NB, NQ, NFQ, NF, AFF, true>(k, gen, br2);  // Navier-Stokes: affine elements
+}
 }  // namespace
 
-void adjointDenseKernels(int type, int p, bool affine, bool gen, AdjointTileKernels& k) {
+void adjointDenseKernels(int type, int p, bool affine, bool gen, bool visc, bool br2, AdjointTileKernels& k) {
 #define SDG_AD(T, P, NB, NQ, NFQ, NF, AFF) \
-  if (type == T && p == P && affine == AFF) { denseOf<NB, NQ, NFQ, NF, AFF>(k, gen); return; }
+  if (type == T && p == P && affine == AFF) { denseOf<NB, NQ, NFQ, NF, AFF>(k, gen, visc, br2); return; }
   SDG_DENSE_CASES(SDG_AD)
 #undef SDG_AD
 }
