@@ -12,6 +12,8 @@ from __future__ import annotations
 
 import ctypes
 import math
+import os
+import shutil
 from ctypes import POINTER, byref, c_double, c_int32, c_int64, c_void_p
 
 import numpy as np
@@ -447,11 +449,20 @@ class Batch:
         return s.value
 
 
+# InitialConditionEnum (src/Utils/Enum.cpp): the driver's function, a given raw-binary file, or the last written
+# step of the same run (raw/{prefix}_{iteration_start}.zst)
+INITIAL_FUNCTION, INITIAL_SPECIFIC_FILE, INITIAL_LAST_STEP = 0, 1, 2
+
+
 class System:
-    """Mirror of SubrosaDG's System<SimulationControl> (src/Utils/SystemControl.cpp:42-236)."""
+    """Mirror of SubrosaDG's System<SimulationControl> (src/Utils/SystemControl.cpp:42-236): setup, then solve()
+    with the reference's outputs -- raw/{prefix}_{i}.zst every io_interval steps (and step 0) and error.txt with
+    one line of relative errors per step (SystemControl.cpp:159-195, View/CommandLine.cpp:95-150,
+    View/IOControl.cpp:318-337)."""
 
     def __init__(self, dimension, polynomial_order, equation=_abi.EULER, convective_flux=_abi.HLLC,
-                 viscous_flux=_abi.VISCOUS_NONE, time_integration=_abi.SSPRK3, device=0):
+                 viscous_flux=_abi.VISCOUS_NONE, time_integration=_abi.SSPRK3, device=0,
+                 initial_condition_kind=INITIAL_FUNCTION):
         self.dimension = dimension
         self.cfg = dict(polynomial_order=polynomial_order, equation=equation, convective_flux=convective_flux,
                         viscous_flux=viscous_flux, time_integration=time_integration)
@@ -463,6 +474,12 @@ class System:
         self.solver = None
         self.initial_condition = None   # callable(coords[n,3]) -> primitive[n, d+2]
         self.boundary_condition = None  # callable(coords[n,3], physical[n]) -> primitive[n, d+2]
+        self.initial_condition_kind = initial_condition_kind
+        self.initial_condition_file = None
+        self.initial_condition_lower_order = False
+        self.output_directory = None    # setViewConfig: raw/ files and error.txt (no outputs when unset)
+        self.output_file_name_prefix = ""
+        self.io_interval = 0
         self.error_history = []
 
     def setMesh(self, mesh: Mesh):
@@ -491,9 +508,23 @@ class System:
         self.cfg.update(shock_capturing=_abi.ARTIFICIAL_VISCOSITY, empirical_tolerance=empirical_tolerance,
                         artificial_viscosity_factor=artificial_viscosity_factor)
 
+    def addInitialCondition(self, raw_binary_path, lower_order=False):
+        """InitialConditionEnum::SpecificFile (SystemControl.cpp:70-74): the state of a raw-binary file (of the
+        order below with lower_order, InitialCondition.cpp:58-80)."""
+        self.initial_condition_kind = INITIAL_SPECIFIC_FILE
+        self.initial_condition_file = raw_binary_path
+        self.initial_condition_lower_order = lower_order
+
     def setTimeIntegration(self, cfl, iteration_range):
         self.cfl = cfl
         self.iteration_start, self.iteration_end = iteration_range
+
+    def setViewConfig(self, output_directory, output_file_name_prefix, io_interval=-1):
+        """Output directory, file prefix and raw-binary interval (SystemControl.cpp:124-140; -1 or 0: the last
+        step only, where the reference asks on stdin for 0)."""
+        self.output_directory = os.fspath(output_directory)
+        self.output_file_name_prefix = output_file_name_prefix
+        self.io_interval = self.iteration_end if io_interval in (0, -1) else int(io_interval)
 
     def setDeltaTime(self, dt):
         self.delta_time = dt
@@ -501,20 +532,74 @@ class System:
     def synchronize(self):
         self.solver = GpuSolver(self.mesh, make_config(**self.cfg), self.device)
 
-    def solve(self):
+    def _raw_path(self, step):
+        return os.path.join(self.output_directory, "raw", f"{self.output_file_name_prefix}_{step}.zst")
+
+    def _variable_list(self):
+        """error.txt header (View/CommandLine.cpp:70-93)."""
+        d = self.dimension
+        incomp = self.cfg["equation"] in (_abi.INCOMPRESSIBLE_EULER, _abi.INCOMPRESSIBLE_NAVIER_STOKES)
+        names = ["Time", "rho"] + ["rho*" + c for c in "uvw"[:d]] + ["rho*e" if incomp else "rho*E"]
+        return "".join(f"|{n:^13}" for n in names) + "|"
+
+    @staticmethod
+    def _line(time_value, error):
+        """One error.txt line (View/CommandLine.cpp:95-106): {:^13.5e} fields."""
+        return "".join(f"|{x:^13.5e}" for x in [time_value, *error]) + "|"
+
+    def solve(self, delete_dir=True):
         s = self.solver
-        pts = s.volume_points()
-        s.initialize_primitive(self.initial_condition(pts[:, : self.dimension]))
+        last_step = self.initial_condition_kind == INITIAL_LAST_STEP
+        error_lines = None
+        if self.output_directory is not None:  # View::initializeSolverFinout (IOControl.cpp:318-335)
+            raw = os.path.join(self.output_directory, "raw")
+            if delete_dir and not last_step and os.path.isdir(raw):
+                shutil.rmtree(raw)
+            os.makedirs(raw, exist_ok=True)
+            error_path = os.path.join(self.output_directory, "error.txt")
+            if last_step and os.path.exists(error_path):  # keep the header, the zero line and the steps done
+                with open(error_path) as f:
+                    error_lines = f.read().splitlines()[: self.iteration_start + 2]
+            else:
+                error_lines = []
+        if self.initial_condition_kind == INITIAL_SPECIFIC_FILE:
+            s.read_raw_binary(self.initial_condition_file, lower_order=self.initial_condition_lower_order)
+        elif last_step:
+            s.read_raw_binary(self._raw_path(self.iteration_start))
+        else:
+            pts = s.volume_points()
+            s.initialize_primitive(self.initial_condition(pts[:, : self.dimension]))
         if s.counts.boundary_face_count:
             bpts, phys = s.boundary_points()
             nfq = s.counts.face_point_count
             s.set_boundary_primitive(self.boundary_condition(bpts[:, : self.dimension], np.repeat(phys, nfq)))
         if self.delta_time == 0.0:
             self.delta_time = s.calculateDeltaTime(self.cfl)
-        for i in range(self.iteration_start + 1, self.iteration_end + 1):
-            err = s.stepSolver(self.delta_time).copy()
-            self.error_history.append((i * self.delta_time, err))
-            if np.isnan(err).all():  # src/Utils/SystemControl.cpp:185-191
-                self.iteration_end = i
-                break
+        error_file = None
+        if error_lines is not None:  # error.txt is written line by line as the reference's error_finout is
+            error_file = open(os.path.join(self.output_directory, "error.txt"), "w")
+            for line in error_lines:
+                error_file.write(line + "\n")
+            if not last_step:
+                s.writeRawBinary(self._raw_path(0))
+                error_file.write(self._variable_list() + "\n" + self._line(0.0, np.zeros(s.nv)) + "\n")
+        io_interval = self.io_interval or self.iteration_end
+        try:
+            for i in range(self.iteration_start + 1, self.iteration_end + 1):
+                err = s.stepSolver(self.delta_time).copy()
+                self.error_history.append((i * self.delta_time, err))
+                if error_file is not None:
+                    if i % io_interval == 0:
+                        s.writeRawBinary(self._raw_path(i))
+                    error_file.write(self._line(i * self.delta_time, err) + "\n")
+                    error_file.flush()
+                if np.isnan(err).all():  # src/Utils/SystemControl.cpp:185-191
+                    if io_interval == self.iteration_end:
+                        io_interval = i
+                    self.iteration_end = i
+                    break
+        finally:
+            if error_file is not None:
+                error_file.close()
+        self.io_interval = io_interval
         return self.error_history
