@@ -1192,7 +1192,7 @@ struct AdjShape {
   //   gradient: t_b [DIM][NV][NB] (BR2: and v_b) | tables
   //   trace:    tables
   static constexpr size_t VOL_SMEM = size_t(EPB) * 8 * NV * NB + sizeof(TensorTables) + 8 * 32;
-  static constexpr size_t GRAD_SMEM = size_t(EPB) * 8 * 2 * DIM * NV * NB + sizeof(TensorTables);
+  static constexpr size_t GRAD_SMEM = size_t(EPB) * 8 * 2 * DIM * NV * NB + sizeof(TensorTables);  // also the bilinear form's s, w
   static constexpr size_t TRACE_SMEM = sizeof(TensorTables);
 };
 
@@ -1731,6 +1731,126 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpGradientBR2Ke
       for (int k = 0; k < DIM; ++k) nl = fma(sign * gm[axis * DIM + k], ltg[(v * DIM + k) * NFQ], nl);
       up[v * NFQ] = fma(0.5 * cl, nl, sign * fma(-0.5, av, at));
       tr[v * NFQ] += fma(-0.5 * cl, nl, 0.5 * sign * av);
+    }
+  }
+}
+
+// V3 for bilinear quadrangles (per-node metric ja_q and 1/|J|_q, per-face n|J_f| from the face metric;
+// tensorGradientTile's non-affine form).  Forward, at node m along each axis b:
+//   tot_k(m) = sum_b [ lift(+) nF(b,+)_k U+(b,+) + lift(-) nF(b,-)_k U+(b,-) - sum_q Dhat[q][m] U_q ja_q[b][k] ]
+//   grad = tot / |J|_m (BR1 gradient traces: its traces); BR2: vol from {U} in place of U+, gradient trace at
+//   (f, j) = trace(vol / |J|) + cl nF_f . (U+ - U-)/2 with cl = sum_q end_q lift_q / |J|_q.
+// Transposed, with s = (1/|J|) (lamG + [BR1] T^T lamTg), w = (1/|J|) T^T lamTg (BR2):
+//   lamU_q -= sum_b sum_k ja_q[b][k] (Dhat^T (s + w)_k)_q,
+//   lamUp(f, j) = sum_line lift nF_f . s  [+ BR2: (1/2) sum_line lift nF_f . w + (cl/2) nF_f . lamTg(f, j)],
+//   BR2: lamTr(f, j) += (1/2) sum_line lift nF_f . w - (cl/2) nF_f . lamTg(f, j).
+template <int DIM, int N, bool BR2>
+__global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpGradientBilinearKernel(AdjArgs a) {
+  using A = AdjShape<DIM, N>;
+  constexpr int NV = A::NV, NB = A::NB, NF = A::NF, NFQ = A::NFQ, EPB = A::EPB, GS = NV * DIM, GSZ = DIM * DIM + 1;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* sS = reinterpret_cast<double*>(smem_raw);  // [EPB][GS][NB]  s
+  double* sW = sS + EPB * GS * NB;                   // [EPB][GS][NB]  w (BR2)
+  TensorTables* T = reinterpret_cast<TensorTables*>(sW + EPB * GS * NB);
+  const int tid = threadIdx.x;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  const int le = tid / NB, node = tid - le * NB;
+  const bool active = le < ecount;
+  const int64_t e = e0 + le;
+  loadTensorTables<DIM, N>(T, a.tables);
+  __syncthreads();
+  if (active) {
+    const double jinv = a.geom[(e * NB + node) * GSZ + DIM * DIM];
+    double lg[GS], lv[GS];
+#pragma unroll
+    for (int c = 0; c < GS; ++c) { lg[c] = a.lamG[(e * GS + c) * NB + node]; lv[c] = 0.0; }
+#pragma unroll
+    for (int b = 0; b < DIM; ++b) {
+      const int ab = axisIndex<DIM, N>(node, b);
+#pragma unroll
+      for (int en = 0; en < 2; ++en) {
+        const int f = T->axisFace[b][en];
+        const int j = T->nodeFacePoint[b][en][node];
+        const double c = en ? T->endp[ab] : T->endm[ab];
+        const double* src = a.lamTg + (a.faceBase + e * NF + f) * GS * NFQ + j;
+#pragma unroll
+        for (int k = 0; k < GS; ++k) lv[k] = fma(c, src[k * NFQ], lv[k]);
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < GS; ++c) {
+      sS[(le * GS + c) * NB + node] = jinv * (BR2 ? lg[c] : lg[c] + lv[c]);
+      sW[(le * GS + c) * NB + node] = BR2 ? jinv * lv[c] : 0.0;
+    }
+  }
+  __syncthreads();
+  if (active) {
+    const double* g = a.geom + (e * NB + node) * GSZ;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double acc = 0.0;
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) {
+        const int ab = axisIndex<DIM, N>(node, b);
+        const int st = strideOf<DIM, N>(b);
+        const int base = node - ab * st;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          double d = 0.0;
+#pragma unroll
+          for (int q = 0; q < N; ++q) {
+            const int o = (le * GS + v * DIM + k) * NB + base + q * st;
+            d = fma(T->dhat[ab][q], sS[o] + sW[o], d);
+          }
+          acc = fma(g[b * DIM + k], d, acc);
+        }
+      }
+      a.lamU[e * A::USTRIDE + v * NB + node] -= acc;
+    }
+  }
+  for (int idx = tid; idx < ecount * NF * NFQ; idx += blockDim.x) {
+    const int te = idx / (NF * NFQ), r = idx - te * (NF * NFQ);
+    const int f = r / NFQ, j = r - f * NFQ;
+    const int axis = T->faceAxis[f], en = T->faceEnd[f];
+    const double* lift = en ? T->liftp : T->liftm;
+    const double* coef = en ? T->endp : T->endm;
+    const int base = T->faceBase[f][j];
+    const int st = strideOf<DIM, N>(axis);
+    const int64_t ee = e0 + te;
+    const double* nF = a.fmetric + (ee * NF + f) * DIM;
+    double cl = 0.0;
+    if constexpr (BR2) {
+#pragma unroll
+      for (int q = 0; q < N; ++q) cl = fma(coef[q] * lift[q], a.geom[(ee * NB + base + q * st) * GSZ + DIM * DIM], cl);
+    }
+    const int64_t slot = a.faceBase + ee * NF + f;
+    const double* ltg = a.lamTg + slot * GS * NFQ + j;
+    double* up = a.lamUp + slot * NV * NFQ + j;
+    double* tr = a.lamTr + slot * NV * NFQ + j;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+      double at = 0.0, av = 0.0, nl = 0.0;
+#pragma unroll
+      for (int q = 0; q < N; ++q) {
+        double ns = 0.0, nw = 0.0;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          const int o = (te * GS + v * DIM + k) * NB + base + q * st;
+          ns = fma(nF[k], sS[o], ns);
+          nw = fma(nF[k], sW[o], nw);
+        }
+        at = fma(lift[q], ns, at);
+        av = fma(lift[q], nw, av);
+      }
+      if constexpr (BR2) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) nl = fma(nF[k], ltg[(v * DIM + k) * NFQ], nl);
+        up[v * NFQ] = fma(0.5 * cl, nl, fma(0.5, av, at));
+        tr[v * NFQ] += fma(-0.5 * cl, nl, 0.5 * av);
+      } else {
+        up[v * NFQ] = at;
+      }
     }
   }
 }

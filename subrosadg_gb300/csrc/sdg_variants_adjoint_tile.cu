@@ -1,5 +1,5 @@
-// Tangent-linear and adjoint element (tile) kernels of tensor blocks (lines, quadrangles, hexahedra; bilinear
-// quadrangles for the Euler equations): the one translation unit that
+// Tangent-linear and adjoint element (tile) kernels of tensor blocks (lines, quadrangles -- affine or bilinear --,
+// hexahedra): the one translation unit that
 // instantiates them.
 #include "sdg_kernels_adjoint.cuh"
 #include "sdg_variants.hpp"
@@ -19,27 +19,34 @@ void tileOf(AdjointTileKernels& k, bool br2, bool gen) {
   k.epb = A::EPB; k.threads = A::THREADS; k.jvpSmem = A::JVP_SMEM;
   k.volSmem = A::VOL_SMEM; k.gradSmem = A::GRAD_SMEM; k.traceSmem = A::TRACE_SMEM;
 }
-// Bilinear quadrangles (per-node metric), the Euler equations.
-template <int N>
-void bilinearOf(AdjointTileKernels& k, bool gen) {
+// Bilinear quadrangles (per-node metric): the Euler equations and Navier-Stokes BR1 / BR2.
+template <int N, bool VISC>
+void bilinearOf(AdjointTileKernels& k, bool br2, bool gen) {
   using A = AdjShape<2, N>;
-  k.jvpStage = reinterpret_cast<const void*>(&jvpStageKernel<2, N, false, false>);
-  k.vjpVolume = gen ? reinterpret_cast<const void*>(&vjpVolumeKernel<2, N, false, true, false>)
-                    : reinterpret_cast<const void*>(&vjpVolumeKernel<2, N, false, false, false>);
+  k.jvpStage = reinterpret_cast<const void*>(&jvpStageKernel<2, N, VISC, false>);
+  k.vjpVolume = gen ? reinterpret_cast<const void*>(&vjpVolumeKernel<2, N, VISC, true, false>)
+                    : reinterpret_cast<const void*>(&vjpVolumeKernel<2, N, VISC, false, false>);
   k.vjpTrace = reinterpret_cast<const void*>(&vjpTraceKernel<2, N>);
+  if constexpr (VISC)
+    k.vjpGradient = br2 ? reinterpret_cast<const void*>(&vjpGradientBilinearKernel<2, N, true>)
+                        : reinterpret_cast<const void*>(&vjpGradientBilinearKernel<2, N, false>);
   k.epb = A::EPB; k.threads = A::THREADS; k.jvpSmem = A::JVP_SMEM;
   k.volSmem = A::VOL_SMEM; k.gradSmem = A::GRAD_SMEM; k.traceSmem = A::TRACE_SMEM;
+}
+template <int N>
+void bilinearOf(AdjointTileKernels& k, bool visc, bool br2, bool gen) {
+  if (visc) bilinearOf<N, true>(k, br2, gen); else bilinearOf<N, false>(k, false, gen);
 }
 }  // namespace
 
 void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, bool affine, AdjointTileKernels& k) {
   if (!affine) {
-    if (dim != 2 || visc) return;
+    if (dim != 2) return;
     switch (n) {
-      case 3: bilinearOf<3>(k, gen); break;
-      case 4: bilinearOf<4>(k, gen); break;
-      case 5: bilinearOf<5>(k, gen); break;
-      case 6: bilinearOf<6>(k, gen); break;
+      case 3: bilinearOf<3>(k, visc, br2, gen); break;
+      case 4: bilinearOf<4>(k, visc, br2, gen); break;
+      case 5: bilinearOf<5>(k, visc, br2, gen); break;
+      case 6: bilinearOf<6>(k, visc, br2, gen); break;
       default: break;
     }
     return;

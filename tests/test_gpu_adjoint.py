@@ -107,6 +107,17 @@ CASES = {
     # (Central: the rounding of a dense block's weakly compressible residual is too large for the small step the
     # Exact flux's upwind switch needs; Exact on triangles is in the shear-layer case)
     "inc-ns-lidcavity-tri-p2-central-br2": lambda: cases.cavity_case(p=2, n=4, flux=sdg.CENTRAL, mu=1e-2, split=1.0),
+    # Navier-Stokes on bilinear (jittered) quadrangles, alone and in the hybrid Kelvin-Helmholtz mesh of the NS
+    # workload (P4, BR2, LF)
+    "ns-jitter-quad-p3-br2-roe-bilinear": lambda: cases.kh_case(n=4, p=3, flux=sdg.ROE, split=0.0, viscous=sdg.BR2,
+                                                                mu=2e-3),
+    "ns-jitter-quad-p2-br1-hllc-bilinear": lambda: cases.kh_case(n=4, p=2, flux=sdg.HLLC, split=0.0, viscous=sdg.BR1,
+                                                                 mu=2e-3),
+    "ns-hybrid-jitter-p4-br2-lf": lambda: cases.kh_case(n=4, p=4, flux=sdg.LAX_FRIEDRICHS, split=0.5, viscous=sdg.BR2,
+                                                        mu=2e-3, dt=1e-4),
+    "ns-channel-walls-jitter-p3-br1-roe": lambda: cases.channel_case(
+        p=3, flux=sdg.ROE, n=3, jitter=0.1, viscous=sdg.BR1, mu=0.01,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
 }
 
 
@@ -238,7 +249,7 @@ def test_vjp_is_the_transpose_of_jvp(name):
 @pytest.mark.parametrize("name", ["euler-quad-p3-roe", "euler-hex-p2-hllc", "ns-hex-p3-br1-roe",
                                   "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq",
                                   "ns-line-p4-br1-roe", "euler-hybrid-p3-lf-bilinear", "euler-tri-p5-roe",
-                                  "ns-hybrid-p3-br1-lf", "ns-tri-p3-br2-hllc",
+                                  "ns-hybrid-p3-br1-lf", "ns-tri-p3-br2-hllc", "ns-hybrid-jitter-p4-br2-lf",
                                   "ns-quad-p4-br1-hllc", "ns-hex-p2-br2-hllc", "ns-channel-walls-quad-p3-br2-roe"])
 def test_trajectory_dot_product_with_checkpointing(name):
     steps, interval = 5, 2
@@ -279,7 +290,8 @@ def test_checkpoint_interval_does_not_change_the_adjoint():
 # the trajectory checks use the smooth fluxes (cfg: Roe + BR1 is the adjoint workload)
 @pytest.mark.parametrize("name", ["euler-hex-p3-central", "ns-hex-p3-br1-roe", "euler-quad-p3-roe",
                                   "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-euler-shearlayer-quad-p2-central",
-                                  "ns-line-walls-p3-br2-roe", "euler-tri-p3-central", "ns-tri-p2-br1-roe"])
+                                  "ns-line-walls-p3-br2-roe", "euler-tri-p3-central", "ns-tri-p2-br1-roe",
+                                  "ns-jitter-quad-p3-br2-roe-bilinear"])
 def test_kinetic_energy_gradient_matches_finite_differences(name):
     steps, interval = 6, 3
     s, dt = make(name)
@@ -331,8 +343,8 @@ def test_torch_autograd_binding():
 
 
 def test_derivatives_refuse_unsupported_configurations():
-    # Navier-Stokes on bilinear blocks (the jittered hybrid Kelvin-Helmholtz mesh)
-    hybrid = sdg.GpuSolver(*cases.kh_case(n=4, p=3, viscous=sdg.BR2, mu=1e-3)[:2], device=0)
+    # Navier-Stokes on bilinear first-order quadrangles (dense blocks of jittered P1 meshes)
+    hybrid = sdg.GpuSolver(*cases.kh_case(n=4, p=1, split=0.0, viscous=sdg.BR2, mu=1e-3)[:2], device=0)
     hybrid.initialize_primitive(cases.kh_primitive(*hybrid.volume_points()[:, :2].T))
     with pytest.raises(sdg.SdgError) as e:
         hybrid.jvp_residual(np.zeros((hybrid.counts.volume_point_count, 4)))
@@ -409,7 +421,7 @@ def test_surface_force_cotangent_matches_central_differences(name):
                                   "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq", "euler-line-farfield-p2-hllc",
                                   "ns-line-walls-p3-br2-roe", "euler-channel-tri-p3-roe",
                                   "euler-channel-hybrid-farfield-p2-hllc", "ns-channel-walls-tri-p2-br2-roe",
-                                  "inc-ns-lidcavity-tri-p2-central-br2"])
+                                  "inc-ns-lidcavity-tri-p2-central-br2", "ns-channel-walls-jitter-p3-br1-roe"])
 def test_force_gradient_through_a_trajectory(name):
     """J = e . force on a wall after N steps: dJ/dU_0 in a seeded direction and dJ/d(boundary primitives) in a
     seeded direction of every boundary point's (rho, u, T), against central differences of the trajectory."""
