@@ -4,10 +4,9 @@
 // the discrete scheme the forward path runs (same quadrature, same fluxes, same SSP-RK stages), so
 //   <lambda, JVP(dU)> = <VJP(lambda), dU>
 // holds to round-off, for one residual and for whole trajectories.  Scope: compressible or incompressible
-// Euler on every element block (tensor blocks: lines, quadrangles -- affine or bilinear --, hexahedra; dense
-// blocks: triangles and first-order quadrangles), Navier-Stokes with BR1 or BR2 on every block but bilinear
-// first-order quadrangles, the Boussinesq source, with or without boundary faces; other configurations
-// (Navier-Stokes on jittered P1 quadrangles, artificial viscosity) return SDG_ERR_UNSUPPORTED.  The cotangents of the point-layout API are mapped
+// Euler and Navier-Stokes (BR1, BR2) on every element block (tensor blocks: lines, quadrangles -- affine or
+// bilinear --, hexahedra; dense blocks: triangles and first-order quadrangles, affine or bilinear), the
+// Boussinesq source, with or without boundary faces; artificial viscosity returns SDG_ERR_UNSUPPORTED.  The cotangents of the point-layout API are mapped
 // by the transposes of the point <-> state conversions (dense blocks: Phi^T in, P^T out, P the projection).
 //
 // Trajectories: the tangent runs stage by stage beside the forward state.  The adjoint stores the state
@@ -119,9 +118,6 @@ AdjointState* adjoint(sdg_handle* h) {
   if (h->hostOnly) throw Failure(SDG_ERR_STATE, "host-only handle (created with device < 0)");
   if (!h->hasState) throw Failure(SDG_ERR_STATE, "no state");
   if (h->adj) return h->adj;
-  for (const DevBlock& B : h->blocks)
-    if (h->ns && !B.affine && B.kind == kDense)
-      throw Failure(SDG_ERR_UNSUPPORTED, "Navier-Stokes derivatives of bilinear first-order quadrangles are not built");
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   const bool gen = h->ph.incomp || h->ph.source;

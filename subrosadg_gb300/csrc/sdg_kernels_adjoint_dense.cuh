@@ -41,6 +41,9 @@ struct DenseAdjShape {
   // gradient transpose (affine): lamTot and lamJmp [NV*2][NB] | phif | dmod | emod | lmod
   static constexpr int GOPS = NFP * NB + 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
   static constexpr size_t GRAD_SMEM = (size_t(EPB) * 2 * 2 * NV * NB + GOPS) * 8;
+  // gradient transpose (general form): lamRt, lamRv [NV*2][NB] | lamRf [NF][NV*2][NB] | point values' cotangent
+  // [NV][NQ] | phi | dphiw | phif | phifw | mref
+  static constexpr size_t GRAD_GENERAL_SMEM = (size_t(EPB) * ((2 + NF) * 2 * NV * NB + NV * NQ) + TABLES) * 8;
 };
 
 // Geometry of point q of element e: contravariant metric, 1/|J| at the point; the M^-1 of the element and its
@@ -411,6 +414,121 @@ __global__ void __launch_bounds__(256) vjpDenseGradientKernel(AdjArgs a) {
       a.lamTr[slot * NV * NFQ + v * NFQ + j] += -0.5 * ld;
     }
     a.lamUp[slot * NV * NFQ + v * NFQ + j] = fma(0.5, ld, lo);
+  }
+}
+
+// Transposed gradient pass of a bilinear dense block (denseGradientTile's general form: per-point metric g_q, the
+// element's own M^-1).  Forward, per variable with the face points' weighted values phifw:
+//   Rt_k = sum_fj phifw_fj O_fj nF_f[k] - sum_q U_q sum_b dphiw_qb g_q[b][k],   Rv_k: (O + S)/2 in place of O
+//   grad = M^-1 Rt;  BR1 gradient traces Phi_f grad;  BR2: Phi_f (M^-1 Rv + M^-1 Rf_f) with
+//   Rf_f,k = sum_{j in f} phifw_fj (O - S)_fj / 2 nF_f[k].
+// Transposed: lamRt = M^-T (lamG + [BR1] Phi_f^T lamTg), BR2: lamRv = M^-T Phi_f^T lamTg over all faces and
+// lamRf_f = M^-T Phi_f^T lamTg over face f's points; then the points' values, O (lamUp) and S (lamTr, BR2).
+template <int NB, int NQ, int NFQ, int NF, bool BR2>
+__global__ void __launch_bounds__(256) vjpDenseGradientGeneralKernel(AdjArgs a) {
+  using S = DenseAdjShape<NB, NQ, NFQ, NF>;
+  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB, NR = NV * 2, GS = NQ * 5 + NB * NB;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  double* sRt = reinterpret_cast<double*>(smem_raw);  // [EPB][NR][NB] lamRt
+  double* sRv = sRt + EPB * NR * NB;                  // [EPB][NR][NB] lamRv (BR2)
+  double* sRf = sRv + EPB * NR * NB;                  // [EPB][NF][NR][NB] lamRf (BR2)
+  double* sUq = sRf + EPB * NF * NR * NB;             // [EPB][NV][NQ] cotangent of the point values
+  double* tab = sUq + EPB * NV * NQ;
+  const double* phi = tab;
+  const double* dphiw = phi + NQ * NB;
+  const double* phif = dphiw + NQ * 2 * NB;
+  const double* phifw = phif + NFP * NB;
+  const int tid = threadIdx.x;
+  const int64_t e0 = int64_t(blockIdx.x) * EPB;
+  const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
+  for (int k = tid; k < S::TABLES; k += blockDim.x) tab[k] = a.tables[k];
+  __syncthreads();
+  // lamRt, lamRv, lamRf = M^-T (...) per (element, component, basis function)
+  for (int idx = tid; idx < ecount * NR * NB; idx += blockDim.x) {
+    const int le = idx / (NR * NB), r = idx - le * NR * NB;
+    const int c = r / NB, m = r - c * NB;
+    const int64_t e = e0 + le;
+    const double* minv = a.geom + e * GS + NQ * 5;
+    const double* tg = a.lamTg + (a.faceBase + e * NF) * NR * NFQ;
+    double t = 0.0, v = 0.0, fsum[NF];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) fsum[f] = 0.0;
+    for (int i = 0; i < NB; ++i) {
+      double trf[NF];  // (Phi_f^T lamTg_f)(i) per face
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        double x = 0.0;
+#pragma unroll
+        for (int j = 0; j < NFQ; ++j) x = fma(phif[(f * NFQ + j) * NB + i], tg[(f * NR + c) * NFQ + j], x);
+        trf[f] = x;
+      }
+      double all = 0.0;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) all += trf[f];
+      const double mi = minv[i * NB + m];
+      t = fma(mi, a.lamG[(e * NR + c) * NB + i] + (BR2 ? 0.0 : all), t);
+      if constexpr (BR2) {
+        v = fma(mi, all, v);
+#pragma unroll
+        for (int f = 0; f < NF; ++f) fsum[f] = fma(mi, trf[f], fsum[f]);
+      }
+    }
+    sRt[(le * NR + c) * NB + m] = t;
+    if constexpr (BR2) {
+      sRv[(le * NR + c) * NB + m] = v;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) sRf[((le * NF + f) * NR + c) * NB + m] = fsum[f];
+    }
+  }
+  __syncthreads();
+  // the points' values: lamUq = -sum_k sum_b g_q[b][k] sum_i dphiw_qb(i) (lamRt + lamRv)_k(i)
+  for (int idx = tid; idx < ecount * NV * NQ; idx += blockDim.x) {
+    const int le = idx / (NV * NQ), r = idx - le * NV * NQ;
+    const int v = r / NQ, q = r - v * NQ;
+    const double* g = a.geom + (e0 + le) * GS + q * 5;
+    double acc = 0.0;
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        double x = 0.0;
+#pragma unroll
+        for (int i = 0; i < NB; ++i) {
+          const double l = sRt[(le * NR + v * 2 + k) * NB + i] + (BR2 ? sRv[(le * NR + v * 2 + k) * NB + i] : 0.0);
+          x = fma(dphiw[(q * 2 + b) * NB + i], l, x);
+        }
+        acc = fma(g[b * 2 + k], x, acc);
+      }
+    sUq[(le * NV + v) * NQ + q] = -acc;
+  }
+  __syncthreads();
+  for (int idx = tid; idx < ecount * NV * NB; idx += blockDim.x) {
+    const int le = idx / (NV * NB), r = idx - le * NV * NB;
+    const int v = r / NB, m = r - v * NB;
+    double acc = 0.0;
+    for (int q = 0; q < NQ; ++q) acc = fma(phi[q * NB + m], sUq[(le * NV + v) * NQ + q], acc);
+    a.lamU[(e0 + le) * S::USTRIDE + v * NB + m] += acc;
+  }
+  // the traces: O from Rt (and Rv / 2, Rf / 2), S from Rv / 2 and -Rf / 2
+  for (int idx = tid; idx < ecount * NFP * NV; idx += blockDim.x) {
+    const int le = idx / (NFP * NV), r = idx - le * NFP * NV;
+    const int fj = r / NV, v = r - fj * NV;
+    const int f = fj / NFQ, j = fj - f * NFQ;
+    const int64_t e = e0 + le;
+    const double n0 = a.fmetric[(e * NF + f) * 2 + 0], n1 = a.fmetric[(e * NF + f) * 2 + 1];
+    double lt = 0.0, lv = 0.0, lf = 0.0;
+#pragma unroll
+    for (int i = 0; i < NB; ++i) {
+      const double w = phifw[fj * NB + i];
+      lt = fma(w, fma(n0, sRt[(le * NR + v * 2) * NB + i], n1 * sRt[(le * NR + v * 2 + 1) * NB + i]), lt);
+      if constexpr (BR2) {
+        lv = fma(w, fma(n0, sRv[(le * NR + v * 2) * NB + i], n1 * sRv[(le * NR + v * 2 + 1) * NB + i]), lv);
+        lf = fma(w, fma(n0, sRf[((le * NF + f) * NR + v * 2) * NB + i], n1 * sRf[((le * NF + f) * NR + v * 2 + 1) * NB + i]), lf);
+      }
+    }
+    const int64_t slot = a.faceBase + e * NF + f;
+    a.lamUp[slot * NV * NFQ + v * NFQ + j] = BR2 ? lt + 0.5 * (lv + lf) : lt;
+    if constexpr (BR2) a.lamTr[slot * NV * NFQ + v * NFQ + j] += 0.5 * (lv - lf);
   }
 }
 

@@ -1,6 +1,5 @@
-// Tangent-linear and adjoint element kernels of dense blocks (triangles, first-order quadrangles): the Euler
-// equations on every element, Navier-Stokes BR1 / BR2 on affine ones; the one translation unit that instantiates
-// them.
+// Tangent-linear and adjoint element kernels of dense blocks (triangles, first-order quadrangles -- affine or
+// bilinear --), the Euler and Navier-Stokes (BR1, BR2) equations: the one translation unit that instantiates them.
 #include "sdg_kernels_adjoint_dense.cuh"
 #include "sdg_variants.hpp"
 
@@ -14,18 +13,22 @@ void denseOf(AdjointTileKernels& k, bool gen, bool br2) {
   k.vjpVolume = gen ? reinterpret_cast<const void*>(&vjpDenseVolumeKernel<NB, NQ, NFQ, NF, AFF, true, VISC>)
                     : reinterpret_cast<const void*>(&vjpDenseVolumeKernel<NB, NQ, NFQ, NF, AFF, false, VISC>);
   k.vjpTrace = reinterpret_cast<const void*>(&vjpDenseTraceKernel<NB, NQ, NFQ, NF>);
-  if constexpr (VISC) {
+  if constexpr (VISC && AFF) {
     k.vjpGradient = br2 ? reinterpret_cast<const void*>(&vjpDenseGradientKernel<NB, NQ, NFQ, NF, true>)
                         : reinterpret_cast<const void*>(&vjpDenseGradientKernel<NB, NQ, NFQ, NF, false>);
     k.gradSmem = S::GRAD_SMEM;
+  } else if constexpr (VISC) {
+    k.vjpGradient = br2 ? reinterpret_cast<const void*>(&vjpDenseGradientGeneralKernel<NB, NQ, NFQ, NF, true>)
+                        : reinterpret_cast<const void*>(&vjpDenseGradientGeneralKernel<NB, NQ, NFQ, NF, false>);
+    k.gradSmem = S::GRAD_GENERAL_SMEM;
   }
   k.epb = S::EPB; k.threads = S::THREADS; k.jvpSmem = S::JVP_SMEM; k.volSmem = S::VJP_SMEM;
   k.traceSmem = S::TRACE_SMEM;
 }
 template <int NB, int NQ, int NFQ, int NF, bool AFF>
 void denseOf(AdjointTileKernels& k, bool gen, bool visc, bool br2) {
-  if (!visc) { denseOf<NB, NQ, NFQ, NF, AFF, false>(k, gen, false); return; }
-  if constexpr (AFF) denseOf<NB, NQ, NFQ, NF, AFF, true>(k, gen, br2);  // Navier-Stokes: affine elements
+  if (visc) denseOf<NB, NQ, NFQ, NF, AFF, true>(k, gen, br2);
+  else denseOf<NB, NQ, NFQ, NF, AFF, false>(k, gen, false);
 }
 }  // namespace
 

@@ -115,6 +115,10 @@ CASES = {
                                                                  mu=2e-3),
     "ns-hybrid-jitter-p4-br2-lf": lambda: cases.kh_case(n=4, p=4, flux=sdg.LAX_FRIEDRICHS, split=0.5, viscous=sdg.BR2,
                                                         mu=2e-3, dt=1e-4),
+    "ns-jitter-quad-p1-br2-roe-bilinear": lambda: cases.kh_case(n=4, p=1, flux=sdg.ROE, split=0.0, viscous=sdg.BR2,
+                                                                mu=2e-3),
+    "ns-jitter-quad-p1-br1-hllc-bilinear": lambda: cases.kh_case(n=5, p=1, flux=sdg.HLLC, split=0.0, viscous=sdg.BR1,
+                                                                 mu=2e-3),
     "ns-channel-walls-jitter-p3-br1-roe": lambda: cases.channel_case(
         p=3, flux=sdg.ROE, n=3, jitter=0.1, viscous=sdg.BR1, mu=0.01,
         conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
@@ -250,6 +254,7 @@ def test_vjp_is_the_transpose_of_jvp(name):
                                   "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq",
                                   "ns-line-p4-br1-roe", "euler-hybrid-p3-lf-bilinear", "euler-tri-p5-roe",
                                   "ns-hybrid-p3-br1-lf", "ns-tri-p3-br2-hllc", "ns-hybrid-jitter-p4-br2-lf",
+                                  "ns-jitter-quad-p1-br2-roe-bilinear",
                                   "ns-quad-p4-br1-hllc", "ns-hex-p2-br2-hllc", "ns-channel-walls-quad-p3-br2-roe"])
 def test_trajectory_dot_product_with_checkpointing(name):
     steps, interval = 5, 2
@@ -343,12 +348,6 @@ def test_torch_autograd_binding():
 
 
 def test_derivatives_refuse_unsupported_configurations():
-    # Navier-Stokes on bilinear first-order quadrangles (dense blocks of jittered P1 meshes)
-    hybrid = sdg.GpuSolver(*cases.kh_case(n=4, p=1, split=0.0, viscous=sdg.BR2, mu=1e-3)[:2], device=0)
-    hybrid.initialize_primitive(cases.kh_primitive(*hybrid.volume_points()[:, :2].T))
-    with pytest.raises(sdg.SdgError) as e:
-        hybrid.jvp_residual(np.zeros((hybrid.counts.volume_point_count, 4)))
-    assert e.value.code == _abi.SDG_ERR_UNSUPPORTED
     mesh, cfg, ic, bc, _, _ = cases.shock_tube_case(p=2, n=8)  # artificial viscosity is not differentiated
     walls = sdg.GpuSolver(mesh, cfg, device=0)
     walls.initialize_primitive(ic(walls.volume_points()))
