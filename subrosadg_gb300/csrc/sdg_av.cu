@@ -100,8 +100,9 @@ __device__ double avDenseSensor(const AvArgs& a, int64_t e) {
   return num / den;
 }
 
-__global__ void __launch_bounds__(kAvThreads) avKernel(AvArgs a) {
-  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+// One CTA-sized chunk `block` of a pass (thread t = block * blockDim + threadIdx).
+__device__ __forceinline__ void avBody(const AvArgs& a, int64_t block) {
+  const int64_t t = block * blockDim.x + threadIdx.x;
   if (a.kind == 0) {
     if (t < a.nodes) a.nodeAV[t] = 0.0;
     return;
@@ -124,6 +125,18 @@ __global__ void __launch_bounds__(kAvThreads) avKernel(AvArgs a) {
     atomicMax(reinterpret_cast<unsigned long long*>(a.nodeAV + a.vert[t * a.nvert + v]), bits);
 }
 
+__global__ void __launch_bounds__(kAvThreads) avKernel(AvArgs a) { avBody(a, blockIdx.x); }
+
+// Batched: CTA c runs work items c, c + gridDim.x, ... of (argument set, chunk) pairs over many instances (the
+// instances' node fields are disjoint, so one level of a batch runs every instance's pass at once).
+__global__ void __launch_bounds__(kAvThreads)
+    avBatchKernel(const AvArgs* __restrict__ args, const int2* __restrict__ items, int nitems) {
+  for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
+    const int2 it = items[w];
+    avBody(args[it.x], it.y);
+  }
+}
+
 // s0 per order (SimulationControl.cpp:892-893)
 const double kAvTolerance[5] = {0.0, -1.20411998266, -1.90848501888, -2.40823996531, -2.79588001734};
 
@@ -136,7 +149,7 @@ double crossNorm(const double* a, const double* b) {
 Rec avRec(int kind, int64_t count) {
   Rec r;
   r.kind = kRecAv; r.cls = 4;
-  r.fn = reinterpret_cast<const void*>(&avKernel); r.bfn = nullptr;
+  r.fn = reinterpret_cast<const void*>(&avKernel); r.bfn = reinterpret_cast<const void*>(&avBatchKernel);
   r.threads = kAvThreads; r.epb = 1; r.smem = 0;
   r.units = (count + kAvThreads - 1) / kAvThreads;
   std::memset(&r.av, 0, sizeof(r.av));

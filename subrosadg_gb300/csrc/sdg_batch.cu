@@ -41,6 +41,7 @@ size_t argSize(int kind) {
     case kRecGradTensor: return sizeof(GradArgs);
     case kRecGradDense: return sizeof(DenseGradArgs);
     case kRecFace: return sizeof(FaceArgs);
+    case kRecAv: return sizeof(AvArgs);
     default: return sizeof(RelArgs);
   }
 }
@@ -51,6 +52,7 @@ const void* argPtr(const Rec& r) {
     case kRecGradTensor: return &r.ga;
     case kRecGradDense: return &r.da;
     case kRecFace: return &r.fa;
+    case kRecAv: return &r.av;
     default: return &r.ra;
   }
 }
@@ -220,7 +222,8 @@ void launchGroup(const Group& g, cudaStream_t s) {
     case kRecStage: SDG_CUDA(cudaLaunchKernel(g.bfn, dim3(g.grid), dim3(g.threads), p5, g.smem, s)); break;
     case kRecGradTensor:
     case kRecGradDense: SDG_CUDA(cudaLaunchKernel(g.bfn, dim3(g.grid), dim3(g.threads), p4, g.smem, s)); break;
-    case kRecFace: SDG_CUDA(cudaLaunchKernel(g.bfn, dim3(g.grid), dim3(g.threads), p3, g.smem, s)); break;
+    case kRecFace:
+    case kRecAv: SDG_CUDA(cudaLaunchKernel(g.bfn, dim3(g.grid), dim3(g.threads), p3, g.smem, s)); break;
     default: SDG_CUDA(cudaLaunchKernel(g.bfn, dim3(5, g.grid), dim3(g.threads), p1, 0, s)); break;
   }
 }
@@ -448,11 +451,6 @@ int sdg_batch_create(sdg_handle* const* instances, int32_t count, sdg_batch** ou
   b->device = b->inst[0]->device;
   for (sdg_handle* h : b->inst)
     if (h->hostOnly != b->planOnly || (!h->hostOnly && h->device != b->device)) return SDG_ERR_INVALID_ARGUMENT;
-  for (sdg_handle* h : b->inst)
-    if (h->av) {  // the per-step sensor records have no batched kernels
-      setCreateError("batches of artificial-viscosity instances are not built");
-      return SDG_ERR_UNSUPPORTED;
-    }
   for (size_t i = 0; i < b->inst.size(); ++i)
     for (size_t j = 0; j < i; ++j)
       if (b->inst[i] == b->inst[j]) return SDG_ERR_INVALID_ARGUMENT;  // an instance appears once
