@@ -50,6 +50,7 @@ enum sdg_element_type { /* gmsh first-order type numbers (src/Solver/SimulationC
   SDG_ELEMENT_LINE = 1,     /* DimensionEnum::D1 / MeshModelEnum::Line; its faces are points */
   SDG_ELEMENT_TRIANGLE = 2,
   SDG_ELEMENT_QUADRANGLE = 3,
+  SDG_ELEMENT_TETRAHEDRON = 4, /* dense modal blocks, P = 1..3, compressible Euler (single instances)      */
   SDG_ELEMENT_HEXAHEDRON = 5
 };
 enum sdg_equation {                                                                    /* Enum.cpp:56-64   */
@@ -100,7 +101,8 @@ typedef struct sdg_mesh {
   const int32_t* quadrangle_node;     /* [quadrangle_count][4]                                      */
   int64_t hexahedron_count;
   const int32_t* hexahedron_node;     /* [hexahedron_count][8]                                      */
-  int64_t boundary_count;             /* boundary elements: points (1D), lines (2D), quadrangles (3D) */
+  int64_t boundary_count;             /* boundary elements: points (1D), lines (2D), quadrangles or
+                                         triangles (3D; a triangle's fourth index is -1)             */
   const int32_t* boundary_node;       /* [boundary_count][1, 2 or 4]                                */
   const int32_t* boundary_physical;   /* [boundary_count] 1-based physical group index              */
   int32_t physical_count;
@@ -111,6 +113,8 @@ typedef struct sdg_mesh {
                                          reference's point normals are -1 at local face 0 and +1 at
                                          local face 1, Geometry.cpp:102-112)                        */
   const int32_t* line_node;           /* [line_count][2]                                            */
+  int64_t tetrahedron_count;          /* 3D: tetrahedra (MeshModelEnum::Tetrahedron), gmsh vertex order */
+  const int32_t* tetrahedron_node;    /* [tetrahedron_count][4]                                      */
 } sdg_mesh;
 
 /* ---- physics and numerics: the runtime form of the reference's SimulationControl -------------- */
@@ -291,6 +295,11 @@ int sdg_mesh_generate_1d(double x0, double lx, int32_t nx, int32_t periodic, con
 int sdg_mesh_generate_3d(double x0, double y0, double z0, double lx, double ly, double lz, int32_t nx,
                          int32_t ny, int32_t nz, int32_t periodic, const int32_t* boundary_condition,
                          sdg_generated_mesh* out);
+/* The same box with every hexahedron split into six tetrahedra around its lowest-to-highest diagonal
+ * (conforming, periodic-compatible); boundary elements are triangles in the same six groups. */
+int sdg_mesh_generate_3d_tetrahedra(double x0, double y0, double z0, double lx, double ly, double lz,
+                                    int32_t nx, int32_t ny, int32_t nz, int32_t periodic,
+                                    const int32_t* boundary_condition, sdg_generated_mesh* out);
 /* Read a gmsh MSH 4.1 ASCII file (first-order or high-order elements; only the primary vertices
  * are used).  Physical groups of dimension d-1 (points in 1D) become boundary groups in file order. */
 int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out);

@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "../subrosadg_gb300/csrc/tetrahedron_rules.h"
 #include "../subrosadg_gb300/csrc/triangle_rules.h"
 
 namespace orc {
@@ -28,12 +29,12 @@ namespace orc {
 // long double for an extended-precision truth (build flag -DORC_REAL="long double").
 using Real = ORC_REAL;
 
-enum ElemType { kLine = 1, kTri = 2, kQuad = 3, kHex = 5 };
+enum ElemType { kLine = 1, kTri = 2, kQuad = 3, kTet = 4, kHex = 5 };
 
-inline int elemDim(int t) { return t == kLine ? 1 : (t == kHex ? 3 : 2); }
-inline int elemFaces(int t) { return t == kLine ? 2 : (t == kTri ? 3 : (t == kQuad ? 4 : 6)); }
-inline int elemVerts(int t) { return t == kLine ? 2 : (t == kTri ? 3 : (t == kQuad ? 4 : 8)); }
-inline int faceVerts(int t) { return t == kLine ? 1 : (t == kHex ? 4 : 2); }
+inline int elemDim(int t) { return t == kLine ? 1 : (t == kHex || t == kTet ? 3 : 2); }
+inline int elemFaces(int t) { return t == kLine ? 2 : (t == kTri ? 3 : (t == kQuad || t == kTet ? 4 : 6)); }
+inline int elemVerts(int t) { return t == kLine ? 2 : (t == kTri ? 3 : (t == kQuad || t == kTet ? 4 : 8)); }
+inline int faceVerts(int t) { return t == kLine ? 1 : (t == kHex ? 4 : (t == kTet ? 3 : 2)); }
 
 // Face vertex lists of each element type (SimulationControl.cpp:170-216).
 inline const int* faceVertexTable(int t) {
@@ -41,7 +42,8 @@ inline const int* faceVertexTable(int t) {
   static const int tri[] = {0, 1, 1, 2, 2, 0};
   static const int quad[] = {0, 1, 1, 2, 2, 3, 3, 0};
   static const int hex[] = {0, 3, 2, 1, 0, 1, 5, 4, 0, 4, 7, 3, 1, 2, 6, 5, 2, 3, 7, 6, 4, 5, 6, 7};
-  return t == kLine ? line : (t == kTri ? tri : (t == kQuad ? quad : hex));
+  static const int tet[] = {0, 2, 1, 0, 1, 3, 0, 3, 2, 3, 1, 2};
+  return t == kLine ? line : (t == kTri ? tri : (t == kQuad ? quad : (t == kTet ? tet : hex)));
 }
 
 // Reference-element vertex coordinates (gmsh conventions).
@@ -51,7 +53,8 @@ inline std::array<Real, 3> refVertex(int t, int v) {
   static const Real quad[4][3] = {{-1, -1, 0}, {1, -1, 0}, {1, 1, 0}, {-1, 1, 0}};
   static const Real hex[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
                                    {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
-  const Real* p = t == kLine ? line[v] : (t == kTri ? tri[v] : (t == kQuad ? quad[v] : hex[v]));
+  static const Real tet[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  const Real* p = t == kLine ? line[v] : (t == kTri ? tri[v] : (t == kQuad ? quad[v] : (t == kTet ? tet[v] : hex[v])));
   return {p[0], p[1], p[2]};
 }
 
@@ -95,6 +98,16 @@ struct Quadrature {
 // Element quadrature of the given order for each element type.
 inline Quadrature elementQuadrature(int t, int order) {
   Quadrature q; q.dim = elemDim(t);
+  if (t == kTet) {  // Keast's symmetric rules of degree 2, 4, 6 (4 / 11 / 24 points, kTetrahedronQuadratureNumber)
+    for (const auto& r : sdg_tables::kTetrahedronRules) {
+      if (r.degree == order) {
+        q.n = r.count;
+        for (int i = 0; i < r.count; ++i) { q.x.insert(q.x.end(), {r.xi[i], r.eta[i], r.zeta[i]}); q.w.push_back(r.weight[i]); }
+        return q;
+      }
+    }
+    throw std::runtime_error("no tetrahedron rule of order " + std::to_string(order));
+  }
   if (t == kTri) {
     for (const auto& r : sdg_tables::kTriangleRules) {
       if (r.degree == order) {
@@ -143,6 +156,16 @@ inline Quadrature faceQuadrature(int t, int order) {
     q.n = 1; q.x = {0.0, 0.0, 0.0}; q.w = {1.0};
     return q;
   }
+  if (t == kTet) {  // triangular faces: Dunavant's odd-degree rules on (0,0),(1,0),(0,1)
+    for (const auto& r : sdg_tables::kFaceTriangleRules) {
+      if (r.degree == order) {
+        q.n = r.count;
+        for (int i = 0; i < r.count; ++i) { q.x.insert(q.x.end(), {r.xi[i], r.eta[i], 0.0}); q.w.push_back(r.weight[i]); }
+        return q;
+      }
+    }
+    throw std::runtime_error("no triangle face rule of order " + std::to_string(order));
+  }
   const int m = linePoints(order);
   std::vector<Real> gx, gw; gaussLegendre(m, gx, gw);
   if (t != kHex) {
@@ -159,6 +182,7 @@ inline Quadrature faceQuadrature(int t, int order) {
 // P1 shape functions of the face reference element (BasisFunction.cpp:76-111 uses gmsh Lagrange1).
 inline void faceShape(int t, const Real* fx, Real* n) {
   if (t == kLine) { n[0] = 1.0; return; }
+  if (t == kTet) { n[0] = 1 - fx[0] - fx[1]; n[1] = fx[0]; n[2] = fx[1]; return; }
   if (t != kHex) { n[0] = 0.5 * (1.0 - fx[0]); n[1] = 0.5 * (1.0 + fx[0]); return; }
   const Real x = fx[0], y = fx[1];
   n[0] = 0.25 * (1 - x) * (1 - y); n[1] = 0.25 * (1 + x) * (1 - y);
@@ -166,6 +190,7 @@ inline void faceShape(int t, const Real* fx, Real* n) {
 }
 inline void faceShapeGrad(int t, const Real* fx, Real* dxi, Real* deta) {
   if (t == kLine) { dxi[0] = 0.0; return; }
+  if (t == kTet) { dxi[0] = -1; dxi[1] = 1; dxi[2] = 0; deta[0] = -1; deta[1] = 0; deta[2] = 1; return; }
   if (t != kHex) { dxi[0] = -0.5; dxi[1] = 0.5; return; }
   const Real x = fx[0], y = fx[1];
   dxi[0] = -0.25 * (1 - y); dxi[1] = 0.25 * (1 - y); dxi[2] = 0.25 * (1 + y); dxi[3] = -0.25 * (1 + y);
@@ -184,6 +209,12 @@ inline void elemShape(int t, const Real* X, Real* n, Real* g /* nv*3 */) {
     n[0] = 1 - X[0] - X[1]; n[1] = X[0]; n[2] = X[1];
     const Real gg[9] = {-1, -1, 0, 1, 0, 0, 0, 1, 0};
     for (int i = 0; i < 9; ++i) g[i] = gg[i];
+    return;
+  }
+  if (t == kTet) {
+    n[0] = 1 - X[0] - X[1] - X[2]; n[1] = X[0]; n[2] = X[1]; n[3] = X[2];
+    const Real gg[12] = {-1, -1, -1, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int i = 0; i < 12; ++i) g[i] = gg[i];
     return;
   }
   const int nv = elemVerts(t);
@@ -235,9 +266,24 @@ inline Dual kernelD(int k, Dual x) {
   return {c * dpn, c * ddpn * x.dx, c * ddpn * x.dy};
 }
 
+// Forward-mode dual in three variables (tetrahedron basis gradients).
+struct Dual3 { Real v, d[3]; };
+inline Dual3 operator+(Dual3 a, Dual3 b) { return {a.v + b.v, {a.d[0] + b.d[0], a.d[1] + b.d[1], a.d[2] + b.d[2]}}; }
+inline Dual3 operator-(Dual3 a, Dual3 b) { return {a.v - b.v, {a.d[0] - b.d[0], a.d[1] - b.d[1], a.d[2] - b.d[2]}}; }
+inline Dual3 operator*(Dual3 a, Dual3 b) {
+  Dual3 r{a.v * b.v, {0, 0, 0}};
+  for (int k = 0; k < 3; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+  return r;
+}
+// f(x) for a scalar function with value fv and derivative fd at x.v
+inline Dual3 lift3(Dual3 x, Real fv, Real fd) { return {fv, {fd * x.d[0], fd * x.d[1], fd * x.d[2]}}; }
+inline Dual3 legendre3(int n, Dual3 x) { Real p, dp; legendre(n, x.v, p, dp); return lift3(x, p, dp); }
+inline Dual3 kernel3(int k, Dual3 x) { const Dual r = kernelD(k, Dual{x.v, 1, 0}); return lift3(x, r.v, r.dx); }
+
 inline int basisCount(int t, int p) {
   if (t == kLine) return p + 1;
   if (t == kTri) return (p + 1) * (p + 2) / 2;
+  if (t == kTet) return (p + 1) * (p + 2) * (p + 3) / 6;
   if (t == kQuad) return (p + 1) * (p + 1);
   return (p + 1) * (p + 1) * (p + 1);
 }
@@ -246,7 +292,30 @@ inline int basisCount(int t, int p) {
 //   line: index a -> l_a(xi); quad: index a*(P+1)+b -> l_a(xi) l_b(eta); hex: index (a*(P+1)+b)*(P+1)+c.
 //   tri : vertices lambda_i; edges (0,1),(1,2),(2,0) with l_a l_b phi_{k-2}(l_b-l_a), k=2..P;
 //         bubbles l0 l1 l2 P_i(l2-l1) P_j(l1-l0), i+j<=P-3.
+//   tet : vertices lambda_i; edges (0,1),(1,2),(2,0),(3,0),(3,2),(3,1) (gmsh's edge order) with
+//         l_a l_b phi_{k-2}(l_b-l_a); face bubbles l_a l_b l_c P_i(l_c-l_b) P_j(l_b-l_a), i+j<=P-3, on the faces
+//         (a,b,c) of the face vertex table; interior l0 l1 l2 l3 P_i(l1-l0) P_j(l2-l1) P_k(l3-l2), i+j+k<=P-4.
 inline void modalBasis(int t, int p, const Real* X, Real* val, Real* grad) {
+  if (t == kTet) {
+    const Dual3 l[4] = {{1 - X[0] - X[1] - X[2], {-1, -1, -1}}, {X[0], {1, 0, 0}}, {X[1], {0, 1, 0}}, {X[2], {0, 0, 1}}};
+    std::vector<Dual3> f(l, l + 4);
+    const int edges[6][2] = {{0, 1}, {1, 2}, {2, 0}, {3, 0}, {3, 2}, {3, 1}};
+    for (const auto& e : edges)
+      for (int k = 2; k <= p; ++k) f.push_back(l[e[0]] * l[e[1]] * kernel3(k, l[e[1]] - l[e[0]]));
+    const int* fv = faceVertexTable(kTet);
+    for (int fc = 0; fc < 4; ++fc) {
+      const Dual3 a = l[fv[fc * 3]], b = l[fv[fc * 3 + 1]], c = l[fv[fc * 3 + 2]];
+      for (int s = 0; s <= p - 3; ++s)
+        for (int i = 0; i <= s; ++i) f.push_back(a * b * c * legendre3(i, c - b) * legendre3(s - i, b - a));
+    }
+    for (int s = 0; s <= p - 4; ++s)
+      for (int i = 0; i <= s; ++i)
+        for (int j = 0; j <= s - i; ++j)
+          f.push_back(l[0] * l[1] * l[2] * l[3] * legendre3(i, l[1] - l[0]) * legendre3(j, l[2] - l[1]) *
+                      legendre3(s - i - j, l[3] - l[2]));
+    for (size_t i = 0; i < f.size(); ++i) { val[i] = f[i].v; for (int k = 0; k < 3; ++k) grad[i * 3 + k] = f[i].d[k]; }
+    return;
+  }
   if (t == kLine) {
     for (int a = 0; a <= p; ++a) {
       Real v, d; lobatto(a, X[0], v, d);
@@ -300,8 +369,25 @@ inline void modalBasis(int t, int p, const Real* X, Real* val, Real* grad) {
 // (reproduces the tables of SimulationControl.cpp:381-523 from the orientation rule:
 //  line faces are traversed in reverse; quadrangle faces map (xi,eta) of the left face to
 //  rotation 0:(eta,xi) 1:(-xi,eta) 2:(-eta,-xi) 3:(xi,-eta) on the right face).
+//  Triangular faces: the right face lists the shared vertices in the opposite orientation with the left
+//  face's first vertex at position `rotation`; in barycentric terms left (xi,eta) is right
+//  0:(eta,xi) 1:(1-xi-eta,eta) 2:(xi,1-xi-eta), matched against the face rule's own points.
 inline std::vector<int> facePermutation(int t, int m, int rotation) {
   std::vector<int> perm;
+  if (t == kTet) {
+    const Quadrature fq = faceQuadrature(kTet, m);
+    for (int j = 0; j < fq.n; ++j) {
+      const Real x = fq.x[j * 3], y = fq.x[j * 3 + 1];
+      const Real X = rotation == 0 ? y : (rotation == 1 ? 1 - x - y : x);
+      const Real Y = rotation == 0 ? x : (rotation == 1 ? y : 1 - x - y);
+      int hit = -1;
+      for (int k = 0; k < fq.n; ++k)
+        if (std::fabs(fq.x[k * 3] - X) < 1e-12 && std::fabs(fq.x[k * 3 + 1] - Y) < 1e-12) hit = k;
+      if (hit < 0) throw std::runtime_error("asymmetric triangle face rule");
+      perm.push_back(hit);
+    }
+    return perm;
+  }
   if (t != kHex) { for (int j = 0; j < m; ++j) perm.push_back(m - 1 - j); return perm; }
   for (int i = 0; i < m; ++i)
     for (int k = 0; k < m; ++k) {
@@ -402,6 +488,8 @@ struct RefElement {
       if (t == kLine || t == kQuad || t == kHex) {
         int r = b;
         for (int dd = 0; dd < dim; ++dd) { deg = std::max(deg, std::max(1, r % (order + 1))); r /= order + 1; }
+      } else if (t == kTet) {  // no artificial viscosity on tetrahedra: the degrees are not needed
+        deg = 0;
       } else if (b < 3) {
         deg = 1;
       } else if (b < 3 + 3 * (order - 1)) {
@@ -421,9 +509,9 @@ struct RefElement {
       }
     lsqInv.assign(size_t(nb) * nb, 0.0);
     invert(nb, ptp.data(), lsqInv.data());
-    const int m = t == kLine ? 1 : linePoints(2 * order + 1);
+    const int m = t == kLine ? 1 : (t == kTet ? 2 * order + 1 : linePoints(2 * order + 1));
     perm.clear();
-    for (int r = 0; r < (t == kHex ? 4 : 1); ++r) perm.push_back(facePermutation(t, m, r));
+    for (int r = 0; r < (t == kHex ? 4 : (t == kTet ? 3 : 1)); ++r) perm.push_back(facePermutation(t, m, r));
   }
 };
 

@@ -118,6 +118,16 @@ static Real innerRadiusOf(int type, const double* nodes, const int* vv) {
     else { sub(2, 0, d1); sub(3, 1, d2); }
     return crossNorm(d1, d2) / per;  // 2 (|d1 x d2| / 2) / perimeter
   }
+  if (type == kTet) {  // 3V/S
+    Real a[3], b[3], c[3];
+    sub(1, 0, a); sub(2, 0, b); sub(3, 0, c);
+    const Real vol = std::fabs(a[0] * (b[1] * c[2] - b[2] * c[1]) - a[1] * (b[0] * c[2] - b[2] * c[0]) +
+                               a[2] * (b[0] * c[1] - b[1] * c[0])) / 6.0;
+    static const int tf[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {3, 1, 2}};
+    Real area = 0;
+    for (const auto& f : tf) { Real d1[3], d2[3]; sub(f[1], f[0], d1); sub(f[2], f[0], d2); area += crossNorm(d1, d2) / 2.0; }
+    return 3.0 * vol / area;
+  }
   static const int faces[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {0, 4, 7, 3}, {1, 2, 6, 5}, {2, 3, 7, 6}, {4, 5, 6, 7}};
   Real area = 0;
   for (const auto& f : faces) {
@@ -212,8 +222,10 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
     static const int quadE[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
     static const int hexE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
                                     {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
-    const int(*E)[2] = B.type == kLine ? lineE : (B.type == kTri ? triE : (B.type == kQuad ? quadE : hexE));
-    const int nE = B.type == kLine ? 1 : (B.type == kTri ? 3 : (B.type == kQuad ? 4 : 12));
+    static const int tetE[6][2] = {{0, 1}, {1, 2}, {2, 0}, {3, 0}, {3, 2}, {3, 1}};
+    const int(*E)[2] = B.type == kLine ? lineE
+                       : (B.type == kTri ? triE : (B.type == kQuad ? quadE : (B.type == kTet ? tetE : hexE)));
+    const int nE = B.type == kLine ? 1 : (B.type == kTri ? 3 : (B.type == kQuad ? 4 : (B.type == kTet ? 6 : 12)));
     Real me = 1e300;
     for (int i = 0; i < nE; ++i) {
       const double* a = &nodes[size_t(vv[E[i][0]]) * 3];
@@ -241,7 +253,7 @@ static void faceGeometry(Problem& P, Face& F, const double* nodes) {
     Real x[3] = {0, 0, 0}, tx[3] = {0, 0, 0}, ty[3] = {0, 0, 0};
     for (int k = 0; k < nfv; ++k) {
       const double* c = &nodes[size_t(vv[ft[F.fl * nfv + k]]) * 3];
-      for (int l = 0; l < 3; ++l) { x[l] += sh[k] * c[l]; tx[l] += dxi[k] * c[l]; if (nfv == 4) ty[l] += deta[k] * c[l]; }
+      for (int l = 0; l < 3; ++l) { x[l] += sh[k] * c[l]; tx[l] += dxi[k] * c[l]; if (nfv >= 3) ty[l] += deta[k] * c[l]; }
     }
     for (int l = 0; l < 3; ++l) F.coord[j * 3 + l] = x[l];
     Real n[3], det;
@@ -286,7 +298,10 @@ static void buildAdjacency(Problem& P, const sdg_mesh& m) {
   const int nbv = P.dim == 1 ? 1 : (P.dim == 2 ? 2 : 4);
   for (int64_t i = 0; i < m.boundary_count; ++i) {
     std::vector<int> key;
-    for (int k = 0; k < nbv; ++k) key.push_back(master(m.boundary_node[i * nbv + k]));
+    for (int k = 0; k < nbv; ++k) {
+      if (nbv == 4 && k == 3 && m.boundary_node[i * nbv + k] == -1) break;  // a triangle in 3D
+      key.push_back(master(m.boundary_node[i * nbv + k]));
+    }
     std::sort(key.begin(), key.end());
     bmap[key] = int(i);
   }
@@ -854,7 +869,7 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
   std::vector<Src> src;
   if (P->dim == 1) src.push_back({kLine, m->line_count, m->line_node});
   else if (P->dim == 2) { src.push_back({kTri, m->triangle_count, m->triangle_node}); src.push_back({kQuad, m->quadrangle_count, m->quadrangle_node}); }
-  else src.push_back({kHex, m->hexahedron_count, m->hexahedron_node});
+  else { src.push_back({kTet, m->tetrahedron_count, m->tetrahedron_node}); src.push_back({kHex, m->hexahedron_count, m->hexahedron_node}); }
   for (const Src& s : src) {
     if (s.n <= 0) continue;
     Block B; B.type = s.type; B.ne = s.n;

@@ -9,7 +9,7 @@ from ._abi import (ADIABATIC_NONSLIP_WALL, ADIABATIC_SLIP_WALL, BR1, BR2, CENTRA
                    HEUN_RK2, HEXAHEDRON, HLLC, INCOMPRESSIBLE_EULER, INCOMPRESSIBLE_NAVIER_STOKES, LINE,
                    ISOTHERMAL_NONSLIP_WALL, LAX_FRIEDRICHS, NAVIER_STOKES, PERIODIC, PRESSURE_OUTFLOW, QUADRANGLE,
                    RIEMANN_FARFIELD, ROE, SHOCK_NONE, ARTIFICIAL_VISCOSITY, SOURCE_BOUSSINESQ, SOURCE_NONE, SSPRK3, TRANSPORT_CONSTANT,
-                   TRANSPORT_NONE, TRANSPORT_SUTHERLAND, TRIANGLE, VELOCITY_INFLOW, VISCOUS_NONE, SdgError)
+                   TETRAHEDRON, TRANSPORT_NONE, TRANSPORT_SUTHERLAND, TRIANGLE, VELOCITY_INFLOW, VISCOUS_NONE, SdgError)
 from .solver import (INITIAL_FUNCTION, INITIAL_LAST_STEP, INITIAL_SPECIFIC_FILE, Batch, GpuSolver, Mesh, System,
                      make_config)
 

@@ -26,7 +26,7 @@ ERRORS = {
 }
 globals().update({name: code for code, name in ERRORS.items()})
 
-LINE, TRIANGLE, QUADRANGLE, HEXAHEDRON = 1, 2, 3, 5
+LINE, TRIANGLE, QUADRANGLE, TETRAHEDRON, HEXAHEDRON = 1, 2, 3, 4, 5
 EULER, NAVIER_STOKES, INCOMPRESSIBLE_EULER, INCOMPRESSIBLE_NAVIER_STOKES = 0, 1, 2, 3
 SOURCE_NONE, SOURCE_BOUSSINESQ = 0, 1
 SHOCK_NONE, ARTIFICIAL_VISCOSITY = 0, 1
@@ -60,6 +60,8 @@ class SdgMesh(ctypes.Structure):
         ("physical_boundary_condition", _p_int32),
         ("line_count", c_int64),
         ("line_node", _p_int32),
+        ("tetrahedron_count", c_int64),
+        ("tetrahedron_node", _p_int32),
     ]
 
 
@@ -159,6 +161,9 @@ SIGNATURES = {
     "sdg_mesh_generate_1d": (c_int32, [c_double, c_double, c_int32, c_int32, _p_int32, c_void_p]),
     "sdg_mesh_generate_3d": (c_int32, [c_double, c_double, c_double, c_double, c_double, c_double, c_int32,
                                        c_int32, c_int32, c_int32, _p_int32, POINTER(SdgGeneratedMesh)]),
+    "sdg_mesh_generate_3d_tetrahedra": (c_int32, [c_double, c_double, c_double, c_double, c_double, c_double,
+                                                  c_int32, c_int32, c_int32, c_int32, _p_int32,
+                                                  POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_read_msh": (c_int32, [c_char_p, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_free": (c_int32, [POINTER(SdgGeneratedMesh)]),
     "sdg_get_node_artificial_viscosity": (c_int32, [c_void_p, _p_double]),

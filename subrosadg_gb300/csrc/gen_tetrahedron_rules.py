@@ -1,0 +1,199 @@
+"""Generate tetrahedron_rules.h: symmetric Gauss rules for tetrahedra and their triangular faces.
+
+The reference obtains its rules from gmsh ("Gauss{order}", src/Mesh/Quadrature.cpp:28-34) with the
+orders of src/Solver/SimulationControl.cpp:268-283: volume 2P, face 2P+1.  For P = 1..3 the point
+counts are
+  tetrahedron volume, orders 2/4/6 : 4 / 11 / 24 points (kTetrahedronQuadratureNumber), the counts of
+      P. Keast, "Moderate-degree tetrahedral quadrature formulas", CMAME 55 (1986);
+  triangle face, orders 3/5/7      : 4 / 7 / 13 points (kTriangleQuadratureNumber), the counts of
+      D.A. Dunavant, "High degree efficient symmetrical Gaussian quadrature rules for the triangle",
+      IJNME 21 (1985).
+This script takes the published orbit structure and starting values, polishes them with Newton's method
+on the moment equations so every monomial up to the rule's degree is integrated to round-off, and writes
+the rules on the reference elements (0,0,0),(1,0,0),(0,1,0),(0,0,1) (weights summing to 1/6) and
+(0,0),(1,0),(0,1) (weights summing to 1/2).
+
+The face rules list their points in the orbit order that the reference's face-point permutations
+(src/Solver/SimulationControl.cpp:405-434, the Triangle cases for P = 1..3) imply: the centroid, then each
+3-point orbit as (a,a), (a,1-2a), (1-2a,a), then the 6-point orbit with barycentric values (x,y,z) as
+(x,y), (y,z), (z,x), (x,z), (y,x), (z,y).  The point values themselves are unpinned against gmsh, which
+is not vendored with the reference.
+
+Run:  python gen_tetrahedron_rules.py > tetrahedron_rules.h
+"""
+import math
+
+import numpy as np
+
+
+def tri_exact(a, b):
+    return math.factorial(a) * math.factorial(b) / math.factorial(a + b + 2)
+
+
+def tet_exact(a, b, c):
+    return math.factorial(a) * math.factorial(b) * math.factorial(c) / math.factorial(a + b + c + 3)
+
+
+def tri_build(params, orbits):
+    pts, w, k = [], [], 0
+    for o in orbits:
+        if o == "c":
+            pts.append((1 / 3, 1 / 3)); w.append(params[k]); k += 1
+        elif o == "s21":
+            a, wt = params[k], params[k + 1]; k += 2
+            for p in [(a, a), (a, 1 - 2 * a), (1 - 2 * a, a)]:
+                pts.append(p); w.append(wt)
+        else:
+            x, y, wt = params[k], params[k + 1], params[k + 2]; k += 3
+            z = 1 - x - y
+            for p in [(x, y), (y, z), (z, x), (x, z), (y, x), (z, y)]:
+                pts.append(p); w.append(wt)
+    return np.array(pts), np.array(w)
+
+
+def tet_build(params, orbits):
+    bary, w, k = [], [], 0
+    for o in orbits:
+        if o == "c":
+            bary.append((0.25, 0.25, 0.25, 0.25)); w.append(params[k]); k += 1
+        elif o == "s31":
+            a, wt = params[k], params[k + 1]; k += 2
+            b = 1 - 3 * a
+            for i in range(4):
+                l = [a] * 4; l[i] = b
+                bary.append(tuple(l)); w.append(wt)
+        elif o == "s22":
+            a, wt = params[k], params[k + 1]; k += 2
+            b = 0.5 - a
+            for i in range(4):
+                for j in range(i + 1, 4):
+                    l = [b] * 4; l[i] = a; l[j] = a
+                    bary.append(tuple(l)); w.append(wt)
+        else:  # s211: (a, a, b, c)
+            a, b, wt = params[k], params[k + 1], params[k + 2]; k += 3
+            c = 1 - 2 * a - b
+            for i in range(4):
+                for j in range(i + 1, 4):
+                    rest = [m for m in range(4) if m not in (i, j)]
+                    for r0, r1 in ((rest[0], rest[1]), (rest[1], rest[0])):
+                        l = [0.0] * 4; l[i] = a; l[j] = a; l[r0] = b; l[r1] = c
+                        bary.append(tuple(l)); w.append(wt)
+    bary = np.array(bary)
+    return bary[:, 1:], np.array(w)
+
+
+def tri_resid(params, orbits, deg):
+    p, w = tri_build(params, orbits)
+    return np.array([(w * p[:, 0] ** a * p[:, 1] ** b).sum() - tri_exact(a, b)
+                     for a in range(deg + 1) for b in range(deg + 1 - a)])
+
+
+def tet_resid(params, orbits, deg):
+    p, w = tet_build(params, orbits)
+    return np.array([(w * p[:, 0] ** a * p[:, 1] ** b * p[:, 2] ** c).sum() - tet_exact(a, b, c)
+                     for a in range(deg + 1) for b in range(deg + 1 - a) for c in range(deg + 1 - a - b)])
+
+
+# Dunavant's odd-degree rules: orbit structure and published values (weights normalised to area 1).
+FACE_RULES = {
+    3: (["c", "s21"], [-27 / 48, 0.2, 25 / 48]),
+    5: (["c", "s21", "s21"], [0.225000000000000, 0.470142064105115, 0.132394152788506,
+                              0.101286507323456, 0.125939180544827]),
+    7: (["c", "s21", "s21", "s111"], [-0.149570044467682, 0.260345966079040, 0.175615257433208,
+                                      0.065130102902216, 0.053347235608838,
+                                      0.048690315425316, 0.312865496004874, 0.077113760890257]),
+}
+# Keast's rules of degree 2, 4 and 6: orbit structure and published values (weights for volume 1/6).
+VOLUME_RULES = {
+    2: (["s31"], [(5 - math.sqrt(5)) / 20, 1 / 24]),
+    4: (["c", "s31", "s22"], [-0.013155555555556, 0.071428571428571, 0.007622222222222,
+                              0.399403576166799, 0.024888888888889]),
+    6: (["s31", "s31", "s31", "s211"], [0.214602871259152, 0.006653791709695,
+                                        0.040673958534611, 0.001679535175887,
+                                        0.322337890142276, 0.009226196923942,
+                                        0.063661001875018, 0.269672331458316, 0.008035714285714]),
+}
+
+
+def polish(resid, orbits, x0, deg):
+    x = np.array(x0, dtype=float)
+    for _ in range(10):
+        r = resid(x, orbits, deg)
+        jac = np.zeros((len(r), len(x)))
+        for i in range(len(x)):
+            h = 1e-7
+            xp = x.copy(); xp[i] += h
+            xm = x.copy(); xm[i] -= h
+            jac[:, i] = (resid(xp, orbits, deg) - resid(xm, orbits, deg)) / (2 * h)
+        step = np.linalg.lstsq(jac, -r, rcond=None)[0]
+        # a step that does not reduce the residual ends the iteration (closed-form values stay as they are)
+        if np.linalg.norm(resid(x + step, orbits, deg)) >= np.linalg.norm(r):
+            break
+        x = x + step
+    return x
+
+
+def weight_positions(orbits):
+    k, out = 0, []
+    for o in orbits:
+        step = {"c": 1, "s21": 2, "s111": 3, "s31": 2, "s22": 2, "s211": 3}[o]
+        out.append(k + step - 1)
+        k += step
+    return out
+
+
+def main():
+    fmt = lambda v: ", ".join("%.17g" % t for t in v)
+    print("// Generated by gen_tetrahedron_rules.py -- do not edit.")
+    print("// Tetrahedron volume rules (Keast 1986 orbit structure) and triangle face rules (Dunavant 1985,")
+    print("// odd degrees, in the reference's face-point orbit order), Newton-polished.")
+    print("// Reference tetrahedron (0,0,0),(1,0,0),(0,1,0),(0,0,1): weights sum to 1/6.")
+    print("// Reference triangle (0,0),(1,0),(0,1): weights sum to 1/2.")
+    print("#pragma once")
+    print("namespace sdg_tables {")
+    print("struct FaceTriangleRule { int degree; int count; const double* xi; const double* eta; const double* weight; };")
+    print("struct TetrahedronRule { int degree; int count; const double* xi; const double* eta; const double* zeta;")
+    print("                         const double* weight; };")
+    faces = []
+    for deg, (orb, p0) in FACE_RULES.items():
+        x0 = np.array(p0)
+        for k in weight_positions(orb):
+            x0[k] *= 0.5
+        x = polish(tri_resid, orb, x0, deg)
+        err = np.abs(tri_resid(x, orb, deg)).max()
+        assert err < 1e-15, (deg, err)
+        assert np.abs(x - x0).max() < 1e-11, (deg, np.abs(x - x0).max())
+        p, w = tri_build(x, orb)
+        n = len(w)
+        print(f"// face degree {deg}: {n} points, max moment error {err:.1e}")
+        print(f"inline constexpr double kFaceTri{deg}Xi[{n}] = {{{fmt(p[:, 0])}}};")
+        print(f"inline constexpr double kFaceTri{deg}Eta[{n}] = {{{fmt(p[:, 1])}}};")
+        print(f"inline constexpr double kFaceTri{deg}W[{n}] = {{{fmt(w)}}};")
+        faces.append((deg, n))
+    vols = []
+    for deg, (orb, p0) in VOLUME_RULES.items():
+        x = polish(tet_resid, orb, p0, deg)
+        err = np.abs(tet_resid(x, orb, deg)).max()
+        assert err < 1e-15, (deg, err)
+        assert np.abs(x - np.array(p0)).max() < 1e-11, (deg, np.abs(x - np.array(p0)).max())
+        p, w = tet_build(x, orb)
+        n = len(w)
+        print(f"// volume degree {deg}: {n} points, max moment error {err:.1e}")
+        print(f"inline constexpr double kTet{deg}Xi[{n}] = {{{fmt(p[:, 0])}}};")
+        print(f"inline constexpr double kTet{deg}Eta[{n}] = {{{fmt(p[:, 1])}}};")
+        print(f"inline constexpr double kTet{deg}Zeta[{n}] = {{{fmt(p[:, 2])}}};")
+        print(f"inline constexpr double kTet{deg}W[{n}] = {{{fmt(w)}}};")
+        vols.append((deg, n))
+    print("inline constexpr FaceTriangleRule kFaceTriangleRules[] = {")
+    for deg, n in faces:
+        print(f"    {{{deg}, {n}, kFaceTri{deg}Xi, kFaceTri{deg}Eta, kFaceTri{deg}W}},")
+    print("};")
+    print("inline constexpr TetrahedronRule kTetrahedronRules[] = {")
+    for deg, n in vols:
+        print(f"    {{{deg}, {n}, kTet{deg}Xi, kTet{deg}Eta, kTet{deg}Zeta, kTet{deg}W}},")
+    print("};")
+    print("}  // namespace sdg_tables")
+
+
+if __name__ == "__main__":
+    main()

@@ -45,6 +45,7 @@ void facePointInParent(int type, int f, const double* fx, double* X) {
   double sh[4];
   if (nfv == 1) sh[0] = 1.0;
   else if (nfv == 2) { sh[0] = 0.5 * (1 - fx[0]); sh[1] = 0.5 * (1 + fx[0]); }
+  else if (nfv == 3) { sh[0] = 1 - fx[0] - fx[1]; sh[1] = fx[0]; sh[2] = fx[1]; }
   else {
     const double x = fx[0], y = fx[1];
     sh[0] = 0.25 * (1 - x) * (1 - y); sh[1] = 0.25 * (1 + x) * (1 - y);
@@ -55,6 +56,24 @@ void facePointInParent(int type, int f, const double* fx, double* X) {
     double V[3]; referenceVertex(type, fl[f * nfv + k], V);
     for (int d = 0; d < 3; ++d) X[d] += sh[k] * V[d];
   }
+}
+
+// Face-point pairing of triangular faces (the Triangle cases of SimulationControl.cpp:405-434, derived from
+// the geometry): the right face lists the shared vertices in the opposite orientation with the left face's
+// first vertex at position r, so left point (xi, eta) is right point r=0: (eta, xi), r=1: (1-xi-eta, eta),
+// r=2: (xi, 1-xi-eta).  Returns [3][nfq].
+std::vector<int> triangleFacePermutation(int type, int p) {
+  const PointRule fr = faceRule(type, p);
+  std::vector<int> perm(size_t(3) * fr.n, -1);
+  for (int r = 0; r < 3; ++r)
+    for (int j = 0; j < fr.n; ++j) {
+      const double x = fr.x[j * 3], y = fr.x[j * 3 + 1];
+      const double X = r == 0 ? y : (r == 1 ? 1 - x - y : x), Y = r == 0 ? x : (r == 1 ? y : 1 - x - y);
+      for (int k = 0; k < fr.n; ++k)
+        if (std::fabs(fr.x[k * 3] - X) < 1e-12 && std::fabs(fr.x[k * 3 + 1] - Y) < 1e-12) perm[size_t(r) * fr.n + j] = k;
+      if (perm[size_t(r) * fr.n + j] < 0) throw Failure(SDG_ERR_INVALID_ARGUMENT, "face rule is not symmetric");
+    }
+  return perm;
 }
 
 // ---- point-layout conversions ----------------------------------------------------------------------
@@ -227,6 +246,12 @@ void shapeGrad(int type, const double* X, double* N, double* G /* [nv][3] */) {
     std::copy(g, g + 9, G);
     return;
   }
+  if (type == SDG_ELEMENT_TETRAHEDRON) {
+    N[0] = 1 - X[0] - X[1] - X[2]; N[1] = X[0]; N[2] = X[1]; N[3] = X[2];
+    const double g[12] = {-1, -1, -1, 1, 0, 0, 0, 1, 0, 0, 0, 1};
+    std::copy(g, g + 12, G);
+    return;
+  }
   for (int v = 0; v < nv; ++v) {
     double R[3]; referenceVertex(type, v, R);
     const double a = 1 + R[0] * X[0], b = 1 + R[1] * X[1];
@@ -273,7 +298,7 @@ double adjugate(int dim, const double J[3][3], double A[3][3]) {
 }
 
 bool isAffine(int type, const double* nodes, const int32_t* vv, double tol) {
-  if (type == SDG_ELEMENT_TRIANGLE || type == SDG_ELEMENT_LINE) return true;
+  if (type == SDG_ELEMENT_TRIANGLE || type == SDG_ELEMENT_LINE || type == SDG_ELEMENT_TETRAHEDRON) return true;
   const auto P = [&](int k, int d) { return nodes[size_t(vv[k]) * 3 + d]; };
   for (int d = 0; d < 3; ++d) {
     if (type == SDG_ELEMENT_QUADRANGLE) {
@@ -293,9 +318,13 @@ double minEdgeOf(int type, const double* nodes, const int32_t* vv) {
   static const int triE[3][2] = {{0, 1}, {1, 2}, {2, 0}};
   static const int quadE[4][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}};
   static const int hexE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+  static const int tetE[6][2] = {{0, 1}, {1, 2}, {2, 0}, {3, 0}, {3, 2}, {3, 1}};
   const int(*E)[2] = type == SDG_ELEMENT_LINE ? lineE
-                     : (type == SDG_ELEMENT_TRIANGLE ? triE : (type == SDG_ELEMENT_QUADRANGLE ? quadE : hexE));
-  const int nE = type == SDG_ELEMENT_LINE ? 1 : (type == SDG_ELEMENT_TRIANGLE ? 3 : (type == SDG_ELEMENT_QUADRANGLE ? 4 : 12));
+                     : (type == SDG_ELEMENT_TRIANGLE ? triE
+                        : (type == SDG_ELEMENT_QUADRANGLE ? quadE : (type == SDG_ELEMENT_TETRAHEDRON ? tetE : hexE)));
+  const int nE = type == SDG_ELEMENT_LINE ? 1
+                 : (type == SDG_ELEMENT_TRIANGLE ? 3
+                    : (type == SDG_ELEMENT_QUADRANGLE ? 4 : (type == SDG_ELEMENT_TETRAHEDRON ? 6 : 12)));
   double best = 1e300;
   for (int i = 0; i < nE; ++i) {
     double s = 0;
@@ -407,7 +436,8 @@ void resolveBlock(DevBlock& B, int slot, bool br2) {
                                        : denseStageVariant(B.type, B.p, B.affine != 0, visc);
   B.gradV = B.kind == kTensor ? tensorGradVariant(B.dim, B.n, B.affine != 0, br2)
                               : denseGradVariant(B.type, B.p, B.affine != 0);
-  if (!B.stageV[0].valid() || !B.stageV[1].valid() || !B.stageV[2].valid() || !B.gradV.valid())
+  // the variant of the block's equations must exist (tetrahedra: the Euler stage only)
+  if (!B.stageV[slot].valid() || (slot > 0 && !B.gradV.valid()))
     throw Failure(SDG_ERR_UNSUPPORTED, "unsupported element block (type, order, affine)");
   const KernelVariant& v = B.stageV[slot];
   B.ustride = ((B.dim + 2) * B.nb + 1) & ~1;
@@ -481,7 +511,7 @@ Rec faceRec(sdg_handle* h, int op) {
   std::memset(&f, 0, sizeof(f));
   f.face = h->face; f.other = h->faceOther; f.faceGrad = h->faceGrad; f.faceFlux = h->faceFlux;
   f.conn = bnd ? h->bconn : h->fconn; f.fgeo = bnd ? h->bgeo : h->fgeo; f.ghost = h->ghost;
-  f.nface = bnd ? h->nBoundary : h->nInterior; f.n1d = h->n1d; f.ph = h->ph;
+  f.nface = bnd ? h->nBoundary : h->nInterior; f.n1d = h->n1d; f.ph = h->ph; f.perm = h->facePerm;
   r.units = (f.nface * h->nfq + kFaceThreads - 1) / kFaceThreads;
   return r;
 }
@@ -842,6 +872,14 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       if (mesh->triangle_count > 0) mb.push_back({SDG_ELEMENT_TRIANGLE, mesh->triangle_count, mesh->triangle_node});
       if (mesh->quadrangle_count > 0) mb.push_back({SDG_ELEMENT_QUADRANGLE, mesh->quadrangle_count, mesh->quadrangle_node});
     } else {
+      if (mesh->tetrahedron_count > 0 && mesh->hexahedron_count > 0)
+        throw Failure(SDG_ERR_UNSUPPORTED, "a mesh of tetrahedra and hexahedra needs pyramids, which are not built");
+      if (mesh->tetrahedron_count > 0) {
+        mb.push_back({SDG_ELEMENT_TETRAHEDRON, mesh->tetrahedron_count, mesh->tetrahedron_node});
+        if (c.polynomial_order > 3) throw Failure(SDG_ERR_UNSUPPORTED, "tetrahedra are built for P = 1..3");
+        if (viscous || h->av)
+          throw Failure(SDG_ERR_UNSUPPORTED, "tetrahedra are built for the Euler equations without artificial viscosity");
+      }
       if (mesh->hexahedron_count > 0) mb.push_back({SDG_ELEMENT_HEXAHEDRON, mesh->hexahedron_count, mesh->hexahedron_node});
     }
     if (mb.empty()) throw Failure(SDG_ERR_INVALID_ARGUMENT, "mesh has no elements of its dimension");
@@ -858,12 +896,15 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     for (const Block& b : mb) {
       DevBlock B;
       B.type = b.type; B.dim = typeDim(b.type); B.p = h->p; B.ne = b.count; B.nface = typeFaces(b.type);
-      B.kind = (b.type == SDG_ELEMENT_TRIANGLE || (b.type == SDG_ELEMENT_QUADRANGLE && h->p == 1)) ? kDense : kTensor;
+      B.kind = (b.type == SDG_ELEMENT_TRIANGLE || b.type == SDG_ELEMENT_TETRAHEDRON ||
+                (b.type == SDG_ELEMENT_QUADRANGLE && h->p == 1))
+                   ? kDense
+                   : kTensor;
       B.n = h->p + 1;
       B.nb = modalCount(b.type, h->p);
       const PointRule vr = volumeRule(b.type, h->p);
       B.nq = vr.n; B.qweight = vr.w;
-      B.nfq = h->dim == 1 ? 1 : (h->dim == 2 ? B.n : B.n * B.n);
+      B.nfq = faceRule(b.type, h->p).n;
       B.affine = 1;
       for (int64_t e = 0; e < b.count && B.affine; ++e)
         if (!isAffine(b.type, nodes, b.vertex + e * typeVertices(b.type), tol)) B.affine = 0;
@@ -940,9 +981,16 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
           for (int f = 0; f < B.nface; ++f) {
             const double* p0 = &nodes[size_t(vv[fl[f * nfv]]) * 3];
             const double* p1 = &nodes[size_t(vv[fl[f * nfv + 1]]) * 3];
-            const double tx = 0.5 * (p1[0] - p0[0]), ty = 0.5 * (p1[1] - p0[1]);
-            B.fmetricHost[(size_t(e) * B.nface + f) * 2 + 0] = ty;
-            B.fmetricHost[(size_t(e) * B.nface + f) * 2 + 1] = -tx;
+            double* m = &B.fmetricHost[(size_t(e) * B.nface + f) * B.dim];
+            if (B.dim == 3) {  // triangular face: n |J_f| = (p1 - p0) x (p2 - p0) (reference area 1/2)
+              const double* p2 = &nodes[size_t(vv[fl[f * nfv + 2]]) * 3];
+              const double a[3] = {p1[0] - p0[0], p1[1] - p0[1], p1[2] - p0[2]};
+              const double c[3] = {p2[0] - p0[0], p2[1] - p0[1], p2[2] - p0[2]};
+              m[0] = a[1] * c[2] - a[2] * c[1]; m[1] = a[2] * c[0] - a[0] * c[2]; m[2] = a[0] * c[1] - a[1] * c[0];
+            } else {
+              const double tx = 0.5 * (p1[0] - p0[0]), ty = 0.5 * (p1[1] - p0[1]);
+              m[0] = ty; m[1] = -tx;
+            }
           }
         }
       }
@@ -953,7 +1001,8 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       h->dof += B.ne * B.nb * h->nv;
       h->blocks.push_back(std::move(B));
     }
-    h->nfq = h->blocks[0].nfq; h->n1d = h->p + 1;
+    h->nfq = h->blocks[0].nfq;
+    h->n1d = h->blocks[0].type == SDG_ELEMENT_TETRAHEDRON ? -h->nfq : h->p + 1;
     for (int op = 0; op < kFaceOps; ++op) h->faceV[op] = facePointVariant(op, h->dim, c.convective_flux);
     h->volumePoints = int64_t(pointOff);
     h->stateCount = stateOff;
@@ -978,6 +1027,12 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         const double tx = 0.5 * (q[1][0] - q[0][0]), ty = 0.5 * (q[1][1] - q[0][1]);
         area = std::sqrt(tx * tx + ty * ty);
         n[0] = ty / area; n[1] = -tx / area;
+      } else if (nfv == 3) {  // triangular face: |J_f| = |(q1 - q0) x (q2 - q0)| (reference area 1/2)
+        double a[3], b[3];
+        for (int d = 0; d < 3; ++d) { a[d] = q[1][d] - q[0][d]; b[d] = q[2][d] - q[0][d]; }
+        const double cx = a[1] * b[2] - a[2] * b[1], cy = a[2] * b[0] - a[0] * b[2], cz = a[0] * b[1] - a[1] * b[0];
+        area = std::sqrt(cx * cx + cy * cy + cz * cz);
+        n[0] = cx / area; n[1] = cy / area; n[2] = cz / area;
       } else {
         double planar = 0;
         for (int d = 0; d < 3; ++d) planar = std::max(planar, std::fabs(q[0][d] + q[2][d] - q[1][d] - q[3][d]));
@@ -996,6 +1051,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
           const double x = fr.x[j * 3], y = fr.x[j * 3 + 1];
           if (nfv == 1) sh[0] = 1.0;
           else if (nfv == 2) { sh[0] = 0.5 * (1 - x); sh[1] = 0.5 * (1 + x); }
+          else if (nfv == 3) { sh[0] = 1 - x - y; sh[1] = x; sh[2] = y; }
           else { sh[0] = 0.25 * (1 - x) * (1 - y); sh[1] = 0.25 * (1 + x) * (1 - y); sh[2] = 0.25 * (1 + x) * (1 + y); sh[3] = 0.25 * (1 - x) * (1 + y); }
           for (int d = 0; d < 3; ++d) {
             double s = 0; for (int k = 0; k < nfv; ++k) s += sh[k] * q[k][d];
@@ -1070,6 +1126,10 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       SDG_CUDA(cudaMemsetAsync(h->grad, 0, h->gradCount * 8, h->stream));
     }
     h->fconn = devAlloc<int>(fconn.size()); upload(h->fconn, fconn, h->stream);
+    if (h->n1d < 0) {
+      const std::vector<int> perm = triangleFacePermutation(h->blocks[0].type, h->p);
+      h->facePerm = devAlloc<int>(perm.size()); upload(h->facePerm, perm, h->stream);
+    }
     h->fgeo = devAlloc<double>(fgeo.size()); upload(h->fgeo, fgeo, h->stream);
     h->bconn = devAlloc<int>(bconn.size()); upload(h->bconn, bconn, h->stream);
     h->bgeo = devAlloc<double>(bgeo.size()); upload(h->bgeo, bgeo, h->stream);
@@ -1132,6 +1192,7 @@ int sdg_destroy(sdg_handle* h) {
   }
   cudaFree(h->nodeAV);
   cudaFree(h->state[0]); cudaFree(h->state[1]); cudaFree(h->face); cudaFree(h->fconn); cudaFree(h->fgeo);
+  cudaFree(h->facePerm);
   cudaFree(h->bconn); cudaFree(h->bgeo); cudaFree(h->ghost); cudaFree(h->scratch); cudaFree(h->relPart);
   cudaFree(h->relOut); cudaFree(h->dtPart); cudaFree(h->status);
   cudaFree(h->faceOther); cudaFree(h->faceGrad); cudaFree(h->faceFlux); cudaFree(h->grad);

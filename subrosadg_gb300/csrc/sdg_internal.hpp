@@ -124,7 +124,8 @@ struct sdg_handle {
   size_t gradCount = 0;
   int* fconn = nullptr; double* fgeo = nullptr; int64_t nInterior = 0;
   int* bconn = nullptr; double* bgeo = nullptr; double* ghost = nullptr; int64_t nBoundary = 0;
-  int nfq = 0, n1d = 0;
+  int nfq = 0, n1d = 0;           // n1d < 0: triangular faces of -n1d points, paired through facePerm
+  int* facePerm = nullptr;        // [3][nfq] right point of left point j at rotation r (triangular faces)
   std::vector<int32_t> adjInterior, adjBoundary;
   std::vector<double> bcoord; std::vector<int32_t> bphys;
   std::vector<int32_t> boundaryParent;  // per boundary face: (block, element) of its parent

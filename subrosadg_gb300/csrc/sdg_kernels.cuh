@@ -123,10 +123,11 @@ struct AvArgs {
   double s0, kappa, factor;
 };
 
-// Points per face of a tensor block: 1 (the point faces of a line), N (quadrangle edges), N^2 (hexahedron faces).
+// Points per face: 1 (the point faces of a line), N (quadrangle edges), N^2 (hexahedron faces).  Triangular
+// faces (tetrahedra) carry n1d = -(points per face) and pair their points through a permutation table.
 template <int DIM>
 __host__ __device__ __forceinline__ constexpr int nfqOf(int n1d) {
-  return DIM == 1 ? 1 : (DIM == 2 ? n1d : n1d * n1d);
+  return DIM == 1 ? 1 : (DIM == 2 ? n1d : (n1d < 0 ? -n1d : n1d * n1d));
 }
 
 template <int DIM, int N>
@@ -470,6 +471,7 @@ struct FaceArgs {
   const double* faceGrad;    // Navier-Stokes: gradient traces [slot][v*d+k][j]
   double* faceFlux;          // Navier-Stokes: face fluxes
   const int* conn;           // interior: (slot L, slot R, rotation); boundary: (slot, condition, 0)
+  const int* perm;           // triangular faces: right point of left point j at rotation r, [3][nfq]
   const double* fgeo;        // per face (n, |J_f|)
   const double* ghost;       // boundary: [face][j][rho, u, e, p]
   int64_t nface;
@@ -513,7 +515,7 @@ __device__ __forceinline__ void faceInteriorPoint(const FaceArgs& a, int64_t t) 
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
   const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
-  const int jr = rightPoint<DIM>(j, rot, n1d);
+  const int jr = (DIM == 3 && n1d < 0) ? a.perm[rot * nfq + j] : rightPoint<DIM>(j, rot, n1d);
   double* L = a.face + int64_t(sl) * NV * nfq + j;
   double* R = a.face + int64_t(sr) * NV * nfq + jr;
   double ul[NV], ur[NV];

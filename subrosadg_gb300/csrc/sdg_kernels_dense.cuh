@@ -18,19 +18,21 @@
 
 namespace sdg {
 
-// Table layout (doubles): phi[NQ][NB] | dphiw[NQ][2][NB] (w_q dphi/dxi_b) | phif[NFP][NB] |
+// Table layout (doubles, d = 2, or 3 on tetrahedra): phi[NQ][NB] | dphiw[NQ][d][NB] (w_q dphi/dxi_b) | phif[NFP][NB] |
 //                         phifw[NFP][NB] (wf_j phif) | mref[NB][NB] (inverse reference mass matrix) |
 //   modal gradient operators of affine elements (M = |J| M_ref folds M^-1 into them):
-//                         dmod[2][NB][NB]  D_b = M_ref^-1 S_b, S_b(k,m) = sum_q w_q dphi_k/dxi_b phi_m
+//                         dmod[d][NB][NB]  D_b = M_ref^-1 S_b, S_b(k,m) = sum_q w_q dphi_k/dxi_b phi_m
 //                         emod[NF][NB][NFQ] E_f = M_ref^-1 Phi_f^T W_f (lift of face f's point values)
 //                         lmod[NF][NFQ][NFQ] L_f = Phi_f E_f (trace at face f of the lift from face f)
 //   source weights:        phiw[NQ][NB] w_q phi (volume source terms)
-inline size_t denseTableSize(int nb, int nq, int nfp) { return size_t(nq) * nb * 3 + size_t(nfp) * nb * 2 + size_t(nb) * nb; }
-inline size_t denseGradOperatorSize(int nb, int nf, int nfq) {
-  return size_t(2) * nb * nb + size_t(nf) * nb * nfq + size_t(nf) * nfq * nfq;
+inline size_t denseTableSize(int nb, int nq, int nfp, int dim = 2) {
+  return size_t(nq) * nb * (1 + dim) + size_t(nfp) * nb * 2 + size_t(nb) * nb;
 }
-inline size_t denseSourceTableOffset(int nb, int nq, int nfp, int nf, int nfq) {
-  return denseTableSize(nb, nq, nfp) + denseGradOperatorSize(nb, nf, nfq);
+inline size_t denseGradOperatorSize(int nb, int nf, int nfq, int dim = 2) {
+  return size_t(dim) * nb * nb + size_t(nf) * nb * nfq + size_t(nf) * nfq * nfq;
+}
+inline size_t denseSourceTableOffset(int nb, int nq, int nfp, int nf, int nfq, int dim = 2) {
+  return denseTableSize(nb, nq, nfp, dim) + denseGradOperatorSize(nb, nf, nfq, dim);
 }
 
 template <class R>
@@ -58,11 +60,11 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
                              std::vector<double>& lsqOut) {
   const int nb = modalCount(type, p);
   const PointRule vr = volumeRule(type, p), fr = faceRule(type, p);
-  const int nq = vr.n, nf = typeFaces(type), nfq = fr.n, nfp = nf * nfq;
-  tables.assign(denseSourceTableOffset(nb, nq, nfp, nf, nfq) + size_t(nq) * nb, 0.0);
+  const int nq = vr.n, nf = typeFaces(type), nfq = fr.n, nfp = nf * nfq, dim = typeDim(type);
+  tables.assign(denseSourceTableOffset(nb, nq, nfp, nf, nfq, dim) + size_t(nq) * nb, 0.0);
   double* phi = tables.data();
   double* dphiw = phi + size_t(nq) * nb;
-  double* phif = dphiw + size_t(nq) * 2 * nb;
+  double* phif = dphiw + size_t(nq) * dim * nb;
   double* phifw = phif + size_t(nfp) * nb;
   double* mref = phifw + size_t(nfp) * nb;
   std::vector<double> v(nb), g(size_t(nb) * 3);
@@ -70,8 +72,7 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
     modalBasis(type, p, &vr.x[q * 3], v.data(), g.data());
     for (int b = 0; b < nb; ++b) {
       phi[size_t(q) * nb + b] = v[b];
-      dphiw[(size_t(q) * 2 + 0) * nb + b] = vr.w[q] * g[b * 3 + 0];
-      dphiw[(size_t(q) * 2 + 1) * nb + b] = vr.w[q] * g[b * 3 + 1];
+      for (int k = 0; k < dim; ++k) dphiw[(size_t(q) * dim + k) * nb + b] = vr.w[q] * g[b * 3 + k];
     }
   }
   for (int f = 0; f < nf; ++f)
@@ -100,15 +101,15 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
   std::copy(inv.begin(), inv.end(), mref);
   {
     double* dmod = mref + size_t(nb) * nb;
-    double* emod = dmod + size_t(2) * nb * nb;
+    double* emod = dmod + size_t(dim) * nb * nb;
     double* lmod = emod + size_t(nf) * nb * nfq;
-    for (int b = 0; b < 2; ++b) {
+    for (int b = 0; b < dim; ++b) {
       std::vector<long double> sb(size_t(nb) * nb, 0.0L);
       for (int k = 0; k < nb; ++k)
         for (int mm = 0; mm < nb; ++mm) {
           long double acc = 0.0L;
           for (int q = 0; q < nq; ++q)
-            acc += (long double)dphiw[(size_t(q) * 2 + b) * nb + k] * (long double)phi[size_t(q) * nb + mm];
+            acc += (long double)dphiw[(size_t(q) * dim + b) * nb + k] * (long double)phi[size_t(q) * nb + mm];
           sb[size_t(k) * nb + mm] = acc;
         }
       for (int i = 0; i < nb; ++i)
@@ -138,7 +139,7 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
         }
   }
   {
-    double* phiw = tables.data() + denseSourceTableOffset(nb, nq, nfp, nf, nfq);
+    double* phiw = tables.data() + denseSourceTableOffset(nb, nq, nfp, nf, nfq, dim);
     for (int q = 0; q < nq; ++q)
       for (int b = 0; b < nb; ++b) phiw[size_t(q) * nb + b] = vr.w[q] * phi[size_t(q) * nb + b];
   }
@@ -160,52 +161,54 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
   }
 }
 
-template <int NB, int NQ, int NFQ, int NF>
+template <int NB, int NQ, int NFQ, int NF, int DIM = 2>
 struct DenseShape {
-  static constexpr int NV = 4;
+  static constexpr int NV = DIM + 2;
   static constexpr int NFP = NF * NFQ;
   static constexpr int USTRIDE = (NV * NB + 1) & ~1;
   static constexpr int FSTRIDE = NF * NV * NFQ;
-  static constexpr int PER_ELEM = USTRIDE + FSTRIDE + 2 * NV * NQ + NV * NB + NV * NB;
+  static_assert(DIM * NQ >= NB && NV * NB >= NQ, "shared-memory reuse of the point and coefficient buffers");
+  static constexpr int PER_ELEM = USTRIDE + FSTRIDE + DIM * NV * NQ + NV * NB + NV * NB;
   static constexpr int EPB = 16;
   static constexpr int THREADS = 256;
-  static constexpr size_t TABLES = size_t(NQ) * NB * 3 + size_t(NFP) * NB * 2 + size_t(NB) * NB;
+  static constexpr size_t TABLES = size_t(NQ) * NB * (1 + DIM) + size_t(NFP) * NB * 2 + size_t(NB) * NB;
   static constexpr size_t SMEM = (size_t(EPB) * PER_ELEM + TABLES) * 8 + 16 + 8 * NV * (THREADS / 32);
   static constexpr size_t smemFor(int epb, int threads) {
     return (size_t(epb) * PER_ELEM + TABLES) * 8 + 16 + 8 * NV * size_t(threads / 32);
   }
 };
 
-template <int NB, int NQ, int NFQ, int NF>
+template <int NB, int NQ, int NFQ, int NF, int DIM = 2>
 __device__ __forceinline__ uint64_t* denseStageBarrier(int epb) {
-  using S = DenseShape<NB, NQ, NFQ, NF>;
+  using S = DenseShape<NB, NQ, NFQ, NF, DIM>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   return reinterpret_cast<uint64_t*>(reinterpret_cast<double*>(smem_raw) + epb * S::PER_ELEM + S::TABLES);
 }
 
-// Dense stage tile (2D), a.epb elements per CTA, any whole number of warps.  geometry: affine [e][5] =
-// (|J| dxi_b/dx_a row-major, 1/|J|); bilinear: [e][NQ][5] followed by the element's M^-1 [NB][NB].
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC>
+// Dense stage tile (triangles and P1 quadrangles: DIM 2; tetrahedra: DIM 3), a.epb elements per CTA, any
+// whole number of warps.  geometry: affine [e][d*d+1] = (|J| dxi_b/dx_a row-major, 1/|J|); bilinear:
+// [e][NQ][d*d+1] followed by the element's M^-1 [NB][NB].
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC, int DIM = 2>
 __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& ph, int64_t tile, uint32_t parity,
                                                bool loadTables) {
-  using S = DenseShape<NB, NQ, NFQ, NF>;
-  constexpr int NV = 4, NFP = S::NFP;
+  using S = DenseShape<NB, NQ, NFQ, NF, DIM>;
+  constexpr int NV = DIM + 2, NFP = S::NFP, GD = DIM * DIM + 1;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int EPB = a.epb;
   double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE]
   double* sF = sU + EPB * S::USTRIDE;                // [EPB][FSTRIDE]
-  double* sQ = sF + EPB * S::FSTRIDE;                // [EPB][2][NV][NQ]
-  double* sR = sQ + EPB * 2 * NV * NQ;               // [EPB][NV][NB]
+  double* sQ = sF + EPB * S::FSTRIDE;                // [EPB][DIM][NV][NQ]
+  double* sR = sQ + EPB * DIM * NV * NQ;             // [EPB][NV][NB]
   double* sN = sR + EPB * NV * NB;                   // [EPB][NV][NB] new state
   double* tab = sN + EPB * NV * NB;
   const double* phi = tab;
   const double* dphiw = phi + NQ * NB;
-  const double* phif = dphiw + NQ * 2 * NB;
+  const double* phif = dphiw + NQ * DIM * NB;
   const double* phifw = phif + NFP * NB;
   const double* mref = phifw + NFP * NB;
   uint64_t* bar = reinterpret_cast<uint64_t*>(tab + S::TABLES);
   double* sRed = reinterpret_cast<double*>(bar + 1);
-  const int GS = AFFINE ? 5 : NQ * 5 + NB * NB;
+  const int GS = AFFINE ? GD : NQ * GD + NB * NB;
 
   const int tid = threadIdx.x;
   const int64_t e0 = tile * EPB;
@@ -242,21 +245,25 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
         for (int b = 0; b < NB; ++b) s = fma(phi[q * NB + b], sU[le * S::USTRIDE + v * NB + b], s);
         U[v] = s;
       }
-      const double* g = AFFINE ? a.geom + e * GS : a.geom + e * GS + q * 5;
-      double ja[2][2] = {{g[0], g[1]}, {g[2], g[3]}};
-      State<2> st;
-      makeState<2>(st, U, ph);
+      const double* g = AFFINE ? a.geom + e * GS : a.geom + e * GS + q * GD;
+      double ja[DIM][DIM];
+#pragma unroll
+      for (int r = 0; r < DIM; ++r)
+#pragma unroll
+        for (int c = 0; c < DIM; ++c) ja[r][c] = g[r * DIM + c];
+      State<DIM> st;
+      makeState<DIM>(st, U, ph);
       const double ep = energyFluxFactor(st, ph);
       // Boussinesq buoyancy S |J| at the point, kept in the new-state buffer until the residual pass
-      if (ph.source) sN[le * NV * NB + q] = st.r * ph.beta * (temperatureOf(st, ph) - ph.tref) / g[4];
-      double tau[2][2] = {{0.0, 0.0}, {0.0, 0.0}}, qh[2] = {0.0, 0.0};
-      double avf[VISC == 2 ? NV * 2 : 1];
+      if (ph.source) sN[le * NV * NB + q] = st.r * ph.beta * (temperatureOf(st, ph) - ph.tref) / g[DIM * DIM];
+      double tau[DIM][DIM] = {}, qh[DIM] = {};
+      double avf[VISC == 2 ? NV * DIM : 1];
       if constexpr (VISC != 0) {
-        // gradient at the point from the element's modal gradient coefficients [nv*2][NB]
-        double g[NV * 2];
-        const double* gc = a.grad + e * NV * 2 * NB;
+        // gradient at the point from the element's modal gradient coefficients [nv*d][NB]
+        double g[NV * DIM];
+        const double* gc = a.grad + e * NV * DIM * NB;
 #pragma unroll
-        for (int c = 0; c < NV * 2; ++c) {
+        for (int c = 0; c < NV * DIM; ++c) {
           double acc = 0.0;
 #pragma unroll
           for (int b = 0; b < NB; ++b) acc = fma(phi[q * NB + b], gc[c * NB + b], acc);
@@ -269,27 +276,36 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
 #pragma unroll
           for (int v = 0; v < NF; ++v) eps = fma(nod[v], a.epsV[e * NF + v], eps);
 #pragma unroll
-          for (int c = 0; c < NV * 2; ++c) avf[c] = eps * g[c];
+          for (int c = 0; c < NV * DIM; ++c) avf[c] = eps * g[c];
         } else {
-          PrimGrad<2> pg;
-          primitiveGradient<2>(g, st.u, st.ir, st.E * st.ir, ph, pg);
-          const double u2 = fma(st.u[0], st.u[0], st.u[1] * st.u[1]);
-          viscousTensor<2>(pg, st.u, fma(ph.incomp ? 0.0 : -0.5, u2, st.E * st.ir) * ph.inv_cv, ph,
-                           tau, qh);
+          PrimGrad<DIM> pg;
+          primitiveGradient<DIM>(g, st.u, st.ir, st.E * st.ir, ph, pg);
+          const double u2 = DIM == 2 ? fma(st.u[0], st.u[0], st.u[1] * st.u[1]) : dotn<DIM>(st.u, st.u);
+          viscousTensor<DIM>(pg, st.u, fma(ph.incomp ? 0.0 : -0.5, u2, st.E * st.ir) * ph.inv_cv, ph,
+                             tau, qh);
         }
       }
 #pragma unroll
-      for (int b = 0; b < 2; ++b) {
-        const double vb = dotn<2>(st.u, ja[b]);
-        double* Q = sQ + ((le * 2 + b) * NV) * NQ + q;
+      for (int b = 0; b < DIM; ++b) {
+        const double vb = dotn<DIM>(st.u, ja[b]);
+        double* Q = sQ + ((le * DIM + b) * NV) * NQ + q;
         Q[0] = st.r * vb;
-        Q[NQ] = fma(-ja[b][1], tau[1][0], fma(-ja[b][0], tau[0][0], fma(st.m[0], vb, ja[b][0] * st.p)));
-        Q[2 * NQ] = fma(-ja[b][1], tau[1][1], fma(-ja[b][0], tau[0][1], fma(st.m[1], vb, ja[b][1] * st.p)));
-        Q[3 * NQ] = ep * vb - dotn<2>(qh, ja[b]);
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          double m = fma(st.m[k], vb, ja[b][k] * st.p);
+#pragma unroll
+          for (int l = 0; l < DIM; ++l) m = fma(-ja[b][l], tau[l][k], m);
+          Q[(1 + k) * NQ] = m;
+        }
+        Q[(DIM + 1) * NQ] = ep * vb - dotn<DIM>(qh, ja[b]);
         if constexpr (VISC == 2) {
 #pragma unroll
-          for (int v = 0; v < NV; ++v)
-            Q[v * NQ] = fma(-ja[b][1], avf[v * 2 + 1], fma(-ja[b][0], avf[v * 2 + 0], Q[v * NQ]));
+          for (int v = 0; v < NV; ++v) {
+            double x = Q[v * NQ];
+#pragma unroll
+            for (int l = 0; l < DIM; ++l) x = fma(-ja[b][l], avf[v * DIM + l], x);
+            Q[v * NQ] = x;
+          }
         }
       }
     }
@@ -301,15 +317,16 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
       for (int v = 0; v < NV; ++v) {
         double s = 0.0;
         for (int q = 0; q < NQ; ++q) {
-          s = fma(sQ[((le * 2 + 0) * NV + v) * NQ + q], dphiw[(q * 2 + 0) * NB + i], s);
-          s = fma(sQ[((le * 2 + 1) * NV + v) * NQ + q], dphiw[(q * 2 + 1) * NB + i], s);
+#pragma unroll
+          for (int b = 0; b < DIM; ++b) s = fma(sQ[((le * DIM + b) * NV + v) * NQ + q], dphiw[(q * DIM + b) * NB + i], s);
         }
         for (int fj = 0; fj < NFP; ++fj) {
           const int f = fj / NFQ, j = fj - f * NFQ;
           s = fma(-sF[le * S::FSTRIDE + (f * NV + v) * NFQ + j], phifw[fj * NB + i], s);
         }
-        if (ph.source && v == 2) {  // y momentum: sum_q w_q |J|_q S_q phi_i(x_q)
-          const double* phiw = a.tables + (NQ * NB * 3 + NFP * NB * 2 + NB * NB + 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ);
+        if (ph.source && v == DIM) {  // last momentum component: sum_q w_q |J|_q S_q phi_i(x_q)
+          const double* phiw = a.tables + (NQ * NB * (1 + DIM) + NFP * NB * 2 + NB * NB + DIM * NB * NB + NF * NB * NFQ +
+                                           NF * NFQ * NFQ);
           for (int q = 0; q < NQ; ++q) s = fma(sN[le * NV * NB + q], phiw[q * NB + i], s);
         }
         sR[(le * NV + v) * NB + i] = s;
@@ -321,8 +338,8 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
       const int le = idx / NB, i = idx - le * NB;
       const int64_t e = e0 + le;
       const double* g = a.geom + e * GS;
-      const double* minv = AFFINE ? mref : g + NQ * 5;
-      const double sc = AFFINE ? g[4] : 1.0;
+      const double* minv = AFFINE ? mref : g + NQ * GD;
+      const double sc = AFFINE ? g[DIM * DIM] : 1.0;
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         double s = 0.0;
@@ -355,7 +372,7 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
     }
     if (a.relerr) {
       // relative error: mean over points of |R Phi^T| per element (TimeIntegration.cpp:279-324)
-      double acc[NV] = {0.0, 0.0, 0.0, 0.0};
+      double acc[NV] = {};
       for (int idx = tid; idx < ecount * NQ; idx += blockDim.x) {
         const int le = idx / NQ, q = idx - le * NQ;
 #pragma unroll
@@ -405,23 +422,23 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
   return true;
 }
 
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC, int DIM = 2>
 __global__ void __launch_bounds__(kMaxTileThreads) denseStageKernel(StageArgs a, Phys ph) {
-  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF>(a.epb), 1);
-  denseStageTile<NB, NQ, NFQ, NF, AFFINE, VISC>(a, ph, blockIdx.x, 0u, true);
+  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF, DIM>(a.epb), 1);
+  denseStageTile<NB, NQ, NFQ, NF, AFFINE, VISC, DIM>(a, ph, blockIdx.x, 0u, true);
 }
 
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC, int DIM = 2>
 __global__ void __launch_bounds__(kMaxTileThreads)
     denseStageBatchKernel(const StageArgs* __restrict__ args, const Phys* __restrict__ phys,
                           const int2* __restrict__ items, int nitems, int epb) {
-  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF>(epb), 1);
+  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF, DIM>(epb), 1);
   uint32_t parity = 0;
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const int2 it = items[w];
     const StageArgs a = args[it.x];
     const Phys ph = phys[it.x];
-    if (!denseStageTile<NB, NQ, NFQ, NF, AFFINE, VISC>(a, ph, it.y, parity, w == int(blockIdx.x))) return;
+    if (!denseStageTile<NB, NQ, NFQ, NF, AFFINE, VISC, DIM>(a, ph, it.y, parity, w == int(blockIdx.x))) return;
     parity ^= 1u;
   }
 }
@@ -803,6 +820,12 @@ __global__ void __launch_bounds__(kMaxTileThreads)
 }
 
 // (type, P) -> (NB, NQ, NFQ): triangle P1..P5 use Dunavant rules of 3,6,12,16,25 points.
+// Tetrahedra (dense blocks of DIM 3): P = 1..3, the Euler stage only.
+#define SDG_TET_CASES(X)                        \
+  X(SDG_ELEMENT_TETRAHEDRON, 1, 4, 4, 4, 4)     \
+  X(SDG_ELEMENT_TETRAHEDRON, 2, 10, 11, 7, 4)   \
+  X(SDG_ELEMENT_TETRAHEDRON, 3, 20, 24, 13, 4)
+
 #define SDG_DENSE_CASES(X)                                  \
   X(SDG_ELEMENT_TRIANGLE, 1, 3, 3, 2, 3, true)              \
   X(SDG_ELEMENT_TRIANGLE, 2, 6, 6, 3, 3, true)              \

@@ -20,6 +20,8 @@ const int* faceVertexList(int t) {
   static const int tri[] = {0, 1, 1, 2, 2, 0};
   static const int quad[] = {0, 1, 1, 2, 2, 3, 3, 0};
   static const int hex[] = {0, 3, 2, 1, 0, 1, 5, 4, 0, 4, 7, 3, 1, 2, 6, 5, 2, 3, 7, 6, 4, 5, 6, 7};
+  static const int tet[] = {0, 2, 1, 0, 1, 3, 0, 3, 2, 3, 1, 2};
+  if (t == SDG_ELEMENT_TETRAHEDRON) return tet;
   return t == SDG_ELEMENT_LINE ? line : (t == SDG_ELEMENT_TRIANGLE ? tri : (t == SDG_ELEMENT_QUADRANGLE ? quad : hex));
 }
 
@@ -78,9 +80,9 @@ Adjacency buildAdjacency(const sdg_mesh& mesh, const std::vector<Block>& blocks)
           if (vis.count >= 2) throw std::runtime_error("a face is shared by more than two elements (a periodic direction needs at least three elements)");
           vis.second = {bi, int(e), f};
           vis.count = 2;
-          if (nfv == 4) {
+          if (nfv >= 3) {
             int r = -1;
-            for (int k = 0; k < 4; ++k) if (mapped[k] == vis.mapped[0]) r = k;
+            for (int k = 0; k < nfv; ++k) if (mapped[k] == vis.mapped[0]) r = k;
             if (r < 0) throw std::runtime_error("inconsistent shared face");
             vis.rotation = r;
           }
@@ -94,12 +96,14 @@ Adjacency buildAdjacency(const sdg_mesh& mesh, const std::vector<Block>& blocks)
   bmap.reserve(size_t(mesh.boundary_count) + 16);
   for (int64_t i = 0; i < mesh.boundary_count; ++i) {
     FaceKey key;
-    for (int k = 0; k < nbv; ++k) {
+    // 3D: a triangle's fourth index is -1
+    const int nk = (nbv == 4 && mesh.boundary_node[i * nbv + 3] == -1) ? 3 : nbv;
+    for (int k = 0; k < nk; ++k) {
       const int32_t v = mesh.boundary_node[i * nbv + k];
       if (v < 0 || v >= mesh.node_count) throw std::runtime_error("boundary vertex index out of range");
       key.v[k] = master(v);
     }
-    std::sort(key.v.begin(), key.v.begin() + nbv);
+    std::sort(key.v.begin(), key.v.begin() + nk);
     bmap[key] = i;
   }
   Adjacency adj;
@@ -145,7 +149,7 @@ namespace {
 
 struct MeshStorage {
   std::vector<double> node;
-  std::vector<int32_t> periodic, line, tri, quad, hex, bnode, bphys, bc;
+  std::vector<int32_t> periodic, line, tri, quad, hex, tet, bnode, bphys, bc;
 };
 
 void publish(MeshStorage* s, int dim, sdg_generated_mesh* out) {
@@ -159,6 +163,7 @@ void publish(MeshStorage* s, int dim, sdg_generated_mesh* out) {
   m.quadrangle_count = int64_t(s->quad.size() / 4); m.quadrangle_node = s->quad.empty() ? nullptr : s->quad.data();
   m.hexahedron_count = int64_t(s->hex.size() / 8); m.hexahedron_node = s->hex.empty() ? nullptr : s->hex.data();
   m.line_count = int64_t(s->line.size() / 2); m.line_node = s->line.empty() ? nullptr : s->line.data();
+  m.tetrahedron_count = int64_t(s->tet.size() / 4); m.tetrahedron_node = s->tet.empty() ? nullptr : s->tet.data();
   m.boundary_count = int64_t(s->bphys.size()); m.boundary_node = s->bnode.empty() ? nullptr : s->bnode.data();
   m.boundary_physical = s->bphys.empty() ? nullptr : s->bphys.data();
   m.physical_count = int32_t(s->bc.size()); m.physical_boundary_condition = s->bc.data();
@@ -323,9 +328,70 @@ int sdg_mesh_generate_3d(double x0, double y0, double z0, double lx, double ly, 
   return SDG_OK;
 }
 
+// Structured tetrahedral box: the hexahedral box of sdg_mesh_generate_3d with every cube split into the six
+// tetrahedra around its diagonal from the lowest to the highest corner (Kuhn's subdivision, conforming
+// between cubes and across periodic sides), vertices ordered for a positive Jacobian.  Boundary elements are
+// the tetrahedron faces on the box sides, triangles with a fourth index of -1, in the same groups.
+int sdg_mesh_generate_3d_tetrahedra(double x0, double y0, double z0, double lx, double ly, double lz, int32_t nx,
+                                    int32_t ny, int32_t nz, int32_t periodic, const int32_t* boundary_condition,
+                                    sdg_generated_mesh* out) {
+  const int rc = sdg_mesh_generate_3d(x0, y0, z0, lx, ly, lz, nx, ny, nz, periodic, boundary_condition, out);
+  if (rc != SDG_OK) return rc;
+  auto* s = static_cast<MeshStorage*>(out->storage);
+  const int64_t px = nx + 1, py = ny + 1;
+  const auto node = [&](int32_t n, int d) { return s->node[size_t(n) * 3 + d]; };
+  const int perms[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  s->tet.reserve(s->hex.size() / 8 * 24);
+  for (size_t h = 0; h < s->hex.size(); h += 8) {
+    // hexahedron corner of offset (dx, dy, dz): vertex list 0..7 of sdg_mesh_generate_3d
+    const auto corner = [&](int dx, int dy, int dz) {
+      static const int at[2][2][2] = {{{0, 4}, {3, 7}}, {{1, 5}, {2, 6}}};
+      return s->hex[h + at[dx][dy][dz]];
+    };
+    for (const auto& pm : perms) {
+      int c[3] = {0, 0, 0};
+      int32_t v[4];
+      v[0] = corner(0, 0, 0);
+      for (int k = 0; k < 3; ++k) { c[pm[k]] = 1; v[k + 1] = corner(c[0], c[1], c[2]); }
+      double a[3][3];
+      for (int k = 0; k < 3; ++k)
+        for (int d = 0; d < 3; ++d) a[k][d] = node(v[k + 1], d) - node(v[0], d);
+      const double det = a[0][0] * (a[1][1] * a[2][2] - a[1][2] * a[2][1]) -
+                         a[0][1] * (a[1][0] * a[2][2] - a[1][2] * a[2][0]) +
+                         a[0][2] * (a[1][0] * a[2][1] - a[1][1] * a[2][0]);
+      if (det < 0) std::swap(v[2], v[3]);
+      s->tet.insert(s->tet.end(), {v[0], v[1], v[2], v[3]});
+    }
+  }
+  s->hex.clear();
+  // boundary triangles: tetrahedron faces whose three vertices lie on one side of the box
+  s->bnode.clear(); s->bphys.clear();
+  const int* fl = sdg::faceVertexList(SDG_ELEMENT_TETRAHEDRON);
+  const auto side = [&](int32_t n) {
+    const int64_t i = n % px, j = (n / px) % py, k = n / (px * py);
+    int m = 0;
+    if (i == 0) m |= 1; if (i == nx) m |= 2; if (j == 0) m |= 4;
+    if (j == ny) m |= 8; if (k == 0) m |= 16; if (k == nz) m |= 32;
+    return m;
+  };
+  for (size_t t = 0; t < s->tet.size(); t += 4)
+    for (int f = 0; f < 4; ++f) {
+      const int32_t a = s->tet[t + fl[f * 3]], b = s->tet[t + fl[f * 3 + 1]], c = s->tet[t + fl[f * 3 + 2]];
+      const int common = side(a) & side(b) & side(c);
+      if (!common) continue;
+      int g = 0;
+      while (!(common & (1 << g))) ++g;
+      s->bnode.insert(s->bnode.end(), {a, b, c, -1});
+      s->bphys.push_back(periodic ? 1 : g + 1);
+    }
+  publish(s, 3, out);
+  return SDG_OK;
+}
+
 // MSH 4.1 ASCII reader: $PhysicalNames (optional), $Entities (physical tags of entities),
 // $Nodes, $Elements, $Periodic (node pairs).  Element types 1/8/26-28 (lines), 2/9/21/23/25 (triangles),
-// 3/10/36-38 (quadrangles), 5/12/92-94 (hexahedra); only the primary vertices are kept.
+// 3/10/36-38 (quadrangles), 4/11/29-31 (tetrahedra), 5/12/92-94 (hexahedra); only the primary vertices are
+// kept.  A 3D mesh holds tetrahedra or hexahedra; its triangular boundary elements get a fourth index of -1.
 int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
   if (!path || !out) return SDG_ERR_INVALID_ARGUMENT;
   std::ifstream in(path);
@@ -356,6 +422,11 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
       case 36: dim = 2; nn = 16; nprim = 4; return true;
       case 37: dim = 2; nn = 25; nprim = 4; return true;
       case 38: dim = 2; nn = 36; nprim = 4; return true;
+      case 4: dim = 3; nn = 4; nprim = 4; return true;
+      case 11: dim = 3; nn = 10; nprim = 4; return true;
+      case 29: dim = 3; nn = 20; nprim = 4; return true;
+      case 30: dim = 3; nn = 35; nprim = 4; return true;
+      case 31: dim = 3; nn = 56; nprim = 4; return true;
       case 5: dim = 3; nn = 8; nprim = 8; return true;
       case 12: dim = 3; nn = 27; nprim = 8; return true;
       case 92: dim = 3; nn = 64; nprim = 8; return true;
@@ -431,8 +502,9 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
     for (const RawEl& r : raw) {
       int dim = 0, nn = 0, nprim = 0; typeInfo(r.type, dim, nn, nprim);
       if (dim == maxDim) {
-        std::vector<int32_t>* dst = maxDim == 1 ? &s->line : (nprim == 3 ? &s->tri : (nprim == 4 ? &s->quad : &s->hex));
-        if (maxDim == 3 && nprim != 8) throw std::runtime_error("only hexahedra are supported in 3D");
+        std::vector<int32_t>* dst = maxDim == 1 ? &s->line
+                                    : maxDim == 2 ? (nprim == 3 ? &s->tri : &s->quad)
+                                                  : (nprim == 4 ? &s->tet : &s->hex);
         for (int64_t v : r.v) dst->push_back(idx(v));
       } else if (dim == maxDim - 1) {
         const auto it = entityPhysical.find({r.edim, r.etag});
@@ -451,8 +523,11 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
       std::sort(tags.begin(), tags.end());
       for (size_t i = 0; i < tags.size(); ++i) remap[tags[i]] = int(i) + 1;
     }
+    if (!s->tet.empty() && !s->hex.empty())
+      throw std::runtime_error("a 3D mesh of tetrahedra and hexahedra needs pyramids, which are not supported");
     for (const BEl& b : bels) {
       for (int64_t v : b.v) s->bnode.push_back(idx(v));
+      if (maxDim == 3 && b.v.size() == 3) s->bnode.push_back(-1);
       s->bphys.push_back(remap[b.phys]);
     }
     s->bc.assign(remap.size(), SDG_BC_PERIODIC);

@@ -6,7 +6,8 @@
 //                    of the left face's first vertex in the right face's vertex list)
 //   periodic pairing src/Mesh/Adjacency.cpp:185-328 (here: a master-node map folds periodic slaves
 //                    onto their masters before the face keys are formed)
-//   boundary faces   src/Mesh/Adjacency.cpp:370-430 (matched to boundary elements by vertex set)
+//   boundary faces   src/Mesh/Adjacency.cpp:370-430 (matched to boundary elements by vertex set; in 3D a
+//                    boundary element is a quadrangle, or a triangle whose fourth index is -1)
 //   1D periodic      src/Mesh/Adjacency.cpp:185-211 (without a node map the two periodic boundary points
 //                    are joined: the first one in boundary-element order is the left side)
 #pragma once
@@ -19,14 +20,20 @@
 
 namespace sdg {
 
-inline int typeDim(int t) { return t == SDG_ELEMENT_LINE ? 1 : (t == SDG_ELEMENT_HEXAHEDRON ? 3 : 2); }
+inline int typeDim(int t) {
+  return t == SDG_ELEMENT_LINE ? 1 : (t == SDG_ELEMENT_HEXAHEDRON || t == SDG_ELEMENT_TETRAHEDRON ? 3 : 2);
+}
 inline int typeFaces(int t) {
-  return t == SDG_ELEMENT_LINE ? 2 : (t == SDG_ELEMENT_TRIANGLE ? 3 : (t == SDG_ELEMENT_QUADRANGLE ? 4 : 6));
+  return t == SDG_ELEMENT_LINE ? 2
+         : (t == SDG_ELEMENT_TRIANGLE ? 3 : (t == SDG_ELEMENT_QUADRANGLE || t == SDG_ELEMENT_TETRAHEDRON ? 4 : 6));
 }
 inline int typeVertices(int t) {
-  return t == SDG_ELEMENT_LINE ? 2 : (t == SDG_ELEMENT_TRIANGLE ? 3 : (t == SDG_ELEMENT_QUADRANGLE ? 4 : 8));
+  return t == SDG_ELEMENT_LINE ? 2
+         : (t == SDG_ELEMENT_TRIANGLE ? 3 : (t == SDG_ELEMENT_QUADRANGLE || t == SDG_ELEMENT_TETRAHEDRON ? 4 : 8));
 }
-inline int typeFaceVertices(int t) { return t == SDG_ELEMENT_LINE ? 1 : (t == SDG_ELEMENT_HEXAHEDRON ? 4 : 2); }
+inline int typeFaceVertices(int t) {
+  return t == SDG_ELEMENT_LINE ? 1 : (t == SDG_ELEMENT_HEXAHEDRON ? 4 : (t == SDG_ELEMENT_TETRAHEDRON ? 3 : 2));
+}
 
 // Face vertex lists in gmsh order (src/Solver/SimulationControl.cpp:170-216).
 const int* faceVertexList(int t);
@@ -39,7 +46,7 @@ struct FaceSide {
 
 struct InteriorFace {
   FaceSide left, right;
-  int rotation = 0;      // 3D only
+  int rotation = 0;      // 3D only: position of the left face's first vertex in the right face's list
 };
 
 struct BoundaryFace {

@@ -7,7 +7,7 @@
 // reference inverts per element (src/Mesh/Geometry.cpp:88-100) is exactly diagonal, the volume term of
 // src/Solver/SpatialDiscrete.cpp:194-266,1016-1032 becomes a sum-factorised 1D derivative per direction,
 // and face traces/lifts (src/Solver/VariableConvertor.cpp:432-485) are 1D end-point interpolations.
-// Triangles and first-order quadrangles (7-point rule) keep a dense modal formulation.
+// Triangles, first-order quadrangles (7-point rule) and tetrahedra keep a dense modal formulation.
 //
 // The modal basis -- used for the dense blocks, for the modal state exchange and for the relative error
 // of src/Solver/TimeIntegration.cpp:279-324 (which depends on the basis) -- is the hierarchic H1 basis
@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/sdg_gpu.h"
+#include "tetrahedron_rules.h"
 #include "triangle_rules.h"
 
 namespace sdg {
@@ -140,9 +141,24 @@ inline Dual2 dkernel(int k, Dual2 t) {
   return {c * s, c * ds * t.x, c * ds * t.y};
 }
 
+// Three-variable forward-mode dual (tetrahedron basis gradients).
+struct Dual3 { double v, g[3]; };
+inline Dual3 d3add(Dual3 a, Dual3 b) { return {a.v + b.v, {a.g[0] + b.g[0], a.g[1] + b.g[1], a.g[2] + b.g[2]}}; }
+inline Dual3 d3sub(Dual3 a, Dual3 b) { return {a.v - b.v, {a.g[0] - b.g[0], a.g[1] - b.g[1], a.g[2] - b.g[2]}}; }
+inline Dual3 d3mul(Dual3 a, Dual3 b) {
+  return {a.v * b.v, {a.g[0] * b.v + a.v * b.g[0], a.g[1] * b.v + a.v * b.g[1], a.g[2] * b.v + a.v * b.g[2]}};
+}
+inline Dual3 d3chain(Dual3 t, double f, double df) { return {f, {df * t.g[0], df * t.g[1], df * t.g[2]}}; }
+inline Dual3 d3legendre(int n, Dual3 t) { double p, dp; legendreP(n, t.v, &p, &dp); return d3chain(t, p, dp); }
+inline Dual3 d3kernel(int k, Dual3 t) {
+  const Dual2 r = dkernel(k, {t.v, 1.0, 0.0});
+  return d3chain(t, r.v, r.x);
+}
+
 inline int modalCount(int type, int p) {
   if (type == SDG_ELEMENT_LINE) return p + 1;
   if (type == SDG_ELEMENT_TRIANGLE) return (p + 1) * (p + 2) / 2;
+  if (type == SDG_ELEMENT_TETRAHEDRON) return (p + 1) * (p + 2) * (p + 3) / 6;
   if (type == SDG_ELEMENT_QUADRANGLE) return (p + 1) * (p + 1);
   return (p + 1) * (p + 1) * (p + 1);
 }
@@ -151,7 +167,37 @@ inline int modalCount(int type, int p) {
 //   line: index a -> l_a(xi); quadrangle: index a*(P+1)+b -> l_a(xi) l_b(eta); hexahedron: (a*(P+1)+b)*(P+1)+c.
 //   triangle  : lambda_0..2; edge functions lambda_a lambda_b phi_{k-2}(lambda_b - lambda_a) on edges
 //               (0,1),(1,2),(2,0), k = 2..P; bubbles lambda_0 lambda_1 lambda_2 P_i(l2-l1) P_j(l1-l0), i+j <= P-3.
+//   tetrahedron: lambda_0..3; edge functions on gmsh's edges (0,1),(1,2),(2,0),(3,0),(3,2),(3,1), k = 2..P;
+//               face bubbles l_a l_b l_c P_i(l_c-l_b) P_j(l_b-l_a), i+j <= P-3, on the faces (a,b,c) of the
+//               face vertex list; interior bubbles l0 l1 l2 l3 P_i(l1-l0) P_j(l2-l1) P_k(l3-l2), i+j+k <= P-4.
+inline void modalBasisTetrahedron(int p, const double* X, double* val, double* grad) {
+  const Dual3 lam[4] = {{1.0 - X[0] - X[1] - X[2], {-1.0, -1.0, -1.0}}, {X[0], {1.0, 0.0, 0.0}},
+                        {X[1], {0.0, 1.0, 0.0}}, {X[2], {0.0, 0.0, 1.0}}};
+  std::vector<Dual3> f(lam, lam + 4);
+  const int edge[6][2] = {{0, 1}, {1, 2}, {2, 0}, {3, 0}, {3, 2}, {3, 1}};
+  for (const auto& e : edge)
+    for (int k = 2; k <= p; ++k) f.push_back(d3mul(d3mul(lam[e[0]], lam[e[1]]), d3kernel(k, d3sub(lam[e[1]], lam[e[0]]))));
+  const int face[4][3] = {{0, 2, 1}, {0, 1, 3}, {0, 3, 2}, {3, 1, 2}};
+  for (const auto& t : face) {
+    const Dual3 a = lam[t[0]], b = lam[t[1]], c = lam[t[2]], bub = d3mul(d3mul(a, b), c);
+    for (int s = 0; s <= p - 3; ++s)
+      for (int i = 0; i <= s; ++i)
+        f.push_back(d3mul(d3mul(bub, d3legendre(i, d3sub(c, b))), d3legendre(s - i, d3sub(b, a))));
+  }
+  const Dual3 inner = d3mul(d3mul(lam[0], lam[1]), d3mul(lam[2], lam[3]));
+  for (int s = 0; s <= p - 4; ++s)
+    for (int i = 0; i <= s; ++i)
+      for (int j = 0; j <= s - i; ++j)
+        f.push_back(d3mul(d3mul(inner, d3legendre(i, d3sub(lam[1], lam[0]))),
+                          d3mul(d3legendre(j, d3sub(lam[2], lam[1])), d3legendre(s - i - j, d3sub(lam[3], lam[2])))));
+  for (size_t i = 0; i < f.size(); ++i) {
+    val[i] = f[i].v;
+    for (int d = 0; d < 3; ++d) grad[i * 3 + d] = f[i].g[d];
+  }
+}
+
 inline void modalBasis(int type, int p, const double* X, double* val, double* grad /* [nb][3] */) {
+  if (type == SDG_ELEMENT_TETRAHEDRON) { modalBasisTetrahedron(p, X, val, grad); return; }
   if (type != SDG_ELEMENT_TRIANGLE) {
     const int m = p + 1, dim = type == SDG_ELEMENT_HEXAHEDRON ? 3 : (type == SDG_ELEMENT_LINE ? 1 : 2);
     double lv[3][kMaxN], ld[3][kMaxN];
@@ -203,10 +249,20 @@ struct PointRule {
   std::vector<double> x, w;  // x: [n][3]
 };
 
-// Volume rule of order 2P (kTriangle/kQuadrangle/kHexahedronQuadratureNumber, SimulationControl.cpp:268-273).
+// Volume rule of order 2P (kTriangle/kQuadrangle/kTetrahedron/kHexahedronQuadratureNumber,
+// SimulationControl.cpp:268-273).
 inline PointRule volumeRule(int type, int p) {
   PointRule r;
   const int order = 2 * p;
+  if (type == SDG_ELEMENT_TETRAHEDRON) {
+    for (const auto& t : sdg_tables::kTetrahedronRules)
+      if (t.degree == order) {
+        r.n = t.count;
+        for (int i = 0; i < t.count; ++i) { r.x.insert(r.x.end(), {t.xi[i], t.eta[i], t.zeta[i]}); r.w.push_back(t.weight[i]); }
+        return r;
+      }
+    throw std::runtime_error("no tetrahedron rule of order " + std::to_string(order));
+  }
   if (type == SDG_ELEMENT_TRIANGLE) {
     for (const auto& t : sdg_tables::kTriangleRules)
       if (t.degree == order) {
@@ -246,6 +302,15 @@ inline PointRule volumeRule(int type, int p) {
 inline PointRule faceRule(int type, int p) {
   PointRule r;
   if (type == SDG_ELEMENT_LINE) { r.n = 1; r.x = {0.0, 0.0, 0.0}; r.w = {1.0}; return r; }
+  if (type == SDG_ELEMENT_TETRAHEDRON) {  // triangular faces: the rule of order 2P+1 on (0,0),(1,0),(0,1)
+    for (const auto& t : sdg_tables::kFaceTriangleRules)
+      if (t.degree == 2 * p + 1) {
+        r.n = t.count;
+        for (int i = 0; i < t.count; ++i) { r.x.insert(r.x.end(), {t.xi[i], t.eta[i], 0.0}); r.w.push_back(t.weight[i]); }
+        return r;
+      }
+    throw std::runtime_error("no triangle face rule of order " + std::to_string(2 * p + 1));
+  }
   const int n = p + 1;
   double g[kMaxN], gw[kMaxN];
   gaussRule(n, g, gw);
@@ -265,6 +330,8 @@ inline void referenceVertex(int type, int v, double* X) {
   static const double quad[4][3] = {{-1, -1, 0}, {1, -1, 0}, {1, 1, 0}, {-1, 1, 0}};
   static const double hex[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
                                    {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+  static const double tet[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  if (type == SDG_ELEMENT_TETRAHEDRON) { X[0] = tet[v][0]; X[1] = tet[v][1]; X[2] = tet[v][2]; return; }
   const double* s = type == SDG_ELEMENT_LINE ? line[v]
                     : (type == SDG_ELEMENT_TRIANGLE ? tri[v] : (type == SDG_ELEMENT_QUADRANGLE ? quad[v] : hex[v]));
   X[0] = s[0]; X[1] = s[1]; X[2] = s[2];

@@ -1,4 +1,4 @@
-// Dense (modal: triangles, P1 quadrangles) stage and gradient kernels: the one translation unit that
+// Dense (modal: triangles, P1 quadrangles, tetrahedra) stage and gradient kernels: the one translation unit that
 // instantiates them, and their registry entries.
 #include "sdg_kernels_dense.cuh"
 #include "sdg_kernels_ns.cuh"
@@ -7,12 +7,12 @@
 namespace sdg {
 
 namespace {
-template <int NB, int NQ, int NFQ, int NF, bool AFF, int VISC>
+template <int NB, int NQ, int NFQ, int NF, bool AFF, int VISC, int DIM = 2>
 KernelVariant stageOf() {
-  using S = DenseShape<NB, NQ, NFQ, NF>;
+  using S = DenseShape<NB, NQ, NFQ, NF, DIM>;
   KernelVariant v;
-  v.single = reinterpret_cast<const void*>(&denseStageKernel<NB, NQ, NFQ, NF, AFF, VISC>);
-  v.batch = reinterpret_cast<const void*>(&denseStageBatchKernel<NB, NQ, NFQ, NF, AFF, VISC>);
+  v.single = reinterpret_cast<const void*>(&denseStageKernel<NB, NQ, NFQ, NF, AFF, VISC, DIM>);
+  v.batch = reinterpret_cast<const void*>(&denseStageBatchKernel<NB, NQ, NFQ, NF, AFF, VISC, DIM>);
   v.nb = NB; v.epb = S::EPB; v.threads = S::THREADS; v.nodeThreads = false;
   v.perElem = size_t(S::PER_ELEM) * 8; v.fixed = S::TABLES * 8 + 16; v.perWarp = 8 * S::NV;
   return v;
@@ -36,6 +36,10 @@ KernelVariant denseStageVariant(int type, int p, bool affine, int visc) {
                      : visc ? stageOf<NB, NQ, NFQ, NF, AFF, 1>() : stageOf<NB, NQ, NFQ, NF, AFF, 0>();
   SDG_DENSE_CASES(SDG_DS)
 #undef SDG_DS
+#define SDG_DT(T, P, NB, NQ, NFQ, NF) \
+  if (type == T && p == P && affine && visc == 0) return stageOf<NB, NQ, NFQ, NF, true, 0, 3>();
+  SDG_TET_CASES(SDG_DT)
+#undef SDG_DT
   return KernelVariant();
 }
 

@@ -33,13 +33,15 @@ class Mesh:
     """First-order mesh in gmsh vertex order (the input format of sdg_create)."""
 
     def __init__(self, dimension, nodes, triangles=None, quadrangles=None, hexahedra=None, boundary=None,
-                 boundary_physical=None, physical_conditions=None, periodic_master=None, lines=None):
+                 boundary_physical=None, physical_conditions=None, periodic_master=None, lines=None,
+                 tetrahedra=None):
         self.dimension = int(dimension)
         self.nodes = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
         self.lines = None if lines is None or len(lines) == 0 else np.ascontiguousarray(lines, np.int32).reshape(-1, 2)
         self.triangles = None if triangles is None or len(triangles) == 0 else np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
         self.quadrangles = None if quadrangles is None or len(quadrangles) == 0 else np.ascontiguousarray(quadrangles, np.int32).reshape(-1, 4)
         self.hexahedra = None if hexahedra is None or len(hexahedra) == 0 else np.ascontiguousarray(hexahedra, np.int32).reshape(-1, 8)
+        self.tetrahedra = None if tetrahedra is None or len(tetrahedra) == 0 else np.ascontiguousarray(tetrahedra, np.int32).reshape(-1, 4)
         nbv = {1: 1, 2: 2}.get(self.dimension, 4)
         self.boundary = np.zeros((0, nbv), np.int32) if boundary is None else np.ascontiguousarray(boundary, np.int32).reshape(-1, nbv)
         self.boundary_physical = np.zeros(0, np.int32) if boundary_physical is None else np.ascontiguousarray(boundary_physical, np.int32)
@@ -62,7 +64,8 @@ class Mesh:
                   arr(m.boundary_physical, m.boundary_count, 1, np.int32),
                   arr(m.physical_boundary_condition, m.physical_count, 1, np.int32),
                   arr(m.periodic_master, m.node_count, 1, np.int32),
-                  arr(m.line_node, m.line_count, 2, np.int32))
+                  arr(m.line_node, m.line_count, 2, np.int32),
+                  arr(m.tetrahedron_node, m.tetrahedron_count, 4, np.int32))
         _abi.load().sdg_mesh_free(byref(g))
         return out
 
@@ -91,6 +94,16 @@ class Mesh:
         g = SdgGeneratedMesh()
         bc = None if boundary_conditions is None else np.ascontiguousarray(boundary_conditions, np.int32)
         check(lib.sdg_mesh_generate_3d(x0, y0, z0, lx, ly, lz, nx, ny, nz, int(periodic), _ptr(bc, _pi), byref(g)))
+        return cls._from_generated(g)
+
+    @classmethod
+    def box_3d_tetrahedra(cls, x0, y0, z0, lx, ly, lz, nx, ny, nz, periodic=True, boundary_conditions=None):
+        """box_3d with every hexahedron split into six tetrahedra (triangular boundary elements, same groups)."""
+        lib = _abi.load()
+        g = SdgGeneratedMesh()
+        bc = None if boundary_conditions is None else np.ascontiguousarray(boundary_conditions, np.int32)
+        check(lib.sdg_mesh_generate_3d_tetrahedra(x0, y0, z0, lx, ly, lz, nx, ny, nz, int(periodic), _ptr(bc, _pi),
+                                                  byref(g)))
         return cls._from_generated(g)
 
     @classmethod
@@ -125,6 +138,8 @@ class Mesh:
         m.physical_boundary_condition = _ptr(self.physical_conditions, _pi)
         m.line_count = 0 if self.lines is None else self.lines.shape[0]
         m.line_node = _ptr(self.lines, _pi)
+        m.tetrahedron_count = 0 if self.tetrahedra is None else self.tetrahedra.shape[0]
+        m.tetrahedron_node = _ptr(self.tetrahedra, _pi)
         return m
 
 

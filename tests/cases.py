@@ -93,6 +93,53 @@ def tgv_case(n=3, p=3, flux=sdg.HLLC, dt=None, steps=3, viscous=None, mu=1.0 / 1
     return (mesh, cfg, lambda pts: tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2]), None, dt, steps)
 
 
+# Even permutations of a tetrahedron's vertex list (orientation kept): shuffling each element's list this way
+# makes shared faces meet at all three rotations.
+_EVEN_TET = np.array([(0, 1, 2, 3), (0, 2, 3, 1), (0, 3, 1, 2), (1, 0, 3, 2), (1, 2, 0, 3), (1, 3, 2, 0),
+                      (2, 0, 1, 3), (2, 1, 3, 0), (2, 3, 0, 1), (3, 0, 2, 1), (3, 1, 0, 2), (3, 2, 1, 0)])
+
+
+def tet_mesh(n=3, length=1.0, periodic=True, conditions=None, seed=7):
+    """Structured tetrahedral box [0, length]^3 (six tetrahedra per cube), vertex lists shuffled (seeded)."""
+    mesh = sdg.Mesh.box_3d_tetrahedra(0, 0, 0, length, length, length, n, n, n, periodic=periodic,
+                                      boundary_conditions=None if periodic else list(conditions))
+    pick = np.random.default_rng(seed).integers(0, len(_EVEN_TET), len(mesh.tetrahedra))
+    mesh.tetrahedra = np.ascontiguousarray(mesh.tetrahedra[np.arange(len(pick))[:, None], _EVEN_TET[pick]])
+    return mesh
+
+
+def tet_tgv_case(n=3, p=2, flux=sdg.HLLC, steps=3, mach=0.3):
+    """Taylor-Green vortex on periodic tetrahedra of [0, 2 pi]^3 (Mach 0.3 for a nonlinear flux)."""
+    mesh = tet_mesh(n, 2 * math.pi)
+    dt = 0.2 * (2 * math.pi / n) / ((1.0 + 1.0 / mach) * (p + 1) ** 2)
+    return (mesh, config(p, flux), lambda pts: tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2], mach=mach), None, dt,
+            steps)
+
+
+def tet_box_case(p=2, flux=sdg.HLLC, conditions=(sdg.RIEMANN_FARFIELD,) * 6, n=3, dt=5e-4, steps=3):
+    """Non-periodic tetrahedral unit box, groups x-, x+, y-, y+, z-, z+: a smooth perturbation of a uniform
+    stream at u = (0.4, 0.1, -0.1), the same stream as the boundary state (inflow at x-, outflow at x+)."""
+    mesh = tet_mesh(n, 1.0, periodic=False, conditions=conditions)
+
+    def ic(pts):
+        x, y, z = pts[:, 0], pts[:, 1], pts[:, 2]
+        rho = 1.0 + 0.1 * np.sin(math.pi * x) * np.sin(math.pi * y) * np.sin(math.pi * z)
+        u = 0.4 + 0.05 * np.cos(math.pi * y)
+        v = 0.1 + 0.05 * np.sin(math.pi * z)
+        w = -0.1 + 0.05 * np.sin(math.pi * x)
+        pr = 1.0 + 0.05 * np.cos(math.pi * x) * np.cos(math.pi * z)
+        return np.stack([rho, u, v, w, pr / (rho * R_GAS)], 1)
+
+    def bc(pts, phys):
+        out = np.zeros((len(pts), 5))
+        out[:, 0] = 1.0
+        out[:, 1], out[:, 2], out[:, 3] = 0.4, 0.1, -0.1
+        out[:, 4] = 1.0 / R_GAS
+        return out
+
+    return (mesh, config(p, flux), ic, bc, dt, steps)
+
+
 def kh_case(n=8, p=4, flux=sdg.LAX_FRIEDRICHS, dt=2e-4, steps=3, jitter=0.1, split=0.5, seed=11, viscous=None,
             mu=1e-4):
     """Kelvin-Helmholtz; with `viscous` the Navier-Stokes case at Re = 1/mu (1e4 by default)."""

@@ -68,7 +68,7 @@ def reference_tables(ref):
     out["quadrature_count"] = counts
     body = _func_body(sc, "getElementPerAdjacencyNodeIndex()")
     faces = {}
-    for name in ("Line", "Triangle", "Quadrangle", "Hexahedron"):
+    for name in ("Line", "Triangle", "Quadrangle", "Tetrahedron", "Hexahedron"):
         m = re.search(r"ElementType == ElementEnum::%s\) \{\s*return \{([^}]*)\};" % name, body, re.S)
         faces[name] = [int(x) for x in m.group(1).replace("\n", " ").split(",")]
     out["face_vertices"] = faces

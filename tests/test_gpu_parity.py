@@ -67,6 +67,14 @@ CASES = {
     "tgv-hex-p3-lf": lambda: cases.tgv_case(n=3, p=3, flux=sdg.LAX_FRIEDRICHS, steps=3),
     "tgv-hex-p4-hllc": lambda: cases.tgv_case(n=3, p=4, flux=sdg.HLLC, steps=2),
     "tgv-hex-p5-roe": lambda: cases.tgv_case(n=3, p=5, flux=sdg.ROE, steps=2),
+    # tetrahedra (dense modal blocks in 3D; shuffled vertex lists: shared faces at all three rotations)
+    "tet-tgv-p1-hllc": lambda: cases.tet_tgv_case(n=3, p=1, flux=sdg.HLLC, steps=4),
+    "tet-tgv-p2-roe": lambda: cases.tet_tgv_case(n=3, p=2, flux=sdg.ROE, steps=3),
+    "tet-tgv-p3-lf": lambda: cases.tet_tgv_case(n=3, p=3, flux=sdg.LAX_FRIEDRICHS, steps=3),
+    "tet-tgv-p3-central": lambda: cases.tet_tgv_case(n=3, p=3, flux=sdg.CENTRAL, steps=2),
+    "tet-farfield-p2-hllc": lambda: cases.tet_box_case(p=2, flux=sdg.HLLC),
+    "tet-slip-inflow-outflow-p3-roe": lambda: cases.tet_box_case(
+        p=3, flux=sdg.ROE, conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW) + (sdg.ADIABATIC_SLIP_WALL,) * 4),
     "kh-hybrid-p4-lf": lambda: cases.kh_case(n=6, p=4, flux=sdg.LAX_FRIEDRICHS, steps=4),
     "kh-jitter-quad-p3-hllc": lambda: cases.kh_case(n=6, p=3, flux=sdg.HLLC, split=0.0, steps=4),
     "kh-jitter-quad-p1-roe": lambda: cases.kh_case(n=6, p=1, flux=sdg.ROE, split=0.0, steps=4),
