@@ -504,6 +504,13 @@ __device__ __forceinline__ int rightPoint(int j, int rot, int n1d) {
   }
 }
 
+// Right point of left point j on an interior face: the tensor rotation, or the permutation table of
+// triangular faces (n1d < 0).
+template <int DIM>
+__device__ __forceinline__ int pairedPoint(const FaceArgs& a, int j, int rot, int nfq) {
+  return (DIM == 3 && a.n1d < 0) ? a.perm[rot * nfq + j] : rightPoint<DIM>(j, rot, a.n1d);
+}
+
 // Interior-face Riemann flux.  Left slot gets +|J_f| h, right slot gets -|J_f| h at the permuted point
 // (SpatialDiscrete.cpp:633-748).
 template <int DIM, int FLUX>
@@ -515,7 +522,7 @@ __device__ __forceinline__ void faceInteriorPoint(const FaceArgs& a, int64_t t) 
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
   const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
-  const int jr = (DIM == 3 && n1d < 0) ? a.perm[rot * nfq + j] : rightPoint<DIM>(j, rot, n1d);
+  const int jr = pairedPoint<DIM>(a, j, rot, nfq);
   double* L = a.face + int64_t(sl) * NV * nfq + j;
   double* R = a.face + int64_t(sr) * NV * nfq + jr;
   double ul[NV], ur[NV];

@@ -449,23 +449,24 @@ __global__ void __launch_bounds__(kMaxTileThreads)
 // gradient coefficients = M^-1 R_vg (SpatialDiscrete.cpp:294-322,844-968,1034-1068; TimeIntegration.cpp:200-228).
 // X = U+ (neighbour trace) gives the total gradient (BR1, and the BR2 volume-point gradient); X = {U} the BR2
 // volume part, to which face f adds its own lift r_f = M^-1 sum_{j in f} wf_j nF_f 1/2[U] phi.
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int DIM = 2>
 struct DenseGradShape {
-  static constexpr int NV = 4, NFP = NF * NFQ, EPB = 8, THREADS = 256;
+  static constexpr int NV = DIM + 2, NFP = NF * NFQ, EPB = 8, THREADS = 256;
   static constexpr int USTRIDE = (NV * NB + 1) & ~1;
   static constexpr int FS = NF * NV * NFQ;
+  static_assert(AFFINE || DIM == 2, "the general (bilinear) form is built for quadrangles");
   // affine: modal operators (phif, dmod, emod, lmod) and one coefficient block per element;
   // bilinear: the general form with the element's own M^-1
-  static constexpr int PER_ELEM = AFFINE ? USTRIDE + 2 * FS + NV * 2 * NB : USTRIDE + 2 * FS + NV * NQ + 3 * NV * 2 * NB;
-  static constexpr size_t TABLES = AFFINE ? size_t(NFP) * NB + size_t(2) * NB * NB + size_t(NF) * NB * NFQ + size_t(NF) * NFQ * NFQ
+  static constexpr int PER_ELEM = AFFINE ? USTRIDE + 2 * FS + NV * DIM * NB : USTRIDE + 2 * FS + NV * NQ + 3 * NV * 2 * NB;
+  static constexpr size_t TABLES = AFFINE ? size_t(NFP) * NB + size_t(DIM) * NB * NB + size_t(NF) * NB * NFQ + size_t(NF) * NFQ * NFQ
                                           : size_t(NQ) * NB * 3 + size_t(NFP) * NB * 2 + size_t(NB) * NB;
   static constexpr size_t SMEM = (size_t(EPB) * PER_ELEM + TABLES) * 8 + 16;
   static constexpr size_t smemFor(int epb) { return (size_t(epb) * PER_ELEM + TABLES) * 8 + 16; }
 };
 
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int DIM = 2>
 __device__ __forceinline__ uint64_t* denseGradBarrier(int epb) {
-  using G = DenseGradShape<NB, NQ, NFQ, NF, AFFINE>;
+  using G = DenseGradShape<NB, NQ, NFQ, NF, AFFINE, DIM>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   return reinterpret_cast<uint64_t*>(reinterpret_cast<double*>(smem_raw) + epb * G::PER_ELEM + G::TABLES);
 }
@@ -475,9 +476,9 @@ struct DenseGradArgs {
   const double* face;
   const double* faceOther;
   double* faceGrad;
-  double* grad;             // modal gradient coefficients [e][nv*2][NB]
+  double* grad;             // modal gradient coefficients [e][nv*d][NB]
   const double* geom;
-  const double* fmetric;    // [e][NF][2] outward n|J_f|
+  const double* fmetric;    // [e][NF][d] outward n|J_f|
   const double* tables;
   unsigned* status;
   int64_t ne, faceBase;
@@ -504,11 +505,11 @@ __device__ __forceinline__ double denseFaceEps(const DenseGradArgs& a, int64_t e
 //   w_vol(v,k) = w_tot(v,k) - (1/|J|) sum_f nF_f[k] E_f (1/2 [U])_f(v)
 // and the BR2 trace at face f adds (1/|J|) nF_f L_f (1/2 [U])_f: the same quantities as the general form
 // below, with M^-1 folded into the precomputed operators.
-template <int NB, int NQ, int NFQ, int NF>
+template <int NB, int NQ, int NFQ, int NF, int DIM = 2>
 __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, int64_t tile, uint32_t parity,
                                                         bool loadTables) {
-  using G = DenseGradShape<NB, NQ, NFQ, NF, true>;
-  constexpr int NV = 4, NFP = G::NFP, FS = G::FS, NR = NV * 2;
+  using G = DenseGradShape<NB, NQ, NFQ, NF, true, DIM>;
+  constexpr int NV = DIM + 2, NFP = G::NFP, FS = G::FS, NR = NV * DIM, GD = DIM * DIM + 1;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   const int EPB = a.epb;
   double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE] modal coefficients
@@ -517,8 +518,8 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
   double* sW = sO + EPB * FS;                        // coefficients whose traces are the face gradients [EPB][NR][NB]
   double* tab = sW + EPB * NR * NB;
   const double* phif = tab;                          // [NFP][NB]
-  const double* dmod = phif + NFP * NB;              // [2][NB][NB]
-  const double* emod = dmod + 2 * NB * NB;           // [NF][NB][NFQ]
+  const double* dmod = phif + NFP * NB;              // [DIM][NB][NB]
+  const double* emod = dmod + DIM * NB * NB;         // [NF][NB][NFQ]
   const double* lmod = emod + NF * NB * NFQ;         // [NF][NFQ][NFQ]
   uint64_t* bar = reinterpret_cast<uint64_t*>(tab + G::TABLES);
 
@@ -535,8 +536,8 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
     bulkLoad(sO, a.faceOther + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
   if (loadTables) {
-    constexpr int OFF_PHIF = NQ * NB * 3, OFF_DMOD = NQ * NB * 3 + NFP * NB * 2 + NB * NB;
-    constexpr int NOPS = 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
+    constexpr int OFF_PHIF = NQ * NB * (1 + DIM), OFF_DMOD = NQ * NB * (1 + DIM) + NFP * NB * 2 + NB * NB;
+    constexpr int NOPS = DIM * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
     for (int k = tid; k < NFP * NB; k += blockDim.x) tab[k] = a.tables[OFF_PHIF + k];
     for (int k = tid; k < NOPS; k += blockDim.x) tab[NFP * NB + k] = a.tables[OFF_DMOD + k];
   }
@@ -554,18 +555,25 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
     const int le = idx / (NV * NB), r = idx - le * NV * NB;
     const int v = r / NB, i = r - v * NB;
     const int64_t e = e0 + le;
-    const double* g = a.geom + e * 5;
-    const double ja00 = g[0], ja01 = g[1], ja10 = g[2], ja11 = g[3], jinv = g[4];
+    const double* g = a.geom + e * GD;
+    const double jinv = g[DIM * DIM];
     const double* u = sU + le * G::USTRIDE + v * NB;
-    double d0 = 0.0, d1 = 0.0;
+    double d[DIM] = {};
 #pragma unroll
     for (int m = 0; m < NB; ++m) {
-      d0 = fma(dmod[i * NB + m], u[m], d0);
-      d1 = fma(dmod[(NB + i) * NB + m], u[m], d1);
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) d[b] = fma(dmod[(b * NB + i) * NB + m], u[m], d[b]);
     }
-    double tot0 = -fma(ja00, d0, ja10 * d1), tot1 = -fma(ja01, d0, ja11 * d1);
-    double jmp0 = 0.0, jmp1 = 0.0;
-    const double* nF = a.fmetric + e * NF * 2;
+    // tot_k = -sum_b (|J| dxi_b/dx_k) d_b, jmp_k: the BR2 jump part
+    double tot[DIM], jmp[DIM] = {};
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      double s = g[(DIM - 1) * DIM + k] * d[DIM - 1];
+#pragma unroll
+      for (int b = DIM - 2; b >= 0; --b) s = fma(g[b * DIM + k], d[b], s);
+      tot[k] = -s;
+    }
+    const double* nF = a.fmetric + e * NF * DIM;
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       const double* O = sO + le * FS + (f * NV + v) * NFQ;
@@ -577,16 +585,19 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
         ep = fma(E[j], O[j], ep);
         ej = fma(E[j], 0.5 * (O[j] - S[j]), ej);
       }
-      const double n0 = nF[f * 2 + 0], n1 = nF[f * 2 + 1];
-      tot0 = fma(n0, ep, tot0); tot1 = fma(n1, ep, tot1);
-      jmp0 = fma(n0, ej, jmp0); jmp1 = fma(n1, ej, jmp1);
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        tot[k] = fma(nF[f * DIM + k], ep, tot[k]);
+        jmp[k] = fma(nF[f * DIM + k], ej, jmp[k]);
+      }
     }
-    const double g0 = jinv * tot0, g1 = jinv * tot1;
-    // artificial viscosity keeps the volume-gradient coefficients (ViscousFluxEnum::None gradient)
-    a.grad[(e * NR + v * 2 + 0) * NB + i] = a.av ? jinv * (tot0 - jmp0) : g0;
-    a.grad[(e * NR + v * 2 + 1) * NB + i] = a.av ? jinv * (tot1 - jmp1) : g1;
-    sW[(le * NR + v * 2 + 0) * NB + i] = a.br2 ? jinv * (tot0 - jmp0) : g0;
-    sW[(le * NR + v * 2 + 1) * NB + i] = a.br2 ? jinv * (tot1 - jmp1) : g1;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) {
+      const double gk = jinv * tot[k];
+      // artificial viscosity keeps the volume-gradient coefficients (ViscousFluxEnum::None gradient)
+      a.grad[(e * NR + v * DIM + k) * NB + i] = a.av ? jinv * (tot[k] - jmp[k]) : gk;
+      sW[(le * NR + v * DIM + k) * NB + i] = a.br2 ? jinv * (tot[k] - jmp[k]) : gk;
+    }
   }
   __syncthreads();
   // 2. face gradient traces per (element, face point, variable)
@@ -595,18 +606,17 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
     const int fj = r / NV, v = r - fj * NV;
     const int f = fj / NFQ, j = fj - f * NFQ;
     const int64_t e = e0 + le;
-    const double* w0 = sW + (le * NR + v * 2) * NB;
-    const double* w1 = w0 + NB;
-    double acc0 = 0.0, acc1 = 0.0;
+    const double* w = sW + (le * NR + v * DIM) * NB;
+    double acc[DIM] = {};
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
-      acc0 = fma(phif[fj * NB + b], w0[b], acc0);
-      acc1 = fma(phif[fj * NB + b], w1[b], acc1);
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) acc[k] = fma(phif[fj * NB + b], w[k * NB + b], acc[k]);
     }
     if (a.av) {
       const double eps = denseFaceEps<NB, NQ, NF>(a, e, fj);
-      acc0 *= eps;
-      acc1 *= eps;
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) acc[k] *= eps;
     } else if (a.br2) {
       const double* O = sO + le * FS + (f * NV + v) * NFQ;
       const double* S = sS + le * FS + (f * NV + v) * NFQ;
@@ -614,20 +624,20 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
       double lift = 0.0;
 #pragma unroll
       for (int jj = 0; jj < NFQ; ++jj) lift = fma(L[jj], 0.5 * (O[jj] - S[jj]), lift);
-      lift *= a.geom[e * 5 + 4];
-      acc0 = fma(a.fmetric[(e * NF + f) * 2 + 0], lift, acc0);
-      acc1 = fma(a.fmetric[(e * NF + f) * 2 + 1], lift, acc1);
+      lift *= a.geom[e * GD + DIM * DIM];
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) acc[k] = fma(a.fmetric[(e * NF + f) * DIM + k], lift, acc[k]);
     }
     double* out = a.faceGrad + (a.faceBase + e * NF + f) * NR * NFQ + j;
-    out[(v * 2 + 0) * NFQ] = acc0;
-    out[(v * 2 + 1) * NFQ] = acc1;
+#pragma unroll
+    for (int k = 0; k < DIM; ++k) out[(v * DIM + k) * NFQ] = acc[k];
   }
   return true;
 }
 
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int DIM = 2>
 __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_t tile, uint32_t parity, bool loadTables) {
-  if constexpr (AFFINE) return denseGradientAffineTile<NB, NQ, NFQ, NF>(a, tile, parity, loadTables);
+  if constexpr (AFFINE) return denseGradientAffineTile<NB, NQ, NFQ, NF, DIM>(a, tile, parity, loadTables);
   using G = DenseGradShape<NB, NQ, NFQ, NF, AFFINE>;
   constexpr int NV = 4, NFP = G::NFP, FS = G::FS, NR = NV * 2;
   const int EPB = a.epb;
@@ -800,31 +810,33 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
   return true;
 }
 
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int DIM = 2>
 __global__ void __launch_bounds__(kMaxTileThreads) denseGradientKernel(DenseGradArgs a) {
-  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF, AFFINE>(a.epb), 1);
-  denseGradientTile<NB, NQ, NFQ, NF, AFFINE>(a, blockIdx.x, 0u, true);
+  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF, AFFINE, DIM>(a.epb), 1);
+  denseGradientTile<NB, NQ, NFQ, NF, AFFINE, DIM>(a, blockIdx.x, 0u, true);
 }
 
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int DIM = 2>
 __global__ void __launch_bounds__(kMaxTileThreads)
     denseGradientBatchKernel(const DenseGradArgs* __restrict__ args, const int2* __restrict__ items, int nitems, int epb) {
-  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF, AFFINE>(epb), 1);
+  if (threadIdx.x == 0) mbarInit(denseGradBarrier<NB, NQ, NFQ, NF, AFFINE, DIM>(epb), 1);
   uint32_t parity = 0;
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const int2 it = items[w];
     const DenseGradArgs a = args[it.x];
-    if (!denseGradientTile<NB, NQ, NFQ, NF, AFFINE>(a, it.y, parity, w == int(blockIdx.x))) return;
+    if (!denseGradientTile<NB, NQ, NFQ, NF, AFFINE, DIM>(a, it.y, parity, w == int(blockIdx.x))) return;
     parity ^= 1u;
   }
 }
 
-// (type, P) -> (NB, NQ, NFQ): triangle P1..P5 use Dunavant rules of 3,6,12,16,25 points.
-// Tetrahedra (dense blocks of DIM 3): P = 1..3, the Euler stage only.
+// Tetrahedra (dense blocks of DIM 3, affine): P = 1..3 with the Keast rules of 4, 11, 24 points and the
+// Dunavant face rules of 4, 7, 13 points.
 #define SDG_TET_CASES(X)                        \
   X(SDG_ELEMENT_TETRAHEDRON, 1, 4, 4, 4, 4)     \
   X(SDG_ELEMENT_TETRAHEDRON, 2, 10, 11, 7, 4)   \
   X(SDG_ELEMENT_TETRAHEDRON, 3, 20, 24, 13, 4)
+
+// (type, P) -> (NB, NQ, NFQ): triangle P1..P5 use Dunavant rules of 3,6,12,16,25 points.
 
 #define SDG_DENSE_CASES(X)                                  \
   X(SDG_ELEMENT_TRIANGLE, 1, 3, 3, 2, 3, true)              \

@@ -50,7 +50,7 @@ __device__ __forceinline__ void exchangePoint(const FaceArgs& a, int64_t t) {
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
   const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
-  const int jr = rightPoint<DIM>(j, rot, n1d);
+  const int jr = pairedPoint<DIM>(a, j, rot, nfq);
   const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
 #pragma unroll
   for (int v = 0; v < NV; ++v) {
@@ -375,7 +375,7 @@ __device__ __forceinline__ void faceNSPoint(const FaceArgs& a, int64_t t) {
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
   const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
-  const int jr = rightPoint<DIM>(j, rot, n1d);
+  const int jr = pairedPoint<DIM>(a, j, rot, nfq);
   const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
   const int64_t LG = int64_t(sl) * NV * DIM * nfq + j, RG = int64_t(sr) * NV * DIM * nfq + jr;
   const Phys& ph = a.ph;
@@ -489,7 +489,7 @@ __device__ __forceinline__ void faceAVPoint(const FaceArgs& a, int64_t t) {
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
   const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
-  const int jr = rightPoint<DIM>(j, rot, n1d);
+  const int jr = pairedPoint<DIM>(a, j, rot, nfq);
   const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
   const int64_t LG = int64_t(sl) * NV * DIM * nfq + j, RG = int64_t(sr) * NV * DIM * nfq + jr;
   const Phys& ph = a.ph;

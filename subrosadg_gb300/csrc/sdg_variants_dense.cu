@@ -17,12 +17,12 @@ KernelVariant stageOf() {
   v.perElem = size_t(S::PER_ELEM) * 8; v.fixed = S::TABLES * 8 + 16; v.perWarp = 8 * S::NV;
   return v;
 }
-template <int NB, int NQ, int NFQ, int NF, bool AFF>
+template <int NB, int NQ, int NFQ, int NF, bool AFF, int DIM = 2>
 KernelVariant gradOf() {
-  using G = DenseGradShape<NB, NQ, NFQ, NF, AFF>;
+  using G = DenseGradShape<NB, NQ, NFQ, NF, AFF, DIM>;
   KernelVariant v;
-  v.single = reinterpret_cast<const void*>(&denseGradientKernel<NB, NQ, NFQ, NF, AFF>);
-  v.batch = reinterpret_cast<const void*>(&denseGradientBatchKernel<NB, NQ, NFQ, NF, AFF>);
+  v.single = reinterpret_cast<const void*>(&denseGradientKernel<NB, NQ, NFQ, NF, AFF, DIM>);
+  v.batch = reinterpret_cast<const void*>(&denseGradientBatchKernel<NB, NQ, NFQ, NF, AFF, DIM>);
   v.nb = NB; v.epb = G::EPB; v.threads = G::THREADS; v.nodeThreads = false;
   v.perElem = size_t(G::PER_ELEM) * 8; v.fixed = G::TABLES * 8 + 16; v.perWarp = 0;
   return v;
@@ -36,8 +36,9 @@ KernelVariant denseStageVariant(int type, int p, bool affine, int visc) {
                      : visc ? stageOf<NB, NQ, NFQ, NF, AFF, 1>() : stageOf<NB, NQ, NFQ, NF, AFF, 0>();
   SDG_DENSE_CASES(SDG_DS)
 #undef SDG_DS
-#define SDG_DT(T, P, NB, NQ, NFQ, NF) \
-  if (type == T && p == P && affine && visc == 0) return stageOf<NB, NQ, NFQ, NF, true, 0, 3>();
+#define SDG_DT(T, P, NB, NQ, NFQ, NF)                                                                   \
+  if (type == T && p == P && affine && visc < 2)                                                          \
+    return visc ? stageOf<NB, NQ, NFQ, NF, true, 1, 3>() : stageOf<NB, NQ, NFQ, NF, true, 0, 3>();
   SDG_TET_CASES(SDG_DT)
 #undef SDG_DT
   return KernelVariant();
@@ -48,6 +49,10 @@ KernelVariant denseGradVariant(int type, int p, bool affine) {
   if (type == T && p == P && affine == AFF) return gradOf<NB, NQ, NFQ, NF, AFF>();
   SDG_DENSE_CASES(SDG_DG)
 #undef SDG_DG
+#define SDG_DGT(T, P, NB, NQ, NFQ, NF) \
+  if (type == T && p == P && affine) return gradOf<NB, NQ, NFQ, NF, true, 3>();
+  SDG_TET_CASES(SDG_DGT)
+#undef SDG_DGT
   return KernelVariant();
 }
 

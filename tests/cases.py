@@ -108,15 +108,18 @@ def tet_mesh(n=3, length=1.0, periodic=True, conditions=None, seed=7):
     return mesh
 
 
-def tet_tgv_case(n=3, p=2, flux=sdg.HLLC, steps=3, mach=0.3):
-    """Taylor-Green vortex on periodic tetrahedra of [0, 2 pi]^3 (Mach 0.3 for a nonlinear flux)."""
+def tet_tgv_case(n=3, p=2, flux=sdg.HLLC, steps=3, mach=0.3, viscous=None, mu=0.02):
+    """Taylor-Green vortex on periodic tetrahedra of [0, 2 pi]^3 (Mach 0.3 for a nonlinear flux); with
+    `viscous` the Navier-Stokes case at Re = 1/mu."""
     mesh = tet_mesh(n, 2 * math.pi)
     dt = 0.2 * (2 * math.pi / n) / ((1.0 + 1.0 / mach) * (p + 1) ** 2)
-    return (mesh, config(p, flux), lambda pts: tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2], mach=mach), None, dt,
+    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
+    return (mesh, cfg, lambda pts: tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2], mach=mach), None, dt,
             steps)
 
 
-def tet_box_case(p=2, flux=sdg.HLLC, conditions=(sdg.RIEMANN_FARFIELD,) * 6, n=3, dt=5e-4, steps=3):
+def tet_box_case(p=2, flux=sdg.HLLC, conditions=(sdg.RIEMANN_FARFIELD,) * 6, n=3, dt=5e-4, steps=3, viscous=None,
+                 mu=0.01):
     """Non-periodic tetrahedral unit box, groups x-, x+, y-, y+, z-, z+: a smooth perturbation of a uniform
     stream at u = (0.4, 0.1, -0.1), the same stream as the boundary state (inflow at x-, outflow at x+)."""
     mesh = tet_mesh(n, 1.0, periodic=False, conditions=conditions)
@@ -137,7 +140,8 @@ def tet_box_case(p=2, flux=sdg.HLLC, conditions=(sdg.RIEMANN_FARFIELD,) * 6, n=3
         out[:, 4] = 1.0 / R_GAS
         return out
 
-    return (mesh, config(p, flux), ic, bc, dt, steps)
+    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
+    return (mesh, cfg, ic, bc, dt, steps)
 
 
 def kh_case(n=8, p=4, flux=sdg.LAX_FRIEDRICHS, dt=2e-4, steps=3, jitter=0.1, split=0.5, seed=11, viscous=None,

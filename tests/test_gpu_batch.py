@@ -42,6 +42,7 @@ MIXED = {
     "euler-line-p3-hllc": lambda: cases.density_wave_1d_case(n=20, p=3),
     "euler-tet-p2-roe": lambda: cases.tet_tgv_case(n=3, p=2, flux=sdg.ROE),
     "euler-tet-box-p3-hllc": lambda: cases.tet_box_case(p=3, flux=sdg.HLLC),
+    "ns-tet-p2-br2-lf": lambda: cases.tet_tgv_case(n=3, p=2, flux=sdg.LAX_FRIEDRICHS, viscous=sdg.BR2, mu=0.02),
     # artificial viscosity: the per-step sensor passes run as batched levels before stage 0
     "av-shocktube-hybrid-p2-lf": lambda: cases.shock_tube_case(p=2, flux=sdg.LAX_FRIEDRICHS, split=0.5, jitter=0.1),
     "av-sod-line-p3-hllc": lambda: cases.sod_1d_case(n=99, p=3),

@@ -75,6 +75,13 @@ CASES = {
     "tet-farfield-p2-hllc": lambda: cases.tet_box_case(p=2, flux=sdg.HLLC),
     "tet-slip-inflow-outflow-p3-roe": lambda: cases.tet_box_case(
         p=3, flux=sdg.ROE, conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW) + (sdg.ADIABATIC_SLIP_WALL,) * 4),
+    "ns-tet-tgv-p2-br1-roe": lambda: cases.tet_tgv_case(n=3, p=2, flux=sdg.ROE, viscous=sdg.BR1, mu=0.02),
+    "ns-tet-tgv-p3-br2-hllc": lambda: cases.tet_tgv_case(n=3, p=3, flux=sdg.HLLC, steps=2, viscous=sdg.BR2, mu=0.02),
+    "ns-tet-walls-p2-br2-lf": lambda: cases.tet_box_case(
+        p=2, flux=sdg.LAX_FRIEDRICHS, viscous=sdg.BR2, mu=0.01,
+        conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
+                    sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL)),
+    "ns-tet-box-p1-br1-hllc": lambda: cases.tet_box_case(p=1, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01),
     "kh-hybrid-p4-lf": lambda: cases.kh_case(n=6, p=4, flux=sdg.LAX_FRIEDRICHS, steps=4),
     "kh-jitter-quad-p3-hllc": lambda: cases.kh_case(n=6, p=3, flux=sdg.HLLC, split=0.0, steps=4),
     "kh-jitter-quad-p1-roe": lambda: cases.kh_case(n=6, p=1, flux=sdg.ROE, split=0.0, steps=4),
