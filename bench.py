@@ -19,6 +19,7 @@ workloads of the metric, each measured the same way on this GPU:
   ns_hybrid    2D Navier-Stokes BR2 Kelvin-Helmholtz, Re 1e4, 256^2 jittered quads with a 50% triangle
                split, P4, Lax-Friedrichs
   vortex2d     2D Euler isentropic vortex, 40^2 quads, P3, Roe, dt 1e-3 (L2-resident, launch bound)
+  tet          3D Euler Taylor-Green vortex (Mach 0.3) on periodic tetrahedra, 32^3 cubes x 6, P3, HLLC
   adjoint      3D Navier-Stokes BR1 Taylor-Green, Re 1600, Mach 0.1, 32^3 hexahedra, P3, Roe, 500 SSP-RK3 steps:
                forward, checkpointed adjoint (every 25 steps) of the integrated kinetic energy, reverse sweep
                of a recorded trajectory, and central-difference checks of dJ/dU0 (seeded direction) and dJ/dmu
@@ -59,11 +60,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="headline workload only")
-    ap.add_argument("--extra", default="batched,batched_small,ns_hybrid,vortex2d,adjoint",
+    ap.add_argument("--extra", default="batched,batched_small,ns_hybrid,vortex2d,tet,adjoint",
                     help="comma list of the other workloads to measure")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-max-elements", type=int, default=50000)
     ap.add_argument("--ns-elements", type=int, default=256, help="quads per direction of the NS hybrid mesh")
+    ap.add_argument("--tet-elements", type=int, default=32, help="cubes per side of the tetrahedral section")
     ap.add_argument("--adjoint-elements", type=int, default=32)
     ap.add_argument("--adjoint-steps", type=int, default=500)
     ap.add_argument("--no-adjoint-check", action="store_true", help="skip the finite-difference checks")
@@ -284,6 +286,35 @@ def bench_ns_hybrid(args, device, torch):
     out = {"workload": f"ns-kh2d-BR2-Re1e4-{n}^2-hybrid-P4-LF", "elements": g.counts.element_count, "dof": dof,
            "value": dof * 3 * steps / (ms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": ms / steps,
            "tiles": [g.tile(k) for k in range(g.counts.block_count)]}
+    g.close()
+    return out
+
+
+def bench_tet(args, device, torch):
+    """3D Euler Taylor-Green vortex (Mach 0.3) on periodic tetrahedra: 32^3 cubes x 6, P3 (20 modes), HLLC."""
+    import ctypes
+
+    import subrosadg_gb300 as sdg
+    from tests import cases
+    n = args.tet_elements
+    mesh, cfg, prim, _, _, _ = cases.tet_tgv_case(n=n, p=3, flux=sdg.HLLC)
+    g = sdg.GpuSolver(mesh, cfg, device=device)
+    g.initialize_primitive(prim(g.volume_points()))
+    dt = g.calculateDeltaTime(0.2)
+    g.autotune()
+    sp = ctypes.c_void_p()
+    g.lib.sdg_get_stream(g.h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value, device=device)
+    for _ in range(args.warmup):
+        g.step_async(dt)
+    g.synchronize()
+    steps = max(3, args.steps)
+    ms = _timed(torch, stream, lambda: g.step_async(dt), steps)
+    g.synchronize()
+    dof = g.counts.degree_of_freedom_count
+    out = {"workload": f"tgv3d-euler-Ma0.3-{n}^3x6-tet-P3-HLLC", "elements": g.counts.element_count, "dof": dof,
+           "value": dof * 3 * steps / (ms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": ms / steps,
+           "l2": f"state {8 * dof / 1e6:.0f} MB per buffer (L2 129 MB)", "tiles": [g.tile(0)]}
     g.close()
     return out
 
@@ -522,6 +553,7 @@ def run_ours(args):
     s.close()
     if not args.no_extra:
         extras = {"batched": bench_batched, "ns_hybrid": bench_ns_hybrid, "vortex2d": bench_vortex,
+                  "tet": bench_tet,
                   "adjoint": bench_adjoint,
                   "batched_small": lambda a, d, t: bench_batched(a, d, t, max_elements=2000)}
         for name in [x for x in args.extra.split(",") if x]:

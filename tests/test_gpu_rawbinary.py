@@ -62,6 +62,9 @@ def make(case):
                                                                        sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW))),
     ("euler-line-p3-farfield", lambda: cases.sod_1d_case(n=9, p=3, av=False)),
     ("ns-line-p2-br1", lambda: cases.density_wave_1d_case(n=8, p=2, viscous=sdg.BR1, mu=0.01)),
+    ("euler-tet-p3", lambda: cases.tet_tgv_case(n=3, p=3)),
+    ("ns-tet-walls-p2-br2", lambda: cases.tet_box_case(p=2, viscous=sdg.BR2, mu=0.01,
+                                                      conditions=(sdg.ADIABATIC_NONSLIP_WALL,) * 6)),
 ])
 def test_raw_binary_layout(tmp_path, name, case):
     s, dt, mesh = make(case())
