@@ -8,7 +8,9 @@
 //                 src/Solver/SimulationControl.cpp:381-523 (face point permutation by rotation)
 // gmsh 4.13.1 is not vendored under the reference tree, so its Lobatto normalisation, point orderings
 // and triangle tables are restated from the published definitions (parity for these is unpinned
-// against gmsh itself; the DG solution does not depend on the basis choice).
+// against gmsh itself; the DG solution does not depend on the basis choice).  Tetrahedra use Keast's
+// volume rules and Dunavant's odd-degree face rules (tetrahedron_rules.h, shared with the GPU host layer),
+// whose point counts are the reference's kTetrahedron/kTriangleQuadratureNumber for P1..P3.
 #pragma once
 #include <array>
 #include <limits>
