@@ -490,8 +490,21 @@ struct RefElement {
       if (t == kLine || t == kQuad || t == kHex) {
         int r = b;
         for (int dd = 0; dd < dim; ++dd) { deg = std::max(deg, std::max(1, r % (order + 1))); r /= order + 1; }
-      } else if (t == kTet) {  // no artificial viscosity on tetrahedra: the degrees are not needed
-        deg = 0;
+      } else if (t == kTet) {  // vertices, then 6 edges x (P-1), 4 faces x (P-1)(P-2)/2, then the interior
+        const int ne = 6 * (order - 1), nfm = (order - 1) * (order - 2) / 2;
+        if (b < 4) {
+          deg = 1;
+        } else if (b < 4 + ne) {
+          deg = 2 + (b - 4) % (order - 1);
+        } else if (b < 4 + ne + 4 * nfm) {
+          int idx = (b - 4 - ne) % nfm, sdeg = 0;
+          while (idx > sdeg) { idx -= sdeg + 1; ++sdeg; }
+          deg = sdeg + 3;
+        } else {
+          int idx = b - 4 - ne - 4 * nfm, sdeg = 0;
+          while (idx >= (sdeg + 1) * (sdeg + 2) / 2) { idx -= (sdeg + 1) * (sdeg + 2) / 2; ++sdeg; }
+          deg = sdeg + 4;
+        }
       } else if (b < 3) {
         deg = 1;
       } else if (b < 3 + 3 * (order - 1)) {

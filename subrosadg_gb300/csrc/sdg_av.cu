@@ -83,7 +83,7 @@ __device__ double avDenseSensor(const AvArgs& a, int64_t e) {
   const double* high = phi + nq * nb;
   const double* w = high + nb;
   const double* c = a.u + e * a.ustride;  // density: the first nb modal coefficients
-  const int gstride = a.affine ? 5 : nq * 5 + nb * nb;
+  const int gs = a.dim * a.dim + 1, gstride = a.affine ? gs : nq * gs + nb * nb;
   double num = 0.0, den = 0.0;
   for (int q = 0; q < nq; ++q) {
     double all = 0.0, hi = 0.0;
@@ -92,7 +92,7 @@ __device__ double avDenseSensor(const AvArgs& a, int64_t e) {
       all += x;
       hi += high[b] * x;
     }
-    const double jinv = a.affine ? a.geom[e * gstride + 4] : a.geom[e * gstride + q * 5 + 4];
+    const double jinv = a.affine ? a.geom[e * gstride + gs - 1] : a.geom[e * gstride + q * gs + gs - 1];
     const double jw = w[q] / jinv;
     num = fma(hi, hi * jw, num);
     den = fma(all, all * jw, den);
@@ -161,8 +161,9 @@ Rec avRec(int kind, int64_t count) {
 
 // Inner radius (gmsh quality "innerRadius", Geometry.cpp:31-41; gmsh 4.13.1 is not vendored): half the length of
 // a line (gmsh MLine), 2A/perimeter for
-// triangles and quadrangles (A of a quadrangle from its diagonals), 3V/S for hexahedra (V by 2x2x2 Gauss
-// quadrature of the trilinear map, each face's area from its diagonals); exact for squares and cubes.
+// triangles and quadrangles (A of a quadrangle from its diagonals), 3V/S for tetrahedra and hexahedra (hexahedra:
+// V by 2x2x2 Gauss quadrature of the trilinear map, each face's area from its diagonals); exact for squares and
+// cubes.
 double innerRadiusOf(int type, const double* nodes, const int32_t* vv) {
   auto sub = [&](int a, int b, double* o) {
     for (int d = 0; d < 3; ++d) o[d] = nodes[size_t(vv[a]) * 3 + d] - nodes[size_t(vv[b]) * 3 + d];
@@ -179,6 +180,20 @@ double innerRadiusOf(int type, const double* nodes, const int32_t* vv) {
     if (type == SDG_ELEMENT_TRIANGLE) { sub(1, 0, d1); sub(2, 0, d2); }
     else { sub(2, 0, d1); sub(3, 1, d2); }
     return crossNorm(d1, d2) / per;
+  }
+  if (type == SDG_ELEMENT_TETRAHEDRON) {
+    double a[3], b[3], c[3];
+    sub(1, 0, a); sub(2, 0, b); sub(3, 0, c);
+    const double vol = std::fabs(a[0] * (b[1] * c[2] - b[2] * c[1]) - a[1] * (b[0] * c[2] - b[2] * c[0]) +
+                                 a[2] * (b[0] * c[1] - b[1] * c[0])) / 6.0;
+    const int* fl = faceVertexList(type);
+    double area = 0;
+    for (int f = 0; f < 4; ++f) {
+      double d1[3], d2[3];
+      sub(fl[f * 3 + 1], fl[f * 3], d1); sub(fl[f * 3 + 2], fl[f * 3], d2);
+      area += crossNorm(d1, d2) / 2.0;
+    }
+    return 3.0 * vol / area;
   }
   static const int faces[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {0, 4, 7, 3}, {1, 2, 6, 5}, {2, 3, 7, 6}, {4, 5, 6, 7}};
   double area = 0;
@@ -225,9 +240,23 @@ void buildAvTables(DevBlock& B) {
   const int nb = B.nb, nq = vr.n, nvert = typeVertices(B.type);
   t.insert(t.end(), B.phi.begin(), B.phi.end());  // [nq][nb]
   // degrees of the modes (modalBasis order): vertices 1; triangle edge modes k = 2..P edge by edge, bubbles
-  // i + j + 3 by increasing i + j; quadrangles (P1 only here) are all degree 1 -- P1 takes the whole density
+  // i + j + 3 by increasing i + j; tetrahedra: six edges of modes k = 2..P, four faces of bubbles s + 3
+  // (s = 0..P-3, s + 1 modes each), interior bubbles s + 4; quadrangles (P1 only here) are all degree 1 --
+  // P1 takes the whole density
+  std::vector<int> tetDegree;
+  if (B.type == SDG_ELEMENT_TETRAHEDRON) {
+    tetDegree.assign(4, 1);
+    for (int e = 0; e < 6; ++e)
+      for (int k = 2; k <= B.p; ++k) tetDegree.push_back(k);
+    for (int f = 0; f < 4; ++f)
+      for (int s = 0; s <= B.p - 3; ++s)
+        for (int i = 0; i <= s; ++i) tetDegree.push_back(s + 3);
+    for (int s = 0; s <= B.p - 4; ++s)
+      for (int i = 0; i < (s + 1) * (s + 2) / 2; ++i) tetDegree.push_back(s + 4);
+    if (int(tetDegree.size()) != nb) throw Failure(SDG_ERR_INVALID_ARGUMENT, "tetrahedron mode count");
+  }
   for (int b = 0; b < nb; ++b) {
-    int deg = 1;
+    int deg = B.type == SDG_ELEMENT_TETRAHEDRON ? tetDegree[b] : 1;
     if (B.type == SDG_ELEMENT_TRIANGLE && b >= 3) {
       if (b < 3 + 3 * (B.p - 1)) {
         deg = 2 + (b - 3) % (B.p - 1);
@@ -242,6 +271,10 @@ void buildAvTables(DevBlock& B) {
   for (int q = 0; q < nq; ++q) t.push_back(vr.w[q]);
   const auto shape = [&](const double* X, double* sh) {
     if (B.type == SDG_ELEMENT_TRIANGLE) { sh[0] = 1.0 - X[0] - X[1]; sh[1] = X[0]; sh[2] = X[1]; return; }
+    if (B.type == SDG_ELEMENT_TETRAHEDRON) {
+      sh[0] = 1.0 - X[0] - X[1] - X[2]; sh[1] = X[0]; sh[2] = X[1]; sh[3] = X[2];
+      return;
+    }
     sh[0] = 0.25 * (1 - X[0]) * (1 - X[1]); sh[1] = 0.25 * (1 + X[0]) * (1 - X[1]);
     sh[2] = 0.25 * (1 + X[0]) * (1 + X[1]); sh[3] = 0.25 * (1 - X[0]) * (1 + X[1]);
   };

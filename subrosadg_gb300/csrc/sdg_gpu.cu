@@ -877,7 +877,6 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       if (mesh->tetrahedron_count > 0) {
         mb.push_back({SDG_ELEMENT_TETRAHEDRON, mesh->tetrahedron_count, mesh->tetrahedron_node});
         if (c.polynomial_order > 3) throw Failure(SDG_ERR_UNSUPPORTED, "tetrahedra are built for P = 1..3");
-        if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "artificial viscosity is not built for tetrahedra");
       }
       if (mesh->hexahedron_count > 0) mb.push_back({SDG_ELEMENT_HEXAHEDRON, mesh->hexahedron_count, mesh->hexahedron_node});
     }

@@ -37,8 +37,9 @@ KernelVariant denseStageVariant(int type, int p, bool affine, int visc) {
   SDG_DENSE_CASES(SDG_DS)
 #undef SDG_DS
 #define SDG_DT(T, P, NB, NQ, NFQ, NF)                                                                   \
-  if (type == T && p == P && affine && visc < 2)                                                          \
-    return visc ? stageOf<NB, NQ, NFQ, NF, true, 1, 3>() : stageOf<NB, NQ, NFQ, NF, true, 0, 3>();
+  if (type == T && p == P && affine)                                                                      \
+    return visc == 2 ? stageOf<NB, NQ, NFQ, NF, true, 2, 3>()                                             \
+                     : visc ? stageOf<NB, NQ, NFQ, NF, true, 1, 3>() : stageOf<NB, NQ, NFQ, NF, true, 0, 3>();
   SDG_TET_CASES(SDG_DT)
 #undef SDG_DT
   return KernelVariant();

@@ -46,6 +46,7 @@ MIXED = {
     # artificial viscosity: the per-step sensor passes run as batched levels before stage 0
     "av-shocktube-hybrid-p2-lf": lambda: cases.shock_tube_case(p=2, flux=sdg.LAX_FRIEDRICHS, split=0.5, jitter=0.1),
     "av-sod-line-p3-hllc": lambda: cases.sod_1d_case(n=99, p=3),
+    "av-shocktube-tet-p2-hllc": lambda: cases.shock_tube_case(p=2, dim=3, n=8, tets=True),
     "ns-line-walls-p2-br2": lambda: _ns(cases.sod_1d_case(n=30, p=2, av=False, smooth=0.05, dt=1e-5,
                                                           conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.RIEMANN_FARFIELD)),
                                         sdg.BR2, 0.01),

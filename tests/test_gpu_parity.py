@@ -82,6 +82,8 @@ CASES = {
         conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
                     sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL)),
     "ns-tet-box-p1-br1-hllc": lambda: cases.tet_box_case(p=1, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01),
+    "av-shocktube-tet-p2-hllc": lambda: cases.shock_tube_case(p=2, dim=3, n=8, tets=True),
+    "av-shocktube-tet-p3-roe": lambda: cases.shock_tube_case(p=3, flux=sdg.ROE, dim=3, n=6, steps=2, tets=True),
     "kh-hybrid-p4-lf": lambda: cases.kh_case(n=6, p=4, flux=sdg.LAX_FRIEDRICHS, steps=4),
     "kh-jitter-quad-p3-hllc": lambda: cases.kh_case(n=6, p=3, flux=sdg.HLLC, split=0.0, steps=4),
     "kh-jitter-quad-p1-roe": lambda: cases.kh_case(n=6, p=1, flux=sdg.ROE, split=0.0, steps=4),

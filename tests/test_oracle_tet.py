@@ -103,9 +103,7 @@ def test_adjacency_matches_the_oracle(periodic):
 
 def test_unsupported_tetrahedral_configurations_are_refused():
     mesh = cases.tet_mesh(3)
-    av = cases.config(2, sdg.HLLC)
-    av.shock_capturing, av.empirical_tolerance = sdg.ARTIFICIAL_VISCOSITY, 1.0
-    for cfg in (cases.config(4, sdg.HLLC), av):
+    for cfg in (cases.config(4, sdg.HLLC), cases.config(5, sdg.ROE)):
         with pytest.raises(sdg.SdgError) as e:
             sdg.GpuSolver(mesh, cfg, device=-1)
         assert "UNSUPPORTED" in str(e.value)
