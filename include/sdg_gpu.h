@@ -50,7 +50,7 @@ enum sdg_element_type { /* gmsh first-order type numbers (src/Solver/SimulationC
   SDG_ELEMENT_LINE = 1,     /* DimensionEnum::D1 / MeshModelEnum::Line; its faces are points */
   SDG_ELEMENT_TRIANGLE = 2,
   SDG_ELEMENT_QUADRANGLE = 3,
-  SDG_ELEMENT_TETRAHEDRON = 4, /* dense modal blocks, P = 1..3, Euler, Navier-Stokes and the artificial
+  SDG_ELEMENT_TETRAHEDRON = 4, /* dense modal blocks, P = 1..3, every equation model and the artificial
                                   viscosity; no derivatives                                             */
   SDG_ELEMENT_HEXAHEDRON = 5
 };

@@ -362,13 +362,15 @@ def inc_channel_case(p=2, flux=sdg.EXACT, viscous=None, mu=0.0, c0=10.0, n=4, dt
     return (mesh, cfg, ic, bc, dt, steps)
 
 
-def cavity_3d_case(p=2, flux=sdg.EXACT, viscous=sdg.BR1, mu=2e-3, c0=10.0, n=3, dt=2e-4, steps=3, boussinesq=False):
+def cavity_3d_case(p=2, flux=sdg.EXACT, viscous=sdg.BR1, mu=2e-3, c0=10.0, n=3, dt=2e-4, steps=3, boussinesq=False,
+                   tets=False):
     """3D cavity on hexahedra (lidcavity_3d_incns.cpp / thermalcavity_3d_incns.cpp shapes); groups
     x-, x+, y-, y+, z-, z+.  Lid: the z+ wall moves at u = 1.  Thermal: x- at T = 1, x+ at T = 0, buoyancy
     on w."""
     conds = ([sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ISOTHERMAL_NONSLIP_WALL] + [sdg.ADIABATIC_NONSLIP_WALL] * 4
              if boussinesq else [sdg.ADIABATIC_NONSLIP_WALL] * 6)
-    mesh = sdg.Mesh.box_3d(0, 0, 0, 1, 1, 1, n, n, n, periodic=False, boundary_conditions=conds)
+    mesh = (tet_mesh(n, 1.0, periodic=False, conditions=conds) if tets else
+            sdg.Mesh.box_3d(0, 0, 0, 1, 1, 1, n, n, n, periodic=False, boundary_conditions=conds))
     cfg = inc_config(p, flux, viscous, mu, c0, source=sdg.SOURCE_BOUSSINESQ if boussinesq else sdg.SOURCE_NONE,
                      beta=1.0 if boussinesq else 0.0, tref=0.5 if boussinesq else 0.0)
 

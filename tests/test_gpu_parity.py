@@ -82,6 +82,10 @@ CASES = {
         conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
                     sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL)),
     "ns-tet-box-p1-br1-hllc": lambda: cases.tet_box_case(p=1, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01),
+    "inc-euler-cavity-tet-p2-exact": lambda: cases.cavity_3d_case(p=2, viscous=None, mu=0.0, tets=True),
+    "inc-lidcavity-tet-p2-exact-br1": lambda: cases.cavity_3d_case(p=2, mu=1e-2, tets=True),
+    "inc-thermalcavity-tet-p3-lf-br2-boussinesq": lambda: cases.cavity_3d_case(
+        p=3, flux=sdg.LAX_FRIEDRICHS, viscous=sdg.BR2, mu=1e-2, boussinesq=True, c0=3.0, steps=2, tets=True),
     "av-shocktube-tet-p2-hllc": lambda: cases.shock_tube_case(p=2, dim=3, n=8, tets=True),
     "av-shocktube-tet-p3-roe": lambda: cases.shock_tube_case(p=3, flux=sdg.ROE, dim=3, n=6, steps=2, tets=True),
     "kh-hybrid-p4-lf": lambda: cases.kh_case(n=6, p=4, flux=sdg.LAX_FRIEDRICHS, steps=4),
