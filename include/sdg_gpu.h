@@ -51,7 +51,7 @@ enum sdg_element_type { /* gmsh first-order type numbers (src/Solver/SimulationC
   SDG_ELEMENT_TRIANGLE = 2,
   SDG_ELEMENT_QUADRANGLE = 3,
   SDG_ELEMENT_TETRAHEDRON = 4, /* dense modal blocks, P = 1..3, every equation model and the artificial
-                                  viscosity; no derivatives                                             */
+                                  viscosity; derivatives of the Euler equations                         */
   SDG_ELEMENT_HEXAHEDRON = 5
 };
 enum sdg_equation {                                                                    /* Enum.cpp:56-64   */

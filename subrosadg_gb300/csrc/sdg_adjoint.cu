@@ -188,7 +188,7 @@ AdjArgs baseArgs(sdg_handle* h, const DevBlock* B, const double* U) {
   a.face = A->curFace ? A->curFace : h->face;
   a.faceGrad = A->curFaceGrad ? A->curFaceGrad : h->faceGrad;
   a.conn = h->fconn; a.fgeo = h->fgeo; a.status = h->status;
-  a.nface = h->nInterior; a.n1d = h->n1d; a.epb = B ? tileKernels(h, *B).epb : 0;
+  a.nface = h->nInterior; a.n1d = h->n1d; a.perm = h->facePerm; a.epb = B ? tileKernels(h, *B).epb : 0;
   return a;
 }
 

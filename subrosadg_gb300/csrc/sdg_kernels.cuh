@@ -506,8 +506,8 @@ __device__ __forceinline__ int rightPoint(int j, int rot, int n1d) {
 
 // Right point of left point j on an interior face: the tensor rotation, or the permutation table of
 // triangular faces (n1d < 0).
-template <int DIM>
-__device__ __forceinline__ int pairedPoint(const FaceArgs& a, int j, int rot, int nfq) {
+template <int DIM, class Args>
+__device__ __forceinline__ int pairedPoint(const Args& a, int j, int rot, int nfq) {
   return (DIM == 3 && a.n1d < 0) ? a.perm[rot * nfq + j] : rightPoint<DIM>(j, rot, a.n1d);
 }
 

@@ -652,7 +652,8 @@ struct AdjArgs {
   int accumulateAll;      // stage 0 in reverse: base += c0 lamIn + c1 lamIn + c2dt VJP (stage unused)
   unsigned* status;
   int64_t ne, faceBase, nface;
-  int n1d, epb;
+  int n1d, epb;           // n1d < 0: triangular faces paired through perm
+  const int* perm;        // triangular faces: [3][nfq] right point of left point j at rotation r
   // boundary faces: ghost states [face][j][rho, u, e, p]; cotangent of each boundary point's ghost
   // primitive (rho, u, T), accumulated with weight ghostScale; NS: the tangent of the neighbour traces
   double* dother;
@@ -1141,7 +1142,7 @@ __device__ __forceinline__ void jvpFacePoint(const AdjArgs& a, const Phys& ph, i
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
   const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
-  const int jr = rightPoint<DIM>(j, rot, n1d);
+  const int jr = pairedPoint<DIM>(a, j, rot, nfq);
   const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
   D1 ul[NV], ur[NV];
 #pragma unroll
@@ -1465,7 +1466,7 @@ __global__ void __launch_bounds__(kFaceThreads) vjpFaceKernel(AdjArgs a, Phys ph
   if (f < a.nface) {
     const int j = int(t - f * nfq);
     const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
-    const int jr = rightPoint<DIM>(j, rot, n1d);
+    const int jr = pairedPoint<DIM>(a, j, rot, nfq);
     const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
     double n[DIM];
 #pragma unroll
@@ -1866,7 +1867,7 @@ __global__ void __launch_bounds__(kFaceThreads) vjpExchangeKernel(AdjArgs a) {
   if (f >= a.nface) return;
   const int j = int(t - f * nfq);
   const int sl = a.conn[f * 3 + 0], sr = a.conn[f * 3 + 1], rot = a.conn[f * 3 + 2];
-  const int jr = rightPoint<DIM>(j, rot, n1d);
+  const int jr = pairedPoint<DIM>(a, j, rot, nfq);
   const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
 #pragma unroll
   for (int v = 0; v < NV; ++v) {

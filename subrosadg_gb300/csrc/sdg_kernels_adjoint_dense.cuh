@@ -22,19 +22,19 @@
 
 namespace sdg {
 
-template <int NB, int NQ, int NFQ, int NF>
+template <int NB, int NQ, int NFQ, int NF, int DIM = 2>
 struct DenseAdjShape {
-  static constexpr int NV = 4, NFP = NF * NFQ;
+  static constexpr int NV = DIM + 2, NFP = NF * NFQ;
   static constexpr int USTRIDE = (NV * NB + 1) & ~1;
   static constexpr int FSTRIDE = NF * NV * NFQ;
   static constexpr int EPB = 8, THREADS = 256;
   // phi | dphiw | phif | phifw | mref (the forward dense tables' leading part) | phiw (volume source weights)
-  static constexpr int TABLES = NQ * NB * 3 + NFP * NB * 2 + NB * NB;
-  static constexpr int PHIW = NQ * NB * 3 + NFP * NB * 2 + NB * NB + 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
-  // tangent: u, du | tangent flux slots | tangent fluxes [2][NV][NQ] | tangent source [NQ] | tangent residual
-  static constexpr int JVP_PER = 2 * USTRIDE + FSTRIDE + 2 * NV * NQ + NQ + NV * NB;
-  // adjoint: lamR [NV][NB] | point cotangents [NV][NQ] | Navier-Stokes: point gradient cotangents [NV*2][NQ]
-  static constexpr int VJP_PER = NV * NB + NV * NQ + 2 * NV * NQ;
+  static constexpr int TABLES = NQ * NB * (1 + DIM) + NFP * NB * 2 + NB * NB;
+  static constexpr int PHIW = TABLES + DIM * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
+  // tangent: u, du | tangent flux slots | tangent fluxes [d][NV][NQ] | tangent source [NQ] | tangent residual
+  static constexpr int JVP_PER = 2 * USTRIDE + FSTRIDE + DIM * NV * NQ + NQ + NV * NB;
+  // adjoint: lamR [NV][NB] | point cotangents [NV][NQ] | Navier-Stokes: point gradient cotangents [NV*d][NQ]
+  static constexpr int VJP_PER = NV * NB + NV * NQ + DIM * NV * NQ;
   static constexpr size_t JVP_SMEM = (size_t(EPB) * JVP_PER + TABLES + NQ * NB) * 8;
   static constexpr size_t VJP_SMEM = (size_t(EPB) * VJP_PER + TABLES + NQ * NB) * 8 + 8 * 32;
   static constexpr size_t TRACE_SMEM = size_t(TABLES + NQ * NB) * 8;
@@ -48,44 +48,44 @@ struct DenseAdjShape {
 
 // Geometry of point q of element e: contravariant metric, 1/|J| at the point; the M^-1 of the element and its
 // scale (affine: M_ref^-1 and 1/|J|, bilinear: the element's own inverse and 1).
-template <int NB, int NQ, bool AFFINE>
+template <int NB, int NQ, bool AFFINE, int DIM = 2>
 __device__ __forceinline__ const double* densePointGeom(const double* geom, int64_t e, int q) {
-  constexpr int GS = AFFINE ? 5 : NQ * 5 + NB * NB;
-  return AFFINE ? geom + e * GS : geom + e * GS + q * 5;
+  constexpr int GD = DIM * DIM + 1, GS = AFFINE ? GD : NQ * GD + NB * NB;
+  return AFFINE ? geom + e * GS : geom + e * GS + q * GD;
 }
 
-template <int NB, int NQ, int NFQ, int NF>
+template <int NB, int NQ, int NFQ, int NF, int DIM = 2>
 __device__ __forceinline__ void loadDenseAdjTables(double* tab, const double* src) {
-  using S = DenseAdjShape<NB, NQ, NFQ, NF>;
+  using S = DenseAdjShape<NB, NQ, NFQ, NF, DIM>;
   for (int k = threadIdx.x; k < S::TABLES; k += blockDim.x) tab[k] = src[k];
   for (int k = threadIdx.x; k < NQ * NB; k += blockDim.x) tab[S::TABLES + k] = src[S::PHIW + k];
 }
 
 // Tangent element kernel of a dense block: dR at the stage input u in direction du (face tangents in dflux), the
 // rate tangent and / or the RK combination dout = c0 dbase + c1 du + c2dt s M^-1 dR with the traces of dout.
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool VISC, int DIM = 2>
 __global__ void __launch_bounds__(256) jvpDenseStageKernel(AdjArgs a, Phys ph) {
-  using S = DenseAdjShape<NB, NQ, NFQ, NF>;
-  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB, GS = AFFINE ? 5 : NQ * 5 + NB * NB;
+  using S = DenseAdjShape<NB, NQ, NFQ, NF, DIM>;
+  constexpr int NV = DIM + 2, NFP = S::NFP, EPB = S::EPB, GD = DIM * DIM + 1, GS = AFFINE ? GD : NQ * GD + NB * NB;
   using D1 = Dual<1>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* sU = reinterpret_cast<double*>(smem_raw);  // [EPB][USTRIDE]
   double* sD = sU + EPB * S::USTRIDE;                // [EPB][USTRIDE] tangent state (then the new tangent)
   double* sF = sD + EPB * S::USTRIDE;                // [EPB][FSTRIDE] tangent flux slots
-  double* sQ = sF + EPB * S::FSTRIDE;                // [EPB][2][NV][NQ] tangent contravariant fluxes
-  double* sS = sQ + EPB * 2 * NV * NQ;               // [EPB][NQ] tangent of the source S |J|
+  double* sQ = sF + EPB * S::FSTRIDE;                // [EPB][DIM][NV][NQ] tangent contravariant fluxes
+  double* sS = sQ + EPB * DIM * NV * NQ;             // [EPB][NQ] tangent of the source S |J|
   double* sR = sS + EPB * NQ;                        // [EPB][NV][NB] tangent residual
   double* tab = sR + EPB * NV * NB;
   const double* phi = tab;
   const double* dphiw = phi + NQ * NB;
-  const double* phif = dphiw + NQ * 2 * NB;
+  const double* phif = dphiw + NQ * DIM * NB;
   const double* phifw = phif + NFP * NB;
   const double* mref = phifw + NFP * NB;
   const double* phiw = tab + S::TABLES;
   const int tid = threadIdx.x;
   const int64_t e0 = int64_t(blockIdx.x) * EPB;
   const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
-  loadDenseAdjTables<NB, NQ, NFQ, NF>(tab, a.tables);
+  loadDenseAdjTables<NB, NQ, NFQ, NF, DIM>(tab, a.tables);
   for (int k = tid; k < ecount * S::USTRIDE; k += blockDim.x) {
     sU[k] = a.u[e0 * S::USTRIDE + k];
     sD[k] = a.du[e0 * S::USTRIDE + k];
@@ -106,32 +106,36 @@ __global__ void __launch_bounds__(256) jvpDenseStageKernel(AdjArgs a, Phys ph) {
       }
       U[v].v = s; U[v].d[0] = d;
     }
-    const double* g = densePointGeom<NB, NQ, AFFINE>(a.geom, e, q);
-    const double ja[2][2] = {{g[0], g[1]}, {g[2], g[3]}};
-    D1 gg[VISC ? NV * 2 : 1], Q[2][NV], Qv[2][NV];
+    const double* g = densePointGeom<NB, NQ, AFFINE, DIM>(a.geom, e, q);
+    double ja[DIM][DIM];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r)
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) ja[r][c] = g[r * DIM + c];
+    D1 gg[VISC ? NV * DIM : 1], Q[DIM][NV], Qv[DIM][NV];
     if constexpr (VISC) {  // the gradient at the point from the modal gradient coefficients and their tangent
 #pragma unroll
-      for (int c = 0; c < NV * 2; ++c) {
+      for (int c = 0; c < NV * DIM; ++c) {
         double x = 0.0, dx = 0.0;
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
-          x = fma(phi[q * NB + b], a.grad[(e * NV * 2 + c) * NB + b], x);
-          dx = fma(phi[q * NB + b], a.dgrad[(e * NV * 2 + c) * NB + b], dx);
+          x = fma(phi[q * NB + b], a.grad[(e * NV * DIM + c) * NB + b], x);
+          dx = fma(phi[q * NB + b], a.dgrad[(e * NV * DIM + c) * NB + b], dx);
         }
         gg[c].v = x; gg[c].d[0] = dx;
       }
     }
-    nodeFlux<2, VISC>(U, gg, ja, ph, Q, Qv);
+    nodeFlux<DIM, VISC>(U, gg, ja, ph, Q, Qv);
     const double mscale = VISC && ph.mu > 0.0 ? a.dmu / ph.mu : 0.0;
 #pragma unroll
-    for (int b = 0; b < 2; ++b)
+    for (int b = 0; b < DIM; ++b)
 #pragma unroll
-      for (int v = 0; v < NV; ++v) sQ[((le * 2 + b) * NV + v) * NQ + q] = fma(mscale, Qv[b][v].v, Q[b][v].d[0]);
+      for (int v = 0; v < NV; ++v) sQ[((le * DIM + b) * NV + v) * NQ + q] = fma(mscale, Qv[b][v].v, Q[b][v].d[0]);
     if (ph.source) {
-      State<2, D1> st;
-      makeState<2>(st, U, ph);
+      State<DIM, D1> st;
+      makeState<DIM>(st, U, ph);
       const D1 src = st.r * ph.beta * (temperatureOf(st, ph) - ph.tref);
-      sS[le * NQ + q] = src.d[0] / g[4];
+      sS[le * NQ + q] = src.d[0] / g[DIM * DIM];
     }
   }
   __syncthreads();
@@ -141,14 +145,14 @@ __global__ void __launch_bounds__(256) jvpDenseStageKernel(AdjArgs a, Phys ph) {
     for (int v = 0; v < NV; ++v) {
       double s = 0.0;
       for (int q = 0; q < NQ; ++q) {
-        s = fma(sQ[((le * 2 + 0) * NV + v) * NQ + q], dphiw[(q * 2 + 0) * NB + i], s);
-        s = fma(sQ[((le * 2 + 1) * NV + v) * NQ + q], dphiw[(q * 2 + 1) * NB + i], s);
+#pragma unroll
+        for (int b = 0; b < DIM; ++b) s = fma(sQ[((le * DIM + b) * NV + v) * NQ + q], dphiw[(q * DIM + b) * NB + i], s);
       }
       for (int fj = 0; fj < NFP; ++fj) {
         const int f = fj / NFQ, j = fj - f * NFQ;
         s = fma(-sF[le * S::FSTRIDE + (f * NV + v) * NFQ + j], phifw[fj * NB + i], s);
       }
-      if (ph.source && v == 2)
+      if (ph.source && v == DIM)
         for (int q = 0; q < NQ; ++q) s = fma(sS[le * NQ + q], phiw[q * NB + i], s);
       sR[(le * NV + v) * NB + i] = s;
     }
@@ -158,8 +162,8 @@ __global__ void __launch_bounds__(256) jvpDenseStageKernel(AdjArgs a, Phys ph) {
     const int le = idx / NB, i = idx - le * NB;
     const int64_t e = e0 + le;
     const double* g = a.geom + e * GS;
-    const double* minv = AFFINE ? mref : g + NQ * 5;
-    const double sc = AFFINE ? g[4] : 1.0;
+    const double* minv = AFFINE ? mref : g + NQ * GD;
+    const double sc = AFFINE ? g[DIM * DIM] : 1.0;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       double s = 0.0;
@@ -194,10 +198,11 @@ __global__ void __launch_bounds__(256) jvpDenseStageKernel(AdjArgs a, Phys ph) {
 
 // Adjoint of the volume and lift terms of a dense block: lamU (state layout) and lamH (the flux slots of the
 // block's faces) from lam, the cotangent of du/dt.
-template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool GEN, bool VISC>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, bool GEN, bool VISC, int DIM = 2>
 __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) {
-  using S = DenseAdjShape<NB, NQ, NFQ, NF>;
-  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB, GS = AFFINE ? 5 : NQ * 5 + NB * NB, NR = NV * 2;
+  using S = DenseAdjShape<NB, NQ, NFQ, NF, DIM>;
+  constexpr int NV = DIM + 2, NFP = S::NFP, EPB = S::EPB, GD = DIM * DIM + 1, GS = AFFINE ? GD : NQ * GD + NB * NB,
+                NR = NV * DIM;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* sL = reinterpret_cast<double*>(smem_raw);  // [EPB][NV][NB] lamR = s M^-T lam
   double* sP = sL + EPB * NV * NB;                   // [EPB][NV][NQ] point cotangents of U_q
@@ -206,21 +211,21 @@ __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) 
   double* sRed = tab + S::TABLES + NQ * NB;          // one double per warp
   const double* phi = tab;
   const double* dphiw = phi + NQ * NB;
-  const double* phifw = dphiw + NQ * 2 * NB + NFP * NB;
+  const double* phifw = dphiw + NQ * DIM * NB + NFP * NB;
   const double* mref = phifw + NFP * NB;
   const double* phiw = tab + S::TABLES;
   const int tid = threadIdx.x;
   const int64_t e0 = int64_t(blockIdx.x) * EPB;
   const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
-  loadDenseAdjTables<NB, NQ, NFQ, NF>(tab, a.tables);
+  loadDenseAdjTables<NB, NQ, NFQ, NF, DIM>(tab, a.tables);
   __syncthreads();
   double mupart = 0.0;
   for (int idx = tid; idx < ecount * NB; idx += blockDim.x) {
     const int le = idx / NB, k = idx - le * NB;
     const int64_t e = e0 + le;
     const double* g = a.geom + e * GS;
-    const double* minv = AFFINE ? mref : g + NQ * 5;
-    const double sc = AFFINE ? g[4] : 1.0;
+    const double* minv = AFFINE ? mref : g + NQ * GD;
+    const double sc = AFFINE ? g[DIM * DIM] : 1.0;
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
       double s = 0.0;
@@ -232,14 +237,14 @@ __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) 
   for (int idx = tid; idx < ecount * NQ; idx += blockDim.x) {
     const int le = idx / NQ, q = idx - le * NQ;
     const int64_t e = e0 + le;
-    double lq[2][NV];
+    double lq[DIM][NV];
 #pragma unroll
-    for (int b = 0; b < 2; ++b)
+    for (int b = 0; b < DIM; ++b)
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
         double s = 0.0;
 #pragma unroll
-        for (int i = 0; i < NB; ++i) s = fma(dphiw[(q * 2 + b) * NB + i], sL[(le * NV + v) * NB + i], s);
+        for (int i = 0; i < NB; ++i) s = fma(dphiw[(q * DIM + b) * NB + i], sL[(le * NV + v) * NB + i], s);
         lq[b][v] = s;
       }
     double U[NV];
@@ -250,8 +255,12 @@ __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) 
       for (int b = 0; b < NB; ++b) s = fma(phi[q * NB + b], a.u[e * S::USTRIDE + v * NB + b], s);
       U[v] = s;
     }
-    const double* g = densePointGeom<NB, NQ, AFFINE>(a.geom, e, q);
-    const double ja[2][2] = {{g[0], g[1]}, {g[2], g[3]}};
+    const double* g = densePointGeom<NB, NQ, AFFINE, DIM>(a.geom, e, q);
+    double ja[DIM][DIM];
+#pragma unroll
+    for (int r = 0; r < DIM; ++r)
+#pragma unroll
+      for (int c = 0; c < DIM; ++c) ja[r][c] = g[r * DIM + c];
     double lu[NV], gg[VISC ? NR : 1], lg[VISC ? NR : 1];
     if constexpr (VISC) {
 #pragma unroll
@@ -268,20 +277,25 @@ __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) 
       double lamS = 0.0;
       if (ph.source) {
 #pragma unroll
-        for (int i = 0; i < NB; ++i) lamS = fma(phiw[q * NB + i], sL[(le * NV + 2) * NB + i], lamS);
-        lamS /= g[4];
+        for (int i = 0; i < NB; ++i) lamS = fma(phiw[q * NB + i], sL[(le * NV + DIM) * NB + i], lamS);
+        lamS /= g[DIM * DIM];
       }
-      mupart += volumeReverseGeneric<2, VISC>(U, gg, ja, lq, lamS, ph, lu, lg);
+      mupart += volumeReverseGeneric<DIM, VISC>(U, gg, ja, lq, lamS, ph, lu, lg);
     } else {
-      eulerVolumeReverse<2>(U, ja, lq, ph, lu);
+      eulerVolumeReverse<DIM>(U, ja, lq, ph, lu);
       if constexpr (VISC) {
         // lamF[c][v] = cotangent of Fv_c(v): Q_b contains -sum_c ja[b][c] Fv_c
-        double lamF[2][NV];
+        double lamF[DIM][NV];
 #pragma unroll
-        for (int c = 0; c < 2; ++c)
+        for (int c = 0; c < DIM; ++c)
 #pragma unroll
-          for (int v = 0; v < NV; ++v) lamF[c][v] = -fma(ja[0][c], lq[0][v], ja[1][c] * lq[1][v]);
-        mupart += viscousReverse<2>(U, gg, lamF, ph, lu, lg);
+          for (int v = 0; v < NV; ++v) {
+            double s = ja[DIM - 1][c] * lq[DIM - 1][v];
+#pragma unroll
+            for (int b = DIM - 2; b >= 0; --b) s = fma(ja[b][c], lq[b][v], s);
+            lamF[c][v] = -s;
+          }
+        mupart += viscousReverse<DIM>(U, gg, lamF, ph, lu, lg);
       }
     }
 #pragma unroll
@@ -534,17 +548,17 @@ __global__ void __launch_bounds__(256) vjpDenseGradientGeneralKernel(AdjArgs a) 
 
 // lamU += Phi_f^T lamTr over the block's face points, then the RK combination of the stage's cotangents (the
 // tensor vjpTraceKernel's rule).
-template <int NB, int NQ, int NFQ, int NF>
+template <int NB, int NQ, int NFQ, int NF, int DIM = 2>
 __global__ void __launch_bounds__(256) vjpDenseTraceKernel(AdjArgs a) {
-  using S = DenseAdjShape<NB, NQ, NFQ, NF>;
-  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB;
+  using S = DenseAdjShape<NB, NQ, NFQ, NF, DIM>;
+  constexpr int NV = DIM + 2, NFP = S::NFP, EPB = S::EPB;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* tab = reinterpret_cast<double*>(smem_raw);
-  const double* phif = tab + NQ * NB * 3;
+  const double* phif = tab + NQ * NB * (1 + DIM);
   const int tid = threadIdx.x;
   const int64_t e0 = int64_t(blockIdx.x) * EPB;
   const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
-  loadDenseAdjTables<NB, NQ, NFQ, NF>(tab, a.tables);
+  loadDenseAdjTables<NB, NQ, NFQ, NF, DIM>(tab, a.tables);
   __syncthreads();
   for (int idx = tid; idx < ecount * NB; idx += blockDim.x) {
     const int le = idx / NB, i = idx - le * NB;
