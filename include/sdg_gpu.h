@@ -387,8 +387,8 @@ const char* sdg_batch_last_error(const sdg_batch* batch);
  * conserved variables; cotangents are mapped by the transposes of its point <-> state conversions, so the VJP
  * is the transpose of the JVP in that layout).  Supported: compressible or incompressible Euler and
  * Navier-Stokes (BR1, BR2) on every element block (lines, triangles, quadrangles -- parallelogram or bilinear
- * --, hexahedra, hybrid meshes), the Boussinesq source, any boundary faces; with artificial viscosity
- * SDG_ERR_UNSUPPORTED. */
+ * --, hexahedra, hybrid meshes), the Euler equations on tetrahedra, the Boussinesq source, any boundary
+ * faces; with artificial viscosity or Navier-Stokes on tetrahedra SDG_ERR_UNSUPPORTED. */
 /* w_q |J|_q of every volume point: integral of f = sum over points of weight * f (functionals). */
 int sdg_volume_point_weight(sdg_handle* handle, double* weight);
 /* Change the dynamic viscosity (and kappa = cp mu / Pr) of a Navier-Stokes handle. */
