@@ -51,7 +51,7 @@ enum sdg_element_type { /* gmsh first-order type numbers (src/Solver/SimulationC
   SDG_ELEMENT_TRIANGLE = 2,
   SDG_ELEMENT_QUADRANGLE = 3,
   SDG_ELEMENT_TETRAHEDRON = 4, /* dense modal blocks, P = 1..3, every equation model and the artificial
-                                  viscosity; derivatives of the Euler equations                         */
+                                  viscosity, and their derivatives (not of the artificial viscosity)    */
   SDG_ELEMENT_HEXAHEDRON = 5
 };
 enum sdg_equation {                                                                    /* Enum.cpp:56-64   */
@@ -387,8 +387,8 @@ const char* sdg_batch_last_error(const sdg_batch* batch);
  * conserved variables; cotangents are mapped by the transposes of its point <-> state conversions, so the VJP
  * is the transpose of the JVP in that layout).  Supported: compressible or incompressible Euler and
  * Navier-Stokes (BR1, BR2) on every element block (lines, triangles, quadrangles -- parallelogram or bilinear
- * --, hexahedra, hybrid meshes), the Euler equations on tetrahedra, the Boussinesq source, any boundary
- * faces; with artificial viscosity or Navier-Stokes on tetrahedra SDG_ERR_UNSUPPORTED. */
+ * --, tetrahedra, hexahedra, hybrid meshes), the Boussinesq source, any boundary faces; with artificial
+ * viscosity SDG_ERR_UNSUPPORTED. */
 /* w_q |J|_q of every volume point: integral of f = sum over points of weight * f (functionals). */
 int sdg_volume_point_weight(sdg_handle* handle, double* weight);
 /* Change the dynamic viscosity (and kappa = cp mu / Pr) of a Navier-Stokes handle. */

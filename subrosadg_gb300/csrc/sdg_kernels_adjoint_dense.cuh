@@ -39,8 +39,8 @@ struct DenseAdjShape {
   static constexpr size_t VJP_SMEM = (size_t(EPB) * VJP_PER + TABLES + NQ * NB) * 8 + 8 * 32;
   static constexpr size_t TRACE_SMEM = size_t(TABLES + NQ * NB) * 8;
   // gradient transpose (affine): lamTot and lamJmp [NV*2][NB] | phif | dmod | emod | lmod
-  static constexpr int GOPS = NFP * NB + 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
-  static constexpr size_t GRAD_SMEM = (size_t(EPB) * 2 * 2 * NV * NB + GOPS) * 8;
+  static constexpr int GOPS = NFP * NB + DIM * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
+  static constexpr size_t GRAD_SMEM = (size_t(EPB) * 2 * DIM * NV * NB + GOPS) * 8;
   // gradient transpose (general form): lamRt, lamRv [NV*2][NB] | lamRf [NF][NV*2][NB] | point values' cotangent
   // [NV][NQ] | phi | dphiw | phif | phifw | mref
   static constexpr size_t GRAD_GENERAL_SMEM = (size_t(EPB) * ((2 + NF) * 2 * NV * NB + NV * NQ) + TABLES) * 8;
@@ -353,24 +353,24 @@ __global__ void __launch_bounds__(256) vjpDenseVolumeKernel(AdjArgs a, Phys ph) 
 //   lamU -= sum_b D_b^T (sum_k ja[b][k] lamTot_k),
 //   lamO_f = E_f^T (nF_f . lamTot);  BR2: lamD_f = E_f^T (nF_f . lamJmp) + jinv L_f^T (nF_f . lamTg_f),
 //   lamUp = lamO + lamD/2 (the neighbour traces), lamTr += -lamD/2 (the own traces).
-template <int NB, int NQ, int NFQ, int NF, bool BR2>
+template <int NB, int NQ, int NFQ, int NF, bool BR2, int DIM = 2>
 __global__ void __launch_bounds__(256) vjpDenseGradientKernel(AdjArgs a) {
-  using S = DenseAdjShape<NB, NQ, NFQ, NF>;
-  constexpr int NV = 4, NFP = S::NFP, EPB = S::EPB, NR = NV * 2;
+  using S = DenseAdjShape<NB, NQ, NFQ, NF, DIM>;
+  constexpr int NV = DIM + 2, NFP = S::NFP, EPB = S::EPB, NR = NV * DIM, GD = DIM * DIM + 1;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   double* sT = reinterpret_cast<double*>(smem_raw);  // [EPB][NR][NB] lamTot
   double* sJ = sT + EPB * NR * NB;                   // [EPB][NR][NB] lamJmp (BR2)
   double* tab = sJ + EPB * NR * NB;
   const double* phif = tab;                          // [NFP][NB]
-  const double* dmod = phif + NFP * NB;              // [2][NB][NB]
-  const double* emod = dmod + 2 * NB * NB;           // [NF][NB][NFQ]
+  const double* dmod = phif + NFP * NB;              // [DIM][NB][NB]
+  const double* emod = dmod + DIM * NB * NB;         // [NF][NB][NFQ]
   const double* lmod = emod + NF * NB * NFQ;         // [NF][NFQ][NFQ]
   const int tid = threadIdx.x;
   const int64_t e0 = int64_t(blockIdx.x) * EPB;
   const int ecount = int(a.ne - e0 < EPB ? a.ne - e0 : EPB);
   {
-    constexpr int OFF_PHIF = NQ * NB * 3, OFF_DMOD = NQ * NB * 3 + NFP * NB * 2 + NB * NB;
-    constexpr int NOPS = 2 * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
+    constexpr int OFF_PHIF = NQ * NB * (1 + DIM), OFF_DMOD = NQ * NB * (1 + DIM) + NFP * NB * 2 + NB * NB;
+    constexpr int NOPS = DIM * NB * NB + NF * NB * NFQ + NF * NFQ * NFQ;
     for (int k = tid; k < NFP * NB; k += blockDim.x) tab[k] = a.tables[OFF_PHIF + k];
     for (int k = tid; k < NOPS; k += blockDim.x) tab[NFP * NB + k] = a.tables[OFF_DMOD + k];
   }
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(256) vjpDenseGradientKernel(AdjArgs a) {
     const int le = idx / (NR * NB), r = idx - le * NR * NB;
     const int c = r / NB, i = r - c * NB;
     const int64_t e = e0 + le;
-    const double jinv = a.geom[e * 5 + 4];
+    const double jinv = a.geom[e * GD + DIM * DIM];
     double vol = 0.0;
     for (int fj = 0; fj < NFP; ++fj) {
       const int f = fj / NFQ, j = fj - f * NFQ;
@@ -393,13 +393,17 @@ __global__ void __launch_bounds__(256) vjpDenseGradientKernel(AdjArgs a) {
     const int le = idx / (NV * NB), r = idx - le * NV * NB;
     const int v = r / NB, m = r - v * NB;
     const int64_t e = e0 + le;
-    const double* g = a.geom + e * 5;
+    const double* g = a.geom + e * GD;
     double acc = 0.0;
     for (int i = 0; i < NB; ++i) {
-      const double t0 = sT[(le * NR + v * 2 + 0) * NB + i], t1 = sT[(le * NR + v * 2 + 1) * NB + i];
-      const double d0 = fma(g[0], t0, g[1] * t1), d1 = fma(g[2], t0, g[3] * t1);  // sum_k ja[b][k] lamTot_k
-      acc = fma(dmod[i * NB + m], d0, acc);
-      acc = fma(dmod[(NB + i) * NB + m], d1, acc);
+      const double* t = sT + (le * NR + v * DIM) * NB + i;  // lamTot_k at stride NB
+#pragma unroll
+      for (int b = 0; b < DIM; ++b) {  // d_b = sum_k ja[b][k] lamTot_k
+        double d = g[b * DIM + DIM - 1] * t[(DIM - 1) * NB];
+#pragma unroll
+        for (int kk = DIM - 2; kk >= 0; --kk) d = fma(g[b * DIM + kk], t[kk * NB], d);
+        acc = fma(dmod[(b * NB + i) * NB + m], d, acc);
+      }
     }
     a.lamU[e * S::USTRIDE + v * NB + m] -= acc;
   }
@@ -408,14 +412,20 @@ __global__ void __launch_bounds__(256) vjpDenseGradientKernel(AdjArgs a) {
     const int fj = r / NV, v = r - fj * NV;
     const int f = fj / NFQ, j = fj - f * NFQ;
     const int64_t e = e0 + le;
-    const double jinv = a.geom[e * 5 + 4];
-    const double n0 = a.fmetric[(e * NF + f) * 2 + 0], n1 = a.fmetric[(e * NF + f) * 2 + 1];
+    const double jinv = a.geom[e * GD + DIM * DIM];
+    const double* nf = a.fmetric + (e * NF + f) * DIM;
+    // n . x for components x_k at stride `st`
+    const auto ndot = [&](const double* x, int st) {
+      double r = nf[DIM - 1] * x[(DIM - 1) * st];
+#pragma unroll
+      for (int kk = DIM - 2; kk >= 0; --kk) r = fma(nf[kk], x[kk * st], r);
+      return r;
+    };
     double lo = 0.0, ld = 0.0;
     for (int i = 0; i < NB; ++i) {
       const double E = emod[(f * NB + i) * NFQ + j];
-      lo = fma(E, fma(n0, sT[(le * NR + v * 2 + 0) * NB + i], n1 * sT[(le * NR + v * 2 + 1) * NB + i]), lo);
-      if constexpr (BR2)
-        ld = fma(E, fma(n0, sJ[(le * NR + v * 2 + 0) * NB + i], n1 * sJ[(le * NR + v * 2 + 1) * NB + i]), ld);
+      lo = fma(E, ndot(sT + (le * NR + v * DIM) * NB + i, NB), lo);
+      if constexpr (BR2) ld = fma(E, ndot(sJ + (le * NR + v * DIM) * NB + i, NB), ld);
     }
     const int64_t slot = (a.faceBase + e * NF + f);
     if constexpr (BR2) {
@@ -423,7 +433,7 @@ __global__ void __launch_bounds__(256) vjpDenseGradientKernel(AdjArgs a) {
       double lift = 0.0;
 #pragma unroll
       for (int jj = 0; jj < NFQ; ++jj)
-        lift = fma(lmod[(f * NFQ + jj) * NFQ + j], fma(n0, tg[(v * 2 + 0) * NFQ + jj], n1 * tg[(v * 2 + 1) * NFQ + jj]), lift);
+        lift = fma(lmod[(f * NFQ + jj) * NFQ + j], ndot(tg + v * DIM * NFQ + jj, NFQ), lift);
       ld = fma(jinv, lift, ld);
       a.lamTr[slot * NV * NFQ + v * NFQ + j] += -0.5 * ld;
     }

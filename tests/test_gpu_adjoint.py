@@ -31,6 +31,8 @@ CASES = {
     "euler-tet-p2-hllc": lambda: cases.tet_tgv_case(n=3, p=2, flux=sdg.HLLC),
     "euler-tet-p3-roe": lambda: cases.tet_tgv_case(n=3, p=3, flux=sdg.ROE),
     "euler-tet-box-farfield-p2-roe": lambda: cases.tet_box_case(p=2, flux=sdg.ROE),
+    "ns-tet-p2-br1-roe": lambda: cases.tet_tgv_case(n=3, p=2, flux=sdg.ROE, viscous=sdg.BR1, mu=0.02),
+    "ns-tet-p2-br2-hllc": lambda: cases.tet_tgv_case(n=3, p=2, flux=sdg.HLLC, viscous=sdg.BR2, mu=0.02),
     "euler-hex-p3-central": lambda: cases.tgv_case(n=3, p=3, flux=sdg.CENTRAL),
     "ns-hex-p3-br1-roe": lambda: cases.tgv_case(n=3, p=3, flux=sdg.ROE, viscous=sdg.BR1, mu=0.02),
     "ns-quad-p4-br1-hllc": lambda: cases.vortex_case(n=3, p=4, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.05),
@@ -253,7 +255,7 @@ def test_vjp_is_the_transpose_of_jvp(name):
         assert rel(dmu, (rp - rm) / (2 * hm)) < 1e-6
 
 
-@pytest.mark.parametrize("name", ["euler-quad-p3-roe", "euler-hex-p2-hllc", "euler-tet-p2-hllc", "ns-hex-p3-br1-roe",
+@pytest.mark.parametrize("name", ["euler-quad-p3-roe", "euler-hex-p2-hllc", "euler-tet-p2-hllc", "ns-tet-p2-br2-hllc", "ns-hex-p3-br1-roe",
                                   "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-ns-thermalcavity-hex-p2-exact-br1-boussinesq",
                                   "ns-line-p4-br1-roe", "euler-hybrid-p3-lf-bilinear", "euler-tri-p5-roe",
                                   "ns-hybrid-p3-br1-lf", "ns-tri-p3-br2-hllc", "ns-hybrid-jitter-p4-br2-lf",
