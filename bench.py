@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--elements", type=int, default=64, help="hexahedra per direction")
     ap.add_argument("--order", type=int, default=3)
-    ap.add_argument("--cpu-sample", type=int, default=32, help="hexahedra per direction of the CPU sample")
+    ap.add_argument("--cpu-sample", type=int, default=64, help="hexahedra per direction of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="headline workload only")
@@ -160,43 +160,67 @@ class ClockSampler:
 
 def tgv_problem(n, p):
     import subrosadg_gb300 as sdg
-    from tests import cases
+    from subrosadg_gb300 import workloads as wl
     mesh = sdg.Mesh.box_3d(0, 0, 0, 2 * math.pi, 2 * math.pi, 2 * math.pi, n, n, n, periodic=True)
-    cfg = cases.config(p, sdg.HLLC)
-    return mesh, cfg, lambda pts: cases.tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2])
+    cfg = wl.config(p, sdg.HLLC)
+    return mesh, cfg, lambda pts: wl.tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2])
 
 
-def cpu_baseline(n, p, steps, warmup):
-    """Time the oracle (reference-faithful arithmetic: gradient pass for Euler and dense per-element
-    M^-1 as the reference) on the host cores, on an n^3 sample of the TGV workload."""
-    from oracle import orc
-    mesh, cfg, prim = tgv_problem(n, p)
+VARIANTS = {"faithful": "the reference's arithmetic: the gradient pass also for Euler (TimeIntegration.cpp:340-343) "
+                        "and a dense M^-1 per element (Geometry.cpp:88-100)",
+            "lean": "without the unused Euler gradient pass, one shared reference M^-1 scaled by 1/|J| on the "
+                    "affine hexahedra"}
+
+
+def cpu_baseline(n, p, stages, warmup, variant="faithful"):
+    """Time the oracle -- the CPU restatement of the reference path -- on all host cores, on the TGV workload
+    with n^3 hexahedra: `warmup` untimed RK stages, then `stages` timed ones (SSP-RK3 stages in order, one
+    stage = one update of every DOF).  The mesh comes from the oracle's own generator: nothing of the GPU
+    library is loaded."""
+    from oracle import meshgen, orc
+    from subrosadg_gb300 import _abi
+    from subrosadg_gb300 import workloads as wl
+    mesh = meshgen.box_3d(0, 0, 0, 2 * math.pi, 2 * math.pi, 2 * math.pi, n, n, n, periodic=True)
+    cfg = wl.config(p, _abi.HLLC)
     threads = os.cpu_count() or 1
     orc.set_threads(threads)
-    o = orc.Oracle(mesh, cfg, faithful=True, precision="double")
-    o.initialize_primitive(prim(o.volume_points()))
-    dt = o.delta_time(0.2)
-    o.step(dt, warmup)
     t0 = time.perf_counter()
-    o.step(dt, steps)
+    o = orc.Oracle(mesh, cfg, faithful=True, lean=variant == "lean", precision="double")
+    o.initialize_primitive(wl.tgv_primitive(*o.volume_points().T))
+    dt = o.delta_time(0.2)
+    setup = time.perf_counter() - t0
+    for s in range(warmup):
+        o.stage(s % 3, dt)
+    t0 = time.perf_counter()
+    for s in range(warmup, warmup + stages):
+        o.stage(s % 3, dt)
     t = time.perf_counter() - t0
     dof = o.dof
-    return {"value": dof * 3 * steps / t, "unit": "DOF-stage/s", "cores": threads, "kind": "port",
-            "sample": f"TGV {n}^3 hexahedra P{p} HLLC ({dof} DOF), {steps} SSP-RK3 steps after {warmup} warm-up, "
-                      f"oracle with the reference's gradient pass and dense M^-1, OpenMP {threads} threads",
-            "seconds": t}
+    return {"value": dof * stages / t, "unit": "DOF-stage/s", "cores": threads, "kind": "port",
+            "sample": f"TGV {n}^3 hexahedra P{p} HLLC ({dof} DOF{', the full workload' if n == 64 else ''}), "
+                      f"{stages} SSP-RK3 stages "
+                      f"after {warmup} warm-up stages; oracle ({variant}: {VARIANTS[variant]}), OpenMP {threads} "
+                      f"threads", "seconds": t, "setup_s": setup, "variant": variant}
 
 
 def run_reference(args):
+    """The reference arm: the oracle (CPU restatement of the reference path; the reference itself does not
+    build here) on the host cores.  One step of this arm is one SSP-RK3 stage of the full 64^3 workload (a
+    bounded sample: a whole step takes three), so the line's value is DOF-stage/s of that workload."""
     world, rank, local = dist_env()
     if rank != 0:
         return
-    r = cpu_baseline(args.cpu_sample, args.order, args.steps, args.warmup)
+    r = cpu_baseline(args.elements, args.order, args.steps, args.warmup, "faithful")
+    lean = cpu_baseline(args.elements, args.order, max(1, min(args.steps, 3)), 1, "lean")
     line = {"impl": "reference", "metric": METRIC, "value": r["value"], "unit": "DOF-stage/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": r["sample"]},
+            "config": {"workload": WORKLOAD, "elements": args.elements ** 3,
+                       "step": "one SSP-RK3 stage of the full workload (a step of the GPU arm is three)",
+                       "sample": r["sample"]},
             "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "lean": {k: lean[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "setup_s": r["setup_s"],
             "e2e": {"value": r["value"], "unit": "DOF-stage/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -214,9 +238,9 @@ def _timed(torch, stream, fn, steps):
 def bench_batched(args, device, torch, max_elements=None):
     """Batched workload: all instances in one batched graph step versus one instance after another."""
     import subrosadg_gb300 as sdg
-    from tests import cases
+    from subrosadg_gb300 import workloads as wl
     t0 = time.perf_counter()
-    inst, params = cases.batch_instances(args.batch_count, max_elements=max_elements or args.batch_max_elements)
+    inst, params = wl.batch_instances(args.batch_count, max_elements=max_elements or args.batch_max_elements)
     solvers = []
     for mesh, cfg, prim in inst:
         g = sdg.GpuSolver(mesh, cfg, device=device)
@@ -264,12 +288,12 @@ def bench_batched(args, device, torch, max_elements=None):
 def bench_ns_hybrid(args, device, torch):
     """2D Navier-Stokes BR2 Kelvin-Helmholtz, Re 1e4, Pr 0.71, hybrid 256^2 mesh, P4, LF."""
     import subrosadg_gb300 as sdg
-    from tests import cases
+    from subrosadg_gb300 import workloads as wl
     n = args.ns_elements
     mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=True, jitter=0.1, split_fraction=0.5, seed=11)
-    cfg = cases.ns_config(4, sdg.LAX_FRIEDRICHS, sdg.BR2, 1e-4)
+    cfg = wl.ns_config(4, sdg.LAX_FRIEDRICHS, sdg.BR2, 1e-4)
     g = sdg.GpuSolver(mesh, cfg, device=device)
-    g.initialize_primitive(cases.kh_primitive(*g.volume_points()[:, :2].T))
+    g.initialize_primitive(wl.kh_primitive(*g.volume_points()[:, :2].T))
     dt = g.calculateDeltaTime(0.2)
     g.autotune()
     import ctypes
@@ -295,9 +319,9 @@ def bench_tet(args, device, torch):
     import ctypes
 
     import subrosadg_gb300 as sdg
-    from tests import cases
+    from subrosadg_gb300 import workloads as wl
     n = args.tet_elements
-    mesh, cfg, prim, _, _, _ = cases.tet_tgv_case(n=n, p=3, flux=sdg.HLLC)
+    mesh, cfg, prim, _, _, _ = wl.tet_tgv_case(n=n, p=3, flux=sdg.HLLC)
     g = sdg.GpuSolver(mesh, cfg, device=device)
     g.initialize_primitive(prim(g.volume_points()))
     dt = g.calculateDeltaTime(0.2)
@@ -324,8 +348,8 @@ def bench_vortex(args, device, torch):
     import ctypes
 
     import subrosadg_gb300 as sdg
-    from tests import cases
-    mesh, cfg, prim, _, _, _ = cases.vortex_case(n=40, p=3, flux=sdg.ROE)
+    from subrosadg_gb300 import workloads as wl
+    mesh, cfg, prim, _, _, _ = wl.vortex_case(n=40, p=3, flux=sdg.ROE)
     g = sdg.GpuSolver(mesh, cfg, device=device)
     g.initialize_primitive(prim(g.volume_points()))
     sp = ctypes.c_void_p()
@@ -348,9 +372,9 @@ def bench_vortex(args, device, torch):
 def bench_adjoint(args, device, torch):
     """cfg5: gradient of the integrated kinetic energy at the final time w.r.t. U0 and mu."""
     import subrosadg_gb300 as sdg
-    from tests import cases
+    from subrosadg_gb300 import workloads as wl
     n, steps, K = args.adjoint_elements, args.adjoint_steps, 25
-    mesh, cfg, prim, _, _, _ = cases.tgv_case(n=n, p=3, flux=sdg.ROE, viscous=sdg.BR1, mu=1.0 / 1600.0)
+    mesh, cfg, prim, _, _, _ = wl.tgv_case(n=n, p=3, flux=sdg.ROE, viscous=sdg.BR1, mu=1.0 / 1600.0)
     s = sdg.GpuSolver(mesh, cfg, device=device)
     s.initialize_primitive(prim(s.volume_points()))
     s.autotune()
@@ -518,8 +542,11 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(args.cpu_sample, args.order, 4, 1)
-        cpu.pop("seconds", None)
+        # bounded samples of the same 64^3 workload on the host cores, both variants
+        faithful = cpu_baseline(args.cpu_sample, args.order, 2, 1, "faithful")
+        lean = cpu_baseline(args.cpu_sample, args.order, 3, 1, "lean")
+        cpu = {k: faithful[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cpu["lean"] = {k: lean[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
     if rank != 0:
         return

@@ -199,7 +199,9 @@ int sdg_set_state_point(sdg_handle* handle, const double* conserved);
 int sdg_get_state_point(sdg_handle* handle, double* conserved);
 /* State exchange as modal coefficients in the reference's per-element layout
  * (variable_basis_function_coefficient_: column-major (d+2) x Nb, SolveControl.cpp:45-60),
- * concatenated per block; basis = the hierarchic Lobatto basis documented in the design doc. */
+ * concatenated per block.  Basis: the hierarchic Lobatto basis (integrated Legendre polynomials,
+ * l0 = (1-x)/2, l1 = (1+x)/2, l_k = (P_k - P_{k-2}) / sqrt(2(2k-1)) for k >= 2), tensor products of it on
+ * quadrangles and hexahedra (gmsh's H1Legendre family, src/Mesh/BasisFunction.cpp:46-74). */
 int sdg_set_state_modal(sdg_handle* handle, const double* coefficient);
 int sdg_get_state_modal(sdg_handle* handle, double* coefficient);
 
@@ -243,6 +245,11 @@ int sdg_kernel_time(sdg_handle* handle, double* milliseconds, int64_t* launches)
 /* Diagnostic: sustained FP64 FMA rate of the device, in GFLOP/s (2 flops per FMA), from an
  * independent-chain FMA kernel run for about `milliseconds` ms.  Used as the FP64 roofline. */
 int sdg_measure_fp64_peak(int32_t device, double milliseconds, double* gflops);
+/* Diagnostic: FP64 tensor-core (DMMA) rate of the device, in GFLOP/s (2 M N K flops per mma), from a
+ * kernel of independent mma.sync .f64 chains of one shape run for about `milliseconds` ms.
+ * shape 0: m8n8k4, 1: m16n8k4, 2: m16n8k8, 3: m16n8k16.  Compared with sdg_measure_fp64_peak it decides
+ * whether the basis contractions gain anything from the tensor cores. */
+int sdg_measure_dmma_peak(int32_t device, int32_t shape, double milliseconds, double* gflops);
 
 /* Diagnostic: adjacency as canonical integer tuples, for bit-exact parity checks.
  * interior: [interior_face_count][7] = (typeL, elemL, faceL, typeR, elemR, faceR, rotation)

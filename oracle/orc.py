@@ -41,6 +41,7 @@ def load(precision="double"):
         lib.orc_counts.argtypes = [c_void_p, POINTER(c_int64)]
         lib.orc_calculate_delta_time.argtypes = [c_void_p, c_double, _pd]
         lib.orc_step.argtypes = [c_void_p, c_int, c_double]
+        lib.orc_stage.argtypes = [c_void_p, c_int, c_double]
         lib.orc_adjacency.argtypes = [c_void_p, _pi, _pi]
         lib.orc_set_threads.argtypes = [c_int]
         lib.orc_max_threads.restype = c_int
@@ -53,16 +54,18 @@ class Oracle:
     """CPU restatement of the reference solver on the same mesh/config structs as sdg_create.
 
     faithful=True : the reference's arithmetic -- gradient pass also for Euler, plain explicit inverses
-                    (the timed CPU baseline);
+                    (the reference-faithful timed CPU baseline);
     faithful=False: the checker -- no unused gradient pass, solves refined by one correction step.
+    lean=True     : the lean timed CPU baseline -- no unused Euler gradient pass, plain inverses, one shared
+                    reference inverse scaled by 1/|J| on blocks of affine elements (overrides faithful).
     precision     : "double" (the reference's Real) or "extended" (long double truth).
     """
 
-    def __init__(self, mesh, config, faithful=True, precision="double"):
+    def __init__(self, mesh, config, faithful=True, precision="double", lean=False):
         self.lib = load(precision)
         self._m = mesh.struct()
         self._c = config
-        flags = 3 if faithful else 0
+        flags = 6 if lean else (3 if faithful else 0)
         self.h = self.lib.orc_create(ctypes.addressof(self._m), ctypes.addressof(self._c), flags)
         if not self.h:
             raise RuntimeError("oracle: " + self.lib.orc_last_error().decode())
@@ -123,6 +126,10 @@ class Oracle:
 
     def step(self, dt, n=1):
         self.lib.orc_step(self.h, n, dt)
+
+    def stage(self, stage, dt):
+        """One RK stage (stage 0 also saves U^n as the step's base state, as a step does first)."""
+        self.lib.orc_stage(self.h, stage, dt)
 
     def relative_error(self):
         out = np.zeros(self.nv)

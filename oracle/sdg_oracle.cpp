@@ -46,6 +46,10 @@ struct Block {
   std::vector<Real> jw;       // ne * nq        |J| w
   std::vector<Real> jtiw;     // ne * nq * d*d  J^-T |J| w, column-major d x d per point
   std::vector<Real> minv;     // ne * nb*nb     local mass matrix inverse
+  // shared-inverse (lean) mode on a block of affine elements: M_e^-1 = M_ref^-1 / |J|_e
+  bool sharedInverse = false;
+  std::vector<Real> minvRef;  // nb*nb         inverse of the reference mass matrix sum_q phi_a phi_b w_q
+  std::vector<Real> detJ;     // ne            constant Jacobian determinant of each element
   std::vector<Real> mass;     // ne * nb*nb     local mass matrix (kept when refining solves)
   std::vector<Real> minEdge;  // ne
   std::vector<Real> innerRadius;  // ne (artificial viscosity length scale)
@@ -76,6 +80,9 @@ struct Problem {
   // condition-number round-off of the hierarchic basis at high order so the checker stays accurate to
   // ~1e-15.  Off for the timed CPU baseline, which mirrors the reference's arithmetic exactly.
   bool refine = true;
+  // Lean CPU-baseline mode: a block whose elements are all affine multiplies by one shared reference inverse
+  // scaled by 1/|J| (M = |J| M_ref exactly for a constant Jacobian) instead of reading a dense inverse per element.
+  bool lean = false;
   Physics ph;
   std::vector<Block> blocks;
   std::vector<Face> interior, boundary;
@@ -156,8 +163,8 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
   B.qcoord.assign(size_t(B.ne) * nq * 3, 0.0);
   B.jw.assign(size_t(B.ne) * nq, 0.0);
   B.jtiw.assign(size_t(B.ne) * nq * d * d, 0.0);
-  B.minv.assign(size_t(B.ne) * nb * nb, 0.0);
-  if (P.refine) B.mass.assign(size_t(B.ne) * nb * nb, 0.0);
+  B.detJ.assign(size_t(B.ne), 0.0);
+  std::vector<char> affine(size_t(B.ne), 1);
   B.minEdge.assign(size_t(B.ne), 0.0);
   B.innerRadius.assign(size_t(B.ne), 0.0);
   std::string failure;
@@ -202,20 +209,12 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
       }
       const Real jw = det * R.vq.w[q];
       B.jw[size_t(e) * nq + q] = jw;
+      if (q == 0) B.detJ[e] = det;
+      else if (std::fabs(det - B.detJ[e]) > 1e-13 * std::fabs(B.detJ[e])) affine[e] = 0;
       // M(a,b) = (J^-T)(a,b) |J| w = (J^-1)(b,a) |J| w, stored column-major at [a + b*d].
       for (int a = 0; a < d; ++a)
         for (int b = 0; b < d; ++b) B.jtiw[(size_t(e) * nq + q) * d * d + a + b * d] = inv[b][a] * jw;
     }
-    // Local mass matrix inverse (Geometry.cpp:88-100).
-    std::vector<Real> m(size_t(nb) * nb, 0.0);
-    for (int a = 0; a < nb; ++a)
-      for (int b = 0; b < nb; ++b) {
-        Real s = 0;
-        for (int q = 0; q < nq; ++q) s += R.phi[size_t(q) * nb + a] * R.phi[size_t(q) * nb + b] * B.jw[size_t(e) * nq + q];
-        m[size_t(a) * nb + b] = s;
-      }
-    invert(nb, m.data(), &B.minv[size_t(e) * nb * nb]);
-    if (P.refine) std::copy(m.begin(), m.end(), &B.mass[size_t(e) * nb * nb]);
     // minEdge quality: shortest straight edge between vertices.
     static const int lineE[1][2] = {{0, 1}};
     static const int triE[3][2] = {{0, 1}, {1, 2}, {2, 0}};
@@ -237,6 +236,34 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
     B.innerRadius[e] = innerRadiusOf(B.type, nodes, vv);
   }
   if (!failure.empty()) throw std::runtime_error(failure);
+  B.sharedInverse = P.lean && !P.refine && std::all_of(affine.begin(), affine.end(), [](char a) { return a != 0; });
+  if (B.sharedInverse) {
+    std::vector<Real> m(size_t(nb) * nb, 0.0);
+    for (int a = 0; a < nb; ++a)
+      for (int b = 0; b < nb; ++b) {
+        Real s = 0;
+        for (int q = 0; q < nq; ++q) s += R.phi[size_t(q) * nb + a] * R.phi[size_t(q) * nb + b] * R.vq.w[q];
+        m[size_t(a) * nb + b] = s;
+      }
+    B.minvRef.assign(size_t(nb) * nb, 0.0);
+    invert(nb, m.data(), B.minvRef.data());
+    return;
+  }
+  B.minv.assign(size_t(B.ne) * nb * nb, 0.0);
+  if (P.refine) B.mass.assign(size_t(B.ne) * nb * nb, 0.0);
+#pragma omp parallel for schedule(static)
+  for (int64_t e = 0; e < B.ne; ++e) {
+    // Local mass matrix inverse (Geometry.cpp:88-100).
+    std::vector<Real> m(size_t(nb) * nb, 0.0);
+    for (int a = 0; a < nb; ++a)
+      for (int b = 0; b < nb; ++b) {
+        Real s = 0;
+        for (int q = 0; q < nq; ++q) s += R.phi[size_t(q) * nb + a] * R.phi[size_t(q) * nb + b] * B.jw[size_t(e) * nq + q];
+        m[size_t(a) * nb + b] = s;
+      }
+    invert(nb, m.data(), &B.minv[size_t(e) * nb * nb]);
+    if (P.refine) std::copy(m.begin(), m.end(), &B.mass[size_t(e) * nb * nb]);
+  }
 }
 
 static void faceGeometry(Problem& P, Face& F, const double* nodes) {
@@ -403,8 +430,14 @@ static void gradientTrace(const Problem& P, int b, int e, int f, Real* out /* nf
 // x += (R - x M) M^-1.
 static void applyMinv(const Problem& P, const Block& B, int64_t e, int nr, const Real* R, Real* x) {
   const int nb = B.ref.nb;
-  const Real* Mi = &B.minv[size_t(e) * nb * nb];
   for (int i = 0; i < nr * nb; ++i) x[i] = 0;
+  if (B.sharedInverse) {  // lean mode, affine block: M^-1 = M_ref^-1 / |J|
+    gemmAcc(nr, nb, nb, R, B.minvRef.data(), x, 1);
+    const Real s = 1.0 / B.detJ[e];
+    for (int i = 0; i < nr * nb; ++i) x[i] *= s;
+    return;
+  }
+  const Real* Mi = &B.minv[size_t(e) * nb * nb];
   gemmAcc(nr, nb, nb, R, Mi, x, 1);
   if (!P.refine) return;
   const Real* M = &B.mass[size_t(e) * nb * nb];
@@ -787,15 +820,21 @@ static void relativeError(Problem& P) {
   for (int v = 0; v < nv; ++v) P.relErr[v] = acc[v] / Real(P.totalElements);
 }
 
-static void step(Problem& P, Real dt) {
-  for (Block& B : P.blocks) B.last = B.coef;  // TimeIntegration.cpp:70-102
-  if (P.av) artificialViscosity(P);            // once per step, TimeIntegration.cpp:336-338
-  const int nstage = P.rk + 1;
-  for (int s = 0; s < nstage; ++s) {
-    if (P.gradientPass()) gradientQuadratureAndResidual(P);
-    quadratureAndResidual(P);
-    update(P, s, dt);
+// One RK stage s of Solver::stepSolver (TimeIntegration.cpp:339-347); stage 0 first saves U^n
+// (TimeIntegration.cpp:70-102) and evaluates the once-per-step artificial viscosity (:336-338).
+static void stage(Problem& P, int s, Real dt) {
+  if (s == 0) {
+    for (Block& B : P.blocks) B.last = B.coef;
+    if (P.av) artificialViscosity(P);
   }
+  if (P.gradientPass()) gradientQuadratureAndResidual(P);
+  quadratureAndResidual(P);
+  update(P, s, dt);
+}
+
+static void step(Problem& P, Real dt) {
+  const int nstage = P.rk + 1;
+  for (int s = 0; s < nstage; ++s) stage(P, s, dt);
   relativeError(P);
 }
 
@@ -844,6 +883,7 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
   auto P = std::make_unique<Problem>();
   const int faithful = flags & 1;
   P->refine = (flags & 2) == 0;
+  P->lean = (flags & 4) != 0;
   P->dim = m->dimension; P->nv = P->dim + 2; P->p = c->polynomial_order;
   P->eq = c->equation; P->flux = c->convective_flux; P->visc = c->viscous_flux; P->rk = c->time_integration;
   P->faithful = faithful != 0;
@@ -925,8 +965,10 @@ static thread_local std::string g_orc_error;
 const char* orc_last_error() { return g_orc_error.c_str(); }
 
 // flags: bit 0 = run the gradient pass also for Euler (as the reference does); bit 1 = multiply by the
-// plain explicit inverses (no refinement), i.e. the reference's arithmetic.  The timed CPU baseline uses 3,
-// the parity checker 0.
+// plain explicit inverses (no refinement), i.e. the reference's arithmetic; bit 2 (with bit 1) = lean: blocks
+// of affine elements use one shared reference inverse scaled by 1/|J| instead of a dense inverse per element.
+// The timed CPU baselines use 3 (reference-faithful) and 6 (lean: no Euler gradient pass, shared inverse);
+// the parity checker uses 0.
 void* orc_create(const sdg_mesh* mesh, const sdg_config* config, int flags) {
   try {
     return orc::create(mesh, config, flags);
@@ -1054,6 +1096,15 @@ int orc_calculate_delta_time(void* h, double cfl, double* dt) {
 int orc_step(void* h, int n, double dt) {
   orc::Problem& P = *static_cast<orc::Problem*>(h);
   for (int i = 0; i < n; ++i) orc::step(P, orc::Real(dt));
+  return 0;
+}
+
+// One RK stage (0 .. stages-1) of a step; the last stage also evaluates the step's relative error.
+int orc_stage(void* h, int s, double dt) {
+  orc::Problem& P = *static_cast<orc::Problem*>(h);
+  if (s < 0 || s > P.rk) return 1;
+  orc::stage(P, s, orc::Real(dt));
+  if (s == P.rk) orc::relativeError(P);
   return 0;
 }
 

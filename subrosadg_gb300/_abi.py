@@ -154,6 +154,7 @@ SIGNATURES = {
     "sdg_set_kernel_timing": (c_int32, [c_void_p, c_int32]),
     "sdg_kernel_time": (c_int32, [c_void_p, _p_double, POINTER(c_int64)]),
     "sdg_measure_fp64_peak": (c_int32, [c_int32, c_double, _p_double]),
+    "sdg_measure_dmma_peak": (c_int32, [c_int32, c_int32, c_double, _p_double]),
     "sdg_delta_time_noalloc": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_int32, c_int32, c_double, c_double,
                                          c_void_p, c_void_p]),
     "sdg_mesh_generate_2d": (c_int32, [c_double, c_double, c_double, c_double, c_int32, c_int32, c_double,

@@ -39,6 +39,48 @@ __global__ void fp64ProbeKernel(double* out, int iters, double a, double b) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// FP64 tensor-core (DMMA) issue probe: every warp runs CHAINS independent accumulator chains of
+// mma.sync .f64 of one shape (bounded loop, no waits, registers only).  SHAPE 0: m8n8k4 (sm_80 form),
+// 1: m16n8k4, 2: m16n8k8, 3: m16n8k16 (the sm_90+ forms).  The operands are tiny so nothing overflows.
+template <int SHAPE>
+__global__ void dmmaProbeKernel(double* out, int iters) {
+  constexpr int CHAINS = 4;
+  const double a = 1e-9 * double(threadIdx.x & 31), b = 1e-9;
+  double acc[CHAINS][4];
+#pragma unroll
+  for (int c = 0; c < CHAINS; ++c)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc[c][r] = 0.0;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < CHAINS; ++c) {
+      if constexpr (SHAPE == 0) {
+        asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                     : "+d"(acc[c][0]), "+d"(acc[c][1]) : "d"(a), "d"(b));
+      } else if constexpr (SHAPE == 1) {
+        asm volatile("mma.sync.aligned.m16n8k4.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5}, {%6}, {%0,%1,%2,%3};"
+                     : "+d"(acc[c][0]), "+d"(acc[c][1]), "+d"(acc[c][2]), "+d"(acc[c][3]) : "d"(a), "d"(a), "d"(b));
+      } else if constexpr (SHAPE == 2) {
+        asm volatile("mma.sync.aligned.m16n8k8.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                     "{%0,%1,%2,%3};"
+                     : "+d"(acc[c][0]), "+d"(acc[c][1]), "+d"(acc[c][2]), "+d"(acc[c][3])
+                     : "d"(a), "d"(a), "d"(a), "d"(a), "d"(b), "d"(b));
+      } else {
+        asm volatile("mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, "
+                     "{%4,%5,%6,%7,%8,%9,%10,%11}, {%12,%13,%14,%15}, {%0,%1,%2,%3};"
+                     : "+d"(acc[c][0]), "+d"(acc[c][1]), "+d"(acc[c][2]), "+d"(acc[c][3])
+                     : "d"(a), "d"(a), "d"(a), "d"(a), "d"(a), "d"(a), "d"(a), "d"(a), "d"(b), "d"(b), "d"(b), "d"(b));
+      }
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int c = 0; c < CHAINS; ++c)
+#pragma unroll
+    for (int r = 0; r < 4; ++r) s += acc[c][r];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 void facePointInParent(int type, int f, const double* fx, double* X) {
   const int nfv = typeFaceVertices(type);
   const int* fl = faceVertexList(type);
@@ -766,22 +808,22 @@ void stateToPoints(sdg_handle* h, int which) {
   }
 }
 
-double measureFp64Peak(int device, double ms) {
+// Times launch(iters) on the legacy stream, doubling iters until one launch takes at least ms/2, and
+// returns flopPerIter(threads * blocks) * iters / time in GFLOP/s.
+template <class Launch>
+double timeProbe(int device, double ms, double flopsPerIteration, Launch launch) {
   SDG_CUDA(cudaSetDevice(device));
-  cudaDeviceProp prop;
-  SDG_CUDA(cudaGetDeviceProperties(&prop, device));
-  const int threads = 256, blocks = prop.multiProcessorCount * 8;
-  double* out = devAlloc<double>(size_t(threads) * blocks);
   cudaEvent_t e0, e1;
   SDG_CUDA(cudaEventCreate(&e0));
   SDG_CUDA(cudaEventCreate(&e1));
   int iters = 256;
   float t = 0.f;
-  fp64ProbeKernel<<<blocks, threads>>>(out, 16, 1.0000001, 1e-9);
+  launch(16);
+  SDG_CUDA(cudaGetLastError());
   SDG_CUDA(cudaDeviceSynchronize());
   for (int round = 0; round < 12; ++round) {
     SDG_CUDA(cudaEventRecord(e0));
-    fp64ProbeKernel<<<blocks, threads>>>(out, iters, 1.0000001, 1e-9);
+    launch(iters);
     SDG_CUDA(cudaEventRecord(e1));
     SDG_CUDA(cudaEventSynchronize(e1));
     SDG_CUDA(cudaEventElapsedTime(&t, e0, e1));
@@ -790,8 +832,41 @@ double measureFp64Peak(int device, double ms) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  return flopsPerIteration * iters / (double(t) * 1e6);
+}
+
+double measureFp64Peak(int device, double ms) {
+  SDG_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  SDG_CUDA(cudaGetDeviceProperties(&prop, device));
+  const int threads = 256, blocks = prop.multiProcessorCount * 8;
+  double* out = devAlloc<double>(size_t(threads) * blocks);
+  const double r = timeProbe(device, ms, 2.0 * 8.0 * double(threads) * blocks, [&](int iters) {
+    fp64ProbeKernel<<<blocks, threads>>>(out, iters, 1.0000001, 1e-9);
+  });
   cudaFree(out);
-  return 2.0 * 8.0 * double(threads) * blocks * iters / (double(t) * 1e6);
+  return r;
+}
+
+double measureDmmaPeak(int device, int shape, double ms) {
+  SDG_CUDA(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  SDG_CUDA(cudaGetDeviceProperties(&prop, device));
+  const int threads = 256, blocks = prop.multiProcessorCount * 8;
+  double* out = devAlloc<double>(size_t(threads) * blocks);
+  static const int mnk[4][3] = {{8, 8, 4}, {16, 8, 4}, {16, 8, 8}, {16, 8, 16}};
+  const double perMma = 2.0 * mnk[shape][0] * mnk[shape][1] * mnk[shape][2];
+  const double warps = double(threads / 32) * blocks;
+  const double r = timeProbe(device, ms, perMma * 4.0 * warps, [&](int iters) {
+    switch (shape) {
+      case 0: dmmaProbeKernel<0><<<blocks, threads>>>(out, iters); break;
+      case 1: dmmaProbeKernel<1><<<blocks, threads>>>(out, iters); break;
+      case 2: dmmaProbeKernel<2><<<blocks, threads>>>(out, iters); break;
+      default: dmmaProbeKernel<3><<<blocks, threads>>>(out, iters); break;
+    }
+  });
+  cudaFree(out);
+  return r;
 }
 
 }  // namespace
@@ -1505,6 +1580,17 @@ int sdg_measure_fp64_peak(int32_t device, double milliseconds, double* gflops) {
   if (!gflops || !(milliseconds > 0)) return SDG_ERR_INVALID_ARGUMENT;
   try {
     *gflops = measureFp64Peak(device, milliseconds);
+  } catch (const Failure& f) {
+    g_create_error = f.what();
+    return f.code;
+  }
+  return SDG_OK;
+}
+
+int sdg_measure_dmma_peak(int32_t device, int32_t shape, double milliseconds, double* gflops) {
+  if (!gflops || !(milliseconds > 0) || shape < 0 || shape > 3) return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    *gflops = measureDmmaPeak(device, shape, milliseconds);
   } catch (const Failure& f) {
     g_create_error = f.what();
     return f.code;

@@ -1,12 +1,9 @@
-"""Seeded synthetic workloads shared by the tests, the golden fixtures and bench.py.
+"""Seeded synthetic test cases: the benchmark workloads (re-exported from subrosadg_gb300.workloads) plus the
+boundary-condition, incompressible, artificial-viscosity and 1D cases of the parity tests.
 
-The reference's headline workloads are canonical analytic flows; no dataset is involved.
-  vortex2d : periodic isentropic vortex (strength 5, rho=1, u=(1,1), p=1) on [-5,5]^2, quads, Roe
-  tgv3d    : Taylor-Green vortex, Mach 0.1, periodic [0,2pi]^3, hexahedra, HLLC
-  kh2d     : Kelvin-Helmholtz shear layer on [0,1]^2 (rho 1/2 bands, u=+-0.5, seeded 1e-2 sinusoidal v),
-             jittered quads with a seeded half split into triangles, LF
-Thermodynamics follow the example drivers: cp = 2.5, cv = 25/14 (R = 1/1.4), gamma = 1.4
-(examples/periodic_2d_ceuler.cpp:51), so the primitive temperature is T = p / (rho R).
+Each *_case returns (mesh, config, initial primitive function of the volume points, boundary primitive
+function or None, dt, steps).  Thermodynamics follow the example drivers: cp = 2.5, cv = 25/14 (R = 1/1.4),
+gamma = 1.4 (examples/periodic_2d_ceuler.cpp:51).
 """
 from __future__ import annotations
 
@@ -15,107 +12,9 @@ import math
 import numpy as np
 
 import subrosadg_gb300 as sdg
-
-GAMMA = 1.4
-CP, CV = 2.5, 25.0 / 14.0
-R_GAS = CP - CV
-
-
-def vortex_primitive(x, y, beta=5.0, gamma=GAMMA, period=10.0):
-    # nearest periodic image of the vortex centre at the origin
-    x = (x + period / 2) % period - period / 2
-    y = (y + period / 2) % period - period / 2
-    r2 = x * x + y * y
-    du = beta / (2 * math.pi) * np.exp(0.5 * (1 - r2))
-    u = 1.0 - du * y
-    v = 1.0 + du * x
-    t = 1.0 - (gamma - 1) * beta ** 2 / (8 * gamma * math.pi ** 2) * np.exp(1 - r2)
-    rho = t ** (1.0 / (gamma - 1))
-    p = rho ** gamma
-    return np.stack([rho, u, v, p / (rho * R_GAS)], 1)
-
-
-def tgv_primitive(x, y, z, mach=0.1, gamma=GAMMA):
-    p0 = 1.0 / (gamma * mach ** 2)
-    u = np.sin(x) * np.cos(y) * np.cos(z)
-    v = -np.cos(x) * np.sin(y) * np.cos(z)
-    w = np.zeros_like(x)
-    p = p0 + (np.cos(2 * x) + np.cos(2 * y)) * (np.cos(2 * z) + 2.0) / 16.0
-    rho = p / p0  # isothermal start, T0 = p0 / (rho0 R)
-    return np.stack([rho, u, v, w, p / (rho * R_GAS)], 1)
-
-
-def kh_primitive(x, y, seed=7, pressure=2.5):
-    rng = np.random.default_rng(seed)
-    k = int(rng.integers(1, 4))
-    phase = float(rng.uniform(0, 2 * math.pi))
-    band = (y >= 0.25) & (y <= 0.75)
-    rho = np.where(band, 2.0, 1.0)
-    u = np.where(band, 0.5, -0.5)
-    v = 1e-2 * np.sin(2 * math.pi * k * x + phase)
-    p = np.full_like(x, pressure)  # 2.5: examples/khinstability_2d_ceuler.cpp:33-40
-    return np.stack([rho, u, v, p / (rho * R_GAS)], 1)
-
-
-def uniform_primitive(n, dim, rho=1.0, vel=(0.3, -0.2, 0.1), p=1.0):
-    out = np.zeros((n, dim + 2))
-    out[:, 0] = rho
-    out[:, 1:1 + dim] = vel[:dim]
-    out[:, dim + 1] = p / (rho * R_GAS)
-    return out
-
-
-def config(p, flux, equation=sdg.EULER, viscous=sdg.VISCOUS_NONE, mu=0.0, prandtl=0.71, rk=sdg.SSPRK3):
-    return sdg.make_config(p, equation=equation, convective_flux=flux, viscous_flux=viscous, time_integration=rk,
-                           cp=CP, cv=CV, gamma=GAMMA, mu=mu, prandtl=prandtl)
-
-
-def ns_config(p, flux, viscous, mu, prandtl=0.71, transport=sdg.TRANSPORT_CONSTANT):
-    """Compressible Navier-Stokes with BR1/BR2 (the reference fixes Pr = 0.71, PhysicalModel.cpp:91)."""
-    c = config(p, flux, equation=sdg.NAVIER_STOKES, viscous=viscous, mu=mu, prandtl=prandtl)
-    c.transport_model = transport
-    return c
-
-
-def vortex_case(n=8, p=3, flux=sdg.ROE, dt=1e-3, steps=4, viscous=None, mu=0.0):
-    mesh = sdg.Mesh.box_2d(-5.0, -5.0, 10.0, 10.0, n, n, periodic=True)
-    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
-    return (mesh, cfg, lambda pts: vortex_primitive(pts[:, 0], pts[:, 1]), None, dt, steps)
-
-
-def tgv_case(n=3, p=3, flux=sdg.HLLC, dt=None, steps=3, viscous=None, mu=1.0 / 1600.0):
-    """Taylor-Green vortex; with `viscous` the Navier-Stokes case at Re = 1/mu (1600 by default)."""
-    mesh = sdg.Mesh.box_3d(0, 0, 0, 2 * math.pi, 2 * math.pi, 2 * math.pi, n, n, n, periodic=True)
-    if dt is None:
-        # CFL 0.2 with minEdge = 2 pi / n and max(|u|+c) ~ 1 + 1/Mach (TimeIntegration.cpp:119-125)
-        dt = 0.2 * (2 * math.pi / n) / ((1.0 + 1.0 / 0.1 + 0.05) * (p + 1) ** 2)
-    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
-    return (mesh, cfg, lambda pts: tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2]), None, dt, steps)
-
-
-# Even permutations of a tetrahedron's vertex list (orientation kept): shuffling each element's list this way
-# makes shared faces meet at all three rotations.
-_EVEN_TET = np.array([(0, 1, 2, 3), (0, 2, 3, 1), (0, 3, 1, 2), (1, 0, 3, 2), (1, 2, 0, 3), (1, 3, 2, 0),
-                      (2, 0, 1, 3), (2, 1, 3, 0), (2, 3, 0, 1), (3, 0, 2, 1), (3, 1, 0, 2), (3, 2, 1, 0)])
-
-
-def tet_mesh(n=3, length=1.0, periodic=True, conditions=None, seed=7):
-    """Structured tetrahedral box [0, length]^3 (six tetrahedra per cube), vertex lists shuffled (seeded)."""
-    mesh = sdg.Mesh.box_3d_tetrahedra(0, 0, 0, length, length, length, n, n, n, periodic=periodic,
-                                      boundary_conditions=None if periodic else list(conditions))
-    pick = np.random.default_rng(seed).integers(0, len(_EVEN_TET), len(mesh.tetrahedra))
-    mesh.tetrahedra = np.ascontiguousarray(mesh.tetrahedra[np.arange(len(pick))[:, None], _EVEN_TET[pick]])
-    return mesh
-
-
-def tet_tgv_case(n=3, p=2, flux=sdg.HLLC, steps=3, mach=0.3, viscous=None, mu=0.02):
-    """Taylor-Green vortex on periodic tetrahedra of [0, 2 pi]^3 (Mach 0.3 for a nonlinear flux); with
-    `viscous` the Navier-Stokes case at Re = 1/mu."""
-    mesh = tet_mesh(n, 2 * math.pi)
-    dt = 0.2 * (2 * math.pi / n) / ((1.0 + 1.0 / mach) * (p + 1) ** 2)
-    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
-    return (mesh, cfg, lambda pts: tgv_primitive(pts[:, 0], pts[:, 1], pts[:, 2], mach=mach), None, dt,
-            steps)
+from subrosadg_gb300.workloads import (CP, CV, GAMMA, R_GAS, batch_instances, config, kh_case, kh_primitive,  # noqa: F401
+                                       ns_config, tet_mesh, tet_tgv_case, tgv_case, tgv_primitive, uniform_primitive,
+                                       vortex_case, vortex_primitive)
 
 
 def tet_box_case(p=2, flux=sdg.HLLC, conditions=(sdg.RIEMANN_FARFIELD,) * 6, n=3, dt=5e-4, steps=3, viscous=None,
@@ -142,14 +41,6 @@ def tet_box_case(p=2, flux=sdg.HLLC, conditions=(sdg.RIEMANN_FARFIELD,) * 6, n=3
 
     cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
     return (mesh, cfg, ic, bc, dt, steps)
-
-
-def kh_case(n=8, p=4, flux=sdg.LAX_FRIEDRICHS, dt=2e-4, steps=3, jitter=0.1, split=0.5, seed=11, viscous=None,
-            mu=1e-4):
-    """Kelvin-Helmholtz; with `viscous` the Navier-Stokes case at Re = 1/mu (1e4 by default)."""
-    mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=True, jitter=jitter, split_fraction=split, seed=seed)
-    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
-    return (mesh, cfg, lambda pts: kh_primitive(pts[:, 0], pts[:, 1]), None, dt, steps)
 
 
 def channel_case(p=2, flux=sdg.HLLC, conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.PRESSURE_OUTFLOW,
@@ -443,34 +334,6 @@ def shock_tube_case(p=3, flux=sdg.HLLC, n=8, dt=2e-4, steps=3, split=0.0, jitter
         return out
 
     return with_av((mesh, cfg, ic, bc, dt, steps), tolerance, factor)
-
-
-def batch_instances(count=256, seed=2024, min_elements=500, max_elements=50000, orders=(1, 2, 3, 4, 5)):
-    """The batched workload: `count` independent 2D Kelvin-Helmholtz solves on [0,1]^2 (periodic), element
-    counts log-uniform in [min_elements, max_elements], P uniform in `orders`, jittered (10% of h) quads or
-    the hybrid with a 50% triangle split, Mach of the shear speed uniform in [0.1, 0.8] (p = rho c^2 / gamma
-    with c = 0.5 / Mach in the light band), Re = 1 / mu log-uniform in [1e2, 1e4], Euler or Navier-Stokes
-    (BR2) with equal odds, Lax-Friedrichs flux, SSP-RK3.  Returns a list of (mesh, cfg, primitive) and the
-    parameter records."""
-    rng = np.random.default_rng(seed)
-    out, params = [], []
-    for i in range(count):
-        target = math.exp(rng.uniform(math.log(min_elements), math.log(max_elements)))
-        p = int(rng.choice(orders))
-        hybrid = bool(rng.random() < 0.5)
-        mach = float(rng.uniform(0.1, 0.8))
-        re = float(math.exp(rng.uniform(math.log(1e2), math.log(1e4))))
-        ns = bool(rng.random() < 0.5)
-        split = 0.5 if hybrid else 0.0
-        n = max(3, int(round(math.sqrt(target / (1.0 + split)))))
-        mesh = sdg.Mesh.box_2d(0.0, 0.0, 1.0, 1.0, n, n, periodic=True, jitter=0.1, split_fraction=split,
-                               seed=seed * 1000 + i)
-        cfg = ns_config(p, sdg.LAX_FRIEDRICHS, sdg.BR2, 1.0 / re) if ns else config(p, sdg.LAX_FRIEDRICHS)
-        pressure = 0.25 / (GAMMA * mach * mach)
-        out.append((mesh, cfg, (lambda pr, sd: (lambda pts: kh_primitive(pts[:, 0], pts[:, 1], seed=sd, pressure=pr)))(
-            pressure, seed + i)))
-        params.append({"n": n, "order": p, "hybrid": hybrid, "mach": mach, "reynolds": re, "navier_stokes": ns})
-    return out, params
 
 
 def golden_cases():

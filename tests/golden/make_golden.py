@@ -1,7 +1,7 @@
 """Generate the golden fixtures of the test suite.
 
-Part 1 -- known answers read as text from the reference (run in a container that has the
-reference tree at /root/reference):
+Part 1 -- known answers read as text from the reference source tree, whose root is passed
+with --reference:
   * face quadrature permutations by rotation   src/Solver/SimulationControl.cpp:381-523
   * quadrature point counts by order           src/Solver/SimulationControl.cpp:268-273
   * face vertex lists                          src/Solver/SimulationControl.cpp:170-216
@@ -11,7 +11,7 @@ reference tree at /root/reference):
 Part 2 -- oracle reference vectors on small seeded meshes (the oracle is the CPU restatement
 of the reference algorithm; these pin it across machines and edits).
 
-    python tests/golden/make_golden.py [--reference /root/reference]
+    python tests/golden/make_golden.py --reference <root of the SubrosaDG source tree>
 """
 from __future__ import annotations
 
@@ -132,7 +132,7 @@ def oracle_vectors():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", required=True, help="root of the SubrosaDG source tree (read only)")
     args = ap.parse_args()
     tables = reference_tables(args.reference)
     with open(os.path.join(HERE, "reference_tables.json"), "w") as f:

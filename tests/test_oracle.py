@@ -197,3 +197,46 @@ def test_vortex_advects_at_freestream_speed():
     exact = cases.vortex_primitive(pts[:, 0] - t, pts[:, 1] - t)
     rho = o.state_point()[:, 0]
     assert np.abs(rho - exact[:, 0]).max() < 5e-3
+
+
+# ---- the timed CPU baselines and the oracle's own mesh generator ----------------------------------------
+
+@pytest.mark.parametrize("periodic", [True, False])
+def test_oracle_box_generator_equals_library_generator(periodic):
+    """oracle/meshgen.box_3d (used by the CPU baselines, which load nothing of the GPU library) builds the
+    library's structured box bit for bit."""
+    from oracle import meshgen
+    bc = None if periodic else [sdg.RIEMANN_FARFIELD, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_SLIP_WALL,
+                                sdg.VELOCITY_INFLOW, sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_NONSLIP_WALL]
+    a = sdg.Mesh.box_3d(0.1, 0.2, 0.3, 1.5, 2.5, 2 * math.pi, 3, 4, 5, periodic=periodic, boundary_conditions=bc)
+    b = meshgen.box_3d(0.1, 0.2, 0.3, 1.5, 2.5, 2 * math.pi, 3, 4, 5, periodic=periodic, boundary_conditions=bc)
+    for k in ("nodes", "hexahedra", "boundary", "boundary_physical", "physical_conditions", "periodic_master"):
+        x, y = getattr(a, k), getattr(b, k)
+        assert (x is None and y is None) or (x.dtype == y.dtype and np.array_equal(x, y)), k
+
+
+def test_stages_compose_a_step():
+    """Three orc_stage calls are one orc_step, bit for bit (the reference arm of bench.py times stages)."""
+    mesh, cfg, prim, _, dt, _ = cases.tgv_case(n=3, p=2)
+    a, b = Oracle(mesh, cfg, faithful=True), Oracle(mesh, cfg, faithful=True)
+    for o in (a, b):
+        o.initialize_primitive(prim(o.volume_points()))
+    a.step(dt, 2)
+    for s in range(6):
+        b.stage(s % 3, dt)
+    assert np.array_equal(a.state_point(), b.state_point())
+    assert np.array_equal(a.relative_error(), b.relative_error())
+
+
+@pytest.mark.parametrize("case", [lambda: cases.tgv_case(n=3, p=3), lambda: cases.kh_case(n=4, p=3, steps=2)],
+                         ids=["tgv-hex-affine", "kh-hybrid-jittered"])
+def test_lean_baseline_computes_the_same_scheme(case):
+    """The lean CPU baseline (no Euler gradient pass, one shared reference inverse on affine blocks) and the
+    reference-faithful one advance the same discrete scheme: states agree to round-off."""
+    mesh, cfg, prim, _, dt, steps = case()
+    f, l = Oracle(mesh, cfg, faithful=True), Oracle(mesh, cfg, lean=True)
+    for o in (f, l):
+        o.initialize_primitive(prim(o.volume_points()))
+        o.step(dt, steps)
+    a, b = f.state_point(), l.state_point()
+    assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(a)
