@@ -260,23 +260,30 @@ int sdg_adjacency(const sdg_handle* handle, int32_t* interior, int32_t* boundary
 /* Allocation-free CFL time step.  Some callers cannot call cudaMalloc where they need a time step -- a
  * framework whose memory pool forbids raw device allocations, a real-time loop that must not allocate, a
  * host that only records work into a stream it was handed.  This entry point has no counterpart in the
- * reference; it returns the same dt as sdg_calculate_delta_time, computed from device arrays the caller
- * already holds, and allocates nothing:
- *   state_point   device [point_count][dimension+2] conserved values at the volume points
+ * reference.  For one element block it returns the dt that sdg_calculate_delta_time computes over that
+ * block, from device arrays the caller already holds, and allocates nothing:
+ *   state_point   device [point_count][dimension+2] conserved values at the block's volume points
  *   minimum_edge  device [point_count / points_per_element] shortest edge per element (minEdge quality)
- *   delta_time    device pointer to one double that receives dt
+ *   points_per_element  volume points per element of the block; point_count must be a multiple of it
+ *   dimension     1, 2 or 3
+ *   specific_heat_ratio  gamma of the ideal gas (> 1; ignored when reference_sound_speed > 0)
+ *   reference_sound_speed  0 for the compressible models (sound speed sqrt(gamma p / rho)); the constant c0
+ *                 of the incompressible models (sdg_config.reference_sound_speed) otherwise
+ *   delta_time    device pointer to one double that receives dt (overwritten by every call)
  *   stream        cudaStream_t to enqueue on (NULL: the legacy default stream); the result is ready
  *                 when the stream reaches that point
+ * A mesh of several blocks (triangles and quadrangles) needs one call per block, with that block's points,
+ * minEdge and points_per_element, into separate doubles; dt is their minimum, which the caller takes.
  * Its scratch is a file-scope __device__ array of 131072 doubles (1 MiB) that every GPU which loads
  * the library holds until the process exits.  point_count above 33,554,432 is rejected with
- * SDG_ERR_INVALID_ARGUMENT.  The first call on a device looks up the array's device address with that
- * device current (make that first call before any stream capture).  All calls share the array, so calls
- * that overlap on the GPU race; serialise them.  Errors: SDG_ERR_INVALID_ARGUMENT, SDG_ERR_CUDA, with text
- * in sdg_last_error(NULL). */
+ * SDG_ERR_INVALID_ARGUMENT.  The first call on a device (and in each new CUDA context of it) looks up the
+ * array's device address with that device current: make that first call before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU race; serialise them.  Errors:
+ * SDG_ERR_INVALID_ARGUMENT, SDG_ERR_CUDA, with text in sdg_last_error(NULL). */
 int sdg_delta_time_noalloc(const double* state_point, const double* minimum_edge, int64_t point_count,
                            int32_t points_per_element, int32_t dimension, int32_t polynomial_order,
-                           double specific_heat_ratio, double courant_friedrichs_lewy_number, double* delta_time,
-                           void* stream);
+                           double specific_heat_ratio, double reference_sound_speed,
+                           double courant_friedrichs_lewy_number, double* delta_time, void* stream);
 
 /* Structured mesh generators of the reference's example drivers (gmsh transfinite + periodic
  * setups in examples/periodic_2d_ceuler.cpp:63-94 and examples/periodic_3d_ceuler.cpp:60-130),
@@ -334,6 +341,16 @@ int sdg_read_raw_binary(sdg_handle* handle, const char* path, int32_t lower_orde
  * one by one instead (kernel timing always does).  The reference has no equivalent: its step is a
  * oneTBB loop (src/Solver/TimeIntegration.cpp:326-350). */
 int sdg_set_graph(sdg_handle* handle, int32_t enable);
+/* Check of the failure detection of the device waits.  The tensor-block stage kernels stage each element
+ * tile with TMA bulk copies that complete on an mbarrier, and wait for it at most `wait_limit` try_wait
+ * rounds (0: the default, 2^24).  extra_expected_bytes > 0 (at most 65536) makes them declare that many
+ * bytes beyond what their copies carry, so the wait can end only by its limit: every copy still lands, the
+ * kernel withdraws the extra bytes, waits (bounded) until its copies have landed, flags the timeout and
+ * returns, and the call reports SDG_ERR_TIMEOUT.  Nothing faults and no wait is unbounded.  The timeout
+ * is sticky: the handle's state is no longer a valid step result; create a new handle.  (0, 0) restores the
+ * normal kernels.  The reference has no equivalent (its only detection is the NaN check,
+ * src/Utils/SystemControl.cpp:185-191). */
+int sdg_set_wait_check(sdg_handle* handle, uint32_t wait_limit, uint32_t extra_expected_bytes);
 /* Elements per CTA and threads per CTA of block `block`'s stage kernel and gradient kernel. */
 int sdg_get_tile(const sdg_handle* handle, int32_t block, int32_t* elements_per_cta, int32_t* threads,
                  int32_t* gradient_elements_per_cta, int32_t* gradient_threads);

@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import os
-from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_uint64, c_void_p
+from ctypes import POINTER, c_char_p, c_double, c_int32, c_int64, c_uint32, c_uint64, c_void_p
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIBRARY_PATH = os.path.join(_HERE, "lib", "libsdg_gpu.so")
@@ -156,7 +156,7 @@ SIGNATURES = {
     "sdg_measure_fp64_peak": (c_int32, [c_int32, c_double, _p_double]),
     "sdg_measure_dmma_peak": (c_int32, [c_int32, c_int32, c_double, _p_double]),
     "sdg_delta_time_noalloc": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_int32, c_int32, c_double, c_double,
-                                         c_void_p, c_void_p]),
+                                         c_double, c_void_p, c_void_p]),
     "sdg_mesh_generate_2d": (c_int32, [c_double, c_double, c_double, c_double, c_int32, c_int32, c_double,
                                        c_double, c_uint64, c_int32, _p_int32, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_generate_1d": (c_int32, [c_double, c_double, c_int32, c_int32, _p_int32, c_void_p]),
@@ -174,6 +174,7 @@ SIGNATURES = {
     "sdg_write_raw_binary": (c_int32, [c_void_p, c_char_p]),
     "sdg_read_raw_binary": (c_int32, [c_void_p, c_char_p, c_int32]),
     "sdg_set_graph": (c_int32, [c_void_p, c_int32]),
+    "sdg_set_wait_check": (c_int32, [c_void_p, c_uint32, c_uint32]),
     "sdg_get_tile": (c_int32, [c_void_p, c_int32, _p_int32, _p_int32, _p_int32, _p_int32]),
     "sdg_set_tile": (c_int32, [c_void_p, c_int32, c_int32, c_int32, c_int32, c_int32]),
     "sdg_autotune": (c_int32, [c_void_p, c_int32]),

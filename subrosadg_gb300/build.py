@@ -74,5 +74,25 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     return target
 
 
+CPP = os.path.join(ROOT, "subrosadg_gb300", "cpp")
+DRIVERS = ["periodic_2d_ceuler"]
+
+
+def build_drivers(force: bool = False) -> list:
+    """Compile the C++23 example drivers (cpp/*.cpp over the C++ mirror gpu_solver.hpp) against libsdg_gpu.so."""
+    lib = build_library(force=force)
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"
+    out = []
+    for name in DRIVERS:
+        target = os.path.join(LIBDIR, "sdg_" + name)
+        deps = [os.path.join(CPP, name + ".cpp"), os.path.join(CPP, "gpu_solver.hpp"), lib,
+                os.path.join(ROOT, "include", "sdg_gpu.h")]
+        if force or _stale(target, deps):
+            _run([cxx, "-std=c++23", "-O2", "-Wall", "-Wextra", "-o", target, os.path.join(CPP, name + ".cpp"),
+                  "-L" + LIBDIR, "-lsdg_gpu", "-Wl,-rpath,$ORIGIN"], CPP)
+        out.append(target)
+    return out
+
+
 if __name__ == "__main__":
-    print("built", build_library(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print("built", build_library(force="--force" in sys.argv, verbose="-v" in sys.argv), *build_drivers())

@@ -391,6 +391,14 @@ int sdg_set_graph(sdg_handle* h, int32_t enable) {
   return SDG_OK;
 }
 
+int sdg_set_wait_check(sdg_handle* h, uint32_t wait_limit, uint32_t extra_expected_bytes) {
+  if (!h || extra_expected_bytes > 65536) return SDG_ERR_INVALID_ARGUMENT;
+  h->waitLimit = wait_limit;
+  h->txExtra = extra_expected_bytes;
+  dropGraph(h);
+  return SDG_OK;
+}
+
 int sdg_get_tile(const sdg_handle* h, int32_t block, int32_t* epb, int32_t* threads, int32_t* gepb, int32_t* gthreads) {
   if (!h || block < 0 || block >= int32_t(h->blocks.size())) return SDG_ERR_INVALID_ARGUMENT;
   const DevBlock& B = h->blocks[block];

@@ -501,6 +501,7 @@ Rec stageRec(sdg_handle* h, DevBlock& B) {
   std::memset(&a, 0, sizeof(a));
   a.face = h->face; a.geom = B.geom; a.tables = B.tables; a.status = h->status;
   a.ne = B.ne; a.faceBase = B.faceBase; a.epb = B.epb;
+  a.txExtra = h->txExtra; a.waitLimit = h->waitLimit; a.diagMetric = B.diagMetric;
   if (viscousPath(h)) { a.fluxSrc = h->faceFlux; a.grad = h->grad + B.gradOffset; }
   if (h->av) { a.av = 1; a.epsV = B.epsV; a.avTab = B.avTab; }
   r.ph = h->ph;
@@ -1029,6 +1030,13 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         B.minEdge[e] = minEdgeOf(b.type, nodes, vv);
       }
       if (bad) throw Failure(SDG_ERR_MESH, "inverted or degenerate element");
+      // axis-aligned affine tensor elements (structured boxes): every off-diagonal metric term is exactly
+      // zero, and the stage kernel skips those products (the same values)
+      B.diagMetric = B.kind == kTensor && B.affine;
+      for (int64_t e = 0; e < B.ne && B.diagMetric; ++e)
+        for (int r = 0; r < B.dim; ++r)
+          for (int cc = 0; cc < B.dim; ++cc)
+            if (r != cc && B.geomHost[size_t(e) * B.geomStride + r * B.dim + cc] != 0.0) B.diagMetric = 0;
       if (B.kind == kTensor) {
         B.ops.build(B.n);
         buildTensorTables(B);

@@ -45,9 +45,14 @@ __device__ __forceinline__ void bulkLoad(void* dst, const void* src, uint32_t by
 }
 // Orders this thread's earlier generic-proxy accesses of shared memory before later bulk copies into it.
 __device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-// Bounded wait on phase `parity`; returns false (and the caller flags a timeout) if it never completes.
-__device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t it = 0; it < kWaitLimit; ++it) {
+// Withdraws `bytes` from the barrier's pending transaction count (bytes that no copy will deliver).
+__device__ __forceinline__ void mbarCompleteTx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.complete_tx.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(bar)), "r"(bytes) : "memory");
+}
+// Bounded wait on phase `parity` (at most `limit` try_wait rounds); returns false (and the caller flags a
+// timeout) if it never completes.
+__device__ __forceinline__ bool mbarWait(uint64_t* bar, uint32_t parity, uint32_t limit = kWaitLimit) {
+  for (uint32_t it = 0; it < limit; ++it) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -97,6 +102,12 @@ struct StageArgs {
   int av;                 // artificial viscosity (the viscous variant with the flux eps grad U)
   const double* epsV;     // artificial viscosity at the element vertices [e][nvert]
   const double* avTab;    // artificial-viscosity tables of the block (avTableLayout)
+  // Check of the bounded wait (sdg_set_wait_check): extra bytes declared to the tile's mbarrier beyond what
+  // its copies carry, so that the wait can end only by its limit; and that limit (0: kWaitLimit rounds).
+  unsigned txExtra;
+  unsigned waitLimit;
+  int diagMetric;         // affine block with diagonal metric terms only (structured axis-aligned boxes)
+  int pad;
 };
 
 // Artificial-viscosity tables of a block (doubles):
@@ -208,7 +219,7 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
   if (tid == 0) {
     fenceProxyAsync();
     const uint32_t ub = uint32_t(ecount) * S::USTRIDE * 8, fb = uint32_t(ecount) * S::FSTRIDE * 8;
-    mbarExpectTx(bar, a.doVolume ? ub + fb : ub);
+    mbarExpectTx(bar, (a.doVolume ? ub + fb : ub) + a.txExtra);
     bulkLoad(sU, a.uin + e0 * S::USTRIDE, ub, bar);
     if (a.doVolume) bulkLoad(sF, (a.fluxSrc ? a.fluxSrc : a.face) + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
@@ -218,10 +229,11 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
     for (int k = tid; k < int(sizeof(TensorTables) / 8); k += blockDim.x) dst[k] = src[k];
   }
   __syncthreads();
-  const bool arrived = mbarWait(bar, parity);
+  const bool arrived = mbarWait(bar, parity, a.waitLimit ? a.waitLimit : kWaitLimit);
   if (__syncthreads_or(!arrived)) {  // uniform decision: every thread leaves together
     if (tid == 0) {
       atomicOr(a.status, kStatusTimeout);
+      if (a.txExtra) mbarCompleteTx(bar, a.txExtra);  // the phase now completes once the real copies land
       mbarWait(bar, parity);  // bounded: let copies still in flight land before the CTA exits
     }
     return false;
@@ -264,6 +276,31 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
         viscousTensor<DIM>(pg, s.u, fma(ph.incomp ? 0.0 : -0.5, u2, s.E * s.ir) * ph.inv_cv, ph,
                            tau, q);
       }
+      if (AFFINE && a.diagMetric) {
+        // axis-aligned element: ja[b][c] = 0 for c != b.  The same products as the general form below
+        // without its multiplications by zero (every skipped term is an exact +-0): equal values, at most
+        // the sign of an exact zero differs.
+#pragma unroll
+        for (int b = 0; b < DIM; ++b) {
+          const double jb = ja[b][b];
+          const double vb = s.u[b] * jb;
+          double* G = sG + ((le * DIM + b) * NV) * NB + node;
+          G[0] = s.r * vb;
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) {
+            double x = k == b ? fma(s.m[k], vb, jb * s.p) : s.m[k] * vb;
+            if constexpr (VISC == 1) x = fma(-jb, tau[b][k], x);
+            G[(1 + k) * NB] = x;
+          }
+          double xe = ep * vb;
+          if constexpr (VISC == 1) xe -= q[b] * jb;
+          G[(NV - 1) * NB] = xe;
+          if constexpr (VISC == 2) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) G[v * NB] = fma(-jb, gv[v * DIM + b], G[v * NB]);
+          }
+        }
+      } else {
 #pragma unroll
       for (int b = 0; b < DIM; ++b) {
         const double vb = dotn<DIM>(s.u, ja[b]);
@@ -290,6 +327,7 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
             G[v * NB] = x;
           }
         }
+      }
       }
     }
     __syncthreads();
@@ -341,11 +379,18 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
         for (int v = 0; v < NV; ++v) a.rate[(e * NB + node) * NV + v] = du[v] * jinv;
       }
       if (a.doUpdate) {
+        if (a.uin == a.ubase && a.c1 == 0.0 && a.c0 == 1.0) {
+          // first stage of a step (every RK table starts with {1, 0, 1}): U = U^n + dt M^-1 R, and U^n is
+          // the staged tile itself, so the base state is not read again
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          const double u0 = a.ubase[gi + v * NB];
-          const double u1 = sU[le * S::USTRIDE + v * NB + node];
-          unew[v] = fma(sc, du[v], fma(a.c1, u1, a.c0 * u0));
+          for (int v = 0; v < NV; ++v) unew[v] = fma(sc, du[v], sU[le * S::USTRIDE + v * NB + node]);
+        } else {
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            const double u0 = a.ubase[gi + v * NB];
+            const double u1 = sU[le * S::USTRIDE + v * NB + node];
+            unew[v] = fma(sc, du[v], fma(a.c1, u1, a.c0 * u0));
+          }
         }
       }
     }

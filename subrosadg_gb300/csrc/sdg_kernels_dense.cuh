@@ -347,9 +347,11 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
         const double du = sc * s;
         sQ[(le * NV + v) * NB + i] = du;  // sQ reused: du per basis function
         if (a.doUpdate) {
-          const double u0 = a.ubase[e * S::USTRIDE + v * NB + i];
           const double u1 = sU[le * S::USTRIDE + v * NB + i];
-          const double un = fma(a.c2dt, du, fma(a.c1, u1, a.c0 * u0));
+          // first stage of a step (every RK table starts with {1, 0, 1}): the base state is the staged tile
+          const bool first = a.uin == a.ubase && a.c1 == 0.0 && a.c0 == 1.0;
+          const double un = first ? fma(a.c2dt, du, u1)
+                                  : fma(a.c2dt, du, fma(a.c1, u1, a.c0 * a.ubase[e * S::USTRIDE + v * NB + i]));
           sN[(le * NV + v) * NB + i] = un;
           a.uout[e * S::USTRIDE + v * NB + i] = un;
         } else {

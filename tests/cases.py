@@ -356,3 +356,25 @@ def golden_cases():
         "wave1d_line_p3_hllc": lambda: density_wave_1d_case(n=10, p=3, steps=3),
         "av_sod1d_line_p3_hllc": lambda: sod_1d_case(n=19, p=3, steps=3),
     }
+
+
+def transformed(case, matrix):
+    """The same case on the mesh mapped by the linear map `matrix` (a rotation or shear keeps elements affine,
+    with off-diagonal metric terms): nodes x' = A x, initial state evaluated at A^-1 x' (periodic on the mapped
+    lattice)."""
+    mesh, cfg, prim, bprim, dt, steps = case
+    a = np.asarray(matrix, np.float64)
+    d = mesh.dimension
+    full = np.eye(3)
+    full[:d, :d] = a
+    mesh.nodes = np.ascontiguousarray(mesh.nodes @ full.T)
+    inv = np.linalg.inv(full)
+    return (mesh, cfg, lambda pts: prim(np.ascontiguousarray(pts @ inv.T)), bprim, dt, steps)
+
+
+def rotation_2d(degrees):
+    t = math.radians(degrees)
+    return [[math.cos(t), -math.sin(t)], [math.sin(t), math.cos(t)]]
+
+
+SHEAR_3D = [[1.0, 0.3, 0.0], [0.0, 1.0, 0.2], [0.1, 0.0, 1.0]]

@@ -18,6 +18,7 @@ def built():
     from oracle import build as oracle_build
     from subrosadg_gb300 import build as lib_build
     lib_build.build_library()
+    lib_build.build_drivers()
     oracle_build.build()
     yield
 

@@ -67,6 +67,15 @@ CASES = {
     "tgv-hex-p3-lf": lambda: cases.tgv_case(n=3, p=3, flux=sdg.LAX_FRIEDRICHS, steps=3),
     "tgv-hex-p4-hllc": lambda: cases.tgv_case(n=3, p=4, flux=sdg.HLLC, steps=2),
     "tgv-hex-p5-roe": lambda: cases.tgv_case(n=3, p=5, flux=sdg.ROE, steps=2),
+    # affine elements with off-diagonal metric terms (the structured boxes above take the diagonal-metric path)
+    "tgv-hex-p3-sheared-hllc": lambda: cases.transformed(cases.tgv_case(n=3, p=3, flux=sdg.HLLC), cases.SHEAR_3D),
+    "tgv-hex-p2-sheared-roe": lambda: cases.transformed(cases.tgv_case(n=4, p=2, flux=sdg.ROE), cases.SHEAR_3D),
+    "vortex-quad-p3-rotated-roe": lambda: cases.transformed(cases.vortex_case(n=6, p=3, flux=sdg.ROE),
+                                                            cases.rotation_2d(30.0)),
+    "ns-tgv-hex-p3-sheared-br1-roe": lambda: cases.transformed(
+        cases.tgv_case(n=3, p=3, flux=sdg.ROE, steps=2, viscous=sdg.BR1, mu=0.02), cases.SHEAR_3D),
+    "ns-vortex-quad-p2-rotated-br2-hllc": lambda: cases.transformed(
+        cases.vortex_case(n=5, p=2, flux=sdg.HLLC, steps=3, viscous=sdg.BR2, mu=0.05), cases.rotation_2d(20.0)),
     # tetrahedra (dense modal blocks in 3D; shuffled vertex lists: shared faces at all three rotations)
     "tet-tgv-p1-hllc": lambda: cases.tet_tgv_case(n=3, p=1, flux=sdg.HLLC, steps=4),
     "tet-tgv-p2-roe": lambda: cases.tet_tgv_case(n=3, p=2, flux=sdg.ROE, steps=3),
