@@ -28,6 +28,8 @@ def load(precision="double"):
         lib = ctypes.CDLL(path)
         lib.orc_create.restype = c_void_p
         lib.orc_create.argtypes = [c_void_p, c_void_p, c_int]
+        lib.orc_create_sampled.restype = c_void_p
+        lib.orc_create_sampled.argtypes = [c_void_p, c_void_p, c_int, c_int64, POINTER(c_int64)]
         lib.orc_last_error.restype = ctypes.c_char_p
         lib.orc_destroy.argtypes = [c_void_p]
         for name in ("orc_volume_point_coordinate", "orc_set_initial_primitive", "orc_set_state_point",
@@ -59,14 +61,22 @@ class Oracle:
     lean=True     : the lean timed CPU baseline -- no unused Euler gradient pass, plain inverses, one shared
                     reference inverse scaled by 1/|J| on blocks of affine elements (overrides faithful).
     precision     : "double" (the reference's Real) or "extended" (long double truth).
+    sample        : global element indices (block order): evaluate the residual of these elements only (the
+                    element-sample mode for meshes too large for the extended build; residual_point is zero
+                    elsewhere; stepping is refused).
     """
 
-    def __init__(self, mesh, config, faithful=True, precision="double", lean=False):
+    def __init__(self, mesh, config, faithful=True, precision="double", lean=False, sample=None):
         self.lib = load(precision)
         self._m = mesh.struct()
         self._c = config
         flags = 6 if lean else (3 if faithful else 0)
-        self.h = self.lib.orc_create(ctypes.addressof(self._m), ctypes.addressof(self._c), flags)
+        if sample is None:
+            self.h = self.lib.orc_create(ctypes.addressof(self._m), ctypes.addressof(self._c), flags)
+        else:
+            self._sample = np.ascontiguousarray(sample, np.int64)
+            self.h = self.lib.orc_create_sampled(ctypes.addressof(self._m), ctypes.addressof(self._c), flags,
+                                                 len(self._sample), self._sample.ctypes.data_as(POINTER(c_int64)))
         if not self.h:
             raise RuntimeError("oracle: " + self.lib.orc_last_error().decode())
         c = (c_int64 * 6)()

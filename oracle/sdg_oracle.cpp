@@ -46,6 +46,11 @@ struct Block {
   std::vector<Real> jw;       // ne * nq        |J| w
   std::vector<Real> jtiw;     // ne * nq * d*d  J^-T |J| w, column-major d x d per point
   std::vector<Real> minv;     // ne * nb*nb     local mass matrix inverse
+  // element-sample mode (orc_create_sampled): what each element is needed for -- 0 its residual, 1 its
+  // gradient (a neighbour of a sampled element, gradient pass on), 2 its coefficients only (traces), 3 nothing;
+  // and the slot of its dense M^-1 (and M) in minv / mass (-1: none).  Empty: every element at level 0.
+  std::vector<signed char> level;
+  std::vector<int32_t> slot;
   // shared-inverse (lean) mode on a block of affine elements: M_e^-1 = M_ref^-1 / |J|_e
   bool sharedInverse = false;
   std::vector<Real> minvRef;  // nb*nb         inverse of the reference mass matrix sum_q phi_a phi_b w_q
@@ -99,7 +104,17 @@ struct Problem {
   bool ns() const { return eq == 1 || eq == 3; }  // compressible or incompressible Navier-Stokes
   bool gradientPass() const { return ns() || faithful || av; }
   int nfq() const { return blocks[0].ref.nfq; }
+  bool sampled = false;
 };
+
+// Is element e of block B needed at `lvl` (0 residual, 1 gradient, 2 coefficients)?  Always outside sample mode.
+static inline bool needed(const Block& B, int64_t e, int lvl) { return B.level.empty() || B.level[size_t(e)] <= lvl; }
+// A face is evaluated at `lvl` when either parent is needed there.
+static inline bool faceNeeded(const Problem& P, const Face& F, int lvl) {
+  return needed(P.blocks[F.bl], F.el, lvl) || (F.br >= 0 && needed(P.blocks[F.br], F.er, lvl));
+}
+// Slot of element e's dense inverse.
+static inline size_t minvSlot(const Block& B, int64_t e) { return B.slot.empty() ? size_t(e) : size_t(B.slot[size_t(e)]); }
 
 // ---- setup ----------------------------------------------------------------------------------------
 
@@ -170,6 +185,7 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
   std::string failure;
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < B.ne; ++e) {
+    if (!needed(B, e, 2)) continue;
     const int* vv = &B.verts[size_t(e) * nvert];
     for (int q = 0; q < nq; ++q) {
       Real sh[8], g[24];
@@ -249,10 +265,20 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
     invert(nb, m.data(), B.minvRef.data());
     return;
   }
-  B.minv.assign(size_t(B.ne) * nb * nb, 0.0);
-  if (P.refine) B.mass.assign(size_t(B.ne) * nb * nb, 0.0);
+  // sample mode: inverses only where a residual or gradient is evaluated, in compact slots
+  const int minvLevel = P.gradientPass() ? 1 : 0;
+  int64_t slots = B.ne;
+  if (P.sampled) {
+    B.slot.assign(size_t(B.ne), -1);
+    slots = 0;
+    for (int64_t e = 0; e < B.ne; ++e)
+      if (needed(B, e, minvLevel)) B.slot[size_t(e)] = int32_t(slots++);
+  }
+  B.minv.assign(size_t(slots) * nb * nb, 0.0);
+  if (P.refine) B.mass.assign(size_t(slots) * nb * nb, 0.0);
 #pragma omp parallel for schedule(static)
   for (int64_t e = 0; e < B.ne; ++e) {
+    if (!needed(B, e, minvLevel)) continue;
     // Local mass matrix inverse (Geometry.cpp:88-100).
     std::vector<Real> m(size_t(nb) * nb, 0.0);
     for (int a = 0; a < nb; ++a)
@@ -261,8 +287,8 @@ static void buildGeometry(Problem& P, Block& B, const double* nodes) {
         for (int q = 0; q < nq; ++q) s += R.phi[size_t(q) * nb + a] * R.phi[size_t(q) * nb + b] * B.jw[size_t(e) * nq + q];
         m[size_t(a) * nb + b] = s;
       }
-    invert(nb, m.data(), &B.minv[size_t(e) * nb * nb]);
-    if (P.refine) std::copy(m.begin(), m.end(), &B.mass[size_t(e) * nb * nb]);
+    invert(nb, m.data(), &B.minv[minvSlot(B, e) * nb * nb]);
+    if (P.refine) std::copy(m.begin(), m.end(), &B.mass[minvSlot(B, e) * nb * nb]);
   }
 }
 
@@ -437,10 +463,10 @@ static void applyMinv(const Problem& P, const Block& B, int64_t e, int nr, const
     for (int i = 0; i < nr * nb; ++i) x[i] *= s;
     return;
   }
-  const Real* Mi = &B.minv[size_t(e) * nb * nb];
+  const Real* Mi = &B.minv[minvSlot(B, e) * nb * nb];
   gemmAcc(nr, nb, nb, R, Mi, x, 1);
   if (!P.refine) return;
-  const Real* M = &B.mass[size_t(e) * nb * nb];
+  const Real* M = &B.mass[minvSlot(B, e) * nb * nb];
   std::vector<Real> res(R, R + size_t(nr) * nb);
   gemmAcc(nr, nb, nb, x, M, res.data(), -1);
   gemmAcc(nr, nb, nb, res.data(), Mi, x, 1);
@@ -455,6 +481,7 @@ static void gradientQuadratureAndResidual(Problem& P) {
     const int nq = B.ref.nq, nb = B.ref.nb;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
+      if (!needed(B, e, 1)) continue;
       Real vals[216 * kMaxVar];
       interp(nv, nb, nq, &B.coef[size_t(e) * nv * nb], B.ref.phi.data(), vals);
       Real* Q = &B.qvg[size_t(e) * nr * nq * d];
@@ -471,6 +498,7 @@ static void gradientQuadratureAndResidual(Problem& P) {
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < int64_t(P.interior.size()); ++i) {
     const Face& F = P.interior[i];
+    if (!faceNeeded(P, F, 1)) continue;
     PointVar L[64], R[64];
     trace(P, F.bl, F.el, F.fl, L); trace(P, F.br, F.er, F.fr, R);
     Block& BL = P.blocks[F.bl]; Block& BR = P.blocks[F.br];
@@ -503,6 +531,7 @@ static void gradientQuadratureAndResidual(Problem& P) {
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < int64_t(P.boundary.size()); ++i) {
     const Face& F = P.boundary[i];
+    if (!faceNeeded(P, F, 1)) continue;
     PointVar L[64];
     trace(P, F.bl, F.el, F.fl, L);
     Block& BL = P.blocks[F.bl];
@@ -523,6 +552,7 @@ static void gradientQuadratureAndResidual(Problem& P) {
     const int nq = B.ref.nq, nb = B.ref.nb, nf = B.ref.nface, nfl = nf * nfq;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
+      if (!needed(B, e, 1)) continue;
       const Real* QF = &B.qfvg[size_t(e) * nr * nfl];
       const Real* QV = &B.qvg[size_t(e) * nr * nq * d];
       Real* RV = &B.rvg[size_t(e) * nr * nb];
@@ -626,6 +656,7 @@ static void quadratureAndResidual(Problem& P) {
     const int nq = B.ref.nq, nb = B.ref.nb;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
+      if (!needed(B, e, 0)) continue;
       Real vals[216 * kMaxVar];
       std::vector<Real> gvals;
       interp(nv, nb, nq, &B.coef[size_t(e) * nv * nb], B.ref.phi.data(), vals);
@@ -671,6 +702,7 @@ static void quadratureAndResidual(Problem& P) {
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < int64_t(P.interior.size()); ++i) {
     const Face& F = P.interior[i];
+    if (!faceNeeded(P, F, 0)) continue;
     PointVar L[64], R[64];
     trace(P, F.bl, F.el, F.fl, L); trace(P, F.br, F.er, F.fr, R);
     Block& BL = P.blocks[F.bl]; Block& BR = P.blocks[F.br];
@@ -720,6 +752,7 @@ static void quadratureAndResidual(Problem& P) {
 #pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < int64_t(P.boundary.size()); ++i) {
     const Face& F = P.boundary[i];
+    if (!faceNeeded(P, F, 0)) continue;
     PointVar L[64];
     trace(P, F.bl, F.el, F.fl, L);
     Block& BL = P.blocks[F.bl];
@@ -760,6 +793,7 @@ static void quadratureAndResidual(Problem& P) {
     const int nq = B.ref.nq, nb = B.ref.nb, nfl = B.ref.nface * nfq;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
+      if (!needed(B, e, 0)) continue;
       const Real* QV = &B.qvol[size_t(e) * nv * nq * d];
       const Real* QF = &B.qface[size_t(e) * nv * nfl];
       Real* Rr = &B.res[size_t(e) * nv * nb];
@@ -846,6 +880,7 @@ static void project(Problem& P, const Real* cons) {
     const int nq = B.ref.nq, nb = B.ref.nb;
 #pragma omp parallel for schedule(static)
     for (int64_t e = 0; e < B.ne; ++e) {
+      if (!needed(B, e, 2)) continue;
       const Real* u = &cons[(off + size_t(e) * nq) * nv];
       std::vector<Real> t(size_t(nv) * nb, 0.0);
       for (int b = 0; b < nb; ++b)
@@ -879,7 +914,33 @@ static void project(Problem& P, const Real* cons) {
   P.hasState = true;
 }
 
-static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
+// Levels of the element-sample mode: the sampled elements (0), their face neighbours (1: their gradients when
+// the gradient pass runs, else their coefficients only) and, with the gradient pass, the neighbours of those (2).
+static void sampleLevels(Problem& P, int64_t count, const int64_t* sample) {
+  for (Block& B : P.blocks) B.level.assign(size_t(B.ne), 3);
+  std::vector<int64_t> first(P.blocks.size() + 1, 0);
+  for (size_t b = 0; b < P.blocks.size(); ++b) first[b + 1] = first[b] + P.blocks[b].ne;
+  for (int64_t i = 0; i < count; ++i) {
+    const int64_t g = sample[i];
+    if (g < 0 || g >= first.back()) throw std::runtime_error("sampled element index out of range");
+    const size_t b = size_t(std::upper_bound(first.begin(), first.end(), g) - first.begin()) - 1;
+    P.blocks[b].level[size_t(g - first[b])] = 0;
+  }
+  const int rings = P.gradientPass() ? 2 : 1;
+  for (int ring = 1; ring <= rings; ++ring) {
+    const int lvl = ring == rings ? 2 : 1;
+    std::vector<std::pair<int, int>> mark;
+    for (const Face& F : P.interior) {
+      const signed char l = P.blocks[F.bl].level[F.el], r = P.blocks[F.br].level[F.er];
+      if (l < ring && r > lvl) mark.push_back({F.br, F.er});
+      if (r < ring && l > lvl) mark.push_back({F.bl, F.el});
+    }
+    for (const auto& [b, e] : mark) P.blocks[b].level[size_t(e)] = std::min<signed char>(P.blocks[b].level[size_t(e)], lvl);
+  }
+}
+
+static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags, int64_t sampleCount = 0,
+                       const int64_t* sample = nullptr) {
   auto P = std::make_unique<Problem>();
   const int faithful = flags & 1;
   P->refine = (flags & 2) == 0;
@@ -918,6 +979,12 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
     P->blocks.push_back(std::move(B));
   }
   if (P->blocks.empty()) throw std::runtime_error("mesh has no elements");
+  buildAdjacency(*P, *m);
+  if (sample) {
+    if (P->lean || P->av) throw std::runtime_error("the element-sample mode has no lean or artificial-viscosity form");
+    P->sampled = true;
+    sampleLevels(*P, sampleCount, sample);
+  }
   for (Block& B : P->blocks) {
     buildGeometry(*P, B, m->node_coordinate);
     P->totalElements += B.ne;
@@ -942,9 +1009,11 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags) {
     }
   }
   if (P->av) P->nodeAV.assign(size_t(m->node_count), 0.0);
-  buildAdjacency(*P, *m);
-  for (Face& F : P->interior) faceGeometry(*P, F, m->node_coordinate);
-  for (Face& F : P->boundary) faceGeometry(*P, F, m->node_coordinate);
+  const int faceLevel = P->gradientPass() ? 1 : 0;
+  for (Face& F : P->interior)
+    if (faceNeeded(*P, F, faceLevel)) faceGeometry(*P, F, m->node_coordinate);
+  for (Face& F : P->boundary)
+    if (faceNeeded(*P, F, faceLevel)) faceGeometry(*P, F, m->node_coordinate);
   P->dummy.assign(P->boundary.size() * size_t(P->nfq()), PointVar{});
   P->relErr.assign(P->nv, 0.0);
   return P.release();
@@ -972,6 +1041,23 @@ const char* orc_last_error() { return g_orc_error.c_str(); }
 void* orc_create(const sdg_mesh* mesh, const sdg_config* config, int flags) {
   try {
     return orc::create(mesh, config, flags);
+  } catch (const std::exception& e) {
+    g_orc_error = e.what();
+    return nullptr;
+  }
+}
+
+// Element-sample mode (test infrastructure for meshes too large for the long-double build): only the residual
+// of the `count` elements listed (global indices in block order) is evaluated, with exactly the arithmetic of
+// the full evaluation -- a residual is local to an element and its face neighbours, so on the sampled elements
+// it equals the full evaluation's.  Geometry, inverses and the projection of the initial state are computed
+// only where that residual needs them.  Supports the initial state, the boundary state and orc_residual_point
+// (zeros outside the sample); stepping, dt and relative errors are refused.
+void* orc_create_sampled(const sdg_mesh* mesh, const sdg_config* config, int flags, int64_t count,
+                         const int64_t* elements) {
+  try {
+    if (!elements || count <= 0) throw std::runtime_error("empty element sample");
+    return orc::create(mesh, config, flags, count, elements);
   } catch (const std::exception& e) {
     g_orc_error = e.what();
     return nullptr;
@@ -1073,6 +1159,7 @@ int orc_get_state_modal(void* h, double* out) {
 
 int orc_calculate_delta_time(void* h, double cfl, double* dt) {
   orc::Problem& P = *static_cast<orc::Problem*>(h);
+  if (P.sampled) return 1;
   orc::Real best = 1.79769313486231570e308;
   for (const auto& B : P.blocks) {
     const int nq = B.ref.nq, nb = B.ref.nb;
@@ -1095,6 +1182,7 @@ int orc_calculate_delta_time(void* h, double cfl, double* dt) {
 
 int orc_step(void* h, int n, double dt) {
   orc::Problem& P = *static_cast<orc::Problem*>(h);
+  if (P.sampled) return 1;
   for (int i = 0; i < n; ++i) orc::step(P, orc::Real(dt));
   return 0;
 }
@@ -1102,7 +1190,7 @@ int orc_step(void* h, int n, double dt) {
 // One RK stage (0 .. stages-1) of a step; the last stage also evaluates the step's relative error.
 int orc_stage(void* h, int s, double dt) {
   orc::Problem& P = *static_cast<orc::Problem*>(h);
-  if (s < 0 || s > P.rk) return 1;
+  if (s < 0 || s > P.rk || P.sampled) return 1;
   orc::stage(P, s, orc::Real(dt));
   if (s == P.rk) orc::relativeError(P);
   return 0;
@@ -1124,6 +1212,10 @@ int orc_residual_point(void* h, double* out) {
   for (auto& B : P.blocks) {
     const int nb = B.ref.nb, nq = B.ref.nq, nv = P.nv;
     for (int64_t e = 0; e < B.ne; ++e) {
+      if (!orc::needed(B, e, 0)) {
+        std::fill(out + (off + size_t(e) * nq) * nv, out + (off + size_t(e + 1) * nq) * nv, 0.0);
+        continue;
+      }
       std::vector<orc::Real> du(size_t(nv) * nb), tmp(size_t(nq) * nv);
       orc::applyMinv(P, B, e, nv, &B.res[size_t(e) * nv * nb], du.data());
       orc::interp(nv, nb, nq, du.data(), B.ref.phi.data(), tmp.data());

@@ -10,7 +10,7 @@ from ._abi import (ADIABATIC_NONSLIP_WALL, ADIABATIC_SLIP_WALL, BR1, BR2, CENTRA
                    ISOTHERMAL_NONSLIP_WALL, LAX_FRIEDRICHS, NAVIER_STOKES, PERIODIC, PRESSURE_OUTFLOW, QUADRANGLE,
                    RIEMANN_FARFIELD, ROE, SHOCK_NONE, ARTIFICIAL_VISCOSITY, SOURCE_BOUSSINESQ, SOURCE_NONE, SSPRK3, TRANSPORT_CONSTANT,
                    TETRAHEDRON, TRANSPORT_NONE, TRANSPORT_SUTHERLAND, TRIANGLE, VELOCITY_INFLOW, VISCOUS_NONE, SdgError)
-from .solver import (INITIAL_FUNCTION, INITIAL_LAST_STEP, INITIAL_SPECIFIC_FILE, Batch, GpuSolver, Mesh, System,
-                     make_config)
+from .solver import (BOUNDARY_STEADY, BOUNDARY_TIME_VARYING, INITIAL_FUNCTION, INITIAL_LAST_STEP,
+                     INITIAL_SPECIFIC_FILE, Batch, GpuSolver, Mesh, System, make_config)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

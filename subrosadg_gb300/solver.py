@@ -467,6 +467,8 @@ class Batch:
 # InitialConditionEnum (src/Utils/Enum.cpp): the driver's function, a given raw-binary file, or the last written
 # step of the same run (raw/{prefix}_{iteration_start}.zst)
 INITIAL_FUNCTION, INITIAL_SPECIFIC_FILE, INITIAL_LAST_STEP = 0, 1, 2
+# BoundaryTimeEnum (src/Utils/Enum.cpp:102-105)
+BOUNDARY_STEADY, BOUNDARY_TIME_VARYING = 0, 1
 
 
 class System:
@@ -477,8 +479,9 @@ class System:
 
     def __init__(self, dimension, polynomial_order, equation=_abi.EULER, convective_flux=_abi.HLLC,
                  viscous_flux=_abi.VISCOUS_NONE, time_integration=_abi.SSPRK3, device=0,
-                 initial_condition_kind=INITIAL_FUNCTION):
+                 initial_condition_kind=INITIAL_FUNCTION, boundary_time=BOUNDARY_STEADY):
         self.dimension = dimension
+        self.boundary_time = boundary_time  # SolveControl's BoundaryTimeEnum
         self.cfg = dict(polynomial_order=polynomial_order, equation=equation, convective_flux=convective_flux,
                         viscous_flux=viscous_flux, time_integration=time_integration)
         self.device = device
@@ -488,7 +491,9 @@ class System:
         self.delta_time = 0.0
         self.solver = None
         self.initial_condition = None   # callable(coords[n,3]) -> primitive[n, d+2]
-        self.boundary_condition = None  # callable(coords[n,3], physical[n]) -> primitive[n, d+2]
+        # callable(coords[n,3], physical[n]) -> primitive[n, d+2]; with BOUNDARY_TIME_VARYING
+        # callable(coords[n,3], time, physical[n]) (the reference's TimeVarying signature)
+        self.boundary_condition = None
         self.initial_condition_kind = initial_condition_kind
         self.initial_condition_file = None
         self.initial_condition_lower_order = False
@@ -547,6 +552,11 @@ class System:
     def synchronize(self):
         self.solver = GpuSolver(self.mesh, make_config(**self.cfg), self.device)
 
+    def _boundary_primitive(self, pts, physical, time):
+        if self.boundary_time == BOUNDARY_TIME_VARYING:
+            return self.boundary_condition(pts, time, physical)
+        return self.boundary_condition(pts, physical)
+
     def _raw_path(self, step):
         return os.path.join(self.output_directory, "raw", f"{self.output_file_name_prefix}_{step}.zst")
 
@@ -584,10 +594,11 @@ class System:
         else:
             pts = s.volume_points()
             s.initialize_primitive(self.initial_condition(pts[:, : self.dimension]))
+        bpts = bphys = None
         if s.counts.boundary_face_count:
             bpts, phys = s.boundary_points()
-            nfq = s.counts.face_point_count
-            s.set_boundary_primitive(self.boundary_condition(bpts[:, : self.dimension], np.repeat(phys, nfq)))
+            bpts, bphys = bpts[:, : self.dimension], np.repeat(phys, s.counts.face_point_count)
+            s.set_boundary_primitive(self._boundary_primitive(bpts, bphys, 0.0))
         if self.delta_time == 0.0:
             self.delta_time = s.calculateDeltaTime(self.cfl)
         error_file = None
@@ -599,9 +610,15 @@ class System:
                 s.writeRawBinary(self._raw_path(0))
                 error_file.write(self._variable_list() + "\n" + self._line(0.0, np.zeros(s.nv)) + "\n")
         io_interval = self.io_interval or self.iteration_end
+        iteration = 0  # TimeIntegration::iteration_ (TimeIntegration.cpp:37): 0 until a step has been taken
         try:
             for i in range(self.iteration_start + 1, self.iteration_end + 1):
+                if self.boundary_time == BOUNDARY_TIME_VARYING and bpts is not None:
+                    # Solver::updateBoundaryVariable at the start of each step, at time iteration_ * dt
+                    # (TimeIntegration.cpp:333-335, BoundaryCondition.cpp:29-74)
+                    s.set_boundary_primitive(self._boundary_primitive(bpts, bphys, iteration * self.delta_time))
                 err = s.stepSolver(self.delta_time).copy()
+                iteration = i
                 self.error_history.append((i * self.delta_time, err))
                 if error_file is not None:
                     if i % io_interval == 0:

@@ -43,7 +43,8 @@ def test_bounded_wait_runs_out_and_is_reported(graph):
     rc = lib.sdg_step(g.h, 1, dt)
     assert rc == SDG_ERR_TIMEOUT, (rc, lib.sdg_last_error(g.h))
     assert b"timed out" in lib.sdg_last_error(g.h)
-    assert lib.sdg_synchronize(g.h) == 0  # the stream and the context are still healthy
+    # the timeout is sticky on this handle (its state is no longer a step's result)
+    assert lib.sdg_step(g.h, 1, dt) == SDG_ERR_TIMEOUT
     g.close()
     _normal_step_matches_oracle(mesh, cfg, prim, dt)
 

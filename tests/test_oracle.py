@@ -240,3 +240,38 @@ def test_lean_baseline_computes_the_same_scheme(case):
         o.step(dt, steps)
     a, b = f.state_point(), l.state_point()
     assert np.linalg.norm(a - b) <= 1e-12 * np.linalg.norm(a)
+
+
+@pytest.mark.parametrize("case", [lambda: cases.tgv_case(n=5, p=3),
+                                  lambda: cases.kh_case(n=7, p=3, viscous=sdg.BR2, mu=2e-3),
+                                  lambda: cases.tgv_case(n=4, p=2, viscous=sdg.BR1, mu=0.02),
+                                  lambda: cases.channel_case(p=2, viscous=sdg.BR2, mu=0.01, conditions=(
+                                      sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_NONSLIP_WALL,
+                                      sdg.VELOCITY_INFLOW))],
+                         ids=["tgv-euler", "kh-hybrid-br2", "tgv-br1", "channel-walls-br2"])
+@pytest.mark.parametrize("faithful", [False, True])
+def test_element_sample_mode_equals_full_evaluation(case, faithful):
+    """The oracle's element-sample mode (the truth of the stated-size GPU tests) gives the full evaluation's
+    residual bit for bit on the sampled elements and zeros elsewhere."""
+    mesh, cfg, prim, bprim, _, _ = case()
+    full = Oracle(mesh, cfg, faithful=faithful)
+    pts = full.volume_points()
+    sample = np.sort(np.random.default_rng(5).choice(full.elements, 7, replace=False))
+    part = Oracle(mesh, cfg, faithful=faithful, sample=sample)
+    for o in (full, part):
+        o.initialize_primitive(prim(pts))
+        if o.boundary:
+            bp, ph = full.boundary_points()
+            o.set_boundary_primitive(bprim(bp, np.repeat(ph, full.nfq)))
+    rf, rs = full.residual_point(), part.residual_point()
+    g = sdg.GpuSolver(mesh, cfg, device=-1)
+    c = g.counts
+    rows, off, first = np.zeros(len(rf), bool), 0, 0
+    for b in range(c.block_count):
+        ne, nq = c.block_element_count[b], c.block_volume_point_count[b]
+        for e in sample[(sample >= first) & (sample < first + ne)] - first:
+            rows[off + e * nq: off + (e + 1) * nq] = True
+        off, first = off + ne * nq, first + ne
+    assert np.array_equal(rs[rows], rf[rows])
+    assert not rs[~rows].any()
+    assert part.lib.orc_step(part.h, 1, 1e-3) != 0  # stepping is refused in the sample mode
