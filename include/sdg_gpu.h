@@ -333,6 +333,14 @@ int sdg_get_node_artificial_viscosity(sdg_handle* handle, double* out);
  * viscosity value per mesh node (zero).  Needs libzstd.so.1 at run time (else SDG_ERR_UNSUPPORTED).
  * lower_order = 1 reads a file written at order P-1 into the leading coefficients (SpecificFile). */
 int sdg_write_raw_binary(sdg_handle* handle, const char* path);
+/* The caller's boundary-face order for the boundary block of raw-binary files: faces[k] = (element type,
+ * element index within its type, local face) of the caller's k-th boundary face, every boundary face once.
+ * The reference writes that block in its own adjacency order (the boundary entries of
+ * AdjacencyElementMesh::element_, src/Mesh/Adjacency.cpp:466-485, written by src/View/RawBinary.cpp:120-154);
+ * a shim passes that order here (parent_index_each_type_, adjacency_sequence_in_parent_ and the parent's type
+ * of each boundary adjacency element) so that the reference's View reads the file unchanged.  Without it the
+ * block follows this library's boundary-face order. */
+int sdg_set_boundary_face_order(sdg_handle* handle, int64_t count, const int32_t* faces);
 int sdg_read_raw_binary(sdg_handle* handle, const char* path, int32_t lower_order);
 
 /* ---- launch shapes: CUDA-graph replay and the autotuner -------------------------------------------

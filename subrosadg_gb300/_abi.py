@@ -172,6 +172,7 @@ SIGNATURES = {
     "sdg_surface_force": (c_int32, [c_void_p, c_int32, _p_double]),
     "sdg_surface_force_cotangent": (c_int32, [c_void_p, c_int32, _p_double, _p_double]),
     "sdg_write_raw_binary": (c_int32, [c_void_p, c_char_p]),
+    "sdg_set_boundary_face_order": (c_int32, [c_void_p, c_int64, _p_int32]),
     "sdg_read_raw_binary": (c_int32, [c_void_p, c_char_p, c_int32]),
     "sdg_set_graph": (c_int32, [c_void_p, c_int32]),
     "sdg_set_wait_check": (c_int32, [c_void_p, c_uint32, c_uint32]),

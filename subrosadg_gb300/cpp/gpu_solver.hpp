@@ -29,9 +29,11 @@ namespace sdg_cpp {
 
 // Compile-time configuration, the runtime-free part of the reference's SimulationControl
 // (src/Solver/SimulationControl.cpp:1197-1279); values are the reference's enum values (src/Utils/Enum.cpp).
+// BoundaryTime: 0 steady, 1 time-varying ghost states (BoundaryTimeEnum, src/Utils/Enum.cpp:102-105).
 template <int Dimension, int PolynomialOrder, int Equation, int ConvectiveFlux, int ViscousFlux = SDG_VISCOUS_NONE,
-          int TimeIntegration = SDG_SSPRK3>
+          int TimeIntegration = SDG_SSPRK3, int BoundaryTime = 0>
 struct Control {
+  static constexpr int kBoundaryTime = BoundaryTime;
   static constexpr int kDimension = Dimension;
   static constexpr int kPolynomialOrder = PolynomialOrder;
   static constexpr int kEquationModel = Equation;
@@ -136,11 +138,14 @@ class GpuSolver {
     if (handle_) sdg_destroy(handle_);
   }
 
+  // The driver's boundary state: boundary(x, time, physical index) (time 0 and unused for steady states).
+  using BoundaryFunction = std::function<Primitive(const Point&, double, int)>;
+
   // Solver::initializeSolver (src/Solver/InitialCondition.cpp:85-149): build the problem, then the initial
   // state from the driver's primitive function at the volume points and the ghost states at the boundary
-  // points (boundary(x, physical index)).
+  // points at time 0.
   void initializeSolver(const Mesh& mesh, const PhysicalModel& pm, const std::function<Primitive(const Point&)>& ic,
-                        const std::function<Primitive(const Point&, int)>& boundary = {}, int device = 0) {
+                        const BoundaryFunction& boundary = {}, int device = 0) {
     const sdg_mesh m = mesh.view();
     sdg_config c{};
     c.polynomial_order = SC::kPolynomialOrder;
@@ -166,17 +171,28 @@ class GpuSolver {
       for (int v = 0; v < nv; ++v) prim[size_t(q) * nv + v] = p[v];
     }
     check(sdg_set_initial_primitive(handle_, prim.data()), handle_, "sdg_set_initial_primitive");
-    if (counts_.boundary_face_count > 0 && boundary) {
-      const int64_t nb = counts_.boundary_point_count;
-      std::vector<double> bx(size_t(nb) * 3), bp(size_t(nb) * nv);
-      std::vector<int32_t> phys(size_t(counts_.boundary_face_count));
-      check(sdg_boundary_point_coordinate(handle_, bx.data(), phys.data()), handle_, "sdg_boundary_point_coordinate");
-      for (int64_t q = 0; q < nb; ++q) {
-        const Primitive p = boundary({bx[q * 3], bx[q * 3 + 1], bx[q * 3 + 2]}, phys[q / counts_.face_point_count]);
-        for (int v = 0; v < nv; ++v) bp[size_t(q) * nv + v] = p[v];
-      }
-      check(sdg_set_boundary_primitive(handle_, bp.data()), handle_, "sdg_set_boundary_primitive");
+    boundary_ = boundary;
+    if (counts_.boundary_face_count > 0 && boundary_) {
+      bx_.resize(size_t(counts_.boundary_point_count) * 3);
+      bphys_.resize(size_t(counts_.boundary_face_count));
+      check(sdg_boundary_point_coordinate(handle_, bx_.data(), bphys_.data()), handle_, "sdg_boundary_point_coordinate");
+      updateBoundaryVariable(0.0);
     }
+  }
+
+  // Solver::updateBoundaryVariable (src/Solver/BoundaryCondition.cpp:29-74): ghost states of the boundary
+  // points at `time`.
+  void updateBoundaryVariable(double time) {
+    if (bx_.empty()) return;
+    const int nv = SC::kConservedVariableNumber;
+    const int64_t nb = counts_.boundary_point_count;
+    std::vector<double> bp(size_t(nb) * nv);
+    for (int64_t q = 0; q < nb; ++q) {
+      const Primitive p = boundary_({bx_[q * 3], bx_[q * 3 + 1], bx_[q * 3 + 2]}, time,
+                                    bphys_[q / counts_.face_point_count]);
+      for (int v = 0; v < nv; ++v) bp[size_t(q) * nv + v] = p[v];
+    }
+    check(sdg_set_boundary_primitive(handle_, bp.data()), handle_, "sdg_set_boundary_primitive");
   }
 
   // Solver::calculateDeltaTime (TimeIntegration.cpp:104-131).
@@ -213,6 +229,9 @@ class GpuSolver {
  private:
   sdg_handle* handle_ = nullptr;
   sdg_counts counts_{};
+  BoundaryFunction boundary_;
+  std::vector<double> bx_;       // boundary point coordinates
+  std::vector<int32_t> bphys_;   // physical group of each boundary face
 };
 
 // The reference's System<SC> facade over GpuSolver<SC> (src/Utils/SystemControl.cpp:42-236).
@@ -249,7 +268,7 @@ class System {
     io_interval_ = io_interval;
   }
   void setInitialCondition(std::function<Primitive(const Point&)> f) { ic_ = std::move(f); }
-  void setBoundaryCondition(std::function<Primitive(const Point&, int)> f) { bc_ = std::move(f); }
+  void setBoundaryCondition(typename GpuSolver<SC>::BoundaryFunction f) { bc_ = std::move(f); }
 
   // System::synchronize (SystemControl.cpp:146-157): problem setup and the initial state on `device`.
   void synchronize(int device = 0) { solver_.initializeSolver(mesh_, physical_model_, ic_, bc_, device); }
@@ -270,9 +289,12 @@ class System {
       error << variableList() << '\n' << line(0.0, {}) << '\n';
     }
     int step = time_integration_.iteration_start;
+    int iteration = 0;  // TimeIntegration::iteration_ (TimeIntegration.cpp:37): 0 until a step has been taken
     for (int i = time_integration_.iteration_start + 1; i <= time_integration_.iteration_end; ++i) {
+      // BoundaryTimeEnum::TimeVarying: ghost states at the start of each step (TimeIntegration.cpp:333-335)
+      if constexpr (SC::kBoundaryTime == 1) solver_.updateBoundaryVariable(iteration * dt);
       solver_.stepSolver(time_integration_);
-      step = i;
+      step = iteration = i;
       if (error.is_open()) {
         if (i % io == 0) solver_.writeRawBinary(rawPath(i));
         error << line(i * dt, solver_.relative_error_) << '\n';
@@ -308,7 +330,7 @@ class System {
   TimeIntegration time_integration_;
   GpuSolver<SC> solver_;
   std::function<Primitive(const Point&)> ic_;
-  std::function<Primitive(const Point&, int)> bc_;
+  typename GpuSolver<SC>::BoundaryFunction bc_;
   std::filesystem::path output_directory_;
   std::string prefix_;
   int io_interval_ = 0;

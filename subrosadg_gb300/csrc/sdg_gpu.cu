@@ -1159,6 +1159,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       h->bphys.push_back(f.physical);
       h->boundaryParent.push_back(f.left.block);
       h->boundaryParent.push_back(f.left.element);
+      h->boundaryParent.push_back(f.left.face);
     }
     // canonical adjacency tuples
     {

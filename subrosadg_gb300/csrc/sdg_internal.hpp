@@ -129,7 +129,8 @@ struct sdg_handle {
   int* facePerm = nullptr;        // [3][nfq] right point of left point j at rotation r (triangular faces)
   std::vector<int32_t> adjInterior, adjBoundary;
   std::vector<double> bcoord; std::vector<int32_t> bphys;
-  std::vector<int32_t> boundaryParent;  // per boundary face: (block, element) of its parent
+  std::vector<int32_t> boundaryParent;  // per boundary face: (block, element, local face) of its parent
+  std::vector<int64_t> boundaryOrder;   // sdg_set_boundary_face_order: library boundary face of each caller position
   int64_t nodeCount = 0;                // mesh nodes (raw-binary files carry one value per node)
   double* scratch = nullptr;       // point-layout conversion buffer [volume_points][nv]
   int64_t volumePoints = 0;

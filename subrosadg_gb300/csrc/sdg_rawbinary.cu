@@ -6,8 +6,9 @@
 // Payload, all FP64, in the reference's block order (2D: triangles, quadrangles; 3D: hexahedra):
 //   per element: the modal coefficients, column-major (d+2) x Nb; for Navier-Stokes then the gradient
 //                coefficients, column-major (d+2)*d x Nb (row v*d + k)
-//   per boundary face: the parent element's coefficients (and gradient), in this library's boundary-face
-//                order (the reference's is gmsh/unordered_map order)
+//   per boundary face: the parent element's coefficients (and gradient), in the caller's boundary-face order
+//                (sdg_set_boundary_face_order: the reference's own adjacency order, Adjacency.cpp:466-485) or,
+//                without one, in this library's
 //   per mesh node: the artificial viscosity of the current state (zero without shock capturing)
 // libzstd is loaded at run time (libzstd.so.1, its public C API); without it the calls return
 // SDG_ERR_UNSUPPORTED.
@@ -15,7 +16,9 @@
 
 #include <cmath>
 #include <cstdio>
+#include <array>
 #include <cstring>
+#include <map>
 #include <fstream>
 #include <iterator>
 #include <mutex>
@@ -133,9 +136,11 @@ int sdg_write_raw_binary(sdg_handle* h, const char* path) {
       }
       moff += size_t(B.ne) * nv * B.nb;
     }
-    // boundary faces: the parent's coefficients (and gradient), in boundary-face order
-    for (int64_t i = 0; i < h->nBoundary; ++i) {
-      const int32_t* r = &h->boundaryParent[size_t(i) * 2];
+    // boundary faces: the parent's coefficients (and gradient), in the caller's boundary-face order when one
+    // was given (sdg_set_boundary_face_order), else in this library's
+    for (int64_t k = 0; k < h->nBoundary; ++k) {
+      const int64_t i = h->boundaryOrder.empty() ? k : h->boundaryOrder[size_t(k)];
+      const int32_t* r = &h->boundaryParent[size_t(i) * 3];
       const DevBlock& B = h->blocks[r[0]];
       const double* c = &modal[modalOffset[r[0]] + size_t(r[1]) * nv * B.nb];
       payload.insert(payload.end(), c, c + size_t(nv) * B.nb);
@@ -165,6 +170,31 @@ int sdg_write_raw_binary(sdg_handle* h, const char* path) {
   } catch (const Failure& e) {
     return rawFail(h, e.code, e.what());
   }
+  return SDG_OK;
+}
+
+int sdg_set_boundary_face_order(sdg_handle* h, int64_t count, const int32_t* faces) {
+  if (!h || count != h->nBoundary || (count > 0 && !faces)) {
+    if (h) h->err = "the order must list every boundary face once";
+    return SDG_ERR_INVALID_ARGUMENT;
+  }
+  std::map<std::array<int32_t, 3>, int64_t> index;  // (element type, element, local face) -> library face
+  for (int64_t i = 0; i < h->nBoundary; ++i) {
+    const int32_t* r = &h->boundaryParent[size_t(i) * 3];
+    index[{h->blocks[r[0]].type, r[1], r[2]}] = i;
+  }
+  std::vector<int64_t> order(static_cast<size_t>(count));
+  std::vector<char> seen(static_cast<size_t>(count), 0);
+  for (int64_t k = 0; k < count; ++k) {
+    const auto it = index.find({faces[k * 3], faces[k * 3 + 1], faces[k * 3 + 2]});
+    if (it == index.end() || seen[size_t(it->second)]) {
+      h->err = "boundary face " + std::to_string(k) + " of the order is not a boundary face or is listed twice";
+      return SDG_ERR_INVALID_ARGUMENT;
+    }
+    seen[size_t(it->second)] = 1;
+    order[size_t(k)] = it->second;
+  }
+  h->boundaryOrder = std::move(order);
   return SDG_OK;
 }
 

@@ -313,6 +313,12 @@ class GpuSolver:
         """Solver::writeRawBinary: the reference's zstd raw-binary solution file."""
         self._chk(self.lib.sdg_write_raw_binary(self.h, str(path).encode()))
 
+    def set_boundary_face_order(self, faces):
+        """The caller's boundary-face order of the raw-binary boundary block: rows (element type, element index
+        within its type, local face), every boundary face once (the reference's adjacency order)."""
+        f = np.ascontiguousarray(faces, np.int32).reshape(-1, 3)
+        self._chk(self.lib.sdg_set_boundary_face_order(self.h, len(f), _ptr(f, _pi)))
+
     def read_raw_binary(self, path, lower_order=False):
         """Restart from a raw-binary file (LastStep; lower_order: SpecificFile written at order P-1)."""
         self._chk(self.lib.sdg_read_raw_binary(self.h, str(path).encode(), int(bool(lower_order))))

@@ -126,3 +126,42 @@ def test_raw_binary_carries_the_node_artificial_viscosity(tmp_path):
     av = s.node_artificial_viscosity()
     assert av.max() > 0
     np.testing.assert_array_equal(payload[-len(mesh.nodes):], av)
+
+
+@pytest.mark.parametrize("name,case", [
+    ("euler-channel-hybrid-p3", lambda: cases.channel_case(p=3, n=3, split=0.5, jitter=0.1)),
+    ("euler-tet-box-p2", lambda: cases.tet_box_case(p=2)),
+])
+def test_raw_binary_boundary_block_in_callers_order(tmp_path, name, case):
+    """The boundary block follows the caller's boundary-face order (the reference's adjacency order,
+    src/View/RawBinary.cpp:120-154) given by sdg_set_boundary_face_order: record k is the modal state of the
+    parent of the caller's k-th boundary face."""
+    s, dt, mesh = make(case())
+    s.stepSolver(dt, 1)
+    c = s.counts
+    _, bnd = s.adjacency()  # (type, element, face, physical, condition) per boundary face
+    order = bnd[np.random.default_rng(9).permutation(len(bnd))][:, :3]
+    s.set_boundary_face_order(order)
+    path = tmp_path / "ordered.zst"
+    s.writeRawBinary(path)
+    payload = decode(path)
+    nv = c.conserved_variable_count
+    modal = s.state_modal()
+    block_of = {c.block_element_type[k]: k for k in range(c.block_count)}
+    first, moff = {}, 0
+    pos = 0
+    for k in range(c.block_count):
+        first[k] = moff
+        moff += c.block_element_count[k] * nv * c.block_basis_count[k]
+    pos = moff  # Euler: the element block is the modal state itself
+    for t, e, _ in order:
+        k = block_of[t]
+        nb = c.block_basis_count[k]
+        np.testing.assert_array_equal(payload[pos:pos + nv * nb], modal[first[k] + e * nv * nb: first[k] + (e + 1) * nv * nb])
+        pos += nv * nb
+    assert pos == len(payload) - len(mesh.nodes)
+    # an order that lists a face twice is refused
+    bad = order.copy()
+    bad[1] = bad[0]
+    with pytest.raises(sdg.SdgError):
+        s.set_boundary_face_order(bad)

@@ -53,3 +53,55 @@ def test_outputs_and_last_step_restart(tmp_path):
     c.addInitialCondition(raw / "sod_1d_ceuler_10.zst")
     c.solve()
     np.testing.assert_allclose(c.solver.state_point(), final, rtol=1e-13, atol=1e-15)
+
+
+def test_time_varying_inflow_matches_oracle():
+    """BoundaryTimeEnum::TimeVarying (src/Solver/TimeIntegration.cpp:333-335, BoundaryCondition.cpp:29-74): the
+    System re-evaluates the ghost states at the start of every step at time iteration_ * dt (iteration_ is 0
+    before the first step), here a pulsating velocity inflow into a slip-walled channel with an outflow; the
+    oracle steps with the same per-step ghost states."""
+    from oracle.orc import Oracle
+    from tests import cases
+    conditions = (sdg.ADIABATIC_SLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW)
+    mesh, cfg, ic, _, dt, _ = cases.channel_case(p=2, flux=sdg.HLLC, n=4, conditions=conditions)
+    steps = 12
+
+    def bc(x, t, phys):
+        out = np.zeros((len(x), 4))
+        out[:, 0] = 1.0
+        out[:, 1] = np.where(phys == 4, 0.4 * (1.0 + 0.5 * np.sin(300.0 * t)) * (1.0 + 0.2 * x[:, 1]), 0.0)
+        out[:, 3] = 1.0 / cases.R_GAS
+        return out
+
+    system = sdg.System(2, 2, sdg.EULER, sdg.HLLC, boundary_time=sdg.BOUNDARY_TIME_VARYING)
+    system.setMesh(mesh)
+    system.setThermodynamicModel(cases.CP, cases.CV)
+    system.setTimeIntegration(1.0, (0, steps))
+    system.setDeltaTime(dt)
+    system.initial_condition = lambda x: ic(x)
+    system.boundary_condition = bc
+    system.synchronize()
+    system.solve()
+    got = system.solver.state_point()
+
+    o = Oracle(mesh, cfg, faithful=False)
+    o.initialize_primitive(ic(o.volume_points()))
+    bpts, phys = o.boundary_points()
+    phys = np.repeat(phys, o.nfq)
+    for i in range(1, steps + 1):
+        o.set_boundary_primitive(bc(bpts, (i - 1) * dt, phys))
+        o.step(dt)
+    ref = o.state_point()
+    pv = [np.linalg.norm(got[:, v] - ref[:, v]) / np.linalg.norm(ref[:, v]) for v in range(4)]
+    assert max(pv) <= 1e-10, pv
+    # the ghost states did change: a steady run at the time-0 inflow ends elsewhere
+    s = sdg.System(2, 2, sdg.EULER, sdg.HLLC)
+    s.setMesh(mesh)
+    s.setThermodynamicModel(cases.CP, cases.CV)
+    s.setTimeIntegration(1.0, (0, steps))
+    s.setDeltaTime(dt)
+    s.initial_condition = lambda x: ic(x)
+    s.boundary_condition = lambda x, phys: bc(x, 0.0, phys)
+    s.synchronize()
+    s.solve()
+    assert np.linalg.norm(s.solver.state_point() - ref) > 1e-6 * np.linalg.norm(ref)
