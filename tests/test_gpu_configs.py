@@ -15,7 +15,8 @@ Tolerances (the path computes in FP64):
     its face neighbours), and the reference's FP64 arithmetic is the faithful double oracle on the same sample.
     At Mach 0.1 the residual is a small difference of O(p0) fluxes, so this problem's own conditioning puts the
     reference's FP64 residual 1e-9..1e-8 away from the truth at these sizes;
-  * state after N steps per conserved variable, relative L2 against the double oracle <= 1e-10 (the whole mesh);
+  * state after N steps per conserved variable, L2 difference against the double oracle <= 1e-10 of the
+    variable's scale (its own norm; for a momentum component the momentum's norm), over the whole mesh;
   * relative error of the last step <= 1e-9; dt <= 1e-13.
 States and residuals are compared at the volume points (the GPU path stores nodal values, the oracle the
 reference's modal coefficients).
@@ -38,6 +39,19 @@ def rel_l2(a, b):
 
 def per_var(a, b):
     return [rel_l2(a[:, v], b[:, v]) for v in range(b.shape[1])]
+
+
+def per_var_scaled(a, b):
+    """Per conserved variable, the L2 difference over the variable's natural scale: its own norm, and for the
+    momentum components the norm of the whole momentum (a component that is zero in the initial state, as the
+    Taylor-Green vortex's rho w, carries only round-off of the momentum's size)."""
+    d = b.shape[1] - 2
+    mom = np.linalg.norm(b[:, 1:1 + d])
+    out = []
+    for v in range(b.shape[1]):
+        scale = max(np.linalg.norm(b[:, v]), mom if 1 <= v <= d else 0.0, 1e-300)
+        out.append(float(np.linalg.norm(a[:, v] - b[:, v]) / scale))
+    return out
 
 
 def sample_rows(g, sample):
@@ -85,7 +99,7 @@ def run(mesh, cfg, prim, steps, dt=None, seed=0):
     for _ in range(steps):
         eg = g.stepSolver(dt).copy()
     o.step(dt, steps)
-    pv = per_var(g.state_point(), o.state_point())
+    pv = per_var_scaled(g.state_point(), o.state_point())
     assert max(pv) <= 1e-10, pv
     np.testing.assert_allclose(eg, o.relative_error(), rtol=1e-9, atol=1e-15)
     return err, ref_err, pv
