@@ -264,6 +264,21 @@ def bench_batched(args, device, torch, max_elements=None):
     b.synchronize()
     ms_seq = _timed(torch, stream, lambda: b.step_sequential_async(1), steps)
     b.synchronize()
+    # how busy the GPU is in the sequential run: every launch bracketed by CUDA events (one step), summed over
+    # the instances, against the sequential step's wall time.  If batching only removed the idle gaps between
+    # kernels, ms_seq / busy would bound its gain.
+    import ctypes
+    kms, kn = (ctypes.c_double * 5)(), (ctypes.c_int64 * 5)()
+    for g in solvers:
+        g.lib.sdg_set_kernel_timing(g.h, 1)
+    b.step_sequential_async(1)
+    b.synchronize()
+    busy, launches_seq = 0.0, 0
+    for g in solvers:
+        g.lib.sdg_kernel_time(g.h, kms, kn)
+        busy += sum(kms)
+        launches_seq += sum(kn)
+        g.lib.sdg_set_kernel_timing(g.h, 0)
     dof_stages = sum(g.counts.degree_of_freedom_count * 3 for g in solvers)
     out = {
         "workload": f"{len(solvers)} independent 2D Kelvin-Helmholtz solves (Euler or NS BR2, LF, SSP-RK3)",
@@ -275,7 +290,9 @@ def bench_batched(args, device, torch, max_elements=None):
         "persistent_ctas_per_sm": c["persistent_ctas_per_sm"],
         "sequential": {"value": dof_stages * steps / (ms_seq * 1e-3), "ms_per_step": ms_seq / steps,
                        "launches_per_step": c["sequential_launches_per_step"],
-                       "mode": "plain per-instance launches, instance after instance, same stream and tiles"},
+                       "mode": "plain per-instance launches, instance after instance, same stream and tiles",
+                       "kernel_busy_ms_per_step": busy, "busy_fraction": busy / (ms_seq / steps),
+                       "gap_free_bound_speedup": (ms_seq / steps) / busy, "timed_launches": launches_seq},
         "speedup_vs_sequential": ms_seq / ms_batch,
         "setup_s": setup, "autotune_s": tune, "clocks": clocks.summary(),
     }

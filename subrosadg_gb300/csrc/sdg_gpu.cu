@@ -1030,13 +1030,23 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         B.minEdge[e] = minEdgeOf(b.type, nodes, vv);
       }
       if (bad) throw Failure(SDG_ERR_MESH, "inverted or degenerate element");
-      // axis-aligned affine tensor elements (structured boxes): every off-diagonal metric term is exactly
-      // zero, and the stage kernel skips those products (the same values)
+      // axis-aligned affine tensor elements (structured boxes): every off-diagonal metric term is zero up to
+      // the round-off of the Jacobian sums (|off| <= 1e-13 of the element's largest term); they are set to
+      // zero and the stage kernel skips those products
       B.diagMetric = B.kind == kTensor && B.affine;
-      for (int64_t e = 0; e < B.ne && B.diagMetric; ++e)
+      for (int64_t e = 0; e < B.ne && B.diagMetric; ++e) {
+        const double* g = &B.geomHost[size_t(e) * B.geomStride];
+        double big = 0.0;
+        for (int r = 0; r < B.dim * B.dim; ++r) big = std::max(big, std::fabs(g[r]));
         for (int r = 0; r < B.dim; ++r)
           for (int cc = 0; cc < B.dim; ++cc)
-            if (r != cc && B.geomHost[size_t(e) * B.geomStride + r * B.dim + cc] != 0.0) B.diagMetric = 0;
+            if (r != cc && std::fabs(g[r * B.dim + cc]) > 1e-13 * big) B.diagMetric = 0;
+      }
+      if (B.diagMetric)
+        for (int64_t e = 0; e < B.ne; ++e)
+          for (int r = 0; r < B.dim; ++r)
+            for (int cc = 0; cc < B.dim; ++cc)
+              if (r != cc) B.geomHost[size_t(e) * B.geomStride + r * B.dim + cc] = 0.0;
       if (B.kind == kTensor) {
         B.ops.build(B.n);
         buildTensorTables(B);

@@ -181,7 +181,7 @@ __device__ __forceinline__ int strideOf(int a) {
 }
 
 // Tensor-block stage tile: one thread per node, a.epb elements per CTA.  Shared memory (dynamic):
-// sU [epb][USTRIDE] | sF [epb][FSTRIDE] | sG [epb][DIM][NV][NB] | TensorTables | mbarrier | sRed [warps][NV].
+// sU [epb][USTRIDE] | sF [epb][FSTRIDE] | sG [epb][DIM][NV][NB] | TensorTables | mbarrier | [warps][NV] (spare).
 template <int DIM, int N>
 __device__ __forceinline__ uint64_t* tensorStageBarrier(int epb) {
   using S = TensorShape<DIM, N>;
@@ -205,7 +205,6 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
   double* sG = sF + epb * S::FSTRIDE;                               // [epb][DIM][NV][NB]
   TensorTables* T = reinterpret_cast<TensorTables*>(sG + epb * DIM * NV * NB);
   uint64_t* bar = reinterpret_cast<uint64_t*>(T + 1);
-  double* sRed = reinterpret_cast<double*>(bar + 1);                // [warps][NV]
 
   const int tid = threadIdx.x;
   const int64_t e0 = tile * epb;
@@ -432,21 +431,22 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
         }
         __syncthreads();
       }
-      // deterministic reduction: warp shuffle, then warps summed in order by thread v
-      const double* fin = sG + le * DIM * NV * NB + (DIM & 1) * NV * NB;
-      const int warp = tid >> 5, nwarp = (blockDim.x + 31) >> 5;
+      // deterministic reduction: warp v sums variable v's |rel| over the tile's nodes straight from shared
+      // memory (a strided pass per lane, then one shuffle tree), so each variable costs one warp's work
+      // instead of a shuffle tree in every warp
+      {
+        const int warp = tid >> 5, lane = tid & 31, nwarp = (blockDim.x + 31) >> 5;
+        const double* fin = sG + (DIM & 1) * NV * NB;
+        for (int v = warp; v < NV; v += nwarp) {
+          double x = 0.0;
+          for (int k = lane; k < ecount * NB; k += 32) {
+            const int te = k / NB;
+            x += fabs(fin[te * DIM * NV * NB + v * NB + (k - te * NB)]);
+          }
 #pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        double x = active ? fabs(fin[v * NB + node]) : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if ((tid & 31) == 0) sRed[warp * NV + v] = x;
-      }
-      __syncthreads();
-      if (tid < NV) {
-        double acc = 0.0;
-        for (int w = 0; w < nwarp; ++w) acc += sRed[w * NV + tid];
-        a.relerr[tile * NV + tid] = acc / double(NB);
+          for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+          if (lane == 0) a.relerr[tile * NV + v] = x / double(NB);
+        }
       }
     }
     if (a.doUpdate && active) {
