@@ -116,6 +116,14 @@ typedef struct sdg_mesh {
   const int32_t* line_node;           /* [line_count][2]                                            */
   int64_t tetrahedron_count;          /* 3D: tetrahedra (MeshModelEnum::Tetrahedron), gmsh vertex order */
   const int32_t* tetrahedron_node;    /* [tetrahedron_count][4]                                      */
+  /* Curved (high-order) geometry of 2D meshes, as the drivers' setOrder(P) makes it and
+     src/Mesh/ReadControl.cpp:243-256 reads it: geometry_order q in 2..5 (0 or 1: straight-sided) and, per
+     element, the node indices of its order-q Lagrange element in gmsh's node order (the corners first, equal
+     to the vertex lists above).  The Jacobians and face normals are then those of the order-q map at every
+     quadrature point (src/Mesh/Geometry.cpp:44-86, 102-127).                                          */
+  int32_t geometry_order;
+  const int32_t* triangle_geometry_node;   /* [triangle_count][(q+1)(q+2)/2], or NULL                  */
+  const int32_t* quadrangle_geometry_node; /* [quadrangle_count][(q+1)^2], or NULL                     */
 } sdg_mesh;
 
 /* ---- physics and numerics: the runtime form of the reference's SimulationControl -------------- */

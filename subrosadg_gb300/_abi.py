@@ -62,6 +62,9 @@ class SdgMesh(ctypes.Structure):
         ("line_node", _p_int32),
         ("tetrahedron_count", c_int64),
         ("tetrahedron_node", _p_int32),
+        ("geometry_order", c_int32),
+        ("triangle_geometry_node", _p_int32),
+        ("quadrangle_geometry_node", _p_int32),
     ]
 
 

@@ -119,6 +119,7 @@ AdjointState* adjoint(sdg_handle* h) {
   if (!h->hasState) throw Failure(SDG_ERR_STATE, "no state");
   if (h->adj) return h->adj;
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
+  if (h->curved) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives on curved (high-order) geometry are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   const bool gen = h->ph.incomp || h->ph.source;
   adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, gen, A->k);
@@ -625,6 +626,7 @@ ForceArgs forceInputs(sdg_handle* h, int physical, ForceInputs& in, bool pointOu
   ForceArgs a;
   std::memset(&a, 0, sizeof(a));
   a.face = h->face; a.faceGrad = h->faceGrad; a.conn = h->bconn; a.fgeo = h->bgeo; a.select = in.select;
+  a.fgeoPoint = h->curved ? 1 : 0;
   a.fw = in.fw; a.out = in.out; a.nface = h->nBoundary; a.n1d = h->n1d; a.ns = h->ns ? 1 : 0;
   return a;
 }

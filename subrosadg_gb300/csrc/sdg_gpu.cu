@@ -20,6 +20,7 @@
 #include <mutex>
 #include <set>
 
+#include "sdg_geometry.hpp"
 #include "sdg_internal.hpp"
 
 namespace sdg {
@@ -522,7 +523,7 @@ Rec gradRec(sdg_handle* h, DevBlock& B, int which) {
     GradArgs& a = r.ga;
     std::memset(&a, 0, sizeof(a));
     a.u = u; a.face = h->face; a.faceOther = h->faceOther; a.faceGrad = h->faceGrad; a.grad = g;
-    a.geom = B.geom; a.fmetric = B.fmetric; a.tables = B.tables; a.status = h->status;
+    a.geom = B.geom; a.fmetric = B.fmetric; a.fmetricPoint = B.curved; a.tables = B.tables; a.status = h->status;
     a.ne = B.ne; a.faceBase = B.faceBase; a.br2 = br2; a.epb = B.gepb;
     if (h->av) { a.av = 1; a.epsV = B.epsV; a.avTab = B.avTab; }
   } else {
@@ -530,7 +531,7 @@ Rec gradRec(sdg_handle* h, DevBlock& B, int which) {
     DenseGradArgs& a = r.da;
     std::memset(&a, 0, sizeof(a));
     a.u = u; a.face = h->face; a.faceOther = h->faceOther; a.faceGrad = h->faceGrad; a.grad = g;
-    a.geom = B.geom; a.fmetric = B.fmetric; a.tables = B.tables; a.status = h->status;
+    a.geom = B.geom; a.fmetric = B.fmetric; a.fmetricPoint = B.curved; a.tables = B.tables; a.status = h->status;
     a.ne = B.ne; a.faceBase = B.faceBase; a.br2 = br2; a.epb = B.gepb;
     if (h->av) { a.av = 1; a.epsV = B.epsV; a.avTab = B.avTab; }
   }
@@ -555,6 +556,7 @@ Rec faceRec(sdg_handle* h, int op) {
   f.face = h->face; f.other = h->faceOther; f.faceGrad = h->faceGrad; f.faceFlux = h->faceFlux;
   f.conn = bnd ? h->bconn : h->fconn; f.fgeo = bnd ? h->bgeo : h->fgeo; f.ghost = h->ghost;
   f.nface = bnd ? h->nBoundary : h->nInterior; f.n1d = h->n1d; f.ph = h->ph; f.perm = h->facePerm;
+  f.fgeoPoint = h->curved ? 1 : 0;
   r.units = (f.nface * h->nfq + kFaceThreads - 1) / kFaceThreads;
   return r;
 }
@@ -945,8 +947,13 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     if (h->dim == 1) {
       if (mesh->line_count > 0) mb.push_back({SDG_ELEMENT_LINE, mesh->line_count, mesh->line_node});
     } else if (h->dim == 2) {
-      if (mesh->triangle_count > 0) mb.push_back({SDG_ELEMENT_TRIANGLE, mesh->triangle_count, mesh->triangle_node});
-      if (mesh->quadrangle_count > 0) mb.push_back({SDG_ELEMENT_QUADRANGLE, mesh->quadrangle_count, mesh->quadrangle_node});
+      const int gq = mesh->geometry_order > 1 ? mesh->geometry_order : 1;
+      if (mesh->triangle_count > 0)
+        mb.push_back({SDG_ELEMENT_TRIANGLE, mesh->triangle_count, mesh->triangle_node,
+                      gq > 1 ? mesh->triangle_geometry_node : nullptr, gq});
+      if (mesh->quadrangle_count > 0)
+        mb.push_back({SDG_ELEMENT_QUADRANGLE, mesh->quadrangle_count, mesh->quadrangle_node,
+                      gq > 1 ? mesh->quadrangle_geometry_node : nullptr, gq});
     } else {
       if (mesh->tetrahedron_count > 0 && mesh->hexahedron_count > 0)
         throw Failure(SDG_ERR_UNSUPPORTED, "a mesh of tetrahedra and hexahedra needs pyramids, which are not built");
@@ -957,6 +964,12 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       if (mesh->hexahedron_count > 0) mb.push_back({SDG_ELEMENT_HEXAHEDRON, mesh->hexahedron_count, mesh->hexahedron_node});
     }
     if (mb.empty()) throw Failure(SDG_ERR_INVALID_ARGUMENT, "mesh has no elements of its dimension");
+    if (mesh->geometry_order > 1) {
+      if (mesh->dimension != 2) throw Failure(SDG_ERR_UNSUPPORTED, "curved (high-order) geometry is built for 2D meshes");
+      if (mesh->geometry_order > 5) throw Failure(SDG_ERR_INVALID_ARGUMENT, "geometry order must be 1..5");
+      for (const Block& b : mb)
+        if (!b.geometry) throw Failure(SDG_ERR_INVALID_ARGUMENT, "geometry_order > 1 needs the geometry nodes of every block");
+    }
     for (const Block& b : mb) if (!b.vertex) throw Failure(SDG_ERR_INVALID_ARGUMENT, "null element array");
     Adjacency adj;
     try { adj = buildAdjacency(*mesh, mb); } catch (const std::runtime_error& e) { throw Failure(SDG_ERR_MESH, e.what()); }
@@ -967,8 +980,10 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     const double tol = 1e-12 * std::max(1.0, extent);
     size_t stateOff = 0, pointOff = 0;
     int64_t faceSlots = 0, relParts = 0;
+    std::vector<CurvedMap2d> blockMap(mb.size());  // the order-q map of each curved block
     for (const Block& b : mb) {
       DevBlock B;
+      CurvedMap2d& curved = blockMap[size_t(&b - mb.data())];
       B.type = b.type; B.dim = typeDim(b.type); B.p = h->p; B.ne = b.count; B.nface = typeFaces(b.type);
       B.kind = (b.type == SDG_ELEMENT_TRIANGLE || b.type == SDG_ELEMENT_TETRAHEDRON ||
                 (b.type == SDG_ELEMENT_QUADRANGLE && h->p == 1))
@@ -982,6 +997,27 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       B.affine = 1;
       for (int64_t e = 0; e < b.count && B.affine; ++e)
         if (!isAffine(b.type, nodes, b.vertex + e * typeVertices(b.type), tol)) B.affine = 0;
+      // curved elements: some geometry node off the straight (first-order) map of its element's vertices
+      const int ngeo = b.geometry ? gmshNodeCount(b.type, b.geometryOrder) : 0;
+      if (b.geometry) {
+        curved.init(b.type, b.geometryOrder);
+        const int nvt = typeVertices(b.type);
+        for (int64_t e = 0; e < b.count && !B.curved; ++e) {
+          const int32_t* g = b.geometry + e * ngeo;
+          for (int k = 0; k < nvt; ++k)
+            if (g[k] != b.vertex[e * nvt + k]) throw Failure(SDG_ERR_MESH, "geometry nodes must start with the element's vertices");
+          for (int n = nvt; n < ngeo && !B.curved; ++n) {
+            double X[3] = {0, 0, 0}, J[3][3], x[3];
+            const auto& l = curved.lattice[n];
+            if (b.type == SDG_ELEMENT_QUADRANGLE) { X[0] = -1.0 + 2.0 * l[0] / b.geometryOrder; X[1] = -1.0 + 2.0 * l[1] / b.geometryOrder; }
+            else { X[0] = double(l[0]) / b.geometryOrder; X[1] = double(l[1]) / b.geometryOrder; }
+            jacobianAt(b.type, B.dim, nodes, b.vertex + e * nvt, X, J, x);
+            for (int d = 0; d < 3; ++d)
+              if (std::fabs(x[d] - nodes[size_t(g[n]) * 3 + d]) > tol) B.curved = 1;
+          }
+        }
+      }
+      if (B.curved) { B.affine = 0; h->curved = true; }
       if (!B.affine && b.type == SDG_ELEMENT_HEXAHEDRON)
         throw Failure(SDG_ERR_UNSUPPORTED, "hexahedra must be parallelepipeds (affine) in this version");
       // geometry: affine [e][d*d+1]; bilinear tensor quads per point [e][q][d*d+1]; bilinear dense quads
@@ -1005,7 +1041,8 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         std::vector<double> jw(B.nq);
         for (int q = 0; q < B.nq; ++q) {
           double J[3][3], x[3], A[3][3];
-          jacobianAt(b.type, B.dim, nodes, vv, &vr.x[q * 3], J, x);
+          if (B.curved) curved.eval(nodes, b.geometry + e * ngeo, &vr.x[q * 3], J, x);
+          else jacobianAt(b.type, B.dim, nodes, vv, &vr.x[q * 3], J, x);
           for (int l = 0; l < 3; ++l) B.qcoord[(size_t(e) * B.nq + q) * 3 + l] = x[l];
           const double det = adjugate(B.dim, J, A);
           if (!(det > 0)) bad = true;
@@ -1063,7 +1100,25 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       }
       B.stateOffset = stateOff; stateOff += size_t(B.ne) * B.ustride;
       B.gradOffset = h->gradCount; h->gradCount += size_t(B.ne) * h->nv * B.dim * B.nb;
-      if (!B.affine || B.kind == kDense) {  // outward n|J_f| of each local face (straight faces: constant)
+      if (B.curved) {  // curved faces: outward n|J_f| at every face point of every local face, [e][f][j][d]
+        const PointRule fr = faceRule(b.type, h->p);
+        const int* fl = faceVertexList(b.type);
+        B.fmetricHost.assign(size_t(B.ne) * B.nface * fr.n * B.dim, 0.0);
+        for (int64_t e = 0; e < B.ne; ++e)
+          for (int f = 0; f < B.nface; ++f)
+            for (int j = 0; j < fr.n; ++j) {
+              double X[3], J[3][3], x[3], va[3], vb[3];
+              facePointInParent(b.type, f, &fr.x[j * 3], X);
+              curved.eval(nodes, b.geometry + e * ngeo, X, J, x);
+              referenceVertex(b.type, fl[f * 2], va);
+              referenceVertex(b.type, fl[f * 2 + 1], vb);
+              // tangent dx/ds of the edge parametrised on [-1, 1] from its first to its second vertex
+              const double tx = J[0][0] * 0.5 * (vb[0] - va[0]) + J[0][1] * 0.5 * (vb[1] - va[1]);
+              const double ty = J[1][0] * 0.5 * (vb[0] - va[0]) + J[1][1] * 0.5 * (vb[1] - va[1]);
+              double* m = &B.fmetricHost[((size_t(e) * B.nface + f) * fr.n + j) * B.dim];
+              m[0] = ty; m[1] = -tx;
+            }
+      } else if (!B.affine || B.kind == kDense) {  // outward n|J_f| of each local face (straight faces: constant)
         B.fmetricHost.assign(size_t(B.ne) * B.nface * B.dim, 0.0);
         const int* fl = faceVertexList(b.type);
         const int nfv = typeFaceVertices(b.type);
@@ -1102,7 +1157,32 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
 
     // faces: slots, orientation, straight-face geometry from the left parent's vertices (Geometry.cpp:102-169)
     const auto slotOf = [&](const FaceSide& s) { return h->blocks[s.block].faceBase + int64_t(s.element) * h->blocks[s.block].nface + s.face; };
+    // curved meshes: per face point [nfq][n (3), |J_f|] from the left parent's map (Geometry.cpp:102-127 on the
+    // face element's own high-order nodes, which are the parent's face nodes), and the point coordinates
+    const auto faceGeomCurved = [&](const FaceSide& s, double* g, std::vector<double>* coords) {
+      const DevBlock& B = h->blocks[s.block];
+      const Block& b = mb[s.block];
+      const PointRule fr = faceRule(B.type, B.p);
+      const int* fl = faceVertexList(B.type);
+      const int ngeo = b.geometry ? gmshNodeCount(b.type, b.geometryOrder) : 0;
+      const int32_t* vv = b.vertex + int64_t(s.element) * typeVertices(B.type);
+      for (int j = 0; j < fr.n; ++j) {
+        double X[3], J[3][3], x[3], va[3], vb[3];
+        facePointInParent(B.type, s.face, &fr.x[j * 3], X);
+        if (B.curved) blockMap[s.block].eval(nodes, b.geometry + int64_t(s.element) * ngeo, X, J, x);
+        else jacobianAt(B.type, B.dim, nodes, vv, X, J, x);
+        referenceVertex(B.type, fl[s.face * 2], va);
+        referenceVertex(B.type, fl[s.face * 2 + 1], vb);
+        const double tx = J[0][0] * 0.5 * (vb[0] - va[0]) + J[0][1] * 0.5 * (vb[1] - va[1]);
+        const double ty = J[1][0] * 0.5 * (vb[0] - va[0]) + J[1][1] * 0.5 * (vb[1] - va[1]);
+        const double area = std::sqrt(tx * tx + ty * ty);
+        double* gj = g + size_t(j) * 4;
+        gj[0] = ty / area; gj[1] = -tx / area; gj[2] = 0.0; gj[3] = area;
+        if (coords) coords->insert(coords->end(), {x[0], x[1], x[2]});
+      }
+    };
     const auto faceGeom = [&](const FaceSide& s, double* g, std::vector<double>* coords) {
+      if (h->curved) { faceGeomCurved(s, g, coords); return; }
       const DevBlock& B = h->blocks[s.block];
       const int nfv = typeFaceVertices(B.type);
       const int32_t* vv = mb[s.block].vertex + int64_t(s.element) * typeVertices(B.type);
@@ -1153,19 +1233,20 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     };
     h->nInterior = int64_t(adj.interior.size());
     h->nBoundary = int64_t(adj.boundary.size());
+    const int fgs = h->curved ? 4 * h->nfq : 4;  // face geometry doubles per face (per point when curved)
     std::vector<int> fconn(size_t(h->nInterior) * 3);
-    std::vector<double> fgeo(size_t(h->nInterior) * 4);
+    std::vector<double> fgeo(size_t(h->nInterior) * fgs);
     for (int64_t i = 0; i < h->nInterior; ++i) {
       const InteriorFace& f = adj.interior[i];
       fconn[i * 3] = int(slotOf(f.left)); fconn[i * 3 + 1] = int(slotOf(f.right)); fconn[i * 3 + 2] = f.rotation;
-      faceGeom(f.left, &fgeo[i * 4], nullptr);
+      faceGeom(f.left, &fgeo[i * fgs], nullptr);
     }
     std::vector<int> bconn(size_t(h->nBoundary) * 3);
-    std::vector<double> bgeo(size_t(h->nBoundary) * 4);
+    std::vector<double> bgeo(size_t(h->nBoundary) * fgs);
     for (int64_t i = 0; i < h->nBoundary; ++i) {
       const BoundaryFace& f = adj.boundary[i];
       bconn[i * 3] = int(slotOf(f.left)); bconn[i * 3 + 1] = f.condition; bconn[i * 3 + 2] = 0;
-      faceGeom(f.left, &bgeo[i * 4], &h->bcoord);
+      faceGeom(f.left, &bgeo[i * fgs], &h->bcoord);
       h->bphys.push_back(f.physical);
       h->boundaryParent.push_back(f.left.block);
       h->boundaryParent.push_back(f.left.element);

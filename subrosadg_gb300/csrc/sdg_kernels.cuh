@@ -520,9 +520,15 @@ struct FaceArgs {
   const double* fgeo;        // per face (n, |J_f|)
   const double* ghost;       // boundary: [face][j][rho, u, e, p]
   int64_t nface;
-  int n1d, pad;
+  int n1d;
+  int fgeoPoint;             // 1: fgeo per face point [face][j][n, |J_f|] (curved meshes); 0: per face
   Phys ph;
 };
+
+// (n, |J_f|) of face point j of face f: per face, or per point on curved meshes.
+__device__ __forceinline__ const double* faceGeometry(const double* fgeo, int fgeoPoint, int64_t f, int j, int nfq) {
+  return fgeo + (fgeoPoint ? (f * nfq + j) * 4 : f * 4);
+}
 
 enum FaceOp { kOpFace = 0, kOpFaceBoundary = 1, kOpExchange = 2, kOpExchangeBoundary = 3, kOpFaceNS = 4,
               kOpFaceNSBoundary = 5, kOpFaceAV = 6, kOpFaceAVBoundary = 7 };
@@ -574,9 +580,10 @@ __device__ __forceinline__ void faceInteriorPoint(const FaceArgs& a, int64_t t) 
 #pragma unroll
   for (int v = 0; v < NV; ++v) { ul[v] = L[v * nfq]; ur[v] = R[v * nfq]; }
   double n[DIM];
+  const double* fg = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = fg[k];
+  const double area = fg[3];
   State<DIM> l, r;
   makeState<DIM>(l, ul, a.ph);
   makeState<DIM>(r, ur, a.ph);
@@ -606,9 +613,10 @@ __device__ __forceinline__ void faceBoundaryPoint(const FaceArgs& a, int64_t t) 
 #pragma unroll
   for (int v = 0; v < NV; ++v) ul[v] = L[v * nfq];
   double n[DIM];
+  const double* fg = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = fg[k];
+  const double area = fg[3];
   State<DIM> s;
   makeState<DIM>(s, ul, a.ph);
   Comp<DIM> l, g, b;

@@ -677,6 +677,7 @@ struct ForceArgs {
   double dir[3];            // cotangent: the direction of the force component
   int64_t nface;
   int n1d, ns;
+  int fgeoPoint, pad;       // 1: fgeo per face point (curved meshes)
 };
 
 template <int DIM>
@@ -700,9 +701,10 @@ __global__ void __launch_bounds__(kFaceThreads) surfaceForceKernel(ForceArgs a, 
   State<DIM> s;
   makeState<DIM>(s, ul, ph);
   double n[DIM];
+  const double* fg = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double wa = a.fw[j] * a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = fg[k];
+  const double wa = a.fw[j] * fg[3];
   double tn[DIM];
 #pragma unroll
   for (int k = 0; k < DIM; ++k) tn[k] = 0.0;

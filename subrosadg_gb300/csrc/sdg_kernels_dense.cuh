@@ -490,6 +490,8 @@ struct DenseGradArgs {
                             // the volume-gradient trace, no lifts
   const double* epsV;       // [e][nvert]
   const double* avTab;      // dense artificial-viscosity table
+  int fmetricPoint;         // 1: fmetric per face point [e][NF][NFP][d] (curved blocks); 0: per face
+  int pad;
 };
 
 // Artificial viscosity at face point fj of element e of a dense block (nodal_adjacency_value_ x vertex values).
@@ -699,14 +701,15 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
     const int v = r / NB, i = r - v * NB;
     const int64_t e = e0 + le;
     double tot[2] = {0.0, 0.0}, vol[2] = {0.0, 0.0};
-    const double* nF = a.fmetric + e * NF * 2;
     for (int fj = 0; fj < NFP; ++fj) {
       const int f = fj / NFQ, j = fj - f * NFQ;
+      // outward n|J_f| of face f (per face point on curved blocks)
+      const double* nF = a.fmetric + (a.fmetricPoint ? (e * NF + f) * NFQ + j : e * NF + f) * 2;
       const double w = phifw[fj * NB + i];
       const double o = sO[le * FS + (f * NV + v) * NFQ + j], sv = sS[le * FS + (f * NV + v) * NFQ + j];
       const double xt = w * o, xv = w * 0.5 * (o + sv);
-      tot[0] = fma(xt, nF[f * 2 + 0], tot[0]); tot[1] = fma(xt, nF[f * 2 + 1], tot[1]);
-      vol[0] = fma(xv, nF[f * 2 + 0], vol[0]); vol[1] = fma(xv, nF[f * 2 + 1], vol[1]);
+      tot[0] = fma(xt, nF[0], tot[0]); tot[1] = fma(xt, nF[1], tot[1]);
+      vol[0] = fma(xv, nF[0], vol[0]); vol[1] = fma(xv, nF[1], vol[1]);
     }
     double d[2][2] = {{0.0, 0.0}, {0.0, 0.0}};  // d[b][k] = sum_q U_q |J| dxi_b/dx_k w_q dphi_i/dxi_b
     for (int q = 0; q < NQ; ++q) {
@@ -773,14 +776,27 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
     for (int idx = tid; idx < ecount * NV * NB; idx += blockDim.x) {
       const int le = idx / (NV * NB), r = idx - le * NV * NB;
       const int v = r / NB, i = r - v * NB;
-      const double* nF = a.fmetric + (e0 + le) * NF * 2 + f * 2;
-      double acc = 0.0;
-      for (int j = 0; j < NFQ; ++j) {
-        const double jump = 0.5 * (sO[le * FS + (f * NV + v) * NFQ + j] - sS[le * FS + (f * NV + v) * NFQ + j]);
-        acc = fma(phifw[(f * NFQ + j) * NB + i], jump, acc);
+      double acc0 = 0.0, acc1 = 0.0;
+      if (a.fmetricPoint) {  // curved: n|J_f| varies along the face
+        for (int j = 0; j < NFQ; ++j) {
+          const double* nF = a.fmetric + (((e0 + le) * NF + f) * NFQ + j) * 2;
+          const double jump = 0.5 * (sO[le * FS + (f * NV + v) * NFQ + j] - sS[le * FS + (f * NV + v) * NFQ + j]);
+          const double t = phifw[(f * NFQ + j) * NB + i] * jump;
+          acc0 = fma(t, nF[0], acc0);
+          acc1 = fma(t, nF[1], acc1);
+        }
+      } else {
+        const double* nF = a.fmetric + (e0 + le) * NF * 2 + f * 2;
+        double acc = 0.0;
+        for (int j = 0; j < NFQ; ++j) {
+          const double jump = 0.5 * (sO[le * FS + (f * NV + v) * NFQ + j] - sS[le * FS + (f * NV + v) * NFQ + j]);
+          acc = fma(phifw[(f * NFQ + j) * NB + i], jump, acc);
+        }
+        acc0 = acc * nF[0];
+        acc1 = acc * nF[1];
       }
-      sRt[(le * NR + v * 2 + 0) * NB + i] = acc * nF[0];
-      sRt[(le * NR + v * 2 + 1) * NB + i] = acc * nF[1];
+      sRt[(le * NR + v * 2 + 0) * NB + i] = acc0;
+      sRt[(le * NR + v * 2 + 1) * NB + i] = acc1;
     }
     __syncthreads();
     for (int idx = tid; idx < ecount * NR * NB; idx += blockDim.x) {

@@ -38,6 +38,8 @@ struct GradArgs {
                             // eps times the volume-gradient trace, no lifts
   const double* epsV;       // [e][nvert] artificial viscosity at the vertices
   const double* avTab;      // tensor artificial-viscosity table (x[N] first)
+  int fmetricPoint;         // 1: fmetric per face point [e][nface][nfq][d] (curved blocks); 0: per face
+  int pad;
 };
 
 // Exchange of traces across interior faces: each side receives the other side's trace at its own points.
@@ -82,8 +84,9 @@ __device__ __forceinline__ void exchangeBoundaryPoint(const FaceArgs& a, int64_t
     return;
   }
   double n[DIM];
+  const double* fg = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  for (int k = 0; k < DIM; ++k) n[k] = fg[k];
   State<DIM> s;
   makeState<DIM>(s, ul, a.ph);
   Comp<DIM> l, g, b;
@@ -240,6 +243,8 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
 #pragma unroll
         for (int k = 0; k < DIM; ++k) {
           if constexpr (AFFINE) nF[b][en][k] = en ? ja[b][k] : -ja[b][k];
+          else if (a.fmetricPoint)
+            nF[b][en][k] = a.fmetric[((e * NF + T->axisFace[b][en]) * NFQ + T->nodeFacePoint[b][en][node]) * DIM + k];
           else nF[b][en][k] = a.fmetric[(e * NF + T->axisFace[b][en]) * DIM + k];
         }
 #pragma unroll
@@ -325,7 +330,8 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
         for (int k = 0; k < DIM; ++k) nf[k] = en ? g[axis * DIM + k] : -g[axis * DIM + k];
       } else {
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) nf[k] = a.fmetric[(ee * NF + f) * DIM + k];
+        for (int k = 0; k < DIM; ++k)
+          nf[k] = a.fmetric[(a.fmetricPoint ? (ee * NF + f) * NFQ + j : ee * NF + f) * DIM + k];
       }
     }
 #pragma unroll
@@ -383,9 +389,10 @@ __device__ __forceinline__ void faceNSPoint(const FaceArgs& a, int64_t t) {
 #pragma unroll
   for (int v = 0; v < NV; ++v) { ul[v] = a.face[L + v * nfq]; ur[v] = a.face[R + v * nfq]; }
   double n[DIM];
+  const double* fg = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = fg[k];
+  const double area = fg[3];
   State<DIM> l, r;
   makeState<DIM>(l, ul, ph);
   makeState<DIM>(r, ur, ph);
@@ -443,9 +450,10 @@ __device__ __forceinline__ void faceNSBoundaryPoint(const FaceArgs& a, int64_t t
 #pragma unroll
   for (int v = 0; v < NV; ++v) ul[v] = a.face[L + v * nfq];
   double n[DIM];
+  const double* fg = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = fg[k];
+  const double area = fg[3];
   State<DIM> s;
   makeState<DIM>(s, ul, ph);
   Comp<DIM> l, g, b;
@@ -497,9 +505,10 @@ __device__ __forceinline__ void faceAVPoint(const FaceArgs& a, int64_t t) {
 #pragma unroll
   for (int v = 0; v < NV; ++v) { ul[v] = a.face[L + v * nfq]; ur[v] = a.face[R + v * nfq]; }
   double n[DIM];
+  const double* fg = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = fg[k];
+  const double area = fg[3];
   State<DIM> l, r;
   makeState<DIM>(l, ul, ph);
   makeState<DIM>(r, ur, ph);
@@ -536,9 +545,10 @@ __device__ __forceinline__ void faceAVBoundaryPoint(const FaceArgs& a, int64_t t
 #pragma unroll
   for (int v = 0; v < NV; ++v) ul[v] = a.face[L + v * nfq];
   double n[DIM];
+  const double* fg = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq);
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = fg[k];
+  const double area = fg[3];
   State<DIM> s;
   makeState<DIM>(s, ul, ph);
   Comp<DIM> l, g, b;

@@ -58,7 +58,9 @@ struct BoundaryFace {
 struct Block {
   int type = 0;
   int64_t count = 0;
-  const int32_t* vertex = nullptr;  // [count][typeVertices]
+  const int32_t* vertex = nullptr;    // [count][typeVertices]
+  const int32_t* geometry = nullptr;  // curved 2D meshes: [count][gmsh node count of order geometryOrder]
+  int geometryOrder = 1;
 };
 
 struct Adjacency {
