@@ -308,6 +308,14 @@ typedef struct sdg_generated_mesh {
 int sdg_mesh_generate_2d(double x0, double y0, double lx, double ly, int32_t nx, int32_t ny,
                          double jitter, double split_fraction, uint64_t seed, int32_t periodic,
                          const int32_t* boundary_condition, sdg_generated_mesh* out);
+/* Annulus inner_radius <= r <= outer_radius of nr x ntheta curved elements with geometry order q (1..5):
+ * element (i, j) spans [r_i, r_i+1] x [theta_j, theta_j+1]; its order-q Lagrange nodes lie on the exact
+ * circles and rays (the curved meshes of the reference's cylinder drivers, examples/cylinder_2d_ceuler.cpp,
+ * after setOrder(P)).  split_fraction of the quadrangles (seeded) are split into two curved triangles.  Two
+ * boundary groups: the inner circle (1) and the outer circle (2), with boundary_condition[0..1]. */
+int sdg_mesh_generate_annulus(double inner_radius, double outer_radius, int32_t nr, int32_t ntheta,
+                              int32_t geometry_order, double split_fraction, uint64_t seed,
+                              const int32_t* boundary_condition, sdg_generated_mesh* out);
 /* 1D segment [x0, x0+lx], nx lines (examples/sod_1d_ceuler.cpp:68-82 and periodic_1d_ceuler.cpp:63-77:
  * gmsh transfinite curves); periodic = 1 joins the two end points (one group, SDG_BC_PERIODIC), else two
  * groups (x0 end, x0+lx end) with boundary_condition[0..1]. */
@@ -323,8 +331,10 @@ int sdg_mesh_generate_3d(double x0, double y0, double z0, double lx, double ly, 
 int sdg_mesh_generate_3d_tetrahedra(double x0, double y0, double z0, double lx, double ly, double lz,
                                     int32_t nx, int32_t ny, int32_t nz, int32_t periodic,
                                     const int32_t* boundary_condition, sdg_generated_mesh* out);
-/* Read a gmsh MSH 4.1 ASCII file (first-order or high-order elements; only the primary vertices
- * are used).  Physical groups of dimension d-1 (points in 1D) become boundary groups in file order. */
+/* Read a gmsh MSH 4.1 ASCII file (first-order or high-order elements).  A 2D mesh of order q > 1 keeps
+ * every element's nodes as its curved geometry (geometry_order q); 1D and 3D meshes are read by their
+ * primary vertices (straight-sided).  Physical groups of dimension d-1 (points in 1D) become boundary groups
+ * in file order. */
 int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out);
 int sdg_mesh_free(sdg_generated_mesh* mesh);
 

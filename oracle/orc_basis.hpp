@@ -426,6 +426,88 @@ inline void invert(int n, const Real* a, Real* inv) {
   }
 }
 
+// ---- curved (high-order) 2D geometry ------------------------------------------------------------------
+// gmsh's node order of an order-q Lagrange triangle or quadrangle, restated from its convention: the corners,
+// then the q-1 interior points of each edge (corner k to corner k+1), then the interior nodes as the element of
+// order q-2 (quadrangle) or q-3 (triangle) whose corners sit one lattice step inside each corner, recursively.
+// Reference positions are built ring by ring from the corners (not from lattice indices).
+inline std::vector<std::array<Real, 2>> gmshNodePositions(int t, int q) {
+  std::vector<std::array<Real, 2>> out;
+  std::vector<std::array<Real, 2>> c;
+  if (t == kQuad) c = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
+  else c = {{0, 0}, {1, 0}, {0, 1}};
+  const int nc = int(c.size()), shrink = t == kQuad ? 2 : 3;
+  int r = q;
+  while (r >= 0) {
+    if (r == 0) {  // a single node: the centre of the remaining ring
+      std::array<Real, 2> m = {0, 0};
+      for (const auto& p : c) { m[0] += p[0] / nc; m[1] += p[1] / nc; }
+      out.push_back(m);
+      break;
+    }
+    for (const auto& p : c) out.push_back(p);
+    for (int k = 0; k < nc; ++k) {
+      const auto& a = c[k];
+      const auto& b = c[(k + 1) % nc];
+      for (int i = 1; i < r; ++i) out.push_back({a[0] + (b[0] - a[0]) * i / r, a[1] + (b[1] - a[1]) * i / r});
+    }
+    if (r - shrink < 0) break;
+    // inner corners: one lattice step along both edges adjacent to each corner
+    std::vector<std::array<Real, 2>> inner(c.size());
+    const Real f = Real(1) / Real(r);
+    for (int k = 0; k < nc; ++k) {
+      const auto& p = c[k];
+      const auto& nx = c[(k + 1) % nc];
+      const auto& pv = c[(k + nc - 1) % nc];
+      inner[k] = {p[0] + (nx[0] - p[0]) * f + (pv[0] - p[0]) * f, p[1] + (nx[1] - p[1]) * f + (pv[1] - p[1]) * f};
+    }
+    c = inner;
+    r -= shrink;
+  }
+  return out;
+}
+
+// Lagrange basis through given nodes by the inverse Vandermonde matrix of the monomials x^a y^b (a, b <= q on
+// quadrangles, a + b <= q on triangles): N_n(X) = sum_m C[m][n] mono_m(X).
+struct CurvedBasis {
+  int t = 0, q = 1, nn = 0;
+  std::vector<std::array<int, 2>> mono;
+  std::vector<Real> C;  // [nn][nn], C[m * nn + n]
+  void init(int type, int order) {
+    t = type; q = order;
+    const auto pos = gmshNodePositions(type, order);
+    nn = int(pos.size());
+    mono.clear();
+    for (int a = 0; a <= q; ++a)
+      for (int b = 0; b <= q; ++b)
+        if (type == kQuad || a + b <= q) mono.push_back({a, b});
+    std::vector<Real> V(size_t(nn) * nn);
+    for (int n = 0; n < nn; ++n)
+      for (int m = 0; m < nn; ++m) V[size_t(n) * nn + m] = ipow(pos[n][0], mono[m][0]) * ipow(pos[n][1], mono[m][1]);
+    C.assign(size_t(nn) * nn, 0);
+    invert(nn, V.data(), C.data());
+  }
+  static Real ipow(Real x, int k) { Real r = 1; for (int i = 0; i < k; ++i) r *= x; return r; }
+  // N[n], G[n][2] at X
+  void eval(const Real* X, Real* N, Real* G) const {
+    std::vector<Real> mv(nn), mx(nn), my(nn);
+    for (int m = 0; m < nn; ++m) {
+      const int a = mono[m][0], b = mono[m][1];
+      mv[m] = ipow(X[0], a) * ipow(X[1], b);
+      mx[m] = a ? a * ipow(X[0], a - 1) * ipow(X[1], b) : 0;
+      my[m] = b ? b * ipow(X[0], a) * ipow(X[1], b - 1) : 0;
+    }
+    for (int n = 0; n < nn; ++n) {
+      Real v = 0, gx = 0, gy = 0;
+      for (int m = 0; m < nn; ++m) {
+        const Real cc = C[size_t(m) * nn + n];
+        v += cc * mv[m]; gx += cc * mx[m]; gy += cc * my[m];
+      }
+      N[n] = v; G[n * 2] = gx; G[n * 2 + 1] = gy;
+    }
+  }
+};
+
 // Reference-element operator tables for one (type, P) (ElementBasisFunction, BasisFunction.cpp:136-230).
 struct RefElement {
   int type = 0, dim = 0, p = 0, nb = 0, nq = 0, nface = 0, nfq = 0;

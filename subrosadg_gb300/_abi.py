@@ -163,6 +163,8 @@ SIGNATURES = {
     "sdg_mesh_generate_2d": (c_int32, [c_double, c_double, c_double, c_double, c_int32, c_int32, c_double,
                                        c_double, c_uint64, c_int32, _p_int32, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_generate_1d": (c_int32, [c_double, c_double, c_int32, c_int32, _p_int32, c_void_p]),
+    "sdg_mesh_generate_annulus": (c_int32, [c_double, c_double, c_int32, c_int32, c_int32, c_double, c_uint64,
+                                            _p_int32, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_generate_3d": (c_int32, [c_double, c_double, c_double, c_double, c_double, c_double, c_int32,
                                        c_int32, c_int32, c_int32, _p_int32, POINTER(SdgGeneratedMesh)]),
     "sdg_mesh_generate_3d_tetrahedra": (c_int32, [c_double, c_double, c_double, c_double, c_double, c_double,

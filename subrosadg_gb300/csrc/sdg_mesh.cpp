@@ -1,5 +1,6 @@
 // Mesh layer: adjacency reconstruction, structured generators and an MSH 4.1 reader.
 // See sdg_mesh.hpp for the reference functions each part replaces.
+#include "sdg_geometry.hpp"
 #include "sdg_mesh.hpp"
 
 #include <algorithm>
@@ -150,6 +151,8 @@ namespace {
 struct MeshStorage {
   std::vector<double> node;
   std::vector<int32_t> periodic, line, tri, quad, hex, tet, bnode, bphys, bc;
+  int geometryOrder = 1;
+  std::vector<int32_t> triGeo, quadGeo;  // curved 2D meshes: gmsh-ordered geometry nodes per element
 };
 
 void publish(MeshStorage* s, int dim, sdg_generated_mesh* out) {
@@ -167,6 +170,11 @@ void publish(MeshStorage* s, int dim, sdg_generated_mesh* out) {
   m.boundary_count = int64_t(s->bphys.size()); m.boundary_node = s->bnode.empty() ? nullptr : s->bnode.data();
   m.boundary_physical = s->bphys.empty() ? nullptr : s->bphys.data();
   m.physical_count = int32_t(s->bc.size()); m.physical_boundary_condition = s->bc.data();
+  if (s->geometryOrder > 1) {
+    m.geometry_order = s->geometryOrder;
+    m.triangle_geometry_node = s->triGeo.empty() ? nullptr : s->triGeo.data();
+    m.quadrangle_geometry_node = s->quadGeo.empty() ? nullptr : s->quadGeo.data();
+  }
   out->storage = s;
 }
 
@@ -247,6 +255,64 @@ int sdg_mesh_generate_2d(double x0, double y0, double lx, double ly, int32_t nx,
   for (int j = 0; j < ny; ++j) { s->bnode.insert(s->bnode.end(), {(j + 1) * px, j * px}); s->bphys.push_back(periodic ? 1 : 4); }
   if (periodic) s->bc = {SDG_BC_PERIODIC};
   else s->bc.assign(boundary_condition, boundary_condition + 4);
+  publish(s, 2, out);
+  return SDG_OK;
+}
+
+int sdg_mesh_generate_annulus(double inner_radius, double outer_radius, int32_t nr, int32_t ntheta,
+                              int32_t geometry_order, double split_fraction, uint64_t seed,
+                              const int32_t* boundary_condition, sdg_generated_mesh* out) {
+  if (!out || !boundary_condition || nr < 1 || ntheta < 3 || !(inner_radius > 0) || !(outer_radius > inner_radius) ||
+      geometry_order < 1 || geometry_order > 5 || split_fraction < 0 || split_fraction > 1)
+    return SDG_ERR_INVALID_ARGUMENT;
+  auto* s = new MeshStorage();
+  const int q = geometry_order;
+  const int64_t fr = int64_t(q) * nr + 1, ft = int64_t(q) * ntheta;  // the fine node lattice (theta periodic)
+  const auto id = [&](int64_t I, int64_t J) { return int32_t(I * ft + ((J % ft) + ft) % ft); };
+  s->node.resize(size_t(fr * ft) * 3);
+  const double twoPi = 6.283185307179586476925286766559;
+  for (int64_t I = 0; I < fr; ++I)
+    for (int64_t J = 0; J < ft; ++J) {
+      const double r = inner_radius + (outer_radius - inner_radius) * double(I) / double(fr - 1);
+      const double t = twoPi * double(J) / double(ft);
+      const size_t n = size_t(id(I, J));
+      s->node[n * 3 + 0] = r * std::cos(t); s->node[n * 3 + 1] = r * std::sin(t); s->node[n * 3 + 2] = 0.0;
+    }
+  const std::vector<std::array<int, 2>> quadLat = sdg::gmshLattice(SDG_ELEMENT_QUADRANGLE, q);
+  const std::vector<std::array<int, 2>> triLat = sdg::gmshLattice(SDG_ELEMENT_TRIANGLE, q);
+  std::mt19937_64 rsplit(seed);
+  const auto unit = [](std::mt19937_64& g) { return double(g() >> 11) * (1.0 / 9007199254740992.0); };
+  for (int64_t i = 0; i < nr; ++i)
+    for (int64_t j = 0; j < ntheta; ++j) {
+      const int64_t I0 = q * i, J0 = q * j;
+      // vertices counter-clockwise: (r, theta) -> (r + dr, theta) -> (r + dr, theta + dt) -> (r, theta + dt)
+      const int32_t a = id(I0, J0), b = id(I0 + q, J0), c = id(I0 + q, J0 + q), d = id(I0, J0 + q);
+      if (split_fraction > 0 && unit(rsplit) < split_fraction) {
+        // triangles (a, b, c) and (a, c, d): their order-q nodes are points of the element's lattice
+        s->tri.insert(s->tri.end(), {a, b, c});
+        s->tri.insert(s->tri.end(), {a, c, d});
+        if (q > 1) {
+          for (const auto& l : triLat) s->triGeo.push_back(id(I0 + l[0] + l[1], J0 + l[1]));
+          for (const auto& l : triLat) s->triGeo.push_back(id(I0 + l[0], J0 + l[0] + l[1]));
+        }
+      } else {
+        s->quad.insert(s->quad.end(), {a, b, c, d});
+        if (q > 1)
+          for (const auto& l : quadLat) s->quadGeo.push_back(id(I0 + l[0], J0 + l[1]));
+      }
+    }
+  // boundary lines: the inner circle (group 1) and the outer circle (group 2), in the direction of the elements'
+  // own edges
+  for (int64_t j = 0; j < ntheta; ++j) {
+    s->bnode.insert(s->bnode.end(), {id(0, q * (j + 1)), id(0, q * j)});
+    s->bphys.push_back(1);
+  }
+  for (int64_t j = 0; j < ntheta; ++j) {
+    s->bnode.insert(s->bnode.end(), {id(fr - 1, q * j), id(fr - 1, q * (j + 1))});
+    s->bphys.push_back(2);
+  }
+  s->bc.assign(boundary_condition, boundary_condition + 2);
+  s->geometryOrder = q;
   publish(s, 2, out);
   return SDG_OK;
 }
@@ -390,8 +456,10 @@ int sdg_mesh_generate_3d_tetrahedra(double x0, double y0, double z0, double lx, 
 
 // MSH 4.1 ASCII reader: $PhysicalNames (optional), $Entities (physical tags of entities),
 // $Nodes, $Elements, $Periodic (node pairs).  Element types 1/8/26-28 (lines), 2/9/21/23/25 (triangles),
-// 3/10/36-38 (quadrangles), 4/11/29-31 (tetrahedra), 5/12/92-94 (hexahedra); only the primary vertices are
-// kept.  A 3D mesh holds tetrahedra or hexahedra; its triangular boundary elements get a fourth index of -1.
+// 3/10/36-38 (quadrangles), 4/11/29-31 (tetrahedra), 5/12/92-94 (hexahedra).  The primary vertices form the
+// element lists; a 2D mesh of order q > 1 also keeps every element's full node list as its curved geometry
+// (geometry_order q; 3D and 1D meshes are read by their vertices).  A 3D mesh holds tetrahedra or hexahedra;
+// its triangular boundary elements get a fourth index of -1.
 int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
   if (!path || !out) return SDG_ERR_INVALID_ARGUMENT;
   std::ifstream in(path);
@@ -436,7 +504,7 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
       default: return false;
     }
   };
-  struct RawEl { int type; int edim; int etag; std::vector<int64_t> v; };
+  struct RawEl { int type; int edim; int etag; std::vector<int64_t> v, all; };
   std::vector<RawEl> raw;
   std::string line;
   try {
@@ -477,8 +545,8 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
           if (!typeInfo(type, dim, nn, nprim)) throw std::runtime_error("unsupported element type " + std::to_string(type));
           for (int64_t i = 0; i < n; ++i) {
             int64_t tag; in >> tag;
-            RawEl r; r.type = type; r.edim = ed; r.etag = et; r.v.resize(nprim);
-            for (int k = 0; k < nn; ++k) { int64_t v; in >> v; if (k < nprim) r.v[k] = v; }
+            RawEl r; r.type = type; r.edim = ed; r.etag = et; r.v.resize(nprim); r.all.resize(nn);
+            for (int k = 0; k < nn; ++k) { int64_t v; in >> v; r.all[k] = v; if (k < nprim) r.v[k] = v; }
             maxDim = std::max(maxDim, dim);
             raw.push_back(std::move(r));
           }
@@ -499,6 +567,17 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
       if (it == nodeIndex.end()) throw std::runtime_error("element references an unknown node");
       return it->second;
     };
+    // 2D meshes of order q > 1 (the drivers' setOrder(P)): every element's full node list in gmsh order is
+    // kept as its curved geometry (ReadControl.cpp:243-256); lines and 3D elements keep their vertices only
+    int order2d = 0;
+    for (const RawEl& r : raw) {
+      int dim = 0, nn = 0, nprim = 0; typeInfo(r.type, dim, nn, nprim);
+      if (dim != 2 || maxDim != 2) continue;
+      int q = 1;
+      while (sdg::gmshNodeCount(nprim == 3 ? SDG_ELEMENT_TRIANGLE : SDG_ELEMENT_QUADRANGLE, q) < nn) ++q;
+      if (order2d && q != order2d) throw std::runtime_error("2D elements of different geometry orders");
+      order2d = q;
+    }
     for (const RawEl& r : raw) {
       int dim = 0, nn = 0, nprim = 0; typeInfo(r.type, dim, nn, nprim);
       if (dim == maxDim) {
@@ -506,6 +585,8 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
                                     : maxDim == 2 ? (nprim == 3 ? &s->tri : &s->quad)
                                                   : (nprim == 4 ? &s->tet : &s->hex);
         for (int64_t v : r.v) dst->push_back(idx(v));
+        if (maxDim == 2 && order2d > 1)
+          for (int64_t v : r.all) (nprim == 3 ? s->triGeo : s->quadGeo).push_back(idx(v));
       } else if (dim == maxDim - 1) {
         const auto it = entityPhysical.find({r.edim, r.etag});
         if (it == entityPhysical.end() || it->second.empty()) continue;
@@ -523,6 +604,7 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
       std::sort(tags.begin(), tags.end());
       for (size_t i = 0; i < tags.size(); ++i) remap[tags[i]] = int(i) + 1;
     }
+    if (order2d > 1) s->geometryOrder = order2d;
     if (!s->tet.empty() && !s->hex.empty())
       throw std::runtime_error("a 3D mesh of tetrahedra and hexahedra needs pyramids, which are not supported");
     for (const BEl& b : bels) {

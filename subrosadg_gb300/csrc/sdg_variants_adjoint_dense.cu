@@ -52,7 +52,7 @@ void denseOf(AdjointTileKernels& k, bool gen, bool visc, bool br2) {
 void adjointDenseKernels(int type, int p, bool affine, bool gen, bool visc, bool br2, AdjointTileKernels& k) {
 #define SDG_AD(T, P, NB, NQ, NFQ, NF, AFF) \
   if (type == T && p == P && affine == AFF) { denseOf<NB, NQ, NFQ, NF, AFF>(k, gen, visc, br2); return; }
-  SDG_DENSE_CASES(SDG_AD)
+  SDG_DENSE_ADJOINT_CASES(SDG_AD)
 #undef SDG_AD
 #define SDG_ADT(T, P, NB, NQ, NFQ, NF) \
   if (type == T && p == P && affine) {                                                   \

@@ -34,8 +34,15 @@ class Mesh:
 
     def __init__(self, dimension, nodes, triangles=None, quadrangles=None, hexahedra=None, boundary=None,
                  boundary_physical=None, physical_conditions=None, periodic_master=None, lines=None,
-                 tetrahedra=None):
+                 tetrahedra=None, geometry_order=1, triangle_geometry=None, quadrangle_geometry=None):
         self.dimension = int(dimension)
+        # curved 2D meshes: order-q geometry nodes per element in gmsh order (corners first)
+        self.geometry_order = int(geometry_order)
+        q = self.geometry_order
+        self.triangle_geometry = None if triangle_geometry is None or len(triangle_geometry) == 0 else \
+            np.ascontiguousarray(triangle_geometry, np.int32).reshape(-1, (q + 1) * (q + 2) // 2)
+        self.quadrangle_geometry = None if quadrangle_geometry is None or len(quadrangle_geometry) == 0 else \
+            np.ascontiguousarray(quadrangle_geometry, np.int32).reshape(-1, (q + 1) ** 2)
         self.nodes = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
         self.lines = None if lines is None or len(lines) == 0 else np.ascontiguousarray(lines, np.int32).reshape(-1, 2)
         self.triangles = None if triangles is None or len(triangles) == 0 else np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
@@ -66,6 +73,15 @@ class Mesh:
                   arr(m.periodic_master, m.node_count, 1, np.int32),
                   arr(m.line_node, m.line_count, 2, np.int32),
                   arr(m.tetrahedron_node, m.tetrahedron_count, 4, np.int32))
+        q = m.geometry_order
+        if q > 1:
+            out.geometry_order = q
+            if m.triangle_count:
+                out.triangle_geometry = arr(m.triangle_geometry_node, m.triangle_count, (q + 1) * (q + 2) // 2,
+                                            np.int32).reshape(m.triangle_count, -1)
+            if m.quadrangle_count:
+                out.quadrangle_geometry = arr(m.quadrangle_geometry_node, m.quadrangle_count, (q + 1) ** 2,
+                                              np.int32).reshape(m.quadrangle_count, -1)
         _abi.load().sdg_mesh_free(byref(g))
         return out
 
@@ -107,6 +123,18 @@ class Mesh:
         return cls._from_generated(g)
 
     @classmethod
+    def annulus(cls, inner_radius, outer_radius, nr, ntheta, geometry_order=1, split_fraction=0.0, seed=0,
+                boundary_conditions=(_abi.RIEMANN_FARFIELD, _abi.RIEMANN_FARFIELD)):
+        """Curved annulus of nr x ntheta elements of geometry order q (nodes on the exact circles); groups 1 (inner
+        circle) and 2 (outer circle)."""
+        lib = _abi.load()
+        g = SdgGeneratedMesh()
+        bc = np.ascontiguousarray(boundary_conditions, np.int32)
+        check(lib.sdg_mesh_generate_annulus(inner_radius, outer_radius, nr, ntheta, geometry_order, split_fraction,
+                                            seed, _ptr(bc, _pi), byref(g)))
+        return cls._from_generated(g)
+
+    @classmethod
     def read_msh(cls, path):
         lib = _abi.load()
         g = SdgGeneratedMesh()
@@ -140,6 +168,9 @@ class Mesh:
         m.line_node = _ptr(self.lines, _pi)
         m.tetrahedron_count = 0 if self.tetrahedra is None else self.tetrahedra.shape[0]
         m.tetrahedron_node = _ptr(self.tetrahedra, _pi)
+        m.geometry_order = self.geometry_order if self.geometry_order > 1 else 0
+        m.triangle_geometry_node = _ptr(self.triangle_geometry, _pi)
+        m.quadrangle_geometry_node = _ptr(self.quadrangle_geometry, _pi)
         return m
 
 

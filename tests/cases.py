@@ -378,3 +378,97 @@ def rotation_2d(degrees):
 
 
 SHEAR_3D = [[1.0, 0.3, 0.0], [0.0, 1.0, 0.2], [0.1, 0.0, 1.0]]
+
+
+# ---- curved (high-order) 2D geometry ------------------------------------------------------------------------
+
+def annulus_case(p=3, q=None, flux=sdg.HLLC, nr=3, ntheta=10, split=0.0, steps=3, dt=2e-4, viscous=None, mu=0.0,
+                 conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD), seed=5):
+    """Flow in the curved annulus 1 <= r <= 2 (nodes of the order-q geometry on the exact circles): a slip wall
+    (or a no-slip wall with `viscous`) at the inner circle, farfield at the outer one, a smooth perturbed stream
+    inside; q defaults to the polynomial order, as the reference's drivers set it (setOrder(P))."""
+    mesh = sdg.Mesh.annulus(1.0, 2.0, nr, ntheta, geometry_order=q or p, split_fraction=split, seed=seed,
+                            boundary_conditions=conditions)
+    cfg = config(p, flux) if viscous is None else ns_config(p, flux, viscous, mu)
+
+    def ic(pts):
+        x, y = pts[:, 0], pts[:, 1]
+        rho = 1.0 + 0.1 * np.sin(x) * np.cos(y)
+        u = 0.3 + 0.05 * np.cos(y)
+        v = 0.05 * np.sin(x)
+        pr = 1.0 + 0.05 * np.cos(x + y)
+        return np.stack([rho, u, v, pr / (rho * R_GAS)], 1)
+
+    def bc(pts, phys):
+        out = np.zeros((len(pts), 4))
+        out[:, 0] = 1.0
+        out[:, 1] = 0.3
+        out[:, 3] = 1.0 / R_GAS
+        return out
+
+    return (mesh, cfg, ic, bc, dt, steps)
+
+
+def with_geometry_nodes(mesh, q):
+    """The same straight-sided 2D mesh given as an order-q mesh: geometry nodes on the straight element maps
+    (a gmsh mesh of straight elements after setOrder(q))."""
+    from subrosadg_gb300.solver import Mesh
+    index = {}
+    for i, x in enumerate(mesh.nodes):
+        index.setdefault((round(x[0], 12), round(x[1], 12)), i)
+    new = list(mesh.nodes)
+
+    def node_at(x):
+        key = (round(x[0], 12), round(x[1], 12))
+        if key not in index:
+            index[key] = len(new)
+            new.append(np.array([x[0], x[1], 0.0]))
+        return index[key]
+
+    def lattice(kind):
+        out, r, o = [], q, 0
+        if kind == "quad":
+            while r >= 0:
+                if r == 0:
+                    out.append((o, o))
+                    break
+                a, b = o, o + r
+                out += [(a, a), (b, a), (b, b), (a, b)]
+                out += [(a + k, a) for k in range(1, r)] + [(b, a + k) for k in range(1, r)]
+                out += [(b - k, b) for k in range(1, r)] + [(a, b - k) for k in range(1, r)]
+                r, o = r - 2, o + 1
+            return [(-1 + 2 * i / q, -1 + 2 * j / q) for i, j in out]
+        while r >= 0:
+            if r == 0:
+                out.append((o, o))
+                break
+            out += [(o, o), (o + r, o), (o, o + r)]
+            out += [(o + k, o) for k in range(1, r)] + [(o + r - k, o + k) for k in range(1, r)]
+            out += [(o, o + r - k) for k in range(1, r)]
+            r, o = r - 3, o + 1
+        return [(i / q, j / q) for i, j in out]
+
+    def geo(elems, kind):
+        if elems is None:
+            return None
+        rows = []
+        for el in elems:
+            v = mesh.nodes[el]
+            row = []
+            for X, Y in lattice(kind):
+                if kind == "quad":
+                    sh = [0.25 * (1 - X) * (1 - Y), 0.25 * (1 + X) * (1 - Y), 0.25 * (1 + X) * (1 + Y),
+                          0.25 * (1 - X) * (1 + Y)]
+                else:
+                    sh = [1 - X - Y, X, Y]
+                row.append(node_at(sum(s * v[k] for k, s in enumerate(sh))))
+            rows.append(row)
+        return np.array(rows, np.int32)
+
+    tg, qg = geo(mesh.triangles, "tri"), geo(mesh.quadrangles, "quad")
+    master = None
+    if mesh.periodic_master is not None:
+        master = np.concatenate([mesh.periodic_master, np.arange(len(mesh.nodes), len(new), dtype=np.int32)])
+    return Mesh(2, np.array(new), triangles=mesh.triangles, quadrangles=mesh.quadrangles, boundary=mesh.boundary,
+                boundary_physical=mesh.boundary_physical, physical_conditions=mesh.physical_conditions,
+                periodic_master=master, geometry_order=q, triangle_geometry=tg, quadrangle_geometry=qg)

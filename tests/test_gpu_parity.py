@@ -67,6 +67,24 @@ CASES = {
     "tgv-hex-p3-lf": lambda: cases.tgv_case(n=3, p=3, flux=sdg.LAX_FRIEDRICHS, steps=3),
     "tgv-hex-p4-hllc": lambda: cases.tgv_case(n=3, p=4, flux=sdg.HLLC, steps=2),
     "tgv-hex-p5-roe": lambda: cases.tgv_case(n=3, p=5, flux=sdg.ROE, steps=2),
+    # curved (high-order) geometry: the annulus 1 <= r <= 2 with its order-q nodes on the circles, slip wall inside,
+    # farfield outside (order q = P as the reference's drivers set it, and one case with q below P)
+    "curved-annulus-quad-p2-hllc": lambda: cases.annulus_case(p=2),
+    "curved-annulus-quad-p3-roe": lambda: cases.annulus_case(p=3, flux=sdg.ROE),
+    "curved-annulus-quad-p4-lf": lambda: cases.annulus_case(p=4, flux=sdg.LAX_FRIEDRICHS, nr=2, ntheta=8),
+    "curved-annulus-quad-p5-hllc": lambda: cases.annulus_case(p=5, nr=2, ntheta=8, steps=2),
+    "curved-annulus-quad-p3-geometry-q2": lambda: cases.annulus_case(p=3, q=2),
+    "curved-annulus-hybrid-p3-hllc": lambda: cases.annulus_case(p=3, split=0.5),
+    "curved-annulus-tri-p2-roe": lambda: cases.annulus_case(p=2, flux=sdg.ROE, split=1.0),
+    "curved-annulus-tri-p4-lf": lambda: cases.annulus_case(p=4, flux=sdg.LAX_FRIEDRICHS, split=1.0, nr=2, ntheta=8),
+    "ns-curved-annulus-quad-p3-br2-hllc": lambda: cases.annulus_case(
+        p=3, viscous=sdg.BR2, mu=0.01, conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.RIEMANN_FARFIELD)),
+    "ns-curved-annulus-hybrid-p2-br1-lf": lambda: cases.annulus_case(
+        p=2, flux=sdg.LAX_FRIEDRICHS, split=0.5, viscous=sdg.BR1, mu=0.01,
+        conditions=(sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD)),
+    "ns-curved-annulus-tri-p3-br2-roe": lambda: cases.annulus_case(
+        p=3, flux=sdg.ROE, split=1.0, viscous=sdg.BR2, mu=0.01, nr=2, ntheta=8,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW)),
     # affine elements with off-diagonal metric terms (the structured boxes above take the diagonal-metric path)
     "tgv-hex-p3-sheared-hllc": lambda: cases.transformed(cases.tgv_case(n=3, p=3, flux=sdg.HLLC), cases.SHEAR_3D),
     "tgv-hex-p2-sheared-roe": lambda: cases.transformed(cases.tgv_case(n=4, p=2, flux=sdg.ROE), cases.SHEAR_3D),
@@ -312,3 +330,25 @@ def test_launch_count_and_shape():
     g.stepSolver(dt)
     # per SSP-RK3 stage: 1 face kernel + 1 element kernel; plus 1 reduction per step
     assert g.launch_count() - n0 == 3 * 2 + 1
+
+
+@pytest.mark.parametrize("q", [2, 3, 4])
+def test_curved_wall_force_of_a_uniform_state_vanishes(q):
+    """The pressure force on the closed curved inner wall of a uniform state is zero to round-off: the face
+    quadrature integrates n|J_f| of the order-q edges exactly and the edges close (the reference's View force,
+    VariableConvertor.cpp:883-906)."""
+    mesh = sdg.Mesh.annulus(1.0, 2.0, 2, 10, geometry_order=q, split_fraction=0.4, seed=1,
+                            boundary_conditions=(sdg.ADIABATIC_SLIP_WALL, sdg.RIEMANN_FARFIELD))
+    g = sdg.GpuSolver(mesh, cases.config(q, sdg.HLLC))
+    g.initialize_primitive(cases.uniform_primitive(g.counts.volume_point_count, 2, vel=(0.0, 0.0)))
+    f = g.surface_force(1)
+    assert np.abs(f).max() < 1e-12, f
+
+
+def test_curved_meshes_refuse_derivatives():
+    mesh, cfg, prim, _, _, _ = cases.annulus_case(p=2)
+    g = sdg.GpuSolver(mesh, cfg)
+    g.initialize_primitive(prim(g.volume_points()))
+    with pytest.raises(sdg.SdgError) as err:
+        g.vjp_residual(np.zeros((g.counts.volume_point_count, 4)))
+    assert err.value.code == 5  # SDG_ERR_UNSUPPORTED
