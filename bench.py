@@ -581,8 +581,9 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": elem_bytes},
         "fp64": {"peak_gflops": fp64.value, "peak_source": "sdg_measure_fp64_peak (independent-chain DFMA probe)",
                  "achieved_gflops": fp64_achieved, "frac": (fp64_achieved / fp64.value) if fp64_achieved else None,
-                 "achieved_source": "ncu FP64 instruction counts of a 40^3 launch (2 per DFMA) scaled by elements "
-                                    "(profiles/tensor_stage_kernel_tgv_hex_p3.md) / the live launch time",
+                 "achieved_source": "ncu FP64 instruction counts per element, mean of the 3 stage launches of a "
+                                    "56^3 step (2 per DFMA), scaled by elements "
+                                    "(profiles/tensor_stage_kernel_tgv_hex_p3.md) / the live mean launch time",
                  "pipe_active_pct": prof.get("fp64_pipe_active_pct"),
                  "note": "the DG stage kernels are FP64-issue bound on GB300"},
         "kernel_ms_per_step": {"element": kms[0] / ksteps, "interior_face": kms[1] / ksteps,

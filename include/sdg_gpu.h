@@ -346,9 +346,13 @@ int sdg_get_node_artificial_viscosity(sdg_handle* handle, double* out);
 /* ---- raw-binary solution files (the reference's writeRawBinary / LastStep and SpecificFile restarts,
  * src/View/RawBinary.cpp:42-191, src/Solver/InitialCondition.cpp:40-80) ---------------------------------
  * u64 ZSTD_compressBound(payload) + one zstd level-1 frame; payload per element the column-major
- * (d+2) x Nb modal coefficients (Navier-Stokes: then the (d+2)*d x Nb gradient coefficients), then per
- * boundary face its parent's coefficients (in this library's boundary-face order), then one artificial
- * viscosity value per mesh node (zero).  Needs libzstd.so.1 at run time (else SDG_ERR_UNSUPPORTED).
+ * (d+2) x Nb modal coefficients (Navier-Stokes: then the (d+2)*d x Nb gradient coefficients of the last
+ * stage input), then per boundary face its parent's coefficients and gradient (BR1: the element's; BR2: its
+ * volume gradient plus the lift of that face, RawBinary.cpp:98-112), in the order of
+ * sdg_set_boundary_face_order, then one artificial viscosity value per mesh node (zero without shock
+ * capturing).  BR2 records of parents with wall faces need the last gradient pass's input state:
+ * SDG_ERR_UNSUPPORTED under forward Euler, which updates in place, and after an adjoint call until the next
+ * step.  Needs libzstd.so.1 at run time (else SDG_ERR_UNSUPPORTED).
  * lower_order = 1 reads a file written at order P-1 into the leading coefficients (SpecificFile). */
 int sdg_write_raw_binary(sdg_handle* handle, const char* path);
 /* The caller's boundary-face order for the boundary block of raw-binary files: faces[k] = (element type,

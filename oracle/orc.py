@@ -45,6 +45,7 @@ def load(precision="double"):
         lib.orc_step.argtypes = [c_void_p, c_int, c_double]
         lib.orc_stage.argtypes = [c_void_p, c_int, c_double]
         lib.orc_adjacency.argtypes = [c_void_p, _pi, _pi]
+        lib.orc_raw_gradient.argtypes = [c_void_p, _pd, _pd]
         lib.orc_set_threads.argtypes = [c_int]
         lib.orc_max_threads.restype = c_int
         lib.orc_real_digits.restype = c_int
@@ -156,6 +157,15 @@ class Oracle:
         b = np.zeros((self.boundary, 5), np.int32)
         self.lib.orc_adjacency(self.h, a.ctypes.data_as(_pi), b.ctypes.data_as(_pi))
         return a, b
+
+    def raw_gradient(self, element_values, boundary_values):
+        """Navier-Stokes gradient records of the reference's raw-binary file: per element (block order) and per
+        boundary face (sorted adjacency order) -- BR2: the volume gradient plus that face's lift."""
+        e = np.zeros(element_values)
+        b = np.zeros(boundary_values)
+        if self.lib.orc_raw_gradient(self.h, e.ctypes.data_as(_pd), b.ctypes.data_as(_pd)) != 0:
+            raise RuntimeError("oracle: raw gradients need a Navier-Stokes problem")
+        return e, b
 
     def interior_face_geometry(self):
         out = np.zeros((self.interior, self.nfq, 4))

@@ -1300,6 +1300,39 @@ int orc_adjacency(void* h, int32_t* interior, int32_t* boundary) {
   return 0;
 }
 
+// The gradient records of the reference's raw-binary file for Navier-Stokes (src/View/RawBinary.cpp:75-154): per
+// element its gradient coefficients (element_out, block order, column-major (d+2)d x Nb), per boundary face in the
+// sorted order of orc_adjacency the record of its parent -- BR1: the element's gradient; BR2: the volume gradient
+// plus the lift of that face (boundary_out) -- of the last stage input, as the reference holds them after a step.
+int orc_raw_gradient(void* h, double* element_out, double* boundary_out) {
+  const orc::Problem& P = *static_cast<orc::Problem*>(h);
+  if (!P.ns()) return 1;
+  const int nr = P.nv * P.dim;
+  size_t off = 0;
+  for (const auto& B : P.blocks) {
+    const size_t n = size_t(B.ne) * nr * B.ref.nb;
+    for (size_t i = 0; i < n; ++i) element_out[off + i] = double(B.gc[i]);
+    off += n;
+  }
+  std::vector<std::pair<std::array<int32_t, 5>, const orc::Face*>> bd;
+  for (const auto& F : P.boundary) bd.push_back({{P.blocks[F.bl].type, F.el, F.fl, F.physical, F.bc}, &F});
+  std::sort(bd.begin(), bd.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  size_t boff = 0;
+  for (const auto& kv : bd) {
+    const orc::Face& F = *kv.second;
+    const auto& B = P.blocks[F.bl];
+    const int nb = B.ref.nb, nblk = P.visc == 1 ? 1 : B.ref.nface;
+    for (int i = 0; i < nr * nb; ++i) {
+      const orc::Real g = P.visc == 1 ? B.gc[size_t(F.el) * nr * nb + i]
+                                      : B.vgc[size_t(F.el) * nr * nb + i] +
+                                            B.igc[(size_t(F.el) * nblk + F.fl) * nr * nb + i];
+      boundary_out[boff + i] = double(g);
+    }
+    boff += size_t(nr) * nb;
+  }
+  return 0;
+}
+
 // Face normals and |J_f| w of every interior face point, in the sorted order of orc_adjacency
 // (for geometry parity checks): [interior][nfq][4] = (nx, ny, nz, |J_f| w).
 int orc_interior_face_geometry(void* h, double* out) {

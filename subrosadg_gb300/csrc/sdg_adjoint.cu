@@ -236,6 +236,7 @@ void traces(sdg_handle* h, const double* u, double* face) {
 // linearisation at the forward traces in h->face.
 void gradientOf(sdg_handle* h, const double* u, double* face, double* other, double* grad, double* faceGrad,
                 bool tangent = false) {
+  if (grad == h->grad) h->gradInput = nullptr;  // a pass at a state that no buffer keeps
   std::vector<Rec> recs;
   Rec x = faceRec(h, kOpExchange);
   x.fa.face = face; x.fa.other = other;
@@ -461,6 +462,7 @@ void jvpSteps(sdg_handle* h, int steps, double dt, double dmu) {
       runRecs(h, update, h->stream);
     }
   }
+  h->gradInput = stepGradientInput(h);
 }
 
 // Forward sweep of `steps` steps from the current state U_0, keeping U every `interval` steps
@@ -477,6 +479,7 @@ void forwardSweep(sdg_handle* h, int steps, double dt, int interval) {
   }
   copyState(h, poolBuffer(h, segments), h->state[0]);
   h->stateVersion++;
+  h->gradInput = stepGradientInput(h);
   A->traj.valid = true;
   A->traj.version = h->stateVersion;
   A->traj.steps = steps; A->traj.interval = interval; A->traj.segments = segments; A->traj.dt = dt;

@@ -550,6 +550,8 @@ int sdg_batch_step_async(sdg_batch* b, int32_t steps) {
     if (b->planOnly) throw Failure(SDG_ERR_STATE, "the batch holds host-only instances: it can only plan");
     SDG_CUDA(cudaSetDevice(b->device));
     stepBatch(b, steps);
+    if (steps > 0)
+      for (sdg_handle* h : b->inst) h->gradInput = stepGradientInput(h);
   } catch (const Failure& f) {
     return batchFail(b, f);
   }
@@ -563,7 +565,10 @@ int sdg_batch_step_sequential_async(sdg_batch* b, int32_t steps) {
     if (!b->haveDt) throw Failure(SDG_ERR_STATE, "sdg_batch_set_delta_time before the first step");
     SDG_CUDA(cudaSetDevice(b->device));
     if (!b->built) build(b);
-    for (sdg_handle* h : b->inst) h->stateVersion++;
+    for (sdg_handle* h : b->inst) {
+      h->stateVersion++;
+      if (steps > 0) h->gradInput = stepGradientInput(h);
+    }
     for (int s = 0; s < steps; ++s)
       for (size_t i = 0; i < b->inst.size(); ++i) runRecs(b->inst[i], b->seqRecs[i], b->stream);
   } catch (const Failure& f) {

@@ -717,6 +717,7 @@ void stepGraph(sdg_handle* h, double dt) {
 }
 
 void stepOnce(sdg_handle* h, double dt) {
+  h->gradInput = stepGradientInput(h);
   if (h->useGraph && !h->timing) { stepGraph(h, dt); return; }
   std::vector<Rec> recs;
   emitStep(h, dt, true, recs);
@@ -1410,6 +1411,7 @@ int sdg_set_state_point(sdg_handle* h, const double* conserved) {
   SDG_CUDA(cudaMemcpyAsync(h->scratch, conserved, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyHostToDevice, h->stream));
   pointsToState(h, 0);
   traceAll(h, 0);
+  if (h->gradInput == h->state[0]) h->gradInput = nullptr;
   SDG_CUDA(cudaStreamSynchronize(h->stream));
   h->hasState = true;
   h->stateVersion++;
@@ -1428,6 +1430,7 @@ int sdg_set_initial_primitive(sdg_handle* h, const double* primitive) {
   checkLaunch(h);
   pointsToState(h, 0);
   traceAll(h, 0);
+  if (h->gradInput == h->state[0]) h->gradInput = nullptr;
   SDG_CUDA(cudaStreamSynchronize(h->stream));
   h->hasState = true;
   h->stateVersion++;
@@ -1532,6 +1535,7 @@ int sdg_set_state_modal(sdg_handle* h, const double* coefficient) {
   SDG_CUDA(cudaSetDevice(h->device));
   SDG_CUDA(cudaMemcpyAsync(h->state[0], st.data(), h->stateCount * 8, cudaMemcpyHostToDevice, h->stream));
   traceAll(h, 0);
+  if (h->gradInput == h->state[0]) h->gradInput = nullptr;
   SDG_CUDA(cudaStreamSynchronize(h->stream));
   h->hasState = true;
   h->stateVersion++;
@@ -1618,6 +1622,7 @@ int sdg_residual_point(sdg_handle* h, double* rate) {
     recs.push_back(r);
   }
   runRecs(h, recs, h->stream);
+  h->gradInput = h->state[0];
   SDG_CUDA(cudaMemcpyAsync(rate, h->scratch, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
   traceAll(h, 0);
   checkStatus(h);

@@ -123,6 +123,8 @@ struct sdg_handle {
   double* faceGrad = nullptr;      // NS: gradient traces
   double* faceFlux = nullptr;      // NS: face fluxes
   double* grad = nullptr;          // NS: total gradient at the nodes
+  const double* gradInput = nullptr;  // NS: state buffer the last gradient pass read, while it still holds
+                                      // that input (null when not kept)
   size_t gradCount = 0;
   int* fconn = nullptr; double* fgeo = nullptr; int64_t nInterior = 0;
   int* bconn = nullptr; double* bgeo = nullptr; double* ghost = nullptr; int64_t nBoundary = 0;
@@ -174,6 +176,8 @@ void traceAll(sdg_handle* h, int which);
 void checkStatus(sdg_handle* h);
 // Error text returned by sdg_last_error(NULL) (failures before a handle exists).
 void setCreateError(const std::string& message);
+// Right point of each left point of a triangular interior face per rotation, [3][nfq].
+std::vector<int> triangleFacePermutation(int type, int p);
 // Face-point record of operation `op` (FaceOp) over the handle's interior or boundary faces.
 Rec faceRec(sdg_handle* h, int op);
 // SSP-RK coefficients (c0 on the step's base state, c1 on the stage input, c2 on dt R) per scheme and stage.
@@ -187,6 +191,11 @@ void cotangentStateToPoints(sdg_handle* h, const double* st, double* pts);
 void destroyAdjoint(sdg_handle* h);
 // The gradient pass and viscous-layout buffers run for Navier-Stokes and for artificial viscosity.
 inline bool viscousPath(const sdg_handle* h) { return h->ns || h->av; }
+// Input state of a step's last gradient pass (the last stage's input): the stage buffer for two- and
+// three-stage schemes; forward Euler updates in place and keeps none.
+inline const double* stepGradientInput(const sdg_handle* h) {
+  return h->cfg.time_integration >= 1 ? h->state[1] : nullptr;
+}
 // The stage-kernel slot of a handle (DevBlock::stageV).
 inline int stageSlot(const sdg_handle* h) { return h->av ? 2 : (h->ns ? 1 : 0); }
 // Artificial viscosity (sdg_av.cu): inner radius of an element, the block tables, the per-step records.

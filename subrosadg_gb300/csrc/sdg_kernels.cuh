@@ -537,7 +537,7 @@ constexpr int kFaceOps = 8;
 // Point of the right face that coincides with point j of the left face (rotation of the right face's
 // vertex list; SimulationControl.cpp:381-523 permutations).
 template <int DIM>
-__device__ __forceinline__ int rightPoint(int j, int rot, int n1d) {
+__host__ __device__ __forceinline__ int rightPoint(int j, int rot, int n1d) {
   if constexpr (DIM == 1) {
     return 0;
   } else if constexpr (DIM == 2) {

@@ -165,3 +165,90 @@ def test_raw_binary_boundary_block_in_callers_order(tmp_path, name, case):
     bad[1] = bad[0]
     with pytest.raises(sdg.SdgError):
         s.set_boundary_face_order(bad)
+
+
+def _records(payload, counts, order_parents):
+    """Split a Navier-Stokes payload into the element gradient records (block order) and the boundary
+    gradient records (file order); order_parents lists the block of each boundary record."""
+    nv, d = counts.conserved_variable_count, counts.dimension
+    nr = nv * d
+    pos, elem = 0, []
+    for k in range(counts.block_count):
+        nb = counts.block_basis_count[k]
+        for _ in range(counts.block_element_count[k]):
+            elem.append(payload[pos + nv * nb: pos + nv * nb + nr * nb])
+            pos += nv * nb + nr * nb
+    bnd = []
+    for k in order_parents:
+        nb = counts.block_basis_count[k]
+        bnd.append(payload[pos + nv * nb: pos + nv * nb + nr * nb])
+        pos += nv * nb + nr * nb
+    return np.concatenate(elem), np.concatenate(bnd) if bnd else np.zeros(0)
+
+
+GRADIENT_CASES = {
+    "channel-quad-p2-br2-walls": lambda: cases.channel_case(
+        p=2, n=3, viscous=sdg.BR2, mu=0.01,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "channel-hybrid-p3-br2-walls": lambda: cases.channel_case(
+        p=3, n=3, split=0.5, jitter=0.1, viscous=sdg.BR2, mu=0.01,
+        conditions=(sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ISOTHERMAL_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "channel-bilinear-p1-br2-walls": lambda: cases.channel_case(
+        p=1, n=3, jitter=0.1, viscous=sdg.BR2, mu=0.01,
+        conditions=(sdg.ADIABATIC_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "channel-quad-p2-br1-walls": lambda: cases.channel_case(
+        p=2, n=3, viscous=sdg.BR1, mu=0.01,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_SLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "annulus-curved-hybrid-p3-br2": lambda: cases.annulus_case(
+        p=3, split=0.5, viscous=sdg.BR2, mu=0.01, nr=2, ntheta=8,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.RIEMANN_FARFIELD)),
+    "cavity-hex-p2-br2-inc": lambda: cases.cavity_3d_case(p=2, viscous=sdg.BR2, mu=1e-2),
+    "tet-box-p2-br2-walls": lambda: cases.tet_box_case(
+        p=2, viscous=sdg.BR2, mu=0.01,
+        conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
+                    sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(GRADIENT_CASES))
+def test_raw_binary_gradient_records_match_the_oracle(tmp_path, name):
+    """Navier-Stokes gradient records of the file against the oracle's (RawBinary.cpp:75-112): per element the
+    gradient coefficients of the last stage input; per boundary face its parent's -- BR1 the element gradient,
+    BR2 the volume gradient plus the lift of that face only. Boundary records follow the oracle's sorted order."""
+    from oracle.orc import Oracle
+    mesh, cfg, prim, bprim, dt, steps = GRADIENT_CASES[name]()
+    g = sdg.GpuSolver(mesh, cfg)
+    o = Oracle(mesh, cfg, faithful=False, precision="extended")
+    p0 = prim(g.volume_points())
+    g.initialize_primitive(p0)
+    o.initialize_primitive(p0)
+    nfq = g.counts.face_point_count
+    bpts, phys = g.boundary_points()
+    g.set_boundary_primitive(bprim(bpts, np.repeat(phys, nfq)))
+    bpo, pho = o.boundary_points()
+    o.set_boundary_primitive(bprim(bpo, np.repeat(pho, nfq)))
+    g.stepSolver(dt, 2)
+    o.step(dt, 2)
+    c = g.counts
+    _, bnd = g.adjacency()  # sorted (type, element, face, physical, condition): the oracle's boundary order
+    g.set_boundary_face_order(bnd[:, :3])
+    path = tmp_path / "ns.zst"
+    g.writeRawBinary(path)
+    block_of = {c.block_element_type[k]: k for k in range(c.block_count)}
+    parents = [block_of[t] for t in bnd[:, 0]]
+    elem, brec = _records(decode(path), c, parents)
+    nr = c.conserved_variable_count * c.dimension
+    o_elem, o_bnd = o.raw_gradient(len(elem), sum(nr * c.block_basis_count[k] for k in parents))
+    scale = np.abs(o_elem).max()
+    assert np.abs(elem - o_elem).max() <= 1e-10 * scale
+    assert np.abs(brec - o_bnd).max() <= 1e-10 * scale
+    # BR2: a boundary record is not its parent's element record (the other faces' lifts are left out)
+    first, off = {}, 0
+    for k in range(c.block_count):
+        first[k] = off
+        off += c.block_element_count[k] * nr * c.block_basis_count[k]
+    parent_rec = np.concatenate([o_elem[first[k] + e * nr * c.block_basis_count[k]:
+                                        first[k] + (e + 1) * nr * c.block_basis_count[k]]
+                                 for k, e in zip(parents, bnd[:, 1])])
+    gap = np.abs(parent_rec - o_bnd).max()
+    assert (gap > 1e-6 * scale) if cfg.viscous_flux == sdg.BR2 else (gap <= 1e-14 * scale)
