@@ -153,37 +153,38 @@ template <int D, class T>
 __device__ __forceinline__ void fluxHLLC(const State<D, T>& l, const State<D, T>& r, const double* n, const Phys& ph,
                                          T* h) {
   const T unl = dotn<D>(l.u, n), unr = dotn<D>(r.u, n);
-  const T cl = sqrtT(ph.gamma * l.p * l.ir), cr = sqrtT(ph.gamma * r.p * r.ir);
+  const T gl = ph.gamma * l.ir, gr = ph.gamma * r.ir;  // c^2 = (gamma/rho) p
+  const T cl = sqrtT(gl * l.p), cr = sqrtT(gr * r.p);
   const T rhoAvg = 0.5 * (l.r + r.r), cAvg = 0.5 * (cl + cr);
   const T ps = fmaxT(0.0, fmaT(-(unr - unl), rhoAvg * cAvg, 0.5 * (l.p + r.p)));
   const double g2 = ph.hllc_g2;
-  // Toro's factor q = sqrt(1 + g2 (ps/p - 1)) only where ps > p: a real branch (measured: whole warps skip
-  // it on smooth flows; the branch-free forms of c q execute ~10 more FP64 instructions per face point)
-  const T ql = ps <= l.p ? T(1.0) : sqrtT(fmaT(g2, fmaT(ps, rcpT(l.p), -1.0), 1.0));
-  const T sl = fmaT(-cl, ql, unl);
+  // Toro's wave speeds u_n -+ c q with q = sqrt(1 + g2 (ps/p - 1)) where ps > p, else q = 1; there
+  // c q = sqrt((gamma/rho) (p + g2 (ps - p))), one square root and no reciprocal.  A real branch (measured:
+  // whole warps skip it on smooth flows; the branch-free forms execute more FP64 instructions per face point)
+  const T sl = unl - (ps <= l.p ? cl : sqrtT(gl * fmaT(g2, ps - l.p, l.p)));
   if (sl >= 0.0) { normalFlux(l, n, unl, h, ph); return; }
-  const T qr = ps <= r.p ? T(1.0) : sqrtT(fmaT(g2, fmaT(ps, rcpT(r.p), -1.0), 1.0));
-  const T sr = fmaT(cr, qr, unr);
+  const T sr = unr + (ps <= r.p ? cr : sqrtT(gr * fmaT(g2, ps - r.p, r.p)));
   if (sr <= 0.0) { normalFlux(r, n, unr, h, ph); return; }
   const T al = l.r * (sl - unl), ar = r.r * (sr - unr);
   const T ss = (r.p - l.p + al * unl - ar * unr) * rcpT(al - ar);
   const bool left = ss >= 0.0;
   const State<D, T>& s = left ? l : r;
   const T sk = left ? sl : sr, un = left ? unl : unr, a = left ? al : ar;
-  T f[D + 2];
-  normalFlux(s, n, un, f, ph);
+  // h = F(U_k) + S_k (U*_k - U_k) with the reference's star state U*_k = [a, a u + (p* - p) n,
+  // a E/rho + p* S* - p u_n] / (S_k - S*), a = rho (S_k - u_n), collected per conserved variable so that
+  // neither F(U_k) nor U*_k is formed (18 fewer FP64 instructions per face point; a/rho = S_k - u_n):
+  //   rho:  a S*/(S_k - S*)                       (= rho* S*)
+  //   m:    m alpha + n (p + A (p* - p))          alpha = (S_k - u_n) S*/(S_k - S*), A = S_k/(S_k - S*)
+  //   E:    E alpha + A (p* S* - p u_n) + p u_n   (the last term only with the compressible p u energy flux)
   const T inv = rcpT(sk - ss);
-  // star state minus the side's conserved state, times the wave speed
-  const T rs = a * inv;
-  h[0] = fmaT(sk, rs - s.r, f[0]);
-  const T dp = ps - s.p;
+  const T A = sk * inv, ssi = ss * inv;
+  const T alpha = (sk - un) * ssi;
+  const T beta = fmaT(A, ps - s.p, s.p);
+  h[0] = a * ssi;
 #pragma unroll
-  for (int k = 0; k < D; ++k) {
-    const T ms = fmaT(a, s.u[k], dp * n[k]) * inv;
-    h[1 + k] = fmaT(sk, ms - s.m[k], f[1 + k]);
-  }
-  const T Es = fmaT(a, s.E * s.ir, fmaT(ps, ss, -s.p * un)) * inv;
-  h[D + 1] = fmaT(sk, Es - s.E, f[D + 1]);
+  for (int k = 0; k < D; ++k) h[1 + k] = fmaT(s.m[k], alpha, beta * n[k]);
+  const T pu = s.p * un;
+  h[D + 1] = fmaT(s.E, alpha, fmaT(A, fmaT(ps, ss, -pu), ph.incomp ? T(0.0) : pu));
 }
 
 // Roe flux with Harten's entropy fix, delta = c/20 (ConvectiveFlux.cpp:240-350).
