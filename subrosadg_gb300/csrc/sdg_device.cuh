@@ -52,6 +52,16 @@ __device__ __forceinline__ double rcp(double x) {
   return r;
 }
 
+// -x by flipping the sign bit on the integer pipe (IEEE negation: exact, NaNs and zeros included), keeping
+// the stores of the right side's face flux off the FP64 pipe.
+__device__ __forceinline__ double negated(double x) {
+#ifdef __CUDA_ARCH__
+  return __hiloint2double(__double2hiint(x) ^ int(0x80000000u), __double2loint(x));
+#else
+  return -x;
+#endif
+}
+
 // Weakly compressible pressure c0^2 (rho - rho0) + padd, in the reference's association: rho - rho0 is exact
 // (Sterbenz) for rho within a factor 2 of rho0, so the c0^2 amplification acts on an exact difference.
 template <class T>

@@ -593,7 +593,7 @@ __device__ __forceinline__ void faceInteriorPoint(const FaceArgs& a, int64_t t) 
   for (int v = 0; v < NV; ++v) {
     const double x = h[v] * area;
     L[v * nfq] = x;
-    R[v * nfq] = -x;
+    R[v * nfq] = negated(x);
   }
 }
 

@@ -25,14 +25,25 @@ namespace sdg {
 //                         emod[NF][NB][NFQ] E_f = M_ref^-1 Phi_f^T W_f (lift of face f's point values)
 //                         lmod[NF][NFQ][NFQ] L_f = Phi_f E_f (trace at face f of the lift from face f)
 //   source weights:        phiw[NQ][NB] w_q phi (volume source terms)
-inline size_t denseTableSize(int nb, int nq, int nfp, int dim = 2) {
+__host__ __device__ constexpr inline size_t denseTableSize(int nb, int nq, int nfp, int dim = 2) {
   return size_t(nq) * nb * (1 + dim) + size_t(nfp) * nb * 2 + size_t(nb) * nb;
 }
-inline size_t denseGradOperatorSize(int nb, int nf, int nfq, int dim = 2) {
+__host__ __device__ constexpr inline size_t denseGradOperatorSize(int nb, int nf, int nfq, int dim = 2) {
   return size_t(dim) * nb * nb + size_t(nf) * nb * nfq + size_t(nf) * nfq * nfq;
 }
-inline size_t denseSourceTableOffset(int nb, int nq, int nfp, int nf, int nfq, int dim = 2) {
+__host__ __device__ constexpr inline size_t denseSourceTableOffset(int nb, int nq, int nfp, int nf, int nfq, int dim = 2) {
   return denseTableSize(nb, nq, nfp, dim) + denseGradOperatorSize(nb, nf, nfq, dim);
+}
+// Stage tables of affine blocks, M_ref^-1 folded in: phi[NQ][NB] | dphiwM[NQ][d][NB] | phif[NFP][NB] |
+// phifwM[NFP][NB] | phiMr[NQ][NB], then phiwM[NQ][NB] (source weights).  dphiwM and phifwM are the weak
+// derivative and face-lift tables with M_ref^-1 applied (the residual pass yields M_ref^-1 R directly: the
+// affine M^-1 = M_ref^-1/|J| costs no N_b x N_b product per element); phiMr = Phi M_ref recovers R Phi^T from
+// M_ref^-1 R for the relative error.
+__host__ __device__ constexpr inline size_t denseFoldedOffset(int nb, int nq, int nfp, int nf, int nfq, int dim = 2) {
+  return denseSourceTableOffset(nb, nq, nfp, nf, nfq, dim) + size_t(nq) * nb;
+}
+__host__ __device__ constexpr inline size_t denseFoldedSize(int nb, int nq, int nfp, int dim = 2) {
+  return size_t(nq) * nb * (2 + dim) + size_t(nfp) * nb * 2;
 }
 
 template <class R>
@@ -61,7 +72,8 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
   const int nb = modalCount(type, p);
   const PointRule vr = volumeRule(type, p), fr = faceRule(type, p);
   const int nq = vr.n, nf = typeFaces(type), nfq = fr.n, nfp = nf * nfq, dim = typeDim(type);
-  tables.assign(denseSourceTableOffset(nb, nq, nfp, nf, nfq, dim) + size_t(nq) * nb, 0.0);
+  tables.assign(denseFoldedOffset(nb, nq, nfp, nf, nfq, dim) + denseFoldedSize(nb, nq, nfp, dim) + size_t(nq) * nb,
+                0.0);
   double* phi = tables.data();
   double* dphiw = phi + size_t(nq) * nb;
   double* phif = dphiw + size_t(nq) * dim * nb;
@@ -143,6 +155,37 @@ inline void buildDenseTables(int type, int p, std::vector<double>& tables, std::
     for (int q = 0; q < nq; ++q)
       for (int b = 0; b < nb; ++b) phiw[size_t(q) * nb + b] = vr.w[q] * phi[size_t(q) * nb + b];
   }
+  {
+    // affine stage tables with M_ref^-1 folded in (long double sums of the long double inverse, rounded once)
+    const double* phiw = tables.data() + denseSourceTableOffset(nb, nq, nfp, nf, nfq, dim);
+    double* fo = tables.data() + denseFoldedOffset(nb, nq, nfp, nf, nfq, dim);
+    double* fphi = fo;
+    double* fdphiw = fphi + size_t(nq) * nb;
+    double* fphif = fdphiw + size_t(nq) * dim * nb;
+    double* fphifw = fphif + size_t(nfp) * nb;
+    double* fphiM = fphifw + size_t(nfp) * nb;
+    double* fphiw = fphiM + size_t(nq) * nb;
+    // row r of `src` ([rows][nb]) times M_ref^-1 (symmetric): out[r][i] = sum_k inv[i][k] src[r][k]
+    const auto fold = [&](const double* src, int rows, double* out) {
+      for (int r = 0; r < rows; ++r)
+        for (int i = 0; i < nb; ++i) {
+          long double acc = 0.0L;
+          for (int k = 0; k < nb; ++k) acc += invl[size_t(i) * nb + k] * (long double)src[size_t(r) * nb + k];
+          out[size_t(r) * nb + i] = double(acc);
+        }
+    };
+    std::copy(phi, phi + size_t(nq) * nb, fphi);
+    fold(dphiw, nq * dim, fdphiw);
+    std::copy(phif, phif + size_t(nfp) * nb, fphif);
+    fold(phifw, nfp, fphifw);
+    fold(phiw, nq, fphiw);
+    for (int q = 0; q < nq; ++q)
+      for (int k = 0; k < nb; ++k) {
+        long double acc = 0.0L;
+        for (int i = 0; i < nb; ++i) acc += (long double)phi[size_t(q) * nb + i] * m[size_t(i) * nb + k];
+        fphiM[size_t(q) * nb + k] = double(acc);
+      }
+  }
   phiOut.assign(phi, phi + size_t(nq) * nb);
   // unweighted least-squares projection (InitialCondition.cpp:91-104): lsq = (Phi^T Phi)^-1 Phi^T  [nb][nq],
   // followed by its row sums [nb] (lsq applied to the constant 1: 1/phi_0 for the constant mode, 0 otherwise),
@@ -171,18 +214,20 @@ struct DenseShape {
   static constexpr int PER_ELEM = USTRIDE + FSTRIDE + DIM * NV * NQ + NV * NB + NV * NB;
   static constexpr int EPB = 16;
   static constexpr int THREADS = 256;
+  // staged tables: bilinear blocks the original layout (M^-1 per element), affine blocks the folded one
   static constexpr size_t TABLES = size_t(NQ) * NB * (1 + DIM) + size_t(NFP) * NB * 2 + size_t(NB) * NB;
-  static constexpr size_t SMEM = (size_t(EPB) * PER_ELEM + TABLES) * 8 + 16 + 8 * NV * (THREADS / 32);
-  static constexpr size_t smemFor(int epb, int threads) {
-    return (size_t(epb) * PER_ELEM + TABLES) * 8 + 16 + 8 * NV * size_t(threads / 32);
+  static constexpr size_t TABLES_AFF = size_t(NQ) * NB * (2 + DIM) + size_t(NFP) * NB * 2;
+  __host__ __device__ static constexpr size_t tables(bool affine) { return affine ? TABLES_AFF : TABLES; }
+  static constexpr size_t smemFor(int epb, int threads, bool affine) {
+    return (size_t(epb) * PER_ELEM + tables(affine)) * 8 + 16 + 8 * NV * size_t(threads / 32);
   }
 };
 
-template <int NB, int NQ, int NFQ, int NF, int DIM = 2>
+template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int DIM = 2>
 __device__ __forceinline__ uint64_t* denseStageBarrier(int epb) {
   using S = DenseShape<NB, NQ, NFQ, NF, DIM>;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  return reinterpret_cast<uint64_t*>(reinterpret_cast<double*>(smem_raw) + epb * S::PER_ELEM + S::TABLES);
+  return reinterpret_cast<uint64_t*>(reinterpret_cast<double*>(smem_raw) + epb * S::PER_ELEM + S::tables(AFFINE));
 }
 
 // Dense stage tile (triangles and P1 quadrangles: DIM 2; tetrahedra: DIM 3), a.epb elements per CTA, any
@@ -201,12 +246,15 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
   double* sR = sQ + EPB * DIM * NV * NQ;             // [EPB][NV][NB]
   double* sN = sR + EPB * NV * NB;                   // [EPB][NV][NB] new state
   double* tab = sN + EPB * NV * NB;
+  // affine: the folded tables (dphiw and phifw carry M_ref^-1; the last block is phiMr = Phi M_ref)
+  constexpr size_t TAB = S::tables(AFFINE);
+  const double* tsrc = AFFINE ? a.tables + denseFoldedOffset(NB, NQ, NFP, NF, NFQ, DIM) : a.tables;
   const double* phi = tab;
   const double* dphiw = phi + NQ * NB;
   const double* phif = dphiw + NQ * DIM * NB;
   const double* phifw = phif + NFP * NB;
-  const double* mref = phifw + NFP * NB;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(tab + S::TABLES);
+  const double* mref = phifw + NFP * NB;  // affine: phiMr [NQ][NB]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tab + TAB);
   double* sRed = reinterpret_cast<double*>(bar + 1);
   const int GS = AFFINE ? GD : NQ * GD + NB * NB;
 
@@ -222,7 +270,7 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
     if (a.doVolume) bulkLoad(sF, (a.fluxSrc ? a.fluxSrc : a.face) + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
   if (loadTables)
-    for (int k = tid; k < int(S::TABLES); k += blockDim.x) tab[k] = a.tables[k];
+    for (int k = tid; k < int(TAB); k += blockDim.x) tab[k] = tsrc[k];
   __syncthreads();
   const bool arrived = mbarWait(bar, parity);
   if (__syncthreads_or(!arrived)) {
@@ -324,9 +372,10 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
           const int f = fj / NFQ, j = fj - f * NFQ;
           s = fma(-sF[le * S::FSTRIDE + (f * NV + v) * NFQ + j], phifw[fj * NB + i], s);
         }
-        if (ph.source && v == DIM) {  // last momentum component: sum_q w_q |J|_q S_q phi_i(x_q)
-          const double* phiw = a.tables + (NQ * NB * (1 + DIM) + NFP * NB * 2 + NB * NB + DIM * NB * NB + NF * NB * NFQ +
-                                           NF * NFQ * NFQ);
+        if (ph.source && v == DIM) {  // last momentum component: sum_q w_q |J|_q S_q phi_i(x_q) (affine: M_ref^-1 of it)
+          const double* phiw = AFFINE ? tsrc + TAB
+                                      : a.tables + (NQ * NB * (1 + DIM) + NFP * NB * 2 + NB * NB + DIM * NB * NB +
+                                                    NF * NB * NFQ + NF * NFQ * NFQ);
           for (int q = 0; q < NQ; ++q) s = fma(sN[le * NV * NB + q], phiw[q * NB + i], s);
         }
         sR[(le * NV + v) * NB + i] = s;
@@ -338,13 +387,17 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
       const int le = idx / NB, i = idx - le * NB;
       const int64_t e = e0 + le;
       const double* g = a.geom + e * GS;
-      const double* minv = AFFINE ? mref : g + NQ * GD;
-      const double sc = AFFINE ? g[DIM * DIM] : 1.0;
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        double s = 0.0;
-        for (int k = 0; k < NB; ++k) s = fma(minv[i * NB + k], sR[(le * NV + v) * NB + k], s);
-        const double du = sc * s;
+        double du;
+        if constexpr (AFFINE) {
+          du = g[DIM * DIM] * sR[(le * NV + v) * NB + i];  // M^-1 R = (1/|J|) (M_ref^-1 R)
+        } else {
+          const double* minv = g + NQ * GD;
+          double s = 0.0;
+          for (int k = 0; k < NB; ++k) s = fma(minv[i * NB + k], sR[(le * NV + v) * NB + k], s);
+          du = s;
+        }
         sQ[(le * NV + v) * NB + i] = du;  // sQ reused: du per basis function
         if (a.doUpdate) {
           const double u1 = sU[le * S::USTRIDE + v * NB + i];
@@ -373,14 +426,16 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
       }
     }
     if (a.relerr) {
-      // relative error: mean over points of |R Phi^T| per element (TimeIntegration.cpp:279-324)
+      // relative error: mean over points of |R Phi^T| per element (TimeIntegration.cpp:279-324); affine blocks
+      // hold M_ref^-1 R, and R Phi^T = (M_ref^-1 R) (Phi M_ref)^T
+      const double* rphi = AFFINE ? mref : phi;
       double acc[NV] = {};
       for (int idx = tid; idx < ecount * NQ; idx += blockDim.x) {
         const int le = idx / NQ, q = idx - le * NQ;
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
           double s = 0.0;
-          for (int b = 0; b < NB; ++b) s = fma(phi[q * NB + b], sR[(le * NV + v) * NB + b], s);
+          for (int b = 0; b < NB; ++b) s = fma(rphi[q * NB + b], sR[(le * NV + v) * NB + b], s);
           acc[v] += fabs(s);
         }
       }
@@ -426,7 +481,7 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
 
 template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC, int DIM = 2>
 __global__ void __launch_bounds__(kMaxTileThreads) denseStageKernel(StageArgs a, Phys ph) {
-  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF, DIM>(a.epb), 1);
+  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF, AFFINE, DIM>(a.epb), 1);
   denseStageTile<NB, NQ, NFQ, NF, AFFINE, VISC, DIM>(a, ph, blockIdx.x, 0u, true);
 }
 
@@ -434,7 +489,7 @@ template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int VISC, int DIM = 2>
 __global__ void __launch_bounds__(kMaxTileThreads)
     denseStageBatchKernel(const StageArgs* __restrict__ args, const Phys* __restrict__ phys,
                           const int2* __restrict__ items, int nitems, int epb) {
-  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF, DIM>(epb), 1);
+  if (threadIdx.x == 0) mbarInit(denseStageBarrier<NB, NQ, NFQ, NF, AFFINE, DIM>(epb), 1);
   uint32_t parity = 0;
   for (int w = blockIdx.x; w < nitems; w += gridDim.x) {
     const int2 it = items[w];

@@ -427,7 +427,7 @@ __device__ __forceinline__ void faceNSPoint(const FaceArgs& a, int64_t t) {
   for (int v = 0; v < NV; ++v) {
     const double x = fma(-0.5, fl[v] + fr[v], h[v]) * area;
     a.faceFlux[L + v * nfq] = x;
-    a.faceFlux[R + v * nfq] = -x;
+    a.faceFlux[R + v * nfq] = negated(x);
   }
 }
 
@@ -524,7 +524,7 @@ __device__ __forceinline__ void faceAVPoint(const FaceArgs& a, int64_t t) {
     }
     const double x = fma(-0.5, gl + gr, h[v]) * area;
     a.faceFlux[L + v * nfq] = x;
-    a.faceFlux[R + v * nfq] = -x;
+    a.faceFlux[R + v * nfq] = negated(x);
   }
 }
 

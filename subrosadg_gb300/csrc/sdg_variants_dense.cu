@@ -14,7 +14,7 @@ KernelVariant stageOf() {
   v.single = reinterpret_cast<const void*>(&denseStageKernel<NB, NQ, NFQ, NF, AFF, VISC, DIM>);
   v.batch = reinterpret_cast<const void*>(&denseStageBatchKernel<NB, NQ, NFQ, NF, AFF, VISC, DIM>);
   v.nb = NB; v.epb = S::EPB; v.threads = S::THREADS; v.nodeThreads = false;
-  v.perElem = size_t(S::PER_ELEM) * 8; v.fixed = S::TABLES * 8 + 16; v.perWarp = 8 * S::NV;
+  v.perElem = size_t(S::PER_ELEM) * 8; v.fixed = S::tables(AFF) * 8 + 16; v.perWarp = 8 * S::NV;
   return v;
 }
 template <int NB, int NQ, int NFQ, int NF, bool AFF, int DIM = 2>
