@@ -302,6 +302,22 @@ def bench_batched(args, device, torch, max_elements=None):
     return out
 
 
+def kernel_split(g, dt, steps):
+    """Device time per step of each kernel class (every launch bracketed by CUDA events on the solver's stream,
+    a separate pass after the timed one): element, interior face, boundary face, reduction, gradient."""
+    import ctypes
+    g.lib.sdg_set_kernel_timing(g.h, 1)
+    for _ in range(steps):
+        g.step_async(dt)
+    kms = (ctypes.c_double * 5)()
+    kn = (ctypes.c_int64 * 5)()
+    g.lib.sdg_kernel_time(g.h, kms, kn)
+    g.lib.sdg_set_kernel_timing(g.h, 0)
+    g.synchronize()
+    names = ("element", "interior_face", "boundary_face", "reduction", "gradient")
+    return {k: kms[i] / steps for i, k in enumerate(names)}
+
+
 def bench_ns_hybrid(args, device, torch):
     """2D Navier-Stokes BR2 Kelvin-Helmholtz, Re 1e4, Pr 0.71, hybrid 256^2 mesh, P4, LF."""
     import subrosadg_gb300 as sdg
@@ -326,7 +342,8 @@ def bench_ns_hybrid(args, device, torch):
     dof = g.counts.degree_of_freedom_count
     out = {"workload": f"ns-kh2d-BR2-Re1e4-{n}^2-hybrid-P4-LF", "elements": g.counts.element_count, "dof": dof,
            "value": dof * 3 * steps / (ms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": ms / steps,
-           "tiles": [g.tile(k) for k in range(g.counts.block_count)]}
+           "tiles": [g.tile(k) for k in range(g.counts.block_count)],
+           "kernel_ms_per_step": kernel_split(g, dt, 3)}
     g.close()
     return out
 
@@ -355,7 +372,8 @@ def bench_tet(args, device, torch):
     dof = g.counts.degree_of_freedom_count
     out = {"workload": f"tgv3d-euler-Ma0.3-{n}^3x6-tet-P3-HLLC", "elements": g.counts.element_count, "dof": dof,
            "value": dof * 3 * steps / (ms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": ms / steps,
-           "l2": f"state {8 * dof / 1e6:.0f} MB per buffer (L2 129 MB)", "tiles": [g.tile(0)]}
+           "l2": f"state {8 * dof / 1e6:.0f} MB per buffer (L2 129 MB)", "tiles": [g.tile(0)],
+           "kernel_ms_per_step": kernel_split(g, dt, 3)}
     g.close()
     return out
 
