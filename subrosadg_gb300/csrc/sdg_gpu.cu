@@ -158,6 +158,46 @@ __global__ void stateToPointKernel(const double* __restrict__ st, double* __rest
   }
 }
 
+// Point layout of a buffer that may be host memory the GPU reaches over the CPU-GPU link: per CTA a run of
+// whole elements, the point-layout side read or written as one contiguous stretch (consecutive threads,
+// consecutive addresses), the state-layout side through shared memory.  tile: [elements][nq][nv].
+// pointsToTensorStateKernel: tensor blocks (points are the nodes) from points to state;
+// stateToPointsTiledKernel: any block from state to points (phi null: tensor, else the dense Phi).
+__global__ void pointsToTensorStateKernel(const double* __restrict__ pts, double* __restrict__ st, int64_t ne, int nb,
+                                          int nv, int ustride, int epc) {
+  extern __shared__ double tile[];
+  const int64_t e0 = int64_t(blockIdx.x) * epc;
+  const int ecount = int(ne - e0 < epc ? ne - e0 : epc);
+  const int n = ecount * nb * nv;
+  const double* src = pts + e0 * nb * nv;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) tile[i] = src[i];
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int le = i / (nv * nb), r = i - le * nv * nb, v = r / nb, b = r - v * nb;
+    st[(e0 + le) * ustride + v * nb + b] = tile[(le * nb + b) * nv + v];
+  }
+}
+
+__global__ void stateToPointsTiledKernel(const double* __restrict__ st, double* __restrict__ pts,
+                                         const double* __restrict__ phi, int64_t ne, int nb, int nq, int nv,
+                                         int ustride, int epc) {
+  extern __shared__ double tile[];
+  const int64_t e0 = int64_t(blockIdx.x) * epc;
+  const int ecount = int(ne - e0 < epc ? ne - e0 : epc);
+  const int n = ecount * nq * nv;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const int le = i / (nv * nq), r = i - le * nv * nq, v = r / nq, q = r - v * nq;
+    const double* u = st + (e0 + le) * ustride + v * nb;
+    double s;
+    if (!phi) s = u[q];
+    else { s = 0.0; for (int b = 0; b < nb; ++b) s = fma(phi[q * nb + b], u[b], s); }
+    tile[(le * nq + q) * nv + v] = s;
+  }
+  __syncthreads();
+  double* dst = pts + e0 * nq * nv;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = tile[i];
+}
+
 // Transposes of the two conversions on dense blocks, for cotangents: st = Phi^T pts (of stateToPoint) and
 // pts = P^T st (of pointToState, P the least-squares projection [nb][nq]).
 __global__ void phiTransposeKernel(const double* __restrict__ pts, double* __restrict__ st, const double* __restrict__ phi,
@@ -739,6 +779,65 @@ int fail(sdg_handle* h, const Failure& f) {
 
 // Convert a point-layout array in h->scratch to the state buffer `which` (tensor: transpose; dense:
 // unweighted least-squares projection, InitialCondition.cpp:91-104).
+// The host buffer itself when it is pinned host memory the device reaches at the same address (page-locked
+// and mapped, as every cudaHostAlloc / cudaHostRegister allocation is under unified addressing), else null.
+const double* mappedHost(const double* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost && at.devicePointer == static_cast<const void*>(p) ? p : nullptr;
+}
+
+// Elements per CTA of the tiled conversions: the tile ([elements][nq][nv] doubles) within 48 KB.
+int conversionElements(const DevBlock& B, int nv) {
+  const int per = B.nq * nv;
+  return per > 6144 ? 1 : 6144 / per;
+}
+
+// Conserved variables at the volume points (point layout) -> state[which].  A pinned host buffer is read in
+// place over the CPU-GPU link on tensor blocks (one pass: transfer and transpose together); otherwise, and on
+// dense blocks (whose least-squares projection re-reads each point), the block's points are first copied to
+// the scratch buffer.
+void uploadPoints(sdg_handle* h, const double* conserved, int which) {
+  const double* mapped = mappedHost(conserved);
+  for (DevBlock& B : h->blocks) {
+    const size_t off = B.pointOffset * h->nv, count = size_t(B.ne) * B.nq * h->nv;
+    if (mapped && B.kind == kTensor) {
+      const int epc = conversionElements(B, h->nv);
+      const int64_t grid = (B.ne + epc - 1) / epc;
+      pointsToTensorStateKernel<<<unsigned(grid), 256, size_t(epc) * B.nq * h->nv * 8, h->stream>>>(
+          mapped + off, h->state[which] + B.stateOffset, B.ne, B.nb, h->nv, B.ustride, epc);
+    } else {
+      SDG_CUDA(cudaMemcpyAsync(h->scratch + off, conserved + off, count * 8, cudaMemcpyHostToDevice, h->stream));
+      const int grid = int((B.ne * B.nb + 255) / 256);
+      pointToStateKernel<<<grid, 256, 0, h->stream>>>(h->scratch + off, h->state[which] + B.stateOffset,
+                                                      B.kind == kDense ? B.lsqDev : nullptr, B.ne, B.nb, B.nq, h->nv,
+                                                      B.ustride);
+    }
+    checkLaunch(h);
+  }
+}
+
+// state[which] -> conserved variables at the volume points in a host buffer: written in place over the link
+// when it is pinned, else through the scratch buffer and one copy.
+void downloadPoints(sdg_handle* h, int which, double* conserved) {
+  double* mapped = const_cast<double*>(mappedHost(conserved));
+  double* dst = mapped ? mapped : h->scratch;
+  for (DevBlock& B : h->blocks) {
+    const int epc = conversionElements(B, h->nv);
+    const int64_t grid = (B.ne + epc - 1) / epc;
+    stateToPointsTiledKernel<<<unsigned(grid), 256, size_t(epc) * B.nq * h->nv * 8, h->stream>>>(
+        h->state[which] + B.stateOffset, dst + B.pointOffset * h->nv, B.kind == kDense ? B.phiDev : nullptr, B.ne,
+        B.nb, B.nq, h->nv, B.ustride, epc);
+    checkLaunch(h);
+  }
+  if (!mapped)
+    SDG_CUDA(cudaMemcpyAsync(conserved, h->scratch, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyDeviceToHost,
+                             h->stream));
+}
+
 void pointsToState(sdg_handle* h, int which) {
   for (DevBlock& B : h->blocks) {
     const int64_t work = B.ne * (B.kind == kTensor ? B.nb : B.nb);
@@ -1408,8 +1507,7 @@ int sdg_set_state_point(sdg_handle* h, const double* conserved) {
   if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
   SDG_API_BEGIN
   SDG_CUDA(cudaSetDevice(h->device));
-  SDG_CUDA(cudaMemcpyAsync(h->scratch, conserved, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyHostToDevice, h->stream));
-  pointsToState(h, 0);
+  uploadPoints(h, conserved, 0);
   traceAll(h, 0);
   if (h->gradInput == h->state[0]) h->gradInput = nullptr;
   SDG_CUDA(cudaStreamSynchronize(h->stream));
@@ -1467,8 +1565,7 @@ int sdg_get_state_point(sdg_handle* h, double* conserved) {
   if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
   SDG_API_BEGIN
   SDG_CUDA(cudaSetDevice(h->device));
-  stateToPoints(h, 0);
-  SDG_CUDA(cudaMemcpyAsync(conserved, h->scratch, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  downloadPoints(h, 0, conserved);
   SDG_CUDA(cudaStreamSynchronize(h->stream));
   return SDG_OK;
   SDG_API_END(h)

@@ -1,0 +1,47 @@
+"""Pinned host buffers: sdg_set_state_point / sdg_get_state_point read and write page-locked host memory in
+place (kernels over the CPU-GPU link); pageable buffers go through a staging copy.  Both paths run the same
+arithmetic, so the states and point values they produce are bit-identical."""
+import numpy as np
+import pytest
+
+import subrosadg_gb300 as sdg
+from tests import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def _pinned(n):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+
+
+@pytest.mark.parametrize("name,case", [
+    ("hex-p3", lambda: cases.tgv_case(n=4, p=3)),
+    ("hybrid-p4", lambda: cases.kh_case(n=6, p=4)),
+    ("tet-p2", lambda: cases.tet_tgv_case(n=3, p=2)),
+    ("line-p3", lambda: cases.sod_1d_case(n=9, p=3)),
+])
+def test_pinned_and_pageable_buffers_agree(name, case):
+    mesh, cfg, prim, _, dt, _ = case()
+    s = sdg.GpuSolver(mesh, cfg)
+    s.initialize_primitive(prim(s.volume_points()))
+    s.stepSolver(dt, 1)
+    nv = s.counts.conserved_variable_count
+    u = s.state_point()                      # pageable download
+    pin = _pinned(u.size).reshape(u.shape)
+    s.state_point(pin)                       # pinned download
+    np.testing.assert_array_equal(pin, u)
+    modal = s.state_modal()
+    rng = np.random.default_rng(3)
+    v = u * (1.0 + 1e-3 * rng.standard_normal(u.shape))
+    s.set_state_point(v)                     # pageable upload
+    a = s.state_modal()
+    pin[...] = v
+    s.set_state_point(pin)                   # pinned upload
+    np.testing.assert_array_equal(s.state_modal(), a)
+    assert not np.array_equal(a, modal)
+    out = _pinned(u.size).reshape(-1, nv)
+    s.state_point(out)
+    np.testing.assert_array_equal(out, s.state_point())
