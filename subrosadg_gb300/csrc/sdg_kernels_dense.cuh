@@ -609,6 +609,9 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
     }
     return false;
   }
+  // 0. the own traces are only needed through the jump 1/2 (U+ - U-): form it once per face point
+  for (int k = tid; k < ecount * FS; k += blockDim.x) sS[k] = 0.5 * (sO[k] - sS[k]);
+  __syncthreads();
   // 1. coefficients per (element, variable, basis function)
   for (int idx = tid; idx < ecount * NV * NB; idx += blockDim.x) {
     const int le = idx / (NV * NB), r = idx - le * NV * NB;
@@ -636,13 +639,13 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
 #pragma unroll
     for (int f = 0; f < NF; ++f) {
       const double* O = sO + le * FS + (f * NV + v) * NFQ;
-      const double* S = sS + le * FS + (f * NV + v) * NFQ;
+      const double* Jm = sS + le * FS + (f * NV + v) * NFQ;  // 1/2 (U+ - U-)
       const double* E = emod + (f * NB + i) * NFQ;
       double ep = 0.0, ej = 0.0;
 #pragma unroll
       for (int j = 0; j < NFQ; ++j) {
         ep = fma(E[j], O[j], ep);
-        ej = fma(E[j], 0.5 * (O[j] - S[j]), ej);
+        ej = fma(E[j], Jm[j], ej);
       }
 #pragma unroll
       for (int k = 0; k < DIM; ++k) {
@@ -677,12 +680,11 @@ __device__ __forceinline__ bool denseGradientAffineTile(const DenseGradArgs& a, 
 #pragma unroll
       for (int k = 0; k < DIM; ++k) acc[k] *= eps;
     } else if (a.br2) {
-      const double* O = sO + le * FS + (f * NV + v) * NFQ;
-      const double* S = sS + le * FS + (f * NV + v) * NFQ;
+      const double* Jm = sS + le * FS + (f * NV + v) * NFQ;
       const double* L = lmod + (f * NFQ + j) * NFQ;
       double lift = 0.0;
 #pragma unroll
-      for (int jj = 0; jj < NFQ; ++jj) lift = fma(L[jj], 0.5 * (O[jj] - S[jj]), lift);
+      for (int jj = 0; jj < NFQ; ++jj) lift = fma(L[jj], Jm[jj], lift);
       lift *= a.geom[e * GD + DIM * DIM];
 #pragma unroll
       for (int k = 0; k < DIM; ++k) acc[k] = fma(a.fmetric[(e * NF + f) * DIM + k], lift, acc[k]);
@@ -740,7 +742,8 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
     }
     return false;
   }
-  // values at the volume points
+  // values at the volume points; the own traces are only needed through {U} = 1/2 (U+ + U-) (volume part)
+  // and 1/2 [U] = U+ - {U} (lifts): the average replaces them, once per face point
   for (int idx = tid; idx < ecount * NV * NQ; idx += blockDim.x) {
     const int le = idx / (NV * NQ), r = idx - le * NV * NQ;
     const int v = r / NQ, q = r - v * NQ;
@@ -749,6 +752,7 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
     for (int b = 0; b < NB; ++b) acc = fma(phi[q * NB + b], sU[le * G::USTRIDE + v * NB + b], acc);
     sUq[(le * NV + v) * NQ + q] = acc;
   }
+  for (int k = tid; k < ecount * FS; k += blockDim.x) sS[k] = 0.5 * (sO[k] + sS[k]);
   __syncthreads();
   // gradient residuals (total, BR2 volume part)
   for (int idx = tid; idx < ecount * NV * NB; idx += blockDim.x) {
@@ -761,8 +765,8 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
       // outward n|J_f| of face f (per face point on curved blocks)
       const double* nF = a.fmetric + (a.fmetricPoint ? (e * NF + f) * NFQ + j : e * NF + f) * 2;
       const double w = phifw[fj * NB + i];
-      const double o = sO[le * FS + (f * NV + v) * NFQ + j], sv = sS[le * FS + (f * NV + v) * NFQ + j];
-      const double xt = w * o, xv = w * 0.5 * (o + sv);
+      const double o = sO[le * FS + (f * NV + v) * NFQ + j], avg = sS[le * FS + (f * NV + v) * NFQ + j];
+      const double xt = w * o, xv = w * avg;
       tot[0] = fma(xt, nF[0], tot[0]); tot[1] = fma(xt, nF[1], tot[1]);
       vol[0] = fma(xv, nF[0], vol[0]); vol[1] = fma(xv, nF[1], vol[1]);
     }
@@ -835,7 +839,7 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
       if (a.fmetricPoint) {  // curved: n|J_f| varies along the face
         for (int j = 0; j < NFQ; ++j) {
           const double* nF = a.fmetric + (((e0 + le) * NF + f) * NFQ + j) * 2;
-          const double jump = 0.5 * (sO[le * FS + (f * NV + v) * NFQ + j] - sS[le * FS + (f * NV + v) * NFQ + j]);
+          const double jump = sO[le * FS + (f * NV + v) * NFQ + j] - sS[le * FS + (f * NV + v) * NFQ + j];
           const double t = phifw[(f * NFQ + j) * NB + i] * jump;
           acc0 = fma(t, nF[0], acc0);
           acc1 = fma(t, nF[1], acc1);
@@ -844,7 +848,7 @@ __device__ __forceinline__ bool denseGradientTile(const DenseGradArgs& a, int64_
         const double* nF = a.fmetric + (e0 + le) * NF * 2 + f * 2;
         double acc = 0.0;
         for (int j = 0; j < NFQ; ++j) {
-          const double jump = 0.5 * (sO[le * FS + (f * NV + v) * NFQ + j] - sS[le * FS + (f * NV + v) * NFQ + j]);
+          const double jump = sO[le * FS + (f * NV + v) * NFQ + j] - sS[le * FS + (f * NV + v) * NFQ + j];
           acc = fma(phifw[(f * NFQ + j) * NB + i], jump, acc);
         }
         acc0 = acc * nF[0];

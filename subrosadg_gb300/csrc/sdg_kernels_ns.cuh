@@ -201,6 +201,11 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
     return false;
   }
   constexpr int GS = DIM * DIM + 1;
+  // BR2: the own traces are only needed through {U} = 1/2 (U+ + U-) (volume gradient) and 1/2 [U] = U+ - {U}
+  // (lift): form the average once per face point instead of once per node on its line
+  if constexpr (BR2) {
+    for (int k = tid; k < ecount * FS; k += blockDim.x) sS[k] = 0.5 * (sO[k] + sS[k]);
+  }
   int ax[DIM];
 #pragma unroll
   for (int b = 0; b < DIM; ++b) ax[b] = axisIndex<DIM, N>(node, b);
@@ -260,8 +265,8 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
         const int fm = T->axisFace[b][0], fp = T->axisFace[b][1];
         const int jm = T->nodeFacePoint[b][0][node], jp = T->nodeFacePoint[b][1][node];
         const double om = sO[le * FS + (fm * NV + v) * NFQ + jm], op = sO[le * FS + (fp * NV + v) * NFQ + jp];
-        const double sm = BR2 ? sS[le * FS + (fm * NV + v) * NFQ + jm] : 0.0;
-        const double sp = BR2 ? sS[le * FS + (fp * NV + v) * NFQ + jp] : 0.0;
+        const double am = BR2 ? sS[le * FS + (fm * NV + v) * NFQ + jm] : 0.0;  // {U} at the two ends
+        const double ap = BR2 ? sS[le * FS + (fp * NV + v) * NFQ + jp] : 0.0;
         if constexpr (AFFINE) {
           double dref = 0.0;
 #pragma unroll
@@ -271,7 +276,7 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
 #pragma unroll
           for (int k = 0; k < DIM; ++k) tot[k] = fma(ja[b][k], tt, tot[k]);
           if constexpr (BR2) {
-            const double tv = fma(lp, 0.5 * (op + sp), fma(-lm, 0.5 * (om + sm), -dref));
+            const double tv = fma(lp, ap, fma(-lm, am, -dref));
 #pragma unroll
             for (int k = 0; k < DIM; ++k) vol[k] = fma(ja[b][k], tv, vol[k]);
           }
@@ -284,7 +289,7 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
             for (int q = 0; q < N; ++q) dk = fma(T->dhat[q][ax[b]], P[q * st], dk);
             tot[k] = fma(lp * nF[b][1][k], op, fma(lm * nF[b][0][k], om, tot[k] - dk));
             if constexpr (BR2)
-              vol[k] = fma(lp * nF[b][1][k], 0.5 * (op + sp), fma(lm * nF[b][0][k], 0.5 * (om + sm), vol[k] - dk));
+              vol[k] = fma(lp * nF[b][1][k], ap, fma(lm * nF[b][0][k], am, vol[k] - dk));
           }
         }
       }
@@ -336,7 +341,7 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      const double jump = BR2 ? 0.5 * (sO[te * FS + (f * NV + v) * NFQ + j] - sS[te * FS + (f * NV + v) * NFQ + j]) : 0.0;
+      const double jump = BR2 ? sO[te * FS + (f * NV + v) * NFQ + j] - sS[te * FS + (f * NV + v) * NFQ + j] : 0.0;
 #pragma unroll
       for (int k = 0; k < DIM; ++k) {
         const double* gsrc = src + (te * NV * DIM + v * DIM + k) * NB + base;
