@@ -387,6 +387,7 @@ def bench_vortex(args, device, torch):
     mesh, cfg, prim, _, _, _ = wl.vortex_case(n=40, p=3, flux=sdg.ROE)
     g = sdg.GpuSolver(mesh, cfg, device=device)
     g.initialize_primitive(prim(g.volume_points()))
+    g.autotune()
     sp = ctypes.c_void_p()
     g.lib.sdg_get_stream(g.h, ctypes.byref(sp))
     stream = torch.cuda.ExternalStream(sp.value, device=device)
@@ -397,9 +398,12 @@ def bench_vortex(args, device, torch):
     ms = _timed(torch, stream, lambda: g.step_async(1e-3), steps)
     g.synchronize()
     dof = g.counts.degree_of_freedom_count
+    split = kernel_split(g, 1e-3, 20)
     out = {"workload": "vortex2d-euler-40^2-quad-P3-Roe-dt1e-3", "dof": dof, "steps": steps,
            "value": dof * 3 * steps / (ms * 1e-3), "unit": "DOF-stage/s", "us_per_step": 1e3 * ms / steps,
-           "note": "state L2-resident: latency and launch bound (graph replay of 7 launches per step)"}
+           "kernel_us_per_step": {k: 1e3 * v for k, v in split.items()},
+           "note": "state L2-resident: latency and launch bound (graph replay of 7 launches per step); "
+                   "kernel_us_per_step: device time of each class with every launch bracketed by events"}
     g.close()
     return out
 
@@ -434,12 +438,25 @@ def bench_adjoint(args, device, torch):
     lam1, mubar1 = s.adjoint_recorded(lamN)
     t_rev = time.perf_counter() - t0
     mem = ctypes_int64(s)
+    # the same gradient with every stage input kept in HBM by the forward sweep (no segment recompute)
+    s.set_adjoint_trajectory_store(True)
+    s.set_state_point(u0)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    lam2, mubar2 = s.adjoint_steps(dt, steps, lamN, checkpoint_interval=K)
+    t_adj2 = time.perf_counter() - t0
+    mem2 = ctypes_int64(s)
+    stored = {"adjoint_ms_per_step": 1e3 * t_adj2 / steps, "adjoint_over_forward": t_adj2 / t_fwd,
+              "equals_checkpointed": bool(np.array_equal(lam0, lam2) and mubar == mubar2), "bytes": mem2,
+              "note": "sdg_set_adjoint_trajectory_store: the forward sweep keeps all steps x 3 stage inputs "
+                      "when HBM has room; the reverse re-forms only each stage input's traces and gradient pass"}
+    s.set_adjoint_trajectory_store(False)
     out = {"workload": f"ns-tgv3d-BR1-Roe-Re1600-Ma0.1-{n}^3-hex-P3-{steps}steps-checkpoint{K}",
            "dof": s.counts.degree_of_freedom_count, "steps": steps, "J": J0,
            "forward_ms_per_step": 1e3 * t_fwd / steps, "adjoint_ms_per_step": 1e3 * t_adj / steps,
            "adjoint_over_forward": t_adj / t_fwd, "reverse_only_over_forward": t_rev / t_fwd,
            "recorded_equals_one_call": bool(np.array_equal(lam0, lam1) and mubar == mubar1),
-           "dJ_dmu": mubar, "checkpoint_bytes": mem,
+           "dJ_dmu": mubar, "checkpoint_bytes": mem, "trajectory_store": stored,
            "note": "wall-clock of synchronous calls; full adjoint = forward sweep with checkpoints + per-segment "
                    "recompute + reverse sweep"}
     if not args.no_adjoint_check:
@@ -596,7 +613,9 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
                      "kernel": "tensorStageKernel<3,4,affine>", "avg_launch_ms": elem_avg_ms,
-                     "algorithmic_bytes_per_launch": elem_bytes},
+                     "algorithmic_bytes_per_launch": elem_bytes,
+                     "binding": "fp64 pipe (CUDA-core DFMA; neither HBM nor tensor cores)",
+                     "binding_frac": (fp64_achieved / fp64.value) if fp64_achieved else None},
         "fp64": {"peak_gflops": fp64.value, "peak_source": "sdg_measure_fp64_peak (independent-chain DFMA probe)",
                  "achieved_gflops": fp64_achieved, "frac": (fp64_achieved / fp64.value) if fp64_achieved else None,
                  "achieved_source": "ncu FP64 instruction counts per element, mean of the 3 stage launches of a "

@@ -258,6 +258,12 @@ int sdg_measure_fp64_peak(int32_t device, double milliseconds, double* gflops);
  * shape 0: m8n8k4, 1: m16n8k4, 2: m16n8k8, 3: m16n8k16.  Compared with sdg_measure_fp64_peak it decides
  * whether the basis contractions gain anything from the tensor cores. */
 int sdg_measure_dmma_peak(int32_t device, int32_t shape, double milliseconds, double* gflops);
+/* Diagnostic: the device reciprocal every flux kernel uses for 1/rho and the wave-speed quotients
+ * (rcp.approx.ftz.f64 estimate + two Newton-Raphson steps), applied to x[0..n) on `device`: out[i] = rcp(x[i]).
+ * Host buffers.  Its accuracy is checked against IEEE 1/x by the tests: within 1 ulp for normal x whose
+ * reciprocal is normal (|x| in [2^-1022, 2^1022]); the flush-to-zero estimate leaves subnormal inputs
+ * and outputs outside that range (no density or pressure of a flow comes near it). */
+int sdg_probe_reciprocal(int32_t device, const double* x, double* out, int64_t n);
 
 /* Diagnostic: adjacency as canonical integer tuples, for bit-exact parity checks.
  * interior: [interior_face_count][7] = (typeL, elemL, faceL, typeR, elemR, faceR, rotation)
@@ -481,6 +487,12 @@ int sdg_surface_force(sdg_handle* handle, int32_t physical, double* force);
 /* Cotangent of direction . force with respect to the state ([volume_points][nv], the layout of the
  * adjoint's final cotangent): pressure and (Navier-Stokes) viscous stress through the gradient traces. */
 int sdg_surface_force_cotangent(sdg_handle* handle, int32_t physical, const double* direction, double* cotangent);
+/* Trajectory store (enable = 1; default 0): the forward sweep of sdg_adjoint_steps / sdg_forward_steps keeps
+ * every stage input of every step in device memory when it fits (step_count x stages states, with 2 GiB left
+ * free), and the reverse sweep reads them instead of recomputing each checkpoint interval from its checkpoint:
+ * it then re-forms only the traces and (Navier-Stokes) the gradient pass of each stage input.  Without room the
+ * checkpoint scheme runs.  Results are bit-identical between the two schemes. */
+int sdg_set_adjoint_trajectory_store(sdg_handle* handle, int32_t enable);
 /* Device bytes held for checkpoints, stage states and (Navier-Stokes, when HBM has room) the forward quantities
  * of one segment's stage inputs (grown on demand, released with the handle). */
 int sdg_adjoint_memory(sdg_handle* handle, int64_t* bytes);

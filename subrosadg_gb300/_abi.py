@@ -158,6 +158,7 @@ SIGNATURES = {
     "sdg_kernel_time": (c_int32, [c_void_p, _p_double, POINTER(c_int64)]),
     "sdg_measure_fp64_peak": (c_int32, [c_int32, c_double, _p_double]),
     "sdg_measure_dmma_peak": (c_int32, [c_int32, c_int32, c_double, _p_double]),
+    "sdg_probe_reciprocal": (c_int32, [c_int32, _p_double, _p_double, c_int64]),
     "sdg_delta_time_noalloc": (c_int32, [c_void_p, c_void_p, c_int64, c_int32, c_int32, c_int32, c_double, c_double,
                                          c_double, c_void_p, c_void_p]),
     "sdg_mesh_generate_2d": (c_int32, [c_double, c_double, c_double, c_double, c_int32, c_int32, c_double,
@@ -202,6 +203,7 @@ SIGNATURES = {
     "sdg_jvp_steps": (c_int32, [c_void_p, c_int32, c_double, _p_double, c_double, _p_double]),
     "sdg_adjoint_steps": (c_int32, [c_void_p, c_int32, c_double, c_int32, _p_double, _p_double, _p_double]),
     "sdg_adjoint_memory": (c_int32, [c_void_p, POINTER(c_int64)]),
+    "sdg_set_adjoint_trajectory_store": (c_int32, [c_void_p, c_int32]),
     "sdg_forward_steps": (c_int32, [c_void_p, c_int32, c_double, c_int32]),
     "sdg_adjoint_recorded": (c_int32, [c_void_p, _p_double, _p_double, _p_double]),
 }

@@ -50,6 +50,7 @@ struct Trajectory {
   uint64_t version = 0;   // the handle's state version at U_N
   int steps = 0, interval = 0, segments = 0;
   double dt = 0.0;
+  bool stored = false;    // every stage input kept by the forward sweep (no segment recompute)
 };
 
 struct AdjointState {
@@ -89,6 +90,7 @@ struct AdjointState {
   const double* curFace = nullptr;
   const double* curGrad = nullptr;
   const double* curFaceGrad = nullptr;
+  bool storeTrajectory = false;    // sdg_set_adjoint_trajectory_store: keep every stage input when HBM has room
 };
 
 namespace sdg {
@@ -465,17 +467,53 @@ void jvpSteps(sdg_handle* h, int steps, double dt, double dmu) {
   h->gradInput = stepGradientInput(h);
 }
 
+void releaseForwardStore(sdg_handle* h);
+
+// Pool buffers [first, first + count) allocated, when the device keeps at least 2 GiB free beside the ones
+// still missing; false (nothing allocated) otherwise.
+bool reservePool(sdg_handle* h, size_t first, size_t count) {
+  AdjointState* A = h->adj;
+  const size_t have = A->pool.size() > first ? std::min(A->pool.size() - first, count) : 0;
+  const size_t missing = count - have;
+  size_t freeB = 0, totalB = 0;
+  SDG_CUDA(cudaMemGetInfo(&freeB, &totalB));
+  if (missing * h->stateCount * sizeof(double) + (size_t(2) << 30) > freeB) return false;
+  for (size_t i = 0; i < count; ++i) poolBuffer(h, first + i);
+  return true;
+}
+
 // Forward sweep of `steps` steps from the current state U_0, keeping U every `interval` steps
-// (pool[0..segments)) and U_N (pool[segments]); records the trajectory for the reverse sweep.
+// (pool[0..segments)) and U_N (pool[segments]); records the trajectory for the reverse sweep.  With the
+// trajectory store on and HBM room for all steps x stages states, every stage input is kept as well
+// (pool[segments + 1 + n S + s]): the reverse sweep then reads them instead of recomputing each segment.
 void forwardSweep(sdg_handle* h, int steps, double dt, int interval) {
   AdjointState* A = h->adj;
   const int segments = (steps + interval - 1) / interval;
+  const int S = h->cfg.time_integration + 1;
+  const size_t storeBase = size_t(segments) + 1;
   std::vector<Rec> recs;
   emitStep(h, dt, true, recs);
-  for (int g = 0; g < segments; ++g) {
-    copyState(h, poolBuffer(h, g), h->state[0]);
-    const int n = std::min(interval, steps - g * interval);
-    for (int k = 0; k < n; ++k) runRecs(h, recs, h->stream);
+  bool stored = false;
+  if (A->storeTrajectory) {
+    releaseForwardStore(h);  // the stored trajectory replaces the per-segment forward store
+    stored = reservePool(h, 0, storeBase + size_t(steps) * S);
+  }
+  if (stored) {
+    std::vector<std::vector<Rec>> stage(S);  // the step's records by stage (the reduction with the last)
+    for (const Rec& r : recs) stage[std::min(S - 1, r.seq / 8)].push_back(r);
+    for (int n = 0; n < steps; ++n) {
+      if (n % interval == 0) copyState(h, poolBuffer(h, n / interval), h->state[0]);
+      for (int s = 0; s < S; ++s) {
+        copyState(h, poolBuffer(h, storeBase + size_t(n) * S + s), h->state[s == 0 ? 0 : 1]);
+        runRecs(h, stage[s], h->stream);
+      }
+    }
+  } else {
+    for (int g = 0; g < segments; ++g) {
+      copyState(h, poolBuffer(h, g), h->state[0]);
+      const int n = std::min(interval, steps - g * interval);
+      for (int k = 0; k < n; ++k) runRecs(h, recs, h->stream);
+    }
   }
   copyState(h, poolBuffer(h, segments), h->state[0]);
   h->stateVersion++;
@@ -483,6 +521,7 @@ void forwardSweep(sdg_handle* h, int steps, double dt, int interval) {
   A->traj.valid = true;
   A->traj.version = h->stateVersion;
   A->traj.steps = steps; A->traj.interval = interval; A->traj.segments = segments; A->traj.dt = dt;
+  A->traj.stored = stored;
 }
 
 // Doubles of one stored stage input: traces, node gradient, gradient traces.
@@ -511,6 +550,12 @@ bool forwardStore(sdg_handle* h, size_t slots) {
 }
 
 double* fwdSlot(sdg_handle* h, size_t i) { return h->adj->fwdStore + i * fwdSlotSize(h); }
+
+void releaseForwardStore(sdg_handle* h) {
+  AdjointState* A = h->adj;
+  if (A->fwdStore) cudaFree(A->fwdStore);
+  A->fwdStore = nullptr; A->fwdSlots = 0; A->fwdTried = false;
+}
 
 // Keep the traces of the current stage input (h->face) in stored slot i.
 void keepTraces(sdg_handle* h, size_t i) {
@@ -559,7 +604,8 @@ double backwardSweep(sdg_handle* h) {
   const double dt = T.dt;
   const size_t storeBase = size_t(segments) + 1;
   const auto stages = stepByStage(h, dt, S);
-  const bool keep = forwardStore(h, size_t(interval) * S);
+  const bool stored = T.stored;  // every stage input kept by the forward sweep: no recompute
+  const bool keep = !stored && forwardStore(h, size_t(interval) * S);
   SDG_CUDA(cudaMemsetAsync(A->lamBase, 0, h->stateCount * 8, h->stream));
   SDG_CUDA(cudaMemsetAsync(A->muAcc, 0, 8, h->stream));
   if (!A->ghostPending) clearGhost(h);  // a functional's cotangent may have left its own ghost part
@@ -569,23 +615,25 @@ double backwardSweep(sdg_handle* h) {
     const int n0 = g * interval, n1 = std::min(steps, n0 + interval);
     // recompute the segment from its checkpoint, keeping every stage input (and, with room, its forward
     // quantities: the flux records leave the traces, gradient and gradient traces of the stage input)
-    copyState(h, h->state[0], poolBuffer(h, g));
-    traces(h, h->state[0], h->face);
-    for (int n = n0; n < n1; ++n)
-      for (int s = 0; s < S; ++s) {
-        const size_t slot = size_t(n - n0) * S + s;
-        copyState(h, poolBuffer(h, storeBase + slot), h->state[s == 0 ? 0 : 1]);
-        if (keep) {
-          keepTraces(h, slot);
-          runRecs(h, intoSlot(h, stages[s], slot), h->stream);
-        } else {
-          runRecs(h, stages[s], h->stream);
+    if (!stored) {
+      copyState(h, h->state[0], poolBuffer(h, g));
+      traces(h, h->state[0], h->face);
+      for (int n = n0; n < n1; ++n)
+        for (int s = 0; s < S; ++s) {
+          const size_t slot = size_t(n - n0) * S + s;
+          copyState(h, poolBuffer(h, storeBase + slot), h->state[s == 0 ? 0 : 1]);
+          if (keep) {
+            keepTraces(h, slot);
+            runRecs(h, intoSlot(h, stages[s], slot), h->stream);
+          } else {
+            runRecs(h, stages[s], h->stream);
+          }
         }
-      }
+    }
     // reverse
     for (int n = n1 - 1; n >= n0; --n)
       for (int s = S - 1; s >= 0; --s) {
-        const size_t slot = size_t(n - n0) * S + s;
+        const size_t slot = stored ? size_t(n) * S + s : size_t(n - n0) * S + s;
         copyState(h, h->state[1], poolBuffer(h, storeBase + slot));
         if (keep) useForward(h, slot);
         else forwardAt(h, h->state[1]);
@@ -874,6 +922,18 @@ int sdg_adjoint_boundary_cotangent(sdg_handle* h, double* out) {
     SDG_CUDA(cudaSetDevice(h->device));
     SDG_CUDA(cudaMemcpyAsync(out, A->lamGhost, n * 8, cudaMemcpyDeviceToHost, h->stream));
     SDG_CUDA(cudaStreamSynchronize(h->stream));
+  } catch (const Failure& f) {
+    return adjFail(h, f);
+  }
+  return SDG_OK;
+}
+
+int sdg_set_adjoint_trajectory_store(sdg_handle* h, int32_t enable) {
+  if (!h || (enable != 0 && enable != 1)) return SDG_ERR_INVALID_ARGUMENT;
+  try {
+    AdjointState* A = adjoint(h);
+    A->storeTrajectory = enable != 0;
+    A->traj.valid = false;  // a recorded trajectory was kept under the other scheme
   } catch (const Failure& f) {
     return adjFail(h, f);
   }

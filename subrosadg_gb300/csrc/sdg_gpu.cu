@@ -597,7 +597,16 @@ Rec faceRec(sdg_handle* h, int op) {
   f.conn = bnd ? h->bconn : h->fconn; f.fgeo = bnd ? h->bgeo : h->fgeo; f.ghost = h->ghost;
   f.nface = bnd ? h->nBoundary : h->nInterior; f.n1d = h->n1d; f.ph = h->ph; f.perm = h->facePerm;
   f.fgeoPoint = h->curved ? 1 : 0;
-  r.units = (f.nface * h->nfq + kFaceThreads - 1) / kFaceThreads;
+  const int64_t points = f.nface * h->nfq;
+  r.units = (points + kFaceThreads - 1) / kFaceThreads;
+  // one thread per face point does a whole Riemann flux in FP64: with fewer points than two full CTAs per SM,
+  // narrower CTAs spread them over every SM instead of leaving most SMs idle (one-instance launches only)
+  const int64_t sms = h->hostOnly ? 0 : multiprocessorCount(h->device);
+  if (points > 0 && points < sms * 2 * kFaceThreads) {
+    const int64_t t = std::min<int64_t>(kFaceThreads, std::max<int64_t>(32, ((points + 2 * sms - 1) / (2 * sms) + 31) / 32 * 32));
+    r.soloThreads = int(t);
+    r.soloUnits = (points + t - 1) / t;
+  }
   return r;
 }
 
@@ -687,8 +696,10 @@ void launchOne(const Rec& r, cudaStream_t s) {
     default: p[0] = const_cast<RelArgs*>(&r.ra); break;
   }
   if (r.units <= 0) return;
-  if (r.units > 0x7fffffffLL) throw Failure(SDG_ERR_UNSUPPORTED, "launch exceeds the grid limit");
-  SDG_CUDA(cudaLaunchKernel(r.fn, dim3(unsigned(r.units)), dim3(unsigned(r.threads)), p, r.smem, s));
+  const int64_t units = r.soloThreads ? r.soloUnits : r.units;
+  const int threads = r.soloThreads ? r.soloThreads : r.threads;
+  if (units > 0x7fffffffLL) throw Failure(SDG_ERR_UNSUPPORTED, "launch exceeds the grid limit");
+  SDG_CUDA(cudaLaunchKernel(r.fn, dim3(unsigned(units)), dim3(unsigned(threads)), p, r.smem, s));
 }
 
 }  // namespace
@@ -949,6 +960,11 @@ double measureFp64Peak(int device, double ms) {
   });
   cudaFree(out);
   return r;
+}
+
+__global__ void reciprocalProbeKernel(const double* __restrict__ x, double* __restrict__ r, int64_t n) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) r[i] = rcp(x[i]);
 }
 
 double measureDmmaPeak(int device, int shape, double ms) {
@@ -1794,6 +1810,25 @@ int sdg_measure_dmma_peak(int32_t device, int32_t shape, double milliseconds, do
   try {
     *gflops = measureDmmaPeak(device, shape, milliseconds);
   } catch (const Failure& f) {
+    g_create_error = f.what();
+    return f.code;
+  }
+  return SDG_OK;
+}
+
+int sdg_probe_reciprocal(int32_t device, const double* x, double* out, int64_t n) {
+  if (!x || !out || n <= 0 || n > (int64_t(1) << 30)) return SDG_ERR_INVALID_ARGUMENT;
+  double* d = nullptr;
+  try {
+    SDG_CUDA(cudaSetDevice(device));
+    SDG_CUDA(cudaMalloc(&d, size_t(n) * 16));
+    SDG_CUDA(cudaMemcpy(d, x, size_t(n) * 8, cudaMemcpyHostToDevice));
+    reciprocalProbeKernel<<<unsigned((n + 255) / 256), 256>>>(d, d + n, n);
+    SDG_CUDA(cudaGetLastError());
+    SDG_CUDA(cudaMemcpy(out, d + n, size_t(n) * 8, cudaMemcpyDeviceToHost));
+    SDG_CUDA(cudaFree(d));
+  } catch (const Failure& f) {
+    if (d) cudaFree(d);
     g_create_error = f.what();
     return f.code;
   }

@@ -88,6 +88,8 @@ struct Rec {
   int threads = 0, epb = 0;
   size_t smem = 0;
   int64_t units = 0;               // CTAs of the one-instance launch (tiles / point chunks / variables)
+  int soloThreads = 0;             // face records of small meshes: narrower CTAs for the one-instance launch
+  int64_t soloUnits = 0;           // (the batched work lists keep threads / units)
   StageArgs sa;
   Phys ph;
   GradArgs ga;

@@ -411,6 +411,17 @@ class GpuSolver:
         self._chk(self.lib.sdg_adjoint_steps(self.h, steps, dt, checkpoint_interval, _ptr(c), _ptr(out), byref(mu)))
         return out, mu.value
 
+    def adjoint_memory(self):
+        """Device bytes held by the adjoint's checkpoints, stage states and forward store."""
+        b = c_int64()
+        self._chk(self.lib.sdg_adjoint_memory(self.h, byref(b)))
+        return b.value
+
+    def set_adjoint_trajectory_store(self, enable=True):
+        """Keep every stage input of the forward sweep in device memory when it fits, so the reverse sweep
+        recomputes no checkpoint interval (sdg_set_adjoint_trajectory_store)."""
+        self._chk(self.lib.sdg_set_adjoint_trajectory_store(self.h, 1 if enable else 0))
+
     def forward_steps(self, dt, steps, checkpoint_interval=25):
         """Advance `steps` steps keeping the checkpoints of the trajectory (for adjoint_recorded)."""
         self._chk(self.lib.sdg_forward_steps(self.h, steps, dt, checkpoint_interval))
