@@ -90,7 +90,6 @@ struct AdjointState {
   const double* curFace = nullptr;
   const double* curGrad = nullptr;
   const double* curFaceGrad = nullptr;
-  bool storeTrajectory = false;    // sdg_set_adjoint_trajectory_store: keep every stage input when HBM has room
 };
 
 namespace sdg {
@@ -494,7 +493,7 @@ void forwardSweep(sdg_handle* h, int steps, double dt, int interval) {
   std::vector<Rec> recs;
   emitStep(h, dt, true, recs);
   bool stored = false;
-  if (A->storeTrajectory) {
+  if (h->adjointTrajectoryStore) {
     releaseForwardStore(h);  // the stored trajectory replaces the per-segment forward store
     stored = reservePool(h, 0, storeBase + size_t(steps) * S);
   }
@@ -930,13 +929,8 @@ int sdg_adjoint_boundary_cotangent(sdg_handle* h, double* out) {
 
 int sdg_set_adjoint_trajectory_store(sdg_handle* h, int32_t enable) {
   if (!h || (enable != 0 && enable != 1)) return SDG_ERR_INVALID_ARGUMENT;
-  try {
-    AdjointState* A = adjoint(h);
-    A->storeTrajectory = enable != 0;
-    A->traj.valid = false;  // a recorded trajectory was kept under the other scheme
-  } catch (const Failure& f) {
-    return adjFail(h, f);
-  }
+  h->adjointTrajectoryStore = enable != 0;
+  if (h->adj) h->adj->traj.valid = false;  // a recorded trajectory was kept under the other scheme
   return SDG_OK;
 }
 

@@ -158,6 +158,7 @@ struct sdg_handle {
   int64_t graphKernels = 0;
   int64_t elements = 0, dof = 0;
   struct AdjointState* adj = nullptr;  // tangent-linear / adjoint buffers, created on first use
+  bool adjointTrajectoryStore = false; // sdg_set_adjoint_trajectory_store: keep every stage input when HBM has room
   uint64_t stateVersion = 0;          // bumped by every call that changes the state or the physics
   std::string err;
 };
