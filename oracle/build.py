@@ -24,7 +24,8 @@ VARIANTS = {"liborc.so": [], "liborc_ext.so": ["-DORC_REAL=long double"]}
 
 def _build_one(target, extra, force):
     srcs = [os.path.join(HERE, f) for f in ("sdg_oracle.cpp", "orc_basis.hpp", "orc_physics.hpp", "build.py")]
-    srcs += [os.path.join(ROOT, "subrosadg_gb300", "csrc", "triangle_rules.h"), os.path.join(ROOT, "include", "sdg_gpu.h")]
+    srcs += [os.path.join(ROOT, "subrosadg_gb300", "csrc", f) for f in ("triangle_rules.h", "tetrahedron_rules.h")]
+    srcs += [os.path.join(ROOT, "include", "sdg_gpu.h")]
     if not force and os.path.exists(target) and all(os.path.getmtime(s) <= os.path.getmtime(target) for s in srcs):
         return target
     cxx = os.environ.get("CXX") or shutil.which("g++") or "g++"

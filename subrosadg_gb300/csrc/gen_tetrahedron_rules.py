@@ -8,6 +8,9 @@ counts are
   triangle face, orders 3/5/7      : 4 / 7 / 13 points (kTriangleQuadratureNumber), the counts of
       D.A. Dunavant, "High degree efficient symmetrical Gaussian quadrature rules for the triangle",
       IJNME 21 (1985).
+For P = 4 the face rule is Dunavant's degree-9 rule (19 points, the reference's count); the volume rule of
+order 8 is the Grundmann-Moeller rule s = 4 (70 points, exact to degree 9) in place of gmsh's 43-point rule,
+whose values are not in the reference tree.
 This script takes the published orbit structure and starting values, polishes them with Newton's method
 on the moment equations so every monomial up to the rule's degree is integrated to round-off, and writes
 the rules on the reference elements (0,0,0),(1,0,0),(0,1,0),(0,0,1) (weights summing to 1/6) and
@@ -102,6 +105,12 @@ FACE_RULES = {
     7: (["c", "s21", "s21", "s111"], [-0.149570044467682, 0.260345966079040, 0.175615257433208,
                                       0.065130102902216, 0.053347235608838,
                                       0.048690315425316, 0.312865496004874, 0.077113760890257]),
+    9: (["c", "s21", "s21", "s21", "s21", "s111"], [0.097135796282799,
+                                                     0.489682519198738, 0.031334700227139,
+                                                     0.437089591492937, 0.077827541004774,
+                                                     0.188203535619033, 0.079647738927210,
+                                                     0.044729513394453, 0.025577675658698,
+                                                     0.036838412054736, 0.221962989160766, 0.043283539377289]),
 }
 # Keast's rules of degree 2, 4 and 6: orbit structure and published values (weights for volume 1/6).
 VOLUME_RULES = {
@@ -113,6 +122,38 @@ VOLUME_RULES = {
                                         0.322337890142276, 0.009226196923942,
                                         0.063661001875018, 0.269672331458316, 0.008035714285714]),
 }
+
+
+def compositions(total, parts):
+    """All tuples of `parts` non-negative integers summing to `total`, in lexicographic order."""
+    if parts == 1:
+        yield (total,)
+        return
+    for first in range(total, -1, -1):
+        for rest in compositions(total - first, parts - 1):
+            yield (first,) + rest
+
+
+def grundmann_moeller(s, n=3):
+    """The Grundmann-Moeller rule of degree 2s+1 on the n-simplex of volume 1/n! (A. Grundmann, H.M. Moeller,
+    "Invariant integration formulas for the n-simplex by combinatorial methods", SIAM J. Numer. Anal. 15 (1978)):
+    Q[f] = sum_{i=0..s} (-1)^i 2^{-2s} (d+n-2i)^d / (i! (d+n-i)!) sum_{|b| = s-i} f((2 b_j + 1)/(d+n-2i)),
+    d = 2s+1, the points in barycentric coordinates; coinciding points of different levels are merged."""
+    d = 2 * s + 1
+    pts, ws = [], []
+    for i in range(s + 1):
+        den = d + n - 2 * i
+        wt = (-1) ** i * 2.0 ** (-2 * s) * den ** d / (math.factorial(i) * math.factorial(d + n - i))
+        for beta in compositions(s - i, n + 1):
+            x = tuple((2 * b + 1) / den for b in beta[1:])
+            for k, q in enumerate(pts):
+                if max(abs(a - c) for a, c in zip(q, x)) < 1e-15:
+                    ws[k] += wt
+                    break
+            else:
+                pts.append(x)
+                ws.append(wt)
+    return np.array(pts), np.array(ws)
 
 
 def polish(resid, orbits, x0, deg):
@@ -184,6 +225,26 @@ def main():
         print(f"inline constexpr double kTet{deg}Zeta[{n}] = {{{fmt(p[:, 2])}}};")
         print(f"inline constexpr double kTet{deg}W[{n}] = {{{fmt(w)}}};")
         vols.append((deg, n))
+    # order 8 (P4): the reference's gmsh rule has 43 points and is not restated here (gmsh is not vendored);
+    # the Grundmann-Moeller rule s = 4 (degree 9, 70 points) integrates every order-8 integrand exactly
+    p, w = grundmann_moeller(4)
+    # the alternating-sign weights of the closed form lose ~1e-16 to cancellation: refine them on the rounded
+    # points by least squares on the exact moments, residuals summed exactly (math.fsum)
+    mom = [(a, b, c) for a in range(10) for b in range(10 - a) for c in range(10 - a - b)]
+    V = np.array([p[:, 0] ** a * p[:, 1] ** b * p[:, 2] ** c for a, b, c in mom])
+    for _ in range(3):
+        r = np.array([tet_exact(a, b, c) - math.fsum(V[k] * w) for k, (a, b, c) in enumerate(mom)])
+        w = w + np.linalg.lstsq(V, r, rcond=None)[0]
+    err = max(abs((w * p[:, 0] ** a * p[:, 1] ** b * p[:, 2] ** c).sum() - tet_exact(a, b, c))
+              for a in range(10) for b in range(10 - a) for c in range(10 - a - b))
+    assert err < 1e-15, err
+    n = len(w)
+    print(f"// volume order 8: Grundmann-Moeller s = 4 (exact to degree 9), {n} points, max moment error {err:.1e}")
+    print(f"inline constexpr double kTet8Xi[{n}] = {{{fmt(p[:, 0])}}};")
+    print(f"inline constexpr double kTet8Eta[{n}] = {{{fmt(p[:, 1])}}};")
+    print(f"inline constexpr double kTet8Zeta[{n}] = {{{fmt(p[:, 2])}}};")
+    print(f"inline constexpr double kTet8W[{n}] = {{{fmt(w)}}};")
+    vols.append((8, n))
     print("inline constexpr FaceTriangleRule kFaceTriangleRules[] = {")
     for deg, n in faces:
         print(f"    {{{deg}, {n}, kFaceTri{deg}Xi, kFaceTri{deg}Eta, kFaceTri{deg}W}},")

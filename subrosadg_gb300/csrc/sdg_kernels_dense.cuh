@@ -212,7 +212,11 @@ struct DenseShape {
   static constexpr int FSTRIDE = NF * NV * NFQ;
   static_assert(DIM * NQ >= NB && NV * NB >= NQ, "shared-memory reuse of the point and coefficient buffers");
   static constexpr int PER_ELEM = USTRIDE + FSTRIDE + DIM * NV * NQ + NV * NB + NV * NB;
-  static constexpr int EPB = 16;
+  static constexpr size_t TABLES_MAX_ = size_t(NQ) * NB * (2 + DIM) + size_t(NFP) * NB * 2 + size_t(NB) * NB;
+  // 16 elements per CTA, fewer where the tile and its tables would exceed the 227 KB opt-in shared memory
+  static constexpr long long EPB_FIT =
+      (227LL * 1024 - 16 - 8LL * NV * 8 - (long long)TABLES_MAX_ * 8) / ((long long)PER_ELEM * 8);
+  static constexpr int EPB = EPB_FIT < 16 ? (EPB_FIT > 0 ? int(EPB_FIT) : 1) : 16;
   static constexpr int THREADS = 256;
   // staged tables: bilinear blocks the original layout (M^-1 per element), affine blocks the folded one
   static constexpr size_t TABLES = size_t(NQ) * NB * (1 + DIM) + size_t(NFP) * NB * 2 + size_t(NB) * NB;
@@ -908,10 +912,15 @@ __global__ void __launch_bounds__(kMaxTileThreads)
 
 // Tetrahedra (dense blocks of DIM 3, affine): P = 1..3 with the Keast rules of 4, 11, 24 points and the
 // Dunavant face rules of 4, 7, 13 points.
-#define SDG_TET_CASES(X)                        \
+#define SDG_TET_ADJOINT_CASES(X)                \
   X(SDG_ELEMENT_TETRAHEDRON, 1, 4, 4, 4, 4)     \
   X(SDG_ELEMENT_TETRAHEDRON, 2, 10, 11, 7, 4)   \
   X(SDG_ELEMENT_TETRAHEDRON, 3, 20, 24, 13, 4)
+// P4: 35 modes, the 69-point Grundmann-Moeller volume rule (tetrahedron_rules.h), 19-point faces; stage and
+// gradient kernels only (its derivative kernels' tables would not fit the shared memory)
+#define SDG_TET_CASES(X)                        \
+  SDG_TET_ADJOINT_CASES(X)                      \
+  X(SDG_ELEMENT_TETRAHEDRON, 4, 35, 69, 19, 4)
 
 // (type, P) -> (NB, NQ, NFQ): triangle P1..P5 use Dunavant rules of 3,6,12,16,25 points.
 

@@ -60,7 +60,7 @@ void adjointDenseKernels(int type, int p, bool affine, bool gen, bool visc, bool
     else tetOf<NB, NQ, NFQ, NF, false>(k, gen, false);                                   \
     return;                                                                              \
   }
-  SDG_TET_CASES(SDG_ADT)
+  SDG_TET_ADJOINT_CASES(SDG_ADT)
 #undef SDG_ADT
 }
 

@@ -380,6 +380,12 @@ def test_derivatives_refuse_unsupported_configurations():
     with pytest.raises(sdg.SdgError) as e:
         walls.vjp_residual(np.zeros((walls.counts.volume_point_count, 4)))
     assert e.value.code == _abi.SDG_ERR_UNSUPPORTED
+    mesh, cfg, ic, _, _, _ = cases.tet_tgv_case(n=3, p=4, flux=sdg.ROE)  # tetrahedra P4: no derivative kernels
+    tet = sdg.GpuSolver(mesh, cfg, device=0)
+    tet.initialize_primitive(ic(tet.volume_points()))
+    with pytest.raises(sdg.SdgError) as e:
+        tet.vjp_residual(np.zeros((tet.counts.volume_point_count, 5)))
+    assert e.value.code == _abi.SDG_ERR_UNSUPPORTED
 
 
 def test_recorded_trajectory_adjoint_equals_the_one_call_adjoint():

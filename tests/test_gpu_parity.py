@@ -109,6 +109,17 @@ CASES = {
         conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
                     sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL)),
     "ns-tet-box-p1-br1-hllc": lambda: cases.tet_box_case(p=1, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01),
+    # tetrahedra P4 (35 modes, the 69-point Grundmann-Moeller volume rule, 19-point Dunavant faces)
+    "tet-tgv-p4-hllc": lambda: cases.tet_tgv_case(n=3, p=4, flux=sdg.HLLC, steps=2),
+    "tet-tgv-p4-roe": lambda: cases.tet_tgv_case(n=3, p=4, flux=sdg.ROE, steps=2),
+    "ns-tet-tgv-p4-br2-lf": lambda: cases.tet_tgv_case(n=3, p=4, flux=sdg.LAX_FRIEDRICHS, steps=2, viscous=sdg.BR2,
+                                                       mu=0.02),
+    "ns-tet-walls-p4-br1-hllc": lambda: cases.tet_box_case(
+        p=4, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01, steps=2,
+        conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
+                    sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL)),
+    "inc-lidcavity-tet-p4-exact-br2": lambda: cases.cavity_3d_case(p=4, viscous=sdg.BR2, mu=1e-2, steps=2, tets=True),
+    "av-shocktube-tet-p4-hllc": lambda: cases.shock_tube_case(p=4, dim=3, n=6, steps=2, tets=True),
     "inc-euler-cavity-tet-p2-exact": lambda: cases.cavity_3d_case(p=2, viscous=None, mu=0.0, tets=True),
     "inc-lidcavity-tet-p2-exact-br1": lambda: cases.cavity_3d_case(p=2, mu=1e-2, tets=True),
     "inc-thermalcavity-tet-p3-lf-br2-boussinesq": lambda: cases.cavity_3d_case(
