@@ -50,7 +50,7 @@ enum sdg_element_type { /* gmsh first-order type numbers (src/Solver/SimulationC
   SDG_ELEMENT_LINE = 1,     /* DimensionEnum::D1 / MeshModelEnum::Line; its faces are points */
   SDG_ELEMENT_TRIANGLE = 2,
   SDG_ELEMENT_QUADRANGLE = 3,
-  SDG_ELEMENT_TETRAHEDRON = 4, /* dense modal blocks, P = 1..4, every equation model and the artificial
+  SDG_ELEMENT_TETRAHEDRON = 4, /* dense modal blocks, P = 1..5, every equation model and the artificial
                                   viscosity, and their derivatives for P = 1..3 (not of the artificial
                                   viscosity)                                                          */
   SDG_ELEMENT_HEXAHEDRON = 5

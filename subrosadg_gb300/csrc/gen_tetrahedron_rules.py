@@ -37,19 +37,25 @@ def tet_exact(a, b, c):
     return math.factorial(a) * math.factorial(b) * math.factorial(c) / math.factorial(a + b + c + 3)
 
 
-def tri_build(params, orbits):
+def tri_build(params, orbits, alt=False):
+    """Points and weights of a symmetric triangle rule.  The orbits are listed in the order the reference's
+    Triangle permutation tables imply: for P1..P4 (a,a), (a,1-2a), (1-2a,a) and (x,y), (y,z), (z,x), (x,z),
+    (y,x), (z,y); for P5 (`alt`: its table swaps rotations 1 and 2 against that order) (a,a), (1-2a,a),
+    (a,1-2a) and (x,y), (z,x), (y,z), (z,y), (y,x), (x,z)."""
     pts, w, k = [], [], 0
     for o in orbits:
         if o == "c":
             pts.append((1 / 3, 1 / 3)); w.append(params[k]); k += 1
         elif o == "s21":
             a, wt = params[k], params[k + 1]; k += 2
-            for p in [(a, a), (a, 1 - 2 * a), (1 - 2 * a, a)]:
+            orbit = [(a, a), (a, 1 - 2 * a), (1 - 2 * a, a)]
+            for p in ([orbit[i] for i in (0, 2, 1)] if alt else orbit):
                 pts.append(p); w.append(wt)
         else:
             x, y, wt = params[k], params[k + 1], params[k + 2]; k += 3
             z = 1 - x - y
-            for p in [(x, y), (y, z), (z, x), (x, z), (y, x), (z, y)]:
+            orbit = [(x, y), (y, z), (z, x), (x, z), (y, x), (z, y)]
+            for p in ([orbit[i] for i in (0, 2, 1, 5, 4, 3)] if alt else orbit):
                 pts.append(p); w.append(wt)
     return np.array(pts), np.array(w)
 
@@ -111,6 +117,14 @@ FACE_RULES = {
                                                      0.188203535619033, 0.079647738927210,
                                                      0.044729513394453, 0.025577675658698,
                                                      0.036838412054736, 0.221962989160766, 0.043283539377289]),
+    # degree 11: 27 points, one orbit outside the triangle (Dunavant's rule as published)
+    11: (["s21"] * 5 + ["s111"] * 2, [0.534611048270758, 0.000927006328961,
+                                       0.398969302965855, 0.077149534914813,
+                                       0.203309900431282, 0.059322977380774,
+                                       0.119350912282581, 0.036184540503418,
+                                       0.032364948111276, 0.013659731002678,
+                                       0.050178138310495, 0.356620648261293, 0.052337111962204,
+                                       0.021022016536166, 0.171488980304042, 0.020707659639141]),
 }
 # Keast's rules of degree 2, 4 and 6: orbit structure and published values (weights for volume 1/6).
 VOLUME_RULES = {
@@ -203,8 +217,10 @@ def main():
         x = polish(tri_resid, orb, x0, deg)
         err = np.abs(tri_resid(x, orb, deg)).max()
         assert err < 1e-15, (deg, err)
-        assert np.abs(x - x0).max() < 1e-11, (deg, np.abs(x - x0).max())
-        p, w = tri_build(x, orb)
+        # the published 15 digits move by up to 4e-11 on the degree-11 rule (an orbit outside the triangle
+        # makes its moment system ill-conditioned)
+        assert np.abs(x - x0).max() < (1e-10 if deg == 11 else 1e-11), (deg, np.abs(x - x0).max())
+        p, w = tri_build(x, orb, alt=deg == 11)
         n = len(w)
         print(f"// face degree {deg}: {n} points, max moment error {err:.1e}")
         print(f"inline constexpr double kFaceTri{deg}Xi[{n}] = {{{fmt(p[:, 0])}}};")
@@ -225,26 +241,30 @@ def main():
         print(f"inline constexpr double kTet{deg}Zeta[{n}] = {{{fmt(p[:, 2])}}};")
         print(f"inline constexpr double kTet{deg}W[{n}] = {{{fmt(w)}}};")
         vols.append((deg, n))
-    # order 8 (P4): the reference's gmsh rule has 43 points and is not restated here (gmsh is not vendored);
-    # the Grundmann-Moeller rule s = 4 (degree 9, 70 points) integrates every order-8 integrand exactly
-    p, w = grundmann_moeller(4)
-    # the alternating-sign weights of the closed form lose ~1e-16 to cancellation: refine them on the rounded
-    # points by least squares on the exact moments, residuals summed exactly (math.fsum)
-    mom = [(a, b, c) for a in range(10) for b in range(10 - a) for c in range(10 - a - b)]
-    V = np.array([p[:, 0] ** a * p[:, 1] ** b * p[:, 2] ** c for a, b, c in mom])
-    for _ in range(3):
-        r = np.array([tet_exact(a, b, c) - math.fsum(V[k] * w) for k, (a, b, c) in enumerate(mom)])
-        w = w + np.linalg.lstsq(V, r, rcond=None)[0]
-    err = max(abs((w * p[:, 0] ** a * p[:, 1] ** b * p[:, 2] ** c).sum() - tet_exact(a, b, c))
-              for a in range(10) for b in range(10 - a) for c in range(10 - a - b))
-    assert err < 1e-15, err
-    n = len(w)
-    print(f"// volume order 8: Grundmann-Moeller s = 4 (exact to degree 9), {n} points, max moment error {err:.1e}")
-    print(f"inline constexpr double kTet8Xi[{n}] = {{{fmt(p[:, 0])}}};")
-    print(f"inline constexpr double kTet8Eta[{n}] = {{{fmt(p[:, 1])}}};")
-    print(f"inline constexpr double kTet8Zeta[{n}] = {{{fmt(p[:, 2])}}};")
-    print(f"inline constexpr double kTet8W[{n}] = {{{fmt(w)}}};")
-    vols.append((8, n))
+    # orders 8 and 10 (P4, P5): Grundmann-Moeller s = 4 (degree 9) and s = 5 (degree 11; 126 points, the
+    # reference's count, 125 once the doubled centroid is merged); the reference's order-8 gmsh rule has 43
+    # points and is not restated here (gmsh is not vendored)
+    for order, gm in ((8, 4), (10, 5)):
+        p, w = grundmann_moeller(gm)
+        top = 2 * gm + 1
+        # the alternating-sign weights of the closed form lose ~1e-16 to cancellation: refine them on the
+        # rounded points by least squares on the exact moments, residuals summed exactly (math.fsum)
+        mom = [(a, b, c) for a in range(top + 1) for b in range(top + 1 - a) for c in range(top + 1 - a - b)]
+        V = np.array([p[:, 0] ** a * p[:, 1] ** b * p[:, 2] ** c for a, b, c in mom])
+        for _ in range(3):
+            r = np.array([tet_exact(a, b, c) - math.fsum(V[k] * w) for k, (a, b, c) in enumerate(mom)])
+            w = w + np.linalg.lstsq(V, r, rcond=None)[0]
+        err = max(abs((w * p[:, 0] ** a * p[:, 1] ** b * p[:, 2] ** c).sum() - tet_exact(a, b, c))
+                  for a, b, c in mom)
+        assert err < 1e-15, err
+        n = len(w)
+        print(f"// volume order {order}: Grundmann-Moeller s = {gm} (exact to degree {top}), {n} points, "
+              f"max moment error {err:.1e}")
+        print(f"inline constexpr double kTet{order}Xi[{n}] = {{{fmt(p[:, 0])}}};")
+        print(f"inline constexpr double kTet{order}Eta[{n}] = {{{fmt(p[:, 1])}}};")
+        print(f"inline constexpr double kTet{order}Zeta[{n}] = {{{fmt(p[:, 2])}}};")
+        print(f"inline constexpr double kTet{order}W[{n}] = {{{fmt(w)}}};")
+        vols.append((order, n))
     print("inline constexpr FaceTriangleRule kFaceTriangleRules[] = {")
     for deg, n in faces:
         print(f"    {{{deg}, {n}, kFaceTri{deg}Xi, kFaceTri{deg}Eta, kFaceTri{deg}W}},")

@@ -1075,8 +1075,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         throw Failure(SDG_ERR_UNSUPPORTED, "a mesh of tetrahedra and hexahedra needs pyramids, which are not built");
       if (mesh->tetrahedron_count > 0) {
         mb.push_back({SDG_ELEMENT_TETRAHEDRON, mesh->tetrahedron_count, mesh->tetrahedron_node});
-        if (c.polynomial_order > 4)
-          throw Failure(SDG_ERR_UNSUPPORTED, "tetrahedra are built for P = 1..4 (the P5 operator tables exceed shared memory)");
+        if (c.polynomial_order > 5) throw Failure(SDG_ERR_UNSUPPORTED, "tetrahedra are built for P = 1..5");
       }
       if (mesh->hexahedron_count > 0) mb.push_back({SDG_ELEMENT_HEXAHEDRON, mesh->hexahedron_count, mesh->hexahedron_node});
     }

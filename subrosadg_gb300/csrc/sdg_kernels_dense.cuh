@@ -212,16 +212,21 @@ struct DenseShape {
   static constexpr int FSTRIDE = NF * NV * NFQ;
   static_assert(DIM * NQ >= NB && NV * NB >= NQ, "shared-memory reuse of the point and coefficient buffers");
   static constexpr int PER_ELEM = USTRIDE + FSTRIDE + DIM * NV * NQ + NV * NB + NV * NB;
-  static constexpr size_t TABLES_MAX_ = size_t(NQ) * NB * (2 + DIM) + size_t(NFP) * NB * 2 + size_t(NB) * NB;
+  // staged tables: bilinear blocks the original layout (M^-1 per element), affine blocks the folded one
+  static constexpr size_t TABLES = size_t(NQ) * NB * (1 + DIM) + size_t(NFP) * NB * 2 + size_t(NB) * NB;
+  static constexpr size_t TABLES_AFF = size_t(NQ) * NB * (2 + DIM) + size_t(NFP) * NB * 2;
+  // tables above 160 KB (tetrahedra P5: 377 KB) are read in place from global memory (L2-resident, shared by
+  // every CTA) instead of being staged per CTA
+  static constexpr bool GLOBAL_TABLES = TABLES_AFF * 8 > 160 * 1024;
+  __host__ __device__ static constexpr size_t tables(bool affine) {
+    return affine ? (GLOBAL_TABLES ? 0 : TABLES_AFF) : TABLES;
+  }
+  static constexpr size_t TABLES_MAX_ = GLOBAL_TABLES ? 0 : TABLES_AFF + size_t(NB) * NB;
   // 16 elements per CTA, fewer where the tile and its tables would exceed the 227 KB opt-in shared memory
   static constexpr long long EPB_FIT =
       (227LL * 1024 - 16 - 8LL * NV * 8 - (long long)TABLES_MAX_ * 8) / ((long long)PER_ELEM * 8);
   static constexpr int EPB = EPB_FIT < 16 ? (EPB_FIT > 0 ? int(EPB_FIT) : 1) : 16;
   static constexpr int THREADS = 256;
-  // staged tables: bilinear blocks the original layout (M^-1 per element), affine blocks the folded one
-  static constexpr size_t TABLES = size_t(NQ) * NB * (1 + DIM) + size_t(NFP) * NB * 2 + size_t(NB) * NB;
-  static constexpr size_t TABLES_AFF = size_t(NQ) * NB * (2 + DIM) + size_t(NFP) * NB * 2;
-  __host__ __device__ static constexpr size_t tables(bool affine) { return affine ? TABLES_AFF : TABLES; }
   static constexpr size_t smemFor(int epb, int threads, bool affine) {
     return (size_t(epb) * PER_ELEM + tables(affine)) * 8 + 16 + 8 * NV * size_t(threads / 32);
   }
@@ -250,10 +255,12 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
   double* sR = sQ + EPB * DIM * NV * NQ;             // [EPB][NV][NB]
   double* sN = sR + EPB * NV * NB;                   // [EPB][NV][NB] new state
   double* tab = sN + EPB * NV * NB;
-  // affine: the folded tables (dphiw and phifw carry M_ref^-1; the last block is phiMr = Phi M_ref)
+  // affine: the folded tables (dphiw and phifw carry M_ref^-1; the last block is phiMr = Phi M_ref), staged in
+  // shared memory or, when too large, read in place (GT)
   constexpr size_t TAB = S::tables(AFFINE);
+  constexpr bool GT = AFFINE && S::GLOBAL_TABLES;
   const double* tsrc = AFFINE ? a.tables + denseFoldedOffset(NB, NQ, NFP, NF, NFQ, DIM) : a.tables;
-  const double* phi = tab;
+  const double* phi = GT ? tsrc : tab;
   const double* dphiw = phi + NQ * NB;
   const double* phif = dphiw + NQ * DIM * NB;
   const double* phifw = phif + NFP * NB;
@@ -274,7 +281,8 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
     if (a.doVolume) bulkLoad(sF, (a.fluxSrc ? a.fluxSrc : a.face) + (a.faceBase + e0 * NF) * NV * NFQ, fb, bar);
   }
   if (loadTables)
-    for (int k = tid; k < int(TAB); k += blockDim.x) tab[k] = tsrc[k];
+    if (!GT)
+      for (int k = tid; k < int(TAB); k += blockDim.x) tab[k] = tsrc[k];
   __syncthreads();
   const bool arrived = mbarWait(bar, parity);
   if (__syncthreads_or(!arrived)) {
@@ -377,7 +385,7 @@ __device__ __forceinline__ bool denseStageTile(const StageArgs& a, const Phys& p
           s = fma(-sF[le * S::FSTRIDE + (f * NV + v) * NFQ + j], phifw[fj * NB + i], s);
         }
         if (ph.source && v == DIM) {  // last momentum component: sum_q w_q |J|_q S_q phi_i(x_q) (affine: M_ref^-1 of it)
-          const double* phiw = AFFINE ? tsrc + TAB
+          const double* phiw = AFFINE ? tsrc + S::TABLES_AFF
                                       : a.tables + (NQ * NB * (1 + DIM) + NFP * NB * 2 + NB * NB + DIM * NB * NB +
                                                     NF * NB * NFQ + NF * NFQ * NFQ);
           for (int q = 0; q < NQ; ++q) s = fma(sN[le * NV * NB + q], phiw[q * NB + i], s);
@@ -512,7 +520,7 @@ __global__ void __launch_bounds__(kMaxTileThreads)
 // volume part, to which face f adds its own lift r_f = M^-1 sum_{j in f} wf_j nF_f 1/2[U] phi.
 template <int NB, int NQ, int NFQ, int NF, bool AFFINE, int DIM = 2>
 struct DenseGradShape {
-  static constexpr int NV = DIM + 2, NFP = NF * NFQ, EPB = 8, THREADS = 256;
+  static constexpr int NV = DIM + 2, NFP = NF * NFQ, THREADS = 256;
   static constexpr int USTRIDE = (NV * NB + 1) & ~1;
   static constexpr int FS = NF * NV * NFQ;
   static_assert(AFFINE || DIM == 2, "the general (bilinear) form is built for quadrangles");
@@ -521,6 +529,10 @@ struct DenseGradShape {
   static constexpr int PER_ELEM = AFFINE ? USTRIDE + 2 * FS + NV * DIM * NB : USTRIDE + 2 * FS + NV * NQ + 3 * NV * 2 * NB;
   static constexpr size_t TABLES = AFFINE ? size_t(NFP) * NB + size_t(DIM) * NB * NB + size_t(NF) * NB * NFQ + size_t(NF) * NFQ * NFQ
                                           : size_t(NQ) * NB * 3 + size_t(NFP) * NB * 2 + size_t(NB) * NB;
+  // 8 elements per CTA, fewer where tile and tables would exceed the 227 KB opt-in shared memory (P5
+  // tetrahedra: 191 KB of tables, 2 elements)
+  static constexpr long long EPB_FIT = (227LL * 1024 - 16 - (long long)TABLES * 8) / ((long long)PER_ELEM * 8);
+  static constexpr int EPB = EPB_FIT < 8 ? (EPB_FIT > 0 ? int(EPB_FIT) : 1) : 8;
   static constexpr size_t SMEM = (size_t(EPB) * PER_ELEM + TABLES) * 8 + 16;
   static constexpr size_t smemFor(int epb) { return (size_t(epb) * PER_ELEM + TABLES) * 8 + 16; }
 };
@@ -916,11 +928,13 @@ __global__ void __launch_bounds__(kMaxTileThreads)
   X(SDG_ELEMENT_TETRAHEDRON, 1, 4, 4, 4, 4)     \
   X(SDG_ELEMENT_TETRAHEDRON, 2, 10, 11, 7, 4)   \
   X(SDG_ELEMENT_TETRAHEDRON, 3, 20, 24, 13, 4)
-// P4: 35 modes, the 69-point Grundmann-Moeller volume rule (tetrahedron_rules.h), 19-point faces; stage and
-// gradient kernels only (its derivative kernels' tables would not fit the shared memory)
+// P4: 35 modes, the 69-point Grundmann-Moeller volume rule (tetrahedron_rules.h), 19-point faces; P5: 56 modes,
+// the 125-point Grundmann-Moeller rule, 27-point faces, the stage tables read from global memory.  Stage and
+// gradient kernels only (the derivative kernels' tables would not fit the shared memory)
 #define SDG_TET_CASES(X)                        \
   SDG_TET_ADJOINT_CASES(X)                      \
-  X(SDG_ELEMENT_TETRAHEDRON, 4, 35, 69, 19, 4)
+  X(SDG_ELEMENT_TETRAHEDRON, 4, 35, 69, 19, 4)  \
+  X(SDG_ELEMENT_TETRAHEDRON, 5, 56, 125, 27, 4)
 
 // (type, P) -> (NB, NQ, NFQ): triangle P1..P5 use Dunavant rules of 3,6,12,16,25 points.
 

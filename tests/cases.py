@@ -298,10 +298,10 @@ def with_av(case, tolerance=1.0, factor=1.0):
 
 
 def shock_tube_case(p=3, flux=sdg.HLLC, n=8, dt=2e-4, steps=3, split=0.0, jitter=0.0, dim=2, tolerance=1.0,
-                    factor=1.0, tets=False):
+                    factor=1.0, tets=False, width=0.02):
     """Sod's shock tube (rho, p) = (1, 1) | (0.125, 0.1) at x = 0.5 in a slip-walled box [0,1] x [0,1/4]
-    (x [0,1/4] in 3D; `tets`: tetrahedra), smoothed over a few % of the length so the projected state stays
-    positive."""
+    (x [0,1/4] in 3D; `tets`: tetrahedra), smoothed over `width` (a few % of the length) so the projected state
+    stays positive."""
     if dim == 3 and tets:
         mesh = sdg.Mesh.box_3d_tetrahedra(0, 0, 0, 1.0, 0.25, 0.25, n, max(2, n // 4), max(2, n // 4), periodic=False,
                                           boundary_conditions=[sdg.ADIABATIC_SLIP_WALL] * 6)
@@ -315,7 +315,7 @@ def shock_tube_case(p=3, flux=sdg.HLLC, n=8, dt=2e-4, steps=3, split=0.0, jitter
 
     def ic(pts):
         x = pts[:, 0]
-        t = 0.5 * (1.0 + np.tanh((x - 0.5) / 0.02))
+        t = 0.5 * (1.0 + np.tanh((x - 0.5) / width))
         rho = 1.0 + (0.125 - 1.0) * t
         pr = 1.0 + (0.1 - 1.0) * t
         out = np.zeros((len(pts), dim + 2))

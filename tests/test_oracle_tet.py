@@ -36,9 +36,9 @@ def _array(text, name):
 def _rules():
     text = open(RULES).read()
     face = {d: (_array(text, f"kFaceTri{d}Xi"), _array(text, f"kFaceTri{d}Eta"), _array(text, f"kFaceTri{d}W"))
-            for d in (3, 5, 7, 9)}
+            for d in (3, 5, 7, 9, 11)}
     vol = {d: (_array(text, f"kTet{d}Xi"), _array(text, f"kTet{d}Eta"), _array(text, f"kTet{d}Zeta"),
-               _array(text, f"kTet{d}W")) for d in (2, 4, 6, 8)}
+               _array(text, f"kTet{d}W")) for d in (2, 4, 6, 8, 10)}
     return face, vol
 
 
@@ -52,19 +52,20 @@ def test_rules_integrate_their_degree_and_match_the_reference_counts():
                 exact = math.factorial(a) * math.factorial(b) / math.factorial(a + b + 2)
                 assert abs((w * x ** a * y ** b).sum() - exact) < 1e-16
     for d, (x, y, z, w) in vol.items():
-        # order 8: Grundmann-Moeller s = 4, 69 points (the reference's gmsh rule has 43), exact to degree 9
-        assert len(w) == (69 if d == 8 else counts["Tetrahedron"][d])
+        # orders 8 and 10: Grundmann-Moeller s = 4 and 5 (69 points against the reference's 43; 126 points,
+        # the reference's count, with the doubled centroid merged into 125), exact to degrees 9 and 11
+        assert len(w) == {8: 69, 10: 125}.get(d, counts["Tetrahedron"][d])
         assert np.all(x >= 0) and np.all(y >= 0) and np.all(z >= 0) and np.all(x + y + z <= 1)
-        top = 9 if d == 8 else d
+        top = {8: 9, 10: 11}.get(d, d)
         for a in range(top + 1):
             for b in range(top + 1 - a):
                 for c in range(top + 1 - a - b):
                     exact = math.factorial(a) * math.factorial(b) * math.factorial(c) / math.factorial(a + b + c + 3)
                     # the Grundmann-Moeller weights alternate in sign: a little more cancellation in the sum
-                    assert abs((w * x ** a * y ** b * z ** c).sum() - exact) < (2e-16 if d == 8 else 1e-16)
+                    assert abs((w * x ** a * y ** b * z ** c).sum() - exact) < (2e-16 if d >= 8 else 1e-16)
 
 
-@pytest.mark.parametrize("p", [1, 2, 3, 4])
+@pytest.mark.parametrize("p", [1, 2, 3, 4, 5])
 def test_face_point_pairing_matches_the_reference_tables(p):
     """A right face lists the shared vertices in the opposite orientation with the left face's first vertex
     at position r: left (xi, eta) is right r=0 (eta, xi), r=1 (1-xi-eta, eta), r=2 (xi, 1-xi-eta).  On the
@@ -106,12 +107,12 @@ def test_adjacency_matches_the_oracle(periodic):
     g.close()
 
 
-def test_unsupported_tetrahedral_configurations_are_refused():
+def test_tetrahedra_of_orders_four_and_five_are_accepted():
     mesh = cases.tet_mesh(3)
-    for cfg in (cases.config(5, sdg.HLLC), cases.config(5, sdg.ROE)):
-        with pytest.raises(sdg.SdgError) as e:
-            sdg.GpuSolver(mesh, cfg, device=-1)
-        assert "UNSUPPORTED" in str(e.value)
+    for p in (4, 5):
+        g = sdg.GpuSolver(mesh, cases.config(p, sdg.HLLC), device=-1)
+        assert g.counts.face_point_count == {4: 19, 5: 27}[p]
+        g.close()
 
 
 @pytest.mark.parametrize("p,flux", [(1, sdg.ROE), (2, sdg.HLLC), (3, sdg.LAX_FRIEDRICHS)])
