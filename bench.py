@@ -9,7 +9,8 @@ dt from CFL 0.2 -- seeded synthetic initial state of that shape (no dataset invo
 
 Prints one JSON line.  value = DOF-stage updates/s with the state resident in HBM (CUDA events on the
 library's stream, the step replayed as a CUDA graph); e2e = the same metric through the C ABI with host
-buffers (pinned), the state uploaded and downloaded every step.  The line also carries the other
+buffers (pinned), the state uploaded every step (sdg_set_state_point) and the new state returned by
+sdg_step_state_point.  The line also carries the other
 workloads of the metric, each measured the same way on this GPU:
   batched      256 independent 2D Euler / Navier-Stokes Kelvin-Helmholtz solves (500..50,000 elements,
                P1..P5, quads or hybrid, Mach 0.1..0.8, Re 1e2..1e4): one batched graph step of all
@@ -574,18 +575,17 @@ def run_ours(args):
         npts = c.volume_point_count * s.nv
         host_in = torch.empty(npts, dtype=torch.float64, pin_memory=True)
         host_out = torch.empty(npts, dtype=torch.float64, pin_memory=True)
-        s.state_point(host_out.numpy().reshape(-1, s.nv))
+        out_view = host_out.numpy().reshape(-1, s.nv)
+        s.state_point(out_view)
         host_in.copy_(host_out)
         for _ in range(2):
             s.set_state_point(host_in.numpy())
-            s.stepSolver(dt)
-            s.state_point(host_out.numpy().reshape(-1, s.nv))
+            s.step_state_point(dt, out_view)
         replicas.barrier(pg)
         t0 = time.perf_counter()
         for _ in range(args.steps):
             s.set_state_point(host_in.numpy())          # H2D of the step's input state
-            s.stepSolver(dt)                            # step + relative error (D2H)
-            s.state_point(host_out.numpy().reshape(-1, s.nv))  # D2H of the step's result
+            s.step_state_point(dt, out_view)            # step, its relative error and its new state (D2H)
         t_e2e = time.perf_counter() - t0
         t_e2e = replicas.max_over_ranks(pg, t_e2e, device=f"cuda:{device}")
         e2e = {"value": world * dof * stages * args.steps / t_e2e, "unit": "DOF-stage/s",

@@ -224,6 +224,14 @@ int sdg_calculate_delta_time(sdg_handle* handle, double courant_friedrichs_lewy_
 int sdg_step(sdg_handle* handle, int32_t step_count, double delta_time);
 /* Same, enqueued on the handle's stream without a host synchronisation. */
 int sdg_step_async(sdg_handle* handle, int32_t step_count, double delta_time);
+/* One step (sdg_step with step_count 1) that also returns the new state as sdg_get_state_point does, and
+ * the step's relative error when relative_error is not null (d+2 doubles).  The reference's solve loop
+ * reads the state after Solver::stepSolver (src/Solver/TimeIntegration.cpp:326-350) for its views; here,
+ * when `conserved` is pinned host memory (cudaHostAlloc / cudaHostRegister), the last RK stage of tensor
+ * blocks writes each element's new state straight into it while the stage computes, so no transfer
+ * follows the step; dense blocks, and pageable buffers, are converted and copied after the step.  The
+ * captured step graph is re-captured when the buffer differs from the previous call's. */
+int sdg_step_state_point(sdg_handle* handle, double delta_time, double* conserved, double* relative_error);
 
 /* Solver::relative_error_ of the last step: per conserved variable, the element mean of
  * mean_q |R Phi^T| (TimeIntegration.cpp:279-324).  NaN entries signal a blow-up. */

@@ -672,6 +672,7 @@ void emitStep(sdg_handle* h, double dt, bool relerr, std::vector<Rec>& out) {
       a.c2dt = kRk[h->cfg.time_integration][s][2] * dt;
       a.doUpdate = 1; a.doTrace = 1; a.doVolume = 1;
       a.relerr = (relerr && last) ? h->relPart + B.relOffset * h->nv : nullptr;
+      if (last && h->pointsOut && B.kind == kTensor) a.pointsOut = h->pointsOut + B.pointOffset * h->nv;
       r.seq = s * 8 + 3;
       out.push_back(r);
     }
@@ -742,7 +743,7 @@ namespace {
 
 // One step through a captured CUDA graph (re-captured when dt or the tiles change).
 void stepGraph(sdg_handle* h, double dt) {
-  if (!h->graphExec || h->graphDt != dt) {
+  if (!h->graphExec || h->graphDt != dt || h->graphOut != h->pointsOut) {
     dropGraph(h);
     std::vector<Rec> recs;
     emitStep(h, dt, true, recs);
@@ -760,6 +761,7 @@ void stepGraph(sdg_handle* h, double dt) {
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) { h->graphExec = nullptr; SDG_CUDA(e); }
     h->graphDt = dt;
+    h->graphOut = h->pointsOut;
     h->graphKernels = 0;
     for (const Rec& r : recs) h->graphKernels += r.units > 0;
   }
@@ -832,11 +834,13 @@ void uploadPoints(sdg_handle* h, const double* conserved, int which) {
 }
 
 // state[which] -> conserved variables at the volume points in a host buffer: written in place over the link
-// when it is pinned, else through the scratch buffer and one copy.
-void downloadPoints(sdg_handle* h, int which, double* conserved) {
+// when it is pinned, else through the scratch buffer and one copy.  skipTensor (pinned buffers only): the
+// tensor blocks' points are already there (written by the step's last stage).
+void downloadPoints(sdg_handle* h, int which, double* conserved, bool skipTensor = false) {
   double* mapped = const_cast<double*>(mappedHost(conserved));
   double* dst = mapped ? mapped : h->scratch;
   for (DevBlock& B : h->blocks) {
+    if (mapped && skipTensor && B.kind == kTensor) continue;
     const int epc = conversionElements(B, h->nv);
     const int64_t grid = (B.ne + epc - 1) / epc;
     stateToPointsTiledKernel<<<unsigned(grid), 256, size_t(epc) * B.nq * h->nv * 8, h->stream>>>(
@@ -1700,6 +1704,30 @@ int sdg_step(sdg_handle* h, int32_t steps, double dt) {
   if (steps > 0)
     SDG_CUDA(cudaMemcpyAsync(h->relerr, h->relOut, h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
   checkStatus(h);
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_step_state_point(sdg_handle* h, double dt, double* conserved, double* relative_error) {
+  if (!h || !conserved || !std::isfinite(dt)) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  if (!h->hasState) { h->err = "step before an initial state"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  h->pointsOut = const_cast<double*>(mappedHost(conserved));
+  try {
+    stepOnce(h, dt);
+  } catch (...) {
+    h->pointsOut = nullptr;
+    throw;
+  }
+  h->pointsOut = nullptr;
+  h->stateVersion++;
+  downloadPoints(h, 0, conserved, true);
+  SDG_CUDA(cudaMemcpyAsync(h->relerr, h->relOut, h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  checkStatus(h);
+  if (relative_error)
+    for (int v = 0; v < h->nv; ++v) relative_error[v] = h->relerr[v];
   return SDG_OK;
   SDG_API_END(h)
 }

@@ -155,6 +155,8 @@ struct sdg_handle {
   bool useGraph = true;            // sdg_step replays a captured CUDA graph of one step
   cudaGraphExec_t graphExec = nullptr;
   double graphDt = 0.0;
+  double* pointsOut = nullptr;     // sdg_step_state_point: mapped host buffer the last stage of tensor blocks fills
+  double* graphOut = nullptr;      // pointsOut the captured graph was made with
   int64_t graphKernels = 0;
   int64_t elements = 0, dof = 0;
   struct AdjointState* adj = nullptr;  // tangent-linear / adjoint buffers, created on first use

@@ -108,6 +108,8 @@ struct StageArgs {
   unsigned waitLimit;
   int diagMetric;         // affine block with diagonal metric terms only (structured axis-aligned boxes)
   int pad;
+  double* pointsOut;      // tensor blocks, updating stages: also write the new state in point layout ([e][q][v])
+                          // here (a pinned host buffer the device maps), or null
 };
 
 // Artificial-viscosity tables of a block (doubles):
@@ -458,6 +460,15 @@ __device__ __forceinline__ bool tensorStageTile(const StageArgs& a, const Phys& 
       }
     }
     __syncthreads();
+    if (a.doUpdate && a.pointsOut) {
+      // the tile's new state as one contiguous run of the point layout (nodes are the volume points):
+      // consecutive threads on consecutive addresses, so host-memory writes over the CPU-GPU link go out whole
+      double* dst = a.pointsOut + e0 * (NB * NV);
+      for (int i = tid; i < ecount * (NB * NV); i += blockDim.x) {
+        const int te = i / (NB * NV), r = i - te * (NB * NV), q = r / NV, v = r - q * NV;
+        dst[i] = sU[te * S::USTRIDE + v * NB + q];
+      }
+    }
   }
   // 5. face traces of the (new) state: 1D end-point interpolation along each face's normal axis
   if (a.doTrace) {

@@ -298,6 +298,14 @@ class GpuSolver:
         self._chk(self.lib.sdg_relative_error(self.h, _ptr(self.relative_error_)))
         return self.relative_error_
 
+    def step_state_point(self, dt, out=None):
+        """One stepSolver step returning the new state at the volume points (sdg_step_state_point): a pinned
+        `out` is filled by the last stage itself on tensor blocks.  Returns (state, relative error)."""
+        if out is None:
+            out = np.zeros((self.counts.volume_point_count, self.nv))
+        self._chk(self.lib.sdg_step_state_point(self.h, dt, _ptr(out), _ptr(self.relative_error_)))
+        return out, self.relative_error_
+
     def step_async(self, dt, steps=1):
         self._chk(self.lib.sdg_step_async(self.h, steps, dt))
 

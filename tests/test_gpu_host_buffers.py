@@ -45,3 +45,38 @@ def test_pinned_and_pageable_buffers_agree(name, case):
     out = _pinned(u.size).reshape(-1, nv)
     s.state_point(out)
     np.testing.assert_array_equal(out, s.state_point())
+
+
+@pytest.mark.parametrize("name,case", [
+    ("hex-p3", lambda: cases.tgv_case(n=4, p=3)),
+    ("hybrid-p4", lambda: cases.kh_case(n=6, p=4)),
+    ("tet-p2", lambda: cases.tet_tgv_case(n=3, p=2)),
+    ("line-p3", lambda: cases.sod_1d_case(n=9, p=3)),
+    ("ns-hex-p2", lambda: cases.tgv_case(n=3, p=2, viscous=sdg.BR1)),
+])
+def test_step_state_point_matches_step_then_download(name, case):
+    """sdg_step_state_point: the last stage of tensor blocks writes the new state into a pinned buffer
+    itself; the state, the point values and the relative error are those of sdg_step + sdg_get_state_point,
+    bit for bit, for pinned and pageable buffers, with the step graph re-captured between the two forms."""
+    mesh, cfg, prim, _, dt, _ = case()
+    a = sdg.GpuSolver(mesh, cfg)
+    b = sdg.GpuSolver(mesh, cfg)
+    for s in (a, b):
+        s.initialize_primitive(prim(s.volume_points()))
+    nv = a.counts.conserved_variable_count
+    pin = _pinned(a.counts.volume_point_count * nv).reshape(-1, nv)
+    for step in range(3):
+        err_a = a.stepSolver(dt).copy()
+        u_a = a.state_point()
+        if step == 1:
+            u_b, err_b = b.step_state_point(dt)          # pageable: converted and copied after the step
+            u_b = u_b.copy()
+        else:
+            pin[...] = np.nan
+            u_b, err_b = b.step_state_point(dt, pin)     # pinned: written by the last stage
+        np.testing.assert_array_equal(u_b, u_a)
+        np.testing.assert_array_equal(err_b, err_a)
+        np.testing.assert_array_equal(b.state_modal(), a.state_modal())
+    b.stepSolver(dt)                                     # back to the plain step graph
+    a.stepSolver(dt)
+    np.testing.assert_array_equal(b.state_modal(), a.state_modal())
