@@ -117,14 +117,16 @@ typedef struct sdg_mesh {
   const int32_t* line_node;           /* [line_count][2]                                            */
   int64_t tetrahedron_count;          /* 3D: tetrahedra (MeshModelEnum::Tetrahedron), gmsh vertex order */
   const int32_t* tetrahedron_node;    /* [tetrahedron_count][4]                                      */
-  /* Curved (high-order) geometry of 2D meshes, as the drivers' setOrder(P) makes it and
-     src/Mesh/ReadControl.cpp:243-256 reads it: geometry_order q in 2..5 (0 or 1: straight-sided) and, per
-     element, the node indices of its order-q Lagrange element in gmsh's node order (the corners first, equal
-     to the vertex lists above).  The Jacobians and face normals are then those of the order-q map at every
-     quadrature point (src/Mesh/Geometry.cpp:44-86, 102-127).                                          */
+  /* Curved (high-order) geometry, as the drivers' setOrder(P) makes it and src/Mesh/ReadControl.cpp:243-256
+     reads it: geometry_order q in 2..5 (0 or 1: straight-sided) and, per element, the node indices of its
+     order-q Lagrange element in gmsh's node order (the corners first, equal to the vertex lists above).  The
+     Jacobians and face normals are then those of the order-q map at every quadrature point
+     (src/Mesh/Geometry.cpp:44-86, 102-147).  Triangles, quadrangles and hexahedra; tetrahedra stay
+     straight-sided.                                                                                 */
   int32_t geometry_order;
   const int32_t* triangle_geometry_node;   /* [triangle_count][(q+1)(q+2)/2], or NULL                  */
   const int32_t* quadrangle_geometry_node; /* [quadrangle_count][(q+1)^2], or NULL                     */
+  const int32_t* hexahedron_geometry_node; /* [hexahedron_count][(q+1)^3], or NULL                     */
 } sdg_mesh;
 
 /* ---- physics and numerics: the runtime form of the reference's SimulationControl -------------- */
@@ -346,9 +348,9 @@ int sdg_mesh_generate_3d(double x0, double y0, double z0, double lx, double ly, 
 int sdg_mesh_generate_3d_tetrahedra(double x0, double y0, double z0, double lx, double ly, double lz,
                                     int32_t nx, int32_t ny, int32_t nz, int32_t periodic,
                                     const int32_t* boundary_condition, sdg_generated_mesh* out);
-/* Read a gmsh MSH 4.1 ASCII file (first-order or high-order elements).  A 2D mesh of order q > 1 keeps
- * every element's nodes as its curved geometry (geometry_order q); 1D and 3D meshes are read by their
- * primary vertices (straight-sided).  Physical groups of dimension d-1 (points in 1D) become boundary groups
+/* Read a gmsh MSH 4.1 ASCII file (first-order or high-order elements).  A 2D mesh, or a 3D mesh of
+ * hexahedra, of order q > 1 keeps every element's nodes as its curved geometry (geometry_order q); 1D meshes
+ * and tetrahedra are read by their primary vertices (straight-sided).  Physical groups of dimension d-1 (points in 1D) become boundary groups
  * in file order. */
 int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out);
 int sdg_mesh_free(sdg_generated_mesh* mesh);

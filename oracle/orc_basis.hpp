@@ -467,20 +467,114 @@ inline std::vector<std::array<Real, 2>> gmshNodePositions(int t, int q) {
   return out;
 }
 
-// Lagrange basis through given nodes by the inverse Vandermonde matrix of the monomials x^a y^b (a, b <= q on
-// quadrangles, a + b <= q on triangles): N_n(X) = sum_m C[m][n] mono_m(X).
+// Hexahedron ([-1,1]^3, gmsh corner order: z = -1 counter-clockwise from (-1,-1), then z = +1): the 8 corners,
+// the q-1 interior points of each edge of gmsh's edge table in edge direction, each face's interior nodes in
+// gmsh's face order as the quadrangle construction above on the face's inner corners (one lattice step in
+// from each face corner along the face's two edges), then the interior as a hexahedron on the inner corners
+// (one lattice step along each of a corner's three edges), recursively.  Positions are built from corner
+// points, not lattice indices.
+inline std::vector<std::array<Real, 3>> gmshHexNodePositions(int q) {
+  static const int edges[12][2] = {{0, 1}, {0, 3}, {0, 4}, {1, 2}, {1, 5}, {2, 3},
+                                   {2, 6}, {3, 7}, {4, 5}, {4, 7}, {5, 6}, {6, 7}};
+  static const int faces[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {0, 4, 7, 3}, {1, 2, 6, 5}, {2, 3, 7, 6}, {4, 5, 6, 7}};
+  static const int nbr[8][3] = {{1, 3, 4}, {0, 2, 5}, {1, 3, 6}, {0, 2, 7}, {0, 5, 7}, {1, 4, 6}, {2, 5, 7}, {3, 4, 6}};
+  using P3 = std::array<Real, 3>;
+  const auto lerp = [](const P3& a, const P3& b, Real t) {
+    return P3{a[0] + (b[0] - a[0]) * t, a[1] + (b[1] - a[1]) * t, a[2] + (b[2] - a[2]) * t};
+  };
+  // the quadrangle construction on four 3D corners (the order of gmshNodePositions for kQuad)
+  const auto quad = [&](std::array<P3, 4> c, int r, std::vector<P3>& out) {
+    while (r >= 0) {
+      if (r == 0) {
+        P3 m = {0, 0, 0};
+        for (const auto& p : c) for (int d = 0; d < 3; ++d) m[d] += p[d] / 4;
+        out.push_back(m);
+        return;
+      }
+      for (const auto& p : c) out.push_back(p);
+      for (int k = 0; k < 4; ++k)
+        for (int i = 1; i < r; ++i) out.push_back(lerp(c[k], c[(k + 1) % 4], Real(i) / Real(r)));
+      if (r - 2 < 0) return;
+      std::array<P3, 4> in;
+      for (int k = 0; k < 4; ++k) {
+        const P3& p = c[k];
+        const P3& nx = c[(k + 1) % 4];
+        const P3& pv = c[(k + 3) % 4];
+        for (int d = 0; d < 3; ++d) in[k][d] = p[d] + (nx[d] - p[d]) / r + (pv[d] - p[d]) / r;
+      }
+      c = in;
+      r -= 2;
+    }
+  };
+  std::vector<P3> out;
+  std::array<P3, 8> c = {P3{-1, -1, -1}, P3{1, -1, -1}, P3{1, 1, -1}, P3{-1, 1, -1},
+                         P3{-1, -1, 1},  P3{1, -1, 1},  P3{1, 1, 1},  P3{-1, 1, 1}};
+  int r = q;
+  while (r >= 0) {
+    if (r == 0) {
+      P3 m = {0, 0, 0};
+      for (const auto& p : c) for (int d = 0; d < 3; ++d) m[d] += p[d] / 8;
+      out.push_back(m);
+      break;
+    }
+    for (const auto& p : c) out.push_back(p);
+    for (const auto& e : edges)
+      for (int i = 1; i < r; ++i) out.push_back(lerp(c[e[0]], c[e[1]], Real(i) / Real(r)));
+    if (r - 2 < 0) break;
+    for (const auto& f : faces) {
+      std::array<P3, 4> fc;
+      for (int k = 0; k < 4; ++k) {
+        const P3& p = c[f[k]];
+        const P3& nx = c[f[(k + 1) % 4]];
+        const P3& pv = c[f[(k + 3) % 4]];
+        for (int d = 0; d < 3; ++d) fc[k][d] = p[d] + (nx[d] - p[d]) / r + (pv[d] - p[d]) / r;
+      }
+      quad(fc, r - 2, out);
+    }
+    std::array<P3, 8> in;
+    for (int k = 0; k < 8; ++k)
+      for (int d = 0; d < 3; ++d) {
+        Real v = c[k][d];
+        for (int a = 0; a < 3; ++a) v += (c[nbr[k][a]][d] - c[k][d]) / r;
+        in[k][d] = v;
+      }
+    c = in;
+    r -= 2;
+  }
+  return out;
+}
+
+// Lagrange basis through the gmsh-ordered nodes.  Quadrangles and triangles: the inverse Vandermonde matrix of
+// the monomials x^a y^b (a, b <= q on quadrangles, a + b <= q on triangles): N_n(X) = sum_m C[m][n] mono_m(X).
+// Hexahedra: products L_i(x) L_j(y) L_k(z) of the 1D Lagrange polynomials through the q+1 equispaced
+// coordinates (each from the inverse 1D Vandermonde matrix), (i, j, k) the node's coordinate indices.
 struct CurvedBasis {
   int t = 0, q = 1, nn = 0;
-  std::vector<std::array<int, 2>> mono;
-  std::vector<Real> C;  // [nn][nn], C[m * nn + n]
+  std::vector<std::array<int, 3>> mono;  // monomial exponents (2D), or the node's coordinate indices (hexahedra)
+  std::vector<Real> C;  // 2D: [nn][nn], C[m * nn + n]; hexahedra: the 1D [q+1][q+1], C1[a * (q+1) + i]
   void init(int type, int order) {
     t = type; q = order;
+    mono.clear();
+    if (type == kHex) {
+      const auto pos = gmshHexNodePositions(order);
+      nn = int(pos.size());
+      for (const auto& p : pos) {
+        std::array<int, 3> ijk;
+        for (int d = 0; d < 3; ++d) ijk[d] = int(std::lround(double((p[d] + 1) * q / 2)));
+        mono.push_back(ijk);
+      }
+      std::vector<Real> V(size_t(q + 1) * (q + 1));
+      for (int i = 0; i <= q; ++i)
+        for (int a = 0; a <= q; ++a) V[size_t(i) * (q + 1) + a] = ipow(Real(-1) + Real(2 * i) / Real(q), a);
+      C.assign(size_t(q + 1) * (q + 1), 0);
+      invert(q + 1, V.data(), C.data());
+      return;
+    }
     const auto pos = gmshNodePositions(type, order);
     nn = int(pos.size());
-    mono.clear();
     for (int a = 0; a <= q; ++a)
       for (int b = 0; b <= q; ++b)
-        if (type == kQuad || a + b <= q) mono.push_back({a, b});
+        if (type == kQuad || a + b <= q) mono.push_back({a, b, 0});
     std::vector<Real> V(size_t(nn) * nn);
     for (int n = 0; n < nn; ++n)
       for (int m = 0; m < nn; ++m) V[size_t(n) * nn + m] = ipow(pos[n][0], mono[m][0]) * ipow(pos[n][1], mono[m][1]);
@@ -488,8 +582,26 @@ struct CurvedBasis {
     invert(nn, V.data(), C.data());
   }
   static Real ipow(Real x, int k) { Real r = 1; for (int i = 0; i < k; ++i) r *= x; return r; }
-  // N[n], G[n][2] at X
+  // the 1D Lagrange polynomial i at x and its derivative (hexahedra)
+  void lagrange(int i, Real x, Real& v, Real& d) const {
+    v = 0; d = 0;
+    for (int a = 0; a <= q; ++a) {
+      const Real c = C[size_t(a) * (q + 1) + i];
+      v += c * ipow(x, a);
+      if (a) d += c * a * ipow(x, a - 1);
+    }
+  }
+  // N[n], G[n][3] at X
   void eval(const Real* X, Real* N, Real* G) const {
+    if (t == kHex) {
+      for (int n = 0; n < nn; ++n) {
+        Real v[3], d[3];
+        for (int k = 0; k < 3; ++k) lagrange(mono[n][k], X[k], v[k], d[k]);
+        N[n] = v[0] * v[1] * v[2];
+        G[n * 3] = d[0] * v[1] * v[2]; G[n * 3 + 1] = v[0] * d[1] * v[2]; G[n * 3 + 2] = v[0] * v[1] * d[2];
+      }
+      return;
+    }
     std::vector<Real> mv(nn), mx(nn), my(nn);
     for (int m = 0; m < nn; ++m) {
       const int a = mono[m][0], b = mono[m][1];
@@ -503,7 +615,7 @@ struct CurvedBasis {
         const Real cc = C[size_t(m) * nn + n];
         v += cc * mv[m]; gx += cc * mx[m]; gy += cc * my[m];
       }
-      N[n] = v; G[n * 2] = gx; G[n * 2 + 1] = gy;
+      N[n] = v; G[n * 3] = gx; G[n * 3 + 1] = gy; G[n * 3 + 2] = 0;
     }
   }
 };

@@ -46,7 +46,7 @@ struct Block {
   std::vector<Real> jw;       // ne * nq        |J| w
   std::vector<Real> jtiw;     // ne * nq * d*d  J^-T |J| w, column-major d x d per point
   std::vector<Real> minv;     // ne * nb*nb     local mass matrix inverse
-  // curved 2D geometry: the order-q map through each element's gmsh-ordered geometry nodes
+  // curved geometry: the order-q map through each element's gmsh-ordered geometry nodes
   bool curved = false;
   int geoOrder = 1;
   std::vector<int> geo;       // ne * (nodes of the order-q element)
@@ -177,10 +177,16 @@ static Real innerRadiusOf(int type, const double* nodes, const int* vv) {
   return 3.0 * vol / area;
 }
 
-// Reference vertices of the 2D element types.
-static void refVertex2d(int type, int v, Real* X) {
+// Reference vertices of the element types with curved geometry (quadrangles, triangles, hexahedra).
+static void refVertexCurved(int type, int v, Real* X) {
   static const Real quad[4][2] = {{-1, -1}, {1, -1}, {1, 1}, {-1, 1}};
   static const Real tri[3][2] = {{0, 0}, {1, 0}, {0, 1}};
+  if (type == kHex) {
+    X[0] = (v == 1 || v == 2 || v == 5 || v == 6) ? 1 : -1;
+    X[1] = (v == 2 || v == 3 || v == 6 || v == 7) ? 1 : -1;
+    X[2] = v >= 4 ? 1 : -1;
+    return;
+  }
   X[0] = type == kQuad ? quad[v][0] : tri[v][0];
   X[1] = type == kQuad ? quad[v][1] : tri[v][1];
   X[2] = 0;
@@ -189,15 +195,15 @@ static void refVertex2d(int type, int v, Real* X) {
 // The curved map of element e: x(X) and J[l][k] = dx_l/dX_k (the gmsh Jacobian of Geometry.cpp:44-67 for
 // high-order elements).
 static void curvedMap(const Block& B, int64_t e, const double* nodes, const Real* X, Real J[3][3], Real* x) {
-  const int nn = B.cb.nn;
-  std::vector<Real> N(nn), G(size_t(nn) * 2);
+  const int nn = B.cb.nn, d = B.type == kHex ? 3 : 2;
+  std::vector<Real> N(nn), G(size_t(nn) * 3);
   B.cb.eval(X, N.data(), G.data());
   for (int l = 0; l < 3; ++l) { x[l] = 0; for (int k = 0; k < 3; ++k) J[l][k] = 0; }
   for (int n = 0; n < nn; ++n) {
     const double* c = &nodes[size_t(B.geo[size_t(e) * nn + n]) * 3];
     for (int l = 0; l < 3; ++l) x[l] += N[n] * c[l];
-    for (int l = 0; l < 2; ++l)
-      for (int k = 0; k < 2; ++k) J[l][k] += G[n * 2 + k] * c[l];
+    for (int l = 0; l < d; ++l)
+      for (int k = 0; k < d; ++k) J[l][k] += G[n * 3 + k] * c[l];
   }
 }
 
@@ -337,14 +343,17 @@ static void faceGeometry(Problem& P, Face& F, const double* nodes) {
     faceShape(B.type, &R.fq.x[j * 3], sh);
     faceShapeGrad(B.type, &R.fq.x[j * 3], dxi, deta);
     Real x[3] = {0, 0, 0}, tx[3] = {0, 0, 0}, ty[3] = {0, 0, 0};
-    if (B.curved) {  // the face point and the edge tangent through the parent's curved map
-      Real X[3] = {0, 0, 0}, dX[3] = {0, 0, 0}, V[3], J[3][3];
+    if (B.curved) {  // the face point and the face tangents through the parent's curved map
+      Real X[3] = {0, 0, 0}, dX[3] = {0, 0, 0}, dY[3] = {0, 0, 0}, V[3], J[3][3];
       for (int k = 0; k < nfv; ++k) {
-        refVertex2d(B.type, ft[F.fl * nfv + k], V);
-        for (int l = 0; l < 2; ++l) { X[l] += sh[k] * V[l]; dX[l] += dxi[k] * V[l]; }
+        refVertexCurved(B.type, ft[F.fl * nfv + k], V);
+        for (int l = 0; l < 3; ++l) { X[l] += sh[k] * V[l]; dX[l] += dxi[k] * V[l]; if (nfv >= 3) dY[l] += deta[k] * V[l]; }
       }
       curvedMap(B, F.el, nodes, X, J, x);
-      for (int l = 0; l < 2; ++l) tx[l] = J[l][0] * dX[0] + J[l][1] * dX[1];
+      for (int l = 0; l < 3; ++l) {
+        tx[l] = J[l][0] * dX[0] + J[l][1] * dX[1] + J[l][2] * dX[2];
+        ty[l] = J[l][0] * dY[0] + J[l][1] * dY[1] + J[l][2] * dY[2];
+      }
     } else {
       for (int k = 0; k < nfv; ++k) {
         const double* c = &nodes[size_t(vv[ft[F.fl * nfv + k]]) * 3];
@@ -1019,8 +1028,10 @@ static Problem* create(const sdg_mesh* m, const sdg_config* c, int flags, int64_
     Block B; B.type = s.type; B.ne = s.n;
     B.ref.build(s.type, P->p);
     B.verts.assign(s.v, s.v + size_t(s.n) * elemVerts(s.type));
-    const int32_t* g = s.type == kTri ? m->triangle_geometry_node : (s.type == kQuad ? m->quadrangle_geometry_node : nullptr);
-    if (m->geometry_order > 1 && g) {  // curved 2D geometry (ReadControl.cpp:243-256)
+    const int32_t* g = s.type == kTri ? m->triangle_geometry_node
+                       : s.type == kQuad ? m->quadrangle_geometry_node
+                       : s.type == kHex ? m->hexahedron_geometry_node : nullptr;
+    if (m->geometry_order > 1 && g) {  // curved geometry (ReadControl.cpp:243-256)
       B.curved = true;
       B.geoOrder = m->geometry_order;
       B.cb.init(s.type, B.geoOrder);

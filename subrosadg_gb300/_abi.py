@@ -65,6 +65,7 @@ class SdgMesh(ctypes.Structure):
         ("geometry_order", c_int32),
         ("triangle_geometry_node", _p_int32),
         ("quadrangle_geometry_node", _p_int32),
+        ("hexahedron_geometry_node", _p_int32),
     ]
 
 

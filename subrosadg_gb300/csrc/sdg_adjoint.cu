@@ -121,6 +121,8 @@ AdjointState* adjoint(sdg_handle* h) {
   if (h->adj) return h->adj;
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
   if (h->curved) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives on curved (high-order) geometry are not built");
+  if (h->facePoint)
+    throw Failure(SDG_ERR_UNSUPPORTED, "derivatives on hexahedra that are not parallelepipeds are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   const bool gen = h->ph.incomp || h->ph.source;
   adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, gen, A->k);
@@ -676,7 +678,7 @@ ForceArgs forceInputs(sdg_handle* h, int physical, ForceInputs& in, bool pointOu
   ForceArgs a;
   std::memset(&a, 0, sizeof(a));
   a.face = h->face; a.faceGrad = h->faceGrad; a.conn = h->bconn; a.fgeo = h->bgeo; a.select = in.select;
-  a.fgeoPoint = h->curved ? 1 : 0;
+  a.fgeoPoint = h->facePoint ? 1 : 0;
   a.fw = in.fw; a.out = in.out; a.nface = h->nBoundary; a.n1d = h->n1d; a.ns = h->ns ? 1 : 0;
   return a;
 }

@@ -101,6 +101,35 @@ void facePointInParent(int type, int f, const double* fx, double* X) {
   }
 }
 
+// Outward n|J_f| (unnormalised) at face point fx of local face f, from the parent's Jacobian J there: the
+// face's tangents are J times the derivatives of its P1 map into the parent's reference element (the map of
+// facePointInParent); edges: n|J_f| = (t_y, -t_x); quadrangle and triangle faces: n|J_f| = t_xi x t_eta
+// (Geometry.cpp:115-147).  For a straight-sided parent this is the face's own P1 map differentiated.
+void faceNormalScaled(int type, int f, const double* fx, const double J[3][3], double* nJ) {
+  const int nfv = typeFaceVertices(type);
+  const int* fl = faceVertexList(type);
+  double ds[4] = {0, 0, 0, 0}, dt[4] = {0, 0, 0, 0};
+  if (nfv == 2) { ds[0] = -0.5; ds[1] = 0.5; }
+  else if (nfv == 3) { ds[0] = -1.0; ds[1] = 1.0; dt[0] = -1.0; dt[2] = 1.0; }
+  else if (nfv == 4) {
+    const double x = fx[0], y = fx[1];
+    ds[0] = -0.25 * (1 - y); ds[1] = 0.25 * (1 - y); ds[2] = 0.25 * (1 + y); ds[3] = -0.25 * (1 + y);
+    dt[0] = -0.25 * (1 - x); dt[1] = -0.25 * (1 + x); dt[2] = 0.25 * (1 + x); dt[3] = 0.25 * (1 - x);
+  }
+  double dXs[3] = {0, 0, 0}, dXt[3] = {0, 0, 0};
+  for (int k = 0; k < nfv; ++k) {
+    double V[3]; referenceVertex(type, fl[f * nfv + k], V);
+    for (int d = 0; d < 3; ++d) { dXs[d] += ds[k] * V[d]; dXt[d] += dt[k] * V[d]; }
+  }
+  double t1[3] = {0, 0, 0}, t2[3] = {0, 0, 0};
+  for (int l = 0; l < 3; ++l)
+    for (int k = 0; k < 3; ++k) { t1[l] += J[l][k] * dXs[k]; t2[l] += J[l][k] * dXt[k]; }
+  if (nfv == 2) { nJ[0] = t1[1]; nJ[1] = -t1[0]; nJ[2] = 0.0; return; }
+  nJ[0] = t1[1] * t2[2] - t1[2] * t2[1];
+  nJ[1] = t1[2] * t2[0] - t1[0] * t2[2];
+  nJ[2] = t1[0] * t2[1] - t1[1] * t2[0];
+}
+
 // Face-point pairing of triangular faces (the Triangle cases of SimulationControl.cpp:405-434, derived from
 // the geometry): the right face lists the shared vertices in the opposite orientation with the left face's
 // first vertex at position r, so left point (xi, eta) is right point r=0: (eta, xi), r=1: (1-xi-eta, eta),
@@ -563,7 +592,7 @@ Rec gradRec(sdg_handle* h, DevBlock& B, int which) {
     GradArgs& a = r.ga;
     std::memset(&a, 0, sizeof(a));
     a.u = u; a.face = h->face; a.faceOther = h->faceOther; a.faceGrad = h->faceGrad; a.grad = g;
-    a.geom = B.geom; a.fmetric = B.fmetric; a.fmetricPoint = B.curved; a.tables = B.tables; a.status = h->status;
+    a.geom = B.geom; a.fmetric = B.fmetric; a.fmetricPoint = B.facePoint; a.tables = B.tables; a.status = h->status;
     a.ne = B.ne; a.faceBase = B.faceBase; a.br2 = br2; a.epb = B.gepb;
     if (h->av) { a.av = 1; a.epsV = B.epsV; a.avTab = B.avTab; }
   } else {
@@ -571,7 +600,7 @@ Rec gradRec(sdg_handle* h, DevBlock& B, int which) {
     DenseGradArgs& a = r.da;
     std::memset(&a, 0, sizeof(a));
     a.u = u; a.face = h->face; a.faceOther = h->faceOther; a.faceGrad = h->faceGrad; a.grad = g;
-    a.geom = B.geom; a.fmetric = B.fmetric; a.fmetricPoint = B.curved; a.tables = B.tables; a.status = h->status;
+    a.geom = B.geom; a.fmetric = B.fmetric; a.fmetricPoint = B.facePoint; a.tables = B.tables; a.status = h->status;
     a.ne = B.ne; a.faceBase = B.faceBase; a.br2 = br2; a.epb = B.gepb;
     if (h->av) { a.av = 1; a.epsV = B.epsV; a.avTab = B.avTab; }
   }
@@ -596,7 +625,7 @@ Rec faceRec(sdg_handle* h, int op) {
   f.face = h->face; f.other = h->faceOther; f.faceGrad = h->faceGrad; f.faceFlux = h->faceFlux;
   f.conn = bnd ? h->bconn : h->fconn; f.fgeo = bnd ? h->bgeo : h->fgeo; f.ghost = h->ghost;
   f.nface = bnd ? h->nBoundary : h->nInterior; f.n1d = h->n1d; f.ph = h->ph; f.perm = h->facePerm;
-  f.fgeoPoint = h->curved ? 1 : 0;
+  f.fgeoPoint = h->facePoint ? 1 : 0;
   const int64_t points = f.nface * h->nfq;
   r.units = (points + kFaceThreads - 1) / kFaceThreads;
   // one thread per face point does a whole Riemann flux in FP64: with fewer points than two full CTAs per SM,
@@ -1081,11 +1110,16 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         mb.push_back({SDG_ELEMENT_TETRAHEDRON, mesh->tetrahedron_count, mesh->tetrahedron_node});
         if (c.polynomial_order > 5) throw Failure(SDG_ERR_UNSUPPORTED, "tetrahedra are built for P = 1..5");
       }
-      if (mesh->hexahedron_count > 0) mb.push_back({SDG_ELEMENT_HEXAHEDRON, mesh->hexahedron_count, mesh->hexahedron_node});
+      const int gq = mesh->geometry_order > 1 ? mesh->geometry_order : 1;
+      if (mesh->hexahedron_count > 0)
+        mb.push_back({SDG_ELEMENT_HEXAHEDRON, mesh->hexahedron_count, mesh->hexahedron_node,
+                      gq > 1 ? mesh->hexahedron_geometry_node : nullptr, gq});
     }
     if (mb.empty()) throw Failure(SDG_ERR_INVALID_ARGUMENT, "mesh has no elements of its dimension");
     if (mesh->geometry_order > 1) {
-      if (mesh->dimension != 2) throw Failure(SDG_ERR_UNSUPPORTED, "curved (high-order) geometry is built for 2D meshes");
+      if (mesh->dimension == 1) throw Failure(SDG_ERR_UNSUPPORTED, "curved (high-order) geometry is built in 2D and 3D");
+      if (mesh->dimension == 3 && mesh->tetrahedron_count > 0)
+        throw Failure(SDG_ERR_UNSUPPORTED, "curved (high-order) tetrahedra are not built");
       if (mesh->geometry_order > 5) throw Failure(SDG_ERR_INVALID_ARGUMENT, "geometry order must be 1..5");
       for (const Block& b : mb)
         if (!b.geometry) throw Failure(SDG_ERR_INVALID_ARGUMENT, "geometry_order > 1 needs the geometry nodes of every block");
@@ -1100,10 +1134,10 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     const double tol = 1e-12 * std::max(1.0, extent);
     size_t stateOff = 0, pointOff = 0;
     int64_t faceSlots = 0, relParts = 0;
-    std::vector<CurvedMap2d> blockMap(mb.size());  // the order-q map of each curved block
+    std::vector<CurvedMap> blockMap(mb.size());  // the order-q map of each curved block
     for (const Block& b : mb) {
       DevBlock B;
-      CurvedMap2d& curved = blockMap[size_t(&b - mb.data())];
+      CurvedMap& curved = blockMap[size_t(&b - mb.data())];
       B.type = b.type; B.dim = typeDim(b.type); B.p = h->p; B.ne = b.count; B.nface = typeFaces(b.type);
       B.kind = (b.type == SDG_ELEMENT_TRIANGLE || b.type == SDG_ELEMENT_TETRAHEDRON ||
                 (b.type == SDG_ELEMENT_QUADRANGLE && h->p == 1))
@@ -1127,10 +1161,8 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
           for (int k = 0; k < nvt; ++k)
             if (g[k] != b.vertex[e * nvt + k]) throw Failure(SDG_ERR_MESH, "geometry nodes must start with the element's vertices");
           for (int n = nvt; n < ngeo && !B.curved; ++n) {
-            double X[3] = {0, 0, 0}, J[3][3], x[3];
-            const auto& l = curved.lattice[n];
-            if (b.type == SDG_ELEMENT_QUADRANGLE) { X[0] = -1.0 + 2.0 * l[0] / b.geometryOrder; X[1] = -1.0 + 2.0 * l[1] / b.geometryOrder; }
-            else { X[0] = double(l[0]) / b.geometryOrder; X[1] = double(l[1]) / b.geometryOrder; }
+            double X[3], J[3][3], x[3];
+            gmshLatticePoint(b.type, b.geometryOrder, curved.lattice[n], X);
             jacobianAt(b.type, B.dim, nodes, b.vertex + e * nvt, X, J, x);
             for (int d = 0; d < 3; ++d)
               if (std::fabs(x[d] - nodes[size_t(g[n]) * 3 + d]) > tol) B.curved = 1;
@@ -1138,8 +1170,10 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
         }
       }
       if (B.curved) { B.affine = 0; h->curved = true; }
-      if (!B.affine && b.type == SDG_ELEMENT_HEXAHEDRON)
-        throw Failure(SDG_ERR_UNSUPPORTED, "hexahedra must be parallelepipeds (affine) in this version");
+      // per-point face metrics: curved blocks, and hexahedra that are not parallelepipeds (their faces are
+      // bilinear: in general neither planar nor of constant |J_f|)
+      B.facePoint = B.curved || (b.type == SDG_ELEMENT_HEXAHEDRON && !B.affine);
+      if (B.facePoint) h->facePoint = true;
       // geometry: affine [e][d*d+1]; bilinear tensor quads per point [e][q][d*d+1]; bilinear dense quads
       // [e][q][d*d+1] followed by the element's modal M^-1 [nb][nb] (Geometry.cpp:88-100)
       const int gs = B.dim * B.dim + 1;
@@ -1220,23 +1254,19 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
       }
       B.stateOffset = stateOff; stateOff += size_t(B.ne) * B.ustride;
       B.gradOffset = h->gradCount; h->gradCount += size_t(B.ne) * h->nv * B.dim * B.nb;
-      if (B.curved) {  // curved faces: outward n|J_f| at every face point of every local face, [e][f][j][d]
+      if (B.facePoint) {  // outward n|J_f| at every face point of every local face, [e][f][j][d]
         const PointRule fr = faceRule(b.type, h->p);
-        const int* fl = faceVertexList(b.type);
         B.fmetricHost.assign(size_t(B.ne) * B.nface * fr.n * B.dim, 0.0);
+#pragma omp parallel for schedule(static)
         for (int64_t e = 0; e < B.ne; ++e)
           for (int f = 0; f < B.nface; ++f)
             for (int j = 0; j < fr.n; ++j) {
-              double X[3], J[3][3], x[3], va[3], vb[3];
+              double X[3], J[3][3], x[3], nJ[3];
               facePointInParent(b.type, f, &fr.x[j * 3], X);
-              curved.eval(nodes, b.geometry + e * ngeo, X, J, x);
-              referenceVertex(b.type, fl[f * 2], va);
-              referenceVertex(b.type, fl[f * 2 + 1], vb);
-              // tangent dx/ds of the edge parametrised on [-1, 1] from its first to its second vertex
-              const double tx = J[0][0] * 0.5 * (vb[0] - va[0]) + J[0][1] * 0.5 * (vb[1] - va[1]);
-              const double ty = J[1][0] * 0.5 * (vb[0] - va[0]) + J[1][1] * 0.5 * (vb[1] - va[1]);
-              double* m = &B.fmetricHost[((size_t(e) * B.nface + f) * fr.n + j) * B.dim];
-              m[0] = ty; m[1] = -tx;
+              if (B.curved) curved.eval(nodes, b.geometry + e * ngeo, X, J, x);
+              else jacobianAt(b.type, B.dim, nodes, b.vertex + e * typeVertices(b.type), X, J, x);
+              faceNormalScaled(b.type, f, &fr.x[j * 3], J, nJ);
+              for (int k = 0; k < B.dim; ++k) B.fmetricHost[((size_t(e) * B.nface + f) * fr.n + j) * B.dim + k] = nJ[k];
             }
       } else if (!B.affine || B.kind == kDense) {  // outward n|J_f| of each local face (straight faces: constant)
         B.fmetricHost.assign(size_t(B.ne) * B.nface * B.dim, 0.0);
@@ -1277,32 +1307,28 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
 
     // faces: slots, orientation, straight-face geometry from the left parent's vertices (Geometry.cpp:102-169)
     const auto slotOf = [&](const FaceSide& s) { return h->blocks[s.block].faceBase + int64_t(s.element) * h->blocks[s.block].nface + s.face; };
-    // curved meshes: per face point [nfq][n (3), |J_f|] from the left parent's map (Geometry.cpp:102-127 on the
-    // face element's own high-order nodes, which are the parent's face nodes), and the point coordinates
-    const auto faceGeomCurved = [&](const FaceSide& s, double* g, std::vector<double>* coords) {
+    // per-point face geometry: [nfq][n (3), |J_f|] from the left parent's map (Geometry.cpp:102-147 on the
+    // face element's own nodes, which are the parent's face nodes), and the point coordinates
+    const auto faceGeomPoint = [&](const FaceSide& s, double* g, std::vector<double>* coords) {
       const DevBlock& B = h->blocks[s.block];
       const Block& b = mb[s.block];
       const PointRule fr = faceRule(B.type, B.p);
-      const int* fl = faceVertexList(B.type);
       const int ngeo = b.geometry ? gmshNodeCount(b.type, b.geometryOrder) : 0;
       const int32_t* vv = b.vertex + int64_t(s.element) * typeVertices(B.type);
       for (int j = 0; j < fr.n; ++j) {
-        double X[3], J[3][3], x[3], va[3], vb[3];
+        double X[3], J[3][3], x[3], nJ[3];
         facePointInParent(B.type, s.face, &fr.x[j * 3], X);
         if (B.curved) blockMap[s.block].eval(nodes, b.geometry + int64_t(s.element) * ngeo, X, J, x);
         else jacobianAt(B.type, B.dim, nodes, vv, X, J, x);
-        referenceVertex(B.type, fl[s.face * 2], va);
-        referenceVertex(B.type, fl[s.face * 2 + 1], vb);
-        const double tx = J[0][0] * 0.5 * (vb[0] - va[0]) + J[0][1] * 0.5 * (vb[1] - va[1]);
-        const double ty = J[1][0] * 0.5 * (vb[0] - va[0]) + J[1][1] * 0.5 * (vb[1] - va[1]);
-        const double area = std::sqrt(tx * tx + ty * ty);
+        faceNormalScaled(B.type, s.face, &fr.x[j * 3], J, nJ);
+        const double area = std::sqrt(nJ[0] * nJ[0] + nJ[1] * nJ[1] + nJ[2] * nJ[2]);
         double* gj = g + size_t(j) * 4;
-        gj[0] = ty / area; gj[1] = -tx / area; gj[2] = 0.0; gj[3] = area;
+        gj[0] = nJ[0] / area; gj[1] = nJ[1] / area; gj[2] = nJ[2] / area; gj[3] = area;
         if (coords) coords->insert(coords->end(), {x[0], x[1], x[2]});
       }
     };
     const auto faceGeom = [&](const FaceSide& s, double* g, std::vector<double>* coords) {
-      if (h->curved) { faceGeomCurved(s, g, coords); return; }
+      if (h->facePoint) { faceGeomPoint(s, g, coords); return; }
       const DevBlock& B = h->blocks[s.block];
       const int nfv = typeFaceVertices(B.type);
       const int32_t* vv = mb[s.block].vertex + int64_t(s.element) * typeVertices(B.type);
@@ -1353,7 +1379,7 @@ int sdg_create(const sdg_mesh* mesh, const sdg_config* config, int32_t device, s
     };
     h->nInterior = int64_t(adj.interior.size());
     h->nBoundary = int64_t(adj.boundary.size());
-    const int fgs = h->curved ? 4 * h->nfq : 4;  // face geometry doubles per face (per point when curved)
+    const int fgs = h->facePoint ? 4 * h->nfq : 4;  // face geometry doubles per face (or per face point)
     std::vector<int> fconn(size_t(h->nInterior) * 3);
     std::vector<double> fgeo(size_t(h->nInterior) * fgs);
     for (int64_t i = 0; i < h->nInterior; ++i) {

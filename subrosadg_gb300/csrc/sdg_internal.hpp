@@ -37,7 +37,8 @@ enum Kind { kTensor = 0, kDense = 1 };
 struct DevBlock {
   int type = 0, dim = 2, p = 1, n = 0, kind = kTensor, affine = 1;
   int diagMetric = 0;              // affine tensor block whose metric terms |J| dxi/dx are all diagonal
-  int curved = 0;                  // 2D block with curved (high-order) elements: per-point face metrics
+  int curved = 0;                  // block with curved (high-order) elements
+  int facePoint = 0;               // face metrics per face point (curved blocks, hexahedra not parallelepipeds)
   int nb = 0, nq = 0, nface = 0, nfq = 0, ustride = 0, fstride = 0, geomStride = 0;
   int64_t ne = 0, faceBase = 0;
   size_t stateOffset = 0;          // doubles
@@ -149,7 +150,8 @@ struct sdg_handle {
   bool timing = false;             // bracket launches with events (sdg_set_kernel_timing)
   std::vector<std::array<cudaEvent_t, 2>> timedEvents;
   std::vector<int> timedClass;
-  bool curved = false;             // some block curved: face geometry and face metrics per face point
+  bool curved = false;             // some block curved
+  bool facePoint = false;          // some block with per-point face metrics: face geometry per face point
   unsigned waitLimit = 0;          // sdg_set_wait_check: mbarrier wait rounds of the tensor stage kernels
   unsigned txExtra = 0;            // sdg_set_wait_check: bytes declared beyond the tile copies
   bool useGraph = true;            // sdg_step replays a captured CUDA graph of one step

@@ -152,7 +152,7 @@ struct MeshStorage {
   std::vector<double> node;
   std::vector<int32_t> periodic, line, tri, quad, hex, tet, bnode, bphys, bc;
   int geometryOrder = 1;
-  std::vector<int32_t> triGeo, quadGeo;  // curved 2D meshes: gmsh-ordered geometry nodes per element
+  std::vector<int32_t> triGeo, quadGeo, hexGeo;  // curved meshes: gmsh-ordered geometry nodes per element
 };
 
 void publish(MeshStorage* s, int dim, sdg_generated_mesh* out) {
@@ -174,6 +174,7 @@ void publish(MeshStorage* s, int dim, sdg_generated_mesh* out) {
     m.geometry_order = s->geometryOrder;
     m.triangle_geometry_node = s->triGeo.empty() ? nullptr : s->triGeo.data();
     m.quadrangle_geometry_node = s->quadGeo.empty() ? nullptr : s->quadGeo.data();
+    m.hexahedron_geometry_node = s->hexGeo.empty() ? nullptr : s->hexGeo.data();
   }
   out->storage = s;
 }
@@ -278,8 +279,8 @@ int sdg_mesh_generate_annulus(double inner_radius, double outer_radius, int32_t 
       const size_t n = size_t(id(I, J));
       s->node[n * 3 + 0] = r * std::cos(t); s->node[n * 3 + 1] = r * std::sin(t); s->node[n * 3 + 2] = 0.0;
     }
-  const std::vector<std::array<int, 2>> quadLat = sdg::gmshLattice(SDG_ELEMENT_QUADRANGLE, q);
-  const std::vector<std::array<int, 2>> triLat = sdg::gmshLattice(SDG_ELEMENT_TRIANGLE, q);
+  const std::vector<std::array<int, 3>> quadLat = sdg::gmshLattice(SDG_ELEMENT_QUADRANGLE, q);
+  const std::vector<std::array<int, 3>> triLat = sdg::gmshLattice(SDG_ELEMENT_TRIANGLE, q);
   std::mt19937_64 rsplit(seed);
   const auto unit = [](std::mt19937_64& g) { return double(g() >> 11) * (1.0 / 9007199254740992.0); };
   for (int64_t i = 0; i < nr; ++i)
@@ -567,15 +568,17 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
       if (it == nodeIndex.end()) throw std::runtime_error("element references an unknown node");
       return it->second;
     };
-    // 2D meshes of order q > 1 (the drivers' setOrder(P)): every element's full node list in gmsh order is
-    // kept as its curved geometry (ReadControl.cpp:243-256); lines and 3D elements keep their vertices only
+    // 2D meshes and hexahedra of order q > 1 (the drivers' setOrder(P)): every element's full node list in
+    // gmsh order is kept as its curved geometry (ReadControl.cpp:243-256); lines and tetrahedra keep their
+    // vertices only
     int order2d = 0;
     for (const RawEl& r : raw) {
       int dim = 0, nn = 0, nprim = 0; typeInfo(r.type, dim, nn, nprim);
-      if (dim != 2 || maxDim != 2) continue;
+      if (dim != maxDim || (dim != 2 && !(dim == 3 && nprim == 8))) continue;
+      const int et = dim == 3 ? SDG_ELEMENT_HEXAHEDRON : (nprim == 3 ? SDG_ELEMENT_TRIANGLE : SDG_ELEMENT_QUADRANGLE);
       int q = 1;
-      while (sdg::gmshNodeCount(nprim == 3 ? SDG_ELEMENT_TRIANGLE : SDG_ELEMENT_QUADRANGLE, q) < nn) ++q;
-      if (order2d && q != order2d) throw std::runtime_error("2D elements of different geometry orders");
+      while (sdg::gmshNodeCount(et, q) < nn) ++q;
+      if (order2d && q != order2d) throw std::runtime_error("elements of different geometry orders");
       order2d = q;
     }
     for (const RawEl& r : raw) {
@@ -587,6 +590,8 @@ int sdg_mesh_read_msh(const char* path, sdg_generated_mesh* out) {
         for (int64_t v : r.v) dst->push_back(idx(v));
         if (maxDim == 2 && order2d > 1)
           for (int64_t v : r.all) (nprim == 3 ? s->triGeo : s->quadGeo).push_back(idx(v));
+        if (maxDim == 3 && nprim == 8 && order2d > 1)
+          for (int64_t v : r.all) s->hexGeo.push_back(idx(v));
       } else if (dim == maxDim - 1) {
         const auto it = entityPhysical.find({r.edim, r.etag});
         if (it == entityPhysical.end() || it->second.empty()) continue;

@@ -59,7 +59,7 @@ struct Block {
   int type = 0;
   int64_t count = 0;
   const int32_t* vertex = nullptr;    // [count][typeVertices]
-  const int32_t* geometry = nullptr;  // curved 2D meshes: [count][gmsh node count of order geometryOrder]
+  const int32_t* geometry = nullptr;  // curved meshes: [count][gmsh node count of order geometryOrder]
   int geometryOrder = 1;
 };
 

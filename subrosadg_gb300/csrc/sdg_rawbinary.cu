@@ -222,7 +222,7 @@ class Br2Records {
       const double* g = &B.geomHost[size_t(e) * B.geomStride];
       const double sg = T.faceEnd[f] ? 1.0 : -1.0;
       for (int k = 0; k < d; ++k) nF[k] = sg * g[T.faceAxis[f] * d + k];
-    } else if (B.curved) {
+    } else if (B.facePoint) {
       for (int k = 0; k < d; ++k) nF[k] = B.fmetricHost[((size_t(e) * B.nface + f) * nfq_ + j) * d + k];
     } else {
       for (int k = 0; k < d; ++k) nF[k] = B.fmetricHost[(size_t(e) * B.nface + f) * d + k];

@@ -28,6 +28,9 @@ struct KernelVariant {
 // Tile kernels (elements of one block per CTA).  Unsupported combinations return an invalid variant.
 KernelVariant tensorStageVariant(int dim, int n, bool affine, int visc);  // visc: 0 Euler, 1 NS, 2 AV
 KernelVariant tensorGradVariant(int dim, int n, bool affine, bool br2);
+// Hexahedra that are not parallelepipeds (sdg_variants_tensor_hex.cu), reached through the two above.
+KernelVariant hexNonAffineStageVariant(int n, int visc);
+KernelVariant hexNonAffineGradVariant(int n, bool br2);
 KernelVariant denseStageVariant(int type, int p, bool affine, int visc);
 KernelVariant denseGradVariant(int type, int p, bool affine);
 // Face-point kernels (FaceOp op, flux only for the Riemann operations) and the relative-error reduction.

@@ -37,6 +37,7 @@ KernelVariant tensorStageVariant(int dim, int n, bool affine, int visc) {
     if (affine) return visc == 2 ? stageOf<D, NN, true, 2>() : visc ? stageOf<D, NN, true, 1>() : stageOf<D, NN, true, 0>(); \
     if constexpr (D == 2)                                                                                    \
       return visc == 2 ? stageOf<D, NN, false, 2>() : visc ? stageOf<D, NN, false, 1>() : stageOf<D, NN, false, 0>(); \
+    if constexpr (D == 3) return hexNonAffineStageVariant(NN, visc);                                         \
     return KernelVariant();                                                                                  \
   }
   SDG_TENSOR_ORDERS(SDG_TS)
@@ -49,6 +50,7 @@ KernelVariant tensorGradVariant(int dim, int n, bool affine, bool br2) {
   if (dim == D && n == NN) {                                                                  \
     if (affine) return br2 ? gradOf<D, NN, true, true>() : gradOf<D, NN, true, false>();       \
     if constexpr (D == 2) return br2 ? gradOf<D, NN, false, true>() : gradOf<D, NN, false, false>(); \
+    if constexpr (D == 3) return hexNonAffineGradVariant(NN, br2);                            \
     return KernelVariant();                                                                   \
   }
   SDG_TENSOR_ORDERS(SDG_TG)

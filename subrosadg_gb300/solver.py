@@ -34,15 +34,18 @@ class Mesh:
 
     def __init__(self, dimension, nodes, triangles=None, quadrangles=None, hexahedra=None, boundary=None,
                  boundary_physical=None, physical_conditions=None, periodic_master=None, lines=None,
-                 tetrahedra=None, geometry_order=1, triangle_geometry=None, quadrangle_geometry=None):
+                 tetrahedra=None, geometry_order=1, triangle_geometry=None, quadrangle_geometry=None,
+                 hexahedron_geometry=None):
         self.dimension = int(dimension)
-        # curved 2D meshes: order-q geometry nodes per element in gmsh order (corners first)
+        # curved meshes: order-q geometry nodes per element in gmsh order (corners first)
         self.geometry_order = int(geometry_order)
         q = self.geometry_order
         self.triangle_geometry = None if triangle_geometry is None or len(triangle_geometry) == 0 else \
             np.ascontiguousarray(triangle_geometry, np.int32).reshape(-1, (q + 1) * (q + 2) // 2)
         self.quadrangle_geometry = None if quadrangle_geometry is None or len(quadrangle_geometry) == 0 else \
             np.ascontiguousarray(quadrangle_geometry, np.int32).reshape(-1, (q + 1) ** 2)
+        self.hexahedron_geometry = None if hexahedron_geometry is None or len(hexahedron_geometry) == 0 else \
+            np.ascontiguousarray(hexahedron_geometry, np.int32).reshape(-1, (q + 1) ** 3)
         self.nodes = np.ascontiguousarray(nodes, dtype=np.float64).reshape(-1, 3)
         self.lines = None if lines is None or len(lines) == 0 else np.ascontiguousarray(lines, np.int32).reshape(-1, 2)
         self.triangles = None if triangles is None or len(triangles) == 0 else np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
@@ -82,6 +85,9 @@ class Mesh:
             if m.quadrangle_count:
                 out.quadrangle_geometry = arr(m.quadrangle_geometry_node, m.quadrangle_count, (q + 1) ** 2,
                                               np.int32).reshape(m.quadrangle_count, -1)
+            if m.hexahedron_count and m.hexahedron_geometry_node:
+                out.hexahedron_geometry = arr(m.hexahedron_geometry_node, m.hexahedron_count, (q + 1) ** 3,
+                                              np.int32).reshape(m.hexahedron_count, -1)
         _abi.load().sdg_mesh_free(byref(g))
         return out
 
@@ -171,6 +177,7 @@ class Mesh:
         m.geometry_order = self.geometry_order if self.geometry_order > 1 else 0
         m.triangle_geometry_node = _ptr(self.triangle_geometry, _pi)
         m.quadrangle_geometry_node = _ptr(self.quadrangle_geometry, _pi)
+        m.hexahedron_geometry_node = _ptr(self.hexahedron_geometry, _pi)
         return m
 
 

@@ -109,6 +109,50 @@ CASES = {
         conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
                     sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL)),
     "ns-tet-box-p1-br1-hllc": lambda: cases.tet_box_case(p=1, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01),
+    # hexahedra that are not parallelepipeds (trilinear maps of a smoothly warped box: the metric |J| dxi/dx and
+    # 1/|J| per node, normals and |J_f| per face point of the bilinear faces)
+    "warped-hex-tgv-p1-hllc": lambda: cases.warped(cases.tgv_case(n=4, p=1, flux=sdg.HLLC, steps=3)),
+    "warped-hex-tgv-p3-hllc": lambda: cases.warped(cases.tgv_case(n=3, p=3, flux=sdg.HLLC, steps=2)),
+    "warped-hex-tgv-p5-roe": lambda: cases.warped(cases.tgv_case(n=3, p=5, flux=sdg.ROE, steps=2)),
+    "warped-hex-farfield-p2-lf": lambda: cases.warped(cases.hex_box_case(p=2, flux=sdg.LAX_FRIEDRICHS)),
+    "warped-hex-slip-inflow-outflow-p4-roe": lambda: cases.warped(cases.hex_box_case(
+        p=4, flux=sdg.ROE, steps=2,
+        conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW) + (sdg.ADIABATIC_SLIP_WALL,) * 4)),
+    "ns-warped-hex-tgv-p2-br1-roe": lambda: cases.warped(cases.tgv_case(n=3, p=2, flux=sdg.ROE, viscous=sdg.BR1,
+                                                                        mu=0.02)),
+    "ns-warped-hex-walls-p3-br2-lf": lambda: cases.warped(cases.hex_box_case(
+        p=3, flux=sdg.LAX_FRIEDRICHS, viscous=sdg.BR2, mu=0.01, steps=2,
+        conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
+                    sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL))),
+    "ns-warped-hex-walls-p5-br1-hllc": lambda: cases.warped(cases.hex_box_case(
+        p=5, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01, steps=2,
+        conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
+                    sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL))),
+    "inc-warped-lidcavity-hex-p3-exact-br2": lambda: cases.warped(cases.cavity_3d_case(p=3, viscous=sdg.BR2, mu=1e-2,
+                                                                                       steps=2)),
+    "av-warped-shocktube-hex-p3-hllc": lambda: cases.warped(cases.shock_tube_case(p=3, dim=3, n=6, steps=2),
+                                                            amplitude=0.04),
+    # curved hexahedra: order-q geometry nodes (gmsh's hexahedron node order) on a warped box; the per-node metric
+    # and the per-face-point normals and |J_f| of the order-q map
+    "curved-hex-tgv-p2-q2-hllc": lambda: cases.curved_hex(cases.tgv_case(n=3, p=2, flux=sdg.HLLC, steps=2), 2),
+    "curved-hex-tgv-p3-q3-roe": lambda: cases.curved_hex(cases.tgv_case(n=3, p=3, flux=sdg.ROE, steps=2), 3),
+    "curved-hex-tgv-p4-q2-lf": lambda: cases.curved_hex(cases.tgv_case(n=3, p=4, flux=sdg.LAX_FRIEDRICHS, steps=2), 2),
+    "curved-hex-tgv-p5-q5-hllc": lambda: cases.curved_hex(cases.tgv_case(n=3, p=5, flux=sdg.HLLC, steps=2), 5),
+    "curved-hex-farfield-p3-q3-hllc": lambda: cases.curved_hex(cases.hex_box_case(p=3, flux=sdg.HLLC, steps=2), 3),
+    "ns-curved-hex-tgv-p2-q2-br1-roe": lambda: cases.curved_hex(cases.tgv_case(n=3, p=2, flux=sdg.ROE,
+                                                                               viscous=sdg.BR1, mu=0.02), 2),
+    "ns-curved-hex-walls-p3-q3-br2-lf": lambda: cases.curved_hex(cases.hex_box_case(
+        p=3, flux=sdg.LAX_FRIEDRICHS, viscous=sdg.BR2, mu=0.01, steps=2,
+        conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
+                    sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL)), 3),
+    "ns-curved-hex-walls-p4-q4-br1-hllc": lambda: cases.curved_hex(cases.hex_box_case(
+        p=4, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01, steps=2,
+        conditions=(sdg.VELOCITY_INFLOW, sdg.PRESSURE_OUTFLOW, sdg.ISOTHERMAL_NONSLIP_WALL,
+                    sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD, sdg.ADIABATIC_SLIP_WALL)), 4),
+    "inc-curved-lidcavity-hex-p3-q3-exact-br2": lambda: cases.curved_hex(
+        cases.cavity_3d_case(p=3, viscous=sdg.BR2, mu=1e-2, steps=2), 3),
+    "av-curved-shocktube-hex-p3-q3-hllc": lambda: cases.curved_hex(cases.shock_tube_case(p=3, dim=3, n=6, steps=2),
+                                                                   3, amplitude=0.04),
     # tetrahedra P4 (35 modes, the 69-point Grundmann-Moeller volume rule, 19-point Dunavant faces)
     "tet-tgv-p4-hllc": lambda: cases.tet_tgv_case(n=3, p=4, flux=sdg.HLLC, steps=2),
     "tet-tgv-p4-roe": lambda: cases.tet_tgv_case(n=3, p=4, flux=sdg.ROE, steps=2),
@@ -368,6 +412,30 @@ def test_curved_wall_force_of_a_uniform_state_vanishes(q):
     g.initialize_primitive(cases.uniform_primitive(g.counts.volume_point_count, 2, vel=(0.0, 0.0)))
     f = g.surface_force(1)
     assert np.abs(f).max() < 1e-12, f
+
+
+@pytest.mark.parametrize("q", [1, 2, 3])
+def test_warped_hexahedra_wall_force_of_a_uniform_state_vanishes(q):
+    """Per-point face geometry of bilinear (q = 1) and order-q hexahedron faces: the pressure force of a uniform
+    state on the closed (warped) boundary of a box is zero to round-off, since the face rule integrates the
+    faces' n|J_f| exactly and the boundary closes."""
+    case = cases.hex_box_case(p=q + 1, conditions=(sdg.ADIABATIC_SLIP_WALL,) * 6)
+    mesh = (cases.warped(case) if q == 1 else cases.curved_hex(case, q))[0]
+    g = sdg.GpuSolver(mesh, cases.config(q + 1, sdg.HLLC))
+    g.initialize_primitive(cases.uniform_primitive(g.counts.volume_point_count, 3, vel=(0.0, 0.0, 0.0)))
+    f = sum(g.surface_force(k) for k in range(1, 7))
+    assert np.abs(f).max() < 1e-12, f
+
+
+@pytest.mark.parametrize("q", [1, 2])
+def test_warped_hexahedra_refuse_derivatives(q):
+    case = cases.tgv_case(n=3, p=2)
+    mesh, cfg, prim, _, _, _ = cases.warped(case) if q == 1 else cases.curved_hex(case, q)
+    g = sdg.GpuSolver(mesh, cfg)
+    g.initialize_primitive(prim(g.volume_points()))
+    with pytest.raises(sdg.SdgError) as err:
+        g.vjp_residual(np.zeros((g.counts.volume_point_count, 5)))
+    assert err.value.code == 5  # SDG_ERR_UNSUPPORTED
 
 
 def test_curved_meshes_refuse_derivatives():
