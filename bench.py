@@ -21,6 +21,8 @@ workloads of the metric, each measured the same way on this GPU:
                split, P4, Lax-Friedrichs
   vortex2d     2D Euler isentropic vortex, 40^2 quads, P3, Roe, dt 1e-3 (L2-resident, launch bound)
   tet          3D Euler Taylor-Green vortex (Mach 0.3) on periodic tetrahedra, 32^3 cubes x 6, P3, HLLC
+  curved       3D Navier-Stokes BR2 (HLLC, Re 200, Mach 0.2) along a no-slip wall on 32^3 curved hexahedra of
+               geometry order 3, P3: the shape of the sphere driver
   adjoint      3D Navier-Stokes BR1 Taylor-Green, Re 1600, Mach 0.1, 32^3 hexahedra, P3, Roe, 500 SSP-RK3 steps:
                forward, checkpointed adjoint (every 25 steps) of the integrated kinetic energy, reverse sweep
                of a recorded trajectory, and central-difference checks of dJ/dU0 (seeded direction) and dJ/dmu
@@ -61,12 +63,13 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="headline workload only")
-    ap.add_argument("--extra", default="batched,batched_small,ns_hybrid,vortex2d,tet,adjoint",
+    ap.add_argument("--extra", default="batched,batched_small,ns_hybrid,vortex2d,tet,curved,adjoint",
                     help="comma list of the other workloads to measure")
     ap.add_argument("--batch-count", type=int, default=256)
     ap.add_argument("--batch-max-elements", type=int, default=50000)
     ap.add_argument("--ns-elements", type=int, default=256, help="quads per direction of the NS hybrid mesh")
     ap.add_argument("--tet-elements", type=int, default=32, help="cubes per side of the tetrahedral section")
+    ap.add_argument("--curved-elements", type=int, default=32, help="curved hexahedra per side of the curved section")
     ap.add_argument("--adjoint-elements", type=int, default=32)
     ap.add_argument("--adjoint-steps", type=int, default=500)
     ap.add_argument("--no-adjoint-check", action="store_true", help="skip the finite-difference checks")
@@ -379,6 +382,40 @@ def bench_tet(args, device, torch):
     return out
 
 
+def bench_curved(args, device, torch):
+    """Navier-Stokes BR2 with HLLC along a curved no-slip wall on curved hexahedra (geometry order 3), P3, Re 200,
+    Mach 0.2: the shape of examples/sphere_3d_cns.cpp, n^3 elements of a warped box."""
+    import ctypes
+
+    import subrosadg_gb300 as sdg
+    from subrosadg_gb300 import workloads as wl
+    n = args.curved_elements
+    mesh, cfg, prim, bprim, _, _ = wl.curved_wall_case(n=n, p=3, q=3)
+    g = sdg.GpuSolver(mesh, cfg, device=device)
+    g.initialize_primitive(prim(g.volume_points()))
+    bpts, phys = g.boundary_points()
+    g.set_boundary_primitive(bprim(bpts, np.repeat(phys, g.counts.face_point_count)))
+    dt = g.calculateDeltaTime(0.2)
+    g.autotune()
+    sp = ctypes.c_void_p()
+    g.lib.sdg_get_stream(g.h, ctypes.byref(sp))
+    stream = torch.cuda.ExternalStream(sp.value, device=device)
+    for _ in range(args.warmup):
+        g.step_async(dt)
+    g.synchronize()
+    steps = max(3, args.steps)
+    ms = _timed(torch, stream, lambda: g.step_async(dt), steps)
+    g.synchronize()
+    dof = g.counts.degree_of_freedom_count
+    err = g.relative_error()
+    out = {"workload": f"ns-curved-wall-BR2-HLLC-Re200-Ma0.2-{n}^3-hex-P3-q3", "elements": g.counts.element_count,
+           "dof": dof, "value": dof * 3 * steps / (ms * 1e-3), "unit": "DOF-stage/s", "ms_per_step": ms / steps,
+           "finite": bool(np.all(np.isfinite(err))), "tiles": [g.tile(0)],
+           "kernel_ms_per_step": kernel_split(g, dt, 3)}
+    g.close()
+    return out
+
+
 def bench_vortex(args, device, torch):
     """2D Euler isentropic vortex, 40^2 quads, P3, Roe, dt 1e-3: state ~0.8 MB (L2-resident)."""
     import ctypes
@@ -635,7 +672,7 @@ def run_ours(args):
     s.close()
     if not args.no_extra:
         extras = {"batched": bench_batched, "ns_hybrid": bench_ns_hybrid, "vortex2d": bench_vortex,
-                  "tet": bench_tet,
+                  "tet": bench_tet, "curved": bench_curved,
                   "adjoint": bench_adjoint,
                   "batched_small": lambda a, d, t: bench_batched(a, d, t, max_elements=2000)}
         for name in [x for x in args.extra.split(",") if x]:

@@ -123,6 +123,126 @@ def tet_tgv_case(n=3, p=2, flux=sdg.HLLC, steps=3, mach=0.3, viscous=None, mu=0.
             steps)
 
 
+def _warp(x, lo, span, amplitude):
+    s = np.sin(2.0 * math.pi * (x - lo) / span)
+    d = amplitude * span / (2.0 * math.pi) * np.stack([s[:, 1] * s[:, 2], s[:, 2] * s[:, 0], s[:, 0] * s[:, 1]], 1)
+    return np.ascontiguousarray(x + d)
+
+
+def warped(case, amplitude=0.08):
+    """The same case on a smoothly deformed 3D mesh: node x moves by amplitude L/(2 pi) times
+    (sin k y sin k z, sin k z sin k x, sin k x sin k y), k = 2 pi / L per direction over the mesh's bounding box.
+    The deformation is periodic over the box (opposite faces of a periodic box stay translates of each other)
+    and leaves no hexahedron a parallelepiped: the elements are general trilinear maps, their faces bilinear
+    (neither planar nor of constant |J_f|) -- the mapped hexahedra of the reference's 3D drivers
+    (examples/sphere_3d_cns.cpp, examples/protuberance_3d_ceuler.cpp) at geometry order 1."""
+    mesh, cfg, ic, bc, dt, steps = case
+    lo, hi = mesh.nodes.min(0), mesh.nodes.max(0)
+    mesh.nodes = _warp(mesh.nodes, lo, hi - lo, amplitude)
+    return (mesh, cfg, ic, bc, dt, steps)
+
+
+_HEX_CORNERS = [(-1, -1, -1), (1, -1, -1), (1, 1, -1), (-1, 1, -1), (-1, -1, 1), (1, -1, 1), (1, 1, 1), (-1, 1, 1)]
+_HEX_EDGES = [(0, 1), (0, 3), (0, 4), (1, 2), (1, 5), (2, 3), (2, 6), (3, 7), (4, 5), (4, 7), (5, 6), (6, 7)]
+_HEX_FACES = [(0, 3, 2, 1), (0, 1, 5, 4), (0, 4, 7, 3), (1, 2, 6, 5), (2, 3, 7, 6), (4, 5, 6, 7)]
+_HEX_NEIGHBOURS = [(1, 3, 4), (0, 2, 5), (1, 3, 6), (0, 2, 7), (0, 5, 7), (1, 4, 6), (2, 5, 7), (3, 4, 6)]
+
+
+def _quad_nodes(c, r):
+    """gmsh's order-r quadrangle nodes on four corner points c (3D): corners, edge interiors in edge direction,
+    then the inner quadrangle of order r - 2 one lattice step inside, recursively."""
+    out = []
+    while r >= 0:
+        if r == 0:
+            out.append(sum(c) / 4.0)
+            break
+        out += list(c)
+        for k in range(4):
+            out += [c[k] + (c[(k + 1) % 4] - c[k]) * i / r for i in range(1, r)]
+        if r < 2:
+            break
+        c = [c[k] + (c[(k + 1) % 4] - c[k]) / r + (c[(k - 1) % 4] - c[k]) / r for k in range(4)]
+        r -= 2
+    return out
+
+
+def hex_lattice(q):
+    """Reference points of gmsh's order-q hexahedron in its node order: the 8 corners, the edge interiors
+    (gmsh's edge table, in edge direction), each face's interior as an order q-2 quadrangle whose corners follow
+    the face's vertex list (gmsh's face table), then the interior as an order q-2 hexahedron, recursively."""
+    c = [np.array(p, dtype=float) for p in _HEX_CORNERS]
+    out, r = [], q
+    while r >= 0:
+        if r == 0:
+            out.append(sum(c) / 8.0)
+            break
+        out += c
+        for a, b in _HEX_EDGES:
+            out += [c[a] + (c[b] - c[a]) * i / r for i in range(1, r)]
+        if r < 2:
+            break
+        for f in _HEX_FACES:
+            fc = [c[f[k]] + (c[f[(k + 1) % 4]] - c[f[k]]) / r + (c[f[(k - 1) % 4]] - c[f[k]]) / r for k in range(4)]
+            out += _quad_nodes(fc, r - 2)
+        c = [c[k] + sum((c[m] - c[k]) / r for m in _HEX_NEIGHBOURS[k]) for k in range(8)]
+        r -= 2
+    return np.array(out)
+
+
+def curved_hex(case, q, amplitude=0.08):
+    """The same case on curved hexahedra of geometry order q: each element's gmsh-ordered order-q nodes are
+    placed by its trilinear map and then moved, with the vertices, by the `warped` deformation, so every face is
+    a curved surface (the order-q elements of the reference's 3D drivers after setOrder(P), e.g.
+    examples/sphere_3d_cns.cpp:379).  Interior nodes are per element; the corners are the mesh vertices."""
+    mesh, cfg, ic, bc, dt, steps = case
+    x = mesh.nodes
+    lo, hi = x.min(0), x.max(0)
+    lat = hex_lattice(q)
+    sx = np.stack([(1 + sgn * lat[:, d]) / 2 for d in range(3) for sgn in (-1, 1)], 1)  # [(1-X)/2, (1+X)/2, ...]
+    shape = np.stack([sx[:, 0 + (c[0] > 0)] * sx[:, 2 + (c[1] > 0)] * sx[:, 4 + (c[2] > 0)] for c in _HEX_CORNERS], 1)
+    hexes = mesh.hexahedra
+    pts = np.einsum("qk,ekd->eqd", shape, x[hexes])[:, 8:, :]
+    ne, extra = len(hexes), len(lat) - 8
+    ids = len(x) + np.arange(ne * extra, dtype=np.int32).reshape(ne, extra)
+    nodes = _warp(np.concatenate([x, pts.reshape(-1, 3)]), lo, hi - lo, amplitude)
+    periodic = None
+    if mesh.periodic_master is not None:
+        periodic = np.concatenate([mesh.periodic_master, ids.reshape(-1)])
+    out = Mesh(3, nodes, hexahedra=hexes, boundary=mesh.boundary, boundary_physical=mesh.boundary_physical,
+                   physical_conditions=mesh.physical_conditions, periodic_master=periodic, geometry_order=q,
+                   hexahedron_geometry=np.concatenate([hexes, ids], 1))
+    return (out, cfg, ic, bc, dt, steps)
+
+
+def curved_wall_case(n=32, p=3, q=3, flux=sdg.HLLC, viscous=sdg.BR2, re=200.0, amplitude=0.08, steps=3):
+    """Navier-Stokes along a curved no-slip wall, the shape of examples/sphere_3d_cns.cpp (P3, HLLC, BR2, curved
+    hexahedra of geometry order 3 after setOrder(3), a Riemann farfield and an adiabatic no-slip wall, the stream
+    rho = 1.4, v = 0.2, T = 1 (Mach 0.2) and mu = 1.4 * 0.2 / Re with Re = 200): the unit box of n^3 curved
+    hexahedra of geometry order q (curved_hex of the warped box), the wall at z = 0 (group 5) and the farfield on
+    the other five sides.  The initial state is the stream with a smooth density perturbation."""
+    conds = [sdg.RIEMANN_FARFIELD] * 4 + [sdg.ADIABATIC_NONSLIP_WALL, sdg.RIEMANN_FARFIELD]
+    mesh = Mesh.box_3d(0, 0, 0, 1, 1, 1, n, n, n, periodic=False, boundary_conditions=conds)
+    cfg = ns_config(p, flux, viscous, 1.4 * 0.2 / re)
+
+    def ic(pts):
+        x, y, z = pts[:, 0], pts[:, 1], pts[:, 2]
+        out = np.zeros((len(pts), 5))
+        out[:, 0] = 1.4 * (1.0 + 0.02 * np.sin(2 * math.pi * x) * np.sin(2 * math.pi * y) * np.sin(math.pi * z))
+        out[:, 2] = 0.2
+        out[:, 4] = 1.4 / out[:, 0]  # p = rho R T = 1 with R = 1/1.4
+        return out
+
+    def bc(pts, phys):
+        out = np.zeros((len(pts), 5))
+        out[:, 0] = 1.4
+        out[:, 2] = np.where(phys == 5, 0.0, 0.2)
+        out[:, 4] = 1.0
+        return out
+
+    dt = 0.2 * (1.0 / n) / ((0.2 + 1.0) * (p + 1) ** 2)
+    return curved_hex((mesh, cfg, ic, bc, dt, steps), q, amplitude)
+
+
 def kh_case(n=8, p=4, flux=sdg.LAX_FRIEDRICHS, dt=2e-4, steps=3, jitter=0.1, split=0.5, seed=11, viscous=None,
             mu=1e-4):
     """Kelvin-Helmholtz; with `viscous` the Navier-Stokes case at Re = 1/mu (1e4 by default)."""
