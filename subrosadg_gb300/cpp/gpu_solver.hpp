@@ -51,6 +51,10 @@ struct Mesh {
   std::vector<double> node;  // [n][3]
   std::vector<int32_t> line, triangle, quadrangle, tetrahedron, hexahedron;
   std::vector<int32_t> boundary_node, boundary_physical, physical_boundary_condition, periodic_master;
+  // curved meshes (setOrder(P), ReadControl.cpp:243-256): geometry order q > 1 and each element's gmsh-ordered
+  // order-q nodes
+  int geometry_order = 1;
+  std::vector<int32_t> triangle_geometry, quadrangle_geometry, hexahedron_geometry;
 
   sdg_mesh view() const {
     sdg_mesh m{};
@@ -73,6 +77,12 @@ struct Mesh {
     m.line_node = line.data();
     m.tetrahedron_count = int64_t(tetrahedron.size() / 4);
     m.tetrahedron_node = tetrahedron.data();
+    if (geometry_order > 1) {
+      m.geometry_order = geometry_order;
+      m.triangle_geometry_node = triangle_geometry.empty() ? nullptr : triangle_geometry.data();
+      m.quadrangle_geometry_node = quadrangle_geometry.empty() ? nullptr : quadrangle_geometry.data();
+      m.hexahedron_geometry_node = hexahedron_geometry.empty() ? nullptr : hexahedron_geometry.data();
+    }
     return m;
   }
 
@@ -93,6 +103,13 @@ struct Mesh {
     take(m.boundary_node, m.boundary_count * nbv, out.boundary_node);
     take(m.boundary_physical, m.boundary_count, out.boundary_physical);
     take(m.physical_boundary_condition, int64_t(m.physical_count), out.physical_boundary_condition);
+    if (m.geometry_order > 1) {
+      const int64_t q = m.geometry_order;
+      out.geometry_order = int(q);
+      take(m.triangle_geometry_node, m.triangle_count * (q + 1) * (q + 2) / 2, out.triangle_geometry);
+      take(m.quadrangle_geometry_node, m.quadrangle_count * (q + 1) * (q + 1), out.quadrangle_geometry);
+      take(m.hexahedron_geometry_node, m.hexahedron_count * (q + 1) * (q + 1) * (q + 1), out.hexahedron_geometry);
+    }
     sdg_mesh_free(&g);
     return out;
   }
