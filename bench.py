@@ -9,8 +9,9 @@ dt from CFL 0.2 -- seeded synthetic initial state of that shape (no dataset invo
 
 Prints one JSON line.  value = DOF-stage updates/s with the state resident in HBM (CUDA events on the
 library's stream, the step replayed as a CUDA graph); e2e = the same metric through the C ABI with host
-buffers (pinned), the state uploaded every step (sdg_set_state_point) and the new state returned by
-sdg_step_state_point.  The line also carries the other
+buffers (pinned), every step taking its input state from the host and returning its new state to the host:
+streamed through sdg_step_state_point_from_async (each step's input transfer overlapping the previous step),
+and, under e2e.synchronous, through sdg_set_state_point + sdg_step_state_point.  The line also carries the other
 workloads of the metric, each measured the same way on this GPU:
   batched      256 independent 2D Euler / Navier-Stokes Kelvin-Helmholtz solves (500..50,000 elements,
                P1..P5, quads or hybrid, Mach 0.1..0.8, Re 1e2..1e4): one batched graph step of all
@@ -606,28 +607,50 @@ def run_ours(args):
     fp64_flops = prof["fp64_flops_per_element"] * ne if "fp64_flops_per_element" in prof else None
     fp64_achieved = fp64_flops / (elem_avg_ms * 1e-3) / 1e9 if fp64_flops else None
 
-    # end to end through the C ABI with pinned host buffers: upload state, step, download state
+    # end to end through the C ABI with pinned host buffers: every step uploads its input state and returns its
+    # new state.  Streamed: sdg_step_state_point_from_async, each step's input transfer (copy engine) running
+    # while the previous step computes, the new state written by the last stage; synchronous:
+    # sdg_set_state_point + sdg_step_state_point, each call waiting for its own transfers.
     e2e = None
     if not args.no_e2e:
         npts = c.volume_point_count * s.nv
         host_in = torch.empty(npts, dtype=torch.float64, pin_memory=True)
         host_out = torch.empty(npts, dtype=torch.float64, pin_memory=True)
         out_view = host_out.numpy().reshape(-1, s.nv)
+        in_view = host_in.numpy().reshape(-1, s.nv)
         s.state_point(out_view)
         host_in.copy_(host_out)
         for _ in range(2):
-            s.set_state_point(host_in.numpy())
+            s.set_state_point(in_view)
             s.step_state_point(dt, out_view)
         replicas.barrier(pg)
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            s.set_state_point(host_in.numpy())          # H2D of the step's input state
+            s.set_state_point(in_view)                  # H2D of the step's input state
             s.step_state_point(dt, out_view)            # step, its relative error and its new state (D2H)
-        t_e2e = time.perf_counter() - t0
-        t_e2e = replicas.max_over_ranks(pg, t_e2e, device=f"cuda:{device}")
+        t_sync = replicas.max_over_ranks(pg, time.perf_counter() - t0, device=f"cuda:{device}")
+        for _ in range(2):
+            s.step_state_point_from(dt, in_view, out_view, asynchronous=True)
+        s.synchronize()
+        replicas.barrier(pg)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            s.step_state_point_from(dt, in_view, out_view, asynchronous=True)  # H2D in, step, D2H out
+        s.synchronize()
+        relerr_streamed = s.relative_error()                                  # D2H of the last relative error
+        t_e2e = replicas.max_over_ranks(pg, time.perf_counter() - t0, device=f"cuda:{device}")
         e2e = {"value": world * dof * stages * args.steps / t_e2e, "unit": "DOF-stage/s",
-               "h2d_bytes_per_step": npts * 8, "d2h_bytes_per_step": npts * 8 + s.nv * 8,
-               "ms_per_step": 1e3 * t_e2e / args.steps}
+               "h2d_bytes_per_step": npts * 8, "d2h_bytes_per_step": npts * 8,
+               "ms_per_step": 1e3 * t_e2e / args.steps,
+               "mode": "streamed: sdg_step_state_point_from_async per step (pinned input copied on the copy engine "
+                       "while the previous step computes; the new state written to pinned memory by the last "
+                       "stage), one synchronize at the end",
+               "relative_error_finite": bool(np.all(np.isfinite(relerr_streamed))),
+               "synchronous": {"value": world * dof * stages * args.steps / t_sync, "unit": "DOF-stage/s",
+                               "ms_per_step": 1e3 * t_sync / args.steps,
+                               "mode": "sdg_set_state_point + sdg_step_state_point per step, each waiting for "
+                                       "its transfers",
+                               "h2d_bytes_per_step": npts * 8, "d2h_bytes_per_step": npts * 8 + s.nv * 8}}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -234,6 +234,20 @@ int sdg_step_async(sdg_handle* handle, int32_t step_count, double delta_time);
  * follows the step; dense blocks, and pageable buffers, are converted and copied after the step.  The
  * captured step graph is re-captured when the buffer differs from the previous call's. */
 int sdg_step_state_point(sdg_handle* handle, double delta_time, double* conserved, double* relative_error);
+/* One step from a host state to a host state: conserved_in becomes the state (as sdg_set_state_point), it is
+ * advanced one step (sdg_step) and the new state is written to conserved_out (as sdg_step_state_point), with
+ * the step's relative error when relative_error is not null.  The input crosses to the device on the copy
+ * engine into a staging buffer of its own (volume_point_count x (d+2) doubles, allocated on first use).
+ * The _async form returns once the work is enqueued: the transfer of a call's input then runs while the
+ * previous call's step computes, for a caller streaming independent states through the solver.  Both buffers
+ * must stay valid and unchanged until sdg_synchronize; sdg_relative_error then gives the last call's relative
+ * error.  Pinned buffers (cudaHostAlloc / cudaHostRegister) make both transfers asynchronous; with pageable
+ * ones the copies are staged by the driver and the calls wait for them.  States, point values and relative
+ * errors are those of sdg_set_state_point + sdg_step + sdg_get_state_point, bit for bit. */
+int sdg_step_state_point_from(sdg_handle* handle, double delta_time, const double* conserved_in,
+                              double* conserved_out, double* relative_error);
+int sdg_step_state_point_from_async(sdg_handle* handle, double delta_time, const double* conserved_in,
+                                    double* conserved_out);
 
 /* Solver::relative_error_ of the last step: per conserved variable, the element mean of
  * mean_q |R Phi^T| (TimeIntegration.cpp:279-324).  NaN entries signal a blow-up. */

@@ -150,6 +150,8 @@ SIGNATURES = {
     "sdg_step": (c_int32, [c_void_p, c_int32, c_double]),
     "sdg_step_async": (c_int32, [c_void_p, c_int32, c_double]),
     "sdg_step_state_point": (c_int32, [c_void_p, c_double, _p_double, _p_double]),
+    "sdg_step_state_point_from": (c_int32, [c_void_p, c_double, _p_double, _p_double, _p_double]),
+    "sdg_step_state_point_from_async": (c_int32, [c_void_p, c_double, _p_double, _p_double]),
     "sdg_relative_error": (c_int32, [c_void_p, _p_double]),
     "sdg_residual_point": (c_int32, [c_void_p, _p_double]),
     "sdg_synchronize": (c_int32, [c_void_p]),

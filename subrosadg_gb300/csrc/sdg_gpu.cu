@@ -882,11 +882,13 @@ void downloadPoints(sdg_handle* h, int which, double* conserved, bool skipTensor
                              h->stream));
 }
 
-void pointsToState(sdg_handle* h, int which) {
+// Point-layout device array `src` (default: the scratch buffer) -> state[which].
+void pointsToState(sdg_handle* h, int which, const double* src = nullptr) {
+  if (!src) src = h->scratch;
   for (DevBlock& B : h->blocks) {
     const int64_t work = B.ne * (B.kind == kTensor ? B.nb : B.nb);
     const int grid = int((work + 255) / 256);
-    pointToStateKernel<<<grid, 256, 0, h->stream>>>(h->scratch + B.pointOffset * h->nv, h->state[which] + B.stateOffset,
+    pointToStateKernel<<<grid, 256, 0, h->stream>>>(src + B.pointOffset * h->nv, h->state[which] + B.stateOffset,
                                                     B.kind == kDense ? B.lsqDev : nullptr, B.ne, B.nb, B.nq, h->nv,
                                                     B.ustride);
     checkLaunch(h);
@@ -1515,6 +1517,10 @@ int sdg_destroy(sdg_handle* h) {
   cudaFree(h->bconn); cudaFree(h->bgeo); cudaFree(h->ghost); cudaFree(h->scratch); cudaFree(h->relPart);
   cudaFree(h->relOut); cudaFree(h->dtPart); cudaFree(h->status);
   cudaFree(h->faceOther); cudaFree(h->faceGrad); cudaFree(h->faceFlux); cudaFree(h->grad);
+  if (h->copyStream) { cudaStreamSynchronize(h->copyStream); cudaStreamDestroy(h->copyStream); }
+  if (h->copyDone) cudaEventDestroy(h->copyDone);
+  if (h->stageFree) cudaEventDestroy(h->stageFree);
+  cudaFree(h->inStage);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
   return SDG_OK;
@@ -1750,6 +1756,65 @@ int sdg_step_state_point(sdg_handle* h, double dt, double* conserved, double* re
   h->pointsOut = nullptr;
   h->stateVersion++;
   downloadPoints(h, 0, conserved, true);
+  SDG_CUDA(cudaMemcpyAsync(h->relerr, h->relOut, h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
+  checkStatus(h);
+  if (relative_error)
+    for (int v = 0; v < h->nv; ++v) relative_error[v] = h->relerr[v];
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+namespace {
+
+// One step from a host state to a host state.  The input crosses the CPU-GPU link on the copy engine into the
+// staging buffer, on a stream of its own, once the previous call's conversion has consumed that buffer: the
+// transfer of a call runs while the previous call's step computes.  The conversion, the traces and the step run
+// on the handle's stream; the last stage of tensor blocks writes the new state into a pinned output buffer.
+void stepFromTo(sdg_handle* h, double dt, const double* in, double* out) {
+  if (!h->inStage) {
+    h->inStage = devAlloc<double>(size_t(h->volumePoints) * h->nv);
+    SDG_CUDA(cudaStreamCreateWithFlags(&h->copyStream, cudaStreamNonBlocking));
+    SDG_CUDA(cudaEventCreateWithFlags(&h->copyDone, cudaEventDisableTiming));
+    SDG_CUDA(cudaEventCreateWithFlags(&h->stageFree, cudaEventDisableTiming));
+    SDG_CUDA(cudaEventRecord(h->stageFree, h->stream));
+  }
+  SDG_CUDA(cudaStreamWaitEvent(h->copyStream, h->stageFree, 0));
+  SDG_CUDA(cudaMemcpyAsync(h->inStage, in, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyHostToDevice,
+                           h->copyStream));
+  SDG_CUDA(cudaEventRecord(h->copyDone, h->copyStream));
+  SDG_CUDA(cudaStreamWaitEvent(h->stream, h->copyDone, 0));
+  pointsToState(h, 0, h->inStage);
+  SDG_CUDA(cudaEventRecord(h->stageFree, h->stream));
+  traceAll(h, 0);
+  h->hasState = true;
+  h->pointsOut = const_cast<double*>(mappedHost(out));
+  try {
+    stepOnce(h, dt);
+  } catch (...) {
+    h->pointsOut = nullptr;
+    throw;
+  }
+  h->pointsOut = nullptr;
+  h->stateVersion++;
+  downloadPoints(h, 0, out, true);
+}
+
+}  // namespace
+
+int sdg_step_state_point_from_async(sdg_handle* h, double dt, const double* in, double* out) {
+  if (!h || !in || !out || !std::isfinite(dt)) return SDG_ERR_INVALID_ARGUMENT;
+  if (h->hostOnly) { h->err = "host-only handle (created with device < 0)"; return SDG_ERR_STATE; }
+  SDG_API_BEGIN
+  SDG_CUDA(cudaSetDevice(h->device));
+  stepFromTo(h, dt, in, out);
+  return SDG_OK;
+  SDG_API_END(h)
+}
+
+int sdg_step_state_point_from(sdg_handle* h, double dt, const double* in, double* out, double* relative_error) {
+  const int rc = sdg_step_state_point_from_async(h, dt, in, out);
+  if (rc != SDG_OK) return rc;
+  SDG_API_BEGIN
   SDG_CUDA(cudaMemcpyAsync(h->relerr, h->relOut, h->nv * 8, cudaMemcpyDeviceToHost, h->stream));
   checkStatus(h);
   if (relative_error)

@@ -139,6 +139,11 @@ struct sdg_handle {
   std::vector<int64_t> boundaryOrder;   // sdg_set_boundary_face_order: library boundary face of each caller position
   int64_t nodeCount = 0;                // mesh nodes (raw-binary files carry one value per node)
   double* scratch = nullptr;       // point-layout conversion buffer [volume_points][nv]
+  // sdg_step_state_point_from: staging buffer of the input state [volume_points][nv], the stream its transfers
+  // run on, and the events that order a transfer after the previous conversion and before its own (on first use)
+  double* inStage = nullptr;
+  cudaStream_t copyStream = nullptr;
+  cudaEvent_t copyDone = nullptr, stageFree = nullptr;
   int64_t volumePoints = 0;
   double* relPart = nullptr; int64_t relParts = 0;
   double* relOut = nullptr; double* dtPart = nullptr; int64_t dtParts = 0;

@@ -313,6 +313,20 @@ class GpuSolver:
         self._chk(self.lib.sdg_step_state_point(self.h, dt, _ptr(out), _ptr(self.relative_error_)))
         return out, self.relative_error_
 
+    def step_state_point_from(self, dt, conserved_in, out=None, asynchronous=False):
+        """One step from a host state to a host state (sdg_step_state_point_from[_async]).  Synchronous: returns
+        (state, relative error).  Asynchronous: enqueues and returns `out`; both buffers stay in use until
+        synchronize(), and relative_error() then gives the last call's relative error."""
+        p = conserved_in if conserved_in.flags.c_contiguous and conserved_in.dtype == np.float64 else \
+            np.ascontiguousarray(conserved_in, np.float64)
+        if out is None:
+            out = np.zeros((self.counts.volume_point_count, self.nv))
+        if asynchronous:
+            self._chk(self.lib.sdg_step_state_point_from_async(self.h, dt, _ptr(p), _ptr(out)))
+            return out
+        self._chk(self.lib.sdg_step_state_point_from(self.h, dt, _ptr(p), _ptr(out), _ptr(self.relative_error_)))
+        return out, self.relative_error_
+
     def step_async(self, dt, steps=1):
         self._chk(self.lib.sdg_step_async(self.h, steps, dt))
 

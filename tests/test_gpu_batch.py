@@ -39,6 +39,9 @@ MIXED = {
     "ns-channel-walls-p2": lambda: cases.channel_case(p=2, flux=sdg.HLLC, n=4, viscous=sdg.BR2, mu=0.01,
                                                       conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW,
                                                                   sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
+    "euler-warped-hex-p3-hllc": lambda: cases.warped(cases.tgv_case(n=3, p=3)),
+    "ns-curved-hex-p2-q2-br2": lambda: cases.curved_hex(cases.tgv_case(n=3, p=2, flux=sdg.LAX_FRIEDRICHS,
+                                                                        viscous=sdg.BR2, mu=0.02), 2),
     "euler-line-p3-hllc": lambda: cases.density_wave_1d_case(n=20, p=3),
     "euler-tet-p2-roe": lambda: cases.tet_tgv_case(n=3, p=2, flux=sdg.ROE),
     "euler-tet-box-p3-hllc": lambda: cases.tet_box_case(p=3, flux=sdg.HLLC),

@@ -80,3 +80,50 @@ def test_step_state_point_matches_step_then_download(name, case):
     b.stepSolver(dt)                                     # back to the plain step graph
     a.stepSolver(dt)
     np.testing.assert_array_equal(b.state_modal(), a.state_modal())
+
+
+@pytest.mark.parametrize("name,case", [
+    ("hex-p3", lambda: cases.tgv_case(n=4, p=3)),
+    ("hybrid-p4", lambda: cases.kh_case(n=6, p=4)),
+    ("tet-p2", lambda: cases.tet_tgv_case(n=3, p=2)),
+    ("ns-hex-p2", lambda: cases.tgv_case(n=3, p=2, viscous=sdg.BR1)),
+])
+def test_step_state_point_from_matches_set_step_get(name, case):
+    """sdg_step_state_point_from[_async]: host state in, one step, host state out.  Every call equals
+    sdg_set_state_point + sdg_step + sdg_get_state_point bit for bit, for pinned and pageable buffers, and a chain
+    of asynchronous calls (each call's input transfer overlapping the previous call's step) gives each call's
+    own result in its own output buffer."""
+    mesh, cfg, prim, _, dt, _ = case()
+    a = sdg.GpuSolver(mesh, cfg)
+    b = sdg.GpuSolver(mesh, cfg)
+    a.initialize_primitive(prim(a.volume_points()))
+    nv = a.counts.conserved_variable_count
+    u0 = a.state_point()
+    rng = np.random.default_rng(5)
+    inputs = [u0 * (1.0 + 1e-3 * rng.standard_normal(u0.shape)) for _ in range(3)]
+    expected, errs = [], []
+    for u in inputs:
+        a.set_state_point(u)
+        errs.append(a.stepSolver(dt).copy())
+        expected.append(a.state_point())
+    # synchronous, pageable and pinned
+    out, err = b.step_state_point_from(dt, inputs[0])
+    np.testing.assert_array_equal(out, expected[0])
+    np.testing.assert_array_equal(err, errs[0])
+    pin_in = [_pinned(u.size).reshape(u.shape) for u in inputs]
+    pin_out = [_pinned(u.size).reshape(-1, nv) for u in inputs]
+    for pi, u in zip(pin_in, inputs):
+        pi[...] = u
+    out, err = b.step_state_point_from(dt, pin_in[1], pin_out[1])
+    np.testing.assert_array_equal(pin_out[1], expected[1])
+    np.testing.assert_array_equal(err, errs[1])
+    # asynchronous chain
+    for po in pin_out:
+        po[...] = np.nan
+    for pi, po in zip(pin_in, pin_out):
+        b.step_state_point_from(dt, pi, po, asynchronous=True)
+    b.synchronize()
+    for po, e in zip(pin_out, expected):
+        np.testing.assert_array_equal(po, e)
+    np.testing.assert_array_equal(b.relative_error(), errs[-1])
+    np.testing.assert_array_equal(b.state_modal(), a.state_modal())
