@@ -608,7 +608,7 @@ def run_ours(args):
     fp64_achieved = fp64_flops / (elem_avg_ms * 1e-3) / 1e9 if fp64_flops else None
 
     # end to end through the C ABI with pinned host buffers: every step uploads its input state and returns its
-    # new state.  Streamed: sdg_step_state_point_from_async, each step's input transfer (copy engine) running
+    # new state.  Streamed: sdg_step_state_point_from_async, each step's input transfer (a copy kernel) running
     # while the previous step computes, the new state written by the last stage; synchronous:
     # sdg_set_state_point + sdg_step_state_point, each call waiting for its own transfers.
     e2e = None
@@ -642,7 +642,7 @@ def run_ours(args):
         e2e = {"value": world * dof * stages * args.steps / t_e2e, "unit": "DOF-stage/s",
                "h2d_bytes_per_step": npts * 8, "d2h_bytes_per_step": npts * 8,
                "ms_per_step": 1e3 * t_e2e / args.steps,
-               "mode": "streamed: sdg_step_state_point_from_async per step (pinned input copied on the copy engine "
+               "mode": "streamed: sdg_step_state_point_from_async per step (pinned input read by a copy kernel "
                        "while the previous step computes; the new state written to pinned memory by the last "
                        "stage), one synchronize at the end",
                "relative_error_finite": bool(np.all(np.isfinite(relerr_streamed))),

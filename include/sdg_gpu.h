@@ -236,8 +236,9 @@ int sdg_step_async(sdg_handle* handle, int32_t step_count, double delta_time);
 int sdg_step_state_point(sdg_handle* handle, double delta_time, double* conserved, double* relative_error);
 /* One step from a host state to a host state: conserved_in becomes the state (as sdg_set_state_point), it is
  * advanced one step (sdg_step) and the new state is written to conserved_out (as sdg_step_state_point), with
- * the step's relative error when relative_error is not null.  The input crosses to the device on the copy
- * engine into a staging buffer of its own (volume_point_count x (d+2) doubles, allocated on first use).
+ * the step's relative error when relative_error is not null.  The input crosses to the device into a staging
+ * buffer of its own (volume_point_count x (d+2) doubles, allocated on first use) on a stream of its own: read
+ * in place by a narrow copy kernel when pinned, by the copy engine when pageable.
  * The _async form returns once the work is enqueued: the transfer of a call's input then runs while the
  * previous call's step computes, for a caller streaming independent states through the solver.  Both buffers
  * must stay valid and unchanged until sdg_synchronize; sdg_relative_error then gives the last call's relative

@@ -207,6 +207,24 @@ __global__ void pointsToTensorStateKernel(const double* __restrict__ pts, double
   }
 }
 
+// Copy n doubles from host memory the device maps (pinned) to device memory: a grid-stride loop, eight loads
+// in flight per thread, so that a small grid (one narrow CTA per SM) keeps the CPU-GPU link busy beside other
+// kernels while taking few of their registers and warp slots.
+__global__ void __launch_bounds__(128) hostCopyKernel(const double* __restrict__ src, double* __restrict__ dst,
+                                                      int64_t n) {
+  constexpr int kInFlight = 8;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (; i + (kInFlight - 1) * stride < n; i += kInFlight * stride) {
+    double v[kInFlight];
+#pragma unroll
+    for (int k = 0; k < kInFlight; ++k) v[k] = src[i + k * stride];
+#pragma unroll
+    for (int k = 0; k < kInFlight; ++k) dst[i + k * stride] = v[k];
+  }
+  for (; i < n; i += stride) dst[i] = src[i];
+}
+
 __global__ void stateToPointsTiledKernel(const double* __restrict__ st, double* __restrict__ pts,
                                          const double* __restrict__ phi, int64_t ne, int nb, int nq, int nv,
                                          int ustride, int epc) {
@@ -1766,21 +1784,31 @@ int sdg_step_state_point(sdg_handle* h, double dt, double* conserved, double* re
 
 namespace {
 
-// One step from a host state to a host state.  The input crosses the CPU-GPU link on the copy engine into the
-// staging buffer, on a stream of its own, once the previous call's conversion has consumed that buffer: the
-// transfer of a call runs while the previous call's step computes.  The conversion, the traces and the step run
-// on the handle's stream; the last stage of tensor blocks writes the new state into a pinned output buffer.
+// One step from a host state to a host state.  The input crosses the CPU-GPU link into the staging buffer on
+// a stream of its own (high priority), once the previous call's conversion has consumed that buffer: the
+// transfer of a call runs while the previous call's step computes.  A pinned input is read by a copy kernel
+// (zero-copy), a pageable one by the copy engine.  The conversion, the traces and the step run on the handle's
+// stream; the last stage of tensor blocks writes the new state into a pinned output buffer.
 void stepFromTo(sdg_handle* h, double dt, const double* in, double* out) {
+  const int64_t n = h->volumePoints * h->nv;
   if (!h->inStage) {
-    h->inStage = devAlloc<double>(size_t(h->volumePoints) * h->nv);
-    SDG_CUDA(cudaStreamCreateWithFlags(&h->copyStream, cudaStreamNonBlocking));
+    h->inStage = devAlloc<double>(size_t(n));
+    int lo = 0, hi = 0;
+    SDG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    SDG_CUDA(cudaStreamCreateWithPriority(&h->copyStream, cudaStreamNonBlocking, hi));
     SDG_CUDA(cudaEventCreateWithFlags(&h->copyDone, cudaEventDisableTiming));
     SDG_CUDA(cudaEventCreateWithFlags(&h->stageFree, cudaEventDisableTiming));
     SDG_CUDA(cudaEventRecord(h->stageFree, h->stream));
   }
   SDG_CUDA(cudaStreamWaitEvent(h->copyStream, h->stageFree, 0));
-  SDG_CUDA(cudaMemcpyAsync(h->inStage, in, size_t(h->volumePoints) * h->nv * 8, cudaMemcpyHostToDevice,
-                           h->copyStream));
+  if (const double* mapped = mappedHost(in)) {
+    const int sms = multiprocessorCount(h->device);
+    hostCopyKernel<<<unsigned(sms), 128, 0, h->copyStream>>>(mapped, h->inStage, n);
+    SDG_CUDA(cudaGetLastError());
+    h->launches++;
+  } else {
+    SDG_CUDA(cudaMemcpyAsync(h->inStage, in, size_t(n) * 8, cudaMemcpyHostToDevice, h->copyStream));
+  }
   SDG_CUDA(cudaEventRecord(h->copyDone, h->copyStream));
   SDG_CUDA(cudaStreamWaitEvent(h->stream, h->copyDone, 0));
   pointsToState(h, 0, h->inStage);
