@@ -225,6 +225,30 @@ __global__ void __launch_bounds__(128) hostCopyKernel(const double* __restrict__
   for (; i < n; i += stride) dst[i] = src[i];
 }
 
+// The same copy into a tensor block's state layout: point-layout element e's value (q, v) (the nodes are the
+// points) goes to dst[e * ustride + v * nb + q].  The writes of a warp fall within a few elements' contiguous
+// state, which L2 merges before HBM.
+__global__ void __launch_bounds__(128) hostCopyTensorKernel(const double* __restrict__ src, double* __restrict__ dst,
+                                                            int64_t ne, int nb, int nv, int ustride) {
+  constexpr int kInFlight = 8;
+  const int64_t n = ne * nb * nv, stride = int64_t(gridDim.x) * blockDim.x;
+  const int per = nb * nv;
+  const auto target = [&](int64_t i) {
+    const int64_t e = i / per;
+    const int r = int(i - e * per), q = r / nv, v = r - q * nv;
+    return e * ustride + v * nb + q;
+  };
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (; i + (kInFlight - 1) * stride < n; i += kInFlight * stride) {
+    double x[kInFlight];
+#pragma unroll
+    for (int k = 0; k < kInFlight; ++k) x[k] = src[i + k * stride];
+#pragma unroll
+    for (int k = 0; k < kInFlight; ++k) dst[target(i + k * stride)] = x[k];
+  }
+  for (; i < n; i += stride) dst[target(i)] = src[i];
+}
+
 __global__ void stateToPointsTiledKernel(const double* __restrict__ st, double* __restrict__ pts,
                                          const double* __restrict__ phi, int64_t ne, int nb, int nq, int nv,
                                          int ustride, int epc) {
@@ -1791,8 +1815,12 @@ namespace {
 // stream; the last stage of tensor blocks writes the new state into a pinned output buffer.
 void stepFromTo(sdg_handle* h, double dt, const double* in, double* out) {
   const int64_t n = h->volumePoints * h->nv;
+  bool allTensor = true;
+  for (const DevBlock& B : h->blocks) allTensor = allTensor && B.kind == kTensor;
   if (!h->inStage) {
-    h->inStage = devAlloc<double>(size_t(n));
+    const size_t stage = std::max<size_t>(size_t(n), h->stateCount);
+    h->inStage = devAlloc<double>(stage);
+    SDG_CUDA(cudaMemsetAsync(h->inStage, 0, stage * 8, h->stream));  // the state layout's padding stays zero
     int lo = 0, hi = 0;
     SDG_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
     SDG_CUDA(cudaStreamCreateWithPriority(&h->copyStream, cudaStreamNonBlocking, hi));
@@ -1801,8 +1829,16 @@ void stepFromTo(sdg_handle* h, double dt, const double* in, double* out) {
     SDG_CUDA(cudaEventRecord(h->stageFree, h->stream));
   }
   SDG_CUDA(cudaStreamWaitEvent(h->copyStream, h->stageFree, 0));
-  if (const double* mapped = mappedHost(in)) {
-    const int sms = multiprocessorCount(h->device);
+  const double* mapped = mappedHost(in);
+  const int sms = multiprocessorCount(h->device);
+  if (mapped && allTensor) {  // straight into the state layout: the conversion rides on the transfer
+    for (const DevBlock& B : h->blocks) {
+      hostCopyTensorKernel<<<unsigned(sms), 128, 0, h->copyStream>>>(
+          mapped + B.pointOffset * h->nv, h->inStage + B.stateOffset, B.ne, B.nb, h->nv, B.ustride);
+      SDG_CUDA(cudaGetLastError());
+      h->launches++;
+    }
+  } else if (mapped) {
     hostCopyKernel<<<unsigned(sms), 128, 0, h->copyStream>>>(mapped, h->inStage, n);
     SDG_CUDA(cudaGetLastError());
     h->launches++;
@@ -1811,7 +1847,10 @@ void stepFromTo(sdg_handle* h, double dt, const double* in, double* out) {
   }
   SDG_CUDA(cudaEventRecord(h->copyDone, h->copyStream));
   SDG_CUDA(cudaStreamWaitEvent(h->stream, h->copyDone, 0));
-  pointsToState(h, 0, h->inStage);
+  if (mapped && allTensor)
+    SDG_CUDA(cudaMemcpyAsync(h->state[0], h->inStage, h->stateCount * 8, cudaMemcpyDeviceToDevice, h->stream));
+  else
+    pointsToState(h, 0, h->inStage);
   SDG_CUDA(cudaEventRecord(h->stageFree, h->stream));
   traceAll(h, 0);
   h->hasState = true;
