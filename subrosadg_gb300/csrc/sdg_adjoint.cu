@@ -120,9 +120,9 @@ AdjointState* adjoint(sdg_handle* h) {
   if (!h->hasState) throw Failure(SDG_ERR_STATE, "no state");
   if (h->adj) return h->adj;
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
-  if (h->curved) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives on curved (high-order) geometry are not built");
-  if (h->facePoint)
-    throw Failure(SDG_ERR_UNSUPPORTED, "derivatives on hexahedra that are not parallelepipeds are not built");
+  for (const DevBlock& B : h->blocks)
+    if (B.curved && B.kind == kDense)
+      throw Failure(SDG_ERR_UNSUPPORTED, "derivatives on curved triangles are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   const bool gen = h->ph.incomp || h->ph.source;
   adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, gen, A->k);
@@ -186,12 +186,13 @@ AdjArgs baseArgs(sdg_handle* h, const DevBlock* B, const double* U) {
   const double* grad = A->curGrad ? A->curGrad : h->grad;
   if (B) {
     a.u = U + B->stateOffset; a.geom = B->geom; a.tables = B->tables; a.fmetric = B->fmetric;
+    a.fmetricPoint = B->facePoint;
     a.grad = h->ns ? grad + B->gradOffset : nullptr;
     a.ne = B->ne; a.faceBase = B->faceBase;
   }
   a.face = A->curFace ? A->curFace : h->face;
   a.faceGrad = A->curFaceGrad ? A->curFaceGrad : h->faceGrad;
-  a.conn = h->fconn; a.fgeo = h->fgeo; a.status = h->status;
+  a.conn = h->fconn; a.fgeo = h->fgeo; a.fgeoPoint = h->facePoint ? 1 : 0; a.status = h->status;
   a.nface = h->nInterior; a.n1d = h->n1d; a.perm = h->facePerm; a.epb = B ? tileKernels(h, *B).epb : 0;
   return a;
 }

@@ -660,7 +660,9 @@ struct AdjArgs {
   const double* ghost;
   double* lamGhost;
   double ghostScale;
-  const double* fmetric;  // dense blocks: outward n|J_f| of each local face [e][NF][d]
+  const double* fmetric;  // outward n|J_f| of each local face [e][NF][d], or of each face point [e][NF][nfq][d]
+  int fgeoPoint;          // 1: fgeo per face point [face][j][n, |J_f|] (curved meshes, non-parallelepiped hexahedra)
+  int fmetricPoint;       // 1: fmetric per face point
 };
 
 // ---- surface force (the reference's View force, VariableConvertor.cpp:883-906, Paraview.cpp:99-106) ------
@@ -765,8 +767,8 @@ __global__ void __launch_bounds__(kFaceThreads) surfaceForceTraceCotangentKernel
   const int64_t L = int64_t(a.conn[f * 3]) * NV * nfq + j, LG = int64_t(a.conn[f * 3]) * NG * nfq + j;
   double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double scale = a.select[f] ? a.fw[j] * a.fgeo[f * 4 + 3] : 0.0;
+  for (int k = 0; k < DIM; ++k) n[k] = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[k];
+  const double scale = a.select[f] ? a.fw[j] * faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[3] : 0.0;
   double ul[NV], gg[NG];
 #pragma unroll
   for (int v = 0; v < NV; ++v) ul[v] = a.face[L + v * nfq];
@@ -907,7 +909,7 @@ __global__ void __launch_bounds__(kFaceThreads) jvpExchangeBoundaryKernel(AdjArg
   const int64_t L = int64_t(sl) * NV * nfq + j;
   double n[DIM], gp[NV];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  for (int k = 0; k < DIM; ++k) n[k] = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[k];
   ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
   D1 ul[NV], gd[NV], o[NV];
 #pragma unroll
@@ -935,7 +937,7 @@ __global__ void __launch_bounds__(kFaceThreads) vjpExchangeBoundaryKernel(AdjArg
   const int64_t L = int64_t(sl) * NV * nfq + j;
   double n[DIM], gp[NV], lo[NV], ul[NV];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
+  for (int k = 0; k < DIM; ++k) n[k] = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[k];
   ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
 #pragma unroll
   for (int v = 0; v < NV; ++v) { lo[v] = a.lamUp[L + v * nfq]; ul[v] = a.face[L + v * nfq]; }
@@ -975,8 +977,8 @@ __global__ void __launch_bounds__(kFaceThreads) jvpBoundaryNSKernel(AdjArgs a, P
   const int64_t L = int64_t(sl) * NV * nfq + j, LG = int64_t(sl) * NV * DIM * nfq + j;
   double n[DIM], gp[NV];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[k];
+  const double area = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[3];
   ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
   D1 ul[NV], gd[NV], gr[NV * DIM], h[NV], hv[NV];
 #pragma unroll
@@ -1011,8 +1013,8 @@ __global__ void __launch_bounds__(kFaceThreads) vjpBoundaryNSKernel(AdjArgs a, P
     const int64_t L = int64_t(sl) * NV * nfq + j, LG = int64_t(sl) * NV * DIM * nfq + j;
     double n[DIM], gp[NV], lh[NV], ul[NV], gg[NG];
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-    const double area = a.fgeo[f * 4 + 3];
+    for (int k = 0; k < DIM; ++k) n[k] = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[k];
+    const double area = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[3];
     ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
 #pragma unroll
     for (int v = 0; v < NV; ++v) { lh[v] = a.lamH[L + v * nfq] * area; ul[v] = a.face[L + v * nfq]; }
@@ -1076,8 +1078,8 @@ __global__ void __launch_bounds__(kFaceThreads) jvpBoundaryKernel(AdjArgs a, Phy
   const int64_t L = int64_t(sl) * NV * nfq + j;
   double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[k];
+  const double area = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[3];
   double gp[NV];
   ghostPrimitiveOf<DIM>(a.ghost, t, ph, gp);
   D1 ul[NV], gd[NV], h[NV];
@@ -1105,8 +1107,8 @@ __global__ void __launch_bounds__(kFaceThreads) vjpBoundaryKernel(AdjArgs a, Phy
   const int64_t L = int64_t(sl) * NV * nfq + j;
   double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[k];
+  const double area = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[3];
   double lh[NV], ul[NV], gp[NV];
 #pragma unroll
   for (int v = 0; v < NV; ++v) { lh[v] = a.lamH[L + v * nfq] * area; ul[v] = a.face[L + v * nfq]; }
@@ -1163,8 +1165,8 @@ __device__ __forceinline__ void jvpFacePoint(const AdjArgs& a, const Phys& ph, i
   }
   double n[DIM];
 #pragma unroll
-  for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-  const double area = a.fgeo[f * 4 + 3];
+  for (int k = 0; k < DIM; ++k) n[k] = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[k];
+  const double area = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[3];
   D1 h[NV], hv[NV];
   faceFluxPoint<DIM, FLUX, VISC>(ul, ur, gl, gr, n, ph, h, hv);
   const double mscale = VISC && ph.mu > 0.0 ? a.dmu / ph.mu : 0.0;
@@ -1472,8 +1474,8 @@ __global__ void __launch_bounds__(kFaceThreads) vjpFaceKernel(AdjArgs a, Phys ph
     const int64_t L = int64_t(sl) * NV * nfq + j, R = int64_t(sr) * NV * nfq + jr;
     double n[DIM];
 #pragma unroll
-    for (int k = 0; k < DIM; ++k) n[k] = a.fgeo[f * 4 + k];
-    const double area = a.fgeo[f * 4 + 3];
+    for (int k = 0; k < DIM; ++k) n[k] = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[k];
+    const double area = faceGeometry(a.fgeo, a.fgeoPoint, f, j, nfq)[3];
     double lh[NV], ul[NV], ur[NV], laml[NV], lamr[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
@@ -1738,8 +1740,9 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpGradientBR2Ke
   }
 }
 
-// V3 for bilinear quadrangles (per-node metric ja_q and 1/|J|_q, per-face n|J_f| from the face metric;
-// tensorGradientTile's non-affine form).  Forward, at node m along each axis b:
+// V3 for non-affine tensor blocks -- bilinear and curved quadrangles, trilinear and curved hexahedra -- (per-node
+// metric ja_q and 1/|J|_q, n|J_f| from the face metric per face or per face point; tensorGradientTile's
+// non-affine form).  Forward, at node m along each axis b:
 //   tot_k(m) = sum_b [ lift(+) nF(b,+)_k U+(b,+) + lift(-) nF(b,-)_k U+(b,-) - sum_q Dhat[q][m] U_q ja_q[b][k] ]
 //   grad = tot / |J|_m (BR1 gradient traces: its traces); BR2: vol from {U} in place of U+, gradient trace at
 //   (f, j) = trace(vol / |J|) + cl nF_f . (U+ - U-)/2 with cl = sum_q end_q lift_q / |J|_q.
@@ -1821,7 +1824,7 @@ __global__ void __launch_bounds__(TensorShape<DIM, N>::THREADS) vjpGradientBilin
     const int base = T->faceBase[f][j];
     const int st = strideOf<DIM, N>(axis);
     const int64_t ee = e0 + te;
-    const double* nF = a.fmetric + (ee * NF + f) * DIM;
+    const double* nF = a.fmetric + (a.fmetricPoint ? (ee * NF + f) * NFQ + j : ee * NF + f) * DIM;
     double cl = 0.0;
     if constexpr (BR2) {
 #pragma unroll

@@ -66,6 +66,8 @@ struct AdjointTileKernels {
 void adjointFaceKernels(int dim, int flux, bool visc, bool gen, AdjointKernels& k);
 void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, bool affine, AdjointTileKernels& k);
 void adjointDenseKernels(int type, int p, bool affine, bool gen, bool visc, bool br2, AdjointTileKernels& k);
+// Hexahedra that are not parallelepipeds (sdg_variants_adjoint_hex.cu), reached through adjointTileKernels.
+void adjointHexNonAffineKernels(int n, bool visc, bool br2, bool gen, AdjointTileKernels& k);
 
 // Largest tile size the kernels are compiled for (their __launch_bounds__).
 constexpr int kMaxThreads = 512;

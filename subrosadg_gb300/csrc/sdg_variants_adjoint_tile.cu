@@ -41,6 +41,7 @@ void bilinearOf(AdjointTileKernels& k, bool visc, bool br2, bool gen) {
 
 void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, bool affine, AdjointTileKernels& k) {
   if (!affine) {
+    if (dim == 3) { adjointHexNonAffineKernels(n, visc, br2, gen, k); return; }
     if (dim != 2) return;
     switch (n) {
       case 3: bilinearOf<3>(k, visc, br2, gen); break;

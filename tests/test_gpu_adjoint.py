@@ -127,6 +127,23 @@ CASES = {
     "ns-channel-walls-jitter-p3-br1-roe": lambda: cases.channel_case(
         p=3, flux=sdg.ROE, n=3, jitter=0.1, viscous=sdg.BR1, mu=0.01,
         conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.PRESSURE_OUTFLOW, sdg.ADIABATIC_NONSLIP_WALL, sdg.VELOCITY_INFLOW)),
+    # per-face-point geometry: hexahedra that are not parallelepipeds (trilinear, and curved of geometry order 2),
+    # curved quadrangles
+    "euler-warped-hex-p2-hllc": lambda: cases.warped(cases.tgv_case(n=3, p=2, flux=sdg.HLLC)),
+    "ns-warped-hex-p2-br1-roe": lambda: cases.warped(cases.tgv_case(n=3, p=2, flux=sdg.ROE, viscous=sdg.BR1,
+                                                                    mu=0.02)),
+    "ns-warped-hex-box-p2-br1-hllc": lambda: cases.warped(_box3d(p=2, flux=sdg.HLLC, viscous=True)),
+    "ns-curved-hex-p2-q2-br2-lf": lambda: cases.curved_hex(cases.tgv_case(n=3, p=2, flux=sdg.LAX_FRIEDRICHS,
+                                                                          viscous=sdg.BR2, mu=0.02), 2),
+    "euler-curved-annulus-quad-p3-roe": lambda: cases.annulus_case(p=3, flux=sdg.ROE),
+    # (walls on both circles: the outer farfield's branch switch where u.n crosses 0 on the circle would be
+    # straddled by the difference quotient)
+    "ns-curved-annulus-quad-p2-br1-hllc": lambda: cases.annulus_case(
+        p=2, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01,
+        conditions=(sdg.ADIABATIC_NONSLIP_WALL, sdg.ADIABATIC_SLIP_WALL)),
+    "ns-curved-annulus-quad-p3-br2-roe": lambda: cases.annulus_case(
+        p=3, flux=sdg.ROE, viscous=sdg.BR2, mu=0.01,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_SLIP_WALL)),
 }
 
 

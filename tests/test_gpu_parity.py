@@ -427,19 +427,8 @@ def test_warped_hexahedra_wall_force_of_a_uniform_state_vanishes(q):
     assert np.abs(f).max() < 1e-12, f
 
 
-@pytest.mark.parametrize("q", [1, 2])
-def test_warped_hexahedra_refuse_derivatives(q):
-    case = cases.tgv_case(n=3, p=2)
-    mesh, cfg, prim, _, _, _ = cases.warped(case) if q == 1 else cases.curved_hex(case, q)
-    g = sdg.GpuSolver(mesh, cfg)
-    g.initialize_primitive(prim(g.volume_points()))
-    with pytest.raises(sdg.SdgError) as err:
-        g.vjp_residual(np.zeros((g.counts.volume_point_count, 5)))
-    assert err.value.code == 5  # SDG_ERR_UNSUPPORTED
-
-
-def test_curved_meshes_refuse_derivatives():
-    mesh, cfg, prim, _, _, _ = cases.annulus_case(p=2)
+def test_curved_triangles_refuse_derivatives():
+    mesh, cfg, prim, _, _, _ = cases.annulus_case(p=2, split=1.0)
     g = sdg.GpuSolver(mesh, cfg)
     g.initialize_primitive(prim(g.volume_points()))
     with pytest.raises(sdg.SdgError) as err:
