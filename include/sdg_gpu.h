@@ -472,9 +472,10 @@ const char* sdg_batch_last_error(const sdg_batch* batch);
  * viscosity mu.  All vectors are in the volume-point layout of sdg_set_state_point ([point][d+2],
  * conserved variables; cotangents are mapped by the transposes of its point <-> state conversions, so the VJP
  * is the transpose of the JVP in that layout).  Supported: compressible or incompressible Euler and
- * Navier-Stokes (BR1, BR2) on every element block (lines, triangles, quadrangles -- parallelogram, bilinear
- * or curved --, tetrahedra (P1-P3), hexahedra -- parallelepiped, trilinear or curved --, hybrid meshes), the
- * Boussinesq source, any boundary faces; with artificial viscosity or curved triangles SDG_ERR_UNSUPPORTED. */
+ * Navier-Stokes (BR1, BR2) on every element block (lines, triangles -- straight or curved --, quadrangles --
+ * parallelogram, bilinear or curved --, tetrahedra (P1-P3), hexahedra -- parallelepiped, trilinear or curved
+ * --, hybrid meshes), the Boussinesq source, any boundary faces; with artificial viscosity
+ * SDG_ERR_UNSUPPORTED. */
 /* w_q |J|_q of every volume point: integral of f = sum over points of weight * f (functionals). */
 int sdg_volume_point_weight(sdg_handle* handle, double* weight);
 /* Change the dynamic viscosity (and kappa = cp mu / Pr) of a Navier-Stokes handle. */

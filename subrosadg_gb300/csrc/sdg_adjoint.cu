@@ -120,9 +120,6 @@ AdjointState* adjoint(sdg_handle* h) {
   if (!h->hasState) throw Failure(SDG_ERR_STATE, "no state");
   if (h->adj) return h->adj;
   if (h->av) throw Failure(SDG_ERR_UNSUPPORTED, "derivatives of the artificial viscosity are not built");
-  for (const DevBlock& B : h->blocks)
-    if (B.curved && B.kind == kDense)
-      throw Failure(SDG_ERR_UNSUPPORTED, "derivatives on curved triangles are not built");
   std::unique_ptr<AdjointState> A(new AdjointState());
   const bool gen = h->ph.incomp || h->ph.source;
   adjointFaceKernels(h->dim, h->cfg.convective_flux, h->ns, gen, A->k);

@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(256) vjpDenseGradientKernel(AdjArgs a) {
     const int f = fj / NFQ, j = fj - f * NFQ;
     const int64_t e = e0 + le;
     const double jinv = a.geom[e * GD + DIM * DIM];
-    const double* nf = a.fmetric + (e * NF + f) * DIM;
+    const double* nf = a.fmetric + (a.fmetricPoint ? (e * NF + f) * NFQ + j : e * NF + f) * DIM;
     // n . x for components x_k at stride `st`
     const auto ndot = [&](const double* x, int st) {
       double r = nf[DIM - 1] * x[(DIM - 1) * st];
@@ -539,7 +539,8 @@ __global__ void __launch_bounds__(256) vjpDenseGradientGeneralKernel(AdjArgs a) 
     const int fj = r / NV, v = r - fj * NV;
     const int f = fj / NFQ, j = fj - f * NFQ;
     const int64_t e = e0 + le;
-    const double n0 = a.fmetric[(e * NF + f) * 2 + 0], n1 = a.fmetric[(e * NF + f) * 2 + 1];
+    const double* nfp = a.fmetric + (a.fmetricPoint ? (e * NF + f) * NFQ + j : e * NF + f) * 2;
+    const double n0 = nfp[0], n1 = nfp[1];
     double lt = 0.0, lv = 0.0, lf = 0.0;
 #pragma unroll
     for (int i = 0; i < NB; ++i) {

@@ -938,7 +938,7 @@ __global__ void __launch_bounds__(kMaxTileThreads)
 
 // (type, P) -> (NB, NQ, NFQ): triangle P1..P5 use Dunavant rules of 3,6,12,16,25 points.
 
-// The element blocks with derivative kernels (the curved, non-affine triangles have none).
+// The element blocks with derivative kernels (every dense block of 2D, curved triangles included).
 #define SDG_DENSE_ADJOINT_CASES(X)                          \
   X(SDG_ELEMENT_TRIANGLE, 1, 3, 3, 2, 3, true)              \
   X(SDG_ELEMENT_TRIANGLE, 2, 6, 6, 3, 3, true)              \
@@ -946,9 +946,14 @@ __global__ void __launch_bounds__(kMaxTileThreads)
   X(SDG_ELEMENT_TRIANGLE, 4, 15, 16, 5, 3, true)            \
   X(SDG_ELEMENT_TRIANGLE, 5, 21, 25, 6, 3, true)            \
   X(SDG_ELEMENT_QUADRANGLE, 1, 4, 7, 2, 4, true)            \
-  X(SDG_ELEMENT_QUADRANGLE, 1, 4, 7, 2, 4, false)
+  X(SDG_ELEMENT_QUADRANGLE, 1, 4, 7, 2, 4, false)           \
+  X(SDG_ELEMENT_TRIANGLE, 1, 3, 3, 2, 3, false)             \
+  X(SDG_ELEMENT_TRIANGLE, 2, 6, 6, 3, 3, false)             \
+  X(SDG_ELEMENT_TRIANGLE, 3, 10, 12, 4, 3, false)           \
+  X(SDG_ELEMENT_TRIANGLE, 4, 15, 16, 5, 3, false)           \
+  X(SDG_ELEMENT_TRIANGLE, 5, 21, 25, 6, 3, false)
 
-// Forward kernels: the above and curved (non-affine) triangles.
+// Forward kernels: the same blocks.
 #define SDG_DENSE_CASES(X)                                  \
   X(SDG_ELEMENT_TRIANGLE, 1, 3, 3, 2, 3, true)              \
   X(SDG_ELEMENT_TRIANGLE, 2, 6, 6, 3, 3, true)              \

@@ -141,6 +141,13 @@ CASES = {
     "ns-curved-annulus-quad-p2-br1-hllc": lambda: cases.annulus_case(
         p=2, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01,
         conditions=(sdg.ADIABATIC_NONSLIP_WALL, sdg.ADIABATIC_SLIP_WALL)),
+    "euler-curved-annulus-tri-p2-hllc": lambda: cases.annulus_case(p=2, flux=sdg.HLLC, split=1.0),
+    "ns-curved-annulus-hybrid-p2-br2-roe": lambda: cases.annulus_case(
+        p=2, flux=sdg.ROE, viscous=sdg.BR2, mu=0.01, split=0.5,
+        conditions=(sdg.ADIABATIC_NONSLIP_WALL, sdg.ADIABATIC_SLIP_WALL)),
+    "ns-curved-annulus-tri-p3-br1-hllc": lambda: cases.annulus_case(
+        p=3, flux=sdg.HLLC, viscous=sdg.BR1, mu=0.01, split=1.0,
+        conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_SLIP_WALL)),
     "ns-curved-annulus-quad-p3-br2-roe": lambda: cases.annulus_case(
         p=3, flux=sdg.ROE, viscous=sdg.BR2, mu=0.01,
         conditions=(sdg.ISOTHERMAL_NONSLIP_WALL, sdg.ADIABATIC_SLIP_WALL)),

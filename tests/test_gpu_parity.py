@@ -425,12 +425,3 @@ def test_warped_hexahedra_wall_force_of_a_uniform_state_vanishes(q):
     g.initialize_primitive(cases.uniform_primitive(g.counts.volume_point_count, 3, vel=(0.0, 0.0, 0.0)))
     f = sum(g.surface_force(k) for k in range(1, 7))
     assert np.abs(f).max() < 1e-12, f
-
-
-def test_curved_triangles_refuse_derivatives():
-    mesh, cfg, prim, _, _, _ = cases.annulus_case(p=2, split=1.0)
-    g = sdg.GpuSolver(mesh, cfg)
-    g.initialize_primitive(prim(g.volume_points()))
-    with pytest.raises(sdg.SdgError) as err:
-        g.vjp_residual(np.zeros((g.counts.volume_point_count, 4)))
-    assert err.value.code == 5  # SDG_ERR_UNSUPPORTED
