@@ -254,9 +254,9 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
         }
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
-      double tot[DIM], vol[DIM];
+      double tot[DIM], vol[DIM], dsum[DIM];  // dsum (non-affine): -sum_b of the line derivatives, added once
 #pragma unroll
-      for (int k = 0; k < DIM; ++k) { tot[k] = 0.0; vol[k] = 0.0; }
+      for (int k = 0; k < DIM; ++k) { tot[k] = 0.0; vol[k] = 0.0; dsum[k] = 0.0; }
 #pragma unroll
       for (int b = 0; b < DIM; ++b) {
         const int st = strideOf<DIM, N>(b);
@@ -283,14 +283,22 @@ __device__ __forceinline__ bool tensorGradientTile(const GradArgs& a, int64_t ti
         } else {
 #pragma unroll
           for (int k = 0; k < DIM; ++k) {
-            double dk = 0.0;
+            double dk = dsum[k];
             const double* P = sP + ((le * DIM + b) * DIM + k) * NV * NB + v * NB + base;
 #pragma unroll
-            for (int q = 0; q < N; ++q) dk = fma(T->dhat[q][ax[b]], P[q * st], dk);
-            tot[k] = fma(lp * nF[b][1][k], op, fma(lm * nF[b][0][k], om, tot[k] - dk));
+            for (int q = 0; q < N; ++q) dk = fma(-T->dhat[q][ax[b]], P[q * st], dk);
+            dsum[k] = dk;
+            tot[k] = fma(lp * nF[b][1][k], op, fma(lm * nF[b][0][k], om, tot[k]));
             if constexpr (BR2)
-              vol[k] = fma(lp * nF[b][1][k], ap, fma(lm * nF[b][0][k], am, vol[k] - dk));
+              vol[k] = fma(lp * nF[b][1][k], ap, fma(lm * nF[b][0][k], am, vol[k]));
           }
+        }
+      }
+      if constexpr (!AFFINE) {
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          tot[k] += dsum[k];
+          if constexpr (BR2) vol[k] += dsum[k];
         }
       }
 #pragma unroll
