@@ -284,7 +284,9 @@ def test_vjp_is_the_transpose_of_jvp(name):
                                   "ns-line-p4-br1-roe", "euler-hybrid-p3-lf-bilinear", "euler-tri-p5-roe",
                                   "ns-hybrid-p3-br1-lf", "ns-tri-p3-br2-hllc", "ns-hybrid-jitter-p4-br2-lf",
                                   "ns-jitter-quad-p1-br2-roe-bilinear",
-                                  "ns-quad-p4-br1-hllc", "ns-hex-p2-br2-hllc", "ns-channel-walls-quad-p3-br2-roe"])
+                                  "ns-quad-p4-br1-hllc", "ns-hex-p2-br2-hllc", "ns-channel-walls-quad-p3-br2-roe",
+                                  "ns-warped-hex-p2-br1-roe", "ns-curved-hex-p2-q2-br2-lf",
+                                  "ns-curved-annulus-hybrid-p2-br2-roe"])
 def test_trajectory_dot_product_with_checkpointing(name):
     steps, interval = 5, 2
     a, dt = make(name)
@@ -346,7 +348,8 @@ def test_trajectory_store_gives_the_checkpointed_adjoint(name):
 @pytest.mark.parametrize("name", ["euler-hex-p3-central", "ns-hex-p3-br1-roe", "euler-quad-p3-roe",
                                   "inc-ns-taylorvortex-quad-p4-exact-br2", "inc-euler-shearlayer-quad-p2-central",
                                   "ns-line-walls-p3-br2-roe", "euler-tri-p3-central", "ns-tri-p2-br1-roe",
-                                  "ns-jitter-quad-p3-br2-roe-bilinear"])
+                                  "ns-jitter-quad-p3-br2-roe-bilinear", "ns-warped-hex-p2-br1-roe",
+                                  "euler-curved-annulus-quad-p3-roe"])
 def test_kinetic_energy_gradient_matches_finite_differences(name):
     steps, interval = 6, 3
     s, dt = make(name)
@@ -451,7 +454,8 @@ def test_surface_force_of_a_fluid_at_rest_is_the_pressure_times_the_area():
                                   "ns-channel-walls-quad-p3-br1-roe", "ns-box-walls-hex-p2-br1-roe",
                                   "inc-ns-thermalcavity-quad-p3-exact-br1-boussinesq", "inc-ns-lidcavity-hex-p2-lf-br2",
                                   "ns-line-walls-p3-br2-roe", "euler-channel-tri-p3-roe",
-                                  "euler-channel-hybrid-farfield-p2-hllc", "ns-channel-walls-tri-p2-br2-roe"])
+                                  "euler-channel-hybrid-farfield-p2-hllc", "ns-channel-walls-tri-p2-br2-roe",
+                                  "ns-warped-hex-box-p2-br1-hllc", "ns-curved-annulus-tri-p3-br1-hllc"])
 def test_surface_force_cotangent_matches_central_differences(name):
     s, _ = make(name)
     group, e = _force_group(s)
