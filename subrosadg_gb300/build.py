@@ -45,8 +45,8 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
     """Compile libsdg_gpu.so (CUDA kernels + C ABI + host mesh layer)."""
     os.makedirs(LIBDIR, exist_ok=True)
     target = os.path.join(LIBDIR, "libsdg_gpu.so")
-    units = ["sdg_variants_tensor.cu", "sdg_variants_tensor_hex.cu", "sdg_variants_dense.cu", "sdg_variants_face.cu", "sdg_variants_adjoint_face.cu",
-             "sdg_variants_adjoint_tile.cu", "sdg_variants_adjoint_hex.cu", "sdg_variants_adjoint_dense.cu", "sdg_gpu.cu", "sdg_batch.cu",
+    units = ["sdg_variants_tensor.cu", "sdg_variants_tensor_hex.cu", "sdg_variants_dense.cu", "sdg_variants_dense_tet.cu", "sdg_variants_face.cu", "sdg_variants_adjoint_face.cu",
+             "sdg_variants_adjoint_tile.cu", "sdg_variants_adjoint_hex.cu", "sdg_variants_adjoint_dense_tet.cu", "sdg_variants_adjoint_dense.cu", "sdg_gpu.cu", "sdg_batch.cu",
              "sdg_adjoint.cu", "sdg_rawbinary.cu",
              "sdg_mesh.cpp", "sdg_noalloc.cu", "sdg_av.cu"]
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".cpp", ".hpp", ".h"))]

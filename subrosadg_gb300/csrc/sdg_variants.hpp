@@ -33,6 +33,9 @@ KernelVariant hexNonAffineStageVariant(int n, int visc);
 KernelVariant hexNonAffineGradVariant(int n, bool br2);
 KernelVariant denseStageVariant(int type, int p, bool affine, int visc);
 KernelVariant denseGradVariant(int type, int p, bool affine);
+// Tetrahedra (sdg_variants_dense_tet.cu), reached through the two above.
+KernelVariant tetStageVariant(int p, bool affine, int visc);
+KernelVariant tetGradVariant(int p, bool affine);
 // Face-point kernels (FaceOp op, flux only for the Riemann operations) and the relative-error reduction.
 KernelVariant facePointVariant(int op, int dim, int flux);
 KernelVariant relerrVariant();
@@ -66,6 +69,8 @@ struct AdjointTileKernels {
 void adjointFaceKernels(int dim, int flux, bool visc, bool gen, AdjointKernels& k);
 void adjointTileKernels(int dim, int n, bool visc, bool br2, bool gen, bool affine, AdjointTileKernels& k);
 void adjointDenseKernels(int type, int p, bool affine, bool gen, bool visc, bool br2, AdjointTileKernels& k);
+// Tetrahedra (sdg_variants_adjoint_dense_tet.cu), reached through adjointDenseKernels.
+void adjointTetKernels(int p, bool affine, bool gen, bool visc, bool br2, AdjointTileKernels& k);
 // Hexahedra that are not parallelepipeds (sdg_variants_adjoint_hex.cu), reached through adjointTileKernels.
 void adjointHexNonAffineKernels(int n, bool visc, bool br2, bool gen, AdjointTileKernels& k);
 

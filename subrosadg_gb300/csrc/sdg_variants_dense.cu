@@ -1,5 +1,5 @@
-// Dense (modal: triangles, P1 quadrangles, tetrahedra) stage and gradient kernels: the one translation unit that
-// instantiates them, and their registry entries.
+// Dense (modal) stage and gradient kernels of 2D blocks (triangles, P1 quadrangles): the translation unit that
+// instantiates them, and the registry entries of every dense block (tetrahedra: sdg_variants_dense_tet.cu).
 #include "sdg_kernels_dense.cuh"
 #include "sdg_kernels_ns.cuh"
 #include "sdg_variants.hpp"
@@ -36,12 +36,7 @@ KernelVariant denseStageVariant(int type, int p, bool affine, int visc) {
                      : visc ? stageOf<NB, NQ, NFQ, NF, AFF, 1>() : stageOf<NB, NQ, NFQ, NF, AFF, 0>();
   SDG_DENSE_CASES(SDG_DS)
 #undef SDG_DS
-#define SDG_DT(T, P, NB, NQ, NFQ, NF)                                                                   \
-  if (type == T && p == P && affine)                                                                      \
-    return visc == 2 ? stageOf<NB, NQ, NFQ, NF, true, 2, 3>()                                             \
-                     : visc ? stageOf<NB, NQ, NFQ, NF, true, 1, 3>() : stageOf<NB, NQ, NFQ, NF, true, 0, 3>();
-  SDG_TET_CASES(SDG_DT)
-#undef SDG_DT
+  if (type == SDG_ELEMENT_TETRAHEDRON) return tetStageVariant(p, affine, visc);
   return KernelVariant();
 }
 
@@ -50,10 +45,7 @@ KernelVariant denseGradVariant(int type, int p, bool affine) {
   if (type == T && p == P && affine == AFF) return gradOf<NB, NQ, NFQ, NF, AFF>();
   SDG_DENSE_CASES(SDG_DG)
 #undef SDG_DG
-#define SDG_DGT(T, P, NB, NQ, NFQ, NF) \
-  if (type == T && p == P && affine) return gradOf<NB, NQ, NFQ, NF, true, 3>();
-  SDG_TET_CASES(SDG_DGT)
-#undef SDG_DGT
+  if (type == SDG_ELEMENT_TETRAHEDRON) return tetGradVariant(p, affine);
   return KernelVariant();
 }
 
